@@ -1,0 +1,136 @@
+"""Python front end of libgpugi_bvhmake.so (the bvhmake restatement).
+
+`build_bvh` returns the arrays in the layout the traversal kernels and the
+file format use: `hierarchy` float32 [N, 8] (min.xyz, firstChild bits,
+max.xyz, escape bits), `slots` int32 [S, 4] with leaf_size slots per block.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_LIB = None
+LIB_DIR = Path(__file__).resolve().parent / "lib"
+
+BUILD_METHODS = {"kdtree": 0, "sweep": 1}
+FIT_METHODS = {"aabox": 0, "ellipsoid": 1}
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        path = LIB_DIR / "libgpugi_bvhmake.so"
+        if not path.exists():
+            raise RuntimeError(f"{path} is missing: run `python -m gpugi_gb300.build` first")
+        lib = C.CDLL(str(path))
+        P, U32, U64, I = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+        lib.gpugi_bvh_build.argtypes = [P, U32, P, U32, U32, U32, U32, U64, C.POINTER(P)]
+        lib.gpugi_bvh_build.restype = I
+        lib.gpugi_bvh_info.argtypes = [P] + [C.POINTER(U32)] * 5
+        lib.gpugi_bvh_export.argtypes = [P, P, P, P]
+        lib.gpugi_bvh_write_file.argtypes = [P, C.c_char_p]
+        lib.gpugi_bvh_read_file.argtypes = [C.c_char_p, C.POINTER(P)]
+        lib.gpugi_bvh_vertices.argtypes = [P, C.POINTER(U32), P]
+        lib.gpugi_bvh_free.argtypes = [P]
+        lib.gpugi_bvh_free.restype = None
+        lib.gpugi_bvh_last_error.restype = C.c_char_p
+        _LIB = lib
+    return _LIB
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class BVH:
+    hierarchy: np.ndarray   # float32 [N, 8]
+    slots: np.ndarray       # int32 [S, 4]
+    parents: np.ndarray     # uint32 [N]
+    leaf_size: int
+    bounds_kind: int        # 0 = AABB, 1 = ellipsoid
+    max_depth: int
+    positions: np.ndarray | None = None
+
+    @property
+    def num_nodes(self) -> int:
+        return self.hierarchy.shape[0]
+
+    @property
+    def num_slots(self) -> int:
+        return self.slots.shape[0]
+
+    @property
+    def first_child(self) -> np.ndarray:
+        return self.hierarchy[:, 3].view(np.uint32)
+
+    @property
+    def escape(self) -> np.ndarray:
+        return self.hierarchy[:, 7].view(np.uint32)
+
+
+def _collect(handle) -> BVH:
+    lib = _lib()
+    n, nb, ls, bk, md = (C.c_uint32() for _ in range(5))
+    lib.gpugi_bvh_info(handle, C.byref(n), C.byref(nb), C.byref(ls), C.byref(bk), C.byref(md))
+    hier = np.zeros((n.value, 8), dtype=np.float32)
+    slots = np.zeros((nb.value * ls.value, 4), dtype=np.int32)
+    parents = np.zeros(n.value, dtype=np.uint32)
+    lib.gpugi_bvh_export(handle, _ptr(hier), _ptr(slots), _ptr(parents))
+    return BVH(hier, slots, parents, ls.value, bk.value, md.value)
+
+
+def build_bvh(positions: np.ndarray, triangles: np.ndarray, method: str = "sweep", fit: str = "aabox",
+              leaf_size: int = 8, seed: int = 1) -> BVH:
+    lib = _lib()
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    tri = np.ascontiguousarray(triangles, dtype=np.uint32)
+    h = C.c_void_p()
+    rc = lib.gpugi_bvh_build(_ptr(pos), pos.shape[0], _ptr(tri), tri.shape[0], BUILD_METHODS[method],
+                             FIT_METHODS[fit], leaf_size, seed, C.byref(h))
+    if rc != 0:
+        raise ValueError(f"gpugi_bvh_build failed ({rc}): {lib.gpugi_bvh_last_error().decode()}")
+    try:
+        b = _collect(h)
+        b.positions = pos
+        return b
+    finally:
+        lib.gpugi_bvh_free(h)
+
+
+def write_bvh_file(positions: np.ndarray, triangles: np.ndarray, path: str, **kw) -> None:
+    """Build and write bvhmake's NamedArray file."""
+    lib = _lib()
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    tri = np.ascontiguousarray(triangles, dtype=np.uint32)
+    h = C.c_void_p()
+    rc = lib.gpugi_bvh_build(_ptr(pos), pos.shape[0], _ptr(tri), tri.shape[0],
+                             BUILD_METHODS[kw.get("method", "sweep")], FIT_METHODS[kw.get("fit", "aabox")],
+                             kw.get("leaf_size", 8), kw.get("seed", 1), C.byref(h))
+    if rc != 0:
+        raise ValueError(lib.gpugi_bvh_last_error().decode())
+    try:
+        if lib.gpugi_bvh_write_file(h, str(path).encode()) != 0:
+            raise OSError(lib.gpugi_bvh_last_error().decode())
+    finally:
+        lib.gpugi_bvh_free(h)
+
+
+def read_bvh_file(path: str) -> BVH:
+    lib = _lib()
+    h = C.c_void_p()
+    if lib.gpugi_bvh_read_file(str(path).encode(), C.byref(h)) != 0:
+        raise OSError(lib.gpugi_bvh_last_error().decode())
+    try:
+        b = _collect(h)
+        nv = C.c_uint32()
+        lib.gpugi_bvh_vertices(h, C.byref(nv), None)
+        pos = np.zeros((nv.value, 3), dtype=np.float32)
+        lib.gpugi_bvh_vertices(h, C.byref(nv), _ptr(pos))
+        b.positions = pos
+        return b
+    finally:
+        lib.gpugi_bvh_free(h)

@@ -1,0 +1,177 @@
+// Scene upload: validation of the escape tree, repacking of leaf children,
+// and the per-slot triangle precompute (p0, e0, e1, n) on the device.
+//
+// Replaces Scene::UploadGeometry / UploadHierarchy (gpugi/scene/scene.cpp:
+// 75-130) for the CUDA path.
+#include <cstring>
+
+#include "ctx.cuh"
+
+namespace gpugi {
+
+// Precompute each valid slot's triangle record with the operation order of
+// IntersectTriangle (intersectiontests.glsl:66-68).
+__global__ void k_prepare_triangles(const int4* __restrict__ slots, uint32_t numSlots,
+                                    const float* __restrict__ pos, float4* __restrict__ tris) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= numSlots) return;
+    int4 s = slots[i];
+    float4 a = make_float4(0, 0, 0, 0), b = a, c = a;
+    if (s.x != s.y) {
+        float3 p0 = make_float3(pos[3 * (size_t)s.x], pos[3 * (size_t)s.x + 1], pos[3 * (size_t)s.x + 2]);
+        float3 p1 = make_float3(pos[3 * (size_t)s.y], pos[3 * (size_t)s.y + 1], pos[3 * (size_t)s.y + 2]);
+        float3 p2 = make_float3(pos[3 * (size_t)s.z], pos[3 * (size_t)s.z + 1], pos[3 * (size_t)s.z + 2]);
+        float3 e0 = X::sub3(p1, p0);
+        float3 e1 = X::sub3(p0, p2);
+        float3 n = X::cross(e1, e0);
+        a = make_float4(p0.x, p0.y, p0.z, e0.x);
+        b = make_float4(e0.y, e0.z, e1.x, e1.y);
+        c = make_float4(e1.z, n.x, n.y, n.z);
+    }
+    tris[3 * (size_t)i] = a;
+    tris[3 * (size_t)i + 1] = b;
+    tris[3 * (size_t)i + 2] = c;
+}
+
+static uint32_t bits_of(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+template <typename T>
+static gpugi_status upload(gpugi_ctx* ctx, gpugi_scene* sc, const T* host, size_t count, const T** dst) {
+    *dst = nullptr;
+    if (count == 0) return GPUGI_OK;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "cudaMalloc failed for scene buffer");
+    sc->allocations.push_back(p);
+    if (host) {
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(p, host, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(p, 0, count * sizeof(T), ctx->stream));
+    }
+    *dst = static_cast<const T*>(p);
+    return GPUGI_OK;
+}
+
+}  // namespace gpugi
+
+using namespace gpugi;
+
+extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarchy, uint32_t numNodes,
+                                           uint32_t boundsKind, const int32_t* slots, uint32_t numSlots,
+                                           uint32_t leafSize, const float* positions, const float* vertexInfo,
+                                           uint32_t numVertices, const gpugi_material* materials,
+                                           uint32_t numMaterials, gpugi_scene** out) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!out) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (!hierarchy || !slots || !positions || numNodes == 0 || numSlots == 0 || numVertices == 0)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "empty scene: hierarchy, slots and positions are required");
+    if (boundsKind > GPUGI_BOUNDS_ELLIPSOID) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown bounds kind");
+    if (leafSize == 0 || leafSize > 32 || numSlots % leafSize != 0)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "leafSize must be in [1, 32] and divide numSlots");
+    if (numNodes >= 0x80000000u) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "too many nodes");
+    if (numMaterials > 0 && !materials) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "materials is NULL");
+    const uint32_t numBlocks = numSlots / leafSize;
+    if (numBlocks > LEAF_BLOCK_MASK + 1u) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "too many leaf blocks");
+
+    // Leaf slots: indices in range; count the leading valid slots per block.
+    std::vector<uint32_t> counts(numBlocks, 0);
+    for (uint32_t blk = 0; blk < numBlocks; ++blk) {
+        uint32_t c = 0;
+        bool ended = false;
+        for (uint32_t k = 0; k < leafSize; ++k) {
+            const int32_t* s = slots + 4 * ((size_t)blk * leafSize + k);
+            if (s[0] == s[1]) {
+                ended = true;
+                continue;
+            }
+            if (s[0] < 0 || s[1] < 0 || s[2] < 0 || (uint32_t)s[0] >= numVertices || (uint32_t)s[1] >= numVertices ||
+                (uint32_t)s[2] >= numVertices)
+                return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "leaf slot references a vertex out of range");
+            if (numMaterials > 0 && (s[3] < 0 || (uint32_t)s[3] >= numMaterials))
+                return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "leaf slot references a material out of range");
+            if (!ended) ++c;
+        }
+        counts[blk] = c;
+    }
+    // Escape tree: children and escapes point strictly forward (preorder), so
+    // every walk terminates within numNodes steps and stays in bounds.
+    std::vector<float> nodes(hierarchy, hierarchy + 8 * (size_t)numNodes);
+    for (uint32_t i = 0; i < numNodes; ++i) {
+        uint32_t child = bits_of(hierarchy[8 * (size_t)i + 3]);
+        uint32_t esc = bits_of(hierarchy[8 * (size_t)i + 7]);
+        if (child & LEAF_FLAG) {
+            uint32_t blk = child & 0x7FFFFFFFu;
+            if (blk >= numBlocks) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "leaf block index out of range");
+            uint32_t enc = LEAF_FLAG | (counts[blk] << LEAF_COUNT_SHIFT) | blk;
+            std::memcpy(&nodes[8 * (size_t)i + 3], &enc, 4);
+        } else if (child <= i || child >= numNodes) {
+            return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "firstChild must point forward to a node (preorder)");
+        }
+        if (esc != 0 && (esc <= i || esc >= numNodes))
+            return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "escape must be 0 or point forward (preorder)");
+    }
+
+    cudaError_t se = cudaSetDevice(ctx->device);
+    if (se != cudaSuccess) return cuda_fail(ctx, se, "cudaSetDevice");
+    gpugi_scene* sc = new gpugi_scene();
+    sc->ctx = ctx;
+    sc->numLeafBlocks = numBlocks;
+    auto cleanup = [&](gpugi_status st) {
+        gpugi_scene_destroy(sc);
+        return st;
+    };
+    gpugi_status st;
+    const float4* dNodes;
+    if ((st = upload(ctx, sc, reinterpret_cast<const float4*>(nodes.data()), 2 * (size_t)numNodes, &dNodes)))
+        return cleanup(st);
+    const int4* dSlots;
+    if ((st = upload(ctx, sc, reinterpret_cast<const int4*>(slots), numSlots, &dSlots))) return cleanup(st);
+    const float* dPos;
+    if ((st = upload(ctx, sc, positions, 3 * (size_t)numVertices, &dPos))) return cleanup(st);
+    const float4* dInfo;
+    if ((st = upload(ctx, sc, reinterpret_cast<const float4*>(vertexInfo), numVertices, &dInfo)))
+        return cleanup(st);
+    const float4* dMat = nullptr;
+    if (numMaterials > 0 &&
+        (st = upload(ctx, sc, reinterpret_cast<const float4*>(materials), 6 * (size_t)numMaterials, &dMat)))
+        return cleanup(st);
+    const float4* dTris;
+    if ((st = upload<float4>(ctx, sc, nullptr, 3 * (size_t)numSlots, &dTris))) return cleanup(st);
+    k_prepare_triangles<<<(numSlots + 255) / 256, 256, 0, ctx->stream>>>(dSlots, numSlots, dPos,
+                                                                         const_cast<float4*>(dTris));
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "scene upload"));
+
+    sc->dev.nodes = dNodes;
+    sc->dev.tris = dTris;
+    sc->dev.slots = dSlots;
+    sc->dev.positions = dPos;
+    sc->dev.vinfo = dInfo;
+    sc->dev.materials = dMat;
+    sc->dev.numNodes = numNodes;
+    sc->dev.numSlots = numSlots;
+    sc->dev.leafSize = leafSize;
+    sc->dev.boundsKind = boundsKind;
+    sc->dev.numVertices = numVertices;
+    sc->dev.numMaterials = numMaterials;
+    sc->hostPositions.assign(positions, positions + 3 * (size_t)numVertices);
+    sc->hostSlots.assign(slots, slots + 4 * (size_t)numSlots);
+    if (numMaterials)
+        sc->hostMaterials.assign(reinterpret_cast<const float*>(materials),
+                                 reinterpret_cast<const float*>(materials) + 24 * (size_t)numMaterials);
+    *out = sc;
+    return GPUGI_OK;
+}
+
+extern "C" void gpugi_scene_destroy(gpugi_scene* sc) {
+    if (!sc) return;
+    if (sc->ctx) cudaStreamSynchronize(sc->ctx->stream);
+    for (void* p : sc->allocations) cudaFree(p);
+    delete sc;
+}

@@ -1,0 +1,122 @@
+// Ray-query kernels behind gpugi_trace_closest / gpugi_trace_any.
+//
+// One ray per thread; rays and results are structure-of-arrays so every
+// load and store of a warp is a single coalesced 128-B transaction. The
+// walk itself reads 32-B nodes and 48-B triangle records through the
+// read-only (non-coherent) path with 16-B vector loads.
+#include "ctx.cuh"
+#include "trace.cuh"
+
+namespace gpugi {
+
+template <int BOUNDS>
+__global__ void __launch_bounds__(256) k_trace_closest(DevScene s, const float* __restrict__ ox,
+                                                       const float* __restrict__ oy, const float* __restrict__ oz,
+                                                       const float* __restrict__ dx, const float* __restrict__ dy,
+                                                       const float* __restrict__ dz, const float* __restrict__ tmax,
+                                                       uint64_t n, int32_t* __restrict__ slot, float* __restrict__ t,
+                                                       float* __restrict__ u, float* __restrict__ v, uint32_t* err) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 o = make_float3(__ldg(ox + i), __ldg(oy + i), __ldg(oz + i));
+    const float3 d = make_float3(__ldg(dx + i), __ldg(dy + i), __ldg(dz + i));
+    TraceResult r = trace_ray<false, BOUNDS>(s, o, d, __ldg(tmax + i), err);
+    slot[i] = r.slot;
+    t[i] = r.t;
+    u[i] = r.u;
+    v[i] = r.v;
+}
+
+template <int BOUNDS>
+__global__ void __launch_bounds__(256) k_trace_any(DevScene s, const float* __restrict__ ox,
+                                                   const float* __restrict__ oy, const float* __restrict__ oz,
+                                                   const float* __restrict__ dx, const float* __restrict__ dy,
+                                                   const float* __restrict__ dz, const float* __restrict__ tmax,
+                                                   uint64_t n, uint8_t* __restrict__ occluded, uint32_t* err) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 o = make_float3(__ldg(ox + i), __ldg(oy + i), __ldg(oz + i));
+    const float3 d = make_float3(__ldg(dx + i), __ldg(dy + i), __ldg(dz + i));
+    TraceResult r = trace_ray<true, BOUNDS>(s, o, d, __ldg(tmax + i), err);
+    occluded[i] = r.slot >= 0 ? 1 : 0;
+}
+
+template <int BOUNDS, bool ANY>
+__global__ void __launch_bounds__(256) k_trace_stats(DevScene s, const float* __restrict__ ox,
+                                                     const float* __restrict__ oy, const float* __restrict__ oz,
+                                                     const float* __restrict__ dx, const float* __restrict__ dy,
+                                                     const float* __restrict__ dz, const float* __restrict__ tmax,
+                                                     uint64_t n, unsigned long long* sums, uint32_t* err) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    WalkCounters c;
+    if (i < n) {
+        const float3 o = make_float3(ox[i], oy[i], oz[i]);
+        const float3 d = make_float3(dx[i], dy[i], dz[i]);
+        trace_ray<ANY, BOUNDS, true>(s, o, d, tmax[i], err, &c);
+    }
+    unsigned long long a = c.nodes, b = c.slots, t = c.tris;
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+        t += __shfl_down_sync(0xffffffffu, t, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(sums, a);
+        atomicAdd(sums + 1, b);
+        atomicAdd(sums + 2, t);
+    }
+}
+
+gpugi_status launch_trace_stats(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
+                                const float* oz, const float* dx, const float* dy, const float* dz,
+                                const float* tmax, uint64_t n, uint32_t anyHit, unsigned long long* sums) {
+    if (n == 0) return GPUGI_OK;
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    if (!ell && !anyHit)
+        k_trace_stats<0, false><<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
+    else if (!ell)
+        k_trace_stats<0, true><<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
+    else if (!anyHit)
+        k_trace_stats<1, false><<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
+    else
+        k_trace_stats<1, true><<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
+    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
+static unsigned grid_for(uint64_t n, uint32_t block) { return (unsigned)((n + block - 1) / block); }
+
+gpugi_status launch_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
+                                  const float* oz, const float* dx, const float* dy, const float* dz,
+                                  const float* tmax, uint64_t n, int32_t* slot, float* t, float* u, float* v) {
+    if (n == 0) return GPUGI_OK;
+    if (n > (uint64_t)0xFFFFFFFFu * 256u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many rays");
+    const uint32_t block = ctx->traceBlock;
+    if (sc->dev.boundsKind == GPUGI_BOUNDS_AABB)
+        k_trace_closest<0><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
+                                                                           slot, t, u, v, ctx->errWord);
+    else
+        k_trace_closest<1><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
+                                                                           slot, t, u, v, ctx->errWord);
+    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
+gpugi_status launch_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
+                              const float* oz, const float* dx, const float* dy, const float* dz,
+                              const float* tmax, uint64_t n, uint8_t* occluded) {
+    if (n == 0) return GPUGI_OK;
+    if (n > (uint64_t)0xFFFFFFFFu * 256u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many rays");
+    const uint32_t block = ctx->traceBlock;
+    if (sc->dev.boundsKind == GPUGI_BOUNDS_AABB)
+        k_trace_any<0><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
+                                                                       occluded, ctx->errWord);
+    else
+        k_trace_any<1><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
+                                                                       occluded, ctx->errWord);
+    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
+}  // namespace gpugi

@@ -1,0 +1,150 @@
+// Stackless escape-pointer BVH walk and its intersection tests (device code).
+//
+// Same walk as gpugi's TraceRay/TraceRayAnyHit (gpugi/shader/traceray.glsl:
+// 25-180): nodes are visited in preorder; a node whose bounds are hit with
+// firstHit <= rayLength descends into firstChild (or tests the leaf block and
+// then continues at escape), a missed node continues at escape, and escape 0
+// ends the walk. Leaf slots are tested in order and a triangle is accepted
+// when hit < rayLength (strict, so ties keep the first slot found). The
+// node/leaf state machine of the shader is written here as two nested loops
+// that perform the same sequence of tests.
+#pragma once
+#include "common.cuh"
+#include "scene.cuh"
+
+namespace gpugi {
+
+// IntersectBox (intersectiontests.glsl:9-20). min/max are IEEE minNum/maxNum
+// (fminf/fmaxf): an axis-parallel ray produces inf*0 = NaN slabs that drop out.
+GPUGI_D bool intersect_box(float3 o, float3 inv, float4 lo, float4 hi, float& firstHit) {
+    float tbx = X::mul(inv.x, X::sub(lo.x, o.x)), tby = X::mul(inv.y, X::sub(lo.y, o.y)),
+          tbz = X::mul(inv.z, X::sub(lo.z, o.z));
+    float ttx = X::mul(inv.x, X::sub(hi.x, o.x)), tty = X::mul(inv.y, X::sub(hi.y, o.y)),
+          ttz = X::mul(inv.z, X::sub(hi.z, o.z));
+    float mnx = fminf(ttx, tbx), mny = fminf(tty, tby), mnz = fminf(ttz, tbz);
+    float mxx = fmaxf(ttx, tbx), mxy = fmaxf(tty, tby), mxz = fmaxf(ttz, tbz);
+    float t0 = fmaxf(mnx, mny), t1 = fmaxf(mnx, mnz);
+    firstHit = fmaxf(0.0f, fmaxf(t0, t1));
+    float l0 = fminf(mxx, mxy), l1 = fminf(mxx, mxz);
+    float lastHit = fminf(l0, l1);
+    return firstHit <= lastHit;
+}
+
+// Ray against a stored axis-aligned ellipsoid {center, radii}; arithmetic of
+// IntersectVirtualEllipsoid (intersectiontests.glsl:26-52), including its
+// +1e-15 radius guard.
+GPUGI_D bool intersect_ellipsoid(float3 ro, float3 rd, float4 c, float4 r, float& firstHit) {
+    float3 radii = make_float3(X::add(r.x, 1e-15f), X::add(r.y, 1e-15f), X::add(r.z, 1e-15f));
+    float3 o = X::sub3(ro, xyz(c));
+    float t = X::dot(o, rd);
+    t = fmaxf(0.0f, -t);
+    o = X::add3(o, X::scale(t, rd));
+    o = X::div3(o, radii);
+    float odoto = X::dot(o, o);
+    float3 d = X::div3(rd, radii);
+    float odotd = X::dot(o, d);
+    float ddotd = X::dot(d, d);
+    float phalf = X::div(odotd, ddotd);
+    float q = X::div(X::sub(odoto, 1.0f), ddotd);
+    float rad = X::sub(X::mul(phalf, phalf), q);
+    if (rad < 0.0f) return false;
+    rad = __fsqrt_rn(rad);
+    firstHit = fmaxf(0.0f, X::add(X::sub(-phalf, rad), t));
+    return X::add(X::add(-phalf, rad), t) >= 0.0f;
+}
+
+// IntersectTriangle (intersectiontests.glsl:63-79) on the precomputed record
+// {p0, e0, e1, n}. Returns hit distance and the two barycentrics (y, z).
+GPUGI_D bool intersect_triangle(float3 o, float3 d, const float4* rec, float& hit, float& by, float& bz) {
+    float4 a = __ldg(rec), b = __ldg(rec + 1), c = __ldg(rec + 2);
+    float3 p0 = make_float3(a.x, a.y, a.z);
+    float3 e0 = make_float3(a.w, b.x, b.y);
+    float3 e1 = make_float3(b.z, b.w, c.x);
+    float3 n = make_float3(c.y, c.z, c.w);
+    float3 e2 = X::scale(X::rcp(X::dot(n, d)), X::sub3(p0, o));
+    float3 i = X::cross(d, e2);
+    by = X::dot(i, e1);
+    bz = X::dot(i, e0);
+    float bx = X::sub(1.0f, X::add(bz, by));
+    hit = X::dot(n, e2);
+    return (hit > 0.0001f) && bx >= 0.0f && by >= 0.0f && bz >= 0.0f;
+}
+
+struct TraceResult {
+    int32_t slot;  // -1 = miss
+    float t;
+    float u, v;
+};
+
+// Fetch counters of one walk, the analogue of TRACERAY_DEBUG_VARS
+// (traceray.glsl:59-61,131-133): node fetches, leaf slot fetches (the shader
+// also fetches the first invalid slot of a block before leaving it) and
+// valid triangles tested.
+struct WalkCounters {
+    uint32_t nodes = 0, slots = 0, tris = 0;
+};
+
+// The walk. ANY_HIT returns at the first accepted triangle (result.slot set
+// to the accepting slot). Every loop is bounded: a validated hierarchy
+// strictly increases the node index, so numNodes visits always suffice; the
+// cap only guards against device memory corruption and reports
+// DEVERR_TRAVERSAL_CAP instead of spinning.
+template <bool ANY_HIT, int BOUNDS, bool COUNT = false>
+GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLength, uint32_t* errWord,
+                              WalkCounters* cnt = nullptr) {
+    TraceResult r;
+    r.slot = -1;
+    r.u = r.v = 0.0f;
+    const float3 inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
+    uint32_t node = 0;
+    uint32_t budget = s.numNodes;
+    const float4* __restrict__ nodes = s.nodes;
+    while (true) {
+        if (budget-- == 0) {
+            raise_error(errWord, DEVERR_TRAVERSAL_CAP);
+            break;
+        }
+        if (COUNT) ++cnt->nodes;
+        const float4 a = __ldg(nodes + 2 * node);
+        const float4 b = __ldg(nodes + 2 * node + 1);
+        const uint32_t child = __float_as_uint(a.w);
+        const uint32_t escape = __float_as_uint(b.w);
+        float firstHit;
+        bool hit;
+        if (BOUNDS == 0) hit = intersect_box(o, inv, a, b, firstHit);
+        else hit = intersect_ellipsoid(o, d, a, b, firstHit);
+        if (hit && firstHit <= rayLength) {
+            if (child & LEAF_FLAG) {
+                const uint32_t count = (child >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK;
+                const uint32_t slot0 = (child & LEAF_BLOCK_MASK) * s.leafSize;
+                if (COUNT) cnt->slots += count < s.leafSize ? count + 1 : count;
+                for (uint32_t k = 0; k < count; ++k) {
+                    if (COUNT) ++cnt->tris;
+                    float h, by, bz;
+                    if (intersect_triangle(o, d, s.tris + 3 * (size_t)(slot0 + k), h, by, bz) && h < rayLength) {
+                        rayLength = h;
+                        r.slot = (int32_t)(slot0 + k);
+                        r.u = by;
+                        r.v = bz;
+                        if (ANY_HIT) {
+                            // the shader stops fetching at the accepting slot
+                            if (COUNT) cnt->slots -= (count < s.leafSize ? count + 1 : count) - (k + 1);
+                            r.t = rayLength;
+                            return r;
+                        }
+                    }
+                }
+                node = escape;
+            } else {
+                node = child;
+            }
+        } else {
+            node = escape;
+        }
+        if (node == 0) break;
+    }
+    r.t = rayLength;
+    return r;
+}
+
+}  // namespace gpugi

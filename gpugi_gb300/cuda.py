@@ -1,0 +1,219 @@
+"""ctypes front end of libgpugi_cuda.so (include/gpugi_cuda.h).
+
+This module only binds the C ABI; it has no compute of its own and no CPU
+fallback. Loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_DIR = Path(__file__).resolve().parent / "lib"
+_LIB = None
+
+STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "INVALID_SCENE", 3: "OUT_OF_MEMORY", 4: "CUDA", 5: "DEVICE",
+          6: "UNSUPPORTED"}
+
+
+class GpugiError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"gpugi status {status} ({STATUS.get(status, '?')}): {msg}")
+        self.status = status
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = LIB_DIR / "libgpugi_cuda.so"
+        if not path.exists():
+            raise RuntimeError(f"{path} is missing: the CUDA extension must be built (python -m gpugi_gb300.build)")
+        _LIB = C.CDLL(str(path))
+        _declare(_LIB)
+    return _LIB
+
+
+def _declare(L):
+    P, U32, U64, I, F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_float
+    L.gpugi_create.argtypes = [C.POINTER(P), P]
+    L.gpugi_destroy.argtypes = [P]
+    L.gpugi_destroy.restype = None
+    L.gpugi_last_error.argtypes = [P]
+    L.gpugi_last_error.restype = C.c_char_p
+    L.gpugi_sync.argtypes = [P]
+    L.gpugi_device_error_bits.argtypes = [P, C.POINTER(U32)]
+    L.gpugi_stream.argtypes = [P]
+    L.gpugi_stream.restype = P
+    L.gpugi_version.restype = C.c_char_p
+    L.gpugi_scene_upload.argtypes = [P, P, U32, U32, P, U32, U32, P, P, U32, P, U32, C.POINTER(P)]
+    L.gpugi_scene_destroy.argtypes = [P]
+    L.gpugi_scene_destroy.restype = None
+    for name in ("gpugi_trace_closest", "gpugi_trace_closest_device"):
+        getattr(L, name).argtypes = [P, P] + [P] * 7 + [U64] + [P] * 4
+    for name in ("gpugi_trace_any", "gpugi_trace_any_device"):
+        getattr(L, name).argtypes = [P, P] + [P] * 7 + [U64, P]
+    L.gpugi_set_trace_config.argtypes = [P, U32, U32]
+    L.gpugi_trace_stats_device.argtypes = [P, P] + [P] * 7 + [U64, U32, P]
+    for name, args in _EXTRA_DECLS.items():
+        if hasattr(L, name):
+            getattr(L, name).argtypes = args
+
+
+# Signatures of the renderer entry points, filled in by render.py.
+_EXTRA_DECLS: dict = {}
+
+
+def _ptr(a):
+    """Pointer of a numpy array or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return C.c_void_p(a.ctypes.data)
+    return C.c_void_p(a.data_ptr())
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+
+        class Opts(C.Structure):
+            _fields_ = [("device", C.c_int), ("flags", C.c_uint32)]
+
+        opts = Opts(device, 0)
+        st = lib().gpugi_create(C.byref(self._h), C.byref(opts))
+        if st != 0:
+            raise GpugiError(st, "gpugi_create failed (no CUDA device?)")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, st: int):
+        if st != 0:
+            raise GpugiError(st, lib().gpugi_last_error(self._h).decode())
+
+    def sync(self):
+        self.check(lib().gpugi_sync(self._h))
+
+    def device_error_bits(self) -> int:
+        b = C.c_uint32()
+        self.check(lib().gpugi_device_error_bits(self._h, C.byref(b)))
+        return b.value
+
+    @property
+    def stream(self) -> int:
+        return lib().gpugi_stream(self._h) or 0
+
+    def set_trace_config(self, block_size: int = 128, shared_nodes: int = 0):
+        self.check(lib().gpugi_set_trace_config(self._h, block_size, shared_nodes))
+
+    def close(self):
+        if self._h:
+            lib().gpugi_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_scene(self, bvh, positions, vertex_info=None, materials=None) -> "DeviceScene":
+        return DeviceScene(self, bvh, positions, vertex_info, materials)
+
+
+class DeviceScene:
+    def __init__(self, ctx: Context, bvh, positions, vertex_info=None, materials=None):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
+        slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
+        pos = np.ascontiguousarray(positions, dtype=np.float32)
+        vi = None if vertex_info is None else np.ascontiguousarray(vertex_info, dtype=np.float32)
+        mats = None if materials is None else np.ascontiguousarray(materials, dtype=np.float32).reshape(-1, 24)
+        nm = 0 if mats is None else mats.shape[0]
+        st = lib().gpugi_scene_upload(ctx.handle, _ptr(hier), hier.shape[0], bvh.bounds_kind, _ptr(slots),
+                                      slots.shape[0], bvh.leaf_size, _ptr(pos), _ptr(vi), pos.shape[0], _ptr(mats),
+                                      nm, C.byref(self._h))
+        ctx.check(st)
+        self.num_nodes = hier.shape[0]
+        self.num_slots = slots.shape[0]
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().gpugi_scene_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+RAY_KEYS = ("ox", "oy", "oz", "dx", "dy", "dz", "tmax")
+
+
+def trace_closest(ctx: Context, scene: DeviceScene, rays: dict) -> dict:
+    """Host arrays in, host arrays out (copies through the context)."""
+    r = [np.ascontiguousarray(rays[k], dtype=np.float32) for k in RAY_KEYS]
+    n = r[0].shape[0]
+    out = dict(slot=np.empty(n, np.int32), t=np.empty(n, np.float32), u=np.empty(n, np.float32),
+               v=np.empty(n, np.float32))
+    ctx.check(lib().gpugi_trace_closest(ctx.handle, scene.handle, *[_ptr(a) for a in r], n, _ptr(out["slot"]),
+                                        _ptr(out["t"]), _ptr(out["u"]), _ptr(out["v"])))
+    return out
+
+
+def trace_any(ctx: Context, scene: DeviceScene, rays: dict) -> np.ndarray:
+    r = [np.ascontiguousarray(rays[k], dtype=np.float32) for k in RAY_KEYS]
+    n = r[0].shape[0]
+    occ = np.empty(n, np.uint8)
+    ctx.check(lib().gpugi_trace_any(ctx.handle, scene.handle, *[_ptr(a) for a in r], n, _ptr(occ)))
+    return occ
+
+
+def trace_closest_device(ctx: Context, scene: DeviceScene, rays: dict, out: dict) -> None:
+    """Device tensors (torch) in and out; asynchronous on the context stream."""
+    n = rays["ox"].numel()
+    ctx.check(lib().gpugi_trace_closest_device(ctx.handle, scene.handle, *[_ptr(rays[k]) for k in RAY_KEYS], n,
+                                               _ptr(out["slot"]), _ptr(out["t"]), _ptr(out["u"]), _ptr(out["v"])))
+
+
+def trace_any_device(ctx: Context, scene: DeviceScene, rays: dict, occluded) -> None:
+    n = rays["ox"].numel()
+    ctx.check(lib().gpugi_trace_any_device(ctx.handle, scene.handle, *[_ptr(rays[k]) for k in RAY_KEYS], n,
+                                           _ptr(occluded)))
+
+
+def trace_stats_device(ctx: Context, scene: DeviceScene, rays: dict, any_hit: bool = False) -> np.ndarray:
+    """Sums over the rays of (nodes visited, leaf slots fetched, valid triangles tested)."""
+    n = rays["ox"].numel()
+    sums = np.zeros(3, np.uint64)
+    ctx.check(lib().gpugi_trace_stats_device(ctx.handle, scene.handle, *[_ptr(rays[k]) for k in RAY_KEYS], n,
+                                             int(any_hit), _ptr(sums)))
+    return sums
+
+
+def algorithmic_bytes(sums: np.ndarray, n_rays: int, any_hit: bool = False) -> int:
+    """gpugi's own fetch pattern per ray: 24 B ray in + 16 B out (4 B any-hit)
+    + 32 B per node + 16 B per leaf slot + 36 B per valid triangle
+    (gpugi/scene/scene.hpp:30-38, traceray.glsl:126,137-139)."""
+    s = [int(x) for x in sums]
+    return n_rays * (24 + (4 if any_hit else 16)) + 32 * s[0] + 16 * s[1] + 36 * s[2]
+
+
+def vertex_info(normals: np.ndarray, texcoords: np.ndarray) -> np.ndarray:
+    """VertexInfo {atan2(n.y, n.x), n.z, u, v} per vertex (gpugi/scene/scene.cpp:79-84)."""
+    n = np.asarray(normals, dtype=np.float32)
+    out = np.zeros((n.shape[0], 4), dtype=np.float32)
+    out[:, 0] = np.arctan2(n[:, 1], n[:, 0])
+    out[:, 1] = n[:, 2]
+    out[:, 2:4] = texcoords
+    return out

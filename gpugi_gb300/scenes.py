@@ -1,0 +1,258 @@
+"""Seeded synthetic scenes and ray sets.
+
+gpugi loads its geometry from `.bim` files that are not part of the
+reference snapshot, so every workload here is generated from a seed. All
+randomness comes from a counter-based splitmix64 hash (vectorised in numpy
+uint64 arithmetic), so the same seed gives the same arrays on every machine.
+
+A scene is a dict of numpy arrays:
+  positions  float32 [V, 3]
+  normals    float32 [V, 3]   (unit shading normals)
+  texcoords  float32 [V, 2]
+  triangles  uint32  [T, 4]   {v0, v1, v2, material}
+  materials  float32 [M, 24]  material records (see `material_record`)
+  plus optional light descriptions used by the renderers.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    """splitmix64 finaliser on a uint64 array (Steele, Lea, Flood 2014)."""
+    with np.errstate(over="ignore"):
+        z = (x + np.uint64(0x9E3779B97F4A7C15)) & _M64
+        z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+        z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+        return z ^ (z >> np.uint64(31))
+
+
+class Stream:
+    """A counter-based random stream: stream(seed, tag) draws are reproducible."""
+
+    def __init__(self, seed: int, tag: int = 0):
+        self._key = int(_splitmix64(np.array([(seed * 0x100000001B3 + tag) & 0xFFFFFFFFFFFFFFFF],
+                                             dtype=np.uint64))[0])
+        self._ctr = 0
+
+    def u64(self, n: int) -> np.ndarray:
+        idx = np.arange(self._ctr, self._ctr + n, dtype=np.uint64)
+        self._ctr += n
+        with np.errstate(over="ignore"):
+            return _splitmix64((idx * np.uint64(0xD1342543DE82EF95)) ^ np.uint64(self._key))
+
+    def uniform(self, n: int, lo: float = 0.0, hi: float = 1.0) -> np.ndarray:
+        """float64 uniform in [lo, hi) with 53 random bits."""
+        u = (self.u64(n) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+        return lo + (hi - lo) * u
+
+    def unit_vectors(self, n: int) -> np.ndarray:
+        """Uniform directions on the sphere by rejection from the cube (no transcendental calls)."""
+        out = np.empty((0, 3), dtype=np.float64)
+        while out.shape[0] < n:
+            m = 2 * (n - out.shape[0]) + 64
+            c = self.uniform(3 * m, -1.0, 1.0).reshape(m, 3)
+            r2 = np.einsum("ij,ij->i", c, c)
+            keep = (r2 <= 1.0) & (r2 > 1e-6)
+            out = np.concatenate([out, c[keep] / np.sqrt(r2[keep])[:, None]])
+        return out[:n]
+
+    def quaternions(self, n: int) -> np.ndarray:
+        out = np.empty((0, 4), dtype=np.float64)
+        while out.shape[0] < n:
+            m = 3 * (n - out.shape[0]) + 64
+            c = self.uniform(4 * m, -1.0, 1.0).reshape(m, 4)
+            r2 = np.einsum("ij,ij->i", c, c)
+            keep = (r2 <= 1.0) & (r2 > 1e-6)
+            out = np.concatenate([out, c[keep] / np.sqrt(r2[keep])[:, None]])
+        return out[:n]
+
+
+def quat_to_matrix(q: np.ndarray) -> np.ndarray:
+    w, x, y, z = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], -1),
+        np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], -1),
+        np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1),
+    ], -2)
+
+
+# --------------------------------------------------------------------------
+# Materials
+# --------------------------------------------------------------------------
+MATERIAL_FLOATS = 24  # 6 x float4, see include/gpugi_cuda.h (gpugi_material)
+
+
+def material_record(albedo=(0.5, 0.5, 0.5), emissivity=(0.0, 0.0, 0.0), specular=(0.0, 0.0, 0.0),
+                    roughness: float = 1.0, opacity=(1.0, 1.0, 1.0), refraction_index: float = 1.5,
+                    reflectiveness=(1.0, 1.0, 1.0)) -> np.ndarray:
+    """Constant-valued material in the device layout.
+
+    Mirrors the JSON-to-GPU mapping of Scene::LoadMaterial
+    (gpugi/scene/scene.cpp:155-179): fresnel0 = specularColor,
+    fresnel1 = 1 - fresnel0, Phong exponent = 1 / (roughness^2 + 1e-20),
+    reflectiveness.w = exponent. Textures are replaced by their constant value.
+    """
+    exponent = np.float32(1.0) / (np.float32(roughness) * np.float32(roughness) + np.float32(1e-20))
+    f0 = np.asarray(specular, dtype=np.float32)
+    rec = np.zeros(MATERIAL_FLOATS, dtype=np.float32)
+    rec[0:3] = albedo
+    rec[3] = refraction_index
+    rec[4:7] = opacity
+    rec[8:11] = reflectiveness
+    rec[11] = exponent
+    rec[12:15] = emissivity
+    rec[16:19] = f0
+    rec[20:23] = np.float32(1.0) - f0
+    return rec
+
+
+def lambert(albedo, emissivity=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """A purely diffuse material: no Phong reflection (specularColor = 0)."""
+    return material_record(albedo=albedo, emissivity=emissivity, specular=(0.0, 0.0, 0.0))
+
+
+# --------------------------------------------------------------------------
+# Meshes
+# --------------------------------------------------------------------------
+def icosphere(level: int):
+    """Unit icosphere. Triangle order: level by level, every triangle
+    (a, b, c) is replaced by (a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+             (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    v = np.array(verts, dtype=np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array(faces, dtype=np.int64)
+    for _ in range(level):
+        edges = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+        key = np.minimum(edges[:, 0], edges[:, 1]) * (1 << 32) + np.maximum(edges[:, 0], edges[:, 1])
+        uniq, first, inv = np.unique(key, return_index=True, return_inverse=True)
+        # midpoints get indices in order of first appearance
+        order = np.argsort(first, kind="stable")
+        rank = np.empty_like(order)
+        rank[order] = np.arange(order.size)
+        mid_idx = v.shape[0] + rank[inv]
+        e = edges[first[order]]
+        mids = v[e[:, 0]] + v[e[:, 1]]
+        mids /= np.linalg.norm(mids, axis=1, keepdims=True)
+        v = np.concatenate([v, mids])
+        nf = f.shape[0]
+        ab, bc, ca = mid_idx[:nf], mid_idx[nf:2 * nf], mid_idx[2 * nf:]
+        a, b, c = f[:, 0], f[:, 1], f[:, 2]
+        f = np.stack([np.stack([a, ab, ca], 1), np.stack([b, bc, ab], 1), np.stack([c, ca, bc], 1),
+                      np.stack([ab, bc, ca], 1)], 1).reshape(-1, 3)
+    return v, f
+
+
+def box_mesh():
+    """Unit cube [-0.5, 0.5]^3 as 12 outward-facing triangles."""
+    v = np.array([[x, y, z] for x in (-0.5, 0.5) for y in (-0.5, 0.5) for z in (-0.5, 0.5)], dtype=np.float64)
+    f = np.array([[0, 1, 3], [0, 3, 2], [4, 6, 7], [4, 7, 5], [0, 4, 5], [0, 5, 1],
+                  [2, 3, 7], [2, 7, 6], [0, 2, 6], [0, 6, 4], [1, 5, 7], [1, 7, 3]], dtype=np.int64)
+    return v, f
+
+
+def torus_mesh(nu: int = 24, nv: int = 12, R: float = 0.35, r: float = 0.15):
+    u = np.arange(nu) * (2 * math.pi / nu)
+    w = np.arange(nv) * (2 * math.pi / nv)
+    uu, ww = np.meshgrid(u, w, indexing="ij")
+    v = np.stack([(R + r * np.cos(ww)) * np.cos(uu), (R + r * np.cos(ww)) * np.sin(uu), r * np.sin(ww)], -1)
+    v = v.reshape(-1, 3)
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    a = i * nv + j
+    b = ((i + 1) % nu) * nv + j
+    c = ((i + 1) % nu) * nv + (j + 1) % nv
+    d = i * nv + (j + 1) % nv
+    f = np.concatenate([np.stack([a, b, c], -1).reshape(-1, 3), np.stack([a, c, d], -1).reshape(-1, 3)])
+    return v, f
+
+
+def vertex_normals(v: np.ndarray, f: np.ndarray) -> np.ndarray:
+    fn = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    n = np.zeros_like(v)
+    for k in range(3):
+        np.add.at(n, f[:, k], fn)
+    ln = np.linalg.norm(n, axis=1, keepdims=True)
+    ln[ln == 0] = 1.0
+    return n / ln
+
+
+def _pack(v, f, mats, material_ids=None, normals=None, texcoords=None, **extra):
+    tris = np.zeros((f.shape[0], 4), dtype=np.uint32)
+    tris[:, :3] = f
+    if material_ids is not None:
+        tris[:, 3] = material_ids
+    if normals is None:
+        normals = vertex_normals(v, f)
+    if texcoords is None:
+        texcoords = np.zeros((v.shape[0], 2))
+    scene = dict(positions=np.ascontiguousarray(v, dtype=np.float32),
+                 normals=np.ascontiguousarray(normals, dtype=np.float32),
+                 texcoords=np.ascontiguousarray(texcoords, dtype=np.float32),
+                 triangles=np.ascontiguousarray(tris),
+                 materials=np.ascontiguousarray(np.asarray(mats, dtype=np.float32).reshape(-1, MATERIAL_FLOATS)))
+    scene.update(extra)
+    return scene
+
+
+# --------------------------------------------------------------------------
+# Workload 1: closest-hit queries against a displaced icosphere
+# --------------------------------------------------------------------------
+def displaced_icosphere(num_triangles: int = 65536, seed: int = 1, amplitude: float = 0.05):
+    """Icosphere subdivided until it has >= num_triangles triangles, truncated
+    to the first num_triangles in generation order, every vertex moved
+    radially by uniform[-amplitude, amplitude], then scaled into the unit
+    cube [0, 1]^3 (largest extent 1, centred in the cube).
+    65,536 triangles = level 6 (81,920) truncated."""
+    level = 0
+    while 20 * 4 ** level < num_triangles:
+        level += 1
+    v, f = icosphere(level)
+    f = f[:num_triangles]
+    used, remap = np.unique(f, return_inverse=True)
+    v = v[used]
+    f = remap.reshape(-1, 3)
+    rs = Stream(seed, 1)
+    radius = 1.0 + rs.uniform(v.shape[0], -amplitude, amplitude)
+    n = v.copy()
+    v = v * radius[:, None]
+    lo, hi = v.min(0), v.max(0)
+    v = (v - (lo + hi) * 0.5) / (hi - lo).max() + 0.5
+    return _pack(v, f, [lambert((0.5, 0.5, 0.5))], normals=n)
+
+
+def aimed_rays(n: int, positions: np.ndarray, seed: int = 1, spread: float = 1.5, tmax: float = math.inf):
+    """Rays from a box `spread` times the object's bounding box, each aimed at
+    a uniform point of the object's bounding box (most of them hit)."""
+    rs = Stream(seed, 3)
+    lo, hi = positions.min(0).astype(np.float64), positions.max(0).astype(np.float64)
+    c, h = (lo + hi) / 2, (hi - lo) / 2
+    o = c + h * spread * rs.uniform(3 * n, -1.0, 1.0).reshape(n, 3)
+    tgt = lo + (hi - lo) * rs.uniform(3 * n).reshape(n, 3)
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o = o.astype(np.float32)
+    d = d.astype(np.float32)
+    return dict(ox=np.ascontiguousarray(o[:, 0]), oy=np.ascontiguousarray(o[:, 1]),
+                oz=np.ascontiguousarray(o[:, 2]), dx=np.ascontiguousarray(d[:, 0]),
+                dy=np.ascontiguousarray(d[:, 1]), dz=np.ascontiguousarray(d[:, 2]),
+                tmax=np.full(n, tmax, dtype=np.float32))
+
+
+def random_rays(n: int, seed: int = 1, origin_lo: float = -2.0, origin_hi: float = 2.0, tmax: float = math.inf):
+    """SoA rays: origins uniform in [lo, hi]^3, directions uniform on the sphere."""
+    rs = Stream(seed, 2)
+    o = rs.uniform(3 * n, origin_lo, origin_hi).reshape(n, 3).astype(np.float32)
+    d = rs.unit_vectors(n).astype(np.float32)
+    return dict(ox=np.ascontiguousarray(o[:, 0]), oy=np.ascontiguousarray(o[:, 1]),
+                oz=np.ascontiguousarray(o[:, 2]), dx=np.ascontiguousarray(d[:, 0]),
+                dy=np.ascontiguousarray(d[:, 1]), dz=np.ascontiguousarray(d[:, 2]),
+                tmax=np.full(n, tmax, dtype=np.float32))

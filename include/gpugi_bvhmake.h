@@ -1,0 +1,70 @@
+/* gpugi_bvhmake.h — C ABI of the offline BVH builder (host-only C++).
+ *
+ * This library stands in for gpugi's `bvhmake` tool: it builds the
+ * stackless escape-pointer hierarchy and the fixed-size leaf blocks that the
+ * traversal kernels consume, and reads/writes bvhmake's NamedArray file.
+ *
+ *   gpugi_bvh_build       replaces BVHBuilder::BuildBVH        (bvhmake/bvhbuilder.cpp:526-555)
+ *                         with BuildSweep/BuildKdtree           (bvhmake/buildmethods/sweep.cpp:27-259,
+ *                                                                bvhmake/buildmethods/kdtree.cpp:9-157)
+ *                         and FitBox/FitEllipsoid               (bvhmake/fitmethods/aaboxfit.cpp:5-33,
+ *                                                                bvhmake/fitmethods/aaellipsoidfit.cpp:6-79)
+ *   gpugi_bvh_export      replaces BVHBuilder::ExportBVH + ExportTriangles + the
+ *                         node repacking of Scene::UploadHierarchy
+ *                                                               (bvhmake/bvhbuilder.cpp:569-612,710-722;
+ *                                                                gpugi/scene/scene.cpp:92-106)
+ *   gpugi_bvh_write_file  replaces the NamedArray export of bvhmake's main
+ *   gpugi_bvh_read_file                                         (bvhmake/main.cpp:27-146,
+ *                                                                documentation/fileformat.tex)
+ *
+ * Conventions: 0 = OK, negative = error (see gpugi_bvh_last_error). The
+ * caller owns every array passed in; the handle owns the built tree.
+ */
+#ifndef GPUGI_BVHMAKE_H
+#define GPUGI_BVHMAKE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gpugi_bvh gpugi_bvh;
+
+enum gpugi_build_method { GPUGI_BUILD_KDTREE = 0, GPUGI_BUILD_SWEEP = 1 };
+enum gpugi_fit_method { GPUGI_FIT_AABOX = 0, GPUGI_FIT_ELLIPSOID = 1 };
+
+/* Build a hierarchy over `numTriangles` triangles, each 4 uint32
+ * {v0, v1, v2, material}, indexing `positions` (3 floats per vertex).
+ * leafSize is the number of triangle slots per leaf block (bvhmake: 8).
+ * seed drives the ellipsoid fit's particle swarm (the reference leaves it
+ * uninitialised, bvhmake/fitmethods/optimize.inl:158). */
+int gpugi_bvh_build(const float* positions, uint32_t numVertices, const uint32_t* triangles,
+                    uint32_t numTriangles, uint32_t buildMethod, uint32_t fitMethod,
+                    uint32_t leafSize, uint64_t seed, gpugi_bvh** out);
+
+/* Sizes of the built hierarchy. boundsKind: 0 = AABB, 1 = ellipsoid. */
+int gpugi_bvh_info(const gpugi_bvh* bvh, uint32_t* numNodes, uint32_t* numLeafBlocks,
+                   uint32_t* leafSize, uint32_t* boundsKind, uint32_t* maxDepth);
+
+/* Export in the GPU layout of Scene::TreeNode<Box> (gpugi/scene/scene.hpp:30-38):
+ * 8 floats per node {min.xyz, firstChild bits, max.xyz, escape bits}
+ * (ellipsoid: {center.xyz, firstChild, radii.xyz, escape}), leafSize
+ * int32x4 slots per leaf block {v0, v1, v2, material}, invalid = {0,0,0,0},
+ * and optionally the parent index of every node (may be NULL). */
+int gpugi_bvh_export(const gpugi_bvh* bvh, float* hierarchy, int32_t* slots, uint32_t* parents);
+
+/* Write/read bvhmake's NamedArray file ("vertices", "triangles",
+ * "hierarchy", "bounding_aabox"/"bounding_ellipsoid"). The reader returns a
+ * handle usable with gpugi_bvh_info/gpugi_bvh_export and fills the vertex
+ * positions through gpugi_bvh_vertices. */
+int gpugi_bvh_write_file(const gpugi_bvh* bvh, const char* path);
+int gpugi_bvh_read_file(const char* path, gpugi_bvh** out);
+int gpugi_bvh_vertices(const gpugi_bvh* bvh, uint32_t* numVertices, float* positions /* may be NULL */);
+
+void gpugi_bvh_free(gpugi_bvh* bvh);
+const char* gpugi_bvh_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

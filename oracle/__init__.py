@@ -1,0 +1,109 @@
+"""ORACLE — test infrastructure only.
+
+ctypes front end of oracle/lib/liboracle.so, the CPU restatement of gpugi's
+shaders. Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline
+leg may import this package; the product never does.
+
+Parity status: UNPINNED (the reference ships no golden vectors and cannot be
+built or run here); see oracle/glsl.hpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        from . import build as _b
+        path = _b.build()
+        L = C.CDLL(str(path))
+        P, U32, U64, I = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+        L.oracle_trace_closest.argtypes = [P, U32, U32, P, U32, U32, P, U32] + [P] * 7 + [U64, P, P, P, P, P, I]
+        L.oracle_trace_any.argtypes = [P, U32, U32, P, U32, U32, P, U32] + [P] * 7 + [U64, P, P, I]
+        L.oracle_bruteforce_closest.argtypes = [P, U32, P] + [P] * 7 + [U64, P, P, I]
+        if hasattr(L, "oracle_render"):
+            L.oracle_render.restype = I
+        _LIB = L
+    return _LIB
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def threads() -> int:
+    return int(os.environ.get("ORACLE_THREADS", "0"))
+
+
+def _scene_args(bvh, positions):
+    hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
+    slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    keep = (hier, slots, pos)
+    return keep, [_p(hier), hier.shape[0], bvh.bounds_kind, _p(slots), slots.shape[0], bvh.leaf_size, _p(pos),
+                  pos.shape[0]]
+
+
+def _rays(rays):
+    return [np.ascontiguousarray(rays[k], dtype=np.float32) for k in ("ox", "oy", "oz", "dx", "dy", "dz", "tmax")]
+
+
+def trace_closest(bvh, positions, rays, counters=False, num_threads=None):
+    keep, sargs = _scene_args(bvh, positions)
+    r = _rays(rays)
+    n = r[0].shape[0]
+    slot = np.empty(n, np.int32)
+    t = np.empty(n, np.float32)
+    u = np.empty(n, np.float32)
+    v = np.empty(n, np.float32)
+    cnt = np.empty((n, 3), np.uint32) if counters else None
+    lib().oracle_trace_closest(*sargs, *[_p(a) for a in r], n, _p(slot), _p(t), _p(u), _p(v), _p(cnt),
+                               threads() if num_threads is None else num_threads)
+    out = dict(slot=slot, t=t, u=u, v=v)
+    if counters:
+        out["counters"] = cnt
+    return out
+
+
+def trace_any(bvh, positions, rays, counters=False, num_threads=None):
+    keep, sargs = _scene_args(bvh, positions)
+    r = _rays(rays)
+    n = r[0].shape[0]
+    occ = np.empty(n, np.uint8)
+    cnt = np.empty((n, 3), np.uint32) if counters else None
+    lib().oracle_trace_any(*sargs, *[_p(a) for a in r], n, _p(occ), _p(cnt),
+                           threads() if num_threads is None else num_threads)
+    out = dict(occluded=occ)
+    if counters:
+        out["counters"] = cnt
+    return out
+
+
+def bruteforce_closest(slots, positions, rays, num_threads=None):
+    slots = np.ascontiguousarray(slots, dtype=np.int32)
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    r = _rays(rays)
+    n = r[0].shape[0]
+    slot = np.empty(n, np.int32)
+    t = np.empty(n, np.float32)
+    lib().oracle_bruteforce_closest(_p(slots), slots.shape[0], _p(pos), *[_p(a) for a in r], n, _p(slot), _p(t),
+                                    threads() if num_threads is None else num_threads)
+    return dict(slot=slot, t=t)
+
+
+def algorithmic_bytes(counters: np.ndarray, any_hit: bool = False) -> np.ndarray:
+    """Bytes per ray of gpugi's own fetch pattern: 24 (ray in) + 16 (t, id, u, v
+    out; 4 for any-hit) + 32 per node + 16 per leaf slot + 36 per valid triangle
+    (node 32 B, gpugi/scene/scene.hpp:30-38; slot 16 B, traceray.glsl:126;
+    3 x 12 B positions, traceray.glsl:137-139)."""
+    c = counters.astype(np.int64)
+    out_bytes = 4 if any_hit else 16
+    return 24 + out_bytes + 32 * c[:, 0] + 16 * c[:, 1] + 36 * c[:, 2]

@@ -1,0 +1,125 @@
+"""The bvhmake restatement produces a valid escape tree in gpugi's layout.
+
+Checks the invariants bvhmake asserts or relies on (bvhmake/bvhbuilder.cpp:
+551, 699-722; buildmethods/*): preorder with the root at 0, every triangle in
+exactly one leaf slot, padding only at the end of a block, escape(left) =
+right, escape(right) = parent's escape, escape(root) = 0, and bounds that
+contain every triangle below them.
+"""
+import numpy as np
+import pytest
+
+from gpugi_gb300 import bvh, scenes
+
+
+def _check_tree(b, tris, positions):
+    n = b.num_nodes
+    fc = b.first_child
+    esc = b.escape
+    L = b.leaf_size
+    assert esc[0] == 0
+    seen = np.zeros(tris.shape[0], dtype=np.int64)
+    tri_key = {tuple(t): i for i, t in enumerate(tris.tolist())}
+    # subtree triangle boxes, bottom-up
+    lo = np.full((n, 3), np.inf, np.float32)
+    hi = np.full((n, 3), -np.inf, np.float32)
+    for i in range(n - 1, -1, -1):
+        c = int(fc[i])
+        if c & 0x80000000:
+            blk = c & 0x7FFFFFFF
+            block = b.slots[blk * L:(blk + 1) * L]
+            valid = block[:, 0] != block[:, 1]
+            k = int(valid.sum())
+            assert k >= 1 and valid[:k].all() and not valid[k:].any()  # padding at the end only
+            assert (block[~valid] == 0).all()
+            for t in block[valid]:
+                seen[tri_key[tuple(int(x) for x in t)]] += 1
+                p = positions[t[:3]]
+                lo[i] = np.minimum(lo[i], p.min(0))
+                hi[i] = np.maximum(hi[i], p.max(0))
+        else:
+            assert i < c < n, "left child follows its parent (preorder)"
+            r = int(esc[c])
+            assert c < r < n, "escape(left) is the right sibling"
+            assert esc[r] == esc[i], "escape(right) is the parent's escape"
+            assert b.parents[c] == i and b.parents[r] == i
+            lo[i] = np.minimum(lo[c], lo[r])
+            hi[i] = np.maximum(hi[c], hi[r])
+    assert (seen == 1).all(), "every triangle appears in exactly one leaf slot"
+    if b.bounds_kind == 0:
+        assert (b.hierarchy[:, 0:3] <= lo).all() and (b.hierarchy[:, 4:7] >= hi).all()
+    else:  # ellipsoid contains the box corners of everything below
+        c, r = b.hierarchy[:, 0:3].astype(np.float64), b.hierarchy[:, 4:7].astype(np.float64)
+        for corner in range(8):
+            sel = [(corner >> k) & 1 for k in range(3)]
+            p = np.where(np.array(sel, bool)[None, :], hi, lo).astype(np.float64)
+            q = ((p - c) / r) ** 2
+            inside = q.sum(1)
+            # leaves may be tighter than the box ellipsoid: check vertices instead below
+        for i in range(n):
+            ci = int(fc[i])
+            if ci & 0x80000000:
+                blk = ci & 0x7FFFFFFF
+                block = b.slots[blk * L:(blk + 1) * L]
+                block = block[block[:, 0] != block[:, 1]]
+                p = positions[block[:, :3].reshape(-1)].astype(np.float64)
+                assert (((p - c[i]) / r[i]) ** 2).sum(1).max() <= 1.0 + 1e-6
+
+
+@pytest.mark.parametrize("method", ["sweep", "kdtree"])
+@pytest.mark.parametrize("leaf_size", [1, 2, 8])
+def test_escape_tree_invariants(built, method, leaf_size):
+    sc = scenes.displaced_icosphere(2000, seed=5)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, leaf_size=leaf_size)
+    _check_tree(b, sc["triangles"], sc["positions"])
+
+
+def test_ellipsoid_bounds_contain_leaves(built):
+    sc = scenes.displaced_icosphere(600, seed=7)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="kdtree", fit="ellipsoid")
+    assert b.bounds_kind == 1
+    _check_tree(b, sc["triangles"], sc["positions"])
+
+
+@pytest.mark.parametrize("ntri", [1, 7, 8, 9, 17])
+def test_small_scenes(built, ntri):
+    sc = scenes.displaced_icosphere(ntri, seed=2)
+    for method in ("sweep", "kdtree"):
+        b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method)
+        _check_tree(b, sc["triangles"], sc["positions"])
+        if ntri <= 8:
+            assert b.num_nodes == 1 and (b.first_child[0] & 0x80000000)
+
+
+def test_deterministic(built):
+    sc = scenes.displaced_icosphere(3000, seed=11)
+    a = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    assert np.array_equal(a.hierarchy.view(np.uint32), b.hierarchy.view(np.uint32))
+    assert np.array_equal(a.slots, b.slots)
+
+
+def test_rejects_bad_input(built):
+    sc = scenes.displaced_icosphere(64, seed=1)
+    with pytest.raises(ValueError):
+        bvh.build_bvh(sc["positions"], sc["triangles"][:0])
+    bad = sc["triangles"].copy()
+    bad[3, 1] = 10 ** 6
+    with pytest.raises(ValueError):
+        bvh.build_bvh(sc["positions"], bad)
+    bad = sc["triangles"].copy()
+    bad[5, 1] = bad[5, 0]
+    with pytest.raises(ValueError):
+        bvh.build_bvh(sc["positions"], bad)
+
+
+def test_file_round_trip(built, tmp_path):
+    sc = scenes.displaced_icosphere(1500, seed=3)
+    p = tmp_path / "scene.bim"
+    bvh.write_bvh_file(sc["positions"], sc["triangles"], str(p), method="sweep", leaf_size=4)
+    b = bvh.read_bvh_file(str(p))
+    ref = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", leaf_size=4)
+    assert b.leaf_size == 4
+    assert np.array_equal(b.hierarchy.view(np.uint32), ref.hierarchy.view(np.uint32))
+    assert np.array_equal(b.slots, ref.slots)
+    assert np.array_equal(b.positions, sc["positions"])

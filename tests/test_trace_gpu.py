@@ -1,0 +1,189 @@
+"""GPU traversal parity: the sm_103a kernels against the oracle, through the C ABI.
+
+Bar (bit-exact for index work): hit slot identical, t identical to the bit
+(the spec allows 2 ulp; the kernels reproduce the exact IEEE sequence),
+barycentrics identical, any-hit flags identical.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from gpugi_gb300 import bvh, cuda, scenes
+
+pytestmark = pytest.mark.gpu
+
+T_ULP_TOL = 2  # spec tolerance on t; the implementation is expected to be exact
+
+
+def _bits(a):
+    return np.asarray(a, np.float32).view(np.int32)
+
+
+def _compare_closest(g, o):
+    assert np.array_equal(g["slot"], o["slot"]), f"{(g['slot'] != o['slot']).sum()} slot mismatches"
+    dt = np.abs(_bits(g["t"]).astype(np.int64) - _bits(o["t"]).astype(np.int64))
+    assert dt.max() <= T_ULP_TOL
+    assert (dt == 0).all(), "t differs in the last bits"
+    hit = o["slot"] >= 0
+    assert np.array_equal(_bits(g["u"])[hit], _bits(o["u"])[hit])
+    assert np.array_equal(_bits(g["v"])[hit], _bits(o["v"])[hit])
+
+
+@pytest.fixture(scope="module")
+def icosphere_65536():
+    sc = scenes.displaced_icosphere(65536, seed=1)
+    return sc
+
+
+@pytest.mark.parametrize("method,leaf", [("sweep", 8), ("kdtree", 8), ("sweep", 2)])
+def test_closest_and_any_match_oracle(cuda_ctx, icosphere_65536, method, leaf):
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, leaf_size=leaf)
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    for rays in (scenes.random_rays(1 << 18, seed=3), scenes.aimed_rays(1 << 18, sc["positions"], seed=4)):
+        g = cuda.trace_closest(cuda_ctx, ds, rays)
+        o = oracle.trace_closest(b, sc["positions"], rays)
+        _compare_closest(g, o)
+        occ = cuda.trace_any(cuda_ctx, ds, rays)
+        oa = oracle.trace_any(b, sc["positions"], rays)["occluded"]
+        assert np.array_equal(occ, oa)
+    ds.close()
+
+
+def test_full_size_properties(cuda_ctx, icosphere_65536):
+    """2^20 rays of the closest-hit workload: exact against the oracle, and
+    size-independent checks (any-hit == closest-hit hit mask, t > 1e-4)."""
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    rays = scenes.random_rays(1 << 20, seed=1)
+    g = cuda.trace_closest(cuda_ctx, ds, rays)
+    o = oracle.trace_closest(b, sc["positions"], rays)
+    _compare_closest(g, o)
+    occ = cuda.trace_any(cuda_ctx, ds, rays)
+    assert np.array_equal(occ.astype(bool), g["slot"] >= 0)
+    assert (g["t"][g["slot"] >= 0] > 1e-4).all()
+    assert np.isinf(g["t"][g["slot"] < 0]).all()
+    ds.close()
+
+
+def test_device_entry_points(cuda_ctx, icosphere_65536):
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    rays = scenes.aimed_rays(100_003, sc["positions"], seed=12)
+    dr = {k: torch.from_numpy(rays[k]).cuda() for k in cuda.RAY_KEYS}
+    n = rays["ox"].shape[0]
+    out = dict(slot=torch.empty(n, dtype=torch.int32, device="cuda"), t=torch.empty(n, device="cuda"),
+               u=torch.empty(n, device="cuda"), v=torch.empty(n, device="cuda"))
+    torch.cuda.synchronize()
+    cuda.trace_closest_device(cuda_ctx, ds, dr, out)
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    cuda.trace_any_device(cuda_ctx, ds, dr, occ)
+    cuda_ctx.sync()
+    g = {k: v.cpu().numpy() for k, v in out.items()}
+    o = oracle.trace_closest(b, sc["positions"], rays)
+    _compare_closest(g, o)
+    assert np.array_equal(occ.cpu().numpy(), oracle.trace_any(b, sc["positions"], rays)["occluded"])
+    ds.close()
+
+
+def test_walk_statistics_match_oracle_counters(cuda_ctx, icosphere_65536):
+    """The device fetch counters (used for the roofline's algorithmic bytes)
+    equal the oracle's TRACERAY_DEBUG_VARS-style counters."""
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    for any_hit in (False, True):
+        for rays in (scenes.random_rays(50_000, seed=31), scenes.aimed_rays(50_000, sc["positions"], seed=32)):
+            dr = {k: torch.from_numpy(rays[k]).cuda() for k in cuda.RAY_KEYS}
+            sums = cuda.trace_stats_device(cuda_ctx, ds, dr, any_hit=any_hit)
+            f = oracle.trace_any if any_hit else oracle.trace_closest
+            c = f(b, sc["positions"], rays, counters=True)["counters"].astype(np.uint64).sum(0)
+            assert np.array_equal(sums, c), (any_hit, sums, c)
+            assert cuda.algorithmic_bytes(sums, 50_000, any_hit) == int(
+                oracle.algorithmic_bytes(f(b, sc["positions"], rays, counters=True)["counters"], any_hit).sum())
+    ds.close()
+
+
+def test_triangle_known_answers_gpu(cuda_ctx):
+    import json
+    from pathlib import Path
+    cases = json.loads((Path(__file__).resolve().parent / "golden" / "kat_triangles.json").read_text())["cases"]
+    for c in cases:
+        positions = np.array(c["triangle"], dtype=np.float32)
+        tri = np.array([[0, 1, 2, 0]], dtype=np.uint32)
+        b = bvh.build_bvh(positions, tri)
+        ds = cuda_ctx.upload_scene(b, positions)
+        rays = {k: np.array([v], np.float32) for k, v in zip(("ox", "oy", "oz"), c["origin"])}
+        rays.update({k: np.array([v], np.float32) for k, v in zip(("dx", "dy", "dz"), c["direction"])})
+        rays["tmax"] = np.array([c["tmax"] if c["tmax"] is not None else math.inf], np.float32)
+        g = cuda.trace_closest(cuda_ctx, ds, rays)
+        assert (g["slot"][0] >= 0) == c["walk_hit"], c["name"]
+        if c["walk_hit"]:
+            assert g["t"][0] == np.float32(c["t"]) and g["u"][0] == np.float32(c["u"]), c["name"]
+            assert g["v"][0] == np.float32(c["v"]), c["name"]
+        ds.close()
+
+
+def test_edge_rays(cuda_ctx):
+    """Axis-parallel directions (inf*0 = NaN slabs), origins inside the mesh,
+    on bounding planes, zero-length tmax, NaN-free misses, n = 0."""
+    sc = scenes.displaced_icosphere(5000, seed=3)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", leaf_size=4)
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    dirs = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+                     [0.6, 0.8, 0], [0, 0.6, -0.8], [-0.6, 0, 0.8]], np.float32)
+    lo, hi = sc["positions"].min(0), sc["positions"].max(0)
+    origins = [np.zeros(3), (lo + hi) / 2, lo, hi, np.array([lo[0], 0.5, 0.5]), np.array([2.0, 0.5, 0.5]),
+               np.array([0.5, 0.5, 0.5]), np.array([0.5, 0.5, -3.0])]
+    o = np.array([oo for oo in origins for _ in dirs], np.float32)
+    d = np.array([dd for _ in origins for dd in dirs], np.float32)
+    rays = dict(ox=o[:, 0].copy(), oy=o[:, 1].copy(), oz=o[:, 2].copy(), dx=d[:, 0].copy(), dy=d[:, 1].copy(),
+                dz=d[:, 2].copy())
+    for tm in (math.inf, 3.402823466e38, 0.3, 0.0, 1e-4):
+        rays["tmax"] = np.full(o.shape[0], tm, np.float32)
+        g = cuda.trace_closest(cuda_ctx, ds, rays)
+        orc = oracle.trace_closest(b, sc["positions"], rays)
+        _compare_closest(g, orc)
+        assert np.array_equal(cuda.trace_any(cuda_ctx, ds, rays), oracle.trace_any(b, sc["positions"], rays)["occluded"])
+    empty = {k: np.zeros(0, np.float32) for k in cuda.RAY_KEYS}
+    g = cuda.trace_closest(cuda_ctx, ds, empty)
+    assert g["slot"].shape == (0,)
+    ds.close()
+
+
+@pytest.mark.parametrize("ntri", [1, 3, 8, 9])
+def test_tiny_scenes(cuda_ctx, ntri):
+    sc = scenes.displaced_icosphere(ntri, seed=2)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    rays = scenes.aimed_rays(20000, sc["positions"], seed=5, spread=3.0)
+    _compare_closest(cuda.trace_closest(cuda_ctx, ds, rays), oracle.trace_closest(b, sc["positions"], rays))
+    ds.close()
+
+
+def test_rejects_malformed_hierarchy(cuda_ctx):
+    sc = scenes.displaced_icosphere(512, seed=2)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    bad = bvh.BVH(b.hierarchy.copy(), b.slots.copy(), b.parents, b.leaf_size, 0, b.max_depth)
+    esc = bad.hierarchy[:, 7].view(np.uint32)
+    esc[5] = 2  # an escape pointing backwards would loop
+    with pytest.raises(cuda.GpugiError) as e:
+        cuda_ctx.upload_scene(bad, sc["positions"])
+    assert e.value.status == 2
+    bad = bvh.BVH(b.hierarchy.copy(), b.slots.copy(), b.parents, b.leaf_size, 0, b.max_depth)
+    bad.slots[3, 2] = 10 ** 7
+    with pytest.raises(cuda.GpugiError):
+        cuda_ctx.upload_scene(bad, sc["positions"])
+    bad = bvh.BVH(b.hierarchy.copy(), b.slots.copy(), b.parents, b.leaf_size, 0, b.max_depth)
+    fc = bad.hierarchy[:, 3].view(np.uint32)
+    leaf = np.nonzero(fc & 0x80000000)[0][0]
+    fc[leaf] = 0x80000000 | 0x7FFFFFF
+    with pytest.raises(cuda.GpugiError):
+        cuda_ctx.upload_scene(bad, sc["positions"])
+    assert cuda_ctx.device_error_bits() == 0
