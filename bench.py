@@ -206,6 +206,7 @@ def run_ours(args, world, rank, local):
     dev = torch.device("cuda", local)
     sc, b, host_batches = make_workload()
     ctx = cuda.Context(local)
+    ctx.set_trace_config(mode=args.trace_mode)
     ds = ctx.upload_scene(b, sc["positions"])
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     batches = [{k: torch.from_numpy(rb[k]).to(dev) for k in cuda.RAY_KEYS} for rb in host_batches]
@@ -282,7 +283,8 @@ def run_ours(args, world, rank, local):
                          "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)" if peak_src == "measured"
                          else "fallback 6.8 TB/s",
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3,
-                         "kernel": "k_trace_closest<AABB>"},
+                         "kernel": "k_trace_persistent<closest, AABB>" if args.trace_mode == 1
+                         else "k_trace_closest<AABB>"},
             "gpu_launches": args.steps,
             "clocks": clk.summary()}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -301,6 +303,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--trace-mode", type=int, default=1, help="0: thread per ray, 1: persistent lane refill")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

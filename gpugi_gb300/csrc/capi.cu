@@ -70,7 +70,9 @@ gpugi_status gpugi_create(gpugi_ctx** out, const gpugi_opts* opts) {
         return GPUGI_ERROR_INVALID_ARGUMENT;
     }
     if ((e = cudaSetDevice(ctx->device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaMalloc(&ctx->errWord, 16)) != cudaSuccess || (e = cudaMemset(ctx->errWord, 0, 16)) != cudaSuccess) {
+        (e = cudaMalloc(&ctx->errWord, 16)) != cudaSuccess || (e = cudaMemset(ctx->errWord, 0, 16)) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->scratch, 256)) != cudaSuccess || (e = cudaMemset(ctx->scratch, 0, 256)) != cudaSuccess) {
+        if (ctx->errWord) cudaFree(ctx->errWord);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return GPUGI_ERROR_CUDA;
@@ -86,6 +88,7 @@ void gpugi_destroy(gpugi_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->stageDev) cudaFree(ctx->stageDev);
     if (ctx->errWord) cudaFree(ctx->errWord);
+    if (ctx->scratch) cudaFree(ctx->scratch);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -108,12 +111,13 @@ gpugi_status gpugi_device_error_bits(gpugi_ctx* ctx, uint32_t* bits) {
     return GPUGI_OK;
 }
 
-gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t blockSize, uint32_t sharedNodes) {
+gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (mode > 1) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "mode must be 0 (thread per ray) or 1 (persistent)");
     if (blockSize == 0 || blockSize > 256 || blockSize % 32 != 0)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "blockSize must be a multiple of 32 in [32, 256]");
+    ctx->traceMode = mode;
     ctx->traceBlock = blockSize;
-    ctx->sharedNodes = sharedNodes;
     return GPUGI_OK;
 }
 

@@ -17,8 +17,9 @@ struct gpugi_ctx {
     void* stageDev = nullptr;
     size_t stageDevBytes = 0;
     // trace tuning
+    uint32_t traceMode = 1;  // 0 = one thread per ray, 1 = persistent lane refill
     uint32_t traceBlock = 128;
-    uint32_t sharedNodes = 0;
+    void* scratch = nullptr;  // 256 B of device counters (work distribution)
     int numSMs = 0;
 };
 
@@ -50,6 +51,10 @@ gpugi_status launch_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float
                               const float* oz, const float* dx, const float* dy, const float* dz,
                               const float* tmax, uint64_t n, uint8_t* occluded);
 
+gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
+                                     const float* oy, const float* oz, const float* dx, const float* dy,
+                                     const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
+                                     float* u, float* v, uint8_t* occluded);
 gpugi_status launch_trace_stats(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
                                 const float* oz, const float* dx, const float* dy, const float* dz,
                                 const float* tmax, uint64_t n, uint32_t anyHit, unsigned long long* sums);

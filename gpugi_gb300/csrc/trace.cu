@@ -41,6 +41,79 @@ __global__ void __launch_bounds__(256) k_trace_any(DevScene s, const float* __re
     occluded[i] = r.slot >= 0 ? 1 : 0;
 }
 
+// Persistent walk: a grid sized to fill the GPU once; every warp keeps all 32
+// lanes busy by handing each finished lane the next ray index from a global
+// counter (one atomic per warp per refill). Each ray still performs exactly
+// trace_ray's sequence of tests, so results are identical.
+template <bool ANY_HIT, int BOUNDS>
+__global__ void __launch_bounds__(128) k_trace_persistent(
+    DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
+    const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
+    const float* __restrict__ tmax, uint64_t n, int32_t* __restrict__ slot, float* __restrict__ t,
+    float* __restrict__ u, float* __restrict__ v, uint8_t* __restrict__ occluded, unsigned long long* counter,
+    uint32_t* err) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lanesBelow = (1u << lane) - 1u;
+    WalkState w;
+    uint64_t ray = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        const bool need = !active && !exhausted;
+        const unsigned needMask = __ballot_sync(0xffffffffu, need);
+        if (needMask) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(counter, (unsigned long long)__popc(needMask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (need) {
+                const uint64_t my = base + (uint64_t)__popc(needMask & lanesBelow);
+                if (my < n) {
+                    ray = my;
+                    walk_begin(w, s, make_float3(__ldg(ox + my), __ldg(oy + my), __ldg(oz + my)),
+                               make_float3(__ldg(dx + my), __ldg(dy + my), __ldg(dz + my)), __ldg(tmax + my));
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err)) {
+            if (ANY_HIT) {
+                occluded[ray] = w.slot >= 0 ? 1 : 0;
+            } else {
+                slot[ray] = w.slot;
+                t[ray] = w.len;
+                u[ray] = w.u;
+                v[ray] = w.v;
+            }
+            active = false;
+        }
+    }
+}
+
+gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
+                                     const float* oy, const float* oz, const float* dx, const float* dy,
+                                     const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
+                                     float* u, float* v, uint8_t* occluded) {
+    if (n == 0) return GPUGI_OK;
+    unsigned long long* counter = reinterpret_cast<unsigned long long*>(ctx->scratch);
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
+    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
+              const float*, uint64_t, int32_t*, float*, float*, float*, uint8_t*, unsigned long long*, uint32_t*);
+    if (!ell) k = anyHit ? k_trace_persistent<true, 0> : k_trace_persistent<false, 0>;
+    else k = anyHit ? k_trace_persistent<true, 1> : k_trace_persistent<false, 1>;
+    int perSM = 0;
+    GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k, 128, 0));
+    uint64_t grid = (uint64_t)ctx->numSMs * (uint64_t)(perSM > 0 ? perSM : 1);
+    const uint64_t needed = (n + 127) / 128;
+    if (grid > needed) grid = needed;
+    k<<<(unsigned)grid, 128, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, occluded,
+                                               counter, ctx->errWord);
+    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
 template <int BOUNDS, bool ANY>
 __global__ void __launch_bounds__(256) k_trace_stats(DevScene s, const float* __restrict__ ox,
                                                      const float* __restrict__ oy, const float* __restrict__ oz,
@@ -92,6 +165,8 @@ gpugi_status launch_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const f
                                   const float* tmax, uint64_t n, int32_t* slot, float* t, float* u, float* v) {
     if (n == 0) return GPUGI_OK;
     if (n > (uint64_t)0xFFFFFFFFu * 256u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many rays");
+    if (ctx->traceMode == 1)
+        return launch_trace_persistent(ctx, sc, false, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, nullptr);
     const uint32_t block = ctx->traceBlock;
     if (sc->dev.boundsKind == GPUGI_BOUNDS_AABB)
         k_trace_closest<0><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
@@ -108,6 +183,9 @@ gpugi_status launch_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float
                               const float* tmax, uint64_t n, uint8_t* occluded) {
     if (n == 0) return GPUGI_OK;
     if (n > (uint64_t)0xFFFFFFFFu * 256u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many rays");
+    if (ctx->traceMode == 1)
+        return launch_trace_persistent(ctx, sc, true, ox, oy, oz, dx, dy, dz, tmax, n, nullptr, nullptr, nullptr,
+                                       nullptr, occluded);
     const uint32_t block = ctx->traceBlock;
     if (sc->dev.boundsKind == GPUGI_BOUNDS_AABB)
         k_trace_any<0><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,

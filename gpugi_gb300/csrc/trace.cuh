@@ -147,4 +147,74 @@ GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLe
     return r;
 }
 
+// One ray's walk as a resumable state machine, advanced one test at a time.
+// The sequence of node and triangle tests is the same as trace_ray's; the
+// state lets a persistent warp refill a finished lane with the next ray
+// instead of idling until the warp's longest walk ends.
+struct WalkState {
+    float3 o, d, inv;
+    float len;
+    uint32_t node;  // next node to test, NODE_DONE when the escape chain ended
+    uint32_t cur, end;  // leaf slots still to test
+    uint32_t budget;
+    int32_t slot;
+    float u, v;
+};
+constexpr uint32_t NODE_DONE = 0xFFFFFFFFu;
+
+GPUGI_D void walk_begin(WalkState& w, const DevScene& s, float3 o, float3 d, float tmax) {
+    w.o = o;
+    w.d = d;
+    w.inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
+    w.len = tmax;
+    w.node = 0;
+    w.cur = w.end = 0;
+    w.budget = s.numNodes;
+    w.slot = -1;
+    w.u = w.v = 0.0f;
+}
+
+// Perform one test. Returns true when the walk is over (for ANY_HIT also
+// when a triangle was accepted).
+template <bool ANY_HIT, int BOUNDS>
+GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord) {
+    if (w.cur < w.end) {
+        float h, by, bz;
+        if (intersect_triangle(w.o, w.d, s.tris + 3 * (size_t)w.cur, h, by, bz) && h < w.len) {
+            w.len = h;
+            w.slot = (int32_t)w.cur;
+            w.u = by;
+            w.v = bz;
+            if (ANY_HIT) return true;
+        }
+        ++w.cur;
+    } else {
+        if (w.budget-- == 0) {
+            raise_error(errWord, DEVERR_TRAVERSAL_CAP);
+            w.node = NODE_DONE;
+            return true;
+        }
+        const float4 a = __ldg(s.nodes + 2 * w.node);
+        const float4 b = __ldg(s.nodes + 2 * w.node + 1);
+        const uint32_t child = __float_as_uint(a.w);
+        const uint32_t escape = __float_as_uint(b.w);
+        float firstHit;
+        bool hit;
+        if (BOUNDS == 0) hit = intersect_box(w.o, w.inv, a, b, firstHit);
+        else hit = intersect_ellipsoid(w.o, w.d, a, b, firstHit);
+        if (hit && firstHit <= w.len) {
+            if (child & LEAF_FLAG) {
+                w.cur = (child & LEAF_BLOCK_MASK) * s.leafSize;
+                w.end = w.cur + ((child >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK);
+                w.node = escape ? escape : NODE_DONE;
+            } else {
+                w.node = child;
+            }
+        } else {
+            w.node = escape ? escape : NODE_DONE;
+        }
+    }
+    return w.cur >= w.end && w.node == NODE_DONE;
+}
+
 }  // namespace gpugi

@@ -106,8 +106,8 @@ class Context:
     def stream(self) -> int:
         return lib().gpugi_stream(self._h) or 0
 
-    def set_trace_config(self, block_size: int = 128, shared_nodes: int = 0):
-        self.check(lib().gpugi_set_trace_config(self._h, block_size, shared_nodes))
+    def set_trace_config(self, mode: int = 1, block_size: int = 128):
+        self.check(lib().gpugi_set_trace_config(self._h, mode, block_size))
 
     def close(self):
         if self._h:

@@ -135,9 +135,11 @@ gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* scene,
                                       const float* dx, const float* dy, const float* dz,
                                       const float* tmax, uint64_t n, uint32_t anyHit, uint64_t sums[3]);
 
-/* Traversal tuning (set by the autotuner): threads per block and the number
- * of top-of-tree nodes staged in shared memory (0 disables staging). */
-gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t blockSize, uint32_t sharedNodes);
+/* Traversal tuning (set by the autotuner). mode 0: one thread per ray, grid
+ * of ceil(n / blockSize) blocks; mode 1 (default): persistent warps that
+ * refill finished lanes from a device ray counter. Both perform the same
+ * tests per ray and return identical results. */
+gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,750 @@
+// ORACLE — test infrastructure only (see glsl.hpp for the parity status).
+//
+// CPU restatement of gpugi's rendering passes, one shader invocation per
+// pixel or light particle, run on std::threads:
+//   random.glsl:1-87, helper.glsl:22-47       RNG, samplers, ONB, normal packing
+//   scenedata.glsl:94-105                     GetTriangleHitInfo
+//   materials.glsl:19-436                     BSDF sampling / evaluation
+//   lightsource.glsl:3-93                     EstimateDirectLight (NEE)
+//   pathtracer.comp:16-110                    PT pass
+//   lighttracer.comp:48-193 +
+//   screenreproject.glsl:19-227 +
+//   showlightcaches.comp:9-65                 LT pass
+//   bidirpathtracer/*                         BPT light-cache + eye pass
+// Two documented additions that the reference lacks: a constant sky radiance
+// returned on a miss (the reference samples a cube map, black by default) and
+// directional light samples (normalThetaCos == 3) for a sun.
+#include <atomic>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "oracle.hpp"
+
+using namespace glsl;
+
+namespace oracle {
+
+static const float PI = 3.14159265358979f;
+static const float PI_2 = 6.28318530717958f;
+static const float DIVISOR_EPSILON = 1e-5f;
+static const float RAY_HIT_EPSILON = 0.0001f;
+static const float RAY_MAX = 3.402823466e+38f;
+
+// ---------------------------------------------------------------- random.glsl
+static uint wanghash(uint x) {
+    x = (x ^ 61u) ^ (x >> 16);
+    x *= 9u;
+    x = x ^ (x >> 4);
+    x *= 0x27d4eb2du;
+    x = x ^ (x >> 15);
+    return x;
+}
+static uint RandomUInt(uint& seed) {
+    seed ^= (seed << 13);
+    seed ^= (seed >> 17);
+    seed ^= (seed << 5);
+    return seed;
+}
+static uint InitRandomSeed(uint frameSeed, uint invocationID) { return wanghash(frameSeed + invocationID); }
+// float(RandomUInt) / 4294967297.0: the float literal rounds to 2^32.
+static float Random(uint& seed) { return float(RandomUInt(seed)) / 4294967297.0f; }
+static vec2 Random2(uint& seed) {
+    float a = Random(seed);
+    float b = Random(seed);
+    return vec2(a, b);
+}
+static vec3 SampleDirection(vec2 r) {
+    float cosTheta = r.x * 2.0f - 1.0f;
+    float sinTheta = sqrt((1.0f - cosTheta) * (1.0f + cosTheta));
+    float phi = r.y * PI_2;
+    return normalize(vec3(sinTheta * std::sin(phi), sinTheta * std::cos(phi), cosTheta));
+}
+static vec3 SampleHemisphereCosine(vec2 r, vec3 U, vec3 V, vec3 W) {
+    float phi = PI_2 * r.x;
+    float sinTheta = sqrt(r.y);
+    float x = sinTheta * std::cos(phi);
+    float y = sinTheta * std::sin(phi);
+    float z = sqrt(1.0f - r.y);
+    return x * U + y * V + z * W;
+}
+static vec3 SamplePhongLobe(vec2 r, float exponent, vec3 U, vec3 V, vec3 W) {
+    float phi = PI_2 * r.x;
+    float power = std::pow(r.y, 1.0f / (exponent + 1.0f));
+    float scale = sqrt(1.0f - power * power);
+    float x = std::cos(phi) * scale;
+    float y = std::sin(phi) * scale;
+    float z = power;
+    return x * U + y * V + z * W;
+}
+
+// ---------------------------------------------------------------- helper.glsl
+static void CreateONB(vec3 n, vec3& U, vec3& V) {
+    U = cross(n, vec3(0.0f, 1.0f, 0.0f));
+    vec3 a = abs(U);
+    if (a.x < 0.0001f && a.y < 0.0001f && a.z < 0.0001f) U = cross(n, vec3(1.0f, 0.0f, 0.0f));
+    U = normalize(U);
+    V = cross(n, U);
+}
+static float GetLuminance(vec3 rgb) { return dot(rgb, vec3(0.212671f, 0.715160f, 0.072169f)); }
+static vec3 UnpackNormal(vec2 p) {
+    float sinPhi = sqrt(saturate((1.0f - p.y) * (1.0f + p.y)));
+    return vec3(std::cos(p.x) * sinPhi, std::sin(p.x) * sinPhi, p.y);
+}
+static vec3 UnpackNormal2(float p0, float p1) {
+    float sinPhi = sqrt(1.0f - p1 * p1);
+    return vec3(std::cos(p0) * sinPhi, std::sin(p0) * sinPhi, p1);
+}
+static vec2 PackNormal(vec3 n) {
+    return vec2(n.x == 0.0f ? sign(n.y) * PI / 2 : std::atan2(n.y, n.x), n.z);
+}
+
+// ------------------------------------------------------------ materials.glsl
+struct MaterialData {
+    vec4 Reflectiveness;
+    vec3 Opacity, Diffuse, Emissivity, Fresnel0;
+    float RefractionIndexAvg;
+    vec3 Fresnel1;
+};
+
+struct RenderScene {
+    Scene geo;
+    const float* materials = nullptr;  // 24 floats per material
+    uint32_t numMaterials = 0;
+};
+
+static MaterialData SampleMaterialData(const RenderScene& s, int id) {
+    const float* m = s.materials + 24 * (size_t)id;
+    MaterialData d;
+    d.Diffuse = vec3(m[0], m[1], m[2]);
+    d.RefractionIndexAvg = m[3];
+    d.Opacity = vec3(m[4], m[5], m[6]);
+    d.Reflectiveness = vec4(m[8], m[9], m[10], m[11]);
+    d.Emissivity = vec3(m[12], m[13], m[14]);
+    d.Fresnel0 = vec3(m[16], m[17], m[18]);
+    d.Fresnel1 = vec3(m[20], m[21], m[22]);
+    return d;
+}
+
+static float AvgProbability(vec3 c) { return (c.x + c.y + c.z + DIVISOR_EPSILON) / (3.0f + DIVISOR_EPSILON); }
+static float Avg(vec3 c) { return (c.x + c.y + c.z) / 3.0f; }
+
+// USE_CONSTANT_REFLECTION is the active branch (materials.glsl:3-4,52-55).
+static void GetBSDFDecisionPropabilities(const MaterialData& m, float, vec3& preflect, vec3& prefract,
+                                         vec3& pdiffuse) {
+    preflect = m.Fresnel0;
+    prefract = vec3(1.0f) - saturate(preflect);
+    pdiffuse = prefract * m.Opacity;
+    prefract = prefract - pdiffuse;
+}
+static vec3 GetDiffuseProbability(const MaterialData& m, float) {
+    vec3 preflect = m.Fresnel0;
+    return (vec3(1.0f) - saturate(preflect)) * m.Opacity;
+}
+
+// materials.glsl:118-277
+static vec3 SampleBSDFImpl(vec3 incidentDirection, const MaterialData& m, uint& seed, vec3 N, vec3& pathThroughput,
+                           bool adjoint, float& pdf, bool* isReflectedDiffuse) {
+    float cosTheta = dot(N, incidentDirection);
+    float cosThetaAbs = saturate(abs(cosTheta));
+    vec3 reflectRefractDir = incidentDirection - (2.0f * cosTheta) * N;
+    vec2 randomSamples = Random2(seed);
+    vec3 preflect, prefract, pdiffuse;
+    GetBSDFDecisionPropabilities(m, cosThetaAbs, preflect, prefract, pdiffuse);
+    float avgPReflect = AvgProbability(preflect);
+    float avgPRefract = AvgProbability(prefract);
+    float avgPDiffuse = Avg(pdiffuse);
+    vec3 pphong = preflect;
+    float avgPPhong = avgPReflect;
+    float pathDecisionVar = Random(seed);
+    if (avgPDiffuse > pathDecisionVar) {
+        if (isReflectedDiffuse) *isReflectedDiffuse = true;
+        pathThroughput *= (m.Diffuse * pdiffuse) / avgPDiffuse;
+        if (cosTheta > 0.0f) N = -N;
+        vec3 U, V;
+        CreateONB(N, U, V);
+        vec3 outDir = SampleHemisphereCosine(randomSamples, U, V, N);
+        float cosThetaOut = dot(N, outDir);
+        pdf = saturate(cosThetaOut) / PI;
+        return outDir;
+    } else if (avgPDiffuse + avgPRefract > pathDecisionVar) {
+        pphong = prefract;
+        avgPPhong = avgPRefract;
+        float eta = cosTheta < 0.0f ? 1.0f / m.RefractionIndexAvg : m.RefractionIndexAvg;
+        float etaSq = eta * eta;
+        float sinTheta2Sq = etaSq * (1.0f - cosTheta * cosTheta);
+        if (sinTheta2Sq < 1.0f) {
+            reflectRefractDir = eta * incidentDirection +
+                                (sign(cosTheta) * (sqrt(saturate(1.0f - sinTheta2Sq)) - eta * cosThetaAbs)) * N;
+            if (!adjoint) pathThroughput /= etaSq;
+        }
+    }
+    reflectRefractDir = normalize(reflectRefractDir);
+    vec3 RU, RV;
+    CreateONB(reflectRefractDir, RU, RV);
+    // The rejection loop is disabled in the reference (plausible = true), so
+    // exactly one lobe sample is taken and counter == 1.
+    vec3 outDir = SamplePhongLobe(randomSamples, m.Reflectiveness.w, RU, RV, reflectRefractDir);
+    if (!adjoint) pathThroughput *= abs(dot(N, outDir)) / abs(dot(N, reflectRefractDir));
+    float cosThetaOutAbs = abs(dot(outDir, reflectRefractDir));
+    pdf = (m.Reflectiveness.w + 1.0f) / PI_2 * std::pow(cosThetaOutAbs, m.Reflectiveness.w);
+    pdf *= 1.0f;
+    pathThroughput *= pphong / avgPPhong;
+    if (isReflectedDiffuse) *isReflectedDiffuse = false;
+    return outDir;
+}
+
+// materials.glsl:306-391
+static vec3 BSDFImpl(vec3 incidentDirection, vec3 excidentDirection, const MaterialData& m, vec3 N, float& pdf,
+                     bool adjoint, bool specularOnly) {
+    vec3 bsdf(0.0f);
+    float cosTheta = dot(N, incidentDirection);
+    float cosThetaAbs = saturate(abs(cosTheta));
+    float cosThetaOut = dot(N, excidentDirection);
+    vec3 preflect, prefract, pdiffuse;
+    GetBSDFDecisionPropabilities(m, cosThetaAbs, preflect, prefract, pdiffuse);
+    float phongFactor_brdf = (m.Reflectiveness.w + 1.0f) / (2 * PI_2 * abs(cosThetaOut) + DIVISOR_EPSILON);
+    float phongNormalization_pdf = (m.Reflectiveness.w + 1.0f) / PI_2;
+    vec3 reflectRefractDir = normalize(incidentDirection - (2.0f * cosTheta) * N);
+    float reflectionDotExcident_powN = std::pow(saturate(dot(reflectRefractDir, excidentDirection)), m.Reflectiveness.w);
+    float reflrefrBRDFFactor = phongFactor_brdf * reflectionDotExcident_powN;
+    float reflrefrPDFFactor = phongNormalization_pdf * reflectionDotExcident_powN;
+    bsdf = preflect * reflrefrBRDFFactor;
+    bsdf *= abs(cosThetaOut) / cosThetaAbs;
+    pdf = AvgProbability(preflect) * reflrefrPDFFactor;
+    if (!specularOnly && cosTheta * cosThetaOut < 0.0f) {
+        bsdf += pdiffuse * m.Diffuse / PI;
+        pdf += Avg(pdiffuse) * saturate(cosThetaOut) / PI;
+    }
+    float eta = cosTheta < 0.0f ? 1.0f / m.RefractionIndexAvg : m.RefractionIndexAvg;
+    float etaSq = eta * eta;
+    float sinTheta2Sq = etaSq * (1.0f - cosTheta * cosTheta);
+    if (sinTheta2Sq < 1.0f) {
+        reflectRefractDir = normalize(eta * incidentDirection +
+                                      (sign(cosTheta) * (sqrt(saturate(1.0f - sinTheta2Sq)) - eta * cosThetaAbs)) * N);
+        float refractionDotExcident_powN = std::pow(saturate(dot(reflectRefractDir, excidentDirection)), m.Reflectiveness.w);
+        reflrefrBRDFFactor = phongFactor_brdf * refractionDotExcident_powN;
+        reflrefrPDFFactor = phongNormalization_pdf * refractionDotExcident_powN;
+        if (!adjoint) reflrefrBRDFFactor /= etaSq;
+        reflrefrBRDFFactor *= abs(dot(N, excidentDirection)) / abs(dot(N, reflectRefractDir));
+    }
+    bsdf += prefract * reflrefrBRDFFactor;
+    pdf += AvgProbability(prefract) * reflrefrPDFFactor;
+    return bsdf;
+}
+static vec3 BSDF(vec3 i, vec3 e, const MaterialData& m, vec3 N, float& pdf) { return BSDFImpl(i, e, m, N, pdf, false, false); }
+static vec3 AdjointBSDF(vec3 i, vec3 e, const MaterialData& m, vec3 N, float& pdf) {
+    return BSDFImpl(-e, -i, m, N, pdf, true, false);
+}
+// materials.glsl:415-436
+static float AdjointBSDFShadingNormalCorrectedOutDotN(vec3 incomingLight, vec3 toCamera, vec3 gN, vec3 sN) {
+    if (dot(incomingLight, gN) * dot(incomingLight, sN) < 0 || dot(toCamera, gN) * dot(toCamera, sN) < 0) return 0.0f;
+    return saturate(abs(dot(incomingLight, sN) * dot(toCamera, gN)) / max(abs(dot(incomingLight, gN)), DIVISOR_EPSILON));
+}
+static float AdjointBSDFShadingNormalCorrection(vec3 inDir, vec3 outDir, vec3 gN, vec3 sN) {
+    if (dot(inDir, gN) * dot(inDir, sN) < 0 || dot(outDir, gN) * dot(outDir, sN) < 0) return 0.0f;
+    return saturate(abs(dot(inDir, sN) * dot(outDir, gN)) / max(abs(dot(inDir, gN) * dot(outDir, sN)), DIVISOR_EPSILON));
+}
+
+// ------------------------------------------------------------ scenedata.glsl
+static void GetTriangleHitInfo(const Scene& s, ivec4 tri, vec3 bc, vec3& normal, vec2& texcoord) {
+    vec4 v0 = s.vertexInfo[tri.x], v1 = s.vertexInfo[tri.y], v2 = s.vertexInfo[tri.z];
+    normal = normalize(UnpackNormal(vec2(v0.x, v0.y)) * bc.x + UnpackNormal(vec2(v1.x, v1.y)) * bc.y +
+                       UnpackNormal(vec2(v2.x, v2.y)) * bc.z);
+    texcoord = vec2(v0.z, v0.w) * bc.x + vec2(v1.z, v1.w) * bc.y + vec2(v2.z, v2.w) * bc.z;
+}
+
+// ------------------------------------------------------------ render params
+struct Params {
+    int width, height;
+    int maxPathLength;
+    int rrStartDepth;         // Russian roulette from this bounce on (0 = reference)
+    vec3 camU, camV, camW, camPos;
+    float pixelArea;
+    uint frameSeed;
+    int numLightSamples;
+    const vec4* lightSamples;  // 2 texels per sample
+    vec3 sky;                  // constant radiance on a miss (addition)
+    int numRaysPerLightSample; // LT / BPT
+};
+
+struct Image {
+    float* rgba;  // width*height*4, accumulated
+    int width, height;
+    std::mutex* locks;  // one per row, for LT splats
+};
+
+static void Splat(Image& img, int x, int y, vec3 c) {
+    if (x < 0 || y < 0 || x >= img.width || y >= img.height) return;  // GLSL image atomics ignore OOB
+    std::lock_guard<std::mutex> g(img.locks[y]);
+    float* p = img.rgba + 4 * ((size_t)y * img.width + x);
+    p[0] += c.x;
+    p[1] += c.y;
+    p[2] += c.z;
+}
+
+// ------------------------------------------------------------ lightsource.glsl
+// Returns the NEE radiance; directional samples (normalThetaCos == 3, the
+// position texel holding the direction towards the light) are the sun addition.
+static vec3 EstimateDirectLight(const RenderScene& s, const Params& P, vec3 pos, vec3 normal, int idx, vec3 viewDir,
+                                const MaterialData& m, bool sampleAreaLights) {
+    vec4 pn0 = P.lightSamples[2 * idx];
+    vec4 in1 = P.lightSamples[2 * idx + 1];
+    Ray lightRay;
+    if (in1.w > 2.5f) {  // directional (addition)
+        lightRay.Direction = pn0.xyz();
+        float surfaceCos = saturate(dot(lightRay.Direction, normal));
+        if (surfaceCos <= 0.0f) return vec3(0.0f);
+        lightRay.Origin = RAY_HIT_EPSILON * lightRay.Direction + pos;
+        if (!TraceRayAnyHit(s.geo, lightRay, RAY_MAX, nullptr)) {
+            float pdf;
+            vec3 bsdf = BSDF(viewDir, lightRay.Direction, m, normal, pdf);
+            return (surfaceCos * in1.xyz()) * bsdf;
+        }
+        return vec3(0.0f);
+    }
+    lightRay.Direction = pn0.xyz() - pos;
+    float lightDistSq = dot(lightRay.Direction, lightRay.Direction) + DIVISOR_EPSILON;
+    float lightDist = sqrt(lightDistSq);
+    lightRay.Direction /= lightDist;
+    float surfaceCos = saturate(dot(lightRay.Direction, normal));
+    if (surfaceCos <= 0.0f) return vec3(0.0f);
+    if (in1.w > 1.5f) {
+        lightRay.Origin = RAY_HIT_EPSILON * lightRay.Direction + pos;
+        if (!TraceRayAnyHit(s.geo, lightRay, lightDist - RAY_HIT_EPSILON * 2, nullptr)) {
+            vec3 irradiance = (surfaceCos / lightDistSq) * in1.xyz();
+            float pdf;
+            vec3 bsdf = BSDF(viewDir, lightRay.Direction, m, normal, pdf);
+            return irradiance * bsdf;
+        }
+    } else if (sampleAreaLights) {
+        vec3 lightNormal = UnpackNormal(vec2(pn0.w, in1.w));
+        float f = saturate(dot(lightNormal, -lightRay.Direction));
+        if (f > 0.0f) {
+            lightRay.Origin = RAY_HIT_EPSILON * lightRay.Direction + pos;
+            if (!TraceRayAnyHit(s.geo, lightRay, lightDist - RAY_HIT_EPSILON * 2, nullptr)) {
+                float pdf;
+                vec3 intensity = in1.xyz() * f;
+                vec3 bsdf = BSDF(viewDir, lightRay.Direction, m, normal, pdf);
+                vec3 irradiance = (surfaceCos / lightDistSq) * intensity;
+                return irradiance * bsdf;
+            }
+        }
+    }
+    return vec3(0.0f);
+}
+
+static Ray PrimaryRay(const Params& P, uint& seed, int x, int y) {
+    vec2 sub = Random2(seed) - 0.5f;
+    vec2 screen = (sub + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
+    Ray r;
+    r.Origin = P.camPos;
+    r.Direction = normalize(screen.x * P.camU + screen.y * P.camV + P.camW);
+    return r;
+}
+
+// ------------------------------------------------------------ pathtracer.comp
+static vec3 PathtracePixel(const RenderScene& s, const Params& P, int x, int y) {
+    const float lightSampleWeight = float(P.numLightSamples) / 1;
+    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    vec3 color(0.0f), pathThroughput(1.0f);
+    bool didNEE = false;
+    Ray ray = PrimaryRay(P, seed, x, y);
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        if (rayHit == RAY_MAX) {
+            color += pathThroughput * P.sky;
+            break;
+        }
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 hitNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        if (!didNEE) color += pathThroughput * m.Emissivity;
+        didNEE = m.Reflectiveness.w < 500.0f;
+        int sampleIndex = int(RandomUInt(seed) % (uint)P.numLightSamples);
+        vec3 radiance = EstimateDirectLight(s, P, ray.Origin, hitNormal, sampleIndex, ray.Direction, m, didNEE);
+        color += radiance * pathThroughput * lightSampleWeight;
+        vec3 throughput(1.0f);
+        float pdf;
+        ray.Direction = SampleBSDFImpl(ray.Direction, m, seed, hitNormal, throughput, false, pdf, nullptr);
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+        pathThroughput *= throughput;
+        if (i >= P.rrStartDepth) {
+            float p = saturate(GetLuminance(throughput));
+            if (Random(seed) >= p) break;
+            pathThroughput /= p;
+        }
+    }
+    return color;
+}
+
+// ------------------------------------------------------------ lightcache.glsl
+struct LightCacheEntry {
+    vec3 Flux;
+    int MaterialIndex;
+    vec3 Position;
+    float Normal0;
+    vec2 Texcoord;
+    float Normal1;
+    int PathLength;
+    vec2 IncidentDirectionPacked;
+    float ChainedN, ChainedT;
+};
+static_assert(sizeof(LightCacheEntry) == 64, "LightCacheEntry is 64 bytes");
+static float MISHeuristic(float p) { return min(1e18f, p); }
+static float InitialMIS() { return 1.0f; }
+static float DistanceMISHeuristic(float d, float) { return MISHeuristic(d * d); }
+
+struct LightCache {
+    LightCacheEntry* entries;
+    uint32_t capacity;
+    std::atomic<uint32_t> count;
+};
+
+// ------------------------------------------------------ screenreproject.glsl
+static void ProjectToScreen(const RenderScene& s, const Params& P, Image& img, const Ray& ray, vec3 geometryNormal,
+                            vec3 shadingNormal, const MaterialData& m, vec3 pathThroughput, bool computeMIS) {
+    Ray cameraRay;
+    cameraRay.Direction = P.camPos - ray.Origin;
+    float camViewDotRay = -dot(P.camW, cameraRay.Direction);
+    if (!(camViewDotRay > 0.0f)) return;
+    vec3 proj(-dot(P.camU, cameraRay.Direction), -dot(P.camV, cameraRay.Direction), camViewDotRay);
+    vec2 screen(proj.x / proj.z, proj.y / proj.z);
+    screen.x /= dot(P.camU, P.camU);
+    screen.y /= dot(P.camV, P.camV);
+    if (!(screen.x >= -1.0f && screen.x < 1.0f && screen.y > -1.0f && screen.y <= 1.0f)) return;
+    float cameraDistSq = dot(cameraRay.Direction, cameraRay.Direction);
+    float cameraDist = sqrt(cameraDistSq);
+    cameraRay.Direction /= cameraDist;
+    cameraRay.Origin = cameraRay.Direction * RAY_HIT_EPSILON + ray.Origin;
+    vec2 pixelPos = (screen * 0.5f + vec2(0.5f)) * vec2((float)P.width, (float)P.height);
+    int px = (int)std::nearbyint(pixelPos.x), py = (int)std::nearbyint(pixelPos.y);
+    if (TraceRayAnyHit(s.geo, cameraRay, cameraDist, nullptr)) return;
+    float cosAtCamera = saturate(camViewDotRay / cameraDist);
+    float fluxToIrradiance = AdjointBSDFShadingNormalCorrectedOutDotN(ray.Direction, cameraRay.Direction,
+                                                                      geometryNormal, shadingNormal) /
+                             (cosAtCamera * cosAtCamera * cosAtCamera * P.pixelArea * cameraDistSq);
+    float pdf;
+    vec3 bsdf = AdjointBSDF(ray.Direction, cameraRay.Direction, m, shadingNormal, pdf);
+    if (computeMIS) {
+        float e2l = InitialMIS();
+        float l2e = MISHeuristic(pdf);
+        float mis = e2l / max(l2e + e2l, DIVISOR_EPSILON);
+        bsdf *= mis;
+    }
+    Splat(img, px, py, pathThroughput * fluxToIrradiance * bsdf);
+}
+
+// ------------------------------------------------------------ lighttracer.comp
+static void LighttraceThread(const RenderScene& s, const Params& P, Image& img, uint gid, LightCache* cache) {
+    uint seed = InitRandomSeed(P.frameSeed, gid);
+    int lightSampleIndex = int(gid / (uint)P.numRaysPerLightSample);
+    vec4 pn0 = P.lightSamples[2 * lightSampleIndex];
+    vec4 in1 = P.lightSamples[2 * lightSampleIndex + 1];
+    if (cache) {
+        LightCacheEntry& e = cache->entries[gid];
+        e.Flux = in1.xyz() / PI_2 / (float)P.numRaysPerLightSample;
+        e.MaterialIndex = -1;
+        e.Position = pn0.xyz();
+        e.Normal0 = pn0.w;
+        e.Normal1 = in1.w;
+        e.Texcoord = vec2(0.0f);
+        e.IncidentDirectionPacked = PackNormal(vec3(0.0f));
+        e.PathLength = 0;
+        e.ChainedN = e.ChainedT = 0.0f;
+    }
+    vec3 pathThroughput = in1.xyz() * (PI / (float)P.numRaysPerLightSample);
+    Ray ray;
+    ray.Origin = pn0.xyz();
+    if (in1.w > 1.5f) {
+        ray.Direction = SampleDirection(Random2(seed));
+        pathThroughput *= 4.0f;
+    } else {
+        vec3 normal = UnpackNormal(vec2(pn0.w, in1.w));
+        vec3 U, V;
+        CreateONB(normal, U, V);
+        ray.Direction = SampleHemisphereCosine(Random2(seed), U, V, normal);
+    }
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        if (rayHit == RAY_MAX) break;
+        vec3 geometryNormal = hit.normal;  // not normalised (lighttracer.comp:105)
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 shadingNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, shadingNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        if (cache && m.Reflectiveness.w < 100.0f) {
+            uint32_t k = cache->count.fetch_add(1);
+            if (k < cache->capacity) {
+                LightCacheEntry& e = cache->entries[k];
+                e.Flux = pathThroughput;
+                e.MaterialIndex = hit.triangle.w;
+                e.Position = ray.Origin;
+                vec2 pn = PackNormal(shadingNormal);
+                e.Normal0 = pn.x;
+                e.Normal1 = pn.y;
+                e.Texcoord = tc;
+                e.IncidentDirectionPacked = PackNormal(ray.Direction);
+                e.PathLength = i + 1;
+                e.ChainedN = e.ChainedT = 0.0f;
+            }
+        }
+        ProjectToScreen(s, P, img, ray, geometryNormal, shadingNormal, m, pathThroughput, cache != nullptr);
+        vec3 throughput(1.0f);
+        float samplePDF;
+        bool diffuse;
+        vec3 newDirection = SampleBSDFImpl(ray.Direction, m, seed, shadingNormal, throughput, true, samplePDF, &diffuse);
+        throughput *= AdjointBSDFShadingNormalCorrection(ray.Direction, newDirection, geometryNormal, shadingNormal);
+        pathThroughput *= throughput;
+        if (i >= P.rrStartDepth) {
+            float p = saturate(GetLuminance(throughput));
+            if (Random(seed) >= p) break;
+            pathThroughput /= p;
+        }
+        ray.Direction = newDirection;
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+    }
+}
+
+// showlightcaches.comp:9-65: the light samples seen directly by the camera
+// (LightPathtracer::Draw runs it after the light trace, lightpathtracer.cpp:48).
+static void ShowLightSample(const RenderScene& s, const Params& P, Image& img, int idx) {
+    vec4 pn0 = P.lightSamples[2 * idx];
+    vec4 in1 = P.lightSamples[2 * idx + 1];
+    Ray cameraRay;
+    cameraRay.Direction = P.camPos - pn0.xyz();
+    float camViewDotRay = -dot(P.camW, cameraRay.Direction);
+    if (!(camViewDotRay > 0.0f)) return;
+    vec3 proj(-dot(P.camU, cameraRay.Direction), -dot(P.camV, cameraRay.Direction), camViewDotRay);
+    vec2 screen(proj.x / proj.z, proj.y / proj.z);
+    screen.x /= dot(P.camU, P.camU);
+    screen.y /= dot(P.camV, P.camV);
+    if (!(screen.x >= -1.0f && screen.x < 1.0f && screen.y > -1.0f && screen.y <= 1.0f)) return;
+    float cameraDistSq = dot(cameraRay.Direction, cameraRay.Direction);
+    float cameraDist = sqrt(cameraDistSq);
+    cameraRay.Direction /= cameraDist;
+    cameraRay.Origin = cameraRay.Direction * RAY_HIT_EPSILON + pn0.xyz();
+    if (TraceRayAnyHit(s.geo, cameraRay, cameraDist, nullptr)) return;
+    vec3 normal = UnpackNormal(vec2(pn0.w, in1.w));
+    float cosTheta = dot(normal, cameraRay.Direction);
+    float cosAtCamera = saturate(camViewDotRay / cameraDist);
+    float intensityToRadiance = cosTheta / (PI_2 * cosAtCamera * cosAtCamera * cosAtCamera * P.pixelArea * cameraDistSq);
+    vec3 color = in1.xyz() * intensityToRadiance;
+    vec2 pix = (screen * 0.5f + vec2(0.5f)) * vec2((float)P.width, (float)P.height);
+    Splat(img, (int)pix.x, (int)pix.y, color);  // ivec2() truncates
+}
+
+// ----------------------------------------------- pathtracer_bidir.comp
+static vec3 BidirPixel(const RenderScene& s, const Params& P, const LightCache& cache, uint32_t numEntries, int x,
+                       int y) {
+    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    Ray ray = PrimaryRay(P, seed, x, y);
+    vec3 color(0.0f), pathThroughput(1.0f);
+    const uint actual = numEntries;
+    const float lightSampleWeight = float(actual);
+    float lastConnectionProbability = InitialMIS();
+    float lastCosAbs = 1.0f;
+    float mis = 0.0f;
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        if (rayHit == RAY_MAX) {
+            color += pathThroughput * P.sky;  // addition: the reference's eye pass adds nothing on a miss
+            break;
+        }
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 hitNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        float incidentSurfaceCosSat = saturate(-dot(hitNormal, ray.Direction));
+        float connectionLightToEyePath = DistanceMISHeuristic(rayHit, lastCosAbs) * MISHeuristic(incidentSurfaceCosSat / PI);
+        mis = (i == 0) ? 1.0f : (lastConnectionProbability / max(lastConnectionProbability + connectionLightToEyePath, DIVISOR_EPSILON));
+        color += mis * pathThroughput * m.Emissivity;
+        if (actual > 0) {
+            uint li = RandomUInt(seed) % actual;
+            const LightCacheEntry& e = cache.entries[li];
+            int pathLength = e.PathLength + i + 1;
+            if (pathLength <= P.maxPathLength) {
+                Ray lightRay;
+                lightRay.Direction = e.Position - ray.Origin;
+                float lightDistSq = dot(lightRay.Direction, lightRay.Direction);
+                float lightDist = sqrt(lightDistSq);
+                lightRay.Direction /= max(lightDist, DIVISOR_EPSILON);
+                lightRay.Origin = RAY_HIT_EPSILON * lightRay.Direction + ray.Origin;
+                if (!TraceRayAnyHit(s.geo, lightRay, lightDist - RAY_HIT_EPSILON * 2, nullptr)) {
+                    vec3 lightSampleHitNormal(0.0f, 1.0f, 0.0f);
+                    float connectionLightPathToEyePath;
+                    float cosLight = 0.0f;
+                    vec3 lightSampleIntensity;
+                    float cosCamera = abs(dot(lightRay.Direction, hitNormal));
+                    if (e.Normal1 < 1.5f) {
+                        lightSampleHitNormal = UnpackNormal2(e.Normal0, e.Normal1);
+                        cosLight = abs(dot(lightRay.Direction, lightSampleHitNormal));
+                    }
+                    float pdf;
+                    vec3 bsdf = BSDF(ray.Direction, lightRay.Direction, m, hitNormal, pdf);
+                    float connectionEyePathToLightPath = MISHeuristic(pdf);
+                    if (i > 0) {
+                        float distMIS = DistanceMISHeuristic(rayHit, lastCosAbs);
+                        connectionEyePathToLightPath *= distMIS;
+                        mis = lastConnectionProbability / max(lastConnectionProbability + connectionEyePathToLightPath, DIVISOR_EPSILON);
+                        if (m.Reflectiveness.w >= 100.0f) mis = 1.0f;
+                    } else {
+                        mis = connectionEyePathToLightPath / max(lastConnectionProbability + connectionEyePathToLightPath, DIVISOR_EPSILON);
+                    }
+                    float misLight = 1.0f;
+                    if (e.Normal1 < 1.5f) {
+                        if (e.MaterialIndex != -1) {
+                            MaterialData lm = SampleMaterialData(s, e.MaterialIndex);
+                            vec3 incidentDir = UnpackNormal(e.IncidentDirectionPacked);
+                            vec3 lightBSDF = AdjointBSDF(lightRay.Direction, -incidentDir, lm, lightSampleHitNormal, pdf);
+                            lightSampleIntensity = e.Flux * lightBSDF * cosLight;
+                            connectionLightPathToEyePath = MISHeuristic(pdf) * DistanceMISHeuristic(lightDist, cosCamera);
+                        } else {
+                            lightSampleIntensity = e.Flux * (cosLight * PI_2);
+                            connectionLightPathToEyePath = MISHeuristic(cosLight / PI) * DistanceMISHeuristic(lightDist, cosCamera);
+                        }
+                        misLight = connectionLightPathToEyePath / max(connectionLightPathToEyePath + connectionEyePathToLightPath, DIVISOR_EPSILON);
+                    } else {
+                        lightSampleIntensity = e.Flux * PI_2;
+                        misLight = 1.0f;
+                    }
+                    mis *= misLight;
+                    vec3 irradiance = (mis * lightSampleWeight * cosCamera / lightDistSq) * lightSampleIntensity;
+                    color += irradiance * pathThroughput * bsdf;
+                }
+            }
+        }
+        float samplePDF;
+        vec3 throughput(1.0f);
+        ray.Direction = SampleBSDFImpl(ray.Direction, m, seed, hitNormal, throughput, false, samplePDF, nullptr);
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+        pathThroughput *= throughput;
+        if (i >= P.rrStartDepth) {
+            float p = saturate(GetLuminance(throughput));
+            if (Random(seed) >= p) break;
+            pathThroughput /= p;
+        }
+        float reverseConnectionProbability = MISHeuristic(samplePDF);
+        if (i == 0) {
+            mis = reverseConnectionProbability / max(reverseConnectionProbability + lastConnectionProbability, DIVISOR_EPSILON);
+        } else {
+            float distMIS = DistanceMISHeuristic(rayHit, lastCosAbs);
+            reverseConnectionProbability *= distMIS;
+            mis = lastConnectionProbability / max(lastConnectionProbability + distMIS * reverseConnectionProbability, DIVISOR_EPSILON);
+            if (m.Reflectiveness.w >= 100.0f) mis = 1.0f;
+        }
+        pathThroughput *= mis;
+        lastConnectionProbability = reverseConnectionProbability;
+        lastCosAbs = abs(dot(ray.Direction, hitNormal));
+    }
+    return color;
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+// One iteration of a pass, accumulated into rgba (w*h*4 floats).
+//   pass: 0 = PT, 1 = LT, 2 = BPT
+//   cam: 13 floats {U, V, W, position, pixelArea}
+//   lightSamples: 8 floats per sample; sky: 3 floats (may be NULL)
+int oracle_render(const float* hierarchy, uint32_t numNodes, uint32_t boundsKind, const int32_t* slots,
+                  uint32_t numSlots, uint32_t leafSize, const float* positions, const float* vertexInfo,
+                  uint32_t numVertices, const float* materials, uint32_t numMaterials, int pass, int width,
+                  int height, int maxPathLength, int rrStartDepth, const float* cam, uint32_t frameSeed,
+                  const float* lightSamples, int numLightSamples, const float* sky, float* rgba, int numThreads) {
+    RenderScene s;
+    s.geo.hierarchy = reinterpret_cast<const vec4*>(hierarchy);
+    s.geo.numNodes = numNodes;
+    s.geo.boundsKind = boundsKind;
+    s.geo.triangles = reinterpret_cast<const ivec4*>(slots);
+    s.geo.numSlots = numSlots;
+    s.geo.leafSize = leafSize;
+    s.geo.positions = positions;
+    s.geo.numVertices = numVertices;
+    s.geo.vertexInfo = reinterpret_cast<const vec4*>(vertexInfo);
+    s.materials = materials;
+    s.numMaterials = numMaterials;
+    Params P;
+    P.width = width;
+    P.height = height;
+    P.maxPathLength = maxPathLength;
+    P.rrStartDepth = rrStartDepth;
+    P.camU = vec3(cam[0], cam[1], cam[2]);
+    P.camV = vec3(cam[3], cam[4], cam[5]);
+    P.camW = vec3(cam[6], cam[7], cam[8]);
+    P.camPos = vec3(cam[9], cam[10], cam[11]);
+    P.pixelArea = cam[12];
+    P.frameSeed = frameSeed;
+    P.numLightSamples = numLightSamples;
+    P.lightSamples = reinterpret_cast<const vec4*>(lightSamples);
+    P.sky = sky ? vec3(sky[0], sky[1], sky[2]) : vec3(0.0f);
+    // LightPathtracer::SetScreenSize (lightpathtracer.cpp:34)
+    const int numPixels = width * height;
+    P.numRaysPerLightSample = std::max(64, (numPixels / numLightSamples / 64) * 64);
+    std::vector<std::mutex> locks(height);
+    Image img{rgba, width, height, locks.data()};
+    if (pass == 0) {
+        ParallelFor((uint64_t)numPixels, numThreads, [&](uint64_t b, uint64_t e) {
+            for (uint64_t p = b; p < e; ++p) {
+                int x = (int)(p % width), y = (int)(p / width);
+                vec3 c = PathtracePixel(s, P, x, y);
+                float* o = rgba + 4 * p;
+                o[0] += c.x;
+                o[1] += c.y;
+                o[2] += c.z;
+            }
+        });
+        return 0;
+    }
+    const uint64_t nThreads = (uint64_t)numLightSamples * P.numRaysPerLightSample;
+    if (pass == 1) {
+        ParallelFor(nThreads, numThreads, [&](uint64_t b, uint64_t e) {
+            for (uint64_t g = b; g < e; ++g) LighttraceThread(s, P, img, (uint)g, nullptr);
+        });
+        for (int i = 0; i < numLightSamples; ++i) ShowLightSample(s, P, img, i);
+        return 0;
+    }
+    if (pass == 2) {
+        // Capacity: every thread stores at most 1 + maxPathLength entries, so
+        // the worst case never overflows (no warm-up estimate needed).
+        std::vector<LightCacheEntry> entries(nThreads * (uint64_t)(maxPathLength + 1));
+        LightCache cache;
+        cache.entries = entries.data();
+        cache.capacity = (uint32_t)entries.size();
+        cache.count = (uint32_t)nThreads;  // resetcounter.comp: initial samples occupy the first slots
+        ParallelFor(nThreads, numThreads, [&](uint64_t b, uint64_t e) {
+            for (uint64_t g = b; g < e; ++g) LighttraceThread(s, P, img, (uint)g, &cache);
+        });
+        uint32_t n = std::min<uint32_t>(cache.count.load(), cache.capacity);
+        ParallelFor((uint64_t)numPixels, numThreads, [&](uint64_t b, uint64_t e) {
+            for (uint64_t p = b; p < e; ++p) {
+                int x = (int)(p % width), y = (int)(p / width);
+                vec3 c = BidirPixel(s, P, cache, n, x, y);
+                float* o = rgba + 4 * p;
+                o[0] += c.x;
+                o[1] += c.y;
+                o[2] += c.z;
+                o[3] += 1.0f;
+            }
+        });
+        return 0;
+    }
+    return -1;
+}
+
+uint32_t oracle_wanghash(uint32_t x) { return wanghash(x); }
+
+}  // extern "C"
