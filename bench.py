@@ -38,6 +38,9 @@ WORKLOAD = ("closest-hit queries: displaced icosphere 65,536 tris (level-6 icosp
             "U[-0.05,0.05], unit cube), bvhmake sweep SAH AABB BVH leaf 8, 2^20 rays/step, origins U[-2,2]^3, "
             "dirs uniform on S^2, tmax=inf")
 FALLBACK_HBM_GBS = 6800.0
+# Kernels of one step per trace mode (the roofline is taken over the whole step).
+KERNELS = {0: "k_trace_closest<AABB>", 1: "k_trace_persistent<closest, AABB>",
+           2: "k_trace_root_filter<closest, AABB> + k_trace_queue<closest, AABB>"}
 
 
 def peaks():
@@ -283,9 +286,8 @@ def run_ours(args, world, rank, local):
                          "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)" if peak_src == "measured"
                          else "fallback 6.8 TB/s",
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3,
-                         "kernel": "k_trace_persistent<closest, AABB>" if args.trace_mode == 1
-                         else "k_trace_closest<AABB>"},
-            "gpu_launches": args.steps,
+                         "kernel": KERNELS[args.trace_mode]},
+            "gpu_launches": args.steps * (2 if args.trace_mode == 2 else 1),
             "clocks": clk.summary()}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(b, sc["positions"], host_batches, seconds=args.cpu_seconds)
@@ -303,7 +305,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--trace-mode", type=int, default=1, help="0: thread per ray, 1: persistent lane refill")
+    ap.add_argument("--trace-mode", type=int, default=2,
+                    help="0: thread per ray, 1: persistent lane refill, 2: root prefilter + persistent")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

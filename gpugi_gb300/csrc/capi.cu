@@ -31,6 +31,23 @@ gpugi_status ensure_stage(gpugi_ctx* ctx, size_t bytes) {
     return GPUGI_OK;
 }
 
+gpugi_status ensure_queue(gpugi_ctx* ctx, uint64_t n) {
+    if (n <= ctx->queueCap) return GPUGI_OK;
+    if (ctx->queue) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->queue);
+        ctx->queue = nullptr;
+        ctx->queueCap = 0;
+    }
+    const uint64_t want = n + n / 4;
+    if (cudaMalloc(&ctx->queue, want * sizeof(uint32_t)) != cudaSuccess) {
+        ctx->queue = nullptr;
+        return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "ray queue allocation failed");
+    }
+    ctx->queueCap = want;
+    return GPUGI_OK;
+}
+
 static gpugi_status check_device_error(gpugi_ctx* ctx) {
     uint32_t bits = 0;
     GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(&bits, ctx->errWord, 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -86,9 +103,11 @@ void gpugi_destroy(gpugi_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->renderFree) ctx->renderFree(ctx);
     if (ctx->stageDev) cudaFree(ctx->stageDev);
     if (ctx->errWord) cudaFree(ctx->errWord);
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->queue) cudaFree(ctx->queue);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -113,7 +132,9 @@ gpugi_status gpugi_device_error_bits(gpugi_ctx* ctx, uint32_t* bits) {
 
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
-    if (mode > 1) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "mode must be 0 (thread per ray) or 1 (persistent)");
+    if (mode > 2)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT,
+                    "mode must be 0 (thread per ray), 1 (persistent) or 2 (root prefilter + persistent)");
     if (blockSize == 0 || blockSize > 256 || blockSize % 32 != 0)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "blockSize must be a multiple of 32 in [32, 256]");
     ctx->traceMode = mode;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <string>
 #include <vector>
 
@@ -17,11 +18,29 @@ struct gpugi_ctx {
     void* stageDev = nullptr;
     size_t stageDevBytes = 0;
     // trace tuning
-    uint32_t traceMode = 1;  // 0 = one thread per ray, 1 = persistent lane refill
+    uint32_t traceMode = 2;  // 0 = thread per ray, 1 = persistent lane refill, 2 = root prefilter + 1
     uint32_t traceBlock = 128;
     void* scratch = nullptr;  // 256 B of device counters (work distribution)
+    uint32_t* queue = nullptr;  // ray-index queue of the root prefilter (mode 2)
+    uint64_t queueCap = 0;
     int numSMs = 0;
+    // wavefront renderer buffers (owned by render.cu)
+    void* render = nullptr;
+    void (*renderFree)(gpugi_ctx*) = nullptr;
 };
+
+namespace gpugi {
+struct LightTriangle {
+    float v[3][3];
+    float lum[3];
+};
+struct PointLight {
+    float position[3], intensity[3];
+};
+struct DirLight {
+    float dir[3], irradiance[3];  // dir points towards the light
+};
+}  // namespace gpugi
 
 struct gpugi_scene {
     gpugi_ctx* ctx = nullptr;
@@ -33,6 +52,14 @@ struct gpugi_scene {
     std::vector<int32_t> hostSlots;
     std::vector<float> hostMaterials;
     uint32_t numLeafBlocks = 0;
+    // light tables (Scene::LoadLightSources / ComputePointLightTable)
+    bool lightsReady = false;
+    std::vector<gpugi::LightTriangle> lightTris;
+    std::vector<float> lightSummedArea;
+    float lightAreaSum = 0.0f, totalAreaLightFlux = 0.0f, totalPointLightFlux = 0.0f;
+    std::vector<gpugi::PointLight> pointLights;
+    std::vector<float> pointLightSummedFlux;
+    std::vector<gpugi::DirLight> dirLights;
 };
 
 namespace gpugi {
@@ -43,6 +70,12 @@ gpugi_status fail(gpugi_ctx* ctx, gpugi_status st, const std::string& msg);
 gpugi_status cuda_fail(gpugi_ctx* ctx, cudaError_t e, const char* what);
 // Grow the context's device staging buffer to at least `bytes`.
 gpugi_status ensure_stage(gpugi_ctx* ctx, size_t bytes);
+// Grow the context's ray-index queue to at least n entries.
+gpugi_status ensure_queue(gpugi_ctx* ctx, uint64_t n);
+gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
+                                   const float* oy, const float* oz, const float* dx, const float* dy,
+                                   const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
+                                   float* u, float* v, uint8_t* occluded);
 // Launch the traversal kernels (device pointers, async on ctx->stream).
 gpugi_status launch_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
                                   const float* oz, const float* dx, const float* dy, const float* dz,
@@ -58,6 +91,9 @@ gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool
 gpugi_status launch_trace_stats(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
                                 const float* oz, const float* dx, const float* dy, const float* dz,
                                 const float* tmax, uint64_t n, uint32_t anyHit, unsigned long long* sums);
+// Light tables and the host light sampler (host.cu).
+void build_light_tables(gpugi_scene* sc);
+void generate_light_samples(gpugi_scene* sc, uint64_t& rng, uint32_t numSamples, float* out);
 
 }  // namespace gpugi
 

@@ -114,6 +114,135 @@ gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool
     return GPUGI_OK;
 }
 
+// Root prefilter (mode 2), first of two launches: one thread per ray with
+// fully coalesced loads and stores tests the root bounds (the first test of
+// every walk). Rays that miss it are finished here; the others are appended
+// to a queue with warp-ballot compaction for the persistent walker.
+template <bool ANY_HIT, int BOUNDS>
+__global__ void __launch_bounds__(256) k_trace_root_filter(
+    DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
+    const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
+    const float* __restrict__ tmax, uint64_t n, int32_t* __restrict__ slot, float* __restrict__ t,
+    float* __restrict__ u, float* __restrict__ v, uint8_t* __restrict__ occluded, uint32_t* __restrict__ queue,
+    unsigned long long* counters) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool pass = false;
+    if (i < n) {
+        const float3 o = make_float3(__ldg(ox + i), __ldg(oy + i), __ldg(oz + i));
+        const float3 d = make_float3(__ldg(dx + i), __ldg(dy + i), __ldg(dz + i));
+        const float len = __ldg(tmax + i);
+        const float4 a = __ldg(s.nodes), b = __ldg(s.nodes + 1);
+        float firstHit;
+        bool hit;
+        if (BOUNDS == 0) hit = intersect_box(o, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a, b, firstHit);
+        else hit = intersect_ellipsoid(o, d, a, b, firstHit);
+        pass = hit && firstHit <= len;
+        if (!pass) {
+            if (ANY_HIT) {
+                occluded[i] = 0;
+            } else {
+                slot[i] = -1;
+                t[i] = len;
+                u[i] = 0.0f;
+                v[i] = 0.0f;
+            }
+        }
+    }
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned ballot = __ballot_sync(0xffffffffu, pass);
+    unsigned long long base = 0;
+    if (lane == 0 && ballot) base = atomicAdd(counters + 1, (unsigned long long)__popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (pass) queue[base + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)i;
+}
+
+// Second launch: the persistent walker over the queued ray indices.
+template <bool ANY_HIT, int BOUNDS>
+__global__ void __launch_bounds__(128) k_trace_queue(
+    DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
+    const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
+    const float* __restrict__ tmax, int32_t* __restrict__ slot, float* __restrict__ t, float* __restrict__ u,
+    float* __restrict__ v, uint8_t* __restrict__ occluded, const uint32_t* __restrict__ queue,
+    unsigned long long* counters, uint32_t* err) {
+    const uint64_t n = counters[1];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lanesBelow = (1u << lane) - 1u;
+    WalkState w;
+    uint32_t ray = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        const bool need = !active && !exhausted;
+        const unsigned needMask = __ballot_sync(0xffffffffu, need);
+        if (needMask) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(counters + 2, (unsigned long long)__popc(needMask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (need) {
+                const uint64_t my = base + (uint64_t)__popc(needMask & lanesBelow);
+                if (my < n) {
+                    ray = __ldg(queue + my);
+                    walk_begin(w, s, make_float3(__ldg(ox + ray), __ldg(oy + ray), __ldg(oz + ray)),
+                               make_float3(__ldg(dx + ray), __ldg(dy + ray), __ldg(dz + ray)), __ldg(tmax + ray));
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err)) {
+            if (ANY_HIT) {
+                occluded[ray] = w.slot >= 0 ? 1 : 0;
+            } else {
+                slot[ray] = w.slot;
+                t[ray] = w.len;
+                u[ray] = w.u;
+                v[ray] = w.v;
+            }
+            active = false;
+        }
+    }
+}
+
+gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
+                                   const float* oy, const float* oz, const float* dx, const float* dy,
+                                   const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
+                                   float* u, float* v, uint8_t* occluded) {
+    if (n == 0) return GPUGI_OK;
+    if (n > 0xFFFFFFFFull) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "mode 2 handles at most 2^32-1 rays per call");
+    gpugi_status st = ensure_queue(ctx, n);
+    if (st) return st;
+    unsigned long long* counters = reinterpret_cast<unsigned long long*>(ctx->scratch);
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    const unsigned grid1 = (unsigned)((n + 255) / 256);
+#define GPUGI_FILTER(A, B)                                                                                          \
+    k_trace_root_filter<A, B><<<grid1, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, \
+                                                              v, occluded, ctx->queue, counters)
+    if (!ell) {
+        if (anyHit) GPUGI_FILTER(true, 0);
+        else GPUGI_FILTER(false, 0);
+    } else {
+        if (anyHit) GPUGI_FILTER(true, 1);
+        else GPUGI_FILTER(false, 1);
+    }
+#undef GPUGI_FILTER
+    void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
+              const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
+              uint32_t*);
+    if (!ell) k = anyHit ? k_trace_queue<true, 0> : k_trace_queue<false, 0>;
+    else k = anyHit ? k_trace_queue<true, 1> : k_trace_queue<false, 1>;
+    int perSM = 0;
+    GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k, 128, 0));
+    uint64_t grid = (uint64_t)ctx->numSMs * (uint64_t)(perSM > 0 ? perSM : 1);
+    const uint64_t needed = (n + 127) / 128;
+    if (grid > needed) grid = needed;
+    k<<<(unsigned)grid, 128, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded,
+                                               ctx->queue, counters, ctx->errWord);
+    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
 template <int BOUNDS, bool ANY>
 __global__ void __launch_bounds__(256) k_trace_stats(DevScene s, const float* __restrict__ ox,
                                                      const float* __restrict__ oy, const float* __restrict__ oz,
@@ -165,6 +294,8 @@ gpugi_status launch_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const f
                                   const float* tmax, uint64_t n, int32_t* slot, float* t, float* u, float* v) {
     if (n == 0) return GPUGI_OK;
     if (n > (uint64_t)0xFFFFFFFFu * 256u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many rays");
+    if (ctx->traceMode == 2)
+        return launch_trace_filtered(ctx, sc, false, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, nullptr);
     if (ctx->traceMode == 1)
         return launch_trace_persistent(ctx, sc, false, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, nullptr);
     const uint32_t block = ctx->traceBlock;
@@ -183,6 +314,9 @@ gpugi_status launch_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float
                               const float* tmax, uint64_t n, uint8_t* occluded) {
     if (n == 0) return GPUGI_OK;
     if (n > (uint64_t)0xFFFFFFFFu * 256u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many rays");
+    if (ctx->traceMode == 2)
+        return launch_trace_filtered(ctx, sc, true, ox, oy, oz, dx, dy, dz, tmax, n, nullptr, nullptr, nullptr,
+                                     nullptr, occluded);
     if (ctx->traceMode == 1)
         return launch_trace_persistent(ctx, sc, true, ox, oy, oz, dx, dy, dz, tmax, n, nullptr, nullptr, nullptr,
                                        nullptr, occluded);

@@ -256,3 +256,86 @@ def random_rays(n: int, seed: int = 1, origin_lo: float = -2.0, origin_hi: float
                 oz=np.ascontiguousarray(o[:, 2]), dx=np.ascontiguousarray(d[:, 0]),
                 dy=np.ascontiguousarray(d[:, 1]), dz=np.ascontiguousarray(d[:, 2]),
                 tmax=np.full(n, tmax, dtype=np.float32))
+
+
+# --------------------------------------------------------------------------
+# Workload 2: enclosed room for the path tracer
+# --------------------------------------------------------------------------
+def _grid_quad(origin, eu, ev, n: int):
+    """A planar quad origin + [0,1]eu + [0,1]ev split into n x n cells (2 n^2
+    triangles). Winding makes the normal cross(eu, ev)."""
+    i, j = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    v = (np.asarray(origin, np.float64)[None, None] + (i / n)[..., None] * np.asarray(eu, np.float64)
+         + (j / n)[..., None] * np.asarray(ev, np.float64)).reshape(-1, 3)
+    a = (np.arange(n)[:, None] * (n + 1) + np.arange(n)[None, :]).reshape(-1)
+    f = np.concatenate([np.stack([a, a + n + 1, a + n + 2], 1), np.stack([a, a + n + 2, a + 1], 1)])
+    nrm = np.cross(eu, ev)
+    nrm = nrm / np.linalg.norm(nrm)
+    return v, f, np.repeat(nrm[None], v.shape[0], 0)
+
+
+CORNELL_CAMERA = ((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0), 40.0)
+
+
+def cornell_room(seed: int = 1, sphere_level: int = 6, wall_grid: int = 40, light_radiance: float = 10.0):
+    """Room [-1,1] x [0,2] x [-1,1] open towards +z: five wall quads (split
+    into wall_grid^2 cells), two boxes rotated about y, an icosphere
+    (level 6: 81,920 triangles) and a 0.5 x 0.5 ceiling light of radiance
+    (10, 10, 10) facing down. Lambertian albedos uniform in [0.1, 0.9]^3.
+    Defaults give about 100k triangles. Camera: CORNELL_CAMERA."""
+    rs = Stream(seed, 5)
+    parts_v, parts_f, parts_n, mat_ids, mats = [], [], [], [], []
+
+    def add(v, f, n, mid):
+        base = sum(p.shape[0] for p in parts_v)
+        parts_v.append(np.asarray(v, np.float64))
+        parts_f.append(np.asarray(f) + base)
+        parts_n.append(np.asarray(n, np.float64))
+        mat_ids.append(np.full(len(f), mid, np.uint32))
+
+    def new_material(rec):
+        mats.append(rec)
+        return len(mats) - 1
+
+    def albedo():
+        return tuple(rs.uniform(3, 0.1, 0.9))
+
+    g = wall_grid
+    # (origin, eu, ev) with cross(eu, ev) pointing into the room
+    walls = [((-1, 0, -1), (0, 0, 2), (2, 0, 0)),    # floor, normal +y
+             ((-1, 2, -1), (2, 0, 0), (0, 0, 2)),    # ceiling, normal -y
+             ((-1, 0, -1), (2, 0, 0), (0, 2, 0)),    # back wall z=-1, normal +z
+             ((-1, 0, -1), (0, 2, 0), (0, 0, 2)),    # left wall x=-1, normal +x
+             ((1, 0, -1), (0, 0, 2), (0, 2, 0))]     # right wall x=1, normal -x
+    for o, eu, ev in walls:
+        v, f, n = _grid_quad(o, eu, ev, g)
+        add(v, f, n, new_material(lambert(albedo())))
+    for center, half, angle in (((-0.35, 0.6, -0.3), (0.3, 0.6, 0.3), 0.3), ((0.4, 0.3, 0.3), (0.3, 0.3, 0.3), -0.3)):
+        c, s = math.cos(angle), math.sin(angle)
+        rot = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+        mid = new_material(lambert(albedo()))
+        for axis in range(3):
+            for sign in (-1.0, 1.0):
+                nrm = np.zeros(3)
+                nrm[axis] = sign
+                ua, va = [a for a in range(3) if a != axis]
+                eu = np.zeros(3)
+                ev = np.zeros(3)
+                eu[ua] = 2 * half[ua]
+                ev[va] = 2 * half[va]
+                if np.dot(np.cross(eu, ev), nrm) < 0:
+                    eu, ev = ev, eu
+                o = np.zeros(3)
+                o[axis] = sign * half[axis]
+                o -= (eu + ev) / 2
+                v, f, n = _grid_quad(o, eu, ev, 1)
+                add(v @ rot.T + np.asarray(center), f, n @ rot.T, mid)
+    sv, sf = icosphere(sphere_level)
+    add(sv * 0.25 + np.array([0.45, 0.85, 0.3]), sf, sv, new_material(lambert(albedo())))
+    lv, lf, ln = _grid_quad((-0.25, 1.999, -0.25), (0.5, 0, 0), (0, 0, 0.5), 1)  # normal -y
+    add(lv, lf, ln, new_material(material_record(albedo=(0.0, 0.0, 0.0), specular=(0.0, 0.0, 0.0),
+                                                 emissivity=(light_radiance,) * 3)))
+    v = np.concatenate(parts_v)
+    f = np.concatenate(parts_f)
+    n = np.concatenate(parts_n)
+    return _pack(v, f, np.stack(mats), material_ids=np.concatenate(mat_ids), normals=n)

@@ -136,10 +136,92 @@ gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* scene,
                                       const float* tmax, uint64_t n, uint32_t anyHit, uint64_t sums[3]);
 
 /* Traversal tuning (set by the autotuner). mode 0: one thread per ray, grid
- * of ceil(n / blockSize) blocks; mode 1 (default): persistent warps that
- * refill finished lanes from a device ray counter. Both perform the same
- * tests per ray and return identical results. */
+ * of ceil(n / blockSize) blocks; mode 1: persistent warps that refill
+ * finished lanes from a device ray counter; mode 2 (default): a coalesced
+ * root-bounds prefilter that finishes rays missing the scene and queues the
+ * rest (warp-ballot compaction) for the persistent walker. All modes perform
+ * the same tests per ray and return identical results. */
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize);
+
+/* ------------------------------------------------------------------------
+ * Rendering passes (wavefront): PT, LT and BPT.
+ *
+ *   gpugi_render(pass = PT)   Pathtracer::Draw + pathtracer.comp
+ *                             (gpugi/renderer/pathtracer.cpp:47-53, gpugi/shader/pathtracer.comp)
+ *   gpugi_render(pass = LT)   LightPathtracer::Draw + lighttracer.comp + showlightcaches.comp
+ *                             (gpugi/renderer/lightpathtracer.cpp:45-49)
+ *   gpugi_render(pass = BPT)  BidirectionalPathtracer::Draw: reset counter, light
+ *                             trace into the light cache, eye pass
+ *                             (gpugi/renderer/bidirectionalpathtracer.cpp:182-203)
+ * ------------------------------------------------------------------------ */
+typedef struct gpugi_image gpugi_image;
+
+enum gpugi_pass { GPUGI_PASS_PT = 0, GPUGI_PASS_LT = 1, GPUGI_PASS_BPT = 2 };
+
+/* Camera UBO (gpugi/shader/globaluniforms.glsl:7-15): U, V scaled by
+ * tan(fov/2)*aspect and tan(fov/2), W unit view direction. */
+typedef struct gpugi_camera {
+    float U[3], V[3], W[3], position[3];
+    float pixelArea;
+} gpugi_camera;
+
+typedef struct gpugi_render_params {
+    uint32_t pass;             /* gpugi_pass */
+    uint32_t width, height;    /* must match the image */
+    uint32_t maxPathLength;    /* MAX_PATHLENGTH */
+    uint32_t rrStartDepth;     /* Russian roulette from this bounce on; 0 = the reference */
+    uint32_t iteration;        /* first iteration: FrameSeed(s) = WangHash(iteration + s) */
+    uint32_t samples;          /* iterations (samples per pixel) rendered by this call */
+    uint32_t numLightSamples;  /* initial light samples per iteration (PT/BPT 128, LT 256) */
+    float sky[3];              /* constant radiance on a miss (addition; 0 = the reference's black) */
+    uint32_t flags;            /* reserved, 0 */
+} gpugi_render_params;
+
+/* Camera::ComputeCameraParams (gpugi/camera/camera.cpp:76-85) and the pixel
+ * area of RendererSystem::SetCamera (gpugi/renderer/renderersystem.cpp:208). */
+gpugi_status gpugi_camera_lookat(const float position[3], const float lookat[3], const float up[3],
+                                 float yFovDegrees, uint32_t width, uint32_t height, gpugi_camera* out);
+
+/* Accumulation image: RGBA32F (the backbuffer) plus, with flags & 1, an FP64
+ * RGB accumulation used only for converged oracle images and error sums. */
+gpugi_status gpugi_image_create(gpugi_ctx* ctx, uint32_t width, uint32_t height, uint32_t flags,
+                                gpugi_image** out);
+void gpugi_image_destroy(gpugi_image* image);
+gpugi_status gpugi_image_clear(gpugi_ctx* ctx, gpugi_image* image);
+/* Copy the accumulation to host memory (either pointer may be NULL). */
+gpugi_status gpugi_image_read(gpugi_ctx* ctx, const gpugi_image* image, float* rgba, double* rgb64);
+/* TextureMSE (gpugi/imageut/texturemse.cpp:39-65, utils/sqerror.frag):
+ * mean over pixels of |rgb / divisor - reference|^2 (the RGB sum, not the
+ * channel mean), reduced in FP64 on the device. reference: host, 3 floats per
+ * pixel. useFp64 selects the FP64 accumulation as the source. */
+gpugi_status gpugi_image_mse(gpugi_ctx* ctx, const gpugi_image* image, double divisor, const float* reference,
+                             uint32_t useFp64, double* mse);
+
+/* Light sources of a scene (Scene::LoadLightSources, gpugi/scene/scene.cpp:244-293,
+ * and point lights, :295-307) and the host light sampler
+ * (LightSampler::GenerateRandomSamples, gpugi/scene/lightsampler.cpp:18-95).
+ * Emissive triangles are found from the materials at upload. A directional
+ * light (direction towards the light, irradiance) is an addition; its
+ * samples carry normalThetaCos = 3. Samples: 8 floats each
+ * {position.xyz, normalPhi, intensity.xyz, normalThetaCos}. */
+gpugi_status gpugi_scene_add_point_light(gpugi_scene* scene, const float position[3], const float intensity[3]);
+gpugi_status gpugi_scene_add_directional_light(gpugi_scene* scene, const float towardsLight[3],
+                                               const float irradiance[3]);
+gpugi_status gpugi_generate_light_samples(const gpugi_scene* scene, uint64_t* rngState, uint32_t numSamples,
+                                          float* out);
+
+/* Render `samples` iterations of one pass into the image. lightSamples:
+ * host, samples * numLightSamples * 8 floats (one light-sample set per
+ * iteration, as RendererSystem::PerIterationBufferUpdate regenerates them);
+ * NULL generates them on the host with rngState (required then). Asynchronous
+ * on the context stream. */
+gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* scene, const gpugi_camera* camera,
+                          const gpugi_render_params* params, const float* lightSamples, uint64_t* rngState,
+                          gpugi_image* image);
+
+/* Rays traced by the last gpugi_render call, by kind: {camera/extension
+ * (closest hit), shadow/connection (any hit)}. Synchronises. */
+gpugi_status gpugi_render_ray_counts(gpugi_ctx* ctx, uint64_t counts[2]);
 
 #ifdef __cplusplus
 }

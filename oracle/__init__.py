@@ -99,6 +99,36 @@ def bruteforce_closest(slots, positions, rays, num_threads=None):
     return dict(slot=slot, t=t)
 
 
+PASSES = {"PT": 0, "LT": 1, "BPT": 2}
+
+
+def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.ndarray, frame_seed: int,
+           light_samples: np.ndarray, max_path_length: int = 8, rr_start_depth: int = 0, sky=(0.0, 0.0, 0.0),
+           accum: np.ndarray | None = None, num_threads=None) -> np.ndarray:
+    """One iteration of a pass (restated pathtracer.comp / lighttracer.comp /
+    BPT), accumulated into accum (H, W, 4) float32, which is returned."""
+    from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
+    L = lib()
+    P, U32, I, F = C.c_void_p, C.c_uint32, C.c_int, C.c_float
+    L.oracle_render.argtypes = [P, U32, U32, P, U32, U32, P, P, U32, P, U32, I, I, I, I, I, P, U32, P, I, P, P, I]
+    hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
+    slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
+    pos = np.ascontiguousarray(scene["positions"], dtype=np.float32)
+    vi = np.ascontiguousarray(vertex_info(scene["normals"], scene["texcoords"]), dtype=np.float32)
+    mats = np.ascontiguousarray(scene["materials"], dtype=np.float32)
+    cam = np.ascontiguousarray(camera, dtype=np.float32)
+    ls = np.ascontiguousarray(light_samples, dtype=np.float32).reshape(-1, 8)
+    skya = np.asarray(sky, dtype=np.float32)
+    if accum is None:
+        accum = np.zeros((height, width, 4), np.float32)
+    rc = L.oracle_render(_p(hier), hier.shape[0], bvh.bounds_kind, _p(slots), slots.shape[0], bvh.leaf_size,
+                         _p(pos), _p(vi), pos.shape[0], _p(mats), mats.shape[0], PASSES[pass_], width, height,
+                         max_path_length, rr_start_depth, _p(cam), frame_seed & 0xFFFFFFFF, _p(ls), ls.shape[0],
+                         _p(skya), _p(accum), threads() if num_threads is None else num_threads)
+    assert rc == 0
+    return accum
+
+
 def algorithmic_bytes(counters: np.ndarray, any_hit: bool = False) -> np.ndarray:
     """Bytes per ray of gpugi's own fetch pattern: 24 (ray in) + 16 (t, id, u, v
     out; 4 for any-hit) + 32 per node + 16 per leaf slot + 36 per valid triangle

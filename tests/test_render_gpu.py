@@ -1,0 +1,141 @@
+"""GPU wavefront renderers (PT, LT, BPT) against the oracle, through the C ABI.
+
+The oracle and the kernels draw the same per-path RNG streams in the same
+order (wanghash seeds, xorshift32) on bit-identical hierarchies, and take the
+same light-sample arrays. Shading uses CUDA's sinf/cosf/powf instead of the C
+library's, so values differ in the last bits and a path may eventually branch
+differently; the bars are therefore:
+  * depth-1 PT (emission + NEE at the first hit): per-pixel relative error
+    below 1e-4 of the image maximum (near bit-identical paths);
+  * full-depth PT / LT / BPT: image means within 2 %, 8x8-block means within
+    a statistical bound estimated from four independent batches.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gpugi_gb300 import bvh, cuda, render, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def room(cuda_ctx):
+    sc = scenes.cornell_room(seed=1, sphere_level=3, wall_grid=8)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]),
+                               sc["materials"])
+    yield sc, b, ds
+    ds.close()
+
+
+def _light_sets(ds, n_sets, n, seed=123):
+    state = [seed]
+    return np.stack([render.generate_light_samples(ds, state, n) for _ in range(n_sets)])
+
+
+def _oracle(b, sc, pass_, W, H, cam, ls, iters, first=0, **kw):
+    acc = None
+    for s in range(iters):
+        acc = oracle.render(b, sc, pass_, W, H, cam.as_array(), render.wanghash(first + s), ls[s], accum=acc, **kw)
+    return acc
+
+
+def test_light_sampler_matches_scene_lights(cuda_ctx, room):
+    sc, b, ds = room
+    ls = render.generate_light_samples(ds, [123], 128)
+    assert np.all(ls[:, 7] < 1.5)  # area-light samples (normal.z of a downward light is 0)
+    assert np.allclose(ls[:, 1], 1.999 - 1e-4, atol=1e-6)
+    assert (np.abs(ls[:, 0]) <= 0.25 + 1e-6).all() and (np.abs(ls[:, 2]) <= 0.25 + 1e-6).all()
+    # each sample carries luminance * area / n = 10 * 0.25 / 128
+    assert np.allclose(ls[:, 4:7], 10.0 * 0.25 / 128, rtol=1e-5)
+
+
+def test_pt_direct_light_matches_oracle(cuda_ctx, room):
+    sc, b, ds = room
+    W = H = 48
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    ls = _light_sets(ds, 4, 128)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, img, "PT", max_path_length=1, samples=4, iteration=0, light_samples=ls)
+    g = img.read()
+    o = _oracle(b, sc, "PT", W, H, cam, ls, 4, max_path_length=1)
+    err = np.abs(g[..., :3] - o[..., :3])
+    assert err.max() <= 1e-4 * np.abs(o[..., :3]).max() + 1e-6
+    img.close()
+
+
+def _stat_compare(g_batches, o_img, tol_mean=0.02, z=6.0):
+    """g_batches: (K, H, W, 3) per-batch means; o_img: oracle mean image."""
+    g = g_batches.mean(0)
+    assert abs(g.mean() / o_img.mean() - 1) < tol_mean, (g.mean(), o_img.mean())
+    K = g_batches.shape[0]
+    H, W = g.shape[:2]
+    blk = lambda a: a[..., : H // 8 * 8, : W // 8 * 8, :].reshape(*a.shape[:-3], H // 8, 8, W // 8, 8, 3).mean((-4, -2))
+    gb = blk(g_batches)                          # (K, h, w, 3)
+    se = gb.std(0, ddof=1) / np.sqrt(K)          # standard error of the GPU block mean
+    d = np.abs(gb.mean(0) - blk(o_img[None])[0])
+    assert (d <= z * np.sqrt(2) * se + 1e-3 * np.abs(gb.mean(0)) + 1e-5).mean() > 0.97
+
+
+@pytest.mark.parametrize("pass_,iters", [("PT", 32), ("BPT", 32), ("LT", 48)])
+def test_full_depth_passes_match_oracle(cuda_ctx, room, pass_, iters):
+    sc, b, ds = room
+    W = H = 32
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    nls = render.DEFAULT_LIGHT_SAMPLES[pass_]
+    ls = _light_sets(ds, iters, nls)
+    K = 4
+    per = iters // K
+    batches = []
+    for k in range(K):
+        img = render.Image(cuda_ctx, W, H)
+        render.render(cuda_ctx, ds, cam, img, pass_, max_path_length=6, samples=per, iteration=k * per,
+                      light_samples=ls[k * per:(k + 1) * per])
+        batches.append(img.read()[..., :3] / per)
+        img.close()
+    o = _oracle(b, sc, pass_, W, H, cam, ls, iters, max_path_length=6)[..., :3] / iters
+    _stat_compare(np.stack(batches), o, tol_mean=0.03)
+    assert cuda_ctx.device_error_bits() == 0
+
+
+def test_bpt_counts_iterations_in_alpha(cuda_ctx, room):
+    sc, b, ds = room
+    W = H = 16
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, img, "BPT", max_path_length=4, samples=3, rng_state=[7])
+    assert np.all(img.read()[..., 3] == 3.0)  # pathtracer_bidir.comp:248 writes vec4(color, 1)
+    img.close()
+
+
+def test_fp64_accumulation_and_mse(cuda_ctx, room):
+    sc, b, ds = room
+    W = H = 24
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    img = render.Image(cuda_ctx, W, H, fp64=True)
+    render.render(cuda_ctx, ds, cam, img, "PT", max_path_length=4, samples=16, rng_state=[5])
+    f32 = img.read()[..., :3].astype(np.float64)
+    f64 = img.read64()
+    assert np.allclose(f32, f64, rtol=1e-4, atol=1e-5)
+    ref = (f64 / 16 * 0.9).astype(np.float32)
+    expect = ((f64 / 16 - ref.astype(np.float64)) ** 2).sum(-1).mean()
+    assert abs(img.mse(16, ref, use_fp64=True) / expect - 1) < 1e-9
+    assert abs(img.mse(16, ref, use_fp64=False) / expect - 1) < 1e-3
+    img.close()
+
+
+def test_ray_counts_and_rr(cuda_ctx, room):
+    sc, b, ds = room
+    W = H = 32
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, img, "PT", max_path_length=8, samples=2, rng_state=[3])
+    closest, shadow = render.ray_counts(cuda_ctx)
+    assert closest >= 2 * W * H and closest <= 8 * 2 * W * H
+    assert 0 < shadow <= closest
+    # Russian roulette only after depth 3 keeps more paths alive
+    render.render(cuda_ctx, ds, cam, img, "PT", max_path_length=8, samples=2, rr_start_depth=3, rng_state=[3])
+    closest_rr3, _ = render.ray_counts(cuda_ctx)
+    assert closest_rr3 > closest
+    img.close()

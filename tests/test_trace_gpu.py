@@ -43,7 +43,7 @@ def test_closest_and_any_match_oracle(cuda_ctx, icosphere_65536, method, leaf):
     b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, leaf_size=leaf)
     ds = cuda_ctx.upload_scene(b, sc["positions"])
     try:
-        for mode in (0, 1):  # one thread per ray / persistent lane refill
+        for mode in (0, 1, 2):  # thread per ray / persistent lane refill / root prefilter + persistent
             cuda_ctx.set_trace_config(mode=mode)
             for rays in (scenes.random_rays(1 << 18, seed=3), scenes.aimed_rays(1 << 18, sc["positions"], seed=4)):
                 g = cuda.trace_closest(cuda_ctx, ds, rays)
@@ -53,7 +53,7 @@ def test_closest_and_any_match_oracle(cuda_ctx, icosphere_65536, method, leaf):
                 oa = oracle.trace_any(b, sc["positions"], rays)["occluded"]
                 assert np.array_equal(occ, oa)
     finally:
-        cuda_ctx.set_trace_config(mode=1)
+        cuda_ctx.set_trace_config(mode=2)
     ds.close()
 
 
