@@ -57,6 +57,28 @@ def test_closest_and_any_match_oracle(cuda_ctx, icosphere_65536, method, leaf):
     ds.close()
 
 
+@pytest.mark.parametrize("method", ["kdtree", "sweep"])
+def test_ellipsoid_bounds_match_oracle_and_bruteforce(cuda_ctx, method):
+    """Ellipsoid nodes (the BVH kind of the large BDPT workload): the walk
+    over fitted ellipsoids is bit-exact against the oracle and finds the same
+    closest hits as brute force (the fit contains every triangle)."""
+    sc = scenes.displaced_icosphere(6000, seed=9)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, fit="ellipsoid")
+    assert b.bounds_kind == 1
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    for mode in (0, 1, 2):
+        cuda_ctx.set_trace_config(mode=mode)
+        for rays in (scenes.aimed_rays(40_000, sc["positions"], seed=13), scenes.random_rays(40_000, seed=14)):
+            g = cuda.trace_closest(cuda_ctx, ds, rays)
+            _compare_closest(g, oracle.trace_closest(b, sc["positions"], rays))
+            assert np.array_equal(cuda.trace_any(cuda_ctx, ds, rays),
+                                  oracle.trace_any(b, sc["positions"], rays)["occluded"])
+            bf = oracle.bruteforce_closest(b.slots, sc["positions"], rays)
+            assert (g["t"].view(np.uint32) == bf["t"].view(np.uint32)).mean() > 0.999
+    cuda_ctx.set_trace_config(mode=2)
+    ds.close()
+
+
 def test_full_size_properties(cuda_ctx, icosphere_65536):
     """2^20 rays of the closest-hit workload: exact against the oracle, and
     size-independent checks (any-hit == closest-hit hit mask, t > 1e-4)."""
