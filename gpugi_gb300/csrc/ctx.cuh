@@ -91,6 +91,11 @@ gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool
 gpugi_status launch_trace_stats(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
                                 const float* oz, const float* dx, const float* dy, const float* dz,
                                 const float* tmax, uint64_t n, uint32_t anyHit, unsigned long long* sums);
+gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
+                                      const float* oy, const float* oz, const float* dx, const float* dy,
+                                      const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
+                                      float* u, float* v, uint8_t* occluded, uint32_t* queue,
+                                      unsigned long long* counters);
 // Light tables and the host light sampler (host.cu).
 void build_light_tables(gpugi_scene* sc);
 void generate_light_samples(gpugi_scene* sc, uint64_t& rng, uint32_t numSamples, float* out);

@@ -243,6 +243,43 @@ gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool a
     return GPUGI_OK;
 }
 
+// The same two launches as launch_trace_filtered, on scratch memory the
+// caller provides (queue of n entries, 4 zeroed counters); allocates nothing.
+gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
+                                      const float* oy, const float* oz, const float* dx, const float* dy,
+                                      const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
+                                      float* u, float* v, uint8_t* occluded, uint32_t* queue,
+                                      unsigned long long* counters) {
+    if (n == 0) return GPUGI_OK;
+    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    const unsigned grid1 = (unsigned)((n + 255) / 256);
+#define GPUGI_FILTER_ON(A, B)                                                                                       \
+    k_trace_root_filter<A, B><<<grid1, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, \
+                                                              v, occluded, queue, counters)
+    if (!ell) {
+        if (anyHit) GPUGI_FILTER_ON(true, 0);
+        else GPUGI_FILTER_ON(false, 0);
+    } else {
+        if (anyHit) GPUGI_FILTER_ON(true, 1);
+        else GPUGI_FILTER_ON(false, 1);
+    }
+#undef GPUGI_FILTER_ON
+    void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
+              const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
+              uint32_t*);
+    if (!ell) k = anyHit ? k_trace_queue<true, 0> : k_trace_queue<false, 0>;
+    else k = anyHit ? k_trace_queue<true, 1> : k_trace_queue<false, 1>;
+    int perSM = 0;
+    GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k, 128, 0));
+    uint64_t grid = (uint64_t)ctx->numSMs * (uint64_t)(perSM > 0 ? perSM : 1);
+    const uint64_t needed = (n + 127) / 128;
+    if (grid > needed) grid = needed;
+    k<<<(unsigned)grid, 128, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded,
+                                               queue, counters, ctx->errWord);
+    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
 template <int BOUNDS, bool ANY>
 __global__ void __launch_bounds__(256) k_trace_stats(DevScene s, const float* __restrict__ ox,
                                                      const float* __restrict__ oy, const float* __restrict__ oz,

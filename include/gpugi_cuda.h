@@ -126,6 +126,26 @@ gpugi_status gpugi_trace_any_device(gpugi_ctx* ctx, const gpugi_scene* scene,
                                     const float* dx, const float* dy, const float* dz,
                                     const float* tmax, uint64_t n, uint8_t* occluded);
 
+/* Closest hit without any device allocation in the call. No counterpart in
+ * the reference: it exists for callers that cannot let the library call
+ * cudaMalloc, such as an engine that owns all device memory through its own
+ * pool, or a frame loop where an allocation would synchronise the device.
+ * Same arguments (device pointers) and results as gpugi_trace_closest_device.
+ * Scratch memory is a static device array in the library, held by every GPU
+ * that loads it until the process exits; it bounds n to
+ * GPUGI_NOALLOC_MAX_RAYS (larger n returns GPUGI_ERROR_INVALID_ARGUMENT).
+ * The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (other
+ * streams, other contexts on the same device) race and must be serialised
+ * by the caller. Asynchronous on the context stream. */
+#define GPUGI_NOALLOC_MAX_RAYS (1u << 20)
+gpugi_status gpugi_trace_closest_noalloc(gpugi_ctx* ctx, const gpugi_scene* scene,
+                                         const float* ox, const float* oy, const float* oz,
+                                         const float* dx, const float* dy, const float* dz,
+                                         const float* tmax, uint64_t n,
+                                         int32_t* slot, float* t, float* u, float* v);
+
 /* Fetch statistics of the walk for n device rays: sums over all rays of
  * {nodes visited, leaf slots fetched, valid triangles tested}, the analogue
  * of TRACERAY_DEBUG_VARS (gpugi/shader/traceray.glsl:59-61,131-133). Used to
