@@ -210,6 +210,7 @@ def run_ours(args, world, rank, local):
     sc, b, host_batches = make_workload()
     ctx = cuda.Context(local)
     ctx.set_trace_config(mode=args.trace_mode)
+    ctx.set_scene_layout(args.shared_nodes, 0)
     ds = ctx.upload_scene(b, sc["positions"])
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     batches = [{k: torch.from_numpy(rb[k]).to(dev) for k in cuda.RAY_KEYS} for rb in host_batches]
@@ -305,6 +306,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--shared-nodes", type=int, default=0,
+                    help="top-of-tree nodes staged in shared memory by the walkers")
     ap.add_argument("--trace-mode", type=int, default=2,
                     help="0: thread per ray, 1: persistent lane refill, 2: root prefilter + persistent")
     args = ap.parse_args()

@@ -31,7 +31,7 @@ HOST_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
               "-I", str(INCLUDE), "-I", str(CSRC)] + ARCH
 
-CUDA_SOURCES = ["trace.cu", "scene.cu", "render.cu", "capi.cu", "host.cu", "noalloc.cu"]
+CUDA_SOURCES = ["trace.cu", "scene.cu", "render.cu", "capi.cu", "host.cu", "noalloc.cu", "nrc.cu", "tune.cu"]
 
 
 def _run(cmd):
@@ -86,9 +86,10 @@ def build_headless(force=False) -> Path | None:
         return None
     out = LIB / "gpugi_headless"
     srcs = sorted(src_dir.glob("*.cpp"))
-    if force or _stale(out, srcs + _headers() + [LIB / "libgpugi_cuda.so"]):
+    deps = srcs + _headers() + [LIB / "libgpugi_cuda.so", LIB / "libgpugi_bvhmake.so"]
+    if force or _stale(out, deps):
         _run([CXX] + HOST_FLAGS + ["-I", str(INCLUDE), "-I", str(src_dir), "-o", str(out)] + [str(s) for s in srcs]
-             + ["-L", str(LIB), "-lgpugi_cuda", "-Wl,-rpath,$ORIGIN", "-pthread"])
+             + ["-L", str(LIB), "-lgpugi_cuda", "-lgpugi_bvhmake", "-Wl,-rpath,$ORIGIN", "-pthread"])
     return out
 
 

@@ -34,6 +34,10 @@ def _lib():
         lib.gpugi_bvh_write_file.argtypes = [P, C.c_char_p]
         lib.gpugi_bvh_read_file.argtypes = [C.c_char_p, C.POINTER(P)]
         lib.gpugi_bvh_vertices.argtypes = [P, C.POINTER(U32), P]
+        lib.gpugi_bvh_set_vertex_attributes.argtypes = [P, P, P]
+        lib.gpugi_bvh_vertex_attributes.argtypes = [P, P, P]
+        lib.gpugi_bvh_set_materials.argtypes = [P, P, U32]
+        lib.gpugi_bvh_materials.argtypes = [P, C.POINTER(U32), P]
         lib.gpugi_bvh_free.argtypes = [P]
         lib.gpugi_bvh_free.restype = None
         lib.gpugi_bvh_last_error.restype = C.c_char_p
@@ -54,6 +58,9 @@ class BVH:
     bounds_kind: int        # 0 = AABB, 1 = ellipsoid
     max_depth: int
     positions: np.ndarray | None = None
+    normals: np.ndarray | None = None      # from a file: float32 [V, 3]
+    texcoords: np.ndarray | None = None    # from a file: float32 [V, 2]
+    materials: np.ndarray | None = None    # from a file: float32 [M, 24] (empty when absent)
 
     @property
     def num_nodes(self) -> int:
@@ -101,8 +108,10 @@ def build_bvh(positions: np.ndarray, triangles: np.ndarray, method: str = "sweep
         lib.gpugi_bvh_free(h)
 
 
-def write_bvh_file(positions: np.ndarray, triangles: np.ndarray, path: str, **kw) -> None:
-    """Build and write bvhmake's NamedArray file."""
+def write_bvh_file(positions: np.ndarray, triangles: np.ndarray, path: str, normals=None, texcoords=None,
+                   materials=None, **kw) -> None:
+    """Build and write bvhmake's NamedArray file (vertex normals/texcoords
+    and material records are optional)."""
     lib = _lib()
     pos = np.ascontiguousarray(positions, dtype=np.float32)
     tri = np.ascontiguousarray(triangles, dtype=np.uint32)
@@ -113,6 +122,15 @@ def write_bvh_file(positions: np.ndarray, triangles: np.ndarray, path: str, **kw
     if rc != 0:
         raise ValueError(lib.gpugi_bvh_last_error().decode())
     try:
+        nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32)
+        tc = None if texcoords is None else np.ascontiguousarray(texcoords, dtype=np.float32)
+        for a, k in ((nrm, 3), (tc, 2)):
+            if a is not None and a.shape != (pos.shape[0], k):
+                raise ValueError("vertex attribute arrays need one row per vertex")
+        lib.gpugi_bvh_set_vertex_attributes(h, None if nrm is None else _ptr(nrm), None if tc is None else _ptr(tc))
+        if materials is not None:
+            mats = np.ascontiguousarray(materials, dtype=np.float32).reshape(-1, 24)
+            lib.gpugi_bvh_set_materials(h, _ptr(mats), mats.shape[0])
         if lib.gpugi_bvh_write_file(h, str(path).encode()) != 0:
             raise OSError(lib.gpugi_bvh_last_error().decode())
     finally:
@@ -131,6 +149,14 @@ def read_bvh_file(path: str) -> BVH:
         pos = np.zeros((nv.value, 3), dtype=np.float32)
         lib.gpugi_bvh_vertices(h, C.byref(nv), _ptr(pos))
         b.positions = pos
+        b.normals = np.zeros((nv.value, 3), dtype=np.float32)
+        b.texcoords = np.zeros((nv.value, 2), dtype=np.float32)
+        lib.gpugi_bvh_vertex_attributes(h, _ptr(b.normals), _ptr(b.texcoords))
+        nm = C.c_uint32()
+        lib.gpugi_bvh_materials(h, C.byref(nm), None)
+        b.materials = np.zeros((nm.value, 24), dtype=np.float32)
+        if nm.value:
+            lib.gpugi_bvh_materials(h, C.byref(nm), _ptr(b.materials))
         return b
     finally:
         lib.gpugi_bvh_free(h)

@@ -160,6 +160,9 @@ struct Node {
 
 struct gpugi_bvh {
     std::vector<float> positions;      // 3 per vertex
+    std::vector<float> normals;        // 3 per vertex (file attribute; may be empty)
+    std::vector<float> texcoords;      // 2 per vertex (file attribute; may be empty)
+    std::vector<float> materials;      // 24 per material ("gpugi_materials" chunk; may be empty)
     std::vector<uint32_t> triangles;   // 4 per triangle
     uint32_t leafSize = 8;
     uint32_t boundsKind = GPUGI_FIT_AABOX;
@@ -649,8 +652,12 @@ int gpugi_bvh_write_file(const gpugi_bvh* b, const char* path) {
     const uint32_t nv = (uint32_t)(b->positions.size() / 3), nn = (uint32_t)b->nodes.size();
     // "vertices": {position, normal, texcoord} = 32 bytes (filedef.hpp:15-20).
     std::vector<float> verts((size_t)nv * 8, 0.0f);
-    for (uint32_t v = 0; v < nv; ++v)
+    const bool haveN = b->normals.size() == 3 * (size_t)nv, haveT = b->texcoords.size() == 2 * (size_t)nv;
+    for (uint32_t v = 0; v < nv; ++v) {
         for (int k = 0; k < 3; ++k) verts[8 * (size_t)v + k] = b->positions[3 * (size_t)v + k];
+        for (int k = 0; k < 3 && haveN; ++k) verts[8 * (size_t)v + 3 + k] = b->normals[3 * (size_t)v + k];
+        for (int k = 0; k < 2 && haveT; ++k) verts[8 * (size_t)v + 6 + k] = b->texcoords[2 * (size_t)v + k];
+    }
     // "hierarchy": {parent, firstChild, escape} (filedef.hpp:41-46).
     std::vector<uint32_t> hier((size_t)nn * 3);
     for (uint32_t i = 0; i < nn; ++i) {
@@ -672,7 +679,9 @@ int gpugi_bvh_write_file(const gpugi_bvh* b, const char* path) {
               WriteChunk(f, b->boundsKind == GPUGI_FIT_ELLIPSOID ? "bounding_ellipsoid" : "bounding_aabox", nn, 24,
                          bv.data()) &&
               WriteChunk(f, "hierarchy", nn, 12, hier.data()) &&
-              WriteChunk(f, "triangles", nBlocks, 16 * b->leafSize, b->leaves.data());
+              WriteChunk(f, "triangles", nBlocks, 16 * b->leafSize, b->leaves.data()) &&
+              (b->materials.empty() ||
+               WriteChunk(f, "gpugi_materials", (uint32_t)(b->materials.size() / 24), 96, b->materials.data()));
     std::fclose(f);
     if (!ok) {
         g_lastError = "short write";
@@ -706,6 +715,18 @@ int gpugi_bvh_read_file(const char* path, gpugi_bvh** out) {
             b->positions.resize((size_t)h.numElements * 3);
             for (uint32_t v = 0; v < h.numElements; ++v)
                 std::memcpy(&b->positions[3 * (size_t)v], &data[(size_t)v * h.elementSize], 12);
+            if (h.elementSize >= 32) {
+                b->normals.resize((size_t)h.numElements * 3);
+                b->texcoords.resize((size_t)h.numElements * 2);
+                for (uint32_t v = 0; v < h.numElements; ++v) {
+                    std::memcpy(&b->normals[3 * (size_t)v], &data[(size_t)v * h.elementSize + 12], 12);
+                    std::memcpy(&b->texcoords[2 * (size_t)v], &data[(size_t)v * h.elementSize + 24], 8);
+                }
+            }
+        } else if (name == "gpugi_materials") {
+            if (h.elementSize != 96) { rc = -4; g_lastError = "gpugi_materials element must be 96 bytes"; break; }
+            b->materials.resize((size_t)h.numElements * 24);
+            std::memcpy(b->materials.data(), data.data(), bytes);
         } else if (name == "hierarchy") {
             if (h.elementSize != 12) { rc = -4; g_lastError = "hierarchy element must be 12 bytes"; break; }
             hier.resize((size_t)h.numElements * 3);
@@ -753,6 +774,44 @@ int gpugi_bvh_vertices(const gpugi_bvh* b, uint32_t* numVertices, float* positio
     if (!b) return -1;
     if (numVertices) *numVertices = (uint32_t)(b->positions.size() / 3);
     if (positions) std::memcpy(positions, b->positions.data(), b->positions.size() * sizeof(float));
+    return 0;
+}
+
+int gpugi_bvh_set_vertex_attributes(gpugi_bvh* b, const float* normals, const float* texcoords) {
+    if (!b) return -1;
+    const size_t nv = b->positions.size() / 3;
+    if (normals) b->normals.assign(normals, normals + 3 * nv);
+    else b->normals.clear();
+    if (texcoords) b->texcoords.assign(texcoords, texcoords + 2 * nv);
+    else b->texcoords.clear();
+    return 0;
+}
+
+int gpugi_bvh_vertex_attributes(const gpugi_bvh* b, float* normals, float* texcoords) {
+    if (!b) return -1;
+    const size_t nv = b->positions.size() / 3;
+    if (normals) {
+        if (b->normals.size() == 3 * nv) std::memcpy(normals, b->normals.data(), 3 * nv * sizeof(float));
+        else std::memset(normals, 0, 3 * nv * sizeof(float));
+    }
+    if (texcoords) {
+        if (b->texcoords.size() == 2 * nv) std::memcpy(texcoords, b->texcoords.data(), 2 * nv * sizeof(float));
+        else std::memset(texcoords, 0, 2 * nv * sizeof(float));
+    }
+    return 0;
+}
+
+int gpugi_bvh_set_materials(gpugi_bvh* b, const float* records, uint32_t numMaterials) {
+    if (!b || (numMaterials && !records)) return -1;
+    b->materials.assign(records, records + 24 * (size_t)numMaterials);
+    return 0;
+}
+
+int gpugi_bvh_materials(const gpugi_bvh* b, uint32_t* numMaterials, float* records) {
+    if (!b) return -1;
+    if (numMaterials) *numMaterials = (uint32_t)(b->materials.size() / 24);
+    if (records && !b->materials.empty())
+        std::memcpy(records, b->materials.data(), b->materials.size() * sizeof(float));
     return 0;
 }
 

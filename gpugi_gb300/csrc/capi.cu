@@ -142,6 +142,16 @@ gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t bloc
     return GPUGI_OK;
 }
 
+gpugi_status gpugi_set_scene_layout(gpugi_ctx* ctx, uint32_t sharedNodes, uint32_t renderSharedNodes) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    // 227 KB of shared memory per block at most: 7,000 nodes of 32 B
+    if (sharedNodes > 7000 || renderSharedNodes > 7000)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "at most 7000 staged nodes (227 KB of shared memory)");
+    ctx->sharedNodes = sharedNodes;
+    ctx->renderSharedNodes = renderSharedNodes;
+    return GPUGI_OK;
+}
+
 gpugi_status gpugi_trace_closest_device(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
                                         const float* oz, const float* dx, const float* dy, const float* dz,
                                         const float* tmax, uint64_t n, int32_t* slot, float* t, float* u,

@@ -20,10 +20,15 @@ struct gpugi_ctx {
     // trace tuning
     uint32_t traceMode = 2;  // 0 = thread per ray, 1 = persistent lane refill, 2 = root prefilter + 1
     uint32_t traceBlock = 128;
+    uint32_t sharedNodes = 0;        // top-of-tree nodes laid out first and staged by ray-query walkers
+    uint32_t renderSharedNodes = 0;  // nodes staged by the renderer's walkers
     void* scratch = nullptr;  // 256 B of device counters (work distribution)
     uint32_t* queue = nullptr;  // ray-index queue of the root prefilter (mode 2)
     uint64_t queueCap = 0;
     int numSMs = 0;
+    // batched rendering
+    uint32_t batchPaths = 16u << 20;  // path-queue capacity of one round
+    uint32_t batchGraph = 1;          // replay rounds as a CUDA graph
     // wavefront renderer buffers (owned by render.cu)
     void* render = nullptr;
     void (*renderFree)(gpugi_ctx*) = nullptr;
@@ -96,6 +101,15 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
                                       const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
                                       float* u, float* v, uint8_t* occluded, uint32_t* queue,
                                       unsigned long long* counters);
+// Launch shape of a persistent walker: grid, dynamic shared memory and the
+// number of top-of-tree nodes it stages (at most maxStage).
+struct WalkerLaunch {
+    unsigned grid = 1;
+    size_t smem = 0;
+    uint32_t stage = 0;
+};
+gpugi_status walker_launch_config(gpugi_ctx* ctx, const gpugi_scene* sc, const void* kernel, uint64_t n,
+                                  uint32_t maxStage, WalkerLaunch& out);
 // Light tables and the host light sampler (host.cu).
 void build_light_tables(gpugi_scene* sc);
 void generate_light_samples(gpugi_scene* sc, uint64_t& rng, uint32_t numSamples, float* out);

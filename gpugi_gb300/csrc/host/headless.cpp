@@ -1,0 +1,118 @@
+// Headless front end of the C++ renderer classes: loads a scene file, sets
+// up a RendererSystem like Application does (application.cpp:211-260,
+// 346-376) and draws a number of iterations, then writes the normalised
+// backbuffer as PFM (Application::SaveImage) and prints a JSON summary.
+//
+//   gpugi_headless --scene FILE [--renderer Pathtracer|LightPathtracer|
+//                  BidirectionalPathtracer|NrcPathtracer] [--size W H]
+//                  [--camera px py pz lx ly lz fovy] [--iterations N]
+//                  [--path-length L] [--rr-start D] [--sky r g b]
+//                  [--point-light px py pz ir ig ib] [--reference FILE.pfm]
+//                  [--out FILE.pfm] [--device D]
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gpugi_renderer.hpp"
+
+namespace {
+
+struct Args {
+    std::string scene, renderer = "Pathtracer", out, reference;
+    int width = 256, height = 256, iterations = 16, device = 0;
+    unsigned pathLength = 8, rrStart = 0;
+    float cam[7] = {0.0f, 1.0f, 3.4f, 0.0f, 1.0f, 0.0f, 40.0f};
+    float sky[3] = {0.0f, 0.0f, 0.0f};
+    std::vector<PointLight> pointLights;
+};
+
+[[noreturn]] void usage(const char* msg) {
+    std::fprintf(stderr, "gpugi_headless: %s\n", msg);
+    std::exit(2);
+}
+
+Args parse(int argc, char** argv) {
+    Args a;
+    auto need = [&](int& i, int n) {
+        if (i + n >= argc) usage((std::string("missing values after ") + argv[i]).c_str());
+    };
+    for (int i = 1; i < argc; ++i) {
+        const std::string k = argv[i];
+        if (k == "--scene") { need(i, 1); a.scene = argv[++i]; }
+        else if (k == "--renderer") { need(i, 1); a.renderer = argv[++i]; }
+        else if (k == "--out") { need(i, 1); a.out = argv[++i]; }
+        else if (k == "--reference") { need(i, 1); a.reference = argv[++i]; }
+        else if (k == "--size") { need(i, 2); a.width = std::atoi(argv[++i]); a.height = std::atoi(argv[++i]); }
+        else if (k == "--iterations") { need(i, 1); a.iterations = std::atoi(argv[++i]); }
+        else if (k == "--device") { need(i, 1); a.device = std::atoi(argv[++i]); }
+        else if (k == "--path-length") { need(i, 1); a.pathLength = (unsigned)std::atoi(argv[++i]); }
+        else if (k == "--rr-start") { need(i, 1); a.rrStart = (unsigned)std::atoi(argv[++i]); }
+        else if (k == "--camera") { need(i, 7); for (float& c : a.cam) c = std::strtof(argv[++i], nullptr); }
+        else if (k == "--sky") { need(i, 3); for (float& c : a.sky) c = std::strtof(argv[++i], nullptr); }
+        else if (k == "--point-light") {
+            need(i, 6);
+            PointLight p;
+            p.position = ei::Vec3(std::strtof(argv[i + 1], nullptr), std::strtof(argv[i + 2], nullptr),
+                                  std::strtof(argv[i + 3], nullptr));
+            p.intensity = ei::Vec3(std::strtof(argv[i + 4], nullptr), std::strtof(argv[i + 5], nullptr),
+                                   std::strtof(argv[i + 6], nullptr));
+            a.pointLights.push_back(p);
+            i += 6;
+        } else usage((std::string("unknown argument ") + k).c_str());
+    }
+    if (a.scene.empty()) usage("--scene is required");
+    if (a.width <= 0 || a.height <= 0 || a.iterations < 0) usage("bad size or iteration count");
+    return a;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    const Args a = parse(argc, argv);
+    try {
+        RendererSystem system(a.device);
+        system.SetScreenSize(ei::IVec2(a.width, a.height));
+        system.SetMaxPathLength(a.pathLength);
+        system.SetRussianRouletteStart(a.rrStart);
+        auto scene = std::make_shared<Scene>(system.GetContext(), a.scene);
+        for (const PointLight& p : a.pointLights) scene->AddPointLight(p);
+        system.SetScene(scene);
+        system.SetCamera(Camera(ei::Vec3(a.cam[0], a.cam[1], a.cam[2]), ei::Vec3(a.cam[3], a.cam[4], a.cam[5]),
+                                (float)a.width / (float)a.height, a.cam[6]));
+        auto env = std::make_shared<Environment>();
+        env->radiance = ei::Vec3(a.sky[0], a.sky[1], a.sky[2]);
+        system.SetEnvironmentMap(env);
+        if (a.renderer == "Pathtracer") system.SetRenderer<Pathtracer>();
+        else if (a.renderer == "LightPathtracer") system.SetRenderer<LightPathtracer>();
+        else if (a.renderer == "BidirectionalPathtracer") system.SetRenderer<BidirectionalPathtracer>();
+        else if (a.renderer == "NrcPathtracer") system.SetRenderer<NrcPathtracer>();
+        else usage("unknown renderer");
+
+        for (int i = 0; i < a.iterations; ++i) system.Draw();
+
+        const unsigned long iterations = system.GetIterationCount();
+        double mse = -1.0;
+        if (!a.reference.empty()) {
+            TextureMSE tmse;
+            tmse.LoadReferenceFromPFM(a.reference);
+            if (!tmse.HasValidReferenceImage()) usage("cannot read the reference image");
+            mse = tmse.ComputeCurrentMSE64(system.GetBackbuffer(), (unsigned)iterations);
+        }
+        if (!a.out.empty()) {
+            const std::vector<float> rgba = system.GetBackbuffer().ReadRGBA();
+            if (!WritePfm(rgba.data(), ei::IVec2(a.width, a.height), a.out, (std::uint32_t)iterations)) return 1;
+        }
+        std::printf(
+            "{\"renderer\": \"%s\", \"iterations\": %lu, \"render_ms\": %llu, \"width\": %d, \"height\": %d, "
+            "\"mse\": %.9g}\n",
+            system.GetActiveRenderer()->GetName().c_str(), iterations, (unsigned long long)system.GetRenderTime(),
+            a.width, a.height, mse);
+        scene.reset();
+        return 0;
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "gpugi_headless: %s\n", e.what());
+        return 1;
+    }
+}

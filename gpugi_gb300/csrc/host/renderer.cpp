@@ -1,0 +1,373 @@
+// Implementation of the C++ renderer interface (gpugi_renderer.hpp) over the
+// C ABI of the CUDA library.
+#include "gpugi_renderer.hpp"
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+
+namespace {
+
+void check_status(gpugi_ctx* ctx, gpugi_status st, const char* what) {
+    if (st != GPUGI_OK) {
+        const char* msg = ctx ? gpugi_last_error(ctx) : "";
+        throw GpugiError((int)st, std::string(what) + ": " + (msg ? msg : ""));
+    }
+}
+
+ei::Vec3 sub(const ei::Vec3& a, const ei::Vec3& b) { return ei::Vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
+ei::Vec3 scale(const ei::Vec3& a, float s) { return ei::Vec3(a.x * s, a.y * s, a.z * s); }
+ei::Vec3 cross(const ei::Vec3& a, const ei::Vec3& b) {
+    return ei::Vec3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+float len(const ei::Vec3& a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+ei::Vec3 normalize(const ei::Vec3& a) { return scale(a, 1.0f / len(a)); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- DeviceImage
+DeviceImage::DeviceImage(gpugi_ctx* ctx, int width, int height, bool fp64)
+    : m_ctx(ctx), m_width(width), m_height(height), m_fp64(fp64) {
+    if (width <= 0 || height <= 0) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "image size must be positive");
+    check_status(ctx, gpugi_image_create(ctx, (uint32_t)width, (uint32_t)height, fp64 ? 1u : 0u, &m_image),
+                 "gpugi_image_create");
+}
+
+DeviceImage::~DeviceImage() { gpugi_image_destroy(m_image); }
+
+void DeviceImage::ClearToZero() { check_status(m_ctx, gpugi_image_clear(m_ctx, m_image), "gpugi_image_clear"); }
+
+std::vector<float> DeviceImage::ReadRGBA() const {
+    std::vector<float> out((size_t)m_width * m_height * 4);
+    check_status(m_ctx, gpugi_image_read(m_ctx, m_image, out.data(), nullptr), "gpugi_image_read");
+    return out;
+}
+
+std::vector<double> DeviceImage::ReadRGB64() const {
+    if (!m_fp64) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "image has no FP64 accumulation");
+    std::vector<double> out((size_t)m_width * m_height * 3);
+    check_status(m_ctx, gpugi_image_read(m_ctx, m_image, nullptr, out.data()), "gpugi_image_read");
+    return out;
+}
+
+// --------------------------------------------------------------------- Camera
+Camera::Camera() : m_position(), m_lookat(), m_up(), m_yfov(0.0f), m_aspectRatio(1.0f) {}
+
+Camera::Camera(const ei::Vec3& position, const ei::Vec3& lookat, float aspectRatio, float verticalFOV,
+               const ei::Vec3& up)
+    : m_position(position), m_lookat(lookat), m_up(up), m_yfov(verticalFOV), m_aspectRatio(aspectRatio) {}
+
+// camera.cpp:76-85
+void Camera::ComputeCameraParams(ei::Vec3& cameraU, ei::Vec3& cameraV, ei::Vec3& cameraW) const {
+    cameraW = normalize(sub(m_lookat, m_position));
+    cameraU = normalize(cross(cameraW, m_up));
+    cameraV = normalize(cross(cameraU, cameraW));
+    const float f = std::tan(m_yfov / 2.0f * (3.14159265358979f / 180.0f));
+    cameraU = scale(cameraU, f * m_aspectRatio);
+    cameraV = scale(cameraV, f);
+}
+
+// ---------------------------------------------------------------------- Scene
+Scene::Scene(gpugi_ctx* ctx, const std::string& file) : m_ctx(ctx) {
+    gpugi_bvh* bvh = nullptr;
+    if (gpugi_bvh_read_file(file.c_str(), &bvh) != 0)
+        throw GpugiError(GPUGI_ERROR_INVALID_SCENE, std::string("cannot load ") + file + ": " + gpugi_bvh_last_error());
+    std::unique_ptr<gpugi_bvh, void (*)(gpugi_bvh*)> guard(bvh, gpugi_bvh_free);
+    uint32_t boundsKind = 0;
+    gpugi_bvh_info(bvh, &m_numNodes, &m_numLeafBlocks, &m_leafSize, &boundsKind, &m_maxDepth);
+    m_bvhType = boundsKind == GPUGI_FIT_ELLIPSOID ? ei::Types3D::ELLIPSOID : ei::Types3D::BOX;
+    std::vector<float> hierarchy((size_t)m_numNodes * 8);
+    std::vector<int32_t> slots((size_t)m_numLeafBlocks * m_leafSize * 4);
+    gpugi_bvh_export(bvh, hierarchy.data(), slots.data(), nullptr);
+    gpugi_bvh_vertices(bvh, &m_numVertices, nullptr);
+    std::vector<float> positions((size_t)m_numVertices * 3), normals((size_t)m_numVertices * 3),
+        texcoords((size_t)m_numVertices * 2);
+    gpugi_bvh_vertices(bvh, &m_numVertices, positions.data());
+    gpugi_bvh_vertex_attributes(bvh, normals.data(), texcoords.data());
+    // VertexInfo {atan2(n.y, n.x), n.z, u, v} (scene.cpp:79-84)
+    std::vector<float> vinfo((size_t)m_numVertices * 4);
+    for (size_t v = 0; v < m_numVertices; ++v) {
+        vinfo[4 * v] = std::atan2(normals[3 * v + 1], normals[3 * v]);
+        vinfo[4 * v + 1] = normals[3 * v + 2];
+        vinfo[4 * v + 2] = texcoords[2 * v];
+        vinfo[4 * v + 3] = texcoords[2 * v + 1];
+    }
+    gpugi_bvh_materials(bvh, &m_numMaterials, nullptr);
+    std::vector<float> materials((size_t)m_numMaterials * 24);
+    if (m_numMaterials) {
+        gpugi_bvh_materials(bvh, &m_numMaterials, materials.data());
+    } else {
+        // one grey Lambertian: diffuse 0.5, ior 1.5, opacity 1, reflectiveness 1 (exponent 1), fresnel (0, 1)
+        m_numMaterials = 1;
+        materials.assign(24, 0.0f);
+        materials[0] = materials[1] = materials[2] = 0.5f;
+        materials[3] = 1.5f;
+        materials[4] = materials[5] = materials[6] = 1.0f;
+        materials[8] = materials[9] = materials[10] = 1.0f;
+        materials[11] = 1.0f;
+        materials[20] = materials[21] = materials[22] = 1.0f;
+    }
+    // scene box = root node bounds (AABB: min/max; ellipsoid: center +- radii)
+    if (m_numNodes) {
+        const float* r = hierarchy.data();
+        if (m_bvhType == ei::Types3D::BOX) {
+            m_boxMin = ei::Vec3(r[0], r[1], r[2]);
+            m_boxMax = ei::Vec3(r[4], r[5], r[6]);
+        } else {
+            m_boxMin = ei::Vec3(r[0] - r[4], r[1] - r[5], r[2] - r[6]);
+            m_boxMax = ei::Vec3(r[0] + r[4], r[1] + r[5], r[2] + r[6]);
+        }
+    }
+    check_status(ctx,
+                 gpugi_scene_upload(ctx, hierarchy.data(), m_numNodes, boundsKind, slots.data(),
+                                    (uint32_t)(slots.size() / 4), m_leafSize, positions.data(), vinfo.data(),
+                                    m_numVertices, reinterpret_cast<const gpugi_material*>(materials.data()),
+                                    m_numMaterials, &m_scene),
+                 "gpugi_scene_upload");
+}
+
+Scene::~Scene() { gpugi_scene_destroy(m_scene); }
+
+const char* Scene::GetBvhTypeDefineString() const {
+    return m_bvhType == ei::Types3D::ELLIPSOID ? "#define BOUNDINGBOX_ELLIPSOID\n" : "#define BOUNDINGBOX_BOX\n";
+}
+
+void Scene::AddPointLight(const PointLight& light) {
+    const float p[3] = {light.position.x, light.position.y, light.position.z};
+    const float i[3] = {light.intensity.x, light.intensity.y, light.intensity.z};
+    check_status(m_ctx, gpugi_scene_add_point_light(m_scene, p, i), "gpugi_scene_add_point_light");
+    m_pointLights.push_back(light);
+}
+
+// ------------------------------------------------------------- RendererSystem
+RendererSystem::RendererSystem(int device) {
+    gpugi_opts opts{device, 0};
+    check_status(nullptr, gpugi_create(&m_ctx, &opts), "gpugi_create");
+}
+
+RendererSystem::~RendererSystem() {
+    m_activeRenderer.reset();
+    m_backbuffer.reset();
+    m_scene.reset();
+    gpugi_destroy(m_ctx);
+}
+
+void RendererSystem::Check(gpugi_status status) const { check_status(m_ctx, status, "gpugi"); }
+
+void RendererSystem::SetScene(std::shared_ptr<Scene> scene) {
+    m_scene = std::move(scene);
+    PerIterationBufferUpdate(false);
+    m_iterationCount = 0;
+    m_renderTime = 0;
+    if (m_backbuffer) m_backbuffer->ClearToZero();
+    if (m_activeRenderer) m_activeRenderer->SetScene(m_scene);
+}
+
+void RendererSystem::SetEnvironmentMap(std::shared_ptr<Environment> env) {
+    m_envMap = std::move(env);
+    if (m_activeRenderer) m_activeRenderer->SetEnvironmentMap(m_envMap);
+}
+
+void RendererSystem::UpdateCameraParams() {
+    ei::Vec3 U, V, W;
+    m_camera.ComputeCameraParams(U, V, W);
+    const ei::Vec3& p = m_camera.GetPosition();
+    const float v[12] = {U.x, U.y, U.z, V.x, V.y, V.z, W.x, W.y, W.z, p.x, p.y, p.z};
+    std::memcpy(m_cameraParams.U, v, sizeof m_cameraParams.U);
+    std::memcpy(m_cameraParams.V, v + 3, sizeof m_cameraParams.V);
+    std::memcpy(m_cameraParams.W, v + 6, sizeof m_cameraParams.W);
+    std::memcpy(m_cameraParams.position, v + 9, sizeof m_cameraParams.position);
+    // renderersystem.cpp:206: |U| |V| 4 / (width height)
+    if (m_backbuffer)
+        m_cameraParams.pixelArea =
+            len(U) * len(V) * 4.0f / (float)(m_backbuffer->GetWidth() * m_backbuffer->GetHeight());
+}
+
+void RendererSystem::SetCamera(const Camera& camera) {
+    m_iterationCount = 0;
+    m_renderTime = 0;
+    m_camera = camera;
+    UpdateCameraParams();
+    if (m_backbuffer) m_backbuffer->ClearToZero();
+    if (m_activeRenderer) m_activeRenderer->SetCamera(camera);
+}
+
+void RendererSystem::SetScreenSize(const ei::IVec2& newSize) {
+    m_backbuffer.reset();
+    m_backbuffer.reset(new DeviceImage(m_ctx, newSize.x, newSize.y));
+    m_backbuffer->ClearToZero();
+    m_iterationCount = 0;
+    m_renderTime = 0;
+    UpdateCameraParams();
+    if (m_activeRenderer) m_activeRenderer->SetScreenSize(*m_backbuffer);
+}
+
+void RendererSystem::Draw() {
+    if (!m_activeRenderer) return;
+    Check(gpugi_sync(m_ctx));
+    const auto begin = std::chrono::steady_clock::now();
+    m_activeRenderer->Draw();
+    PerIterationBufferUpdate();
+    Check(gpugi_sync(m_ctx));
+    const auto end = std::chrono::steady_clock::now();
+    m_renderTime += (uint64)std::chrono::duration_cast<std::chrono::milliseconds>(end - begin).count();
+}
+
+void RendererSystem::SetNumInitialLightSamples(unsigned int numInitialLightSamples) {
+    m_numInitialLightSamples = numInitialLightSamples;
+    m_lightSamples.assign((size_t)numInitialLightSamples * 8, 0.0f);
+    PerIterationBufferUpdate(false);
+}
+
+void RendererSystem::ResetIterationCount() { m_iterationCount = 0; }
+
+// renderersystem.cpp:95-116: advance the iteration, draw the next light samples.
+void RendererSystem::PerIterationBufferUpdate(bool iterationIncrement) {
+    if (iterationIncrement) ++m_iterationCount;
+    if (m_scene && m_numInitialLightSamples)
+        Check(gpugi_generate_light_samples(m_scene->GetHandle(), &m_lightSamplerState, m_numInitialLightSamples,
+                                           m_lightSamples.data()));
+}
+
+gpugi_render_params RendererSystem::MakeRenderParams(gpugi_pass pass) const {
+    gpugi_render_params p{};
+    p.pass = (uint32_t)pass;
+    p.width = (uint32_t)m_backbuffer->GetWidth();
+    p.height = (uint32_t)m_backbuffer->GetHeight();
+    p.maxPathLength = m_maxPathLength;
+    p.rrStartDepth = m_rrStartDepth;
+    p.iteration = (uint32_t)m_iterationCount;
+    p.samples = 1;
+    p.numLightSamples = m_numInitialLightSamples;
+    const ei::Vec3 sky = GetSkyRadiance();
+    p.sky[0] = sky.x;
+    p.sky[1] = sky.y;
+    p.sky[2] = sky.z;
+    p.flags = 0;
+    return p;
+}
+
+// ------------------------------------------------------------------ Renderers
+namespace {
+void draw_pass(RendererSystem& sys, gpugi_pass pass) {
+    if (!sys.GetScene()) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "no scene set");
+    const gpugi_render_params p = sys.MakeRenderParams(pass);
+    sys.Check(gpugi_render(sys.GetContext(), sys.GetScene()->GetHandle(), &sys.GetCameraParams(), &p,
+                           sys.GetInitialLightSamples(), nullptr, sys.GetBackbuffer().GetHandle()));
+}
+}  // namespace
+
+// pathtracer.cpp:20-29
+Pathtracer::Pathtracer(RendererSystem& rendererSystem) : Renderer(rendererSystem) {
+    m_rendererSystem.SetNumInitialLightSamples(128);
+}
+void Pathtracer::Draw() { draw_pass(m_rendererSystem, GPUGI_PASS_PT); }
+
+// lightpathtracer.cpp:12-17
+LightPathtracer::LightPathtracer(RendererSystem& rendererSystem) : Renderer(rendererSystem) {
+    m_rendererSystem.SetNumInitialLightSamples(256);
+}
+void LightPathtracer::Draw() { draw_pass(m_rendererSystem, GPUGI_PASS_LT); }
+
+// bidirectionalpathtracer.cpp:20-26
+BidirectionalPathtracer::BidirectionalPathtracer(RendererSystem& rendererSystem) : Renderer(rendererSystem) {
+    m_rendererSystem.SetNumInitialLightSamples(128);
+}
+void BidirectionalPathtracer::Draw() { draw_pass(m_rendererSystem, GPUGI_PASS_BPT); }
+
+NrcPathtracer::NrcPathtracer(RendererSystem& rendererSystem, const NrcSettings& settings)
+    : Renderer(rendererSystem), m_settings(settings) {
+    m_rendererSystem.SetNumInitialLightSamples(128);
+}
+
+NrcPathtracer::~NrcPathtracer() { gpugi_nrc_destroy(m_nrc); }
+
+void NrcPathtracer::SetScene(std::shared_ptr<Scene> scene) {
+    gpugi_nrc_destroy(m_nrc);
+    m_nrc = nullptr;
+    if (!scene) return;
+    ei::Vec3 lo, hi;
+    scene->GetBoundingBox(lo, hi);
+    const float bmin[3] = {lo.x, lo.y, lo.z}, bmax[3] = {hi.x, hi.y, hi.z};
+    m_rendererSystem.Check(gpugi_nrc_create(m_rendererSystem.GetContext(), bmin, bmax, m_settings.seed,
+                                            m_settings.learningRate, &m_nrc));
+}
+
+void NrcPathtracer::Draw() {
+    if (!m_rendererSystem.GetScene() || !m_nrc) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "no scene set");
+    const gpugi_render_params p = m_rendererSystem.MakeRenderParams(GPUGI_PASS_PT);
+    gpugi_nrc_params q{};
+    q.terminateDepth = m_settings.terminateDepth;
+    q.trainFraction = m_settings.trainFraction;
+    q.maxTrainSamples = m_settings.maxTrainSamples;
+    q.trainSteps = m_settings.trainSteps;
+    q.train = m_train ? 1u : 0u;
+    m_rendererSystem.Check(gpugi_render_nrc(m_rendererSystem.GetContext(), m_rendererSystem.GetScene()->GetHandle(),
+                                            &m_rendererSystem.GetCameraParams(), &p,
+                                            m_rendererSystem.GetInitialLightSamples(), nullptr, m_nrc, &q,
+                                            m_rendererSystem.GetBackbuffer().GetHandle()));
+}
+
+// -------------------------------------------------------------------- imageut
+// hdrimage.cpp:6-33: "PF", size, scale -1 (little endian), rows as stored.
+bool WritePfm(const float* rgba, const ei::IVec2& size, const std::string& filename, std::uint32_t divisor) {
+    std::ofstream file(filename.c_str(), std::ios::binary);
+    if (!file) {
+        std::fprintf(stderr, "Error writing hdr image to %s\n", filename.c_str());
+        return false;
+    }
+    file.write("PF\n", 3);
+    file << size.x << " " << size.y << "\n";
+    file.write("-1.000000\n", 10);
+    const float d = divisor ? (float)divisor : 1.0f;
+    for (int i = 0; i < size.x * size.y; ++i) {
+        const float out[3] = {rgba[4 * i] / d, rgba[4 * i + 1] / d, rgba[4 * i + 2] / d};
+        file.write(reinterpret_cast<const char*>(out), sizeof out);
+    }
+    return (bool)file;
+}
+
+std::unique_ptr<float[]> LoadPfm(const std::string& filename, ei::IVec2& size) {
+    std::ifstream file(filename.c_str(), std::ios::binary);
+    if (!file) {
+        std::fprintf(stderr, "Error reading hdr image from %s\n", filename.c_str());
+        return nullptr;
+    }
+    char header[3];
+    file.read(header, 3);
+    if (!file || std::memcmp(header, "PF\n", 3) != 0) return nullptr;
+    float scale = 0.0f;
+    file >> size.x >> size.y >> scale;
+    file.get();  // the single whitespace before the raster
+    if (!file || size.x <= 0 || size.y <= 0 || scale >= 0.0f) return nullptr;  // little-endian only
+    std::unique_ptr<float[]> out(new float[(size_t)size.x * size.y * 3]);
+    file.read(reinterpret_cast<char*>(out.get()), (std::streamsize)((size_t)size.x * size.y * 3 * sizeof(float)));
+    if (!file) return nullptr;
+    return out;
+}
+
+void TextureMSE::LoadReferenceFromPFM(const std::string& filename) {
+    auto data = LoadPfm(filename, m_size);
+    m_reference.clear();
+    if (data) m_reference.assign(data.get(), data.get() + (size_t)m_size.x * m_size.y * 3);
+}
+
+// texturemse.cpp:39-65: mean over pixels of the squared RGB error of the
+// normalised accumulation; reduced in FP64 (FP64 accumulation when the image has one).
+double TextureMSE::ComputeCurrentMSE64(const DeviceImage& texture, unsigned int divisor) {
+    if (m_reference.empty()) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "no reference image loaded");
+    if (m_size.x != texture.GetWidth() || m_size.y != texture.GetHeight())
+        throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "reference size differs from the image");
+    double mse = 0.0;
+    check_status(texture.GetContext(),
+                 gpugi_image_mse(texture.GetContext(), texture.GetHandle(), (double)(divisor ? divisor : 1),
+                                 m_reference.data(), texture.HasFP64() ? 1u : 0u, &mse),
+                 "gpugi_image_mse");
+    return mse;
+}
+
+float TextureMSE::ComputeCurrentMSE(const DeviceImage& texture, unsigned int divisor) {
+    return (float)ComputeCurrentMSE64(texture, divisor);
+}

@@ -42,6 +42,7 @@ constexpr int kMaxDepth = 64;
 struct PathSoA {
     float *ox, *oy, *oz, *dx, *dy, *dz, *tx, *ty, *tz, *lastP;
     uint32_t *seed, *pixel, *info;  // info: bit 0 = didNEE, bits 8..31 = sample (iteration) index
+    uint32_t* job;                  // batched render: index of the path's job
 };
 struct HitSoA {
     int32_t* slot;
@@ -50,7 +51,10 @@ struct HitSoA {
 struct ShadowSoA {
     float *ox, *oy, *oz, *dx, *dy, *dz, *tmax, *cr, *cg, *cb;
     uint32_t* pixel;
+    uint32_t* train;  // radiance-cache training vertex that also receives the contribution, or kNoTrain
+    uint32_t* job;    // batched render: index of the ray's job
 };
+constexpr uint32_t kNoTrain = 0xFFFFFFFFu;
 
 // Light-cache entry (bidirpathtracer/lightcache.glsl:1-16), 64 bytes.
 struct CacheEntry {
@@ -87,6 +91,19 @@ struct RenderConst {
     uint32_t cacheCap;           // entries per sample
     Counters* cnt;
     uint32_t* err;
+    // radiance cache (PT with NRC); unused by the other passes
+    int nrcTerminateDepth;       // render paths query the cache at this vertex
+    uint32_t nrcTrainThreshold;  // pixel hash below this: a training path
+    float* tvRec;                // training vertices: 16 floats {pos, dir, normal, albedo, T, pad}
+    float* tvC;                  // training vertices: 3 floats, radiance accumulated after the vertex
+    uint32_t* tvCount;           // vertices recorded per training path
+    uint32_t* trainPaths;        // counter of training paths
+    uint32_t trainCap;           // training paths the buffers hold
+    float* queries;              // 12 floats per cache query
+    float* qT;                   // 3 floats: throughput at the query
+    uint32_t* qPixel;
+    uint32_t* queryCount;
+    uint32_t queryCap;
 };
 
 // ------------------------------------------------------------ accumulation
@@ -107,7 +124,9 @@ GPUGI_D void store_path(const PathSoA& P, uint32_t i, float3 o, float3 d, float3
     P.tx[i] = tp.x; P.ty[i] = tp.y; P.tz[i] = tp.z;
     P.seed[i] = seed; P.pixel[i] = pixel; P.info[i] = info; P.lastP[i] = lastP;
 }
-GPUGI_D void store_shadow(const ShadowSoA& Q, uint32_t i, float3 o, float3 d, float tmax, float3 c, uint32_t pixel) {
+GPUGI_D void store_shadow(const ShadowSoA& Q, uint32_t i, float3 o, float3 d, float tmax, float3 c, uint32_t pixel,
+                          uint32_t train = kNoTrain) {
+    Q.train[i] = train;
     Q.ox[i] = o.x; Q.oy[i] = o.y; Q.oz[i] = o.z;
     Q.dx[i] = d.x; Q.dy[i] = d.y; Q.dz[i] = d.z;
     Q.tmax[i] = tmax; Q.cr[i] = c.x; Q.cg[i] = c.y; Q.cb[i] = c.z; Q.pixel[i] = pixel;
@@ -116,7 +135,9 @@ GPUGI_D void store_shadow(const ShadowSoA& Q, uint32_t i, float3 o, float3 d, fl
 // Persistent refill loop shared by the extend and shadow kernels.
 template <bool ANY_HIT, int BOUNDS, typename Load, typename Finish>
 GPUGI_D void persistent_walks(const DevScene& s, uint32_t n, unsigned long long* work, uint32_t* err, Load load,
-                              Finish finish) {
+                              Finish finish, uint32_t stage) {
+    extern __shared__ float4 s_top[];
+    stage_top_nodes(s, s_top, stage);
     const unsigned lane = threadIdx.x & 31u;
     WalkState w;
     uint32_t ray = 0;
@@ -143,7 +164,7 @@ GPUGI_D void persistent_walks(const DevScene& s, uint32_t n, unsigned long long*
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err)) {
+        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err, s_top, stage)) {
             finish(ray, w);
             active = false;
         }
@@ -151,7 +172,7 @@ GPUGI_D void persistent_walks(const DevScene& s, uint32_t n, unsigned long long*
 }
 
 template <int BOUNDS>
-__global__ void __launch_bounds__(128) k_extend(RenderConst rc, PathSoA A, HitSoA H, int depth) {
+__global__ void __launch_bounds__(128) k_extend(RenderConst rc, PathSoA A, HitSoA H, int depth, uint32_t stage) {
     const uint32_t n = rc.cnt->path[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&rc.cnt->rays[0], (unsigned long long)n);
     persistent_walks<false, BOUNDS>(
@@ -166,11 +187,12 @@ __global__ void __launch_bounds__(128) k_extend(RenderConst rc, PathSoA A, HitSo
             H.t[i] = w.len;
             H.u[i] = w.u;
             H.v[i] = w.v;
-        });
+        },
+        stage);
 }
 
 template <int BOUNDS>
-__global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int depth) {
+__global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int depth, uint32_t stage) {
     const uint32_t n = rc.cnt->shadow[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&rc.cnt->rays[1], (unsigned long long)n);
     persistent_walks<true, BOUNDS>(
@@ -181,8 +203,18 @@ __global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int
             tmax = Q.tmax[i];
         },
         [&](uint32_t i, const WalkState& w) {
-            if (w.slot < 0) splat(rc, Q.pixel[i], make_float3(Q.cr[i], Q.cg[i], Q.cb[i]));
-        });
+            if (w.slot < 0) {
+                const float3 c = make_float3(Q.cr[i], Q.cg[i], Q.cb[i]);
+                splat(rc, Q.pixel[i], c);
+                const uint32_t tr = Q.train[i];
+                if (tr != kNoTrain) {  // radiance-cache training vertex accumulator
+                    atomicAdd(rc.tvC + 3 * (size_t)tr, c.x);
+                    atomicAdd(rc.tvC + 3 * (size_t)tr + 1, c.y);
+                    atomicAdd(rc.tvC + 3 * (size_t)tr + 2, c.z);
+                }
+            }
+        },
+        stage);
 }
 
 // ------------------------------------------------------------ generation
@@ -327,50 +359,58 @@ GPUGI_D bool roulette(const RenderConst& rc, int depth, float3 throughput, float
          base_ < (n); base_ += gridDim.x * blockDim.x, k = base_ + (threadIdx.x & 31u))                         \
         for (bool valid = k < (n), once_ = true; once_; once_ = false)
 
-// pathtracer.comp:48-105, one bounce.
+// pathtracer.comp:48-105, one bounce of one path: the per-lane part of the
+// PT shade kernels (the queue appends are warp-wide and follow).
+struct PtLane {
+    bool survive = false, shadow = false;
+    float3 o, d, tp, sro, srd, contrib;
+    float srl = 0.0f;
+    uint32_t seed = 0, pixel = 0, info = 0;
+};
+
+GPUGI_D void pt_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
+                           PtLane& L) {
+    const float lightSampleWeight = (float)rc.numLightSamples;
+    L.o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+    L.d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+    L.tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+    L.seed = A.seed[k];
+    L.pixel = A.pixel[k];
+    L.info = A.info[k];
+    Hit h = load_hit(rc, H, k, L.o, L.d);
+    if (!h.valid) {
+        splat(rc, L.pixel, L.tp * rc.sky);
+        return;
+    }
+    L.o = h.pos;
+    if (!(L.info & 1u)) splat(rc, L.pixel, L.tp * h.m.Emissivity);
+    const bool didNEE = h.m.Reflectiveness.w < 500.0f;
+    L.info = (L.info & ~1u) | (didNEE ? 1u : 0u);
+    const uint32_t li = random_uint(L.seed) % rc.numLightSamples;
+    float3 rad;
+    if (direct_light(rc, L.info >> 8, L.o, h.N, li, L.d, h.m, didNEE, rad, L.sro, L.srd, L.srl)) {
+        L.contrib = rad * L.tp * lightSampleWeight;
+        L.shadow = L.contrib.x != 0.0f || L.contrib.y != 0.0f || L.contrib.z != 0.0f;
+    }
+    float3 thr = f3(1.0f);
+    float pdf;
+    L.d = sample_bsdf(L.d, h.m, L.seed, h.N, thr, false, pdf);
+    L.o = L.o + L.d * kRAY_HIT_EPSILON;
+    L.tp *= thr;
+    L.survive = roulette(rc, depth, thr, L.tp, L.seed) && depth + 1 < rc.maxPathLength;
+}
+
 __global__ void __launch_bounds__(128) k_pt_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q,
                                                   int depth) {
     const uint32_t n = rc.cnt->path[depth];
-    const float lightSampleWeight = (float)rc.numLightSamples;
     WARP_LOOP(n, k, valid) {
-        bool survive = false, shadow = false;
-        float3 o, d, tp, sro, srd, contrib;
-        float srl = 0.0f;
-        uint32_t seed = 0, pixel = 0, info = 0;
-        if (valid) {
-            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
-            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
-            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
-            pixel = A.pixel[k];
-            info = A.info[k];
-            Hit h = load_hit(rc, H, k, o, d);
-            if (!h.valid) {
-                splat(rc, pixel, tp * rc.sky);
-            } else {
-                o = h.pos;
-                if (!(info & 1u)) splat(rc, pixel, tp * h.m.Emissivity);
-                const bool didNEE = h.m.Reflectiveness.w < 500.0f;
-                info = (info & ~1u) | (didNEE ? 1u : 0u);
-                const uint32_t li = random_uint(seed) % rc.numLightSamples;
-                float3 rad;
-                if (direct_light(rc, info >> 8, o, h.N, li, d, h.m, didNEE, rad, sro, srd, srl)) {
-                    contrib = rad * tp * lightSampleWeight;
-                    shadow = contrib.x != 0.0f || contrib.y != 0.0f || contrib.z != 0.0f;
-                }
-                float3 thr = f3(1.0f);
-                float pdf;
-                d = sample_bsdf(d, h.m, seed, h.N, thr, false, pdf);
-                o = o + d * kRAY_HIT_EPSILON;
-                tp *= thr;
-                survive = roulette(rc, depth, thr, tp, seed) && depth + 1 < rc.maxPathLength;
-            }
-        }
+        PtLane L;
+        if (valid) pt_shade_lane(rc, A, H, k, depth, L);
         uint32_t qs, qb;
-        warp_append(&rc.cnt->shadow[depth], shadow, qs);
-        if (shadow) store_shadow(Q, qs, sro, srd, srl, contrib, pixel);
-        warp_append(&rc.cnt->path[depth + 1], survive, qb);
-        if (survive) store_path(B, qb, o, d, tp, seed, pixel, info, 1.0f);
+        warp_append(&rc.cnt->shadow[depth], L.shadow, qs);
+        if (L.shadow) store_shadow(Q, qs, L.sro, L.srd, L.srl, L.contrib, L.pixel);
+        warp_append(&rc.cnt->path[depth + 1], L.survive, qb);
+        if (L.survive) store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, 1.0f);
     }
 }
 
@@ -609,6 +649,168 @@ __global__ void __launch_bounds__(128) k_bpt_shade(RenderConst rc, PathSoA A, Pa
     }
 }
 
+// ------------------------------------------------------------ radiance cache
+// Camera paths for the path tracer with a radiance cache: as
+// k_camera_generate, plus the choice of training paths (a per-frame hash of
+// the pixel below nrcTrainThreshold) and their buffer slot (kept in lastP).
+__global__ void k_nrc_generate(RenderConst rc, PathSoA A) {
+    const uint32_t total = (uint32_t)rc.numPixels;
+    if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
+    const uint32_t frame = rc.iteration + rc.sampleBase;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < total; pix += gridDim.x * blockDim.x) {
+        const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
+        uint32_t seed = wanghash(wanghash(frame) + pix);
+        const float3 d = primary_direction(rc, seed, x, y);
+        uint32_t info = 0;
+        float slotBits = 0.0f;
+        if (wanghash(pix ^ wanghash(frame + 0x9E3779B9u)) < rc.nrcTrainThreshold) {
+            const uint32_t slot = atomicAdd(rc.trainPaths, 1u);
+            if (slot < rc.trainCap) {
+                info |= 2u;
+                slotBits = __uint_as_float(slot);
+                rc.tvCount[slot] = 0;
+            }
+        }
+        store_path(A, pix, rc.camPos, d, f3(1.0f), seed, pix, info, slotBits);
+    }
+}
+
+GPUGI_D void add3(float* p, float3 c) {
+    atomicAdd(p, c.x);
+    atomicAdd(p + 1, c.y);
+    atomicAdd(p + 2, c.z);
+}
+
+// One bounce of the path tracer with a radiance cache. Render paths stop at
+// vertex nrcTerminateDepth and query the cache for the radiance reflected
+// there towards the previous vertex; training paths continue as plain path
+// tracing and record every vertex {position, outgoing direction, normal,
+// albedo, throughput}; the radiance that later reaches each vertex (NEE via
+// the shadow queue, emission and sky found by the next segment) is
+// accumulated into the vertex's tvC entry.
+__global__ void __launch_bounds__(128) k_nrc_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q,
+                                                   int depth) {
+    const uint32_t n = rc.cnt->path[depth];
+    const float lightSampleWeight = (float)rc.numLightSamples;
+    const uint32_t stride = (uint32_t)rc.maxPathLength;
+    WARP_LOOP(n, k, valid) {
+        bool survive = false, shadow = false, query = false;
+        float3 o, d, tp, sro, srd, contrib, qN, qAlbedo;
+        float srl = 0.0f, lastP = 0.0f;
+        uint32_t seed = 0, pixel = 0, info = 0, train = kNoTrain;
+        if (valid) {
+            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+            seed = A.seed[k];
+            pixel = A.pixel[k];
+            info = A.info[k];
+            lastP = A.lastP[k];
+            const bool training = (info & 2u) != 0;
+            const uint32_t tslot = __float_as_uint(lastP);
+            const uint32_t prevVertex = (training && depth > 0) ? tslot * stride + depth - 1 : kNoTrain;
+            Hit h = load_hit(rc, H, k, o, d);
+            if (!h.valid) {
+                const float3 c = tp * rc.sky;
+                splat(rc, pixel, c);
+                if (prevVertex != kNoTrain) add3(rc.tvC + 3 * (size_t)prevVertex, c);
+            } else {
+                o = h.pos;
+                if (!(info & 1u)) {
+                    const float3 e = tp * h.m.Emissivity;
+                    splat(rc, pixel, e);
+                    if (prevVertex != kNoTrain) add3(rc.tvC + 3 * (size_t)prevVertex, e);
+                }
+                if (!training && depth == rc.nrcTerminateDepth) {
+                    query = true;
+                    qN = h.N;
+                    qAlbedo = h.m.Diffuse;
+                } else {
+                    const bool didNEE = h.m.Reflectiveness.w < 500.0f;
+                    info = (info & ~1u) | (didNEE ? 1u : 0u);
+                    if (training) {
+                        const uint32_t v = tslot * stride + (uint32_t)depth;
+                        float* r = rc.tvRec + 16 * (size_t)v;
+                        r[0] = o.x; r[1] = o.y; r[2] = o.z;
+                        r[3] = -d.x; r[4] = -d.y; r[5] = -d.z;
+                        r[6] = h.N.x; r[7] = h.N.y; r[8] = h.N.z;
+                        r[9] = h.m.Diffuse.x; r[10] = h.m.Diffuse.y; r[11] = h.m.Diffuse.z;
+                        r[12] = tp.x; r[13] = tp.y; r[14] = tp.z;
+                        rc.tvC[3 * (size_t)v] = rc.tvC[3 * (size_t)v + 1] = rc.tvC[3 * (size_t)v + 2] = 0.0f;
+                        rc.tvCount[tslot] = (uint32_t)depth + 1;
+                        train = v;
+                    }
+                    const uint32_t li = random_uint(seed) % rc.numLightSamples;
+                    float3 rad;
+                    if (direct_light(rc, info >> 8, o, h.N, li, d, h.m, didNEE, rad, sro, srd, srl)) {
+                        contrib = rad * tp * lightSampleWeight;
+                        shadow = contrib.x != 0.0f || contrib.y != 0.0f || contrib.z != 0.0f;
+                    }
+                    float3 thr = f3(1.0f);
+                    float pdf;
+                    d = sample_bsdf(d, h.m, seed, h.N, thr, false, pdf);
+                    o = o + d * kRAY_HIT_EPSILON;
+                    tp *= thr;
+                    survive = roulette(rc, depth, thr, tp, seed) && depth + 1 < rc.maxPathLength;
+                }
+            }
+        }
+        uint32_t qs, qb, qq;
+        warp_append(&rc.cnt->shadow[depth], shadow, qs);
+        if (shadow) store_shadow(Q, qs, sro, srd, srl, contrib, pixel, train);
+        warp_append(rc.queryCount, query, qq);
+        if (query && qq < rc.queryCap) {
+            float* r = rc.queries + 12 * (size_t)qq;
+            r[0] = o.x; r[1] = o.y; r[2] = o.z;
+            r[3] = -d.x; r[4] = -d.y; r[5] = -d.z;
+            r[6] = qN.x; r[7] = qN.y; r[8] = qN.z;
+            r[9] = qAlbedo.x; r[10] = qAlbedo.y; r[11] = qAlbedo.z;
+            rc.qT[3 * (size_t)qq] = tp.x;
+            rc.qT[3 * (size_t)qq + 1] = tp.y;
+            rc.qT[3 * (size_t)qq + 2] = tp.z;
+            rc.qPixel[qq] = pixel;
+        }
+        warp_append(&rc.cnt->path[depth + 1], survive, qb);
+        if (survive) store_path(B, qb, o, d, tp, seed, pixel, info, lastP);
+    }
+}
+
+// Splat throughput x cache radiance for every query.
+__global__ void k_nrc_apply(RenderConst rc, const float* __restrict__ radiance) {
+    const uint32_t n = min(*rc.queryCount, rc.queryCap);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const float3 t = make_float3(rc.qT[3 * q], rc.qT[3 * q + 1], rc.qT[3 * q + 2]);
+        splat(rc, rc.qPixel[q], t * make_float3(radiance[3 * q], radiance[3 * q + 1], radiance[3 * q + 2]));
+    }
+}
+
+// Training targets: the radiance reflected at vertex k towards vertex k-1 is
+// the sum of everything accumulated at vertices >= k divided by the
+// throughput at arrival T_k. Samples: 15 floats {query, target}.
+__global__ void k_nrc_targets(RenderConst rc, float* __restrict__ samples, uint32_t* sampleCount, uint32_t cap) {
+    const uint32_t paths = min(*rc.trainPaths, rc.trainCap);
+    const uint32_t stride = (uint32_t)rc.maxPathLength;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < paths; p += gridDim.x * blockDim.x) {
+        const uint32_t nv = min(rc.tvCount[p], stride);
+        float3 S = f3(0.0f);
+        for (int k = (int)nv - 1; k >= 0; --k) {
+            const size_t v = (size_t)p * stride + k;
+            S += make_float3(rc.tvC[3 * v], rc.tvC[3 * v + 1], rc.tvC[3 * v + 2]);
+            const float* r = rc.tvRec + 16 * v;
+            const float3 T = make_float3(r[12], r[13], r[14]);
+            const float3 y = make_float3(T.x > 1e-20f ? S.x / T.x : 0.0f, T.y > 1e-20f ? S.y / T.y : 0.0f,
+                                         T.z > 1e-20f ? S.z / T.z : 0.0f);
+            const uint32_t i = atomicAdd(sampleCount, 1u);
+            if (i >= cap) continue;
+            float* o = samples + 15 * (size_t)i;
+            for (int c = 0; c < 12; ++c) o[c] = r[c];
+            o[12] = y.x;
+            o[13] = y.y;
+            o[14] = y.z;
+        }
+    }
+}
+
 // Sum over pixels of |rgb * scale - ref|^2 in FP64 (sqerror.frag:12-17 + the
 // mip-chain mean of TextureMSE::ComputeCurrentMSE).
 __global__ void k_mse(const float4* __restrict__ rgba, const double* __restrict__ rgb64,
@@ -640,6 +842,145 @@ __global__ void k_mse(const float4* __restrict__ rgba, const double* __restrict_
     }
 }
 
+// ------------------------------------------------------------ batched jobs
+// Many path-tracing jobs (each its own scene, camera, image, resolution,
+// sample count and path length) share one wavefront: their paths sit in the
+// same queues, every stage is one launch over all of them, and each path
+// and shadow ray carries its job index. The job constants come from a
+// device table, so the launch sequence does not change between rounds and is
+// replayed as one CUDA graph.
+
+// Largest j < numJobs with offsets[j] <= p (offsets[numJobs] > p).
+GPUGI_D uint32_t find_job(const uint32_t* __restrict__ offsets, uint32_t numJobs, uint32_t p) {
+    uint32_t lo = 0, hi = numJobs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(offsets + mid) <= p) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_batch_generate(const RenderConst* __restrict__ jobs, const uint32_t* __restrict__ offsets,
+                                 uint32_t numJobs, Counters* cnt, PathSoA A) {
+    const uint32_t total = offsets[numJobs];
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt->path[0] = total;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+        const uint32_t j = find_job(offsets, numJobs, p);
+        const RenderConst& rc = jobs[j];
+        const uint32_t local = p - offsets[j];
+        const uint32_t s = local / (uint32_t)rc.numPixels, pix = local % (uint32_t)rc.numPixels;
+        const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
+        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + pix);
+        const float3 d = primary_direction(rc, seed, x, y);
+        store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, s << 8, 1.0f);
+        A.job[p] = j;
+    }
+}
+
+// persistent_walks over rays of different scenes: load() returns the ray's
+// scene, whose bounds kind selects the node test per step.
+template <bool ANY_HIT, typename Load, typename Finish>
+GPUGI_D void persistent_walks_multi(uint32_t n, unsigned long long* work, uint32_t* err, Load load, Finish finish) {
+    const unsigned lane = threadIdx.x & 31u;
+    WalkState w;
+    const DevScene* sc = nullptr;
+    uint32_t ray = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        const bool need = !active && !exhausted;
+        const unsigned needMask = __ballot_sync(0xffffffffu, need);
+        if (needMask) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(work, (unsigned long long)__popc(needMask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (need) {
+                const unsigned long long my = base + (unsigned long long)__popc(needMask & ((1u << lane) - 1u));
+                if (my < n) {
+                    ray = (uint32_t)my;
+                    float3 o, d;
+                    float tmax;
+                    sc = load(ray, o, d, tmax);
+                    walk_begin(w, *sc, o, d, tmax);
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) {
+            const bool done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? walk_step<ANY_HIT, 1>(w, *sc, err)
+                                                                      : walk_step<ANY_HIT, 0>(w, *sc, err);
+            if (done) {
+                finish(ray, w);
+                active = false;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_batch_extend(const RenderConst* __restrict__ jobs, Counters* cnt,
+                                                      uint32_t* err, PathSoA A, HitSoA H, int depth) {
+    const uint32_t n = cnt->path[depth];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays[0], (unsigned long long)n);
+    persistent_walks_multi<false>(
+        n, &cnt->extendWork[depth], err,
+        [&](uint32_t i, float3& o, float3& d, float& tmax) -> const DevScene* {
+            o = make_float3(A.ox[i], A.oy[i], A.oz[i]);
+            d = make_float3(A.dx[i], A.dy[i], A.dz[i]);
+            tmax = kRAY_MAX;
+            return &jobs[A.job[i]].s;
+        },
+        [&](uint32_t i, const WalkState& w) {
+            H.slot[i] = w.slot;
+            H.t[i] = w.len;
+            H.u[i] = w.u;
+            H.v[i] = w.v;
+        });
+}
+
+__global__ void __launch_bounds__(128) k_batch_shadow(const RenderConst* __restrict__ jobs, Counters* cnt,
+                                                      uint32_t* err, ShadowSoA Q, int depth) {
+    const uint32_t n = cnt->shadow[depth];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays[1], (unsigned long long)n);
+    persistent_walks_multi<true>(
+        n, &cnt->shadowWork[depth], err,
+        [&](uint32_t i, float3& o, float3& d, float& tmax) -> const DevScene* {
+            o = make_float3(Q.ox[i], Q.oy[i], Q.oz[i]);
+            d = make_float3(Q.dx[i], Q.dy[i], Q.dz[i]);
+            tmax = Q.tmax[i];
+            return &jobs[Q.job[i]].s;
+        },
+        [&](uint32_t i, const WalkState& w) {
+            if (w.slot < 0) splat(jobs[Q.job[i]], Q.pixel[i], make_float3(Q.cr[i], Q.cg[i], Q.cb[i]));
+        });
+}
+
+__global__ void __launch_bounds__(128) k_batch_pt_shade(const RenderConst* __restrict__ jobs, Counters* cnt,
+                                                        PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q, int depth) {
+    const uint32_t n = cnt->path[depth];
+    WARP_LOOP(n, k, valid) {
+        PtLane L;
+        uint32_t j = 0;
+        if (valid) {
+            j = A.job[k];
+            pt_shade_lane(jobs[j], A, H, k, depth, L);
+        }
+        uint32_t qs, qb;
+        warp_append(&cnt->shadow[depth], L.shadow, qs);
+        if (L.shadow) {
+            store_shadow(Q, qs, L.sro, L.srd, L.srl, L.contrib, L.pixel);
+            Q.job[qs] = j;
+        }
+        warp_append(&cnt->path[depth + 1], L.survive, qb);
+        if (L.survive) {
+            store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, 1.0f);
+            B.job[qb] = j;
+        }
+    }
+}
+
 // ------------------------------------------------------------ buffers
 struct RenderBuffers {
     size_t pathCap = 0, cacheBytes = 0, lightBytes = 0;
@@ -654,12 +995,30 @@ struct RenderBuffers {
     float* hostLights = nullptr;  // pinned staging for light samples
     size_t hostLightBytes = 0;
     uint32_t maxSamples = 0;
+    // radiance-cache pass
+    void* nrcBlock = nullptr;
+    size_t nrcQueryCap = 0, nrcTrainCap = 0, nrcStride = 0, nrcSampleCap = 0;
+    float *queries = nullptr, *qT = nullptr, *radiance = nullptr, *tvRec = nullptr, *tvC = nullptr,
+          *samples = nullptr;
+    uint32_t *qPixel = nullptr, *tvCount = nullptr, *nrcCounters = nullptr;  // counters: queries, paths, samples
+    // batched rendering: job table + path offsets (device, pinned staging) and the replayed graph
+    RenderConst *dJobs = nullptr, *hJobs = nullptr;
+    uint32_t *dOffsets = nullptr, *hOffsets = nullptr;
+    uint32_t jobCap = 0;
+    cudaGraphExec_t batchExec = nullptr;
+    std::vector<uintptr_t> batchKey;  // what the captured launches depend on
 };
 
 static void free_render(gpugi_ctx* ctx) {
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
     if (!rb) return;
+    if (rb->batchExec) cudaGraphExecDestroy(rb->batchExec);
+    if (rb->dJobs) cudaFree(rb->dJobs);
+    if (rb->dOffsets) cudaFree(rb->dOffsets);
+    if (rb->hJobs) cudaFreeHost(rb->hJobs);
+    if (rb->hOffsets) cudaFreeHost(rb->hOffsets);
     if (rb->block) cudaFree(rb->block);
+    if (rb->nrcBlock) cudaFree(rb->nrcBlock);
     if (rb->hostLights) cudaFreeHost(rb->hostLights);
     delete rb;
     ctx->render = nullptr;
@@ -685,7 +1044,7 @@ static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheByt
     samples = std::max(samples, rb->maxSamples);
     auto a = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t col = a(paths * 4);
-    const size_t total = 2 * 13 * col + 4 * col + 11 * col + a(sizeof(Counters)) + a(cacheBytes) +
+    const size_t total = 2 * 14 * col + 4 * col + 13 * col + a(sizeof(Counters)) + a(cacheBytes) +
                          a(4 * (size_t)samples) + a(lightBytes);
     if (cudaMalloc(&rb->block, total) != cudaSuccess) {
         rb->block = nullptr;
@@ -704,6 +1063,7 @@ static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheByt
         P->seed = reinterpret_cast<uint32_t*>(take(col));
         P->pixel = reinterpret_cast<uint32_t*>(take(col));
         P->info = reinterpret_cast<uint32_t*>(take(col));
+        P->job = reinterpret_cast<uint32_t*>(take(col));
     }
     rb->H.slot = reinterpret_cast<int32_t*>(take(col));
     rb->H.t = reinterpret_cast<float*>(take(col));
@@ -713,6 +1073,8 @@ static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheByt
                     &rb->Q.cg, &rb->Q.cb};
     for (float** q : qf) *q = reinterpret_cast<float*>(take(col));
     rb->Q.pixel = reinterpret_cast<uint32_t*>(take(col));
+    rb->Q.train = reinterpret_cast<uint32_t*>(take(col));
+    rb->Q.job = reinterpret_cast<uint32_t*>(take(col));
     rb->cnt = reinterpret_cast<Counters*>(take(sizeof(Counters)));
     rb->cache = reinterpret_cast<CacheEntry*>(take(cacheBytes));
     rb->cacheCount = reinterpret_cast<uint32_t*>(take(4 * (size_t)samples));
@@ -724,19 +1086,16 @@ static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheByt
     return GPUGI_OK;
 }
 
-static int persistent_grid(gpugi_ctx* ctx, const void* kernel) {
-    int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, 0);
-    return ctx->numSMs * (perSM > 0 ? perSM : 1);
-}
-
 // One chunk of `samples` iterations of a pass.
 static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderConst rc, uint32_t pass) {
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
     auto extend = ell ? (const void*)k_extend<1> : (const void*)k_extend<0>;
     auto shadowK = ell ? (const void*)k_shadow<1> : (const void*)k_shadow<0>;
-    const int gridE = persistent_grid(ctx, extend), gridS = persistent_grid(ctx, shadowK);
+    WalkerLaunch LE, LS;
+    gpugi_status cst = walker_launch_config(ctx, sc, extend, 1ull << 40, ctx->renderSharedNodes, LE);
+    if (!cst) cst = walker_launch_config(ctx, sc, shadowK, 1ull << 40, ctx->renderSharedNodes, LS);
+    if (cst) return cst;
     int gridShade = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gridShade, (const void*)k_pt_shade, 128, 0);
     gridShade = ctx->numSMs * std::max(gridShade, 1);
@@ -745,13 +1104,13 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
 
     auto bounces = [&](int kind /*0 PT, 1 light, 2 light+cache, 3 BPT eye*/) -> gpugi_status {
         for (int depth = 0; depth < rc.maxPathLength; ++depth) {
-            if (ell) k_extend<1><<<gridE, 128, 0, ctx->stream>>>(rc, A, rb->H, depth);
-            else k_extend<0><<<gridE, 128, 0, ctx->stream>>>(rc, A, rb->H, depth);
+            if (ell) k_extend<1><<<LE.grid, 128, LE.smem, ctx->stream>>>(rc, A, rb->H, depth, LE.stage);
+            else k_extend<0><<<LE.grid, 128, LE.smem, ctx->stream>>>(rc, A, rb->H, depth, LE.stage);
             if (kind == 0) k_pt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
             else if (kind == 3) k_bpt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
             else k_light_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth, kind == 2);
-            if (ell) k_shadow<1><<<gridS, 128, 0, ctx->stream>>>(rc, rb->Q, depth);
-            else k_shadow<0><<<gridS, 128, 0, ctx->stream>>>(rc, rb->Q, depth);
+            if (ell) k_shadow<1><<<LS.grid, 128, LS.smem, ctx->stream>>>(rc, rb->Q, depth, LS.stage);
+            else k_shadow<0><<<LS.grid, 128, LS.smem, ctx->stream>>>(rc, rb->Q, depth, LS.stage);
             std::swap(A, B);
         }
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
@@ -778,6 +1137,105 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
         if ((st = bounces(3))) return st;
     }
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
+
+static RenderConst make_render_const(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_camera* cam,
+                                     const gpugi_render_params* p, gpugi_image* im, RenderBuffers* rb) {
+    RenderConst rc{};
+    rc.s = sc->dev;
+    rc.camU = f3(cam->U[0], cam->U[1], cam->U[2]);
+    rc.camV = f3(cam->V[0], cam->V[1], cam->V[2]);
+    rc.camW = f3(cam->W[0], cam->W[1], cam->W[2]);
+    rc.camPos = f3(cam->position[0], cam->position[1], cam->position[2]);
+    rc.pixelArea = cam->pixelArea;
+    rc.width = (int)p->width;
+    rc.height = (int)p->height;
+    rc.numPixels = (int)(p->width * p->height);
+    rc.maxPathLength = (int)p->maxPathLength;
+    rc.rrStartDepth = (int)p->rrStartDepth;
+    rc.iteration = p->iteration;
+    rc.numLightSamples = p->numLightSamples;
+    rc.sky = f3(p->sky[0], p->sky[1], p->sky[2]);
+    rc.image = im->rgba;
+    rc.image64 = im->rgb64;
+    rc.cache = rb->cache;
+    rc.cacheCount = rb->cacheCount;
+    rc.cnt = rb->cnt;
+    rc.err = ctx->errWord;
+    rc.lightSamples = rb->lights;
+    return rc;
+}
+
+// Light samples of `ns` iterations into the pinned staging buffer and on to
+// the device (host sampler or caller's arrays).
+static gpugi_status upload_light_sets(gpugi_ctx* ctx, const gpugi_scene* sc, RenderBuffers* rb, const float* lightSamples,
+                                      uint64_t* rngState, uint32_t first, uint32_t ns, uint32_t numLightSamples) {
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // the staging buffer may still feed a copy
+    const size_t setFloats = (size_t)numLightSamples * 8;
+    if (lightSamples) {
+        std::memcpy(rb->hostLights, lightSamples + (size_t)first * setFloats, ns * setFloats * sizeof(float));
+    } else {
+        for (uint32_t s = 0; s < ns; ++s)
+            generate_light_samples(const_cast<gpugi_scene*>(sc), *rngState, numLightSamples,
+                                   rb->hostLights + s * setFloats);
+    }
+    GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->lights, rb->hostLights, ns * setFloats * sizeof(float),
+                                        cudaMemcpyHostToDevice, ctx->stream));
+    return GPUGI_OK;
+}
+
+static gpugi_status ensure_nrc_buffers(gpugi_ctx* ctx, RenderBuffers* rb, size_t queries, size_t trainPaths,
+                                       size_t stride, size_t samples) {
+    if (queries <= rb->nrcQueryCap && trainPaths <= rb->nrcTrainCap && stride <= rb->nrcStride &&
+        samples <= rb->nrcSampleCap)
+        return GPUGI_OK;
+    cudaStreamSynchronize(ctx->stream);
+    if (rb->nrcBlock) cudaFree(rb->nrcBlock);
+    rb->nrcBlock = nullptr;
+    queries = std::max(queries, rb->nrcQueryCap);
+    trainPaths = std::max(trainPaths, rb->nrcTrainCap);
+    stride = std::max(stride, rb->nrcStride);
+    samples = std::max(samples, rb->nrcSampleCap);
+    auto a = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t verts = trainPaths * stride;
+    const size_t total = a(queries * 48) + a(queries * 12) + a(queries * 4) + a(queries * 12) + a(verts * 64) +
+                         a(verts * 12) + a(trainPaths * 4) + a(samples * 60) + a(64);
+    if (cudaMalloc(&rb->nrcBlock, total) != cudaSuccess) {
+        rb->nrcBlock = nullptr;
+        rb->nrcQueryCap = rb->nrcTrainCap = rb->nrcStride = rb->nrcSampleCap = 0;
+        return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "radiance-cache buffers");
+    }
+    char* p = static_cast<char*>(rb->nrcBlock);
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += a(bytes);
+        return r;
+    };
+    rb->queries = reinterpret_cast<float*>(take(queries * 48));
+    rb->qT = reinterpret_cast<float*>(take(queries * 12));
+    rb->qPixel = reinterpret_cast<uint32_t*>(take(queries * 4));
+    rb->radiance = reinterpret_cast<float*>(take(queries * 12));
+    rb->tvRec = reinterpret_cast<float*>(take(verts * 64));
+    rb->tvC = reinterpret_cast<float*>(take(verts * 12));
+    rb->tvCount = reinterpret_cast<uint32_t*>(take(trainPaths * 4));
+    rb->samples = reinterpret_cast<float*>(take(samples * 60));
+    rb->nrcCounters = reinterpret_cast<uint32_t*>(take(64));
+    rb->nrcQueryCap = queries;
+    rb->nrcTrainCap = trainPaths;
+    rb->nrcStride = stride;
+    rb->nrcSampleCap = samples;
+    return GPUGI_OK;
+}
+
+static gpugi_status ensure_host_lights(gpugi_ctx* ctx, RenderBuffers* rb, size_t lightBytes) {
+    if (rb->hostLightBytes >= lightBytes) return GPUGI_OK;
+    if (rb->hostLights) cudaFreeHost(rb->hostLights);
+    rb->hostLights = nullptr;
+    rb->hostLightBytes = 0;
+    GPUGI_CUDA_TRY(ctx, cudaMallocHost(&rb->hostLights, lightBytes));
+    rb->hostLightBytes = lightBytes;
     return GPUGI_OK;
 }
 
@@ -907,57 +1365,278 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
                                      (uint32_t)chunk);
     if (st) return st;
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
-    if (rb->hostLightBytes < lightBytes) {
-        if (rb->hostLights) cudaFreeHost(rb->hostLights);
-        rb->hostLights = nullptr;
-        rb->hostLightBytes = 0;
-        GPUGI_CUDA_TRY(ctx, cudaMallocHost(&rb->hostLights, lightBytes));
-        rb->hostLightBytes = lightBytes;
-    }
+    if ((st = ensure_host_lights(ctx, rb, lightBytes))) return st;
 
-    RenderConst rc;
-    rc.s = sc->dev;
-    rc.camU = f3(cam->U[0], cam->U[1], cam->U[2]);
-    rc.camV = f3(cam->V[0], cam->V[1], cam->V[2]);
-    rc.camW = f3(cam->W[0], cam->W[1], cam->W[2]);
-    rc.camPos = f3(cam->position[0], cam->position[1], cam->position[2]);
-    rc.pixelArea = cam->pixelArea;
-    rc.width = (int)p->width;
-    rc.height = (int)p->height;
-    rc.numPixels = (int)numPixels;
-    rc.maxPathLength = (int)p->maxPathLength;
-    rc.rrStartDepth = (int)p->rrStartDepth;
-    rc.iteration = p->iteration;
-    rc.numLightSamples = p->numLightSamples;
-    rc.sky = f3(p->sky[0], p->sky[1], p->sky[2]);
+    RenderConst rc = make_render_const(ctx, sc, cam, p, im, rb);
     rc.numRaysPerLightSample = (int)raysPerLight;
     rc.lightThreads = lightThreads;
-    rc.image = im->rgba;
-    rc.image64 = im->rgb64;
-    rc.cache = rb->cache;
-    rc.cacheCount = rb->cacheCount;
     rc.cacheCap = (uint32_t)cachePerSample;
-    rc.cnt = rb->cnt;
-    rc.err = ctx->errWord;
-    rc.lightSamples = rb->lights;
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
     for (uint32_t s0 = 0; s0 < p->samples; s0 += (uint32_t)chunk) {
         const uint32_t ns = std::min<uint32_t>((uint32_t)chunk, p->samples - s0);
-        // the pinned staging buffer may still feed the previous chunk's copy
-        GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        const size_t setFloats = (size_t)p->numLightSamples * 8;
-        if (lightSamples) {
-            std::memcpy(rb->hostLights, lightSamples + (size_t)s0 * setFloats, ns * setFloats * sizeof(float));
-        } else {
-            for (uint32_t s = 0; s < ns; ++s)
-                generate_light_samples(const_cast<gpugi_scene*>(sc), *rngState, p->numLightSamples,
-                                       rb->hostLights + s * setFloats);
-        }
-        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->lights, rb->hostLights, ns * setFloats * sizeof(float),
-                                            cudaMemcpyHostToDevice, ctx->stream));
+        if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, s0, ns, p->numLightSamples))) return st;
         rc.samples = ns;
         rc.sampleBase = s0;
         if ((st = render_chunk(ctx, sc, rc, p->pass))) return st;
+    }
+    return GPUGI_OK;
+}
+
+
+gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_camera* cam,
+                              const gpugi_render_params* p, const float* lightSamples, uint64_t* rngState,
+                              gpugi_nrc* nn, const gpugi_nrc_params* np, gpugi_image* im) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!sc || !cam || !p || !im || !nn || !np) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
+    if (p->pass != GPUGI_PASS_PT) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "the radiance cache serves the PT pass");
+    if (p->width != im->width || p->height != im->height)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
+    if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth || p->numLightSamples == 0 ||
+        p->samples == 0)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "bad render parameters");
+    if (!sc->dev.vinfo || !sc->dev.materials)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "scene lacks vertex info or materials");
+    if (!lightSamples && !rngState)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "either lightSamples or rngState is required");
+    if (!(np->trainFraction >= 0.0f && np->trainFraction <= 1.0f))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "trainFraction must be in [0, 1]");
+    const uint32_t numPixels = p->width * p->height;
+    const size_t lightBytes = (size_t)p->numLightSamples * 32;
+    gpugi_status st = ensure_buffers(ctx, numPixels, 0, lightBytes, 1);
+    if (st) return st;
+    RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
+    if ((st = ensure_host_lights(ctx, rb, lightBytes))) return st;
+    const size_t trainCap = (size_t)(np->trainFraction * numPixels * 1.25) + 64;
+    const size_t sampleCap = np->maxTrainSamples ? np->maxTrainSamples : 65536;
+    if ((st = ensure_nrc_buffers(ctx, rb, numPixels, trainCap, p->maxPathLength, sampleCap))) return st;
+
+    RenderConst rc = make_render_const(ctx, sc, cam, p, im, rb);
+    rc.samples = 1;
+    rc.nrcTerminateDepth = (int)np->terminateDepth;
+    rc.nrcTrainThreshold = (uint32_t)std::min(4294967295.0, (double)np->trainFraction * 4294967296.0);
+    rc.tvRec = rb->tvRec;
+    rc.tvC = rb->tvC;
+    rc.tvCount = rb->tvCount;
+    rc.trainPaths = rb->nrcCounters + 1;
+    rc.trainCap = (uint32_t)trainCap;
+    rc.queries = rb->queries;
+    rc.qT = rb->qT;
+    rc.qPixel = rb->qPixel;
+    rc.queryCount = rb->nrcCounters;
+    rc.queryCap = numPixels;
+    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    WalkerLaunch LE, LS;
+    if ((st = walker_launch_config(ctx, sc, ell ? (const void*)k_extend<1> : (const void*)k_extend<0>, 1ull << 40,
+                                   ctx->renderSharedNodes, LE)) ||
+        (st = walker_launch_config(ctx, sc, ell ? (const void*)k_shadow<1> : (const void*)k_shadow<0>, 1ull << 40,
+                                   ctx->renderSharedNodes, LS)))
+        return st;
+    int perSM = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, (const void*)k_nrc_shade, 128, 0);
+    const int gridShade = ctx->numSMs * std::max(perSM, 1);
+    const int genBlocks = ctx->numSMs * 8;
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
+    for (uint32_t frame = 0; frame < p->samples; ++frame) {
+        if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, frame, 1, p->numLightSamples))) return st;
+        rc.sampleBase = frame;
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), ctx->stream));
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->nrcCounters, 0, 64, ctx->stream));
+        PathSoA A = rb->A, B = rb->B;
+        k_nrc_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
+        for (int depth = 0; depth < rc.maxPathLength; ++depth) {
+            if (ell) k_extend<1><<<LE.grid, 128, LE.smem, ctx->stream>>>(rc, A, rb->H, depth, LE.stage);
+            else k_extend<0><<<LE.grid, 128, LE.smem, ctx->stream>>>(rc, A, rb->H, depth, LE.stage);
+            k_nrc_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
+            if (ell) k_shadow<1><<<LS.grid, 128, LS.smem, ctx->stream>>>(rc, rb->Q, depth, LS.stage);
+            else k_shadow<0><<<LS.grid, 128, LS.smem, ctx->stream>>>(rc, rb->Q, depth, LS.stage);
+            std::swap(A, B);
+        }
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+        // cache lookups of this frame (the network as trained by earlier frames)
+        uint32_t counts[2] = {0, 0};
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(counts, rb->nrcCounters, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        const uint32_t nq = std::min<uint32_t>(counts[0], numPixels);
+        if (nq) {
+            if ((st = gpugi_nrc_infer_device(ctx, nn, rb->queries, nq, rb->radiance))) return st;
+            k_nrc_apply<<<ctx->numSMs * 4, 256, 0, ctx->stream>>>(rc, rb->radiance);
+        }
+        // training on this frame's training paths
+        if (np->train && counts[1] > 0) {
+            k_nrc_targets<<<ctx->numSMs * 2, 128, 0, ctx->stream>>>(rc, rb->samples, rb->nrcCounters + 2,
+                                                                     (uint32_t)sampleCap);
+            uint32_t ns = 0;
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(&ns, rb->nrcCounters + 2, 4, cudaMemcpyDeviceToHost, ctx->stream));
+            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+            ns = std::min<uint32_t>(ns, (uint32_t)sampleCap);
+            for (uint32_t k = 0; k < std::max<uint32_t>(1u, np->trainSteps) && ns; ++k)
+                if ((st = gpugi_nrc_train_device(ctx, nn, rb->samples, ns, nullptr))) return st;
+        }
+    }
+    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
+
+// Validation shared by gpugi_render and the jobs of gpugi_render_batch.
+static gpugi_status check_render_args(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_camera* cam,
+                                      const gpugi_render_params* p, const float* lightSamples,
+                                      const uint64_t* rngState, const gpugi_image* im) {
+    if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
+    if (p->pass > GPUGI_PASS_BPT) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->width != im->width || p->height != im->height)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
+    if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "maxPathLength must be in [1, 64]");
+    if (p->numLightSamples == 0 || p->samples == 0)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "numLightSamples and samples must be > 0");
+    if (!sc->dev.vinfo || !sc->dev.materials)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "scene lacks vertex info or materials");
+    if (!lightSamples && !rngState)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "either lightSamples or rngState is required");
+    return GPUGI_OK;
+}
+
+gpugi_status gpugi_set_batch_config(gpugi_ctx* ctx, uint32_t pathsPerRound, uint32_t useGraph) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (pathsPerRound < 1024 || pathsPerRound > (64u << 20))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "pathsPerRound must be in [1024, 64M]");
+    ctx->batchPaths = pathsPerRound;
+    ctx->batchGraph = useGraph ? 1u : 0u;
+    return GPUGI_OK;
+}
+
+gpugi_status gpugi_render_batch(gpugi_ctx* ctx, const gpugi_job* jobs, uint32_t numJobs) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (numJobs && !jobs) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL jobs");
+    std::vector<uint32_t> pt;  // jobs of the fused PT wavefront
+    uint32_t maxDepth = 0;
+    uint64_t maxLightBytes = 0;
+    const uint32_t cap = ctx->batchPaths;
+    for (uint32_t j = 0; j < numJobs; ++j) {
+        const gpugi_job& J = jobs[j];
+        gpugi_status st = check_render_args(ctx, J.scene, &J.camera, &J.params, J.lightSamples, J.rngState, J.image);
+        if (st) return st;
+        if (J.params.pass != GPUGI_PASS_PT) continue;
+        const uint64_t pix = (uint64_t)J.params.width * J.params.height;
+        if (pix > cap) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "a job image is larger than the path queue");
+        pt.push_back(j);
+        maxDepth = std::max(maxDepth, J.params.maxPathLength);
+        maxLightBytes += std::min<uint64_t>(J.params.samples, cap / pix) * J.params.numLightSamples * 32ull;
+    }
+    if (!pt.empty()) {
+        const uint32_t nj = (uint32_t)pt.size();
+        gpugi_status st = ensure_buffers(ctx, cap, 0, maxLightBytes, 1);
+        if (st) return st;
+        RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
+        if ((st = ensure_host_lights(ctx, rb, maxLightBytes))) return st;
+        if (nj > rb->jobCap) {
+            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+            if (rb->dJobs) cudaFree(rb->dJobs);
+            if (rb->dOffsets) cudaFree(rb->dOffsets);
+            if (rb->hJobs) cudaFreeHost(rb->hJobs);
+            if (rb->hOffsets) cudaFreeHost(rb->hOffsets);
+            rb->dJobs = rb->hJobs = nullptr;
+            rb->dOffsets = rb->hOffsets = nullptr;
+            rb->jobCap = 0;
+            GPUGI_CUDA_TRY(ctx, cudaMalloc(&rb->dJobs, nj * sizeof(RenderConst)));
+            GPUGI_CUDA_TRY(ctx, cudaMalloc(&rb->dOffsets, (nj + 1) * sizeof(uint32_t)));
+            GPUGI_CUDA_TRY(ctx, cudaMallocHost(&rb->hJobs, nj * sizeof(RenderConst)));
+            GPUGI_CUDA_TRY(ctx, cudaMallocHost(&rb->hOffsets, (nj + 1) * sizeof(uint32_t)));
+            rb->jobCap = nj;
+        }
+        // launch shapes (no node staging: the walkers serve several scenes)
+        WalkerLaunch LE, LS;
+        if ((st = walker_launch_config(ctx, jobs[pt[0]].scene, (const void*)k_batch_extend, 1ull << 40, 0, LE)) ||
+            (st = walker_launch_config(ctx, jobs[pt[0]].scene, (const void*)k_batch_shadow, 1ull << 40, 0, LS)))
+            return st;
+        int perSM = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, (const void*)k_batch_pt_shade, 128, 0);
+        const unsigned gridShade = (unsigned)(ctx->numSMs * std::max(perSM, 1));
+        const unsigned genBlocks = (unsigned)ctx->numSMs * 8;
+        auto record = [&](cudaStream_t stream) {
+            cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), stream);
+            PathSoA A = rb->A, B = rb->B;
+            k_batch_generate<<<genBlocks, 256, 0, stream>>>(rb->dJobs, rb->dOffsets, nj, rb->cnt, A);
+            for (int depth = 0; depth < (int)maxDepth; ++depth) {
+                k_batch_extend<<<LE.grid, 128, 0, stream>>>(rb->dJobs, rb->cnt, ctx->errWord, A, rb->H, depth);
+                k_batch_pt_shade<<<gridShade, 128, 0, stream>>>(rb->dJobs, rb->cnt, A, B, rb->H, rb->Q, depth);
+                k_batch_shadow<<<LS.grid, 128, 0, stream>>>(rb->dJobs, rb->cnt, ctx->errWord, rb->Q, depth);
+                std::swap(A, B);
+            }
+        };
+        if (ctx->batchGraph) {
+            const std::vector<uintptr_t> key = {(uintptr_t)rb->block, (uintptr_t)rb->dJobs, nj, maxDepth, LE.grid,
+                                                LS.grid, gridShade, (uintptr_t)ctx->errWord};
+            if (!rb->batchExec || key != rb->batchKey) {
+                if (rb->batchExec) cudaGraphExecDestroy(rb->batchExec);
+                rb->batchExec = nullptr;
+                cudaGraph_t graph = nullptr;
+                GPUGI_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+                record(ctx->stream);
+                const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+                if (ce != cudaSuccess) return cuda_fail(ctx, ce, "capturing the batch wavefront");
+                const cudaError_t ie = cudaGraphInstantiate(&rb->batchExec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ie != cudaSuccess) {
+                    rb->batchExec = nullptr;
+                    return cuda_fail(ctx, ie, "instantiating the batch graph");
+                }
+                rb->batchKey = key;
+            }
+        }
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
+        std::vector<uint32_t> done(nj, 0);
+        for (;;) {
+            // plan a round: each unfinished job adds as many samples as still fit
+            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // staging buffers are free again
+            uint64_t used = 0, lightOff = 0;
+            bool any = false;
+            rb->hOffsets[0] = 0;
+            for (uint32_t q = 0; q < nj; ++q) {
+                const gpugi_job& J = jobs[pt[q]];
+                const uint64_t pix = (uint64_t)J.params.width * J.params.height;
+                const uint32_t c =
+                    (uint32_t)std::min<uint64_t>(J.params.samples - done[q], (cap - used) / pix);
+                RenderConst rc = make_render_const(ctx, J.scene, &J.camera, &J.params, J.image, rb);
+                rc.samples = c;
+                rc.sampleBase = done[q];
+                rc.lightSamples = rb->lights + lightOff / 16;
+                if (c) {
+                    const size_t setFloats = (size_t)J.params.numLightSamples * 8;
+                    float* dst = rb->hostLights + lightOff / 4;
+                    if (J.lightSamples)
+                        std::memcpy(dst, J.lightSamples + (size_t)done[q] * setFloats, c * setFloats * sizeof(float));
+                    else
+                        for (uint32_t k = 0; k < c; ++k)
+                            generate_light_samples(const_cast<gpugi_scene*>(J.scene), *J.rngState,
+                                                   J.params.numLightSamples, dst + k * setFloats);
+                    lightOff += c * setFloats * sizeof(float);
+                    any = true;
+                }
+                rb->hJobs[q] = rc;
+                used += c * pix;
+                rb->hOffsets[q + 1] = (uint32_t)used;
+                done[q] += c;
+            }
+            if (!any) break;
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->lights, rb->hostLights, lightOff, cudaMemcpyHostToDevice,
+                                                ctx->stream));
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->dJobs, rb->hJobs, nj * sizeof(RenderConst),
+                                                cudaMemcpyHostToDevice, ctx->stream));
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->dOffsets, rb->hOffsets, (nj + 1) * sizeof(uint32_t),
+                                                cudaMemcpyHostToDevice, ctx->stream));
+            if (ctx->batchGraph) GPUGI_CUDA_TRY(ctx, cudaGraphLaunch(rb->batchExec, ctx->stream));
+            else record(ctx->stream);
+            GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+        }
+    }
+    // other passes: one job after another
+    for (uint32_t j = 0; j < numJobs; ++j) {
+        const gpugi_job& J = jobs[j];
+        if (J.params.pass == GPUGI_PASS_PT) continue;
+        gpugi_status st = gpugi_render(ctx, J.scene, &J.camera, &J.params, J.lightSamples, J.rngState, J.image);
+        if (st) return st;
     }
     return GPUGI_OK;
 }

@@ -39,6 +39,54 @@ static uint32_t bits_of(float f) {
     return u;
 }
 
+// Device node order: the nodes of the top tree levels first, breadth first
+// (as many whole levels as fit in maxTop), then every other node in its
+// original preorder. Child and escape words are renumbered; leaf words are
+// kept. The walk visits the same logical nodes in the same order, only their
+// addresses change. Returns the number of leading (top) nodes.
+static uint32_t relayout_nodes(std::vector<float>& nodes, uint32_t numNodes, uint32_t maxTop) {
+    std::vector<uint32_t> depth(numNodes, 0);
+    uint32_t maxDepth = 0;
+    for (uint32_t i = 0; i < numNodes; ++i) {  // preorder: parents precede children
+        const uint32_t child = bits_of(nodes[8 * (size_t)i + 3]);
+        if (child & LEAF_FLAG) continue;
+        const uint32_t right = bits_of(nodes[8 * (size_t)child + 7]);
+        depth[child] = depth[right] = depth[i] + 1;
+        maxDepth = std::max(maxDepth, depth[i] + 1);
+    }
+    std::vector<uint32_t> perLevel(maxDepth + 2, 0);
+    for (uint32_t d : depth) ++perLevel[d];
+    uint32_t levels = 0, top = 0;
+    while (levels <= maxDepth && top + perLevel[levels] <= maxTop) top += perLevel[levels++];
+    if (top <= 1) return 0;  // nothing worth staging: keep the original order
+    std::vector<uint32_t> map(numNodes, UINT32_MAX);
+    uint32_t next = 0;
+    std::vector<uint32_t> queue{0};
+    for (size_t q = 0; q < queue.size(); ++q) {  // breadth first over the top levels, siblings adjacent
+        const uint32_t i = queue[q];
+        map[i] = next++;
+        const uint32_t child = bits_of(nodes[8 * (size_t)i + 3]);
+        if ((child & LEAF_FLAG) || depth[i] + 1 >= levels) continue;
+        queue.push_back(child);
+        queue.push_back(bits_of(nodes[8 * (size_t)child + 7]));
+    }
+    for (uint32_t i = 0; i < numNodes; ++i)
+        if (map[i] == UINT32_MAX) map[i] = next++;
+    std::vector<float> out(nodes.size());
+    for (uint32_t i = 0; i < numNodes; ++i) {
+        float* o = &out[8 * (size_t)map[i]];
+        std::memcpy(o, &nodes[8 * (size_t)i], 8 * sizeof(float));
+        const uint32_t child = bits_of(nodes[8 * (size_t)i + 3]);
+        const uint32_t esc = bits_of(nodes[8 * (size_t)i + 7]);
+        const uint32_t nc = (child & LEAF_FLAG) ? child : map[child];
+        const uint32_t ne = esc ? map[esc] : 0u;
+        std::memcpy(&o[3], &nc, 4);
+        std::memcpy(&o[7], &ne, 4);
+    }
+    nodes.swap(out);
+    return top;
+}
+
 template <typename T>
 static gpugi_status upload(gpugi_ctx* ctx, gpugi_scene* sc, const T* host, size_t count, const T** dst) {
     *dst = nullptr;
@@ -116,6 +164,8 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
             return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "escape must be 0 or point forward (preorder)");
     }
 
+    const uint32_t topNodes = relayout_nodes(nodes, numNodes, ctx->sharedNodes);
+
     cudaError_t se = cudaSetDevice(ctx->device);
     if (se != cudaSuccess) return cuda_fail(ctx, se, "cudaSetDevice");
     gpugi_scene* sc = new gpugi_scene();
@@ -160,6 +210,7 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     sc->dev.boundsKind = boundsKind;
     sc->dev.numVertices = numVertices;
     sc->dev.numMaterials = numMaterials;
+    sc->dev.topNodes = topNodes;
     sc->hostPositions.assign(positions, positions + 3 * (size_t)numVertices);
     sc->hostSlots.assign(slots, slots + 4 * (size_t)numSlots);
     if (numMaterials)

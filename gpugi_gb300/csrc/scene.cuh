@@ -32,6 +32,10 @@ struct DevScene {
     uint32_t boundsKind = 0;
     uint32_t numVertices = 0;
     uint32_t numMaterials = 0;
+    // Nodes are stored with the top tree levels first (breadth-first), the
+    // rest in preorder; persistent walkers stage nodes [0, topNodes) in
+    // shared memory. Node 0 is the root; an escape of 0 still ends the walk.
+    uint32_t topNodes = 0;
 };
 
 // Material view (constant-valued MaterialData, materials.glsl:9-30).

@@ -41,6 +41,21 @@ __global__ void __launch_bounds__(256) k_trace_any(DevScene s, const float* __re
     occluded[i] = r.slot >= 0 ? 1 : 0;
 }
 
+gpugi_status walker_launch_config(gpugi_ctx* ctx, const gpugi_scene* sc, const void* kernel, uint64_t n,
+                                  uint32_t maxStage, WalkerLaunch& out) {
+    out.stage = sc->dev.topNodes < maxStage ? sc->dev.topNodes : maxStage;
+    out.smem = (size_t)out.stage * 32;
+    if (out.smem > 48 * 1024)
+        GPUGI_CUDA_TRY(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)out.smem));
+    int perSM = 0;
+    GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, out.smem));
+    uint64_t grid = (uint64_t)ctx->numSMs * (uint64_t)(perSM > 0 ? perSM : 1);
+    const uint64_t needed = (n + 127) / 128;
+    if (grid > needed) grid = needed;
+    out.grid = (unsigned)(grid > 0 ? grid : 1);
+    return GPUGI_OK;
+}
+
 // Persistent walk: a grid sized to fill the GPU once; every warp keeps all 32
 // lanes busy by handing each finished lane the next ray index from a global
 // counter (one atomic per warp per refill). Each ray still performs exactly
@@ -51,7 +66,9 @@ __global__ void __launch_bounds__(128) k_trace_persistent(
     const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
     const float* __restrict__ tmax, uint64_t n, int32_t* __restrict__ slot, float* __restrict__ t,
     float* __restrict__ u, float* __restrict__ v, uint8_t* __restrict__ occluded, unsigned long long* counter,
-    uint32_t* err) {
+    uint32_t* err, uint32_t stage) {
+    extern __shared__ float4 s_top[];
+    stage_top_nodes(s, s_top, stage);
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanesBelow = (1u << lane) - 1u;
     WalkState w;
@@ -77,7 +94,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err)) {
+        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err, s_top, stage)) {
             if (ANY_HIT) {
                 occluded[ray] = w.slot >= 0 ? 1 : 0;
             } else {
@@ -100,16 +117,15 @@ gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
     void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
-              const float*, uint64_t, int32_t*, float*, float*, float*, uint8_t*, unsigned long long*, uint32_t*);
+              const float*, uint64_t, int32_t*, float*, float*, float*, uint8_t*, unsigned long long*, uint32_t*,
+              uint32_t);
     if (!ell) k = anyHit ? k_trace_persistent<true, 0> : k_trace_persistent<false, 0>;
     else k = anyHit ? k_trace_persistent<true, 1> : k_trace_persistent<false, 1>;
-    int perSM = 0;
-    GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k, 128, 0));
-    uint64_t grid = (uint64_t)ctx->numSMs * (uint64_t)(perSM > 0 ? perSM : 1);
-    const uint64_t needed = (n + 127) / 128;
-    if (grid > needed) grid = needed;
-    k<<<(unsigned)grid, 128, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, occluded,
-                                               counter, ctx->errWord);
+    WalkerLaunch L;
+    gpugi_status st = walker_launch_config(ctx, sc, (const void*)k, n, ctx->sharedNodes, L);
+    if (st) return st;
+    k<<<L.grid, 128, L.smem, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, occluded,
+                                            counter, ctx->errWord, L.stage);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }
@@ -163,7 +179,9 @@ __global__ void __launch_bounds__(128) k_trace_queue(
     const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
     const float* __restrict__ tmax, int32_t* __restrict__ slot, float* __restrict__ t, float* __restrict__ u,
     float* __restrict__ v, uint8_t* __restrict__ occluded, const uint32_t* __restrict__ queue,
-    unsigned long long* counters, uint32_t* err) {
+    unsigned long long* counters, uint32_t* err, uint32_t stage) {
+    extern __shared__ float4 s_top[];
+    stage_top_nodes(s, s_top, stage);
     const uint64_t n = counters[1];
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanesBelow = (1u << lane) - 1u;
@@ -190,7 +208,7 @@ __global__ void __launch_bounds__(128) k_trace_queue(
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err)) {
+        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err, s_top, stage)) {
             if (ANY_HIT) {
                 occluded[ray] = w.slot >= 0 ? 1 : 0;
             } else {
@@ -214,33 +232,8 @@ gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool a
     if (st) return st;
     unsigned long long* counters = reinterpret_cast<unsigned long long*>(ctx->scratch);
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
-    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    const unsigned grid1 = (unsigned)((n + 255) / 256);
-#define GPUGI_FILTER(A, B)                                                                                          \
-    k_trace_root_filter<A, B><<<grid1, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, \
-                                                              v, occluded, ctx->queue, counters)
-    if (!ell) {
-        if (anyHit) GPUGI_FILTER(true, 0);
-        else GPUGI_FILTER(false, 0);
-    } else {
-        if (anyHit) GPUGI_FILTER(true, 1);
-        else GPUGI_FILTER(false, 1);
-    }
-#undef GPUGI_FILTER
-    void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
-              const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
-              uint32_t*);
-    if (!ell) k = anyHit ? k_trace_queue<true, 0> : k_trace_queue<false, 0>;
-    else k = anyHit ? k_trace_queue<true, 1> : k_trace_queue<false, 1>;
-    int perSM = 0;
-    GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k, 128, 0));
-    uint64_t grid = (uint64_t)ctx->numSMs * (uint64_t)(perSM > 0 ? perSM : 1);
-    const uint64_t needed = (n + 127) / 128;
-    if (grid > needed) grid = needed;
-    k<<<(unsigned)grid, 128, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded,
-                                               ctx->queue, counters, ctx->errWord);
-    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
-    return GPUGI_OK;
+    return launch_trace_filtered_on(ctx, sc, anyHit, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, occluded,
+                                    ctx->queue, counters);
 }
 
 // The same two launches as launch_trace_filtered, on scratch memory the
@@ -266,16 +259,14 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
 #undef GPUGI_FILTER_ON
     void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
               const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
-              uint32_t*);
+              uint32_t*, uint32_t);
     if (!ell) k = anyHit ? k_trace_queue<true, 0> : k_trace_queue<false, 0>;
     else k = anyHit ? k_trace_queue<true, 1> : k_trace_queue<false, 1>;
-    int perSM = 0;
-    GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k, 128, 0));
-    uint64_t grid = (uint64_t)ctx->numSMs * (uint64_t)(perSM > 0 ? perSM : 1);
-    const uint64_t needed = (n + 127) / 128;
-    if (grid > needed) grid = needed;
-    k<<<(unsigned)grid, 128, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded,
-                                               queue, counters, ctx->errWord);
+    WalkerLaunch L;
+    gpugi_status st = walker_launch_config(ctx, sc, (const void*)k, n, ctx->sharedNodes, L);
+    if (st) return st;
+    k<<<L.grid, 128, L.smem, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded, queue,
+                                            counters, ctx->errWord, L.stage);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }

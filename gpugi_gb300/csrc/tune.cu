@@ -1,0 +1,178 @@
+// Autotuner: picks the launch settings of a context by timing candidates on
+// the scene at hand (CUDA events on the context stream).
+//
+//  * ray queries: trace mode (thread per ray with block size 64/128/256,
+//    persistent lane refill, root prefilter + persistent walker) on
+//    synthetic rays over the scene's bounds;
+//  * batched rendering: the path-queue capacity of a round (small rounds keep
+//    the wavefront state in L2, large rounds have fewer launches and
+//    shorter tails) on a 512 x 512 path-tracing job of the scene.
+//
+// The traversal is stackless (escape pointers), so there is no stack depth
+// to tune.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ctx.cuh"
+#include "shade.cuh"
+
+using namespace gpugi;
+
+namespace {
+
+// Rays with origins uniform in the scene box scaled by 2 about its centre
+// and directions uniform on the sphere (hash-based, reproducible).
+__global__ void k_tune_rays(float3 center, float3 half, uint64_t n, uint32_t seed, float* ox, float* oy, float* oz,
+                            float* dx, float* dy, float* dz, float* tmax) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t s = wanghash(wanghash(seed) + (uint32_t)i);
+        const float u0 = random01(s), u1 = random01(s), u2 = random01(s), u3 = random01(s), u4 = random01(s);
+        ox[i] = center.x + (2.0f * u0 - 1.0f) * 2.0f * half.x;
+        oy[i] = center.y + (2.0f * u1 - 1.0f) * 2.0f * half.y;
+        oz[i] = center.z + (2.0f * u2 - 1.0f) * 2.0f * half.z;
+        const float z = 2.0f * u3 - 1.0f, r = sqrtf(fmaxf(0.0f, 1.0f - z * z)), phi = 6.2831853f * u4;
+        dx[i] = r * cosf(phi);
+        dy[i] = r * sinf(phi);
+        dz[i] = z;
+        tmax[i] = kRAY_MAX;
+    }
+}
+
+struct Events {
+    cudaEvent_t a = nullptr, b = nullptr;
+    Events() {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    }
+    ~Events() {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+gpugi_status gpugi_autotune(gpugi_ctx* ctx, const gpugi_scene* sc, uint32_t flags, gpugi_tuning* out) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!sc || !out) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
+    *out = gpugi_tuning{};
+    out->traceMode = ctx->traceMode;
+    out->traceBlock = ctx->traceBlock;
+    out->batchPaths = ctx->batchPaths;
+    // scene bounds from the root node (AABB: min/max, ellipsoid: centre/radii)
+    float4 root[2];
+    GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(root, sc->dev.nodes, sizeof root, cudaMemcpyDeviceToHost, ctx->stream));
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    float3 center, half;
+    if (sc->dev.boundsKind == GPUGI_BOUNDS_AABB) {
+        center = make_float3(0.5f * (root[0].x + root[1].x), 0.5f * (root[0].y + root[1].y), 0.5f * (root[0].z + root[1].z));
+        half = make_float3(0.5f * (root[1].x - root[0].x), 0.5f * (root[1].y - root[0].y), 0.5f * (root[1].z - root[0].z));
+    } else {
+        center = make_float3(root[0].x, root[0].y, root[0].z);
+        half = make_float3(root[1].x, root[1].y, root[1].z);
+    }
+    Events ev;
+    if (flags & GPUGI_TUNE_TRACE) {
+        const uint64_t n = 1u << 20;
+        float* buf = nullptr;
+        GPUGI_CUDA_TRY(ctx, cudaMalloc(&buf, n * 11 * sizeof(float)));
+        float* r[7];
+        for (int k = 0; k < 7; ++k) r[k] = buf + k * n;
+        int32_t* slot = reinterpret_cast<int32_t*>(buf + 7 * n);
+        float *t = buf + 8 * n, *u = buf + 9 * n, *v = buf + 10 * n;
+        k_tune_rays<<<ctx->numSMs * 8, 256, 0, ctx->stream>>>(center, half, n, 0x5EEDu, r[0], r[1], r[2], r[3], r[4],
+                                                             r[5], r[6]);
+        struct Cand {
+            uint32_t mode, block;
+        };
+        const Cand cands[] = {{0, 64}, {0, 128}, {0, 256}, {1, 128}, {2, 128}};
+        const uint32_t keepMode = ctx->traceMode, keepBlock = ctx->traceBlock;
+        double best = -1.0;
+        gpugi_status st = GPUGI_OK;
+        for (const Cand& c : cands) {
+            ctx->traceMode = c.mode;
+            ctx->traceBlock = c.block;
+            float ms = 0.0f;
+            for (int rep = 0; rep < 4 && !st; ++rep) {  // one warm-up, three timed
+                if (rep == 1) cudaEventRecord(ev.a, ctx->stream);
+                st = launch_trace_closest(ctx, sc, r[0], r[1], r[2], r[3], r[4], r[5], r[6], n, slot, t, u, v);
+            }
+            if (st) break;
+            cudaEventRecord(ev.b, ctx->stream);
+            cudaEventSynchronize(ev.b);
+            cudaEventElapsedTime(&ms, ev.a, ev.b);
+            const double mrays = 3.0 * n / (ms * 1e-3) / 1e6;
+            if (mrays > best) {
+                best = mrays;
+                out->traceMode = c.mode;
+                out->traceBlock = c.block;
+            }
+        }
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(buf);
+        if (st) {
+            ctx->traceMode = keepMode;
+            ctx->traceBlock = keepBlock;
+            return st;
+        }
+        ctx->traceMode = out->traceMode;
+        ctx->traceBlock = out->traceBlock;
+        out->traceMraysPerSecond = best;
+    }
+    if ((flags & GPUGI_TUNE_BATCH) && sc->dev.vinfo && sc->dev.materials) {
+        const uint32_t W = 512, H = 512, spp = 64;
+        gpugi_image* im = nullptr;
+        gpugi_status st = gpugi_image_create(ctx, W, H, 0, &im);
+        if (st) return st;
+        gpugi_job job{};
+        job.scene = sc;
+        const float ext = std::max(half.x, std::max(half.y, half.z));
+        const float pos[3] = {center.x, center.y, center.z + 3.0f * ext}, at[3] = {center.x, center.y, center.z},
+                    up[3] = {0.0f, 1.0f, 0.0f};
+        gpugi_camera_lookat(pos, at, up, 45.0f, W, H, &job.camera);
+        job.params.pass = GPUGI_PASS_PT;
+        job.params.width = W;
+        job.params.height = H;
+        job.params.maxPathLength = 8;
+        job.params.samples = spp;
+        job.params.numLightSamples = 128;
+        job.params.sky[0] = job.params.sky[1] = job.params.sky[2] = 0.1f;
+        job.image = im;
+        uint64_t rng = 123;
+        job.rngState = &rng;
+        const uint32_t keepPaths = ctx->batchPaths;
+        const uint32_t caps[] = {256u << 10, 1u << 20, 4u << 20, 16u << 20};
+        double best = -1.0;
+        for (uint32_t cap : caps) {
+            ctx->batchPaths = cap;
+            job.params.samples = 4;  // warm-up: buffers, graph capture
+            if ((st = gpugi_render_batch(ctx, &job, 1))) break;
+            job.params.samples = spp;
+            cudaStreamSynchronize(ctx->stream);
+            cudaEventRecord(ev.a, ctx->stream);
+            if ((st = gpugi_render_batch(ctx, &job, 1))) break;
+            cudaEventRecord(ev.b, ctx->stream);
+            cudaEventSynchronize(ev.b);
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ev.a, ev.b);
+            const double mpaths = (double)W * H * spp / (ms * 1e-3) / 1e6;
+            if (mpaths > best) {
+                best = mpaths;
+                out->batchPaths = cap;
+            }
+        }
+        gpugi_image_destroy(im);
+        if (st) {
+            ctx->batchPaths = keepPaths;
+            return st;
+        }
+        ctx->batchPaths = out->batchPaths;
+        out->batchMpathsPerSecond = best;
+    }
+    return GPUGI_OK;
+}
+
+}  // extern "C"

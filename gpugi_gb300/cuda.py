@@ -54,6 +54,7 @@ def _declare(L):
     for name in ("gpugi_trace_any", "gpugi_trace_any_device"):
         getattr(L, name).argtypes = [P, P] + [P] * 7 + [U64, P]
     L.gpugi_set_trace_config.argtypes = [P, U32, U32]
+    L.gpugi_set_scene_layout.argtypes = [P, U32, U32]
     L.gpugi_trace_stats_device.argtypes = [P, P] + [P] * 7 + [U64, U32, P]
     for name, args in _EXTRA_DECLS.items():
         if hasattr(L, name):
@@ -106,8 +107,25 @@ class Context:
     def stream(self) -> int:
         return lib().gpugi_stream(self._h) or 0
 
-    def set_trace_config(self, mode: int = 1, block_size: int = 128):
+    def set_trace_config(self, mode: int = 2, block_size: int = 128):
         self.check(lib().gpugi_set_trace_config(self._h, mode, block_size))
+
+    def set_scene_layout(self, shared_nodes: int = 0, render_shared_nodes: int = 0):
+        """Top-of-tree nodes staged in shared memory, for scenes uploaded afterwards."""
+        self.check(lib().gpugi_set_scene_layout(self._h, shared_nodes, render_shared_nodes))
+
+    def autotune(self, scene: "DeviceScene", trace: bool = True, batch: bool = False) -> dict:
+        """gpugi_autotune: times candidate launch settings on the scene and applies the fastest."""
+
+        class Tuning(C.Structure):
+            _fields_ = [("traceMode", C.c_uint32), ("traceBlock", C.c_uint32), ("batchPaths", C.c_uint32),
+                        ("traceMraysPerSecond", C.c_double), ("batchMpathsPerSecond", C.c_double)]
+
+        t = Tuning()
+        L = lib()
+        L.gpugi_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(Tuning)]
+        self.check(L.gpugi_autotune(self._h, scene.handle, (1 if trace else 0) | (2 if batch else 0), C.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
     def close(self):
         if self._h:

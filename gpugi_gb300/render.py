@@ -50,6 +50,8 @@ def _declare():
     L.gpugi_generate_light_samples.argtypes = [P, C.POINTER(U64), U32, P]
     L.gpugi_render.argtypes = [P, P, C.POINTER(Camera), C.POINTER(RenderParams), P, C.POINTER(U64), P]
     L.gpugi_render_ray_counts.argtypes = [P, P]
+    L.gpugi_render_batch.argtypes = [P, P, U32]
+    L.gpugi_set_batch_config.argtypes = [P, U32, U32]
     L._render_declared = True
     return L
 
@@ -148,6 +150,47 @@ def render(ctx: cuda.Context, scene: cuda.DeviceScene, camera: Camera, image: Im
                              C.byref(st) if ls is None else None, image.handle))
     if rng_state is not None and ls is None:
         rng_state[0] = st.value
+
+
+class Job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("params", RenderParams), ("lightSamples", C.c_void_p),
+                ("rngState", C.POINTER(C.c_uint64)), ("image", C.c_void_p)]
+
+
+def render_batch(ctx: cuda.Context, jobs: list[dict]) -> None:
+    """gpugi_render_batch over jobs given as dicts with the keys of render():
+    scene, camera, image, pass_ (default PT), max_path_length, samples,
+    iteration, num_light_samples, sky, rr_start_depth, light_samples or
+    rng_state (a one-element list, updated)."""
+    L = _declare()
+    arr = (Job * len(jobs))()
+    keep, states = [], []
+    for i, j in enumerate(jobs):
+        pass_ = j.get("pass_", "PT")
+        img = j["image"]
+        nls = j.get("num_light_samples") or DEFAULT_LIGHT_SAMPLES[pass_]
+        samples = j.get("samples", 1)
+        p = RenderParams(PASSES[pass_], img.width, img.height, j.get("max_path_length", 8),
+                         j.get("rr_start_depth", 0), j.get("iteration", 0), samples, nls,
+                         _f3(j.get("sky", (0.0, 0.0, 0.0))), 0)
+        ls = j.get("light_samples")
+        st = None
+        if ls is not None:
+            ls = np.ascontiguousarray(ls, dtype=np.float32)
+            assert ls.shape == (samples, nls, 8)
+            keep.append(ls)
+        else:
+            st = C.c_uint64(j["rng_state"][0])
+            states.append((st, j["rng_state"]))
+        arr[i] = Job(j["scene"].handle, j["camera"], p, cuda._ptr(ls) if ls is not None else None,
+                     C.pointer(st) if st is not None else None, img.handle)
+    ctx.check(L.gpugi_render_batch(ctx.handle, arr, len(jobs)))
+    for st, ref in states:
+        ref[0] = st.value
+
+
+def set_batch_config(ctx: cuda.Context, paths_per_round: int = 16 << 20, use_graph: bool = True) -> None:
+    ctx.check(_declare().gpugi_set_batch_config(ctx.handle, paths_per_round, int(bool(use_graph))))
 
 
 def ray_counts(ctx: cuda.Context) -> tuple[int, int]:

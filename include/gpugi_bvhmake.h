@@ -61,6 +61,20 @@ int gpugi_bvh_write_file(const gpugi_bvh* bvh, const char* path);
 int gpugi_bvh_read_file(const char* path, gpugi_bvh** out);
 int gpugi_bvh_vertices(const gpugi_bvh* bvh, uint32_t* numVertices, float* positions /* may be NULL */);
 
+/* Per-vertex normal (3 floats) and texture coordinate (2 floats) of the
+ * "vertices" chunk's 32-byte records {position, normal, texcoord}
+ * (bvhmake/filedef.hpp:15-20). Set before gpugi_bvh_write_file (either
+ * array may be NULL: zeros are written); read after gpugi_bvh_read_file. */
+int gpugi_bvh_set_vertex_attributes(gpugi_bvh* bvh, const float* normals, const float* texcoords);
+int gpugi_bvh_vertex_attributes(const gpugi_bvh* bvh, float* normals, float* texcoords);
+
+/* Material records carried in an extra "gpugi_materials" chunk (24 floats
+ * each, the gpugi_material layout of gpugi_cuda.h). No counterpart in the
+ * reference, which keeps materials in the scene's JSON next to the file;
+ * readers that do not know the chunk skip it, as the format allows. */
+int gpugi_bvh_set_materials(gpugi_bvh* bvh, const float* records, uint32_t numMaterials);
+int gpugi_bvh_materials(const gpugi_bvh* bvh, uint32_t* numMaterials, float* records /* may be NULL */);
+
 void gpugi_bvh_free(gpugi_bvh* bvh);
 const char* gpugi_bvh_last_error(void);
 

@@ -163,6 +163,14 @@ gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* scene,
  * the same tests per ray and return identical results. */
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize);
 
+/* Scene layout tuning (set by the autotuner), applied to scenes uploaded
+ * afterwards: the top tree levels (up to sharedNodes nodes, whole levels) are
+ * stored first, breadth first, and the persistent walkers stage them in
+ * shared memory: the ray queries stage up to sharedNodes, the renderers'
+ * walkers up to renderSharedNodes. 0 disables staging. The logical walk and
+ * every result are unchanged. */
+gpugi_status gpugi_set_scene_layout(gpugi_ctx* ctx, uint32_t sharedNodes, uint32_t renderSharedNodes);
+
 /* ------------------------------------------------------------------------
  * Rendering passes (wavefront): PT, LT and BPT.
  *
@@ -238,6 +246,103 @@ gpugi_status gpugi_generate_light_samples(const gpugi_scene* scene, uint64_t* rn
 gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* scene, const gpugi_camera* camera,
                           const gpugi_render_params* params, const float* lightSamples, uint64_t* rngState,
                           gpugi_image* image);
+
+/* ------------------------------------------------------------------------
+ * Neural radiance cache (NRC). No counterpart in the reference: a project
+ * addition. A 64-64-64-64-64-3 ReLU MLP (no biases; one input is a constant
+ * 1), FP16 weights and activations, FP32 accumulation on the tensor cores,
+ * trained online with Adam on a relative L2 loss.
+ * Query records: 12 floats {position, outgoing direction, normal, albedo};
+ * training samples: 15 floats {query, target radiance rgb}. Positions are
+ * normalised to the box given at creation.
+ * ------------------------------------------------------------------------ */
+typedef struct gpugi_nrc gpugi_nrc;
+#define GPUGI_NRC_PARAMS 17408  /* 4 x 64 x 64 + 64 x 16 (output padded to 16) */
+
+gpugi_status gpugi_nrc_create(gpugi_ctx* ctx, const float boxMin[3], const float boxMax[3], uint64_t seed,
+                              float learningRate, gpugi_nrc** out);
+void gpugi_nrc_destroy(gpugi_nrc* nrc);
+/* FP32 master weights, layer l at l*4096, row-major [in][out] (out = 16 for l = 4). */
+gpugi_status gpugi_nrc_get_weights(gpugi_ctx* ctx, const gpugi_nrc* nrc, float* weights);
+gpugi_status gpugi_nrc_set_weights(gpugi_ctx* ctx, gpugi_nrc* nrc, const float* weights);
+/* radiance[3 i + c] = max(network(query i)_c, 0). Device pointers, asynchronous. */
+gpugi_status gpugi_nrc_infer_device(gpugi_ctx* ctx, const gpugi_nrc* nrc, const float* queries, uint64_t n,
+                                    float* radiance);
+/* One Adam step on n device samples; *loss (host, may be NULL) receives the
+ * mean relative L2 loss before the step (synchronises when non-NULL). */
+gpugi_status gpugi_nrc_train_device(gpugi_ctx* ctx, gpugi_nrc* nrc, const float* samples, uint64_t n, float* loss);
+/* The loss gradient without a weight update (host outputs: predictions
+ * n*3 may be NULL, gradient GPUGI_NRC_PARAMS floats). For checking. */
+gpugi_status gpugi_nrc_gradient_device(gpugi_ctx* ctx, gpugi_nrc* nrc, const float* samples, uint64_t n,
+                                       float* predictions, float* gradient, float* loss);
+/* The 64-half input encoding of n queries (device output, n * 64 halves). */
+gpugi_status gpugi_nrc_encode_device(gpugi_ctx* ctx, const gpugi_nrc* nrc, const float* queries, uint64_t n,
+                                     void* encodedHalf);
+
+/* Path tracing with the radiance cache (params->pass must be PT). Each of
+ * params->samples frames: camera paths of the non-training pixels stop at
+ * vertex terminateDepth and add throughput x cache(vertex); a trainFraction
+ * of the pixels (chosen by a per-frame hash) trace full PT paths whose
+ * vertices become training samples {query, radiance reflected towards the
+ * previous vertex}; after the frame's lookups, trainSteps Adam steps run on
+ * those samples (when train != 0). Both kinds of path splat into image.
+ * Synchronises twice per frame (query and sample counts). */
+typedef struct gpugi_nrc_params {
+    uint32_t terminateDepth;  /* vertex index (0 = first hit) where render paths query the cache */
+    float trainFraction;      /* share of pixels tracing training paths, in [0, 1] */
+    uint32_t maxTrainSamples; /* cap on samples per frame (0: 65536) */
+    uint32_t trainSteps;      /* Adam steps per frame on all of the frame's samples (0 counts as 1) */
+    uint32_t train;           /* 0: use the cache without updating it */
+} gpugi_nrc_params;
+
+gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* scene, const gpugi_camera* camera,
+                              const gpugi_render_params* params, const float* lightSamples, uint64_t* rngState,
+                              gpugi_nrc* nrc, const gpugi_nrc_params* nrcParams, gpugi_image* image);
+
+/* Batched rendering: many jobs, each with its own scene, camera, image,
+ * resolution, sample count and path length, in one wavefront. No single
+ * counterpart in the reference (RendererSystem::Draw renders one scene per
+ * call, gpugi/renderer/renderersystem.cpp:235-258); per job the result is
+ * gpugi_render's with the same arguments (same seeds and light samples).
+ * PT jobs share the queues: each stage (generate, then per bounce extend,
+ * shade, shadow) is one launch over the paths of all jobs, and the whole
+ * sequence is captured once as a CUDA graph and replayed per round of at
+ * most the context's path-queue capacity (gpugi_set_batch_config).
+ * LT and BPT jobs are rendered one after another with gpugi_render.
+ * Jobs that share an rngState draw their light samples in round order. */
+typedef struct gpugi_job {
+    const gpugi_scene* scene;
+    gpugi_camera camera;
+    gpugi_render_params params;
+    const float* lightSamples;  /* params.samples x numLightSamples x 8 floats, or NULL */
+    uint64_t* rngState;         /* host light sampler state when lightSamples is NULL */
+    gpugi_image* image;
+} gpugi_job;
+
+gpugi_status gpugi_render_batch(gpugi_ctx* ctx, const gpugi_job* jobs, uint32_t numJobs);
+
+/* Path-queue capacity of one batched round (paths in flight; default 16M,
+ * at least the largest job image) and whether rounds replay a CUDA graph
+ * (default 1). */
+gpugi_status gpugi_set_batch_config(gpugi_ctx* ctx, uint32_t pathsPerRound, uint32_t useGraph);
+
+/* Autotuner. No counterpart in the reference (its launch shapes are fixed
+ * local sizes, e.g. gpugi/renderer/pathtracer.cpp:11). Times candidates on
+ * the scene with CUDA events and applies the fastest to the context:
+ * GPUGI_TUNE_TRACE: ray-query kernels (gpugi_set_trace_config mode and block
+ * size) on 2^20 synthetic rays over the scene bounds; GPUGI_TUNE_BATCH: the
+ * path-queue capacity of batched rounds on a 512 x 512, 64-spp PT job
+ * (needs vertex info and materials). The traversal is stackless, so no stack
+ * depth is tuned. Synchronises; allocates temporary buffers. */
+#define GPUGI_TUNE_TRACE 1u
+#define GPUGI_TUNE_BATCH 2u
+typedef struct gpugi_tuning {
+    uint32_t traceMode, traceBlock; /* chosen ray-query settings */
+    uint32_t batchPaths;            /* chosen paths per batched round */
+    double traceMraysPerSecond;     /* closest-hit rate of the chosen setting (0 if not tuned) */
+    double batchMpathsPerSecond;    /* camera paths per second of the chosen capacity (0 if not tuned) */
+} gpugi_tuning;
+gpugi_status gpugi_autotune(gpugi_ctx* ctx, const gpugi_scene* scene, uint32_t flags, gpugi_tuning* out);
 
 /* Rays traced by the last gpugi_render call, by kind: {camera/extension
  * (closest hit), shadow/connection (any hit)}. Synchronises. */

@@ -123,3 +123,18 @@ def test_file_round_trip(built, tmp_path):
     assert np.array_equal(b.hierarchy.view(np.uint32), ref.hierarchy.view(np.uint32))
     assert np.array_equal(b.slots, ref.slots)
     assert np.array_equal(b.positions, sc["positions"])
+
+
+def test_file_carries_vertex_attributes_and_materials(built, tmp_path):
+    sc = scenes.cornell_room(seed=2, sphere_level=1, wall_grid=2)
+    p = tmp_path / "room.bim"
+    bvh.write_bvh_file(sc["positions"], sc["triangles"], str(p), normals=sc["normals"], texcoords=sc["texcoords"],
+                       materials=sc["materials"], method="sweep", leaf_size=8)
+    b = bvh.read_bvh_file(str(p))
+    assert np.array_equal(b.normals, sc["normals"])
+    assert np.array_equal(b.texcoords, sc["texcoords"])
+    assert np.array_equal(b.materials, sc["materials"].reshape(-1, 24))
+    # without attributes the file still round-trips, with zero attributes and no materials
+    bvh.write_bvh_file(sc["positions"], sc["triangles"], str(p), method="sweep", leaf_size=8)
+    b = bvh.read_bvh_file(str(p))
+    assert not b.normals.any() and b.materials.shape == (0, 24)

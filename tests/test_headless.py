@@ -1,0 +1,102 @@
+"""The C++ renderer classes (RendererSystem, Pathtracer, ..., TextureMSE)
+through the headless driver, against the Python front end of the same C ABI.
+
+The driver sets up a RendererSystem the way the reference's Application
+does; its first iteration uses the first light-sample set drawn from the
+sampler state 123 and the frame seed of iteration 0, so the same images
+come out of gpugi_render(samples=N, rngState=123).
+"""
+import json
+import subprocess
+
+import numpy as np
+import pytest
+
+from gpugi_gb300 import build, bvh, cuda, render, scenes
+
+EXE = build.LIB / "gpugi_headless"
+
+
+def _read_pfm(path):
+    with open(path, "rb") as f:
+        assert f.readline() == b"PF\n"
+        w, h = map(int, f.readline().split())
+        assert float(f.readline()) < 0
+        return np.frombuffer(f.read(), dtype="<f4").reshape(h, w, 3)
+
+
+def test_cli_rejects_bad_arguments(built):
+    r = subprocess.run([str(EXE)], capture_output=True, text=True)
+    assert r.returncode == 2 and "--scene is required" in r.stderr
+    r = subprocess.run([str(EXE), "--scene", "x.bim", "--size", "0", "4"], capture_output=True, text=True)
+    assert r.returncode == 2
+
+
+@pytest.fixture(scope="module")
+def room_file(tmp_path_factory, built):
+    sc = scenes.cornell_room(seed=1, sphere_level=3, wall_grid=8)
+    p = tmp_path_factory.mktemp("scene") / "room.bim"
+    bvh.write_bvh_file(sc["positions"], sc["triangles"], str(p), normals=sc["normals"], texcoords=sc["texcoords"],
+                       materials=sc["materials"], method="sweep", leaf_size=8)
+    return sc, p
+
+
+def _run(args):
+    r = subprocess.run([str(EXE)] + [str(a) for a in args], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+CAM = [0.0, 1.0, 3.4, 0.0, 1.0, 0.0, 40.0]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("renderer,pass_", [("Pathtracer", "PT"), ("BidirectionalPathtracer", "BPT"),
+                                            ("LightPathtracer", "LT")])
+def test_headless_matches_the_c_abi(cuda_ctx, room_file, tmp_path, renderer, pass_):
+    sc, path = room_file
+    W = H = 32
+    iters = 4
+    out = tmp_path / "out.pfm"
+    info = _run(["--scene", path, "--renderer", renderer, "--size", W, H, "--camera", *CAM, "--iterations", iters,
+                 "--path-length", 6, "--out", out])
+    assert info["iterations"] == iters and info["renderer"] == renderer
+    got = _read_pfm(out)
+
+    b = bvh.read_bvh_file(str(path))
+    ds = cuda_ctx.upload_scene(b, b.positions, cuda.vertex_info(b.normals, b.texcoords), b.materials)
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, img, pass_, max_path_length=6, samples=iters, rng_state=[123])
+    expect = img.read()[..., :3] / iters
+    if pass_ == "BPT":
+        # eye paths pick light-cache entries by index, and the cache is
+        # filled in atomic order: runs differ like independent samples
+        assert abs(got.mean() / expect.mean() - 1) < 0.05, (got.mean(), expect.mean())
+    else:
+        # same seeds and light samples: equal up to float rounding in the
+        # camera and normal encoding, which may divert a few paths
+        close = np.abs(got - expect) <= 1e-4 * np.abs(expect).max() + 1e-6
+        assert close.mean() > 0.97, close.mean()
+        assert abs(got.mean() / expect.mean() - 1) < 0.02
+    img.close()
+    ds.close()
+
+
+@pytest.mark.gpu
+def test_headless_texture_mse_and_nrc(cuda_ctx, room_file, tmp_path):
+    sc, path = room_file
+    ref = tmp_path / "ref.pfm"
+    common = ["--scene", path, "--size", 32, 32, "--camera", *CAM, "--path-length", 6]
+    _run(common + ["--iterations", 8, "--out", ref])
+    # the same run again, measured against the first: MSE ~ 0 (atomic order aside)
+    info = _run(common + ["--iterations", 8, "--reference", ref])
+    assert 0.0 <= info["mse"] < 1e-9
+    # a shorter run is noisier
+    info4 = _run(common + ["--iterations", 2, "--reference", ref])
+    assert info4["mse"] > 1e-6
+    nrc = tmp_path / "nrc.pfm"
+    info_nrc = _run(common + ["--renderer", "NrcPathtracer", "--iterations", 8, "--out", nrc])
+    assert info_nrc["renderer"] == "NrcPathtracer"
+    img = _read_pfm(nrc)
+    assert np.isfinite(img).all() and img.mean() > 0

@@ -1,0 +1,119 @@
+"""Radiance-cache MLP kernels against the NumPy reference (tests/nrc_reference.py).
+
+Bars: the encoding to fp16 resolution; the forward pass to 2 % of the output
+range (fp32 accumulation in a different order, fp16 activations); the loss
+gradient per layer to 5 % in norm and 0.995 cosine similarity; one Adam
+step to the reference update; and training that actually learns.
+"""
+import numpy as np
+import pytest
+
+import nrc_reference as ref
+from gpugi_gb300 import nrc
+
+pytestmark = pytest.mark.gpu
+
+BOX_MIN, BOX_MAX = np.array([-1.0, 0.0, -1.0]), np.array([1.0, 2.0, 1.0])
+
+
+def _queries(rng, n):
+    q = np.concatenate([rng.uniform(BOX_MIN, BOX_MAX, (n, 3)), rng.normal(size=(n, 3)), rng.normal(size=(n, 3)),
+                        rng.uniform(0.1, 0.9, (n, 3))], 1).astype(np.float32)
+    q[:, 3:6] /= np.linalg.norm(q[:, 3:6], axis=1, keepdims=True)
+    q[:, 6:9] /= np.linalg.norm(q[:, 6:9], axis=1, keepdims=True)
+    return q
+
+
+def _target(q):
+    """A smooth radiance field to learn."""
+    p = q[:, 0:3]
+    return np.stack([1.0 + 0.5 * np.sin(3 * p[:, 0]) * q[:, 9], 0.8 + 0.4 * np.cos(2 * p[:, 1] + q[:, 4]),
+                     0.5 + 0.3 * p[:, 2] * q[:, 11]], 1).astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def cache(cuda_ctx):
+    c = nrc.RadianceCache(cuda_ctx, BOX_MIN, BOX_MAX, seed=3)
+    yield c
+    c.close()
+
+
+def test_encoding_matches_reference(cuda_ctx, cache):
+    import torch
+    q = _queries(np.random.default_rng(1), 1000)
+    enc = cache.encode(torch.from_numpy(q).cuda()).float().cpu().numpy()
+    expect = ref.encode(q, BOX_MIN, BOX_MAX)
+    assert np.abs(enc - expect).max() < 2e-3 * max(1.0, np.abs(expect).max())
+
+
+def test_forward_matches_reference(cuda_ctx, cache):
+    import torch
+    rng = np.random.default_rng(2)
+    q = _queries(rng, 4099)  # ragged tile count
+    w = (rng.uniform(-1, 1, nrc.PARAMS) * 0.25).astype(np.float32)
+    cache.set_weights(w)
+    tq = torch.from_numpy(q).cuda()
+    x0 = cache.encode(tq).cpu().numpy()
+    _, out = ref.forward(x0, w)
+    got = cache.infer(tq).cpu().numpy()
+    expect = np.maximum(out[:, :3], 0)
+    assert np.abs(got - expect).max() <= 0.02 * np.abs(expect).max() + 1e-3
+
+
+def test_gradient_matches_reference(cuda_ctx, cache):
+    import torch
+    rng = np.random.default_rng(3)
+    n = 3000
+    q = _queries(rng, n)
+    y = _target(q)
+    w = (rng.uniform(-1, 1, nrc.PARAMS) * 0.2).astype(np.float32)
+    cache.set_weights(w)
+    samples = torch.from_numpy(np.concatenate([q, y], 1)).cuda()
+    x0 = cache.encode(samples[:, :12].contiguous()).cpu().numpy()
+    pred, grad, loss = cache.gradient(samples)
+    rloss, rpred, rgrad = ref.loss_and_grad(x0, w, y)
+    assert abs(loss / rloss - 1) < 0.02
+    assert np.abs(pred - rpred).max() <= 0.02 * np.abs(rpred).max() + 1e-3
+    for l, (i, o) in enumerate(ref.LAYER_SHAPES):
+        a = grad[l * 4096: l * 4096 + i * o]
+        b = rgrad[l * 4096: l * 4096 + i * o]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        cos = float(a @ b) / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
+        assert rel < 0.05 and cos > 0.995, (l, rel, cos)
+
+
+def test_adam_step_matches_reference(cuda_ctx, cache):
+    import torch
+    rng = np.random.default_rng(4)
+    q = _queries(rng, 2048)
+    samples = torch.from_numpy(np.concatenate([q, _target(q)], 1)).cuda()
+    w0 = (rng.uniform(-1, 1, nrc.PARAMS) * 0.2).astype(np.float32)
+    c = nrc.RadianceCache(cuda_ctx, BOX_MIN, BOX_MAX, seed=9, learning_rate=1e-2)
+    c.set_weights(w0)
+    _, g, _ = c.gradient(samples)
+    c.train(samples)
+    w1 = c.weights()
+    m = 0.1 * g
+    v = 0.01 * g * g
+    expect = w0 - 1e-2 * (m / 0.1) / (np.sqrt(v / 0.01) + 1e-8)
+    assert np.allclose(w1, expect, atol=1e-5, rtol=1e-3)
+    c.close()
+
+
+def test_training_learns_a_smooth_field(cuda_ctx):
+    import torch
+    rng = np.random.default_rng(5)
+    c = nrc.RadianceCache(cuda_ctx, BOX_MIN, BOX_MAX, seed=11, learning_rate=1e-2)
+    q_test = _queries(rng, 4096)
+    y_test = _target(q_test)
+    first = None
+    for step in range(300):
+        q = _queries(rng, 16384)
+        loss = c.train(torch.from_numpy(np.concatenate([q, _target(q)], 1)).cuda())
+        if first is None:
+            first = loss
+    pred = c.infer(torch.from_numpy(q_test).cuda()).cpu().numpy()
+    rel = np.sqrt(((pred - y_test) ** 2).mean()) / np.sqrt((y_test ** 2).mean())
+    assert loss < 0.1 * first, (first, loss)
+    assert rel < 0.1, rel
+    c.close()

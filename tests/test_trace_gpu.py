@@ -79,6 +79,28 @@ def test_ellipsoid_bounds_match_oracle_and_bruteforce(cuda_ctx, method):
     ds.close()
 
 
+@pytest.mark.parametrize("shared_nodes", [0, 3, 64, 2048, 7000])
+def test_staged_layouts_give_identical_results(cuda_ctx, icosphere_65536, shared_nodes):
+    """The breadth-first top-level layout and its shared-memory staging change
+    node addresses only: every mode returns the oracle's results."""
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    cuda_ctx.set_scene_layout(shared_nodes, shared_nodes)
+    try:
+        ds = cuda_ctx.upload_scene(b, sc["positions"])
+        rays = scenes.aimed_rays(1 << 17, sc["positions"], seed=77, spread=2.5)
+        o = oracle.trace_closest(b, sc["positions"], rays)
+        oa = oracle.trace_any(b, sc["positions"], rays)["occluded"]
+        for mode in (0, 1, 2):
+            cuda_ctx.set_trace_config(mode=mode)
+            _compare_closest(cuda.trace_closest(cuda_ctx, ds, rays), o)
+            assert np.array_equal(cuda.trace_any(cuda_ctx, ds, rays), oa)
+        ds.close()
+    finally:
+        cuda_ctx.set_trace_config(mode=2)
+        cuda_ctx.set_scene_layout(0, 0)
+
+
 def test_full_size_properties(cuda_ctx, icosphere_65536):
     """2^20 rays of the closest-hit workload: exact against the oracle, and
     size-independent checks (any-hit == closest-hit hit mask, t > 1e-4)."""
