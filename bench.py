@@ -40,7 +40,9 @@ WORKLOAD = ("closest-hit queries: displaced icosphere 65,536 tris (level-6 icosp
 FALLBACK_HBM_GBS = 6800.0
 # Kernels of one step per trace mode (the roofline is taken over the whole step).
 KERNELS = {0: "k_trace_closest<AABB>", 1: "k_trace_persistent<closest, AABB>",
-           2: "k_trace_root_filter<closest, AABB> + k_trace_queue<closest, AABB>"}
+           2: "k_trace_root_filter<closest, AABB> + k_trace_queue<closest, AABB>",
+           3: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 8>",
+           4: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 4>"}
 
 
 def peaks():
@@ -288,13 +290,104 @@ def run_ours(args, world, rank, local):
                          else "fallback 6.8 TB/s",
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3,
                          "kernel": KERNELS[args.trace_mode]},
-            "gpu_launches": args.steps * (2 if args.trace_mode == 2 else 1),
+            "gpu_launches": args.steps * (2 if args.trace_mode >= 2 else 1),
             "clocks": clk.summary()}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(b, sc["positions"], host_batches, seconds=args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ds.close()
+    ctx.close()
+
+
+def run_nrc(args):
+    """Time to equal RMSE, path tracing with the radiance cache vs plain path
+    tracing, on the heightfield workload (522k-triangle fBm terrain + 500
+    boxes, sun of irradiance 5, sky 0.5, Lambertian albedos U[0.1, 0.8],
+    depth 8). RMSE is TextureMSE's, in FP64, against an FP64-accumulated
+    plain-PT image of --nrc-ref-spp samples. Plain PT accumulates 1024 spp
+    (doubling chunks); its final RMSE is the target and its wall time T_pt.
+    The cache path tracer first trains for --nrc-warmup frames (timed, not
+    accumulated), then accumulates frames until its RMSE reaches the target
+    or its time exceeds 3 T_pt. Wall times: host clock around synchronised
+    calls (both renderers synchronise internally)."""
+    from gpugi_gb300 import bvh, cuda, nrc, render, scenes
+    W, H = args.nrc_size
+    depth, sky = 8, (0.5, 0.5, 0.5)
+    ctx = cuda.Context(0)
+    sc = scenes.heightfield_boxes(seed=1)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]), sc["materials"])
+    render.add_directional_light(ds, scenes.HEIGHTFIELD_SUN, (5.0, 5.0, 5.0))
+    cam = render.camera_lookat(*scenes.HEIGHTFIELD_CAMERA, W, H)
+
+    def timed(fn):
+        ctx.sync()
+        t0 = time.perf_counter()
+        fn()
+        ctx.sync()
+        return time.perf_counter() - t0
+
+    conv = render.Image(ctx, W, H, fp64=True)
+    t_ref = timed(lambda: render.render(ctx, ds, cam, conv, "PT", max_path_length=depth, samples=args.nrc_ref_spp,
+                                        iteration=1 << 24, rng_state=[99], sky=sky))
+    ref = (conv.read64() / args.nrc_ref_spp).astype(np.float32)
+    conv.close()
+
+    def rmse(img, n):
+        return float(np.sqrt(img.mse(n, ref, use_fp64=True)))
+
+    pt = render.Image(ctx, W, H, fp64=True)
+    t_pt, spp, pt_curve = 0.0, 0, []
+    for c in [1, 1, 2, 4, 8, 16, 32, 64, 128, 256, 512]:
+        t_pt += timed(lambda: render.render(ctx, ds, cam, pt, "PT", max_path_length=depth, samples=c, iteration=spp,
+                                            rng_state=[7 + spp], sky=sky))
+        spp += c
+        pt_curve.append((spp, round(t_pt, 5), round(rmse(pt, spp), 6)))
+    target = pt_curve[-1][2]
+    pt.close()
+
+    box = ((-1.05, -0.25, -1.05), (1.05, 0.35, 1.05))
+    cache = nrc.RadianceCache(ctx, *box, seed=5)
+    spf = args.nrc_spf
+    opts = dict(max_path_length=depth, sky=sky, terminate_depth=1, train_fraction=args.nrc_train_fraction,
+                train_steps=args.nrc_train_steps, samples_per_frame=spf)
+    scratch = render.Image(ctx, W, H)
+    t_nrc = timed(lambda: nrc.render_nrc(ctx, ds, cam, scratch, cache, samples=args.nrc_warmup * spf,
+                                         iteration=1 << 20, rng_state=[11], **opts))
+    t_warm = t_nrc
+    scratch.close()
+    img = render.Image(ctx, W, H, fp64=True)
+    frames, nrc_curve, reached = 0, [], None
+    at_equal_time = None
+    chunk = 1
+    while t_nrc < 3.0 * t_pt and frames < 4096:
+        t_nrc += timed(lambda: nrc.render_nrc(ctx, ds, cam, img, cache, samples=chunk * spf, iteration=frames * spf,
+                                              rng_state=[13 + frames], **opts))
+        frames += chunk
+        r = rmse(img, frames * spf)
+        nrc_curve.append((frames * spf, round(t_nrc, 5), round(r, 6)))
+        if at_equal_time is None and t_nrc >= t_pt:
+            at_equal_time = r
+        if r <= target:
+            reached = t_nrc
+            break
+        chunk = min(chunk * 2, 16)
+    line = {"metric": "time to the 1024-spp plain-PT RMSE, NRC path tracing vs plain PT", "unit": "ratio",
+            "value": (reached / t_pt) if reached else None, "higher_is_better": False,
+            "t_pt_s": round(t_pt, 4), "t_nrc_s": round(reached, 4) if reached else None,
+            "t_nrc_warmup_s": round(t_warm, 4), "target_rmse": target,
+            "nrc_rmse_at_equal_time": at_equal_time,
+            "config": {"workload": "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8",
+                       "resolution": [W, H], "reference_spp": args.nrc_ref_spp, "reference_s": round(t_ref, 2),
+                       "nrc": {"terminate_depth": 1, "train_fraction": args.nrc_train_fraction,
+                               "train_steps": args.nrc_train_steps, "samples_per_frame": spf,
+                               "warmup_frames": args.nrc_warmup, "max_train_samples": 65536,
+                               "mlp": "64-64x4-3 ReLU fp16, fp32 accumulate, Adam lr 1e-2"}},
+            "pt_curve": pt_curve, "nrc_curve": nrc_curve, "data": "synthetic", "dtype": "f32 paths, f16 MLP"}
+    print(json.dumps(line), flush=True)
+    for x in (img, cache, ds):
+        x.close()
     ctx.close()
 
 
@@ -308,9 +401,23 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--shared-nodes", type=int, default=0,
                     help="top-of-tree nodes staged in shared memory by the walkers")
-    ap.add_argument("--trace-mode", type=int, default=2,
-                    help="0: thread per ray, 1: persistent lane refill, 2: root prefilter + persistent")
+    ap.add_argument("--trace-mode", type=int, default=3,
+                    help="0: thread per ray, 1: persistent lane refill, 2: root prefilter + persistent, "
+                         "3/4: root prefilter + 8/4-lane group walker")
+    ap.add_argument("--workload", choices=["trace", "nrc"], default="trace",
+                    help="trace: the closest-hit headline; nrc: time-to-equal-RMSE of the radiance cache")
+    ap.add_argument("--nrc-size", type=int, nargs=2, default=[640, 360])
+    ap.add_argument("--nrc-ref-spp", type=int, default=16384)
+    ap.add_argument("--nrc-spf", type=int, default=4, help="samples per cache frame")
+    ap.add_argument("--nrc-warmup", type=int, default=32, help="training frames before accumulation")
+    ap.add_argument("--nrc-train-fraction", type=float, default=0.03)
+    ap.add_argument("--nrc-train-steps", type=int, default=2)
     args = ap.parse_args()
+    if args.workload == "nrc":
+        from __graft_entry__ import build
+        build()
+        run_nrc(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup(args)

@@ -18,7 +18,7 @@ struct gpugi_ctx {
     void* stageDev = nullptr;
     size_t stageDevBytes = 0;
     // trace tuning
-    uint32_t traceMode = 2;  // 0 = thread per ray, 1 = persistent lane refill, 2 = root prefilter + 1
+    uint32_t traceMode = 3;  // 0 thread per ray, 1 persistent lane refill, 2 root prefilter + 1, 3/4 + 8/4-lane groups
     uint32_t traceBlock = 128;
     uint32_t sharedNodes = 0;        // top-of-tree nodes laid out first and staged by ray-query walkers
     uint32_t renderSharedNodes = 0;  // nodes staged by the renderer's walkers
@@ -32,6 +32,10 @@ struct gpugi_ctx {
     // wavefront renderer buffers (owned by render.cu)
     void* render = nullptr;
     void (*renderFree)(gpugi_ctx*) = nullptr;
+    // back references (the `ctx` fields) of live scenes, images and caches:
+    // gpugi_destroy clears them, so objects released after their context
+    // only free their own device memory
+    std::vector<gpugi_ctx**> children;
 };
 
 namespace gpugi {
@@ -68,6 +72,22 @@ struct gpugi_scene {
 };
 
 namespace gpugi {
+
+inline void attach_child(gpugi_ctx* ctx, gpugi_ctx** ref) {
+    *ref = ctx;
+    ctx->children.push_back(ref);
+}
+inline void detach_child(gpugi_ctx** ref) {
+    gpugi_ctx* ctx = *ref;
+    if (!ctx) return;
+    for (size_t i = 0; i < ctx->children.size(); ++i)
+        if (ctx->children[i] == ref) {
+            ctx->children[i] = ctx->children.back();
+            ctx->children.pop_back();
+            break;
+        }
+    *ref = nullptr;
+}
 
 // Set ctx->lastError and return the status.
 gpugi_status fail(gpugi_ctx* ctx, gpugi_status st, const std::string& msg);

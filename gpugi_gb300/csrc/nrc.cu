@@ -19,7 +19,10 @@ using namespace gpugi::nrc;
 struct gpugi_nrc {
     gpugi_ctx* ctx = nullptr;
     float3 boxMin, boxInv;
-    float lr = 1e-2f, beta1 = 0.9f, beta2 = 0.99f, eps = 1e-8f, lossScale = 128.0f;
+    // Per-sample output gradients are stored in fp16 unnormalised, times
+    // lossScale (and clamped below the fp16 range); the 1 / (3 n) of the mean
+    // is applied in fp32 after the weight-gradient GEMM.
+    float lr = 1e-2f, beta1 = 0.9f, beta2 = 0.99f, eps = 1e-8f, lossScale = 8.0f;
     uint32_t step = 0;
     float* master = nullptr;   // fp32 [l][in][out]
     float* m = nullptr;
@@ -242,7 +245,7 @@ __global__ void __launch_bounds__(128) k_nrc_fwd_bwd(const float* __restrict__ s
                     const float y = samples[15 * row + 12 + col];
                     const float den = p * p + 0.01f;
                     lossAcc += (p - y) * (p - y) / den;
-                    d = 2.0f * (p - y) / den * invCount * lossScale;
+                    d = fminf(fmaxf(2.0f * (p - y) / den * lossScale, -30000.0f), 30000.0f);
                     if (predOut) predOut[3 * row + col] = p;
                 }
                 dy[j][i] = d;
@@ -458,7 +461,7 @@ gpugi_status gpugi_nrc_create(gpugi_ctx* ctx, const float boxMin[3], const float
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!boxMin || !boxMax || !out) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
     gpugi_nrc* nn = new gpugi_nrc();
-    nn->ctx = ctx;
+    attach_child(ctx, &nn->ctx);
     nn->lr = learningRate > 0.0f ? learningRate : 1e-2f;
     nn->boxMin = make_float3(boxMin[0], boxMin[1], boxMin[2]);
     float ext[3];
@@ -486,12 +489,15 @@ gpugi_status gpugi_nrc_create(gpugi_ctx* ctx, const float boxMin[3], const float
             w[layer_offset(l) + i] = (2.0f * u - 1.0f) * lim;
         }
     }
-    GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(nn->master, w.data(), P * 4, cudaMemcpyHostToDevice, ctx->stream));
-    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(nn->m, 0, P * 4, ctx->stream));
-    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(nn->v, 0, P * 4, ctx->stream));
-    gpugi_status st = nrc_publish(ctx, nn);
-    if (st) return st;
-    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaError_t e = cudaMemcpyAsync(nn->master, w.data(), P * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(nn->m, 0, P * 4, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(nn->v, 0, P * 4, ctx->stream);
+    gpugi_status st = e == cudaSuccess ? nrc_publish(ctx, nn) : cuda_fail(ctx, e, "NRC initialisation");
+    if (!st && (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) st = cuda_fail(ctx, e, "NRC initialisation");
+    if (st) {
+        gpugi_nrc_destroy(nn);
+        return st;
+    }
     *out = nn;
     return GPUGI_OK;
 }
@@ -499,6 +505,7 @@ gpugi_status gpugi_nrc_create(gpugi_ctx* ctx, const float boxMin[3], const float
 void gpugi_nrc_destroy(gpugi_nrc* nn) {
     if (!nn) return;
     if (nn->ctx) cudaStreamSynchronize(nn->ctx->stream);
+    detach_child(&nn->ctx);
     for (void* p : {(void*)nn->master, (void*)nn->m, (void*)nn->v, (void*)nn->grad, (void*)nn->wFwd, (void*)nn->wBwd,
                     (void*)nn->acts, (void*)nn->dys, (void*)nn->lossSum})
         if (p) cudaFree(p);
@@ -573,7 +580,8 @@ gpugi_status gpugi_nrc_train_device(gpugi_ctx* ctx, gpugi_nrc* nn, const float* 
     if (st) return st;
     nn->step++;
     const float c1 = 1.0f - std::pow(nn->beta1, (float)nn->step), c2 = 1.0f - std::pow(nn->beta2, (float)nn->step);
-    k_nrc_adam<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->m, nn->v, nn->grad, 1.0f / nn->lossScale,
+    const float gradScale = 1.0f / (3.0f * (float)n * nn->lossScale);
+    k_nrc_adam<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->m, nn->v, nn->grad, gradScale,
                                                                 nn->lr, nn->beta1, nn->beta2, nn->eps, c1, c2, nn->wFwd,
                                                                 nn->wBwd);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
@@ -593,7 +601,7 @@ gpugi_status gpugi_nrc_gradient_device(gpugi_ctx* ctx, gpugi_nrc* nn, const floa
     GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(gradient, nn->grad, kParams * 4, cudaMemcpyDeviceToHost, ctx->stream));
     if (loss) GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(loss, nn->lossSum, 4, cudaMemcpyDeviceToHost, ctx->stream));
     GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    const float inv = 1.0f / nn->lossScale;
+    const float inv = 1.0f / (3.0f * (float)n * nn->lossScale);
     for (int i = 0; i < kParams; ++i) gradient[i] *= inv;
     return GPUGI_OK;
 }

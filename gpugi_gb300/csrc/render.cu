@@ -654,14 +654,15 @@ __global__ void __launch_bounds__(128) k_bpt_shade(RenderConst rc, PathSoA A, Pa
 // k_camera_generate, plus the choice of training paths (a per-frame hash of
 // the pixel below nrcTrainThreshold) and their buffer slot (kept in lastP).
 __global__ void k_nrc_generate(RenderConst rc, PathSoA A) {
-    const uint32_t total = (uint32_t)rc.numPixels;
+    const uint32_t total = rc.samples * (uint32_t)rc.numPixels;
     if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
-    const uint32_t frame = rc.iteration + rc.sampleBase;
-    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < total; pix += gridDim.x * blockDim.x) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+        const uint32_t s = p / (uint32_t)rc.numPixels, pix = p % (uint32_t)rc.numPixels;
+        const uint32_t frame = rc.iteration + rc.sampleBase + s;
         const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
         uint32_t seed = wanghash(wanghash(frame) + pix);
         const float3 d = primary_direction(rc, seed, x, y);
-        uint32_t info = 0;
+        uint32_t info = s << 8;
         float slotBits = 0.0f;
         if (wanghash(pix ^ wanghash(frame + 0x9E3779B9u)) < rc.nrcTrainThreshold) {
             const uint32_t slot = atomicAdd(rc.trainPaths, 1u);
@@ -671,7 +672,7 @@ __global__ void k_nrc_generate(RenderConst rc, PathSoA A) {
                 rc.tvCount[slot] = 0;
             }
         }
-        store_path(A, pix, rc.camPos, d, f3(1.0f), seed, pix, info, slotBits);
+        store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, info, slotBits);
     }
 }
 
@@ -790,7 +791,11 @@ __global__ void k_nrc_apply(RenderConst rc, const float* __restrict__ radiance) 
 __global__ void k_nrc_targets(RenderConst rc, float* __restrict__ samples, uint32_t* sampleCount, uint32_t cap) {
     const uint32_t paths = min(*rc.trainPaths, rc.trainCap);
     const uint32_t stride = (uint32_t)rc.maxPathLength;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < paths; p += gridDim.x * blockDim.x) {
+    // paths in a shuffled order (multiplication by a prime modulo the count
+    // is a permutation), so a full sample buffer drops paths uniformly
+    const uint64_t offset = wanghash(rc.iteration + rc.sampleBase);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < paths; q += gridDim.x * blockDim.x) {
+        const uint32_t p = (uint32_t)(((uint64_t)q * 2654435761ull + offset) % paths);
         const uint32_t nv = min(rc.tvCount[p], stride);
         float3 S = f3(0.0f);
         for (int k = (int)nv - 1; k >= 0; --k) {
@@ -1250,7 +1255,7 @@ gpugi_status gpugi_image_create(gpugi_ctx* ctx, uint32_t width, uint32_t height,
     if (!out || width == 0 || height == 0 || (uint64_t)width * height > (1ull << 31))
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "bad image size");
     gpugi_image* im = new gpugi_image();
-    im->ctx = ctx;
+    attach_child(ctx, &im->ctx);
     im->width = width;
     im->height = height;
     im->flags = flags;
@@ -1267,6 +1272,7 @@ gpugi_status gpugi_image_create(gpugi_ctx* ctx, uint32_t width, uint32_t height,
 void gpugi_image_destroy(gpugi_image* im) {
     if (!im) return;
     if (im->ctx) cudaStreamSynchronize(im->ctx->stream);
+    detach_child(&im->ctx);
     if (im->rgba) cudaFree(im->rgba);
     if (im->rgb64) cudaFree(im->rgb64);
     delete im;
@@ -1401,17 +1407,20 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     if (!(np->trainFraction >= 0.0f && np->trainFraction <= 1.0f))
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "trainFraction must be in [0, 1]");
     const uint32_t numPixels = p->width * p->height;
-    const size_t lightBytes = (size_t)p->numLightSamples * 32;
-    gpugi_status st = ensure_buffers(ctx, numPixels, 0, lightBytes, 1);
+    const uint32_t spf = std::max<uint32_t>(1u, std::min(np->samplesPerFrame, p->samples));
+    if ((uint64_t)spf * numPixels > (64ull << 20))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "samplesPerFrame x pixels exceeds 64M paths");
+    const uint32_t framePaths = spf * numPixels;
+    const size_t lightBytes = (size_t)spf * p->numLightSamples * 32;
+    gpugi_status st = ensure_buffers(ctx, framePaths, 0, lightBytes, spf);
     if (st) return st;
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
     if ((st = ensure_host_lights(ctx, rb, lightBytes))) return st;
-    const size_t trainCap = (size_t)(np->trainFraction * numPixels * 1.25) + 64;
+    const size_t trainCap = (size_t)(np->trainFraction * framePaths * 1.25) + 64;
     const size_t sampleCap = np->maxTrainSamples ? np->maxTrainSamples : 65536;
-    if ((st = ensure_nrc_buffers(ctx, rb, numPixels, trainCap, p->maxPathLength, sampleCap))) return st;
+    if ((st = ensure_nrc_buffers(ctx, rb, framePaths, trainCap, p->maxPathLength, sampleCap))) return st;
 
     RenderConst rc = make_render_const(ctx, sc, cam, p, im, rb);
-    rc.samples = 1;
     rc.nrcTerminateDepth = (int)np->terminateDepth;
     rc.nrcTrainThreshold = (uint32_t)std::min(4294967295.0, (double)np->trainFraction * 4294967296.0);
     rc.tvRec = rb->tvRec;
@@ -1423,7 +1432,7 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     rc.qT = rb->qT;
     rc.qPixel = rb->qPixel;
     rc.queryCount = rb->nrcCounters;
-    rc.queryCap = numPixels;
+    rc.queryCap = framePaths;
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
     WalkerLaunch LE, LS;
     if ((st = walker_launch_config(ctx, sc, ell ? (const void*)k_extend<1> : (const void*)k_extend<0>, 1ull << 40,
@@ -1436,8 +1445,10 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     const int gridShade = ctx->numSMs * std::max(perSM, 1);
     const int genBlocks = ctx->numSMs * 8;
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
-    for (uint32_t frame = 0; frame < p->samples; ++frame) {
-        if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, frame, 1, p->numLightSamples))) return st;
+    for (uint32_t frame = 0; frame < p->samples; frame += spf) {
+        const uint32_t ns = std::min(spf, p->samples - frame);
+        if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, frame, ns, p->numLightSamples))) return st;
+        rc.samples = ns;
         rc.sampleBase = frame;
         GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), ctx->stream));
         GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->nrcCounters, 0, 64, ctx->stream));
@@ -1456,7 +1467,7 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         uint32_t counts[2] = {0, 0};
         GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(counts, rb->nrcCounters, 8, cudaMemcpyDeviceToHost, ctx->stream));
         GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        const uint32_t nq = std::min<uint32_t>(counts[0], numPixels);
+        const uint32_t nq = std::min<uint32_t>(counts[0], framePaths);
         if (nq) {
             if ((st = gpugi_nrc_infer_device(ctx, nn, rb->queries, nq, rb->radiance))) return st;
             k_nrc_apply<<<ctx->numSMs * 4, 256, 0, ctx->stream>>>(rc, rb->radiance);

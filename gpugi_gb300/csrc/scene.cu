@@ -169,7 +169,7 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     cudaError_t se = cudaSetDevice(ctx->device);
     if (se != cudaSuccess) return cuda_fail(ctx, se, "cudaSetDevice");
     gpugi_scene* sc = new gpugi_scene();
-    sc->ctx = ctx;
+    attach_child(ctx, &sc->ctx);
     sc->numLeafBlocks = numBlocks;
     auto cleanup = [&](gpugi_status st) {
         gpugi_scene_destroy(sc);
@@ -223,6 +223,7 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
 extern "C" void gpugi_scene_destroy(gpugi_scene* sc) {
     if (!sc) return;
     if (sc->ctx) cudaStreamSynchronize(sc->ctx->stream);
+    detach_child(&sc->ctx);
     for (void* p : sc->allocations) cudaFree(p);
     delete sc;
 }

@@ -222,6 +222,164 @@ __global__ void __launch_bounds__(128) k_trace_queue(
     }
 }
 
+// Group walker (modes 3 and 4), second launch after the root prefilter: G
+// lanes walk one ray together. A node round tests the G consecutive nodes
+// [node, node + G) of the preorder array (one coalesced 32G-byte load), then
+// resolves which of them the sequential walk visits by pointer jumping over
+// the in-window successors (log2 G shuffles): the walk leaves the window at
+// a node outside it, at the end of the escape chain, or at a hit leaf. A leaf
+// round tests G slots of the leaf block at once and applies the sequential
+// acceptance rule (a slot is accepted when hit < rayLength, so the result is
+// the first slot reaching the minimum; any hit: the first accepted slot).
+// Every node decision uses the same arithmetic and the same rayLength as in
+// trace_ray, so results are identical; tests of nodes the walk skips are
+// discarded. A round advances one ray by several of trace_ray's steps, which
+// shortens the dependent fetch chain of the longest walks.
+template <bool ANY_HIT, int BOUNDS, int G>
+__global__ void __launch_bounds__(128) k_trace_group(
+    DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
+    const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
+    const float* __restrict__ tmax, int32_t* __restrict__ slot, float* __restrict__ t, float* __restrict__ u,
+    float* __restrict__ v, uint8_t* __restrict__ occluded, const uint32_t* __restrict__ queue,
+    unsigned long long* counters, uint32_t* err) {
+    static_assert(G == 4 || G == 8 || G == 16, "group size");
+    constexpr uint32_t kDone = 0xFFFFFFFFu, kLeafMark = 0x80000000u;
+    const uint64_t n = counters[1];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned gl = lane & (G - 1), gbase = lane & ~(unsigned)(G - 1);
+    const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << gbase;
+    float3 o = make_float3(0.0f, 0.0f, 0.0f), d = o, inv = o;
+    float len = 0.0f, bu = 0.0f, bv = 0.0f;
+    int32_t best = -1;
+    uint32_t node = 0, cur = 0, end = 0, resume = kDone, budget = 0, ray = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        // refill: one atomic per warp for all groups that need a ray
+        const bool need = !active && !exhausted;
+        const unsigned needMask = __ballot_sync(0xffffffffu, need && gl == 0);
+        if (needMask) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(counters + 2, (unsigned long long)__popc(needMask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (need) {
+                const uint64_t my = base + (uint64_t)__popc(needMask & ((1u << gbase) - 1u));
+                if (my < n) {
+                    ray = __ldg(queue + my);
+                    o = make_float3(__ldg(ox + ray), __ldg(oy + ray), __ldg(oz + ray));
+                    d = make_float3(__ldg(dx + ray), __ldg(dy + ray), __ldg(dz + ray));
+                    inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
+                    len = __ldg(tmax + ray);
+                    best = -1;
+                    bu = bv = 0.0f;
+                    node = 0;
+                    cur = end = 0;
+                    resume = kDone;
+                    budget = s.numNodes;
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (!active) continue;
+        bool finished = false;
+        if (cur < end) {
+            // leaf round: slots [cur, min(cur + G, end))
+            const uint32_t k = cur + gl;
+            float h = 0.0f, by = 0.0f, bz = 0.0f;
+            bool ok = false;
+            if (k < end) ok = intersect_triangle(o, d, s.tris + 3 * (size_t)k, h, by, bz) && h < len;
+            if (ANY_HIT) {
+                uint32_t key = ok ? k : kDone;
+#pragma unroll
+                for (int off = G / 2; off > 0; off >>= 1) key = min(key, __shfl_xor_sync(gmask, key, off));
+                if (key != kDone) {
+                    best = (int32_t)key;
+                    finished = true;
+                }
+            } else {
+                unsigned long long key = ok ? ((unsigned long long)__float_as_uint(h) << 32) | k : ~0ull;
+#pragma unroll
+                for (int off = G / 2; off > 0; off >>= 1) {
+                    const unsigned long long other = __shfl_xor_sync(gmask, key, off);
+                    key = other < key ? other : key;
+                }
+                const uint32_t win = (uint32_t)key;
+                const unsigned src = gbase + ((key != ~0ull) ? (win - cur) : 0u);
+                const float wu = __shfl_sync(gmask, by, src), wv = __shfl_sync(gmask, bz, src);
+                if (key != ~0ull) {
+                    best = (int32_t)win;
+                    len = __uint_as_float((uint32_t)(key >> 32));
+                    bu = wu;
+                    bv = wv;
+                }
+            }
+            cur = min(cur + G, end);
+            if (!finished && cur >= end) {
+                node = resume;
+                if (node == kDone) finished = true;
+            }
+        } else {
+            // node round: nodes [node, node + G)
+            if (budget-- == 0) {
+                raise_error(err, DEVERR_TRAVERSAL_CAP);
+                finished = true;
+            } else {
+                const uint32_t p = node + gl;
+                uint32_t next = kDone, child = 0, escape = 0;
+                if (p < s.numNodes) {
+                    const float4 a = __ldg(s.nodes + 2 * (size_t)p), b = __ldg(s.nodes + 2 * (size_t)p + 1);
+                    child = __float_as_uint(a.w);
+                    escape = __float_as_uint(b.w);
+                    float firstHit;
+                    bool hit;
+                    if (BOUNDS == 0) hit = intersect_box(o, inv, a, b, firstHit);
+                    else hit = intersect_ellipsoid(o, d, a, b, firstHit);
+                    if (hit && firstHit <= len) next = (child & LEAF_FLAG) ? (kLeafMark | gl) : child;
+                    else next = escape ? escape : kDone;
+                }
+                // pointer jumping over successors inside the window
+#pragma unroll
+                for (int r = 1; r < G; r <<= 1) {
+                    const bool chase = next < kLeafMark && next - node < (uint32_t)G;
+                    const uint32_t w = __shfl_sync(gmask, next, gbase + (chase ? next - node : gl));
+                    next = chase ? w : next;
+                }
+                const uint32_t r0 = __shfl_sync(gmask, next, gbase);
+                if (r0 == kDone) {
+                    finished = true;
+                } else if (r0 & kLeafMark) {
+                    const unsigned src = gbase + (r0 & (kLeafMark - 1u));
+                    const uint32_t lc = __shfl_sync(gmask, child, src), le = __shfl_sync(gmask, escape, src);
+                    cur = (lc & LEAF_BLOCK_MASK) * s.leafSize;
+                    end = cur + ((lc >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK);
+                    resume = le ? le : kDone;
+                    if (cur >= end) {  // empty leaf block
+                        node = resume;
+                        if (node == kDone) finished = true;
+                    }
+                } else {
+                    node = r0;
+                }
+            }
+        }
+        if (finished) {
+            if (gl == 0) {
+                if (ANY_HIT) {
+                    occluded[ray] = best >= 0 ? 1 : 0;
+                } else {
+                    slot[ray] = best;
+                    t[ray] = len;
+                    u[ray] = bu;
+                    v[ray] = bv;
+                }
+            }
+            active = false;
+        }
+    }
+}
+
 gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
                                    const float* oy, const float* oz, const float* dx, const float* dy,
                                    const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
@@ -257,6 +415,25 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         else GPUGI_FILTER_ON(false, 1);
     }
 #undef GPUGI_FILTER_ON
+    if (ctx->traceMode == 3 || ctx->traceMode == 4) {
+        void (*kg)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
+                   const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
+                   uint32_t*);
+        if (ctx->traceMode == 3) {
+            if (!ell) kg = anyHit ? k_trace_group<true, 0, 8> : k_trace_group<false, 0, 8>;
+            else kg = anyHit ? k_trace_group<true, 1, 8> : k_trace_group<false, 1, 8>;
+        } else {
+            if (!ell) kg = anyHit ? k_trace_group<true, 0, 4> : k_trace_group<false, 0, 4>;
+            else kg = anyHit ? k_trace_group<true, 1, 4> : k_trace_group<false, 1, 4>;
+        }
+        WalkerLaunch L;
+        gpugi_status st = walker_launch_config(ctx, sc, (const void*)kg, 1ull << 40, 0, L);
+        if (st) return st;
+        kg<<<L.grid, 128, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded, queue,
+                                           counters, ctx->errWord);
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+        return GPUGI_OK;
+    }
     void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
               const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
               uint32_t*, uint32_t);
@@ -322,7 +499,7 @@ gpugi_status launch_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const f
                                   const float* tmax, uint64_t n, int32_t* slot, float* t, float* u, float* v) {
     if (n == 0) return GPUGI_OK;
     if (n > (uint64_t)0xFFFFFFFFu * 256u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many rays");
-    if (ctx->traceMode == 2)
+    if (ctx->traceMode >= 2)
         return launch_trace_filtered(ctx, sc, false, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, nullptr);
     if (ctx->traceMode == 1)
         return launch_trace_persistent(ctx, sc, false, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, nullptr);
@@ -342,7 +519,7 @@ gpugi_status launch_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float
                               const float* tmax, uint64_t n, uint8_t* occluded) {
     if (n == 0) return GPUGI_OK;
     if (n > (uint64_t)0xFFFFFFFFu * 256u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many rays");
-    if (ctx->traceMode == 2)
+    if (ctx->traceMode >= 2)
         return launch_trace_filtered(ctx, sc, true, ox, oy, oz, dx, dy, dz, tmax, n, nullptr, nullptr, nullptr,
                                      nullptr, occluded);
     if (ctx->traceMode == 1)

@@ -5,7 +5,9 @@ fallback. Loading fails loudly when the library is missing.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -65,6 +67,25 @@ def _declare(L):
 _EXTRA_DECLS: dict = {}
 
 
+# Live handles, closed at interpreter exit in dependency order (caches,
+# images and scenes before their contexts) while the library and the CUDA
+# runtime are still loaded.
+_LIVE: "weakref.WeakKeyDictionary" = weakref.WeakKeyDictionary()
+
+
+def _register(obj, rank: int) -> None:
+    _LIVE[obj] = rank
+
+
+@atexit.register
+def _close_all() -> None:
+    for obj, _ in sorted(list(_LIVE.items()), key=lambda kv: kv[1]):
+        try:
+            obj.close()
+        except Exception:
+            pass
+
+
 def _ptr(a):
     """Pointer of a numpy array or a torch tensor (host or device)."""
     if a is None:
@@ -86,6 +107,7 @@ class Context:
         st = lib().gpugi_create(C.byref(self._h), C.byref(opts))
         if st != 0:
             raise GpugiError(st, "gpugi_create failed (no CUDA device?)")
+        _register(self, 3)
 
     @property
     def handle(self):
@@ -107,7 +129,7 @@ class Context:
     def stream(self) -> int:
         return lib().gpugi_stream(self._h) or 0
 
-    def set_trace_config(self, mode: int = 2, block_size: int = 128):
+    def set_trace_config(self, mode: int = 3, block_size: int = 128):
         self.check(lib().gpugi_set_trace_config(self._h, mode, block_size))
 
     def set_scene_layout(self, shared_nodes: int = 0, render_shared_nodes: int = 0):
@@ -156,6 +178,7 @@ class DeviceScene:
                                       slots.shape[0], bvh.leaf_size, _ptr(pos), _ptr(vi), pos.shape[0], _ptr(mats),
                                       nm, C.byref(self._h))
         ctx.check(st)
+        _register(self, 2)
         self.num_nodes = hier.shape[0]
         self.num_slots = slots.shape[0]
 

@@ -35,7 +35,7 @@ def _declare():
 
 class NrcParams(C.Structure):
     _fields_ = [("terminateDepth", C.c_uint32), ("trainFraction", C.c_float), ("maxTrainSamples", C.c_uint32),
-                ("trainSteps", C.c_uint32), ("train", C.c_uint32)]
+                ("trainSteps", C.c_uint32), ("train", C.c_uint32), ("samplesPerFrame", C.c_uint32)]
 
 
 def _torch_to_ctx():
@@ -62,6 +62,7 @@ class RadianceCache:
         bmin = (C.c_float * 3)(*map(float, box_min))
         bmax = (C.c_float * 3)(*map(float, box_max))
         ctx.check(L.gpugi_nrc_create(ctx.handle, bmin, bmax, seed, float(learning_rate), C.byref(self._h)))
+        cuda._register(self, 0)
 
     @property
     def handle(self):
@@ -133,7 +134,8 @@ def render_nrc(ctx: cuda.Context, scene: cuda.DeviceScene, camera, image, cache:
                max_path_length: int = 8, samples: int = 1, iteration: int = 0, num_light_samples: int = 128,
                sky=(0.0, 0.0, 0.0), rr_start_depth: int = 0, light_samples: np.ndarray | None = None,
                rng_state: list | None = None, terminate_depth: int = 1, train_fraction: float = 0.03,
-               max_train_samples: int = 65536, train_steps: int = 1, train: bool = True) -> None:
+               max_train_samples: int = 65536, train_steps: int = 1, train: bool = True,
+               samples_per_frame: int = 1) -> None:
     """`samples` frames of path tracing with the radiance cache (gpugi_render_nrc)."""
     from . import render
     L = _declare()
@@ -142,7 +144,8 @@ def render_nrc(ctx: cuda.Context, scene: cuda.DeviceScene, camera, image, cache:
     ls = None if light_samples is None else np.ascontiguousarray(light_samples, dtype=np.float32)
     if ls is not None:
         assert ls.shape == (samples, num_light_samples, 8)
-    q = NrcParams(terminate_depth, float(train_fraction), max_train_samples, train_steps, int(bool(train)))
+    q = NrcParams(terminate_depth, float(train_fraction), max_train_samples, train_steps, int(bool(train)),
+                  samples_per_frame)
     st = C.c_uint64(rng_state[0] if rng_state else 0)
     ctx.check(L.gpugi_render_nrc(ctx.handle, scene.handle, C.byref(camera), C.byref(p), cuda._ptr(ls),
                                  C.byref(st) if ls is None else None, cache.handle, C.byref(q), image.handle))

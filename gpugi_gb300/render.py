@@ -75,6 +75,7 @@ class Image:
         self.fp64 = fp64
         self._h = C.c_void_p()
         ctx.check(_declare().gpugi_image_create(ctx.handle, width, height, 1 if fp64 else 0, C.byref(self._h)))
+        cuda._register(self, 1)
 
     @property
     def handle(self):

@@ -339,3 +339,96 @@ def cornell_room(seed: int = 1, sphere_level: int = 6, wall_grid: int = 40, ligh
     f = np.concatenate(parts_f)
     n = np.concatenate(parts_n)
     return _pack(v, f, np.stack(mats), material_ids=np.concatenate(mat_ids), normals=n)
+
+
+def _value_noise(rs: Stream, n: int, cells: int) -> np.ndarray:
+    """Bilinearly interpolated lattice noise in [-1, 1] on an n x n grid over [0, 1]^2."""
+    lattice = rs.uniform((cells + 1) * (cells + 1), -1.0, 1.0).reshape(cells + 1, cells + 1)
+    t = np.linspace(0.0, cells, n)
+    i = np.minimum(t.astype(np.int64), cells - 1)
+    f = t - i
+    f = f * f * (3.0 - 2.0 * f)  # smoothstep fade
+    a = lattice[i][:, i]
+    b = lattice[i][:, i + 1]
+    c = lattice[i + 1][:, i]
+    d = lattice[i + 1][:, i + 1]
+    fx, fz = f[:, None], f[None, :]
+    return (a * (1 - fz) + b * fz) * (1 - fx) + (c * (1 - fz) + d * fz) * fx
+
+
+def _flat_box(half: float):
+    """Axis-aligned cube of half-size `half` about the origin: 6 faces of 4
+    own vertices (flat shading normals), 12 outward triangles."""
+    vs, fs, ns = [], [], []
+    for axis in range(3):
+        for sign in (-1.0, 1.0):
+            nrm = np.zeros(3)
+            nrm[axis] = sign
+            ua, va = [a for a in range(3) if a != axis]
+            eu = np.zeros(3)
+            ev = np.zeros(3)
+            eu[ua] = 2 * half
+            ev[va] = 2 * half
+            if np.dot(np.cross(eu, ev), nrm) < 0:
+                eu, ev = ev, eu
+            o = nrm * half - (eu + ev) / 2
+            v, f, n = _grid_quad(o, eu, ev, 1)
+            fs.append(f + 4 * len(vs))
+            vs.append(v)
+            ns.append(n)
+    return np.concatenate(vs), np.concatenate(fs), np.concatenate(ns)
+
+
+HEIGHTFIELD_CAMERA = ((0.0, 0.55, 1.35), (0.0, 0.0, -0.1), (0.0, 1.0, 0.0), 50.0)
+HEIGHTFIELD_SUN = (0.45, 0.8, 0.4)   # towards the sun (normalised by the library)
+
+
+def heightfield_boxes(seed: int = 1, grid: int = 512, amplitude: float = 0.2, num_boxes: int = 500,
+                      octaves: int = 6):
+    """The radiance-cache workload: a grid x grid-vertex fBm heightfield over
+    [-1, 1]^2 (2 (grid-1)^2 triangles: 522,242 for 512) with heights scaled
+    to +-amplitude, plus num_boxes boxes (side U[0.02, 0.08], rotated about
+    y) standing on it. Lambertian albedos U[0.1, 0.8]^3: one material for the
+    terrain, one per box. Lit by a directional sun (HEIGHTFIELD_SUN,
+    irradiance 5) and a constant sky of 0.5 (renderer parameters).
+    Camera: HEIGHTFIELD_CAMERA."""
+    rs = Stream(seed, 11)
+    h = np.zeros((grid, grid))
+    amp, cells = 1.0, 4
+    for _ in range(octaves):
+        h += amp * _value_noise(rs, grid, cells)
+        amp *= 0.5
+        cells *= 2
+    h *= amplitude / max(np.abs(h).max(), 1e-9)
+    xs = np.linspace(-1.0, 1.0, grid)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    tv = np.stack([X, h, Z], -1).reshape(-1, 3)
+    a = (np.arange(grid - 1)[:, None] * grid + np.arange(grid - 1)[None, :]).reshape(-1)
+    # winding with +y normals: (a, a+1, a+grid+1), (a, a+grid+1, a+grid)
+    tf = np.concatenate([np.stack([a, a + 1, a + grid + 1], 1), np.stack([a, a + grid + 1, a + grid], 1)])
+    tn = vertex_normals(tv, tf)
+    if tn[:, 1].mean() < 0:
+        tf = tf[:, ::-1].copy()
+        tn = -tn
+    parts_v, parts_f, parts_n, ids = [tv], [tf], [tn], [np.zeros(len(tf), np.uint32)]
+    mats = [lambert(tuple(rs.uniform(3, 0.1, 0.8)))]
+    base = tv.shape[0]
+    pos = rs.uniform(2 * num_boxes, -0.9, 0.9).reshape(num_boxes, 2)
+    side = rs.uniform(num_boxes, 0.02, 0.08)
+    ang = rs.uniform(num_boxes, 0.0, 2 * math.pi)
+    for k in range(num_boxes):
+        gi = int(round((pos[k, 0] + 1.0) * 0.5 * (grid - 1)))
+        gk = int(round((pos[k, 1] + 1.0) * 0.5 * (grid - 1)))
+        y0 = h[gi, gk]
+        c, s = math.cos(ang[k]), math.sin(ang[k])
+        rot = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+        v, f, n = _flat_box(side[k] * 0.5)
+        v = v @ rot.T + np.array([pos[k, 0], y0 + 0.4 * side[k], pos[k, 1]])
+        parts_v.append(v)
+        parts_f.append(f + base)
+        parts_n.append(n @ rot.T)
+        ids.append(np.full(len(f), len(mats), np.uint32))
+        mats.append(lambert(tuple(rs.uniform(3, 0.1, 0.8))))
+        base += v.shape[0]
+    return _pack(np.concatenate(parts_v), np.concatenate(parts_f), np.stack(mats), material_ids=np.concatenate(ids),
+                 normals=np.concatenate(parts_n))

@@ -157,10 +157,13 @@ gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* scene,
 
 /* Traversal tuning (set by the autotuner). mode 0: one thread per ray, grid
  * of ceil(n / blockSize) blocks; mode 1: persistent warps that refill
- * finished lanes from a device ray counter; mode 2 (default): a coalesced
+ * finished lanes from a device ray counter; mode 2: a coalesced
  * root-bounds prefilter that finishes rays missing the scene and queues the
- * rest (warp-ballot compaction) for the persistent walker. All modes perform
- * the same tests per ray and return identical results. */
+ * rest (warp-ballot compaction) for the persistent walker; modes 3
+ * (default) and 4: the same prefilter, then groups of 8 (mode 3) or 4 (mode 4) lanes walk one
+ * ray together, testing a window of consecutive preorder nodes or leaf slots
+ * per round. All modes make the same decisions per ray as TraceRay and
+ * return identical results. blockSize applies to mode 0. */
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize);
 
 /* Scene layout tuning (set by the autotuner), applied to scenes uploaded
@@ -279,20 +282,23 @@ gpugi_status gpugi_nrc_gradient_device(gpugi_ctx* ctx, gpugi_nrc* nrc, const flo
 gpugi_status gpugi_nrc_encode_device(gpugi_ctx* ctx, const gpugi_nrc* nrc, const float* queries, uint64_t n,
                                      void* encodedHalf);
 
-/* Path tracing with the radiance cache (params->pass must be PT). Each of
- * params->samples frames: camera paths of the non-training pixels stop at
- * vertex terminateDepth and add throughput x cache(vertex); a trainFraction
- * of the pixels (chosen by a per-frame hash) trace full PT paths whose
- * vertices become training samples {query, radiance reflected towards the
- * previous vertex}; after the frame's lookups, trainSteps Adam steps run on
- * those samples (when train != 0). Both kinds of path splat into image.
- * Synchronises twice per frame (query and sample counts). */
+/* Path tracing with the radiance cache (params->pass must be PT).
+ * params->samples iterations run as frames of samplesPerFrame iterations
+ * (one wavefront each). Camera paths stop at vertex terminateDepth and add
+ * throughput x cache(vertex), except a trainFraction of the paths (chosen by
+ * a hash of pixel and iteration) that trace full PT paths whose vertices
+ * become training samples {query, radiance reflected towards the previous
+ * vertex}; after the frame's lookups, trainSteps Adam steps run on those
+ * samples (at most maxTrainSamples, drawn in a shuffled path order) when
+ * train != 0. Both kinds of path splat into image. Synchronises twice per
+ * frame (query and sample counts). */
 typedef struct gpugi_nrc_params {
     uint32_t terminateDepth;  /* vertex index (0 = first hit) where render paths query the cache */
     float trainFraction;      /* share of pixels tracing training paths, in [0, 1] */
     uint32_t maxTrainSamples; /* cap on samples per frame (0: 65536) */
     uint32_t trainSteps;      /* Adam steps per frame on all of the frame's samples (0 counts as 1) */
     uint32_t train;           /* 0: use the cache without updating it */
+    uint32_t samplesPerFrame; /* samples (iterations) traced per frame, one wavefront (0 counts as 1) */
 } gpugi_nrc_params;
 
 gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* scene, const gpugi_camera* camera,
