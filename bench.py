@@ -42,7 +42,8 @@ FALLBACK_HBM_GBS = 6800.0
 KERNELS = {0: "k_trace_closest<AABB>", 1: "k_trace_persistent<closest, AABB>",
            2: "k_trace_root_filter<closest, AABB> + k_trace_queue<closest, AABB>",
            3: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 8>",
-           4: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 4>"}
+           4: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 4>",
+           5: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 16>"}
 
 
 def peaks():

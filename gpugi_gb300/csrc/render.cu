@@ -171,51 +171,81 @@ GPUGI_D void persistent_walks(const DevScene& s, uint32_t n, unsigned long long*
     }
 }
 
-template <int BOUNDS>
+// Closest hits of the path queue. GROUP: 8-lane group walks (group_walks),
+// otherwise one lane per ray with the top nodes staged in shared memory.
+template <int BOUNDS, bool GROUP>
 __global__ void __launch_bounds__(128) k_extend(RenderConst rc, PathSoA A, HitSoA H, int depth, uint32_t stage) {
     const uint32_t n = rc.cnt->path[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&rc.cnt->rays[0], (unsigned long long)n);
-    persistent_walks<false, BOUNDS>(
-        rc.s, n, &rc.cnt->extendWork[depth], rc.err,
-        [&](uint32_t i, float3& o, float3& d, float& tmax) {
-            o = make_float3(A.ox[i], A.oy[i], A.oz[i]);
-            d = make_float3(A.dx[i], A.dy[i], A.dz[i]);
-            tmax = kRAY_MAX;
-        },
-        [&](uint32_t i, const WalkState& w) {
-            H.slot[i] = w.slot;
-            H.t[i] = w.len;
-            H.u[i] = w.u;
-            H.v[i] = w.v;
-        },
-        stage);
+    auto load = [&](auto i, float3& o, float3& d, float& tmax) {
+        o = make_float3(A.ox[i], A.oy[i], A.oz[i]);
+        d = make_float3(A.dx[i], A.dy[i], A.dz[i]);
+        tmax = kRAY_MAX;
+    };
+    if constexpr (GROUP) {
+        group_walks<false, BOUNDS, 8>(rc.s, n, &rc.cnt->extendWork[depth], rc.err, load,
+                                      [&](uint64_t i, const GroupWalk& g) {
+                                          H.slot[i] = g.slot;
+                                          H.t[i] = g.len;
+                                          H.u[i] = g.u;
+                                          H.v[i] = g.v;
+                                      });
+    } else {
+        persistent_walks<false, BOUNDS>(
+            rc.s, n, &rc.cnt->extendWork[depth], rc.err, load,
+            [&](uint32_t i, const WalkState& w) {
+                H.slot[i] = w.slot;
+                H.t[i] = w.len;
+                H.u[i] = w.u;
+                H.v[i] = w.v;
+            },
+            stage);
+    }
 }
 
-template <int BOUNDS>
+// Shadow rays: unoccluded contributions are splatted (and added to their
+// radiance-cache training vertex).
+GPUGI_D void shadow_unoccluded(const RenderConst& rc, const ShadowSoA& Q, uint32_t i) {
+    const float3 c = make_float3(Q.cr[i], Q.cg[i], Q.cb[i]);
+    splat(rc, Q.pixel[i], c);
+    const uint32_t tr = Q.train[i];
+    if (tr != kNoTrain) {
+        atomicAdd(rc.tvC + 3 * (size_t)tr, c.x);
+        atomicAdd(rc.tvC + 3 * (size_t)tr + 1, c.y);
+        atomicAdd(rc.tvC + 3 * (size_t)tr + 2, c.z);
+    }
+}
+
+template <int BOUNDS, bool GROUP>
 __global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int depth, uint32_t stage) {
     const uint32_t n = rc.cnt->shadow[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&rc.cnt->rays[1], (unsigned long long)n);
-    persistent_walks<true, BOUNDS>(
-        rc.s, n, &rc.cnt->shadowWork[depth], rc.err,
-        [&](uint32_t i, float3& o, float3& d, float& tmax) {
-            o = make_float3(Q.ox[i], Q.oy[i], Q.oz[i]);
-            d = make_float3(Q.dx[i], Q.dy[i], Q.dz[i]);
-            tmax = Q.tmax[i];
-        },
-        [&](uint32_t i, const WalkState& w) {
-            if (w.slot < 0) {
-                const float3 c = make_float3(Q.cr[i], Q.cg[i], Q.cb[i]);
-                splat(rc, Q.pixel[i], c);
-                const uint32_t tr = Q.train[i];
-                if (tr != kNoTrain) {  // radiance-cache training vertex accumulator
-                    atomicAdd(rc.tvC + 3 * (size_t)tr, c.x);
-                    atomicAdd(rc.tvC + 3 * (size_t)tr + 1, c.y);
-                    atomicAdd(rc.tvC + 3 * (size_t)tr + 2, c.z);
-                }
-            }
-        },
-        stage);
+    auto load = [&](auto i, float3& o, float3& d, float& tmax) {
+        o = make_float3(Q.ox[i], Q.oy[i], Q.oz[i]);
+        d = make_float3(Q.dx[i], Q.dy[i], Q.dz[i]);
+        tmax = Q.tmax[i];
+    };
+    if constexpr (GROUP) {
+        group_walks<true, BOUNDS, 8>(rc.s, n, &rc.cnt->shadowWork[depth], rc.err, load,
+                                     [&](uint64_t i, const GroupWalk& g) {
+                                         if (g.slot < 0) shadow_unoccluded(rc, Q, (uint32_t)i);
+                                     });
+    } else {
+        persistent_walks<true, BOUNDS>(
+            rc.s, n, &rc.cnt->shadowWork[depth], rc.err, load,
+            [&](uint32_t i, const WalkState& w) {
+                if (w.slot < 0) shadow_unoccluded(rc, Q, i);
+            },
+            stage);
+    }
 }
+
+// Launch shapes and launches of the walkers for a scene: group walks when the
+// context's trace mode is 3 or 4, else lane walks with staged top nodes.
+struct Walkers {
+    bool ell = false, group = false;
+    WalkerLaunch LE, LS;
+};
 
 // ------------------------------------------------------------ generation
 // Primary ray (pathtracer.comp:132-139) in exact IEEE operations, so camera
@@ -883,65 +913,25 @@ __global__ void k_batch_generate(const RenderConst* __restrict__ jobs, const uin
     }
 }
 
-// persistent_walks over rays of different scenes: load() returns the ray's
-// scene, whose bounds kind selects the node test per step.
-template <bool ANY_HIT, typename Load, typename Finish>
-GPUGI_D void persistent_walks_multi(uint32_t n, unsigned long long* work, uint32_t* err, Load load, Finish finish) {
-    const unsigned lane = threadIdx.x & 31u;
-    WalkState w;
-    const DevScene* sc = nullptr;
-    uint32_t ray = 0;
-    bool active = false, exhausted = false;
-    while (true) {
-        const bool need = !active && !exhausted;
-        const unsigned needMask = __ballot_sync(0xffffffffu, need);
-        if (needMask) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(work, (unsigned long long)__popc(needMask));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (need) {
-                const unsigned long long my = base + (unsigned long long)__popc(needMask & ((1u << lane) - 1u));
-                if (my < n) {
-                    ray = (uint32_t)my;
-                    float3 o, d;
-                    float tmax;
-                    sc = load(ray, o, d, tmax);
-                    walk_begin(w, *sc, o, d, tmax);
-                    active = true;
-                } else {
-                    exhausted = true;
-                }
-            }
-        }
-        if (!__any_sync(0xffffffffu, active)) break;
-        if (active) {
-            const bool done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? walk_step<ANY_HIT, 1>(w, *sc, err)
-                                                                      : walk_step<ANY_HIT, 0>(w, *sc, err);
-            if (done) {
-                finish(ray, w);
-                active = false;
-            }
-        }
-    }
-}
-
+// Walks of rays of several scenes: 8-lane group walks (group_walks_multi);
+// each item's scene comes from its job.
 __global__ void __launch_bounds__(128) k_batch_extend(const RenderConst* __restrict__ jobs, Counters* cnt,
                                                       uint32_t* err, PathSoA A, HitSoA H, int depth) {
     const uint32_t n = cnt->path[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays[0], (unsigned long long)n);
-    persistent_walks_multi<false>(
+    group_walks_multi<false, 8>(
         n, &cnt->extendWork[depth], err,
-        [&](uint32_t i, float3& o, float3& d, float& tmax) -> const DevScene* {
+        [&](uint64_t i, float3& o, float3& d, float& tmax) -> const DevScene* {
             o = make_float3(A.ox[i], A.oy[i], A.oz[i]);
             d = make_float3(A.dx[i], A.dy[i], A.dz[i]);
             tmax = kRAY_MAX;
             return &jobs[A.job[i]].s;
         },
-        [&](uint32_t i, const WalkState& w) {
-            H.slot[i] = w.slot;
-            H.t[i] = w.len;
-            H.u[i] = w.u;
-            H.v[i] = w.v;
+        [&](uint64_t i, const GroupWalk& g) {
+            H.slot[i] = g.slot;
+            H.t[i] = g.len;
+            H.u[i] = g.u;
+            H.v[i] = g.v;
         });
 }
 
@@ -949,16 +939,16 @@ __global__ void __launch_bounds__(128) k_batch_shadow(const RenderConst* __restr
                                                       uint32_t* err, ShadowSoA Q, int depth) {
     const uint32_t n = cnt->shadow[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays[1], (unsigned long long)n);
-    persistent_walks_multi<true>(
+    group_walks_multi<true, 8>(
         n, &cnt->shadowWork[depth], err,
-        [&](uint32_t i, float3& o, float3& d, float& tmax) -> const DevScene* {
+        [&](uint64_t i, float3& o, float3& d, float& tmax) -> const DevScene* {
             o = make_float3(Q.ox[i], Q.oy[i], Q.oz[i]);
             d = make_float3(Q.dx[i], Q.dy[i], Q.dz[i]);
             tmax = Q.tmax[i];
             return &jobs[Q.job[i]].s;
         },
-        [&](uint32_t i, const WalkState& w) {
-            if (w.slot < 0) splat(jobs[Q.job[i]], Q.pixel[i], make_float3(Q.cr[i], Q.cg[i], Q.cb[i]));
+        [&](uint64_t i, const GroupWalk& g) {
+            if (g.slot < 0) splat(jobs[Q.job[i]], Q.pixel[i], make_float3(Q.cr[i], Q.cg[i], Q.cb[i]));
         });
 }
 
@@ -1091,15 +1081,52 @@ static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheByt
     return GPUGI_OK;
 }
 
+static gpugi_status walkers_config(gpugi_ctx* ctx, const gpugi_scene* sc, Walkers& W) {
+    W.ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    W.group = ctx->traceMode >= 3;
+    const void *ke, *ks;
+    if (W.group) {
+        ke = W.ell ? (const void*)k_extend<1, true> : (const void*)k_extend<0, true>;
+        ks = W.ell ? (const void*)k_shadow<1, true> : (const void*)k_shadow<0, true>;
+    } else {
+        ke = W.ell ? (const void*)k_extend<1, false> : (const void*)k_extend<0, false>;
+        ks = W.ell ? (const void*)k_shadow<1, false> : (const void*)k_shadow<0, false>;
+    }
+    const uint32_t stage = W.group ? 0 : ctx->renderSharedNodes;
+    gpugi_status st = walker_launch_config(ctx, sc, ke, 1ull << 40, stage, W.LE);
+    if (!st) st = walker_launch_config(ctx, sc, ks, 1ull << 40, stage, W.LS);
+    return st;
+}
+
+static void launch_extend(gpugi_ctx* ctx, const Walkers& W, const RenderConst& rc, const PathSoA& A, const HitSoA& H,
+                          int depth) {
+    const WalkerLaunch& L = W.LE;
+    if (W.group) {
+        if (W.ell) k_extend<1, true><<<L.grid, 128, 0, ctx->stream>>>(rc, A, H, depth, 0);
+        else k_extend<0, true><<<L.grid, 128, 0, ctx->stream>>>(rc, A, H, depth, 0);
+    } else {
+        if (W.ell) k_extend<1, false><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage);
+        else k_extend<0, false><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage);
+    }
+}
+
+static void launch_shadow(gpugi_ctx* ctx, const Walkers& W, const RenderConst& rc, const ShadowSoA& Q, int depth) {
+    const WalkerLaunch& L = W.LS;
+    if (W.group) {
+        if (W.ell) k_shadow<1, true><<<L.grid, 128, 0, ctx->stream>>>(rc, Q, depth, 0);
+        else k_shadow<0, true><<<L.grid, 128, 0, ctx->stream>>>(rc, Q, depth, 0);
+    } else {
+        if (W.ell) k_shadow<1, false><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage);
+        else k_shadow<0, false><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage);
+    }
+}
+
 // One chunk of `samples` iterations of a pass.
 static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderConst rc, uint32_t pass) {
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    auto extend = ell ? (const void*)k_extend<1> : (const void*)k_extend<0>;
-    auto shadowK = ell ? (const void*)k_shadow<1> : (const void*)k_shadow<0>;
-    WalkerLaunch LE, LS;
-    gpugi_status cst = walker_launch_config(ctx, sc, extend, 1ull << 40, ctx->renderSharedNodes, LE);
-    if (!cst) cst = walker_launch_config(ctx, sc, shadowK, 1ull << 40, ctx->renderSharedNodes, LS);
+    Walkers W;
+    gpugi_status cst = walkers_config(ctx, sc, W);
     if (cst) return cst;
     int gridShade = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gridShade, (const void*)k_pt_shade, 128, 0);
@@ -1109,13 +1136,11 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
 
     auto bounces = [&](int kind /*0 PT, 1 light, 2 light+cache, 3 BPT eye*/) -> gpugi_status {
         for (int depth = 0; depth < rc.maxPathLength; ++depth) {
-            if (ell) k_extend<1><<<LE.grid, 128, LE.smem, ctx->stream>>>(rc, A, rb->H, depth, LE.stage);
-            else k_extend<0><<<LE.grid, 128, LE.smem, ctx->stream>>>(rc, A, rb->H, depth, LE.stage);
+            launch_extend(ctx, W, rc, A, rb->H, depth);
             if (kind == 0) k_pt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
             else if (kind == 3) k_bpt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
             else k_light_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth, kind == 2);
-            if (ell) k_shadow<1><<<LS.grid, 128, LS.smem, ctx->stream>>>(rc, rb->Q, depth, LS.stage);
-            else k_shadow<0><<<LS.grid, 128, LS.smem, ctx->stream>>>(rc, rb->Q, depth, LS.stage);
+            launch_shadow(ctx, W, rc, rb->Q, depth);
             std::swap(A, B);
         }
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
@@ -1433,13 +1458,8 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     rc.qPixel = rb->qPixel;
     rc.queryCount = rb->nrcCounters;
     rc.queryCap = framePaths;
-    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    WalkerLaunch LE, LS;
-    if ((st = walker_launch_config(ctx, sc, ell ? (const void*)k_extend<1> : (const void*)k_extend<0>, 1ull << 40,
-                                   ctx->renderSharedNodes, LE)) ||
-        (st = walker_launch_config(ctx, sc, ell ? (const void*)k_shadow<1> : (const void*)k_shadow<0>, 1ull << 40,
-                                   ctx->renderSharedNodes, LS)))
-        return st;
+    Walkers W;
+    if ((st = walkers_config(ctx, sc, W))) return st;
     int perSM = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, (const void*)k_nrc_shade, 128, 0);
     const int gridShade = ctx->numSMs * std::max(perSM, 1);
@@ -1455,11 +1475,9 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         PathSoA A = rb->A, B = rb->B;
         k_nrc_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
         for (int depth = 0; depth < rc.maxPathLength; ++depth) {
-            if (ell) k_extend<1><<<LE.grid, 128, LE.smem, ctx->stream>>>(rc, A, rb->H, depth, LE.stage);
-            else k_extend<0><<<LE.grid, 128, LE.smem, ctx->stream>>>(rc, A, rb->H, depth, LE.stage);
+            launch_extend(ctx, W, rc, A, rb->H, depth);
             k_nrc_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
-            if (ell) k_shadow<1><<<LS.grid, 128, LS.smem, ctx->stream>>>(rc, rb->Q, depth, LS.stage);
-            else k_shadow<0><<<LS.grid, 128, LS.smem, ctx->stream>>>(rc, rb->Q, depth, LS.stage);
+            launch_shadow(ctx, W, rc, rb->Q, depth);
             std::swap(A, B);
         }
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(256) k_trace_root_filter(
     const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
     const float* __restrict__ tmax, uint64_t n, int32_t* __restrict__ slot, float* __restrict__ t,
     float* __restrict__ u, float* __restrict__ v, uint8_t* __restrict__ occluded, uint32_t* __restrict__ queue,
-    unsigned long long* counters) {
+    unsigned long long* counters, uint32_t rayBase) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool pass = false;
     if (i < n) {
@@ -169,7 +169,63 @@ __global__ void __launch_bounds__(256) k_trace_root_filter(
     unsigned long long base = 0;
     if (lane == 0 && ballot) base = atomicAdd(counters + 1, (unsigned long long)__popc(ballot));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (pass) queue[base + __popc(ballot & ((1u << lane) - 1u))] = (uint32_t)i;
+    if (pass) queue[base + __popc(ballot & ((1u << lane) - 1u))] = rayBase + (uint32_t)i;
+}
+
+// The same prefilter for four consecutive rays per thread with 16-B loads
+// and stores (all ray and result arrays 16-B aligned; rays [0, 4 n4)). Rays
+// that pass are appended with one atomic per warp (warp prefix sum of the
+// per-thread counts). Results of passing rays are written too and later
+// overwritten by the walker.
+template <bool ANY_HIT, int BOUNDS>
+__global__ void __launch_bounds__(256) k_trace_root_filter4(
+    DevScene s, const float4* __restrict__ ox, const float4* __restrict__ oy, const float4* __restrict__ oz,
+    const float4* __restrict__ dx, const float4* __restrict__ dy, const float4* __restrict__ dz,
+    const float4* __restrict__ tmax, uint64_t n4, int4* __restrict__ slot, float4* __restrict__ t,
+    float4* __restrict__ u, float4* __restrict__ v, uchar4* __restrict__ occluded, uint32_t* __restrict__ queue,
+    unsigned long long* counters) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned pass = 0;
+    if (i < n4) {
+        const float4 X = __ldg(ox + i), Y = __ldg(oy + i), Z = __ldg(oz + i);
+        const float4 DX = __ldg(dx + i), DY = __ldg(dy + i), DZ = __ldg(dz + i), L = __ldg(tmax + i);
+        const float4 a = __ldg(s.nodes), b = __ldg(s.nodes + 1);
+        const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w}, zs[4] = {Z.x, Z.y, Z.z, Z.w};
+        const float dxs[4] = {DX.x, DX.y, DX.z, DX.w}, dys[4] = {DY.x, DY.y, DY.z, DY.w},
+                    dzs[4] = {DZ.x, DZ.y, DZ.z, DZ.w}, ls[4] = {L.x, L.y, L.z, L.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float3 o = make_float3(xs[k], ys[k], zs[k]), d = make_float3(dxs[k], dys[k], dzs[k]);
+            float firstHit;
+            bool hit;
+            if (BOUNDS == 0) hit = intersect_box(o, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a, b, firstHit);
+            else hit = intersect_ellipsoid(o, d, a, b, firstHit);
+            if (hit && firstHit <= ls[k]) pass |= 1u << k;
+        }
+        if (ANY_HIT) {
+            occluded[i] = make_uchar4(0, 0, 0, 0);
+        } else {
+            slot[i] = make_int4(-1, -1, -1, -1);
+            t[i] = L;
+            u[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            v[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned cnt = __popc(pass);
+    unsigned incl = cnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const unsigned up = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= (unsigned)off) incl += up;
+    }
+    unsigned long long base = 0;
+    if (lane == 31 && incl) base = atomicAdd(counters + 1, (unsigned long long)incl);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    uint64_t at = base + (incl - cnt);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (pass & (1u << k)) queue[at++] = (uint32_t)(4 * i + k);
 }
 
 // Second launch: the persistent walker over the queued ray indices.
@@ -223,18 +279,8 @@ __global__ void __launch_bounds__(128) k_trace_queue(
 }
 
 // Group walker (modes 3 and 4), second launch after the root prefilter: G
-// lanes walk one ray together. A node round tests the G consecutive nodes
-// [node, node + G) of the preorder array (one coalesced 32G-byte load), then
-// resolves which of them the sequential walk visits by pointer jumping over
-// the in-window successors (log2 G shuffles): the walk leaves the window at
-// a node outside it, at the end of the escape chain, or at a hit leaf. A leaf
-// round tests G slots of the leaf block at once and applies the sequential
-// acceptance rule (a slot is accepted when hit < rayLength, so the result is
-// the first slot reaching the minimum; any hit: the first accepted slot).
-// Every node decision uses the same arithmetic and the same rayLength as in
-// trace_ray, so results are identical; tests of nodes the walk skips are
-// discarded. A round advances one ray by several of trace_ray's steps, which
-// shortens the dependent fetch chain of the longest walks.
+// lanes walk each queued ray together (group_step), which shortens the
+// dependent fetch chain of the longest walks.
 template <bool ANY_HIT, int BOUNDS, int G>
 __global__ void __launch_bounds__(128) k_trace_group(
     DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
@@ -242,142 +288,25 @@ __global__ void __launch_bounds__(128) k_trace_group(
     const float* __restrict__ tmax, int32_t* __restrict__ slot, float* __restrict__ t, float* __restrict__ u,
     float* __restrict__ v, uint8_t* __restrict__ occluded, const uint32_t* __restrict__ queue,
     unsigned long long* counters, uint32_t* err) {
-    static_assert(G == 4 || G == 8 || G == 16, "group size");
-    constexpr uint32_t kDone = 0xFFFFFFFFu, kLeafMark = 0x80000000u;
-    const uint64_t n = counters[1];
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned gl = lane & (G - 1), gbase = lane & ~(unsigned)(G - 1);
-    const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << gbase;
-    float3 o = make_float3(0.0f, 0.0f, 0.0f), d = o, inv = o;
-    float len = 0.0f, bu = 0.0f, bv = 0.0f;
-    int32_t best = -1;
-    uint32_t node = 0, cur = 0, end = 0, resume = kDone, budget = 0, ray = 0;
-    bool active = false, exhausted = false;
-    while (true) {
-        // refill: one atomic per warp for all groups that need a ray
-        const bool need = !active && !exhausted;
-        const unsigned needMask = __ballot_sync(0xffffffffu, need && gl == 0);
-        if (needMask) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(counters + 2, (unsigned long long)__popc(needMask));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (need) {
-                const uint64_t my = base + (uint64_t)__popc(needMask & ((1u << gbase) - 1u));
-                if (my < n) {
-                    ray = __ldg(queue + my);
-                    o = make_float3(__ldg(ox + ray), __ldg(oy + ray), __ldg(oz + ray));
-                    d = make_float3(__ldg(dx + ray), __ldg(dy + ray), __ldg(dz + ray));
-                    inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
-                    len = __ldg(tmax + ray);
-                    best = -1;
-                    bu = bv = 0.0f;
-                    node = 0;
-                    cur = end = 0;
-                    resume = kDone;
-                    budget = s.numNodes;
-                    active = true;
-                } else {
-                    exhausted = true;
-                }
-            }
-        }
-        if (!__any_sync(0xffffffffu, active)) break;
-        if (!active) continue;
-        bool finished = false;
-        if (cur < end) {
-            // leaf round: slots [cur, min(cur + G, end))
-            const uint32_t k = cur + gl;
-            float h = 0.0f, by = 0.0f, bz = 0.0f;
-            bool ok = false;
-            if (k < end) ok = intersect_triangle(o, d, s.tris + 3 * (size_t)k, h, by, bz) && h < len;
+    group_walks<ANY_HIT, BOUNDS, G>(
+        s, counters[1], counters + 2, err,
+        [&](uint64_t i, float3& o, float3& d, float& len) {
+            const uint32_t ray = __ldg(queue + i);
+            o = make_float3(__ldg(ox + ray), __ldg(oy + ray), __ldg(oz + ray));
+            d = make_float3(__ldg(dx + ray), __ldg(dy + ray), __ldg(dz + ray));
+            len = __ldg(tmax + ray);
+        },
+        [&](uint64_t i, const GroupWalk& g) {
+            const uint32_t ray = __ldg(queue + i);
             if (ANY_HIT) {
-                uint32_t key = ok ? k : kDone;
-#pragma unroll
-                for (int off = G / 2; off > 0; off >>= 1) key = min(key, __shfl_xor_sync(gmask, key, off));
-                if (key != kDone) {
-                    best = (int32_t)key;
-                    finished = true;
-                }
+                occluded[ray] = g.slot >= 0 ? 1 : 0;
             } else {
-                unsigned long long key = ok ? ((unsigned long long)__float_as_uint(h) << 32) | k : ~0ull;
-#pragma unroll
-                for (int off = G / 2; off > 0; off >>= 1) {
-                    const unsigned long long other = __shfl_xor_sync(gmask, key, off);
-                    key = other < key ? other : key;
-                }
-                const uint32_t win = (uint32_t)key;
-                const unsigned src = gbase + ((key != ~0ull) ? (win - cur) : 0u);
-                const float wu = __shfl_sync(gmask, by, src), wv = __shfl_sync(gmask, bz, src);
-                if (key != ~0ull) {
-                    best = (int32_t)win;
-                    len = __uint_as_float((uint32_t)(key >> 32));
-                    bu = wu;
-                    bv = wv;
-                }
+                slot[ray] = g.slot;
+                t[ray] = g.len;
+                u[ray] = g.u;
+                v[ray] = g.v;
             }
-            cur = min(cur + G, end);
-            if (!finished && cur >= end) {
-                node = resume;
-                if (node == kDone) finished = true;
-            }
-        } else {
-            // node round: nodes [node, node + G)
-            if (budget-- == 0) {
-                raise_error(err, DEVERR_TRAVERSAL_CAP);
-                finished = true;
-            } else {
-                const uint32_t p = node + gl;
-                uint32_t next = kDone, child = 0, escape = 0;
-                if (p < s.numNodes) {
-                    const float4 a = __ldg(s.nodes + 2 * (size_t)p), b = __ldg(s.nodes + 2 * (size_t)p + 1);
-                    child = __float_as_uint(a.w);
-                    escape = __float_as_uint(b.w);
-                    float firstHit;
-                    bool hit;
-                    if (BOUNDS == 0) hit = intersect_box(o, inv, a, b, firstHit);
-                    else hit = intersect_ellipsoid(o, d, a, b, firstHit);
-                    if (hit && firstHit <= len) next = (child & LEAF_FLAG) ? (kLeafMark | gl) : child;
-                    else next = escape ? escape : kDone;
-                }
-                // pointer jumping over successors inside the window
-#pragma unroll
-                for (int r = 1; r < G; r <<= 1) {
-                    const bool chase = next < kLeafMark && next - node < (uint32_t)G;
-                    const uint32_t w = __shfl_sync(gmask, next, gbase + (chase ? next - node : gl));
-                    next = chase ? w : next;
-                }
-                const uint32_t r0 = __shfl_sync(gmask, next, gbase);
-                if (r0 == kDone) {
-                    finished = true;
-                } else if (r0 & kLeafMark) {
-                    const unsigned src = gbase + (r0 & (kLeafMark - 1u));
-                    const uint32_t lc = __shfl_sync(gmask, child, src), le = __shfl_sync(gmask, escape, src);
-                    cur = (lc & LEAF_BLOCK_MASK) * s.leafSize;
-                    end = cur + ((lc >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK);
-                    resume = le ? le : kDone;
-                    if (cur >= end) {  // empty leaf block
-                        node = resume;
-                        if (node == kDone) finished = true;
-                    }
-                } else {
-                    node = r0;
-                }
-            }
-        }
-        if (finished) {
-            if (gl == 0) {
-                if (ANY_HIT) {
-                    occluded[ray] = best >= 0 ? 1 : 0;
-                } else {
-                    slot[ray] = best;
-                    t[ray] = len;
-                    u[ray] = bu;
-                    v[ray] = bv;
-                }
-            }
-            active = false;
-        }
-    }
+        });
 }
 
 gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
@@ -403,28 +332,59 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
                                       unsigned long long* counters) {
     if (n == 0) return GPUGI_OK;
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    const unsigned grid1 = (unsigned)((n + 255) / 256);
-#define GPUGI_FILTER_ON(A, B)                                                                                       \
-    k_trace_root_filter<A, B><<<grid1, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, \
-                                                              v, occluded, queue, counters)
-    if (!ell) {
-        if (anyHit) GPUGI_FILTER_ON(true, 0);
-        else GPUGI_FILTER_ON(false, 0);
-    } else {
-        if (anyHit) GPUGI_FILTER_ON(true, 1);
-        else GPUGI_FILTER_ON(false, 1);
+    // four rays per thread with 16-B accesses when every array allows it
+    auto al = [](const void* p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; };
+    const bool vec = al(ox) && al(oy) && al(oz) && al(dx) && al(dy) && al(dz) && al(tmax) && al(slot) && al(t) &&
+                     al(u) && al(v) && (occluded == nullptr || ((uintptr_t)occluded & 3u) == 0);
+    const uint64_t n4 = vec ? n / 4 : 0, head = 4 * n4;
+    if (n4) {
+        const unsigned grid4 = (unsigned)((n4 + 255) / 256);
+        auto f4 = [](const float* p) { return reinterpret_cast<const float4*>(p); };
+#define GPUGI_FILTER4_ON(A, B)                                                                                        \
+    k_trace_root_filter4<A, B><<<grid4, 256, 0, ctx->stream>>>(                                                      \
+        sc->dev, f4(ox), f4(oy), f4(oz), f4(dx), f4(dy), f4(dz), f4(tmax), n4, reinterpret_cast<int4*>(slot),          \
+        reinterpret_cast<float4*>(t), reinterpret_cast<float4*>(u), reinterpret_cast<float4*>(v),                     \
+        reinterpret_cast<uchar4*>(occluded), queue, counters)
+        if (!ell) {
+            if (anyHit) GPUGI_FILTER4_ON(true, 0);
+            else GPUGI_FILTER4_ON(false, 0);
+        } else {
+            if (anyHit) GPUGI_FILTER4_ON(true, 1);
+            else GPUGI_FILTER4_ON(false, 1);
+        }
+#undef GPUGI_FILTER4_ON
     }
+    if (head < n) {
+        const uint64_t m = n - head;
+        const unsigned grid1 = (unsigned)((m + 255) / 256);
+        auto sh = [&](const float* p) { return p + head; };
+#define GPUGI_FILTER_ON(A, B)                                                                                        \
+    k_trace_root_filter<A, B><<<grid1, 256, 0, ctx->stream>>>(                                                       \
+        sc->dev, sh(ox), sh(oy), sh(oz), sh(dx), sh(dy), sh(dz), sh(tmax), m, slot ? slot + head : nullptr,            \
+        t ? t + head : nullptr, u ? u + head : nullptr, v ? v + head : nullptr, occluded ? occluded + head : nullptr, \
+        queue, counters, (uint32_t)head)
+        if (!ell) {
+            if (anyHit) GPUGI_FILTER_ON(true, 0);
+            else GPUGI_FILTER_ON(false, 0);
+        } else {
+            if (anyHit) GPUGI_FILTER_ON(true, 1);
+            else GPUGI_FILTER_ON(false, 1);
+        }
 #undef GPUGI_FILTER_ON
-    if (ctx->traceMode == 3 || ctx->traceMode == 4) {
+    }
+    if (ctx->traceMode >= 3) {
         void (*kg)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
                    const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
                    uint32_t*);
         if (ctx->traceMode == 3) {
             if (!ell) kg = anyHit ? k_trace_group<true, 0, 8> : k_trace_group<false, 0, 8>;
             else kg = anyHit ? k_trace_group<true, 1, 8> : k_trace_group<false, 1, 8>;
-        } else {
+        } else if (ctx->traceMode == 4) {
             if (!ell) kg = anyHit ? k_trace_group<true, 0, 4> : k_trace_group<false, 0, 4>;
             else kg = anyHit ? k_trace_group<true, 1, 4> : k_trace_group<false, 1, 4>;
+        } else {
+            if (!ell) kg = anyHit ? k_trace_group<true, 0, 16> : k_trace_group<false, 0, 16>;
+            else kg = anyHit ? k_trace_group<true, 1, 16> : k_trace_group<false, 1, 16>;
         }
         WalkerLaunch L;
         gpugi_status st = walker_launch_config(ctx, sc, (const void*)kg, 1ull << 40, 0, L);

@@ -243,4 +243,191 @@ GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord, const
     return w.cur >= w.end && w.node == NODE_DONE;
 }
 
+// ---------------------------------------------------------------- group walk
+// G lanes walk one ray together (G = 4, 8 or 16; every lane of the group
+// holds the same state and calls group_step with it). A node round tests
+// the G consecutive nodes [node, node + G) of the node array (one coalesced
+// load), then resolves which of them the sequential walk visits by pointer
+// jumping over the successors inside the window (log2 G shuffles): the walk
+// leaves the window at a node outside it, at the end of the escape chain or
+// at a hit leaf. A leaf round tests G slots of the leaf block at once and
+// applies the sequential acceptance rule: a slot is accepted when
+// hit < rayLength, so the result is the first slot reaching the minimum (any
+// hit: the first accepted slot). Every node decision uses trace_ray's
+// arithmetic with the same rayLength, so results are identical; tests of
+// nodes the walk skips are discarded. Successors may point backwards (the
+// breadth-first top-level layout): they simply end the round.
+struct GroupWalk {
+    float3 o, d, inv;
+    float len, u, v;
+    int32_t slot;
+    uint32_t node, cur, end, resume, budget;
+};
+constexpr uint32_t kGroupDone = 0xFFFFFFFFu, kGroupLeaf = 0x80000000u;
+
+GPUGI_D void group_begin(GroupWalk& g, const DevScene& s, float3 o, float3 d, float tmax) {
+    g.o = o;
+    g.d = d;
+    g.inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
+    g.len = tmax;
+    g.u = g.v = 0.0f;
+    g.slot = -1;
+    g.node = 0;
+    g.cur = g.end = 0;
+    g.resume = kGroupDone;
+    g.budget = s.numNodes;
+}
+
+// One round; returns true when the walk is over. gl = lane in the group,
+// gbase = first lane of the group, gmask = the group's lanes.
+template <bool ANY_HIT, int BOUNDS, int G>
+GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned gl, unsigned gbase,
+                        unsigned gmask) {
+    static_assert(G == 4 || G == 8 || G == 16, "group size");
+    if (g.cur < g.end) {
+        const uint32_t k = g.cur + gl;
+        float h = 0.0f, by = 0.0f, bz = 0.0f;
+        bool ok = false;
+        if (k < g.end) ok = intersect_triangle(g.o, g.d, s.tris + 3 * (size_t)k, h, by, bz) && h < g.len;
+        if (ANY_HIT) {
+            uint32_t key = ok ? k : kGroupDone;
+#pragma unroll
+            for (int off = G / 2; off > 0; off >>= 1) key = min(key, __shfl_xor_sync(gmask, key, off));
+            if (key != kGroupDone) {
+                g.slot = (int32_t)key;
+                return true;
+            }
+        } else {
+            unsigned long long key = ok ? ((unsigned long long)__float_as_uint(h) << 32) | k : ~0ull;
+#pragma unroll
+            for (int off = G / 2; off > 0; off >>= 1) {
+                const unsigned long long other = __shfl_xor_sync(gmask, key, off);
+                key = other < key ? other : key;
+            }
+            const uint32_t win = (uint32_t)key;
+            const unsigned src = gbase + ((key != ~0ull) ? (win - g.cur) : 0u);
+            const float wu = __shfl_sync(gmask, by, src), wv = __shfl_sync(gmask, bz, src);
+            if (key != ~0ull) {
+                g.slot = (int32_t)win;
+                g.len = __uint_as_float((uint32_t)(key >> 32));
+                g.u = wu;
+                g.v = wv;
+            }
+        }
+        g.cur = min(g.cur + G, g.end);
+        if (g.cur >= g.end) {
+            g.node = g.resume;
+            if (g.node == kGroupDone) return true;
+        }
+        return false;
+    }
+    if (g.budget-- == 0) {
+        raise_error(err, DEVERR_TRAVERSAL_CAP);
+        return true;
+    }
+    const uint32_t p = g.node + gl;
+    uint32_t next = kGroupDone, child = 0, escape = 0;
+    if (p < s.numNodes) {
+        const float4 a = __ldg(s.nodes + 2 * (size_t)p), b = __ldg(s.nodes + 2 * (size_t)p + 1);
+        child = __float_as_uint(a.w);
+        escape = __float_as_uint(b.w);
+        float firstHit;
+        bool hit;
+        if (BOUNDS == 0) hit = intersect_box(g.o, g.inv, a, b, firstHit);
+        else hit = intersect_ellipsoid(g.o, g.d, a, b, firstHit);
+        if (hit && firstHit <= g.len) next = (child & LEAF_FLAG) ? (kGroupLeaf | gl) : child;
+        else next = escape ? escape : kGroupDone;
+    }
+#pragma unroll
+    for (int r = 1; r < G; r <<= 1) {
+        const bool chase = next < kGroupLeaf && next - g.node < (uint32_t)G;
+        const uint32_t w = __shfl_sync(gmask, next, gbase + (chase ? next - g.node : gl));
+        next = chase ? w : next;
+    }
+    const uint32_t r0 = __shfl_sync(gmask, next, gbase);
+    if (r0 == kGroupDone) return true;
+    if (r0 & kGroupLeaf) {
+        const unsigned src = gbase + (r0 & (kGroupLeaf - 1u));
+        const uint32_t lc = __shfl_sync(gmask, child, src), le = __shfl_sync(gmask, escape, src);
+        g.cur = (lc & LEAF_BLOCK_MASK) * s.leafSize;
+        g.end = g.cur + ((lc >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK);
+        g.resume = le ? le : kGroupDone;
+        if (g.cur >= g.end) {  // empty leaf block
+            g.node = g.resume;
+            return g.node == kGroupDone;
+        }
+        return false;
+    }
+    g.node = r0;
+    return false;
+}
+
+// Persistent loop of group walks over n work items: groups that need a ray
+// take the next item (one atomic per warp). load(i, o, d, tmax) fills the
+// ray of item i; finish(i, walk) runs in the group's first lane. With MULTI
+// the rays belong to different scenes: load returns the item's scene and its
+// bounds kind selects the node test per round; otherwise every ray walks
+// `scene` with the BOUNDS test.
+template <bool ANY_HIT, int BOUNDS, int G, bool MULTI, typename Load, typename Finish>
+GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long long* work, uint32_t* err, Load load,
+                              Finish finish) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned gl = lane & (G - 1), gbase = lane & ~(unsigned)(G - 1);
+    const unsigned gmask = ((1u << G) - 1u) << gbase;
+    GroupWalk g;
+    const DevScene* sc = nullptr;
+    uint64_t item = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        const bool need = !active && !exhausted;
+        const unsigned needMask = __ballot_sync(0xffffffffu, need && gl == 0);
+        if (needMask) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(work, (unsigned long long)__popc(needMask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (need) {
+                const uint64_t my = base + (uint64_t)__popc(needMask & ((1u << gbase) - 1u));
+                if (my < n) {
+                    item = my;
+                    float3 o, d;
+                    float tmax;
+                    if constexpr (MULTI) {
+                        sc = load(item, o, d, tmax);
+                        group_begin(g, *sc, o, d, tmax);
+                    } else {
+                        load(item, o, d, tmax);
+                        group_begin(g, scene, o, d, tmax);
+                    }
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (!active) continue;
+        bool done;
+        if constexpr (MULTI)
+            done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? group_step<ANY_HIT, 1, G>(g, *sc, err, gl, gbase, gmask)
+                                                           : group_step<ANY_HIT, 0, G>(g, *sc, err, gl, gbase, gmask);
+        else
+            done = group_step<ANY_HIT, BOUNDS, G>(g, scene, err, gl, gbase, gmask);
+        if (done) {
+            if (gl == 0) finish(item, g);
+            active = false;
+        }
+    }
+}
+
+template <bool ANY_HIT, int BOUNDS, int G, typename Load, typename Finish>
+GPUGI_D void group_walks(const DevScene& scene, uint64_t n, unsigned long long* work, uint32_t* err, Load load,
+                         Finish finish) {
+    group_walks_impl<ANY_HIT, BOUNDS, G, false>(scene, n, work, err, load, finish);
+}
+
+template <bool ANY_HIT, int G, typename Load, typename Finish>
+GPUGI_D void group_walks_multi(uint64_t n, unsigned long long* work, uint32_t* err, Load load, Finish finish) {
+    group_walks_impl<ANY_HIT, 0, G, true>(DevScene{}, n, work, err, load, finish);
+}
+
 }  // namespace gpugi

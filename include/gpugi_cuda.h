@@ -160,9 +160,9 @@ gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* scene,
  * finished lanes from a device ray counter; mode 2: a coalesced
  * root-bounds prefilter that finishes rays missing the scene and queues the
  * rest (warp-ballot compaction) for the persistent walker; modes 3
- * (default) and 4: the same prefilter, then groups of 8 (mode 3) or 4 (mode 4) lanes walk one
- * ray together, testing a window of consecutive preorder nodes or leaf slots
- * per round. All modes make the same decisions per ray as TraceRay and
+ * (default), 4 and 5: the same prefilter, then groups of 8 (mode 3), 4
+ * (mode 4) or 16 (mode 5) lanes walk one ray together, testing a window of
+ * consecutive preorder nodes or leaf slots per round. All modes make the same decisions per ray as TraceRay and
  * return identical results. blockSize applies to mode 0. */
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize);
 

@@ -101,7 +101,7 @@ def test_autotune_picks_a_candidate_and_keeps_results(cuda_ctx, scenes3):
     ds = cuda_ctx.upload_scene(b, sc["positions"])
     try:
         t = cuda_ctx.autotune(ds, trace=True)
-        assert (t["traceMode"], t["traceBlock"]) in {(0, 64), (0, 128), (0, 256), (1, 128), (2, 128), (3, 128), (4, 128)}
+        assert (t["traceMode"], t["traceBlock"]) in {(0, 64), (0, 128), (0, 256), (1, 128), (2, 128), (3, 128), (4, 128), (5, 128)}
         assert t["traceMraysPerSecond"] > 0
         rays = scenes.aimed_rays(50_000, sc["positions"], seed=8)
         g = cuda.trace_closest(cuda_ctx, ds, rays)
