@@ -349,46 +349,49 @@ def run_nrc(args):
     pt.close()
 
     box = ((-1.05, -0.25, -1.05), (1.05, 0.35, 1.05))
-    cache = nrc.RadianceCache(ctx, *box, seed=5)
-    spf = args.nrc_spf
-    opts = dict(max_path_length=depth, sky=sky, terminate_depth=1, train_fraction=args.nrc_train_fraction,
-                train_steps=args.nrc_train_steps, samples_per_frame=spf)
-    scratch = render.Image(ctx, W, H)
-    t_nrc = timed(lambda: nrc.render_nrc(ctx, ds, cam, scratch, cache, samples=args.nrc_warmup * spf,
-                                         iteration=1 << 20, rng_state=[11], **opts))
-    t_warm = t_nrc
-    scratch.close()
-    img = render.Image(ctx, W, H, fp64=True)
-    frames, nrc_curve, reached = 0, [], None
-    at_equal_time = None
-    chunk = 1
-    while t_nrc < 3.0 * t_pt and frames < 4096:
-        t_nrc += timed(lambda: nrc.render_nrc(ctx, ds, cam, img, cache, samples=chunk * spf, iteration=frames * spf,
-                                              rng_state=[13 + frames], **opts))
-        frames += chunk
-        r = rmse(img, frames * spf)
-        nrc_curve.append((frames * spf, round(t_nrc, 5), round(r, 6)))
-        if at_equal_time is None and t_nrc >= t_pt:
-            at_equal_time = r
-        if r <= target:
-            reached = t_nrc
-            break
-        chunk = min(chunk * 2, 16)
-    line = {"metric": "time to the 1024-spp plain-PT RMSE, NRC path tracing vs plain PT", "unit": "ratio",
-            "value": (reached / t_pt) if reached else None, "higher_is_better": False,
-            "t_pt_s": round(t_pt, 4), "t_nrc_s": round(reached, 4) if reached else None,
-            "t_nrc_warmup_s": round(t_warm, 4), "target_rmse": target,
-            "nrc_rmse_at_equal_time": at_equal_time,
-            "config": {"workload": "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8",
-                       "resolution": [W, H], "reference_spp": args.nrc_ref_spp, "reference_s": round(t_ref, 2),
-                       "nrc": {"terminate_depth": 1, "train_fraction": args.nrc_train_fraction,
-                               "train_steps": args.nrc_train_steps, "samples_per_frame": spf,
-                               "warmup_frames": args.nrc_warmup, "max_train_samples": 65536,
-                               "mlp": "64-64x4-3 ReLU fp16, fp32 accumulate, Adam lr 1e-2"}},
-            "pt_curve": pt_curve, "nrc_curve": nrc_curve, "data": "synthetic", "dtype": "f32 paths, f16 MLP"}
-    print(json.dumps(line), flush=True)
-    for x in (img, cache, ds):
-        x.close()
+    configs = [tuple(int(x) for x in c.split(",")) for c in args.nrc_configs.split(";")] if args.nrc_configs else \
+        [(args.nrc_td, args.nrc_spf, args.nrc_train_steps)]
+    for td, spf, steps in configs:
+        # training paths: about 1.5 x 65,536 vertices per frame (3 per path)
+        tf = args.nrc_train_fraction or min(0.05, 1.5 * 65536 / (3.0 * W * H * spf))
+        cache = nrc.RadianceCache(ctx, *box, seed=5)
+        opts = dict(max_path_length=depth, sky=sky, terminate_depth=td, train_fraction=tf, train_steps=steps,
+                    samples_per_frame=spf)
+        scratch = render.Image(ctx, W, H)
+        t_nrc = timed(lambda: nrc.render_nrc(ctx, ds, cam, scratch, cache, samples=args.nrc_warmup * spf,
+                                             iteration=1 << 20, rng_state=[11], **opts))
+        t_warm = t_nrc
+        scratch.close()
+        img = render.Image(ctx, W, H, fp64=True)
+        frames, nrc_curve, reached, at_equal_time, chunk = 0, [], None, None, 1
+        while t_nrc < 3.0 * t_pt and frames * spf < 8192:
+            t_nrc += timed(lambda: nrc.render_nrc(ctx, ds, cam, img, cache, samples=chunk * spf,
+                                                  iteration=frames * spf, rng_state=[13 + frames], **opts))
+            frames += chunk
+            r = rmse(img, frames * spf)
+            nrc_curve.append((frames * spf, round(t_nrc, 5), round(r, 6)))
+            if at_equal_time is None and t_nrc >= t_pt:
+                at_equal_time = r
+            if r <= target:
+                reached = t_nrc
+                break
+            chunk = min(chunk * 2, max(1, 64 // spf))
+        line = {"metric": "time to the 1024-spp plain-PT RMSE, NRC path tracing vs plain PT", "unit": "ratio",
+                "value": (reached / t_pt) if reached else None, "higher_is_better": False,
+                "t_pt_s": round(t_pt, 4), "t_nrc_s": round(reached, 4) if reached else None,
+                "t_nrc_warmup_s": round(t_warm, 4), "target_rmse": target,
+                "nrc_rmse_at_equal_time": at_equal_time,
+                "config": {"workload": "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8",
+                           "resolution": [W, H], "reference_spp": args.nrc_ref_spp, "reference_s": round(t_ref, 2),
+                           "nrc": {"terminate_depth": td, "train_fraction": round(tf, 5), "train_steps": steps,
+                                   "samples_per_frame": spf, "warmup_frames": args.nrc_warmup,
+                                   "max_train_samples": 65536, "ema": 0.99,
+                                   "mlp": "64-64x4-3 ReLU fp16, fp32 accumulate, Adam lr 1e-2"}},
+                "pt_curve": pt_curve, "nrc_curve": nrc_curve, "data": "synthetic", "dtype": "f32 paths, f16 MLP"}
+        print(json.dumps(line), flush=True)
+        img.close()
+        cache.close()
+    ds.close()
     ctx.close()
 
 
@@ -409,10 +412,13 @@ def main():
                     help="trace: the closest-hit headline; nrc: time-to-equal-RMSE of the radiance cache")
     ap.add_argument("--nrc-size", type=int, nargs=2, default=[640, 360])
     ap.add_argument("--nrc-ref-spp", type=int, default=16384)
-    ap.add_argument("--nrc-spf", type=int, default=4, help="samples per cache frame")
-    ap.add_argument("--nrc-warmup", type=int, default=32, help="training frames before accumulation")
-    ap.add_argument("--nrc-train-fraction", type=float, default=0.03)
-    ap.add_argument("--nrc-train-steps", type=int, default=2)
+    ap.add_argument("--nrc-spf", type=int, default=16, help="samples per cache frame")
+    ap.add_argument("--nrc-warmup", type=int, default=16, help="training frames before accumulation")
+    ap.add_argument("--nrc-train-fraction", type=float, default=0.0,
+                    help="share of training paths (0: about 98k training vertices per frame)")
+    ap.add_argument("--nrc-configs", default="", help="'td,spf,steps;...' several cache settings in one run")
+    ap.add_argument("--nrc-train-steps", type=int, default=4)
+    ap.add_argument("--nrc-td", type=int, default=2, help="path vertex where render paths query the cache")
     args = ap.parse_args()
     if args.workload == "nrc":
         from __graft_entry__ import build

@@ -130,6 +130,12 @@ struct WalkerLaunch {
 };
 gpugi_status walker_launch_config(gpugi_ctx* ctx, const gpugi_scene* sc, const void* kernel, uint64_t n,
                                   uint32_t maxStage, WalkerLaunch& out);
+// Radiance cache with element counts in device memory (nrc.cu): inference
+// of min(n, *count) queries, one Adam step on min(cap, *count) samples.
+gpugi_status nrc_infer_counted(gpugi_ctx* ctx, const gpugi_nrc* nn, const float* queries, uint64_t n,
+                               const uint32_t* count, float* out);
+gpugi_status nrc_train_counted(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples, uint64_t cap,
+                               const uint32_t* count);
 // Light tables and the host light sampler (host.cu).
 void build_light_tables(gpugi_scene* sc);
 void generate_light_samples(gpugi_scene* sc, uint64_t& rng, uint32_t numSamples, float* out);

@@ -30,6 +30,12 @@ struct gpugi_nrc {
     float* grad = nullptr;     // fp32 [l][in][out]
     __half* wFwd = nullptr;    // [l][out][in]
     __half* wBwd = nullptr;    // [l][in][out]
+    // inference weights: an exponential moving average of the trained weights
+    // (decay emaDecay, bias-corrected; the raw weights while emaSteps == 0)
+    float* ema = nullptr;      // fp32 running sum (1 - d) sum d^k w
+    __half* wInf = nullptr;    // [l][out][in]
+    float emaDecay = 0.99f;
+    uint32_t emaSteps = 0;
     __half* acts = nullptr;    // training: X_l per sample, [l][n][64]
     __half* dys = nullptr;     // training: dY_l per sample (scaled), [l][n][64]
     float* lossSum = nullptr;  // device scalar
@@ -159,9 +165,12 @@ GPUGI_D void encode_tile(const float* __restrict__ records, int stride, uint64_t
 }
 
 // Inference: out[i] = network(query i), 3 floats, clamped at 0.
+// With count != NULL the number of queries is min(n, *count) (device side).
 __global__ void __launch_bounds__(128) k_nrc_infer(const float* __restrict__ queries, uint64_t n,
+                                                   const uint32_t* __restrict__ count,
                                                    const __half* __restrict__ wFwd, float3 boxMin, float3 boxInv,
                                                    float* __restrict__ out) {
+    if (count) n = min(n, (uint64_t)*count);
     extern __shared__ __half smem[];
     __half* sW = smem;                                  // 5 x 64 x kRow
     __half* sX = smem + kLayers * 64 * kRow + (threadIdx.x >> 5) * 16 * kRow;
@@ -203,10 +212,12 @@ __global__ void __launch_bounds__(128) k_nrc_infer(const float* __restrict__ que
 // weight-gradient GEMM, and accumulates the loss. Relative L2 loss of the
 // NRC: (p - y)^2 / (sg(p)^2 + 0.01), averaged over samples and channels.
 __global__ void __launch_bounds__(128) k_nrc_fwd_bwd(const float* __restrict__ samples, uint64_t n,
+                                                     const uint32_t* __restrict__ count,
                                                      const __half* __restrict__ wFwd, const __half* __restrict__ wBwd,
                                                      float3 boxMin, float3 boxInv, float lossScale,
                                                      __half* __restrict__ acts, __half* __restrict__ dys,
                                                      uint64_t cap, float* lossSum, float* predOut) {
+    if (count) n = min(n, (uint64_t)*count);
     extern __shared__ __half smem[];
     __half* sWf = smem;
     __half* sWb = smem + kLayers * 64 * kRow;
@@ -216,7 +227,7 @@ __global__ void __launch_bounds__(128) k_nrc_fwd_bwd(const float* __restrict__ s
     __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    const float invCount = 1.0f / (3.0f * (float)n);
+    const float invCount = n ? 1.0f / (3.0f * (float)n) : 0.0f;
     float lossAcc = 0.0f;
     for (uint64_t tile = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < n; tile += warps) {
         const uint64_t base = tile * 16;
@@ -325,8 +336,10 @@ __global__ void __launch_bounds__(128) k_nrc_fwd_bwd(const float* __restrict__ s
 // block; warp w owns rows in [16w, 16w+16). Partial sums go to grad with
 // atomics (fp32).
 __global__ void __launch_bounds__(128) k_nrc_weight_grad(const __half* __restrict__ acts,
-                                                         const __half* __restrict__ dys, uint64_t n, uint64_t cap,
+                                                         const __half* __restrict__ dys, uint64_t n,
+                                                         const uint32_t* __restrict__ count, uint64_t cap,
                                                          float* __restrict__ grad) {
+    if (count) n = min(n, ((uint64_t)*count + 15) / 16 * 16);
     __shared__ __align__(16) __half sX[16 * kRow];
     __shared__ __align__(16) __half sY[16 * kRow];
     const int l = blockIdx.y;
@@ -382,13 +395,23 @@ __global__ void __launch_bounds__(128) k_nrc_weight_grad(const __half* __restric
 }
 
 // Adam (fp32 master weights), then the two fp16 layouts.
+// With count != NULL the gradient is the sum over min(*count, cap) samples
+// and gradScale is 1 / (3 count lossScale); no samples: no update.
 __global__ void k_nrc_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                           const float* __restrict__ grad, float gradScale, float lr, float b1, float b2, float eps,
-                           float c1, float c2, __half* __restrict__ wFwd, __half* __restrict__ wBwd) {
+                           const float* __restrict__ grad, float gradScale, const uint32_t* __restrict__ count,
+                           uint64_t cap, float lossScale, float lr, float b1, float b2, float eps, float c1, float c2,
+                           __half* __restrict__ wFwd, __half* __restrict__ wBwd, float* __restrict__ ema,
+                           float emaDecay, float emaCorr, __half* __restrict__ wInf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
+    bool update = true;
+    if (count) {
+        const uint64_t c = min((uint64_t)*count, cap);
+        update = c > 0;
+        gradScale = update ? 1.0f / (3.0f * (float)c * lossScale) : 0.0f;
+    }
     const float gr = grad[i] * gradScale;
-    if (isfinite(gr)) {
+    if (update && isfinite(gr)) {
         const float mi = b1 * m[i] + (1.0f - b1) * gr;
         const float vi = b2 * v[i] + (1.0f - b2) * gr * gr;
         m[i] = mi;
@@ -401,9 +424,19 @@ __global__ void k_nrc_adam(float* __restrict__ w, float* __restrict__ m, float* 
     const __half h = __float2half(w[i]);
     wBwd[i] = h;
     wFwd[layer_offset(l) + out * kIn + in] = h;
+    float inf = w[i];
+    if (emaDecay > 0.0f) {
+        const float e = emaDecay * ema[i] + (1.0f - emaDecay) * w[i];
+        ema[i] = e;
+        inf = e * emaCorr;
+    }
+    wInf[layer_offset(l) + out * kIn + in] = __float2half(inf);
 }
 
-__global__ void k_nrc_publish(const float* __restrict__ w, __half* __restrict__ wFwd, __half* __restrict__ wBwd) {
+// fp16 layouts of the master weights (after creation or set_weights); the
+// inference weights restart from them.
+__global__ void k_nrc_publish(const float* __restrict__ w, __half* __restrict__ wFwd, __half* __restrict__ wBwd,
+                              float* __restrict__ ema, __half* __restrict__ wInf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     const int l = i < 4 * 4096 ? i / 4096 : 4;
@@ -412,6 +445,8 @@ __global__ void k_nrc_publish(const float* __restrict__ w, __half* __restrict__ 
     const __half h = __float2half(w[i]);
     wBwd[i] = h;
     wFwd[layer_offset(l) + out * kIn + in] = h;
+    wInf[layer_offset(l) + out * kIn + in] = h;
+    ema[i] = 0.0f;
 }
 
 // The input encoding alone (64 halves per query), for inspection and tests.
@@ -431,14 +466,22 @@ constexpr size_t kTrainSmem = (size_t)2 * kLayers * 64 * kRow * 2 + 4 * 16 * kRo
 }  // namespace gpugi
 
 // ------------------------------------------------------------------ C ABI
+// Advance the EMA step count; returns 1 / (1 - d^t) (bias correction of a
+// running average started at zero).
+static float ema_correction(gpugi_nrc* nn) {
+    nn->emaSteps++;
+    return nn->emaDecay > 0.0f ? 1.0f / (1.0f - std::pow(nn->emaDecay, (float)nn->emaSteps)) : 1.0f;
+}
+
 static gpugi_status nrc_publish(gpugi_ctx* ctx, gpugi_nrc* nn) {
-    k_nrc_publish<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->wFwd, nn->wBwd);
+    nn->emaSteps = 0;
+    k_nrc_publish<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->wFwd, nn->wBwd, nn->ema, nn->wInf);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }
 
-gpugi_status gpugi_nrc_infer_device_impl(gpugi_ctx* ctx, const gpugi_nrc* nn, const float* queries, uint64_t n,
-                                         float* out) {
+gpugi_status gpugi::nrc_infer_counted(gpugi_ctx* ctx, const gpugi_nrc* nn, const float* queries, uint64_t n,
+                                      const uint32_t* count, float* out) {
     if (n == 0) return GPUGI_OK;
     static bool attr = false;
     if (!attr) {
@@ -449,7 +492,30 @@ gpugi_status gpugi_nrc_infer_device_impl(gpugi_ctx* ctx, const gpugi_nrc* nn, co
     uint64_t blocks = (tiles + 3) / 4;
     const uint64_t maxBlocks = (uint64_t)ctx->numSMs * 4;
     if (blocks > maxBlocks) blocks = maxBlocks;
-    k_nrc_infer<<<(unsigned)blocks, 128, kInferSmem, ctx->stream>>>(queries, n, nn->wFwd, nn->boxMin, nn->boxInv, out);
+    k_nrc_infer<<<(unsigned)blocks, 128, kInferSmem, ctx->stream>>>(queries, n, count, nn->wInf, nn->boxMin,
+                                                                    nn->boxInv, out);
+    GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    return GPUGI_OK;
+}
+
+extern "C" {
+static gpugi_status nrc_grad(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples, uint64_t n, float* predOut,
+                             const uint32_t* count);
+}
+
+// One Adam step on min(*count, cap) device samples, without a host round trip.
+gpugi_status gpugi::nrc_train_counted(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples, uint64_t cap,
+                                      const uint32_t* count) {
+    if (cap == 0) return GPUGI_OK;
+    gpugi_status st = nrc_grad(ctx, nn, samples, cap, nullptr, count);
+    if (st) return st;
+    nn->step++;
+    const float c1 = 1.0f - std::pow(nn->beta1, (float)nn->step), c2 = 1.0f - std::pow(nn->beta2, (float)nn->step);
+    const float emaCorr = ema_correction(nn);
+    k_nrc_adam<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->m, nn->v, nn->grad, 0.0f, count, cap,
+                                                                nn->lossScale, nn->lr, nn->beta1, nn->beta2, nn->eps,
+                                                                c1, c2, nn->wFwd, nn->wBwd, nn->ema, nn->emaDecay,
+                                                                emaCorr, nn->wInf);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }
@@ -471,6 +537,7 @@ gpugi_status gpugi_nrc_create(gpugi_ctx* ctx, const float boxMin[3], const float
     bool ok = cudaMalloc(&nn->master, P * 4) == cudaSuccess && cudaMalloc(&nn->m, P * 4) == cudaSuccess &&
               cudaMalloc(&nn->v, P * 4) == cudaSuccess && cudaMalloc(&nn->grad, P * 4) == cudaSuccess &&
               cudaMalloc(&nn->wFwd, P * 2) == cudaSuccess && cudaMalloc(&nn->wBwd, P * 2) == cudaSuccess &&
+              cudaMalloc(&nn->ema, P * 4) == cudaSuccess && cudaMalloc(&nn->wInf, P * 2) == cudaSuccess &&
               cudaMalloc(&nn->lossSum, 4) == cudaSuccess;
     if (!ok) {
         gpugi_nrc_destroy(nn);
@@ -507,6 +574,7 @@ void gpugi_nrc_destroy(gpugi_nrc* nn) {
     if (nn->ctx) cudaStreamSynchronize(nn->ctx->stream);
     detach_child(&nn->ctx);
     for (void* p : {(void*)nn->master, (void*)nn->m, (void*)nn->v, (void*)nn->grad, (void*)nn->wFwd, (void*)nn->wBwd,
+                    (void*)nn->ema, (void*)nn->wInf,
                     (void*)nn->acts, (void*)nn->dys, (void*)nn->lossSum})
         if (p) cudaFree(p);
     delete nn;
@@ -528,14 +596,22 @@ gpugi_status gpugi_nrc_set_weights(gpugi_ctx* ctx, gpugi_nrc* nn, const float* w
     return GPUGI_OK;
 }
 
+gpugi_status gpugi_nrc_set_ema(gpugi_ctx* ctx, gpugi_nrc* nn, float decay) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!nn || !(decay >= 0.0f && decay < 1.0f)) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "decay in [0, 1)");
+    nn->emaDecay = decay;
+    return nrc_publish(ctx, nn);
+}
+
 gpugi_status gpugi_nrc_infer_device(gpugi_ctx* ctx, const gpugi_nrc* nn, const float* queries, uint64_t n,
                                     float* radiance) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!nn || (n && (!queries || !radiance))) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    return gpugi_nrc_infer_device_impl(ctx, nn, queries, n, radiance);
+    return nrc_infer_counted(ctx, nn, queries, n, nullptr, radiance);
 }
 
-static gpugi_status nrc_grad(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples, uint64_t n, float* predOut) {
+static gpugi_status nrc_grad(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples, uint64_t n, float* predOut,
+                             const uint32_t* count = nullptr) {
     if (n > nn->cap) {
         if (nn->acts) cudaFree(nn->acts);
         if (nn->dys) cudaFree(nn->dys);
@@ -558,7 +634,7 @@ static gpugi_status nrc_grad(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples
     uint64_t blocks = (tiles + 3) / 4;
     const uint64_t maxBlocks = (uint64_t)ctx->numSMs * 2;
     if (blocks > maxBlocks) blocks = maxBlocks;
-    k_nrc_fwd_bwd<<<(unsigned)blocks, 128, kTrainSmem, ctx->stream>>>(samples, n, nn->wFwd, nn->wBwd, nn->boxMin,
+    k_nrc_fwd_bwd<<<(unsigned)blocks, 128, kTrainSmem, ctx->stream>>>(samples, n, count, nn->wFwd, nn->wBwd, nn->boxMin,
                                                                       nn->boxInv, nn->lossScale, nn->acts, nn->dys,
                                                                       nn->cap, nn->lossSum, predOut);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
@@ -567,7 +643,7 @@ static gpugi_status nrc_grad(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples
     uint64_t gb = (n + 511) / 512;
     if (gb > (uint64_t)ctx->numSMs) gb = ctx->numSMs;
     k_nrc_weight_grad<<<dim3((unsigned)gb, kLayers), 128, 0, ctx->stream>>>(nn->acts, nn->dys, (n + 15) / 16 * 16,
-                                                                           nn->cap, nn->grad);
+                                                                           count, nn->cap, nn->grad);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }
@@ -581,9 +657,11 @@ gpugi_status gpugi_nrc_train_device(gpugi_ctx* ctx, gpugi_nrc* nn, const float* 
     nn->step++;
     const float c1 = 1.0f - std::pow(nn->beta1, (float)nn->step), c2 = 1.0f - std::pow(nn->beta2, (float)nn->step);
     const float gradScale = 1.0f / (3.0f * (float)n * nn->lossScale);
-    k_nrc_adam<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->m, nn->v, nn->grad, gradScale,
-                                                                nn->lr, nn->beta1, nn->beta2, nn->eps, c1, c2, nn->wFwd,
-                                                                nn->wBwd);
+    const float emaCorr = ema_correction(nn);
+    k_nrc_adam<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->m, nn->v, nn->grad, gradScale, nullptr,
+                                                                n, nn->lossScale, nn->lr, nn->beta1, nn->beta2, nn->eps,
+                                                                c1, c2, nn->wFwd, nn->wBwd, nn->ema, nn->emaDecay,
+                                                                emaCorr, nn->wInf);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     if (loss) {
         GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(loss, nn->lossSum, 4, cudaMemcpyDeviceToHost, ctx->stream));

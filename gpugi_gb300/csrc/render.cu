@@ -171,10 +171,14 @@ GPUGI_D void persistent_walks(const DevScene& s, uint32_t n, unsigned long long*
     }
 }
 
-// Closest hits of the path queue. GROUP: 8-lane group walks (group_walks),
-// otherwise one lane per ray with the top nodes staged in shared memory.
-template <int BOUNDS, bool GROUP>
-__global__ void __launch_bounds__(128) k_extend(RenderConst rc, PathSoA A, HitSoA H, int depth, uint32_t stage) {
+// Closest hits of the path queue. Queues shorter than groupBelow rays are
+// walked by 8-lane groups (group_walks: a short queue leaves lanes idle, and
+// groups shorten the longest walks); longer ones with one lane per ray (more
+// rays in flight; top nodes staged in shared memory). The choice depends on
+// the device-side count, so it costs no host round trip.
+template <int BOUNDS>
+__global__ void __launch_bounds__(128) k_extend(RenderConst rc, PathSoA A, HitSoA H, int depth, uint32_t stage,
+                                                uint32_t groupBelow) {
     const uint32_t n = rc.cnt->path[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&rc.cnt->rays[0], (unsigned long long)n);
     auto load = [&](auto i, float3& o, float3& d, float& tmax) {
@@ -182,7 +186,7 @@ __global__ void __launch_bounds__(128) k_extend(RenderConst rc, PathSoA A, HitSo
         d = make_float3(A.dx[i], A.dy[i], A.dz[i]);
         tmax = kRAY_MAX;
     };
-    if constexpr (GROUP) {
+    if (n < groupBelow) {
         group_walks<false, BOUNDS, 8>(rc.s, n, &rc.cnt->extendWork[depth], rc.err, load,
                                       [&](uint64_t i, const GroupWalk& g) {
                                           H.slot[i] = g.slot;
@@ -216,8 +220,9 @@ GPUGI_D void shadow_unoccluded(const RenderConst& rc, const ShadowSoA& Q, uint32
     }
 }
 
-template <int BOUNDS, bool GROUP>
-__global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int depth, uint32_t stage) {
+template <int BOUNDS>
+__global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int depth, uint32_t stage,
+                                                uint32_t groupBelow) {
     const uint32_t n = rc.cnt->shadow[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&rc.cnt->rays[1], (unsigned long long)n);
     auto load = [&](auto i, float3& o, float3& d, float& tmax) {
@@ -225,7 +230,7 @@ __global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int
         d = make_float3(Q.dx[i], Q.dy[i], Q.dz[i]);
         tmax = Q.tmax[i];
     };
-    if constexpr (GROUP) {
+    if (n < groupBelow) {
         group_walks<true, BOUNDS, 8>(rc.s, n, &rc.cnt->shadowWork[depth], rc.err, load,
                                      [&](uint64_t i, const GroupWalk& g) {
                                          if (g.slot < 0) shadow_unoccluded(rc, Q, (uint32_t)i);
@@ -243,7 +248,8 @@ __global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int
 // Launch shapes and launches of the walkers for a scene: group walks when the
 // context's trace mode is 3 or 4, else lane walks with staged top nodes.
 struct Walkers {
-    bool ell = false, group = false;
+    bool ell = false;
+    uint32_t groupBelowE = 0, groupBelowS = 0;  // queue lengths below which groups walk
     WalkerLaunch LE, LS;
 };
 
@@ -913,42 +919,95 @@ __global__ void k_batch_generate(const RenderConst* __restrict__ jobs, const uin
     }
 }
 
-// Walks of rays of several scenes: 8-lane group walks (group_walks_multi);
-// each item's scene comes from its job.
+// Walks of rays of several scenes: each ray's scene comes from its job, and
+// the scene's bounds kind selects the node test per step. As in k_extend,
+// queues shorter than groupBelow are walked by 8-lane groups.
+template <bool ANY_HIT, typename Load, typename Finish>
+GPUGI_D void persistent_walks_multi(uint32_t n, unsigned long long* work, uint32_t* err, Load load, Finish finish) {
+    const unsigned lane = threadIdx.x & 31u;
+    WalkState w;
+    const DevScene* sc = nullptr;
+    uint32_t ray = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        const bool need = !active && !exhausted;
+        const unsigned needMask = __ballot_sync(0xffffffffu, need);
+        if (needMask) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(work, (unsigned long long)__popc(needMask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (need) {
+                const unsigned long long my = base + (unsigned long long)__popc(needMask & ((1u << lane) - 1u));
+                if (my < n) {
+                    ray = (uint32_t)my;
+                    float3 o, d;
+                    float tmax;
+                    sc = load(ray, o, d, tmax);
+                    walk_begin(w, *sc, o, d, tmax);
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) {
+            const bool done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? walk_step<ANY_HIT, 1>(w, *sc, err)
+                                                                      : walk_step<ANY_HIT, 0>(w, *sc, err);
+            if (done) {
+                finish(ray, w.slot, w.len, w.u, w.v);
+                active = false;
+            }
+        }
+    }
+}
+
+template <bool ANY_HIT, typename Load, typename Finish>
+GPUGI_D void walks_multi(uint32_t n, uint32_t groupBelow, unsigned long long* work, uint32_t* err, Load load,
+                         Finish finish) {
+    if (n < groupBelow)
+        group_walks_multi<ANY_HIT, 8>(n, work, err, load, [&](uint64_t i, const GroupWalk& g) {
+            finish((uint32_t)i, g.slot, g.len, g.u, g.v);
+        });
+    else
+        persistent_walks_multi<ANY_HIT>(n, work, err, load, finish);
+}
+
 __global__ void __launch_bounds__(128) k_batch_extend(const RenderConst* __restrict__ jobs, Counters* cnt,
-                                                      uint32_t* err, PathSoA A, HitSoA H, int depth) {
+                                                      uint32_t* err, PathSoA A, HitSoA H, int depth,
+                                                      uint32_t groupBelow) {
     const uint32_t n = cnt->path[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays[0], (unsigned long long)n);
-    group_walks_multi<false, 8>(
-        n, &cnt->extendWork[depth], err,
+    walks_multi<false>(
+        n, groupBelow, &cnt->extendWork[depth], err,
         [&](uint64_t i, float3& o, float3& d, float& tmax) -> const DevScene* {
             o = make_float3(A.ox[i], A.oy[i], A.oz[i]);
             d = make_float3(A.dx[i], A.dy[i], A.dz[i]);
             tmax = kRAY_MAX;
             return &jobs[A.job[i]].s;
         },
-        [&](uint64_t i, const GroupWalk& g) {
-            H.slot[i] = g.slot;
-            H.t[i] = g.len;
-            H.u[i] = g.u;
-            H.v[i] = g.v;
+        [&](uint32_t i, int32_t slot, float t, float u, float v) {
+            H.slot[i] = slot;
+            H.t[i] = t;
+            H.u[i] = u;
+            H.v[i] = v;
         });
 }
 
 __global__ void __launch_bounds__(128) k_batch_shadow(const RenderConst* __restrict__ jobs, Counters* cnt,
-                                                      uint32_t* err, ShadowSoA Q, int depth) {
+                                                      uint32_t* err, ShadowSoA Q, int depth, uint32_t groupBelow) {
     const uint32_t n = cnt->shadow[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays[1], (unsigned long long)n);
-    group_walks_multi<true, 8>(
-        n, &cnt->shadowWork[depth], err,
+    walks_multi<true>(
+        n, groupBelow, &cnt->shadowWork[depth], err,
         [&](uint64_t i, float3& o, float3& d, float& tmax) -> const DevScene* {
             o = make_float3(Q.ox[i], Q.oy[i], Q.oz[i]);
             d = make_float3(Q.dx[i], Q.dy[i], Q.dz[i]);
             tmax = Q.tmax[i];
             return &jobs[Q.job[i]].s;
         },
-        [&](uint64_t i, const GroupWalk& g) {
-            if (g.slot < 0) splat(jobs[Q.job[i]], Q.pixel[i], make_float3(Q.cr[i], Q.cg[i], Q.cb[i]));
+        [&](uint32_t i, int32_t slot, float, float, float) {
+            if (slot < 0) splat(jobs[Q.job[i]], Q.pixel[i], make_float3(Q.cr[i], Q.cg[i], Q.cb[i]));
         });
 }
 
@@ -1083,42 +1142,29 @@ static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheByt
 
 static gpugi_status walkers_config(gpugi_ctx* ctx, const gpugi_scene* sc, Walkers& W) {
     W.ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    W.group = ctx->traceMode >= 3;
-    const void *ke, *ks;
-    if (W.group) {
-        ke = W.ell ? (const void*)k_extend<1, true> : (const void*)k_extend<0, true>;
-        ks = W.ell ? (const void*)k_shadow<1, true> : (const void*)k_shadow<0, true>;
-    } else {
-        ke = W.ell ? (const void*)k_extend<1, false> : (const void*)k_extend<0, false>;
-        ks = W.ell ? (const void*)k_shadow<1, false> : (const void*)k_shadow<0, false>;
-    }
-    const uint32_t stage = W.group ? 0 : ctx->renderSharedNodes;
-    gpugi_status st = walker_launch_config(ctx, sc, ke, 1ull << 40, stage, W.LE);
-    if (!st) st = walker_launch_config(ctx, sc, ks, 1ull << 40, stage, W.LS);
+    const void* ke = W.ell ? (const void*)k_extend<1> : (const void*)k_extend<0>;
+    const void* ks = W.ell ? (const void*)k_shadow<1> : (const void*)k_shadow<0>;
+    gpugi_status st = walker_launch_config(ctx, sc, ke, 1ull << 40, ctx->renderSharedNodes, W.LE);
+    if (!st) st = walker_launch_config(ctx, sc, ks, 1ull << 40, ctx->renderSharedNodes, W.LS);
+    // group walks while fewer rays than half the resident lanes are queued
+    // (trace modes 3-5; the lane walk otherwise)
+    const bool group = ctx->traceMode >= 3;
+    W.groupBelowE = group ? W.LE.grid * 128u / 2u : 0u;
+    W.groupBelowS = group ? W.LS.grid * 128u / 2u : 0u;
     return st;
 }
 
 static void launch_extend(gpugi_ctx* ctx, const Walkers& W, const RenderConst& rc, const PathSoA& A, const HitSoA& H,
                           int depth) {
     const WalkerLaunch& L = W.LE;
-    if (W.group) {
-        if (W.ell) k_extend<1, true><<<L.grid, 128, 0, ctx->stream>>>(rc, A, H, depth, 0);
-        else k_extend<0, true><<<L.grid, 128, 0, ctx->stream>>>(rc, A, H, depth, 0);
-    } else {
-        if (W.ell) k_extend<1, false><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage);
-        else k_extend<0, false><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage);
-    }
+    if (W.ell) k_extend<1><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage, W.groupBelowE);
+    else k_extend<0><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage, W.groupBelowE);
 }
 
 static void launch_shadow(gpugi_ctx* ctx, const Walkers& W, const RenderConst& rc, const ShadowSoA& Q, int depth) {
     const WalkerLaunch& L = W.LS;
-    if (W.group) {
-        if (W.ell) k_shadow<1, true><<<L.grid, 128, 0, ctx->stream>>>(rc, Q, depth, 0);
-        else k_shadow<0, true><<<L.grid, 128, 0, ctx->stream>>>(rc, Q, depth, 0);
-    } else {
-        if (W.ell) k_shadow<1, false><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage);
-        else k_shadow<0, false><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage);
-    }
+    if (W.ell) k_shadow<1><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage, W.groupBelowS);
+    else k_shadow<0><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage, W.groupBelowS);
 }
 
 // One chunk of `samples` iterations of a pass.
@@ -1436,7 +1482,13 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     if ((uint64_t)spf * numPixels > (64ull << 20))
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "samplesPerFrame x pixels exceeds 64M paths");
     const uint32_t framePaths = spf * numPixels;
-    const size_t lightBytes = (size_t)spf * p->numLightSamples * 32;
+    // light samples go up in blocks of whole frames (up to 64 MB), so the
+    // staging buffer is reused, and waited for, once per block
+    const size_t setBytes = (size_t)p->numLightSamples * 32;
+    uint32_t blockFrames = (uint32_t)std::min<size_t>((p->samples + spf - 1) / spf,
+                                                      std::max<size_t>(1, (64u << 20) / (setBytes * spf)));
+    const uint32_t blockSamples = blockFrames * spf;
+    const size_t lightBytes = (size_t)blockSamples * setBytes;
     gpugi_status st = ensure_buffers(ctx, framePaths, 0, lightBytes, spf);
     if (st) return st;
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
@@ -1467,7 +1519,12 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
     for (uint32_t frame = 0; frame < p->samples; frame += spf) {
         const uint32_t ns = std::min(spf, p->samples - frame);
-        if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, frame, ns, p->numLightSamples))) return st;
+        const uint32_t inBlock = frame % blockSamples;
+        if (inBlock == 0 &&
+            (st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, frame,
+                                    std::min(blockSamples, p->samples - frame), p->numLightSamples)))
+            return st;
+        rc.lightSamples = rb->lights + 2 * (size_t)inBlock * p->numLightSamples;
         rc.samples = ns;
         rc.sampleBase = frame;
         GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), ctx->stream));
@@ -1481,26 +1538,18 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
             std::swap(A, B);
         }
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
-        // cache lookups of this frame (the network as trained by earlier frames)
-        uint32_t counts[2] = {0, 0};
-        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(counts, rb->nrcCounters, 8, cudaMemcpyDeviceToHost, ctx->stream));
-        GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        const uint32_t nq = std::min<uint32_t>(counts[0], framePaths);
-        if (nq) {
-            if ((st = gpugi_nrc_infer_device(ctx, nn, rb->queries, nq, rb->radiance))) return st;
-            k_nrc_apply<<<ctx->numSMs * 4, 256, 0, ctx->stream>>>(rc, rb->radiance);
-        }
+        // cache lookups of this frame (the network as trained by earlier
+        // frames); counts stay on the device, so frames queue back to back
+        if ((st = nrc_infer_counted(ctx, nn, rb->queries, framePaths, rb->nrcCounters, rb->radiance))) return st;
+        k_nrc_apply<<<ctx->numSMs * 4, 256, 0, ctx->stream>>>(rc, rb->radiance);
         // training on this frame's training paths
-        if (np->train && counts[1] > 0) {
+        if (np->train && np->trainFraction > 0.0f) {
             k_nrc_targets<<<ctx->numSMs * 2, 128, 0, ctx->stream>>>(rc, rb->samples, rb->nrcCounters + 2,
                                                                      (uint32_t)sampleCap);
-            uint32_t ns = 0;
-            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(&ns, rb->nrcCounters + 2, 4, cudaMemcpyDeviceToHost, ctx->stream));
-            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-            ns = std::min<uint32_t>(ns, (uint32_t)sampleCap);
-            for (uint32_t k = 0; k < std::max<uint32_t>(1u, np->trainSteps) && ns; ++k)
-                if ((st = gpugi_nrc_train_device(ctx, nn, rb->samples, ns, nullptr))) return st;
+            for (uint32_t k = 0; k < std::max<uint32_t>(1u, np->trainSteps); ++k)
+                if ((st = nrc_train_counted(ctx, nn, rb->samples, sampleCap, rb->nrcCounters + 2))) return st;
         }
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     }
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
@@ -1583,20 +1632,23 @@ gpugi_status gpugi_render_batch(gpugi_ctx* ctx, const gpugi_job* jobs, uint32_t 
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, (const void*)k_batch_pt_shade, 128, 0);
         const unsigned gridShade = (unsigned)(ctx->numSMs * std::max(perSM, 1));
         const unsigned genBlocks = (unsigned)ctx->numSMs * 8;
+        const uint32_t groupE = ctx->traceMode >= 3 ? LE.grid * 128u / 2u : 0u;
+        const uint32_t groupS = ctx->traceMode >= 3 ? LS.grid * 128u / 2u : 0u;
         auto record = [&](cudaStream_t stream) {
             cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), stream);
             PathSoA A = rb->A, B = rb->B;
             k_batch_generate<<<genBlocks, 256, 0, stream>>>(rb->dJobs, rb->dOffsets, nj, rb->cnt, A);
             for (int depth = 0; depth < (int)maxDepth; ++depth) {
-                k_batch_extend<<<LE.grid, 128, 0, stream>>>(rb->dJobs, rb->cnt, ctx->errWord, A, rb->H, depth);
+                k_batch_extend<<<LE.grid, 128, 0, stream>>>(rb->dJobs, rb->cnt, ctx->errWord, A, rb->H, depth,
+                                                            groupE);
                 k_batch_pt_shade<<<gridShade, 128, 0, stream>>>(rb->dJobs, rb->cnt, A, B, rb->H, rb->Q, depth);
-                k_batch_shadow<<<LS.grid, 128, 0, stream>>>(rb->dJobs, rb->cnt, ctx->errWord, rb->Q, depth);
+                k_batch_shadow<<<LS.grid, 128, 0, stream>>>(rb->dJobs, rb->cnt, ctx->errWord, rb->Q, depth, groupS);
                 std::swap(A, B);
             }
         };
         if (ctx->batchGraph) {
             const std::vector<uintptr_t> key = {(uintptr_t)rb->block, (uintptr_t)rb->dJobs, nj, maxDepth, LE.grid,
-                                                LS.grid, gridShade, (uintptr_t)ctx->errWord};
+                                                LS.grid, gridShade, (uintptr_t)ctx->errWord, groupE, groupS};
             if (!rb->batchExec || key != rb->batchKey) {
                 if (rb->batchExec) cudaGraphExecDestroy(rb->batchExec);
                 rb->batchExec = nullptr;

@@ -25,6 +25,7 @@ def _declare():
     L.gpugi_nrc_train_device.argtypes = [P, P, P, U64, P]
     L.gpugi_nrc_gradient_device.argtypes = [P, P, P, U64, P, P, P]
     L.gpugi_nrc_encode_device.argtypes = [P, P, P, U64, P]
+    L.gpugi_nrc_set_ema.argtypes = [P, P, F]
     from . import render
     render._declare()
     L.gpugi_render_nrc.argtypes = [P, P, C.POINTER(render.Camera), C.POINTER(render.RenderParams), P,
@@ -77,6 +78,10 @@ class RadianceCache:
         w = np.ascontiguousarray(w, np.float32)
         assert w.shape == (PARAMS,)
         self.ctx.check(_declare().gpugi_nrc_set_weights(self.ctx.handle, self._h, cuda._ptr(w)))
+
+    def set_ema(self, decay: float):
+        """Decay of the moving average of the weights that inference uses (0: the trained weights)."""
+        self.ctx.check(_declare().gpugi_nrc_set_ema(self.ctx.handle, self._h, float(decay)))
 
     def infer(self, queries) -> "object":
         """queries: torch (n, 12) float32 cuda tensor -> (n, 3) radiance tensor."""

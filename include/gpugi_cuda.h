@@ -268,6 +268,10 @@ void gpugi_nrc_destroy(gpugi_nrc* nrc);
 /* FP32 master weights, layer l at l*4096, row-major [in][out] (out = 16 for l = 4). */
 gpugi_status gpugi_nrc_get_weights(gpugi_ctx* ctx, const gpugi_nrc* nrc, float* weights);
 gpugi_status gpugi_nrc_set_weights(gpugi_ctx* ctx, gpugi_nrc* nrc, const float* weights);
+/* Inference (and the render pass) use an exponential moving average of the
+ * trained weights, bias-corrected (decay 0.99 by default; 0 = the trained
+ * weights themselves). Setting it, or the weights, restarts the average. */
+gpugi_status gpugi_nrc_set_ema(gpugi_ctx* ctx, gpugi_nrc* nrc, float decay);
 /* radiance[3 i + c] = max(network(query i)_c, 0). Device pointers, asynchronous. */
 gpugi_status gpugi_nrc_infer_device(gpugi_ctx* ctx, const gpugi_nrc* nrc, const float* queries, uint64_t n,
                                     float* radiance);
@@ -290,8 +294,9 @@ gpugi_status gpugi_nrc_encode_device(gpugi_ctx* ctx, const gpugi_nrc* nrc, const
  * become training samples {query, radiance reflected towards the previous
  * vertex}; after the frame's lookups, trainSteps Adam steps run on those
  * samples (at most maxTrainSamples, drawn in a shuffled path order) when
- * train != 0. Both kinds of path splat into image. Synchronises twice per
- * frame (query and sample counts). */
+ * train != 0. Both kinds of path splat into image. Asynchronous: element
+ * counts stay in device memory; the call returns once every frame is queued
+ * (it waits only when the light-sample staging buffer is reused). */
 typedef struct gpugi_nrc_params {
     uint32_t terminateDepth;  /* vertex index (0 = first hit) where render paths query the cache */
     float trainFraction;      /* share of pixels tracing training paths, in [0, 1] */
