@@ -301,6 +301,233 @@ def run_ours(args, world, rank, local):
     ctx.close()
 
 
+def run_passes(args):
+    """Per-pass throughput of the wavefront renderers on the Cornell workload:
+    room of ~98k triangles (5 walls, 2 rotated boxes, level-6 sphere, 0.5 x
+    0.5 ceiling light of radiance 10, albedos U[0.1, 0.9]), 512 x 512, 16 spp,
+    depth 8, Russian roulette after depth 3. For PT, LT and BPT: samples/s
+    (iterations x pixels per second) and Mrays/s (closest-hit + any-hit rays
+    traced, counted on the device), CUDA events around 16 spp after one
+    warm-up iteration. Beside each, the CPU restatement of the same pass on all
+    host threads over a bounded sample (64 x 64, 2 iterations)."""
+    import torch
+    import oracle
+    from gpugi_gb300 import bvh, cuda, render, scenes
+    W = H = 512
+    spp, depth, rr = 16, 8, 3
+    ctx = cuda.Context(0)
+    sc = scenes.cornell_room(seed=1)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]), sc["materials"])
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    out = {}
+    for pass_ in ("PT", "LT", "BPT"):
+        img = render.Image(ctx, W, H)
+        render.render(ctx, ds, cam, img, pass_, max_path_length=depth, samples=1, rr_start_depth=rr, rng_state=[1])
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        render.render(ctx, ds, cam, img, pass_, max_path_length=depth, samples=spp, iteration=1, rr_start_depth=rr,
+                      rng_state=[2])
+        e1.record(stream)
+        e1.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        closest, anyhit = render.ray_counts(ctx)
+        img.close()
+        # CPU restatement, bounded sample
+        cw = ch = 64
+        ccam = render.camera_lookat(*scenes.CORNELL_CAMERA, cw, ch)
+        nls = render.DEFAULT_LIGHT_SAMPLES[pass_]
+        st = [3]
+        t0 = time.perf_counter()
+        acc = None
+        for it in range(2):
+            ls = render.generate_light_samples(ds, st, nls)
+            acc = oracle.render(b, sc, pass_, cw, ch, ccam.as_array(), render.wanghash(it), ls,
+                                max_path_length=depth, rr_start_depth=rr, accum=acc)
+        cpu = time.perf_counter() - t0
+        out[pass_] = {"samples_per_s": W * H * spp / sec, "mrays_per_s": (closest + anyhit) / sec / 1e6,
+                      "ms_per_iteration": sec / spp * 1e3, "closest_rays": closest, "any_hit_rays": anyhit,
+                      "cpu_samples_per_s": cw * ch * 2 / cpu, "cpu_threads": os.cpu_count()}
+    line = {"metric": "samples/s and Mrays/s per pass", "config": {
+        "workload": "Cornell room ~98k tris, 512x512, 16 spp, depth 8, RR after depth 3", "parallelism": "single GPU"},
+        "passes": out, "data": "synthetic", "dtype": "f32",
+        "cpu_sample": "64x64, 2 iterations of the same pass on all host threads"}
+    print(json.dumps(line), flush=True)
+    ds.close()
+    ctx.close()
+
+
+def run_large(args):
+    """Large workload: ~7.9M triangles (20k instances of displaced icospheres
+    and boxes in a 100^3 volume), 64 materials (Lambertian / Phong exponent
+    U[10, 1000]), 256 small area lights (radiance log-uniform [1, 100]),
+    ellipsoid-bounded sweep hierarchy. Reports (1) closest-hit ray queries on
+    2^22 rays (origins uniform in the volume, directions uniform), with the
+    algorithmic-byte roofline fraction: the scene (~0.5 GB) exceeds L2;
+    (2) BPT and PT at 1920 x 1080, 8 spp, depth 6: samples/s and Mrays/s."""
+    import torch
+    from gpugi_gb300 import bvh, cuda, render, scenes
+    hbm, peak_src = peaks()
+    ctx = cuda.Context(0)
+    t0 = time.perf_counter()
+    sc = scenes.large_instanced(seed=1)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", fit="ellipsoid")
+    t_build = time.perf_counter() - t0
+    ds = ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]), sc["materials"])
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def ev_time(fn, reps=1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    # (1) ray queries
+    n = 1 << 22
+    g = torch.Generator(device="cuda").manual_seed(5)
+    o = torch.rand((3, n), device="cuda", generator=g) * 100.0
+    d = torch.randn((3, n), device="cuda", generator=g)
+    d /= d.norm(dim=0, keepdim=True)
+    rays = {"ox": o[0].contiguous(), "oy": o[1].contiguous(), "oz": o[2].contiguous(), "dx": d[0].contiguous(),
+            "dy": d[1].contiguous(), "dz": d[2].contiguous(), "tmax": torch.full((n,), 3.402823466e38, device="cuda")}
+    out = dict(slot=torch.empty(n, dtype=torch.int32, device="cuda"), t=torch.empty(n, device="cuda"),
+               u=torch.empty(n, device="cuda"), v=torch.empty(n, device="cuda"))
+    torch.cuda.synchronize()
+    cuda.trace_closest_device(ctx, ds, rays, out)
+    ctx.sync()
+    sec = ev_time(lambda: cuda.trace_closest_device(ctx, ds, rays, out), reps=5)
+    sums = cuda.trace_stats_device(ctx, ds, rays)
+    alg = cuda.algorithmic_bytes(sums, n)
+    queries = {"mrays_per_s": n / sec / 1e6, "ms_per_launch": sec * 1e3, "rays": n,
+               "roofline": {"bound": "hbm", "achieved": alg / sec / 1e9, "peak": hbm, "unit": "GB/s",
+                            "frac": alg / sec / 1e9 / hbm, "peak_source": peak_src, "alg_bytes_per_launch": alg},
+               "hit_fraction": float((out["slot"] >= 0).float().mean().item())}
+    # (2) passes
+    W, H, spp, depth = 1920, 1080, 8, 6
+    cam = render.camera_lookat(*scenes.LARGE_CAMERA, W, H)
+    passes = {}
+    for pass_ in ("BPT", "PT"):
+        img = render.Image(ctx, W, H)
+        render.render(ctx, ds, cam, img, pass_, max_path_length=depth, samples=1, rng_state=[1])
+        ctx.sync()
+        sec = ev_time(lambda: render.render(ctx, ds, cam, img, pass_, max_path_length=depth, samples=spp,
+                                            iteration=1, rng_state=[2]))
+        closest, anyhit = render.ray_counts(ctx)
+        passes[pass_] = {"samples_per_s": W * H * spp / sec, "mrays_per_s": (closest + anyhit) / sec / 1e6,
+                         "s_per_frame_8spp": sec, "mean": float(img.read()[..., :3].mean() / spp)}
+        img.close()
+    line = {"metric": "large scene: closest-hit Mrays/s and BPT/PT samples/s", "queries": queries, "passes": passes,
+            "config": {"workload": "~7.9M tris (20k instances, 100^3), 64 materials, 256 area lights, ellipsoid BVH; "
+                                   "queries 2^22 random rays; passes 1920x1080 8 spp depth 6",
+                       "triangles": int(sc["triangles"].shape[0]), "nodes": int(b.num_nodes),
+                       "build_s": round(t_build, 1)}, "data": "synthetic", "dtype": "f32"}
+    print(json.dumps(line), flush=True)
+    ds.close()
+    ctx.close()
+
+
+def run_batch(args):
+    """Batched rendering workload: 8 scenes of instanced icospheres, boxes and
+    tori (triangle counts log-uniform in [10k, 2M]), each with a random
+    resolution in {256^2, 512^2, 768^2, 1024^2} and spp in {4, 16, 64}, PT,
+    LT and BPT at depth 8 (24 jobs). One gpugi_render_batch call (PT jobs in
+    one wavefront replayed as a CUDA graph per round; LT and BPT jobs one
+    after another) against the same jobs as 24 gpugi_render calls. Wall time
+    of synchronised calls; samples = pixels x spp summed over jobs."""
+    from gpugi_gb300 import bvh, cuda, render, scenes
+    rs = scenes.Stream(args.batch_seed, 23)
+    ctx = cuda.Context(0)
+    tris = np.exp(rs.uniform(8, math.log(1e4), math.log(2e6)))
+    res = [256, 512, 768, 1024]
+    spps = [4, 16, 64]
+    specs, dss = [], []
+    for k in range(8):
+        sc = scenes.instanced_scene(seed=100 + k, num_triangles=int(tris[k]))
+        b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+        ds = ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]), sc["materials"])
+        dss.append(ds)
+        r = res[int(rs.u64(1)[0] % 4)]
+        spp = spps[int(rs.u64(1)[0] % 3)]
+        cam = render.camera_lookat((0.0, 1.0, 7.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 45.0, r, r)
+        specs.append((ds, cam, r, spp, sc["triangles"].shape[0]))
+
+    def make_jobs():
+        jobs = []
+        for k, (ds, cam, r, spp, _) in enumerate(specs):
+            for pass_ in ("PT", "LT", "BPT"):
+                jobs.append(dict(scene=ds, camera=cam, image=render.Image(ctx, r, r), pass_=pass_, samples=spp,
+                                 max_path_length=8, rng_state=[1000 + k]))
+        return jobs
+
+    def timed(fn):
+        ctx.sync()
+        t0 = time.perf_counter()
+        fn()
+        ctx.sync()
+        return time.perf_counter() - t0
+
+    def run_single(jobs):
+        for j in jobs:
+            render.render(ctx, j["scene"], j["camera"], j["image"], j["pass_"], max_path_length=8,
+                          samples=j["samples"], rng_state=j["rng_state"])
+
+    def samples(jobs, passes):
+        return sum(j["image"].width * j["image"].height * j["samples"] for j in jobs if j["pass_"] in passes)
+
+    result = {}
+    for name, fn in (("batch", lambda js: render.render_batch(ctx, js)), ("single", run_single)):
+        warm = make_jobs()
+        fn(warm)  # buffers, graph capture
+        for j in warm:
+            j["image"].close()
+        jobs = make_jobs()
+        pt_jobs = [j for j in jobs if j["pass_"] == "PT"]
+        t_pt = timed(lambda: fn(pt_jobs))
+        other = [j for j in jobs if j["pass_"] != "PT"]
+        t_other = timed(lambda: fn(other))
+        result[name] = {"pt_s": round(t_pt, 4), "pt_samples_per_s": samples(jobs, ("PT",)) / t_pt,
+                        "lt_bpt_s": round(t_other, 4), "all_samples_per_s": samples(jobs, ("PT", "LT", "BPT")) /
+                        (t_pt + t_other)}
+        for j in jobs:
+            j["image"].close()
+    # many small jobs: 64 PT jobs of 128 x 128 at 4 spp over the same 8 scenes
+    def small_jobs():
+        return [dict(scene=specs[k % 8][0], camera=render.camera_lookat((0.0, 1.0, 7.0), (0.0, 0.0, 0.0),
+                                                                        (0.0, 1.0, 0.0), 45.0, 128, 128),
+                     image=render.Image(ctx, 128, 128), pass_="PT", samples=4, max_path_length=8,
+                     rng_state=[2000 + k]) for k in range(64)]
+    small = {}
+    for name, fn in (("batch", lambda js: render.render_batch(ctx, js)), ("single", run_single)):
+        warm = small_jobs()
+        fn(warm)
+        for j in warm:
+            j["image"].close()
+        jobs = small_jobs()
+        t = timed(lambda: fn(jobs))
+        small[name] = {"s": round(t, 5), "samples_per_s": 64 * 128 * 128 * 4 / t}
+        for j in jobs:
+            j["image"].close()
+    result["small_jobs_64x128x128x4spp"] = small
+    line = {"metric": "samples/s, 24 jobs of 8 scenes: batched vs one call per job",
+            "value": result["batch"]["all_samples_per_s"], "unit": "samples/s", "higher_is_better": True,
+            "pt_speedup_batched": result["single"]["pt_s"] / result["batch"]["pt_s"],
+            "small_jobs_speedup_batched": small["single"]["s"] / small["batch"]["s"], "runs": result,
+            "config": {"workload": "8 instanced scenes, tris log-uniform [10k, 2M], res {256..1024}^2, "
+                                   "spp {4,16,64}, PT+LT+BPT depth 8",
+                       "scenes": [{"tris": t, "res": r, "spp": s_} for (_, _, r, s_, t) in specs],
+                       "paths_per_round": 16 << 20},
+            "data": "synthetic", "dtype": "f32"}
+    print(json.dumps(line), flush=True)
+    for ds in dss:
+        ds.close()
+    ctx.close()
+
+
 def run_nrc(args):
     """Time to equal RMSE, path tracing with the radiance cache vs plain path
     tracing, on the heightfield workload (522k-triangle fBm terrain + 500
@@ -314,7 +541,7 @@ def run_nrc(args):
     calls (both renderers synchronise internally)."""
     from gpugi_gb300 import bvh, cuda, nrc, render, scenes
     W, H = args.nrc_size
-    depth, sky = 8, (0.5, 0.5, 0.5)
+    depth, sky, rr = 8, (0.5, 0.5, 0.5), args.nrc_rr
     ctx = cuda.Context(0)
     sc = scenes.heightfield_boxes(seed=1)
     b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
@@ -331,7 +558,7 @@ def run_nrc(args):
 
     conv = render.Image(ctx, W, H, fp64=True)
     t_ref = timed(lambda: render.render(ctx, ds, cam, conv, "PT", max_path_length=depth, samples=args.nrc_ref_spp,
-                                        iteration=1 << 24, rng_state=[99], sky=sky))
+                                        iteration=1 << 24, rng_state=[99], sky=sky, rr_start_depth=rr))
     ref = (conv.read64() / args.nrc_ref_spp).astype(np.float32)
     conv.close()
 
@@ -342,7 +569,7 @@ def run_nrc(args):
     t_pt, spp, pt_curve = 0.0, 0, []
     for c in [1, 1, 2, 4, 8, 16, 32, 64, 128, 256, 512]:
         t_pt += timed(lambda: render.render(ctx, ds, cam, pt, "PT", max_path_length=depth, samples=c, iteration=spp,
-                                            rng_state=[7 + spp], sky=sky))
+                                            rng_state=[7 + spp], sky=sky, rr_start_depth=rr))
         spp += c
         pt_curve.append((spp, round(t_pt, 5), round(rmse(pt, spp), 6)))
     target = pt_curve[-1][2]
@@ -356,7 +583,7 @@ def run_nrc(args):
         tf = args.nrc_train_fraction or min(0.05, 1.5 * 65536 / (3.0 * W * H * spf))
         cache = nrc.RadianceCache(ctx, *box, seed=5)
         opts = dict(max_path_length=depth, sky=sky, terminate_depth=td, train_fraction=tf, train_steps=steps,
-                    samples_per_frame=spf)
+                    samples_per_frame=spf, rr_start_depth=rr)
         scratch = render.Image(ctx, W, H)
         t_nrc = timed(lambda: nrc.render_nrc(ctx, ds, cam, scratch, cache, samples=args.nrc_warmup * spf,
                                              iteration=1 << 20, rng_state=[11], **opts))
@@ -382,6 +609,7 @@ def run_nrc(args):
                 "t_nrc_warmup_s": round(t_warm, 4), "target_rmse": target,
                 "nrc_rmse_at_equal_time": at_equal_time,
                 "config": {"workload": "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8",
+                           "rr_start_depth": rr,
                            "resolution": [W, H], "reference_spp": args.nrc_ref_spp, "reference_s": round(t_ref, 2),
                            "nrc": {"terminate_depth": td, "train_fraction": round(tf, 5), "train_steps": steps,
                                    "samples_per_frame": spf, "warmup_frames": args.nrc_warmup,
@@ -408,8 +636,10 @@ def main():
     ap.add_argument("--trace-mode", type=int, default=3,
                     help="0: thread per ray, 1: persistent lane refill, 2: root prefilter + persistent, "
                          "3/4: root prefilter + 8/4-lane group walker")
-    ap.add_argument("--workload", choices=["trace", "nrc"], default="trace",
-                    help="trace: the closest-hit headline; nrc: time-to-equal-RMSE of the radiance cache")
+    ap.add_argument("--batch-seed", type=int, default=1)
+    ap.add_argument("--workload", choices=["trace", "nrc", "passes", "batch", "large"], default="trace",
+                    help="trace: the closest-hit headline; nrc: time-to-equal-RMSE of the radiance cache; "
+                         "passes: samples/s and Mrays/s of PT, LT and BPT; batch: batched vs per-job rendering")
     ap.add_argument("--nrc-size", type=int, nargs=2, default=[640, 360])
     ap.add_argument("--nrc-ref-spp", type=int, default=16384)
     ap.add_argument("--nrc-spf", type=int, default=16, help="samples per cache frame")
@@ -419,11 +649,12 @@ def main():
     ap.add_argument("--nrc-configs", default="", help="'td,spf,steps;...' several cache settings in one run")
     ap.add_argument("--nrc-train-steps", type=int, default=4)
     ap.add_argument("--nrc-td", type=int, default=2, help="path vertex where render paths query the cache")
+    ap.add_argument("--nrc-rr", type=int, default=0, help="Russian roulette start depth of both tracers")
     args = ap.parse_args()
-    if args.workload == "nrc":
+    if args.workload != "trace":
         from __graft_entry__ import build
         build()
-        run_nrc(args)
+        {"nrc": run_nrc, "passes": run_passes, "batch": run_batch, "large": run_large}[args.workload](args)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -298,18 +298,17 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
                 return true;
             }
         } else {
-            unsigned long long key = ok ? ((unsigned long long)__float_as_uint(h) << 32) | k : ~0ull;
+            // minimum hit distance (positive floats order like their bits),
+            // then the lowest slot reaching it
+            uint32_t hb = ok ? __float_as_uint(h) : kGroupDone;
 #pragma unroll
-            for (int off = G / 2; off > 0; off >>= 1) {
-                const unsigned long long other = __shfl_xor_sync(gmask, key, off);
-                key = other < key ? other : key;
-            }
-            const uint32_t win = (uint32_t)key;
-            const unsigned src = gbase + ((key != ~0ull) ? (win - g.cur) : 0u);
+            for (int off = G / 2; off > 0; off >>= 1) hb = min(hb, __shfl_xor_sync(gmask, hb, off));
+            const unsigned tie = __ballot_sync(gmask, ok && __float_as_uint(h) == hb);
+            const unsigned src = tie ? (unsigned)(__ffs(tie) - 1) : gbase;
             const float wu = __shfl_sync(gmask, by, src), wv = __shfl_sync(gmask, bz, src);
-            if (key != ~0ull) {
-                g.slot = (int32_t)win;
-                g.len = __uint_as_float((uint32_t)(key >> 32));
+            if (tie) {
+                g.slot = (int32_t)(g.cur + (src - gbase));
+                g.len = __uint_as_float(hb);
                 g.u = wu;
                 g.v = wv;
             }

@@ -432,3 +432,118 @@ def heightfield_boxes(seed: int = 1, grid: int = 512, amplitude: float = 0.2, nu
         base += v.shape[0]
     return _pack(np.concatenate(parts_v), np.concatenate(parts_f), np.stack(mats), material_ids=np.concatenate(ids),
                  normals=np.concatenate(parts_n))
+
+
+def instanced_scene(seed: int = 1, num_triangles: int = 100_000, extent: float = 2.0):
+    """Random instances of an icosphere (level 3), a box and a torus (scale
+    U[0.05, 0.5], random rotation, position uniform in [-extent, extent]^3)
+    flattened into one mesh until about num_triangles triangles, plus a
+    ground quad below them and one area light (a random quad above the
+    instances, radiance U[5, 20]). Lambertian albedos U[0.1, 0.9]^3, one of 16
+    materials per instance. The batched-rendering workload draws 8 of these
+    with log-uniform triangle counts."""
+    rs = Stream(seed, 17)
+    iv, iff = icosphere(3)
+    bv, bf, bn = _flat_box(0.5)
+    tv, tf = torus_mesh()
+    meshes = [(iv, iff, iv), (bv, bf, bn), (tv, tf, vertex_normals(tv, tf))]
+    mats = [lambert(tuple(rs.uniform(3, 0.1, 0.9))) for _ in range(16)]
+    parts_v, parts_f, parts_n, ids = [], [], [], []
+    base = 0
+    total = 0
+    while total < num_triangles:
+        kind = int(rs.u64(1)[0] % 3)
+        v0, f0, n0 = meshes[kind]
+        s = rs.uniform(1, 0.05, 0.5)[0]
+        rot = quat_to_matrix(rs.quaternions(1)[0])
+        pos = rs.uniform(3, -extent, extent)
+        parts_v.append((v0 * s) @ rot.T + pos)
+        parts_n.append(n0 @ rot.T)
+        parts_f.append(f0 + base)
+        ids.append(np.full(len(f0), int(rs.u64(1)[0] % 16), np.uint32))
+        base += v0.shape[0]
+        total += len(f0)
+    g = 1.5 * extent
+    gv, gf, gn = _grid_quad((-g, -extent - 0.5, g), (2 * g, 0, 0), (0, 0, -2 * g), 1)  # ground, normal +y
+    parts_v.append(gv)
+    parts_f.append(gf + base)
+    parts_n.append(gn)
+    ids.append(np.full(len(gf), 0, np.uint32))
+    base += gv.shape[0]
+    size = rs.uniform(1, 0.5, 1.0)[0]
+    lc = rs.uniform(2, -0.5 * extent, 0.5 * extent)
+    lv, lf, ln = _grid_quad((lc[0] - size / 2, extent + 0.5, lc[1] - size / 2), (size, 0, 0), (0, 0, size), 1)
+    radiance = rs.uniform(1, 5.0, 20.0)[0]
+    mats.append(material_record(albedo=(0.0, 0.0, 0.0), specular=(0.0, 0.0, 0.0), emissivity=(radiance,) * 3))
+    parts_v.append(lv)
+    parts_f.append(lf + base)
+    parts_n.append(ln)
+    ids.append(np.full(len(lf), len(mats) - 1, np.uint32))
+    return _pack(np.concatenate(parts_v), np.concatenate(parts_f), np.stack(mats), material_ids=np.concatenate(ids),
+                 normals=np.concatenate(parts_n))
+
+
+def large_instanced(seed: int = 1, num_instances: int = 20_000, volume: float = 100.0, num_lights: int = 256,
+                    num_materials: int = 64):
+    """The large BDPT workload: num_instances instances of a radially
+    displaced icosphere (level 3, 1,280 triangles; 30 %) or a box (70 %),
+    scale U[0.5, 2], random rotation, positions uniform in [0, volume]^3
+    (about 7.9M triangles for 20k instances); num_materials materials, half
+    Lambertian (albedo U[0.1, 0.9]^3), half Phong (specular U[0.2, 0.9]^3,
+    exponent U[10, 1000]); num_lights light quads of side 0.5 with radiance
+    log-uniform in [1, 100], facing random directions. Meant for an
+    ellipsoid-bounded hierarchy."""
+    rs = Stream(seed, 29)
+    iv, iff = icosphere(3)
+    disp = 1.0 + rs.uniform(iv.shape[0], -0.05, 0.05)
+    iv = iv * disp[:, None]
+    inrm = vertex_normals(iv, iff)
+    bv, bf, bn = _flat_box(0.5)
+    mats = []
+    for k in range(num_materials):
+        if k % 2 == 0:
+            mats.append(lambert(tuple(rs.uniform(3, 0.1, 0.9))))
+        else:
+            exponent = rs.uniform(1, 10.0, 1000.0)[0]
+            mats.append(material_record(albedo=tuple(rs.uniform(3, 0.05, 0.4)), specular=tuple(rs.uniform(3, 0.2, 0.9)),
+                                        roughness=float(1.0 / math.sqrt(exponent))))
+    kinds = (rs.u64(num_instances) % np.uint64(10)) < np.uint64(3)
+    scale = rs.uniform(num_instances, 0.5, 2.0)
+    quats = rs.quaternions(num_instances)
+    pos = rs.uniform(3 * num_instances, 0.0, volume).reshape(num_instances, 3)
+    matid = (rs.u64(num_instances) % np.uint64(num_materials)).astype(np.uint32)
+    parts_v, parts_f, parts_n, ids = [], [], [], []
+    base = 0
+    for is_sphere, mesh in ((True, (iv, iff, inrm)), (False, (bv, bf, bn))):
+        sel = np.nonzero(kinds == is_sphere)[0]
+        v0, f0, n0 = mesh
+        R = np.stack([quat_to_matrix(q) for q in quats[sel]])            # (k, 3, 3)
+        vv = np.einsum("kij,vj->kvi", R, v0) * scale[sel][:, None, None] + pos[sel][:, None, :]
+        nn = np.einsum("kij,vj->kvi", R, n0)
+        ff = f0[None, :, :] + (base + np.arange(len(sel)) * v0.shape[0])[:, None, None]
+        parts_v.append(vv.reshape(-1, 3))
+        parts_n.append(nn.reshape(-1, 3))
+        parts_f.append(ff.reshape(-1, 3))
+        ids.append(np.repeat(matid[sel], f0.shape[0]))
+        base += len(sel) * v0.shape[0]
+    # lights: quads of side 0.5 with a random orientation
+    lpos = rs.uniform(3 * num_lights, 0.0, volume).reshape(num_lights, 3)
+    ldir = rs.unit_vectors(num_lights)
+    lrad = np.exp(rs.uniform(num_lights, 0.0, math.log(100.0)))
+    for k in range(num_lights):
+        nrm = ldir[k]
+        a = np.cross(nrm, [0.0, 1.0, 0.0] if abs(nrm[1]) < 0.9 else [1.0, 0.0, 0.0])
+        a /= np.linalg.norm(a)
+        b = np.cross(nrm, a)        # (b, a) winding makes the normal nrm: cross(b, a) = nrm
+        v, f, n = _grid_quad(lpos[k] - 0.25 * (a + b), 0.5 * b, 0.5 * a, 1)
+        parts_v.append(v)
+        parts_f.append(f + base)
+        parts_n.append(n)
+        mats.append(material_record(albedo=(0.0, 0.0, 0.0), specular=(0.0, 0.0, 0.0), emissivity=(lrad[k],) * 3))
+        ids.append(np.full(len(f), len(mats) - 1, np.uint32))
+        base += v.shape[0]
+    return _pack(np.concatenate(parts_v), np.concatenate(parts_f), np.stack(mats), material_ids=np.concatenate(ids),
+                 normals=np.concatenate(parts_n))
+
+
+LARGE_CAMERA = ((50.0, 50.0, -60.0), (50.0, 50.0, 50.0), (0.0, 1.0, 0.0), 55.0)
