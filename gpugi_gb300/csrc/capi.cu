@@ -1,4 +1,5 @@
 // Context lifetime, error reporting and the ray-query entry points of the C ABI.
+#include <algorithm>
 #include <cstring>
 
 #include "ctx.cuh"
@@ -63,6 +64,143 @@ static gpugi_status check_device_error(gpugi_ctx* ctx) {
 
 static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+static gpugi_status ensure_pipeline(gpugi_ctx* ctx) {
+    if (ctx->copyIn) return GPUGI_OK;
+    GPUGI_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copyIn, cudaStreamNonBlocking));
+    GPUGI_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copyOut, cudaStreamNonBlocking));
+    for (int k = 0; k < 8; ++k) {
+        GPUGI_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->evIn[k], cudaEventDisableTiming));
+        GPUGI_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->evTraced[k], cudaEventDisableTiming));
+    }
+    return GPUGI_OK;
+}
+
+// Ray queries on host arrays. Rays go through device staging in chunks of at
+// most 2^22. With trace modes 2-5 a chunk is split into ctx->hostParts parts
+// whose copies in (copyIn stream), traversal (context stream) and copies out
+// (copyOut stream) overlap: part p+1 uploads while part p is traced, and part
+// p downloads while part p+1 is traced. Each part has its own queue range and
+// counters. Returns when every result is in host memory.
+// Device address of page-locked host memory (cudaHostAlloc / cudaHostRegister),
+// or nullptr for any other memory.
+static void* mapped_host(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the error of an unknown pointer
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+static gpugi_status trace_host(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* const src[7],
+                               uint64_t n, int32_t* slot, float* t, float* u, float* v, uint8_t* occ) {
+    // Page-locked arrays: the kernels read the rays and write the results
+    // over the host link themselves (zero copy), with no staging round trip.
+    if (ctx->hostZeroCopy) {
+        const float* dsrc[7];
+        bool ok = true;
+        for (int k = 0; k < 7 && ok; ++k) ok = (dsrc[k] = static_cast<const float*>(mapped_host(src[k]))) != nullptr;
+        void* dout[4] = {nullptr, nullptr, nullptr, nullptr};
+        if (ok && anyHit) ok = (dout[0] = mapped_host(occ)) != nullptr;
+        if (ok && !anyHit) {
+            void* outs[4] = {slot, t, u, v};
+            for (int k = 0; k < 4 && ok; ++k) ok = (dout[k] = mapped_host(outs[k])) != nullptr;
+        }
+        if (ok) {
+            gpugi_status st = anyHit ? launch_trace_any(ctx, sc, dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4], dsrc[5],
+                                                        dsrc[6], n, static_cast<uint8_t*>(dout[0]))
+                                     : launch_trace_closest(ctx, sc, dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4],
+                                                            dsrc[5], dsrc[6], n, static_cast<int32_t*>(dout[0]),
+                                                            static_cast<float*>(dout[1]), static_cast<float*>(dout[2]),
+                                                            static_cast<float*>(dout[3]));
+            if (st) return st;
+            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+            return GPUGI_OK;
+        }
+    }
+    const uint64_t chunk = n < (1ull << 22) ? n : (1ull << 22);
+    const size_t col = align256(chunk * 4);
+    gpugi_status st = ensure_stage(ctx, 11 * col);
+    if (st) return st;
+    char* base = static_cast<char*>(ctx->stageDev);
+    float* d[7];
+    for (int k = 0; k < 7; ++k) d[k] = reinterpret_cast<float*>(base + k * col);
+    int32_t* dSlot = reinterpret_cast<int32_t*>(base + 7 * col);
+    float* dT = reinterpret_cast<float*>(base + 8 * col);
+    float* dU = reinterpret_cast<float*>(base + 9 * col);
+    float* dV = reinterpret_cast<float*>(base + 10 * col);
+    uint8_t* dOcc = reinterpret_cast<uint8_t*>(base + 7 * col);
+    const uint32_t parts = std::min<uint32_t>(std::max<uint32_t>(ctx->hostParts, 1u), 8u);
+    const bool pipe = ctx->traceMode >= 2 && parts > 1 && chunk >= (1ull << 16);
+    if (pipe) {
+        if ((st = ensure_pipeline(ctx)) || (st = ensure_queue(ctx, chunk))) return st;
+    }
+    for (uint64_t off = 0; off < n; off += chunk) {
+        const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
+        if (!pipe) {
+            for (int k = 0; k < 7; ++k)
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(d[k], src[k] + off, m * 4, cudaMemcpyHostToDevice, ctx->stream));
+            if (anyHit) st = launch_trace_any(ctx, sc, d[0], d[1], d[2], d[3], d[4], d[5], d[6], m, dOcc);
+            else st = launch_trace_closest(ctx, sc, d[0], d[1], d[2], d[3], d[4], d[5], d[6], m, dSlot, dT, dU, dV);
+            if (st) return st;
+            if (anyHit) {
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(occ + off, dOcc, m, cudaMemcpyDeviceToHost, ctx->stream));
+            } else {
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(slot + off, dSlot, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(t + off, dT, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(u + off, dU, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(v + off, dV, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            }
+            continue;
+        }
+        // parts of whole float4 groups, so every part starts 16-B aligned
+        const uint64_t per = ((m + parts - 1) / parts + 3) / 4 * 4;
+        unsigned long long* counters = reinterpret_cast<unsigned long long*>(ctx->scratch);
+        for (uint32_t p = 0; p < parts; ++p) {
+            const uint64_t p0 = p * per;
+            if (p0 >= m) break;
+            const uint64_t mp = std::min(per, m - p0);
+            for (int k = 0; k < 7; ++k)
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(d[k] + p0, src[k] + off + p0, mp * 4, cudaMemcpyHostToDevice,
+                                                    ctx->copyIn));
+            GPUGI_CUDA_TRY(ctx, cudaEventRecord(ctx->evIn[p], ctx->copyIn));
+        }
+        for (uint32_t p = 0; p < parts; ++p) {
+            const uint64_t p0 = p * per;
+            if (p0 >= m) break;
+            const uint64_t mp = std::min(per, m - p0);
+            GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->evIn[p], 0));
+            GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counters + 4 * p, 0, 4 * sizeof(unsigned long long), ctx->stream));
+            if ((st = launch_trace_filtered_on(ctx, sc, anyHit, d[0] + p0, d[1] + p0, d[2] + p0, d[3] + p0, d[4] + p0,
+                                               d[5] + p0, d[6] + p0, mp, anyHit ? nullptr : dSlot + p0,
+                                               anyHit ? nullptr : dT + p0, anyHit ? nullptr : dU + p0,
+                                               anyHit ? nullptr : dV + p0, anyHit ? dOcc + p0 : nullptr,
+                                               ctx->queue + p0, counters + 4 * p)))
+                return st;
+            GPUGI_CUDA_TRY(ctx, cudaEventRecord(ctx->evTraced[p], ctx->stream));
+        }
+        for (uint32_t p = 0; p < parts; ++p) {
+            const uint64_t p0 = p * per;
+            if (p0 >= m) break;
+            const uint64_t mp = std::min(per, m - p0);
+            GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copyOut, ctx->evTraced[p], 0));
+            if (anyHit) {
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(occ + off + p0, dOcc + p0, mp, cudaMemcpyDeviceToHost, ctx->copyOut));
+            } else {
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(slot + off + p0, dSlot + p0, mp * 4, cudaMemcpyDeviceToHost,
+                                                    ctx->copyOut));
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(t + off + p0, dT + p0, mp * 4, cudaMemcpyDeviceToHost, ctx->copyOut));
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(u + off + p0, dU + p0, mp * 4, cudaMemcpyDeviceToHost, ctx->copyOut));
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(v + off + p0, dV + p0, mp * 4, cudaMemcpyDeviceToHost, ctx->copyOut));
+            }
+        }
+        // the next chunk reuses the staging columns
+        GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->copyOut));
+    }
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return GPUGI_OK;
+}
+
 }  // namespace gpugi
 
 using namespace gpugi;
@@ -108,6 +246,16 @@ void gpugi_destroy(gpugi_ctx* ctx) {
     if (ctx->errWord) cudaFree(ctx->errWord);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->queue) cudaFree(ctx->queue);
+    if (ctx->copyIn) {
+        cudaStreamSynchronize(ctx->copyIn);
+        cudaStreamSynchronize(ctx->copyOut);
+        cudaStreamDestroy(ctx->copyIn);
+        cudaStreamDestroy(ctx->copyOut);
+        for (int k = 0; k < 8; ++k) {
+            cudaEventDestroy(ctx->evIn[k]);
+            cudaEventDestroy(ctx->evTraced[k]);
+        }
+    }
     cudaStreamDestroy(ctx->stream);
     for (gpugi_ctx** ref : ctx->children) *ref = nullptr;
     delete ctx;
@@ -141,6 +289,14 @@ gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t bloc
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "blockSize must be a multiple of 32 in [32, 256]");
     ctx->traceMode = mode;
     ctx->traceBlock = blockSize;
+    return GPUGI_OK;
+}
+
+gpugi_status gpugi_set_host_pipeline(gpugi_ctx* ctx, uint32_t parts, uint32_t zeroCopy) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (parts < 1 || parts > 8) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "parts must be in [1, 8]");
+    ctx->hostParts = parts;
+    ctx->hostZeroCopy = zeroCopy ? 1u : 0u;
     return GPUGI_OK;
 }
 
@@ -199,30 +355,9 @@ gpugi_status gpugi_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const fl
     if (!sc || (n && (!ox || !oy || !oz || !dx || !dy || !dz || !tmax || !slot || !t || !u || !v)))
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
     if (n == 0) return GPUGI_OK;
-    const uint64_t chunk = n < (1ull << 22) ? n : (1ull << 22);
-    const size_t col = align256(chunk * 4);
-    gpugi_status st = ensure_stage(ctx, 11 * col);
+    const float* const src[7] = {ox, oy, oz, dx, dy, dz, tmax};
+    gpugi_status st = trace_host(ctx, sc, false, src, n, slot, t, u, v, nullptr);
     if (st) return st;
-    char* base = static_cast<char*>(ctx->stageDev);
-    float* d[7];
-    for (int k = 0; k < 7; ++k) d[k] = reinterpret_cast<float*>(base + k * col);
-    int32_t* dSlot = reinterpret_cast<int32_t*>(base + 7 * col);
-    float* dT = reinterpret_cast<float*>(base + 8 * col);
-    float* dU = reinterpret_cast<float*>(base + 9 * col);
-    float* dV = reinterpret_cast<float*>(base + 10 * col);
-    const float* src[7] = {ox, oy, oz, dx, dy, dz, tmax};
-    for (uint64_t off = 0; off < n; off += chunk) {
-        const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
-        for (int k = 0; k < 7; ++k)
-            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(d[k], src[k] + off, m * 4, cudaMemcpyHostToDevice, ctx->stream));
-        if ((st = launch_trace_closest(ctx, sc, d[0], d[1], d[2], d[3], d[4], d[5], d[6], m, dSlot, dT, dU, dV)))
-            return st;
-        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(slot + off, dSlot, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(t + off, dT, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(u + off, dU, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(v + off, dV, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    }
-    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return check_device_error(ctx);
 }
 
@@ -233,23 +368,9 @@ gpugi_status gpugi_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float*
     if (!sc || (n && (!ox || !oy || !oz || !dx || !dy || !dz || !tmax || !occluded)))
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
     if (n == 0) return GPUGI_OK;
-    const uint64_t chunk = n < (1ull << 22) ? n : (1ull << 22);
-    const size_t col = align256(chunk * 4);
-    gpugi_status st = ensure_stage(ctx, 8 * col);
+    const float* const src[7] = {ox, oy, oz, dx, dy, dz, tmax};
+    gpugi_status st = trace_host(ctx, sc, true, src, n, nullptr, nullptr, nullptr, nullptr, occluded);
     if (st) return st;
-    char* base = static_cast<char*>(ctx->stageDev);
-    float* d[7];
-    for (int k = 0; k < 7; ++k) d[k] = reinterpret_cast<float*>(base + k * col);
-    uint8_t* dOcc = reinterpret_cast<uint8_t*>(base + 7 * col);
-    const float* src[7] = {ox, oy, oz, dx, dy, dz, tmax};
-    for (uint64_t off = 0; off < n; off += chunk) {
-        const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
-        for (int k = 0; k < 7; ++k)
-            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(d[k], src[k] + off, m * 4, cudaMemcpyHostToDevice, ctx->stream));
-        if ((st = launch_trace_any(ctx, sc, d[0], d[1], d[2], d[3], d[4], d[5], d[6], m, dOcc))) return st;
-        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(occluded + off, dOcc, m, cudaMemcpyDeviceToHost, ctx->stream));
-    }
-    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return check_device_error(ctx);
 }
 

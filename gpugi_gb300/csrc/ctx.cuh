@@ -26,6 +26,12 @@ struct gpugi_ctx {
     uint32_t* queue = nullptr;  // ray-index queue of the root prefilter (mode 2)
     uint64_t queueCap = 0;
     int numSMs = 0;
+    // host-pointer ray queries: copies in, traversal and copies out of
+    // hostParts parts of a call overlap on three streams (trace modes 2-5)
+    uint32_t hostParts = 2;
+    uint32_t hostZeroCopy = 1;  // page-locked host arrays are read and written by the kernels directly
+    cudaStream_t copyIn = nullptr, copyOut = nullptr;
+    cudaEvent_t evIn[8] = {}, evTraced[8] = {};
     // batched rendering
     uint32_t batchPaths = 16u << 20;  // path-queue capacity of one round
     uint32_t batchGraph = 1;          // replay rounds as a CUDA graph

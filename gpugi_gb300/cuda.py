@@ -57,6 +57,7 @@ def _declare(L):
         getattr(L, name).argtypes = [P, P] + [P] * 7 + [U64, P]
     L.gpugi_set_trace_config.argtypes = [P, U32, U32]
     L.gpugi_set_scene_layout.argtypes = [P, U32, U32]
+    L.gpugi_set_host_pipeline.argtypes = [P, U32, U32]
     L.gpugi_trace_stats_device.argtypes = [P, P] + [P] * 7 + [U64, U32, P]
     for name, args in _EXTRA_DECLS.items():
         if hasattr(L, name):
@@ -131,6 +132,11 @@ class Context:
 
     def set_trace_config(self, mode: int = 3, block_size: int = 128):
         self.check(lib().gpugi_set_trace_config(self._h, mode, block_size))
+
+    def set_host_pipeline(self, parts: int = 2, zero_copy: bool = True):
+        """Host-pointer queries: kernels access page-locked arrays directly (zero_copy), else
+        staging split into `parts` overlapping parts (1: no overlap)."""
+        self.check(lib().gpugi_set_host_pipeline(self._h, parts, int(bool(zero_copy))))
 
     def set_scene_layout(self, shared_nodes: int = 0, render_shared_nodes: int = 0):
         """Top-of-tree nodes staged in shared memory, for scenes uploaded afterwards."""

@@ -166,6 +166,15 @@ gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* scene,
  * return identical results. blockSize applies to mode 0. */
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize);
 
+/* Host-pointer ray queries (gpugi_trace_closest / gpugi_trace_any). With
+ * zeroCopy (default 1) and every array page-locked (cudaHostAlloc,
+ * cudaHostRegister), the kernels read the rays and write the results over
+ * the host link directly. Otherwise the arrays go through device staging,
+ * and each call is split into `parts` parts (1-8, default 2) whose copies to
+ * the device, traversal and copies back overlap on separate streams (trace
+ * modes 2-5; 1 disables the overlap). Results are the same on every path. */
+gpugi_status gpugi_set_host_pipeline(gpugi_ctx* ctx, uint32_t parts, uint32_t zeroCopy);
+
 /* Scene layout tuning (set by the autotuner), applied to scenes uploaded
  * afterwards: the top tree levels (up to sharedNodes nodes, whole levels) are
  * stored first, breadth first, and the persistent walkers stage them in

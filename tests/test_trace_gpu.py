@@ -236,3 +236,40 @@ def test_rejects_malformed_hierarchy(cuda_ctx):
     with pytest.raises(cuda.GpugiError):
         cuda_ctx.upload_scene(bad, sc["positions"])
     assert cuda_ctx.device_error_bits() == 0
+
+
+@pytest.mark.parametrize("parts,pinned", [(1, False), (2, False), (3, False), (8, False), (2, True)])
+def test_host_paths_give_identical_results(cuda_ctx, icosphere_65536, parts, pinned):
+    """Host-pointer queries: staged and split into overlapping parts (copies
+    in, traversal, copies out on three streams), or on page-locked arrays
+    read and written by the kernels directly; both return the oracle's
+    results, including a ray count that is not a multiple of the part size."""
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    cuda_ctx.set_host_pipeline(parts, zero_copy=True)
+    try:
+        rays = scenes.aimed_rays(300_001, sc["positions"], seed=21, spread=2.5)
+        if pinned:
+            rays = {k: torch.from_numpy(np.ascontiguousarray(v, dtype=np.float32)).pin_memory().numpy()
+                    for k, v in rays.items()}
+            n = rays["ox"].shape[0]
+            out = dict(slot=torch.empty(n, dtype=torch.int32).pin_memory().numpy(),
+                       t=torch.empty(n).pin_memory().numpy(), u=torch.empty(n).pin_memory().numpy(),
+                       v=torch.empty(n).pin_memory().numpy())
+            cuda_ctx.check(cuda.lib().gpugi_trace_closest(
+                cuda_ctx.handle, ds.handle, *[cuda._ptr(rays[k]) for k in cuda.RAY_KEYS], n,
+                *[cuda._ptr(out[k]) for k in ("slot", "t", "u", "v")]))
+            g = out
+            occ = torch.empty(n, dtype=torch.uint8).pin_memory().numpy()
+            cuda_ctx.check(cuda.lib().gpugi_trace_any(cuda_ctx.handle, ds.handle,
+                                                      *[cuda._ptr(rays[k]) for k in cuda.RAY_KEYS], n, cuda._ptr(occ)))
+        else:
+            g = cuda.trace_closest(cuda_ctx, ds, rays)
+            occ = cuda.trace_any(cuda_ctx, ds, rays)
+        _compare_closest(g, oracle.trace_closest(b, sc["positions"], rays))
+        assert np.array_equal(occ, oracle.trace_any(b, sc["positions"], rays)["occluded"])
+    finally:
+        cuda_ctx.set_host_pipeline(2)
+        ds.close()
