@@ -55,9 +55,9 @@ def _headers():
 def build_bvhmake(force=False) -> Path:
     LIB.mkdir(parents=True, exist_ok=True)
     out = LIB / "libgpugi_bvhmake.so"
-    src = CSRC / "bvhmake" / "bvhmake.cpp"
-    if force or _stale(out, [src] + _headers()):
-        _run([CXX] + HOST_FLAGS + ["-shared", "-o", str(out), str(src), "-pthread"])
+    srcs = [CSRC / "bvhmake" / "bvhmake.cpp", CSRC / "bvhmake" / "material_json.cpp"]
+    if force or _stale(out, srcs + _headers()):
+        _run([CXX] + HOST_FLAGS + ["-shared", "-o", str(out)] + [str(s) for s in srcs] + ["-pthread"])
     return out
 
 

@@ -38,6 +38,14 @@ def _lib():
         lib.gpugi_bvh_vertex_attributes.argtypes = [P, P, P]
         lib.gpugi_bvh_set_materials.argtypes = [P, P, U32]
         lib.gpugi_bvh_materials.argtypes = [P, C.POINTER(U32), P]
+        lib.gpugi_bvh_set_material_names.argtypes = [P, P, U32]
+        lib.gpugi_bvh_material_name.argtypes = [P, U32]
+        lib.gpugi_bvh_material_name.restype = C.c_char_p
+        lib.gpugi_bvh_num_material_names.argtypes = [P]
+        lib.gpugi_bvh_num_material_names.restype = U32
+        lib.gpugi_materials_from_json.argtypes = [C.c_char_p, P, U32, P]
+        lib.gpugi_materials_from_json.restype = I
+        lib.gpugi_materials_json_error.restype = C.c_char_p
         lib.gpugi_bvh_free.argtypes = [P]
         lib.gpugi_bvh_free.restype = None
         lib.gpugi_bvh_last_error.restype = C.c_char_p
@@ -61,6 +69,7 @@ class BVH:
     normals: np.ndarray | None = None      # from a file: float32 [V, 3]
     texcoords: np.ndarray | None = None    # from a file: float32 [V, 2]
     materials: np.ndarray | None = None    # from a file: float32 [M, 24] (empty when absent)
+    material_names: list | None = None     # from a file: the "materialref" chunk
 
     @property
     def num_nodes(self) -> int:
@@ -108,8 +117,25 @@ def build_bvh(positions: np.ndarray, triangles: np.ndarray, method: str = "sweep
         lib.gpugi_bvh_free(h)
 
 
+def _names_array(names):
+    arr = (C.c_char_p * len(names))(*[n.encode() for n in names])
+    return C.cast(arr, C.c_void_p), arr
+
+
+def materials_from_json(text: str, names) -> np.ndarray:
+    """Material records of the named materials of a gpugi scene JSON
+    (Scene::LoadMaterial's mapping and defaults)."""
+    lib = _lib()
+    ptr, keep = _names_array(list(names))
+    out = np.zeros((len(names), 24), dtype=np.float32)
+    rc = lib.gpugi_materials_from_json(text.encode(), ptr, len(names), _ptr(out))
+    if rc != 0:
+        raise ValueError(lib.gpugi_materials_json_error().decode())
+    return out
+
+
 def write_bvh_file(positions: np.ndarray, triangles: np.ndarray, path: str, normals=None, texcoords=None,
-                   materials=None, **kw) -> None:
+                   materials=None, material_names=None, **kw) -> None:
     """Build and write bvhmake's NamedArray file (vertex normals/texcoords
     and material records are optional)."""
     lib = _lib()
@@ -131,6 +157,10 @@ def write_bvh_file(positions: np.ndarray, triangles: np.ndarray, path: str, norm
         if materials is not None:
             mats = np.ascontiguousarray(materials, dtype=np.float32).reshape(-1, 24)
             lib.gpugi_bvh_set_materials(h, _ptr(mats), mats.shape[0])
+        if material_names is not None:
+            ptr, keep = _names_array(list(material_names))
+            if lib.gpugi_bvh_set_material_names(h, ptr, len(material_names)) != 0:
+                raise ValueError(lib.gpugi_bvh_last_error().decode())
         if lib.gpugi_bvh_write_file(h, str(path).encode()) != 0:
             raise OSError(lib.gpugi_bvh_last_error().decode())
     finally:
@@ -157,6 +187,8 @@ def read_bvh_file(path: str) -> BVH:
         b.materials = np.zeros((nm.value, 24), dtype=np.float32)
         if nm.value:
             lib.gpugi_bvh_materials(h, C.byref(nm), _ptr(b.materials))
+        b.material_names = [lib.gpugi_bvh_material_name(h, i).decode()
+                            for i in range(lib.gpugi_bvh_num_material_names(h))]
         return b
     finally:
         lib.gpugi_bvh_free(h)

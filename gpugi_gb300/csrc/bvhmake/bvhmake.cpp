@@ -163,6 +163,7 @@ struct gpugi_bvh {
     std::vector<float> normals;        // 3 per vertex (file attribute; may be empty)
     std::vector<float> texcoords;      // 2 per vertex (file attribute; may be empty)
     std::vector<float> materials;      // 24 per material ("gpugi_materials" chunk; may be empty)
+    std::vector<std::string> materialNames;  // "materialref" chunk
     std::vector<uint32_t> triangles;   // 4 per triangle
     uint32_t leafSize = 8;
     uint32_t boundsKind = GPUGI_FIT_AABOX;
@@ -682,6 +683,12 @@ int gpugi_bvh_write_file(const gpugi_bvh* b, const char* path) {
               WriteChunk(f, "triangles", nBlocks, 16 * b->leafSize, b->leaves.data()) &&
               (b->materials.empty() ||
                WriteChunk(f, "gpugi_materials", (uint32_t)(b->materials.size() / 24), 96, b->materials.data()));
+    if (ok && !b->materialNames.empty()) {
+        std::vector<char> names(b->materialNames.size() * 32, 0);
+        for (size_t i = 0; i < b->materialNames.size(); ++i)
+            std::strncpy(&names[32 * i], b->materialNames[i].c_str(), 31);
+        ok = WriteChunk(f, "materialref", (uint32_t)b->materialNames.size(), 32, names.data());
+    }
     std::fclose(f);
     if (!ok) {
         g_lastError = "short write";
@@ -722,6 +729,15 @@ int gpugi_bvh_read_file(const char* path, gpugi_bvh** out) {
                     std::memcpy(&b->normals[3 * (size_t)v], &data[(size_t)v * h.elementSize + 12], 12);
                     std::memcpy(&b->texcoords[2 * (size_t)v], &data[(size_t)v * h.elementSize + 24], 8);
                 }
+            }
+        } else if (name == "materialref") {
+            if (h.elementSize != 32) { rc = -4; g_lastError = "materialref element must be 32 bytes"; break; }
+            b->materialNames.clear();
+            for (uint32_t i = 0; i < h.numElements; ++i) {
+                char nm[33];
+                std::memcpy(nm, &data[32 * (size_t)i], 32);
+                nm[32] = 0;
+                b->materialNames.emplace_back(nm);
             }
         } else if (name == "gpugi_materials") {
             if (h.elementSize != 96) { rc = -4; g_lastError = "gpugi_materials element must be 96 bytes"; break; }
@@ -800,6 +816,25 @@ int gpugi_bvh_vertex_attributes(const gpugi_bvh* b, float* normals, float* texco
     }
     return 0;
 }
+
+int gpugi_bvh_set_material_names(gpugi_bvh* b, const char* const* names, uint32_t numNames) {
+    if (!b || (numNames && !names)) return -1;
+    b->materialNames.clear();
+    for (uint32_t i = 0; i < numNames; ++i) {
+        if (!names[i] || std::strlen(names[i]) > 31) {
+            g_lastError = "material names must be 1-31 characters";
+            return -2;
+        }
+        b->materialNames.emplace_back(names[i]);
+    }
+    return 0;
+}
+
+const char* gpugi_bvh_material_name(const gpugi_bvh* b, uint32_t index) {
+    return (b && index < b->materialNames.size()) ? b->materialNames[index].c_str() : nullptr;
+}
+
+uint32_t gpugi_bvh_num_material_names(const gpugi_bvh* b) { return b ? (uint32_t)b->materialNames.size() : 0; }
 
 int gpugi_bvh_set_materials(gpugi_bvh* b, const float* records, uint32_t numMaterials) {
     if (!b || (numMaterials && !records)) return -1;

@@ -127,8 +127,10 @@ struct PointLight {
 class Scene {
 public:
     // Loads bvhmake's NamedArray file: hierarchy, bounding volumes, triangle
-    // blocks, vertices {position, normal, texcoord} and the material records
-    // of its "gpugi_materials" chunk (a single grey Lambertian when absent).
+    // blocks, vertices {position, normal, texcoord}. Materials come from the
+    // scene JSON beside the file (<stem>.json, by the "materialref" names,
+    // with Scene::LoadMaterial's mapping), else from the file's
+    // "gpugi_materials" chunk, else a single grey Lambertian.
     Scene(gpugi_ctx* ctx, const std::string& file);
     ~Scene();
     Scene(const Scene&) = delete;

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 
 namespace {
 
@@ -94,11 +95,28 @@ Scene::Scene(gpugi_ctx* ctx, const std::string& file) : m_ctx(ctx) {
         vinfo[4 * v + 2] = texcoords[2 * v];
         vinfo[4 * v + 3] = texcoords[2 * v + 1];
     }
-    gpugi_bvh_materials(bvh, &m_numMaterials, nullptr);
-    std::vector<float> materials((size_t)m_numMaterials * 24);
-    if (m_numMaterials) {
-        gpugi_bvh_materials(bvh, &m_numMaterials, materials.data());
+    // Materials: the scene JSON next to the file (<stem>.json, as bvhmake
+    // writes it) looked up by the "materialref" names, as Scene::LoadMaterial
+    // does; else the file's "gpugi_materials" chunk; else one grey Lambertian.
+    std::vector<float> materials;
+    const uint32_t numNames = gpugi_bvh_num_material_names(bvh);
+    const size_t dot = file.find_last_of('.');
+    const std::string jsonPath = (dot == std::string::npos ? file : file.substr(0, dot)) + ".json";
+    std::ifstream json(jsonPath, std::ios::binary);
+    if (numNames && json) {
+        const std::string text((std::istreambuf_iterator<char>(json)), std::istreambuf_iterator<char>());
+        std::vector<const char*> names(numNames);
+        for (uint32_t i = 0; i < numNames; ++i) names[i] = gpugi_bvh_material_name(bvh, i);
+        materials.resize((size_t)numNames * 24);
+        if (gpugi_materials_from_json(text.c_str(), names.data(), numNames, materials.data()) != 0)
+            throw GpugiError(GPUGI_ERROR_INVALID_SCENE, jsonPath + ": " + gpugi_materials_json_error());
+        m_numMaterials = numNames;
     } else {
+        gpugi_bvh_materials(bvh, &m_numMaterials, nullptr);
+        materials.resize((size_t)m_numMaterials * 24);
+        if (m_numMaterials) gpugi_bvh_materials(bvh, &m_numMaterials, materials.data());
+    }
+    if (!m_numMaterials) {
         // one grey Lambertian: diffuse 0.5, ior 1.5, opacity 1, reflectiveness 1 (exponent 1), fresnel (0, 1)
         m_numMaterials = 1;
         materials.assign(24, 0.0f);

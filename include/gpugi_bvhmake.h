@@ -75,6 +75,21 @@ int gpugi_bvh_vertex_attributes(const gpugi_bvh* bvh, float* normals, float* tex
 int gpugi_bvh_set_materials(gpugi_bvh* bvh, const float* records, uint32_t numMaterials);
 int gpugi_bvh_materials(const gpugi_bvh* bvh, uint32_t* numMaterials, float* records /* may be NULL */);
 
+/* Material names of the "materialref" chunk (32-byte names, the order of the
+ * triangles' material indices; bvhbuilder.cpp:622-630). Set before writing;
+ * after reading, name i is returned (NULL past the end). */
+int gpugi_bvh_set_material_names(gpugi_bvh* bvh, const char* const* names, uint32_t numNames);
+const char* gpugi_bvh_material_name(const gpugi_bvh* bvh, uint32_t index);
+uint32_t gpugi_bvh_num_material_names(const gpugi_bvh* bvh);
+
+/* Material records (24 floats each, the gpugi_material layout) for the named
+ * materials of a scene JSON's "materials" object, with the parameter mapping
+ * and defaults of Scene::LoadMaterial (gpugi/scene/scene.cpp:132-180).
+ * 0 = OK; negative: parse error, missing material or a texture reference
+ * (see gpugi_materials_json_error). */
+int gpugi_materials_from_json(const char* json, const char* const* names, uint32_t numNames, float* records);
+const char* gpugi_materials_json_error(void);
+
 void gpugi_bvh_free(gpugi_bvh* bvh);
 const char* gpugi_bvh_last_error(void);
 

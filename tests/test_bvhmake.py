@@ -138,3 +138,51 @@ def test_file_carries_vertex_attributes_and_materials(built, tmp_path):
     bvh.write_bvh_file(sc["positions"], sc["triangles"], str(p), method="sweep", leaf_size=8)
     b = bvh.read_bvh_file(str(p))
     assert not b.normals.any() and b.materials.shape == (0, 24)
+
+
+SCENE_JSON = """{
+  "scene": "room.bim", "accelerator": "aabox",
+  "materials": {
+    "Matte":  {"type": "legacy", "albedo": [0.25, 0.5, 0.75], "roughness": [0.5], "opacity": [1]},
+    "Coated": {"albedo": [0.1, 0.1, 0.1], "specularColor": [0.2, 0.3, 0.4], "roughness": 0.1,
+               "opacity": [0.0, 0.0, 0.0], "refractionIndex": 1.33},
+    "Lamp":   {"emissivity": [10, 20, 30], "reflectiveness": [0.5, 0.6, 0.7]},
+    "Textured": {"albedo": "wood.png"}
+  },
+  "lights": {}, "cameras": {}
+}"""
+
+
+def test_material_json_uses_load_material_mapping(built):
+    """Scene::LoadMaterial (gpugi/scene/scene.cpp:132-180): fresnel0 defaults
+    to 0.03, fresnel1 = 1 - fresnel0, exponent = 1 / (roughness^2 + 1e-20),
+    scalar parameters read the first array element, reflectiveness.w is the
+    exponent, unset values take the defaults."""
+    m = bvh.materials_from_json(SCENE_JSON, ["Lamp", "Matte", "Coated"])
+    f = np.float32
+    lamp, matte, coated = m
+    assert np.allclose(lamp[0:3], 0.5) and lamp[3] == f(1.5) and np.allclose(lamp[4:7], 1.0)
+    assert np.allclose(lamp[8:11], [0.5, 0.6, 0.7]) and lamp[11] == f(1.0) / (f(1.0) + f(1e-20))
+    assert np.allclose(lamp[12:15], [10, 20, 30]) and np.allclose(lamp[16:19], 0.03)
+    assert np.allclose(lamp[20:23], 0.97)
+    assert np.allclose(matte[0:3], [0.25, 0.5, 0.75]) and matte[11] == f(1.0) / (f(0.25) + f(1e-20))
+    assert np.allclose(coated[16:19], [0.2, 0.3, 0.4]) and np.allclose(coated[20:23], [0.8, 0.7, 0.6])
+    assert np.allclose(coated[4:7], 0.0) and coated[3] == f(1.33)
+    assert np.isclose(coated[11], 1.0 / (0.1 * 0.1))
+
+
+@pytest.mark.parametrize("text,names", [(SCENE_JSON, ["Textured"]), (SCENE_JSON, ["Missing"]),
+                                        ('{"materials": {', ["Matte"]), ("[1, 2]", ["Matte"])])
+def test_material_json_errors(built, text, names):
+    with pytest.raises(ValueError):
+        bvh.materials_from_json(text, names)
+
+
+def test_file_carries_material_names(built, tmp_path):
+    sc = scenes.displaced_icosphere(500, seed=5)
+    p = tmp_path / "named.bim"
+    bvh.write_bvh_file(sc["positions"], sc["triangles"], str(p), material_names=["Matte", "Coated"])
+    b = bvh.read_bvh_file(str(p))
+    assert b.material_names == ["Matte", "Coated"]
+    with pytest.raises(ValueError):
+        bvh.write_bvh_file(sc["positions"], sc["triangles"], str(p), material_names=["x" * 40])

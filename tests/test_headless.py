@@ -100,3 +100,26 @@ def test_headless_texture_mse_and_nrc(cuda_ctx, room_file, tmp_path):
     assert info_nrc["renderer"] == "NrcPathtracer"
     img = _read_pfm(nrc)
     assert np.isfinite(img).all() and img.mean() > 0
+
+
+@pytest.mark.gpu
+def test_headless_reads_materials_from_scene_json(cuda_ctx, room_file, tmp_path):
+    """A scene file with material names and a gpugi-style scene JSON beside
+    it renders like the same file carrying the material records."""
+    sc, path = room_file
+    mats = sc["materials"].reshape(-1, 24)
+    names = [f"mat{i}" for i in range(mats.shape[0])]
+    entries = {n: {"type": "legacy", "albedo": [float(x) for x in m[0:3]], "specularColor": [0, 0, 0],
+                   "roughness": [1], "opacity": [1], "emissivity": [float(x) for x in m[12:15]]}
+               for n, m in zip(names, mats)}
+    named = tmp_path / "named.bim"
+    bvh.write_bvh_file(sc["positions"], sc["triangles"], str(named), normals=sc["normals"],
+                       texcoords=sc["texcoords"], material_names=names, method="sweep", leaf_size=8)
+    (tmp_path / "named.json").write_text(json.dumps({"scene": "named.bim", "materials": entries}))
+    assert np.allclose(bvh.materials_from_json((tmp_path / "named.json").read_text(), names), mats)
+    common = ["--size", 32, 32, "--camera", *CAM, "--path-length", 6, "--iterations", 4]
+    a, b_ = tmp_path / "a.pfm", tmp_path / "b.pfm"
+    _run(["--scene", path] + common + ["--out", a])
+    _run(["--scene", named] + common + ["--out", b_])
+    ia, ib = _read_pfm(a), _read_pfm(b_)
+    assert np.abs(ia - ib).max() <= 1e-5 * np.abs(ia).max() + 1e-6
