@@ -1,8 +1,8 @@
 """The C++ renderer classes (RendererSystem, Pathtracer, ..., TextureMSE)
 through the headless driver, against the Python front end of the same C ABI.
 
-The driver sets up a RendererSystem the way the reference's Application
-does; its first iteration uses the first light-sample set drawn from the
+The headless program sets up a RendererSystem the way the reference's
+Application does; its first iteration uses the first light-sample set drawn from the
 sampler state 123 and the frame seed of iteration 0, so the same images
 come out of gpugi_render(samples=N, rngState=123).
 """

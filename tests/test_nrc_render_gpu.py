@@ -1,7 +1,7 @@
 """Path tracing with the radiance cache (gpugi_render_nrc) on the GPU.
 
-The reference has no radiance cache; the plain path tracer (itself checked
-against the oracle in test_render_gpu.py) is the judge:
+The reference has no radiance cache; the cache is checked against the plain
+path tracer (itself checked against the oracle in test_render_gpu.py):
   * with no cache lookups the pass is exactly the path tracer, whether the
     paths are render paths or training paths (atomic splat order aside);
   * on a sky-lit floor whose reflected radiance is known in closed form
