@@ -361,8 +361,8 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
     return false;
 }
 
-// Persistent loop of group walks over n work items: groups that need a ray
-// take the next item (one atomic per warp). load(i, o, d, tmax) fills the
+// Persistent loop of group walks over n work items: a group takes the next
+// item with one atomic when its walk ends. load(i, o, d, tmax) fills the
 // ray of item i; finish(i, walk) runs in the group's first lane. With MULTI
 // the rays belong to different scenes: load returns the item's scene and its
 // bounds kind selects the node test per round; otherwise every ray walks
@@ -370,51 +370,39 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
 template <bool ANY_HIT, int BOUNDS, int G, bool MULTI, typename Load, typename Finish>
 GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long long* work, uint32_t* err, Load load,
                               Finish finish) {
+    // Each group fetches its next item with its own atomic and leaves the
+    // loop once the items are exhausted: the loop has no warp-wide
+    // synchronisation, so the last long walks of a warp do not wait for
+    // idle groups at every round (all shuffles stay inside the group).
     const unsigned lane = threadIdx.x & 31u;
     const unsigned gl = lane & (G - 1), gbase = lane & ~(unsigned)(G - 1);
     const unsigned gmask = ((1u << G) - 1u) << gbase;
     GroupWalk g;
     const DevScene* sc = nullptr;
-    uint64_t item = 0;
-    bool active = false, exhausted = false;
     while (true) {
-        const bool need = !active && !exhausted;
-        const unsigned needMask = __ballot_sync(0xffffffffu, need && gl == 0);
-        if (needMask) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(work, (unsigned long long)__popc(needMask));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (need) {
-                const uint64_t my = base + (uint64_t)__popc(needMask & ((1u << gbase) - 1u));
-                if (my < n) {
-                    item = my;
-                    float3 o, d;
-                    float tmax;
-                    if constexpr (MULTI) {
-                        sc = load(item, o, d, tmax);
-                        group_begin(g, *sc, o, d, tmax);
-                    } else {
-                        load(item, o, d, tmax);
-                        group_begin(g, scene, o, d, tmax);
-                    }
-                    active = true;
-                } else {
-                    exhausted = true;
-                }
-            }
+        unsigned long long my = 0;
+        if (gl == 0) my = atomicAdd(work, 1ull);
+        my = __shfl_sync(gmask, my, gbase);
+        if (my >= n) break;
+        float3 o, d;
+        float tmax;
+        if constexpr (MULTI) {
+            sc = load(my, o, d, tmax);
+            group_begin(g, *sc, o, d, tmax);
+        } else {
+            load(my, o, d, tmax);
+            group_begin(g, scene, o, d, tmax);
         }
-        if (!__any_sync(0xffffffffu, active)) break;
-        if (!active) continue;
-        bool done;
-        if constexpr (MULTI)
-            done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? group_step<ANY_HIT, 1, G>(g, *sc, err, gl, gbase, gmask)
-                                                           : group_step<ANY_HIT, 0, G>(g, *sc, err, gl, gbase, gmask);
-        else
-            done = group_step<ANY_HIT, BOUNDS, G>(g, scene, err, gl, gbase, gmask);
-        if (done) {
-            if (gl == 0) finish(item, g);
-            active = false;
+        bool done = false;
+        while (!done) {
+            if constexpr (MULTI)
+                done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID
+                           ? group_step<ANY_HIT, 1, G>(g, *sc, err, gl, gbase, gmask)
+                           : group_step<ANY_HIT, 0, G>(g, *sc, err, gl, gbase, gmask);
+            else
+                done = group_step<ANY_HIT, BOUNDS, G>(g, scene, err, gl, gbase, gmask);
         }
+        if (gl == 0) finish(my, g);
     }
 }
 
