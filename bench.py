@@ -432,6 +432,73 @@ def run_large(args):
     ctx.close()
 
 
+def run_build(args):
+    """Hierarchy build on the GPU (gpugi_scene_build, linear BVH) against the
+    host build (bvhmake sweep SAH, then gpugi_scene_upload), on the large
+    workload's ~7.9M triangles (AABB nodes) and on the 65,536-triangle
+    icosphere of the headline. Build: wall time from host arrays to a
+    traversable scene (after one untimed GPU build). Traversal: closest-hit
+    Mrays/s on each tree (large: 2^22 random rays inside the volume;
+    icosphere: the headline's 2^20 rays), CUDA events."""
+    import torch
+    from gpugi_gb300 import bvh, cuda, scenes
+    ctx = cuda.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def ev_time(fn, reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fn()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    def to_dev(r):
+        return {k: torch.from_numpy(np.ascontiguousarray(r[k])).cuda() for k in cuda.RAY_KEYS}
+
+    out = {}
+    big = scenes.large_instanced(seed=1)
+    n = 1 << 22
+    g = torch.Generator(device="cuda").manual_seed(5)
+    o = torch.rand((3, n), device="cuda", generator=g) * 100.0
+    d = torch.randn((3, n), device="cuda", generator=g)
+    d /= d.norm(dim=0, keepdim=True)
+    big_rays = {"ox": o[0].contiguous(), "oy": o[1].contiguous(), "oz": o[2].contiguous(), "dx": d[0].contiguous(),
+                "dy": d[1].contiguous(), "dz": d[2].contiguous(),
+                "tmax": torch.full((n,), 3.402823466e38, device="cuda")}
+    ico, _, batches = make_workload()
+    ico_rays = to_dev(batches[0])
+    for name, sc, rays in (("large", big, big_rays), ("icosphere", ico, ico_rays)):
+        m = rays["ox"].numel()
+        res = {"triangles": int(sc["triangles"].shape[0]), "rays": m}
+        t0 = time.perf_counter()
+        hb = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+        host = ctx.upload_scene(hb, sc["positions"])
+        res["host_build_s"] = time.perf_counter() - t0
+        ctx.build_scene(sc["positions"], sc["triangles"]).close()
+        ctx.sync()
+        t0 = time.perf_counter()
+        gpu = ctx.build_scene(sc["positions"], sc["triangles"])
+        res["gpu_build_s"] = time.perf_counter() - t0
+        res["nodes"] = {"host_sweep": host.num_nodes, "gpu_lbvh": gpu.num_nodes}
+        outs = dict(slot=torch.empty(m, dtype=torch.int32, device="cuda"), t=torch.empty(m, device="cuda"),
+                    u=torch.empty(m, device="cuda"), v=torch.empty(m, device="cuda"))
+        torch.cuda.synchronize()
+        for key, ds in (("host_sweep", host), ("gpu_lbvh", gpu)):
+            sec = ev_time(lambda: cuda.trace_closest_device(ctx, ds, rays, outs), 5)
+            res[f"{key}_mrays_per_s"] = m / sec / 1e6
+        out[name] = res
+        host.close()
+        gpu.close()
+    line = {"metric": "hierarchy build time, GPU linear BVH vs host sweep SAH", "unit": "s", "results": out,
+            "config": {"workload": "large: ~7.9M tris (20k instances in 100^3); icosphere: 65,536 tris (headline)",
+                       "leaf_size": 8, "bounds": "AABB"}, "data": "synthetic", "dtype": "f32"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_batch(args):
     """Batched rendering workload: 8 scenes of instanced icospheres, boxes and
     tori (triangle counts log-uniform in [10k, 2M]), each with a random
@@ -530,25 +597,44 @@ def run_batch(args):
 
 
 def run_nrc(args):
-    """Time to equal RMSE, path tracing with the radiance cache vs plain path
-    tracing, on the heightfield workload (522k-triangle fBm terrain + 500
-    boxes, sun of irradiance 5, sky 0.5, Lambertian albedos U[0.1, 0.8],
-    depth 8). RMSE is TextureMSE's, in FP64, against an FP64-accumulated
-    plain-PT image of --nrc-ref-spp samples. Plain PT accumulates 1024 spp
-    (doubling chunks); its final RMSE is the target and its wall time T_pt.
-    The cache path tracer first trains for --nrc-warmup frames (timed, not
-    accumulated), then accumulates frames until its RMSE reaches the target
-    or its time exceeds 3 T_pt. Wall times: host clock around synchronised
-    calls (both renderers synchronise internally)."""
+    """Time to equal RMSE, rendering with the radiance cache vs the plain
+    renderer of the same pass. PT (default): the heightfield workload
+    (522k-triangle fBm terrain + 500 boxes, sun of irradiance 5, sky 0.5,
+    Lambertian albedos U[0.1, 0.8], depth 8). BPT (--nrc-pass BPT): the large
+    workload (~7.9M triangles in 20k instances, 64 Lambertian / Phong
+    materials, 256 area lights, ellipsoid hierarchy, depth 6), with eye
+    paths that stop at the cache vertex. RMSE is TextureMSE's, in FP64,
+    against an FP64-accumulated image of the plain pass with --nrc-ref-spp
+    samples. The plain pass accumulates 1024 spp (doubling chunks); its final
+    RMSE is the target and its wall time T_plain. The cache renderer first
+    trains for --nrc-warmup frames (timed, not accumulated), then accumulates
+    frames until its RMSE reaches the target or its time exceeds 3 T_plain.
+    Wall times: host clock around synchronised calls (both renderers
+    synchronise internally)."""
     from gpugi_gb300 import bvh, cuda, nrc, render, scenes
-    W, H = args.nrc_size
-    depth, sky, rr = 8, (0.5, 0.5, 0.5), args.nrc_rr
+    pass_ = args.nrc_pass
+    W, H = args.nrc_size if args.nrc_size else ((640, 360) if pass_ == "PT" else (480, 270))
+    rr = args.nrc_rr
     ctx = cuda.Context(0)
-    sc = scenes.heightfield_boxes(seed=1)
-    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    if pass_ == "PT":
+        depth, sky = 8, (0.5, 0.5, 0.5)
+        sc = scenes.heightfield_boxes(seed=1)
+        b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+        box = ((-1.05, -0.25, -1.05), (1.05, 0.35, 1.05))
+        cam_args = scenes.HEIGHTFIELD_CAMERA
+        workload = "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8"
+    else:
+        depth, sky = 6, (0.0, 0.0, 0.0)
+        sc = scenes.large_instanced(seed=1)
+        b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", fit="ellipsoid")
+        box = ((-3.0, -3.0, -3.0), (103.0, 103.0, 103.0))
+        cam_args = scenes.LARGE_CAMERA
+        workload = ("~7.9M tris (20k instances in 100^3), 64 Lambertian/Phong materials, 256 area lights, "
+                    "ellipsoid BVH, depth 6")
     ds = ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]), sc["materials"])
-    render.add_directional_light(ds, scenes.HEIGHTFIELD_SUN, (5.0, 5.0, 5.0))
-    cam = render.camera_lookat(*scenes.HEIGHTFIELD_CAMERA, W, H)
+    if pass_ == "PT":
+        render.add_directional_light(ds, scenes.HEIGHTFIELD_SUN, (5.0, 5.0, 5.0))
+    cam = render.camera_lookat(*cam_args, W, H)
 
     def timed(fn):
         ctx.sync()
@@ -558,7 +644,7 @@ def run_nrc(args):
         return time.perf_counter() - t0
 
     conv = render.Image(ctx, W, H, fp64=True)
-    t_ref = timed(lambda: render.render(ctx, ds, cam, conv, "PT", max_path_length=depth, samples=args.nrc_ref_spp,
+    t_ref = timed(lambda: render.render(ctx, ds, cam, conv, pass_, max_path_length=depth, samples=args.nrc_ref_spp,
                                         iteration=1 << 24, rng_state=[99], sky=sky, rr_start_depth=rr))
     ref = (conv.read64() / args.nrc_ref_spp).astype(np.float32)
     conv.close()
@@ -569,14 +655,13 @@ def run_nrc(args):
     pt = render.Image(ctx, W, H, fp64=True)
     t_pt, spp, pt_curve = 0.0, 0, []
     for c in [1, 1, 2, 4, 8, 16, 32, 64, 128, 256, 512]:
-        t_pt += timed(lambda: render.render(ctx, ds, cam, pt, "PT", max_path_length=depth, samples=c, iteration=spp,
+        t_pt += timed(lambda: render.render(ctx, ds, cam, pt, pass_, max_path_length=depth, samples=c, iteration=spp,
                                             rng_state=[7 + spp], sky=sky, rr_start_depth=rr))
         spp += c
         pt_curve.append((spp, round(t_pt, 5), round(rmse(pt, spp), 6)))
     target = pt_curve[-1][2]
     pt.close()
 
-    box = ((-1.05, -0.25, -1.05), (1.05, 0.35, 1.05))
     configs = [tuple(int(x) for x in c.split(",")) for c in args.nrc_configs.split(";")] if args.nrc_configs else \
         [(args.nrc_td, args.nrc_spf, args.nrc_train_steps)]
     for td, spf, steps in configs:
@@ -584,7 +669,7 @@ def run_nrc(args):
         tf = args.nrc_train_fraction or min(0.05, 1.5 * 65536 / (3.0 * W * H * spf))
         cache = nrc.RadianceCache(ctx, *box, seed=5)
         opts = dict(max_path_length=depth, sky=sky, terminate_depth=td, train_fraction=tf, train_steps=steps,
-                    samples_per_frame=spf, rr_start_depth=rr)
+                    samples_per_frame=spf, rr_start_depth=rr, pass_=pass_)
         scratch = render.Image(ctx, W, H)
         t_nrc = timed(lambda: nrc.render_nrc(ctx, ds, cam, scratch, cache, samples=args.nrc_warmup * spf,
                                              iteration=1 << 20, rng_state=[11], **opts))
@@ -604,13 +689,13 @@ def run_nrc(args):
                 reached = t_nrc
                 break
             chunk = min(chunk * 2, max(1, 64 // spf))
-        line = {"metric": "time to the 1024-spp plain-PT RMSE, NRC path tracing vs plain PT", "unit": "ratio",
+        line = {"metric": f"time to the 1024-spp plain-{pass_} RMSE, {pass_} with the radiance cache vs plain {pass_}",
+                "unit": "ratio",
                 "value": (reached / t_pt) if reached else None, "higher_is_better": False,
                 "t_pt_s": round(t_pt, 4), "t_nrc_s": round(reached, 4) if reached else None,
                 "t_nrc_warmup_s": round(t_warm, 4), "target_rmse": target,
                 "nrc_rmse_at_equal_time": at_equal_time,
-                "config": {"workload": "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8",
-                           "rr_start_depth": rr,
+                "config": {"workload": workload, "pass": pass_, "rr_start_depth": rr,
                            "resolution": [W, H], "reference_spp": args.nrc_ref_spp, "reference_s": round(t_ref, 2),
                            "nrc": {"terminate_depth": td, "train_fraction": round(tf, 5), "train_steps": steps,
                                    "samples_per_frame": spf, "warmup_frames": args.nrc_warmup,
@@ -642,10 +727,13 @@ def main():
                     help="parts of a host-pointer query whose copies and traversal overlap")
     ap.add_argument("--no-zero-copy", action="store_true",
                     help="stage page-locked host arrays through device memory instead of direct access")
-    ap.add_argument("--workload", choices=["trace", "nrc", "passes", "batch", "large"], default="trace",
+    ap.add_argument("--workload", choices=["trace", "nrc", "passes", "batch", "large", "build"], default="trace",
                     help="trace: the closest-hit headline; nrc: time-to-equal-RMSE of the radiance cache; "
-                         "passes: samples/s and Mrays/s of PT, LT and BPT; batch: batched vs per-job rendering")
-    ap.add_argument("--nrc-size", type=int, nargs=2, default=[640, 360])
+                         "passes: samples/s and Mrays/s of PT, LT and BPT; batch: batched vs per-job rendering; "
+                         "large: the 7.9M-triangle workload; build: GPU vs host hierarchy build")
+    ap.add_argument("--nrc-pass", choices=["PT", "BPT"], default="PT",
+                    help="PT: heightfield workload; BPT: large workload (eye paths stop at the cache vertex)")
+    ap.add_argument("--nrc-size", type=int, nargs=2, default=None, help="default 640 360 (PT), 480 270 (BPT)")
     ap.add_argument("--nrc-ref-spp", type=int, default=16384)
     ap.add_argument("--nrc-spf", type=int, default=16, help="samples per cache frame")
     ap.add_argument("--nrc-warmup", type=int, default=16, help="training frames before accumulation")
@@ -659,7 +747,8 @@ def main():
     if args.workload != "trace":
         from __graft_entry__ import build
         build()
-        {"nrc": run_nrc, "passes": run_passes, "batch": run_batch, "large": run_large}[args.workload](args)
+        {"nrc": run_nrc, "passes": run_passes, "batch": run_batch, "large": run_large,
+         "build": run_build}[args.workload](args)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -69,6 +69,7 @@ GPUGI_HD float3 xyz(float4 v) { return make_float3(v.x, v.y, v.z); }
 constexpr uint32_t DEVERR_TRAVERSAL_CAP = 0x1u;
 constexpr uint32_t DEVERR_QUEUE_OVERFLOW = 0x2u;
 constexpr uint32_t DEVERR_WAIT_TIMEOUT = 0x4u;
+constexpr uint32_t DEVERR_BUILD = 0x8u;  // GPU hierarchy build: a walk to the root exceeded the tree depth bound
 
 GPUGI_D void raise_error(uint32_t* word, uint32_t bits) {
     if (word) atomicOr(word, bits);

@@ -142,6 +142,9 @@ gpugi_status nrc_infer_counted(gpugi_ctx* ctx, const gpugi_nrc* nn, const float*
                                const uint32_t* count, float* out);
 gpugi_status nrc_train_counted(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples, uint64_t cap,
                                const uint32_t* count);
+// Per-slot triangle records {p0, e0, e1, n} of a device slot array (scene.cu).
+void prepare_triangles(cudaStream_t stream, const int4* slots, uint32_t numSlots, const float* positions,
+                       float4* tris);
 // Light tables and the host light sampler (host.cu).
 void build_light_tables(gpugi_scene* sc);
 void generate_light_samples(gpugi_scene* sc, uint64_t& rng, uint32_t numSamples, float* out);

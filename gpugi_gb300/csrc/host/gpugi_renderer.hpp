@@ -307,10 +307,24 @@ public:
     void SetTraining(bool train) { m_train = train; }
     gpugi_nrc* GetCache() const { return m_nrc; }
 
+protected:
+    NrcPathtracer(RendererSystem& rendererSystem, const NrcSettings& settings, gpugi_pass pass);
+
 private:
     NrcSettings m_settings;
     gpugi_nrc* m_nrc = nullptr;
     bool m_train = true;
+    gpugi_pass m_pass = GPUGI_PASS_PT;
+};
+
+// Bidirectional path tracer whose eye paths end in the radiance cache at
+// vertex terminateDepth; shorter paths keep BPT's strategies, extra PT
+// training paths (trainFraction of the pixels) feed the cache.
+class NrcBidirectionalPathtracer : public NrcPathtracer {
+public:
+    explicit NrcBidirectionalPathtracer(RendererSystem& rendererSystem, const NrcSettings& settings = NrcSettings())
+        : NrcPathtracer(rendererSystem, settings, GPUGI_PASS_BPT) {}
+    std::string GetName() const override { return "NrcBidirectionalPathtracer"; }
 };
 
 // imageut: RGB PFM files; rows bottom-up as the backbuffer stores them.

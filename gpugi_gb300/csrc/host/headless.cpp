@@ -4,7 +4,8 @@
 // backbuffer as PFM (Application::SaveImage) and prints a JSON summary.
 //
 //   gpugi_headless --scene FILE [--renderer Pathtracer|LightPathtracer|
-//                  BidirectionalPathtracer|NrcPathtracer] [--size W H]
+//                  BidirectionalPathtracer|NrcPathtracer|
+//                  NrcBidirectionalPathtracer] [--size W H]
 //                  [--camera px py pz lx ly lz fovy] [--iterations N]
 //                  [--path-length L] [--rr-start D] [--sky r g b]
 //                  [--point-light px py pz ir ig ib] [--reference FILE.pfm]
@@ -88,6 +89,7 @@ int main(int argc, char** argv) {
         else if (a.renderer == "LightPathtracer") system.SetRenderer<LightPathtracer>();
         else if (a.renderer == "BidirectionalPathtracer") system.SetRenderer<BidirectionalPathtracer>();
         else if (a.renderer == "NrcPathtracer") system.SetRenderer<NrcPathtracer>();
+        else if (a.renderer == "NrcBidirectionalPathtracer") system.SetRenderer<NrcBidirectionalPathtracer>();
         else usage("unknown renderer");
 
         for (int i = 0; i < a.iterations; ++i) system.Draw();

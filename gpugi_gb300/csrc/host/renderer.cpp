@@ -296,8 +296,11 @@ BidirectionalPathtracer::BidirectionalPathtracer(RendererSystem& rendererSystem)
 void BidirectionalPathtracer::Draw() { draw_pass(m_rendererSystem, GPUGI_PASS_BPT); }
 
 NrcPathtracer::NrcPathtracer(RendererSystem& rendererSystem, const NrcSettings& settings)
-    : Renderer(rendererSystem), m_settings(settings) {
-    m_rendererSystem.SetNumInitialLightSamples(128);
+    : NrcPathtracer(rendererSystem, settings, GPUGI_PASS_PT) {}
+
+NrcPathtracer::NrcPathtracer(RendererSystem& rendererSystem, const NrcSettings& settings, gpugi_pass pass)
+    : Renderer(rendererSystem), m_settings(settings), m_pass(pass) {
+    m_rendererSystem.SetNumInitialLightSamples(128);  // pathtracer.cpp:28, bidirectionalpathtracer.cpp:25
 }
 
 NrcPathtracer::~NrcPathtracer() { gpugi_nrc_destroy(m_nrc); }
@@ -315,7 +318,7 @@ void NrcPathtracer::SetScene(std::shared_ptr<Scene> scene) {
 
 void NrcPathtracer::Draw() {
     if (!m_rendererSystem.GetScene() || !m_nrc) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "no scene set");
-    const gpugi_render_params p = m_rendererSystem.MakeRenderParams(GPUGI_PASS_PT);
+    const gpugi_render_params p = m_rendererSystem.MakeRenderParams(m_pass);
     gpugi_nrc_params q{};
     q.terminateDepth = m_settings.terminateDepth;
     q.trainFraction = m_settings.trainFraction;

@@ -42,7 +42,8 @@ constexpr int kMaxDepth = 64;
 struct PathSoA {
     float *ox, *oy, *oz, *dx, *dy, *dz, *tx, *ty, *tz, *lastP;
     uint32_t *seed, *pixel, *info;  // info: bit 0 = didNEE, bits 8..31 = sample (iteration) index
-    uint32_t* job;                  // batched render: index of the path's job
+    uint32_t* job;                  // batched render: index of the path's job; BPT with the radiance
+                                    // cache: float bits of the product of the path's MIS factors
 };
 struct HitSoA {
     int32_t* slot;
@@ -55,6 +56,7 @@ struct ShadowSoA {
     uint32_t* job;    // batched render: index of the ray's job
 };
 constexpr uint32_t kNoTrain = 0xFFFFFFFFu;
+constexpr uint32_t kNoPixel = 0xFFFFFFFFu;  // a path that only trains the radiance cache: no splat
 
 // Light-cache entry (bidirpathtracer/lightcache.glsl:1-16), 64 bytes.
 struct CacheEntry {
@@ -108,7 +110,7 @@ struct RenderConst {
 
 // ------------------------------------------------------------ accumulation
 GPUGI_D void splat(const RenderConst& rc, uint32_t pixel, float3 c, float w = 0.0f) {
-    if (!(c.x != 0.0f || c.y != 0.0f || c.z != 0.0f || w != 0.0f)) return;
+    if (!(c.x != 0.0f || c.y != 0.0f || c.z != 0.0f || w != 0.0f) || pixel == kNoPixel) return;
     atomicAdd(rc.image + pixel, make_float4(c.x, c.y, c.z, w));
     if (rc.image64) {
         atomicAdd(rc.image64 + 3 * (size_t)pixel, (double)c.x);
@@ -572,116 +574,143 @@ __global__ void k_show_light_samples(RenderConst rc) {
     }
 }
 
-// pathtracer_bidir.comp:54-245, one bounce of the eye pass.
+// pathtracer_bidir.comp:54-245, one bounce of one eye path: the per-lane
+// part of the BPT shade kernels. connectCap bounds the length of the paths
+// formed by light-cache connections (maxPathLength in the reference). With
+// the radiance cache (terminateDepth >= 0) the path stops at vertex
+// terminateDepth after its emission term and queries the cache there with
+// its throughput divided by the product of the MIS factors applied so far
+// (kept in the job column as float bits).
+struct BptLane {
+    bool survive = false, shadow = false, query = false;
+    float3 o, d, tp, sro, srd, contrib, qN, qAlbedo, qT;
+    float srl = 0.0f, lastP = 1.0f, misProd = 1.0f;
+    uint32_t seed = 0, pixel = 0, info = 0;
+};
+
+GPUGI_D void bpt_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
+                            int connectCap, int terminateDepth, BptLane& L) {
+    L.o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+    L.d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+    L.tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+    L.seed = A.seed[k];
+    L.pixel = A.pixel[k];
+    L.info = A.info[k];
+    L.lastP = A.lastP[k];
+    if (terminateDepth >= 0) L.misProd = __uint_as_float(A.job[k]);
+    float3& o = L.o;
+    float3& d = L.d;
+    float3& tp = L.tp;
+    uint32_t& seed = L.seed;
+    const float lastP = L.lastP;
+    Hit h = load_hit(rc, H, k, o, d);
+    if (!h.valid) {
+        splat(rc, L.pixel, tp * rc.sky);
+        return;
+    }
+    const uint32_t s = L.info >> 8;
+    o = h.pos;
+    const float rayHit = h.t;
+    const float incCos = saturate(-dot(h.N, d));
+    const float cLE = distance_mis(rayHit) * mis_heuristic(incCos / kPI);
+    float mis = depth == 0 ? 1.0f : lastP / fmaxf(lastP + cLE, kDIVISOR_EPSILON);
+    splat(rc, L.pixel, mis * tp * h.m.Emissivity);
+    if (depth == terminateDepth) {
+        L.query = true;
+        L.qN = h.N;
+        L.qAlbedo = h.m.Diffuse;
+        L.qT = L.misProd > 0.0f ? tp / L.misProd : f3(0.0f);
+        return;
+    }
+    const uint32_t actual = min(rc.cacheCount[s], rc.cacheCap);
+    if (actual > 0) {
+        const uint32_t li = random_uint(seed) % actual;
+        const CacheEntry* ep = rc.cache + (size_t)s * rc.cacheCap + li;
+        const float4 e0 = ep->fluxMat, e1 = ep->posN0, e2 = ep->tcN1Len, e3 = ep->incident;
+        const int pathLength = __float_as_int(e2.w) + depth + 1;
+        if (pathLength <= connectCap) {
+            float3 Ld = xyz(e1) - o;
+            const float lightDistSq = dot(Ld, Ld);
+            const float lightDist = sqrtf(lightDistSq);
+            Ld /= fmaxf(lightDist, kDIVISOR_EPSILON);
+            float3 lN = f3(0.0f, 1.0f, 0.0f);
+            float cosLight = 0.0f;
+            const float cosCamera = fabsf(dot(Ld, h.N));
+            const bool lambertian = e2.z < 1.5f;
+            if (lambertian) {
+                lN = unpack_normal_raw(e1.w, e2.z);
+                cosLight = fabsf(dot(Ld, lN));
+            }
+            float pdf;
+            const float3 bsdf = eval_bsdf(d, Ld, h.m, h.N, pdf, false);
+            float cEL = mis_heuristic(pdf);
+            if (depth > 0) {
+                cEL *= distance_mis(rayHit);
+                mis = lastP / fmaxf(lastP + cEL, kDIVISOR_EPSILON);
+                if (h.m.Reflectiveness.w >= 100.0f) mis = 1.0f;
+            } else {
+                mis = cEL / fmaxf(lastP + cEL, kDIVISOR_EPSILON);
+            }
+            const float3 flux = xyz(e0);
+            const int lmat = __float_as_int(e0.w);
+            float misLight = 1.0f;
+            float3 intensity;
+            if (lambertian) {
+                float cLtoE;
+                if (lmat != -1) {
+                    const MaterialData lm = load_material(rc.s, lmat);
+                    const float3 inc = unpack_normal(e3.x, e3.y);
+                    const float3 lb = adjoint_bsdf(Ld, -inc, lm, lN, pdf);
+                    intensity = flux * lb * cosLight;
+                    cLtoE = mis_heuristic(pdf) * distance_mis(lightDist);
+                } else {
+                    intensity = flux * (cosLight * kPI_2);
+                    cLtoE = mis_heuristic(cosLight / kPI) * distance_mis(lightDist);
+                }
+                misLight = cLtoE / fmaxf(cLtoE + cEL, kDIVISOR_EPSILON);
+            } else {
+                intensity = flux * kPI_2;
+            }
+            mis *= misLight;
+            const float3 irr = (mis * (float)actual * cosCamera / lightDistSq) * intensity;
+            L.contrib = irr * tp * bsdf;
+            L.shadow = L.contrib.x != 0.0f || L.contrib.y != 0.0f || L.contrib.z != 0.0f;
+            L.sro = kRAY_HIT_EPSILON * Ld + o;
+            L.srd = Ld;
+            L.srl = lightDist - kRAY_HIT_EPSILON * 2;
+        }
+    }
+    float3 thr = f3(1.0f);
+    float samplePDF;
+    d = sample_bsdf(d, h.m, seed, h.N, thr, false, samplePDF);
+    o = o + d * kRAY_HIT_EPSILON;
+    tp *= thr;
+    L.survive = roulette(rc, depth, thr, tp, seed) && depth + 1 < rc.maxPathLength;
+    float rcp = mis_heuristic(samplePDF);
+    if (depth == 0) {
+        mis = rcp / fmaxf(rcp + lastP, kDIVISOR_EPSILON);
+    } else {
+        const float dm = distance_mis(rayHit);
+        rcp *= dm;
+        mis = lastP / fmaxf(lastP + dm * rcp, kDIVISOR_EPSILON);
+        if (h.m.Reflectiveness.w >= 100.0f) mis = 1.0f;
+    }
+    tp *= mis;
+    L.misProd *= mis;
+    L.lastP = rcp;
+}
+
 __global__ void __launch_bounds__(128) k_bpt_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q,
                                                    int depth) {
     const uint32_t n = rc.cnt->path[depth];
     WARP_LOOP(n, k, valid) {
-        bool survive = false, shadow = false;
-        float3 o, d, tp, sro, srd, contrib;
-        float srl = 0.0f, lastP = 1.0f;
-        uint32_t seed = 0, pixel = 0, info = 0;
-        if (valid) {
-            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
-            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
-            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
-            pixel = A.pixel[k];
-            info = A.info[k];
-            lastP = A.lastP[k];
-            Hit h = load_hit(rc, H, k, o, d);
-            if (!h.valid) {
-                splat(rc, pixel, tp * rc.sky);
-            } else {
-                const uint32_t s = info >> 8;
-                o = h.pos;
-                const float rayHit = h.t;
-                const float incCos = saturate(-dot(h.N, d));
-                const float cLE = distance_mis(rayHit) * mis_heuristic(incCos / kPI);
-                float mis = depth == 0 ? 1.0f : lastP / fmaxf(lastP + cLE, kDIVISOR_EPSILON);
-                splat(rc, pixel, mis * tp * h.m.Emissivity);
-                const uint32_t actual = min(rc.cacheCount[s], rc.cacheCap);
-                if (actual > 0) {
-                    const uint32_t li = random_uint(seed) % actual;
-                    const CacheEntry* ep = rc.cache + (size_t)s * rc.cacheCap + li;
-                    const float4 e0 = ep->fluxMat, e1 = ep->posN0, e2 = ep->tcN1Len, e3 = ep->incident;
-                    const int pathLength = __float_as_int(e2.w) + depth + 1;
-                    if (pathLength <= rc.maxPathLength) {
-                        float3 L = xyz(e1) - o;
-                        const float lightDistSq = dot(L, L);
-                        const float lightDist = sqrtf(lightDistSq);
-                        L /= fmaxf(lightDist, kDIVISOR_EPSILON);
-                        float3 lN = f3(0.0f, 1.0f, 0.0f);
-                        float cosLight = 0.0f;
-                        const float cosCamera = fabsf(dot(L, h.N));
-                        const bool lambertian = e2.z < 1.5f;
-                        if (lambertian) {
-                            lN = unpack_normal_raw(e1.w, e2.z);
-                            cosLight = fabsf(dot(L, lN));
-                        }
-                        float pdf;
-                        const float3 bsdf = eval_bsdf(d, L, h.m, h.N, pdf, false);
-                        float cEL = mis_heuristic(pdf);
-                        if (depth > 0) {
-                            cEL *= distance_mis(rayHit);
-                            mis = lastP / fmaxf(lastP + cEL, kDIVISOR_EPSILON);
-                            if (h.m.Reflectiveness.w >= 100.0f) mis = 1.0f;
-                        } else {
-                            mis = cEL / fmaxf(lastP + cEL, kDIVISOR_EPSILON);
-                        }
-                        const float3 flux = xyz(e0);
-                        const int lmat = __float_as_int(e0.w);
-                        float misLight = 1.0f;
-                        float3 intensity;
-                        if (lambertian) {
-                            float cLtoE;
-                            if (lmat != -1) {
-                                const MaterialData lm = load_material(rc.s, lmat);
-                                const float3 inc = unpack_normal(e3.x, e3.y);
-                                const float3 lb = adjoint_bsdf(L, -inc, lm, lN, pdf);
-                                intensity = flux * lb * cosLight;
-                                cLtoE = mis_heuristic(pdf) * distance_mis(lightDist);
-                            } else {
-                                intensity = flux * (cosLight * kPI_2);
-                                cLtoE = mis_heuristic(cosLight / kPI) * distance_mis(lightDist);
-                            }
-                            misLight = cLtoE / fmaxf(cLtoE + cEL, kDIVISOR_EPSILON);
-                        } else {
-                            intensity = flux * kPI_2;
-                        }
-                        mis *= misLight;
-                        const float3 irr = (mis * (float)actual * cosCamera / lightDistSq) * intensity;
-                        contrib = irr * tp * bsdf;
-                        shadow = contrib.x != 0.0f || contrib.y != 0.0f || contrib.z != 0.0f;
-                        sro = kRAY_HIT_EPSILON * L + o;
-                        srd = L;
-                        srl = lightDist - kRAY_HIT_EPSILON * 2;
-                    }
-                }
-                float3 thr = f3(1.0f);
-                float samplePDF;
-                d = sample_bsdf(d, h.m, seed, h.N, thr, false, samplePDF);
-                o = o + d * kRAY_HIT_EPSILON;
-                tp *= thr;
-                survive = roulette(rc, depth, thr, tp, seed) && depth + 1 < rc.maxPathLength;
-                float rcp = mis_heuristic(samplePDF);
-                if (depth == 0) {
-                    mis = rcp / fmaxf(rcp + lastP, kDIVISOR_EPSILON);
-                } else {
-                    const float dm = distance_mis(rayHit);
-                    rcp *= dm;
-                    mis = lastP / fmaxf(lastP + dm * rcp, kDIVISOR_EPSILON);
-                    if (h.m.Reflectiveness.w >= 100.0f) mis = 1.0f;
-                }
-                tp *= mis;
-                lastP = rcp;
-            }
-        }
+        BptLane L;
+        if (valid) bpt_shade_lane(rc, A, H, k, depth, rc.maxPathLength, -1, L);
         uint32_t qs, qb;
-        warp_append(&rc.cnt->shadow[depth], shadow, qs);
-        if (shadow) store_shadow(Q, qs, sro, srd, srl, contrib, pixel);
-        warp_append(&rc.cnt->path[depth + 1], survive, qb);
-        if (survive) store_path(B, qb, o, d, tp, seed, pixel, info, lastP);
+        warp_append(&rc.cnt->shadow[depth], L.shadow, qs);
+        if (L.shadow) store_shadow(Q, qs, L.sro, L.srd, L.srl, L.contrib, L.pixel);
+        warp_append(&rc.cnt->path[depth + 1], L.survive, qb);
+        if (L.survive) store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, L.lastP);
     }
 }
 
@@ -718,97 +747,189 @@ GPUGI_D void add3(float* p, float3 c) {
     atomicAdd(p + 2, c.z);
 }
 
-// One bounce of the path tracer with a radiance cache. Render paths stop at
-// vertex nrcTerminateDepth and query the cache for the radiance reflected
-// there towards the previous vertex; training paths continue as plain path
-// tracing and record every vertex {position, outgoing direction, normal,
-// albedo, throughput}; the radiance that later reaches each vertex (NEE via
-// the shadow queue, emission and sky found by the next segment) is
-// accumulated into the vertex's tvC entry.
+// One bounce of the path tracer with a radiance cache, per lane. Render
+// paths stop at vertex nrcTerminateDepth and query the cache for the
+// radiance reflected there towards the previous vertex; training paths
+// continue as plain path tracing and record every vertex {position,
+// outgoing direction, normal, albedo, throughput}; the radiance that later
+// reaches each vertex (NEE via the shadow queue, emission and sky found by
+// the next segment) is accumulated into the vertex's tvC entry. A training
+// path with pixel kNoPixel (BPT with the cache) only trains.
+struct NrcLane {
+    bool survive = false, shadow = false, query = false;
+    float3 o, d, tp, sro, srd, contrib, qN, qAlbedo, qT;
+    float srl = 0.0f, lastP = 0.0f;
+    uint32_t seed = 0, pixel = 0, info = 0, train = kNoTrain;
+};
+
+GPUGI_D void nrc_pt_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
+                         NrcLane& L) {
+    const float lightSampleWeight = (float)rc.numLightSamples;
+    const uint32_t stride = (uint32_t)rc.maxPathLength;
+    float3& o = L.o;
+    float3& d = L.d;
+    float3& tp = L.tp;
+    o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+    d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+    tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+    L.seed = A.seed[k];
+    L.pixel = A.pixel[k];
+    L.info = A.info[k];
+    L.lastP = A.lastP[k];
+    const bool training = (L.info & 2u) != 0;
+    const uint32_t tslot = __float_as_uint(L.lastP);
+    const uint32_t prevVertex = (training && depth > 0) ? tslot * stride + depth - 1 : kNoTrain;
+    Hit h = load_hit(rc, H, k, o, d);
+    if (!h.valid) {
+        const float3 c = tp * rc.sky;
+        splat(rc, L.pixel, c);
+        if (prevVertex != kNoTrain) add3(rc.tvC + 3 * (size_t)prevVertex, c);
+        return;
+    }
+    o = h.pos;
+    if (!(L.info & 1u)) {
+        const float3 e = tp * h.m.Emissivity;
+        splat(rc, L.pixel, e);
+        if (prevVertex != kNoTrain) add3(rc.tvC + 3 * (size_t)prevVertex, e);
+    }
+    if (!training && depth == rc.nrcTerminateDepth) {
+        L.query = true;
+        L.qN = h.N;
+        L.qAlbedo = h.m.Diffuse;
+        L.qT = tp;
+        return;
+    }
+    const bool didNEE = h.m.Reflectiveness.w < 500.0f;
+    L.info = (L.info & ~1u) | (didNEE ? 1u : 0u);
+    if (training) {
+        const uint32_t v = tslot * stride + (uint32_t)depth;
+        float* r = rc.tvRec + 16 * (size_t)v;
+        r[0] = o.x; r[1] = o.y; r[2] = o.z;
+        r[3] = -d.x; r[4] = -d.y; r[5] = -d.z;
+        r[6] = h.N.x; r[7] = h.N.y; r[8] = h.N.z;
+        r[9] = h.m.Diffuse.x; r[10] = h.m.Diffuse.y; r[11] = h.m.Diffuse.z;
+        r[12] = tp.x; r[13] = tp.y; r[14] = tp.z;
+        rc.tvC[3 * (size_t)v] = rc.tvC[3 * (size_t)v + 1] = rc.tvC[3 * (size_t)v + 2] = 0.0f;
+        rc.tvCount[tslot] = (uint32_t)depth + 1;
+        L.train = v;
+    }
+    const uint32_t li = random_uint(L.seed) % rc.numLightSamples;
+    float3 rad;
+    if (direct_light(rc, L.info >> 8, o, h.N, li, d, h.m, didNEE, rad, L.sro, L.srd, L.srl)) {
+        L.contrib = rad * tp * lightSampleWeight;
+        L.shadow = L.contrib.x != 0.0f || L.contrib.y != 0.0f || L.contrib.z != 0.0f;
+    }
+    float3 thr = f3(1.0f);
+    float pdf;
+    d = sample_bsdf(d, h.m, L.seed, h.N, thr, false, pdf);
+    o = o + d * kRAY_HIT_EPSILON;
+    tp *= thr;
+    L.survive = roulette(rc, depth, thr, tp, L.seed) && depth + 1 < rc.maxPathLength;
+}
+
+// Cache query record: 12 floats {position, direction towards the previous
+// vertex, normal, albedo}, the throughput it is weighted with and its pixel.
+GPUGI_D void store_query(const RenderConst& rc, uint32_t q, float3 o, float3 d, float3 n, float3 albedo, float3 t,
+                         uint32_t pixel) {
+    float* r = rc.queries + 12 * (size_t)q;
+    r[0] = o.x; r[1] = o.y; r[2] = o.z;
+    r[3] = -d.x; r[4] = -d.y; r[5] = -d.z;
+    r[6] = n.x; r[7] = n.y; r[8] = n.z;
+    r[9] = albedo.x; r[10] = albedo.y; r[11] = albedo.z;
+    rc.qT[3 * (size_t)q] = t.x;
+    rc.qT[3 * (size_t)q + 1] = t.y;
+    rc.qT[3 * (size_t)q + 2] = t.z;
+    rc.qPixel[q] = pixel;
+}
+
 __global__ void __launch_bounds__(128) k_nrc_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q,
                                                    int depth) {
     const uint32_t n = rc.cnt->path[depth];
-    const float lightSampleWeight = (float)rc.numLightSamples;
-    const uint32_t stride = (uint32_t)rc.maxPathLength;
+    WARP_LOOP(n, k, valid) {
+        NrcLane L;
+        if (valid) nrc_pt_lane(rc, A, H, k, depth, L);
+        uint32_t qs, qb, qq;
+        warp_append(&rc.cnt->shadow[depth], L.shadow, qs);
+        if (L.shadow) store_shadow(Q, qs, L.sro, L.srd, L.srl, L.contrib, L.pixel, L.train);
+        warp_append(rc.queryCount, L.query, qq);
+        if (L.query && qq < rc.queryCap) store_query(rc, qq, L.o, L.d, L.qN, L.qAlbedo, L.qT, L.pixel);
+        warp_append(&rc.cnt->path[depth + 1], L.survive, qb);
+        if (L.survive) store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, L.lastP);
+    }
+}
+
+// Eye paths of BPT with a radiance cache: one render path per pixel and
+// sample as k_camera_generate(bidir), followed by nTrain training paths at
+// hashed pixels. Training paths trace plain PT paths that only feed the
+// cache (pixel kNoPixel: no splat), so every pixel keeps the BPT estimator.
+__global__ void k_nrc_bpt_generate(RenderConst rc, PathSoA A, uint32_t nTrain) {
+    const uint32_t render = rc.samples * (uint32_t)rc.numPixels, total = render + nTrain;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        rc.cnt->path[0] = total;
+        *rc.trainPaths = nTrain;
+    }
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+        if (p < render) {
+            const uint32_t s = p / (uint32_t)rc.numPixels, pix = p % (uint32_t)rc.numPixels;
+            const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
+            uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + pix);
+            const float3 d = primary_direction(rc, seed, x, y);
+            store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, s << 8, 1.0f);
+            A.job[p] = __float_as_uint(1.0f);
+            splat(rc, pix, f3(0.0f), 1.0f);
+        } else {
+            const uint32_t slot = p - render, s = slot % rc.samples;
+            const uint32_t frame = rc.iteration + rc.sampleBase + s;
+            const uint32_t pix = wanghash(slot ^ wanghash(frame + 0x9E3779B9u)) % (uint32_t)rc.numPixels;
+            const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
+            uint32_t seed = wanghash(wanghash(frame ^ 0x5bd1e995u) + slot);
+            const float3 d = primary_direction(rc, seed, x, y);
+            rc.tvCount[slot] = 0;
+            store_path(A, p, rc.camPos, d, f3(1.0f), seed, kNoPixel, (s << 8) | 2u, __uint_as_float(slot));
+            A.job[p] = __float_as_uint(1.0f);
+        }
+    }
+}
+
+// One bounce of BPT with a radiance cache: render paths run the BPT eye
+// bounce and stop at vertex nrcTerminateDepth (light-cache connections
+// limited to paths of that length; longer paths come from the cache query);
+// training paths run the PT training bounce.
+__global__ void __launch_bounds__(128) k_nrc_bpt_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H,
+                                                       ShadowSoA Q, int depth) {
+    const uint32_t n = rc.cnt->path[depth];
+    const int cap = min(rc.maxPathLength, rc.nrcTerminateDepth);
     WARP_LOOP(n, k, valid) {
         bool survive = false, shadow = false, query = false;
-        float3 o, d, tp, sro, srd, contrib, qN, qAlbedo;
-        float srl = 0.0f, lastP = 0.0f;
+        float3 o, d, tp, sro, srd, contrib, qN, qA, qT;
+        float srl = 0.0f, lastP = 0.0f, misProd = 1.0f;
         uint32_t seed = 0, pixel = 0, info = 0, train = kNoTrain;
         if (valid) {
-            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
-            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
-            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
-            pixel = A.pixel[k];
-            info = A.info[k];
-            lastP = A.lastP[k];
-            const bool training = (info & 2u) != 0;
-            const uint32_t tslot = __float_as_uint(lastP);
-            const uint32_t prevVertex = (training && depth > 0) ? tslot * stride + depth - 1 : kNoTrain;
-            Hit h = load_hit(rc, H, k, o, d);
-            if (!h.valid) {
-                const float3 c = tp * rc.sky;
-                splat(rc, pixel, c);
-                if (prevVertex != kNoTrain) add3(rc.tvC + 3 * (size_t)prevVertex, c);
+            if (A.info[k] & 2u) {
+                NrcLane L;
+                nrc_pt_lane(rc, A, H, k, depth, L);
+                survive = L.survive; shadow = L.shadow;
+                o = L.o; d = L.d; tp = L.tp; sro = L.sro; srd = L.srd; contrib = L.contrib; srl = L.srl;
+                lastP = L.lastP; seed = L.seed; pixel = L.pixel; info = L.info; train = L.train;
             } else {
-                o = h.pos;
-                if (!(info & 1u)) {
-                    const float3 e = tp * h.m.Emissivity;
-                    splat(rc, pixel, e);
-                    if (prevVertex != kNoTrain) add3(rc.tvC + 3 * (size_t)prevVertex, e);
-                }
-                if (!training && depth == rc.nrcTerminateDepth) {
-                    query = true;
-                    qN = h.N;
-                    qAlbedo = h.m.Diffuse;
-                } else {
-                    const bool didNEE = h.m.Reflectiveness.w < 500.0f;
-                    info = (info & ~1u) | (didNEE ? 1u : 0u);
-                    if (training) {
-                        const uint32_t v = tslot * stride + (uint32_t)depth;
-                        float* r = rc.tvRec + 16 * (size_t)v;
-                        r[0] = o.x; r[1] = o.y; r[2] = o.z;
-                        r[3] = -d.x; r[4] = -d.y; r[5] = -d.z;
-                        r[6] = h.N.x; r[7] = h.N.y; r[8] = h.N.z;
-                        r[9] = h.m.Diffuse.x; r[10] = h.m.Diffuse.y; r[11] = h.m.Diffuse.z;
-                        r[12] = tp.x; r[13] = tp.y; r[14] = tp.z;
-                        rc.tvC[3 * (size_t)v] = rc.tvC[3 * (size_t)v + 1] = rc.tvC[3 * (size_t)v + 2] = 0.0f;
-                        rc.tvCount[tslot] = (uint32_t)depth + 1;
-                        train = v;
-                    }
-                    const uint32_t li = random_uint(seed) % rc.numLightSamples;
-                    float3 rad;
-                    if (direct_light(rc, info >> 8, o, h.N, li, d, h.m, didNEE, rad, sro, srd, srl)) {
-                        contrib = rad * tp * lightSampleWeight;
-                        shadow = contrib.x != 0.0f || contrib.y != 0.0f || contrib.z != 0.0f;
-                    }
-                    float3 thr = f3(1.0f);
-                    float pdf;
-                    d = sample_bsdf(d, h.m, seed, h.N, thr, false, pdf);
-                    o = o + d * kRAY_HIT_EPSILON;
-                    tp *= thr;
-                    survive = roulette(rc, depth, thr, tp, seed) && depth + 1 < rc.maxPathLength;
-                }
+                BptLane L;
+                bpt_shade_lane(rc, A, H, k, depth, cap, rc.nrcTerminateDepth, L);
+                survive = L.survive; shadow = L.shadow; query = L.query;
+                o = L.o; d = L.d; tp = L.tp; sro = L.sro; srd = L.srd; contrib = L.contrib; srl = L.srl;
+                qN = L.qN; qA = L.qAlbedo; qT = L.qT;
+                lastP = L.lastP; misProd = L.misProd; seed = L.seed; pixel = L.pixel; info = L.info;
             }
         }
         uint32_t qs, qb, qq;
         warp_append(&rc.cnt->shadow[depth], shadow, qs);
         if (shadow) store_shadow(Q, qs, sro, srd, srl, contrib, pixel, train);
         warp_append(rc.queryCount, query, qq);
-        if (query && qq < rc.queryCap) {
-            float* r = rc.queries + 12 * (size_t)qq;
-            r[0] = o.x; r[1] = o.y; r[2] = o.z;
-            r[3] = -d.x; r[4] = -d.y; r[5] = -d.z;
-            r[6] = qN.x; r[7] = qN.y; r[8] = qN.z;
-            r[9] = qAlbedo.x; r[10] = qAlbedo.y; r[11] = qAlbedo.z;
-            rc.qT[3 * (size_t)qq] = tp.x;
-            rc.qT[3 * (size_t)qq + 1] = tp.y;
-            rc.qT[3 * (size_t)qq + 2] = tp.z;
-            rc.qPixel[qq] = pixel;
-        }
+        if (query && qq < rc.queryCap) store_query(rc, qq, o, d, qN, qA, qT, pixel);
         warp_append(&rc.cnt->path[depth + 1], survive, qb);
-        if (survive) store_path(B, qb, o, d, tp, seed, pixel, info, lastP);
+        if (survive) {
+            store_path(B, qb, o, d, tp, seed, pixel, info, lastP);
+            B.job[qb] = __float_as_uint(misProd);
+        }
     }
 }
 
@@ -1465,7 +1586,9 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
                               gpugi_nrc* nn, const gpugi_nrc_params* np, gpugi_image* im) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!sc || !cam || !p || !im || !nn || !np) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass != GPUGI_PASS_PT) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "the radiance cache serves the PT pass");
+    if (p->pass != GPUGI_PASS_PT && p->pass != GPUGI_PASS_BPT)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "the radiance cache serves the PT and BPT passes");
+    const bool bpt = p->pass == GPUGI_PASS_BPT;
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth || p->numLightSamples == 0 ||
@@ -1489,11 +1612,26 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
                                                       std::max<size_t>(1, (64u << 20) / (setBytes * spf)));
     const uint32_t blockSamples = blockFrames * spf;
     const size_t lightBytes = (size_t)blockSamples * setBytes;
-    gpugi_status st = ensure_buffers(ctx, framePaths, 0, lightBytes, spf);
+    // BPT: light particles per sample as LightPathtracer::SetScreenSize
+    // (gpugi/renderer/lightpathtracer.cpp:34); the light pass only needs
+    // min(maxPathLength, terminateDepth) bounces, since longer paths are the
+    // cache's; training paths come on top of the render paths.
+    uint32_t lightThreads = 0, raysPerLight = 0, lightDepth = 0, nTrain = 0;
+    uint64_t cachePerSample = 0;
+    size_t paths = framePaths;
+    if (bpt) {
+        raysPerLight = std::max<uint32_t>(64u, (numPixels / p->numLightSamples / 64u) * 64u);
+        lightThreads = raysPerLight * p->numLightSamples;
+        lightDepth = std::min(p->maxPathLength, np->terminateDepth);
+        cachePerSample = (uint64_t)lightThreads * (lightDepth + 1);
+        nTrain = np->train ? (uint32_t)(np->trainFraction * (double)framePaths) : 0u;
+        paths = std::max<size_t>((size_t)framePaths + nTrain, (size_t)spf * lightThreads);
+    }
+    gpugi_status st = ensure_buffers(ctx, paths, (size_t)spf * cachePerSample * 64, lightBytes, spf);
     if (st) return st;
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
     if ((st = ensure_host_lights(ctx, rb, lightBytes))) return st;
-    const size_t trainCap = (size_t)(np->trainFraction * framePaths * 1.25) + 64;
+    const size_t trainCap = bpt ? (size_t)nTrain + 64 : (size_t)(np->trainFraction * framePaths * 1.25) + 64;
     const size_t sampleCap = np->maxTrainSamples ? np->maxTrainSamples : 65536;
     if ((st = ensure_nrc_buffers(ctx, rb, framePaths, trainCap, p->maxPathLength, sampleCap))) return st;
 
@@ -1510,10 +1648,14 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     rc.qPixel = rb->qPixel;
     rc.queryCount = rb->nrcCounters;
     rc.queryCap = framePaths;
+    rc.numRaysPerLightSample = (int)raysPerLight;
+    rc.lightThreads = lightThreads;
+    rc.cacheCap = (uint32_t)cachePerSample;
     Walkers W;
     if ((st = walkers_config(ctx, sc, W))) return st;
     int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, (const void*)k_nrc_shade, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, bpt ? (const void*)k_nrc_bpt_shade : (const void*)k_nrc_shade,
+                                                  128, 0);
     const int gridShade = ctx->numSMs * std::max(perSM, 1);
     const int genBlocks = ctx->numSMs * 8;
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
@@ -1530,10 +1672,29 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), ctx->stream));
         GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->nrcCounters, 0, 64, ctx->stream));
         PathSoA A = rb->A, B = rb->B;
-        k_nrc_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
+        if (bpt) {
+            // light pass with the light cache (lighttracer.comp with
+            // SAVE_LIGHT_CACHE), bounded to lightDepth bounces
+            RenderConst rl = rc;
+            rl.maxPathLength = (int)lightDepth;
+            k_light_generate<<<genBlocks, 256, 0, ctx->stream>>>(rl, A, true);
+            for (int depth = 0; depth < rl.maxPathLength; ++depth) {
+                launch_extend(ctx, W, rl, A, rb->H, depth);
+                k_light_shade<<<gridShade, 128, 0, ctx->stream>>>(rl, A, B, rb->H, rb->Q, depth, true);
+                launch_shadow(ctx, W, rl, rb->Q, depth);
+                std::swap(A, B);
+            }
+            GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), ctx->stream));
+            A = rb->A;
+            B = rb->B;
+            k_nrc_bpt_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A, nTrain);
+        } else {
+            k_nrc_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
+        }
         for (int depth = 0; depth < rc.maxPathLength; ++depth) {
             launch_extend(ctx, W, rc, A, rb->H, depth);
-            k_nrc_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
+            if (bpt) k_nrc_bpt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
+            else k_nrc_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
             launch_shadow(ctx, W, rc, rb->Q, depth);
             std::swap(A, B);
         }

@@ -33,6 +33,11 @@ __global__ void k_prepare_triangles(const int4* __restrict__ slots, uint32_t num
     tris[3 * (size_t)i + 2] = c;
 }
 
+void prepare_triangles(cudaStream_t stream, const int4* slots, uint32_t numSlots, const float* positions,
+                       float4* tris) {
+    if (numSlots) k_prepare_triangles<<<(numSlots + 255) / 256, 256, 0, stream>>>(slots, numSlots, positions, tris);
+}
+
 static uint32_t bits_of(float f) {
     uint32_t u;
     std::memcpy(&u, &f, 4);

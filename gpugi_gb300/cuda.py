@@ -51,6 +51,8 @@ def _declare(L):
     L.gpugi_scene_upload.argtypes = [P, P, U32, U32, P, U32, U32, P, P, U32, P, U32, C.POINTER(P)]
     L.gpugi_scene_destroy.argtypes = [P]
     L.gpugi_scene_destroy.restype = None
+    L.gpugi_scene_build.argtypes = [P, P, U32, P, U32, P, P, U32, U32, C.POINTER(P)]
+    L.gpugi_scene_export.argtypes = [P, P, C.POINTER(U32), C.POINTER(U32), P, P]
     for name in ("gpugi_trace_closest", "gpugi_trace_closest_device"):
         getattr(L, name).argtypes = [P, P] + [P] * 7 + [U64] + [P] * 4
     for name in ("gpugi_trace_any", "gpugi_trace_any_device"):
@@ -169,11 +171,29 @@ class Context:
     def upload_scene(self, bvh, positions, vertex_info=None, materials=None) -> "DeviceScene":
         return DeviceScene(self, bvh, positions, vertex_info, materials)
 
+    def build_scene(self, positions, triangles, vertex_info=None, materials=None, leaf_size: int = 8) -> "DeviceScene":
+        """Scene whose hierarchy is built on the GPU (gpugi_scene_build)."""
+        return DeviceScene(self, None, positions, vertex_info, materials, triangles=triangles, leaf_size=leaf_size)
+
 
 class DeviceScene:
-    def __init__(self, ctx: Context, bvh, positions, vertex_info=None, materials=None):
+    def __init__(self, ctx: Context, bvh, positions, vertex_info=None, materials=None, triangles=None,
+                 leaf_size: int = 8):
         self.ctx = ctx
         self._h = C.c_void_p()
+        if bvh is None:
+            tris = np.ascontiguousarray(triangles, dtype=np.uint32)
+            pos = np.ascontiguousarray(positions, dtype=np.float32)
+            vi = None if vertex_info is None else np.ascontiguousarray(vertex_info, dtype=np.float32)
+            mats = None if materials is None else np.ascontiguousarray(materials, dtype=np.float32).reshape(-1, 24)
+            nm = 0 if mats is None else mats.shape[0]
+            ctx.check(lib().gpugi_scene_build(ctx.handle, _ptr(pos), pos.shape[0], _ptr(tris), tris.shape[0],
+                                              _ptr(vi), _ptr(mats), nm, leaf_size, C.byref(self._h)))
+            _register(self, 2)
+            nn, ns = C.c_uint32(), C.c_uint32()
+            ctx.check(lib().gpugi_scene_export(ctx.handle, self._h, C.byref(nn), C.byref(ns), None, None))
+            self.num_nodes, self.num_slots, self.leaf_size = nn.value, ns.value, leaf_size
+            return
         hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
         slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
         pos = np.ascontiguousarray(positions, dtype=np.float32)
@@ -187,6 +207,25 @@ class DeviceScene:
         _register(self, 2)
         self.num_nodes = hier.shape[0]
         self.num_slots = slots.shape[0]
+        self.leaf_size = bvh.leaf_size
+
+    def export(self):
+        """The scene's hierarchy and leaf slots as a bvh.BVH (device node order)."""
+        from . import bvh as B
+        nn, ns = C.c_uint32(), C.c_uint32()
+        self.ctx.check(lib().gpugi_scene_export(self.ctx.handle, self._h, C.byref(nn), C.byref(ns), None, None))
+        hier = np.zeros((nn.value, 8), np.float32)
+        slots = np.zeros((ns.value, 4), np.int32)
+        self.ctx.check(lib().gpugi_scene_export(self.ctx.handle, self._h, C.byref(nn), C.byref(ns), _ptr(hier),
+                                                _ptr(slots)))
+        child = hier[:, 3].view(np.uint32)
+        parents = np.zeros(nn.value, np.uint32)
+        inner = np.nonzero((child & 0x80000000) == 0)[0]
+        left = child[inner]
+        parents[left] = inner
+        parents[hier[left, 7].view(np.uint32)] = inner
+        return B.BVH(hierarchy=hier, slots=slots, parents=parents, leaf_size=self.leaf_size, bounds_kind=0,
+                     max_depth=0)
 
     @property
     def handle(self):

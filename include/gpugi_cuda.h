@@ -102,6 +102,26 @@ gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarchy, uint32_t
                                 uint32_t numMaterials, gpugi_scene** out);
 void gpugi_scene_destroy(gpugi_scene* scene);
 
+/* Build the hierarchy on the GPU and create the scene. Replaces a host
+ * build with bvhmake (BVHBuilder::BuildBVH + FitBox + ExportBVH/
+ * ExportTriangles, bvhmake/bvhbuilder.cpp:526-612,710-722) followed by
+ * gpugi_scene_upload: same node and leaf-block layout (preorder escape tree,
+ * root at 0, AABB nodes, leaves of at most leafSize triangles padded with
+ * {0,0,0,0}), but a linear BVH: triangles sorted by the 63-bit Morton code
+ * of their box centre, split where the codes' common prefix ends.
+ *   triangles   4 uint32 per triangle {v0, v1, v2, material}; v0 != v1
+ * Other arguments as gpugi_scene_upload. Synchronous. */
+gpugi_status gpugi_scene_build(gpugi_ctx* ctx, const float* positions, uint32_t numVertices,
+                               const uint32_t* triangles, uint32_t numTriangles, const float* vertexInfo,
+                               const gpugi_material* materials, uint32_t numMaterials, uint32_t leafSize,
+                               gpugi_scene** out);
+
+/* The scene's hierarchy (8 floats per node, leaf words {0x80000000 | block})
+ * in device node order and its leaf slots (4 int32 each). Call with
+ * hierarchy and slots NULL for the sizes. */
+gpugi_status gpugi_scene_export(gpugi_ctx* ctx, const gpugi_scene* scene, uint32_t* numNodes, uint32_t* numSlots,
+                                float* hierarchy, int32_t* slots);
+
 /* Closest hit for n rays in SoA layout. tmax is the initial rayLength
  * (gpugi uses RAY_MAX = 3.402823466e38, stdheader.glsl:6). Outputs per ray:
  * slot = leaf slot index of the hit triangle or -1, t = final rayLength,
@@ -295,17 +315,27 @@ gpugi_status gpugi_nrc_gradient_device(gpugi_ctx* ctx, gpugi_nrc* nrc, const flo
 gpugi_status gpugi_nrc_encode_device(gpugi_ctx* ctx, const gpugi_nrc* nrc, const float* queries, uint64_t n,
                                      void* encodedHalf);
 
-/* Path tracing with the radiance cache (params->pass must be PT).
- * params->samples iterations run as frames of samplesPerFrame iterations
- * (one wavefront each). Camera paths stop at vertex terminateDepth and add
- * throughput x cache(vertex), except a trainFraction of the paths (chosen by
- * a hash of pixel and iteration) that trace full PT paths whose vertices
- * become training samples {query, radiance reflected towards the previous
- * vertex}; after the frame's lookups, trainSteps Adam steps run on those
+/* Path tracing (params->pass PT) or bidirectional path tracing (BPT) with
+ * the radiance cache. params->samples iterations run as frames of
+ * samplesPerFrame iterations (one wavefront each).
+ * PT: camera paths stop at vertex terminateDepth and add throughput x
+ * cache(vertex), except a trainFraction of the paths (chosen by a hash of
+ * pixel and iteration) that trace full PT paths whose vertices become
+ * training samples {query, radiance reflected towards the previous vertex}.
+ * Both kinds of path splat into image.
+ * BPT: the light pass (light cache and camera splats) runs
+ * min(maxPathLength, terminateDepth) bounces; eye paths run
+ * pathtracer_bidir.comp's bounce with light-cache connections limited to
+ * paths of terminateDepth bounces and stop at vertex terminateDepth, adding
+ * (eye throughput without its MIS factors) x cache(vertex): paths of at
+ * most terminateDepth bounces keep BPT's estimator, longer ones come from
+ * the cache. trainFraction x pixels x samplesPerFrame extra PT training
+ * paths per frame only feed the cache (train != 0).
+ * After the frame's lookups, trainSteps Adam steps run on the training
  * samples (at most maxTrainSamples, drawn in a shuffled path order) when
- * train != 0. Both kinds of path splat into image. Asynchronous: element
- * counts stay in device memory; the call returns once every frame is queued
- * (it waits only when the light-sample staging buffer is reused). */
+ * train != 0. Asynchronous: element counts stay in device memory; the call
+ * returns once every frame is queued (it waits only when the light-sample
+ * staging buffer is reused). */
 typedef struct gpugi_nrc_params {
     uint32_t terminateDepth;  /* vertex index (0 = first hit) where render paths query the cache */
     float trainFraction;      /* share of pixels tracing training paths, in [0, 1] */

@@ -95,11 +95,12 @@ def test_headless_texture_mse_and_nrc(cuda_ctx, room_file, tmp_path):
     # a shorter run is noisier
     info4 = _run(common + ["--iterations", 2, "--reference", ref])
     assert info4["mse"] > 1e-6
-    nrc = tmp_path / "nrc.pfm"
-    info_nrc = _run(common + ["--renderer", "NrcPathtracer", "--iterations", 8, "--out", nrc])
-    assert info_nrc["renderer"] == "NrcPathtracer"
-    img = _read_pfm(nrc)
-    assert np.isfinite(img).all() and img.mean() > 0
+    for renderer in ("NrcPathtracer", "NrcBidirectionalPathtracer"):
+        nrc = tmp_path / f"{renderer}.pfm"
+        info_nrc = _run(common + ["--renderer", renderer, "--iterations", 8, "--out", nrc])
+        assert info_nrc["renderer"] == renderer
+        img = _read_pfm(nrc)
+        assert np.isfinite(img).all() and img.mean() > 0
 
 
 @pytest.mark.gpu
