@@ -219,10 +219,24 @@ __global__ void __launch_bounds__(256) k_trace_root_filter4(
         const unsigned up = __shfl_up_sync(0xffffffffu, incl, off);
         if (lane >= (unsigned)off) incl += up;
     }
-    unsigned long long base = 0;
-    if (lane == 31 && incl) base = atomicAdd(counters + 1, (unsigned long long)incl);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    uint64_t at = base + (incl - cnt);
+    // one queue reservation per block: warp totals, their exclusive prefix
+    // sum, one atomic (instead of one per warp on the same counter)
+    __shared__ unsigned s_warp[32];
+    __shared__ unsigned long long s_base;
+    const unsigned warp = threadIdx.x >> 5;
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned total = 0;
+        for (unsigned w = 0; w < (blockDim.x + 31u) >> 5; ++w) {
+            const unsigned c = s_warp[w];
+            s_warp[w] = total;
+            total += c;
+        }
+        s_base = total ? atomicAdd(counters + 1, (unsigned long long)total) : 0ull;
+    }
+    __syncthreads();
+    uint64_t at = s_base + s_warp[warp] + (incl - cnt);
 #pragma unroll
     for (int k = 0; k < 4; ++k)
         if (pass & (1u << k)) queue[at++] = (uint32_t)(4 * i + k);

@@ -290,9 +290,7 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
         bool ok = false;
         if (k < g.end) ok = intersect_triangle(g.o, g.d, s.tris + 3 * (size_t)k, h, by, bz) && h < g.len;
         if (ANY_HIT) {
-            uint32_t key = ok ? k : kGroupDone;
-#pragma unroll
-            for (int off = G / 2; off > 0; off >>= 1) key = min(key, __shfl_xor_sync(gmask, key, off));
+            const uint32_t key = __reduce_min_sync(gmask, ok ? k : kGroupDone);
             if (key != kGroupDone) {
                 g.slot = (int32_t)key;
                 return true;
@@ -300,9 +298,7 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
         } else {
             // minimum hit distance (positive floats order like their bits),
             // then the lowest slot reaching it
-            uint32_t hb = ok ? __float_as_uint(h) : kGroupDone;
-#pragma unroll
-            for (int off = G / 2; off > 0; off >>= 1) hb = min(hb, __shfl_xor_sync(gmask, hb, off));
+            const uint32_t hb = __reduce_min_sync(gmask, ok ? __float_as_uint(h) : kGroupDone);
             const unsigned tie = __ballot_sync(gmask, ok && __float_as_uint(h) == hb);
             const unsigned src = tie ? (unsigned)(__ffs(tie) - 1) : gbase;
             const float wu = __shfl_sync(gmask, by, src), wv = __shfl_sync(gmask, bz, src);
@@ -361,29 +357,29 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
     return false;
 }
 
-// Persistent loop of group walks over n work items: a group takes the next
-// item with one atomic when its walk ends. load(i, o, d, tmax) fills the
-// ray of item i; finish(i, walk) runs in the group's first lane. With MULTI
-// the rays belong to different scenes: load returns the item's scene and its
-// bounds kind selects the node test per round; otherwise every ray walks
-// `scene` with the BOUNDS test.
+// Persistent loop of group walks over n work items. Group k of the grid
+// takes item k first, then, whenever its walk ends, item (groups in the
+// grid) + the value of one atomic increment of *work (which starts at 0).
+// load(i, o, d, tmax) fills the ray of item i; finish(i, walk) runs in the
+// group's first lane. With MULTI the rays belong to different scenes: load
+// returns the item's scene and its bounds kind selects the node test per
+// round; otherwise every ray walks `scene` with the BOUNDS test.
 template <bool ANY_HIT, int BOUNDS, int G, bool MULTI, typename Load, typename Finish>
 GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long long* work, uint32_t* err, Load load,
                               Finish finish) {
-    // Each group fetches its next item with its own atomic and leaves the
-    // loop once the items are exhausted: the loop has no warp-wide
-    // synchronisation, so the last long walks of a warp do not wait for
-    // idle groups at every round (all shuffles stay inside the group).
+    // The loop has no warp-wide synchronisation: all shuffles stay inside
+    // the group, and a group leaves once the items are exhausted. The first
+    // item needs no atomic, so a launch does not start with one increment
+    // per group queued on the same counter (tens of thousands of them
+    // serialise in L2 for ~10 us); small launches cost no atomics at all.
     const unsigned lane = threadIdx.x & 31u;
     const unsigned gl = lane & (G - 1), gbase = lane & ~(unsigned)(G - 1);
     const unsigned gmask = ((1u << G) - 1u) << gbase;
+    const uint64_t perBlock = blockDim.x / G;
+    const uint64_t groups = (uint64_t)gridDim.x * perBlock;
     GroupWalk g;
     const DevScene* sc = nullptr;
-    while (true) {
-        unsigned long long my = 0;
-        if (gl == 0) my = atomicAdd(work, 1ull);
-        my = __shfl_sync(gmask, my, gbase);
-        if (my >= n) break;
+    for (uint64_t my = (uint64_t)blockIdx.x * perBlock + threadIdx.x / G; my < n;) {
         float3 o, d;
         float tmax;
         if constexpr (MULTI) {
@@ -403,6 +399,9 @@ GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long l
                 done = group_step<ANY_HIT, BOUNDS, G>(g, scene, err, gl, gbase, gmask);
         }
         if (gl == 0) finish(my, g);
+        unsigned long long next = 0;
+        if (gl == 0) next = atomicAdd(work, 1ull);
+        my = groups + __shfl_sync(gmask, next, gbase);
     }
 }
 
