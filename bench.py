@@ -213,7 +213,7 @@ def run_ours(args, world, rank, local):
     sc, b, host_batches = make_workload()
     ctx = cuda.Context(local)
     ctx.set_trace_config(mode=args.trace_mode)
-    ctx.set_host_pipeline(args.host_parts, not args.no_zero_copy)
+    ctx.set_host_pipeline(args.host_parts, args.zero_copy)
     ctx.set_scene_layout(args.shared_nodes, 0)
     ds = ctx.upload_scene(b, sc["positions"])
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
@@ -725,8 +725,8 @@ def main():
     ap.add_argument("--batch-seed", type=int, default=1)
     ap.add_argument("--host-parts", type=int, default=2,
                     help="parts of a host-pointer query whose copies and traversal overlap")
-    ap.add_argument("--no-zero-copy", action="store_true",
-                    help="stage page-locked host arrays through device memory instead of direct access")
+    ap.add_argument("--zero-copy", action="store_true",
+                    help="kernels read and write the page-locked host arrays directly instead of staging")
     ap.add_argument("--workload", choices=["trace", "nrc", "passes", "batch", "large", "build"], default="trace",
                     help="trace: the closest-hit headline; nrc: time-to-equal-RMSE of the radiance cache; "
                          "passes: samples/s and Mrays/s of PT, LT and BPT; batch: batched vs per-job rendering; "

@@ -108,6 +108,38 @@ __global__ void k_centre_bounds(const float* __restrict__ pos, const uint4* __re
     }
 }
 
+// bvhmake's input rules, checked before any kernel indexes with the
+// triangles: bit 0 = vertex index out of range, bit 1 = v0 == v1 (the
+// padding triangle), bit 2 = material out of range.
+__global__ void k_validate(const uint4* __restrict__ tris, uint32_t n, uint32_t numVertices, uint32_t numMaterials,
+                           uint32_t* bad) {
+    uint32_t bits = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint4 t = tris[i];
+        if (t.x >= numVertices || t.y >= numVertices || t.z >= numVertices) bits |= 1u;
+        else if (t.x == t.y) bits |= 2u;
+        if (numMaterials > 0 && t.w >= numMaterials) bits |= 4u;
+    }
+    bits = __reduce_or_sync(0xffffffffu, bits);
+    if ((threadIdx.x & 31u) == 0 && bits) atomicOr(bad, bits);
+}
+
+// Triangles whose material emits (Emissivity, the fourth float4 of a
+// gpugi_material record): flags for an order-preserving compaction.
+__global__ void k_flag_emissive(const uint4* __restrict__ tris, uint32_t n, const float4* __restrict__ mats,
+                                uint32_t* __restrict__ flag) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 e = __ldg(mats + 6 * (size_t)tris[i].w + 3);
+        flag[i] = (e.x != 0.0f || e.y != 0.0f || e.z != 0.0f) ? 1u : 0u;
+    }
+}
+
+__global__ void k_compact(const uint4* __restrict__ tris, uint32_t n, const uint32_t* __restrict__ flag,
+                          const uint32_t* __restrict__ pos, uint4* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (flag[i]) out[pos[i]] = tris[i];
+}
+
 // Spread the low 21 bits of v to every third bit of a 63-bit word.
 GPUGI_D uint64_t spread3(uint32_t v) {
     uint64_t x = v & 0x1FFFFFu;
@@ -438,6 +470,14 @@ static gpugi_status build_into(gpugi_ctx* ctx, gpugi_scene* sc, const float* pos
     const uint32_t init[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
     GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(bounds, init, sizeof init, cudaMemcpyHostToDevice, st));
     const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->numSMs * 8);
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counters, 0, 32, st));
+    k_validate<<<grid, 256, 0, st>>>(dTri, n, numVertices, numMaterials, counters);
+    uint32_t bad = 0;
+    GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(&bad, counters, 4, cudaMemcpyDeviceToHost, st));
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if (bad & 1u) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "triangle references a vertex out of range");
+    if (bad & 2u) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "triangle with v0 == v1");
+    if (bad & 4u) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "triangle references a material out of range");
     k_centre_bounds<<<grid, 256, 0, st>>>(dPos, dTri, n, bounds);
     k_morton<<<grid, 256, 0, st>>>(dPos, dTri, n, bounds, keys, vals);
     size_t tempBytes = 0, scanBytes = 0;
@@ -547,11 +587,42 @@ static gpugi_status build_into(gpugi_ctx* ctx, gpugi_scene* sc, const float* pos
     sc->dev.numMaterials = numMaterials;
     sc->dev.topNodes = 0;
     sc->numLeafBlocks = numBlocks;
-    // host copies for the light tables: the triangles (their order only
-    // changes which light triangle a sample index picks), positions, materials
-    sc->hostPositions.assign(positions, positions + 3 * (size_t)numVertices);
-    sc->hostSlots.assign(reinterpret_cast<const int32_t*>(triangles),
-                         reinterpret_cast<const int32_t*>(triangles) + 4 * (size_t)n);
+    // Host copies for the light tables (Scene::LoadLightSources): only the
+    // emissive triangles, in input order, each with its own three vertices.
+    bool anyEmissive = false;
+    for (uint32_t m = 0; m < numMaterials; ++m) {
+        const float* e = reinterpret_cast<const float*>(materials) + 24 * (size_t)m + 12;
+        anyEmissive = anyEmissive || e[0] != 0.0f || e[1] != 0.0f || e[2] != 0.0f;
+    }
+    if (anyEmissive) {
+        // flag and blockOf are free again (the kernels that read them are
+        // queued before on the same stream)
+        k_flag_emissive<<<grid, 256, 0, st>>>(dTri, n, dMat, flag);
+        GPUGI_CUDA_TRY(ctx, cub::DeviceScan::ExclusiveSum(temp, scanBytes, flag, blockOf, (int)n, st));
+        uint32_t last[2];
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(&last[0], flag + n - 1, 4, cudaMemcpyDeviceToHost, st));
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(&last[1], blockOf + n - 1, 4, cudaMemcpyDeviceToHost, st));
+        GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        const uint32_t ne = last[0] + last[1];
+        std::vector<uint32_t> list(4 * (size_t)ne);
+        if (ne) {
+            uint4* emissive;
+            if (S.get(&emissive, ne)) return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "builder scratch");
+            k_compact<<<grid, 256, 0, st>>>(dTri, n, flag, blockOf, emissive);
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(list.data(), emissive, 16 * (size_t)ne, cudaMemcpyDeviceToHost, st));
+            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        }
+        sc->hostSlots.resize(4 * (size_t)ne);
+        sc->hostPositions.resize(9 * (size_t)ne);
+        for (uint32_t k = 0; k < ne; ++k) {
+            for (int v = 0; v < 3; ++v) {
+                sc->hostSlots[4 * (size_t)k + v] = (int32_t)(3 * k + v);
+                for (int c = 0; c < 3; ++c)
+                    sc->hostPositions[9 * (size_t)k + 3 * v + c] = positions[3 * (size_t)list[4 * (size_t)k + v] + c];
+            }
+            sc->hostSlots[4 * (size_t)k + 3] = (int32_t)list[4 * (size_t)k + 3];
+        }
+    }
     if (numMaterials)
         sc->hostMaterials.assign(reinterpret_cast<const float*>(materials),
                                  reinterpret_cast<const float*>(materials) + 24 * (size_t)numMaterials);
@@ -571,16 +642,6 @@ extern "C" gpugi_status gpugi_scene_build(gpugi_ctx* ctx, const float* positions
     if (leafSize == 0 || leafSize > 32) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "leafSize must be in [1, 32]");
     if (numMaterials > 0 && !materials) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "materials is NULL");
     if (numTriangles >= 0x10000000u) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many triangles (2^28 at most)");
-    // bvhmake's input rules: vertex indices in range, v0 != v1 (a slot with
-    // v0 == v1 is the invalid padding triangle), materials in range
-    for (uint32_t t = 0; t < numTriangles; ++t) {
-        const uint32_t* q = triangles + 4 * (size_t)t;
-        if (q[0] >= numVertices || q[1] >= numVertices || q[2] >= numVertices)
-            return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "triangle references a vertex out of range");
-        if (q[0] == q[1]) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "triangle with v0 == v1");
-        if (numMaterials > 0 && q[3] >= numMaterials)
-            return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "triangle references a material out of range");
-    }
     cudaError_t se = cudaSetDevice(ctx->device);
     if (se != cudaSuccess) return cuda_fail(ctx, se, "cudaSetDevice");
     gpugi_scene* sc = new gpugi_scene();

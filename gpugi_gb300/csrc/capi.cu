@@ -68,6 +68,7 @@ static gpugi_status ensure_pipeline(gpugi_ctx* ctx) {
     if (ctx->copyIn) return GPUGI_OK;
     GPUGI_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copyIn, cudaStreamNonBlocking));
     GPUGI_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copyOut, cudaStreamNonBlocking));
+    GPUGI_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->compute2, cudaStreamNonBlocking));
     for (int k = 0; k < 8; ++k) {
         GPUGI_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->evIn[k], cudaEventDisableTiming));
         GPUGI_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->evTraced[k], cudaEventDisableTiming));
@@ -77,10 +78,11 @@ static gpugi_status ensure_pipeline(gpugi_ctx* ctx) {
 
 // Ray queries on host arrays. Rays go through device staging in chunks of at
 // most 2^22. With trace modes 2-5 a chunk is split into ctx->hostParts parts
-// whose copies in (copyIn stream), traversal (context stream) and copies out
-// (copyOut stream) overlap: part p+1 uploads while part p is traced, and part
-// p downloads while part p+1 is traced. Each part has its own queue range and
-// counters. Returns when every result is in host memory.
+// whose copies in (copyIn stream), traversal (the context stream and a second
+// one, alternating by part) and copies out (copyOut stream) overlap: part p+1
+// uploads while part p is traced, part p downloads while part p+1 is traced,
+// and the traversals of neighbouring parts overlap too. Each part has its own
+// queue range and counters. Returns when every result is in host memory.
 // Device address of page-locked host memory (cudaHostAlloc / cudaHostRegister),
 // or nullptr for any other memory.
 static void* mapped_host(const void* p) {
@@ -165,19 +167,22 @@ static gpugi_status trace_host(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHi
                                                     ctx->copyIn));
             GPUGI_CUDA_TRY(ctx, cudaEventRecord(ctx->evIn[p], ctx->copyIn));
         }
+        // parts alternate between two traversal streams: the walker of part
+        // p+1 starts on the SMs that part p's walker frees in its tail
         for (uint32_t p = 0; p < parts; ++p) {
             const uint64_t p0 = p * per;
             if (p0 >= m) break;
             const uint64_t mp = std::min(per, m - p0);
-            GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->evIn[p], 0));
-            GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counters + 4 * p, 0, 4 * sizeof(unsigned long long), ctx->stream));
+            cudaStream_t cs = (p & 1u) ? ctx->compute2 : ctx->stream;
+            GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(cs, ctx->evIn[p], 0));
+            GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counters + 4 * p, 0, 4 * sizeof(unsigned long long), cs));
             if ((st = launch_trace_filtered_on(ctx, sc, anyHit, d[0] + p0, d[1] + p0, d[2] + p0, d[3] + p0, d[4] + p0,
                                                d[5] + p0, d[6] + p0, mp, anyHit ? nullptr : dSlot + p0,
                                                anyHit ? nullptr : dT + p0, anyHit ? nullptr : dU + p0,
                                                anyHit ? nullptr : dV + p0, anyHit ? dOcc + p0 : nullptr,
-                                               ctx->queue + p0, counters + 4 * p)))
+                                               ctx->queue + p0, counters + 4 * p, cs)))
                 return st;
-            GPUGI_CUDA_TRY(ctx, cudaEventRecord(ctx->evTraced[p], ctx->stream));
+            GPUGI_CUDA_TRY(ctx, cudaEventRecord(ctx->evTraced[p], cs));
         }
         for (uint32_t p = 0; p < parts; ++p) {
             const uint64_t p0 = p * per;
@@ -198,6 +203,7 @@ static gpugi_status trace_host(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHi
         GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->copyOut));
     }
     GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->compute2) GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->compute2));
     return GPUGI_OK;
 }
 
@@ -249,8 +255,10 @@ void gpugi_destroy(gpugi_ctx* ctx) {
     if (ctx->copyIn) {
         cudaStreamSynchronize(ctx->copyIn);
         cudaStreamSynchronize(ctx->copyOut);
+        cudaStreamSynchronize(ctx->compute2);
         cudaStreamDestroy(ctx->copyIn);
         cudaStreamDestroy(ctx->copyOut);
+        cudaStreamDestroy(ctx->compute2);
         for (int k = 0; k < 8; ++k) {
             cudaEventDestroy(ctx->evIn[k]);
             cudaEventDestroy(ctx->evTraced[k]);

@@ -29,8 +29,9 @@ struct gpugi_ctx {
     // host-pointer ray queries: copies in, traversal and copies out of
     // hostParts parts of a call overlap on three streams (trace modes 2-5)
     uint32_t hostParts = 2;
-    uint32_t hostZeroCopy = 1;  // page-locked host arrays are read and written by the kernels directly
+    uint32_t hostZeroCopy = 0;  // 1: page-locked host arrays are read and written by the kernels directly
     cudaStream_t copyIn = nullptr, copyOut = nullptr;
+    cudaStream_t compute2 = nullptr;  // second traversal stream of the host-pointer pipeline
     cudaEvent_t evIn[8] = {}, evTraced[8] = {};
     // batched rendering
     uint32_t batchPaths = 16u << 20;  // path-queue capacity of one round
@@ -126,7 +127,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
                                       const float* oy, const float* oz, const float* dx, const float* dy,
                                       const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
                                       float* u, float* v, uint8_t* occluded, uint32_t* queue,
-                                      unsigned long long* counters);
+                                      unsigned long long* counters, cudaStream_t stream = nullptr);
 // Launch shape of a persistent walker: grid, dynamic shared memory and the
 // number of top-of-tree nodes it stages (at most maxStage).
 struct WalkerLaunch {

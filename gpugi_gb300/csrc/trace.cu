@@ -343,8 +343,9 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
                                       const float* oy, const float* oz, const float* dx, const float* dy,
                                       const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
                                       float* u, float* v, uint8_t* occluded, uint32_t* queue,
-                                      unsigned long long* counters) {
+                                      unsigned long long* counters, cudaStream_t stream) {
     if (n == 0) return GPUGI_OK;
+    cudaStream_t cs = stream ? stream : ctx->stream;
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
     // four rays per thread with 16-B accesses when every array allows it
     auto al = [](const void* p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; };
@@ -355,7 +356,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         const unsigned grid4 = (unsigned)((n4 + 255) / 256);
         auto f4 = [](const float* p) { return reinterpret_cast<const float4*>(p); };
 #define GPUGI_FILTER4_ON(A, B)                                                                                        \
-    k_trace_root_filter4<A, B><<<grid4, 256, 0, ctx->stream>>>(                                                      \
+    k_trace_root_filter4<A, B><<<grid4, 256, 0, cs>>>(                                                      \
         sc->dev, f4(ox), f4(oy), f4(oz), f4(dx), f4(dy), f4(dz), f4(tmax), n4, reinterpret_cast<int4*>(slot),          \
         reinterpret_cast<float4*>(t), reinterpret_cast<float4*>(u), reinterpret_cast<float4*>(v),                     \
         reinterpret_cast<uchar4*>(occluded), queue, counters)
@@ -373,7 +374,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         const unsigned grid1 = (unsigned)((m + 255) / 256);
         auto sh = [&](const float* p) { return p + head; };
 #define GPUGI_FILTER_ON(A, B)                                                                                        \
-    k_trace_root_filter<A, B><<<grid1, 256, 0, ctx->stream>>>(                                                       \
+    k_trace_root_filter<A, B><<<grid1, 256, 0, cs>>>(                                                       \
         sc->dev, sh(ox), sh(oy), sh(oz), sh(dx), sh(dy), sh(dz), sh(tmax), m, slot ? slot + head : nullptr,            \
         t ? t + head : nullptr, u ? u + head : nullptr, v ? v + head : nullptr, occluded ? occluded + head : nullptr, \
         queue, counters, (uint32_t)head)
@@ -403,7 +404,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         WalkerLaunch L;
         gpugi_status st = walker_launch_config(ctx, sc, (const void*)kg, 1ull << 40, 0, L);
         if (st) return st;
-        kg<<<L.grid, 128, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded, queue,
+        kg<<<L.grid, 128, 0, cs>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded, queue,
                                            counters, ctx->errWord);
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
         return GPUGI_OK;
@@ -416,7 +417,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
     WalkerLaunch L;
     gpugi_status st = walker_launch_config(ctx, sc, (const void*)k, n, ctx->sharedNodes, L);
     if (st) return st;
-    k<<<L.grid, 128, L.smem, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded, queue,
+    k<<<L.grid, 128, L.smem, cs>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded, queue,
                                             counters, ctx->errWord, L.stage);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;

@@ -135,9 +135,9 @@ class Context:
     def set_trace_config(self, mode: int = 3, block_size: int = 128):
         self.check(lib().gpugi_set_trace_config(self._h, mode, block_size))
 
-    def set_host_pipeline(self, parts: int = 2, zero_copy: bool = True):
-        """Host-pointer queries: kernels access page-locked arrays directly (zero_copy), else
-        staging split into `parts` overlapping parts (1: no overlap)."""
+    def set_host_pipeline(self, parts: int = 2, zero_copy: bool = False):
+        """Host-pointer queries: staging split into `parts` overlapping parts (1: no overlap),
+        or kernels accessing page-locked arrays directly (zero_copy)."""
         self.check(lib().gpugi_set_host_pipeline(self._h, parts, int(bool(zero_copy))))
 
     def set_scene_layout(self, shared_nodes: int = 0, render_shared_nodes: int = 0):

@@ -47,6 +47,7 @@ typedef enum gpugi_status {
 #define GPUGI_DEVERR_TRAVERSAL_CAP 0x1u   /* a walk exceeded numNodes visits */
 #define GPUGI_DEVERR_QUEUE_OVERFLOW 0x2u  /* a wavefront queue or light cache overflowed */
 #define GPUGI_DEVERR_WAIT_TIMEOUT 0x4u    /* a bounded device wait ran out */
+#define GPUGI_DEVERR_BUILD 0x8u           /* the GPU hierarchy build found an inconsistent tree */
 
 enum gpugi_bounds_kind { GPUGI_BOUNDS_AABB = 0, GPUGI_BOUNDS_ELLIPSOID = 1 };
 
@@ -186,13 +187,15 @@ gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* scene,
  * return identical results. blockSize applies to mode 0. */
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize);
 
-/* Host-pointer ray queries (gpugi_trace_closest / gpugi_trace_any). With
- * zeroCopy (default 1) and every array page-locked (cudaHostAlloc,
- * cudaHostRegister), the kernels read the rays and write the results over
- * the host link directly. Otherwise the arrays go through device staging,
- * and each call is split into `parts` parts (1-8, default 2) whose copies to
- * the device, traversal and copies back overlap on separate streams (trace
- * modes 2-5; 1 disables the overlap). Results are the same on every path. */
+/* Host-pointer ray queries (gpugi_trace_closest / gpugi_trace_any). The
+ * arrays go through device staging, and each call is split into `parts`
+ * parts (1-8, default 2) whose copies to the device, traversal and copies
+ * back overlap on separate streams (trace modes 2-5; neighbouring parts are
+ * traversed on two streams, so one part's walker tail overlaps the next
+ * part's walk; 1 disables the overlap). With zeroCopy (default 0) and every
+ * array page-locked (cudaHostAlloc, cudaHostRegister), the kernels instead
+ * read the rays and write the results over the host link directly, in one
+ * part. Results are the same on every path. */
 gpugi_status gpugi_set_host_pipeline(gpugi_ctx* ctx, uint32_t parts, uint32_t zeroCopy);
 
 /* Scene layout tuning (set by the autotuner), applied to scenes uploaded

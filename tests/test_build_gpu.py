@@ -94,6 +94,13 @@ def test_render_equals_host_built_scene(cuda_ctx):
     diff = np.abs(imgs[0] - imgs[1]).max(-1)
     assert (diff <= 1e-4 * np.abs(imgs[0]).max() + 1e-6).mean() > 0.995
     assert abs(imgs[1].mean() / imgs[0].mean() - 1) < 1e-3
+    # light tables of the GPU-built scene (its emissive triangles): the same
+    # total flux per sample, positions on the ceiling light
+    a = render.generate_light_samples(host, [9], 512)
+    b = render.generate_light_samples(gpu, [9], 512)
+    assert np.allclose(a[:, 4:7], b[:, 4:7], rtol=1e-6)
+    assert np.allclose(b[:, 1], a[:, 1], atol=1e-6)  # the ceiling light's plane (the sampler's 1e-4 offset included)
+    assert (np.abs(b[:, [0, 2]]) <= 0.25 + 1e-6).all()
     for x in (host, gpu):
         x.close()
 
@@ -110,3 +117,9 @@ def test_rejects_bad_triangles(cuda_ctx):
         cuda_ctx.build_scene(sc["positions"], bad)
     with pytest.raises(cuda.GpugiError):
         cuda_ctx.build_scene(sc["positions"], sc["triangles"], leaf_size=33)
+    bad = sc["triangles"].copy()
+    bad[7, 3] = 1
+    with pytest.raises(cuda.GpugiError):
+        cuda_ctx.build_scene(sc["positions"], bad, materials=scenes.lambert((0.5, 0.5, 0.5))[None])
+    ds = cuda_ctx.build_scene(sc["positions"], sc["triangles"])  # the context stays usable
+    ds.close()
