@@ -284,6 +284,16 @@ public:
     void Draw() override;
 };
 
+// WhittedRayTracer (gpugi/renderer/whittedraytracer.hpp): follows specular and
+// glossy decisions, ends at the first diffuse decision with two NEE samples.
+class WhittedRayTracer : public Renderer {
+public:
+    explicit WhittedRayTracer(RendererSystem& rendererSystem);
+    std::string GetName() const override { return "WhittedRayTracer"; }
+    void SetScreenSize(const DeviceImage&) override {}
+    void Draw() override;
+};
+
 // Path tracer whose camera paths end in the neural radiance cache, trained
 // online on a fraction of full-length paths of every iteration.
 struct NrcSettings {

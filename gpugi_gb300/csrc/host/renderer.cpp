@@ -295,6 +295,11 @@ BidirectionalPathtracer::BidirectionalPathtracer(RendererSystem& rendererSystem)
 }
 void BidirectionalPathtracer::Draw() { draw_pass(m_rendererSystem, GPUGI_PASS_BPT); }
 
+WhittedRayTracer::WhittedRayTracer(RendererSystem& rendererSystem) : Renderer(rendererSystem) {
+    m_rendererSystem.SetNumInitialLightSamples(128);  // whittedraytracer.cpp:17
+}
+void WhittedRayTracer::Draw() { draw_pass(m_rendererSystem, GPUGI_PASS_WHITTED); }
+
 NrcPathtracer::NrcPathtracer(RendererSystem& rendererSystem, const NrcSettings& settings)
     : NrcPathtracer(rendererSystem, settings, GPUGI_PASS_PT) {}
 

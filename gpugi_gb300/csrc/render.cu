@@ -347,7 +347,7 @@ GPUGI_D Hit load_hit(const RenderConst& rc, const HitSoA& H, uint32_t k, float3 
 // assuming visibility and the shadow ray that decides it.
 GPUGI_D bool direct_light(const RenderConst& rc, uint32_t s, float3 pos, float3 N, uint32_t idx, float3 viewDir,
                           const MaterialData& m, bool sampleAreaLights, float3& radiance, float3& ro, float3& rd,
-                          float& rlen) {
+                          float& rlen, bool stopOnDiffuse = false) {
     const float4* ls = rc.lightSamples + 2 * ((size_t)s * rc.numLightSamples + idx);
     const float4 pn0 = __ldg(ls), in1 = __ldg(ls + 1);
     float pdf;
@@ -355,7 +355,7 @@ GPUGI_D bool direct_light(const RenderConst& rc, uint32_t s, float3 pos, float3 
         rd = xyz(pn0);
         float cosS = saturate(dot(rd, N));
         if (cosS <= 0.0f) return false;
-        radiance = (cosS * xyz(in1)) * eval_bsdf(viewDir, rd, m, N, pdf, false);
+        radiance = (cosS * xyz(in1)) * eval_bsdf(viewDir, rd, m, N, pdf, false, stopOnDiffuse);
         ro = kRAY_HIT_EPSILON * rd + pos;
         rlen = kRAY_MAX;
         return true;
@@ -367,11 +367,11 @@ GPUGI_D bool direct_light(const RenderConst& rc, uint32_t s, float3 pos, float3 
     const float cosS = saturate(dot(L, N));
     if (cosS <= 0.0f) return false;
     if (in1.w > 1.5f) {
-        radiance = ((cosS / distSq) * xyz(in1)) * eval_bsdf(viewDir, L, m, N, pdf, false);
+        radiance = ((cosS / distSq) * xyz(in1)) * eval_bsdf(viewDir, L, m, N, pdf, false, stopOnDiffuse);
     } else if (sampleAreaLights) {
         const float f = saturate(dot(unpack_normal(pn0.w, in1.w), -L));
         if (!(f > 0.0f)) return false;
-        radiance = ((cosS / distSq) * (xyz(in1) * f)) * eval_bsdf(viewDir, L, m, N, pdf, false);
+        radiance = ((cosS / distSq) * (xyz(in1) * f)) * eval_bsdf(viewDir, L, m, N, pdf, false, stopOnDiffuse);
     } else {
         return false;
     }
@@ -711,6 +711,90 @@ __global__ void __launch_bounds__(128) k_bpt_shade(RenderConst rc, PathSoA A, Pa
         if (L.shadow) store_shadow(Q, qs, L.sro, L.srd, L.srl, L.contrib, L.pixel);
         warp_append(&rc.cnt->path[depth + 1], L.survive, qb);
         if (L.survive) store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, L.lastP);
+    }
+}
+
+// ------------------------------------------------------------ Whitted
+// whittedraytracer.comp:14-30: one path per pixel and iteration. The seed is
+// InitCoherentRandomSeed (random.glsl:23-28): the same stream for every
+// pixel of a frame; the pixel jitter has no -0.5 offset. The iteration is
+// counted in alpha (the shader writes vec4(color, 1)).
+__global__ void k_whitted_generate(RenderConst rc, PathSoA A) {
+    const uint32_t total = rc.samples * (uint32_t)rc.numPixels;
+    if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+        const uint32_t s = p / (uint32_t)rc.numPixels, pix = p % (uint32_t)rc.numPixels;
+        const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
+        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s));
+        const float2 r = random2(seed);
+        const float sx = X::sub(X::mul(X::div(X::add(r.x, (float)x), (float)rc.width), 2.0f), 1.0f);
+        const float sy = X::sub(X::mul(X::div(X::add(r.y, (float)y), (float)rc.height), 2.0f), 1.0f);
+        const float3 d = X::normalize(X::add3(X::add3(X::scale(sx, rc.camU), X::scale(sy, rc.camV)), rc.camW));
+        store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, s << 8, 1.0f);
+        splat(rc, pix, f3(0.0f), 1.0f);
+    }
+}
+
+// whittedraytracer.comp:44-110, one bounce: emission of every hit; a
+// specular or glossy decision continues the path with a colour-shift
+// throughput; the first diffuse decision ends it with NUM_LIGHT_SAMPLES = 2
+// NEE samples (EstimateDirectLight with the BSDF of STOP_ON_DIFFUSE_BOUNCE)
+// weighted NumInitialLightSamples / 2 / luminance(pdiffuse).
+__global__ void __launch_bounds__(128) k_whitted_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q,
+                                                       int depth) {
+    const uint32_t n = rc.cnt->path[depth];
+    const float lightSampleWeight = (float)rc.numLightSamples / 2.0f;
+    WARP_LOOP(n, k, valid) {
+        bool survive = false, shadow[2] = {false, false};
+        float3 o, d, tp, sro[2], srd[2], contrib[2];
+        float srl[2] = {0.0f, 0.0f};
+        uint32_t seed = 0, pixel = 0, info = 0;
+        if (valid) {
+            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+            seed = A.seed[k];
+            pixel = A.pixel[k];
+            info = A.info[k];
+            Hit h = load_hit(rc, H, k, o, d);
+            if (!h.valid) {
+                splat(rc, pixel, tp * rc.sky);
+            } else {
+                o = h.pos;
+                splat(rc, pixel, tp * h.m.Emissivity);
+                float3 preflect, prefract, pdiffuse;
+                decision_probabilities(h.m, preflect, prefract, pdiffuse);
+                const float pdiffuseAvg = luminance(pdiffuse);
+                float3 thr = f3(1.0f);
+                float pdf;
+                const float3 nd = sample_bsdf(d, h.m, seed, h.N, thr, false, pdf, true);
+                if (thr.x == -1.0f) {
+#pragma unroll
+                    for (int l = 0; l < 2; ++l) {
+                        const uint32_t li = random_uint(seed) % rc.numLightSamples;
+                        float3 rad;
+                        if (direct_light(rc, info >> 8, o, h.N, li, d, h.m, true, rad, sro[l], srd[l], srl[l], true)) {
+                            contrib[l] = rad * tp * (lightSampleWeight / (pdiffuseAvg + kDIVISOR_EPSILON));
+                            shadow[l] = contrib[l].x != 0.0f || contrib[l].y != 0.0f || contrib[l].z != 0.0f;
+                        }
+                    }
+                } else {
+                    d = nd;
+                    o = o + d * kRAY_HIT_EPSILON;
+                    tp *= thr / (luminance(thr) + kDIVISOR_EPSILON);
+                    survive = depth + 1 < rc.maxPathLength;
+                }
+            }
+        }
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            uint32_t qs;
+            warp_append(&rc.cnt->shadow[depth], shadow[l], qs);
+            if (shadow[l]) store_shadow(Q, qs, sro[l], srd[l], srl[l], contrib[l], pixel);
+        }
+        uint32_t qb;
+        warp_append(&rc.cnt->path[depth + 1], survive, qb);
+        if (survive) store_path(B, qb, o, d, tp, seed, pixel, info, 1.0f);
     }
 }
 
@@ -1301,11 +1385,12 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rc.cnt, 0, offsetof(Counters, rays), ctx->stream));
     PathSoA A = rb->A, B = rb->B;
 
-    auto bounces = [&](int kind /*0 PT, 1 light, 2 light+cache, 3 BPT eye*/) -> gpugi_status {
+    auto bounces = [&](int kind /*0 PT, 1 light, 2 light+cache, 3 BPT eye, 4 Whitted*/) -> gpugi_status {
         for (int depth = 0; depth < rc.maxPathLength; ++depth) {
             launch_extend(ctx, W, rc, A, rb->H, depth);
             if (kind == 0) k_pt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
             else if (kind == 3) k_bpt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
+            else if (kind == 4) k_whitted_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
             else k_light_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth, kind == 2);
             launch_shadow(ctx, W, rc, rb->Q, depth);
             std::swap(A, B);
@@ -1318,6 +1403,9 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
     if (pass == GPUGI_PASS_PT) {
         k_camera_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A, false);
         if ((st = bounces(0))) return st;
+    } else if (pass == GPUGI_PASS_WHITTED) {
+        k_whitted_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
+        if ((st = bounces(4))) return st;
     } else if (pass == GPUGI_PASS_LT) {
         k_light_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A, false);
         if ((st = bounces(1))) return st;
@@ -1533,7 +1621,7 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
                           gpugi_image* im) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass > GPUGI_PASS_BPT) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->pass > GPUGI_PASS_WHITTED) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)
@@ -1550,7 +1638,10 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
     const uint32_t raysPerLight =
         std::max<uint32_t>(64u, (numPixels / p->numLightSamples / 64u) * 64u);
     const uint32_t lightThreads = raysPerLight * p->numLightSamples;
-    const uint32_t perSamplePaths = p->pass == GPUGI_PASS_PT ? numPixels : std::max(numPixels, lightThreads);
+    // Whitted: up to two shadow rays per path, so the queues get twice the paths
+    const uint32_t perSamplePaths = p->pass == GPUGI_PASS_PT        ? numPixels
+                                    : p->pass == GPUGI_PASS_WHITTED ? 2 * numPixels
+                                                                    : std::max(numPixels, lightThreads);
     // Light-cache capacity: the worst case (every particle stores its light
     // sample plus one entry per bounce) so it can never overflow.
     const uint64_t cachePerSample = p->pass == GPUGI_PASS_BPT ? (uint64_t)lightThreads * (p->maxPathLength + 1) : 0;
@@ -1722,7 +1813,7 @@ static gpugi_status check_render_args(gpugi_ctx* ctx, const gpugi_scene* sc, con
                                       const gpugi_render_params* p, const float* lightSamples,
                                       const uint64_t* rngState, const gpugi_image* im) {
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass > GPUGI_PASS_BPT) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->pass > GPUGI_PASS_WHITTED) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)

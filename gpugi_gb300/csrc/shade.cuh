@@ -111,9 +111,11 @@ GPUGI_D void decision_probabilities(const MaterialData& m, float3& preflect, flo
 }
 
 // __SampleBSDF (materials.glsl:118-277). The reference's rejection loop is
-// disabled (plausible = true), so exactly one lobe sample is drawn.
+// disabled (plausible = true), so exactly one lobe sample is drawn. With
+// stopOnDiffuse (the Whitted shader's STOP_ON_DIFFUSE_BOUNCE) a diffuse
+// decision sets throughput = (-1, 0, 0) and returns no direction.
 GPUGI_D float3 sample_bsdf(float3 incident, const MaterialData& m, uint32_t& seed, float3 N, float3& throughput,
-                           bool adjoint, float& pdf) {
+                           bool adjoint, float& pdf, bool stopOnDiffuse = false) {
     float cosTheta = dot(N, incident);
     float cosThetaAbs = saturate(fabsf(cosTheta));
     float3 rrDir = incident - (2.0f * cosTheta) * N;
@@ -127,6 +129,10 @@ GPUGI_D float3 sample_bsdf(float3 incident, const MaterialData& m, uint32_t& see
     float avgPPhong = avgPReflect;
     float decision = random01(seed);
     if (avgPDiffuse > decision) {
+        if (stopOnDiffuse) {
+            throughput = f3(-1.0f, 0.0f, 0.0f);
+            return f3(0.0f);
+        }
         throughput *= (m.Diffuse * pdiffuse) / avgPDiffuse;
         if (cosTheta > 0.0f) N = -N;
         float3 U, V;
@@ -156,8 +162,10 @@ GPUGI_D float3 sample_bsdf(float3 incident, const MaterialData& m, uint32_t& see
     return outDir;
 }
 
-// __BSDF (materials.glsl:306-391)
-GPUGI_D float3 eval_bsdf(float3 incident, float3 excident, const MaterialData& m, float3 N, float& pdf, bool adjoint) {
+// __BSDF (materials.glsl:306-391); stopOnDiffuse drops the refractive part
+// (STOP_ON_DIFFUSE_BOUNCE, materials.glsl:355-358).
+GPUGI_D float3 eval_bsdf(float3 incident, float3 excident, const MaterialData& m, float3 N, float& pdf, bool adjoint,
+                         bool stopOnDiffuse = false) {
     float cosTheta = dot(N, incident);
     float cosThetaAbs = saturate(fabsf(cosTheta));
     float cosThetaOut = dot(N, excident);
@@ -177,6 +185,7 @@ GPUGI_D float3 eval_bsdf(float3 incident, float3 excident, const MaterialData& m
         bsdf += pdiffuse * m.Diffuse / kPI;
         pdf += avg3(pdiffuse) * saturate(cosThetaOut) / kPI;
     }
+    if (stopOnDiffuse) return bsdf;
     float eta = cosTheta < 0.0f ? 1.0f / m.RefractionIndexAvg : m.RefractionIndexAvg;
     float etaSq = eta * eta;
     float sin2 = etaSq * (1.0f - cosTheta * cosTheta);

@@ -207,7 +207,7 @@ gpugi_status gpugi_set_host_pipeline(gpugi_ctx* ctx, uint32_t parts, uint32_t ze
 gpugi_status gpugi_set_scene_layout(gpugi_ctx* ctx, uint32_t sharedNodes, uint32_t renderSharedNodes);
 
 /* ------------------------------------------------------------------------
- * Rendering passes (wavefront): PT, LT and BPT.
+ * Rendering passes (wavefront): PT, LT, BPT and the Whitted ray tracer.
  *
  *   gpugi_render(pass = PT)   Pathtracer::Draw + pathtracer.comp
  *                             (gpugi/renderer/pathtracer.cpp:47-53, gpugi/shader/pathtracer.comp)
@@ -216,10 +216,12 @@ gpugi_status gpugi_set_scene_layout(gpugi_ctx* ctx, uint32_t sharedNodes, uint32
  *   gpugi_render(pass = BPT)  BidirectionalPathtracer::Draw: reset counter, light
  *                             trace into the light cache, eye pass
  *                             (gpugi/renderer/bidirectionalpathtracer.cpp:182-203)
+ *   gpugi_render(pass = WHITTED)  WhittedRayTracer::Draw + whittedraytracer.comp with
+ *                             STOP_ON_DIFFUSE_BOUNCE (gpugi/renderer/whittedraytracer.cpp:32-38)
  * ------------------------------------------------------------------------ */
 typedef struct gpugi_image gpugi_image;
 
-enum gpugi_pass { GPUGI_PASS_PT = 0, GPUGI_PASS_LT = 1, GPUGI_PASS_BPT = 2 };
+enum gpugi_pass { GPUGI_PASS_PT = 0, GPUGI_PASS_LT = 1, GPUGI_PASS_BPT = 2, GPUGI_PASS_WHITTED = 3 };
 
 /* Camera UBO (gpugi/shader/globaluniforms.glsl:7-15): U, V scaled by
  * tan(fov/2)*aspect and tan(fov/2), W unit view direction. */
@@ -235,7 +237,7 @@ typedef struct gpugi_render_params {
     uint32_t rrStartDepth;     /* Russian roulette from this bounce on; 0 = the reference */
     uint32_t iteration;        /* first iteration: FrameSeed(s) = WangHash(iteration + s) */
     uint32_t samples;          /* iterations (samples per pixel) rendered by this call */
-    uint32_t numLightSamples;  /* initial light samples per iteration (PT/BPT 128, LT 256) */
+    uint32_t numLightSamples;  /* initial light samples per iteration (PT/BPT/Whitted 128, LT 256) */
     float sky[3];              /* constant radiance on a miss (addition; 0 = the reference's black) */
     uint32_t flags;            /* reserved, 0 */
 } gpugi_render_params;

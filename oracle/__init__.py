@@ -99,14 +99,15 @@ def bruteforce_closest(slots, positions, rays, num_threads=None):
     return dict(slot=slot, t=t)
 
 
-PASSES = {"PT": 0, "LT": 1, "BPT": 2}
+PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3}
 
 
 def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.ndarray, frame_seed: int,
            light_samples: np.ndarray, max_path_length: int = 8, rr_start_depth: int = 0, sky=(0.0, 0.0, 0.0),
            accum: np.ndarray | None = None, num_threads=None) -> np.ndarray:
     """One iteration of a pass (restated pathtracer.comp / lighttracer.comp /
-    BPT), accumulated into accum (H, W, 4) float32, which is returned."""
+    BPT / whittedraytracer.comp), accumulated into accum (H, W, 4) float32,
+    which is returned."""
     from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
     L = lib()
     P, U32, I, F = C.c_void_p, C.c_uint32, C.c_int, C.c_float

@@ -11,6 +11,7 @@
 //   screenreproject.glsl:19-227 +
 //   showlightcaches.comp:9-65                 LT pass
 //   bidirpathtracer/*                         BPT light-cache + eye pass
+//   whittedraytracer.comp:14-115              Whitted ray tracer (STOP_ON_DIFFUSE_BOUNCE)
 // Two documented additions that the reference lacks: a constant sky radiance
 // returned on a miss (the reference samples a cube map, black by default) and
 // directional light samples (normalThetaCos == 3) for a sun.
@@ -144,7 +145,7 @@ static vec3 GetDiffuseProbability(const MaterialData& m, float) {
 
 // materials.glsl:118-277
 static vec3 SampleBSDFImpl(vec3 incidentDirection, const MaterialData& m, uint& seed, vec3 N, vec3& pathThroughput,
-                           bool adjoint, float& pdf, bool* isReflectedDiffuse) {
+                           bool adjoint, float& pdf, bool* isReflectedDiffuse, bool stopOnDiffuse = false) {
     float cosTheta = dot(N, incidentDirection);
     float cosThetaAbs = saturate(abs(cosTheta));
     vec3 reflectRefractDir = incidentDirection - (2.0f * cosTheta) * N;
@@ -159,6 +160,10 @@ static vec3 SampleBSDFImpl(vec3 incidentDirection, const MaterialData& m, uint& 
     float pathDecisionVar = Random(seed);
     if (avgPDiffuse > pathDecisionVar) {
         if (isReflectedDiffuse) *isReflectedDiffuse = true;
+        if (stopOnDiffuse) {  // STOP_ON_DIFFUSE_BOUNCE (materials.glsl:164-167)
+            pathThroughput = vec3(-1.0f, 0.0f, 0.0f);
+            return vec3(0.0f);
+        }
         pathThroughput *= (m.Diffuse * pdiffuse) / avgPDiffuse;
         if (cosTheta > 0.0f) N = -N;
         vec3 U, V;
@@ -196,7 +201,7 @@ static vec3 SampleBSDFImpl(vec3 incidentDirection, const MaterialData& m, uint& 
 
 // materials.glsl:306-391
 static vec3 BSDFImpl(vec3 incidentDirection, vec3 excidentDirection, const MaterialData& m, vec3 N, float& pdf,
-                     bool adjoint, bool specularOnly) {
+                     bool adjoint, bool specularOnly, bool stopOnDiffuse = false) {
     vec3 bsdf(0.0f);
     float cosTheta = dot(N, incidentDirection);
     float cosThetaAbs = saturate(abs(cosTheta));
@@ -216,6 +221,7 @@ static vec3 BSDFImpl(vec3 incidentDirection, vec3 excidentDirection, const Mater
         bsdf += pdiffuse * m.Diffuse / PI;
         pdf += Avg(pdiffuse) * saturate(cosThetaOut) / PI;
     }
+    if (stopOnDiffuse) return bsdf;  // STOP_ON_DIFFUSE_BOUNCE: no refractive NEE (materials.glsl:355-358)
     float eta = cosTheta < 0.0f ? 1.0f / m.RefractionIndexAvg : m.RefractionIndexAvg;
     float etaSq = eta * eta;
     float sinTheta2Sq = etaSq * (1.0f - cosTheta * cosTheta);
@@ -266,6 +272,7 @@ struct Params {
     const vec4* lightSamples;  // 2 texels per sample
     vec3 sky;                  // constant radiance on a miss (addition)
     int numRaysPerLightSample; // LT / BPT
+    bool stopOnDiffuse = false;  // Whitted: BSDF without its refractive part in NEE
 };
 
 struct Image {
@@ -298,7 +305,7 @@ static vec3 EstimateDirectLight(const RenderScene& s, const Params& P, vec3 pos,
         lightRay.Origin = RAY_HIT_EPSILON * lightRay.Direction + pos;
         if (!TraceRayAnyHit(s.geo, lightRay, RAY_MAX, nullptr)) {
             float pdf;
-            vec3 bsdf = BSDF(viewDir, lightRay.Direction, m, normal, pdf);
+            vec3 bsdf = BSDFImpl(viewDir, lightRay.Direction, m, normal, pdf, false, false, P.stopOnDiffuse);
             return (surfaceCos * in1.xyz()) * bsdf;
         }
         return vec3(0.0f);
@@ -314,7 +321,7 @@ static vec3 EstimateDirectLight(const RenderScene& s, const Params& P, vec3 pos,
         if (!TraceRayAnyHit(s.geo, lightRay, lightDist - RAY_HIT_EPSILON * 2, nullptr)) {
             vec3 irradiance = (surfaceCos / lightDistSq) * in1.xyz();
             float pdf;
-            vec3 bsdf = BSDF(viewDir, lightRay.Direction, m, normal, pdf);
+            vec3 bsdf = BSDFImpl(viewDir, lightRay.Direction, m, normal, pdf, false, false, P.stopOnDiffuse);
             return irradiance * bsdf;
         }
     } else if (sampleAreaLights) {
@@ -325,7 +332,7 @@ static vec3 EstimateDirectLight(const RenderScene& s, const Params& P, vec3 pos,
             if (!TraceRayAnyHit(s.geo, lightRay, lightDist - RAY_HIT_EPSILON * 2, nullptr)) {
                 float pdf;
                 vec3 intensity = in1.xyz() * f;
-                vec3 bsdf = BSDF(viewDir, lightRay.Direction, m, normal, pdf);
+                vec3 bsdf = BSDFImpl(viewDir, lightRay.Direction, m, normal, pdf, false, false, P.stopOnDiffuse);
                 vec3 irradiance = (surfaceCos / lightDistSq) * intensity;
                 return irradiance * bsdf;
             }
@@ -378,6 +385,53 @@ static vec3 PathtracePixel(const RenderScene& s, const Params& P, int x, int y) 
             if (Random(seed) >= p) break;
             pathThroughput /= p;
         }
+    }
+    return color;
+}
+
+// ------------------------------------------------------ whittedraytracer.comp
+// One pixel: InitCoherentRandomSeed (random.glsl:23-28) gives every pixel of a
+// frame the same RNG stream; specular/glossy decisions continue the path with
+// a colour-shift throughput, the first diffuse decision ends it with
+// NUM_LIGHT_SAMPLES = 2 NEE samples. The miss sky is the documented addition.
+static vec3 WhittedPixel(const RenderScene& s, const Params& P, int x, int y) {
+    const float lightSampleWeight = float(P.numLightSamples) / 2.0f;
+    uint seed = wanghash(P.frameSeed);
+    vec2 screen = (Random2(seed) + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
+    Ray ray;
+    ray.Origin = P.camPos;
+    ray.Direction = normalize(screen.x * P.camU + screen.y * P.camV + P.camW);
+    vec3 color(0.0f), pathThroughput(1.0f);
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        if (rayHit == RAY_MAX) {
+            color += pathThroughput * P.sky;
+            break;
+        }
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 hitNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        color += pathThroughput * m.Emissivity;
+        vec3 pdiffuse = GetDiffuseProbability(m, abs(dot(hitNormal, ray.Direction)));
+        float pdiffuseAvg = GetLuminance(pdiffuse);
+        vec3 throughput(1.0f);
+        float pdf;
+        vec3 sampleDirection = SampleBSDFImpl(ray.Direction, m, seed, hitNormal, throughput, false, pdf, nullptr, true);
+        if (throughput.x == -1.0f) {
+            for (int l = 0; l < 2; ++l) {
+                int sampleIndex = int(RandomUInt(seed) % (uint)P.numLightSamples);
+                vec3 radiance = EstimateDirectLight(s, P, ray.Origin, hitNormal, sampleIndex, ray.Direction, m, true);
+                color += radiance * pathThroughput * (lightSampleWeight / (pdiffuseAvg + DIVISOR_EPSILON));
+            }
+            break;
+        }
+        ray.Direction = sampleDirection;
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+        pathThroughput *= throughput / (GetLuminance(throughput) + DIVISOR_EPSILON);
     }
     return color;
 }
@@ -657,7 +711,7 @@ using namespace oracle;
 extern "C" {
 
 // One iteration of a pass, accumulated into rgba (w*h*4 floats).
-//   pass: 0 = PT, 1 = LT, 2 = BPT
+//   pass: 0 = PT, 1 = LT, 2 = BPT, 3 = Whitted
 //   cam: 13 floats {U, V, W, position, pixelArea}
 //   lightSamples: 8 floats per sample; sky: 3 floats (may be NULL)
 int oracle_render(const float* hierarchy, uint32_t numNodes, uint32_t boundsKind, const int32_t* slots,
@@ -696,6 +750,21 @@ int oracle_render(const float* hierarchy, uint32_t numNodes, uint32_t boundsKind
     P.numRaysPerLightSample = std::max(64, (numPixels / numLightSamples / 64) * 64);
     std::vector<std::mutex> locks(height);
     Image img{rgba, width, height, locks.data()};
+    P.stopOnDiffuse = pass == 3;  // STOP_ON_DIFFUSE_BOUNCE, a compile-time define of the Whitted shader
+    if (pass == 3) {
+        ParallelFor((uint64_t)numPixels, numThreads, [&](uint64_t b, uint64_t e) {
+            for (uint64_t p = b; p < e; ++p) {
+                int x = (int)(p % width), y = (int)(p / width);
+                vec3 c = WhittedPixel(s, P, x, y);
+                float* o = rgba + 4 * p;
+                o[0] += c.x;
+                o[1] += c.y;
+                o[2] += c.z;
+                o[3] += 1.0f;
+            }
+        });
+        return 0;
+    }
     if (pass == 0) {
         ParallelFor((uint64_t)numPixels, numThreads, [&](uint64_t b, uint64_t e) {
             for (uint64_t p = b; p < e; ++p) {

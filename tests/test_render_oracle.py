@@ -7,7 +7,10 @@ closed-form radiometry on tiny scenes:
   * a Lambertian floor under a point light shows albedo/pi * I cos / d^2
     (lightsource.glsl:25-55 with BSDF = albedo/pi);
   * the light tracer, path tracer and BPT converge to the same image on a
-    diffuse room (the reference's renderer-comparison practice).
+    diffuse room (the reference's renderer-comparison practice);
+  * the Whitted ray tracer on that floor (a diffuse decision at the first
+    hit, two NEE samples weighted 128 / 2) shows the same radiance, with its
+    pixel jitter in [x, x + 1) (whittedraytracer.comp:24, no -0.5).
 """
 import math
 
@@ -72,6 +75,37 @@ def test_point_light_on_lambert_floor(built):
     rel = np.abs(img - expected)[inner] / expected[inner]
     assert np.median(rel) < 0.02
     assert rel.max() < 0.15  # pixel footprint averaging
+
+
+def test_whitted_point_light_on_lambert_floor(built):
+    albedo, I, h = 0.6, 5.0, 1.5
+    sc = _quad_scene(albedo=albedo)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"])
+    W = H = 24
+    cam = render.camera_lookat((0.0, 3.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, -1.0), 40.0, W, H)
+    ls = _point_light_samples((0.0, h, 0.0), (I, I, I))
+    acc = None
+    iters = 32
+    for it in range(iters):
+        acc = oracle.render(b, sc, "WHITTED", W, H, cam.as_array(), render.wanghash(it), ls, max_path_length=4,
+                            accum=acc)
+    assert np.all(acc[..., 3] == iters)
+    img = acc[..., 0] / iters
+    c = cam.as_array()
+    U, V, Wd, P = c[0:3], c[3:6], c[6:9], c[9:12]
+    ys, xs = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    sx = (xs + 0.5) / W * 2 - 1
+    sy = (ys + 0.5) / H * 2 - 1
+    d = sx[..., None] * U + sy[..., None] * V + Wd
+    t = -P[1] / d[..., 1]
+    p = P + t[..., None] * d
+    r2 = p[..., 0] ** 2 + (h - p[..., 1]) ** 2 + p[..., 2] ** 2 + 1e-5
+    cos = h / np.sqrt(r2)
+    expected = albedo / math.pi * I * cos / r2
+    inner = (np.abs(p[..., 0]) < 1.5) & (np.abs(p[..., 2]) < 1.5)
+    rel = np.abs(img - expected)[inner] / expected[inner]
+    assert np.median(rel) < 0.02
+    assert rel.max() < 0.15
 
 
 def test_estimators_agree_on_diffuse_room(built):
