@@ -20,6 +20,10 @@ struct gpugi_ctx {
     // trace tuning
     uint32_t traceMode = 3;  // 0 thread per ray, 1 persistent lane refill, 2 root prefilter + 1, 3/4 + 8/4-lane groups
     uint32_t traceBlock = 128;
+    // photon mapper (PhotonMapper's pm_nphotons, pm_r, pm_progressive; photonmapper.cpp:17-45)
+    uint32_t pmPhotonsPerSample = 1u << 11;
+    float pmQueryRadius = 0.01f;
+    uint32_t pmProgressive = 0;
     uint32_t sharedNodes = 0;        // top-of-tree nodes laid out first and staged by ray-query walkers
     uint32_t renderSharedNodes = 0;  // nodes staged by the renderer's walkers
     void* scratch = nullptr;  // 256 B of device counters (work distribution)

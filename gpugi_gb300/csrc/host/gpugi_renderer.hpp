@@ -284,6 +284,25 @@ public:
     void Draw() override;
 };
 
+// PhotonMapper (gpugi/renderer/photonmapper.hpp): a photon map per iteration,
+// gathered at the first diffuse decision of the eye paths. The settings are
+// the GlobalConfig parameters pm_nphotons, pm_r and pm_progressive.
+class PhotonMapper : public Renderer {
+public:
+    explicit PhotonMapper(RendererSystem& rendererSystem);
+    std::string GetName() const override { return "PhotonMapper"; }
+    void SetScreenSize(const DeviceImage&) override {}
+    void Draw() override;
+    void SetNumPhotonsPerLightSample(unsigned int n) { m_numPhotonsPerLightSample = n; }
+    void SetQueryRadius(float r) { m_queryRadius = r; }
+    void SetProgressiveRadius(bool on) { m_progressiveRadius = on; }
+
+private:
+    unsigned int m_numPhotonsPerLightSample = 1u << 11;
+    float m_queryRadius = 0.01f;
+    bool m_progressiveRadius = false;
+};
+
 // WhittedRayTracer (gpugi/renderer/whittedraytracer.hpp): follows specular and
 // glossy decisions, ends at the first diffuse decision with two NEE samples.
 class WhittedRayTracer : public Renderer {

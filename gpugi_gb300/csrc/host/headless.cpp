@@ -5,7 +5,8 @@
 //
 //   gpugi_headless --scene FILE [--renderer Pathtracer|LightPathtracer|
 //                  BidirectionalPathtracer|NrcPathtracer|
-//                  NrcBidirectionalPathtracer|WhittedRayTracer] [--size W H]
+//                  NrcBidirectionalPathtracer|WhittedRayTracer|PhotonMapper]
+//                  [--size W H]
 //                  [--camera px py pz lx ly lz fovy] [--iterations N]
 //                  [--path-length L] [--rr-start D] [--sky r g b]
 //                  [--point-light px py pz ir ig ib] [--reference FILE.pfm]
@@ -91,6 +92,7 @@ int main(int argc, char** argv) {
         else if (a.renderer == "NrcPathtracer") system.SetRenderer<NrcPathtracer>();
         else if (a.renderer == "NrcBidirectionalPathtracer") system.SetRenderer<NrcBidirectionalPathtracer>();
         else if (a.renderer == "WhittedRayTracer") system.SetRenderer<WhittedRayTracer>();
+        else if (a.renderer == "PhotonMapper") system.SetRenderer<PhotonMapper>();
         else usage("unknown renderer");
 
         for (int i = 0; i < a.iterations; ++i) system.Draw();

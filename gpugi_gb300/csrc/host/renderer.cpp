@@ -300,6 +300,15 @@ WhittedRayTracer::WhittedRayTracer(RendererSystem& rendererSystem) : Renderer(re
 }
 void WhittedRayTracer::Draw() { draw_pass(m_rendererSystem, GPUGI_PASS_WHITTED); }
 
+PhotonMapper::PhotonMapper(RendererSystem& rendererSystem) : Renderer(rendererSystem) {
+    m_rendererSystem.SetNumInitialLightSamples(128);  // photonmapper.cpp:38
+}
+void PhotonMapper::Draw() {
+    m_rendererSystem.Check(gpugi_set_photon_config(m_rendererSystem.GetContext(), m_numPhotonsPerLightSample,
+                                                   m_queryRadius, m_progressiveRadius ? 1u : 0u));
+    draw_pass(m_rendererSystem, GPUGI_PASS_PM);
+}
+
 NrcPathtracer::NrcPathtracer(RendererSystem& rendererSystem, const NrcSettings& settings)
     : NrcPathtracer(rendererSystem, settings, GPUGI_PASS_PT) {}
 

@@ -21,6 +21,7 @@
 // Per-path RNG streams, the order of RNG draws and all shading formulas are
 // those of the shaders, so each estimator is the reference's.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -106,6 +107,14 @@ struct RenderConst {
     uint32_t* qPixel;
     uint32_t* queryCount;
     uint32_t queryCap;
+    // photon mapper; unused by the other passes
+    uint32_t* pmMap;             // HashMap: {cell hash key, list head} per entry
+    uint32_t pmMapSize;          // prime
+    float4* pmPhotons;           // 2 x float4 per photon: {next, flux}, {position, packed direction}
+    uint32_t* pmCount;
+    uint32_t pmCap;
+    float pmSpacing, pmRadiusSq; // HashGridSpacing, PhotonQueryRadiusSq
+    int photonsPerSample;        // NumPhotonsPerLightSample
 };
 
 // ------------------------------------------------------------ accumulation
@@ -798,6 +807,227 @@ __global__ void __launch_bounds__(128) k_whitted_shade(RenderConst rc, PathSoA A
     }
 }
 
+// ------------------------------------------------------------ photon mapper
+// photonmapper/photondistribution.comp, photonmapper/gather.comp and the
+// lossless hash grid of maps/hashmap.glsl + maps/grid.glsl: photons are
+// stored at diffuse decisions in a linked list per grid cell (the list
+// heads sit in an open-addressed table with quadratic probing), and eye
+// paths gather the photons of 2x2x2 cells at their first diffuse decision.
+
+GPUGI_D uint32_t pm_cell_hash(int x, int y, int z) {  // gridCellHash
+    uint32_t h = ((uint32_t)x & 0x7FFu) | (((uint32_t)y & 0x3FFu) << 11) | (((uint32_t)z & 0x7FFu) << 21);
+    return random_uint(h);
+}
+GPUGI_D uint32_t pm_snorm16(float v) {  // packSnorm2x16 component, ties to even
+    return (uint32_t)(uint16_t)(int16_t)rintf(fminf(fmaxf(v, -1.0f), 1.0f) * 32767.0f);
+}
+GPUGI_D uint32_t pack_normal32(float3 n) {  // PackNormal32 (helper.glsl:67-70)
+    const float px = n.x == 0.0f ? signf(n.y) / 2.0f : atan2f(n.y, n.x) / kPI;
+    return pm_snorm16(px) | (pm_snorm16(n.z) << 16);
+}
+GPUGI_D float3 unpack_normal32(uint32_t p) {  // UnpackNormal(uint) (helper.glsl:71-76)
+    auto u = [](uint32_t b) { return fminf(fmaxf((float)(int16_t)(uint16_t)b / 32767.0f, -1.0f), 1.0f); };
+    return unpack_normal(u(p & 0xFFFFu) * kPI, u(p >> 16));
+}
+
+// insertToHashGrid (maps/hashmap.glsl:31-59) of a photon at the end of the
+// photon array; a full array or table drops the photon and raises the
+// queue-overflow bit (the reference writes past its buffer instead).
+GPUGI_D void store_photon(const RenderConst& rc, float3 pos, float3 dir, float3 flux) {
+    const uint32_t idx = atomicAdd(rc.pmCount, 1u);
+    if (idx >= rc.pmCap) {
+        raise_error(rc.err, DEVERR_QUEUE_OVERFLOW);
+        return;
+    }
+    const int cx = (int)ceilf(X::div(pos.x, rc.pmSpacing)), cy = (int)ceilf(X::div(pos.y, rc.pmSpacing)),
+              cz = (int)ceilf(X::div(pos.z, rc.pmSpacing));
+    const uint32_t hash = pm_cell_hash(cx, cy, cz);
+    float4* rec = rc.pmPhotons + 2 * (size_t)idx;
+    rec[1] = make_float4(pos.x, pos.y, pos.z, __uint_as_float(pack_normal32(dir)));
+    uint32_t i = hash % rc.pmMapSize, step = 1;
+    for (uint32_t probe = 0; probe < rc.pmMapSize; ++probe) {
+        const uint32_t key = atomicCAS(rc.pmMap + 2 * (size_t)i, 0xFFFFFFFFu, hash);
+        if (key == hash || key == 0xFFFFFFFFu) {
+            const uint32_t next = atomicExch(rc.pmMap + 2 * (size_t)i + 1, idx);
+            rec[0] = make_float4(__uint_as_float(next), flux.x, flux.y, flux.z);
+            return;
+        }
+        i = (uint32_t)(((uint64_t)i + step * 2 + 1) % rc.pmMapSize);  // quadratic probing
+        ++step;
+    }
+    raise_error(rc.err, DEVERR_QUEUE_OVERFLOW);
+}
+
+// findFirst (maps/hashmap.glsl:61-90): list head of a cell or 0xFFFFFFFF.
+GPUGI_D uint32_t pm_find(const RenderConst& rc, uint32_t hash) {
+    uint32_t i = hash % rc.pmMapSize, step = 1;
+    for (uint32_t probe = 0; probe < rc.pmMapSize; ++probe) {
+        const uint2 e = __ldg(reinterpret_cast<const uint2*>(rc.pmMap) + i);
+        if (e.x == 0xFFFFFFFFu) return 0xFFFFFFFFu;
+        if (e.x == hash) return e.y;
+        i = (uint32_t)(((uint64_t)i + step * 2 + 1) % rc.pmMapSize);
+        ++step;
+    }
+    return 0xFFFFFFFFu;
+}
+
+// photondistribution.comp:10-32: photonsPerSample photons per light sample.
+__global__ void k_photon_generate(RenderConst rc, PathSoA A) {
+    const uint32_t total = rc.numLightSamples * (uint32_t)rc.photonsPerSample;
+    if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase) + g);
+        const uint32_t li = g / (uint32_t)rc.photonsPerSample;
+        const float4* ls = rc.lightSamples + 2 * (size_t)li;
+        const float4 pn0 = __ldg(ls), in1 = __ldg(ls + 1);
+        float3 tp = xyz(in1) * (kPI / (float)rc.photonsPerSample);
+        float3 d;
+        if (in1.w > 1.0f) {
+            d = sample_direction(random2(seed));
+            tp *= 4.0f;
+        } else {
+            const float3 n = unpack_normal(pn0.w, in1.w);
+            float3 U, V;
+            create_onb(n, U, V);
+            d = sample_hemisphere_cosine(random2(seed), U, V, n);
+        }
+        store_path(A, g, xyz(pn0), d, tp, seed, g, 0u, 1.0f);
+    }
+}
+
+// photondistribution.comp:34-105, one bounce: the photon is stored when the
+// adjoint BSDF sample decides for diffuse reflection, then continues (with
+// the photon mapper's Russian roulette, luminance + 0.02).
+__global__ void __launch_bounds__(128) k_photon_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, int depth) {
+    const uint32_t n = rc.cnt->path[depth];
+    WARP_LOOP(n, k, valid) {
+        bool survive = false;
+        float3 o, d, tp;
+        uint32_t seed = 0, gid = 0;
+        if (valid) {
+            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+            seed = A.seed[k];
+            gid = A.pixel[k];
+            const int32_t slot = H.slot[k];
+            if (slot >= 0) {
+                const float4 rec = __ldg(rc.s.tris + 3 * (size_t)slot + 2);
+                const float3 gN = make_float3(rec.y, rec.z, rec.w);  // cross(e1, e0), not normalised
+                o = X::add3(o, X::scale(H.t[k], d));
+                const int4 tri = __ldg(rc.s.slots + slot);
+                const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], nullptr);
+                const MaterialData m = load_material(rc.s, tri.w);
+                float3 thr = f3(1.0f);
+                float pdf;
+                bool diffuse = false;
+                const float3 nd = sample_bsdf(d, m, seed, sN, thr, true, pdf, false, &diffuse);
+                if (diffuse) store_photon(rc, o, d, tp);
+                thr *= shading_correction(d, nd, gN, sN);
+                tp *= thr;
+                survive = depth + 1 < rc.maxPathLength;
+                if (survive && depth >= rc.rrStartDepth) {
+                    const float p = saturate(luminance(thr) + 0.02f);
+                    if (random01(seed) >= p) survive = false;
+                    else tp /= p;
+                }
+                d = nd;
+                o = o + d * kRAY_HIT_EPSILON;
+            }
+        }
+        uint32_t qb;
+        warp_append(&rc.cnt->path[depth + 1], survive, qb);
+        if (survive) store_path(B, qb, o, d, tp, seed, gid, 0u, 1.0f);
+    }
+}
+
+// gather.comp:38-50: one eye path per pixel (jitter without -0.5), the
+// iteration counted in alpha.
+__global__ void k_pm_generate(RenderConst rc, PathSoA A) {
+    const uint32_t total = (uint32_t)rc.numPixels;
+    if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < total; pix += gridDim.x * blockDim.x) {
+        const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
+        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase) + pix);
+        const float2 r = random2(seed);
+        const float sx = X::sub(X::mul(X::div(X::add(r.x, (float)x), (float)rc.width), 2.0f), 1.0f);
+        const float sy = X::sub(X::mul(X::div(X::add(r.y, (float)y), (float)rc.height), 2.0f), 1.0f);
+        const float3 d = X::normalize(X::add3(X::add3(X::scale(sx, rc.camU), X::scale(sy, rc.camV)), rc.camW));
+        store_path(A, pix, rc.camPos, d, f3(1.0f), seed, pix, 0u, 1.0f);
+        splat(rc, pix, f3(0.0f), 1.0f);
+    }
+}
+
+// gather.comp:51-128, one bounce: emission of every hit; at the first
+// diffuse decision the photons of the 2x2x2 cells from round(pos / spacing)
+// are gathered (irradianceEstimate, gather.comp:11-36) and the path ends;
+// otherwise it continues with the +0.02 roulette.
+__global__ void __launch_bounds__(128) k_pm_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, int depth) {
+    const uint32_t n = rc.cnt->path[depth];
+    const float kernel = 1.0f / (kPI * rc.pmRadiusSq);
+    WARP_LOOP(n, k, valid) {
+        bool survive = false;
+        float3 o, d, tp;
+        uint32_t seed = 0, pixel = 0;
+        if (valid) {
+            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+            seed = A.seed[k];
+            pixel = A.pixel[k];
+            Hit h = load_hit(rc, H, k, o, d);
+            if (!h.valid) {
+                splat(rc, pixel, tp * rc.sky);
+            } else {
+                o = h.pos;
+                splat(rc, pixel, tp * h.m.Emissivity);
+                float3 thr = f3(1.0f);
+                float pdf;
+                bool diffuse = false;
+                const float3 nd = sample_bsdf(d, h.m, seed, h.N, thr, false, pdf, false, &diffuse);
+                if (diffuse) {
+                    float3 preflect, prefract, pdiffuse;
+                    decision_probabilities(h.m, preflect, prefract, pdiffuse);
+                    const float3 fr = ((pdiffuse * h.m.Diffuse) / kPI) / avg3(pdiffuse);
+                    const float side = dot(d, h.N);
+                    float3 irr = f3(0.0f);
+                    const int bx = (int)rintf(X::div(o.x, rc.pmSpacing)), by = (int)rintf(X::div(o.y, rc.pmSpacing)),
+                              bz = (int)rintf(X::div(o.z, rc.pmSpacing));
+                    for (int c = 0; c < 8; ++c) {
+                        uint32_t idx = pm_find(rc, pm_cell_hash(bx + (c & 1), by + ((c >> 1) & 1), bz + ((c >> 2) & 1)));
+                        for (uint32_t steps = 0; idx != 0xFFFFFFFFu && steps < rc.pmCap; ++steps) {
+                            const float4 r0 = __ldg(rc.pmPhotons + 2 * (size_t)idx);
+                            const float4 r1 = __ldg(rc.pmPhotons + 2 * (size_t)idx + 1);
+                            const float3 toPhoton = make_float3(r1.x, r1.y, r1.z) - o;
+                            const float rsq = dot(toPhoton, toPhoton);
+                            if (rsq <= rc.pmRadiusSq && fabsf(dot(toPhoton, h.N)) < 0.01f) {
+                                const float3 pdir = unpack_normal32(__float_as_uint(r1.w));
+                                if (!(side * dot(pdir, h.N) < 0.0f))
+                                    irr += fr * make_float3(r0.y, r0.z, r0.w) * (1.0f * kernel);
+                            }
+                            idx = __float_as_uint(r0.x);
+                        }
+                    }
+                    splat(rc, pixel, irr * tp);
+                } else {
+                    d = nd;
+                    o = o + d * kRAY_HIT_EPSILON;
+                    tp *= thr;
+                    survive = depth + 1 < rc.maxPathLength;
+                    if (survive && depth >= rc.rrStartDepth) {
+                        const float p = saturate(luminance(thr) + 0.02f);
+                        if (random01(seed) >= p) survive = false;
+                        else tp /= p;
+                    }
+                }
+            }
+        }
+        uint32_t qb;
+        warp_append(&rc.cnt->path[depth + 1], survive, qb);
+        if (survive) store_path(B, qb, o, d, tp, seed, pixel, 0u, 1.0f);
+    }
+}
+
 // ------------------------------------------------------------ radiance cache
 // Camera paths for the path tracer with a radiance cache: as
 // k_camera_generate, plus the choice of training paths (a per-frame hash of
@@ -1260,6 +1490,12 @@ struct RenderBuffers {
     float *queries = nullptr, *qT = nullptr, *radiance = nullptr, *tvRec = nullptr, *tvC = nullptr,
           *samples = nullptr;
     uint32_t *qPixel = nullptr, *tvCount = nullptr, *nrcCounters = nullptr;  // counters: queries, paths, samples
+    // photon mapper: hash table, photon records, append counter
+    void* pmBlock = nullptr;
+    size_t pmMapSize = 0, pmCap = 0;
+    uint32_t* pmMap = nullptr;
+    float4* pmPhotons = nullptr;
+    uint32_t* pmCount = nullptr;
     // batched rendering: job table + path offsets (device, pinned staging) and the replayed graph
     RenderConst *dJobs = nullptr, *hJobs = nullptr;
     uint32_t *dOffsets = nullptr, *hOffsets = nullptr;
@@ -1278,6 +1514,7 @@ static void free_render(gpugi_ctx* ctx) {
     if (rb->hOffsets) cudaFreeHost(rb->hOffsets);
     if (rb->block) cudaFree(rb->block);
     if (rb->nrcBlock) cudaFree(rb->nrcBlock);
+    if (rb->pmBlock) cudaFree(rb->pmBlock);
     if (rb->hostLights) cudaFreeHost(rb->hostLights);
     delete rb;
     ctx->render = nullptr;
@@ -1406,6 +1643,27 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
     } else if (pass == GPUGI_PASS_WHITTED) {
         k_whitted_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
         if ((st = bounces(4))) return st;
+    } else if (pass == GPUGI_PASS_PM) {
+        // PhotonMapper::Draw (photonmapper.cpp:79-114): clear the grid, distribute
+        // the photons of this iteration, gather (one iteration per call)
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rc.pmMap, 0xFF, 8 * (size_t)rc.pmMapSize, ctx->stream));
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rc.pmCount, 0, 4, ctx->stream));
+        k_photon_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
+        for (int depth = 0; depth < rc.maxPathLength; ++depth) {
+            launch_extend(ctx, W, rc, A, rb->H, depth);
+            k_photon_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, depth);
+            std::swap(A, B);
+        }
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rc.cnt, 0, offsetof(Counters, rays), ctx->stream));
+        A = rb->A;
+        B = rb->B;
+        k_pm_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
+        for (int depth = 0; depth < rc.maxPathLength; ++depth) {
+            launch_extend(ctx, W, rc, A, rb->H, depth);
+            k_pm_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, depth);
+            std::swap(A, B);
+        }
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     } else if (pass == GPUGI_PASS_LT) {
         k_light_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A, false);
         if ((st = bounces(1))) return st;
@@ -1512,6 +1770,51 @@ static gpugi_status ensure_nrc_buffers(gpugi_ctx* ctx, RenderBuffers* rb, size_t
     rb->nrcStride = stride;
     rb->nrcSampleCap = samples;
     return GPUGI_OK;
+}
+
+// Smallest prime >= n (the hash table size, photonmapper.cpp:138-143).
+static size_t next_prime(size_t n) {
+    if (n <= 2) return 2;
+    for (size_t c = n | 1;; c += 2) {
+        bool prime = true;
+        for (size_t d = 3; d * d <= c && prime; d += 2) prime = c % d != 0;
+        if (prime) return c;
+    }
+}
+
+// Hash table of at least 1.5x the photons of an iteration, and photon
+// records for every diffuse bounce of every photon (never overflows).
+static gpugi_status ensure_pm_buffers(gpugi_ctx* ctx, RenderBuffers* rb, uint64_t photons, uint32_t maxPathLength) {
+    const size_t mapSize = next_prime((size_t)(photons * 3 / 2));
+    const size_t cap = (size_t)photons * maxPathLength;
+    if (mapSize == rb->pmMapSize && cap <= rb->pmCap) return GPUGI_OK;
+    cudaStreamSynchronize(ctx->stream);
+    if (rb->pmBlock) cudaFree(rb->pmBlock);
+    rb->pmBlock = nullptr;
+    rb->pmMapSize = rb->pmCap = 0;
+    const size_t mapBytes = (8 * mapSize + 255) & ~size_t(255), photonBytes = 32 * cap;
+    if (cudaMalloc(&rb->pmBlock, mapBytes + photonBytes + 256) != cudaSuccess) {
+        rb->pmBlock = nullptr;
+        return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "photon map buffers");
+    }
+    char* base = static_cast<char*>(rb->pmBlock);
+    rb->pmMap = reinterpret_cast<uint32_t*>(base);
+    rb->pmPhotons = reinterpret_cast<float4*>(base + mapBytes);
+    rb->pmCount = reinterpret_cast<uint32_t*>(base + mapBytes + photonBytes);
+    rb->pmMapSize = mapSize;
+    rb->pmCap = cap;
+    return GPUGI_OK;
+}
+
+// Query radius of an iteration: fixed, or shrunk by Knaus-Zwicker's
+// r_k = r_(k-1) sqrt((k + 0.7) / (k + 1)) from iteration 1 on
+// (photonmapper.cpp:84-87), in closed form through log-gamma.
+static float pm_radius(const gpugi_ctx* ctx, uint32_t iteration) {
+    const double r0 = ctx->pmQueryRadius;
+    if (!ctx->pmProgressive || iteration == 0) return (float)r0;
+    const double k = iteration;
+    const double logProd = std::lgamma(k + 1.7) - std::lgamma(1.7) - (std::lgamma(k + 2.0) - std::lgamma(2.0));
+    return (float)(r0 * std::exp(0.5 * logProd));
 }
 
 static gpugi_status ensure_host_lights(gpugi_ctx* ctx, RenderBuffers* rb, size_t lightBytes) {
@@ -1621,7 +1924,7 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
                           gpugi_image* im) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass > GPUGI_PASS_WHITTED) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->pass > GPUGI_PASS_PM) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)
@@ -1639,8 +1942,12 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
         std::max<uint32_t>(64u, (numPixels / p->numLightSamples / 64u) * 64u);
     const uint32_t lightThreads = raysPerLight * p->numLightSamples;
     // Whitted: up to two shadow rays per path, so the queues get twice the paths
+    const bool pm = p->pass == GPUGI_PASS_PM;
+    const uint64_t photons = pm ? (uint64_t)p->numLightSamples * ctx->pmPhotonsPerSample : 0;
+    if (photons > (64ull << 20)) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "more than 64M photons per iteration");
     const uint32_t perSamplePaths = p->pass == GPUGI_PASS_PT        ? numPixels
                                     : p->pass == GPUGI_PASS_WHITTED ? 2 * numPixels
+                                    : pm                            ? std::max<uint32_t>(numPixels, (uint32_t)photons)
                                                                     : std::max(numPixels, lightThreads);
     // Light-cache capacity: the worst case (every particle stores its light
     // sample plus one entry per bounce) so it can never overflow.
@@ -1649,23 +1956,38 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
     uint64_t chunk = std::max<uint64_t>(1, (16ull << 20) / perSamplePaths);
     if (cachePerSample) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, (4ull << 30) / (cachePerSample * 64)));
     chunk = std::min<uint64_t>(chunk, p->samples);
+    if (pm) chunk = 1;  // one photon map per iteration
     const size_t lightBytes = chunk * p->numLightSamples * 32;
     gpugi_status st = ensure_buffers(ctx, chunk * perSamplePaths, chunk * cachePerSample * 64, lightBytes,
                                      (uint32_t)chunk);
     if (st) return st;
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
     if ((st = ensure_host_lights(ctx, rb, lightBytes))) return st;
+    if (pm && (st = ensure_pm_buffers(ctx, rb, photons, p->maxPathLength))) return st;
 
     RenderConst rc = make_render_const(ctx, sc, cam, p, im, rb);
     rc.numRaysPerLightSample = (int)raysPerLight;
     rc.lightThreads = lightThreads;
     rc.cacheCap = (uint32_t)cachePerSample;
+    if (pm) {
+        rc.pmMap = rb->pmMap;
+        rc.pmMapSize = (uint32_t)rb->pmMapSize;
+        rc.pmPhotons = rb->pmPhotons;
+        rc.pmCount = rb->pmCount;
+        rc.pmCap = (uint32_t)(photons * p->maxPathLength);
+        rc.photonsPerSample = (int)ctx->pmPhotonsPerSample;
+    }
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
     for (uint32_t s0 = 0; s0 < p->samples; s0 += (uint32_t)chunk) {
         const uint32_t ns = std::min<uint32_t>((uint32_t)chunk, p->samples - s0);
         if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, s0, ns, p->numLightSamples))) return st;
         rc.samples = ns;
         rc.sampleBase = s0;
+        if (pm) {
+            const float r = pm_radius(ctx, p->iteration + s0);
+            rc.pmRadiusSq = r * r;
+            rc.pmSpacing = r * 2.01f;
+        }
         if ((st = render_chunk(ctx, sc, rc, p->pass))) return st;
     }
     return GPUGI_OK;
@@ -1813,7 +2135,7 @@ static gpugi_status check_render_args(gpugi_ctx* ctx, const gpugi_scene* sc, con
                                       const gpugi_render_params* p, const float* lightSamples,
                                       const uint64_t* rngState, const gpugi_image* im) {
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass > GPUGI_PASS_WHITTED) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->pass > GPUGI_PASS_PM) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)
@@ -1824,6 +2146,19 @@ static gpugi_status check_render_args(gpugi_ctx* ctx, const gpugi_scene* sc, con
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "scene lacks vertex info or materials");
     if (!lightSamples && !rngState)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "either lightSamples or rngState is required");
+    return GPUGI_OK;
+}
+
+gpugi_status gpugi_set_photon_config(gpugi_ctx* ctx, uint32_t photonsPerLightSample, float queryRadius,
+                                     uint32_t progressive) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (photonsPerLightSample == 0 || photonsPerLightSample > (1u << 20))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "photonsPerLightSample must be in [1, 2^20]");
+    if (!(queryRadius > 0.0f) || !(queryRadius < 1e30f))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "queryRadius must be positive and finite");
+    ctx->pmPhotonsPerSample = photonsPerLightSample;
+    ctx->pmQueryRadius = queryRadius;
+    ctx->pmProgressive = progressive ? 1u : 0u;
     return GPUGI_OK;
 }
 

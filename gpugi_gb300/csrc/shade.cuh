@@ -115,7 +115,7 @@ GPUGI_D void decision_probabilities(const MaterialData& m, float3& preflect, flo
 // stopOnDiffuse (the Whitted shader's STOP_ON_DIFFUSE_BOUNCE) a diffuse
 // decision sets throughput = (-1, 0, 0) and returns no direction.
 GPUGI_D float3 sample_bsdf(float3 incident, const MaterialData& m, uint32_t& seed, float3 N, float3& throughput,
-                           bool adjoint, float& pdf, bool stopOnDiffuse = false) {
+                           bool adjoint, float& pdf, bool stopOnDiffuse = false, bool* reflectedDiffuse = nullptr) {
     float cosTheta = dot(N, incident);
     float cosThetaAbs = saturate(fabsf(cosTheta));
     float3 rrDir = incident - (2.0f * cosTheta) * N;
@@ -128,6 +128,7 @@ GPUGI_D float3 sample_bsdf(float3 incident, const MaterialData& m, uint32_t& see
     float3 pphong = preflect;
     float avgPPhong = avgPReflect;
     float decision = random01(seed);
+    if (reflectedDiffuse) *reflectedDiffuse = avgPDiffuse > decision;  // SAMPLING_DECISION_OUTPUT
     if (avgPDiffuse > decision) {
         if (stopOnDiffuse) {
             throughput = f3(-1.0f, 0.0f, 0.0f);

@@ -11,10 +11,10 @@ import numpy as np
 
 from . import cuda
 
-PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3}
+PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3, "PM": 4}
 # Initial light samples per iteration as each renderer configures them
 # (pathtracer.cpp:28, lightpathtracer.cpp:16, bidirectionalpathtracer.cpp:160).
-DEFAULT_LIGHT_SAMPLES = {"PT": 128, "LT": 256, "BPT": 128, "WHITTED": 128}
+DEFAULT_LIGHT_SAMPLES = {"PT": 128, "LT": 256, "BPT": 128, "WHITTED": 128, "PM": 128}
 
 
 class Camera(C.Structure):
@@ -52,6 +52,7 @@ def _declare():
     L.gpugi_render_ray_counts.argtypes = [P, P]
     L.gpugi_render_batch.argtypes = [P, P, U32]
     L.gpugi_set_batch_config.argtypes = [P, U32, U32]
+    L.gpugi_set_photon_config.argtypes = [P, U32, C.c_float, U32]
     L._render_declared = True
     return L
 
@@ -188,6 +189,13 @@ def render_batch(ctx: cuda.Context, jobs: list[dict]) -> None:
     ctx.check(L.gpugi_render_batch(ctx.handle, arr, len(jobs)))
     for st, ref in states:
         ref[0] = st.value
+
+
+def set_photon_config(ctx: cuda.Context, photons_per_light_sample: int = 2048, query_radius: float = 0.01,
+                      progressive: bool = False) -> None:
+    """Photon mapper settings (gpugi_set_photon_config)."""
+    ctx.check(_declare().gpugi_set_photon_config(ctx.handle, photons_per_light_sample, float(query_radius),
+                                                  int(bool(progressive))))
 
 
 def set_batch_config(ctx: cuda.Context, paths_per_round: int = 16 << 20, use_graph: bool = True) -> None:

@@ -218,10 +218,14 @@ gpugi_status gpugi_set_scene_layout(gpugi_ctx* ctx, uint32_t sharedNodes, uint32
  *                             (gpugi/renderer/bidirectionalpathtracer.cpp:182-203)
  *   gpugi_render(pass = WHITTED)  WhittedRayTracer::Draw + whittedraytracer.comp with
  *                             STOP_ON_DIFFUSE_BOUNCE (gpugi/renderer/whittedraytracer.cpp:32-38)
+ *   gpugi_render(pass = PM)   PhotonMapper::Draw: clear the hash grid, photon
+ *                             distribution, gather (gpugi/renderer/photonmapper.cpp:79-114,
+ *                             gpugi/shader/photonmapper/{photondistribution,gather}.comp);
+ *                             one photon map per iteration, see gpugi_set_photon_config
  * ------------------------------------------------------------------------ */
 typedef struct gpugi_image gpugi_image;
 
-enum gpugi_pass { GPUGI_PASS_PT = 0, GPUGI_PASS_LT = 1, GPUGI_PASS_BPT = 2, GPUGI_PASS_WHITTED = 3 };
+enum gpugi_pass { GPUGI_PASS_PT = 0, GPUGI_PASS_LT = 1, GPUGI_PASS_BPT = 2, GPUGI_PASS_WHITTED = 3, GPUGI_PASS_PM = 4 };
 
 /* Camera UBO (gpugi/shader/globaluniforms.glsl:7-15): U, V scaled by
  * tan(fov/2)*aspect and tan(fov/2), W unit view direction. */
@@ -237,7 +241,7 @@ typedef struct gpugi_render_params {
     uint32_t rrStartDepth;     /* Russian roulette from this bounce on; 0 = the reference */
     uint32_t iteration;        /* first iteration: FrameSeed(s) = WangHash(iteration + s) */
     uint32_t samples;          /* iterations (samples per pixel) rendered by this call */
-    uint32_t numLightSamples;  /* initial light samples per iteration (PT/BPT/Whitted 128, LT 256) */
+    uint32_t numLightSamples;  /* initial light samples per iteration (PT/BPT/Whitted/PM 128, LT 256) */
     float sky[3];              /* constant radiance on a miss (addition; 0 = the reference's black) */
     uint32_t flags;            /* reserved, 0 */
 } gpugi_render_params;
@@ -380,6 +384,13 @@ gpugi_status gpugi_render_batch(gpugi_ctx* ctx, const gpugi_job* jobs, uint32_t 
  * at least the largest job image) and whether rounds replay a CUDA graph
  * (default 1). */
 gpugi_status gpugi_set_batch_config(gpugi_ctx* ctx, uint32_t pathsPerRound, uint32_t useGraph);
+
+/* Photon mapper settings (PhotonMapper's pm_nphotons, pm_r and
+ * pm_progressive; gpugi/renderer/photonmapper.cpp:17-45): photons traced per
+ * light sample (default 2048), query radius (default 0.01; grid spacing
+ * 2.01 x radius) and Knaus-Zwicker radius shrinking per iteration (default 0). */
+gpugi_status gpugi_set_photon_config(gpugi_ctx* ctx, uint32_t photonsPerLightSample, float queryRadius,
+                                     uint32_t progressive);
 
 /* Autotuner. No counterpart in the reference (its launch shapes are fixed
  * local sizes, e.g. gpugi/renderer/pathtracer.cpp:11). Times candidates on

@@ -104,10 +104,11 @@ PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3}
 
 def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.ndarray, frame_seed: int,
            light_samples: np.ndarray, max_path_length: int = 8, rr_start_depth: int = 0, sky=(0.0, 0.0, 0.0),
-           accum: np.ndarray | None = None, num_threads=None) -> np.ndarray:
+           accum: np.ndarray | None = None, num_threads=None, photons_per_light_sample: int = 2048,
+           query_radius: float = 0.01) -> np.ndarray:
     """One iteration of a pass (restated pathtracer.comp / lighttracer.comp /
-    BPT / whittedraytracer.comp), accumulated into accum (H, W, 4) float32,
-    which is returned."""
+    BPT / whittedraytracer.comp / the photon mapper "PM"), accumulated into
+    accum (H, W, 4) float32, which is returned."""
     from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
     L = lib()
     P, U32, I, F = C.c_void_p, C.c_uint32, C.c_int, C.c_float
@@ -122,10 +123,20 @@ def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.nda
     skya = np.asarray(sky, dtype=np.float32)
     if accum is None:
         accum = np.zeros((height, width, 4), np.float32)
+    nt = threads() if num_threads is None else num_threads
+    if pass_ == "PM":
+        L.oracle_render_pm.argtypes = [P, U32, U32, P, U32, U32, P, P, U32, P, U32, I, I, I, I, P, U32, P, I, P, I,
+                                       F, P, I]
+        rc = L.oracle_render_pm(_p(hier), hier.shape[0], bvh.bounds_kind, _p(slots), slots.shape[0], bvh.leaf_size,
+                                _p(pos), _p(vi), pos.shape[0], _p(mats), mats.shape[0], width, height,
+                                max_path_length, rr_start_depth, _p(cam), frame_seed & 0xFFFFFFFF, _p(ls),
+                                ls.shape[0], _p(skya), photons_per_light_sample, float(query_radius), _p(accum), nt)
+        assert rc == 0
+        return accum
     rc = L.oracle_render(_p(hier), hier.shape[0], bvh.bounds_kind, _p(slots), slots.shape[0], bvh.leaf_size,
                          _p(pos), _p(vi), pos.shape[0], _p(mats), mats.shape[0], PASSES[pass_], width, height,
                          max_path_length, rr_start_depth, _p(cam), frame_seed & 0xFFFFFFFF, _p(ls), ls.shape[0],
-                         _p(skya), _p(accum), threads() if num_threads is None else num_threads)
+                         _p(skya), _p(accum), nt)
     assert rc == 0
     return accum
 

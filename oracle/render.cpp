@@ -12,12 +12,17 @@
 //   showlightcaches.comp:9-65                 LT pass
 //   bidirpathtracer/*                         BPT light-cache + eye pass
 //   whittedraytracer.comp:14-115              Whitted ray tracer (STOP_ON_DIFFUSE_BOUNCE)
+//   photonmapper/photondistribution.comp,
+//   photonmapper/gather.comp, maps/grid.glsl   photon mapper (lossless hash grid)
 // Two documented additions that the reference lacks: a constant sky radiance
 // returned on a miss (the reference samples a cube map, black by default) and
 // directional light samples (normalThetaCos == 3) for a sun.
 #include <atomic>
+#include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <unordered_map>
 #include <vector>
 
 #include "oracle.hpp"
@@ -436,6 +441,160 @@ static vec3 WhittedPixel(const RenderScene& s, const Params& P, int x, int y) {
     return color;
 }
 
+// --------------------------------------------------------- photonmapper/*
+// PackNormal32 / UnpackNormal(uint) (helper.glsl:67-76): packSnorm2x16 of
+// (phi / pi, z), rounded to nearest even.
+static uint PackNormal32(vec3 n) {
+    float px = n.x == 0.0f ? sign(n.y) / 2.0f : std::atan2(n.y, n.x) / PI;
+    auto q = [](float v) { return (uint)(uint16_t)(int16_t)std::nearbyint(clamp(v, -1.0f, 1.0f) * 32767.0f); };
+    return q(px) | (q(n.z) << 16);
+}
+static vec3 UnpackNormal32(uint p) {
+    auto u = [](uint bits) { return clamp((float)(int16_t)(uint16_t)bits / 32767.0f, -1.0f, 1.0f); };
+    vec2 v(u(p & 0xFFFFu), u(p >> 16));
+    v.x *= PI;
+    return UnpackNormal(v);
+}
+struct Photon {
+    vec3 flux, pos;
+    uint dir;
+};
+// worldPosToGrid (maps/grid.glsl): ceil(pos / HashGridSpacing)
+struct CellKey {
+    int x, y, z;
+    bool operator==(const CellKey& o) const { return x == o.x && y == o.y && z == o.z; }
+};
+struct CellHash {
+    size_t operator()(const CellKey& k) const {
+        return (size_t)(uint32_t)k.x * 73856093u ^ (size_t)(uint32_t)k.y * 19349663u ^ (size_t)(uint32_t)k.z * 83492791u;
+    }
+};
+// The reference's lossless hash map keeps a linked list per cell; a gather
+// sums over every photon of the queried cells, so a map from cell to photon
+// list gives the same sets (aliased cells are far outside the query radius).
+struct PhotonGrid {
+    float spacing = 0.0f, radiusSq = 0.0f;
+    std::unordered_map<CellKey, std::vector<uint32_t>, CellHash> cells;
+    std::vector<Photon> photons;
+};
+
+// photondistribution.comp:10-106, one photon path.
+static void PhotonThread(const RenderScene& s, const Params& P, uint gid, int photonsPerSample,
+                         std::vector<Photon>& out) {
+    uint seed = InitRandomSeed(P.frameSeed, gid);
+    int lightSampleIndex = int(gid / (uint)photonsPerSample);
+    vec4 pn0 = P.lightSamples[2 * lightSampleIndex];
+    vec4 in1 = P.lightSamples[2 * lightSampleIndex + 1];
+    vec3 pathThroughput = in1.xyz() * (PI / (float)photonsPerSample);
+    Ray ray;
+    ray.Origin = pn0.xyz();
+    if (in1.w > 1.0f) {
+        ray.Direction = SampleDirection(Random2(seed));
+        pathThroughput *= 4.0f;
+    } else {
+        vec3 normal = UnpackNormal(vec2(pn0.w, in1.w));
+        vec3 U, V;
+        CreateONB(normal, U, V);
+        ray.Direction = SampleHemisphereCosine(Random2(seed), U, V, normal);
+    }
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        if (rayHit == RAY_MAX) break;
+        vec3 geometryNormal = hit.normal;
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 shadingNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, shadingNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        vec3 throughput(1.0f);
+        float samplePDF;
+        bool diffuse = false;
+        vec3 newDirection = SampleBSDFImpl(ray.Direction, m, seed, shadingNormal, throughput, true, samplePDF, &diffuse);
+        if (diffuse) out.push_back(Photon{pathThroughput, ray.Origin, PackNormal32(ray.Direction)});
+        throughput *= AdjointBSDFShadingNormalCorrection(ray.Direction, newDirection, geometryNormal, shadingNormal);
+        pathThroughput *= throughput;
+        if (i >= P.rrStartDepth) {  // RUSSIAN_ROULETTE with the photon mapper's +0.02
+            float p = saturate(GetLuminance(throughput) + 0.02f);
+            if (Random(seed) >= p) break;
+            pathThroughput /= p;
+        }
+        ray.Direction = newDirection;
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+    }
+}
+
+// gather.comp:11-36
+static vec3 IrradianceEstimate(const Photon& ph, const Ray& ray, const MaterialData& m, vec3 shadingNormal,
+                               float radiusSq) {
+    vec3 toPhoton = ph.pos - ray.Origin;
+    float rsq = dot(toPhoton, toPhoton);
+    if (rsq <= radiusSq && abs(dot(toPhoton, shadingNormal)) < 0.01f) {
+        vec3 photonDir = UnpackNormal32(ph.dir);
+        if (dot(ray.Direction, shadingNormal) * dot(photonDir, shadingNormal) < 0.0f) return vec3(0.0f);
+        float cosAbs = abs(dot(ray.Direction, shadingNormal));
+        vec3 fr = GetDiffuseProbability(m, cosAbs) * m.Diffuse / PI;
+        float kernel = 1.0f / (PI * radiusSq);
+        fr /= Avg(GetDiffuseProbability(m, cosAbs));
+        return fr * ph.flux * (1.0f * kernel);
+    }
+    return vec3(0.0f);
+}
+
+// gather.comp:38-133, one pixel: eye path to the first diffuse decision,
+// then the photons of the 2x2x2 cells from round(pos / spacing).
+static vec3 GatherPixel(const RenderScene& s, const Params& P, const PhotonGrid& grid, int x, int y) {
+    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    vec2 screen = (Random2(seed) + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
+    Ray ray;
+    ray.Origin = P.camPos;
+    ray.Direction = normalize(screen.x * P.camU + screen.y * P.camV + P.camW);
+    vec3 color(0.0f), pathThroughput(1.0f);
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        if (rayHit == RAY_MAX) {
+            color += pathThroughput * P.sky;  // addition: the reference adds nothing (its cube map lookup is commented out)
+            break;
+        }
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 hitNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        color += pathThroughput * m.Emissivity;
+        vec3 throughput(1.0f);
+        float pdf;
+        bool diffuse = false;
+        vec3 newDirection = SampleBSDFImpl(ray.Direction, m, seed, hitNormal, throughput, false, pdf, &diffuse);
+        if (diffuse) {
+            vec3 irradiance(0.0f);
+            const int bx = (int)std::nearbyint(ray.Origin.x / grid.spacing);
+            const int by = (int)std::nearbyint(ray.Origin.y / grid.spacing);
+            const int bz = (int)std::nearbyint(ray.Origin.z / grid.spacing);
+            for (int c = 0; c < 8; ++c) {
+                auto it = grid.cells.find(CellKey{bx + (c & 1), by + ((c >> 1) & 1), bz + ((c >> 2) & 1)});
+                if (it == grid.cells.end()) continue;
+                for (uint32_t k : it->second)
+                    irradiance += IrradianceEstimate(grid.photons[k], ray, m, hitNormal, grid.radiusSq);
+            }
+            color += irradiance * pathThroughput;
+            break;
+        }
+        ray.Direction = newDirection;
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+        pathThroughput *= throughput;
+        if (i >= P.rrStartDepth) {
+            float p = saturate(GetLuminance(throughput) + 0.02f);
+            if (Random(seed) >= p) break;
+            pathThroughput /= p;
+        }
+    }
+    return color;
+}
+
 // ------------------------------------------------------------ lightcache.glsl
 struct LightCacheEntry {
     vec3 Flux;
@@ -709,6 +868,80 @@ static vec3 BidirPixel(const RenderScene& s, const Params& P, const LightCache& 
 using namespace oracle;
 
 extern "C" {
+
+// Photon mapper iteration (PhotonMapper::Draw, gpugi/renderer/photonmapper.cpp:
+// 79-114): photonsPerLightSample photons per light sample build the grid
+// (spacing 2.01 x queryRadius), then the gather pass; rgba as oracle_render.
+int oracle_render_pm(const float* hierarchy, uint32_t numNodes, uint32_t boundsKind, const int32_t* slots,
+                     uint32_t numSlots, uint32_t leafSize, const float* positions, const float* vertexInfo,
+                     uint32_t numVertices, const float* materials, uint32_t numMaterials, int width, int height,
+                     int maxPathLength, int rrStartDepth, const float* cam, uint32_t frameSeed,
+                     const float* lightSamples, int numLightSamples, const float* sky, int photonsPerLightSample,
+                     float queryRadius, float* rgba, int numThreads) {
+    RenderScene s;
+    s.geo.hierarchy = reinterpret_cast<const vec4*>(hierarchy);
+    s.geo.numNodes = numNodes;
+    s.geo.boundsKind = boundsKind;
+    s.geo.triangles = reinterpret_cast<const ivec4*>(slots);
+    s.geo.numSlots = numSlots;
+    s.geo.leafSize = leafSize;
+    s.geo.positions = positions;
+    s.geo.numVertices = numVertices;
+    s.geo.vertexInfo = reinterpret_cast<const vec4*>(vertexInfo);
+    s.materials = materials;
+    s.numMaterials = numMaterials;
+    Params P;
+    P.width = width;
+    P.height = height;
+    P.maxPathLength = maxPathLength;
+    P.rrStartDepth = rrStartDepth;
+    P.camU = vec3(cam[0], cam[1], cam[2]);
+    P.camV = vec3(cam[3], cam[4], cam[5]);
+    P.camW = vec3(cam[6], cam[7], cam[8]);
+    P.camPos = vec3(cam[9], cam[10], cam[11]);
+    P.pixelArea = cam[12];
+    P.frameSeed = frameSeed;
+    P.numLightSamples = numLightSamples;
+    P.lightSamples = reinterpret_cast<const vec4*>(lightSamples);
+    P.sky = sky ? vec3(sky[0], sky[1], sky[2]) : vec3(0.0f);
+    P.numRaysPerLightSample = 0;
+    if (photonsPerLightSample <= 0 || !(queryRadius > 0.0f)) return -1;
+    const uint64_t nPhotons = (uint64_t)numLightSamples * (uint64_t)photonsPerLightSample;
+    // photons traced in parallel, stored in photon order
+    const int nt = numThreads > 0 ? numThreads : (int)std::max(1u, std::thread::hardware_concurrency());
+    std::vector<std::vector<Photon>> parts(nt);
+    const uint64_t per = (nPhotons + nt - 1) / nt;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&, t]() {
+            for (uint64_t g = t * per; g < std::min<uint64_t>(nPhotons, (t + 1) * per); ++g)
+                PhotonThread(s, P, (uint)g, photonsPerLightSample, parts[t]);
+        });
+    for (auto& th : pool) th.join();
+    PhotonGrid grid;
+    grid.spacing = queryRadius * 2.01f;
+    grid.radiusSq = queryRadius * queryRadius;
+    for (auto& part : parts)
+        for (const Photon& ph : part) {
+            const uint32_t k = (uint32_t)grid.photons.size();
+            grid.photons.push_back(ph);
+            CellKey key{(int)std::ceil(ph.pos.x / grid.spacing), (int)std::ceil(ph.pos.y / grid.spacing),
+                        (int)std::ceil(ph.pos.z / grid.spacing)};
+            grid.cells[key].push_back(k);
+        }
+    ParallelFor((uint64_t)width * height, numThreads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t p = b; p < e; ++p) {
+            int x = (int)(p % width), y = (int)(p / width);
+            vec3 c = GatherPixel(s, P, grid, x, y);
+            float* o = rgba + 4 * p;
+            o[0] += c.x;
+            o[1] += c.y;
+            o[2] += c.z;
+            o[3] += 1.0f;
+        }
+    });
+    return 0;
+}
 
 // One iteration of a pass, accumulated into rgba (w*h*4 floats).
 //   pass: 0 = PT, 1 = LT, 2 = BPT, 3 = Whitted

@@ -52,7 +52,8 @@ CAM = [0.0, 1.0, 3.4, 0.0, 1.0, 0.0, 40.0]
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("renderer,pass_", [("Pathtracer", "PT"), ("BidirectionalPathtracer", "BPT"),
-                                            ("LightPathtracer", "LT"), ("WhittedRayTracer", "WHITTED")])
+                                            ("LightPathtracer", "LT"), ("WhittedRayTracer", "WHITTED"),
+                                            ("PhotonMapper", "PM")])
 def test_headless_matches_the_c_abi(cuda_ctx, room_file, tmp_path, renderer, pass_):
     sc, path = room_file
     W = H = 32

@@ -228,3 +228,46 @@ def test_whitted_matches_oracle_per_pixel(cuda_ctx, glossy_room):
     assert cuda_ctx.device_error_bits() == 0
     for x in (img, img2):
         x.close()
+
+
+def test_photon_mapper_matches_oracle_per_pixel(cuda_ctx, glossy_room):
+    """PhotonMapper (photondistribution.comp + gather.comp) at its defaults,
+    2048 photons per light sample and query radius 0.01: the GPU and the
+    oracle trace the same photons (same seeds, bit-identical walks) into the
+    same grid cells; a gather sums a handful of photons, so a pixel differs
+    when rounding diverts one of them."""
+    sc, b, ds = glossy_room
+    W = H = 48
+    iters = 4
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    ls = _light_sets(ds, iters, 128)
+    render.set_photon_config(cuda_ctx, 2048, 0.01)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, img, "PM", max_path_length=6, samples=iters, iteration=0, light_samples=ls)
+    g = img.read()
+    o = _oracle(b, sc, "PM", W, H, cam, ls, iters, max_path_length=6)
+    assert np.all(g[..., 3] == iters) and np.all(o[..., 3] == iters)
+    close = np.abs(g[..., :3] - o[..., :3]) <= 1e-3 * np.abs(o[..., :3]).max() + 1e-5
+    assert close.all(-1).mean() > 0.9, close.all(-1).mean()
+    assert abs(g[..., :3].mean() / o[..., :3].mean() - 1) < 0.02, (g[..., :3].mean(), o[..., :3].mean())
+    assert cuda_ctx.device_error_bits() == 0
+    img.close()
+
+
+def test_photon_mapper_converges_to_path_tracing(cuda_ctx, room):
+    """On the diffuse room the photon-map estimate (radius 0.02, 4096 photons
+    per light sample) approaches the path-traced image: a density estimate
+    biased by its kernel, so image means agree to a few percent."""
+    sc, b, ds = room
+    W = H = 32
+    cam = render.camera_lookat((0.0, 1.2, 2.0), (0.0, 0.0, -0.3), (0.0, 1.0, 0.0), 40.0, W, H)
+    render.set_photon_config(cuda_ctx, 4096, 0.02)
+    pm = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, pm, "PM", max_path_length=8, samples=32, rng_state=[3])
+    pt = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, pt, "PT", max_path_length=8, samples=256, rng_state=[4])
+    a, r = pm.read()[..., :3].mean() / 32, pt.read()[..., :3].mean() / 256
+    assert abs(a / r - 1) < 0.08, (a, r)
+    render.set_photon_config(cuda_ctx)
+    for x in (pm, pt):
+        x.close()

@@ -134,3 +134,32 @@ def test_estimators_agree_on_diffuse_room(built):
         means[p] = acc[..., :3].mean() / iters
     assert abs(means["BPT"] / means["PT"] - 1) < 0.05, means
     assert abs(means["LT"] / means["PT"] - 1) < 0.06, means
+
+
+def test_photon_map_point_light_on_lambert_floor(built):
+    """Photon mapping on the floor under a point light: the density
+    estimate over the query disc (radius 0.05 here) converges to the same
+    irradiance as NEE, up to the kernel's blur of the smooth falloff."""
+    albedo, I, h = 0.6, 5.0, 1.5
+    sc = _quad_scene(albedo=albedo)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"])
+    W = H = 16
+    cam = render.camera_lookat((0.0, 3.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, -1.0), 30.0, W, H)
+    ls = _point_light_samples((0.0, h, 0.0), (I, I, I), n=16)
+    acc = None
+    iters = 24
+    for it in range(iters):
+        acc = oracle.render(b, sc, "PM", W, H, cam.as_array(), render.wanghash(it), ls, max_path_length=1,
+                            accum=acc, photons_per_light_sample=1 << 14, query_radius=0.05)
+    assert np.all(acc[..., 3] == iters)
+    img = acc[..., 0] / iters
+    c = cam.as_array()
+    U, V, Wd, P = c[0:3], c[3:6], c[6:9], c[9:12]
+    ys, xs = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    d = ((xs + 0.5) / W * 2 - 1)[..., None] * U + ((ys + 0.5) / H * 2 - 1)[..., None] * V + Wd
+    p = P + (-P[1] / d[..., 1])[..., None] * d
+    r2 = p[..., 0] ** 2 + (h - p[..., 1]) ** 2 + p[..., 2] ** 2 + 1e-5
+    expected = albedo / math.pi * I * (h / np.sqrt(r2)) / r2
+    rel = np.abs(img - expected) / expected
+    assert np.median(rel) < 0.05, np.median(rel)
+    assert abs(img.mean() / expected.mean() - 1) < 0.03
