@@ -306,7 +306,9 @@ def run_passes(args):
     """Per-pass throughput of the wavefront renderers on the Cornell workload:
     room of ~98k triangles (5 walls, 2 rotated boxes, level-6 sphere, 0.5 x
     0.5 ceiling light of radiance 10, albedos U[0.1, 0.9]), 512 x 512, 16 spp,
-    depth 8, Russian roulette after depth 3. For PT, LT and BPT: samples/s
+    depth 8, Russian roulette after depth 3. For PT, LT, BPT, the Whitted ray
+    tracer and the photon mapper (2048 photons per light sample, radius
+    0.01, one photon map per iteration): samples/s
     (iterations x pixels per second) and Mrays/s (closest-hit + any-hit rays
     traced, counted on the device), CUDA events around 16 spp after one
     warm-up iteration. Beside each, the CPU restatement of the same pass on all
@@ -323,7 +325,7 @@ def run_passes(args):
     cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
     stream = torch.cuda.ExternalStream(ctx.stream)
     out = {}
-    for pass_ in ("PT", "LT", "BPT"):
+    for pass_ in ("PT", "LT", "BPT", "WHITTED", "PM"):
         img = render.Image(ctx, W, H)
         render.render(ctx, ds, cam, img, pass_, max_path_length=depth, samples=1, rr_start_depth=rr, rng_state=[1])
         ctx.sync()
