@@ -62,6 +62,21 @@ static gpugi_status check_device_error(gpugi_ctx* ctx) {
     return GPUGI_OK;
 }
 
+// The error word as copied into ctx->errHost by a call's last copies (the
+// caller has synchronised them): no extra round trip.
+static gpugi_status check_copied_device_error(gpugi_ctx* ctx) {
+    const uint32_t bits = *ctx->errHost;
+    if (bits) {
+        *ctx->errHost = 0;
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(ctx->errWord, 0, 4, ctx->stream));
+        GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        char msg[96];
+        std::snprintf(msg, sizeof msg, "device guard fired (error bits 0x%x)", bits);
+        return fail(ctx, GPUGI_ERROR_DEVICE, msg);
+    }
+    return GPUGI_OK;
+}
+
 static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 static gpugi_status ensure_pipeline(gpugi_ctx* ctx) {
@@ -116,6 +131,7 @@ static gpugi_status trace_host(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHi
                                                             static_cast<float*>(dout[1]), static_cast<float*>(dout[2]),
                                                             static_cast<float*>(dout[3]));
             if (st) return st;
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->errHost, ctx->errWord, 4, cudaMemcpyDeviceToHost, ctx->stream));
             GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
             return GPUGI_OK;
         }
@@ -153,6 +169,8 @@ static gpugi_status trace_host(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHi
                 GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(u + off, dU, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
                 GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(v + off, dV, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
             }
+            if (off + m >= n)  // the error word after the call's last traversal
+                GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->errHost, ctx->errWord, 4, cudaMemcpyDeviceToHost, ctx->stream));
             continue;
         }
         // parts of whole float4 groups, so every part starts 16-B aligned
@@ -199,7 +217,10 @@ static gpugi_status trace_host(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHi
                 GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(v + off + p0, dV + p0, mp * 4, cudaMemcpyDeviceToHost, ctx->copyOut));
             }
         }
-        // the next chunk reuses the staging columns
+        // the next chunk reuses the staging columns; the last chunk also
+        // brings back the error word (copyOut has waited for every traversal)
+        if (off + m >= n)
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->errHost, ctx->errWord, 4, cudaMemcpyDeviceToHost, ctx->copyOut));
         GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->copyOut));
     }
     GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -232,8 +253,10 @@ gpugi_status gpugi_create(gpugi_ctx** out, const gpugi_opts* opts) {
     }
     if ((e = cudaSetDevice(ctx->device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaMalloc(&ctx->errWord, 16)) != cudaSuccess || (e = cudaMemset(ctx->errWord, 0, 16)) != cudaSuccess ||
-        (e = cudaMalloc(&ctx->scratch, 256)) != cudaSuccess || (e = cudaMemset(ctx->scratch, 0, 256)) != cudaSuccess) {
+        (e = cudaMalloc(&ctx->scratch, 256)) != cudaSuccess || (e = cudaMemset(ctx->scratch, 0, 256)) != cudaSuccess ||
+        (e = cudaMallocHost(&ctx->errHost, 4)) != cudaSuccess) {
         if (ctx->errWord) cudaFree(ctx->errWord);
+        if (ctx->scratch) cudaFree(ctx->scratch);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return GPUGI_ERROR_CUDA;
@@ -250,6 +273,7 @@ void gpugi_destroy(gpugi_ctx* ctx) {
     if (ctx->renderFree) ctx->renderFree(ctx);
     if (ctx->stageDev) cudaFree(ctx->stageDev);
     if (ctx->errWord) cudaFree(ctx->errWord);
+    if (ctx->errHost) cudaFreeHost(ctx->errHost);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->queue) cudaFree(ctx->queue);
     if (ctx->copyIn) {
@@ -277,6 +301,16 @@ gpugi_status gpugi_sync(gpugi_ctx* ctx) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return check_device_error(ctx);
+}
+
+gpugi_status gpugi_debug_raise_device_error(gpugi_ctx* ctx, uint32_t bits) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t cur = 0;
+    GPUGI_CUDA_TRY(ctx, cudaMemcpy(&cur, ctx->errWord, 4, cudaMemcpyDeviceToHost));
+    cur |= bits;
+    GPUGI_CUDA_TRY(ctx, cudaMemcpy(ctx->errWord, &cur, 4, cudaMemcpyHostToDevice));
+    return GPUGI_OK;
 }
 
 gpugi_status gpugi_device_error_bits(gpugi_ctx* ctx, uint32_t* bits) {
@@ -366,7 +400,7 @@ gpugi_status gpugi_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const fl
     const float* const src[7] = {ox, oy, oz, dx, dy, dz, tmax};
     gpugi_status st = trace_host(ctx, sc, false, src, n, slot, t, u, v, nullptr);
     if (st) return st;
-    return check_device_error(ctx);
+    return check_copied_device_error(ctx);
 }
 
 gpugi_status gpugi_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
@@ -379,7 +413,7 @@ gpugi_status gpugi_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float*
     const float* const src[7] = {ox, oy, oz, dx, dy, dz, tmax};
     gpugi_status st = trace_host(ctx, sc, true, src, n, nullptr, nullptr, nullptr, nullptr, occluded);
     if (st) return st;
-    return check_device_error(ctx);
+    return check_copied_device_error(ctx);
 }
 
 }  // extern "C"

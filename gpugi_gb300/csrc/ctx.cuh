@@ -4,6 +4,7 @@
 
 #include <cstddef>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/gpugi_cuda.h"
@@ -13,6 +14,9 @@ struct gpugi_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     uint32_t* errWord = nullptr;  // device error word (GPUGI_DEVERR_*)
+    uint32_t* errHost = nullptr;  // page-locked copy of it, read back with a call's last copies
+    // occupancy of the walker kernels (kernel, dynamic shared bytes) -> blocks per SM
+    std::vector<std::pair<std::pair<const void*, size_t>, int>> occupancy;
     std::string lastError;
     // staging for the host-pointer entry points (grown on demand)
     void* stageDev = nullptr;

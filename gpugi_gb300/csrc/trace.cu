@@ -47,8 +47,13 @@ gpugi_status walker_launch_config(gpugi_ctx* ctx, const gpugi_scene* sc, const v
     out.smem = (size_t)out.stage * 32;
     if (out.smem > 48 * 1024)
         GPUGI_CUDA_TRY(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)out.smem));
-    int perSM = 0;
-    GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, out.smem));
+    int perSM = -1;
+    for (const auto& e : ctx->occupancy)
+        if (e.first.first == kernel && e.first.second == out.smem) perSM = e.second;
+    if (perSM < 0) {
+        GPUGI_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, out.smem));
+        ctx->occupancy.push_back({{kernel, out.smem}, perSM});
+    }
     uint64_t grid = (uint64_t)ctx->numSMs * (uint64_t)(perSM > 0 ? perSM : 1);
     const uint64_t needed = (n + 127) / 128;
     if (grid > needed) grid = needed;

@@ -51,6 +51,7 @@ def _declare(L):
     L.gpugi_scene_upload.argtypes = [P, P, U32, U32, P, U32, U32, P, P, U32, P, U32, C.POINTER(P)]
     L.gpugi_scene_destroy.argtypes = [P]
     L.gpugi_scene_destroy.restype = None
+    L.gpugi_debug_raise_device_error.argtypes = [P, U32]
     L.gpugi_scene_build.argtypes = [P, P, U32, P, U32, P, P, U32, U32, C.POINTER(P)]
     L.gpugi_scene_export.argtypes = [P, P, C.POINTER(U32), C.POINTER(U32), P, P]
     for name in ("gpugi_trace_closest", "gpugi_trace_closest_device"):
@@ -122,6 +123,10 @@ class Context:
 
     def sync(self):
         self.check(lib().gpugi_sync(self._h))
+
+    def debug_raise_device_error(self, bits: int) -> None:
+        """Test support: set device error bits as a device guard would."""
+        self.check(lib().gpugi_debug_raise_device_error(self._h, bits))
 
     def device_error_bits(self) -> int:
         b = C.c_uint32()

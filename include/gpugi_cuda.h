@@ -79,6 +79,9 @@ const char* gpugi_last_error(const gpugi_ctx* ctx);
 gpugi_status gpugi_sync(gpugi_ctx* ctx);
 /* Read and clear the device error word (synchronises). */
 gpugi_status gpugi_device_error_bits(gpugi_ctx* ctx, uint32_t* bits);
+/* Test support: set bits in the device error word, as a device guard would,
+ * so that the reporting of the next synchronising call can be tested. */
+gpugi_status gpugi_debug_raise_device_error(gpugi_ctx* ctx, uint32_t bits);
 /* The cudaStream_t the context enqueues on (returned as void*). */
 void* gpugi_stream(gpugi_ctx* ctx);
 /* Library version string. */

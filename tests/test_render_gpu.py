@@ -271,3 +271,20 @@ def test_photon_mapper_converges_to_path_tracing(cuda_ctx, room):
     render.set_photon_config(cuda_ctx)
     for x in (pm, pt):
         x.close()
+
+
+def test_photon_config_validation_and_progressive_radius(cuda_ctx, room):
+    sc, b, ds = room
+    for bad in ((0, 0.01), (1 << 21, 0.01), (2048, 0.0), (2048, float("nan"))):
+        with pytest.raises(cuda.GpugiError):
+            render.set_photon_config(cuda_ctx, *bad)
+    W = H = 24
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    render.set_photon_config(cuda_ctx, 512, 0.05, progressive=True)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, img, "PM", max_path_length=4, samples=6, iteration=3, rng_state=[1])
+    g = img.read()
+    assert np.all(g[..., 3] == 6) and np.isfinite(g).all() and g[..., :3].mean() > 0
+    assert cuda_ctx.device_error_bits() == 0
+    render.set_photon_config(cuda_ctx)
+    img.close()

@@ -273,3 +273,39 @@ def test_host_paths_give_identical_results(cuda_ctx, icosphere_65536, parts, pin
     finally:
         cuda_ctx.set_host_pipeline(2)
         ds.close()
+
+
+@pytest.mark.parametrize("parts,zero_copy", [(1, False), (2, False), (1, True)])
+def test_device_guard_bits_reach_the_caller(cuda_ctx, icosphere_65536, parts, zero_copy):
+    """A guard bit set on the device (here by the test-support call, as a
+    guard would) fails the next host-pointer query with GPUGI_ERROR_DEVICE
+    once, whatever path the query takes, and is cleared for the next call."""
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    n = 1 << 17
+    rays = scenes.random_rays(n, seed=21)
+    # page-locked inputs and outputs, so zero copy applies when enabled
+    r = {k: torch.from_numpy(np.ascontiguousarray(rays[k], dtype=np.float32)).pin_memory().numpy()
+         for k in cuda.RAY_KEYS}
+    out = dict(slot=torch.empty(n, dtype=torch.int32).pin_memory().numpy(), t=torch.empty(n).pin_memory().numpy(),
+               u=torch.empty(n).pin_memory().numpy(), v=torch.empty(n).pin_memory().numpy())
+
+    def query():
+        cuda_ctx.check(cuda.lib().gpugi_trace_closest(cuda_ctx.handle, ds.handle,
+                                                      *[cuda._ptr(r[k]) for k in cuda.RAY_KEYS], n,
+                                                      *[cuda._ptr(out[k]) for k in ("slot", "t", "u", "v")]))
+
+    cuda_ctx.set_host_pipeline(parts, zero_copy)
+    try:
+        cuda_ctx.debug_raise_device_error(0x2)
+        with pytest.raises(cuda.GpugiError) as e:
+            query()
+        assert e.value.status == 5 and "0x2" in str(e.value)
+        query()  # the bits were cleared
+        _compare_closest(out, oracle.trace_closest(b, sc["positions"], rays))
+        assert cuda_ctx.device_error_bits() == 0
+    finally:
+        cuda_ctx.set_host_pipeline(2, False)
+    ds.close()
