@@ -1588,11 +1588,13 @@ static gpugi_status walkers_config(gpugi_ctx* ctx, const gpugi_scene* sc, Walker
     const void* ks = W.ell ? (const void*)k_shadow<1> : (const void*)k_shadow<0>;
     gpugi_status st = walker_launch_config(ctx, sc, ke, 1ull << 40, ctx->renderSharedNodes, W.LE);
     if (!st) st = walker_launch_config(ctx, sc, ks, 1ull << 40, ctx->renderSharedNodes, W.LS);
-    // group walks while fewer rays than half the resident lanes are queued
-    // (trace modes 3-5; the lane walk otherwise)
+    // group walks while fewer rays than twice the resident lanes are queued
+    // (trace modes 3-5; the lane walk otherwise; measured on the passes
+    // workload: 0.5x, 2x, 8x, 64x the lanes gave PT 262 / 264.5 / 250 / 167 M
+    // samples/s and the photon mapper 124 / 133 / 133 / 133)
     const bool group = ctx->traceMode >= 3;
-    W.groupBelowE = group ? W.LE.grid * 128u / 2u : 0u;
-    W.groupBelowS = group ? W.LS.grid * 128u / 2u : 0u;
+    W.groupBelowE = group ? W.LE.grid * 128u * 2u : 0u;
+    W.groupBelowS = group ? W.LS.grid * 128u * 2u : 0u;
     return st;
 }
 
