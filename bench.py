@@ -505,10 +505,11 @@ def run_batch(args):
     """Batched rendering workload: 8 scenes of instanced icospheres, boxes and
     tori (triangle counts log-uniform in [10k, 2M]), each with a random
     resolution in {256^2, 512^2, 768^2, 1024^2} and spp in {4, 16, 64}, PT,
-    LT and BPT at depth 8 (24 jobs). One gpugi_render_batch call (PT jobs in
-    one wavefront replayed as a CUDA graph per round; LT and BPT jobs one
-    after another) against the same jobs as 24 gpugi_render calls. Wall time
-    of synchronised calls; samples = pixels x spp summed over jobs."""
+    LT and BPT at depth 8 (24 jobs). One gpugi_render_batch call (all 24 jobs
+    in one two-phase wavefront replayed as a CUDA graph per round) against
+    the same jobs as 24 gpugi_render calls; also each pass's 8 jobs alone,
+    and 64 small mixed jobs. Wall time of synchronised calls; samples =
+    pixels x spp summed over jobs."""
     from gpugi_gb300 import bvh, cuda, render, scenes
     rs = scenes.Stream(args.batch_seed, 23)
     ctx = cuda.Context(0)
@@ -526,10 +527,10 @@ def run_batch(args):
         cam = render.camera_lookat((0.0, 1.0, 7.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 45.0, r, r)
         specs.append((ds, cam, r, spp, sc["triangles"].shape[0]))
 
-    def make_jobs():
+    def make_jobs(passes=("PT", "LT", "BPT")):
         jobs = []
         for k, (ds, cam, r, spp, _) in enumerate(specs):
-            for pass_ in ("PT", "LT", "BPT"):
+            for pass_ in passes:
                 jobs.append(dict(scene=ds, camera=cam, image=render.Image(ctx, r, r), pass_=pass_, samples=spp,
                                  max_path_length=8, rng_state=[1000 + k]))
         return jobs
@@ -543,49 +544,45 @@ def run_batch(args):
 
     def run_single(jobs):
         for j in jobs:
-            render.render(ctx, j["scene"], j["camera"], j["image"], j["pass_"], max_path_length=8,
+            render.render(ctx, j["scene"], j["camera"], j["image"], j["pass_"], max_path_length=j["max_path_length"],
                           samples=j["samples"], rng_state=j["rng_state"])
 
-    def samples(jobs, passes):
-        return sum(j["image"].width * j["image"].height * j["samples"] for j in jobs if j["pass_"] in passes)
+    def samples(jobs):
+        return sum(j["image"].width * j["image"].height * j["samples"] for j in jobs)
 
-    result = {}
-    for name, fn in (("batch", lambda js: render.render_batch(ctx, js)), ("single", run_single)):
-        warm = make_jobs()
+    def measure(fn, make):
+        warm = make()
         fn(warm)  # buffers, graph capture
         for j in warm:
             j["image"].close()
-        jobs = make_jobs()
-        pt_jobs = [j for j in jobs if j["pass_"] == "PT"]
-        t_pt = timed(lambda: fn(pt_jobs))
-        other = [j for j in jobs if j["pass_"] != "PT"]
-        t_other = timed(lambda: fn(other))
-        result[name] = {"pt_s": round(t_pt, 4), "pt_samples_per_s": samples(jobs, ("PT",)) / t_pt,
-                        "lt_bpt_s": round(t_other, 4), "all_samples_per_s": samples(jobs, ("PT", "LT", "BPT")) /
-                        (t_pt + t_other)}
+        jobs = make()
+        t = timed(lambda: fn(jobs))
         for j in jobs:
             j["image"].close()
-    # many small jobs: 64 PT jobs of 128 x 128 at 4 spp over the same 8 scenes
+        return t, samples(jobs)
+
+    result = {}
+    for name, fn in (("batch", lambda js: render.render_batch(ctx, js)), ("single", run_single)):
+        t, n = measure(fn, make_jobs)
+        result[name] = {"all_s": round(t, 4), "all_samples_per_s": n / t}
+        for pass_ in ("PT", "LT", "BPT"):
+            t, n = measure(fn, lambda: make_jobs((pass_,)))
+            result[name][pass_ + "_s"] = round(t, 4)
+            result[name][pass_ + "_samples_per_s"] = n / t
+    # many small jobs: 64 jobs of 128 x 128 at 4 spp over the same 8 scenes, PT / LT / BPT in turn
     def small_jobs():
         return [dict(scene=specs[k % 8][0], camera=render.camera_lookat((0.0, 1.0, 7.0), (0.0, 0.0, 0.0),
                                                                         (0.0, 1.0, 0.0), 45.0, 128, 128),
-                     image=render.Image(ctx, 128, 128), pass_="PT", samples=4, max_path_length=8,
-                     rng_state=[2000 + k]) for k in range(64)]
+                     image=render.Image(ctx, 128, 128), pass_=("PT", "LT", "BPT")[k % 3], samples=4,
+                     max_path_length=8, rng_state=[2000 + k]) for k in range(64)]
     small = {}
     for name, fn in (("batch", lambda js: render.render_batch(ctx, js)), ("single", run_single)):
-        warm = small_jobs()
-        fn(warm)
-        for j in warm:
-            j["image"].close()
-        jobs = small_jobs()
-        t = timed(lambda: fn(jobs))
-        small[name] = {"s": round(t, 5), "samples_per_s": 64 * 128 * 128 * 4 / t}
-        for j in jobs:
-            j["image"].close()
-    result["small_jobs_64x128x128x4spp"] = small
+        t, n = measure(fn, small_jobs)
+        small[name] = {"s": round(t, 5), "samples_per_s": n / t}
+    result["small_jobs_64x128x128x4spp_mixed"] = small
     line = {"metric": "samples/s, 24 jobs of 8 scenes: batched vs one call per job",
             "value": result["batch"]["all_samples_per_s"], "unit": "samples/s", "higher_is_better": True,
-            "pt_speedup_batched": result["single"]["pt_s"] / result["batch"]["pt_s"],
+            "speedup_batched": result["single"]["all_s"] / result["batch"]["all_s"],
             "small_jobs_speedup_batched": small["single"]["s"] / small["batch"]["s"], "runs": result,
             "config": {"workload": "8 instanced scenes, tris log-uniform [10k, 2M], res {256..1024}^2, "
                                    "spp {4,16,64}, PT+LT+BPT depth 8",

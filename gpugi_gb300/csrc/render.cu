@@ -82,6 +82,7 @@ struct RenderConst {
     int width, height, numPixels;
     int maxPathLength, rrStartDepth;
     uint32_t iteration, samples, sampleBase;  // sample s of this chunk = iteration sampleBase + s
+    uint32_t pass;               // gpugi_pass (the batched wavefront shades each path by its job's pass)
     uint32_t numLightSamples;
     const float4* lightSamples;  // [samples][numLightSamples][2]
     float3 sky;
@@ -276,17 +277,23 @@ GPUGI_D float3 primary_direction(const RenderConst& rc, uint32_t& seed, int x, i
 
 // pathtracer.comp:16-46 / pathtracer_bidir.comp:16-24: one camera path per
 // pixel and iteration. BPT also counts the iteration in the alpha channel.
+// The eye path of pixel pix in sample s at queue slot p (pathtracer.comp:37-46,
+// pathtracer_bidir.comp:36-52; the bidirectional tracer counts the sample in
+// alpha).
+GPUGI_D void camera_path_start(const RenderConst& rc, const PathSoA& A, uint32_t p, uint32_t s, uint32_t pix,
+                               bool bidir) {
+    const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
+    uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + pix);
+    const float3 d = primary_direction(rc, seed, x, y);
+    store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, s << 8, 1.0f);
+    if (bidir) splat(rc, pix, f3(0.0f), 1.0f);
+}
+
 __global__ void k_camera_generate(RenderConst rc, PathSoA A, bool bidir) {
     const uint32_t total = rc.samples * (uint32_t)rc.numPixels;
     if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
-        const uint32_t s = p / (uint32_t)rc.numPixels, pix = p % (uint32_t)rc.numPixels;
-        const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + pix);
-        const float3 d = primary_direction(rc, seed, x, y);
-        store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, s << 8, 1.0f);
-        if (bidir) splat(rc, pix, f3(0.0f), 1.0f);
-    }
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x)
+        camera_path_start(rc, A, p, p / (uint32_t)rc.numPixels, p % (uint32_t)rc.numPixels, bidir);
 }
 
 GPUGI_D void write_cache(const RenderConst& rc, uint32_t s, uint32_t k, float3 flux, int mat, float3 pos, float n0,
@@ -302,32 +309,35 @@ GPUGI_D void write_cache(const RenderConst& rc, uint32_t s, uint32_t k, float3 f
 // lighttracer.comp:49-93: one particle per thread, numRaysPerLightSample
 // particles per initial light sample. With a light cache (BPT) each thread
 // first stores its own light sample (lighttracer.comp:56-61).
+GPUGI_D void light_path_start(const RenderConst& rc, const PathSoA& A, uint32_t p, uint32_t s, uint32_t gid,
+                              bool withCache) {
+    uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + gid);
+    const uint32_t li = gid / (uint32_t)rc.numRaysPerLightSample;
+    const float4* ls = rc.lightSamples + 2 * ((size_t)s * rc.numLightSamples + li);
+    const float4 pn0 = __ldg(ls), in1 = __ldg(ls + 1);
+    if (withCache) {
+        if (gid == 0) rc.cacheCount[s] = rc.lightThreads;  // resetcounter.comp
+        write_cache(rc, s, gid, xyz(in1) / kPI_2 / (float)rc.numRaysPerLightSample, -1, xyz(pn0), pn0.w, in1.w,
+                    make_float2(0.0f, 0.0f), pack_normal(f3(0.0f)), 0);
+    }
+    float3 tp = xyz(in1) * (kPI / (float)rc.numRaysPerLightSample);
+    float3 d;
+    if (in1.w > 1.5f) {
+        d = sample_direction(random2(seed));
+        tp *= 4.0f;
+    } else {
+        float3 n = unpack_normal(pn0.w, in1.w), U, V;
+        create_onb(n, U, V);
+        d = sample_hemisphere_cosine(random2(seed), U, V, n);
+    }
+    store_path(A, p, xyz(pn0), d, tp, seed, gid, s << 8, 1.0f);
+}
+
 __global__ void k_light_generate(RenderConst rc, PathSoA A, bool withCache) {
     const uint32_t total = rc.samples * rc.lightThreads;
     if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-        const uint32_t s = g / rc.lightThreads, gid = g % rc.lightThreads;
-        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + gid);
-        const uint32_t li = gid / (uint32_t)rc.numRaysPerLightSample;
-        const float4* ls = rc.lightSamples + 2 * ((size_t)s * rc.numLightSamples + li);
-        const float4 pn0 = __ldg(ls), in1 = __ldg(ls + 1);
-        if (withCache) {
-            if (gid == 0) rc.cacheCount[s] = rc.lightThreads;  // resetcounter.comp
-            write_cache(rc, s, gid, xyz(in1) / kPI_2 / (float)rc.numRaysPerLightSample, -1, xyz(pn0), pn0.w, in1.w,
-                        make_float2(0.0f, 0.0f), pack_normal(f3(0.0f)), 0);
-        }
-        float3 tp = xyz(in1) * (kPI / (float)rc.numRaysPerLightSample);
-        float3 d;
-        if (in1.w > 1.5f) {
-            d = sample_direction(random2(seed));
-            tp *= 4.0f;
-        } else {
-            float3 n = unpack_normal(pn0.w, in1.w), U, V;
-            create_onb(n, U, V);
-            d = sample_hemisphere_cosine(random2(seed), U, V, n);
-        }
-        store_path(A, g, xyz(pn0), d, tp, seed, gid, s << 8, 1.0f);
-    }
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x)
+        light_path_start(rc, A, g, g / rc.lightThreads, g % rc.lightThreads, withCache);
 }
 
 // ------------------------------------------------------------ shading
@@ -498,59 +508,100 @@ GPUGI_D bool project_to_screen(const RenderConst& rc, float3 pos, float3 inDir, 
     return true;
 }
 
-// lighttracer.comp:95-192, one bounce (with SAVE_LIGHT_CACHE when withCache).
+// lighttracer.comp:95-192, one bounce of one particle (with SAVE_LIGHT_CACHE
+// when withCache): the per-lane part of the light-shade kernels. The camera
+// connection goes to pixel; the particle keeps gid.
+struct LightLane {
+    bool survive = false, shadow = false;
+    float3 o, d, tp, sro, srd, color;
+    float srl = 0.0f;
+    uint32_t seed = 0, pixel = 0, info = 0, gid = 0;
+};
+
+GPUGI_D void light_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
+                              bool withCache, LightLane& L) {
+    L.o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+    L.d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+    L.tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+    L.seed = A.seed[k];
+    L.gid = A.pixel[k];
+    L.info = A.info[k];
+    const int32_t slot = H.slot[k];
+    if (slot < 0) return;
+    const float t = H.t[k];
+    const float4 rec = __ldg(rc.s.tris + 3 * (size_t)slot + 2);
+    const float3 gN = make_float3(rec.y, rec.z, rec.w);  // cross(e1, e0), not normalised
+    L.o = L.o + t * L.d;
+    const int4 tri = __ldg(rc.s.slots + slot);
+    float2 tc;
+    const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], &tc);
+    const MaterialData m = load_material(rc.s, tri.w);
+    const uint32_t s = L.info >> 8;
+    if (withCache && m.Reflectiveness.w < 100.0f) {
+        const uint32_t e = atomicAdd(rc.cacheCount + s, 1u);
+        if (e < rc.cacheCap) {
+            float2 pn = pack_normal(sN);
+            write_cache(rc, s, e, L.tp, tri.w, L.o, pn.x, pn.y, tc, pack_normal(L.d), depth + 1);
+        } else {
+            raise_error(rc.err, DEVERR_QUEUE_OVERFLOW);
+        }
+    }
+    L.shadow = project_to_screen(rc, L.o, L.d, gN, sN, m, L.tp, withCache, L.sro, L.srd, L.srl, L.color, L.pixel);
+    float3 thr = f3(1.0f);
+    float pdf;
+    const float3 nd = sample_bsdf(L.d, m, L.seed, sN, thr, true, pdf);
+    thr *= shading_correction(L.d, nd, gN, sN);
+    L.tp *= thr;
+    L.survive = roulette(rc, depth, thr, L.tp, L.seed) && depth + 1 < rc.maxPathLength;
+    L.d = nd;
+    L.o = L.o + L.d * kRAY_HIT_EPSILON;
+}
+
 __global__ void __launch_bounds__(128) k_light_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q,
                                                      int depth, bool withCache) {
     const uint32_t n = rc.cnt->path[depth];
     WARP_LOOP(n, k, valid) {
-        bool survive = false, shadow = false;
-        float3 o, d, tp, sro, srd, color;
-        float srl = 0.0f;
-        uint32_t seed = 0, pixel = 0, info = 0, gid = 0;
-        if (valid) {
-            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
-            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
-            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
-            gid = A.pixel[k];
-            info = A.info[k];
-            const int32_t slot = H.slot[k];
-            if (slot >= 0) {
-                const float t = H.t[k];
-                const float4 rec = __ldg(rc.s.tris + 3 * (size_t)slot + 2);
-                const float3 gN = make_float3(rec.y, rec.z, rec.w);  // cross(e1, e0), not normalised
-                o = o + t * d;
-                const int4 tri = __ldg(rc.s.slots + slot);
-                float2 tc;
-                const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], &tc);
-                const MaterialData m = load_material(rc.s, tri.w);
-                const uint32_t s = info >> 8;
-                if (withCache && m.Reflectiveness.w < 100.0f) {
-                    const uint32_t e = atomicAdd(rc.cacheCount + s, 1u);
-                    if (e < rc.cacheCap) {
-                        float2 pn = pack_normal(sN);
-                        write_cache(rc, s, e, tp, tri.w, o, pn.x, pn.y, tc, pack_normal(d), depth + 1);
-                    } else {
-                        raise_error(rc.err, DEVERR_QUEUE_OVERFLOW);
-                    }
-                }
-                shadow = project_to_screen(rc, o, d, gN, sN, m, tp, withCache, sro, srd, srl, color, pixel);
-                float3 thr = f3(1.0f);
-                float pdf;
-                const float3 nd = sample_bsdf(d, m, seed, sN, thr, true, pdf);
-                thr *= shading_correction(d, nd, gN, sN);
-                tp *= thr;
-                survive = roulette(rc, depth, thr, tp, seed) && depth + 1 < rc.maxPathLength;
-                d = nd;
-                o = o + d * kRAY_HIT_EPSILON;
-            }
-        }
+        LightLane L;
+        if (valid) light_shade_lane(rc, A, H, k, depth, withCache, L);
         uint32_t qs, qb;
-        warp_append(&rc.cnt->shadow[depth], shadow, qs);
-        if (shadow) store_shadow(Q, qs, sro, srd, srl, color, pixel);
-        warp_append(&rc.cnt->path[depth + 1], survive, qb);
-        if (survive) store_path(B, qb, o, d, tp, seed, gid, info, 1.0f);
+        warp_append(&rc.cnt->shadow[depth], L.shadow, qs);
+        if (L.shadow) store_shadow(Q, qs, L.sro, L.srd, L.srl, L.color, L.pixel);
+        warp_append(&rc.cnt->path[depth + 1], L.survive, qb);
+        if (L.survive) store_path(B, qb, L.o, L.d, L.tp, L.seed, L.gid, L.info, 1.0f);
     }
+}
+
+// showlightcaches.comp:9-65 without its visibility test: the camera
+// connection of light sample i (sample-major), or false when the sample has
+// no position or does not project onto the image. The caller splats color at
+// pixel when the segment ro + [0, rl] rd is unoccluded.
+GPUGI_D bool light_sample_view(const RenderConst& rc, uint32_t i, float3& ro, float3& rd, float& rl, float3& color,
+                               uint32_t& pixel) {
+    const float4* ls = rc.lightSamples + 2 * (size_t)i;
+    const float4 pn0 = __ldg(ls), in1 = __ldg(ls + 1);
+    if (in1.w > 2.5f) return false;  // directional samples have no position
+    float3 cd = rc.camPos - xyz(pn0);
+    const float camViewDotRay = -dot(rc.camW, cd);
+    if (!(camViewDotRay > 0.0f)) return false;
+    float sx = -dot(rc.camU, cd) / camViewDotRay, sy = -dot(rc.camV, cd) / camViewDotRay;
+    sx /= dot(rc.camU, rc.camU);
+    sy /= dot(rc.camV, rc.camV);
+    if (!(sx >= -1.0f && sx < 1.0f && sy > -1.0f && sy <= 1.0f)) return false;
+    const int px = (int)((sx * 0.5f + 0.5f) * (float)rc.width), py = (int)((sy * 0.5f + 0.5f) * (float)rc.height);
+    if (px < 0 || py < 0 || px >= rc.width || py >= rc.height) return false;
+    const float distSq = dot(cd, cd);
+    const float dist = sqrtf(distSq);
+    cd /= dist;
+    const float3 n = unpack_normal(pn0.w, in1.w);
+    const float cosTheta = dot(n, cd);
+    const float cosAtCamera = saturate(camViewDotRay / dist);
+    const float i2r = cosTheta / (kPI_2 * cosAtCamera * cosAtCamera * cosAtCamera * rc.pixelArea * distSq);
+    ro = cd * kRAY_HIT_EPSILON + xyz(pn0);
+    rd = cd;
+    rl = dist;
+    color = xyz(in1) * i2r;
+    pixel = (uint32_t)(py * rc.width + px);
+    return true;
 }
 
 // showlightcaches.comp:9-65: light samples seen directly by the camera.
@@ -558,28 +609,12 @@ template <int BOUNDS>
 __global__ void k_show_light_samples(RenderConst rc) {
     const uint32_t total = rc.samples * rc.numLightSamples;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const float4* ls = rc.lightSamples + 2 * (size_t)i;
-        const float4 pn0 = __ldg(ls), in1 = __ldg(ls + 1);
-        if (in1.w > 2.5f) continue;  // directional samples have no position
-        float3 cd = rc.camPos - xyz(pn0);
-        const float camViewDotRay = -dot(rc.camW, cd);
-        if (!(camViewDotRay > 0.0f)) continue;
-        float sx = -dot(rc.camU, cd) / camViewDotRay, sy = -dot(rc.camV, cd) / camViewDotRay;
-        sx /= dot(rc.camU, rc.camU);
-        sy /= dot(rc.camV, rc.camV);
-        if (!(sx >= -1.0f && sx < 1.0f && sy > -1.0f && sy <= 1.0f)) continue;
-        const float distSq = dot(cd, cd);
-        const float dist = sqrtf(distSq);
-        cd /= dist;
-        TraceResult r = trace_ray<true, BOUNDS>(rc.s, cd * kRAY_HIT_EPSILON + xyz(pn0), cd, dist, rc.err);
-        if (r.slot >= 0) continue;
-        const float3 n = unpack_normal(pn0.w, in1.w);
-        const float cosTheta = dot(n, cd);
-        const float cosAtCamera = saturate(camViewDotRay / dist);
-        const float i2r = cosTheta / (kPI_2 * cosAtCamera * cosAtCamera * cosAtCamera * rc.pixelArea * distSq);
-        const int px = (int)((sx * 0.5f + 0.5f) * (float)rc.width), py = (int)((sy * 0.5f + 0.5f) * (float)rc.height);
-        if (px < 0 || py < 0 || px >= rc.width || py >= rc.height) continue;
-        splat(rc, (uint32_t)(py * rc.width + px), xyz(in1) * i2r);
+        float3 ro, rd, color;
+        float rl;
+        uint32_t pixel;
+        if (!light_sample_view(rc, i, ro, rd, rl, color, pixel)) continue;
+        TraceResult r = trace_ray<true, BOUNDS>(rc.s, ro, rd, rl, rc.err);
+        if (r.slot < 0) splat(rc, pixel, color);
     }
 }
 
@@ -1319,12 +1354,14 @@ __global__ void k_mse(const float4* __restrict__ rgba, const double* __restrict_
 }
 
 // ------------------------------------------------------------ batched jobs
-// Many path-tracing jobs (each its own scene, camera, image, resolution,
-// sample count and path length) share one wavefront: their paths sit in the
-// same queues, every stage is one launch over all of them, and each path
-// and shadow ray carries its job index. The job constants come from a
-// device table, so the launch sequence does not change between rounds and is
-// replayed as one CUDA graph.
+// Many jobs (each its own scene, camera, image, resolution, sample count,
+// path length and pass: PT, LT or BPT) share one wavefront: their paths sit
+// in the same queues, every stage is one launch over all of them, and each
+// path and shadow ray carries its job index. Phase 0 holds the PT eye paths,
+// the LT particles and the BPT light paths (each BPT job writes its own light
+// caches); phase 1 the BPT eye paths, which connect to those caches. The job
+// constants come from a device table, so the launch sequence does not change
+// between rounds and is replayed as one CUDA graph.
 
 // Largest j < numJobs with offsets[j] <= p (offsets[numJobs] > p).
 GPUGI_D uint32_t find_job(const uint32_t* __restrict__ offsets, uint32_t numJobs, uint32_t p) {
@@ -1337,20 +1374,41 @@ GPUGI_D uint32_t find_job(const uint32_t* __restrict__ offsets, uint32_t numJobs
     return lo;
 }
 
+// The first vertices of the phase's paths (offsets: the phase's path range of
+// every job). An LT particle that is the first of its light sample also
+// queues that sample's camera connection (showlightcaches.comp) as a shadow
+// ray of depth 0, so the shadow walker tests its visibility.
 __global__ void k_batch_generate(const RenderConst* __restrict__ jobs, const uint32_t* __restrict__ offsets,
-                                 uint32_t numJobs, Counters* cnt, PathSoA A) {
+                                 uint32_t numJobs, Counters* cnt, PathSoA A, ShadowSoA Q, int phase) {
     const uint32_t total = offsets[numJobs];
     if (blockIdx.x == 0 && threadIdx.x == 0) cnt->path[0] = total;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
-        const uint32_t j = find_job(offsets, numJobs, p);
-        const RenderConst& rc = jobs[j];
-        const uint32_t local = p - offsets[j];
-        const uint32_t s = local / (uint32_t)rc.numPixels, pix = local % (uint32_t)rc.numPixels;
-        const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + pix);
-        const float3 d = primary_direction(rc, seed, x, y);
-        store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, s << 8, 1.0f);
-        A.job[p] = j;
+    WARP_LOOP(total, p, valid) {
+        bool view = false;
+        float3 ro, rd, color;
+        float rl = 0.0f;
+        uint32_t pixel = 0, j = 0;
+        if (valid) {
+            j = find_job(offsets, numJobs, p);
+            const RenderConst& rc = jobs[j];
+            const uint32_t local = p - offsets[j];
+            if (phase == 1 || rc.pass == GPUGI_PASS_PT) {
+                camera_path_start(rc, A, p, local / (uint32_t)rc.numPixels, local % (uint32_t)rc.numPixels,
+                                  phase == 1);
+            } else {
+                const uint32_t s = local / rc.lightThreads, gid = local % rc.lightThreads;
+                light_path_start(rc, A, p, s, gid, rc.pass == GPUGI_PASS_BPT);
+                if (rc.pass == GPUGI_PASS_LT && gid % (uint32_t)rc.numRaysPerLightSample == 0)
+                    view = light_sample_view(rc, s * rc.numLightSamples + gid / (uint32_t)rc.numRaysPerLightSample,
+                                             ro, rd, rl, color, pixel);
+            }
+            A.job[p] = j;
+        }
+        uint32_t qs;
+        warp_append(&cnt->shadow[0], view, qs);
+        if (view) {
+            store_shadow(Q, qs, ro, rd, rl, color, pixel);
+            Q.job[qs] = j;
+        }
     }
 }
 
@@ -1446,15 +1504,57 @@ __global__ void __launch_bounds__(128) k_batch_shadow(const RenderConst* __restr
         });
 }
 
-__global__ void __launch_bounds__(128) k_batch_pt_shade(const RenderConst* __restrict__ jobs, Counters* cnt,
-                                                        PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q, int depth) {
+// One bounce of the phase-0 paths: PT eye paths, LT particles and BPT light
+// paths (the latter append to their job's light cache).
+__global__ void __launch_bounds__(128) k_batch_shade(const RenderConst* __restrict__ jobs, Counters* cnt,
+                                                     PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q, int depth) {
     const uint32_t n = cnt->path[depth];
     WARP_LOOP(n, k, valid) {
-        PtLane L;
+        bool shadow = false, survive = false;
+        float3 o, d, tp, sro, srd, c;
+        float srl = 0.0f;
+        uint32_t seed = 0, pathPixel = 0, shadowPixel = 0, info = 0, j = 0;
+        if (valid) {
+            j = A.job[k];
+            const RenderConst& rc = jobs[j];
+            if (rc.pass == GPUGI_PASS_PT) {
+                PtLane L;
+                pt_shade_lane(rc, A, H, k, depth, L);
+                shadow = L.shadow, survive = L.survive;
+                o = L.o, d = L.d, tp = L.tp, sro = L.sro, srd = L.srd, c = L.contrib, srl = L.srl;
+                seed = L.seed, pathPixel = shadowPixel = L.pixel, info = L.info;
+            } else {
+                LightLane L;
+                light_shade_lane(rc, A, H, k, depth, rc.pass == GPUGI_PASS_BPT, L);
+                shadow = L.shadow, survive = L.survive;
+                o = L.o, d = L.d, tp = L.tp, sro = L.sro, srd = L.srd, c = L.color, srl = L.srl;
+                seed = L.seed, pathPixel = L.gid, shadowPixel = L.pixel, info = L.info;
+            }
+        }
+        uint32_t qs, qb;
+        warp_append(&cnt->shadow[depth], shadow, qs);
+        if (shadow) {
+            store_shadow(Q, qs, sro, srd, srl, c, shadowPixel);
+            Q.job[qs] = j;
+        }
+        warp_append(&cnt->path[depth + 1], survive, qb);
+        if (survive) {
+            store_path(B, qb, o, d, tp, seed, pathPixel, info, 1.0f);
+            B.job[qb] = j;
+        }
+    }
+}
+
+// One bounce of the phase-1 paths: BPT eye paths.
+__global__ void __launch_bounds__(128) k_batch_bpt_shade(const RenderConst* __restrict__ jobs, Counters* cnt,
+                                                         PathSoA A, PathSoA B, HitSoA H, ShadowSoA Q, int depth) {
+    const uint32_t n = cnt->path[depth];
+    WARP_LOOP(n, k, valid) {
+        BptLane L;
         uint32_t j = 0;
         if (valid) {
             j = A.job[k];
-            pt_shade_lane(jobs[j], A, H, k, depth, L);
+            bpt_shade_lane(jobs[j], A, H, k, depth, jobs[j].maxPathLength, -1, L);
         }
         uint32_t qs, qb;
         warp_append(&cnt->shadow[depth], L.shadow, qs);
@@ -1464,7 +1564,7 @@ __global__ void __launch_bounds__(128) k_batch_pt_shade(const RenderConst* __res
         }
         warp_append(&cnt->path[depth + 1], L.survive, qb);
         if (L.survive) {
-            store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, 1.0f);
+            store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, L.lastP);
             B.job[qb] = j;
         }
     }
@@ -1686,6 +1786,12 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
 }
 
 
+// LightPathtracer::SetScreenSize (gpugi/renderer/lightpathtracer.cpp:34):
+// particles per light sample and iteration.
+static uint32_t rays_per_light_sample(const gpugi_render_params* p) {
+    return std::max<uint32_t>(64u, (p->width * p->height / p->numLightSamples / 64u) * 64u);
+}
+
 static RenderConst make_render_const(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_camera* cam,
                                      const gpugi_render_params* p, gpugi_image* im, RenderBuffers* rb) {
     RenderConst rc{};
@@ -1701,6 +1807,7 @@ static RenderConst make_render_const(gpugi_ctx* ctx, const gpugi_scene* sc, cons
     rc.maxPathLength = (int)p->maxPathLength;
     rc.rrStartDepth = (int)p->rrStartDepth;
     rc.iteration = p->iteration;
+    rc.pass = p->pass;
     rc.numLightSamples = p->numLightSamples;
     rc.sky = f3(p->sky[0], p->sky[1], p->sky[2]);
     rc.image = im->rgba;
@@ -1939,9 +2046,7 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "either lightSamples or rngState is required");
 
     const uint32_t numPixels = p->width * p->height;
-    // LightPathtracer::SetScreenSize (gpugi/renderer/lightpathtracer.cpp:34)
-    const uint32_t raysPerLight =
-        std::max<uint32_t>(64u, (numPixels / p->numLightSamples / 64u) * 64u);
+    const uint32_t raysPerLight = rays_per_light_sample(p);
     const uint32_t lightThreads = raysPerLight * p->numLightSamples;
     // Whitted: up to two shadow rays per path, so the queues get twice the paths
     const bool pm = p->pass == GPUGI_PASS_PM;
@@ -2176,27 +2281,56 @@ gpugi_status gpugi_set_batch_config(gpugi_ctx* ctx, uint32_t pathsPerRound, uint
 gpugi_status gpugi_render_batch(gpugi_ctx* ctx, const gpugi_job* jobs, uint32_t numJobs) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (numJobs && !jobs) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL jobs");
-    std::vector<uint32_t> pt;  // jobs of the fused PT wavefront
-    uint32_t maxDepth = 0;
-    uint64_t maxLightBytes = 0;
+    // The PT, LT and BPT jobs share the wavefront. Per sample a job needs
+    // paths0 phase-0 paths (plus extraQ shadow-queue entries: the LT light
+    // samples' camera connections), paths1 phase-1 paths and cacheBytes of
+    // light cache.
+    struct Fused {
+        uint32_t job, raysPerLight, lightThreads;
+        uint64_t paths0, extraQ, paths1, cacheBytes;
+    };
+    std::vector<Fused> fused;
+    uint32_t depth0 = 0, depth1 = 0;
+    uint64_t lightBytes = 0, cacheNeed = 0, maxCache = 0, cacheSamples = 0;
     const uint32_t cap = ctx->batchPaths;
     for (uint32_t j = 0; j < numJobs; ++j) {
         const gpugi_job& J = jobs[j];
         gpugi_status st = check_render_args(ctx, J.scene, &J.camera, &J.params, J.lightSamples, J.rngState, J.image);
         if (st) return st;
-        if (J.params.pass != GPUGI_PASS_PT) continue;
-        const uint64_t pix = (uint64_t)J.params.width * J.params.height;
-        if (pix > cap) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "a job image is larger than the path queue");
-        pt.push_back(j);
-        maxDepth = std::max(maxDepth, J.params.maxPathLength);
-        maxLightBytes += std::min<uint64_t>(J.params.samples, cap / pix) * J.params.numLightSamples * 32ull;
+        const gpugi_render_params& P = J.params;
+        if (P.pass > GPUGI_PASS_BPT) continue;
+        Fused F{j, rays_per_light_sample(&P), 0, 0, 0, 0, 0};
+        F.lightThreads = F.raysPerLight * P.numLightSamples;
+        const uint64_t pix = (uint64_t)P.width * P.height;
+        if (P.pass == GPUGI_PASS_PT) {
+            F.paths0 = pix;
+        } else {
+            F.paths0 = F.lightThreads;
+            if (P.pass == GPUGI_PASS_LT) F.extraQ = P.numLightSamples;
+            else F.paths1 = pix, F.cacheBytes = (uint64_t)F.lightThreads * (P.maxPathLength + 1) * sizeof(CacheEntry);
+        }
+        if (F.paths0 + F.extraQ > cap || F.paths1 > cap)
+            return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "one sample of a job needs more paths than the path queue");
+        uint64_t most = std::min<uint64_t>(P.samples, cap / (F.paths0 + F.extraQ));
+        if (F.paths1) most = std::min<uint64_t>(most, cap / F.paths1);
+        lightBytes += most * P.numLightSamples * 32ull;
+        depth0 = std::max(depth0, P.maxPathLength);
+        if (P.pass == GPUGI_PASS_BPT) {
+            depth1 = std::max(depth1, P.maxPathLength);
+            cacheNeed += most * F.cacheBytes;
+            maxCache = std::max(maxCache, F.cacheBytes);
+            cacheSamples += most;
+        }
+        fused.push_back(F);
     }
-    if (!pt.empty()) {
-        const uint32_t nj = (uint32_t)pt.size();
-        gpugi_status st = ensure_buffers(ctx, cap, 0, maxLightBytes, 1);
+    if (!fused.empty()) {
+        const uint32_t nj = (uint32_t)fused.size();
+        // light caches of one round: at most 4 GiB, but always one sample of the largest job
+        const uint64_t cacheBudget = std::max<uint64_t>(maxCache, std::min<uint64_t>(cacheNeed, 4ull << 30));
+        gpugi_status st = ensure_buffers(ctx, cap, cacheBudget, lightBytes, (uint32_t)std::max<uint64_t>(1, cacheSamples));
         if (st) return st;
         RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
-        if ((st = ensure_host_lights(ctx, rb, maxLightBytes))) return st;
+        if ((st = ensure_host_lights(ctx, rb, lightBytes))) return st;
         if (nj > rb->jobCap) {
             GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
             if (rb->dJobs) cudaFree(rb->dJobs);
@@ -2207,37 +2341,47 @@ gpugi_status gpugi_render_batch(gpugi_ctx* ctx, const gpugi_job* jobs, uint32_t 
             rb->dOffsets = rb->hOffsets = nullptr;
             rb->jobCap = 0;
             GPUGI_CUDA_TRY(ctx, cudaMalloc(&rb->dJobs, nj * sizeof(RenderConst)));
-            GPUGI_CUDA_TRY(ctx, cudaMalloc(&rb->dOffsets, (nj + 1) * sizeof(uint32_t)));
+            GPUGI_CUDA_TRY(ctx, cudaMalloc(&rb->dOffsets, 2 * (nj + 1) * sizeof(uint32_t)));
             GPUGI_CUDA_TRY(ctx, cudaMallocHost(&rb->hJobs, nj * sizeof(RenderConst)));
-            GPUGI_CUDA_TRY(ctx, cudaMallocHost(&rb->hOffsets, (nj + 1) * sizeof(uint32_t)));
+            GPUGI_CUDA_TRY(ctx, cudaMallocHost(&rb->hOffsets, 2 * (nj + 1) * sizeof(uint32_t)));
             rb->jobCap = nj;
         }
         // launch shapes (no node staging: the walkers serve several scenes)
         WalkerLaunch LE, LS;
-        if ((st = walker_launch_config(ctx, jobs[pt[0]].scene, (const void*)k_batch_extend, 1ull << 40, 0, LE)) ||
-            (st = walker_launch_config(ctx, jobs[pt[0]].scene, (const void*)k_batch_shadow, 1ull << 40, 0, LS)))
+        const gpugi_scene* sc0 = jobs[fused[0].job].scene;
+        if ((st = walker_launch_config(ctx, sc0, (const void*)k_batch_extend, 1ull << 40, 0, LE)) ||
+            (st = walker_launch_config(ctx, sc0, (const void*)k_batch_shadow, 1ull << 40, 0, LS)))
             return st;
-        int perSM = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, (const void*)k_batch_pt_shade, 128, 0);
-        const unsigned gridShade = (unsigned)(ctx->numSMs * std::max(perSM, 1));
+        int perSM0 = 0, perSM1 = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM0, (const void*)k_batch_shade, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM1, (const void*)k_batch_bpt_shade, 128, 0);
+        const unsigned gridShade0 = (unsigned)(ctx->numSMs * std::max(perSM0, 1));
+        const unsigned gridShade1 = (unsigned)(ctx->numSMs * std::max(perSM1, 1));
         const unsigned genBlocks = (unsigned)ctx->numSMs * 8;
         const uint32_t groupE = ctx->traceMode >= 3 ? LE.grid * 128u / 2u : 0u;
         const uint32_t groupS = ctx->traceMode >= 3 ? LS.grid * 128u / 2u : 0u;
-        auto record = [&](cudaStream_t stream) {
+        auto phase = [&](cudaStream_t stream, int ph, uint32_t maxDepth) {
             cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), stream);
             PathSoA A = rb->A, B = rb->B;
-            k_batch_generate<<<genBlocks, 256, 0, stream>>>(rb->dJobs, rb->dOffsets, nj, rb->cnt, A);
+            k_batch_generate<<<genBlocks, 256, 0, stream>>>(rb->dJobs, rb->dOffsets + ph * (nj + 1), nj, rb->cnt, A,
+                                                            rb->Q, ph);
             for (int depth = 0; depth < (int)maxDepth; ++depth) {
                 k_batch_extend<<<LE.grid, 128, 0, stream>>>(rb->dJobs, rb->cnt, ctx->errWord, A, rb->H, depth,
                                                             groupE);
-                k_batch_pt_shade<<<gridShade, 128, 0, stream>>>(rb->dJobs, rb->cnt, A, B, rb->H, rb->Q, depth);
+                if (ph == 0) k_batch_shade<<<gridShade0, 128, 0, stream>>>(rb->dJobs, rb->cnt, A, B, rb->H, rb->Q, depth);
+                else k_batch_bpt_shade<<<gridShade1, 128, 0, stream>>>(rb->dJobs, rb->cnt, A, B, rb->H, rb->Q, depth);
                 k_batch_shadow<<<LS.grid, 128, 0, stream>>>(rb->dJobs, rb->cnt, ctx->errWord, rb->Q, depth, groupS);
                 std::swap(A, B);
             }
         };
+        auto record = [&](cudaStream_t stream) {
+            phase(stream, 0, depth0);
+            if (depth1) phase(stream, 1, depth1);
+        };
         if (ctx->batchGraph) {
-            const std::vector<uintptr_t> key = {(uintptr_t)rb->block, (uintptr_t)rb->dJobs, nj, maxDepth, LE.grid,
-                                                LS.grid, gridShade, (uintptr_t)ctx->errWord, groupE, groupS};
+            const std::vector<uintptr_t> key = {(uintptr_t)rb->block, (uintptr_t)rb->dJobs, nj, depth0, depth1,
+                                                LE.grid, LS.grid, gridShade0, gridShade1, (uintptr_t)ctx->errWord,
+                                                groupE, groupS};
             if (!rb->batchExec || key != rb->batchKey) {
                 if (rb->batchExec) cudaGraphExecDestroy(rb->batchExec);
                 rb->batchExec = nullptr;
@@ -2257,54 +2401,69 @@ gpugi_status gpugi_render_batch(gpugi_ctx* ctx, const gpugi_job* jobs, uint32_t 
         }
         GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
         std::vector<uint32_t> done(nj, 0);
+        uint32_t* off0 = rb->hOffsets;
+        uint32_t* off1 = rb->hOffsets + nj + 1;
         for (;;) {
             // plan a round: each unfinished job adds as many samples as still fit
             GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // staging buffers are free again
-            uint64_t used = 0, lightOff = 0;
+            uint64_t used0 = 0, paths0 = 0, paths1 = 0, usedCache = 0, lightOff = 0, cacheSlot = 0;
             bool any = false;
-            rb->hOffsets[0] = 0;
+            off0[0] = off1[0] = 0;
             for (uint32_t q = 0; q < nj; ++q) {
-                const gpugi_job& J = jobs[pt[q]];
-                const uint64_t pix = (uint64_t)J.params.width * J.params.height;
-                const uint32_t c =
-                    (uint32_t)std::min<uint64_t>(J.params.samples - done[q], (cap - used) / pix);
+                const Fused& F = fused[q];
+                const gpugi_job& J = jobs[F.job];
+                uint64_t c = std::min<uint64_t>(J.params.samples - done[q], (cap - used0) / (F.paths0 + F.extraQ));
+                if (F.paths1) c = std::min<uint64_t>(c, (cap - paths1) / F.paths1);
+                if (F.cacheBytes) c = std::min<uint64_t>(c, (cacheBudget - usedCache) / F.cacheBytes);
                 RenderConst rc = make_render_const(ctx, J.scene, &J.camera, &J.params, J.image, rb);
-                rc.samples = c;
+                rc.samples = (uint32_t)c;
                 rc.sampleBase = done[q];
                 rc.lightSamples = rb->lights + lightOff / 16;
+                rc.numRaysPerLightSample = (int)F.raysPerLight;
+                rc.lightThreads = F.lightThreads;
+                if (F.cacheBytes) {
+                    rc.cache = rb->cache + usedCache / sizeof(CacheEntry);
+                    rc.cacheCount = rb->cacheCount + cacheSlot;
+                    rc.cacheCap = (uint32_t)(F.cacheBytes / sizeof(CacheEntry));
+                }
                 if (c) {
                     const size_t setFloats = (size_t)J.params.numLightSamples * 8;
                     float* dst = rb->hostLights + lightOff / 4;
                     if (J.lightSamples)
                         std::memcpy(dst, J.lightSamples + (size_t)done[q] * setFloats, c * setFloats * sizeof(float));
                     else
-                        for (uint32_t k = 0; k < c; ++k)
+                        for (uint64_t k = 0; k < c; ++k)
                             generate_light_samples(const_cast<gpugi_scene*>(J.scene), *J.rngState,
                                                    J.params.numLightSamples, dst + k * setFloats);
                     lightOff += c * setFloats * sizeof(float);
                     any = true;
                 }
                 rb->hJobs[q] = rc;
-                used += c * pix;
-                rb->hOffsets[q + 1] = (uint32_t)used;
-                done[q] += c;
+                used0 += c * (F.paths0 + F.extraQ);
+                paths0 += c * F.paths0;
+                paths1 += c * F.paths1;
+                usedCache += c * F.cacheBytes;
+                if (F.cacheBytes) cacheSlot += c;
+                off0[q + 1] = (uint32_t)paths0;
+                off1[q + 1] = (uint32_t)paths1;
+                done[q] += (uint32_t)c;
             }
             if (!any) break;
             GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->lights, rb->hostLights, lightOff, cudaMemcpyHostToDevice,
                                                 ctx->stream));
             GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->dJobs, rb->hJobs, nj * sizeof(RenderConst),
                                                 cudaMemcpyHostToDevice, ctx->stream));
-            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->dOffsets, rb->hOffsets, (nj + 1) * sizeof(uint32_t),
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(rb->dOffsets, rb->hOffsets, 2 * (nj + 1) * sizeof(uint32_t),
                                                 cudaMemcpyHostToDevice, ctx->stream));
             if (ctx->batchGraph) GPUGI_CUDA_TRY(ctx, cudaGraphLaunch(rb->batchExec, ctx->stream));
             else record(ctx->stream);
             GPUGI_CUDA_TRY(ctx, cudaGetLastError());
         }
     }
-    // other passes: one job after another
+    // the Whitted ray tracer and the photon mapper: one job after another
     for (uint32_t j = 0; j < numJobs; ++j) {
         const gpugi_job& J = jobs[j];
-        if (J.params.pass == GPUGI_PASS_PT) continue;
+        if (J.params.pass <= GPUGI_PASS_BPT) continue;
         gpugi_status st = gpugi_render(ctx, J.scene, &J.camera, &J.params, J.lightSamples, J.rngState, J.image);
         if (st) return st;
     }

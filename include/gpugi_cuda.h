@@ -366,12 +366,22 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* scene, const gp
  * counterpart in the reference (RendererSystem::Draw renders one scene per
  * call, gpugi/renderer/renderersystem.cpp:235-258); per job the result is
  * gpugi_render's with the same arguments (same seeds and light samples).
- * PT jobs share the queues: each stage (generate, then per bounce extend,
- * shade, shadow) is one launch over the paths of all jobs, and the whole
- * sequence is captured once as a CUDA graph and replayed per round of at
- * most the context's path-queue capacity (gpugi_set_batch_config).
- * LT and BPT jobs are rendered one after another with gpugi_render.
- * Jobs that share an rngState draw their light samples in round order. */
+ * PT, LT and BPT jobs share the queues: each stage (generate, then per
+ * bounce extend, shade, shadow) is one launch over the paths of all jobs.
+ * Phase 0 holds the PT eye paths, the LT particles (with the light samples'
+ * camera connections) and the BPT light paths, which fill each BPT job's
+ * light caches; phase 1 the BPT eye paths. The whole sequence is captured
+ * once as a CUDA graph and replayed per round; a round holds at most the
+ * context's path-queue capacity (gpugi_set_batch_config) of paths per phase
+ * and at most 4 GiB of light caches (at least one sample of the largest BPT
+ * job). A job whose single sample needs more paths than the capacity (PT:
+ * width x height; LT: its particles plus numLightSamples; BPT: its particles,
+ * and width x height) is refused with GPUGI_ERROR_INVALID_ARGUMENT. BPT
+ * connections pick light-cache entries whose order follows the device's
+ * atomic appends, so a BPT job equals gpugi_render's in distribution (and
+ * exactly at maxPathLength 1). Whitted and photon-mapper jobs are rendered
+ * afterwards, one gpugi_render call each. Jobs that share an rngState draw
+ * their light samples in round order. */
 typedef struct gpugi_job {
     const gpugi_scene* scene;
     gpugi_camera camera;
@@ -383,8 +393,8 @@ typedef struct gpugi_job {
 
 gpugi_status gpugi_render_batch(gpugi_ctx* ctx, const gpugi_job* jobs, uint32_t numJobs);
 
-/* Path-queue capacity of one batched round (paths in flight; default 16M,
- * at least the largest job image) and whether rounds replay a CUDA graph
+/* Path-queue capacity of one batched round (paths in flight per phase;
+ * default 16M, in [1024, 64M]) and whether rounds replay a CUDA graph
  * (default 1). */
 gpugi_status gpugi_set_batch_config(gpugi_ctx* ctx, uint32_t pathsPerRound, uint32_t useGraph);
 

@@ -1,8 +1,12 @@
 """Batched rendering (gpugi_render_batch): several jobs with their own
-scenes, cameras, resolutions, sample counts and path lengths in one
-wavefront, replayed as a CUDA graph per round. Every job's image must equal
-gpugi_render's for the same arguments (path tracing is deterministic given
-the seeds and light samples; only the order of the atomic adds differs).
+scenes, cameras, resolutions, sample counts, path lengths and passes (PT,
+LT, BPT) in one wavefront, replayed as a CUDA graph per round. Every PT and
+LT job's image must equal gpugi_render's for the same arguments (the passes
+are deterministic given the seeds and light samples; only the order of the
+atomic adds differs). So must a BPT job's at path length 1: its eye vertices
+connect only to the light samples, which sit at fixed cache slots. Deeper BPT
+connections pick cache entries whose slots follow the atomic order, so there
+the batched and the single-call images agree in distribution.
 """
 import numpy as np
 import pytest
@@ -27,7 +31,7 @@ def scenes3(cuda_ctx):
         x.close()
 
 
-def _jobs(cuda_ctx, scs):
+def _jobs(cuda_ctx, scs, passes=("PT",), bpt_depth=1):
     spec = [  # (scene, W, H, samples, depth, camera)
         (scs[0], 32, 32, 4, 6, scenes.CORNELL_CAMERA),
         (scs[1], 48, 24, 3, 3, ((0.3, 1.2, 3.0), (0.0, 0.8, 0.0), (0.0, 1.0, 0.0), 50.0)),
@@ -35,40 +39,82 @@ def _jobs(cuda_ctx, scs):
     ]
     jobs = []
     for i, (ds, W, H, spp, depth, cam) in enumerate(spec):
-        state = [100 + i]
-        ls = np.stack([render.generate_light_samples(ds, state, 128) for _ in range(spp)])
-        jobs.append(dict(scene=ds, camera=render.camera_lookat(*cam, W, H), image=render.Image(cuda_ctx, W, H),
-                         samples=spp, max_path_length=depth, light_samples=ls, iteration=10 * i))
+        for k, pass_ in enumerate(passes):
+            nls = 128 if pass_ == "PT" else 16
+            state = [100 + i + 10 * k]
+            ls = np.stack([render.generate_light_samples(ds, state, nls) for _ in range(spp)])
+            jobs.append(dict(scene=ds, camera=render.camera_lookat(*cam, W, H), image=render.Image(cuda_ctx, W, H),
+                             pass_=pass_, samples=spp, max_path_length=bpt_depth if pass_ == "BPT" else depth,
+                             num_light_samples=nls, light_samples=ls, iteration=10 * i + k))
     return jobs
 
 
 def _single(cuda_ctx, j):
     img = render.Image(cuda_ctx, j["image"].width, j["image"].height)
-    render.render(cuda_ctx, j["scene"], j["camera"], img, "PT", max_path_length=j["max_path_length"],
-                  samples=j["samples"], iteration=j["iteration"], light_samples=j["light_samples"])
+    render.render(cuda_ctx, j["scene"], j["camera"], img, j["pass_"], max_path_length=j["max_path_length"],
+                  samples=j["samples"], iteration=j["iteration"], num_light_samples=j["num_light_samples"],
+                  light_samples=j["light_samples"])
     out = img.read()
     img.close()
     return out
 
 
-@pytest.mark.parametrize("paths_per_round,use_graph", [(16 << 20, True), (2048, True), (2048, False)])
+@pytest.mark.parametrize("paths_per_round,use_graph", [(16 << 20, True), (4096, True), (4096, False)])
 def test_batch_equals_single_renders(cuda_ctx, scenes3, paths_per_round, use_graph):
     render.set_batch_config(cuda_ctx, paths_per_round, use_graph)
+    jobs = _jobs(cuda_ctx, scenes3, passes=("PT", "LT", "BPT"))
     try:
-        jobs = _jobs(cuda_ctx, scenes3)
         render.render_batch(cuda_ctx, jobs)
         for j in jobs:
             got = j["image"].read()
             expect = _single(cuda_ctx, j)
             assert got.shape == expect.shape
             assert np.allclose(got, expect, rtol=1e-5, atol=1e-6 * np.abs(expect).max()), \
-                np.abs(got - expect).max()
-            assert got[..., :3].mean() > 0
+                (j["pass_"], np.abs(got - expect).max())
+            assert got[..., :3].mean() > 0, j["pass_"]
         assert cuda_ctx.device_error_bits() == 0
     finally:
         render.set_batch_config(cuda_ctx)
         for j in jobs:
             j["image"].close()
+
+
+def test_batch_bpt_agrees_with_single_renders(cuda_ctx, scenes3):
+    """BPT at path length 6 in a batch with PT and LT jobs: over 6 independent
+    iterations, the batched and the single-call estimates of every 8 x 8
+    block and of the image mean agree within 5 standard errors."""
+    render.set_batch_config(cuda_ctx, 1 << 20, True)
+    runs = {"batch": [], "single": []}
+    try:
+        for it in range(6):
+            jobs = _jobs(cuda_ctx, scenes3, passes=("PT", "LT", "BPT"), bpt_depth=6)
+            for j in jobs:
+                j["iteration"] += 1000 * it
+            render.render_batch(cuda_ctx, jobs)
+            j = jobs[2]  # the 32 x 32 BPT job
+            assert j["pass_"] == "BPT"
+            runs["batch"].append(j["image"].read()[..., :3])
+            runs["single"].append(_single(cuda_ctx, j)[..., :3])
+            for x in jobs:
+                x["image"].close()
+        assert cuda_ctx.device_error_bits() == 0
+    finally:
+        render.set_batch_config(cuda_ctx)
+
+    def stats(imgs):
+        b = np.stack(imgs).astype(np.float64)  # (K, 32, 32, 3)
+        blocks = b.reshape(b.shape[0], 4, 8, 4, 8, 3).mean((2, 4))
+        whole = b.mean((1, 2))
+        se = lambda x: x.std(0, ddof=1) / np.sqrt(x.shape[0])
+        return blocks.mean(0), se(blocks), whole.mean(0), se(whole)
+
+    mb, sb, wb, swb = stats(runs["batch"])
+    ms, ss, ws, sws = stats(runs["single"])
+    assert wb.min() > 0
+    z_blocks = np.abs(mb - ms) / np.sqrt(sb ** 2 + ss ** 2 + 1e-30)
+    z_whole = np.abs(wb - ws) / np.sqrt(swb ** 2 + sws ** 2)
+    assert z_blocks.max() < 5.0, z_blocks.max()
+    assert z_whole.max() < 5.0, (wb, ws)
 
 
 def test_batch_runs_other_passes_and_validates(cuda_ctx, scenes3):
@@ -77,20 +123,28 @@ def test_batch_runs_other_passes_and_validates(cuda_ctx, scenes3):
     cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
     state = [5]
     ls = np.stack([render.generate_light_samples(ds, state, 256) for _ in range(2)])
-    lt = render.Image(cuda_ctx, W, H)
-    render.render_batch(cuda_ctx, [dict(scene=ds, camera=cam, image=lt, pass_="LT", samples=2, max_path_length=4,
-                                         light_samples=ls)])
+    # the Whitted ray tracer runs after the fused jobs, one call per job
+    wt = render.Image(cuda_ctx, W, H)
+    render.render_batch(cuda_ctx, [dict(scene=ds, camera=cam, image=wt, pass_="WHITTED", samples=2,
+                                         max_path_length=4, num_light_samples=256, light_samples=ls)])
     ref = render.Image(cuda_ctx, W, H)
-    render.render(cuda_ctx, ds, cam, ref, "LT", max_path_length=4, samples=2, light_samples=ls)
-    assert np.allclose(lt.read(), ref.read(), rtol=1e-5, atol=1e-6 * np.abs(ref.read()).max())
+    render.render(cuda_ctx, ds, cam, ref, "WHITTED", max_path_length=4, samples=2, num_light_samples=256,
+                  light_samples=ls)
+    assert np.allclose(wt.read(), ref.read(), rtol=1e-5, atol=1e-6 * np.abs(ref.read()).max())
+    assert wt.read()[..., :3].mean() > 0
     # an image larger than the path queue is refused
     render.set_batch_config(cuda_ctx, 1024, True)
     big = render.Image(cuda_ctx, 64, 64)
     with pytest.raises(cuda.GpugiError):
         render.render_batch(cuda_ctx, [dict(scene=ds, camera=render.camera_lookat(*scenes.CORNELL_CAMERA, 64, 64),
                                             image=big, rng_state=[1])])
+    # so is an LT sample whose particles and light-sample connections do not fit
+    # (16 light samples x 64 particles + 16 camera connections > 1024)
+    with pytest.raises(cuda.GpugiError):
+        render.render_batch(cuda_ctx, [dict(scene=ds, camera=cam, image=wt, pass_="LT", num_light_samples=16,
+                                            rng_state=[1])])
     render.set_batch_config(cuda_ctx)
-    for x in (lt, ref, big):
+    for x in (wt, ref, big):
         x.close()
 
 
