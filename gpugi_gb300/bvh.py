@@ -46,6 +46,8 @@ def _lib():
         lib.gpugi_materials_from_json.argtypes = [C.c_char_p, P, U32, P]
         lib.gpugi_materials_from_json.restype = I
         lib.gpugi_materials_json_error.restype = C.c_char_p
+        lib.gpugi_bvh_sggx.argtypes = [P, P]
+        lib.gpugi_bvh_sggx.restype = I
         lib.gpugi_bvh_free.argtypes = [P]
         lib.gpugi_bvh_free.restype = None
         lib.gpugi_bvh_last_error.restype = C.c_char_p
@@ -70,6 +72,7 @@ class BVH:
     texcoords: np.ndarray | None = None    # from a file: float32 [V, 2]
     materials: np.ndarray | None = None    # from a file: float32 [M, 24] (empty when absent)
     material_names: list | None = None     # from a file: the "materialref" chunk
+    sggx: np.ndarray | None = None         # uint16 [N, 6] node NDFs {sigma.xyz, r.xyz} ("approx_sggx")
 
     @property
     def num_nodes(self) -> int:
@@ -99,8 +102,17 @@ def _collect(handle) -> BVH:
     return BVH(hier, slots, parents, ls.value, bk.value, md.value)
 
 
+def _sggx(lib, h, num_nodes) -> np.ndarray:
+    out = np.zeros((num_nodes, 6), dtype=np.uint16)
+    if lib.gpugi_bvh_sggx(h, _ptr(out)) != 0:
+        raise ValueError(lib.gpugi_bvh_last_error().decode())
+    return out
+
+
 def build_bvh(positions: np.ndarray, triangles: np.ndarray, method: str = "sweep", fit: str = "aabox",
-              leaf_size: int = 8, seed: int = 1) -> BVH:
+              leaf_size: int = 8, seed: int = 1, normals: np.ndarray | None = None) -> BVH:
+    """Build the hierarchy; with per-vertex normals also the node NDFs
+    (bvhmake's approx_sggx)."""
     lib = _lib()
     pos = np.ascontiguousarray(positions, dtype=np.float32)
     tri = np.ascontiguousarray(triangles, dtype=np.uint32)
@@ -112,6 +124,13 @@ def build_bvh(positions: np.ndarray, triangles: np.ndarray, method: str = "sweep
     try:
         b = _collect(h)
         b.positions = pos
+        if normals is not None:
+            nrm = np.ascontiguousarray(normals, dtype=np.float32)
+            if nrm.shape != (pos.shape[0], 3):
+                raise ValueError("normals need one row per vertex")
+            lib.gpugi_bvh_set_vertex_attributes(h, _ptr(nrm), None)
+            b.normals = nrm
+            b.sggx = _sggx(lib, h, b.num_nodes)
         return b
     finally:
         lib.gpugi_bvh_free(h)
@@ -189,6 +208,13 @@ def read_bvh_file(path: str) -> BVH:
             lib.gpugi_bvh_materials(h, C.byref(nm), _ptr(b.materials))
         b.material_names = [lib.gpugi_bvh_material_name(h, i).decode()
                             for i in range(lib.gpugi_bvh_num_material_names(h))]
+        # node NDFs: the file's approx_sggx chunk, else computed from the normals (when there are any)
+        b.sggx = None
+        if np.any(b.normals):
+            try:
+                b.sggx = _sggx(lib, h, b.num_nodes)
+            except ValueError:
+                b.sggx = None
         return b
     finally:
         lib.gpugi_bvh_free(h)

@@ -173,6 +173,9 @@ struct gpugi_bvh {
     std::vector<uint32_t> leaves;      // leafSize * 4 uint32 per block
     std::vector<uint32_t> escapes, parents;
     uint32_t maxDepth = 0;
+    // "approx_sggx" chunk: 6 uint16 per node (computed from the vertex
+    // normals on first use, or read from a file)
+    mutable std::vector<uint16_t> sggx;
 
     V3 Pos(uint32_t v) const { return V3(positions[3 * v], positions[3 * v + 1], positions[3 * v + 2]); }
     Box TriBox(uint32_t t) const {
@@ -531,11 +534,239 @@ void AssignEscapes(gpugi_bvh& b) {
     }
 }
 
+// --- Node NDFs (bvhmake/processing/approx_sggx.cpp) -------------------------
+// The symmetric SGGX matrix of a node, S = Q^T diag(lambda) Q, from the
+// vertex normals of the triangles below it. Per leaf block: 1000 normals
+// spread over the triangles by area at Halton (2, 3) barycentric points,
+// the eigenvectors Q of their second-moment matrix, and lambda_k the mean
+// |q_k . n| (approx_sggx.cpp:88-154). Inner nodes blend their two children
+// weighted by the children's bounding-volume surfaces (approx_sggx.cpp:
+// 156-184). epsilon's decomposeQl is not available; the eigenvectors come
+// from the cyclic Jacobi method in double precision. S does not depend on
+// the eigenvectors' order or signs (lambda_k pairs with its own q_k), only
+// on their directions, except within a repeated eigenvalue, where the
+// choice of basis can change lambda: parity of these values is unpinned.
+struct Sggx {
+    float xx, xy, xz, yy, yz, zz;
+};
+
+// approx_sggx.cpp:13-25
+inline int HaltonRev(int i, int p) { return i == 0 ? i : p - i; }
+inline float Halton(int base, int i) {
+    float h = 0.0f;
+    const float f = 1.0f / (float)base;
+    float fct = f;
+    while (i > 0) {
+        h += (float)HaltonRev(i % base, base) * fct;
+        i /= base;
+        fct *= f;
+    }
+    return h;
+}
+
+inline float Dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+inline V3 Cross(V3 a, V3 b) { return V3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline V3 Normalize(V3 a) { return a / std::sqrt(Dot(a, a)); }
+// epsilon's surface(Triangle), restated: half the length of the edge cross product.
+inline float TriangleSurface(V3 a, V3 b, V3 c) {
+    V3 n = Cross(b - a, c - a);
+    return std::sqrt(Dot(n, n)) * 0.5f;
+}
+
+// Cyclic Jacobi rotations on a symmetric 3x3 matrix: rows of q are the
+// eigenvectors (Golub & Van Loan, "Matrix Computations", 8.5).
+void SymmetricEigen3(const double in[3][3], double q[3][3]) {
+    double a[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            a[r][c] = in[r][c];
+            q[r][c] = r == c ? 1.0 : 0.0;
+        }
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+        const double diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+        if (off <= 1e-30 * diag || off == 0.0) break;
+        for (int p = 0; p < 2; ++p)
+            for (int r = p + 1; r < 3; ++r) {
+                if (a[p][r] == 0.0) continue;
+                const double theta = (a[r][r] - a[p][p]) / (2.0 * a[p][r]);
+                const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < 3; ++k) {  // A <- A J (columns p, r)
+                    const double akp = a[k][p], akr = a[k][r];
+                    a[k][p] = c * akp - sn * akr;
+                    a[k][r] = sn * akp + c * akr;
+                }
+                for (int k = 0; k < 3; ++k) {  // A <- J^T A (rows p, r)
+                    const double apk = a[p][k], ark = a[r][k];
+                    a[p][k] = c * apk - sn * ark;
+                    a[r][k] = sn * apk + c * ark;
+                }
+                for (int k = 0; k < 3; ++k) {  // eigenvector rows: Q <- J^T Q
+                    const double qp = q[p][k], qr = q[r][k];
+                    q[p][k] = c * qp - sn * qr;
+                    q[r][k] = sn * qp + c * qr;
+                }
+            }
+    }
+}
+
+// ComputeLeafSGGXBase (approx_sggx.cpp:88-154) for leaf block blk.
+Sggx LeafSggx(const gpugi_bvh& b, uint32_t blk) {
+    const int kSamples = 1000;  // NORMAL_SAMPLES
+    std::vector<V3> pos, nrm;
+    for (uint32_t k = 0; k < b.leafSize; ++k) {
+        const uint32_t* t = &b.leaves[4 * ((size_t)blk * b.leafSize + k)];
+        if (t[0] == 0 && t[1] == 0 && t[2] == 0 && t[3] == 0) break;  // INVALID_TRIANGLE
+        for (int v = 0; v < 3; ++v) {
+            pos.push_back(b.Pos(t[v]));
+            nrm.push_back(V3(b.normals[3 * (size_t)t[v]], b.normals[3 * (size_t)t[v] + 1],
+                             b.normals[3 * (size_t)t[v] + 2]));
+        }
+    }
+    const int n = (int)pos.size() / 3;
+    float area = 0.0f;
+    for (int i = 0; i < n; ++i) area += TriangleSurface(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    // The reference interpolates with the second vertex normal twice
+    // (nrm[i*3+1] * gamma, approx_sggx.cpp:114,143); kept.
+    auto sampleNormal = [&](int i, int j) {
+        float al = Halton(2, j), be = Halton(3, j);
+        if (al + be > 1.0f) {
+            al = 1.0f - al;
+            be = 1.0f - be;
+        }
+        const float ga = 1.0f - al - be;
+        return Normalize((nrm[3 * i] * al + nrm[3 * i + 1] * be) + nrm[3 * i + 1] * ga);
+    };
+    auto count = [&](int i) {
+        return (int)((float)kSamples * TriangleSurface(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]) / area);
+    };
+    float E[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int i = 0; i < n; ++i)
+        for (int j = 0, ns = count(i); j < ns; ++j) {
+            const V3 nv = sampleNormal(i, j);
+            E[0][0] += nv.x * nv.x;
+            E[0][1] += nv.x * nv.y;
+            E[0][2] += nv.x * nv.z;
+            E[1][1] += nv.y * nv.y;
+            E[1][2] += nv.y * nv.z;
+            E[2][2] += nv.z * nv.z;
+        }
+    E[1][0] = E[0][1];
+    E[2][0] = E[0][2];
+    E[2][1] = E[1][2];
+    double Ed[3][3], Qd[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Ed[r][c] = E[r][c];
+    SymmetricEigen3(Ed, Qd);
+    V3 q[3];
+    for (int k = 0; k < 3; ++k) q[k] = V3((float)Qd[k][0], (float)Qd[k][1], (float)Qd[k][2]);
+    float lam[3] = {0.0f, 0.0f, 0.0f};
+    int total = 0;
+    for (int i = 0; i < n; ++i) {
+        const int ns = count(i);
+        total += ns;
+        for (int j = 0; j < ns; ++j) {
+            const V3 nv = sampleNormal(i, j);
+            for (int k = 0; k < 3; ++k) lam[k] += std::fabs(Dot(q[k], nv));
+        }
+    }
+    Sggx s{0, 0, 0, 0, 0, 0};
+    if (total == 0) return s;
+    for (int k = 0; k < 3; ++k) lam[k] /= (float)total;
+    float S[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+            S[r][c] = (q[0][r] * lam[0] * q[0][c] + q[1][r] * lam[1] * q[1][c]) + q[2][r] * lam[2] * q[2][c];
+    s.xx = S[0][0];
+    s.xy = S[0][1];
+    s.xz = S[0][2];
+    s.yy = S[1][1];
+    s.yz = S[1][2];
+    s.zz = S[2][2];
+    return s;
+}
+
+// FitMethod::Surface of a node's bounding volume (aaboxfit.cpp:25-28,
+// aaellipsoidfit.cpp:81-84).
+float NodeSurface(const gpugi_bvh& b, uint32_t i) {
+    return b.boundsKind == GPUGI_FIT_ELLIPSOID ? EllipsoidSurface(b.ellipsoids[i]) : BoxSurface(b.boxes[i]);
+}
+
+// The stored form (approx_sggx.cpp:185-187, filedef.hpp:79-95): sigma =
+// sqrt(diagonal) and r = off-diagonal / sqrt(product of the diagonals), as
+// truncated 16-bit integers (r shifted to [0, 65534]). A zero diagonal
+// (division by zero in the reference) stores r = 0.
+void PackSggx(const Sggx& s, uint16_t* o) {
+    auto u16 = [](float v) {
+        if (!(v > 0.0f)) return (uint16_t)0;
+        return v >= 65535.0f ? (uint16_t)65535 : (uint16_t)v;
+    };
+    o[0] = u16(std::sqrt(s.xx) * 65535.0f);
+    o[1] = u16(std::sqrt(s.yy) * 65535.0f);
+    o[2] = u16(std::sqrt(s.zz) * 65535.0f);
+    const float d[3] = {std::sqrt(s.xx * s.yy), std::sqrt(s.xx * s.zz), std::sqrt(s.yy * s.zz)};
+    const float off[3] = {s.xy, s.xz, s.yz};
+    for (int k = 0; k < 3; ++k) o[3 + k] = d[k] > 0.0f ? u16(off[k] / d[k] * 32767.0f + 32767.0f) : (uint16_t)32767;
+}
+
+// ComputeSGGXBases (approx_sggx.cpp:156-203): leaves in parallel, then the
+// inner nodes children-first (reverse preorder).
+void ComputeSggx(const gpugi_bvh& b) {
+    const size_t nn = b.nodes.size();
+    std::vector<Sggx> s(nn);
+    std::vector<uint32_t> leafNodes;
+    for (size_t i = 0; i < nn; ++i)
+        if (b.nodes[i].left & 0x80000000u) leafNodes.push_back((uint32_t)i);
+    const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t)
+        pool.emplace_back([&, t]() {
+            for (size_t k = t; k < leafNodes.size(); k += nt) {
+                const uint32_t i = leafNodes[k];
+                s[i] = LeafSggx(b, b.nodes[i].left & 0x7FFFFFFFu);
+            }
+        });
+    for (auto& th : pool) th.join();
+    for (size_t ii = nn; ii-- > 0;) {
+        const uint32_t left = b.nodes[ii].left;
+        if (left & 0x80000000u) continue;
+        const uint32_t right = b.escapes[left];
+        float lw = NodeSurface(b, left), rw = NodeSurface(b, right);
+        const float wsum = lw + rw;
+        lw /= wsum;
+        rw /= wsum;
+        const Sggx &l = s[left], &r = s[right];
+        s[ii] = Sggx{l.xx * lw + r.xx * rw, l.xy * lw + r.xy * rw, l.xz * lw + r.xz * rw,
+                     l.yy * lw + r.yy * rw, l.yz * lw + r.yz * rw, l.zz * lw + r.zz * rw};
+    }
+    b.sggx.resize(6 * nn);
+    for (size_t i = 0; i < nn; ++i) PackSggx(s[i], &b.sggx[6 * i]);
+}
+
 }  // namespace
 
 extern "C" {
 
 const char* gpugi_bvh_last_error(void) { return g_lastError.c_str(); }
+
+int gpugi_bvh_sggx(const gpugi_bvh* b, uint16_t* out) {
+    if (!b || !out) return -1;
+    if (b->sggx.size() != 6 * b->nodes.size()) {
+        if (b->normals.size() != b->positions.size()) {
+            g_lastError = "node NDFs need the vertex normals (gpugi_bvh_set_vertex_attributes)";
+            return -2;
+        }
+        try {
+            ComputeSggx(*b);
+        } catch (const std::exception& e) {
+            g_lastError = e.what();
+            return -3;
+        }
+    }
+    std::memcpy(out, b->sggx.data(), b->sggx.size() * sizeof(uint16_t));
+    return 0;
+}
 
 int gpugi_bvh_build(const float* positions, uint32_t numVertices, const uint32_t* triangles,
                     uint32_t numTriangles, uint32_t buildMethod, uint32_t fitMethod,
@@ -683,6 +914,11 @@ int gpugi_bvh_write_file(const gpugi_bvh* b, const char* path) {
               WriteChunk(f, "triangles", nBlocks, 16 * b->leafSize, b->leaves.data()) &&
               (b->materials.empty() ||
                WriteChunk(f, "gpugi_materials", (uint32_t)(b->materials.size() / 24), 96, b->materials.data()));
+    // bvhmake's main writes the node NDFs after the hierarchy (main.cpp:143-144)
+    if (ok && (b->sggx.size() == 6 * (size_t)nn || b->normals.size() == 3 * (size_t)nv)) {
+        if (b->sggx.size() != 6 * (size_t)nn) ComputeSggx(*b);
+        ok = WriteChunk(f, "approx_sggx", nn, 12, b->sggx.data());
+    }
     if (ok && !b->materialNames.empty()) {
         std::vector<char> names(b->materialNames.size() * 32, 0);
         for (size_t i = 0; i < b->materialNames.size(); ++i)
@@ -743,6 +979,10 @@ int gpugi_bvh_read_file(const char* path, gpugi_bvh** out) {
             if (h.elementSize != 96) { rc = -4; g_lastError = "gpugi_materials element must be 96 bytes"; break; }
             b->materials.resize((size_t)h.numElements * 24);
             std::memcpy(b->materials.data(), data.data(), bytes);
+        } else if (name == "approx_sggx") {
+            if (h.elementSize != 12) { rc = -4; g_lastError = "approx_sggx element must be 12 bytes"; break; }
+            b->sggx.resize((size_t)h.numElements * 6);
+            std::memcpy(b->sggx.data(), data.data(), bytes);
         } else if (name == "hierarchy") {
             if (h.elementSize != 12) { rc = -4; g_lastError = "hierarchy element must be 12 bytes"; break; }
             hier.resize((size_t)h.numElements * 3);
@@ -766,6 +1006,10 @@ int gpugi_bvh_read_file(const char* path, gpugi_bvh** out) {
     if (rc) return rc;
     if (!haveBV || !haveTris || !haveHier || hier.size() / 3 != bv.size() / 6) {
         g_lastError = "file lacks hierarchy, bounding volumes or triangles";
+        return -5;
+    }
+    if (!b->sggx.empty() && b->sggx.size() != hier.size() * 2) {
+        g_lastError = "approx_sggx does not have one record per node";
         return -5;
     }
     const size_t nn = hier.size() / 3;
@@ -798,6 +1042,7 @@ int gpugi_bvh_set_vertex_attributes(gpugi_bvh* b, const float* normals, const fl
     const size_t nv = b->positions.size() / 3;
     if (normals) b->normals.assign(normals, normals + 3 * nv);
     else b->normals.clear();
+    b->sggx.clear();  // the node NDFs follow the normals
     if (texcoords) b->texcoords.assign(texcoords, texcoords + 2 * nv);
     else b->texcoords.clear();
     return 0;

@@ -70,6 +70,7 @@ constexpr uint32_t DEVERR_TRAVERSAL_CAP = 0x1u;
 constexpr uint32_t DEVERR_QUEUE_OVERFLOW = 0x2u;
 constexpr uint32_t DEVERR_WAIT_TIMEOUT = 0x4u;
 constexpr uint32_t DEVERR_BUILD = 0x8u;  // GPU hierarchy build: a walk to the root exceeded the tree depth bound
+constexpr uint32_t DEVERR_HIERARCHY = 0x10u;  // hierarchy importance: a walk to the root exceeded the node count
 
 GPUGI_D void raise_error(uint32_t* word, uint32_t bits) {
     if (word) atomicOr(word, bits);

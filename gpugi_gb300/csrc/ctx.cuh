@@ -64,6 +64,7 @@ struct PointLight {
 struct DirLight {
     float dir[3], irradiance[3];  // dir points towards the light
 };
+struct HierBuffers;  // hierarchy.cu
 }  // namespace gpugi
 
 struct gpugi_scene {
@@ -84,6 +85,19 @@ struct gpugi_scene {
     std::vector<gpugi::PointLight> pointLights;
     std::vector<float> pointLightSummedFlux;
     std::vector<gpugi::DirLight> dirLights;
+    // Node order on the device: uploaded (preorder) index -> device index;
+    // empty when the two are the same.
+    std::vector<uint32_t> nodeMap;
+    // hierarchy-importance renderer (hierarchy.cu), device node order
+    gpugi::HierBuffers* hier = nullptr;
+};
+
+// Accumulation image (RGBA32F sum, optional FP64 RGB sum).
+struct gpugi_image {
+    gpugi_ctx* ctx = nullptr;
+    uint32_t width = 0, height = 0, flags = 0;
+    float4* rgba = nullptr;
+    double* rgb64 = nullptr;
 };
 
 namespace gpugi {
@@ -157,6 +171,12 @@ void prepare_triangles(cudaStream_t stream, const int4* slots, uint32_t numSlots
 // Light tables and the host light sampler (host.cu).
 void build_light_tables(gpugi_scene* sc);
 void generate_light_samples(gpugi_scene* sc, uint64_t& rng, uint32_t numSamples, float* out);
+// Hierarchy-importance renderer (hierarchy.cu): the GPUGI_PASS_HIERARCHY
+// branch of gpugi_render, and the release of a scene's buffers.
+gpugi_status render_hierarchy(gpugi_ctx* ctx, gpugi_scene* sc, const gpugi_camera* cam,
+                              const gpugi_render_params* p, const float* lightSamples, uint64_t* rngState,
+                              gpugi_image* im);
+void free_hierarchy(gpugi_scene* sc);
 
 }  // namespace gpugi
 

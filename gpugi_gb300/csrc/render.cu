@@ -29,13 +29,6 @@
 #include "shade.cuh"
 #include "trace.cuh"
 
-struct gpugi_image {
-    gpugi_ctx* ctx = nullptr;
-    uint32_t width = 0, height = 0, flags = 0;
-    float4* rgba = nullptr;
-    double* rgb64 = nullptr;
-};
-
 namespace gpugi {
 
 constexpr int kMaxDepth = 64;
@@ -2033,7 +2026,7 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
                           gpugi_image* im) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass > GPUGI_PASS_PM) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->pass > GPUGI_PASS_HIERARCHY) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)
@@ -2044,6 +2037,9 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "scene lacks vertex info or materials");
     if (!lightSamples && !rngState)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "either lightSamples or rngState is required");
+
+    if (p->pass == GPUGI_PASS_HIERARCHY)
+        return render_hierarchy(ctx, const_cast<gpugi_scene*>(sc), cam, p, lightSamples, rngState, im);
 
     const uint32_t numPixels = p->width * p->height;
     const uint32_t raysPerLight = rays_per_light_sample(p);
@@ -2242,7 +2238,7 @@ static gpugi_status check_render_args(gpugi_ctx* ctx, const gpugi_scene* sc, con
                                       const gpugi_render_params* p, const float* lightSamples,
                                       const uint64_t* rngState, const gpugi_image* im) {
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass > GPUGI_PASS_PM) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->pass > GPUGI_PASS_HIERARCHY) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)

@@ -49,7 +49,8 @@ static uint32_t bits_of(float f) {
 // original preorder. Child and escape words are renumbered; leaf words are
 // kept. The walk visits the same logical nodes in the same order, only their
 // addresses change. Returns the number of leading (top) nodes.
-static uint32_t relayout_nodes(std::vector<float>& nodes, uint32_t numNodes, uint32_t maxTop) {
+static uint32_t relayout_nodes(std::vector<float>& nodes, uint32_t numNodes, uint32_t maxTop,
+                               std::vector<uint32_t>& mapOut) {
     std::vector<uint32_t> depth(numNodes, 0);
     uint32_t maxDepth = 0;
     for (uint32_t i = 0; i < numNodes; ++i) {  // preorder: parents precede children
@@ -89,6 +90,7 @@ static uint32_t relayout_nodes(std::vector<float>& nodes, uint32_t numNodes, uin
         std::memcpy(&o[7], &ne, 4);
     }
     nodes.swap(out);
+    mapOut.swap(map);
     return top;
 }
 
@@ -169,7 +171,8 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
             return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "escape must be 0 or point forward (preorder)");
     }
 
-    const uint32_t topNodes = relayout_nodes(nodes, numNodes, ctx->sharedNodes);
+    std::vector<uint32_t> nodeMap;  // uploaded index -> device index (empty: the same)
+    const uint32_t topNodes = relayout_nodes(nodes, numNodes, ctx->sharedNodes, nodeMap);
 
     cudaError_t se = cudaSetDevice(ctx->device);
     if (se != cudaSuccess) return cuda_fail(ctx, se, "cudaSetDevice");
@@ -216,6 +219,7 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     sc->dev.numVertices = numVertices;
     sc->dev.numMaterials = numMaterials;
     sc->dev.topNodes = topNodes;
+    sc->nodeMap.swap(nodeMap);
     sc->hostPositions.assign(positions, positions + 3 * (size_t)numVertices);
     sc->hostSlots.assign(slots, slots + 4 * (size_t)numSlots);
     if (numMaterials)
@@ -229,6 +233,7 @@ extern "C" void gpugi_scene_destroy(gpugi_scene* sc) {
     if (!sc) return;
     if (sc->ctx) cudaStreamSynchronize(sc->ctx->stream);
     detach_child(&sc->ctx);
+    free_hierarchy(sc);
     for (void* p : sc->allocations) cudaFree(p);
     delete sc;
 }

@@ -54,6 +54,9 @@ def _declare(L):
     L.gpugi_debug_raise_device_error.argtypes = [P, U32]
     L.gpugi_scene_build.argtypes = [P, P, U32, P, U32, P, P, U32, U32, C.POINTER(P)]
     L.gpugi_scene_export.argtypes = [P, P, C.POINTER(U32), C.POINTER(U32), P, P]
+    L.gpugi_scene_set_hierarchy_ndf.argtypes = [P, P, P]
+    L.gpugi_hierarchy_importance.argtypes = [P, P, P, U32, U32, P, U32, U32]
+    L.gpugi_hierarchy_read.argtypes = [P, P, P, P, P]
     for name in ("gpugi_trace_closest", "gpugi_trace_closest_device"):
         getattr(L, name).argtypes = [P, P] + [P] * 7 + [U64] + [P] * 4
     for name in ("gpugi_trace_any", "gpugi_trace_any_device"):
@@ -231,6 +234,31 @@ class DeviceScene:
         parents[hier[left, 7].view(np.uint32)] = inner
         return B.BVH(hierarchy=hier, slots=slots, parents=parents, leaf_size=self.leaf_size, bounds_kind=0,
                      max_depth=0)
+
+    def set_hierarchy_ndf(self, sggx: np.ndarray) -> None:
+        """Node NDFs (uint16 [numNodes, 6], bvhmake's approx_sggx in the
+        uploaded node order) and the node materials of the hierarchy-
+        importance renderer."""
+        a = np.ascontiguousarray(sggx, dtype=np.uint16)
+        if a.shape != (self.num_nodes, 6):
+            raise ValueError("sggx must be uint16 [numNodes, 6]")
+        self.ctx.check(lib().gpugi_scene_set_hierarchy_ndf(self.ctx.handle, self._h, _ptr(a)))
+
+    def hierarchy_importance(self, camera, width: int, height: int, light_samples: np.ndarray,
+                             iterations: int = 10) -> None:
+        """The importance pass (acquisition + propagation) with one light-sample set."""
+        ls = np.ascontiguousarray(light_samples, dtype=np.float32).reshape(-1, 8)
+        self.ctx.check(lib().gpugi_hierarchy_importance(self.ctx.handle, self._h, C.byref(camera), width, height,
+                                                        _ptr(ls), ls.shape[0], iterations))
+
+    def hierarchy_read(self):
+        """(importance float32 [numNodes + numSlots, 2], subtree float32
+        [numNodes], node materials uint32 [numNodes, 12]) in the uploaded order."""
+        imp = np.zeros((self.num_nodes + self.num_slots, 2), np.float32)
+        sub = np.zeros(self.num_nodes, np.float32)
+        mats = np.zeros((self.num_nodes, 12), np.uint32)
+        self.ctx.check(lib().gpugi_hierarchy_read(self.ctx.handle, self._h, _ptr(imp), _ptr(sub), _ptr(mats)))
+        return imp, sub, mats
 
     @property
     def handle(self):

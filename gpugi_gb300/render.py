@@ -11,10 +11,10 @@ import numpy as np
 
 from . import cuda
 
-PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3, "PM": 4}
+PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3, "PM": 4, "HIERARCHY": 5}
 # Initial light samples per iteration as each renderer configures them
 # (pathtracer.cpp:28, lightpathtracer.cpp:16, bidirectionalpathtracer.cpp:160).
-DEFAULT_LIGHT_SAMPLES = {"PT": 128, "LT": 256, "BPT": 128, "WHITTED": 128, "PM": 128}
+DEFAULT_LIGHT_SAMPLES = {"PT": 128, "LT": 256, "BPT": 128, "WHITTED": 128, "PM": 128, "HIERARCHY": 128}
 
 
 class Camera(C.Structure):

@@ -16,6 +16,9 @@
  *   gpugi_bvh_write_file  replaces the NamedArray export of bvhmake's main
  *   gpugi_bvh_read_file                                         (bvhmake/main.cpp:27-146,
  *                                                                documentation/fileformat.tex)
+ *   gpugi_bvh_sggx        replaces ComputeSGGXBases + BVHBuilder::ExportApproximation
+ *                                                               (bvhmake/processing/approx_sggx.cpp:88-203,
+ *                                                                bvhmake/bvhbuilder.cpp:557-567)
  *
  * Conventions: 0 = OK, negative = error (see gpugi_bvh_last_error). The
  * caller owns every array passed in; the handle owns the built tree.
@@ -67,6 +70,15 @@ int gpugi_bvh_vertices(const gpugi_bvh* bvh, uint32_t* numVertices, float* posit
  * array may be NULL: zeros are written); read after gpugi_bvh_read_file. */
 int gpugi_bvh_set_vertex_attributes(gpugi_bvh* bvh, const float* normals, const float* texcoords);
 int gpugi_bvh_vertex_attributes(const gpugi_bvh* bvh, float* normals, float* texcoords);
+
+/* Node NDFs ("approx_sggx" chunk, FileDecl::SGGX of bvhmake/filedef.hpp:
+ * 79-95): 6 uint16 per node {sigma.xyz, r.xyz}; sigma = sqrt(S_ii) as
+ * unorm16, r = S_ij / sqrt(S_ii S_jj) mapped to [0, 65534] (S_xy, S_xz,
+ * S_yz), S the node's SGGX matrix fitted to the vertex normals below it.
+ * Computed from the vertex normals (gpugi_bvh_set_vertex_attributes) on
+ * first use, or taken from a file's chunk; gpugi_bvh_write_file writes the
+ * chunk whenever normals or NDFs are present, as bvhmake does. */
+int gpugi_bvh_sggx(const gpugi_bvh* bvh, uint16_t* out);
 
 /* Material records carried in an extra "gpugi_materials" chunk (24 floats
  * each, the gpugi_material layout of gpugi_cuda.h). No counterpart in the

@@ -48,6 +48,7 @@ typedef enum gpugi_status {
 #define GPUGI_DEVERR_QUEUE_OVERFLOW 0x2u  /* a wavefront queue or light cache overflowed */
 #define GPUGI_DEVERR_WAIT_TIMEOUT 0x4u    /* a bounded device wait ran out */
 #define GPUGI_DEVERR_BUILD 0x8u           /* the GPU hierarchy build found an inconsistent tree */
+#define GPUGI_DEVERR_HIERARCHY 0x10u      /* a hierarchy-importance walk to the root exceeded the node count */
 
 enum gpugi_bounds_kind { GPUGI_BOUNDS_AABB = 0, GPUGI_BOUNDS_ELLIPSOID = 1 };
 
@@ -225,10 +226,24 @@ gpugi_status gpugi_set_scene_layout(gpugi_ctx* ctx, uint32_t sharedNodes, uint32
  *                             distribution, gather (gpugi/renderer/photonmapper.cpp:79-114,
  *                             gpugi/shader/photonmapper/{photondistribution,gather}.comp);
  *                             one photon map per iteration, see gpugi_set_photon_config
+ *   gpugi_render(pass = HIERARCHY)  HierarchyImportance::Draw (gpugi/renderer/
+ *                             hierarchyimportance.cpp:83-114): at iteration 0 the importance
+ *                             pass (see gpugi_hierarchy_importance) with the call's first
+ *                             light-sample set at the image size, then per sample
+ *                             hierarchy/hierarchypathtracer.comp; needs an AABB hierarchy and
+ *                             the node NDFs (gpugi_scene_set_hierarchy_ndf); maxPathLength is
+ *                             the shader's MAX_PATHLENGTH (4 in the reference)
  * ------------------------------------------------------------------------ */
 typedef struct gpugi_image gpugi_image;
 
-enum gpugi_pass { GPUGI_PASS_PT = 0, GPUGI_PASS_LT = 1, GPUGI_PASS_BPT = 2, GPUGI_PASS_WHITTED = 3, GPUGI_PASS_PM = 4 };
+enum gpugi_pass {
+    GPUGI_PASS_PT = 0,
+    GPUGI_PASS_LT = 1,
+    GPUGI_PASS_BPT = 2,
+    GPUGI_PASS_WHITTED = 3,
+    GPUGI_PASS_PM = 4,
+    GPUGI_PASS_HIERARCHY = 5
+};
 
 /* Camera UBO (gpugi/shader/globaluniforms.glsl:7-15): U, V scaled by
  * tan(fov/2)*aspect and tan(fov/2), W unit view direction. */
@@ -404,6 +419,40 @@ gpugi_status gpugi_set_batch_config(gpugi_ctx* ctx, uint32_t pathsPerRound, uint
  * 2.01 x radius) and Knaus-Zwicker radius shrinking per iteration (default 0). */
 gpugi_status gpugi_set_photon_config(gpugi_ctx* ctx, uint32_t photonsPerLightSample, float queryRadius,
                                      uint32_t progressive);
+
+/* Hierarchy-importance renderer (HierarchyImportance, gpugi/renderer/
+ * hierarchyimportance.cpp). AABB hierarchies only: the reference's
+ * importance shaders test box (or oriented-box) nodes.
+ *
+ * gpugi_scene_set_hierarchy_ndf  HierarchyImportance::SetScene: the node NDFs
+ *     (bvhmake's "approx_sggx" chunk, 6 uint16 per node in the uploaded node
+ *     order, see gpugi_bvh_sggx) and the node materials of
+ *     ComputeHierarchyMaterials (hierarchyimportance.cpp:136-160): area-
+ *     weighted averages of the triangles' materials below each node, stored
+ *     as packed halves (sampleleafmaterials.comp, pullmaterials.comp).
+ * gpugi_hierarchy_importance  the importance pass of HierarchyImportance::Draw
+ *     (hierarchyimportance.cpp:83-109): `iterations` passes of
+ *     acquisition2.comp (one path of up to 8 vertices per pixel, each vertex
+ *     with one next-event ray; every node entered and every triangle hit adds
+ *     the path importance, halved per vertex) numbered 1..iterations, then
+ *     the propagation (hierarchypropagation_init.comp, _nodes.comp): per node
+ *     x = mean importance, subtree = importance of its children, y =
+ *     (x / subtree)^2 x mean face area. The init shader reads the node's
+ *     minimum corner from an undeclared variable (hierarchypropagation_init.
+ *     comp:59); the node's first texel is used, as in the nodes shader.
+ * gpugi_hierarchy_read  copies of the results in the uploaded node order:
+ *     importance {x, y} per node then per leaf slot (2 x (numNodes + numSlots)
+ *     floats), subtree importance per node, and the node materials (12 uint32
+ *     per node: six pairs of halves {Reflectiveness.xy}, {.zw}, {Opacity.xy},
+ *     {Opacity.z, area}, {Diffuse.xy}, {Diffuse.z, 0}, {Emissivity.xy},
+ *     {Emissivity.z, 0}, {Fresnel0.xy}, {Fresnel0.z, RefractionIndexAvg},
+ *     {Fresnel1.xy}, {Fresnel1.z, 0}). Any pointer may be NULL. */
+gpugi_status gpugi_scene_set_hierarchy_ndf(gpugi_ctx* ctx, gpugi_scene* scene, const uint16_t* sggx);
+gpugi_status gpugi_hierarchy_importance(gpugi_ctx* ctx, gpugi_scene* scene, const gpugi_camera* camera,
+                                        uint32_t width, uint32_t height, const float* lightSamples,
+                                        uint32_t numLightSamples, uint32_t iterations);
+gpugi_status gpugi_hierarchy_read(gpugi_ctx* ctx, const gpugi_scene* scene, float* importance, float* subtree,
+                                  uint32_t* materials);
 
 /* Autotuner. No counterpart in the reference (its launch shapes are fixed
  * local sizes, e.g. gpugi/renderer/pathtracer.cpp:11). Times candidates on

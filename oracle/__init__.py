@@ -141,6 +141,115 @@ def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.nda
     return accum
 
 
+def _render_scene_args(bvh, scene):
+    from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
+    hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
+    slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
+    pos = np.ascontiguousarray(scene["positions"], dtype=np.float32)
+    vi = np.ascontiguousarray(vertex_info(scene["normals"], scene["texcoords"]), dtype=np.float32)
+    mats = np.ascontiguousarray(scene["materials"], dtype=np.float32)
+    keep = (hier, slots, pos, vi, mats)
+    return keep, [_p(hier), hier.shape[0], _p(slots), slots.shape[0], bvh.leaf_size, _p(pos), _p(vi),
+                  pos.shape[0], _p(mats), mats.shape[0]]
+
+
+_SCENE_T = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
+            C.c_void_p, C.c_uint32]
+
+
+def hier_importance(bvh, scene: dict, width: int, height: int, camera: np.ndarray, light_samples: np.ndarray,
+                    iterations: int = 10, num_threads=None):
+    """HierarchyImportance's importance pass (acquisition2.comp x iterations,
+    then the propagation) on an AABB hierarchy: returns (importance
+    float32 [numNodes + numSlots, 2], subtree float32 [numNodes])."""
+    assert bvh.bounds_kind == 0
+    L = lib()
+    I = C.c_int
+    L.oracle_hier_importance.argtypes = _SCENE_T + [I, I, C.c_void_p, C.c_void_p, I, I, C.c_void_p, C.c_void_p, I]
+    L.oracle_hier_importance.restype = I
+    keep, sargs = _render_scene_args(bvh, scene)
+    cam = np.ascontiguousarray(camera, dtype=np.float32)
+    ls = np.ascontiguousarray(light_samples, dtype=np.float32).reshape(-1, 8)
+    imp = np.zeros((bvh.num_nodes + bvh.num_slots, 2), np.float32)
+    sub = np.zeros(bvh.num_nodes, np.float32)
+    rc = L.oracle_hier_importance(*sargs, width, height, _p(cam), _p(ls), ls.shape[0], iterations, _p(imp), _p(sub),
+                                  threads() if num_threads is None else num_threads)
+    assert rc == 0
+    return imp, sub
+
+
+def hier_propagate(bvh, importance: np.ndarray, iterations: int):
+    """The propagation alone: importance [numNodes + numSlots, 2] with the
+    accumulated x; returns (importance with x / iterations and y, subtree)."""
+    L = lib()
+    L.oracle_hier_propagate.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,
+                                        C.c_void_p, C.c_void_p]
+    L.oracle_hier_propagate.restype = C.c_int
+    hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
+    slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
+    imp = np.array(importance, dtype=np.float32, copy=True, order="C")
+    sub = np.zeros(bvh.num_nodes, np.float32)
+    assert L.oracle_hier_propagate(_p(hier), hier.shape[0], _p(slots), slots.shape[0], bvh.leaf_size, iterations,
+                                   _p(imp), _p(sub)) == 0
+    return imp, sub
+
+
+def hier_materials(bvh, scene: dict) -> np.ndarray:
+    """Node materials (sampleleafmaterials.comp + pullmaterials.comp):
+    uint32 [numNodes, 12], six pairs of packed halves per node."""
+    L = lib()
+    L.oracle_hier_materials.argtypes = _SCENE_T + [C.c_void_p]
+    L.oracle_hier_materials.restype = C.c_int
+    keep, sargs = _render_scene_args(bvh, scene)
+    out = np.zeros((bvh.num_nodes, 12), np.uint32)
+    assert L.oracle_hier_materials(*sargs, _p(out)) == 0
+    return out
+
+
+def render_hier(bvh, scene: dict, width: int, height: int, camera: np.ndarray, frame_seed: int,
+                light_samples: np.ndarray, importance: np.ndarray, materials: np.ndarray, sggx: np.ndarray,
+                max_path_length: int = 4, sky=(0.0, 0.0, 0.0), accum: np.ndarray | None = None,
+                num_threads=None) -> np.ndarray:
+    """One iteration of hierarchypathtracer.comp, accumulated into accum (H, W, 4)."""
+    L = lib()
+    I = C.c_int
+    L.oracle_render_hier.argtypes = _SCENE_T + [I, I, I, C.c_void_p, C.c_uint32, C.c_void_p, I, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, I]
+    L.oracle_render_hier.restype = I
+    keep, sargs = _render_scene_args(bvh, scene)
+    cam = np.ascontiguousarray(camera, dtype=np.float32)
+    ls = np.ascontiguousarray(light_samples, dtype=np.float32).reshape(-1, 8)
+    imp = np.ascontiguousarray(importance, dtype=np.float32)
+    mats = np.ascontiguousarray(materials, dtype=np.uint32)
+    sg = np.ascontiguousarray(sggx, dtype=np.uint16)
+    skya = np.asarray(sky, dtype=np.float32)
+    if accum is None:
+        accum = np.zeros((height, width, 4), np.float32)
+    rc = L.oracle_render_hier(*sargs, width, height, max_path_length, _p(cam), frame_seed & 0xFFFFFFFF, _p(ls),
+                              ls.shape[0], _p(skya), _p(imp), _p(mats), _p(sg), _p(accum),
+                              threads() if num_threads is None else num_threads)
+    assert rc == 0
+    return accum
+
+
+def float_to_half(x: np.ndarray) -> np.ndarray:
+    L = lib()
+    L.oracle_float_to_half.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty(x.shape, np.uint16)
+    L.oracle_float_to_half(_p(x), _p(out), x.size)
+    return out
+
+
+def half_to_float(h: np.ndarray) -> np.ndarray:
+    L = lib()
+    L.oracle_half_to_float.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+    h = np.ascontiguousarray(h, dtype=np.uint16)
+    out = np.empty(h.shape, np.float32)
+    L.oracle_half_to_float(_p(h), _p(out), h.size)
+    return out
+
+
 def algorithmic_bytes(counters: np.ndarray, any_hit: bool = False) -> np.ndarray:
     """Bytes per ray of gpugi's own fetch pattern: 24 (ray in) + 16 (t, id, u, v
     out; 4 for any-hit) + 32 per node + 16 per leaf slot + 36 per valid triangle

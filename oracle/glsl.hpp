@@ -83,6 +83,8 @@ inline vec3& operator*=(vec3& a, float s) { a = a * s; return a; }
 inline vec3& operator/=(vec3& a, float s) { a = a / s; return a; }
 inline vec3& operator/=(vec3& a, vec3 b) { a = a / b; return a; }
 inline vec4 operator+(vec4 a, vec4 b) { return vec4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+inline vec4 operator*(vec4 a, float s) { return vec4(a.x * s, a.y * s, a.z * s, a.w * s); }
+inline vec4 operator/(vec4 a, float s) { return vec4(a.x / s, a.y / s, a.z / s, a.w / s); }
 
 inline float min(float a, float b) { return std::fmin(a, b); }
 inline float max(float a, float b) { return std::fmax(a, b); }

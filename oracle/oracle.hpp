@@ -58,6 +58,13 @@ void TraceRay(const Scene& s, const Ray& ray, float& rayLength, HitRecord& hit,
 // Any hit: restates TraceRayAnyHit (traceray.glsl:18-23 with ANY_HIT).
 bool TraceRayAnyHit(const Scene& s, const Ray& ray, float rayLength, TraceCounters* counters);
 
+// FetchIntersectBoxNode (intersectiontests.glsl:100-111) of an AABB node:
+// entry and exit distances, child code, escape and the squared diagonal.
+bool FetchIntersectBoxNode(const Scene& s, glsl::vec3 origin, glsl::vec3 invRayDir, int nodeIdx, float& firstHit,
+                           float& lastHit, uint32_t& childCode, int& escape, float& nodeSizeSq);
+// IntersectTriangle (intersectiontests.glsl:63-79) with the triangle of a leaf slot.
+bool IntersectSlot(const Scene& s, const Ray& ray, int slot, float& hit, glsl::vec3& bary, glsl::ivec4& triangle);
+
 // Thread pool helper: runs fn(begin, end) over [0, n) split into contiguous ranges.
 template <typename F>
 void ParallelFor(uint64_t n, int numThreads, F fn);

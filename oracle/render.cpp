@@ -867,6 +867,576 @@ static vec3 BidirPixel(const RenderScene& s, const Params& P, const LightCache& 
 
 using namespace oracle;
 
+namespace oracle {
+
+// ------------------------------------------------- hierarchy importance
+// HierarchyImportance (gpugi/renderer/hierarchyimportance.cpp:83-160) on AABB
+// hierarchies: importance acquisition (hierarchy/acquisition2.comp with
+// hierarchy/counthits.glsl), propagation (hierarchy/hierarchypropagation_
+// init.comp and _nodes.comp), node materials (hierarchy/sampleleafmaterials
+// .comp, pullmaterials.comp), node NDFs (hierarchy/sggx.glsl) and the path
+// tracer that stops at well-approximated nodes (hierarchy/hierarchypathtracer
+// .comp with traceray.glsl's TRACERAY_IMPORTANCE_BREAK). The importance
+// buffer holds {x, y} per node, then {x, y} per leaf slot.
+
+static const float kNotificationBias = 1.19e-07f;  // hierarchypropagation_init.comp:18
+
+// IEEE binary16 conversions with round-to-nearest-even (packHalf2x16 /
+// unpackHalf2x16; GLSL leaves the rounding of packHalf2x16 open).
+static uint16_t FloatToHalf(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u, a = x & 0x7FFFFFFFu;
+    if (a >= 0x7F800000u) return (uint16_t)(sign | (a > 0x7F800000u ? 0x7E00u : 0x7C00u));
+    if (a >= 0x477FF000u) return (uint16_t)(sign | 0x7C00u);  // >= 65520 rounds to infinity
+    const int e = (int)(a >> 23) - 127;
+    if (e >= -14) {
+        const uint32_t mant = a & 0x7FFFFFu, rem = mant & 0x1FFFu;
+        uint32_t h = ((uint32_t)(e + 15) << 10) | (mant >> 13);
+        if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
+        return (uint16_t)(sign | h);
+    }
+    if (e < -25) return (uint16_t)sign;
+    const uint32_t mant = (a & 0x7FFFFFu) | 0x800000u;
+    const int shift = -e - 1;  // 14..24
+    uint32_t h = mant >> shift;
+    const uint32_t rem = mant & ((1u << shift) - 1u), half = 1u << (shift - 1);
+    if (rem > half || (rem == half && (h & 1u))) ++h;
+    return (uint16_t)(sign | h);
+}
+static float HalfToFloat(uint16_t h) {
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16, e = (h >> 10) & 0x1Fu, m = h & 0x3FFu;
+    uint32_t x;
+    if (e == 0) {
+        const float v = (float)m * 5.9604644775390625e-8f;  // m * 2^-24, exact
+        std::memcpy(&x, &v, 4);
+        x |= sign;
+    } else if (e == 31) {
+        x = sign | 0x7F800000u | (m << 13);
+    } else {
+        x = sign | ((e + 112u) << 23) | (m << 13);
+    }
+    float f;
+    std::memcpy(&f, &x, 4);
+    return f;
+}
+static uint packHalf2x16(vec2 v) { return (uint)FloatToHalf(v.x) | ((uint)FloatToHalf(v.y) << 16); }
+static vec2 unpackHalf2x16(uint p) { return vec2(HalfToFloat((uint16_t)(p & 0xFFFFu)), HalfToFloat((uint16_t)(p >> 16))); }
+
+static inline uint NodeChild(const Scene& s, int i) { return floatBitsToUint(s.hierarchy[2 * i].w); }
+static inline int NodeEscape(const Scene& s, int i) { return floatBitsToInt(s.hierarchy[2 * i + 1].w); }
+
+// TraceRayCountHits (hierarchy/counthits.glsl:1-71): every node entered and
+// every triangle hit up to rayLength gains the path importance.
+static void TraceRayCountHits(const Scene& s, const Ray& ray, float rayLength, float pathImportance, float* imp) {
+    const int TRIANGLES_PER_LEAF = (int)s.leafSize;
+    int currentNodeIndex = 0, currentLeafIndex = 0;
+    vec3 invRayDir = 1.0f / ray.Direction;
+    bool nextIsLeafNode = false;
+    uint64_t guard = (uint64_t)s.numNodes + (uint64_t)s.numSlots + 2;
+    do {
+        if (guard-- == 0) return;
+        if (!nextIsLeafNode) {
+            float newHit, exitDist, nodeSizeSq;
+            uint childCode;
+            int escape;
+            if (FetchIntersectBoxNode(s, ray.Origin, invRayDir, currentNodeIndex, newHit, exitDist, childCode, escape,
+                                      nodeSizeSq) && newHit <= rayLength) {
+                imp[2 * currentNodeIndex] += pathImportance;
+                currentNodeIndex = int(childCode & 0x7FFFFFFFu);
+                nextIsLeafNode = (uint)currentNodeIndex != childCode;
+                if (nextIsLeafNode) {
+                    currentLeafIndex = TRIANGLES_PER_LEAF * currentNodeIndex;
+                    currentNodeIndex = escape;
+                }
+            } else {
+                currentNodeIndex = escape;
+            }
+        }
+        if (nextIsLeafNode) {
+            ivec4 triangle = s.triangles[currentLeafIndex];
+            if (triangle.x == triangle.y) {
+                nextIsLeafNode = false;
+            } else {
+                float newHit;
+                vec3 bary;
+                if (IntersectSlot(s, ray, currentLeafIndex, newHit, bary, triangle) && newHit <= rayLength)
+                    imp[2 * ((int64_t)s.numNodes + currentLeafIndex)] += pathImportance;
+                ++currentLeafIndex;
+                nextIsLeafNode = (currentLeafIndex % TRIANGLES_PER_LEAF) != 0;
+            }
+        }
+    } while (currentNodeIndex != 0 || nextIsLeafNode);
+}
+
+// acquisition2.comp:26-112 (NEXT_EVENT_IMPORTANCE, one light sample, path
+// length 8, no Russian roulette) for one pixel of iteration `iteration`.
+static void AcquirePixel(const RenderScene& s, const Params& P, int iteration, int x, int y, float* imp) {
+    uint seed = InitRandomSeed(wanghash((uint)iteration), (uint)(x + y * P.width));
+    vec2 screen = (Random2(seed) + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
+    float pathImportance = 1.0f;
+    Ray ray;
+    ray.Origin = P.camPos;
+    ray.Direction = normalize(screen.x * P.camU + screen.y * P.camV + P.camW);
+    for (int i = 0; i < 8; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        TraceRayCountHits(s.geo, ray, rayHit * 1.000001f, pathImportance, imp);
+        if (rayHit == RAY_MAX) break;
+        vec3 hitNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        pathImportance *= 0.5f;
+        int sampleIndex = int(RandomUInt(seed) % (uint)P.numLightSamples);
+        vec4 pn0 = P.lightSamples[2 * sampleIndex], in1 = P.lightSamples[2 * sampleIndex + 1];
+        Ray lightRay;
+        lightRay.Direction = pn0.xyz() - ray.Origin;
+        float lightDistSq = dot(lightRay.Direction, lightRay.Direction);
+        float lightDist = sqrt(lightDistSq);
+        lightRay.Direction /= lightDist;
+        vec3 lightSampleDir = UnpackNormal(vec2(pn0.w, in1.w));
+        float f = saturate(dot(lightSampleDir, -lightRay.Direction));
+        if (f > 0.0f) {
+            lightRay.Origin = ray.Origin;
+            HitRecord lh;
+            float lr = lightDist;
+            TraceRay(s.geo, lightRay, lr, lh, nullptr);
+            if (lr < lightDist) TraceRayCountHits(s.geo, lightRay, lr * 1.000001f, pathImportance, imp);
+        }
+        vec3 throughput(1.0f);
+        float pdf;
+        ray.Direction = SampleBSDFImpl(ray.Direction, m, seed, hitNormal, throughput, false, pdf, nullptr);
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+    }
+}
+
+// hierarchypropagation_init.comp + _nodes.comp, run to convergence: the
+// nodes pass fills a node once all its children are filled, so one pass
+// over the nodes children-first (reverse preorder) gives the same values.
+// The init shader reads the node's minimum corner from an undeclared
+// `hierarchy0` (init.comp:59; the shader does not compile for AABB
+// hierarchies); it is the node's first texel, as in the nodes shader.
+static float NodeAvgArea(const Scene& s, int i) {
+    vec3 sides = s.hierarchy[2 * i + 1].xyz() - s.hierarchy[2 * i].xyz();
+    return (sides.x * sides.y + sides.x * sides.z + sides.y * sides.z) * 2.0f / 6.0f;
+}
+static void PropagateImportance(const Scene& s, int iterations, float* imp, float* subtree) {
+    const int n = (int)s.numNodes;
+    for (int i = 0; i < n; ++i) {
+        imp[2 * i] /= (float)iterations;
+        imp[2 * i + 1] = 0.0f;
+        subtree[i] = 0.0f;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        const uint childCode = NodeChild(s, i);
+        float childrenImportance = 0.0f;
+        if (childCode & 0x80000000u) {
+            int t = (int)s.leafSize * (int)(childCode & 0x7FFFFFFFu);
+            for (int k = 0; k < (int)s.leafSize; ++k, ++t) childrenImportance += imp[2 * ((int64_t)n + t)];
+            childrenImportance /= (float)iterations;
+            subtree[i] = max(childrenImportance, kNotificationBias);
+        } else {
+            int c = (int)childCode;
+            while (true) {
+                childrenImportance += subtree[c];
+                c = NodeEscape(s, c);
+                if (c == 0) break;
+                // continue while i is the child's parent: the next sibling of
+                // a binary node's first child is its second child
+                if (c != NodeEscape(s, (int)childCode)) break;
+            }
+            subtree[i] = childrenImportance;
+        }
+        float approximation = imp[2 * i] / childrenImportance;
+        imp[2 * i + 1] = approximation * approximation * NodeAvgArea(s, i);
+    }
+}
+
+// sampleleafmaterials.comp / pullmaterials.comp: area-weighted node
+// materials as 6 uvec2 of packed halves per node; area in Opacity.y's upper half.
+static void StoreHierMaterial(uint* o, const MaterialData& m, float area) {
+    o[0] = packHalf2x16(vec2(m.Reflectiveness.x, m.Reflectiveness.y));
+    o[1] = packHalf2x16(vec2(m.Reflectiveness.z, m.Reflectiveness.w));
+    o[2] = packHalf2x16(vec2(m.Opacity.x, m.Opacity.y));
+    o[3] = packHalf2x16(vec2(m.Opacity.z, area));
+    o[4] = packHalf2x16(vec2(m.Diffuse.x, m.Diffuse.y));
+    o[5] = packHalf2x16(vec2(m.Diffuse.z, 0.0f));
+    o[6] = packHalf2x16(vec2(m.Emissivity.x, m.Emissivity.y));
+    o[7] = packHalf2x16(vec2(m.Emissivity.z, 0.0f));
+    o[8] = packHalf2x16(vec2(m.Fresnel0.x, m.Fresnel0.y));
+    o[9] = packHalf2x16(vec2(m.Fresnel0.z, m.RefractionIndexAvg));
+    o[10] = packHalf2x16(vec2(m.Fresnel1.x, m.Fresnel1.y));
+    o[11] = packHalf2x16(vec2(m.Fresnel1.z, 0.0f));
+}
+static MaterialData LoadHierMaterial(const uint* o) {
+    MaterialData m;
+    vec2 a = unpackHalf2x16(o[0]), b = unpackHalf2x16(o[1]);
+    m.Reflectiveness = vec4(a.x, a.y, b.x, b.y);
+    a = unpackHalf2x16(o[2]);
+    b = unpackHalf2x16(o[3]);
+    m.Opacity = vec3(a.x, a.y, b.x);
+    a = unpackHalf2x16(o[4]);
+    m.Diffuse = vec3(a.x, a.y, unpackHalf2x16(o[5]).x);
+    a = unpackHalf2x16(o[6]);
+    m.Emissivity = vec3(a.x, a.y, unpackHalf2x16(o[7]).x);
+    a = unpackHalf2x16(o[8]);
+    b = unpackHalf2x16(o[9]);
+    m.Fresnel0 = vec3(a.x, a.y, b.x);
+    m.RefractionIndexAvg = b.y;
+    a = unpackHalf2x16(o[10]);
+    m.Fresnel1 = vec3(a.x, a.y, unpackHalf2x16(o[11]).x);
+    return m;
+}
+static void HierarchyMaterials(const RenderScene& rs, uint* out) {
+    const Scene& s = rs.geo;
+    for (int i = (int)s.numNodes - 1; i >= 0; --i) {
+        const uint childCode = NodeChild(s, i);
+        MaterialData mat;
+        mat.Reflectiveness = vec4(0.0f, 0.0f, 0.0f, 0.0f);
+        mat.Opacity = mat.Diffuse = mat.Emissivity = mat.Fresnel0 = mat.Fresnel1 = vec3(0.0f);
+        mat.RefractionIndexAvg = 0.0f;
+        float area = 0.0f;
+        if (childCode & 0x80000000u) {
+            const int base = (int)s.leafSize * (int)(childCode & 0x7FFFFFFFu);
+            for (int k = 0; k < (int)s.leafSize; ++k) {
+                ivec4 t = s.triangles[base + k];
+                if (t.x == t.y) break;
+                vec3 p0 = vec3(s.positions[3 * t.x], s.positions[3 * t.x + 1], s.positions[3 * t.x + 2]);
+                vec3 p1 = vec3(s.positions[3 * t.y], s.positions[3 * t.y + 1], s.positions[3 * t.y + 2]);
+                vec3 p2 = vec3(s.positions[3 * t.z], s.positions[3 * t.z + 1], s.positions[3 * t.z + 2]);
+                vec3 c = cross(p1 - p0, p2 - p0);
+                float triangleArea = sqrt(dot(c, c)) / 2.0f;
+                area += triangleArea;
+                MaterialData m = SampleMaterialData(rs, t.w);
+                mat.Reflectiveness = mat.Reflectiveness + m.Reflectiveness * triangleArea;
+                mat.Opacity += m.Opacity * triangleArea;
+                mat.Diffuse += m.Diffuse * triangleArea;
+                mat.Emissivity += m.Emissivity * triangleArea;
+                mat.Fresnel0 += m.Fresnel0 * triangleArea;
+                mat.Fresnel1 += m.Fresnel1 * triangleArea;
+                mat.RefractionIndexAvg += m.RefractionIndexAvg * triangleArea;
+            }
+        } else {
+            const int second = NodeEscape(s, (int)childCode);
+            for (int c : {(int)childCode, second}) {
+                const uint* o = out + 12 * (size_t)c;
+                float childArea = unpackHalf2x16(o[3]).y;
+                area += childArea;
+                vec2 r0 = unpackHalf2x16(o[0]) * childArea, r1 = unpackHalf2x16(o[1]) * childArea;
+                mat.Reflectiveness = mat.Reflectiveness + vec4(r0.x, r0.y, r1.x, r1.y);
+                vec2 v = unpackHalf2x16(o[2]) * childArea;
+                mat.Opacity = mat.Opacity + vec3(v.x, v.y, unpackHalf2x16(o[3]).x * childArea);
+                v = unpackHalf2x16(o[4]) * childArea;
+                mat.Diffuse = mat.Diffuse + vec3(v.x, v.y, unpackHalf2x16(o[5]).x * childArea);
+                v = unpackHalf2x16(o[6]) * childArea;
+                mat.Emissivity = mat.Emissivity + vec3(v.x, v.y, unpackHalf2x16(o[7]).x * childArea);
+                v = unpackHalf2x16(o[8]) * childArea;
+                mat.Fresnel0 = mat.Fresnel0 + vec3(v.x, v.y, unpackHalf2x16(o[9]).x * childArea);
+                mat.RefractionIndexAvg += unpackHalf2x16(o[9]).y * childArea;
+                v = unpackHalf2x16(o[10]) * childArea;
+                mat.Fresnel1 = mat.Fresnel1 + vec3(v.x, v.y, unpackHalf2x16(o[11]).x * childArea);
+            }
+        }
+        mat.Reflectiveness = mat.Reflectiveness / area;
+        mat.Opacity /= area;
+        mat.Diffuse /= area;
+        mat.Emissivity /= area;
+        mat.Fresnel0 /= area;
+        mat.Fresnel1 /= area;
+        mat.RefractionIndexAvg /= area;
+        StoreHierMaterial(out + 12 * (size_t)i, mat, area);
+    }
+}
+
+// loadSGGX (sggx.glsl:1-14): RG16 unorm texels {sigma.x, sigma.y},
+// {sigma.z, r.x}, {r.y, r.z}; S[col][row].
+struct Mat3 {
+    vec3 c[3];
+};
+static Mat3 LoadSGGX(const uint16_t* n) {
+    vec3 sigma(n[0] / 65535.0f, n[1] / 65535.0f, n[2] / 65535.0f);
+    vec3 r = vec3(n[3] / 65535.0f, n[4] / 65535.0f, n[5] / 65535.0f) * 2.0f - 1.0f;
+    Mat3 m;
+    m.c[0].x = saturate(sigma.x * sigma.x);
+    m.c[1].y = saturate(sigma.y * sigma.y);
+    m.c[2].z = saturate(sigma.z * sigma.z);
+    m.c[0].y = m.c[1].x = clamp(r.x * sigma.x * sigma.y, -1.0f, 1.0f);
+    m.c[0].z = m.c[2].x = clamp(r.y * sigma.x * sigma.z, -1.0f, 1.0f);
+    m.c[1].z = m.c[2].y = clamp(r.z * sigma.y * sigma.z, -1.0f, 1.0f);
+    return m;
+}
+static vec3 MulMV(const Mat3& m, vec3 v) {  // column combination, left to right
+    return (m.c[0] * v.x + m.c[1] * v.y) + m.c[2] * v.z;
+}
+
+// sampleNormal (sggx.glsl:16-56): a visible normal of the node's NDF.
+static vec3 SampleSGGXNormal(vec3 incident, const Mat3& S, uint& seed) {
+    Mat3 local;
+    local.c[2] = -incident;
+    CreateONB(incident, local.c[0], local.c[1]);
+    float Sxx = dot(local.c[0], MulMV(S, local.c[0]));
+    float Sxy = dot(local.c[0], MulMV(S, local.c[1]));
+    float Sxz = dot(local.c[0], MulMV(S, local.c[2]));
+    float Syy = dot(local.c[1], MulMV(S, local.c[1]));
+    float Syz = dot(local.c[1], MulMV(S, local.c[2]));
+    float Szz = dot(local.c[2], MulMV(S, local.c[2]));
+    vec3 m_i, m_j, m_k;
+    float det = max(0.0f, Sxx * Syy * Szz + Sxy * Syz * Sxz * 2.0f - Sxz * Sxz * Syy - Sxy * Sxy * Szz -
+                              Syz * Syz * Sxx - DIVISOR_EPSILON);
+    float tmp = Syy * Szz - Syz * Syz + DIVISOR_EPSILON;
+    m_i = tmp != 0.0f ? vec3(sqrt(det / tmp), 0.0f, 0.0f) : vec3(0.0f);
+    tmp = sqrt(tmp);
+    m_j = (tmp != 0.0f && Szz != 0.0f) ? vec3((Sxy * Szz - Sxz * Syz) / tmp, tmp, 0.0f) / sqrt(Szz) : vec3(0.0f);
+    m_k = Szz != 0.0f ? vec3(Sxz, Syz, Szz) / sqrt(Szz) : vec3(0.0f);
+    float chi0 = Random(seed);
+    float w = sqrt(1.0f - chi0);
+    chi0 = sqrt(chi0);
+    float chi1 = Random(seed) * 6.283185307f;
+    float u = chi0 * std::cos(chi1);
+    float v = chi0 * std::sin(chi1);
+    vec3 normal = (u * m_i + v * m_j) + w * m_k;
+    return normalize(MulMV(local, normal));
+}
+
+// TraceRay / TraceRayAnyHit with TRACERAY_IMPORTANCE_BREAK and HIT_INDEX_OUTPUT
+// (traceray.glsl:25-180) at IMPORTANCE_THRESHOLD 0: a node whose importance y
+// is at most threshold x entry distance ends the descent. Closest hit: the
+// node becomes a hit at a hashed point between entry and exit (rayLength
+// shrinks to it) and the walk continues at its escape; any hit: it occludes
+// when it ends within rayLength, else it is skipped.
+struct ImportanceHit {
+    int node = -1, slot = -1;  // _hitIndex: slot -1 = the node itself
+    float nodeImportance = 0.0f, nodeSizeSq = 0.0f;
+    vec3 bary;
+    ivec4 triangle{0, 0, 0, 0};
+};
+template <bool ANY_HIT>
+static bool TraceImportance(const Scene& s, const float* imp, const Ray& ray, float& rayLength, float threshold,
+                            ImportanceHit* out) {
+    const int TRIANGLES_PER_LEAF = (int)s.leafSize;
+    int currentNodeIndex = 0, currentLeafIndex = 0, lastNodeIndex = 0;
+    float lastNodeImportance = 0.0f, lastNodeSizeSq = 0.0f;
+    vec3 invRayDir = 1.0f / ray.Direction;
+    bool nextIsLeafNode = false;
+    uint64_t guard = (uint64_t)s.numNodes + (uint64_t)s.numSlots + 2;
+    do {
+        if (guard-- == 0) return false;
+        if (!nextIsLeafNode) {
+            float newHit, exitDist, nodeSizeSq;
+            uint childCode;
+            int escape;
+            if (FetchIntersectBoxNode(s, ray.Origin, invRayDir, currentNodeIndex, newHit, exitDist, childCode, escape,
+                                      nodeSizeSq) && newHit <= rayLength) {
+                lastNodeIndex = currentNodeIndex;
+                const float ix = imp[2 * currentNodeIndex], iy = imp[2 * currentNodeIndex + 1];
+                lastNodeImportance = ix;
+                lastNodeSizeSq = nodeSizeSq;
+                if ((ix < 0.0f && newHit > 0.0f) || iy <= threshold * newHit) {
+                    if (ANY_HIT) {
+                        if (exitDist <= rayLength) return true;
+                    } else {
+                        out->nodeImportance = ix;
+                        out->nodeSizeSq = lastNodeSizeSq;
+                        out->node = currentNodeIndex;
+                        rayLength = newHit + (exitDist - newHit) *
+                                                 ((float)(wanghash(floatBitsToUint(exitDist)) % 8388593u) / 8388593.0f);
+                        out->slot = -1;
+                    }
+                    currentNodeIndex = escape;
+                } else {
+                    currentNodeIndex = int(childCode & 0x7FFFFFFFu);
+                    nextIsLeafNode = (uint)currentNodeIndex != childCode;
+                    if (nextIsLeafNode) {
+                        currentLeafIndex = TRIANGLES_PER_LEAF * currentNodeIndex;
+                        currentNodeIndex = escape;
+                    }
+                }
+            } else {
+                currentNodeIndex = escape;
+            }
+        }
+        if (nextIsLeafNode) {
+            ivec4 triangle = s.triangles[currentLeafIndex];
+            if (triangle.x == triangle.y) {
+                nextIsLeafNode = false;
+            } else {
+                float newHit;
+                vec3 bary;
+                if (IntersectSlot(s, ray, currentLeafIndex, newHit, bary, triangle) && newHit < rayLength) {
+                    if (ANY_HIT) return true;
+                    rayLength = newHit;
+                    out->triangle = triangle;
+                    out->bary = bary;
+                    out->node = lastNodeIndex;
+                    out->slot = currentLeafIndex;
+                    out->nodeImportance = lastNodeImportance;
+                    out->nodeSizeSq = lastNodeSizeSq;
+                }
+                ++currentLeafIndex;
+                nextIsLeafNode = (currentLeafIndex % TRIANGLES_PER_LEAF) != 0;
+            }
+        }
+    } while (currentNodeIndex != 0 || nextIsLeafNode);
+    return false;
+}
+
+// EstimateDirectLight with TRACERAY_IMPORTANCE_BREAK (lightsource.glsl:3-93);
+// directional samples are the sun addition, offset like point lights.
+static vec3 EstimateDirectLightImportance(const RenderScene& s, const Params& P, const float* imp, vec3 pos,
+                                          vec3 normal, int idx, vec3 viewDir, const MaterialData& m,
+                                          bool sampleAreaLights, float threshold, float distEpsilon) {
+    vec4 pn0 = P.lightSamples[2 * idx];
+    vec4 in1 = P.lightSamples[2 * idx + 1];
+    Ray lightRay;
+    if (in1.w > 2.5f) {
+        lightRay.Direction = pn0.xyz();
+        float surfaceCos = saturate(dot(lightRay.Direction, normal));
+        if (surfaceCos <= 0.0f) return vec3(0.0f);
+        lightRay.Origin = distEpsilon * lightRay.Direction + pos;
+        float len = RAY_MAX;
+        if (!TraceImportance<true>(s.geo, imp, lightRay, len, threshold, nullptr)) {
+            float pdf;
+            vec3 bsdf = BSDFImpl(viewDir, lightRay.Direction, m, normal, pdf, false, false);
+            return (surfaceCos * in1.xyz()) * bsdf;
+        }
+        return vec3(0.0f);
+    }
+    lightRay.Direction = pn0.xyz() - pos;
+    float lightDistSq = dot(lightRay.Direction, lightRay.Direction) + DIVISOR_EPSILON;
+    float lightDist = sqrt(lightDistSq);
+    lightRay.Direction /= lightDist;
+    float surfaceCos = saturate(dot(lightRay.Direction, normal));
+    if (surfaceCos <= 0.0f) return vec3(0.0f);
+    if (in1.w > 1.5f) {
+        lightRay.Origin = distEpsilon * lightRay.Direction + pos;
+        float len = lightDist - RAY_HIT_EPSILON - distEpsilon;
+        if (!TraceImportance<true>(s.geo, imp, lightRay, len, threshold, nullptr)) {
+            vec3 irradiance = (surfaceCos / lightDistSq) * in1.xyz();
+            float pdf;
+            vec3 bsdf = BSDFImpl(viewDir, lightRay.Direction, m, normal, pdf, false, false);
+            return irradiance * bsdf;
+        }
+    } else if (sampleAreaLights) {
+        vec3 lightNormal = UnpackNormal(vec2(pn0.w, in1.w));
+        float f = saturate(dot(lightNormal, -lightRay.Direction));
+        if (f > 0.0f) {
+            lightRay.Origin = RAY_HIT_EPSILON * lightRay.Direction + pos;
+            float len = lightDist - RAY_HIT_EPSILON * 2;
+            if (!TraceImportance<true>(s.geo, imp, lightRay, len, threshold, nullptr)) {
+                float pdf;
+                vec3 intensity = in1.xyz() * f;
+                vec3 bsdf = BSDFImpl(viewDir, lightRay.Direction, m, normal, pdf, false, false);
+                vec3 irradiance = (surfaceCos / lightDistSq) * intensity;
+                return irradiance * bsdf;
+            }
+        }
+    }
+    return vec3(0.0f);
+}
+
+// hierarchypathtracer.comp:20-149 (one light sample; maxPathLength is the
+// shader's MAX_PATHLENGTH, 4 in the reference): the jittered primary ray
+// without the -0.5 offset, node hits shaded with the node material and a
+// normal sampled from the node NDF, the adjoint BSDF sampled, the importance
+// threshold x20 per bounce, Russian roulette from the first bounce.
+static vec3 HierarchyPixel(const RenderScene& s, const Params& P, const float* imp, const uint* mats,
+                           const uint16_t* sggx, int x, int y) {
+    const float lightSampleWeight = float(P.numLightSamples) / 1;
+    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    vec2 screen = (Random2(seed) + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
+    Ray ray;
+    ray.Origin = P.camPos;
+    ray.Direction = normalize(screen.x * P.camU + screen.y * P.camV + P.camW);
+    vec3 color(0.0f), pathThroughput(1.0f);
+    float pathImportanceThreshold = 0.000430915f;
+    bool didNEE = false;
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        ImportanceHit h;
+        float rayHit = RAY_MAX;
+        TraceImportance<false>(s.geo, imp, ray, rayHit, pathImportanceThreshold, &h);
+        if (rayHit == RAY_MAX) {
+            color += pathThroughput * P.sky;
+            break;
+        }
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 hitNormal;
+        MaterialData m;
+        if (h.slot < 0) {
+            m = LoadHierMaterial(mats + 12 * (size_t)h.node);
+            Mat3 S = LoadSGGX(sggx + 6 * (size_t)h.node);
+            hitNormal = SampleSGGXNormal(ray.Direction, S, seed);
+        } else {
+            vec2 tc;
+            GetTriangleHitInfo(s.geo, h.triangle, h.bary, hitNormal, tc);
+            m = SampleMaterialData(s, h.triangle.w);
+        }
+        float nextThreshold = pathImportanceThreshold * 20.0f;
+        float epsilon = RAY_HIT_EPSILON;
+        if (h.slot < 0) epsilon = sqrt(h.nodeSizeSq) * 0.1f;
+        if (!didNEE) color += pathThroughput * m.Emissivity;
+        didNEE = m.Reflectiveness.w < 500.0f;
+        int sampleIndex = int(RandomUInt(seed) % (uint)P.numLightSamples);
+        vec3 radiance = EstimateDirectLightImportance(s, P, imp, ray.Origin, hitNormal, sampleIndex, ray.Direction, m,
+                                                      didNEE, pathImportanceThreshold, epsilon);
+        color += radiance * pathThroughput * lightSampleWeight;
+        vec3 throughput(1.0f);
+        float pdf;
+        bool isReflectedDiffuse;
+        ray.Direction = SampleBSDFImpl(ray.Direction, m, seed, hitNormal, throughput, true, pdf, &isReflectedDiffuse);
+        ray.Origin = ray.Origin + ray.Direction * epsilon;
+        pathThroughput *= throughput;
+        pathImportanceThreshold = nextThreshold;
+        float p = saturate(GetLuminance(throughput));
+        if (Random(seed) >= p) break;
+        pathThroughput /= p;
+    }
+    return color;
+}
+
+static RenderScene MakeRenderScene(const float* hierarchy, uint32_t numNodes, const int32_t* slots, uint32_t numSlots,
+                                   uint32_t leafSize, const float* positions, const float* vertexInfo,
+                                   uint32_t numVertices, const float* materials, uint32_t numMaterials) {
+    RenderScene s;
+    s.geo.hierarchy = reinterpret_cast<const vec4*>(hierarchy);
+    s.geo.numNodes = numNodes;
+    s.geo.boundsKind = BOUNDS_AABB;
+    s.geo.triangles = reinterpret_cast<const ivec4*>(slots);
+    s.geo.numSlots = numSlots;
+    s.geo.leafSize = leafSize;
+    s.geo.positions = positions;
+    s.geo.numVertices = numVertices;
+    s.geo.vertexInfo = reinterpret_cast<const vec4*>(vertexInfo);
+    s.materials = materials;
+    s.numMaterials = numMaterials;
+    return s;
+}
+static Params MakeCameraParams(int width, int height, const float* cam, const float* lightSamples,
+                               int numLightSamples) {
+    Params P;
+    P.width = width;
+    P.height = height;
+    P.maxPathLength = 0;
+    P.rrStartDepth = 0;
+    P.camU = vec3(cam[0], cam[1], cam[2]);
+    P.camV = vec3(cam[3], cam[4], cam[5]);
+    P.camW = vec3(cam[6], cam[7], cam[8]);
+    P.camPos = vec3(cam[9], cam[10], cam[11]);
+    P.pixelArea = cam[12];
+    P.frameSeed = 0;
+    P.numLightSamples = numLightSamples;
+    P.lightSamples = reinterpret_cast<const vec4*>(lightSamples);
+    P.sky = vec3(0.0f);
+    P.numRaysPerLightSample = 0;
+    return P;
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
 extern "C" {
 
 // Photon mapper iteration (PhotonMapper::Draw, gpugi/renderer/photonmapper.cpp:
@@ -1048,5 +1618,93 @@ int oracle_render(const float* hierarchy, uint32_t numNodes, uint32_t boundsKind
 }
 
 uint32_t oracle_wanghash(uint32_t x) { return wanghash(x); }
+
+// HierarchyImportance::Draw's importance pass on an AABB hierarchy
+// (hierarchyimportance.cpp:83-109): `iterations` acquisition passes of
+// width x height paths (numbered 1..iterations), then the propagation.
+// imp: 2 * (numNodes + numSlots) floats {x, y}; subtree: numNodes floats.
+int oracle_hier_importance(const float* hierarchy, uint32_t numNodes, const int32_t* slots, uint32_t numSlots,
+                           uint32_t leafSize, const float* positions, const float* vertexInfo, uint32_t numVertices,
+                           const float* materials, uint32_t numMaterials, int width, int height, const float* cam,
+                           const float* lightSamples, int numLightSamples, int iterations, float* imp, float* subtree,
+                           int numThreads) {
+    if (iterations < 1 || numLightSamples < 1) return -1;
+    RenderScene s = MakeRenderScene(hierarchy, numNodes, slots, numSlots, leafSize, positions, vertexInfo, numVertices,
+                                    materials, numMaterials);
+    Params P = MakeCameraParams(width, height, cam, lightSamples, numLightSamples);
+    const size_t n = 2 * ((size_t)numNodes + numSlots);
+    const uint64_t pixels = (uint64_t)width * height;
+    int nt = numThreads > 0 ? numThreads : (int)std::max(1u, std::thread::hardware_concurrency());
+    nt = (int)std::min<uint64_t>((uint64_t)nt, std::max<uint64_t>(1, pixels));
+    std::vector<std::vector<float>> part(nt, std::vector<float>(n, 0.0f));
+    std::vector<std::thread> pool;
+    const uint64_t per = (pixels + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&, t]() {
+            for (int it = 1; it <= iterations; ++it)
+                for (uint64_t p = t * per; p < std::min<uint64_t>(pixels, (t + 1) * per); ++p)
+                    AcquirePixel(s, P, it, (int)(p % width), (int)(p / width), part[t].data());
+        });
+    for (auto& th : pool) th.join();
+    for (size_t k = 0; k < n; ++k) {
+        float acc = 0.0f;
+        for (int t = 0; t < nt; ++t) acc += part[t][k];
+        imp[k] = acc;
+    }
+    PropagateImportance(s.geo, iterations, imp, subtree);
+    return 0;
+}
+
+// The propagation alone on accumulated importance x (imp: 2 per node and slot).
+int oracle_hier_propagate(const float* hierarchy, uint32_t numNodes, const int32_t* slots, uint32_t numSlots,
+                          uint32_t leafSize, int iterations, float* imp, float* subtree) {
+    RenderScene s = MakeRenderScene(hierarchy, numNodes, slots, numSlots, leafSize, nullptr, nullptr, 0, nullptr, 0);
+    PropagateImportance(s.geo, iterations, imp, subtree);
+    return 0;
+}
+
+// ComputeHierarchyMaterials (hierarchyimportance.cpp:136-160): 12 uint32 per node.
+int oracle_hier_materials(const float* hierarchy, uint32_t numNodes, const int32_t* slots, uint32_t numSlots,
+                          uint32_t leafSize, const float* positions, const float* vertexInfo, uint32_t numVertices,
+                          const float* materials, uint32_t numMaterials, uint32_t* out) {
+    RenderScene s = MakeRenderScene(hierarchy, numNodes, slots, numSlots, leafSize, positions, vertexInfo, numVertices,
+                                    materials, numMaterials);
+    HierarchyMaterials(s, out);
+    return 0;
+}
+
+// One iteration of the hierarchy path tracer into rgba (alpha counts iterations).
+int oracle_render_hier(const float* hierarchy, uint32_t numNodes, const int32_t* slots, uint32_t numSlots,
+                       uint32_t leafSize, const float* positions, const float* vertexInfo, uint32_t numVertices,
+                       const float* materials, uint32_t numMaterials, int width, int height, int maxPathLength,
+                       const float* cam, uint32_t frameSeed, const float* lightSamples, int numLightSamples,
+                       const float* sky, const float* imp, const uint32_t* hierMaterials, const uint16_t* sggx,
+                       float* rgba, int numThreads) {
+    RenderScene s = MakeRenderScene(hierarchy, numNodes, slots, numSlots, leafSize, positions, vertexInfo, numVertices,
+                                    materials, numMaterials);
+    Params P = MakeCameraParams(width, height, cam, lightSamples, numLightSamples);
+    P.maxPathLength = maxPathLength;
+    P.frameSeed = frameSeed;
+    P.sky = sky ? vec3(sky[0], sky[1], sky[2]) : vec3(0.0f);
+    ParallelFor((uint64_t)width * height, numThreads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t p = b; p < e; ++p) {
+            vec3 c = HierarchyPixel(s, P, imp, hierMaterials, sggx, (int)(p % width), (int)(p / width));
+            float* o = rgba + 4 * p;
+            o[0] += c.x;
+            o[1] += c.y;
+            o[2] += c.z;
+            o[3] += 1.0f;
+        }
+    });
+    return 0;
+}
+
+// packHalf2x16 / unpackHalf2x16 of n values (tests of the conversion).
+void oracle_float_to_half(const float* in, uint16_t* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i) out[i] = FloatToHalf(in[i]);
+}
+void oracle_half_to_float(const uint16_t* in, float* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i) out[i] = HalfToFloat(in[i]);
+}
 
 }  // extern "C"

@@ -152,6 +152,24 @@ static bool TraceImpl(const Scene& s, const Ray& ray, float& rayLength, HitRecor
     return false;
 }
 
+bool FetchIntersectBoxNode(const Scene& s, vec3 origin, vec3 invRayDir, int nodeIdx, float& firstHit,
+                           float& lastHit, uint& childCode, int& escape, float& nodeSizeSq) {
+    vec4 a = s.hierarchy[2 * nodeIdx];
+    vec4 b = s.hierarchy[2 * nodeIdx + 1];
+    childCode = floatBitsToUint(a.w);
+    escape = floatBitsToInt(b.w);
+    vec3 ext = b.xyz() - a.xyz();
+    nodeSizeSq = dot(ext, ext);
+    return IntersectBox(origin, invRayDir, a.xyz(), b.xyz(), firstHit, lastHit);
+}
+
+bool IntersectSlot(const Scene& s, const Ray& ray, int slot, float& hit, vec3& bary, ivec4& triangle) {
+    triangle = s.triangles[slot];
+    vec3 p0 = Position(s, triangle.x), p1 = Position(s, triangle.y), p2 = Position(s, triangle.z);
+    vec3 normal;
+    return IntersectTriangle(ray, p0, p1, p2, hit, bary, normal);
+}
+
 void TraceRay(const Scene& s, const Ray& ray, float& rayLength, HitRecord& hit, TraceCounters* c) {
     hit.slot = -1;
     TraceImpl<false>(s, ray, rayLength, &hit, c);
