@@ -307,12 +307,15 @@ def run_passes(args):
     room of ~98k triangles (5 walls, 2 rotated boxes, level-6 sphere, 0.5 x
     0.5 ceiling light of radiance 10, albedos U[0.1, 0.9]), 512 x 512, 16 spp,
     depth 8, Russian roulette after depth 3. For PT, LT, BPT, the Whitted ray
-    tracer and the photon mapper (2048 photons per light sample, radius
-    0.01, one photon map per iteration): samples/s
+    tracer, the photon mapper (2048 photons per light sample, radius
+    0.01, one photon map per iteration) and the hierarchy-importance renderer
+    (its own 4-vertex paths; the importance pass runs in the warm-up
+    iteration and is timed there): samples/s
     (iterations x pixels per second) and Mrays/s (closest-hit + any-hit rays
-    traced, counted on the device), CUDA events around 16 spp after one
-    warm-up iteration. Beside each, the CPU restatement of the same pass on all
-    host threads over a bounded sample (64 x 64, 2 iterations)."""
+    traced, counted on the device by the wavefront passes), CUDA events
+    around 16 spp after one warm-up iteration. Beside each, the CPU
+    restatement of the same pass on all host threads over a bounded sample
+    (64 x 64, 2 iterations)."""
     import torch
     import oracle
     from gpugi_gb300 import bvh, cuda, render, scenes
@@ -320,18 +323,25 @@ def run_passes(args):
     spp, depth, rr = 16, 8, 3
     ctx = cuda.Context(0)
     sc = scenes.cornell_room(seed=1)
-    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", normals=sc["normals"])
     ds = ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]), sc["materials"])
+    ds.set_hierarchy_ndf(b.sggx)
     cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
     stream = torch.cuda.ExternalStream(ctx.stream)
     out = {}
-    for pass_ in ("PT", "LT", "BPT", "WHITTED", "PM"):
+    for pass_ in ("PT", "LT", "BPT", "WHITTED", "PM", "HIERARCHY"):
+        hier = pass_ == "HIERARCHY"
+        d = 4 if hier else depth
         img = render.Image(ctx, W, H)
-        render.render(ctx, ds, cam, img, pass_, max_path_length=depth, samples=1, rr_start_depth=rr, rng_state=[1])
         ctx.sync()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        render.render(ctx, ds, cam, img, pass_, max_path_length=depth, samples=spp, iteration=1, rr_start_depth=rr,
+        render.render(ctx, ds, cam, img, pass_, max_path_length=d, samples=1, rr_start_depth=rr, rng_state=[1])
+        e1.record(stream)
+        e1.synchronize()
+        first = e0.elapsed_time(e1)
+        e0.record(stream)
+        render.render(ctx, ds, cam, img, pass_, max_path_length=d, samples=spp, iteration=1, rr_start_depth=rr,
                       rng_state=[2])
         e1.record(stream)
         e1.synchronize()
@@ -345,14 +355,26 @@ def run_passes(args):
         st = [3]
         t0 = time.perf_counter()
         acc = None
+        if hier:
+            ls0 = render.generate_light_samples(ds, st, nls)
+            imp, _ = oracle.hier_importance(b, sc, cw, ch, ccam.as_array(), ls0, iterations=10)
+            mats = oracle.hier_materials(b, sc)
         for it in range(2):
-            ls = render.generate_light_samples(ds, st, nls)
-            acc = oracle.render(b, sc, pass_, cw, ch, ccam.as_array(), render.wanghash(it), ls,
-                                max_path_length=depth, rr_start_depth=rr, accum=acc)
+            ls = ls0 if (hier and it == 0) else render.generate_light_samples(ds, st, nls)
+            if hier:
+                acc = oracle.render_hier(b, sc, cw, ch, ccam.as_array(), render.wanghash(it), ls, imp, mats, b.sggx,
+                                         max_path_length=d, accum=acc)
+            else:
+                acc = oracle.render(b, sc, pass_, cw, ch, ccam.as_array(), render.wanghash(it), ls,
+                                    max_path_length=depth, rr_start_depth=rr, accum=acc)
         cpu = time.perf_counter() - t0
-        out[pass_] = {"samples_per_s": W * H * spp / sec, "mrays_per_s": (closest + anyhit) / sec / 1e6,
-                      "ms_per_iteration": sec / spp * 1e3, "closest_rays": closest, "any_hit_rays": anyhit,
+        out[pass_] = {"samples_per_s": W * H * spp / sec, "ms_per_iteration": sec / spp * 1e3,
                       "cpu_samples_per_s": cw * ch * 2 / cpu, "cpu_threads": os.cpu_count()}
+        if hier:  # megakernel: no device ray counters; the warm-up iteration holds the importance pass
+            out[pass_].update({"path_length": d, "first_iteration_ms": first})
+        else:
+            out[pass_].update({"mrays_per_s": (closest + anyhit) / sec / 1e6, "closest_rays": closest,
+                               "any_hit_rays": anyhit})
     line = {"metric": "samples/s and Mrays/s per pass", "config": {
         "workload": "Cornell room ~98k tris, 512x512, 16 spp, depth 8, RR after depth 3", "parallelism": "single GPU"},
         "passes": out, "data": "synthetic", "dtype": "f32",

@@ -152,6 +152,10 @@ public:
     }
     void AddPointLight(const PointLight& light);
     const std::vector<PointLight>& GetPointLights() const { return m_pointLights; }
+    // Node NDFs of the file ("approx_sggx", 6 uint16 per node), computed from
+    // the vertex normals when the file has none; empty without normals
+    // (Scene::GetSGGXBuffer, scene.cpp:127-130).
+    const std::vector<std::uint16_t>& GetSGGX() const { return m_sggx; }
 
 private:
     gpugi_ctx* m_ctx;
@@ -161,6 +165,7 @@ private:
                   m_maxDepth = 0;
     ei::Vec3 m_boxMin, m_boxMax;
     std::vector<PointLight> m_pointLights;
+    std::vector<std::uint16_t> m_sggx;
 };
 
 class RendererSystem;
@@ -309,6 +314,21 @@ class WhittedRayTracer : public Renderer {
 public:
     explicit WhittedRayTracer(RendererSystem& rendererSystem);
     std::string GetName() const override { return "WhittedRayTracer"; }
+    void SetScreenSize(const DeviceImage&) override {}
+    void Draw() override;
+};
+
+// HierarchyImportance (gpugi/renderer/hierarchyimportance.hpp): at the first
+// iteration after a camera change, the importance of every hierarchy node
+// for this view; then a path tracer of at most 4 vertices whose walks stop
+// at nodes that stand in well for their subtree, shading them with the
+// node's averaged material and a normal from its NDF. Needs node NDFs and
+// an AABB hierarchy.
+class HierarchyImportance : public Renderer {
+public:
+    explicit HierarchyImportance(RendererSystem& rendererSystem);
+    std::string GetName() const override { return "HierarchyImportance"; }
+    void SetScene(std::shared_ptr<Scene> scene) override;
     void SetScreenSize(const DeviceImage&) override {}
     void Draw() override;
 };

@@ -138,6 +138,12 @@ Scene::Scene(gpugi_ctx* ctx, const std::string& file) : m_ctx(ctx) {
             m_boxMax = ei::Vec3(r[0] + r[4], r[1] + r[5], r[2] + r[6]);
         }
     }
+    bool haveNormals = false;
+    for (float n : normals) haveNormals |= n != 0.0f;
+    if (haveNormals) {
+        m_sggx.resize((size_t)m_numNodes * 6);
+        if (gpugi_bvh_sggx(bvh, m_sggx.data()) != 0) m_sggx.clear();
+    }
     check_status(ctx,
                  gpugi_scene_upload(ctx, hierarchy.data(), m_numNodes, boundsKind, slots.data(),
                                     (uint32_t)(slots.size() / 4), m_leafSize, positions.data(), vinfo.data(),
@@ -307,6 +313,28 @@ void PhotonMapper::Draw() {
     m_rendererSystem.Check(gpugi_set_photon_config(m_rendererSystem.GetContext(), m_numPhotonsPerLightSample,
                                                    m_queryRadius, m_progressiveRadius ? 1u : 0u));
     draw_pass(m_rendererSystem, GPUGI_PASS_PM);
+}
+
+// hierarchyimportance.cpp:20-27
+HierarchyImportance::HierarchyImportance(RendererSystem& rendererSystem) : Renderer(rendererSystem) {
+    m_rendererSystem.SetNumInitialLightSamples(128);
+}
+// hierarchyimportance.cpp:29-72: the node NDFs and materials of the scene
+void HierarchyImportance::SetScene(std::shared_ptr<Scene> scene) {
+    if (scene->GetSGGX().empty())
+        throw GpugiError(GPUGI_ERROR_INVALID_SCENE, "HierarchyImportance needs the scene's node NDFs (SGGX)");
+    m_rendererSystem.Check(
+        gpugi_scene_set_hierarchy_ndf(m_rendererSystem.GetContext(), scene->GetHandle(), scene->GetSGGX().data()));
+}
+// hierarchyimportance.cpp:83-114; MAX_PATHLENGTH 4 (hierarchypathtracer.comp:17)
+void HierarchyImportance::Draw() {
+    if (!m_rendererSystem.GetScene()) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "no scene set");
+    gpugi_render_params p = m_rendererSystem.MakeRenderParams(GPUGI_PASS_HIERARCHY);
+    p.maxPathLength = 4;
+    m_rendererSystem.Check(gpugi_render(m_rendererSystem.GetContext(), m_rendererSystem.GetScene()->GetHandle(),
+                                        &m_rendererSystem.GetCameraParams(), &p,
+                                        m_rendererSystem.GetInitialLightSamples(), nullptr,
+                                        m_rendererSystem.GetBackbuffer().GetHandle()));
 }
 
 NrcPathtracer::NrcPathtracer(RendererSystem& rendererSystem, const NrcSettings& settings)

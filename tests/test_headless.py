@@ -53,7 +53,7 @@ CAM = [0.0, 1.0, 3.4, 0.0, 1.0, 0.0, 40.0]
 @pytest.mark.gpu
 @pytest.mark.parametrize("renderer,pass_", [("Pathtracer", "PT"), ("BidirectionalPathtracer", "BPT"),
                                             ("LightPathtracer", "LT"), ("WhittedRayTracer", "WHITTED"),
-                                            ("PhotonMapper", "PM")])
+                                            ("PhotonMapper", "PM"), ("HierarchyImportance", "HIERARCHY")])
 def test_headless_matches_the_c_abi(cuda_ctx, room_file, tmp_path, renderer, pass_):
     sc, path = room_file
     W = H = 32
@@ -66,9 +66,13 @@ def test_headless_matches_the_c_abi(cuda_ctx, room_file, tmp_path, renderer, pas
 
     b = bvh.read_bvh_file(str(path))
     ds = cuda_ctx.upload_scene(b, b.positions, cuda.vertex_info(b.normals, b.texcoords), b.materials)
+    depth = 6
+    if pass_ == "HIERARCHY":  # node NDFs from the file's approx_sggx chunk; the renderer's paths end at 4 vertices
+        ds.set_hierarchy_ndf(b.sggx)
+        depth = 4
     cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
     img = render.Image(cuda_ctx, W, H)
-    render.render(cuda_ctx, ds, cam, img, pass_, max_path_length=6, samples=iters, rng_state=[123])
+    render.render(cuda_ctx, ds, cam, img, pass_, max_path_length=depth, samples=iters, rng_state=[123])
     expect = img.read()[..., :3] / iters
     if pass_ == "BPT":
         # eye paths pick light-cache entries by index, and the cache is
