@@ -587,6 +587,10 @@ def run_batch(args):
     for name, fn in (("batch", lambda js: render.render_batch(ctx, js)), ("single", run_single)):
         t, n = measure(fn, make_jobs)
         result[name] = {"all_s": round(t, 4), "all_samples_per_s": n / t}
+        if name == "batch":  # rays the batched walkers traced (device counters of the call)
+            closest, anyhit = render.ray_counts(ctx)
+            result[name].update({"closest_rays": closest, "any_hit_rays": anyhit,
+                                 "mrays_per_s": (closest + anyhit) / t / 1e6})
         for pass_ in ("PT", "LT", "BPT"):
             t, n = measure(fn, lambda: make_jobs((pass_,)))
             result[name][pass_ + "_s"] = round(t, 4)
