@@ -463,7 +463,8 @@ def run_build(args):
     icosphere of the headline. Build: wall time from host arrays to a
     traversable scene (after one untimed GPU build). Traversal: closest-hit
     Mrays/s on each tree (large: 2^22 random rays inside the volume;
-    icosphere: the headline's 2^20 rays), CUDA events."""
+    icosphere: the headline's 2^20 rays), CUDA events; the host LDS tree
+    (bvhmake's largest-dimension split) traversed beside them."""
     import torch
     from gpugi_gb300 import bvh, cuda, scenes
     ctx = cuda.Context(0)
@@ -506,16 +507,20 @@ def run_build(args):
         t0 = time.perf_counter()
         gpu = ctx.build_scene(sc["positions"], sc["triangles"])
         res["gpu_build_s"] = time.perf_counter() - t0
-        res["nodes"] = {"host_sweep": host.num_nodes, "gpu_lbvh": gpu.num_nodes}
+        t0 = time.perf_counter()
+        lb = bvh.build_bvh(sc["positions"], sc["triangles"], method="lds")
+        res["host_lds_build_s"] = time.perf_counter() - t0
+        lds = ctx.upload_scene(lb, sc["positions"])
+        res["nodes"] = {"host_sweep": host.num_nodes, "host_lds": lds.num_nodes, "gpu_lbvh": gpu.num_nodes}
         outs = dict(slot=torch.empty(m, dtype=torch.int32, device="cuda"), t=torch.empty(m, device="cuda"),
                     u=torch.empty(m, device="cuda"), v=torch.empty(m, device="cuda"))
         torch.cuda.synchronize()
-        for key, ds in (("host_sweep", host), ("gpu_lbvh", gpu)):
+        for key, ds in (("host_sweep", host), ("host_lds", lds), ("gpu_lbvh", gpu)):
             sec = ev_time(lambda: cuda.trace_closest_device(ctx, ds, rays, outs), 5)
             res[f"{key}_mrays_per_s"] = m / sec / 1e6
         out[name] = res
-        host.close()
-        gpu.close()
+        for x in (host, lds, gpu):
+            x.close()
     line = {"metric": "hierarchy build time, GPU linear BVH vs host sweep SAH", "unit": "s", "results": out,
             "config": {"workload": "large: ~7.9M tris (20k instances in 100^3); icosphere: 65,536 tris (headline)",
                        "leaf_size": 8, "bounds": "AABB"}, "data": "synthetic", "dtype": "f32"}

@@ -15,7 +15,7 @@ import numpy as np
 _LIB = None
 LIB_DIR = Path(__file__).resolve().parent / "lib"
 
-BUILD_METHODS = {"kdtree": 0, "sweep": 1}
+BUILD_METHODS = {"kdtree": 0, "sweep": 1, "lds": 2}
 FIT_METHODS = {"aabox": 0, "ellipsoid": 1}
 
 

@@ -574,8 +574,9 @@ inline float TriangleSurface(V3 a, V3 b, V3 c) {
 }
 
 // Cyclic Jacobi rotations on a symmetric 3x3 matrix: rows of q are the
-// eigenvectors (Golub & Van Loan, "Matrix Computations", 8.5).
-void SymmetricEigen3(const double in[3][3], double q[3][3]) {
+// eigenvectors, lambda (optional) the eigenvalues in the same order (Golub &
+// Van Loan, "Matrix Computations", 8.5).
+void SymmetricEigen3(const double in[3][3], double q[3][3], double* lambda = nullptr) {
     double a[3][3];
     for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c) {
@@ -609,6 +610,8 @@ void SymmetricEigen3(const double in[3][3], double q[3][3]) {
                 }
             }
     }
+    if (lambda)
+        for (int k = 0; k < 3; ++k) lambda[k] = a[k][k];
 }
 
 // ComputeLeafSGGXBase (approx_sggx.cpp:88-154) for leaf block blk.
@@ -710,6 +713,98 @@ void PackSggx(const Sggx& s, uint16_t* o) {
     for (int k = 0; k < 3; ++k) o[3 + k] = d[k] > 0.0f ? u16(off[k] / d[k] * 32767.0f + 32767.0f) : (uint16_t)32767;
 }
 
+// BuildLDS (bvhmake/buildmethods/lds.cpp:11-164, LDS_SPLITMODE_SWEEP): at
+// every node the triangle centres are projected on the eigenvector of the
+// largest eigenvalue of their covariance (n - 1 normalised), sorted by that
+// projection, and split where the SAH sweep of the sweep builder is
+// smallest (the minimum search starts at 0 here, lds.cpp:145). epsilon's
+// decomposeQl is replaced by the Jacobi method above: the eigenvector's sign
+// (which orders the children) is fixed by making its largest component
+// positive, ties of eigenvalues pick the first as the reference's
+// comparisons do, and the unstable std::sort of the reference is a stable
+// sort: the trees are unpinned.
+void BuildLds(gpugi_bvh& b) {
+    const uint32_t n = (uint32_t)(b.triangles.size() / 4);
+    std::vector<V3> centers(n);
+    std::vector<Box> triBoxes(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        centers[i] = b.Center(i);
+        triBoxes[i] = b.TriBox(i);
+    }
+    std::vector<uint32_t> ids(n);
+    for (uint32_t i = 0; i < n; ++i) ids[i] = i;
+    std::vector<float> proj(n), hx, hy;
+    std::vector<Task> stack{Task{0, n - 1, UINT32_MAX, false}};
+    std::vector<uint32_t> depthStack{1};
+    while (!stack.empty()) {
+        const Task t = stack.back();
+        stack.pop_back();
+        const uint32_t depth = depthStack.back();
+        depthStack.pop_back();
+        b.maxDepth = std::max(b.maxDepth, depth);
+        const uint32_t idx = (uint32_t)b.nodes.size();
+        b.nodes.push_back(Node{0, 0});
+        Link(b, t, idx);
+        Box nodeBox = triBoxes[ids[t.hi]];
+        for (uint32_t i = t.lo; i < t.hi; ++i) nodeBox = BoxUnion(nodeBox, triBoxes[ids[i]]);
+        b.boxes.push_back(nodeBox);
+        if (t.hi - t.lo < b.leafSize) {
+            const uint32_t leaf = b.NewLeaf(ids.data(), t.lo, t.hi);
+            b.nodes[idx].left = 0x80000000u | leaf;
+            b.nodes[idx].right = 0;
+            continue;
+        }
+        // covariance of the centres (lds.cpp:67-82)
+        V3 m = centers[ids[t.lo]];
+        for (uint32_t i = t.lo + 1; i <= t.hi; ++i) m = m + centers[ids[i]];
+        m = m / (float)(t.hi - t.lo + 1);
+        float cov[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (uint32_t i = t.lo; i <= t.hi; ++i) {
+            const V3 e = centers[ids[i]] - m;
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) cov[r][c] += e[r] * e[c];
+        }
+        double covd[3][3], q[3][3], lam[3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) covd[r][c] = cov[r][c] / (float)(t.hi - t.lo);
+        SymmetricEigen3(covd, q, lam);
+        const int k = (lam[0] > lam[1] && lam[0] > lam[2]) ? 0 : (lam[1] > lam[2] ? 1 : 2);
+        int big = 0;
+        for (int c = 1; c < 3; ++c)
+            if (std::fabs(q[k][c]) > std::fabs(q[k][big])) big = c;
+        const double sgn = q[k][big] < 0.0 ? -1.0 : 1.0;
+        const V3 dir((float)(sgn * q[k][0]), (float)(sgn * q[k][1]), (float)(sgn * q[k][2]));
+        for (uint32_t i = t.lo; i <= t.hi; ++i) proj[ids[i]] = Dot(centers[ids[i]], dir);
+        std::stable_sort(ids.begin() + t.lo, ids.begin() + t.hi + 1,
+                         [&](uint32_t l, uint32_t r) { return proj[l] < proj[r]; });
+        // SAH sweep over the sorted range (lds.cpp:118-152)
+        const uint32_t cnt = t.hi - t.lo;
+        hx.assign(cnt, 0.0f);
+        hy.assign(cnt, 0.0f);
+        const float parentSurface = BoxSurface(nodeBox);
+        Box left = triBoxes[ids[t.lo]], right = triBoxes[ids[t.hi]];
+        for (uint32_t i = t.lo; i < t.hi; ++i) {
+            left = BoxUnion(left, triBoxes[ids[i]]);
+            right = BoxUnion(right, triBoxes[ids[t.hi - i + t.lo]]);
+            hx[i - t.lo] = BoxSurface(left) / parentSurface * (float)(int)(i - t.lo + 1);
+            hy[t.hi - i - 1] = BoxSurface(right) / parentSurface * (float)(int)(i - t.lo + 1);
+        }
+        float minCost = std::numeric_limits<float>::infinity();
+        uint32_t split = t.lo;
+        for (uint32_t i = 0; i < cnt; ++i) {
+            const float c = hx[i] + hy[i];
+            if (c < minCost) {
+                minCost = c;
+                split = i + t.lo;
+            }
+        }
+        stack.push_back(Task{split + 1, t.hi, idx, true});
+        depthStack.push_back(depth + 1);
+        stack.push_back(Task{t.lo, split, idx, false});
+        depthStack.push_back(depth + 1);
+    }
+}
+
 // ComputeSGGXBases (approx_sggx.cpp:156-203): leaves in parallel, then the
 // inner nodes children-first (reverse preorder).
 void ComputeSggx(const gpugi_bvh& b) {
@@ -781,7 +876,7 @@ int gpugi_bvh_build(const float* positions, uint32_t numVertices, const uint32_t
         g_lastError = "leafSize must be in [1, 64]";
         return -3;
     }
-    if (buildMethod > GPUGI_BUILD_SWEEP || fitMethod > GPUGI_FIT_ELLIPSOID) {
+    if (buildMethod > GPUGI_BUILD_LDS || fitMethod > GPUGI_FIT_ELLIPSOID) {
         g_lastError = "unknown build or fit method";
         return -4;
     }
@@ -802,6 +897,7 @@ int gpugi_bvh_build(const float* positions, uint32_t numVertices, const uint32_t
         b->leafSize = leafSize;
         b->boundsKind = fitMethod;
         if (buildMethod == GPUGI_BUILD_SWEEP) BuildSweep(*b);
+        else if (buildMethod == GPUGI_BUILD_LDS) BuildLds(*b);
         else BuildKdtree(*b);
         if (b->nodes.size() >= 0x80000000u) {
             g_lastError = "scene too large: the node index MSB is the leaf flag";

@@ -5,8 +5,9 @@
  * traversal kernels consume, and reads/writes bvhmake's NamedArray file.
  *
  *   gpugi_bvh_build       replaces BVHBuilder::BuildBVH        (bvhmake/bvhbuilder.cpp:526-555)
- *                         with BuildSweep/BuildKdtree           (bvhmake/buildmethods/sweep.cpp:27-259,
- *                                                                bvhmake/buildmethods/kdtree.cpp:9-157)
+ *                         with BuildSweep/BuildKdtree/BuildLDS  (bvhmake/buildmethods/sweep.cpp:27-259,
+ *                                                                bvhmake/buildmethods/kdtree.cpp:9-157,
+ *                                                                bvhmake/buildmethods/lds.cpp:11-164)
  *                         and FitBox/FitEllipsoid               (bvhmake/fitmethods/aaboxfit.cpp:5-33,
  *                                                                bvhmake/fitmethods/aaellipsoidfit.cpp:6-79)
  *   gpugi_bvh_export      replaces BVHBuilder::ExportBVH + ExportTriangles + the
@@ -33,7 +34,7 @@ extern "C" {
 
 typedef struct gpugi_bvh gpugi_bvh;
 
-enum gpugi_build_method { GPUGI_BUILD_KDTREE = 0, GPUGI_BUILD_SWEEP = 1 };
+enum gpugi_build_method { GPUGI_BUILD_KDTREE = 0, GPUGI_BUILD_SWEEP = 1, GPUGI_BUILD_LDS = 2 };
 enum gpugi_fit_method { GPUGI_FIT_AABOX = 0, GPUGI_FIT_ELLIPSOID = 1 };
 
 /* Build a hierarchy over `numTriangles` triangles, each 4 uint32

@@ -66,7 +66,7 @@ def _check_tree(b, tris, positions):
                 assert (((p - c[i]) / r[i]) ** 2).sum(1).max() <= 1.0 + 1e-6
 
 
-@pytest.mark.parametrize("method", ["sweep", "kdtree"])
+@pytest.mark.parametrize("method", ["sweep", "kdtree", "lds"])
 @pytest.mark.parametrize("leaf_size", [1, 2, 8])
 def test_escape_tree_invariants(built, method, leaf_size):
     sc = scenes.displaced_icosphere(2000, seed=5)
@@ -84,19 +84,42 @@ def test_ellipsoid_bounds_contain_leaves(built):
 @pytest.mark.parametrize("ntri", [1, 7, 8, 9, 17])
 def test_small_scenes(built, ntri):
     sc = scenes.displaced_icosphere(ntri, seed=2)
-    for method in ("sweep", "kdtree"):
+    for method in ("sweep", "kdtree", "lds"):
         b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method)
         _check_tree(b, sc["triangles"], sc["positions"])
         if ntri <= 8:
             assert b.num_nodes == 1 and (b.first_child[0] & 0x80000000)
 
 
-def test_deterministic(built):
+@pytest.mark.parametrize("method", ["sweep", "lds"])
+def test_deterministic(built, method):
     sc = scenes.displaced_icosphere(3000, seed=11)
-    a = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
-    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    a = bvh.build_bvh(sc["positions"], sc["triangles"], method=method)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method)
     assert np.array_equal(a.hierarchy.view(np.uint32), b.hierarchy.view(np.uint32))
     assert np.array_equal(a.slots, b.slots)
+
+
+def test_lds_splits_along_the_principal_axis(built):
+    """A long thin slab along a diagonal: the largest-dimension split follows
+    the diagonal, so the root's children separate the two ends, and the SAH
+    sweep keeps the tree within a few percent of the sweep builder's cost."""
+    rng = np.random.default_rng(4)
+    n = 512
+    t = np.sort(rng.uniform(0, 1, n)).astype(np.float32)
+    axis = np.array([1.0, 1.0, 0.0], np.float32) / np.sqrt(2)
+    base = t[:, None] * axis[None] * 10
+    off = rng.uniform(-0.01, 0.01, (n, 3, 3)).astype(np.float32)
+    pos = (base[:, None, :] + off).reshape(-1, 3).astype(np.float32)
+    tris = np.concatenate([np.arange(3 * n, dtype=np.uint32).reshape(n, 3), np.zeros((n, 1), np.uint32)], 1)
+    b = bvh.build_bvh(pos, tris, method="lds")
+    _check_tree(b, tris, pos)
+    left = int(b.first_child[0])
+    right = int(b.escape[left])
+    cl = (b.hierarchy[left, 0:3] + b.hierarchy[left, 4:7]) / 2
+    cr = (b.hierarchy[right, 0:3] + b.hierarchy[right, 4:7]) / 2
+    d = cr - cl
+    assert abs(d[0]) > 2 and abs(d[1]) > 2 and abs(d[2]) < 0.1  # split across the diagonal
 
 
 def test_rejects_bad_input(built):

@@ -20,7 +20,7 @@ from gpugi_gb300 import bvh, scenes
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
-@pytest.mark.parametrize("method,leaf", [("sweep", 8), ("kdtree", 8), ("sweep", 2), ("kdtree", 1)])
+@pytest.mark.parametrize("method,leaf", [("sweep", 8), ("kdtree", 8), ("sweep", 2), ("kdtree", 1), ("lds", 8)])
 def test_walk_matches_bruteforce(built, method, leaf):
     sc = scenes.displaced_icosphere(4096, seed=21)
     b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, leaf_size=leaf)
