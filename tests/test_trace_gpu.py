@@ -37,7 +37,7 @@ def icosphere_65536():
     return sc
 
 
-@pytest.mark.parametrize("method,leaf", [("sweep", 8), ("kdtree", 8), ("sweep", 2)])
+@pytest.mark.parametrize("method,leaf", [("sweep", 8), ("kdtree", 8), ("sweep", 2), ("lds", 8)])
 def test_closest_and_any_match_oracle(cuda_ctx, icosphere_65536, method, leaf):
     sc = icosphere_65536
     b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, leaf_size=leaf)
