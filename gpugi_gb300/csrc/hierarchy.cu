@@ -606,6 +606,8 @@ gpugi_status ensure_hier(gpugi_ctx* ctx, gpugi_scene* sc) {
     h->mats = reinterpret_cast<uint2*>(take(48 * (size_t)nn));
     h->ndf = reinterpret_cast<uint16_t*>(take(12 * (size_t)nn));
     sc->hier = h;
+    // zeros until the NDFs and the importance pass fill them (gpugi_hierarchy_read may come first)
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(h->block, 0, bytes, ctx->stream));
     return GPUGI_OK;
 }
 
