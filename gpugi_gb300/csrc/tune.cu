@@ -51,9 +51,60 @@ struct Events {
     }
 };
 
+// Every block re-reads its share of an L2-resident buffer `reps` times with
+// 16-B loads cached in L2 only (ld.global.cg); the sum keeps the loads alive.
+__global__ void k_l2_read(const float4* __restrict__ buf, uint64_t n4, uint32_t reps, float* sink) {
+    float acc = 0.0f;
+    for (uint32_t r = 0; r < reps; ++r)
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x) {
+            const float4 v = __ldcg(buf + i);
+            acc += (v.x + v.y) + (v.z + v.w);
+        }
+    if (acc == -1.0f) sink[0] = acc;  // never true for the zero-filled buffer
+}
+
 }  // namespace
 
 extern "C" {
+
+gpugi_status gpugi_measure_l2_bandwidth(gpugi_ctx* ctx, uint64_t bytes, uint32_t reps, double* gbs) {
+    if (!ctx || !gbs) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (bytes < (1u << 20) || bytes > (64ull << 20) || bytes % 16 || reps == 0 || reps > 4096)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "bytes in [1 MiB, 64 MiB], a multiple of 16; reps in [1, 4096]");
+    float4* buf = nullptr;
+    float* sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (buf) cudaFree(buf);
+        if (sink) cudaFree(sink);
+    };
+    cudaError_t e = cudaMalloc(&buf, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&sink, 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(buf, 0, bytes, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(ctx, e, "L2 bandwidth buffers");
+    }
+    int perSM = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, (const void*)k_l2_read, 256, 0);
+    const unsigned grid = (unsigned)(ctx->numSMs * std::max(perSM, 1));
+    const uint64_t n4 = bytes / 16;
+    k_l2_read<<<grid, 256, 0, ctx->stream>>>(buf, n4, 2, sink);  // warm: the buffer into L2
+    cudaEventRecord(e0, ctx->stream);
+    k_l2_read<<<grid, 256, 0, ctx->stream>>>(buf, n4, reps, sink);
+    cudaEventRecord(e1, ctx->stream);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "L2 bandwidth kernel");
+    *gbs = (double)bytes * reps / (ms * 1e-3) / 1e9;
+    return GPUGI_OK;
+}
 
 gpugi_status gpugi_autotune(gpugi_ctx* ctx, const gpugi_scene* sc, uint32_t flags, gpugi_tuning* out) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;

@@ -454,6 +454,12 @@ gpugi_status gpugi_hierarchy_importance(gpugi_ctx* ctx, gpugi_scene* scene, cons
 gpugi_status gpugi_hierarchy_read(gpugi_ctx* ctx, const gpugi_scene* scene, float* importance, float* subtree,
                                   uint32_t* materials);
 
+/* L2 read bandwidth of the device, for the second roofline of L2-resident
+ * scenes: one launch re-reads a `bytes` buffer (1-64 MiB, L2-resident)
+ * `reps` times with 16-B loads cached in L2 only; GB/s of bytes read, CUDA
+ * events. No counterpart in the reference. Synchronises; allocates. */
+gpugi_status gpugi_measure_l2_bandwidth(gpugi_ctx* ctx, uint64_t bytes, uint32_t reps, double* gbs);
+
 /* Autotuner. No counterpart in the reference (its launch shapes are fixed
  * local sizes, e.g. gpugi/renderer/pathtracer.cpp:11). Times candidates on
  * the scene with CUDA events and applies the fastest to the context:

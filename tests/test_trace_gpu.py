@@ -309,3 +309,16 @@ def test_device_guard_bits_reach_the_caller(cuda_ctx, icosphere_65536, parts, ze
     finally:
         cuda_ctx.set_host_pipeline(2, False)
     ds.close()
+
+
+def test_l2_bandwidth_measurement(cuda_ctx):
+    """The second roofline's denominator: L2 reads of an L2-resident buffer
+    run faster than the HBM copy rate; bad sizes are refused."""
+    import ctypes as C
+    lib = cuda.lib()
+    lib.gpugi_measure_l2_bandwidth.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_double)]
+    g = C.c_double()
+    cuda_ctx.check(lib.gpugi_measure_l2_bandwidth(cuda_ctx.handle, 32 << 20, 50, C.byref(g)))
+    assert g.value > 1000.0
+    with pytest.raises(cuda.GpugiError):
+        cuda_ctx.check(lib.gpugi_measure_l2_bandwidth(cuda_ctx.handle, 1000, 1, C.byref(g)))
