@@ -346,7 +346,7 @@ def run_passes(args):
     cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
     stream = torch.cuda.ExternalStream(ctx.stream)
     out = {}
-    for pass_ in ("PT", "LT", "BPT", "WHITTED", "PM", "HIERARCHY"):
+    for pass_ in (args.passes.split(",") if args.passes else ("PT", "LT", "BPT", "WHITTED", "PM", "HIERARCHY")):
         hier = pass_ == "HIERARCHY"
         d = 4 if hier else depth
         img = render.Image(ctx, W, H)
@@ -764,6 +764,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--passes", default=None,
+                    help="passes workload: comma-separated subset of PT,LT,BPT,WHITTED,PM,HIERARCHY")
     ap.add_argument("--shared-nodes", type=int, default=0,
                     help="top-of-tree nodes staged in shared memory by the walkers")
     ap.add_argument("--trace-mode", type=int, default=3,

@@ -10,8 +10,9 @@
 //
 //   k_hier_parents, k_hier_materials   parent links; node materials bottom up
 //                                      (sampleleafmaterials.comp, pullmaterials.comp)
-//   k_hier_acquire                     acquisition2.comp + counthits.glsl, one thread
-//                                      per pixel and iteration, float atomics
+//   k_acq_*                            acquisition2.comp + counthits.glsl as a
+//                                      wavefront (per path vertex: closest hits, hit
+//                                      counting, shading, next-event rays), float atomics
 //   k_hier_prop_init, k_hier_prop_up   hierarchypropagation_init.comp / _nodes.comp
 //                                      as one bottom-up pass (the second child to
 //                                      finish continues to the parent)
@@ -50,6 +51,8 @@ struct HierBuffers {
     size_t lightCap = 0;          // bytes
     float* hostLights = nullptr;  // pinned staging
     size_t hostLightCap = 0;      // bytes
+    void* acq = nullptr;          // wavefront state of the importance acquisition
+    uint64_t acqCap = 0;          // paths it holds
 };
 
 namespace {
@@ -93,37 +96,84 @@ GPUGI_D bool intersect_box_exit(float3 o, float3 inv, float4 lo, float4 hi, floa
 
 GPUGI_D float3 inv_dir(float3 d) { return make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)); }
 
-// TraceRayCountHits (hierarchy/counthits.glsl:1-71).
-GPUGI_D void count_hits(const DevScene& s, float2* imp, float3 o, float3 d, float len, float importance,
-                        uint32_t* err) {
-    const float3 inv = inv_dir(d);
-    uint32_t node = 0, budget = s.numNodes;
-    while (true) {
-        if (budget-- == 0) {
-            raise_error(err, DEVERR_TRAVERSAL_CAP);
-            return;
-        }
-        const float4 a = __ldg(s.nodes + 2 * node), b = __ldg(s.nodes + 2 * node + 1);
-        const uint32_t child = __float_as_uint(a.w), escape = __float_as_uint(b.w);
-        float fh, lh;
-        if (intersect_box_exit(o, inv, a, b, fh, lh) && fh <= len) {
-            atomicAdd(&imp[node].x, importance);
-            if (child & LEAF_FLAG) {
-                const uint32_t count = (child >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK;
-                const uint32_t slot0 = (child & LEAF_BLOCK_MASK) * s.leafSize;
-                for (uint32_t k = 0; k < count; ++k) {
-                    float h, by, bz;
-                    if (intersect_triangle(o, d, s.tris + 3 * (size_t)(slot0 + k), h, by, bz) && h <= len)
-                        atomicAdd(&imp[s.numNodes + slot0 + k].x, importance);
-                }
-                node = escape;
-            } else {
-                node = child;
+// Adds importance to *dst for every converged lane of the warp that adds to
+// the same address: one atomic of importance x lanes. The callers' lanes all
+// carry the same importance (a power of two), so the product is exact.
+GPUGI_D void add_importance(float* dst, float importance) {
+    const unsigned peers = __match_any_sync(__activemask(), (unsigned long long)dst);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(peers) - 1)) atomicAdd(dst, importance * (float)__popc(peers));
+}
+
+// TraceRayCountHits (hierarchy/counthits.glsl:1-71) as a resumable walk, one
+// node (with its leaf block) per step, for the persistent loop below. Every
+// ray of a launch carries the same importance (acquisition2.comp halves it
+// per vertex for all paths alike), which add_importance relies on.
+struct CountWalk {
+    float3 o, d, inv;
+    float len, importance;
+    uint32_t node, budget;
+};
+GPUGI_D bool count_step(CountWalk& w, const DevScene& s, float2* imp, uint32_t* err) {
+    if (w.budget-- == 0) {
+        raise_error(err, DEVERR_TRAVERSAL_CAP);
+        return true;
+    }
+    const float4 a = __ldg(s.nodes + 2 * w.node), b = __ldg(s.nodes + 2 * w.node + 1);
+    const uint32_t child = __float_as_uint(a.w), escape = __float_as_uint(b.w);
+    float fh, lh;
+    if (intersect_box_exit(w.o, w.inv, a, b, fh, lh) && fh <= w.len) {
+        add_importance(&imp[w.node].x, w.importance);
+        if (child & LEAF_FLAG) {
+            const uint32_t count = (child >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK;
+            const uint32_t slot0 = (child & LEAF_BLOCK_MASK) * s.leafSize;
+            for (uint32_t k = 0; k < count; ++k) {
+                float h, by, bz;
+                if (intersect_triangle(w.o, w.d, s.tris + 3 * (size_t)(slot0 + k), h, by, bz) && h <= w.len)
+                    add_importance(&imp[s.numNodes + slot0 + k].x, w.importance);
             }
+            w.node = escape;
         } else {
-            node = escape;
+            w.node = child;
         }
-        if (node == 0) break;
+    } else {
+        w.node = escape;
+    }
+    return w.node == 0;
+}
+
+// Count walks of n items: a lane whose walk ends takes the next item
+// (warp-aggregated increments of *work), so lanes do not wait for the longest
+// walk of their warp. load(i, o, d, len, importance) returns false for an
+// item without a walk.
+template <typename Load>
+GPUGI_D void persistent_count_walks(const DevScene& s, uint32_t n, unsigned long long* work, float2* imp,
+                                    uint32_t* err, Load load) {
+    const unsigned lane = threadIdx.x & 31u;
+    CountWalk w;
+    bool active = false, exhausted = false;
+    while (true) {
+        const bool need = !active && !exhausted;
+        const unsigned needMask = __ballot_sync(0xffffffffu, need);
+        if (needMask) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(work, (unsigned long long)__popc(needMask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (need) {
+                const unsigned long long my = base + (unsigned long long)__popc(needMask & ((1u << lane) - 1u));
+                if (my < n) {
+                    if (load((uint32_t)my, w.o, w.d, w.len, w.importance)) {
+                        w.inv = inv_dir(w.d);
+                        w.node = 0;
+                        w.budget = s.numNodes;
+                        active = true;
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active && count_step(w, s, imp, err)) active = false;
     }
 }
 
@@ -350,10 +400,41 @@ __global__ void k_hier_materials(DevScene s, const uint32_t* __restrict__ parent
 }
 
 // ------------------------------------------------------------ importance
-// acquisition2.comp:26-112 for pixel pix of iteration `it` (1-based).
-__global__ void k_hier_acquire(HierConst c, uint32_t iterations) {
+// acquisition2.comp:26-112 as a wavefront: per path vertex, one launch each
+// for the closest hits, the hit counting along the path segments, the
+// shading (next-event ray and BSDF sample, the same random draws in the same
+// order as the shader), the next-event rays' closest hits and their hit
+// counting. Each launch runs one kind of walk in every lane, instead of one
+// thread per path alternating between walks and shading.
+struct AcqPaths {
+    float *ox, *oy, *oz, *dx, *dy, *dz, *imp;
+    uint32_t* seed;
+};
+struct AcqRays {  // next-event rays of one vertex
+    float *ox, *oy, *oz, *dx, *dy, *dz, *dist, *imp, *t;
+};
+struct AcqState {
+    AcqPaths A, B;
+    int32_t* slot;  // closest hits of the current paths
+    float *t, *u, *v;
+    AcqRays L;
+    uint32_t* cnt;  // paths per vertex [kAcquirePathLength + 1], then next-event rays per vertex
+    unsigned long long* work;  // work counters of the walks, 4 per vertex
+};
+
+GPUGI_D float3 load3(const float* x, const float* y, const float* z, uint64_t i) {
+    return make_float3(x[i], y[i], z[i]);
+}
+GPUGI_D void store3(float* x, float* y, float* z, uint64_t i, float3 v) {
+    x[i] = v.x;
+    y[i] = v.y;
+    z[i] = v.z;
+}
+
+__global__ void k_acq_generate(HierConst c, uint32_t iterations, AcqPaths A, uint32_t* cnt) {
     const uint32_t numPixels = (uint32_t)(c.width * c.height);
     const uint64_t total = (uint64_t)numPixels * iterations;
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[0] = (uint32_t)total;
     for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total; q += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t it = 1u + (uint32_t)(q / numPixels), pix = (uint32_t)(q % numPixels);
         const int x = (int)(pix % (uint32_t)c.width), y = (int)(pix / (uint32_t)c.width);
@@ -361,34 +442,118 @@ __global__ void k_hier_acquire(HierConst c, uint32_t iterations) {
         const float2 r = random2(seed);
         const float sx = X::sub(X::mul(X::div(X::add(r.x, (float)x), (float)c.width), 2.0f), 1.0f);
         const float sy = X::sub(X::mul(X::div(X::add(r.y, (float)y), (float)c.height), 2.0f), 1.0f);
-        float3 o = c.camPos;
-        float3 d = X::normalize(X::add3(X::add3(X::scale(sx, c.camU), X::scale(sy, c.camV)), c.camW));
-        float importance = 1.0f;
-        for (int i = 0; i < kAcquirePathLength; ++i) {
-            const TraceResult tr = trace_ray<false, 0>(c.s, o, d, kRAY_MAX, c.err);
-            count_hits(c.s, c.imp, o, d, X::mul(tr.t, 1.000001f), importance, c.err);
-            if (tr.slot < 0) break;
-            const int4 tri = __ldg(c.s.slots + tr.slot);
-            const float3 N = hit_normal(c.s, tri, tr.u, tr.v, nullptr);
+        store3(A.ox, A.oy, A.oz, q, c.camPos);
+        store3(A.dx, A.dy, A.dz, q, X::normalize(X::add3(X::add3(X::scale(sx, c.camU), X::scale(sy, c.camV)), c.camW)));
+        A.imp[q] = 1.0f;
+        A.seed[q] = seed;
+    }
+}
+
+// Closest hits with the 8-lane group walk of the ray queries (same results
+// as trace_ray): work items are taken through *work.
+__global__ void __launch_bounds__(128) k_acq_trace(HierConst c, AcqPaths A, const uint32_t* __restrict__ count,
+                                                   AcqState S, unsigned long long* work) {
+    group_walks<false, 0, 8>(
+        c.s, *count, work, c.err,
+        [&](uint64_t i, float3& o, float3& d, float& tmax) {
+            o = load3(A.ox, A.oy, A.oz, i);
+            d = load3(A.dx, A.dy, A.dz, i);
+            tmax = kRAY_MAX;
+        },
+        [&](uint64_t i, const GroupWalk& g) {
+            S.slot[i] = g.slot;
+            S.t[i] = g.len;
+            S.u[i] = g.u;
+            S.v[i] = g.v;
+        });
+}
+
+__global__ void __launch_bounds__(128) k_acq_count(HierConst c, AcqPaths A, const uint32_t* __restrict__ count,
+                                                   const float* __restrict__ t, unsigned long long* work) {
+    persistent_count_walks(c.s, *count, work, c.imp, c.err,
+                           [&](uint32_t k, float3& o, float3& d, float& len, float& importance) {
+                               o = load3(A.ox, A.oy, A.oz, k);
+                               d = load3(A.dx, A.dy, A.dz, k);
+                               len = X::mul(t[k], 1.000001f);
+                               importance = A.imp[k];
+                               return true;
+                           });
+}
+
+// One vertex of the shader's path loop after its two walks: the vertex, the
+// halved importance, the next-event ray (when the light sample faces it) and
+// the BSDF-sampled continuation (when another vertex follows).
+__global__ void __launch_bounds__(128) k_acq_shade(HierConst c, AcqPaths A, AcqPaths B, AcqState S, int vertex) {
+    const uint32_t n = S.cnt[vertex];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t k = base + lane;
+        bool light = false, next = false;
+        float3 o, d, ld;
+        float imp = 0.0f, dist = 0.0f;
+        uint32_t seed = 0;
+        if (k < n && S.slot[k] >= 0) {
+            const int4 tri = __ldg(c.s.slots + S.slot[k]);
+            const float3 N = hit_normal(c.s, tri, S.u[k], S.v[k], nullptr);
             const MaterialData m = load_material(c.s, tri.w);
-            o = X::add3(o, X::scale(tr.t, d));
-            importance = X::mul(importance, 0.5f);
+            d = load3(A.dx, A.dy, A.dz, k);
+            o = X::add3(load3(A.ox, A.oy, A.oz, k), X::scale(S.t[k], d));
+            imp = X::mul(A.imp[k], 0.5f);
+            seed = A.seed[k];
             const uint32_t li = random_uint(seed) % c.numLightSamples;
             const float4 pn0 = __ldg(c.lightSamples + 2 * li), in1 = __ldg(c.lightSamples + 2 * li + 1);
-            float3 ld = X::sub3(xyz(pn0), o);
-            const float dist = __fsqrt_rn(X::dot(ld, ld));
+            ld = X::sub3(xyz(pn0), o);
+            dist = __fsqrt_rn(X::dot(ld, ld));
             ld = make_float3(X::div(ld.x, dist), X::div(ld.y, dist), X::div(ld.z, dist));
-            const float3 lightDir = unpack_normal(pn0.w, in1.w);
-            if (saturate(dot(lightDir, -ld)) > 0.0f) {
-                const TraceResult lr = trace_ray<false, 0>(c.s, o, ld, dist, c.err);
-                if (lr.t < dist) count_hits(c.s, c.imp, o, ld, X::mul(lr.t, 1.000001f), importance, c.err);
-            }
+            light = saturate(dot(unpack_normal(pn0.w, in1.w), -ld)) > 0.0f;
             float3 thr = f3(1.0f);
             float pdf;
             d = sample_bsdf(d, m, seed, N, thr, false, pdf);
-            o = X::add3(o, X::scale(kRAY_HIT_EPSILON, d));
+            next = vertex + 1 < kAcquirePathLength;
+        }
+        uint32_t ql, qn;
+        warp_append(S.cnt + kAcquirePathLength + 1 + vertex, light, ql);
+        if (light) {
+            store3(S.L.ox, S.L.oy, S.L.oz, ql, o);
+            store3(S.L.dx, S.L.dy, S.L.dz, ql, ld);
+            S.L.dist[ql] = dist;
+            S.L.imp[ql] = imp;
+        }
+        warp_append(S.cnt + vertex + 1, next, qn);
+        if (next) {
+            store3(B.ox, B.oy, B.oz, qn, X::add3(o, X::scale(kRAY_HIT_EPSILON, d)));
+            store3(B.dx, B.dy, B.dz, qn, d);
+            B.imp[qn] = imp;
+            B.seed[qn] = seed;
         }
     }
+}
+
+// The next-event rays: closest hit within the light distance (no offset
+// from the surface, as in the shader), then the counting up to an occluder.
+__global__ void __launch_bounds__(128) k_acq_light_trace(HierConst c, AcqRays L, const uint32_t* __restrict__ count,
+                                                         unsigned long long* work) {
+    group_walks<false, 0, 8>(
+        c.s, *count, work, c.err,
+        [&](uint64_t i, float3& o, float3& d, float& tmax) {
+            o = load3(L.ox, L.oy, L.oz, i);
+            d = load3(L.dx, L.dy, L.dz, i);
+            tmax = L.dist[i];
+        },
+        [&](uint64_t i, const GroupWalk& g) { L.t[i] = g.len; });
+}
+
+__global__ void __launch_bounds__(128) k_acq_light_count(HierConst c, AcqRays L, const uint32_t* __restrict__ count,
+                                                         unsigned long long* work) {
+    persistent_count_walks(c.s, *count, work, c.imp, c.err,
+                           [&](uint32_t k, float3& o, float3& d, float& len, float& importance) {
+                               if (!(L.t[k] < L.dist[k])) return false;  // unoccluded: nothing to count
+                               o = load3(L.ox, L.oy, L.oz, k);
+                               d = load3(L.dx, L.dy, L.dz, k);
+                               len = X::mul(L.t[k], 1.000001f);
+                               importance = L.imp[k];
+                               return true;
+                           });
 }
 
 __global__ void k_hier_prop_init(float2* imp, float* subtree, uint32_t* arrive, uint32_t numNodes, float iterations) {
@@ -656,6 +821,47 @@ gpugi_status ensure_lights(gpugi_ctx* ctx, HierBuffers* h, size_t bytes) {
     return GPUGI_OK;
 }
 
+// counters: 2 x (kAcquirePathLength + 1) uint32 in the first 128 bytes, then
+// 4 x kAcquirePathLength uint64 work counters (per vertex: path hits, path
+// counting, next-event hits, next-event counting)
+constexpr size_t kAcqCounterBytes = 128 + 8 * 4 * kAcquirePathLength;
+static_assert(4 * 2 * (kAcquirePathLength + 1) <= 128, "counter layout");
+
+// Wavefront buffers of the acquisition for `paths` paths (grown on demand).
+gpugi_status ensure_acq(gpugi_ctx* ctx, HierBuffers* h, uint64_t paths, AcqState& S) {
+    auto a = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t col = a(4 * paths);
+    if (paths > h->acqCap) {
+        GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (h->acq) cudaFree(h->acq);
+        h->acq = nullptr;
+        h->acqCap = 0;
+        if (cudaMalloc(&h->acq, (2 * 8 + 4 + 9) * col + a(kAcqCounterBytes)) != cudaSuccess) {
+            h->acq = nullptr;
+            return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "acquisition wavefront buffers");
+        }
+        h->acqCap = paths;
+    }
+    const size_t ccol = a(4 * h->acqCap);
+    char* p = static_cast<char*>(h->acq);
+    auto f = [&]() {
+        float* r = reinterpret_cast<float*>(p);
+        p += ccol;
+        return r;
+    };
+    for (AcqPaths* P : {&S.A, &S.B}) {
+        P->ox = f(), P->oy = f(), P->oz = f(), P->dx = f(), P->dy = f(), P->dz = f(), P->imp = f();
+        P->seed = reinterpret_cast<uint32_t*>(f());
+    }
+    S.slot = reinterpret_cast<int32_t*>(f());
+    S.t = f(), S.u = f(), S.v = f();
+    S.L.ox = f(), S.L.oy = f(), S.L.oz = f(), S.L.dx = f(), S.L.dy = f(), S.L.dz = f(), S.L.dist = f(),
+    S.L.imp = f(), S.L.t = f();
+    S.cnt = reinterpret_cast<uint32_t*>(p);
+    S.work = reinterpret_cast<unsigned long long*>(p + 128);
+    return GPUGI_OK;
+}
+
 // The importance pass with light samples already on the device.
 gpugi_status importance_pass(gpugi_ctx* ctx, gpugi_scene* sc, const gpugi_camera* cam, uint32_t width,
                              uint32_t height, const float4* lights, uint32_t numLightSamples, uint32_t iterations) {
@@ -666,8 +872,28 @@ gpugi_status importance_pass(gpugi_ctx* ctx, gpugi_scene* sc, const gpugi_camera
     c.numLightSamples = numLightSamples;
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(h->imp, 0, 8 * ((size_t)nn + sc->dev.numSlots), ctx->stream));
     const uint64_t work = (uint64_t)width * height * iterations;
-    const unsigned grid = (unsigned)std::min<uint64_t>((work + 127) / 128, (uint64_t)ctx->numSMs * 16);
-    k_hier_acquire<<<grid, 128, 0, ctx->stream>>>(c, iterations);
+    if (work > 0xFFFFFFFFull) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "more than 2^32 acquisition paths");
+    AcqState S;
+    gpugi_status st = ensure_acq(ctx, h, work, S);
+    if (st) return st;
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(S.cnt, 0, kAcqCounterBytes, ctx->stream));
+    const unsigned grid = (unsigned)ctx->numSMs * 8;
+    WalkerLaunch LT, LC;
+    if ((st = walker_launch_config(ctx, sc, (const void*)k_acq_trace, 1ull << 40, 0, LT)) ||
+        (st = walker_launch_config(ctx, sc, (const void*)k_acq_count, 1ull << 40, 0, LC)))
+        return st;
+    k_acq_generate<<<grid, 256, 0, ctx->stream>>>(c, iterations, S.A, S.cnt);
+    for (int vtx = 0; vtx < kAcquirePathLength; ++vtx) {
+        const uint32_t* np = S.cnt + vtx;
+        const uint32_t* nl = S.cnt + kAcquirePathLength + 1 + vtx;
+        unsigned long long* w = S.work + 4 * vtx;
+        k_acq_trace<<<LT.grid, 128, 0, ctx->stream>>>(c, S.A, np, S, w);
+        k_acq_count<<<LC.grid, 128, 0, ctx->stream>>>(c, S.A, np, S.t, w + 1);
+        k_acq_shade<<<grid, 128, 0, ctx->stream>>>(c, S.A, S.B, S, vtx);
+        k_acq_light_trace<<<LT.grid, 128, 0, ctx->stream>>>(c, S.L, nl, w + 2);
+        k_acq_light_count<<<LC.grid, 128, 0, ctx->stream>>>(c, S.L, nl, w + 3);
+        std::swap(S.A, S.B);
+    }
     const unsigned nb = (nn + 127) / 128;
     k_hier_prop_init<<<nb, 128, 0, ctx->stream>>>(h->imp, h->subtree, h->arrive, nn, (float)iterations);
     k_hier_prop_up<<<nb, 128, 0, ctx->stream>>>(sc->dev, h->imp, h->subtree, h->parents, h->arrive,
@@ -685,6 +911,7 @@ void free_hierarchy(gpugi_scene* sc) {
     if (h->block) cudaFree(h->block);
     if (h->lights) cudaFree(h->lights);
     if (h->hostLights) cudaFreeHost(h->hostLights);
+    if (h->acq) cudaFree(h->acq);
     delete h;
     sc->hier = nullptr;
 }
