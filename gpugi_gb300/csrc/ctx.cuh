@@ -28,6 +28,11 @@ struct gpugi_ctx {
     uint32_t pmPhotonsPerSample = 1u << 11;
     float pmQueryRadius = 0.01f;
     uint32_t pmProgressive = 0;
+    // importon map light tracer (PixelMapLighttracer's im_nphotons, im_r, im_progressive;
+    // pixelmaplighttracer.cpp:19-41)
+    uint32_t imPhotonsPerSample = 1u << 11;
+    float imQueryRadius = 0.005f;
+    uint32_t imProgressive = 0;
     uint32_t sharedNodes = 0;        // top-of-tree nodes laid out first and staged by ray-query walkers
     uint32_t renderSharedNodes = 0;  // nodes staged by the renderer's walkers
     void* scratch = nullptr;  // 256 B of device counters (work distribution)

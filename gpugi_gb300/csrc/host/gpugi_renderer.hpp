@@ -308,6 +308,27 @@ private:
     bool m_progressiveRadius = false;
 };
 
+// PixelMapLighttracer (gpugi/renderer/pixelmaplighttracer.hpp): an importon
+// map per iteration from the eye paths' diffuse decisions behind specular
+// bounces, photons splatting into it and reprojecting against a G-buffer.
+// The settings are the GlobalConfig parameters im_nphotons, im_r and
+// im_progressive.
+class PixelMapLighttracer : public Renderer {
+public:
+    explicit PixelMapLighttracer(RendererSystem& rendererSystem);
+    std::string GetName() const override { return "PixelMapLighttracer"; }
+    void SetScreenSize(const DeviceImage&) override {}
+    void Draw() override;
+    void SetNumPhotonsPerLightSample(unsigned int n) { m_numPhotonsPerLightSample = n; }
+    void SetQueryRadius(float r) { m_queryRadius = r; }
+    void SetProgressiveRadius(bool on) { m_progressiveRadius = on; }
+
+private:
+    unsigned int m_numPhotonsPerLightSample = 1u << 11;
+    float m_queryRadius = 0.005f;
+    bool m_progressiveRadius = false;
+};
+
 // WhittedRayTracer (gpugi/renderer/whittedraytracer.hpp): follows specular and
 // glossy decisions, ends at the first diffuse decision with two NEE samples.
 class WhittedRayTracer : public Renderer {

@@ -6,7 +6,7 @@
 //   gpugi_headless --scene FILE [--renderer Pathtracer|LightPathtracer|
 //                  BidirectionalPathtracer|NrcPathtracer|
 //                  NrcBidirectionalPathtracer|WhittedRayTracer|PhotonMapper|
-//                  HierarchyImportance]
+//                  PixelMapLighttracer|HierarchyImportance]
 //                  [--size W H]
 //                  [--camera px py pz lx ly lz fovy] [--iterations N]
 //                  [--path-length L] [--rr-start D] [--sky r g b]
@@ -94,6 +94,7 @@ int main(int argc, char** argv) {
         else if (a.renderer == "NrcBidirectionalPathtracer") system.SetRenderer<NrcBidirectionalPathtracer>();
         else if (a.renderer == "WhittedRayTracer") system.SetRenderer<WhittedRayTracer>();
         else if (a.renderer == "PhotonMapper") system.SetRenderer<PhotonMapper>();
+        else if (a.renderer == "PixelMapLighttracer") system.SetRenderer<PixelMapLighttracer>();
         else if (a.renderer == "HierarchyImportance") system.SetRenderer<HierarchyImportance>();
         else usage("unknown renderer");
 

@@ -315,6 +315,15 @@ void PhotonMapper::Draw() {
     draw_pass(m_rendererSystem, GPUGI_PASS_PM);
 }
 
+PixelMapLighttracer::PixelMapLighttracer(RendererSystem& rendererSystem) : Renderer(rendererSystem) {
+    m_rendererSystem.SetNumInitialLightSamples(128);  // pixelmaplighttracer.cpp:29
+}
+void PixelMapLighttracer::Draw() {
+    m_rendererSystem.Check(gpugi_set_importon_config(m_rendererSystem.GetContext(), m_numPhotonsPerLightSample,
+                                                     m_queryRadius, m_progressiveRadius ? 1u : 0u));
+    draw_pass(m_rendererSystem, GPUGI_PASS_IM);
+}
+
 // hierarchyimportance.cpp:20-27
 HierarchyImportance::HierarchyImportance(RendererSystem& rendererSystem) : Renderer(rendererSystem) {
     m_rendererSystem.SetNumInitialLightSamples(128);

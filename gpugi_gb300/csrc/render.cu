@@ -109,6 +109,9 @@ struct RenderConst {
     uint32_t pmCap;
     float pmSpacing, pmRadiusSq; // HashGridSpacing, PhotonQueryRadiusSq
     int photonsPerSample;        // NumPhotonsPerLightSample
+    // importon map light tracer: G-buffer of the first eye hits {position, packed normal .y}, packed normal .x
+    float4* imGbuf;
+    float* imGbufN0;
 };
 
 // ------------------------------------------------------------ accumulation
@@ -919,7 +922,7 @@ __global__ void k_photon_generate(RenderConst rc, PathSoA A) {
             create_onb(n, U, V);
             d = sample_hemisphere_cosine(random2(seed), U, V, n);
         }
-        store_path(A, g, xyz(pn0), d, tp, seed, g, 0u, 1.0f);
+        store_path(A, g, xyz(pn0), d, tp, seed, g, in1.w > 1.0f ? 1u : 0u, 1.0f);  // bit 0: left a point light
     }
 }
 
@@ -1053,6 +1056,269 @@ __global__ void __launch_bounds__(128) k_pm_shade(RenderConst rc, PathSoA A, Pat
         uint32_t qb;
         warp_append(&rc.cnt->path[depth + 1], survive, qb);
         if (survive) store_path(B, qb, o, d, tp, seed, pixel, 0u, 1.0f);
+    }
+}
+
+// ------------------------------------------------------------ importon map light tracer
+// PixelMapLighttracer (pixelmaplighttracer.cpp:76-116) with the lossless hash
+// grid and DEPTH_BUFFER_OCCLUSION_TEST, its compiled configuration: each
+// iteration an eye pass (pixelmaplt/importondistribution.comp) stores at most
+// one importon per pixel, at the eye path's first diffuse decision after at
+// least one specular bounce, and writes the first hit into a G-buffer; then
+// photons (pixelmaplt/photontracing.comp) splat every vertex into the pixels
+// of the importons around it and reproject it onto the image, where the
+// G-buffer's plane test stands in for a visibility ray.
+
+// PackHDR64 / UnpackHDR64 (helper.glsl:116-156): Y as a float, Cg and Co as
+// 12-bit mantissas with a shared exponent. ceil(log2(x)) and exp2 of the
+// integer exponent are taken exactly from the binary exponent.
+GPUGI_D int hdr64_exponent(float maxValue) {
+    if (!(maxValue > 0.0f)) return -126;  // log2(0) = -inf, clamped
+    if (isinf(maxValue)) return 127;
+    int e;
+    const float m = frexpf(maxValue, &e);  // maxValue = m 2^e, m in [0.5, 1)
+    if (m == 0.5f) --e;
+    return min(max(e, -126), 127);
+}
+GPUGI_D float2 pack_hdr64(float3 c) {
+    const float y = X::add(X::add(X::mul(c.x, 0.25f), X::mul(c.y, 0.5f)), X::mul(c.z, 0.25f));
+    const float cg = X::add(X::add(X::mul(c.x, -0.25f), X::mul(c.y, 0.5f)), X::mul(c.z, -0.25f));
+    const float co = X::add(X::mul(c.x, 0.5f), X::mul(c.z, -0.5f));
+    const int e = hdr64_exponent(fmaxf(fabsf(cg), fabsf(co)));
+    const float range = ldexpf(1.0f, e);
+    const float mx = fminf(fmaxf(X::add(X::div(X::mul(cg, 2048.0f), range), 2048.0f), 0.0f), 4095.0f);
+    const float my = fminf(fmaxf(X::add(X::div(X::mul(co, 2048.0f), range), 2048.0f), 0.0f), 4095.0f);
+    return make_float2(y, __uint_as_float(((uint32_t)mx << 20) | ((uint32_t)my << 8) | (uint32_t)(e + 126)));
+}
+GPUGI_D float3 unpack_hdr64(float2 h) {
+    const uint32_t p = __float_as_uint(h.y);
+    const float scale = ldexpf(1.0f, (int)(p & 0xFFu) - 126 - 11);  // range / 2048
+    const float cg = X::mul((float)(p >> 20) - 2048.0f, scale);
+    const float co = X::mul((float)((p >> 8) & 0xFFFu) - 2048.0f, scale);
+    const float tmp = X::sub(h.x, cg);
+    return make_float3(X::add(tmp, co), X::add(h.x, cg), X::sub(tmp, co));
+}
+
+// insertToHashGrid (maps/hashmap.glsl:31-59) of the record idx at pos;
+// returns the previous list head of its cell, or false when the table is full.
+GPUGI_D bool grid_insert(const RenderConst& rc, float3 pos, uint32_t idx, uint32_t& next) {
+    const int cx = (int)ceilf(X::div(pos.x, rc.pmSpacing)), cy = (int)ceilf(X::div(pos.y, rc.pmSpacing)),
+              cz = (int)ceilf(X::div(pos.z, rc.pmSpacing));
+    const uint32_t hash = pm_cell_hash(cx, cy, cz);
+    uint32_t i = hash % rc.pmMapSize, step = 1;
+    for (uint32_t probe = 0; probe < rc.pmMapSize; ++probe) {
+        const uint32_t key = atomicCAS(rc.pmMap + 2 * (size_t)i, 0xFFFFFFFFu, hash);
+        if (key == hash || key == 0xFFFFFFFFu) {
+            next = atomicExch(rc.pmMap + 2 * (size_t)i + 1, idx);
+            return true;
+        }
+        i = (uint32_t)(((uint64_t)i + step * 2 + 1) % rc.pmMapSize);
+        ++step;
+    }
+    return false;
+}
+
+// importondistribution.comp:21-33: one eye path per pixel (jitter with -0.5);
+// the pixel's G-buffer normal half is reset (the reference's alpha write of a
+// missed pixel) and the iteration is counted in alpha.
+__global__ void k_im_generate(RenderConst rc, PathSoA A) {
+    const uint32_t total = (uint32_t)rc.numPixels;
+    if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < total; pix += gridDim.x * blockDim.x) {
+        const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
+        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase) + pix);
+        const float3 d = primary_direction(rc, seed, x, y);
+        store_path(A, pix, rc.camPos, d, f3(1.0f), seed, pix, 0u, 1.0f);
+        rc.imGbufN0[pix] = 0.0f;
+        splat(rc, pix, f3(0.0f), 1.0f);
+    }
+}
+
+// importondistribution.comp:35-120, one bounce: the first hit goes to the
+// G-buffer (position, packed geometry normal facing the camera), emission is
+// added, and at a diffuse decision after the first vertex the importon
+// {throughput, incident direction, position, pixel} is stored in the grid and
+// the path ends; otherwise it continues with the +0.02 roulette.
+__global__ void __launch_bounds__(128) k_im_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, int depth) {
+    const uint32_t n = rc.cnt->path[depth];
+    WARP_LOOP(n, k, valid) {
+        bool survive = false;
+        float3 o, d, tp;
+        uint32_t seed = 0, pixel = 0;
+        if (valid) {
+            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+            seed = A.seed[k];
+            pixel = A.pixel[k];
+            Hit h = load_hit(rc, H, k, o, d);
+            if (!h.valid) {
+                splat(rc, pixel, tp * rc.sky);  // addition: the reference's cube-map lookup is commented out
+            } else {
+                o = h.pos;
+                if (depth == 0) {
+                    const float4 rec = __ldg(rc.s.tris + 3 * (size_t)H.slot[k] + 2);
+                    float3 gN = X::normalize(make_float3(rec.y, rec.z, rec.w));
+                    if (dot(gN, d) > 0.0f) gN = -gN;
+                    const float2 pn = pack_normal(gN);
+                    rc.imGbuf[pixel] = make_float4(o.x, o.y, o.z, pn.y);
+                    rc.imGbufN0[pixel] = pn.x;
+                }
+                splat(rc, pixel, tp * h.m.Emissivity);
+                float3 thr = f3(1.0f);
+                float pdf;
+                bool diffuse = false;
+                const float3 nd = sample_bsdf(d, h.m, seed, h.N, thr, false, pdf, false, &diffuse);
+                if (diffuse) {
+                    if (depth > 0) {
+                        float3 preflect, prefract, pdiffuse;
+                        decision_probabilities(h.m, preflect, prefract, pdiffuse);
+                        tp *= pdiffuse / fmaxf(avg3(pdiffuse), kDIVISOR_EPSILON);
+                        uint32_t next;
+                        if (grid_insert(rc, o, pixel, next)) {
+                            const float2 hdr = pack_hdr64(tp);
+                            float4* rec = rc.pmPhotons + 2 * (size_t)pixel;
+                            rec[0] = make_float4(__uint_as_float(next), hdr.x, hdr.y, __uint_as_float(pack_normal32(d)));
+                            rec[1] = make_float4(o.x, o.y, o.z,
+                                                 __uint_as_float((pixel % (uint32_t)rc.width) |
+                                                                 ((pixel / (uint32_t)rc.width) << 16)));
+                        } else {
+                            raise_error(rc.err, DEVERR_QUEUE_OVERFLOW);
+                        }
+                    }
+                } else {
+                    d = nd;
+                    o = o + d * kRAY_HIT_EPSILON;
+                    tp *= thr;
+                    survive = depth + 1 < rc.maxPathLength;
+                    if (survive && depth >= rc.rrStartDepth) {
+                        const float p = saturate(luminance(thr) + 0.02f);
+                        if (random01(seed) >= p) survive = false;
+                        else tp /= p;
+                    }
+                }
+            }
+        }
+        uint32_t qb;
+        warp_append(&rc.cnt->path[depth + 1], survive, qb);
+        if (survive) store_path(B, qb, o, d, tp, seed, pixel, 0u, 1.0f);
+    }
+}
+
+// ProjectToScreen (screenreproject.glsl:55-227) with DEPTH_BUFFER_OCCLUSION_TEST
+// and the box filter: the vertex counts for the pixel it projects to when it
+// lies on the plane of that pixel's first eye hit (within -5e-4 .. 5e-3 of the
+// camera distance) instead of when a visibility ray reaches the camera. With
+// computeFullBSDF false only the diffuse part, on the camera's side, counts.
+GPUGI_D void project_gbuffer(const RenderConst& rc, float3 pos, float3 inDir, float3 gN, float3 sN,
+                             const MaterialData& m, float3 tp, bool computeFullBSDF) {
+    float3 cd = rc.camPos - pos;
+    const float camViewDotRay = -dot(rc.camW, cd);
+    if (!(camViewDotRay > 0.0f)) return;
+    float sx = -dot(rc.camU, cd) / camViewDotRay, sy = -dot(rc.camV, cd) / camViewDotRay;
+    sx /= dot(rc.camU, rc.camU);
+    sy /= dot(rc.camV, rc.camV);
+    if (!(sx >= -1.0f && sx < 1.0f && sy > -1.0f && sy <= 1.0f)) return;
+    const float distSq = dot(cd, cd);
+    const float dist = sqrtf(distSq);
+    cd /= dist;
+    const float3 ro = cd * kRAY_HIT_EPSILON + pos;
+    const int px = (int)rintf((sx * 0.5f + 0.5f) * (float)rc.width);
+    const int py = (int)rintf((sy * 0.5f + 0.5f) * (float)rc.height);
+    if (px < 0 || py < 0 || px >= rc.width || py >= rc.height) return;  // image loads and atomics outside the image
+    const uint32_t pixel = (uint32_t)(py * rc.width + px);
+    const float4 g = rc.imGbuf[pixel];
+    const float3 occN = unpack_normal(rc.imGbufN0[pixel], g.w);
+    const float3 occPos = make_float3(g.x, g.y, g.z) - (4.0f * kRAY_HIT_EPSILON) * occN;
+    const float planeDist = dot(ro - occPos, occN) / dist;
+    if (!(planeDist >= -5e-4f && planeDist < 5e-3f)) return;
+    const float cosAtCamera = saturate(camViewDotRay / dist);
+    const float fluxToIrradiance = shading_corrected_out_dot_n(inDir, cd, gN, sN) /
+                                   (cosAtCamera * cosAtCamera * cosAtCamera * rc.pixelArea * distSq);
+    float3 bsdf;
+    if (computeFullBSDF) {
+        float pdf;
+        bsdf = adjoint_bsdf(inDir, cd, m, sN, pdf);
+    } else if (dot(inDir, sN) * dot(cd, sN) < 0.0f) {
+        float3 preflect, prefract, pdiffuse;
+        decision_probabilities(m, preflect, prefract, pdiffuse);
+        bsdf = pdiffuse * m.Diffuse * avg3(pdiffuse) / kPI;
+    } else {
+        return;
+    }
+    splat(rc, pixel, tp * fluxToIrradiance * bsdf);
+}
+
+// photontracing.comp:40-136, one bounce of one photon: the importons of the
+// 2x2x2 cells from round(pos / spacing) that lie within the query radius on
+// the surface's plane and on the photon's side receive its irradiance
+// estimate (radianceEstimate, :15-36), the vertex is reprojected, and the
+// photon continues with the adjoint BSDF and the +0.02 roulette. Info bit 0
+// marks a photon whose path is still purely specular (it left a point light).
+__global__ void __launch_bounds__(128) k_im_photon_shade(RenderConst rc, PathSoA A, PathSoA B, HitSoA H, int depth) {
+    const uint32_t n = rc.cnt->path[depth];
+    const float kernel = kPI * rc.pmRadiusSq;
+    WARP_LOOP(n, k, valid) {
+        bool survive = false;
+        float3 o, d, tp;
+        uint32_t seed = 0, gid = 0, info = 0;
+        if (valid) {
+            o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
+            d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
+            tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
+            seed = A.seed[k];
+            gid = A.pixel[k];
+            info = A.info[k];
+            const int32_t slot = H.slot[k];
+            if (slot >= 0) {
+                const float4 rec = __ldg(rc.s.tris + 3 * (size_t)slot + 2);
+                const float3 gN = make_float3(rec.y, rec.z, rec.w);  // cross(e1, e0), not normalised
+                o = X::add3(o, X::scale(H.t[k], d));
+                const int4 tri = __ldg(rc.s.slots + slot);
+                const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], nullptr);
+                const MaterialData m = load_material(rc.s, tri.w);
+                float3 preflect, prefract, pdiffuse;
+                decision_probabilities(m, preflect, prefract, pdiffuse);
+                const float3 bsdfTp = (pdiffuse * m.Diffuse) / kPI * tp;
+                const float side = dot(d, sN);
+                const int bx = (int)rintf(X::div(o.x, rc.pmSpacing)), by = (int)rintf(X::div(o.y, rc.pmSpacing)),
+                          bz = (int)rintf(X::div(o.z, rc.pmSpacing));
+                for (int c = 0; c < 8; ++c) {
+                    uint32_t idx = pm_find(rc, pm_cell_hash(bx + (c & 1), by + ((c >> 1) & 1), bz + ((c >> 2) & 1)));
+                    for (uint32_t steps = 0; idx != 0xFFFFFFFFu && steps < rc.pmCap; ++steps) {
+                        const float4 r0 = __ldg(rc.pmPhotons + 2 * (size_t)idx);
+                        const float4 r1 = __ldg(rc.pmPhotons + 2 * (size_t)idx + 1);
+                        const float3 toImporton = make_float3(r1.x, r1.y, r1.z) - o;
+                        if (dot(toImporton, toImporton) <= rc.pmRadiusSq && fabsf(dot(toImporton, sN)) < 0.01f &&
+                            side * dot(sN, unpack_normal32(__float_as_uint(r0.w))) > 0.0f) {
+                            const uint32_t pc = __float_as_uint(r1.w);
+                            const float3 vt = unpack_hdr64(make_float2(r0.y, r0.z));
+                            splat(rc, (pc >> 16) * (uint32_t)rc.width + (pc & 0xFFFFu), vt * bsdfTp / kernel);
+                        }
+                        idx = __float_as_uint(r0.x);
+                    }
+                }
+                if (avg3(tp) > 1e-10f) project_gbuffer(rc, o, d, gN, sN, m, tp, (info & 1u) != 0);
+                float3 thr = f3(1.0f);
+                float pdf;
+                bool diffuse = false;
+                const float3 nd = sample_bsdf(d, m, seed, sN, thr, true, pdf, false, &diffuse);
+                thr *= shading_correction(d, nd, gN, sN);
+                tp *= thr;
+                if (diffuse) info &= ~1u;
+                survive = depth + 1 < rc.maxPathLength;
+                if (survive && depth >= rc.rrStartDepth) {
+                    const float p = saturate(luminance(thr) + 0.02f);
+                    if (random01(seed) >= p) survive = false;
+                    else tp /= p;
+                }
+                d = nd;
+                o = o + d * kRAY_HIT_EPSILON;
+            }
+        }
+        uint32_t qb;
+        warp_append(&rc.cnt->path[depth + 1], survive, qb);
+        if (survive) store_path(B, qb, o, d, tp, seed, gid, info, 1.0f);
     }
 }
 
@@ -1589,6 +1855,9 @@ struct RenderBuffers {
     uint32_t* pmMap = nullptr;
     float4* pmPhotons = nullptr;
     uint32_t* pmCount = nullptr;
+    // importon map light tracer: G-buffer (float4 + float per pixel), zeroed when allocated
+    void* imBlock = nullptr;
+    size_t imPixels = 0;
     // batched rendering: job table + path offsets (device, pinned staging) and the replayed graph
     RenderConst *dJobs = nullptr, *hJobs = nullptr;
     uint32_t *dOffsets = nullptr, *hOffsets = nullptr;
@@ -1608,6 +1877,7 @@ static void free_render(gpugi_ctx* ctx) {
     if (rb->block) cudaFree(rb->block);
     if (rb->nrcBlock) cudaFree(rb->nrcBlock);
     if (rb->pmBlock) cudaFree(rb->pmBlock);
+    if (rb->imBlock) cudaFree(rb->imBlock);
     if (rb->hostLights) cudaFreeHost(rb->hostLights);
     delete rb;
     ctx->render = nullptr;
@@ -1759,6 +2029,26 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
             std::swap(A, B);
         }
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+    } else if (pass == GPUGI_PASS_IM) {
+        // PixelMapLighttracer::Draw (pixelmaplighttracer.cpp:76-116): clear the
+        // grid, the eye pass stores the importons, then the photons are traced
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rc.pmMap, 0xFF, 8 * (size_t)rc.pmMapSize, ctx->stream));
+        k_im_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
+        for (int depth = 0; depth < rc.maxPathLength; ++depth) {
+            launch_extend(ctx, W, rc, A, rb->H, depth);
+            k_im_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, depth);
+            std::swap(A, B);
+        }
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rc.cnt, 0, offsetof(Counters, rays), ctx->stream));
+        A = rb->A;
+        B = rb->B;
+        k_photon_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
+        for (int depth = 0; depth < rc.maxPathLength; ++depth) {
+            launch_extend(ctx, W, rc, A, rb->H, depth);
+            k_im_photon_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, depth);
+            std::swap(A, B);
+        }
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     } else if (pass == GPUGI_PASS_LT) {
         k_light_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A, false);
         if ((st = bounces(1))) return st;
@@ -1884,11 +2174,14 @@ static size_t next_prime(size_t n) {
     }
 }
 
-// Hash table of at least 1.5x the photons of an iteration, and photon
-// records for every diffuse bounce of every photon (never overflows).
-static gpugi_status ensure_pm_buffers(gpugi_ctx* ctx, RenderBuffers* rb, uint64_t photons, uint32_t maxPathLength) {
-    const size_t mapSize = next_prime((size_t)(photons * 3 / 2));
-    const size_t cap = (size_t)photons * maxPathLength;
+// Hash table of at least mapMin entries (a prime) and cap records of 32
+// bytes. The photon mapper asks for 1.5x the photons of an iteration and a
+// record for every diffuse bounce of every photon (never overflows); the
+// importon map for 1.5x the pixels and one record per pixel
+// (pixelmaplighttracer.cpp:150-158).
+static gpugi_status ensure_pm_buffers(gpugi_ctx* ctx, RenderBuffers* rb, uint64_t mapMin, uint64_t records) {
+    const size_t mapSize = next_prime((size_t)mapMin);
+    const size_t cap = (size_t)records;
     if (mapSize == rb->pmMapSize && cap <= rb->pmCap) return GPUGI_OK;
     cudaStreamSynchronize(ctx->stream);
     if (rb->pmBlock) cudaFree(rb->pmBlock);
@@ -1908,12 +2201,32 @@ static gpugi_status ensure_pm_buffers(gpugi_ctx* ctx, RenderBuffers* rb, uint64_
     return GPUGI_OK;
 }
 
+// G-buffer of the importon map light tracer, zeroed when allocated and at
+// the first iteration of an accumulation (PixelMapLighttracer::SetScreenSize,
+// pixelmaplighttracer.cpp:63-65).
+static gpugi_status ensure_im_buffers(gpugi_ctx* ctx, RenderBuffers* rb, size_t pixels, bool clear) {
+    if (pixels > rb->imPixels) {
+        cudaStreamSynchronize(ctx->stream);
+        if (rb->imBlock) cudaFree(rb->imBlock);
+        rb->imBlock = nullptr;
+        rb->imPixels = 0;
+        if (cudaMalloc(&rb->imBlock, 20 * pixels) != cudaSuccess) {
+            rb->imBlock = nullptr;
+            return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "importon map G-buffer");
+        }
+        rb->imPixels = pixels;
+        clear = true;
+    }
+    if (clear) GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->imBlock, 0, 20 * rb->imPixels, ctx->stream));
+    return GPUGI_OK;
+}
+
 // Query radius of an iteration: fixed, or shrunk by Knaus-Zwicker's
 // r_k = r_(k-1) sqrt((k + 0.7) / (k + 1)) from iteration 1 on
-// (photonmapper.cpp:84-87), in closed form through log-gamma.
-static float pm_radius(const gpugi_ctx* ctx, uint32_t iteration) {
-    const double r0 = ctx->pmQueryRadius;
-    if (!ctx->pmProgressive || iteration == 0) return (float)r0;
+// (photonmapper.cpp:84-87, pixelmaplighttracer.cpp:82-87), in closed form
+// through log-gamma.
+static float grid_radius(double r0, bool progressive, uint32_t iteration) {
+    if (!progressive || iteration == 0) return (float)r0;
     const double k = iteration;
     const double logProd = std::lgamma(k + 1.7) - std::lgamma(1.7) - (std::lgamma(k + 2.0) - std::lgamma(2.0));
     return (float)(r0 * std::exp(0.5 * logProd));
@@ -2026,7 +2339,7 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
                           gpugi_image* im) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass > GPUGI_PASS_HIERARCHY) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->pass > GPUGI_PASS_IM) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)
@@ -2045,12 +2358,13 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
     const uint32_t raysPerLight = rays_per_light_sample(p);
     const uint32_t lightThreads = raysPerLight * p->numLightSamples;
     // Whitted: up to two shadow rays per path, so the queues get twice the paths
-    const bool pm = p->pass == GPUGI_PASS_PM;
-    const uint64_t photons = pm ? (uint64_t)p->numLightSamples * ctx->pmPhotonsPerSample : 0;
+    const bool pm = p->pass == GPUGI_PASS_PM, imap = p->pass == GPUGI_PASS_IM, grid = pm || imap;
+    const uint64_t photons =
+        grid ? (uint64_t)p->numLightSamples * (imap ? ctx->imPhotonsPerSample : ctx->pmPhotonsPerSample) : 0;
     if (photons > (64ull << 20)) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "more than 64M photons per iteration");
     const uint32_t perSamplePaths = p->pass == GPUGI_PASS_PT        ? numPixels
                                     : p->pass == GPUGI_PASS_WHITTED ? 2 * numPixels
-                                    : pm                            ? std::max<uint32_t>(numPixels, (uint32_t)photons)
+                                    : grid                          ? std::max<uint32_t>(numPixels, (uint32_t)photons)
                                                                     : std::max(numPixels, lightThreads);
     // Light-cache capacity: the worst case (every particle stores its light
     // sample plus one entry per bounce) so it can never overflow.
@@ -2059,14 +2373,17 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
     uint64_t chunk = std::max<uint64_t>(1, (16ull << 20) / perSamplePaths);
     if (cachePerSample) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, (4ull << 30) / (cachePerSample * 64)));
     chunk = std::min<uint64_t>(chunk, p->samples);
-    if (pm) chunk = 1;  // one photon map per iteration
+    if (grid) chunk = 1;  // one photon (importon) map per iteration
     const size_t lightBytes = chunk * p->numLightSamples * 32;
     gpugi_status st = ensure_buffers(ctx, chunk * perSamplePaths, chunk * cachePerSample * 64, lightBytes,
                                      (uint32_t)chunk);
     if (st) return st;
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
     if ((st = ensure_host_lights(ctx, rb, lightBytes))) return st;
-    if (pm && (st = ensure_pm_buffers(ctx, rb, photons, p->maxPathLength))) return st;
+    if (pm && (st = ensure_pm_buffers(ctx, rb, photons * 3 / 2, photons * p->maxPathLength))) return st;
+    if (imap && ((st = ensure_pm_buffers(ctx, rb, (uint64_t)numPixels * 3 / 2, numPixels)) ||
+               (st = ensure_im_buffers(ctx, rb, numPixels, p->iteration == 0))))
+        return st;
 
     RenderConst rc = make_render_const(ctx, sc, cam, p, im, rb);
     rc.numRaysPerLightSample = (int)raysPerLight;
@@ -2080,14 +2397,25 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
         rc.pmCap = (uint32_t)(photons * p->maxPathLength);
         rc.photonsPerSample = (int)ctx->pmPhotonsPerSample;
     }
+    if (imap) {
+        rc.pmMap = rb->pmMap;
+        rc.pmMapSize = (uint32_t)rb->pmMapSize;
+        rc.pmPhotons = rb->pmPhotons;
+        rc.pmCount = rb->pmCount;
+        rc.pmCap = numPixels;
+        rc.photonsPerSample = (int)ctx->imPhotonsPerSample;
+        rc.imGbuf = static_cast<float4*>(rb->imBlock);
+        rc.imGbufN0 = reinterpret_cast<float*>(static_cast<char*>(rb->imBlock) + 16 * (size_t)numPixels);
+    }
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
     for (uint32_t s0 = 0; s0 < p->samples; s0 += (uint32_t)chunk) {
         const uint32_t ns = std::min<uint32_t>((uint32_t)chunk, p->samples - s0);
         if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, s0, ns, p->numLightSamples))) return st;
         rc.samples = ns;
         rc.sampleBase = s0;
-        if (pm) {
-            const float r = pm_radius(ctx, p->iteration + s0);
+        if (grid) {
+            const float r = imap ? grid_radius(ctx->imQueryRadius, ctx->imProgressive, p->iteration + s0)
+                               : grid_radius(ctx->pmQueryRadius, ctx->pmProgressive, p->iteration + s0);
             rc.pmRadiusSq = r * r;
             rc.pmSpacing = r * 2.01f;
         }
@@ -2238,7 +2566,7 @@ static gpugi_status check_render_args(gpugi_ctx* ctx, const gpugi_scene* sc, con
                                       const gpugi_render_params* p, const float* lightSamples,
                                       const uint64_t* rngState, const gpugi_image* im) {
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
-    if (p->pass > GPUGI_PASS_HIERARCHY) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->pass > GPUGI_PASS_IM) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)
@@ -2262,6 +2590,19 @@ gpugi_status gpugi_set_photon_config(gpugi_ctx* ctx, uint32_t photonsPerLightSam
     ctx->pmPhotonsPerSample = photonsPerLightSample;
     ctx->pmQueryRadius = queryRadius;
     ctx->pmProgressive = progressive ? 1u : 0u;
+    return GPUGI_OK;
+}
+
+gpugi_status gpugi_set_importon_config(gpugi_ctx* ctx, uint32_t photonsPerLightSample, float queryRadius,
+                                       uint32_t progressive) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (photonsPerLightSample == 0 || photonsPerLightSample > (1u << 20))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "photonsPerLightSample must be in [1, 2^20]");
+    if (!(queryRadius > 0.0f) || !(queryRadius < 1e30f))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "queryRadius must be positive and finite");
+    ctx->imPhotonsPerSample = photonsPerLightSample;
+    ctx->imQueryRadius = queryRadius;
+    ctx->imProgressive = progressive ? 1u : 0u;
     return GPUGI_OK;
 }
 

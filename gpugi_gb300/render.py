@@ -11,10 +11,10 @@ import numpy as np
 
 from . import cuda
 
-PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3, "PM": 4, "HIERARCHY": 5}
+PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3, "PM": 4, "HIERARCHY": 5, "IM": 6}
 # Initial light samples per iteration as each renderer configures them
 # (pathtracer.cpp:28, lightpathtracer.cpp:16, bidirectionalpathtracer.cpp:160).
-DEFAULT_LIGHT_SAMPLES = {"PT": 128, "LT": 256, "BPT": 128, "WHITTED": 128, "PM": 128, "HIERARCHY": 128}
+DEFAULT_LIGHT_SAMPLES = {"PT": 128, "LT": 256, "BPT": 128, "WHITTED": 128, "PM": 128, "HIERARCHY": 128, "IM": 128}
 
 
 class Camera(C.Structure):
@@ -53,6 +53,7 @@ def _declare():
     L.gpugi_render_batch.argtypes = [P, P, U32]
     L.gpugi_set_batch_config.argtypes = [P, U32, U32]
     L.gpugi_set_photon_config.argtypes = [P, U32, C.c_float, U32]
+    L.gpugi_set_importon_config.argtypes = [P, U32, C.c_float, U32]
     L._render_declared = True
     return L
 
@@ -195,6 +196,13 @@ def set_photon_config(ctx: cuda.Context, photons_per_light_sample: int = 2048, q
                       progressive: bool = False) -> None:
     """Photon mapper settings (gpugi_set_photon_config)."""
     ctx.check(_declare().gpugi_set_photon_config(ctx.handle, photons_per_light_sample, float(query_radius),
+                                                  int(bool(progressive))))
+
+
+def set_importon_config(ctx: cuda.Context, photons_per_light_sample: int = 2048, query_radius: float = 0.005,
+                      progressive: bool = False) -> None:
+    """Importon map light tracer settings (gpugi_set_importon_config)."""
+    ctx.check(_declare().gpugi_set_importon_config(ctx.handle, photons_per_light_sample, float(query_radius),
                                                   int(bool(progressive))))
 
 

@@ -233,6 +233,16 @@ gpugi_status gpugi_set_scene_layout(gpugi_ctx* ctx, uint32_t sharedNodes, uint32
  *                             hierarchy/hierarchypathtracer.comp; needs an AABB hierarchy and
  *                             the node NDFs (gpugi_scene_set_hierarchy_ndf); maxPathLength is
  *                             the shader's MAX_PATHLENGTH (4 in the reference)
+ *   gpugi_render(pass = IM)   PixelMapLighttracer::Draw (gpugi/renderer/pixelmaplighttracer.cpp:
+ *                             76-116) as compiled there (lossless hash grid,
+ *                             DEPTH_BUFFER_OCCLUSION_TEST): the eye pass stores one importon
+ *                             per pixel in the hash grid and the first hits in a G-buffer
+ *                             (pixelmaplt/importondistribution.comp), then the photons splat
+ *                             into the importons' pixels and reproject against the G-buffer
+ *                             (pixelmaplt/photontracing.comp); one importon map per iteration,
+ *                             see gpugi_set_importon_config. The G-buffer is cleared at
+ *                             iteration 0 and carries a missed pixel's previous first hit, as
+ *                             the reference's position texture does
  * ------------------------------------------------------------------------ */
 typedef struct gpugi_image gpugi_image;
 
@@ -242,7 +252,8 @@ enum gpugi_pass {
     GPUGI_PASS_BPT = 2,
     GPUGI_PASS_WHITTED = 3,
     GPUGI_PASS_PM = 4,
-    GPUGI_PASS_HIERARCHY = 5
+    GPUGI_PASS_HIERARCHY = 5,
+    GPUGI_PASS_IM = 6
 };
 
 /* Camera UBO (gpugi/shader/globaluniforms.glsl:7-15): U, V scaled by
@@ -394,7 +405,7 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* scene, const gp
  * and width x height) is refused with GPUGI_ERROR_INVALID_ARGUMENT. BPT
  * connections pick light-cache entries whose order follows the device's
  * atomic appends, so a BPT job equals gpugi_render's in distribution (and
- * exactly at maxPathLength 1). Whitted and photon-mapper jobs are rendered
+ * exactly at maxPathLength 1). Whitted, photon-mapper and importon-map jobs are rendered
  * afterwards, one gpugi_render call each. Jobs that share an rngState draw
  * their light samples in round order. */
 typedef struct gpugi_job {
@@ -419,6 +430,13 @@ gpugi_status gpugi_set_batch_config(gpugi_ctx* ctx, uint32_t pathsPerRound, uint
  * 2.01 x radius) and Knaus-Zwicker radius shrinking per iteration (default 0). */
 gpugi_status gpugi_set_photon_config(gpugi_ctx* ctx, uint32_t photonsPerLightSample, float queryRadius,
                                      uint32_t progressive);
+
+/* Importon map light tracer settings (PixelMapLighttracer's im_nphotons,
+ * im_r and im_progressive; gpugi/renderer/pixelmaplighttracer.cpp:19-41):
+ * photons per light sample (default 2048), query radius (default 0.005; grid
+ * spacing 2.01 x radius) and Knaus-Zwicker radius shrinking (default 0). */
+gpugi_status gpugi_set_importon_config(gpugi_ctx* ctx, uint32_t photonsPerLightSample, float queryRadius,
+                                       uint32_t progressive);
 
 /* Hierarchy-importance renderer (HierarchyImportance, gpugi/renderer/
  * hierarchyimportance.cpp). AABB hierarchies only: the reference's

@@ -105,10 +105,13 @@ PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3}
 def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.ndarray, frame_seed: int,
            light_samples: np.ndarray, max_path_length: int = 8, rr_start_depth: int = 0, sky=(0.0, 0.0, 0.0),
            accum: np.ndarray | None = None, num_threads=None, photons_per_light_sample: int = 2048,
-           query_radius: float = 0.01) -> np.ndarray:
+           query_radius: float = 0.01, gbuffer: np.ndarray | None = None) -> np.ndarray:
     """One iteration of a pass (restated pathtracer.comp / lighttracer.comp /
-    BPT / whittedraytracer.comp / the photon mapper "PM"), accumulated into
-    accum (H, W, 4) float32, which is returned."""
+    BPT / whittedraytracer.comp / the photon mapper "PM" / the importon map
+    light tracer "IM"), accumulated into accum (H, W, 4) float32, which is
+    returned. "IM" also needs gbuffer, an (H, W, 5) float32 array of the
+    first eye hits that the caller carries from iteration to iteration
+    (zeros before the first)."""
     from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
     L = lib()
     P, U32, I, F = C.c_void_p, C.c_uint32, C.c_int, C.c_float
@@ -131,6 +134,18 @@ def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.nda
                                 _p(pos), _p(vi), pos.shape[0], _p(mats), mats.shape[0], width, height,
                                 max_path_length, rr_start_depth, _p(cam), frame_seed & 0xFFFFFFFF, _p(ls),
                                 ls.shape[0], _p(skya), photons_per_light_sample, float(query_radius), _p(accum), nt)
+        assert rc == 0
+        return accum
+    if pass_ == "IM":
+        assert gbuffer is not None and gbuffer.shape == (height, width, 5) and gbuffer.dtype == np.float32
+        assert gbuffer.flags.c_contiguous
+        L.oracle_render_im.argtypes = [P, U32, U32, P, U32, U32, P, P, U32, P, U32, I, I, I, I, P, U32, P, I, P, I,
+                                       F, P, P, I]
+        rc = L.oracle_render_im(_p(hier), hier.shape[0], bvh.bounds_kind, _p(slots), slots.shape[0], bvh.leaf_size,
+                                _p(pos), _p(vi), pos.shape[0], _p(mats), mats.shape[0], width, height,
+                                max_path_length, rr_start_depth, _p(cam), frame_seed & 0xFFFFFFFF, _p(ls),
+                                ls.shape[0], _p(skya), photons_per_light_sample, float(query_radius), _p(accum),
+                                _p(gbuffer), nt)
         assert rc == 0
         return accum
     rc = L.oracle_render(_p(hier), hier.shape[0], bvh.bounds_kind, _p(slots), slots.shape[0], bvh.leaf_size,

@@ -595,6 +595,223 @@ static vec3 GatherPixel(const RenderScene& s, const Params& P, const PhotonGrid&
     return color;
 }
 
+// ----------------------------------------------------------- pixelmaplt/*
+// PackHDR64 / UnpackHDR64 (helper.glsl:116-156): YCgCo, Y as a float, Cg and
+// Co as 12-bit mantissas over a shared exponent ceil(log2(max |Cg|, |Co|)),
+// clamped to [-126, 127]; log2 and exp2 taken exactly from the binary exponent.
+static int Hdr64Exponent(float maxValue) {
+    if (!(maxValue > 0.0f)) return -126;
+    if (std::isinf(maxValue)) return 127;
+    int e;
+    float m = std::frexp(maxValue, &e);
+    if (m == 0.5f) --e;
+    return std::min(std::max(e, -126), 127);
+}
+static vec2 PackHDR64(vec3 c) {
+    float y = c.x * 0.25f + c.y * 0.5f + c.z * 0.25f;
+    float cg = c.x * -0.25f + c.y * 0.5f + c.z * -0.25f;
+    float co = c.x * 0.5f + c.z * -0.5f;
+    int e = Hdr64Exponent(max(abs(cg), abs(co)));
+    float range = std::ldexp(1.0f, e);
+    float mx = clamp(cg * 2048.0f / range + 2048.0f, 0.0f, 4095.0f);
+    float my = clamp(co * 2048.0f / range + 2048.0f, 0.0f, 4095.0f);
+    return vec2(y, uintBitsToFloat(((uint)mx << 20) | ((uint)my << 8) | (uint)(e + 126)));
+}
+static vec3 UnpackHDR64(vec2 h) {
+    uint p = floatBitsToUint(h.y);
+    float scale = std::ldexp(1.0f, (int)(p & 0xFFu) - 126) / 2048.0f;
+    float cg = ((float)(p >> 20) - 2048.0f) * scale;
+    float co = ((float)((p >> 8) & 0xFFFu) - 2048.0f) * scale;
+    float tmp = h.x - cg;
+    return vec3(tmp + co, h.x + cg, tmp - co);
+}
+
+struct Importon {
+    vec2 throughput;  // PackHDR64
+    uint dir;         // PackNormal32 of the incident direction
+    vec3 pos;
+    int x, y;
+};
+// G-buffer of the first eye hits: position, packed geometry normal (the
+// reference keeps .x in the output image's alpha and the rest in a texture).
+struct GBufferTexel {
+    float px, py, pz, n1, n0;
+};
+
+// importondistribution.comp:19-120 with DEPTH_BUFFER_OCCLUSION_TEST and the
+// lossless hash map: one eye path; returns its emission and, at a diffuse
+// decision after the first vertex, the importon.
+static vec3 ImportonPixel(const RenderScene& s, const Params& P, int x, int y, GBufferTexel& gb, Importon& imp,
+                          bool& stored) {
+    stored = false;
+    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    Ray ray = PrimaryRay(P, seed, x, y);
+    vec3 color(0.0f), pathThroughput(1.0f);
+    gb.n0 = 0.0f;  // color_a.w of a path that misses
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        if (rayHit == RAY_MAX) {
+            color += pathThroughput * P.sky;  // addition: the reference's cube-map lookup is commented out
+            break;
+        }
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 hitNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        if (i == 0) {
+            vec3 gN = normalize(hit.normal);
+            vec2 packed = PackNormal(dot(gN, ray.Direction) > 0.0f ? -gN : gN);
+            gb = GBufferTexel{ray.Origin.x, ray.Origin.y, ray.Origin.z, packed.y, packed.x};
+        }
+        color += pathThroughput * m.Emissivity;
+        vec3 throughput(1.0f);
+        float pdf;
+        bool diffuse = false;
+        vec3 newDirection = SampleBSDFImpl(ray.Direction, m, seed, hitNormal, throughput, false, pdf, &diffuse);
+        vec3 pDiffuse = GetDiffuseProbability(m, saturate(abs(dot(hitNormal, ray.Direction))));
+        if (diffuse) {
+            if (i > 0) {
+                pathThroughput *= pDiffuse / max(Avg(pDiffuse), DIVISOR_EPSILON);
+                imp = Importon{PackHDR64(pathThroughput), PackNormal32(ray.Direction), ray.Origin, x, y};
+                stored = true;
+            }
+            break;
+        }
+        ray.Direction = newDirection;
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+        pathThroughput *= throughput;
+        if (i >= P.rrStartDepth) {
+            float p = saturate(GetLuminance(throughput) + 0.02f);
+            if (Random(seed) >= p) break;
+            pathThroughput /= p;
+        }
+    }
+    return color;
+}
+
+struct ImportonGrid {
+    float spacing = 0.0f, radiusSq = 0.0f;
+    std::unordered_map<CellKey, std::vector<uint32_t>, CellHash> cells;
+    std::vector<Importon> importons;
+};
+
+// ProjectToScreen (screenreproject.glsl:55-227) under DEPTH_BUFFER_OCCLUSION_TEST:
+// the G-buffer plane test of the pixel replaces the visibility ray.
+static void ProjectToScreenGBuffer(const Params& P, Image& img, const GBufferTexel* gbuf, const Ray& ray,
+                                   vec3 geometryNormal, vec3 shadingNormal, const MaterialData& m,
+                                   vec3 pathThroughput, bool computeFullBSDF) {
+    Ray cameraRay;
+    cameraRay.Direction = P.camPos - ray.Origin;
+    float camViewDotRay = -dot(P.camW, cameraRay.Direction);
+    if (!(camViewDotRay > 0.0f)) return;
+    vec3 proj(-dot(P.camU, cameraRay.Direction), -dot(P.camV, cameraRay.Direction), camViewDotRay);
+    vec2 screen(proj.x / proj.z, proj.y / proj.z);
+    screen.x /= dot(P.camU, P.camU);
+    screen.y /= dot(P.camV, P.camV);
+    if (!(screen.x >= -1.0f && screen.x < 1.0f && screen.y > -1.0f && screen.y <= 1.0f)) return;
+    float cameraDistSq = dot(cameraRay.Direction, cameraRay.Direction);
+    float cameraDist = sqrt(cameraDistSq);
+    cameraRay.Direction /= cameraDist;
+    cameraRay.Origin = cameraRay.Direction * RAY_HIT_EPSILON + ray.Origin;
+    vec2 pixelPos = (screen * 0.5f + vec2(0.5f)) * vec2((float)P.width, (float)P.height);
+    int px = (int)std::nearbyint(pixelPos.x), py = (int)std::nearbyint(pixelPos.y);
+    if (px < 0 || py < 0 || px >= P.width || py >= P.height) return;
+    const GBufferTexel& g = gbuf[(size_t)py * P.width + px];
+    vec3 occluderNormal = UnpackNormal(vec2(g.n0, g.n1));
+    vec3 occluderPos = vec3(g.px, g.py, g.pz) - (4.0f * RAY_HIT_EPSILON) * occluderNormal;
+    float planeDist = dot(cameraRay.Origin - occluderPos, occluderNormal) / cameraDist;
+    if (!(planeDist >= -5e-4f && planeDist < 5e-3f)) return;
+    float cosAtCamera = saturate(camViewDotRay / cameraDist);
+    float fluxToIrradiance = AdjointBSDFShadingNormalCorrectedOutDotN(ray.Direction, cameraRay.Direction,
+                                                                      geometryNormal, shadingNormal) /
+                             (cosAtCamera * cosAtCamera * cosAtCamera * P.pixelArea * cameraDistSq);
+    vec3 bsdf(1.0f);
+    if (computeFullBSDF) {
+        float pdf;
+        bsdf = AdjointBSDF(ray.Direction, cameraRay.Direction, m, shadingNormal, pdf);
+    } else if (dot(ray.Direction, shadingNormal) * dot(cameraRay.Direction, shadingNormal) < 0.0f) {
+        vec3 pDiffuse = GetDiffuseProbability(m, abs(dot(ray.Direction, shadingNormal)));
+        bsdf = pDiffuse * m.Diffuse * Avg(pDiffuse) / PI;
+    } else {
+        bsdf = vec3(0.0f);
+    }
+    Splat(img, px, py, pathThroughput * fluxToIrradiance * bsdf);
+}
+
+// photontracing.comp:38-136 (REPROJECT, USE_PIXEL_CACHE, lossless hash map),
+// one photon path.
+static void ImportonPhotonThread(const RenderScene& s, const Params& P, Image& img, const GBufferTexel* gbuf,
+                                 const ImportonGrid& grid, uint gid, int photonsPerSample) {
+    uint seed = InitRandomSeed(P.frameSeed, gid);
+    int lightSampleIndex = int(gid / (uint)photonsPerSample);
+    vec4 pn0 = P.lightSamples[2 * lightSampleIndex];
+    vec4 in1 = P.lightSamples[2 * lightSampleIndex + 1];
+    vec3 pathThroughput = in1.xyz() * (PI / (float)photonsPerSample);
+    bool specularPath = false;
+    Ray ray;
+    ray.Origin = pn0.xyz();
+    if (in1.w > 1.5f) {
+        ray.Direction = SampleDirection(Random2(seed));
+        pathThroughput *= 4.0f;
+        specularPath = true;
+    } else {
+        vec3 normal = UnpackNormal(vec2(pn0.w, in1.w));
+        vec3 U, V;
+        CreateONB(normal, U, V);
+        ray.Direction = SampleHemisphereCosine(Random2(seed), U, V, normal);
+    }
+    for (int i = 0; i < P.maxPathLength; ++i) {
+        HitRecord hit;
+        float rayHit = RAY_MAX;
+        TraceRay(s.geo, ray, rayHit, hit, nullptr);
+        if (rayHit == RAY_MAX) break;
+        vec3 geometryNormal = hit.normal;
+        ray.Origin = ray.Origin + rayHit * ray.Direction;
+        vec3 shadingNormal;
+        vec2 tc;
+        GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, shadingNormal, tc);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        float cosThetaAbs = saturate(abs(dot(shadingNormal, ray.Direction)));
+        vec3 bsdf = GetDiffuseProbability(m, cosThetaAbs) * m.Diffuse / PI;
+        const int bx = (int)std::nearbyint(ray.Origin.x / grid.spacing);
+        const int by = (int)std::nearbyint(ray.Origin.y / grid.spacing);
+        const int bz = (int)std::nearbyint(ray.Origin.z / grid.spacing);
+        for (int c = 0; c < 8; ++c) {
+            auto it = grid.cells.find(CellKey{bx + (c & 1), by + ((c >> 1) & 1), bz + ((c >> 2) & 1)});
+            if (it == grid.cells.end()) continue;
+            for (uint32_t k : it->second) {  // radianceEstimate (photontracing.comp:15-36)
+                const Importon& im = grid.importons[k];
+                vec3 toImporton = im.pos - ray.Origin;
+                vec3 incidentDirection = UnpackNormal32(im.dir);
+                if (dot(toImporton, toImporton) <= grid.radiusSq && abs(dot(toImporton, shadingNormal)) < 0.01f &&
+                    dot(ray.Direction, shadingNormal) * dot(shadingNormal, incidentDirection) > 0.0f) {
+                    vec3 viewPathThroughput = UnpackHDR64(im.throughput);
+                    Splat(img, im.x, im.y, viewPathThroughput * (bsdf * pathThroughput) / (PI * grid.radiusSq));
+                }
+            }
+        }
+        if (Avg(pathThroughput) > 1e-10f)
+            ProjectToScreenGBuffer(P, img, gbuf, ray, geometryNormal, shadingNormal, m, pathThroughput, specularPath);
+        vec3 throughput(1.0f);
+        float samplePDF;
+        bool diffuse = false;
+        vec3 newDirection = SampleBSDFImpl(ray.Direction, m, seed, shadingNormal, throughput, true, samplePDF, &diffuse);
+        throughput *= AdjointBSDFShadingNormalCorrection(ray.Direction, newDirection, geometryNormal, shadingNormal);
+        pathThroughput *= throughput;
+        specularPath = specularPath && !diffuse;
+        if (i >= P.rrStartDepth) {
+            float p = saturate(GetLuminance(throughput) + 0.02f);
+            if (Random(seed) >= p) break;
+            pathThroughput /= p;
+        }
+        ray.Direction = newDirection;
+        ray.Origin += ray.Direction * RAY_HIT_EPSILON;
+    }
+}
+
 // ------------------------------------------------------------ lightcache.glsl
 struct LightCacheEntry {
     vec3 Flux;
@@ -1509,6 +1726,83 @@ int oracle_render_pm(const float* hierarchy, uint32_t numNodes, uint32_t boundsK
             o[2] += c.z;
             o[3] += 1.0f;
         }
+    });
+    return 0;
+}
+
+// Importon map light tracer iteration (PixelMapLighttracer::Draw,
+// gpugi/renderer/pixelmaplighttracer.cpp:76-116): the eye pass stores the
+// importons (one per pixel at most) and the first hits in gbuf (w*h*5 floats,
+// carried from iteration to iteration: zeros before the first), then the
+// photons splat into the importons' pixels and reproject; rgba as oracle_render.
+int oracle_render_im(const float* hierarchy, uint32_t numNodes, uint32_t boundsKind, const int32_t* slots,
+                     uint32_t numSlots, uint32_t leafSize, const float* positions, const float* vertexInfo,
+                     uint32_t numVertices, const float* materials, uint32_t numMaterials, int width, int height,
+                     int maxPathLength, int rrStartDepth, const float* cam, uint32_t frameSeed,
+                     const float* lightSamples, int numLightSamples, const float* sky, int photonsPerLightSample,
+                     float queryRadius, float* rgba, float* gbuf, int numThreads) {
+    RenderScene s;
+    s.geo.hierarchy = reinterpret_cast<const vec4*>(hierarchy);
+    s.geo.numNodes = numNodes;
+    s.geo.boundsKind = boundsKind;
+    s.geo.triangles = reinterpret_cast<const ivec4*>(slots);
+    s.geo.numSlots = numSlots;
+    s.geo.leafSize = leafSize;
+    s.geo.positions = positions;
+    s.geo.numVertices = numVertices;
+    s.geo.vertexInfo = reinterpret_cast<const vec4*>(vertexInfo);
+    s.materials = materials;
+    s.numMaterials = numMaterials;
+    Params P;
+    P.width = width;
+    P.height = height;
+    P.maxPathLength = maxPathLength;
+    P.rrStartDepth = rrStartDepth;
+    P.camU = vec3(cam[0], cam[1], cam[2]);
+    P.camV = vec3(cam[3], cam[4], cam[5]);
+    P.camW = vec3(cam[6], cam[7], cam[8]);
+    P.camPos = vec3(cam[9], cam[10], cam[11]);
+    P.pixelArea = cam[12];
+    P.frameSeed = frameSeed;
+    P.numLightSamples = numLightSamples;
+    P.lightSamples = reinterpret_cast<const vec4*>(lightSamples);
+    P.sky = sky ? vec3(sky[0], sky[1], sky[2]) : vec3(0.0f);
+    P.numRaysPerLightSample = 0;
+    if (photonsPerLightSample <= 0 || !(queryRadius > 0.0f) || !gbuf) return -1;
+    const size_t numPixels = (size_t)width * height;
+    GBufferTexel* gb = reinterpret_cast<GBufferTexel*>(gbuf);
+    std::vector<Importon> imp(numPixels);
+    std::vector<char> stored(numPixels, 0);
+    ParallelFor((uint64_t)numPixels, numThreads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t p = b; p < e; ++p) {
+            int x = (int)(p % width), y = (int)(p / width);
+            bool st = false;
+            vec3 c = ImportonPixel(s, P, x, y, gb[p], imp[p], st);
+            stored[p] = st;
+            float* o = rgba + 4 * p;
+            o[0] += c.x;
+            o[1] += c.y;
+            o[2] += c.z;
+            o[3] += 1.0f;
+        }
+    });
+    ImportonGrid grid;
+    grid.spacing = queryRadius * 2.01f;
+    grid.radiusSq = queryRadius * queryRadius;
+    for (size_t p = 0; p < numPixels; ++p) {
+        if (!stored[p]) continue;
+        const Importon& im = imp[p];
+        const uint32_t k = (uint32_t)grid.importons.size();
+        grid.importons.push_back(im);
+        CellKey key{(int)std::ceil(im.pos.x / grid.spacing), (int)std::ceil(im.pos.y / grid.spacing),
+                    (int)std::ceil(im.pos.z / grid.spacing)};
+        grid.cells[key].push_back(k);
+    }
+    std::vector<std::mutex> locks(height);
+    Image img{rgba, width, height, locks.data()};
+    const uint64_t nPhotons = (uint64_t)numLightSamples * (uint64_t)photonsPerLightSample;
+    ParallelFor(nPhotons, numThreads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t g = b; g < e; ++g) ImportonPhotonThread(s, P, img, gb, grid, (uint)g, photonsPerLightSample);
     });
     return 0;
 }

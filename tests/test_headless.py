@@ -53,7 +53,8 @@ CAM = [0.0, 1.0, 3.4, 0.0, 1.0, 0.0, 40.0]
 @pytest.mark.gpu
 @pytest.mark.parametrize("renderer,pass_", [("Pathtracer", "PT"), ("BidirectionalPathtracer", "BPT"),
                                             ("LightPathtracer", "LT"), ("WhittedRayTracer", "WHITTED"),
-                                            ("PhotonMapper", "PM"), ("HierarchyImportance", "HIERARCHY")])
+                                            ("PhotonMapper", "PM"), ("PixelMapLighttracer", "IM"),
+                                            ("HierarchyImportance", "HIERARCHY")])
 def test_headless_matches_the_c_abi(cuda_ctx, room_file, tmp_path, renderer, pass_):
     sc, path = room_file
     W = H = 32

@@ -273,6 +273,82 @@ def test_photon_mapper_converges_to_path_tracing(cuda_ctx, room):
         x.close()
 
 
+def _oracle_im(b, sc, W, H, cam, ls, iters, **kw):
+    acc, gbuf = None, np.zeros((H, W, 5), np.float32)
+    for s in range(iters):
+        acc = oracle.render(b, sc, "IM", W, H, cam.as_array(), render.wanghash(s), ls[s], accum=acc, gbuffer=gbuf,
+                            **kw)
+    return acc
+
+
+def test_importon_map_matches_oracle_per_pixel(cuda_ctx, glossy_room):
+    """PixelMapLighttracer (importondistribution.comp + photontracing.comp)
+    at its defaults, 2048 photons per light sample and query radius 0.005:
+    the eye paths store the same importons (bit-identical walks, the same
+    packed throughputs and directions), the photons gather them and
+    reproject against the same G-buffer; a pixel differs when rounding
+    diverts a photon, so most pixels agree to 1e-3 of the image maximum."""
+    sc, b, ds = glossy_room
+    W = H = 48
+    iters = 4
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    ls = _light_sets(ds, iters, 128)
+    render.set_importon_config(cuda_ctx, 2048, 0.005)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, img, "IM", max_path_length=6, samples=iters, iteration=0, light_samples=ls)
+    g = img.read()
+    o = _oracle_im(b, sc, W, H, cam, ls, iters, max_path_length=6, photons_per_light_sample=2048,
+                   query_radius=0.005)
+    assert np.all(g[..., 3] == iters) and np.all(o[..., 3] == iters)
+    close = np.abs(g[..., :3] - o[..., :3]) <= 1e-3 * np.abs(o[..., :3]).max() + 1e-5
+    assert close.all(-1).mean() > 0.9, close.all(-1).mean()
+    assert abs(g[..., :3].mean() / o[..., :3].mean() - 1) < 0.02, (g[..., :3].mean(), o[..., :3].mean())
+    assert cuda_ctx.device_error_bits() == 0
+    img.close()
+
+
+def test_importon_map_converges_to_path_tracing(cuda_ctx, glossy_room):
+    """On the glossy room the importon-map image (reprojected light paths
+    plus importons behind the glossy bounces, radius 0.02) approaches the
+    path-traced image: image means within a few percent, and the importons
+    carry a share of the light (the image is darker without them)."""
+    sc, b, ds = glossy_room
+    W = H = 32
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    render.set_importon_config(cuda_ctx, 4096, 0.02)
+    im = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, im, "IM", max_path_length=8, samples=32, rng_state=[3])
+    pt = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, pt, "PT", max_path_length=8, samples=256, rng_state=[4])
+    a, r = im.read()[..., :3].mean() / 32, pt.read()[..., :3].mean() / 256
+    assert abs(a / r - 1) < 0.08, (a, r)
+    render.set_importon_config(cuda_ctx, 4096, 1e-6)  # a radius that finds no importon
+    none = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, none, "IM", max_path_length=8, samples=32, rng_state=[3])
+    assert none.read()[..., :3].mean() / 32 < 0.97 * a
+    render.set_importon_config(cuda_ctx)
+    assert cuda_ctx.device_error_bits() == 0
+    for x in (im, pt, none):
+        x.close()
+
+
+def test_importon_config_validation_and_progressive_radius(cuda_ctx, room):
+    sc, b, ds = room
+    for bad in ((0, 0.01), (1 << 21, 0.01), (2048, 0.0), (2048, float("nan"))):
+        with pytest.raises(cuda.GpugiError):
+            render.set_importon_config(cuda_ctx, *bad)
+    W = H = 24
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    render.set_importon_config(cuda_ctx, 512, 0.05, progressive=True)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, img, "IM", max_path_length=4, samples=6, iteration=3, rng_state=[1])
+    g = img.read()
+    assert np.all(g[..., 3] == 6) and np.isfinite(g).all() and g[..., :3].mean() > 0
+    assert cuda_ctx.device_error_bits() == 0
+    render.set_importon_config(cuda_ctx)
+    img.close()
+
+
 def test_photon_config_validation_and_progressive_radius(cuda_ctx, room):
     sc, b, ds = room
     for bad in ((0, 0.01), (1 << 21, 0.01), (2048, 0.0), (2048, float("nan"))):

@@ -10,7 +10,10 @@ closed-form radiometry on tiny scenes:
     diffuse room (the reference's renderer-comparison practice);
   * the Whitted ray tracer on that floor (a diffuse decision at the first
     hit, two NEE samples weighted 128 / 2) shows the same radiance, with its
-    pixel jitter in [x, x + 1) (whittedraytracer.comp:24, no -0.5).
+    pixel jitter in [x, x + 1) (whittedraytracer.comp:24, no -0.5);
+  * the importon map light tracer on that floor (no importons: the eye
+    paths end at their first, diffuse, hit) is the photons' reprojection
+    alone, and the G-buffer plane test passes every visible floor point.
 """
 import math
 
@@ -163,3 +166,39 @@ def test_photon_map_point_light_on_lambert_floor(built):
     rel = np.abs(img - expected) / expected
     assert np.median(rel) < 0.05, np.median(rel)
     assert abs(img.mean() / expected.mean() - 1) < 0.03
+
+
+def test_importon_map_point_light_on_lambert_floor(built):
+    """PixelMapLighttracer on the floor under a point light: the eye paths
+    store no importon (their first hit is diffuse), so the image is the
+    reprojection of the photons' first hits (photontracing.comp with
+    REPROJECT), whose G-buffer occlusion test must accept the floor it
+    stands on; the image mean converges to the NEE irradiance of the floor."""
+    albedo, I, h = 0.6, 5.0, 1.5
+    sc = _quad_scene(albedo=albedo)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"])
+    W = H = 16
+    cam = render.camera_lookat((0.0, 3.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, -1.0), 30.0, W, H)
+    ls = _point_light_samples((0.0, h, 0.0), (I, I, I), n=16)
+    acc, gbuf = None, np.zeros((H, W, 5), np.float32)
+    iters = 16
+    for it in range(iters):
+        acc = oracle.render(b, sc, "IM", W, H, cam.as_array(), render.wanghash(it), ls, max_path_length=1,
+                            accum=acc, gbuffer=gbuf, photons_per_light_sample=1 << 14, query_radius=0.05)
+    assert np.all(acc[..., 3] == iters)
+    assert np.allclose(gbuf[..., 1], 0.0, atol=1e-5)  # first hits on the floor y = 0
+    # packed geometry normal facing the camera, +y: (phi, z) = (pi / 2, 0)
+    assert np.allclose(gbuf[..., 3], 0.0, atol=1e-6) and np.allclose(gbuf[..., 4], math.pi / 2, atol=1e-6)
+    img = acc[..., 0] / iters
+    c = cam.as_array()
+    U, V, Wd, P = c[0:3], c[3:6], c[6:9], c[9:12]
+    ys, xs = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    d = ((xs + 0.5) / W * 2 - 1)[..., None] * U + ((ys + 0.5) / H * 2 - 1)[..., None] * V + Wd
+    p = P + (-P[1] / d[..., 1])[..., None] * d
+    r2 = p[..., 0] ** 2 + (h - p[..., 1]) ** 2 + p[..., 2] ** 2 + 1e-5
+    expected = albedo / math.pi * I * (h / np.sqrt(r2)) / r2
+    # border pixels collect half a pixel's splats (nearest-pixel rounding at the image edge, as in the
+    # reference's light tracer), so compare the interior
+    img, expected = img[1:-1, 1:-1], expected[1:-1, 1:-1]
+    assert np.median(np.abs(img - expected) / expected) < 0.06
+    assert abs(img.mean() / expected.mean() - 1) < 0.02, (img.mean(), expected.mean())
