@@ -333,6 +333,7 @@ def run_passes(args):
     around 16 spp after one warm-up iteration. Beside each, the CPU
     restatement of the same pass on all host threads over a bounded sample
     (64 x 64, 2 iterations)."""
+    import numpy as np
     import torch
     import oracle
     from gpugi_gb300 import bvh, cuda, render, scenes
@@ -346,7 +347,7 @@ def run_passes(args):
     cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
     stream = torch.cuda.ExternalStream(ctx.stream)
     out = {}
-    for pass_ in (args.passes.split(",") if args.passes else ("PT", "LT", "BPT", "WHITTED", "PM", "HIERARCHY")):
+    for pass_ in (args.passes.split(",") if args.passes else ("PT", "LT", "BPT", "WHITTED", "PM", "IM", "HIERARCHY")):
         hier = pass_ == "HIERARCHY"
         d = 4 if hier else depth
         img = render.Image(ctx, W, H)
@@ -372,6 +373,7 @@ def run_passes(args):
         st = [3]
         t0 = time.perf_counter()
         acc = None
+        gbuf = np.zeros((ch, cw, 5), np.float32) if pass_ == "IM" else None  # the importon pass's G-buffer
         if hier:
             ls0 = render.generate_light_samples(ds, st, nls)
             imp, _ = oracle.hier_importance(b, sc, cw, ch, ccam.as_array(), ls0, iterations=10)
@@ -383,7 +385,7 @@ def run_passes(args):
                                          max_path_length=d, accum=acc)
             else:
                 acc = oracle.render(b, sc, pass_, cw, ch, ccam.as_array(), render.wanghash(it), ls,
-                                    max_path_length=depth, rr_start_depth=rr, accum=acc)
+                                    max_path_length=depth, rr_start_depth=rr, accum=acc, gbuffer=gbuf)
         cpu = time.perf_counter() - t0
         out[pass_] = {"samples_per_s": W * H * spp / sec, "ms_per_iteration": sec / spp * 1e3,
                       "cpu_samples_per_s": cw * ch * 2 / cpu, "cpu_threads": os.cpu_count()}
@@ -765,7 +767,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--passes", default=None,
-                    help="passes workload: comma-separated subset of PT,LT,BPT,WHITTED,PM,HIERARCHY")
+                    help="passes workload: comma-separated subset of PT,LT,BPT,WHITTED,PM,IM,HIERARCHY")
     ap.add_argument("--shared-nodes", type=int, default=0,
                     help="top-of-tree nodes staged in shared memory by the walkers")
     ap.add_argument("--trace-mode", type=int, default=3,
