@@ -132,6 +132,16 @@ def test_batch_runs_other_passes_and_validates(cuda_ctx, scenes3):
                   light_samples=ls)
     assert np.allclose(wt.read(), ref.read(), rtol=1e-5, atol=1e-6 * np.abs(ref.read()).max())
     assert wt.read()[..., :3].mean() > 0
+    # so does the importon map light tracer, from its cleared G-buffer at iteration 0
+    lsi = np.ascontiguousarray(ls[:, :128])
+    im = render.Image(cuda_ctx, W, H)
+    render.render_batch(cuda_ctx, [dict(scene=ds, camera=cam, image=im, pass_="IM", samples=2, max_path_length=4,
+                                         num_light_samples=128, light_samples=lsi)])
+    refi = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, ds, cam, refi, "IM", max_path_length=4, samples=2, num_light_samples=128,
+                  light_samples=lsi)
+    assert np.allclose(im.read(), refi.read(), rtol=1e-4, atol=1e-5 * np.abs(refi.read()).max())
+    assert im.read()[..., :3].mean() > 0
     # an image larger than the path queue is refused
     render.set_batch_config(cuda_ctx, 1024, True)
     big = render.Image(cuda_ctx, 64, 64)
