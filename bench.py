@@ -325,7 +325,9 @@ def run_passes(args):
     0.5 ceiling light of radiance 10, albedos U[0.1, 0.9]), 512 x 512, 16 spp,
     depth 8, Russian roulette after depth 3. For PT, LT, BPT, the Whitted ray
     tracer, the photon mapper (2048 photons per light sample, radius
-    0.01, one photon map per iteration) and the hierarchy-importance renderer
+    0.01, one photon map per iteration), the importon map light tracer (2048
+    photons per light sample, radius 0.005, one importon map per iteration)
+    and the hierarchy-importance renderer
     (its own 4-vertex paths; the importance pass runs in the warm-up
     iteration and is timed there): samples/s
     (iterations x pixels per second) and Mrays/s (closest-hit + any-hit rays
