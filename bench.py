@@ -136,6 +136,13 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def bench_config(world: int) -> dict:
+    """The `config` object of both arms' lines (the same workload)."""
+    return {"workload": WORKLOAD,
+            "l2": "inputs larger than L2: 8 rotating ray batches (8 x 44 MB rays+results)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+
 def make_workload():
     from gpugi_gb300 import bvh, scenes
     sc = scenes.displaced_icosphere(65536, seed=1)
@@ -208,7 +215,7 @@ def run_reference(args, world, rank):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "parallelism": "host threads"}, "impl": "reference",
+            "config": bench_config(args.gpus), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": f"{args.steps} steps x 2^20 rays on {nthreads} threads (the reference's "
                                        "GLSL path cannot run on this box: no OpenGL; the oracle restatement "
@@ -295,13 +302,14 @@ def run_ours(args, world, rank, local):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD,
-                       "l2": "inputs larger than L2: 8 rotating ray batches (8 x 44 MB rays+results)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "config": bench_config(world),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * 28,
                     "d2h_bytes_per_step": N_RAYS * 16},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per step, read from "
+                                           "the committed profiles/trace_closest_icosphere65536.md (DRAM counters "
+                                           "need ncu and are not measured in this run)" if traffic else None,
                          "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)" if peak_src == "measured"
                          else "fallback 6.8 TB/s",
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3,

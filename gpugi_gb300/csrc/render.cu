@@ -1851,7 +1851,7 @@ struct RenderBuffers {
     uint32_t *qPixel = nullptr, *tvCount = nullptr, *nrcCounters = nullptr;  // counters: queries, paths, samples
     // photon mapper: hash table, photon records, append counter
     void* pmBlock = nullptr;
-    size_t pmMapSize = 0, pmCap = 0;
+    size_t pmMapSize = 0, pmMapCap = 0, pmCap = 0;
     uint32_t* pmMap = nullptr;
     float4* pmPhotons = nullptr;
     uint32_t* pmCount = nullptr;
@@ -2180,14 +2180,23 @@ static size_t next_prime(size_t n) {
 // importon map for 1.5x the pixels and one record per pixel
 // (pixelmaplighttracer.cpp:150-158).
 static gpugi_status ensure_pm_buffers(gpugi_ctx* ctx, RenderBuffers* rb, uint64_t mapMin, uint64_t records) {
+    // The block only grows: the photon mapper (1.5 x photons) and the
+    // importon map (1.5 x pixels) ask for different table sizes, and a switch
+    // between them must not free and allocate again (which synchronises).
+    // pmMapSize is the prime in use, pmMapCap the table entries allocated.
     const size_t mapSize = next_prime((size_t)mapMin);
     const size_t cap = (size_t)records;
-    if (mapSize == rb->pmMapSize && cap <= rb->pmCap) return GPUGI_OK;
+    if (mapSize <= rb->pmMapCap && cap <= rb->pmCap) {
+        rb->pmMapSize = mapSize;
+        return GPUGI_OK;
+    }
+    const size_t mapCap = mapSize > rb->pmMapCap ? mapSize : rb->pmMapCap;
+    const size_t recCap = cap > rb->pmCap ? cap : rb->pmCap;
     cudaStreamSynchronize(ctx->stream);
     if (rb->pmBlock) cudaFree(rb->pmBlock);
     rb->pmBlock = nullptr;
-    rb->pmMapSize = rb->pmCap = 0;
-    const size_t mapBytes = (8 * mapSize + 255) & ~size_t(255), photonBytes = 32 * cap;
+    rb->pmMapSize = rb->pmMapCap = rb->pmCap = 0;
+    const size_t mapBytes = (8 * mapCap + 255) & ~size_t(255), photonBytes = 32 * recCap;
     if (cudaMalloc(&rb->pmBlock, mapBytes + photonBytes + 256) != cudaSuccess) {
         rb->pmBlock = nullptr;
         return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "photon map buffers");
@@ -2197,7 +2206,8 @@ static gpugi_status ensure_pm_buffers(gpugi_ctx* ctx, RenderBuffers* rb, uint64_
     rb->pmPhotons = reinterpret_cast<float4*>(base + mapBytes);
     rb->pmCount = reinterpret_cast<uint32_t*>(base + mapBytes + photonBytes);
     rb->pmMapSize = mapSize;
-    rb->pmCap = cap;
+    rb->pmMapCap = mapCap;
+    rb->pmCap = recCap;
     return GPUGI_OK;
 }
 

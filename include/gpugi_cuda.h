@@ -163,7 +163,11 @@ gpugi_status gpugi_trace_any_device(gpugi_ctx* ctx, const gpugi_scene* scene,
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * All calls share the one array: calls that overlap on the GPU (other
  * streams, other contexts on the same device) race and must be serialised
- * by the caller. Asynchronous on the context stream. */
+ * by the caller. Asynchronous on the context stream. It always runs the
+ * root prefilter and a queue walker (trace mode 2 when the context is set to
+ * mode 0, 1 or 2, the context's group walker for modes 3-5): modes 0 and 1
+ * need no queue and have no allocation-free form, and every mode returns the
+ * same results. */
 #define GPUGI_NOALLOC_MAX_RAYS (1u << 20)
 gpugi_status gpugi_trace_closest_noalloc(gpugi_ctx* ctx, const gpugi_scene* scene,
                                          const float* ox, const float* oy, const float* oz,
