@@ -391,10 +391,10 @@ def run_passes(args):
         for it in range(2):
             ls = ls0 if (hier and it == 0) else render.generate_light_samples(ds, st, nls)
             if hier:
-                acc = oracle.render_hier(b, sc, cw, ch, ccam.as_array(), render.wanghash(it), ls, imp, mats, b.sggx,
+                acc = oracle.render_hier(b, sc, cw, ch, ccam.as_array(), render.frame_seed(it), ls, imp, mats, b.sggx,
                                          max_path_length=d, accum=acc)
             else:
-                acc = oracle.render(b, sc, pass_, cw, ch, ccam.as_array(), render.wanghash(it), ls,
+                acc = oracle.render(b, sc, pass_, cw, ch, ccam.as_array(), render.frame_seed(it), ls,
                                     max_path_length=depth, rr_start_depth=rr, accum=acc, gbuffer=gbuf)
         cpu = time.perf_counter() - t0
         out[pass_] = {"samples_per_s": W * H * spp / sec, "ms_per_iteration": sec / spp * 1e3,

@@ -69,7 +69,8 @@ struct HierConst {
     const float4* lightSamples;  // [set][numLightSamples][2]
     float3 sky;
     int maxPathLength;
-    uint32_t iteration, samples;  // render: sample s of the call has frame seed wanghash(iteration + s)
+    uint32_t iteration, samples;  // render: sample s of the call has frame seed FrameSeed(iteration + s)
+    uint32_t rng;                 // render: 1 PCG streams, 0 the reference's (acquisition always the reference's)
     float4* image;
     double* image64;
     float2* imp;
@@ -438,14 +439,14 @@ __global__ void k_acq_generate(HierConst c, uint32_t iterations, AcqPaths A, uin
     for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total; q += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t it = 1u + (uint32_t)(q / numPixels), pix = (uint32_t)(q % numPixels);
         const int x = (int)(pix % (uint32_t)c.width), y = (int)(pix / (uint32_t)c.width);
-        uint32_t seed = wanghash(wanghash(it) + pix);
+        Rng seed = rng_init(0u, it, pix);  // acquisition: the reference's streams
         const float2 r = random2(seed);
         const float sx = X::sub(X::mul(X::div(X::add(r.x, (float)x), (float)c.width), 2.0f), 1.0f);
         const float sy = X::sub(X::mul(X::div(X::add(r.y, (float)y), (float)c.height), 2.0f), 1.0f);
         store3(A.ox, A.oy, A.oz, q, c.camPos);
         store3(A.dx, A.dy, A.dz, q, X::normalize(X::add3(X::add3(X::scale(sx, c.camU), X::scale(sy, c.camV)), c.camW)));
         A.imp[q] = 1.0f;
-        A.seed[q] = seed;
+        A.seed[q] = seed.s;
     }
 }
 
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(128) k_acq_shade(HierConst c, AcqPaths A, AcqP
         bool light = false, next = false;
         float3 o, d, ld;
         float imp = 0.0f, dist = 0.0f;
-        uint32_t seed = 0;
+        Rng seed{0, 0};
         if (k < n && S.slot[k] >= 0) {
             const int4 tri = __ldg(c.s.slots + S.slot[k]);
             const float3 N = hit_normal(c.s, tri, S.u[k], S.v[k], nullptr);
@@ -499,7 +500,7 @@ __global__ void __launch_bounds__(128) k_acq_shade(HierConst c, AcqPaths A, AcqP
             d = load3(A.dx, A.dy, A.dz, k);
             o = X::add3(load3(A.ox, A.oy, A.oz, k), X::scale(S.t[k], d));
             imp = X::mul(A.imp[k], 0.5f);
-            seed = A.seed[k];
+            seed.s = A.seed[k];
             const uint32_t li = random_uint(seed) % c.numLightSamples;
             const float4 pn0 = __ldg(c.lightSamples + 2 * li), in1 = __ldg(c.lightSamples + 2 * li + 1);
             ld = X::sub3(xyz(pn0), o);
@@ -524,7 +525,7 @@ __global__ void __launch_bounds__(128) k_acq_shade(HierConst c, AcqPaths A, AcqP
             store3(B.ox, B.oy, B.oz, qn, X::add3(o, X::scale(kRAY_HIT_EPSILON, d)));
             store3(B.dx, B.dy, B.dz, qn, d);
             B.imp[qn] = imp;
-            B.seed[qn] = seed;
+            B.seed[qn] = seed.s;
         }
     }
 }
@@ -611,7 +612,7 @@ __global__ void k_hier_prop_up(DevScene s, float2* imp, float* subtree, const ui
 GPUGI_D float3 mat_col(const float3 S[3], float3 v) {  // S * v, columns S[0..2]
     return X::add3(X::add3(X::scale(v.x, S[0]), X::scale(v.y, S[1])), X::scale(v.z, S[2]));
 }
-GPUGI_D float3 sample_sggx_normal(const uint16_t* __restrict__ n, float3 incident, uint32_t& seed) {
+GPUGI_D float3 sample_sggx_normal(const uint16_t* __restrict__ n, float3 incident, Rng& seed) {
     const float sgx = __ldg(n) / 65535.0f, sgy = __ldg(n + 1) / 65535.0f, sgz = __ldg(n + 2) / 65535.0f;
     const float rx = __ldg(n + 3) / 65535.0f * 2.0f - 1.0f, ry = __ldg(n + 4) / 65535.0f * 2.0f - 1.0f,
                 rz = __ldg(n + 5) / 65535.0f * 2.0f - 1.0f;
@@ -692,7 +693,7 @@ __global__ void k_hier_render(HierConst c) {
     for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total; q += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t s = (uint32_t)(q / numPixels), pix = (uint32_t)(q % numPixels);
         const int x = (int)(pix % (uint32_t)c.width), y = (int)(pix / (uint32_t)c.width);
-        uint32_t seed = wanghash(wanghash(c.iteration + s) + pix);
+        Rng seed = rng_init(c.rng, c.iteration + s, pix);
         const float2 r = random2(seed);
         const float sx = X::sub(X::mul(X::div(X::add(r.x, (float)x), (float)c.width), 2.0f), 1.0f);
         const float sy = X::sub(X::mul(X::div(X::add(r.y, (float)y), (float)c.height), 2.0f), 1.0f);
@@ -953,6 +954,7 @@ gpugi_status render_hierarchy(gpugi_ctx* ctx, gpugi_scene* sc, const gpugi_camer
             return st;
         c.iteration = p->iteration + s0;
         c.samples = ns;
+        c.rng = (p->flags & GPUGI_RENDER_REFERENCE_RNG) ? 0u : 1u;
         const uint64_t work = numPixels * ns;
         const unsigned grid = (unsigned)std::min<uint64_t>((work + 127) / 128, (uint64_t)ctx->numSMs * 16);
         k_hier_render<<<grid, 128, 0, ctx->stream>>>(c);

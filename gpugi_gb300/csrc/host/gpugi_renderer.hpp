@@ -236,6 +236,10 @@ public:
     unsigned int GetMaxPathLength() const { return m_maxPathLength; }
     void SetRussianRouletteStart(unsigned int depth) { m_rrStartDepth = depth; }
     unsigned int GetRussianRouletteStart() const { return m_rrStartDepth; }
+    // Random streams of the passes: per-pixel PCG (default) or, with true,
+    // gpugi's own wanghash + xorshift32 streams (GPUGI_RENDER_REFERENCE_RNG).
+    void SetReferenceRandomStreams(bool reference) { m_referenceRng = reference; }
+    bool GetReferenceRandomStreams() const { return m_referenceRng; }
 
     // Access for the renderers.
     gpugi_ctx* GetContext() const { return m_ctx; }
@@ -262,6 +266,7 @@ private:
     uint64_t m_lightSamplerState = 123;  // LightSampler's xorshift state
     unsigned int m_maxPathLength = 8;
     unsigned int m_rrStartDepth = 0;
+    bool m_referenceRng = false;
     std::unique_ptr<Renderer> m_activeRenderer;
 };
 

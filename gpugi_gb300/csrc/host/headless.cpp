@@ -9,7 +9,7 @@
 //                  PixelMapLighttracer|HierarchyImportance]
 //                  [--size W H]
 //                  [--camera px py pz lx ly lz fovy] [--iterations N]
-//                  [--path-length L] [--rr-start D] [--sky r g b]
+//                  [--path-length L] [--rr-start D] [--sky r g b] [--reference-rng]
 //                  [--point-light px py pz ir ig ib] [--reference FILE.pfm]
 //                  [--out FILE.pfm] [--device D]
 #include <cstdio>
@@ -28,6 +28,7 @@ struct Args {
     unsigned pathLength = 8, rrStart = 0;
     float cam[7] = {0.0f, 1.0f, 3.4f, 0.0f, 1.0f, 0.0f, 40.0f};
     float sky[3] = {0.0f, 0.0f, 0.0f};
+    bool referenceRng = false;
     std::vector<PointLight> pointLights;
 };
 
@@ -52,6 +53,7 @@ Args parse(int argc, char** argv) {
         else if (k == "--device") { need(i, 1); a.device = std::atoi(argv[++i]); }
         else if (k == "--path-length") { need(i, 1); a.pathLength = (unsigned)std::atoi(argv[++i]); }
         else if (k == "--rr-start") { need(i, 1); a.rrStart = (unsigned)std::atoi(argv[++i]); }
+        else if (k == "--reference-rng") { a.referenceRng = true; }
         else if (k == "--camera") { need(i, 7); for (float& c : a.cam) c = std::strtof(argv[++i], nullptr); }
         else if (k == "--sky") { need(i, 3); for (float& c : a.sky) c = std::strtof(argv[++i], nullptr); }
         else if (k == "--point-light") {
@@ -79,6 +81,7 @@ int main(int argc, char** argv) {
         system.SetScreenSize(ei::IVec2(a.width, a.height));
         system.SetMaxPathLength(a.pathLength);
         system.SetRussianRouletteStart(a.rrStart);
+        system.SetReferenceRandomStreams(a.referenceRng);
         auto scene = std::make_shared<Scene>(system.GetContext(), a.scene);
         for (const PointLight& p : a.pointLights) scene->AddPointLight(p);
         system.SetScene(scene);

@@ -269,7 +269,7 @@ gpugi_render_params RendererSystem::MakeRenderParams(gpugi_pass pass) const {
     p.sky[0] = sky.x;
     p.sky[1] = sky.y;
     p.sky[2] = sky.z;
-    p.flags = 0;
+    p.flags = m_referenceRng ? GPUGI_RENDER_REFERENCE_RNG : 0u;
     return p;
 }
 

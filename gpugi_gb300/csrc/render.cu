@@ -76,6 +76,7 @@ struct RenderConst {
     int maxPathLength, rrStartDepth;
     uint32_t iteration, samples, sampleBase;  // sample s of this chunk = iteration sampleBase + s
     uint32_t pass;               // gpugi_pass (the batched wavefront shades each path by its job's pass)
+    uint32_t rng;                // 1: PCG streams (default), 0: the reference's wanghash + xorshift32
     uint32_t numLightSamples;
     const float4* lightSamples;  // [samples][numLightSamples][2]
     float3 sky;
@@ -125,12 +126,12 @@ GPUGI_D void splat(const RenderConst& rc, uint32_t pixel, float3 c, float w = 0.
     }
 }
 
-GPUGI_D void store_path(const PathSoA& P, uint32_t i, float3 o, float3 d, float3 tp, uint32_t seed, uint32_t pixel,
+GPUGI_D void store_path(const PathSoA& P, uint32_t i, float3 o, float3 d, float3 tp, Rng seed, uint32_t pixel,
                         uint32_t info, float lastP) {
     P.ox[i] = o.x; P.oy[i] = o.y; P.oz[i] = o.z;
     P.dx[i] = d.x; P.dy[i] = d.y; P.dz[i] = d.z;
     P.tx[i] = tp.x; P.ty[i] = tp.y; P.tz[i] = tp.z;
-    P.seed[i] = seed; P.pixel[i] = pixel; P.info[i] = info; P.lastP[i] = lastP;
+    P.seed[i] = seed.s; P.pixel[i] = pixel; P.info[i] = info; P.lastP[i] = lastP;
 }
 GPUGI_D void store_shadow(const ShadowSoA& Q, uint32_t i, float3 o, float3 d, float tmax, float3 c, uint32_t pixel,
                           uint32_t train = kNoTrain) {
@@ -264,7 +265,7 @@ struct Walkers {
 // ------------------------------------------------------------ generation
 // Primary ray (pathtracer.comp:132-139) in exact IEEE operations, so camera
 // rays, and with them the first hits, are bit-identical to the oracle's.
-GPUGI_D float3 primary_direction(const RenderConst& rc, uint32_t& seed, int x, int y) {
+GPUGI_D float3 primary_direction(const RenderConst& rc, Rng& seed, int x, int y) {
     float2 r = random2(seed);
     const float sx = X::sub(X::mul(X::div(X::add(X::sub(r.x, 0.5f), (float)x), (float)rc.width), 2.0f), 1.0f);
     const float sy = X::sub(X::mul(X::div(X::add(X::sub(r.y, 0.5f), (float)y), (float)rc.height), 2.0f), 1.0f);
@@ -279,7 +280,7 @@ GPUGI_D float3 primary_direction(const RenderConst& rc, uint32_t& seed, int x, i
 GPUGI_D void camera_path_start(const RenderConst& rc, const PathSoA& A, uint32_t p, uint32_t s, uint32_t pix,
                                bool bidir) {
     const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-    uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + pix);
+    Rng seed = rng_init(rc.rng, rc.iteration + rc.sampleBase + s, pix);
     const float3 d = primary_direction(rc, seed, x, y);
     store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, s << 8, 1.0f);
     if (bidir) splat(rc, pix, f3(0.0f), 1.0f);
@@ -307,7 +308,7 @@ GPUGI_D void write_cache(const RenderConst& rc, uint32_t s, uint32_t k, float3 f
 // first stores its own light sample (lighttracer.comp:56-61).
 GPUGI_D void light_path_start(const RenderConst& rc, const PathSoA& A, uint32_t p, uint32_t s, uint32_t gid,
                               bool withCache) {
-    uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + gid);
+    Rng seed = rng_init(rc.rng, rc.iteration + rc.sampleBase + s, gid);
     const uint32_t li = gid / (uint32_t)rc.numRaysPerLightSample;
     const float4* ls = rc.lightSamples + 2 * ((size_t)s * rc.numLightSamples + li);
     const float4 pn0 = __ldg(ls), in1 = __ldg(ls + 1);
@@ -397,7 +398,7 @@ GPUGI_D bool direct_light(const RenderConst& rc, uint32_t s, float3 pos, float3 
 }
 
 // Russian roulette (pathtracer.comp:99-104); rrStartDepth > 0 delays it.
-GPUGI_D bool roulette(const RenderConst& rc, int depth, float3 throughput, float3& tp, uint32_t& seed) {
+GPUGI_D bool roulette(const RenderConst& rc, int depth, float3 throughput, float3& tp, Rng& seed) {
     if (depth < rc.rrStartDepth) return true;
     const float p = saturate(luminance(throughput));
     if (random01(seed) >= p) return false;
@@ -418,7 +419,8 @@ struct PtLane {
     bool survive = false, shadow = false;
     float3 o, d, tp, sro, srd, contrib;
     float srl = 0.0f;
-    uint32_t seed = 0, pixel = 0, info = 0;
+    Rng seed{0, 0};
+    uint32_t pixel = 0, info = 0;
 };
 
 GPUGI_D void pt_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
@@ -427,7 +429,7 @@ GPUGI_D void pt_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSoA
     L.o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
     L.d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
     L.tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-    L.seed = A.seed[k];
+    L.seed = Rng{A.seed[k], rc.rng};
     L.pixel = A.pixel[k];
     L.info = A.info[k];
     Hit h = load_hit(rc, H, k, L.o, L.d);
@@ -511,7 +513,8 @@ struct LightLane {
     bool survive = false, shadow = false;
     float3 o, d, tp, sro, srd, color;
     float srl = 0.0f;
-    uint32_t seed = 0, pixel = 0, info = 0, gid = 0;
+    Rng seed{0, 0};
+    uint32_t pixel = 0, info = 0, gid = 0;
 };
 
 GPUGI_D void light_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
@@ -519,7 +522,7 @@ GPUGI_D void light_shade_lane(const RenderConst& rc, const PathSoA& A, const Hit
     L.o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
     L.d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
     L.tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-    L.seed = A.seed[k];
+    L.seed = Rng{A.seed[k], rc.rng};
     L.gid = A.pixel[k];
     L.info = A.info[k];
     const int32_t slot = H.slot[k];
@@ -625,7 +628,8 @@ struct BptLane {
     bool survive = false, shadow = false, query = false;
     float3 o, d, tp, sro, srd, contrib, qN, qAlbedo, qT;
     float srl = 0.0f, lastP = 1.0f, misProd = 1.0f;
-    uint32_t seed = 0, pixel = 0, info = 0;
+    Rng seed{0, 0};
+    uint32_t pixel = 0, info = 0;
 };
 
 GPUGI_D void bpt_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
@@ -633,7 +637,7 @@ GPUGI_D void bpt_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSo
     L.o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
     L.d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
     L.tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-    L.seed = A.seed[k];
+    L.seed = Rng{A.seed[k], rc.rng};
     L.pixel = A.pixel[k];
     L.info = A.info[k];
     L.lastP = A.lastP[k];
@@ -641,7 +645,7 @@ GPUGI_D void bpt_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSo
     float3& o = L.o;
     float3& d = L.d;
     float3& tp = L.tp;
-    uint32_t& seed = L.seed;
+    Rng& seed = L.seed;
     const float lastP = L.lastP;
     Hit h = load_hit(rc, H, k, o, d);
     if (!h.valid) {
@@ -765,7 +769,7 @@ __global__ void k_whitted_generate(RenderConst rc, PathSoA A) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
         const uint32_t s = p / (uint32_t)rc.numPixels, pix = p % (uint32_t)rc.numPixels;
         const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s));
+        Rng seed = rng_init_coherent(rc.rng, rc.iteration + rc.sampleBase + s);
         const float2 r = random2(seed);
         const float sx = X::sub(X::mul(X::div(X::add(r.x, (float)x), (float)rc.width), 2.0f), 1.0f);
         const float sy = X::sub(X::mul(X::div(X::add(r.y, (float)y), (float)rc.height), 2.0f), 1.0f);
@@ -788,12 +792,13 @@ __global__ void __launch_bounds__(128) k_whitted_shade(RenderConst rc, PathSoA A
         bool survive = false, shadow[2] = {false, false};
         float3 o, d, tp, sro[2], srd[2], contrib[2];
         float srl[2] = {0.0f, 0.0f};
-        uint32_t seed = 0, pixel = 0, info = 0;
+        Rng seed{0, 0};
+    uint32_t pixel = 0, info = 0;
         if (valid) {
             o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
             d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
             tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
+            seed = Rng{A.seed[k], rc.rng};
             pixel = A.pixel[k];
             info = A.info[k];
             Hit h = load_hit(rc, H, k, o, d);
@@ -847,7 +852,7 @@ __global__ void __launch_bounds__(128) k_whitted_shade(RenderConst rc, PathSoA A
 
 GPUGI_D uint32_t pm_cell_hash(int x, int y, int z) {  // gridCellHash
     uint32_t h = ((uint32_t)x & 0x7FFu) | (((uint32_t)y & 0x3FFu) << 11) | (((uint32_t)z & 0x7FFu) << 21);
-    return random_uint(h);
+    return xorshift32(h);
 }
 GPUGI_D uint32_t pm_snorm16(float v) {  // packSnorm2x16 component, ties to even
     return (uint32_t)(uint16_t)(int16_t)rintf(fminf(fmaxf(v, -1.0f), 1.0f) * 32767.0f);
@@ -907,7 +912,7 @@ __global__ void k_photon_generate(RenderConst rc, PathSoA A) {
     const uint32_t total = rc.numLightSamples * (uint32_t)rc.photonsPerSample;
     if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase) + g);
+        Rng seed = rng_init(rc.rng, rc.iteration + rc.sampleBase, g);
         const uint32_t li = g / (uint32_t)rc.photonsPerSample;
         const float4* ls = rc.lightSamples + 2 * (size_t)li;
         const float4 pn0 = __ldg(ls), in1 = __ldg(ls + 1);
@@ -934,12 +939,13 @@ __global__ void __launch_bounds__(128) k_photon_shade(RenderConst rc, PathSoA A,
     WARP_LOOP(n, k, valid) {
         bool survive = false;
         float3 o, d, tp;
-        uint32_t seed = 0, gid = 0;
+        Rng seed{0, 0};
+    uint32_t gid = 0;
         if (valid) {
             o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
             d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
             tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
+            seed = Rng{A.seed[k], rc.rng};
             gid = A.pixel[k];
             const int32_t slot = H.slot[k];
             if (slot >= 0) {
@@ -979,7 +985,7 @@ __global__ void k_pm_generate(RenderConst rc, PathSoA A) {
     if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < total; pix += gridDim.x * blockDim.x) {
         const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase) + pix);
+        Rng seed = rng_init(rc.rng, rc.iteration + rc.sampleBase, pix);
         const float2 r = random2(seed);
         const float sx = X::sub(X::mul(X::div(X::add(r.x, (float)x), (float)rc.width), 2.0f), 1.0f);
         const float sy = X::sub(X::mul(X::div(X::add(r.y, (float)y), (float)rc.height), 2.0f), 1.0f);
@@ -999,12 +1005,13 @@ __global__ void __launch_bounds__(128) k_pm_shade(RenderConst rc, PathSoA A, Pat
     WARP_LOOP(n, k, valid) {
         bool survive = false;
         float3 o, d, tp;
-        uint32_t seed = 0, pixel = 0;
+        Rng seed{0, 0};
+    uint32_t pixel = 0;
         if (valid) {
             o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
             d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
             tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
+            seed = Rng{A.seed[k], rc.rng};
             pixel = A.pixel[k];
             Hit h = load_hit(rc, H, k, o, d);
             if (!h.valid) {
@@ -1126,7 +1133,7 @@ __global__ void k_im_generate(RenderConst rc, PathSoA A) {
     if (blockIdx.x == 0 && threadIdx.x == 0) rc.cnt->path[0] = total;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < total; pix += gridDim.x * blockDim.x) {
         const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-        uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase) + pix);
+        Rng seed = rng_init(rc.rng, rc.iteration + rc.sampleBase, pix);
         const float3 d = primary_direction(rc, seed, x, y);
         store_path(A, pix, rc.camPos, d, f3(1.0f), seed, pix, 0u, 1.0f);
         rc.imGbufN0[pix] = 0.0f;
@@ -1144,12 +1151,13 @@ __global__ void __launch_bounds__(128) k_im_shade(RenderConst rc, PathSoA A, Pat
     WARP_LOOP(n, k, valid) {
         bool survive = false;
         float3 o, d, tp;
-        uint32_t seed = 0, pixel = 0;
+        Rng seed{0, 0};
+    uint32_t pixel = 0;
         if (valid) {
             o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
             d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
             tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
+            seed = Rng{A.seed[k], rc.rng};
             pixel = A.pixel[k];
             Hit h = load_hit(rc, H, k, o, d);
             if (!h.valid) {
@@ -1261,12 +1269,13 @@ __global__ void __launch_bounds__(128) k_im_photon_shade(RenderConst rc, PathSoA
     WARP_LOOP(n, k, valid) {
         bool survive = false;
         float3 o, d, tp;
-        uint32_t seed = 0, gid = 0, info = 0;
+        Rng seed{0, 0};
+    uint32_t gid = 0, info = 0;
         if (valid) {
             o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
             d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
             tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-            seed = A.seed[k];
+            seed = Rng{A.seed[k], rc.rng};
             gid = A.pixel[k];
             info = A.info[k];
             const int32_t slot = H.slot[k];
@@ -1333,7 +1342,7 @@ __global__ void k_nrc_generate(RenderConst rc, PathSoA A) {
         const uint32_t s = p / (uint32_t)rc.numPixels, pix = p % (uint32_t)rc.numPixels;
         const uint32_t frame = rc.iteration + rc.sampleBase + s;
         const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-        uint32_t seed = wanghash(wanghash(frame) + pix);
+        Rng seed = rng_init(rc.rng, frame, pix);
         const float3 d = primary_direction(rc, seed, x, y);
         uint32_t info = s << 8;
         float slotBits = 0.0f;
@@ -1367,7 +1376,8 @@ struct NrcLane {
     bool survive = false, shadow = false, query = false;
     float3 o, d, tp, sro, srd, contrib, qN, qAlbedo, qT;
     float srl = 0.0f, lastP = 0.0f;
-    uint32_t seed = 0, pixel = 0, info = 0, train = kNoTrain;
+    Rng seed{0, 0};
+    uint32_t pixel = 0, info = 0, train = kNoTrain;
 };
 
 GPUGI_D void nrc_pt_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
@@ -1380,7 +1390,7 @@ GPUGI_D void nrc_pt_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& 
     o = make_float3(A.ox[k], A.oy[k], A.oz[k]);
     d = make_float3(A.dx[k], A.dy[k], A.dz[k]);
     tp = make_float3(A.tx[k], A.ty[k], A.tz[k]);
-    L.seed = A.seed[k];
+    L.seed = Rng{A.seed[k], rc.rng};
     L.pixel = A.pixel[k];
     L.info = A.info[k];
     L.lastP = A.lastP[k];
@@ -1480,7 +1490,7 @@ __global__ void k_nrc_bpt_generate(RenderConst rc, PathSoA A, uint32_t nTrain) {
         if (p < render) {
             const uint32_t s = p / (uint32_t)rc.numPixels, pix = p % (uint32_t)rc.numPixels;
             const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-            uint32_t seed = wanghash(wanghash(rc.iteration + rc.sampleBase + s) + pix);
+            Rng seed = rng_init(rc.rng, rc.iteration + rc.sampleBase + s, pix);
             const float3 d = primary_direction(rc, seed, x, y);
             store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, s << 8, 1.0f);
             A.job[p] = __float_as_uint(1.0f);
@@ -1490,7 +1500,7 @@ __global__ void k_nrc_bpt_generate(RenderConst rc, PathSoA A, uint32_t nTrain) {
             const uint32_t frame = rc.iteration + rc.sampleBase + s;
             const uint32_t pix = wanghash(slot ^ wanghash(frame + 0x9E3779B9u)) % (uint32_t)rc.numPixels;
             const int x = (int)(pix % (uint32_t)rc.width), y = (int)(pix / (uint32_t)rc.width);
-            uint32_t seed = wanghash(wanghash(frame ^ 0x5bd1e995u) + slot);
+            Rng seed = rng_init(rc.rng, frame ^ 0x5bd1e995u, slot);
             const float3 d = primary_direction(rc, seed, x, y);
             rc.tvCount[slot] = 0;
             store_path(A, p, rc.camPos, d, f3(1.0f), seed, kNoPixel, (s << 8) | 2u, __uint_as_float(slot));
@@ -1511,7 +1521,8 @@ __global__ void __launch_bounds__(128) k_nrc_bpt_shade(RenderConst rc, PathSoA A
         bool survive = false, shadow = false, query = false;
         float3 o, d, tp, sro, srd, contrib, qN, qA, qT;
         float srl = 0.0f, lastP = 0.0f, misProd = 1.0f;
-        uint32_t seed = 0, pixel = 0, info = 0, train = kNoTrain;
+        Rng seed{0, 0};
+    uint32_t pixel = 0, info = 0, train = kNoTrain;
         if (valid) {
             if (A.info[k] & 2u) {
                 NrcLane L;
@@ -1772,7 +1783,8 @@ __global__ void __launch_bounds__(128) k_batch_shade(const RenderConst* __restri
         bool shadow = false, survive = false;
         float3 o, d, tp, sro, srd, c;
         float srl = 0.0f;
-        uint32_t seed = 0, pathPixel = 0, shadowPixel = 0, info = 0, j = 0;
+        Rng seed{0, 0};
+    uint32_t pathPixel = 0, shadowPixel = 0, info = 0, j = 0;
         if (valid) {
             j = A.job[k];
             const RenderConst& rc = jobs[j];
@@ -2091,6 +2103,7 @@ static RenderConst make_render_const(gpugi_ctx* ctx, const gpugi_scene* sc, cons
     rc.rrStartDepth = (int)p->rrStartDepth;
     rc.iteration = p->iteration;
     rc.pass = p->pass;
+    rc.rng = (p->flags & GPUGI_RENDER_REFERENCE_RNG) ? 0u : 1u;
     rc.numLightSamples = p->numLightSamples;
     rc.sky = f3(p->sky[0], p->sky[1], p->sky[2]);
     rc.image = im->rgba;
@@ -2350,6 +2363,7 @@ gpugi_status gpugi_render(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi_cam
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
     if (p->pass > GPUGI_PASS_IM) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->flags & ~GPUGI_RENDER_KNOWN_FLAGS) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown render flags");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)
@@ -2442,6 +2456,7 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     if (!sc || !cam || !p || !im || !nn || !np) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
     if (p->pass != GPUGI_PASS_PT && p->pass != GPUGI_PASS_BPT)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "the radiance cache serves the PT and BPT passes");
+    if (p->flags & ~GPUGI_RENDER_KNOWN_FLAGS) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown render flags");
     const bool bpt = p->pass == GPUGI_PASS_BPT;
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
@@ -2577,6 +2592,7 @@ static gpugi_status check_render_args(gpugi_ctx* ctx, const gpugi_scene* sc, con
                                       const uint64_t* rngState, const gpugi_image* im) {
     if (!sc || !cam || !p || !im) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
     if (p->pass > GPUGI_PASS_IM) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown pass");
+    if (p->flags & ~GPUGI_RENDER_KNOWN_FLAGS) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown render flags");
     if (p->width != im->width || p->height != im->height)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "params size differs from the image");
     if (p->maxPathLength == 0 || p->maxPathLength > (uint32_t)kMaxDepth)

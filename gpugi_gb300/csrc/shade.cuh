@@ -1,7 +1,7 @@
 // Device shading library: gpugi's RNG, samplers, BSDF and light-transport
 // helpers as CUDA device functions.
 //
-//   RNG / samplers        gpugi/shader/random.glsl:1-87
+//   RNG / samplers        gpugi/shader/random.glsl:1-87 (+ PCG, see Rng)
 //   ONB / normal packing  gpugi/shader/helper.glsl:22-76
 //   hit attributes        gpugi/shader/scenedata.glsl:94-105
 //   BSDF                  gpugi/shader/materials.glsl:33-436 (USE_CONSTANT_REFLECTION)
@@ -29,18 +29,64 @@ GPUGI_HD uint32_t wanghash(uint32_t x) {
     x = x ^ (x >> 15);
     return x;
 }
-GPUGI_D uint32_t random_uint(uint32_t& s) {  // xorshift32
+
+// Random streams of the passes. Two generators share the 32-bit state of a
+// path (the wavefront stores one uint32 per path):
+//  * reference (parity mode): gpugi/shader/random.glsl:1-43. Path seed
+//    InitRandomSeed(FrameSeed, index) = wanghash(FrameSeed + index) with
+//    FrameSeed = WangHash(iteration), draws by xorshift32, and
+//    Random = float(u) / 4294967297.0;
+//  * PCG (the default): PCG-RXS-M-XS-32, the 32-bit-state member of
+//    O'Neill's PCG family (M. E. O'Neill, "PCG: A Family of Simple Fast
+//    Space-Efficient Statistically Good Algorithms for Random Number
+//    Generation", HMC-CS-2014-0905, section 6.3.4): an LCG step
+//    s = s * 747796405 + 2891336453 followed by the RXS-M-XS output
+//    permutation. One step from a given state doubles as the hash that seeds
+//    a path per pixel (Jarzynski and Olano, "Hash Functions for GPU
+//    Rendering", JCGT 9(3), 2020): seed = pcg(pcg(iteration) + index).
+//    Random = float(u >> 8) * 2^-24, in [0, 1).
+// `pcg` is uniform across a launch (a field of the call's constants), so the
+// selection costs no divergence.
+struct Rng {
+    uint32_t s;
+    uint32_t pcg;
+};
+GPUGI_HD uint32_t pcg_output(uint32_t state) {
+    const uint32_t w = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (w >> 22u) ^ w;
+}
+GPUGI_HD uint32_t pcg_hash(uint32_t x) { return pcg_output(x * 747796405u + 2891336453u); }
+GPUGI_HD uint32_t rng_hash(uint32_t pcg, uint32_t x) { return pcg ? pcg_hash(x) : wanghash(x); }
+// InitRandomSeed(FrameSeed(frame), index) of the selected generator.
+GPUGI_HD Rng rng_init(uint32_t pcg, uint32_t frame, uint32_t index) {
+    return Rng{rng_hash(pcg, rng_hash(pcg, frame) + index), pcg};
+}
+// InitCoherentRandomSeed(FrameSeed(frame)): one stream for every pixel.
+GPUGI_HD Rng rng_init_coherent(uint32_t pcg, uint32_t frame) { return Rng{rng_hash(pcg, rng_hash(pcg, frame)), pcg}; }
+// RandomUInt (random.glsl:11-19), also the reference's grid-cell hash.
+GPUGI_HD uint32_t xorshift32(uint32_t& s) {
     s ^= s << 13;
     s ^= s >> 17;
     s ^= s << 5;
     return s;
 }
-// float(u) / 4294967297.0 in GLSL float arithmetic: the literal rounds to 2^32,
-// and a division by a power of two is exact, so this is float(u) * 2^-32.
-GPUGI_D float random01(uint32_t& s) { return __uint2float_rn(random_uint(s)) * 2.3283064365386963e-10f; }
-GPUGI_D float2 random2(uint32_t& s) {
-    float a = random01(s);
-    float b = random01(s);
+GPUGI_D uint32_t random_uint(Rng& r) {
+    if (r.pcg) {
+        r.s = r.s * 747796405u + 2891336453u;
+        return pcg_output(r.s);
+    }
+    return xorshift32(r.s);
+}
+// Reference: float(u) / 4294967297.0 in GLSL float arithmetic; the literal
+// rounds to 2^32, and a division by a power of two is exact, so this is
+// float(u) * 2^-32 (1.0 for u >= 2^32 - 128, as in the shader).
+GPUGI_D float random01(Rng& r) {
+    const uint32_t u = random_uint(r);
+    return r.pcg ? __uint2float_rn(u >> 8) * 5.9604644775390625e-8f : __uint2float_rn(u) * 2.3283064365386963e-10f;
+}
+GPUGI_D float2 random2(Rng& r) {
+    float a = random01(r);
+    float b = random01(r);
     return make_float2(a, b);
 }
 
@@ -114,7 +160,7 @@ GPUGI_D void decision_probabilities(const MaterialData& m, float3& preflect, flo
 // disabled (plausible = true), so exactly one lobe sample is drawn. With
 // stopOnDiffuse (the Whitted shader's STOP_ON_DIFFUSE_BOUNCE) a diffuse
 // decision sets throughput = (-1, 0, 0) and returns no direction.
-GPUGI_D float3 sample_bsdf(float3 incident, const MaterialData& m, uint32_t& seed, float3 N, float3& throughput,
+GPUGI_D float3 sample_bsdf(float3 incident, const MaterialData& m, Rng& seed, float3 N, float3& throughput,
                            bool adjoint, float& pdf, bool stopOnDiffuse = false, bool* reflectedDiffuse = nullptr) {
     float cosTheta = dot(N, incident);
     float cosThetaAbs = saturate(fabsf(cosTheta));

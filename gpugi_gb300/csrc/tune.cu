@@ -26,7 +26,7 @@ namespace {
 __global__ void k_tune_rays(float3 center, float3 half, uint64_t n, uint32_t seed, float* ox, float* oy, float* oz,
                             float* dx, float* dy, float* dz, float* tmax) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t s = wanghash(wanghash(seed) + (uint32_t)i);
+        Rng s = rng_init(0u, seed, (uint32_t)i);
         const float u0 = random01(s), u1 = random01(s), u2 = random01(s), u3 = random01(s), u4 = random01(s);
         ox[i] = center.x + (2.0f * u0 - 1.0f) * 2.0f * half.x;
         oy[i] = center.y + (2.0f * u1 - 1.0f) * 2.0f * half.y;

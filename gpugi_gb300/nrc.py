@@ -140,15 +140,16 @@ def render_nrc(ctx: cuda.Context, scene: cuda.DeviceScene, camera, image, cache:
                sky=(0.0, 0.0, 0.0), rr_start_depth: int = 0, light_samples: np.ndarray | None = None,
                rng_state: list | None = None, terminate_depth: int = 1, train_fraction: float = 0.03,
                max_train_samples: int = 65536, train_steps: int = 1, train: bool = True,
-               samples_per_frame: int = 1, pass_: str = "PT") -> None:
+               samples_per_frame: int = 1, pass_: str = "PT", rng: str = "pcg") -> None:
     """`samples` iterations of path tracing (pass_ "PT") or bidirectional
-    path tracing ("BPT") with the radiance cache (gpugi_render_nrc)."""
+    path tracing ("BPT") with the radiance cache (gpugi_render_nrc); rng
+    selects the random streams as in render.render."""
     from . import render
     L = _declare()
     if pass_ not in ("PT", "BPT"):
         raise ValueError("the radiance cache serves the PT and BPT passes")
     p = render.RenderParams(render.PASSES[pass_], image.width, image.height, max_path_length, rr_start_depth,
-                            iteration, samples, num_light_samples, render._f3(sky), 0)
+                            iteration, samples, num_light_samples, render._f3(sky), render.RNG_FLAGS[rng])
     ls = None if light_samples is None else np.ascontiguousarray(light_samples, dtype=np.float32)
     if ls is not None:
         assert ls.shape == (samples, num_light_samples, 8)

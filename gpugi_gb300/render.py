@@ -15,6 +15,9 @@ PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3, "PM": 4, "HIERARCHY": 5, "IM
 # Initial light samples per iteration as each renderer configures them
 # (pathtracer.cpp:28, lightpathtracer.cpp:16, bidirectionalpathtracer.cpp:160).
 DEFAULT_LIGHT_SAMPLES = {"PT": 128, "LT": 256, "BPT": 128, "WHITTED": 128, "PM": 128, "HIERARCHY": 128, "IM": 128}
+# Random streams (gpugi_render_params.flags): "pcg" (the default) or
+# "reference" (GPUGI_RENDER_REFERENCE_RNG: gpugi's wanghash + xorshift32).
+RNG_FLAGS = {"pcg": 0, "reference": 1}
 
 
 class Camera(C.Structure):
@@ -136,15 +139,16 @@ def generate_light_samples(scene: cuda.DeviceScene, rng_state: list, n: int) -> 
 def render(ctx: cuda.Context, scene: cuda.DeviceScene, camera: Camera, image: Image, pass_: str = "PT",
            max_path_length: int = 8, samples: int = 1, iteration: int = 0, num_light_samples: int | None = None,
            sky=(0.0, 0.0, 0.0), rr_start_depth: int = 0, light_samples: np.ndarray | None = None,
-           rng_state: list | None = None) -> None:
+           rng_state: list | None = None, rng: str = "pcg") -> None:
     """Render `samples` iterations of a pass into the image (asynchronous).
 
     light_samples: (samples, numLightSamples, 8) float32, or None to let the
-    library's host sampler draw them from rng_state (a one-element list)."""
+    library's host sampler draw them from rng_state (a one-element list).
+    rng: the paths' random streams, "pcg" or "reference"."""
     L = _declare()
     nls = num_light_samples or DEFAULT_LIGHT_SAMPLES[pass_]
     p = RenderParams(PASSES[pass_], image.width, image.height, max_path_length, rr_start_depth, iteration, samples,
-                     nls, _f3(sky), 0)
+                     nls, _f3(sky), RNG_FLAGS[rng])
     ls = None if light_samples is None else np.ascontiguousarray(light_samples, dtype=np.float32)
     if ls is not None:
         assert ls.shape == (samples, nls, 8)
@@ -163,7 +167,7 @@ class Job(C.Structure):
 def render_batch(ctx: cuda.Context, jobs: list[dict]) -> None:
     """gpugi_render_batch over jobs given as dicts with the keys of render():
     scene, camera, image, pass_ (default PT), max_path_length, samples,
-    iteration, num_light_samples, sky, rr_start_depth, light_samples or
+    iteration, num_light_samples, sky, rr_start_depth, rng, light_samples or
     rng_state (a one-element list, updated)."""
     L = _declare()
     arr = (Job * len(jobs))()
@@ -175,7 +179,7 @@ def render_batch(ctx: cuda.Context, jobs: list[dict]) -> None:
         samples = j.get("samples", 1)
         p = RenderParams(PASSES[pass_], img.width, img.height, j.get("max_path_length", 8),
                          j.get("rr_start_depth", 0), j.get("iteration", 0), samples, nls,
-                         _f3(j.get("sky", (0.0, 0.0, 0.0))), 0)
+                         _f3(j.get("sky", (0.0, 0.0, 0.0))), RNG_FLAGS[j.get("rng", "pcg")])
         ls = j.get("light_samples")
         st = None
         if ls is not None:
@@ -227,6 +231,20 @@ def wanghash(x: int) -> int:
     return x
 
 
+def pcg_hash(x: int) -> int:
+    """One PCG-RXS-M-XS-32 step used as a hash (the PCG streams' seeding)."""
+    state = ((x & 0xFFFFFFFF) * 747796405 + 2891336453) & 0xFFFFFFFF
+    w = (((state >> ((state >> 28) + 4)) ^ state) * 277803737) & 0xFFFFFFFF
+    return ((w >> 22) ^ w) & 0xFFFFFFFF
+
+
+def frame_seed(iteration: int, rng: str = "pcg") -> int:
+    """FrameSeed of an iteration for the given random streams: WangHash
+    (RendererSystem::PerIterationBufferUpdate, gpugi/renderer/renderersystem.cpp:101)
+    or the PCG hash."""
+    return pcg_hash(iteration) if rng == "pcg" else wanghash(iteration)
+
+
 def smoke_check(ctx: cuda.Context) -> None:
     """One tiny PT iteration on the GPU, compared with the oracle (used by smoke())."""
     import oracle
@@ -242,7 +260,7 @@ def smoke_check(ctx: cuda.Context) -> None:
     img = Image(ctx, w, h)
     render(ctx, ds, cam, img, "PT", max_path_length=1, samples=1, iteration=0, light_samples=ls)
     g = img.read()[..., :3]
-    o = oracle.render(b, sc, "PT", w, h, cam.as_array(), wanghash(0), ls[0], max_path_length=1)[..., :3]
+    o = oracle.render(b, sc, "PT", w, h, cam.as_array(), frame_seed(0), ls[0], max_path_length=1)[..., :3]
     err = np.abs(g - o).max() / max(1e-6, float(np.abs(o).max()))
     assert err < 1e-3, f"direct-light image differs from the oracle (max rel err {err})"
     img.close()

@@ -276,8 +276,17 @@ typedef struct gpugi_render_params {
     uint32_t samples;          /* iterations (samples per pixel) rendered by this call */
     uint32_t numLightSamples;  /* initial light samples per iteration (PT/BPT/Whitted/PM 128, LT 256) */
     float sky[3];              /* constant radiance on a miss (addition; 0 = the reference's black) */
-    uint32_t flags;            /* reserved, 0 */
+    uint32_t flags;            /* GPUGI_RENDER_* bits; other bits must be 0 */
 } gpugi_render_params;
+
+/* Random streams of a pass. Default (flags 0): per-pixel PCG, the
+ * PCG-RXS-M-XS-32 generator (an addition; the path seed of pixel p in
+ * iteration i is pcg(pcg(i) + p)). With GPUGI_RENDER_REFERENCE_RNG the passes
+ * draw gpugi's own streams (gpugi/shader/random.glsl:1-43: seed
+ * wanghash(WangHash(i) + p), xorshift32 draws), the parity mode in which the
+ * images follow the reference's random decisions. */
+#define GPUGI_RENDER_REFERENCE_RNG 1u
+#define GPUGI_RENDER_KNOWN_FLAGS GPUGI_RENDER_REFERENCE_RNG
 
 /* Camera::ComputeCameraParams (gpugi/camera/camera.cpp:76-85) and the pixel
  * area of RendererSystem::SetCamera (gpugi/renderer/renderersystem.cpp:208). */

@@ -105,15 +105,17 @@ PASSES = {"PT": 0, "LT": 1, "BPT": 2, "WHITTED": 3}
 def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.ndarray, frame_seed: int,
            light_samples: np.ndarray, max_path_length: int = 8, rr_start_depth: int = 0, sky=(0.0, 0.0, 0.0),
            accum: np.ndarray | None = None, num_threads=None, photons_per_light_sample: int = 2048,
-           query_radius: float = 0.01, gbuffer: np.ndarray | None = None) -> np.ndarray:
+           query_radius: float = 0.01, gbuffer: np.ndarray | None = None, rng: str = "pcg") -> np.ndarray:
     """One iteration of a pass (restated pathtracer.comp / lighttracer.comp /
     BPT / whittedraytracer.comp / the photon mapper "PM" / the importon map
     light tracer "IM"), accumulated into accum (H, W, 4) float32, which is
     returned. "IM" also needs gbuffer, an (H, W, 5) float32 array of the
     first eye hits that the caller carries from iteration to iteration
-    (zeros before the first)."""
+    (zeros before the first). rng: "pcg" or "reference" random streams;
+    frame_seed must be that generator's FrameSeed of the iteration."""
     from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
     L = lib()
+    set_rng(rng)
     P, U32, I, F = C.c_void_p, C.c_uint32, C.c_int, C.c_float
     L.oracle_render.argtypes = [P, U32, U32, P, U32, U32, P, P, U32, P, U32, I, I, I, I, I, P, U32, P, I, P, P, I]
     hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
@@ -154,6 +156,16 @@ def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.nda
                          _p(skya), _p(accum), nt)
     assert rc == 0
     return accum
+
+
+def set_rng(rng: str) -> None:
+    """Random streams of the following rendering calls ("pcg" or "reference")."""
+    if rng not in ("pcg", "reference"):
+        raise ValueError(rng)
+    L = lib()
+    L.oracle_set_rng.argtypes = [C.c_int]
+    L.oracle_set_rng.restype = None
+    L.oracle_set_rng(1 if rng == "pcg" else 0)
 
 
 def _render_scene_args(bvh, scene):
@@ -224,9 +236,10 @@ def hier_materials(bvh, scene: dict) -> np.ndarray:
 def render_hier(bvh, scene: dict, width: int, height: int, camera: np.ndarray, frame_seed: int,
                 light_samples: np.ndarray, importance: np.ndarray, materials: np.ndarray, sggx: np.ndarray,
                 max_path_length: int = 4, sky=(0.0, 0.0, 0.0), accum: np.ndarray | None = None,
-                num_threads=None) -> np.ndarray:
+                num_threads=None, rng: str = "pcg") -> np.ndarray:
     """One iteration of hierarchypathtracer.comp, accumulated into accum (H, W, 4)."""
     L = lib()
+    set_rng(rng)
     I = C.c_int
     L.oracle_render_hier.argtypes = _SCENE_T + [I, I, I, C.c_void_p, C.c_uint32, C.c_void_p, I, C.c_void_p,
                                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, I]

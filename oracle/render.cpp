@@ -46,20 +46,52 @@ static uint wanghash(uint x) {
     x = x ^ (x >> 15);
     return x;
 }
-static uint RandomUInt(uint& seed) {
+// Random streams. Reference mode: random.glsl as written (wanghash seeds,
+// xorshift32 draws, float(u) / 4294967297.0). PCG mode (the default of the
+// CUDA passes, an addition): PCG-RXS-M-XS-32 (O'Neill, "PCG: A Family of
+// Simple Fast Space-Efficient Statistically Good Algorithms for Random Number
+// Generation", 2014, section 6.3.4) with multiplier 747796405 and increment
+// 2891336453; one step doubles as the seed hash; draws as float(u >> 8) / 2^24.
+struct Rng {
+    uint s;
+    uint pcg;
+};
+static uint PcgOutput(uint state) {
+    uint w = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (w >> 22u) ^ w;
+}
+static uint PcgHash(uint x) { return PcgOutput(x * 747796405u + 2891336453u); }
+static uint SeedHash(uint pcg, uint x) { return pcg ? PcgHash(x) : wanghash(x); }
+static uint XorShift32(uint& seed) {
     seed ^= (seed << 13);
     seed ^= (seed >> 17);
     seed ^= (seed << 5);
     return seed;
 }
-static uint InitRandomSeed(uint frameSeed, uint invocationID) { return wanghash(frameSeed + invocationID); }
+static uint RandomUInt(Rng& r) {
+    if (r.pcg) {
+        r.s = r.s * 747796405u + 2891336453u;
+        return PcgOutput(r.s);
+    }
+    return XorShift32(r.s);
+}
+// InitRandomSeed(frameSeed, invocationID) = hash(frameSeed + invocationID).
+static Rng InitRandomSeed(uint pcg, uint frameSeed, uint invocationID) {
+    return Rng{SeedHash(pcg, frameSeed + invocationID), pcg};
+}
 // float(RandomUInt) / 4294967297.0: the float literal rounds to 2^32.
-static float Random(uint& seed) { return float(RandomUInt(seed)) / 4294967297.0f; }
-static vec2 Random2(uint& seed) {
+static float Random(Rng& r) {
+    uint u = RandomUInt(r);
+    return r.pcg ? float(u >> 8) / 16777216.0f : float(u) / 4294967297.0f;
+}
+static vec2 Random2(Rng& seed) {
     float a = Random(seed);
     float b = Random(seed);
     return vec2(a, b);
 }
+// Mode of the next oracle call (the rendering entry points copy it into
+// their Params; the oracle serves one caller at a time).
+static uint g_rngPcg = 1;
 static vec3 SampleDirection(vec2 r) {
     float cosTheta = r.x * 2.0f - 1.0f;
     float sinTheta = sqrt((1.0f - cosTheta) * (1.0f + cosTheta));
@@ -149,7 +181,7 @@ static vec3 GetDiffuseProbability(const MaterialData& m, float) {
 }
 
 // materials.glsl:118-277
-static vec3 SampleBSDFImpl(vec3 incidentDirection, const MaterialData& m, uint& seed, vec3 N, vec3& pathThroughput,
+static vec3 SampleBSDFImpl(vec3 incidentDirection, const MaterialData& m, Rng& seed, vec3 N, vec3& pathThroughput,
                            bool adjoint, float& pdf, bool* isReflectedDiffuse, bool stopOnDiffuse = false) {
     float cosTheta = dot(N, incidentDirection);
     float cosThetaAbs = saturate(abs(cosTheta));
@@ -273,6 +305,7 @@ struct Params {
     vec3 camU, camV, camW, camPos;
     float pixelArea;
     uint frameSeed;
+    uint rng = g_rngPcg;       // 1 PCG streams, 0 the reference's
     int numLightSamples;
     const vec4* lightSamples;  // 2 texels per sample
     vec3 sky;                  // constant radiance on a miss (addition)
@@ -346,7 +379,7 @@ static vec3 EstimateDirectLight(const RenderScene& s, const Params& P, vec3 pos,
     return vec3(0.0f);
 }
 
-static Ray PrimaryRay(const Params& P, uint& seed, int x, int y) {
+static Ray PrimaryRay(const Params& P, Rng& seed, int x, int y) {
     vec2 sub = Random2(seed) - 0.5f;
     vec2 screen = (sub + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
     Ray r;
@@ -358,7 +391,7 @@ static Ray PrimaryRay(const Params& P, uint& seed, int x, int y) {
 // ------------------------------------------------------------ pathtracer.comp
 static vec3 PathtracePixel(const RenderScene& s, const Params& P, int x, int y) {
     const float lightSampleWeight = float(P.numLightSamples) / 1;
-    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    Rng seed = InitRandomSeed(P.rng, P.frameSeed, (uint)(x + y * P.width));
     vec3 color(0.0f), pathThroughput(1.0f);
     bool didNEE = false;
     Ray ray = PrimaryRay(P, seed, x, y);
@@ -401,7 +434,7 @@ static vec3 PathtracePixel(const RenderScene& s, const Params& P, int x, int y) 
 // NUM_LIGHT_SAMPLES = 2 NEE samples. The miss sky is the documented addition.
 static vec3 WhittedPixel(const RenderScene& s, const Params& P, int x, int y) {
     const float lightSampleWeight = float(P.numLightSamples) / 2.0f;
-    uint seed = wanghash(P.frameSeed);
+    Rng seed{SeedHash(P.rng, P.frameSeed), P.rng};  // InitCoherentRandomSeed
     vec2 screen = (Random2(seed) + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
     Ray ray;
     ray.Origin = P.camPos;
@@ -481,7 +514,7 @@ struct PhotonGrid {
 // photondistribution.comp:10-106, one photon path.
 static void PhotonThread(const RenderScene& s, const Params& P, uint gid, int photonsPerSample,
                          std::vector<Photon>& out) {
-    uint seed = InitRandomSeed(P.frameSeed, gid);
+    Rng seed = InitRandomSeed(P.rng, P.frameSeed, gid);
     int lightSampleIndex = int(gid / (uint)photonsPerSample);
     vec4 pn0 = P.lightSamples[2 * lightSampleIndex];
     vec4 in1 = P.lightSamples[2 * lightSampleIndex + 1];
@@ -545,7 +578,7 @@ static vec3 IrradianceEstimate(const Photon& ph, const Ray& ray, const MaterialD
 // gather.comp:38-133, one pixel: eye path to the first diffuse decision,
 // then the photons of the 2x2x2 cells from round(pos / spacing).
 static vec3 GatherPixel(const RenderScene& s, const Params& P, const PhotonGrid& grid, int x, int y) {
-    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    Rng seed = InitRandomSeed(P.rng, P.frameSeed, (uint)(x + y * P.width));
     vec2 screen = (Random2(seed) + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
     Ray ray;
     ray.Origin = P.camPos;
@@ -644,7 +677,7 @@ struct GBufferTexel {
 static vec3 ImportonPixel(const RenderScene& s, const Params& P, int x, int y, GBufferTexel& gb, Importon& imp,
                           bool& stored) {
     stored = false;
-    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    Rng seed = InitRandomSeed(P.rng, P.frameSeed, (uint)(x + y * P.width));
     Ray ray = PrimaryRay(P, seed, x, y);
     vec3 color(0.0f), pathThroughput(1.0f);
     gb.n0 = 0.0f;  // color_a.w of a path that misses
@@ -745,7 +778,7 @@ static void ProjectToScreenGBuffer(const Params& P, Image& img, const GBufferTex
 // one photon path.
 static void ImportonPhotonThread(const RenderScene& s, const Params& P, Image& img, const GBufferTexel* gbuf,
                                  const ImportonGrid& grid, uint gid, int photonsPerSample) {
-    uint seed = InitRandomSeed(P.frameSeed, gid);
+    Rng seed = InitRandomSeed(P.rng, P.frameSeed, gid);
     int lightSampleIndex = int(gid / (uint)photonsPerSample);
     vec4 pn0 = P.lightSamples[2 * lightSampleIndex];
     vec4 in1 = P.lightSamples[2 * lightSampleIndex + 1];
@@ -871,7 +904,7 @@ static void ProjectToScreen(const RenderScene& s, const Params& P, Image& img, c
 
 // ------------------------------------------------------------ lighttracer.comp
 static void LighttraceThread(const RenderScene& s, const Params& P, Image& img, uint gid, LightCache* cache) {
-    uint seed = InitRandomSeed(P.frameSeed, gid);
+    Rng seed = InitRandomSeed(P.rng, P.frameSeed, gid);
     int lightSampleIndex = int(gid / (uint)P.numRaysPerLightSample);
     vec4 pn0 = P.lightSamples[2 * lightSampleIndex];
     vec4 in1 = P.lightSamples[2 * lightSampleIndex + 1];
@@ -974,7 +1007,7 @@ static void ShowLightSample(const RenderScene& s, const Params& P, Image& img, i
 // ----------------------------------------------- pathtracer_bidir.comp
 static vec3 BidirPixel(const RenderScene& s, const Params& P, const LightCache& cache, uint32_t numEntries, int x,
                        int y) {
-    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    Rng seed = InitRandomSeed(P.rng, P.frameSeed, (uint)(x + y * P.width));
     Ray ray = PrimaryRay(P, seed, x, y);
     vec3 color(0.0f), pathThroughput(1.0f);
     const uint actual = numEntries;
@@ -1189,7 +1222,7 @@ static void TraceRayCountHits(const Scene& s, const Ray& ray, float rayLength, f
 // acquisition2.comp:26-112 (NEXT_EVENT_IMPORTANCE, one light sample, path
 // length 8, no Russian roulette) for one pixel of iteration `iteration`.
 static void AcquirePixel(const RenderScene& s, const Params& P, int iteration, int x, int y, float* imp) {
-    uint seed = InitRandomSeed(wanghash((uint)iteration), (uint)(x + y * P.width));
+    Rng seed = InitRandomSeed(0u, wanghash((uint)iteration), (uint)(x + y * P.width));  // reference streams
     vec2 screen = (Random2(seed) + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
     float pathImportance = 1.0f;
     Ray ray;
@@ -1390,7 +1423,7 @@ static vec3 MulMV(const Mat3& m, vec3 v) {  // column combination, left to right
 }
 
 // sampleNormal (sggx.glsl:16-56): a visible normal of the node's NDF.
-static vec3 SampleSGGXNormal(vec3 incident, const Mat3& S, uint& seed) {
+static vec3 SampleSGGXNormal(vec3 incident, const Mat3& S, Rng& seed) {
     Mat3 local;
     local.c[2] = -incident;
     CreateONB(incident, local.c[0], local.c[1]);
@@ -1562,7 +1595,7 @@ static vec3 EstimateDirectLightImportance(const RenderScene& s, const Params& P,
 static vec3 HierarchyPixel(const RenderScene& s, const Params& P, const float* imp, const uint* mats,
                            const uint16_t* sggx, int x, int y) {
     const float lightSampleWeight = float(P.numLightSamples) / 1;
-    uint seed = InitRandomSeed(P.frameSeed, (uint)(x + y * P.width));
+    Rng seed = InitRandomSeed(P.rng, P.frameSeed, (uint)(x + y * P.width));
     vec2 screen = (Random2(seed) + vec2((float)x, (float)y)) / vec2((float)P.width, (float)P.height) * 2.0f - 1.0f;
     Ray ray;
     ray.Origin = P.camPos;
@@ -1912,6 +1945,9 @@ int oracle_render(const float* hierarchy, uint32_t numNodes, uint32_t boundsKind
 }
 
 uint32_t oracle_wanghash(uint32_t x) { return wanghash(x); }
+uint32_t oracle_pcg_hash(uint32_t x) { return PcgHash(x); }
+// Random streams of the following calls: 1 PCG, 0 the reference's.
+void oracle_set_rng(int pcg) { g_rngPcg = pcg ? 1u : 0u; }
 
 // HierarchyImportance::Draw's importance pass on an AABB hierarchy
 // (hierarchyimportance.cpp:83-109): `iterations` acquisition passes of

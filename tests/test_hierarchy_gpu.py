@@ -93,7 +93,7 @@ def test_render_matches_oracle(cuda_ctx, room):
     imp, _, mats = ds.hierarchy_read()
     acc = None
     for s in range(iters):
-        acc = oracle.render_hier(b, sc, W, H, cam.as_array(), render.wanghash(s), ls[s], imp, mats, b.sggx,
+        acc = oracle.render_hier(b, sc, W, H, cam.as_array(), render.frame_seed(s), ls[s], imp, mats, b.sggx,
                                  max_path_length=4, accum=acc)
     o = acc[..., :3] / iters
     _stat_compare(np.stack(batches), o, tol_mean=0.03)

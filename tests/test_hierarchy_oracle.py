@@ -147,8 +147,8 @@ def test_unbroken_hierarchy_renders_like_the_path_tracer():
     acc_h = acc_p = None
     n = 24
     for it in range(n):
-        acc_h = oracle.render_hier(b, sc, W, H, cam, render.wanghash(it), ls, imp, mats, b.sggx, accum=acc_h)
-        acc_p = oracle.render(b, sc, "PT", W, H, cam, render.wanghash(it + 1000), ls, max_path_length=4, accum=acc_p)
+        acc_h = oracle.render_hier(b, sc, W, H, cam, render.frame_seed(it), ls, imp, mats, b.sggx, accum=acc_h)
+        acc_p = oracle.render(b, sc, "PT", W, H, cam, render.frame_seed(it + 1000), ls, max_path_length=4, accum=acc_p)
     assert np.all(acc_h[..., 3] == n)
     mh, mp = acc_h[..., :3].mean() / n, acc_p[..., :3].mean() / n
     assert mh > 0 and abs(mh / mp - 1) < 0.05, (mh, mp)

@@ -1,7 +1,8 @@
 """GPU wavefront renderers (PT, LT, BPT) against the oracle, through the C ABI.
 
 The oracle and the kernels draw the same per-path RNG streams in the same
-order (wanghash seeds, xorshift32) on bit-identical hierarchies, and take the
+order (PCG by default; wanghash seeds + xorshift32 in the reference mode) on
+bit-identical hierarchies, and take the
 same light-sample arrays. Shading uses CUDA's sinf/cosf/powf instead of the C
 library's, so values differ in the last bits and a path may eventually branch
 differently; the bars are therefore:
@@ -39,10 +40,11 @@ def _light_sets(ds, n_sets, n, seed=123):
     return np.stack([render.generate_light_samples(ds, state, n) for _ in range(n_sets)])
 
 
-def _oracle(b, sc, pass_, W, H, cam, ls, iters, first=0, **kw):
+def _oracle(b, sc, pass_, W, H, cam, ls, iters, first=0, rng="pcg", **kw):
     acc = None
     for s in range(iters):
-        acc = oracle.render(b, sc, pass_, W, H, cam.as_array(), render.wanghash(first + s), ls[s], accum=acc, **kw)
+        acc = oracle.render(b, sc, pass_, W, H, cam.as_array(), render.frame_seed(first + s, rng), ls[s], accum=acc,
+                            rng=rng, **kw)
     return acc
 
 
@@ -56,15 +58,16 @@ def test_light_sampler_matches_scene_lights(cuda_ctx, room):
     assert np.allclose(ls[:, 4:7], 10.0 * 0.25 / 128, rtol=1e-5)
 
 
-def test_pt_direct_light_matches_oracle(cuda_ctx, room):
+@pytest.mark.parametrize("rng", ["pcg", "reference"])
+def test_pt_direct_light_matches_oracle(cuda_ctx, room, rng):
     sc, b, ds = room
     W = H = 48
     cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
     ls = _light_sets(ds, 4, 128)
     img = render.Image(cuda_ctx, W, H)
-    render.render(cuda_ctx, ds, cam, img, "PT", max_path_length=1, samples=4, iteration=0, light_samples=ls)
+    render.render(cuda_ctx, ds, cam, img, "PT", max_path_length=1, samples=4, iteration=0, light_samples=ls, rng=rng)
     g = img.read()
-    o = _oracle(b, sc, "PT", W, H, cam, ls, 4, max_path_length=1)
+    o = _oracle(b, sc, "PT", W, H, cam, ls, 4, max_path_length=1, rng=rng)
     err = np.abs(g[..., :3] - o[..., :3])
     assert err.max() <= 1e-4 * np.abs(o[..., :3]).max() + 1e-6
     img.close()
@@ -83,8 +86,10 @@ def _stat_compare(g_batches, o_img, tol_mean=0.02, z=6.0):
     assert (d <= z * np.sqrt(2) * se + 1e-3 * np.abs(gb.mean(0)) + 1e-5).mean() > 0.97
 
 
-@pytest.mark.parametrize("pass_,iters", [("PT", 32), ("BPT", 32), ("LT", 48)])
-def test_full_depth_passes_match_oracle(cuda_ctx, room, pass_, iters):
+@pytest.mark.parametrize("pass_,iters,rng", [("PT", 32, "pcg"), ("BPT", 32, "pcg"), ("LT", 48, "pcg"),
+                                             ("PT", 32, "reference"), ("BPT", 32, "reference"),
+                                             ("LT", 48, "reference")])
+def test_full_depth_passes_match_oracle(cuda_ctx, room, pass_, iters, rng):
     sc, b, ds = room
     W = H = 32
     cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
@@ -96,10 +101,10 @@ def test_full_depth_passes_match_oracle(cuda_ctx, room, pass_, iters):
     for k in range(K):
         img = render.Image(cuda_ctx, W, H)
         render.render(cuda_ctx, ds, cam, img, pass_, max_path_length=6, samples=per, iteration=k * per,
-                      light_samples=ls[k * per:(k + 1) * per])
+                      light_samples=ls[k * per:(k + 1) * per], rng=rng)
         batches.append(img.read()[..., :3] / per)
         img.close()
-    o = _oracle(b, sc, pass_, W, H, cam, ls, iters, max_path_length=6)[..., :3] / iters
+    o = _oracle(b, sc, pass_, W, H, cam, ls, iters, max_path_length=6, rng=rng)[..., :3] / iters
     _stat_compare(np.stack(batches), o, tol_mean=0.03)
     assert cuda_ctx.device_error_bits() == 0
 
@@ -174,7 +179,7 @@ def test_converged_image_matches_oracle_per_pixel(cuda_ctx, pass_):
         acc = None
         for s in range(per):
             ls = render.generate_light_samples(ds, st, nls)
-            acc = oracle.render(b, sc, pass_, W, H, cam.as_array(), render.wanghash(k * per + s), ls,
+            acc = oracle.render(b, sc, pass_, W, H, cam.as_array(), render.frame_seed(k * per + s), ls,
                                 max_path_length=depth, accum=acc)
         batches.append(acc[..., :3].astype(np.float64) / per)
     batches = np.stack(batches)
@@ -276,7 +281,7 @@ def test_photon_mapper_converges_to_path_tracing(cuda_ctx, room):
 def _oracle_im(b, sc, W, H, cam, ls, iters, **kw):
     acc, gbuf = None, np.zeros((H, W, 5), np.float32)
     for s in range(iters):
-        acc = oracle.render(b, sc, "IM", W, H, cam.as_array(), render.wanghash(s), ls[s], accum=acc, gbuffer=gbuf,
+        acc = oracle.render(b, sc, "IM", W, H, cam.as_array(), render.frame_seed(s), ls[s], accum=acc, gbuffer=gbuf,
                             **kw)
     return acc
 
