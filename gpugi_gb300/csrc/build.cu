@@ -677,6 +677,8 @@ extern "C" gpugi_status gpugi_scene_export(gpugi_ctx* ctx, const gpugi_scene* sc
             std::memcpy(&w, &hierarchy[8 * i + 3], 4);
             if (w & LEAF_FLAG) w = LEAF_FLAG | (w & LEAF_BLOCK_MASK);
             std::memcpy(&hierarchy[8 * i + 3], &w, 4);
+            if (!sc->hostRadii.empty())  // ellipsoid nodes: the radii as uploaded, not their reciprocals
+                for (int c = 0; c < 3; ++c) hierarchy[8 * i + 4 + c] = sc->hostRadii[3 * i + c];
         }
     }
     GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

@@ -93,6 +93,9 @@ struct gpugi_scene {
     // Node order on the device: uploaded (preorder) index -> device index;
     // empty when the two are the same.
     std::vector<uint32_t> nodeMap;
+    // Ellipsoid scenes: the radii as uploaded (3 floats per node, device
+    // order); the device nodes hold their reciprocals.
+    std::vector<float> hostRadii;
     // hierarchy-importance renderer (hierarchy.cu), device node order
     gpugi::HierBuffers* hier = nullptr;
 };

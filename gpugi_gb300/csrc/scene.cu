@@ -173,6 +173,19 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
 
     std::vector<uint32_t> nodeMap;  // uploaded index -> device index (empty: the same)
     const uint32_t topNodes = relayout_nodes(nodes, numNodes, ctx->sharedNodes, nodeMap);
+    // Ellipsoid nodes travel as {center, firstChild}, {1 / (radii + 1e-15), escape}:
+    // the node test then multiplies where the virtual-ellipsoid arithmetic
+    // divides (the guard is the shader's, intersectiontests.glsl:29).
+    std::vector<float> hostRadii;
+    if (boundsKind == GPUGI_BOUNDS_ELLIPSOID) {
+        hostRadii.resize(3 * (size_t)numNodes);
+        for (size_t i = 0; i < numNodes; ++i)
+            for (int c = 0; c < 3; ++c) {
+                float& r = nodes[8 * i + 4 + c];
+                hostRadii[3 * i + c] = r;
+                r = 1.0f / (r + 1e-15f);
+            }
+    }
 
     cudaError_t se = cudaSetDevice(ctx->device);
     if (se != cudaSuccess) return cuda_fail(ctx, se, "cudaSetDevice");
@@ -220,6 +233,7 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     sc->dev.numMaterials = numMaterials;
     sc->dev.topNodes = topNodes;
     sc->nodeMap.swap(nodeMap);
+    sc->hostRadii.swap(hostRadii);
     sc->hostPositions.assign(positions, positions + 3 * (size_t)numVertices);
     sc->hostSlots.assign(slots, slots + 4 * (size_t)numSlots);
     if (numMaterials)

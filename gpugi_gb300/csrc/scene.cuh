@@ -2,7 +2,7 @@
 //
 //   nodes      2 x float4 per node (32 B, 32-B aligned): {min.xyz | child},
 //              {max.xyz | escape}; ellipsoid bounds store {center | child},
-//              {radii | escape}. Same stride and words as gpugi's
+//              {1 / (radii + 1e-15) | escape}. Same stride and words as gpugi's
 //              HierachyBuffer (scene.hpp:30-38) except that a leaf child
 //              also carries the count of leading valid slots (common.cuh).
 //   tris       3 x float4 per leaf slot (48 B): p0, e0 = p1-p0, e1 = p0-p2,

@@ -30,22 +30,26 @@ GPUGI_D bool intersect_box(float3 o, float3 inv, float4 lo, float4 hi, float& fi
     return firstHit <= lastHit;
 }
 
-// Ray against a stored axis-aligned ellipsoid {center, radii}; arithmetic of
-// IntersectVirtualEllipsoid (intersectiontests.glsl:26-52), including its
-// +1e-15 radius guard.
-GPUGI_D bool intersect_ellipsoid(float3 ro, float3 rd, float4 c, float4 r, float& firstHit) {
-    float3 radii = make_float3(X::add(r.x, 1e-15f), X::add(r.y, 1e-15f), X::add(r.z, 1e-15f));
+// Ray against a stored axis-aligned ellipsoid. The node holds {center,
+// ir = 1 / (radii + 1e-15)} (reciprocals taken at upload; the guard is the
+// one of IntersectVirtualEllipsoid, intersectiontests.glsl:26-52). The steps
+// are that function's: advance the ray to its closest approach to the centre
+// for stability, scale into the unit sphere and solve the quadratic; the
+// scaling multiplies by ir and the two quotients by ddotd share one
+// reciprocal, so a node costs one correctly rounded reciprocal and one sqrt
+// instead of eight divisions and a sqrt. The reference never walks
+// ellipsoids, so this test defines the node kind; the oracle restates it
+// operation for operation.
+GPUGI_D bool intersect_ellipsoid(float3 ro, float3 rd, float4 c, float4 ir, float& firstHit) {
     float3 o = X::sub3(ro, xyz(c));
-    float t = X::dot(o, rd);
-    t = fmaxf(0.0f, -t);
+    const float t = fmaxf(0.0f, -X::dot(o, rd));
     o = X::add3(o, X::scale(t, rd));
-    o = X::div3(o, radii);
-    float odoto = X::dot(o, o);
-    float3 d = X::div3(rd, radii);
-    float odotd = X::dot(o, d);
-    float ddotd = X::dot(d, d);
-    float phalf = X::div(odotd, ddotd);
-    float q = X::div(X::sub(odoto, 1.0f), ddotd);
+    o = X::mul3(o, xyz(ir));
+    const float3 d = X::mul3(rd, xyz(ir));
+    const float odoto = X::dot(o, o), odotd = X::dot(o, d), ddotd = X::dot(d, d);
+    const float inv = X::rcp(ddotd);
+    const float phalf = X::mul(odotd, inv);
+    const float q = X::mul(X::sub(odoto, 1.0f), inv);
     float rad = X::sub(X::mul(phalf, phalf), q);
     if (rad < 0.0f) return false;
     rad = __fsqrt_rn(rad);

@@ -260,6 +260,31 @@ def render_hier(bvh, scene: dict, width: int, height: int, camera: np.ndarray, f
     return accum
 
 
+def light_samples(positions, slots, materials, num_samples: int, rng_state: list, point_lights=(),
+                  directional_lights=()) -> np.ndarray:
+    """LightSampler::GenerateRandomSamples (restated, lights.cpp) over a
+    scene's triangle slots and materials; point_lights: (position,
+    intensity) pairs, directional_lights: (unit direction towards the light,
+    irradiance) pairs. rng_state: one-element list with the 64-bit xorshift*
+    state, updated. Returns (num_samples, 8) float32."""
+    L = lib()
+    P, U32 = C.c_void_p, C.c_uint32
+    L.oracle_light_samples.argtypes = [P, P, U32, P, P, U32, P, U32, C.POINTER(C.c_uint64), U32, P]
+    L.oracle_light_samples.restype = C.c_int
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    sl = np.ascontiguousarray(slots, dtype=np.int32).reshape(-1, 4)
+    mats = np.ascontiguousarray(materials, dtype=np.float32).reshape(-1)
+    pts = np.ascontiguousarray(np.array([list(p) + list(i) for p, i in point_lights], np.float32).reshape(-1, 6))
+    drs = np.ascontiguousarray(np.array([list(d) + list(e) for d, e in directional_lights], np.float32).reshape(-1, 6))
+    out = np.zeros((num_samples, 8), np.float32)
+    st = C.c_uint64(rng_state[0])
+    rc = L.oracle_light_samples(_p(pos), _p(sl), sl.shape[0], _p(mats), _p(pts), pts.shape[0], _p(drs), drs.shape[0],
+                                C.byref(st), num_samples, _p(out))
+    assert rc == 0, "light sample outside the summed table"
+    rng_state[0] = st.value
+    return out
+
+
 def float_to_half(x: np.ndarray) -> np.ndarray:
     L = lib()
     L.oracle_float_to_half.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]

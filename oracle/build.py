@@ -14,7 +14,7 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-SOURCES = ["trace.cpp", "render.cpp"]
+SOURCES = ["trace.cpp", "render.cpp", "lights.cpp"]
 OUT = HERE / "lib" / "liboracle.so"
 
 

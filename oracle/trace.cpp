@@ -33,25 +33,28 @@ static bool IntersectBox(vec3 rayOrigin, vec3 invRayDir, vec3 aabbMin, vec3 aabb
     return firstHit <= lastHit;
 }
 
-// Ray against a stored axis-aligned ellipsoid {center, radii}. The arithmetic
-// follows IntersectVirtualEllipsoid (intersectiontests.glsl:26-52), which
-// derives center/radii from a box; here they come from the node
-// (bvhmake's "bounding_ellipsoid" chunk, bvhmake/bvhbuilder.cpp:586-588).
-// The +1e-15 guard of the virtual version is kept so that flat leaves with a
-// zero radius stay finite.
+// Ray against a stored axis-aligned ellipsoid {center, radii} (bvhmake's
+// "bounding_ellipsoid" chunk, bvhmake/bvhbuilder.cpp:586-588). The reference
+// never traverses ellipsoids (its IntersectVirtualEllipsoid,
+// intersectiontests.glsl:26-52, is unused), so the node test is the
+// library's own: that function's steps (closest approach, scaling into the
+// unit sphere, quadratic) with ir = 1 / (radii + 1e-15) (the shader's guard,
+// taken once per node) multiplied in, and one reciprocal of ddotd shared by
+// both quotients.
 static bool IntersectEllipsoid(const Ray& ray, vec3 center, vec3 radiiIn, float& firstHit) {
-    vec3 radii = radiiIn + 1e-15f;
+    const vec3 ir = 1.0f / (radiiIn + 1e-15f);
     vec3 o = ray.Origin - center;
     float t = dot(o, ray.Direction);
     t = max(0.0f, -t);
     o += ray.Direction * t;
-    o /= radii;
+    o *= ir;
     float odoto = dot(o, o);
-    vec3 d = ray.Direction / radii;
+    vec3 d = ray.Direction * ir;
     float odotd = dot(o, d);
     float ddotd = dot(d, d);
-    float phalf = odotd / ddotd;
-    float q = (odoto - 1.0f) / ddotd;
+    float inv = 1.0f / ddotd;
+    float phalf = odotd * inv;
+    float q = (odoto - 1.0f) * inv;
     float rad = phalf * phalf - q;
     if (rad < 0.0f) return false;
     rad = sqrt(rad);

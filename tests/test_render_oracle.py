@@ -247,3 +247,20 @@ def test_rng_modes_agree_in_distribution(built, rng):
     # the floor right under the light: albedo / pi * I / d^2 at normal incidence
     centre = img[H // 2 - 1:H // 2 + 1, W // 2 - 1:W // 2 + 1].mean()
     assert abs(centre / (0.5 / math.pi * 5.0) - 1) < 0.02, centre
+
+
+def test_light_sampler_restatement(built):
+    """oracle/lights.cpp: area samples lie on the ceiling light, carry
+    luminance x area / n each (lightsampler.cpp:36,72), and a point light
+    takes the share of its log flux (scene.cpp:295-307)."""
+    sc = scenes.cornell_room(seed=1, sphere_level=2, wall_grid=2)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ls = oracle.light_samples(sc["positions"], b.slots, sc["materials"], 128, [123])
+    assert np.allclose(ls[:, 1], 1.999 - 1e-4, atol=1e-6)
+    assert (np.abs(ls[:, 0]) <= 0.25 + 1e-6).all() and (np.abs(ls[:, 2]) <= 0.25 + 1e-6).all()
+    assert np.allclose(ls[:, 4:7], 10.0 * 0.25 / 128, rtol=1e-5)
+    both = oracle.light_samples(sc["positions"], b.slots, sc["materials"], 128, [123],
+                                point_lights=[((0.0, 1.0, 0.0), (1000.0, 1000.0, 1000.0))])
+    area_flux = 10.0 * 0.25 * math.pi
+    point_flux = math.log(1.0 + 1000.0 * 4 * math.pi)
+    assert (both[:, 7] == 2.0).sum() == int(point_flux / (point_flux + area_flux) * 128)
