@@ -33,6 +33,27 @@ __global__ void k_prepare_triangles(const int4* __restrict__ slots, uint32_t num
     tris[3 * (size_t)i + 2] = c;
 }
 
+// Records of the watertight test: the exact vertices of each valid slot,
+// {p0.xyz p1.x | p1.yz p2.xy | p2.z 0 0 0}; invalid slots stay zero.
+__global__ void k_prepare_wt_triangles(const int4* __restrict__ slots, uint32_t numSlots,
+                                       const float* __restrict__ pos, float4* __restrict__ tris) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= numSlots) return;
+    int4 s = slots[i];
+    float4 a = make_float4(0, 0, 0, 0), b = a, c = a;
+    if (s.x != s.y) {
+        const float* p0 = pos + 3 * (size_t)s.x;
+        const float* p1 = pos + 3 * (size_t)s.y;
+        const float* p2 = pos + 3 * (size_t)s.z;
+        a = make_float4(p0[0], p0[1], p0[2], p1[0]);
+        b = make_float4(p1[1], p1[2], p2[0], p2[1]);
+        c = make_float4(p2[2], 0.0f, 0.0f, 0.0f);
+    }
+    tris[3 * (size_t)i] = a;
+    tris[3 * (size_t)i + 1] = b;
+    tris[3 * (size_t)i + 2] = c;
+}
+
 void prepare_triangles(cudaStream_t stream, const int4* slots, uint32_t numSlots, const float* positions,
                        float4* tris) {
     if (numSlots) k_prepare_triangles<<<(numSlots + 255) / 256, 256, 0, stream>>>(slots, numSlots, positions, tris);
@@ -240,6 +261,25 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
         sc->hostMaterials.assign(reinterpret_cast<const float*>(materials),
                                  reinterpret_cast<const float*>(materials) + 24 * (size_t)numMaterials);
     *out = sc;
+    return GPUGI_OK;
+}
+
+extern "C" gpugi_status gpugi_scene_set_triangle_test(gpugi_ctx* ctx, gpugi_scene* sc, uint32_t test) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!sc) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "scene is NULL");
+    if (test > GPUGI_TRIANGLE_WATERTIGHT) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown triangle test");
+    if (test == GPUGI_TRIANGLE_WATERTIGHT && !sc->dev.wtris) {
+        const uint32_t n = sc->dev.numSlots;
+        const float4* w = nullptr;
+        gpugi_status st = upload<float4>(ctx, sc, nullptr, 3 * (size_t)n, &w);
+        if (st) return st;
+        k_prepare_wt_triangles<<<(n + 255) / 256, 256, 0, ctx->stream>>>(sc->dev.slots, n, sc->dev.positions,
+                                                                         const_cast<float4*>(w));
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+        GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        sc->dev.wtris = w;
+    }
+    sc->dev.triangleTest = test;
     return GPUGI_OK;
 }
 

@@ -22,6 +22,9 @@ namespace gpugi {
 struct DevScene {
     const float4* nodes = nullptr;
     const float4* tris = nullptr;
+    // watertight test records {p0.xyz p1.x | p1.yz p2.xy | p2.z 0 0 0} per leaf
+    // slot, made on demand (gpugi_scene_set_triangle_test); null otherwise
+    const float4* wtris = nullptr;
     const int4* slots = nullptr;
     const float* positions = nullptr;
     const float4* vinfo = nullptr;
@@ -36,6 +39,9 @@ struct DevScene {
     // rest in preorder; persistent walkers stage nodes [0, topNodes) in
     // shared memory. Node 0 is the root; an escape of 0 still ends the walk.
     uint32_t topNodes = 0;
+    // Triangle test of the ray queries: 0 = the reference's (IntersectTriangle),
+    // 1 = watertight (wtris holds its records).
+    uint32_t triangleTest = 0;
 };
 
 // Material view (constant-valued MaterialData, materials.glsl:9-30).

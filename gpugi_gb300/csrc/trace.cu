@@ -4,12 +4,30 @@
 // load and store of a warp is a single coalesced 128-B transaction. The
 // walk itself reads 32-B nodes and 48-B triangle records through the
 // read-only (non-coherent) path with 16-B vector loads.
+#include <type_traits>
+
 #include "ctx.cuh"
 #include "trace.cuh"
 
 namespace gpugi {
 
-template <int BOUNDS>
+// Picks a kernel instantiation at run time: f receives (any hit, bounds kind,
+// triangle test) as integral constants and returns the kernel's address.
+template <typename F>
+static auto pick_variant(bool anyHit, bool ell, bool wt, F f) {
+    using B0 = std::false_type;
+    using B1 = std::true_type;
+    using I0 = std::integral_constant<int, 0>;
+    using I1 = std::integral_constant<int, 1>;
+    if (anyHit) {
+        if (ell) return wt ? f(B1{}, I1{}, I1{}) : f(B1{}, I1{}, I0{});
+        return wt ? f(B1{}, I0{}, I1{}) : f(B1{}, I0{}, I0{});
+    }
+    if (ell) return wt ? f(B0{}, I1{}, I1{}) : f(B0{}, I1{}, I0{});
+    return wt ? f(B0{}, I0{}, I1{}) : f(B0{}, I0{}, I0{});
+}
+
+template <int BOUNDS, int TRI>
 __global__ void __launch_bounds__(256) k_trace_closest(DevScene s, const float* __restrict__ ox,
                                                        const float* __restrict__ oy, const float* __restrict__ oz,
                                                        const float* __restrict__ dx, const float* __restrict__ dy,
@@ -20,14 +38,14 @@ __global__ void __launch_bounds__(256) k_trace_closest(DevScene s, const float* 
     if (i >= n) return;
     const float3 o = make_float3(__ldg(ox + i), __ldg(oy + i), __ldg(oz + i));
     const float3 d = make_float3(__ldg(dx + i), __ldg(dy + i), __ldg(dz + i));
-    TraceResult r = trace_ray<false, BOUNDS>(s, o, d, __ldg(tmax + i), err);
+    TraceResult r = trace_ray<false, BOUNDS, false, TRI>(s, o, d, __ldg(tmax + i), err);
     slot[i] = r.slot;
     t[i] = r.t;
     u[i] = r.u;
     v[i] = r.v;
 }
 
-template <int BOUNDS>
+template <int BOUNDS, int TRI>
 __global__ void __launch_bounds__(256) k_trace_any(DevScene s, const float* __restrict__ ox,
                                                    const float* __restrict__ oy, const float* __restrict__ oz,
                                                    const float* __restrict__ dx, const float* __restrict__ dy,
@@ -37,7 +55,7 @@ __global__ void __launch_bounds__(256) k_trace_any(DevScene s, const float* __re
     if (i >= n) return;
     const float3 o = make_float3(__ldg(ox + i), __ldg(oy + i), __ldg(oz + i));
     const float3 d = make_float3(__ldg(dx + i), __ldg(dy + i), __ldg(dz + i));
-    TraceResult r = trace_ray<true, BOUNDS>(s, o, d, __ldg(tmax + i), err);
+    TraceResult r = trace_ray<true, BOUNDS, false, TRI>(s, o, d, __ldg(tmax + i), err);
     occluded[i] = r.slot >= 0 ? 1 : 0;
 }
 
@@ -65,7 +83,7 @@ gpugi_status walker_launch_config(gpugi_ctx* ctx, const gpugi_scene* sc, const v
 // lanes busy by handing each finished lane the next ray index from a global
 // counter (one atomic per warp per refill). Each ray still performs exactly
 // trace_ray's sequence of tests, so results are identical.
-template <bool ANY_HIT, int BOUNDS>
+template <bool ANY_HIT, int BOUNDS, int TRI>
 __global__ void __launch_bounds__(128) k_trace_persistent(
     DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
     const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
@@ -99,7 +117,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err, s_top, stage)) {
+        if (active && walk_step<ANY_HIT, BOUNDS, TRI>(w, s, err, s_top, stage)) {
             if (ANY_HIT) {
                 occluded[ray] = w.slot >= 0 ? 1 : 0;
             } else {
@@ -121,11 +139,9 @@ gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool
     unsigned long long* counter = reinterpret_cast<unsigned long long*>(ctx->scratch);
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
-              const float*, uint64_t, int32_t*, float*, float*, float*, uint8_t*, unsigned long long*, uint32_t*,
-              uint32_t);
-    if (!ell) k = anyHit ? k_trace_persistent<true, 0> : k_trace_persistent<false, 0>;
-    else k = anyHit ? k_trace_persistent<true, 1> : k_trace_persistent<false, 1>;
+    auto k = pick_variant(anyHit, ell, sc->dev.triangleTest != 0, [](auto A, auto B, auto T) {
+        return &k_trace_persistent<decltype(A)::value, decltype(B)::value, decltype(T)::value>;
+    });
     WalkerLaunch L;
     gpugi_status st = walker_launch_config(ctx, sc, (const void*)k, n, ctx->sharedNodes, L);
     if (st) return st;
@@ -139,7 +155,7 @@ gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool
 // fully coalesced loads and stores tests the root bounds (the first test of
 // every walk). Rays that miss it are finished here; the others are appended
 // to a queue with warp-ballot compaction for the persistent walker.
-template <bool ANY_HIT, int BOUNDS>
+template <bool ANY_HIT, int BOUNDS, int TRI>
 __global__ void __launch_bounds__(256) k_trace_root_filter(
     DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
     const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
@@ -155,7 +171,8 @@ __global__ void __launch_bounds__(256) k_trace_root_filter(
         const float4 a = __ldg(s.nodes), b = __ldg(s.nodes + 1);
         float firstHit;
         bool hit;
-        if (BOUNDS == 0) hit = intersect_box(o, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a, b, firstHit);
+        if (BOUNDS == 0)
+            hit = intersect_box<TRI != 0>(o, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a, b, firstHit);
         else hit = intersect_ellipsoid(o, d, a, b, firstHit);
         pass = hit && firstHit <= len;
         if (!pass) {
@@ -182,7 +199,7 @@ __global__ void __launch_bounds__(256) k_trace_root_filter(
 // that pass are appended with one atomic per warp (warp prefix sum of the
 // per-thread counts). Results of passing rays are written too and later
 // overwritten by the walker.
-template <bool ANY_HIT, int BOUNDS>
+template <bool ANY_HIT, int BOUNDS, int TRI>
 __global__ void __launch_bounds__(256) k_trace_root_filter4(
     DevScene s, const float4* __restrict__ ox, const float4* __restrict__ oy, const float4* __restrict__ oz,
     const float4* __restrict__ dx, const float4* __restrict__ dy, const float4* __restrict__ dz,
@@ -203,7 +220,8 @@ __global__ void __launch_bounds__(256) k_trace_root_filter4(
             const float3 o = make_float3(xs[k], ys[k], zs[k]), d = make_float3(dxs[k], dys[k], dzs[k]);
             float firstHit;
             bool hit;
-            if (BOUNDS == 0) hit = intersect_box(o, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a, b, firstHit);
+            if (BOUNDS == 0)
+                hit = intersect_box<TRI != 0>(o, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a, b, firstHit);
             else hit = intersect_ellipsoid(o, d, a, b, firstHit);
             if (hit && firstHit <= ls[k]) pass |= 1u << k;
         }
@@ -248,7 +266,7 @@ __global__ void __launch_bounds__(256) k_trace_root_filter4(
 }
 
 // Second launch: the persistent walker over the queued ray indices.
-template <bool ANY_HIT, int BOUNDS>
+template <bool ANY_HIT, int BOUNDS, int TRI>
 __global__ void __launch_bounds__(128) k_trace_queue(
     DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
     const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
@@ -283,7 +301,7 @@ __global__ void __launch_bounds__(128) k_trace_queue(
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && walk_step<ANY_HIT, BOUNDS>(w, s, err, s_top, stage)) {
+        if (active && walk_step<ANY_HIT, BOUNDS, TRI>(w, s, err, s_top, stage)) {
             if (ANY_HIT) {
                 occluded[ray] = w.slot >= 0 ? 1 : 0;
             } else {
@@ -300,14 +318,14 @@ __global__ void __launch_bounds__(128) k_trace_queue(
 // Group walker (modes 3 and 4), second launch after the root prefilter: G
 // lanes walk each queued ray together (group_step), which shortens the
 // dependent fetch chain of the longest walks.
-template <bool ANY_HIT, int BOUNDS, int G>
+template <bool ANY_HIT, int BOUNDS, int G, int TRI>
 __global__ void __launch_bounds__(128, 10) k_trace_group(
     DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
     const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
     const float* __restrict__ tmax, int32_t* __restrict__ slot, float* __restrict__ t, float* __restrict__ u,
     float* __restrict__ v, uint8_t* __restrict__ occluded, const uint32_t* __restrict__ queue,
     unsigned long long* counters, uint32_t* err) {
-    group_walks<ANY_HIT, BOUNDS, G>(
+    group_walks<ANY_HIT, BOUNDS, G, TRI>(
         s, counters[1], counters + 2, err,
         [&](uint64_t i, float3& o, float3& d, float& len) {
             const uint32_t ray = __ldg(queue + i);
@@ -352,6 +370,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
     if (n == 0) return GPUGI_OK;
     cudaStream_t cs = stream ? stream : ctx->stream;
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    const bool wt = sc->dev.triangleTest != 0;
     // four rays per thread with 16-B accesses when every array allows it
     auto al = [](const void* p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; };
     const bool vec = al(ox) && al(oy) && al(oz) && al(dx) && al(dy) && al(dz) && al(tmax) && al(slot) && al(t) &&
@@ -361,7 +380,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         const unsigned grid4 = (unsigned)((n4 + 255) / 256);
         auto f4 = [](const float* p) { return reinterpret_cast<const float4*>(p); };
 #define GPUGI_FILTER4_ON(A, B)                                                                                        \
-    k_trace_root_filter4<A, B><<<grid4, 256, 0, cs>>>(                                                      \
+    (wt ? k_trace_root_filter4<A, B, 1> : k_trace_root_filter4<A, B, 0>)<<<grid4, 256, 0, cs>>>( \
         sc->dev, f4(ox), f4(oy), f4(oz), f4(dx), f4(dy), f4(dz), f4(tmax), n4, reinterpret_cast<int4*>(slot),          \
         reinterpret_cast<float4*>(t), reinterpret_cast<float4*>(u), reinterpret_cast<float4*>(v),                     \
         reinterpret_cast<uchar4*>(occluded), queue, counters)
@@ -379,7 +398,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         const unsigned grid1 = (unsigned)((m + 255) / 256);
         auto sh = [&](const float* p) { return p + head; };
 #define GPUGI_FILTER_ON(A, B)                                                                                        \
-    k_trace_root_filter<A, B><<<grid1, 256, 0, cs>>>(                                                       \
+    (wt ? k_trace_root_filter<A, B, 1> : k_trace_root_filter<A, B, 0>)<<<grid1, 256, 0, cs>>>( \
         sc->dev, sh(ox), sh(oy), sh(oz), sh(dx), sh(dy), sh(dz), sh(tmax), m, slot ? slot + head : nullptr,            \
         t ? t + head : nullptr, u ? u + head : nullptr, v ? v + head : nullptr, occluded ? occluded + head : nullptr, \
         queue, counters, (uint32_t)head)
@@ -393,19 +412,17 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
 #undef GPUGI_FILTER_ON
     }
     if (ctx->traceMode >= 3) {
-        void (*kg)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
-                   const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
-                   uint32_t*);
-        if (ctx->traceMode == 3) {
-            if (!ell) kg = anyHit ? k_trace_group<true, 0, 8> : k_trace_group<false, 0, 8>;
-            else kg = anyHit ? k_trace_group<true, 1, 8> : k_trace_group<false, 1, 8>;
-        } else if (ctx->traceMode == 4) {
-            if (!ell) kg = anyHit ? k_trace_group<true, 0, 4> : k_trace_group<false, 0, 4>;
-            else kg = anyHit ? k_trace_group<true, 1, 4> : k_trace_group<false, 1, 4>;
-        } else {
-            if (!ell) kg = anyHit ? k_trace_group<true, 0, 16> : k_trace_group<false, 0, 16>;
-            else kg = anyHit ? k_trace_group<true, 1, 16> : k_trace_group<false, 1, 16>;
-        }
+        auto kg = ctx->traceMode == 3
+                      ? pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {
+                            return &k_trace_group<decltype(A)::value, decltype(B)::value, 8, decltype(T)::value>;
+                        })
+                  : ctx->traceMode == 4
+                      ? pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {
+                            return &k_trace_group<decltype(A)::value, decltype(B)::value, 4, decltype(T)::value>;
+                        })
+                      : pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {
+                            return &k_trace_group<decltype(A)::value, decltype(B)::value, 16, decltype(T)::value>;
+                        });
         WalkerLaunch L;
         gpugi_status st = walker_launch_config(ctx, sc, (const void*)kg, 1ull << 40, 0, L);
         if (st) return st;
@@ -414,11 +431,9 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
         return GPUGI_OK;
     }
-    void (*k)(DevScene, const float*, const float*, const float*, const float*, const float*, const float*,
-              const float*, int32_t*, float*, float*, float*, uint8_t*, const uint32_t*, unsigned long long*,
-              uint32_t*, uint32_t);
-    if (!ell) k = anyHit ? k_trace_queue<true, 0> : k_trace_queue<false, 0>;
-    else k = anyHit ? k_trace_queue<true, 1> : k_trace_queue<false, 1>;
+    auto k = pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {
+        return &k_trace_queue<decltype(A)::value, decltype(B)::value, decltype(T)::value>;
+    });
     WalkerLaunch L;
     gpugi_status st = walker_launch_config(ctx, sc, (const void*)k, n, ctx->sharedNodes, L);
     if (st) return st;
@@ -428,7 +443,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
     return GPUGI_OK;
 }
 
-template <int BOUNDS, bool ANY>
+template <int BOUNDS, bool ANY, int TRI>
 __global__ void __launch_bounds__(256) k_trace_stats(DevScene s, const float* __restrict__ ox,
                                                      const float* __restrict__ oy, const float* __restrict__ oz,
                                                      const float* __restrict__ dx, const float* __restrict__ dy,
@@ -439,7 +454,7 @@ __global__ void __launch_bounds__(256) k_trace_stats(DevScene s, const float* __
     if (i < n) {
         const float3 o = make_float3(ox[i], oy[i], oz[i]);
         const float3 d = make_float3(dx[i], dy[i], dz[i]);
-        trace_ray<ANY, BOUNDS, true>(s, o, d, tmax[i], err, &c);
+        trace_ray<ANY, BOUNDS, true, TRI>(s, o, d, tmax[i], err, &c);
     }
     unsigned long long a = c.nodes, b = c.slots, t = c.tris;
     for (int off = 16; off > 0; off >>= 1) {
@@ -460,14 +475,10 @@ gpugi_status launch_trace_stats(gpugi_ctx* ctx, const gpugi_scene* sc, const flo
     if (n == 0) return GPUGI_OK;
     const unsigned grid = (unsigned)((n + 255) / 256);
     const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    if (!ell && !anyHit)
-        k_trace_stats<0, false><<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
-    else if (!ell)
-        k_trace_stats<0, true><<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
-    else if (!anyHit)
-        k_trace_stats<1, false><<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
-    else
-        k_trace_stats<1, true><<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
+    auto k = pick_variant(anyHit != 0, ell, sc->dev.triangleTest != 0, [](auto A, auto B, auto T) {
+        return &k_trace_stats<decltype(B)::value, decltype(A)::value, decltype(T)::value>;
+    });
+    k<<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }
@@ -484,12 +495,10 @@ gpugi_status launch_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const f
     if (ctx->traceMode == 1)
         return launch_trace_persistent(ctx, sc, false, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, nullptr);
     const uint32_t block = ctx->traceBlock;
-    if (sc->dev.boundsKind == GPUGI_BOUNDS_AABB)
-        k_trace_closest<0><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
-                                                                           slot, t, u, v, ctx->errWord);
-    else
-        k_trace_closest<1><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
-                                                                           slot, t, u, v, ctx->errWord);
+    auto k = pick_variant(false, sc->dev.boundsKind != GPUGI_BOUNDS_AABB, sc->dev.triangleTest != 0,
+                          [](auto, auto B, auto T) { return &k_trace_closest<decltype(B)::value, decltype(T)::value>; });
+    k<<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v,
+                                                     ctx->errWord);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }
@@ -506,12 +515,10 @@ gpugi_status launch_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float
         return launch_trace_persistent(ctx, sc, true, ox, oy, oz, dx, dy, dz, tmax, n, nullptr, nullptr, nullptr,
                                        nullptr, occluded);
     const uint32_t block = ctx->traceBlock;
-    if (sc->dev.boundsKind == GPUGI_BOUNDS_AABB)
-        k_trace_any<0><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
-                                                                       occluded, ctx->errWord);
-    else
-        k_trace_any<1><<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n,
-                                                                       occluded, ctx->errWord);
+    auto k = pick_variant(true, sc->dev.boundsKind != GPUGI_BOUNDS_AABB, sc->dev.triangleTest != 0,
+                          [](auto, auto B, auto T) { return &k_trace_any<decltype(B)::value, decltype(T)::value>; });
+    k<<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, occluded,
+                                                     ctx->errWord);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }

@@ -15,7 +15,16 @@
 namespace gpugi {
 
 // IntersectBox (intersectiontests.glsl:9-20). min/max are IEEE minNum/maxNum
-// (fminf/fmaxf): an axis-parallel ray produces inf*0 = NaN slabs that drop out.
+// (fminf/fmaxf): an axis-parallel ray produces inf*0 = NaN slabs that drop out
+// (a ray lying in a face plane of the box then misses it).
+// ROBUST is the box test of the watertight mode (an addition): a slab of a
+// ray that lies in one of its bounding planes (a NaN slab value) does not
+// constrain the ray, and the exit distance is widened by 1 + 2 gamma(3),
+// rounded up to 1 + 2^-21 (Ize, "Robust BVH Ray Traversal", JCGT 2(2),
+// 2013), so that rounding never culls a box whose surface the ray touches:
+// a ray through a vertex or edge on the box boundary still reaches the
+// triangles there.
+template <bool ROBUST = false>
 GPUGI_D bool intersect_box(float3 o, float3 inv, float4 lo, float4 hi, float& firstHit) {
     float tbx = X::mul(inv.x, X::sub(lo.x, o.x)), tby = X::mul(inv.y, X::sub(lo.y, o.y)),
           tbz = X::mul(inv.z, X::sub(lo.z, o.z));
@@ -23,10 +32,17 @@ GPUGI_D bool intersect_box(float3 o, float3 inv, float4 lo, float4 hi, float& fi
           ttz = X::mul(inv.z, X::sub(hi.z, o.z));
     float mnx = fminf(ttx, tbx), mny = fminf(tty, tby), mnz = fminf(ttz, tbz);
     float mxx = fmaxf(ttx, tbx), mxy = fmaxf(tty, tby), mxz = fmaxf(ttz, tbz);
+    if (ROBUST) {
+        const float inf = __int_as_float(0x7f800000);
+        if (isnan(tbx) || isnan(ttx)) mnx = -inf, mxx = inf;
+        if (isnan(tby) || isnan(tty)) mny = -inf, mxy = inf;
+        if (isnan(tbz) || isnan(ttz)) mnz = -inf, mxz = inf;
+    }
     float t0 = fmaxf(mnx, mny), t1 = fmaxf(mnx, mnz);
     firstHit = fmaxf(0.0f, fmaxf(t0, t1));
     float l0 = fminf(mxx, mxy), l1 = fminf(mxx, mxz);
     float lastHit = fminf(l0, l1);
+    if (ROBUST) lastHit = X::mul(lastHit, 0x1.000008p+0f);
     return firstHit <= lastHit;
 }
 
@@ -77,6 +93,86 @@ GPUGI_D bool intersect_triangle(float3 o, float3 d, const float4* rec, float& hi
     return intersect_triangle_v(o, d, __ldg(rec), __ldg(rec + 1), __ldg(rec + 2), hit, by, bz);
 }
 
+// Watertight ray/triangle test (an addition; the reference's test above is
+// not watertight): Woop, Benthin and Wald, "Watertight Ray/Triangle
+// Intersection", JCGT 2(1), 2013. Per ray, the axis kz of the largest
+// |direction| component becomes the ray's z axis (kx, ky follow cyclically,
+// swapped when d[kz] < 0 to keep the winding) and the shear
+// S = (d[kx] / d[kz], d[ky] / d[kz], 1 / d[kz]) maps the ray onto +z. Per
+// triangle, the vertices relative to the origin are sheared into that frame
+// and the three 2D edge functions U, V, W are evaluated; an edge function
+// that comes out exactly 0 is evaluated again in double precision (products
+// of two floats are exact there), so rays through shared edges and vertices
+// of a closed mesh see consistent signs and never slip through. Two-sided:
+// U, V, W must not have mixed signs and det = U + V + W must not be 0; then
+// t = T / det with T = U Az + V Bz + W Cz. The hit rule of the reference
+// test is kept: t > 1e-4 (INTERSECT_EPSILON), and the walk accepts
+// t < rayLength. Barycentrics (u, v) = (V, W) / det, the weights of p1 and
+// p2 as in gpugi's convention. Records hold the exact vertices
+// {p0.xyz p1.x | p1.yz p2.xy | p2.z 0 0 0} (48 B, like the reference records).
+struct WtRay {
+    float Sx, Sy, Sz;
+    uint32_t kx, ky, kz;
+};
+GPUGI_D float comp3(float3 v, uint32_t k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+GPUGI_D WtRay wt_setup(float3 d) {
+    WtRay w;
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    w.kz = ax >= ay ? (ax >= az ? 0u : 2u) : (ay >= az ? 1u : 2u);
+    w.kx = w.kz == 2u ? 0u : w.kz + 1u;
+    w.ky = w.kx == 2u ? 0u : w.kx + 1u;
+    const float dz = comp3(d, w.kz);
+    if (dz < 0.0f) {
+        const uint32_t t = w.kx;
+        w.kx = w.ky;
+        w.ky = t;
+    }
+    w.Sx = X::div(comp3(d, w.kx), dz);
+    w.Sy = X::div(comp3(d, w.ky), dz);
+    w.Sz = X::rcp(dz);
+    return w;
+}
+GPUGI_D float wt_edge(float ax, float ay, float bx, float by) {  // ax * by - ay * bx
+    return X::sub(X::mul(ax, by), X::mul(ay, bx));
+}
+GPUGI_D float wt_edge64(float ax, float ay, float bx, float by) {
+    return __double2float_rn(__dsub_rn(__dmul_rn((double)ax, (double)by), __dmul_rn((double)ay, (double)bx)));
+}
+GPUGI_D bool intersect_triangle_wt_v(float3 o, const WtRay& w, float4 ra, float4 rb, float4 rc, float& hit,
+                                     float& by, float& bz) {
+    const float3 A = X::sub3(make_float3(ra.x, ra.y, ra.z), o);
+    const float3 B = X::sub3(make_float3(ra.w, rb.x, rb.y), o);
+    const float3 C = X::sub3(make_float3(rb.z, rb.w, rc.x), o);
+    const float Akz = comp3(A, w.kz), Bkz = comp3(B, w.kz), Ckz = comp3(C, w.kz);
+    const float Ax = X::sub(comp3(A, w.kx), X::mul(w.Sx, Akz)), Ay = X::sub(comp3(A, w.ky), X::mul(w.Sy, Akz));
+    const float Bx = X::sub(comp3(B, w.kx), X::mul(w.Sx, Bkz)), By = X::sub(comp3(B, w.ky), X::mul(w.Sy, Bkz));
+    const float Cx = X::sub(comp3(C, w.kx), X::mul(w.Sx, Ckz)), Cy = X::sub(comp3(C, w.ky), X::mul(w.Sy, Ckz));
+    float U = wt_edge(Cx, Cy, Bx, By), V = wt_edge(Ax, Ay, Cx, Cy), W = wt_edge(Bx, By, Ax, Ay);
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = wt_edge64(Cx, Cy, Bx, By);
+        V = wt_edge64(Ax, Ay, Cx, Cy);
+        W = wt_edge64(Bx, By, Ax, Ay);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = X::add(X::add(U, V), W);
+    if (det == 0.0f) return false;
+    const float T = X::add(X::add(X::mul(U, X::mul(w.Sz, Akz)), X::mul(V, X::mul(w.Sz, Bkz))),
+                           X::mul(W, X::mul(w.Sz, Ckz)));
+    const float rcpDet = X::rcp(det);
+    hit = X::mul(T, rcpDet);
+    by = X::mul(V, rcpDet);
+    bz = X::mul(W, rcpDet);
+    return hit > 0.0001f;
+}
+// The triangle test of a leaf slot: TRI 0 = the reference's, 1 = watertight.
+template <int TRI>
+GPUGI_D bool slot_test(const DevScene& s, float3 o, float3 d, const WtRay& w, uint32_t k, float& hit, float& by,
+                       float& bz) {
+    if (TRI == 0) return intersect_triangle(o, d, s.tris + 3 * (size_t)k, hit, by, bz);
+    const float4* rec = s.wtris + 3 * (size_t)k;
+    return intersect_triangle_wt_v(o, w, __ldg(rec), __ldg(rec + 1), __ldg(rec + 2), hit, by, bz);
+}
+
 struct TraceResult {
     int32_t slot;  // -1 = miss
     float t;
@@ -96,13 +192,14 @@ struct WalkCounters {
 // strictly increases the node index, so numNodes visits always suffice; the
 // cap only guards against device memory corruption and reports
 // DEVERR_TRAVERSAL_CAP instead of spinning.
-template <bool ANY_HIT, int BOUNDS, bool COUNT = false>
+template <bool ANY_HIT, int BOUNDS, bool COUNT = false, int TRI = 0>
 GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLength, uint32_t* errWord,
                               WalkCounters* cnt = nullptr) {
     TraceResult r;
     r.slot = -1;
     r.u = r.v = 0.0f;
     const float3 inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
+    const WtRay wt = TRI ? wt_setup(d) : WtRay{};
     uint32_t node = 0;
     uint32_t budget = s.numNodes;
     const float4* __restrict__ nodes = s.nodes;
@@ -118,7 +215,7 @@ GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLe
         const uint32_t escape = __float_as_uint(b.w);
         float firstHit;
         bool hit;
-        if (BOUNDS == 0) hit = intersect_box(o, inv, a, b, firstHit);
+        if (BOUNDS == 0) hit = intersect_box<TRI != 0>(o, inv, a, b, firstHit);
         else hit = intersect_ellipsoid(o, d, a, b, firstHit);
         if (hit && firstHit <= rayLength) {
             if (child & LEAF_FLAG) {
@@ -128,7 +225,7 @@ GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLe
                 for (uint32_t k = 0; k < count; ++k) {
                     if (COUNT) ++cnt->tris;
                     float h, by, bz;
-                    if (intersect_triangle(o, d, s.tris + 3 * (size_t)(slot0 + k), h, by, bz) && h < rayLength) {
+                    if (slot_test<TRI>(s, o, d, wt, slot0 + k, h, by, bz) && h < rayLength) {
                         rayLength = h;
                         r.slot = (int32_t)(slot0 + k);
                         r.u = by;
@@ -163,6 +260,7 @@ GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLe
 // steps and leaf loops of different lengths.)
 struct WalkState {
     float3 o, d, inv;
+    WtRay wt;  // used by the watertight test only
     float len;
     uint32_t node;  // next node to test, NODE_DONE when the escape chain ended
     uint32_t cur, end;  // leaf slots still to test
@@ -176,6 +274,7 @@ GPUGI_D void walk_begin(WalkState& w, const DevScene& s, float3 o, float3 d, flo
     w.o = o;
     w.d = d;
     w.inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
+    w.wt = wt_setup(d);  // dead code unless a watertight walker reads it
     w.len = tmax;
     w.node = 0;
     w.cur = w.end = 0;
@@ -196,7 +295,7 @@ GPUGI_D void stage_top_nodes(const DevScene& s, float4* smem, uint32_t count) {
 // Node and triangle steps share one fetch (the record address depends on the
 // step kind), so the lanes of a warp that are at different kinds of step
 // wait for one memory round trip per step instead of one per kind.
-template <bool ANY_HIT, int BOUNDS>
+template <bool ANY_HIT, int BOUNDS, int TRI = 0>
 GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord, const float4* top = nullptr,
                        uint32_t topCount = 0) {
     const bool isTri = w.cur < w.end;
@@ -210,14 +309,16 @@ GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord, const
         a = top[2 * w.node];
         b = top[2 * w.node + 1];
     } else {
-        const float4* src = isTri ? s.tris + 3 * (size_t)w.cur : s.nodes + 2 * (size_t)w.node;
+        const float4* src = isTri ? (TRI ? s.wtris : s.tris) + 3 * (size_t)w.cur : s.nodes + 2 * (size_t)w.node;
         a = __ldg(src);
         b = __ldg(src + 1);
         if (isTri) c = __ldg(src + 2);
     }
     if (isTri) {
         float h, by, bz;
-        if (intersect_triangle_v(w.o, w.d, a, b, c, h, by, bz) && h < w.len) {
+        const bool ok = TRI ? intersect_triangle_wt_v(w.o, w.wt, a, b, c, h, by, bz)
+                            : intersect_triangle_v(w.o, w.d, a, b, c, h, by, bz);
+        if (ok && h < w.len) {
             w.len = h;
             w.slot = (int32_t)w.cur;
             w.u = by;
@@ -230,7 +331,7 @@ GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord, const
         const uint32_t escape = __float_as_uint(b.w);
         float firstHit;
         bool hit;
-        if (BOUNDS == 0) hit = intersect_box(w.o, w.inv, a, b, firstHit);
+        if (BOUNDS == 0) hit = intersect_box<TRI != 0>(w.o, w.inv, a, b, firstHit);
         else hit = intersect_ellipsoid(w.o, w.d, a, b, firstHit);
         if (hit && firstHit <= w.len) {
             if (child & LEAF_FLAG) {
@@ -263,6 +364,7 @@ GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord, const
 // breadth-first top-level layout): they simply end the round.
 struct GroupWalk {
     float3 o, d, inv;
+    WtRay wt;  // used by the watertight test only
     float len, u, v;
     int32_t slot;
     uint32_t node, cur, end, resume, budget;
@@ -273,6 +375,7 @@ GPUGI_D void group_begin(GroupWalk& g, const DevScene& s, float3 o, float3 d, fl
     g.o = o;
     g.d = d;
     g.inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
+    g.wt = wt_setup(d);  // dead code unless a watertight walker reads it
     g.len = tmax;
     g.u = g.v = 0.0f;
     g.slot = -1;
@@ -284,7 +387,7 @@ GPUGI_D void group_begin(GroupWalk& g, const DevScene& s, float3 o, float3 d, fl
 
 // One round; returns true when the walk is over. gl = lane in the group,
 // gbase = first lane of the group, gmask = the group's lanes.
-template <bool ANY_HIT, int BOUNDS, int G>
+template <bool ANY_HIT, int BOUNDS, int G, int TRI = 0>
 GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned gl, unsigned gbase,
                         unsigned gmask) {
     static_assert(G == 4 || G == 8 || G == 16, "group size");
@@ -292,7 +395,7 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
         const uint32_t k = g.cur + gl;
         float h = 0.0f, by = 0.0f, bz = 0.0f;
         bool ok = false;
-        if (k < g.end) ok = intersect_triangle(g.o, g.d, s.tris + 3 * (size_t)k, h, by, bz) && h < g.len;
+        if (k < g.end) ok = slot_test<TRI>(s, g.o, g.d, g.wt, k, h, by, bz) && h < g.len;
         if (ANY_HIT) {
             const uint32_t key = __reduce_min_sync(gmask, ok ? k : kGroupDone);
             if (key != kGroupDone) {
@@ -332,7 +435,7 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
         escape = __float_as_uint(b.w);
         float firstHit;
         bool hit;
-        if (BOUNDS == 0) hit = intersect_box(g.o, g.inv, a, b, firstHit);
+        if (BOUNDS == 0) hit = intersect_box<TRI != 0>(g.o, g.inv, a, b, firstHit);
         else hit = intersect_ellipsoid(g.o, g.d, a, b, firstHit);
         if (hit && firstHit <= g.len) next = (child & LEAF_FLAG) ? (kGroupLeaf | gl) : child;
         else next = escape ? escape : kGroupDone;
@@ -368,7 +471,7 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
 // group's first lane. With MULTI the rays belong to different scenes: load
 // returns the item's scene and its bounds kind selects the node test per
 // round; otherwise every ray walks `scene` with the BOUNDS test.
-template <bool ANY_HIT, int BOUNDS, int G, bool MULTI, typename Load, typename Finish>
+template <bool ANY_HIT, int BOUNDS, int G, bool MULTI, int TRI, typename Load, typename Finish>
 GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long long* work, uint32_t* err, Load load,
                               Finish finish) {
     // The loop has no warp-wide synchronisation: all shuffles stay inside
@@ -400,7 +503,7 @@ GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long l
                            ? group_step<ANY_HIT, 1, G>(g, *sc, err, gl, gbase, gmask)
                            : group_step<ANY_HIT, 0, G>(g, *sc, err, gl, gbase, gmask);
             else
-                done = group_step<ANY_HIT, BOUNDS, G>(g, scene, err, gl, gbase, gmask);
+                done = group_step<ANY_HIT, BOUNDS, G, TRI>(g, scene, err, gl, gbase, gmask);
         }
         if (gl == 0) finish(my, g);
         unsigned long long next = 0;
@@ -409,15 +512,15 @@ GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long l
     }
 }
 
-template <bool ANY_HIT, int BOUNDS, int G, typename Load, typename Finish>
+template <bool ANY_HIT, int BOUNDS, int G, int TRI = 0, typename Load, typename Finish>
 GPUGI_D void group_walks(const DevScene& scene, uint64_t n, unsigned long long* work, uint32_t* err, Load load,
                          Finish finish) {
-    group_walks_impl<ANY_HIT, BOUNDS, G, false>(scene, n, work, err, load, finish);
+    group_walks_impl<ANY_HIT, BOUNDS, G, false, TRI>(scene, n, work, err, load, finish);
 }
 
 template <bool ANY_HIT, int G, typename Load, typename Finish>
 GPUGI_D void group_walks_multi(uint64_t n, unsigned long long* work, uint32_t* err, Load load, Finish finish) {
-    group_walks_impl<ANY_HIT, 0, G, true>(DevScene{}, n, work, err, load, finish);
+    group_walks_impl<ANY_HIT, 0, G, true, 0>(DevScene{}, n, work, err, load, finish);
 }
 
 }  // namespace gpugi

@@ -55,6 +55,7 @@ def _declare(L):
     L.gpugi_scene_build.argtypes = [P, P, U32, P, U32, P, P, U32, U32, C.POINTER(P)]
     L.gpugi_scene_export.argtypes = [P, P, C.POINTER(U32), C.POINTER(U32), P, P]
     L.gpugi_scene_set_hierarchy_ndf.argtypes = [P, P, P]
+    L.gpugi_scene_set_triangle_test.argtypes = [P, P, U32]
     L.gpugi_hierarchy_importance.argtypes = [P, P, P, U32, U32, P, U32, U32]
     L.gpugi_hierarchy_read.argtypes = [P, P, P, P, P]
     for name in ("gpugi_trace_closest", "gpugi_trace_closest_device"):
@@ -234,6 +235,11 @@ class DeviceScene:
         parents[hier[left, 7].view(np.uint32)] = inner
         return B.BVH(hierarchy=hier, slots=slots, parents=parents, leaf_size=self.leaf_size, bounds_kind=0,
                      max_depth=0)
+
+    def set_triangle_test(self, watertight: bool) -> None:
+        """Triangle test of the ray queries on this scene: the reference's
+        (False) or the watertight test (True), gpugi_scene_set_triangle_test."""
+        self.ctx.check(lib().gpugi_scene_set_triangle_test(self.ctx.handle, self._h, 1 if watertight else 0))
 
     def set_hierarchy_ndf(self, sggx: np.ndarray) -> None:
         """Node NDFs (uint16 [numNodes, 6], bvhmake's approx_sggx in the

@@ -229,6 +229,38 @@ def displaced_icosphere(num_triangles: int = 65536, seed: int = 1, amplitude: fl
     return _pack(v, f, [lambert((0.5, 0.5, 0.5))], normals=n)
 
 
+def closed_icosphere(level: int = 4, seed: int = 1, amplitude: float = 0.05):
+    """A closed mesh: a level-`level` icosphere whose shared vertices are moved
+    radially by uniform[-amplitude, amplitude], scaled into the unit cube and
+    centred at (0.5, 0.5, 0.5) (star-shaped around the centre, so every ray
+    from the centre must hit it)."""
+    v, f = icosphere(level)
+    rs = Stream(seed, 3)
+    n = v.copy()
+    v = v * (1.0 + rs.uniform(v.shape[0], -amplitude, amplitude))[:, None]
+    lo, hi = v.min(0), v.max(0)
+    v = (v - (lo + hi) * 0.5) / (hi - lo).max() + 0.5
+    return _pack(v, f, [lambert((0.5, 0.5, 0.5))], normals=n)
+
+
+def crack_rays(scene: dict, origin=(0.5, 0.5, 0.5)) -> dict:
+    """Rays from `origin` through every vertex and every edge midpoint of a
+    mesh: the rays a test that is not watertight can let slip between the
+    triangles sharing that vertex or edge."""
+    v = np.asarray(scene["positions"], np.float64)
+    f = np.asarray(scene["triangles"])[:, :3].astype(np.int64)
+    e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+    e = np.unique(np.sort(e, axis=1), axis=0)
+    targets = np.concatenate([v, 0.5 * (v[e[:, 0]] + v[e[:, 1]])])
+    d = targets - np.asarray(origin, np.float64)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    n = d.shape[0]
+    o = np.asarray(origin, np.float32)
+    return {"ox": np.full(n, o[0], np.float32), "oy": np.full(n, o[1], np.float32), "oz": np.full(n, o[2], np.float32),
+            "dx": d[:, 0].astype(np.float32), "dy": d[:, 1].astype(np.float32), "dz": d[:, 2].astype(np.float32),
+            "tmax": np.full(n, np.inf, np.float32)}
+
+
 def aimed_rays(n: int, positions: np.ndarray, seed: int = 1, spread: float = 1.5, tmax: float = math.inf):
     """Rays from a box `spread` times the object's bounding box, each aimed at
     a uniform point of the object's bounding box (most of them hit)."""

@@ -127,6 +127,23 @@ gpugi_status gpugi_scene_build(gpugi_ctx* ctx, const float* positions, uint32_t 
 gpugi_status gpugi_scene_export(gpugi_ctx* ctx, const gpugi_scene* scene, uint32_t* numNodes, uint32_t* numSlots,
                                 float* hierarchy, int32_t* slots);
 
+/* Triangle test of the ray queries on a scene (gpugi_trace_closest / _any,
+ * their _device forms, gpugi_trace_closest_noalloc and gpugi_trace_stats_device).
+ *   GPUGI_TRIANGLE_REFERENCE   the reference's IntersectTriangle (OptiX-style
+ *                              Moeller-Trumbore, gpugi/shader/intersectiontests.glsl:63-79;
+ *                              the default): not watertight, a ray through a
+ *                              shared edge or vertex can miss both triangles
+ *   GPUGI_TRIANGLE_WATERTIGHT  an addition: the watertight test of Woop, Benthin
+ *                              and Wald (JCGT 2013) with the reference's hit
+ *                              rule (t > 1e-4, accepted when t < rayLength)
+ *                              and barycentrics; the first switch builds its
+ *                              48-B vertex records on the device (synchronous)
+ * The walk, its order and the acceptance rule are the same in both. The
+ * rendering passes always use the reference test. */
+#define GPUGI_TRIANGLE_REFERENCE 0u
+#define GPUGI_TRIANGLE_WATERTIGHT 1u
+gpugi_status gpugi_scene_set_triangle_test(gpugi_ctx* ctx, gpugi_scene* scene, uint32_t test);
+
 /* Closest hit for n rays in SoA layout. tmax is the initial rayLength
  * (gpugi uses RAY_MAX = 3.402823466e38, stdheader.glsl:6). Outputs per ray:
  * slot = leaf slot index of the hit triangle or -1, t = final rayLength,

@@ -56,7 +56,17 @@ def _rays(rays):
     return [np.ascontiguousarray(rays[k], dtype=np.float32) for k in ("ox", "oy", "oz", "dx", "dy", "dz", "tmax")]
 
 
-def trace_closest(bvh, positions, rays, counters=False, num_threads=None):
+def set_triangle_test(watertight: bool) -> None:
+    """Triangle test of the following query calls: the reference's
+    IntersectTriangle or the watertight test."""
+    L = lib()
+    L.oracle_set_triangle_test.argtypes = [C.c_int]
+    L.oracle_set_triangle_test.restype = None
+    L.oracle_set_triangle_test(1 if watertight else 0)
+
+
+def trace_closest(bvh, positions, rays, counters=False, num_threads=None, watertight=False):
+    set_triangle_test(watertight)
     keep, sargs = _scene_args(bvh, positions)
     r = _rays(rays)
     n = r[0].shape[0]
@@ -73,7 +83,8 @@ def trace_closest(bvh, positions, rays, counters=False, num_threads=None):
     return out
 
 
-def trace_any(bvh, positions, rays, counters=False, num_threads=None):
+def trace_any(bvh, positions, rays, counters=False, num_threads=None, watertight=False):
+    set_triangle_test(watertight)
     keep, sargs = _scene_args(bvh, positions)
     r = _rays(rays)
     n = r[0].shape[0]
@@ -87,7 +98,8 @@ def trace_any(bvh, positions, rays, counters=False, num_threads=None):
     return out
 
 
-def bruteforce_closest(slots, positions, rays, num_threads=None):
+def bruteforce_closest(slots, positions, rays, num_threads=None, watertight=False):
+    set_triangle_test(watertight)
     slots = np.ascontiguousarray(slots, dtype=np.int32)
     pos = np.ascontiguousarray(positions, dtype=np.float32)
     r = _rays(rays)

@@ -28,6 +28,7 @@ struct Scene {
     uint32_t numVertices = 0;
     const glsl::vec4* vertexInfo = nullptr;
     uint32_t boundsKind = BOUNDS_AABB;
+    uint32_t triangleTest = 0;  // 0: IntersectTriangle as the reference writes it, 1: watertight
 };
 
 struct Ray {

@@ -33,6 +33,26 @@ static bool IntersectBox(vec3 rayOrigin, vec3 invRayDir, vec3 aabbMin, vec3 aabb
     return firstHit <= lastHit;
 }
 
+// The box test of the watertight mode (the library's addition): IntersectBox
+// where a slab with a NaN value (the ray lies in one of its planes) does not
+// constrain the ray, and the exit distance is widened by 1 + 2 gamma(3)
+// rounded up to 1 + 2^-21 (Ize, "Robust BVH Ray Traversal", JCGT 2013).
+static bool IntersectBoxRobust(vec3 rayOrigin, vec3 invRayDir, vec3 aabbMin, vec3 aabbMax, float& firstHit) {
+    vec3 tbot = invRayDir * (aabbMin - rayOrigin);
+    vec3 ttop = invRayDir * (aabbMax - rayOrigin);
+    vec3 tmin = min(ttop, tbot);
+    vec3 tmax = max(ttop, tbot);
+    const float inf = std::numeric_limits<float>::infinity();
+    for (int k = 0; k < 3; ++k)
+        if (std::isnan(tbot[k]) || std::isnan(ttop[k])) {
+            tmin[k] = -inf;
+            tmax[k] = inf;
+        }
+    firstHit = max(0.0f, max(max(tmin.x, tmin.y), max(tmin.x, tmin.z)));
+    float lastHit = min(min(tmax.x, tmax.y), min(tmax.x, tmax.z));
+    return firstHit <= lastHit * 0x1.000008p+0f;
+}
+
 // Ray against a stored axis-aligned ellipsoid {center, radii} (bvhmake's
 // "bounding_ellipsoid" chunk, bvhmake/bvhbuilder.cpp:586-588). The reference
 // never traverses ellipsoids (its IntersectVirtualEllipsoid,
@@ -77,6 +97,67 @@ static bool IntersectTriangle(const Ray& ray, vec3 p0, vec3 p1, vec3 p2, float& 
     return (hit > INTERSECT_EPSILON) && all_ge0(barycentricCoord);
 }
 
+// Watertight test (an addition of the library, not in the reference):
+// Woop, Benthin and Wald, "Watertight Ray/Triangle Intersection", JCGT 2(1),
+// 2013, section 3 and its pseudocode, two-sided, with the reference's hit
+// rule t > INTERSECT_EPSILON and its barycentric convention (y, z = the
+// weights of p1, p2). kz is the axis of the largest |d| component (x, then
+// y, then z on ties); an edge function that is exactly 0 in float is
+// recomputed in double from the same float operands.
+struct WatertightRay {
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+static WatertightRay WatertightSetup(vec3 d) {
+    WatertightRay w;
+    float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    w.kz = ax >= ay ? (ax >= az ? 0 : 2) : (ay >= az ? 1 : 2);
+    w.kx = (w.kz + 1) % 3;
+    w.ky = (w.kx + 1) % 3;
+    if (d[w.kz] < 0.0f) {
+        int t = w.kx;
+        w.kx = w.ky;
+        w.ky = t;
+    }
+    w.Sx = d[w.kx] / d[w.kz];
+    w.Sy = d[w.ky] / d[w.kz];
+    w.Sz = 1.0f / d[w.kz];
+    return w;
+}
+static bool IntersectTriangleWatertight(const Ray& ray, const WatertightRay& w, vec3 p0, vec3 p1, vec3 p2,
+                                        float& hit, vec3& barycentricCoord) {
+    const vec3 A = p0 - ray.Origin;
+    const vec3 B = p1 - ray.Origin;
+    const vec3 C = p2 - ray.Origin;
+    const float Ax = A[w.kx] - w.Sx * A[w.kz];
+    const float Ay = A[w.ky] - w.Sy * A[w.kz];
+    const float Bx = B[w.kx] - w.Sx * B[w.kz];
+    const float By = B[w.ky] - w.Sy * B[w.kz];
+    const float Cx = C[w.kx] - w.Sx * C[w.kz];
+    const float Cy = C[w.ky] - w.Sy * C[w.kz];
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = U + V + W;
+    if (det == 0.0f) return false;
+    const float Az = w.Sz * A[w.kz];
+    const float Bz = w.Sz * B[w.kz];
+    const float Cz = w.Sz * C[w.kz];
+    const float T = U * Az + V * Bz + W * Cz;
+    const float rcpDet = 1.0f / det;
+    hit = T * rcpDet;
+    barycentricCoord.y = V * rcpDet;
+    barycentricCoord.z = W * rcpDet;
+    barycentricCoord.x = 1.0f - (barycentricCoord.z + barycentricCoord.y);
+    return hit > INTERSECT_EPSILON;
+}
+
 static inline vec3 Position(const Scene& s, int32_t idx) {
     const float* p = s.positions + 3 * (int64_t)idx;
     return vec3(p[0], p[1], p[2]);
@@ -91,6 +172,7 @@ static inline bool FetchIntersectNode(const Scene& s, const Ray& ray, vec3 invRa
     escape = floatBitsToInt(b.w);
     if (s.boundsKind == BOUNDS_ELLIPSOID) return IntersectEllipsoid(ray, a.xyz(), b.xyz(), newHit);
     float exitDist;
+    if (s.triangleTest) return IntersectBoxRobust(ray.Origin, invRayDir, a.xyz(), b.xyz(), newHit);
     return IntersectBox(ray.Origin, invRayDir, a.xyz(), b.xyz(), newHit, exitDist);
 }
 
@@ -103,6 +185,7 @@ static bool TraceImpl(const Scene& s, const Ray& ray, float& rayLength, HitRecor
     int currentNodeIndex = 0;
     int currentLeafIndex = 0;
     vec3 invRayDir = 1.0f / ray.Direction;
+    const WatertightRay wt = WatertightSetup(ray.Direction);
     bool nextIsLeafNode = false;
     if (s.numNodes == 0) return false;
     // Iteration guard: a well-formed escape tree visits every node at most
@@ -138,8 +221,11 @@ static bool TraceImpl(const Scene& s, const Ray& ray, float& rayLength, HitRecor
                 vec3 p0 = Position(s, triangle.x), p1 = Position(s, triangle.y), p2 = Position(s, triangle.z);
                 vec3 newTriangleNormal, newBarycentricCoord;
                 float newHit;
-                if (IntersectTriangle(ray, p0, p1, p2, newHit, newBarycentricCoord, newTriangleNormal) &&
-                    newHit < rayLength) {
+                const bool isHit = s.triangleTest
+                                       ? IntersectTriangleWatertight(ray, wt, p0, p1, p2, newHit, newBarycentricCoord)
+                                       : IntersectTriangle(ray, p0, p1, p2, newHit, newBarycentricCoord,
+                                                           newTriangleNormal);
+                if (isHit && newHit < rayLength) {
                     if (ANY_HIT) return true;
                     rayLength = newHit;
                     out->slot = currentLeafIndex;
@@ -190,6 +276,10 @@ bool TraceRayAnyHit(const Scene& s, const Ray& ray, float rayLength, TraceCounte
 // ---------------------------------------------------------------------------
 using namespace oracle;
 
+// Triangle test of the following query calls (0 reference, 1 watertight);
+// the oracle serves one caller at a time.
+static uint32_t g_triangleTest = 0;
+
 static Scene MakeScene(const float* hierarchy, uint32_t numNodes, uint32_t boundsKind,
                        const int32_t* slots, uint32_t numSlots, uint32_t leafSize,
                        const float* positions, uint32_t numVertices) {
@@ -202,10 +292,13 @@ static Scene MakeScene(const float* hierarchy, uint32_t numNodes, uint32_t bound
     s.leafSize = leafSize;
     s.positions = positions;
     s.numVertices = numVertices;
+    s.triangleTest = g_triangleTest;
     return s;
 }
 
 extern "C" {
+
+void oracle_set_triangle_test(int watertight) { g_triangleTest = watertight ? 1u : 0u; }
 
 // Closest-hit queries over SoA rays. Outputs per ray: slot (-1 = miss), t,
 // u = bary.y, v = bary.z, and optional fetch counters (3 uint32 per ray).
@@ -271,6 +364,7 @@ int oracle_bruteforce_closest(const int32_t* slots, uint32_t numSlots, const flo
     ParallelFor(n, numThreads, [&](uint64_t b, uint64_t e) {
         for (uint64_t i = b; i < e; ++i) {
             Ray r{vec3(ox[i], oy[i], oz[i]), vec3(dx[i], dy[i], dz[i])};
+            const WatertightRay wt = WatertightSetup(r.Direction);
             float len = tmax[i];
             int32_t best = -1;
             for (uint32_t k = 0; k < numSlots; ++k) {
@@ -278,8 +372,10 @@ int oracle_bruteforce_closest(const int32_t* slots, uint32_t numSlots, const flo
                 if (tri.x == tri.y) continue;
                 vec3 bc, nrm;
                 float h;
-                if (IntersectTriangle(r, Position(s, tri.x), Position(s, tri.y), Position(s, tri.z), h, bc, nrm) &&
-                    h < len) {
+                const vec3 p0 = Position(s, tri.x), p1 = Position(s, tri.y), p2 = Position(s, tri.z);
+                const bool isHit = s.triangleTest ? IntersectTriangleWatertight(r, wt, p0, p1, p2, h, bc)
+                                                  : IntersectTriangle(r, p0, p1, p2, h, bc, nrm);
+                if (isHit && h < len) {
                     len = h;
                     best = (int32_t)k;
                 }

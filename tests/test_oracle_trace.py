@@ -96,3 +96,41 @@ def test_triangle_known_answers(built):
         if c["walk_hit"]:
             assert o["t"][0] == np.float32(c["t"]), c["name"]
             assert o["u"][0] == np.float32(c["u"]) and o["v"][0] == np.float32(c["v"]), c["name"]
+
+
+def test_watertight_oracle_closes_cracks():
+    """The watertight restatement (Woop, Benthin and Wald 2013, with the robust
+    box test of Ize 2013) hits a closed mesh with every ray from its centre
+    through its vertices and edge midpoints, in the walk and by brute force;
+    the reference's Moeller-Trumbore test lets a share of them slip through
+    (it is not watertight, intersectiontests.glsl:55-79)."""
+    sc = scenes.closed_icosphere(4, seed=1)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    rays = scenes.crack_rays(sc)
+    wt = oracle.trace_closest(b, sc["positions"], rays, watertight=True)
+    assert (wt["slot"] >= 0).all()
+    assert (oracle.bruteforce_closest(b.slots, sc["positions"], rays, watertight=True)["slot"] >= 0).all()
+    assert oracle.trace_any(b, sc["positions"], rays, watertight=True)["occluded"].all()
+    ref = oracle.trace_closest(b, sc["positions"], rays)
+    assert (ref["slot"] < 0).sum() > 100
+
+
+def test_watertight_oracle_matches_bruteforce_and_reference_hits():
+    """Away from edges both tests find the same triangles: the walk equals brute
+    force in watertight mode, and its hits agree with the reference test's on
+    almost every random ray (t within a few ulp: the two tests round
+    differently)."""
+    sc = scenes.displaced_icosphere(4096, seed=3)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    rays = scenes.aimed_rays(20000, sc["positions"], seed=4)
+    wt = oracle.trace_closest(b, sc["positions"], rays, watertight=True)
+    bf = oracle.bruteforce_closest(b.slots, sc["positions"], rays, watertight=True)
+    assert (wt["t"].view(np.uint32) == bf["t"].view(np.uint32)).mean() > 0.999
+    ref = oracle.trace_closest(b, sc["positions"], rays)
+    assert (wt["slot"] == ref["slot"]).mean() > 0.995
+    both = (wt["slot"] >= 0) & (wt["slot"] == ref["slot"])
+    dt = np.abs(wt["t"][both].view(np.int32).astype(np.int64) - ref["t"][both].view(np.int32).astype(np.int64))
+    assert np.median(dt) <= 2
+    hit = wt["slot"] >= 0
+    assert np.allclose(wt["u"][both], ref["u"][both], atol=1e-4)
+    assert hit.mean() > 0.3
