@@ -1,0 +1,298 @@
+// ORACLE — test infrastructure only. Not part of the product.
+//
+// Glue around the reference's own shader text (rewritten by
+// oracle/ref_build.py into oracle/_ref/gen/, compiled against ref_shim.hpp):
+// it binds scene arrays to the shaders' buffers and exports C entry points
+// that tests/test_ref_pinned.py calls side by side with the oracle's.
+//   ref_trace_closest / ref_trace_any   TraceRay / TraceRayAnyHit
+//                                       (gpugi/shader/traceray.glsl with AABOX_BVH,
+//                                       intersectiontests.glsl), leaf blocks of 8 or 2
+//   ref_eval                            random.glsl / helper.glsl functions
+//   ref_render_pt                       pathtracer.comp's main() per pixel
+#include <cstdint>
+#include <thread>
+#include <vector>
+
+#include "ref_shim.hpp"
+
+namespace glslref {
+const vec4* g_textureColours = nullptr;
+thread_local uvec3 gl_GlobalInvocationID;
+}  // namespace glslref
+
+// ------------------------------------------------ traversal, 8-slot leaves
+namespace ref_leaf8 {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 8
+#define AABOX_BVH
+#include "helper.glsl.h"
+#include "scenedata.glsl.h"
+#include "intersectiontests.glsl.h"
+#include "random.glsl.h"
+#include "traceray.glsl.h"
+#define ANY_HIT
+#include "traceray.glsl.h"
+#undef ANY_HIT
+#undef TRIANGLES_PER_LEAF
+}  // namespace ref_leaf8
+
+// ------------------------------------------------ traversal, 2-slot leaves
+namespace ref_leaf2 {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 2
+#include "helper.glsl.h"
+#include "scenedata.glsl.h"
+#include "intersectiontests.glsl.h"
+#include "random.glsl.h"
+#include "traceray.glsl.h"
+#define ANY_HIT
+#include "traceray.glsl.h"
+#undef ANY_HIT
+#undef TRIANGLES_PER_LEAF
+}  // namespace ref_leaf2
+
+// ------------------------------------------------ the path tracer, 8-slot leaves
+namespace ref_pt {
+using namespace glslref;
+int g_maxPathLength = 8;  // MAX_PATHLENGTH, injected by the application (application.cpp:123)
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define main PathtracerMain
+#include "pathtracer.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_pt
+
+namespace {
+
+template <typename F>
+void parallel_for(uint64_t n, int threads, F fn) {
+    if (threads <= 0) threads = (int)std::thread::hardware_concurrency();
+    if (threads < 1) threads = 1;
+    if ((uint64_t)threads > n) threads = (int)(n ? n : 1);
+    std::vector<std::thread> pool;
+    const uint64_t chunk = (n + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) {
+        const uint64_t b = (uint64_t)t * chunk, e = b + chunk < n ? b + chunk : n;
+        if (b >= e) break;
+        pool.emplace_back([=]() { fn(b, e); });
+    }
+    for (auto& th : pool) th.join();
+}
+
+}  // namespace
+
+#define GPUGI_REF_BIND(NS)                                                         \
+    NS::HierachyBuffer = glslref::samplerBuffer{hierarchy, 4};                     \
+    NS::TriangleBuffer = glslref::isamplerBuffer{reinterpret_cast<const glslref::ivec4*>(slots)}; \
+    NS::VertexPositionBuffer = glslref::samplerBuffer{positions, 3};
+
+extern "C" {
+
+// Closest hit with the reference's TraceRay: the Triangle record it returns
+// ({v0, v1, v2, material}, all -1 on a miss), t, u = barycentric.y,
+// v = barycentric.z.
+int ref_trace_closest(const float* hierarchy, const int32_t* slots, const float* positions, int leafSize,
+                      const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
+                      const float* dz, const float* tmax, uint64_t n, int32_t* outTri, float* outT, float* outU,
+                      float* outV, int numThreads) {
+    using namespace glslref;
+    if (leafSize != 8 && leafSize != 2) return 1;
+    if (leafSize == 8) {
+        GPUGI_REF_BIND(ref_leaf8)
+    } else {
+        GPUGI_REF_BIND(ref_leaf2)
+    }
+    parallel_for(n, numThreads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i) {
+            ref_leaf8::Ray r8;
+            ref_leaf2::Ray r2;
+            r8.Origin = r2.Origin = vec3(ox[i], oy[i], oz[i]);
+            r8.Direction = r2.Direction = vec3(dx[i], dy[i], dz[i]);
+            float rayLength = tmax[i];
+            vec3 bary(-1.0f);
+            ivec4 tri(-1, -1, -1, -1);
+            if (leafSize == 8) ref_leaf8::TraceRay(r8, rayLength, bary, tri);
+            else ref_leaf2::TraceRay(r2, rayLength, bary, tri);
+            // the shader leaves its out parameters unwritten on a miss
+            const bool hit = rayLength < tmax[i];
+            outTri[4 * i] = hit ? tri.x : -1;
+            outTri[4 * i + 1] = hit ? tri.y : -1;
+            outTri[4 * i + 2] = hit ? tri.z : -1;
+            outTri[4 * i + 3] = hit ? tri.w : -1;
+            outT[i] = rayLength;
+            outU[i] = hit ? bary.y : 0.0f;
+            outV[i] = hit ? bary.z : 0.0f;
+        }
+    });
+    return 0;
+}
+
+int ref_trace_any(const float* hierarchy, const int32_t* slots, const float* positions, int leafSize,
+                  const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
+                  const float* dz, const float* tmax, uint64_t n, uint8_t* occluded, int numThreads) {
+    using namespace glslref;
+    if (leafSize != 8 && leafSize != 2) return 1;
+    if (leafSize == 8) {
+        GPUGI_REF_BIND(ref_leaf8)
+    } else {
+        GPUGI_REF_BIND(ref_leaf2)
+    }
+    parallel_for(n, numThreads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i) {
+            const vec3 o(ox[i], oy[i], oz[i]), d(dx[i], dy[i], dz[i]);
+            bool hit;
+            if (leafSize == 8) {
+                ref_leaf8::Ray r;
+                r.Origin = o;
+                r.Direction = d;
+                hit = ref_leaf8::TraceRayAnyHit(r, tmax[i]);
+            } else {
+                ref_leaf2::Ray r;
+                r.Origin = o;
+                r.Direction = d;
+                hit = ref_leaf2::TraceRayAnyHit(r, tmax[i]);
+            }
+            occluded[i] = hit ? 1 : 0;
+        }
+    });
+    return 0;
+}
+
+// Functions of random.glsl and helper.glsl over arrays (kind selects):
+//   0 wanghash(u)                        in: u32        out: u32
+//   1 RandomUInt x4 from seed u          in: u32        out: 4 u32 (the stream)
+//   2 Random x4 from seed u              in: u32        out: 4 floats
+//   3 InitRandomSeed(a, b)               in: 2 u32      out: u32
+//   4 SampleDirection(r)                 in: 2 floats   out: 3 floats
+//   5 SampleHemisphereCosine(r, ONB(n))  in: 5 floats   out: 3 floats (r, n)
+//   6 SamplePhongLobe(r, e, ONB(n))      in: 6 floats   out: 3 floats (r, e, n)
+//   7 CreateONB(n)                       in: 3 floats   out: 6 floats (U, V)
+//   8 UnpackNormal(vec2)                 in: 2 floats   out: 3 floats
+//   9 PackNormal(n)                      in: 3 floats   out: 2 floats
+//  10 GetLuminance(c)                    in: 3 floats   out: 1 float
+int ref_eval(int kind, uint64_t n, const void* in, void* out) {
+    using namespace ref_leaf8;
+    const uint32_t* iu = static_cast<const uint32_t*>(in);
+    const float* f = static_cast<const float*>(in);
+    uint32_t* ou = static_cast<uint32_t*>(out);
+    float* of = static_cast<float*>(out);
+    for (uint64_t i = 0; i < n; ++i) {
+        switch (kind) {
+        case 0: ou[i] = wanghash(iu[i]); break;
+        case 1: {
+            uint s = iu[i];
+            for (int k = 0; k < 4; ++k) ou[4 * i + k] = RandomUInt(s);
+            break;
+        }
+        case 2: {
+            uint s = iu[i];
+            for (int k = 0; k < 4; ++k) of[4 * i + k] = Random(s);
+            break;
+        }
+        case 3: ou[i] = InitRandomSeed(iu[2 * i], iu[2 * i + 1]); break;
+        case 4: {
+            vec3 d = SampleDirection(vec2(f[2 * i], f[2 * i + 1]));
+            of[3 * i] = d.x, of[3 * i + 1] = d.y, of[3 * i + 2] = d.z;
+            break;
+        }
+        case 5: {
+            const float* p = f + 5 * i;
+            vec3 N(p[2], p[3], p[4]), U, V;
+            CreateONB(N, U, V);
+            vec3 d = SampleHemisphereCosine(vec2(p[0], p[1]), U, V, N);
+            of[3 * i] = d.x, of[3 * i + 1] = d.y, of[3 * i + 2] = d.z;
+            break;
+        }
+        case 6: {
+            const float* p = f + 6 * i;
+            vec3 N(p[3], p[4], p[5]), U, V;
+            CreateONB(N, U, V);
+            vec3 d = SamplePhongLobe(vec2(p[0], p[1]), p[2], U, V, N);
+            of[3 * i] = d.x, of[3 * i + 1] = d.y, of[3 * i + 2] = d.z;
+            break;
+        }
+        case 7: {
+            vec3 N(f[3 * i], f[3 * i + 1], f[3 * i + 2]), U, V;
+            CreateONB(N, U, V);
+            of[6 * i] = U.x, of[6 * i + 1] = U.y, of[6 * i + 2] = U.z;
+            of[6 * i + 3] = V.x, of[6 * i + 4] = V.y, of[6 * i + 5] = V.z;
+            break;
+        }
+        case 8: {
+            vec3 d = UnpackNormal(vec2(f[2 * i], f[2 * i + 1]));
+            of[3 * i] = d.x, of[3 * i + 1] = d.y, of[3 * i + 2] = d.z;
+            break;
+        }
+        case 9: {
+            vec2 p = PackNormal(vec3(f[3 * i], f[3 * i + 1], f[3 * i + 2]));
+            of[2 * i] = p.x, of[2 * i + 1] = p.y;
+            break;
+        }
+        case 10: of[i] = GetLuminance(vec3(f[3 * i], f[3 * i + 1], f[3 * i + 2])); break;
+        default: return 1;
+        }
+    }
+    return 0;
+}
+
+// One iteration of pathtracer.comp over every pixel of a width x height
+// image (the reference dispatches whole 8x8 groups only; every pixel here),
+// accumulated into accum (RGBA32F). Scene arrays as oracle_render takes
+// them; materials: 24 floats per material (the library's record), turned
+// into the shader's Material UBO with one constant "texture" per map;
+// camera: U, V, W, position, pixelArea (13 floats); sky: the constant
+// environment radiance.
+int ref_render_pt(const float* hierarchy, const int32_t* slots, const float* positions, const float* vertexInfo,
+                  const float* materials, int numMaterials, int width, int height, int maxPathLength,
+                  const float* cam, uint32_t frameSeed, const float* lightSamples, int numLightSamples,
+                  const float* sky, float* accum, int numThreads) {
+    using namespace glslref;
+    if (numMaterials > 256) return 1;  // the shader's UBO holds 256 materials (globaluniforms.glsl:23-27)
+    namespace P = ref_pt;
+    P::HierachyBuffer = samplerBuffer{hierarchy, 4};
+    P::TriangleBuffer = isamplerBuffer{reinterpret_cast<const ivec4*>(slots)};
+    P::VertexPositionBuffer = samplerBuffer{positions, 3};
+    P::VertexInfoBuffer = samplerBuffer{vertexInfo, 4};
+    P::InitialLightSampleBuffer = samplerBuffer{lightSamples, 4};
+    std::vector<vec4> colours(4 * (size_t)numMaterials);
+    for (int m = 0; m < numMaterials; ++m) {
+        const float* r = materials + 24 * (size_t)m;
+        colours[4 * m + 0] = vec4(r[0], r[1], r[2], 1.0f);     // diffuse
+        colours[4 * m + 1] = vec4(r[4], r[5], r[6], 1.0f);     // opacity
+        colours[4 * m + 2] = vec4(r[8], r[9], r[10], r[11]);   // reflectiveness, w = Phong exponent
+        colours[4 * m + 3] = vec4(r[12], r[13], r[14], 1.0f);  // emissivity
+        P::Material& M = P::Materials[m];
+        M.diffuseTexHandle = uvec2(4 * m + 0, 0);
+        M.opacityTexHandle = uvec2(4 * m + 1, 0);
+        M.reflectivenessTexHandle = uvec2(4 * m + 2, 0);
+        M.emissivityTexHandle = uvec2(4 * m + 3, 0);
+        M.Fresnel0 = vec3(r[16], r[17], r[18]);
+        M.RefractionIndexAvg = r[3];
+        M.Fresnel1 = vec3(r[20], r[21], r[22]);
+    }
+    g_textureColours = colours.data();
+    P::BackbufferSize = ivec2(width, height);
+    P::NumInitialLightSamples = numLightSamples;
+    P::CameraU = vec3(cam[0], cam[1], cam[2]);
+    P::CameraV = vec3(cam[3], cam[4], cam[5]);
+    P::CameraW = vec3(cam[6], cam[7], cam[8]);
+    P::CameraPosition = vec3(cam[9], cam[10], cam[11]);
+    P::PixelArea = cam[12];
+    P::FrameSeed = frameSeed;
+    P::IterationCount = 0;
+    P::EnvironmentMap.colour = vec3(sky[0], sky[1], sky[2]);
+    P::OutputTexture = image2D{reinterpret_cast<vec4*>(accum), width};
+    P::g_maxPathLength = maxPathLength;
+    parallel_for((uint64_t)width * height, numThreads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i) {
+            gl_GlobalInvocationID = uvec3((uint)(i % width), (uint)(i / width), 0u);
+            P::PathtracerMain();
+        }
+    });
+    g_textureColours = nullptr;
+    return 0;
+}
+
+}  // extern "C"

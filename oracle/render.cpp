@@ -1949,6 +1949,73 @@ uint32_t oracle_pcg_hash(uint32_t x) { return PcgHash(x); }
 // Random streams of the following calls: 1 PCG, 0 the reference's.
 void oracle_set_rng(int pcg) { g_rngPcg = pcg ? 1u : 0u; }
 
+// The restated random.glsl / helper.glsl functions over arrays, in the
+// reference's random streams; `kind` and layouts as ref_eval of the
+// reference-text build (oracle/ref_glue.cpp), so the two can be compared.
+int oracle_eval(int kind, uint64_t n, const void* in, void* out) {
+    const uint32_t* iu = static_cast<const uint32_t*>(in);
+    const float* f = static_cast<const float*>(in);
+    uint32_t* ou = static_cast<uint32_t*>(out);
+    float* of = static_cast<float*>(out);
+    for (uint64_t i = 0; i < n; ++i) {
+        switch (kind) {
+        case 0: ou[i] = wanghash(iu[i]); break;
+        case 1: {
+            Rng r{iu[i], 0u};
+            for (int k = 0; k < 4; ++k) ou[4 * i + k] = RandomUInt(r);
+            break;
+        }
+        case 2: {
+            Rng r{iu[i], 0u};
+            for (int k = 0; k < 4; ++k) of[4 * i + k] = Random(r);
+            break;
+        }
+        case 3: ou[i] = InitRandomSeed(0u, iu[2 * i], iu[2 * i + 1]).s; break;
+        case 4: {
+            vec3 d = SampleDirection(vec2(f[2 * i], f[2 * i + 1]));
+            of[3 * i] = d.x, of[3 * i + 1] = d.y, of[3 * i + 2] = d.z;
+            break;
+        }
+        case 5: {
+            const float* q = f + 5 * i;
+            vec3 N(q[2], q[3], q[4]), U, V;
+            CreateONB(N, U, V);
+            vec3 d = SampleHemisphereCosine(vec2(q[0], q[1]), U, V, N);
+            of[3 * i] = d.x, of[3 * i + 1] = d.y, of[3 * i + 2] = d.z;
+            break;
+        }
+        case 6: {
+            const float* q = f + 6 * i;
+            vec3 N(q[3], q[4], q[5]), U, V;
+            CreateONB(N, U, V);
+            vec3 d = SamplePhongLobe(vec2(q[0], q[1]), q[2], U, V, N);
+            of[3 * i] = d.x, of[3 * i + 1] = d.y, of[3 * i + 2] = d.z;
+            break;
+        }
+        case 7: {
+            vec3 N(f[3 * i], f[3 * i + 1], f[3 * i + 2]), U, V;
+            CreateONB(N, U, V);
+            of[6 * i] = U.x, of[6 * i + 1] = U.y, of[6 * i + 2] = U.z;
+            of[6 * i + 3] = V.x, of[6 * i + 4] = V.y, of[6 * i + 5] = V.z;
+            break;
+        }
+        case 8: {
+            vec3 d = UnpackNormal(vec2(f[2 * i], f[2 * i + 1]));
+            of[3 * i] = d.x, of[3 * i + 1] = d.y, of[3 * i + 2] = d.z;
+            break;
+        }
+        case 9: {
+            vec2 q = PackNormal(vec3(f[3 * i], f[3 * i + 1], f[3 * i + 2]));
+            of[2 * i] = q.x, of[2 * i + 1] = q.y;
+            break;
+        }
+        case 10: of[i] = GetLuminance(vec3(f[3 * i], f[3 * i + 1], f[3 * i + 2])); break;
+        default: return 1;
+        }
+    }
+    return 0;
+}
+
 // HierarchyImportance::Draw's importance pass on an AABB hierarchy
 // (hierarchyimportance.cpp:83-109): `iterations` acquisition passes of
 // width x height paths (numbered 1..iterations), then the propagation.
