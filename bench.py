@@ -151,25 +151,46 @@ def make_workload():
     return sc, b, batches
 
 
-def cpu_baseline(b, positions, batches, seconds=10.0, threads=None):
-    """The oracle (C++ restatement of the shaders) on the host cores, over a
-    bounded sample of the same workload: whole 2^20-ray batches until
-    `seconds` of wall time have passed."""
+def cpu_tracer():
+    """The reference's CPU implementation of the walk: its own shader text
+    compiled as C++ (oracle/_ref, kind "reference") where it could be built,
+    else the oracle's restatement of it (kind "port"). Returns (kind, trace)
+    with trace(bvh, positions, rays, threads)."""
     import oracle
+    try:
+        from oracle import ref
+        if ref.available():
+            def trace(b, positions, rays, nthreads):
+                os.environ["ORACLE_THREADS"] = str(nthreads)
+                return ref.trace_closest(b, positions, rays)
+            return "reference", trace
+    except (ImportError, OSError, RuntimeError):
+        pass
+    return "port", lambda b, positions, rays, nthreads: oracle.trace_closest(b, positions, rays, num_threads=nthreads)
+
+
+def cpu_baseline(b, positions, batches, seconds=10.0, threads=None):
+    """The reference's walk on the host cores (cpu_tracer), over a bounded
+    sample of the same workload: whole 2^20-ray batches until `seconds` of
+    wall time have passed."""
+    kind, trace = cpu_tracer()
     nthreads = threads or os.cpu_count() or 1
-    oracle.trace_closest(b, positions, batches[0], num_threads=nthreads)  # warm-up, builds the library
+    trace(b, positions, batches[0], nthreads)  # warm-up, builds the library
     rays = 0
     t0 = time.perf_counter()
     k = 0
     while True:
-        oracle.trace_closest(b, positions, batches[k % len(batches)], num_threads=nthreads)
+        trace(b, positions, batches[k % len(batches)], nthreads)
         rays += N_RAYS
         k += 1
         el = time.perf_counter() - t0
         if el >= seconds:
             break
-    return {"value": rays / el / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{k} batches of 2^20 rays of this workload ({rays} rays, {el:.1f} s wall) on {nthreads} threads"}
+    what = ("the reference's traceray.glsl compiled as C++" if kind == "reference"
+            else "the oracle's C++ restatement of traceray.glsl")
+    return {"value": rays / el / 1e6, "unit": UNIT, "cores": nthreads, "kind": kind,
+            "sample": f"{k} batches of 2^20 rays of this workload ({rays} rays, {el:.1f} s wall) on {nthreads} "
+                      f"threads: {what}"}
 
 
 def dist_setup(args):
@@ -204,22 +225,24 @@ def run_reference(args, world, rank):
         return
     sc, b, batches = make_workload()
     nthreads = os.cpu_count() or 1
-    import oracle
+    kind, trace = cpu_tracer()
     for k in range(args.warmup):
-        oracle.trace_closest(b, sc["positions"], batches[k % N_BATCHES], num_threads=nthreads)
+        trace(b, sc["positions"], batches[k % N_BATCHES], nthreads)
     t0 = time.perf_counter()
     for k in range(args.steps):
-        oracle.trace_closest(b, sc["positions"], batches[k % N_BATCHES], num_threads=nthreads)
+        trace(b, sc["positions"], batches[k % N_BATCHES], nthreads)
     el = time.perf_counter() - t0
     value = args.steps * N_RAYS / el / 1e6
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": bench_config(args.gpus), "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": f"{args.steps} steps x 2^20 rays on {nthreads} threads (the reference's "
-                                       "GLSL path cannot run on this box: no OpenGL; the oracle restatement "
-                                       "of its shaders stands in)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
+                             "sample": f"{args.steps} steps x 2^20 rays on {nthreads} threads: " + (
+                                 "the reference's traceray.glsl + intersectiontests.glsl compiled as C++ "
+                                 "(its OpenGL path is unavailable on this box)" if kind == "reference" else
+                                 "the oracle's C++ restatement of the reference's shaders (its OpenGL path is "
+                                 "unavailable on this box and its shader text could not be compiled here)")},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

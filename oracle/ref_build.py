@@ -119,13 +119,21 @@ def generate(reference: Path) -> None:
 
 
 def build(reference: Path | None = None, force: bool = False) -> Path | None:
+    """Rewrite the shaders (when the reference tree is present) and compile.
+    Without the tree, rewritten copies already in oracle/_ref/gen/ (made on a
+    machine that has it) are compiled as they are; without either there is
+    nothing to build and None is returned."""
     ref = Path(reference) if reference else DEFAULT_REFERENCE
-    if not ref.is_dir():
+    have_tree = ref.is_dir()
+    have_gen = all((GEN / (f + ".h")).exists() for f in FILES)
+    if not have_tree and not have_gen:
         return LIB if LIB.exists() else None
-    deps = [HERE / "ref_shim.hpp", HERE / "ref_glue.cpp", Path(__file__)] + [ref / f for f in FILES]
+    srcs = [ref / f for f in FILES] if have_tree else [GEN / (f + ".h") for f in FILES]
+    deps = [HERE / "ref_shim.hpp", HERE / "ref_glue.cpp", Path(__file__)] + srcs
     if not force and LIB.exists() and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
         return LIB
-    generate(ref)
+    if have_tree:
+        generate(ref)
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-shared", "-w",
            "-Wno-narrowing",
            "-I", str(GEN), "-I", str(HERE), "-o", str(LIB), str(HERE / "ref_glue.cpp"), "-pthread"]

@@ -55,7 +55,7 @@ def test_crack_rays_all_hit(cuda_ctx, closed_mesh):
     _same(cuda.trace_closest(cuda_ctx, ds, rays), oracle.trace_closest(b, sc["positions"], rays))
 
 
-@pytest.mark.parametrize("fit", ["box", "ellipsoid"])
+@pytest.mark.parametrize("fit", ["aabox", "ellipsoid"])
 def test_watertight_bit_exact_on_query_workload(cuda_ctx, fit):
     """The closest-hit query workload (65,536-triangle displaced icosphere,
     sweep hierarchy, 2^20 rays) and its ellipsoid variant."""
@@ -67,7 +67,7 @@ def test_watertight_bit_exact_on_query_workload(cuda_ctx, fit):
     o = oracle.trace_closest(b, sc["positions"], rays, watertight=True)
     oa = oracle.trace_any(b, sc["positions"], rays, watertight=True)["occluded"]
     try:
-        for mode in ((0, 1, 2, 3, 4, 5) if fit == "box" else (0, 3)):
+        for mode in ((0, 1, 2, 3, 4, 5) if fit == "aabox" else (0, 3)):
             cuda_ctx.set_trace_config(mode=mode)
             _same(cuda.trace_closest(cuda_ctx, ds, rays), o)
             assert np.array_equal(cuda.trace_any(cuda_ctx, ds, rays), oa)
