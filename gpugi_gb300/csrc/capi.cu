@@ -276,6 +276,11 @@ void gpugi_destroy(gpugi_ctx* ctx) {
     if (ctx->errHost) cudaFreeHost(ctx->errHost);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->queue) cudaFree(ctx->queue);
+    for (auto& ss : ctx->streamScratch) {
+        cudaStreamSynchronize(ss.stream);
+        if (ss.queue) cudaFree(ss.queue);
+        if (ss.counters) cudaFree(ss.counters);
+    }
     if (ctx->copyIn) {
         cudaStreamSynchronize(ctx->copyIn);
         cudaStreamSynchronize(ctx->copyOut);
@@ -369,6 +374,84 @@ gpugi_status gpugi_trace_any_device(gpugi_ctx* ctx, const gpugi_scene* sc, const
     if (!sc || (n && (!ox || !oy || !oz || !dx || !dy || !dz || !tmax || !occluded)))
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
     return launch_trace_any(ctx, sc, ox, oy, oz, dx, dy, dz, tmax, n, occluded);
+}
+
+}  // extern "C"
+
+namespace gpugi {
+
+// Scratch of a caller stream: found by stream, grown when a call needs more
+// queue entries (after the stream's earlier work has finished with it).
+static gpugi_status stream_scratch(gpugi_ctx* ctx, cudaStream_t s, uint64_t n, gpugi_ctx::StreamScratch** out) {
+    gpugi_ctx::StreamScratch* ss = nullptr;
+    for (auto& e : ctx->streamScratch)
+        if (e.stream == s) ss = &e;
+    if (!ss) {
+        if (ctx->streamScratch.size() >= kMaxQueryStreams)
+            return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "more than GPUGI_MAX_QUERY_STREAMS caller streams");
+        ctx->streamScratch.push_back({});
+        ss = &ctx->streamScratch.back();
+        ss->stream = s;
+        if (cudaMalloc(&ss->counters, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+            ctx->streamScratch.pop_back();
+            return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "query counters");
+        }
+    }
+    if (n > ss->cap) {
+        if (ss->queue) {
+            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            cudaFree(ss->queue);
+            ss->queue = nullptr;
+            ss->cap = 0;
+        }
+        const uint64_t want = n + n / 4;
+        if (cudaMalloc(&ss->queue, want * sizeof(uint32_t)) != cudaSuccess) {
+            ss->queue = nullptr;
+            return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "ray queue allocation failed");
+        }
+        ss->cap = want;
+    }
+    *out = ss;
+    return GPUGI_OK;
+}
+
+static gpugi_status trace_async(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
+                                const float* oy, const float* oz, const float* dx, const float* dy, const float* dz,
+                                const float* tmax, uint64_t n, int32_t* slot, float* t, float* u, float* v,
+                                uint8_t* occluded, void* stream) {
+    if (n == 0) return GPUGI_OK;
+    if (n > 0xFFFFFFFFull) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "at most 2^32-1 rays per call");
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    gpugi_ctx::StreamScratch* ss = nullptr;
+    gpugi_status st = stream_scratch(ctx, s, n, &ss);
+    if (st) return st;
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(ss->counters, 0, 4 * sizeof(unsigned long long), s));
+    return launch_trace_filtered_on(ctx, sc, anyHit, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, occluded,
+                                    ss->queue, ss->counters, s);
+}
+
+}  // namespace gpugi
+
+extern "C" {
+
+gpugi_status gpugi_trace_closest_device_async(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox,
+                                              const float* oy, const float* oz, const float* dx, const float* dy,
+                                              const float* dz, const float* tmax, uint64_t n, int32_t* slot,
+                                              float* t, float* u, float* v, void* stream) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!sc || (n && (!ox || !oy || !oz || !dx || !dy || !dz || !tmax || !slot || !t || !u || !v)))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
+    return trace_async(ctx, sc, false, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, nullptr, stream);
+}
+
+gpugi_status gpugi_trace_any_device_async(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
+                                          const float* oz, const float* dx, const float* dy, const float* dz,
+                                          const float* tmax, uint64_t n, uint8_t* occluded, void* stream) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!sc || (n && (!ox || !oy || !oz || !dx || !dy || !dz || !tmax || !occluded)))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
+    return trace_async(ctx, sc, true, ox, oy, oz, dx, dy, dz, tmax, n, nullptr, nullptr, nullptr, nullptr, occluded,
+                       stream);
 }
 
 gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,

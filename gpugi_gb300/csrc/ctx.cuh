@@ -46,6 +46,15 @@ struct gpugi_ctx {
     cudaStream_t copyIn = nullptr, copyOut = nullptr;
     cudaStream_t compute2 = nullptr;  // second traversal stream of the host-pointer pipeline
     cudaEvent_t evIn[8] = {}, evTraced[8] = {};
+    // scratch of the stream-ordered queries (gpugi_trace_*_device_async), one
+    // set per caller stream: ray-index queue + four counters
+    struct StreamScratch {
+        cudaStream_t stream = nullptr;
+        uint32_t* queue = nullptr;
+        uint64_t cap = 0;
+        unsigned long long* counters = nullptr;
+    };
+    std::vector<StreamScratch> streamScratch;
     // batched rendering
     uint32_t batchPaths = 16u << 20;  // path-queue capacity of one round
     uint32_t batchGraph = 1;          // replay rounds as a CUDA graph
@@ -134,6 +143,7 @@ gpugi_status cuda_fail(gpugi_ctx* ctx, cudaError_t e, const char* what);
 gpugi_status ensure_stage(gpugi_ctx* ctx, size_t bytes);
 // Grow the context's ray-index queue to at least n entries.
 gpugi_status ensure_queue(gpugi_ctx* ctx, uint64_t n);
+constexpr size_t kMaxQueryStreams = 8;  // GPUGI_MAX_QUERY_STREAMS
 gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
                                    const float* oy, const float* oz, const float* dx, const float* dy,
                                    const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,

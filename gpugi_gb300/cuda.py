@@ -62,6 +62,8 @@ def _declare(L):
         getattr(L, name).argtypes = [P, P] + [P] * 7 + [U64] + [P] * 4
     for name in ("gpugi_trace_any", "gpugi_trace_any_device"):
         getattr(L, name).argtypes = [P, P] + [P] * 7 + [U64, P]
+    L.gpugi_trace_closest_device_async.argtypes = [P, P] + [P] * 7 + [U64] + [P] * 4 + [P]
+    L.gpugi_trace_any_device_async.argtypes = [P, P] + [P] * 7 + [U64, P, P]
     L.gpugi_set_trace_config.argtypes = [P, U32, U32]
     L.gpugi_set_scene_layout.argtypes = [P, U32, U32]
     L.gpugi_set_host_pipeline.argtypes = [P, U32, U32]
@@ -309,6 +311,21 @@ def trace_closest_device(ctx: Context, scene: DeviceScene, rays: dict, out: dict
     n = rays["ox"].numel()
     ctx.check(lib().gpugi_trace_closest_device(ctx.handle, scene.handle, *[_ptr(rays[k]) for k in RAY_KEYS], n,
                                                _ptr(out["slot"]), _ptr(out["t"]), _ptr(out["u"]), _ptr(out["v"])))
+
+
+def trace_closest_device_async(ctx: Context, scene: DeviceScene, rays: dict, out: dict, stream: int) -> None:
+    """As trace_closest_device, enqueued on a caller stream (a cudaStream_t
+    handle, e.g. torch's Stream.cuda_stream; 0 = the context stream)."""
+    n = rays["ox"].numel()
+    ctx.check(lib().gpugi_trace_closest_device_async(ctx.handle, scene.handle, *[_ptr(rays[k]) for k in RAY_KEYS], n,
+                                                     _ptr(out["slot"]), _ptr(out["t"]), _ptr(out["u"]), _ptr(out["v"]),
+                                                     C.c_void_p(stream or None)))
+
+
+def trace_any_device_async(ctx: Context, scene: DeviceScene, rays: dict, occluded, stream: int) -> None:
+    n = rays["ox"].numel()
+    ctx.check(lib().gpugi_trace_any_device_async(ctx.handle, scene.handle, *[_ptr(rays[k]) for k in RAY_KEYS], n,
+                                                 _ptr(occluded), C.c_void_p(stream or None)))
 
 
 def trace_any_device(ctx: Context, scene: DeviceScene, rays: dict, occluded) -> None:

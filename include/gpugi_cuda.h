@@ -168,6 +168,32 @@ gpugi_status gpugi_trace_any_device(gpugi_ctx* ctx, const gpugi_scene* scene,
                                     const float* dx, const float* dy, const float* dz,
                                     const float* tmax, uint64_t n, uint8_t* occluded);
 
+/* Stream-ordered ray queries: as gpugi_trace_closest_device /
+ * gpugi_trace_any_device, but enqueued on the caller's stream (a
+ * cudaStream_t passed as void*; NULL = the context stream) and ordered only
+ * by it. Calls on different streams may run concurrently: a renderer with
+ * several independent ray batches in flight issues them on two or more
+ * streams, and the tail of one batch's walk (the few deepest rays, while
+ * most SMs are idle) overlaps the next batch's walk. The caller orders each
+ * call after the work that writes its rays (and before the work that reads
+ * its results) on that stream, as for any CUDA library call that takes a
+ * stream. The library keeps one scratch set (ray-index queue and counters)
+ * per stream, up to GPUGI_MAX_QUERY_STREAMS streams per context, allocated
+ * at the first call on a stream and grown when n grows (which waits for the
+ * stream). The context's trace mode selects the walker (modes 0 and 1 run
+ * the mode-2 launches). No counterpart in the reference (its queries are
+ * shader calls inside a dispatch). */
+#define GPUGI_MAX_QUERY_STREAMS 8
+gpugi_status gpugi_trace_closest_device_async(gpugi_ctx* ctx, const gpugi_scene* scene,
+                                              const float* ox, const float* oy, const float* oz,
+                                              const float* dx, const float* dy, const float* dz,
+                                              const float* tmax, uint64_t n,
+                                              int32_t* slot, float* t, float* u, float* v, void* stream);
+gpugi_status gpugi_trace_any_device_async(gpugi_ctx* ctx, const gpugi_scene* scene,
+                                          const float* ox, const float* oy, const float* oz,
+                                          const float* dx, const float* dy, const float* dz,
+                                          const float* tmax, uint64_t n, uint8_t* occluded, void* stream);
+
 /* Closest hit without any device allocation in the call. No counterpart in
  * the reference: it exists for callers that cannot let the library call
  * cudaMalloc, such as an engine that owns all device memory through its own

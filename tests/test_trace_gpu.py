@@ -322,3 +322,34 @@ def test_l2_bandwidth_measurement(cuda_ctx):
     assert g.value > 1000.0
     with pytest.raises(cuda.GpugiError):
         cuda_ctx.check(lib.gpugi_measure_l2_bandwidth(cuda_ctx.handle, 1000, 1, C.byref(g)))
+
+
+def test_stream_ordered_queries_overlap_and_match(cuda_ctx, icosphere_65536):
+    """gpugi_trace_*_device_async on several caller streams: batches issued
+    alternately on three streams (and one on the context stream, NULL) give
+    the results of the context-stream calls; a larger batch on a stream
+    grows its scratch."""
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    streams = [torch.cuda.Stream() for _ in range(3)]
+    sizes = [1 << 14, 3 << 14, 50001, 1 << 18, 1 << 16, 7]
+    host = [scenes.random_rays(n, seed=300 + i) for i, n in enumerate(sizes)]
+    dev = [{k: torch.from_numpy(r[k]).cuda() for k in cuda.RAY_KEYS} for r in host]
+    outs = [dict(slot=torch.empty(n, dtype=torch.int32, device="cuda"), t=torch.empty(n, device="cuda"),
+                 u=torch.empty(n, device="cuda"), v=torch.empty(n, device="cuda")) for n in sizes]
+    occ = [torch.empty(n, dtype=torch.uint8, device="cuda") for n in sizes]
+    torch.cuda.synchronize()
+    for i in range(len(sizes)):
+        s = streams[i % 3].cuda_stream if i != 4 else 0
+        cuda.trace_closest_device_async(cuda_ctx, ds, dev[i], outs[i], s)
+        cuda.trace_any_device_async(cuda_ctx, ds, dev[i], occ[i], s)
+    torch.cuda.synchronize()
+    cuda_ctx.sync()
+    for i in range(len(sizes)):
+        g = {k: v.cpu().numpy() for k, v in outs[i].items()}
+        _compare_closest(g, cuda.trace_closest(cuda_ctx, ds, host[i]))
+        assert np.array_equal(occ[i].cpu().numpy(), cuda.trace_any(cuda_ctx, ds, host[i]))
+    assert cuda_ctx.device_error_bits() == 0
+    ds.close()
