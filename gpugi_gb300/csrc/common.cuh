@@ -39,6 +39,21 @@ struct X {  // namespace-like holder so the names stay short at call sites
     }
 };
 
+// Three-input IEEE minNum/maxNum (PTX min.f32 / max.f32 with three sources,
+// sm_100 and later): NaN operands are ignored like fminf/fmaxf ignore them,
+// so min3(a, b, c) = fminf(fminf(a, b), c) for every input, in one
+// instruction.
+GPUGI_D float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+GPUGI_D float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // ---------------- ordinary float3 helpers (shading; contraction allowed) ---
 GPUGI_HD float3 f3(float a, float b, float c) { return make_float3(a, b, c); }
 GPUGI_HD float3 f3(float s) { return make_float3(s, s, s); }

@@ -38,10 +38,10 @@ GPUGI_D bool intersect_box(float3 o, float3 inv, float4 lo, float4 hi, float& fi
         if (isnan(tby) || isnan(tty)) mny = -inf, mxy = inf;
         if (isnan(tbz) || isnan(ttz)) mnz = -inf, mxz = inf;
     }
-    float t0 = fmaxf(mnx, mny), t1 = fmaxf(mnx, mnz);
-    firstHit = fmaxf(0.0f, fmaxf(t0, t1));
-    float l0 = fminf(mxx, mxy), l1 = fminf(mxx, mxz);
-    float lastHit = fminf(l0, l1);
+    // max(max(mnx, mny), max(mnx, mnz)) of the shader is the maximum of the
+    // three (NaNs ignored either way); likewise for the minimum
+    firstHit = fmaxf(0.0f, max3f(mnx, mny, mnz));
+    float lastHit = min3f(mxx, mxy, mxz);
     if (ROBUST) lastHit = X::mul(lastHit, 0x1.000008p+0f);
     return firstHit <= lastHit;
 }
