@@ -353,28 +353,53 @@ def run_ours(args, world, rank, local):
     ds.set_triangle_test(False)
 
     # End to end through the public C ABI with host buffers: every step copies
-    # its rays from pinned host memory and its results back.
-    pin = [{k: torch.from_numpy(rb[k]).pin_memory().numpy() for k in cuda.RAY_KEYS} for rb in host_batches[:2]]
+    # its rays from page-locked host memory and its results back. Steps are
+    # issued with gpugi_trace_closest_async over several streams, so one
+    # batch's results travel back while the next batch's rays travel in; the
+    # synchronous call (gpugi_trace_closest, one batch at a time) is timed too.
+    ns = max(1, args.e2e_streams)
+    pin = [{k: torch.from_numpy(rb[k]).pin_memory().numpy() for k in cuda.RAY_KEYS}
+           for rb in host_batches[:max(ns, 2)]]
     res = [dict(slot=torch.empty(N_RAYS, dtype=torch.int32).pin_memory().numpy(),
                 t=torch.empty(N_RAYS).pin_memory().numpy(), u=torch.empty(N_RAYS).pin_memory().numpy(),
-                v=torch.empty(N_RAYS).pin_memory().numpy()) for _ in range(2)]
+                v=torch.empty(N_RAYS).pin_memory().numpy()) for _ in range(max(ns, 2))]
     lib = cuda.lib()
+    lib.gpugi_trace_closest_async.argtypes = [ctypes.c_void_p] * 9 + [ctypes.c_uint64] + [ctypes.c_void_p] * 5
+    estreams = [torch.cuda.Stream(device=dev) for _ in range(ns)]
 
-    def e2e_step(k):
+    def e2e_issue(k):
+        r, o, s = pin[k % ns], res[k % ns], estreams[k % ns]
+        ctx.check(lib.gpugi_trace_closest_async(ctx.handle, ds.handle, *[cuda._ptr(r[key]) for key in cuda.RAY_KEYS],
+                                                N_RAYS, cuda._ptr(o["slot"]), cuda._ptr(o["t"]), cuda._ptr(o["u"]),
+                                                cuda._ptr(o["v"]), ctypes.c_void_p(s.cuda_stream)))
+
+    def e2e_sync_step(k):
         r, o = pin[k % 2], res[k % 2]
         ctx.check(lib.gpugi_trace_closest(ctx.handle, ds.handle, *[cuda._ptr(r[key]) for key in cuda.RAY_KEYS],
                                           N_RAYS, cuda._ptr(o["slot"]), cuda._ptr(o["t"]), cuda._ptr(o["u"]),
                                           cuda._ptr(o["v"])))
 
-    for k in range(args.warmup):
-        e2e_step(k)
+    for k in range(max(args.warmup, ns)):
+        e2e_issue(k)
+    torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
     for k in range(args.steps):
-        e2e_step(k)
+        e2e_issue(k)
+    for s in estreams:
+        s.synchronize()
     e2e_s = reduce_max(time.perf_counter() - t0, world, dev)
     e2e_value = world * args.steps * N_RAYS / e2e_s / 1e6
-    assert (res[0]["slot"] >= -1).all()
+    assert (res[0]["slot"] >= -1).all() and ctx.device_error_bits() == 0
+    for k in range(args.warmup):
+        e2e_sync_step(k)
+    barrier(world)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        e2e_sync_step(k)
+    e2e_sync_s = reduce_max(time.perf_counter() - t0, world, dev)
+    e2e_sync = {"value": world * args.steps * N_RAYS / e2e_sync_s / 1e6, "unit": UNIT,
+                "call": "gpugi_trace_closest (synchronous, one batch at a time)"}
 
     peak, peak_src = peaks()
     avg_launch_s = float(np.mean(per_launch_ms)) / 1e3
@@ -390,7 +415,9 @@ def run_ours(args, world, rank, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": bench_config(world),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * 28,
-                    "d2h_bytes_per_step": N_RAYS * 16},
+                    "d2h_bytes_per_step": N_RAYS * 16,
+                    "call": f"gpugi_trace_closest_async from page-locked host arrays over {ns} streams",
+                    "synchronous": e2e_sync},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per step, read from "
@@ -873,6 +900,8 @@ def main():
                     help="top-of-tree nodes staged in shared memory by the walkers")
     ap.add_argument("--streams", type=int, default=2,
                     help="caller streams the headline steps alternate over (1 = no overlap)")
+    ap.add_argument("--e2e-streams", type=int, default=3,
+                    help="streams the end-to-end host-buffer steps alternate over")
     ap.add_argument("--trace-mode", type=int, default=3,
                     help="0: thread per ray, 1: persistent lane refill, 2: root prefilter + persistent, "
                          "3/4: root prefilter + 8/4-lane group walker")

@@ -280,6 +280,7 @@ void gpugi_destroy(gpugi_ctx* ctx) {
         cudaStreamSynchronize(ss.stream);
         if (ss.queue) cudaFree(ss.queue);
         if (ss.counters) cudaFree(ss.counters);
+        if (ss.stage) cudaFree(ss.stage);
     }
     if (ctx->copyIn) {
         cudaStreamSynchronize(ctx->copyIn);
@@ -430,9 +431,83 @@ static gpugi_status trace_async(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyH
                                     ss->queue, ss->counters, s);
 }
 
+// Host-pointer query on a caller stream: rays copied in, the two launches,
+// results copied out, all enqueued on `stream` with no wait. The stream's
+// staging columns grow with n (after the stream's earlier work has finished).
+static gpugi_status trace_host_async(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* const src[7],
+                                     uint64_t n, int32_t* slot, float* t, float* u, float* v, uint8_t* occ,
+                                     void* stream) {
+    if (n == 0) return GPUGI_OK;
+    if (n > 0xFFFFFFFFull) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "at most 2^32-1 rays per call");
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    gpugi_ctx::StreamScratch* ss = nullptr;
+    gpugi_status st = stream_scratch(ctx, s, n, &ss);
+    if (st) return st;
+    const size_t col = align256(n * 4);
+    if (ss->stageBytes < 11 * col) {
+        if (ss->stage) {
+            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            cudaFree(ss->stage);
+            ss->stage = nullptr;
+            ss->stageBytes = 0;
+        }
+        if (cudaMalloc(&ss->stage, 11 * col) != cudaSuccess) {
+            ss->stage = nullptr;
+            return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "query staging allocation failed");
+        }
+        ss->stageBytes = 11 * col;
+    }
+    char* base = static_cast<char*>(ss->stage);
+    float* d[7];
+    for (int k = 0; k < 7; ++k) {
+        d[k] = reinterpret_cast<float*>(base + k * col);
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(d[k], src[k], n * 4, cudaMemcpyHostToDevice, s));
+    }
+    int32_t* dSlot = reinterpret_cast<int32_t*>(base + 7 * col);
+    float* dT = reinterpret_cast<float*>(base + 8 * col);
+    float* dU = reinterpret_cast<float*>(base + 9 * col);
+    float* dV = reinterpret_cast<float*>(base + 10 * col);
+    uint8_t* dOcc = reinterpret_cast<uint8_t*>(base + 7 * col);
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(ss->counters, 0, 4 * sizeof(unsigned long long), s));
+    st = launch_trace_filtered_on(ctx, sc, anyHit, d[0], d[1], d[2], d[3], d[4], d[5], d[6], n,
+                                  anyHit ? nullptr : dSlot, anyHit ? nullptr : dT, anyHit ? nullptr : dU,
+                                  anyHit ? nullptr : dV, anyHit ? dOcc : nullptr, ss->queue, ss->counters, s);
+    if (st) return st;
+    if (anyHit) {
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(occ, dOcc, n, cudaMemcpyDeviceToHost, s));
+    } else {
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(slot, dSlot, n * 4, cudaMemcpyDeviceToHost, s));
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(t, dT, n * 4, cudaMemcpyDeviceToHost, s));
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(u, dU, n * 4, cudaMemcpyDeviceToHost, s));
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(v, dV, n * 4, cudaMemcpyDeviceToHost, s));
+    }
+    return GPUGI_OK;
+}
+
 }  // namespace gpugi
 
 extern "C" {
+
+gpugi_status gpugi_trace_closest_async(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
+                                       const float* oz, const float* dx, const float* dy, const float* dz,
+                                       const float* tmax, uint64_t n, int32_t* slot, float* t, float* u, float* v,
+                                       void* stream) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!sc || (n && (!ox || !oy || !oz || !dx || !dy || !dz || !tmax || !slot || !t || !u || !v)))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
+    const float* const src[7] = {ox, oy, oz, dx, dy, dz, tmax};
+    return trace_host_async(ctx, sc, false, src, n, slot, t, u, v, nullptr, stream);
+}
+
+gpugi_status gpugi_trace_any_async(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox, const float* oy,
+                                   const float* oz, const float* dx, const float* dy, const float* dz,
+                                   const float* tmax, uint64_t n, uint8_t* occluded, void* stream) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!sc || (n && (!ox || !oy || !oz || !dx || !dy || !dz || !tmax || !occluded)))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "NULL argument");
+    const float* const src[7] = {ox, oy, oz, dx, dy, dz, tmax};
+    return trace_host_async(ctx, sc, true, src, n, nullptr, nullptr, nullptr, nullptr, occluded, stream);
+}
 
 gpugi_status gpugi_trace_closest_device_async(gpugi_ctx* ctx, const gpugi_scene* sc, const float* ox,
                                               const float* oy, const float* oz, const float* dx, const float* dy,

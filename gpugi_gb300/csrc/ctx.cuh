@@ -53,6 +53,8 @@ struct gpugi_ctx {
         uint32_t* queue = nullptr;
         uint64_t cap = 0;
         unsigned long long* counters = nullptr;
+        void* stage = nullptr;  // host-pointer queries: device copies of the rays and results
+        size_t stageBytes = 0;
     };
     std::vector<StreamScratch> streamScratch;
     // batched rendering

@@ -194,6 +194,28 @@ gpugi_status gpugi_trace_any_device_async(gpugi_ctx* ctx, const gpugi_scene* sce
                                           const float* dx, const float* dy, const float* dz,
                                           const float* tmax, uint64_t n, uint8_t* occluded, void* stream);
 
+/* Stream-ordered queries over HOST arrays: the rays are copied in, traced
+ * and the results copied back, all enqueued on the caller's stream
+ * (cudaStream_t as void*; NULL = the context stream); the call returns at
+ * once and the results are in the host arrays when the stream has finished
+ * (cudaStreamSynchronize, or an event). Use page-locked host arrays: the
+ * copies from pageable memory are not asynchronous. Calls on different
+ * streams overlap: while one batch's results travel back, the next batch's
+ * rays travel in and a third is traced. The device error word is not read
+ * back by these calls: once the stream has finished, gpugi_device_error_bits
+ * reports it.
+ * Scratch and device staging (44 B per ray) are kept per stream, as for
+ * gpugi_trace_closest_device_async. No counterpart in the reference. */
+gpugi_status gpugi_trace_closest_async(gpugi_ctx* ctx, const gpugi_scene* scene,
+                                       const float* ox, const float* oy, const float* oz,
+                                       const float* dx, const float* dy, const float* dz,
+                                       const float* tmax, uint64_t n,
+                                       int32_t* slot, float* t, float* u, float* v, void* stream);
+gpugi_status gpugi_trace_any_async(gpugi_ctx* ctx, const gpugi_scene* scene,
+                                   const float* ox, const float* oy, const float* oz,
+                                   const float* dx, const float* dy, const float* dz,
+                                   const float* tmax, uint64_t n, uint8_t* occluded, void* stream);
+
 /* Closest hit without any device allocation in the call. No counterpart in
  * the reference: it exists for callers that cannot let the library call
  * cudaMalloc, such as an engine that owns all device memory through its own

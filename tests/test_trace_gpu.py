@@ -353,3 +353,37 @@ def test_stream_ordered_queries_overlap_and_match(cuda_ctx, icosphere_65536):
         assert np.array_equal(occ[i].cpu().numpy(), cuda.trace_any(cuda_ctx, ds, host[i]))
     assert cuda_ctx.device_error_bits() == 0
     ds.close()
+
+
+def test_stream_ordered_host_queries(cuda_ctx, icosphere_65536):
+    """gpugi_trace_closest_async / gpugi_trace_any_async with page-locked host
+    arrays on three streams equal the synchronous host calls."""
+    import ctypes as C
+
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    L = cuda.lib()
+    L.gpugi_trace_closest_async.argtypes = [C.c_void_p] * 9 + [C.c_uint64] + [C.c_void_p] * 5
+    L.gpugi_trace_any_async.argtypes = [C.c_void_p] * 9 + [C.c_uint64, C.c_void_p, C.c_void_p]
+    streams = [torch.cuda.Stream() for _ in range(3)]
+    sizes = [1 << 16, 12345, 1 << 18, 3, 1 << 16, 40000]
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
+    host = [{k: pin(v) for k, v in scenes.random_rays(n, seed=400 + i).items()} for i, n in enumerate(sizes)]
+    outs = [dict(slot=pin(np.empty(n, np.int32)), t=pin(np.empty(n, np.float32)), u=pin(np.empty(n, np.float32)),
+                 v=pin(np.empty(n, np.float32)), occ=pin(np.empty(n, np.uint8))) for n in sizes]
+    for i, n in enumerate(sizes):
+        s = C.c_void_p(streams[i % 3].cuda_stream)
+        r, o = host[i], outs[i]
+        cuda_ctx.check(L.gpugi_trace_closest_async(cuda_ctx.handle, ds.handle, *[cuda._ptr(r[k]) for k in cuda.RAY_KEYS],
+                                                   n, *[cuda._ptr(o[k]) for k in ("slot", "t", "u", "v")], s))
+        cuda_ctx.check(L.gpugi_trace_any_async(cuda_ctx.handle, ds.handle, *[cuda._ptr(r[k]) for k in cuda.RAY_KEYS],
+                                               n, cuda._ptr(o["occ"]), s))
+    for s in streams:
+        s.synchronize()
+    assert cuda_ctx.device_error_bits() == 0
+    for i in range(len(sizes)):
+        _compare_closest({k: outs[i][k] for k in ("slot", "t", "u", "v")}, cuda.trace_closest(cuda_ctx, ds, host[i]))
+        assert np.array_equal(outs[i]["occ"], cuda.trace_any(cuda_ctx, ds, host[i]))
+    ds.close()
