@@ -16,6 +16,7 @@ all host cores (the reference's GLSL path cannot run here).
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
