@@ -16,7 +16,7 @@ _LIB = None
 LIB_DIR = Path(__file__).resolve().parent / "lib"
 
 BUILD_METHODS = {"kdtree": 0, "sweep": 1, "lds": 2}
-FIT_METHODS = {"aabox": 0, "ellipsoid": 1}
+FIT_METHODS = {"aabox": 0, "ellipsoid": 1, "obox": 2}
 
 
 def _lib():
@@ -61,11 +61,11 @@ def _ptr(a: np.ndarray):
 
 @dataclass
 class BVH:
-    hierarchy: np.ndarray   # float32 [N, 8]
+    hierarchy: np.ndarray   # float32 [N, 8] ([N, 12] for oriented boxes: + rotationInv quaternion)
     slots: np.ndarray       # int32 [S, 4]
     parents: np.ndarray     # uint32 [N]
     leaf_size: int
-    bounds_kind: int        # 0 = AABB, 1 = ellipsoid
+    bounds_kind: int        # 0 = AABB, 1 = ellipsoid, 2 = oriented box
     max_depth: int
     positions: np.ndarray | None = None
     normals: np.ndarray | None = None      # from a file: float32 [V, 3]
@@ -95,7 +95,7 @@ def _collect(handle) -> BVH:
     lib = _lib()
     n, nb, ls, bk, md = (C.c_uint32() for _ in range(5))
     lib.gpugi_bvh_info(handle, C.byref(n), C.byref(nb), C.byref(ls), C.byref(bk), C.byref(md))
-    hier = np.zeros((n.value, 8), dtype=np.float32)
+    hier = np.zeros((n.value, 12 if bk.value == 2 else 8), dtype=np.float32)
     slots = np.zeros((nb.value * ls.value, 4), dtype=np.int32)
     parents = np.zeros(n.value, dtype=np.uint32)
     lib.gpugi_bvh_export(handle, _ptr(hier), _ptr(slots), _ptr(parents))

@@ -669,16 +669,17 @@ extern "C" gpugi_status gpugi_scene_export(gpugi_ctx* ctx, const gpugi_scene* sc
         GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(slots, sc->dev.slots, 16 * (size_t)sc->dev.numSlots,
                                             cudaMemcpyDeviceToHost, ctx->stream));
     if (hierarchy) {
-        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(hierarchy, sc->dev.nodes, 32 * (size_t)sc->dev.numNodes,
+        const size_t nf = sc->dev.boundsKind == GPUGI_BOUNDS_OBOX ? 12 : 8;  // floats per node
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(hierarchy, sc->dev.nodes, 4 * nf * (size_t)sc->dev.numNodes,
                                             cudaMemcpyDeviceToHost, ctx->stream));
         GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
         for (size_t i = 0; i < sc->dev.numNodes; ++i) {
             uint32_t w;
-            std::memcpy(&w, &hierarchy[8 * i + 3], 4);
+            std::memcpy(&w, &hierarchy[nf * i + 3], 4);
             if (w & LEAF_FLAG) w = LEAF_FLAG | (w & LEAF_BLOCK_MASK);
-            std::memcpy(&hierarchy[8 * i + 3], &w, 4);
+            std::memcpy(&hierarchy[nf * i + 3], &w, 4);
             if (!sc->hostRadii.empty())  // ellipsoid nodes: the radii as uploaded, not their reciprocals
-                for (int c = 0; c < 3; ++c) hierarchy[8 * i + 4 + c] = sc->hostRadii[3 * i + c];
+                for (int c = 0; c < 3; ++c) hierarchy[nf * i + 4 + c] = sc->hostRadii[3 * i + c];
         }
     }
     GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

@@ -29,6 +29,7 @@
 #include "../../../include/gpugi_bvhmake.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -64,6 +65,13 @@ struct Box {
 };
 struct Ellipsoid {
     V3 center, radii;
+};
+// Oriented box: centre, half sides and the inverse orientation (a unit
+// quaternion x, y, z, w that takes world directions into the box frame), the
+// fields of gpugi's Scene::TreeNode<OBox> (gpugi/scene/scene.hpp:40-49).
+struct OBox {
+    V3 center, halfSides;
+    float qInv[4];
 };
 
 inline Box BoxUnion(const Box& a, const Box& b) { return Box{vmin(a.min, b.min), vmax(a.max, b.max)}; }
@@ -170,6 +178,7 @@ struct gpugi_bvh {
     std::vector<Node> nodes;           // preorder
     std::vector<Box> boxes;            // per node: box of all triangles below
     std::vector<Ellipsoid> ellipsoids; // per node when boundsKind == ellipsoid
+    std::vector<OBox> oboxes;          // per node when boundsKind == obox
     std::vector<uint32_t> leaves;      // leafSize * 4 uint32 per block
     std::vector<uint32_t> escapes, parents;
     uint32_t maxDepth = 0;
@@ -693,6 +702,10 @@ Sggx LeafSggx(const gpugi_bvh& b, uint32_t blk) {
 // FitMethod::Surface of a node's bounding volume (aaboxfit.cpp:25-28,
 // aaellipsoidfit.cpp:81-84).
 float NodeSurface(const gpugi_bvh& b, uint32_t i) {
+    if (b.boundsKind == GPUGI_FIT_OBOX) {  // epsilon's surface(OBox): the box of the half sides
+        const V3 h = b.oboxes[i].halfSides;
+        return 8.0f * ((h.x * h.y + h.x * h.z) + h.y * h.z);
+    }
     return b.boundsKind == GPUGI_FIT_ELLIPSOID ? EllipsoidSurface(b.ellipsoids[i]) : BoxSurface(b.boxes[i]);
 }
 
@@ -839,6 +852,135 @@ void ComputeSggx(const gpugi_bvh& b) {
     for (size_t i = 0; i < nn; ++i) PackSggx(s[i], &b.sggx[6 * i]);
 }
 
+
+// --- Oriented-box fit (GPUGI_FIT_OBOX) -------------------------------------
+// The reference walks oriented-box hierarchies (FetchIntersectOBoxNode,
+// intersectiontests.glsl:114-128; OBOX_BVH, traceray.glsl:68-70) that the
+// missing Bim library supplies; bvhmake itself fits only boxes and
+// ellipsoids. This fit refits the built topology: every node's box around
+// the vertices of the triangles below it. The orientation is the principal
+// axes of those points (the covariance's eigenvectors, cyclic Jacobi in
+// double, right-handed); the extents are measured with the shader's own
+// float rotation, rotate(p - centre, rotationInv), and widened until every
+// point lies inside in that arithmetic, plus a margin of 2^-16 of the
+// extent and 2^-20 of the coordinates' magnitude for the rounding of ray
+// transforms. Each node is fitted to all vertices below it (an inner node
+// around its children's boxes would grow level by level).
+
+// rotate(x, q) (intersectiontests.glsl:82-89), float, in the shader's order.
+V3 QRotate(V3 x, const float q[4]) {
+    const V3 t = Cross(V3(q[0], q[1], q[2]), x);
+    const V3 u((q[3] * t.x + q[1] * t.z) - q[2] * t.y, (q[3] * t.y + q[2] * t.x) - q[0] * t.z,
+               (q[3] * t.z + q[0] * t.y) - q[1] * t.x);
+    return x + u * 2.0f;
+}
+
+OBox FitOBox(const std::vector<V3>& pts) {
+    const size_t n = pts.size();
+    double mean[3] = {0, 0, 0};
+    for (const V3& v : pts)
+        for (int k = 0; k < 3; ++k) mean[k] += v[k];
+    for (int k = 0; k < 3; ++k) mean[k] /= (double)n;
+    double cov[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (const V3& v : pts)
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) cov[r][c] += ((double)v[r] - mean[r]) * ((double)v[c] - mean[c]);
+    double m[3][3];  // rows: box axes in world space (world -> box frame)
+    SymmetricEigen3(cov, m);
+    const double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                       m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                       m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    if (det < 0.0)
+        for (int k = 0; k < 3; ++k) m[2][k] = -m[2][k];
+    // quaternion of the rotation matrix m (Shepperd's method)
+    double q[4];
+    const double tr = m[0][0] + m[1][1] + m[2][2];
+    if (tr > 0.0) {
+        const double sq = std::sqrt(tr + 1.0) * 2.0;
+        q[3] = 0.25 * sq;
+        q[0] = (m[2][1] - m[1][2]) / sq;
+        q[1] = (m[0][2] - m[2][0]) / sq;
+        q[2] = (m[1][0] - m[0][1]) / sq;
+    } else if (m[0][0] > m[1][1] && m[0][0] > m[2][2]) {
+        const double sq = std::sqrt(1.0 + m[0][0] - m[1][1] - m[2][2]) * 2.0;
+        q[3] = (m[2][1] - m[1][2]) / sq;
+        q[0] = 0.25 * sq;
+        q[1] = (m[0][1] + m[1][0]) / sq;
+        q[2] = (m[0][2] + m[2][0]) / sq;
+    } else if (m[1][1] > m[2][2]) {
+        const double sq = std::sqrt(1.0 + m[1][1] - m[0][0] - m[2][2]) * 2.0;
+        q[3] = (m[0][2] - m[2][0]) / sq;
+        q[0] = (m[0][1] + m[1][0]) / sq;
+        q[1] = 0.25 * sq;
+        q[2] = (m[1][2] + m[2][1]) / sq;
+    } else {
+        const double sq = std::sqrt(1.0 + m[2][2] - m[0][0] - m[1][1]) * 2.0;
+        q[3] = (m[1][0] - m[0][1]) / sq;
+        q[0] = (m[0][2] + m[2][0]) / sq;
+        q[1] = (m[1][2] + m[2][1]) / sq;
+        q[2] = 0.25 * sq;
+    }
+    const double qn = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    OBox o;
+    for (int k = 0; k < 4; ++k) o.qInv[k] = (float)(q[k] / qn);
+    const float qFwd[4] = {-o.qInv[0], -o.qInv[1], -o.qInv[2], o.qInv[3]};
+    const V3 c0((float)mean[0], (float)mean[1], (float)mean[2]);
+    V3 lo(INFINITY, INFINITY, INFINITY), hi(-INFINITY, -INFINITY, -INFINITY);
+    float mag = 0.0f;
+    for (const V3& v : pts) {
+        const V3 l = QRotate(v - c0, o.qInv);
+        lo = vmin(lo, l);
+        hi = vmax(hi, l);
+        mag = std::fmax(mag, std::fmax(std::fabs(v.x), std::fmax(std::fabs(v.y), std::fabs(v.z))));
+    }
+    o.center = c0 + QRotate((lo + hi) * 0.5f, qFwd);
+    V3 h = (hi - lo) * 0.5f;
+    for (const V3& v : pts) {  // every point inside in the shader's arithmetic
+        const V3 l = QRotate(v - o.center, o.qInv);
+        for (int k = 0; k < 3; ++k) h[k] = std::fmax(h[k], std::fabs(l[k]));
+    }
+    const float ext = std::fmax(h.x, std::fmax(h.y, h.z));
+    const float pad = ext * (1.0f / 65536.0f) + mag * (1.0f / 1048576.0f) + 1e-30f;
+    for (int k = 0; k < 3; ++k) o.halfSides[k] = h[k] + pad;
+    return o;
+}
+
+void FitOBoxes(gpugi_bvh& b) {
+    const size_t nn = b.nodes.size();
+    b.oboxes.assign(nn, OBox{});
+    // The leaf blocks below a node are contiguous (blocks are allocated in
+    // the order of the preorder walk): a node's box is fitted to the
+    // vertices of all of them.
+    std::vector<uint32_t> lo(nn), hi(nn);
+    for (size_t i = nn; i-- > 0;) {
+        const Node& nd = b.nodes[i];
+        if (nd.left & 0x80000000u) {
+            lo[i] = hi[i] = nd.left & 0x7FFFFFFFu;
+        } else {
+            lo[i] = std::min(lo[nd.left], lo[nd.right]);
+            hi[i] = std::max(hi[nd.left], hi[nd.right]);
+        }
+    }
+    const unsigned nt = std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t) {
+        pool.emplace_back([&]() {
+            std::vector<V3> pts;
+            for (size_t i = next++; i < nn; i = next++) {
+                pts.clear();
+                for (uint64_t sIdx = (uint64_t)lo[i] * b.leafSize; sIdx < ((uint64_t)hi[i] + 1) * b.leafSize; ++sIdx) {
+                    const uint32_t* slot = &b.leaves[4 * sIdx];
+                    if (slot[0] == slot[1]) continue;
+                    for (int c = 0; c < 3; ++c) pts.push_back(b.Pos(slot[c]));
+                }
+                b.oboxes[i] = FitOBox(pts);
+            }
+        });
+    }
+    for (auto& th : pool) th.join();
+}
+
 }  // namespace
 
 extern "C" {
@@ -876,7 +1018,7 @@ int gpugi_bvh_build(const float* positions, uint32_t numVertices, const uint32_t
         g_lastError = "leafSize must be in [1, 64]";
         return -3;
     }
-    if (buildMethod > GPUGI_BUILD_LDS || fitMethod > GPUGI_FIT_ELLIPSOID) {
+    if (buildMethod > GPUGI_BUILD_LDS || fitMethod > GPUGI_FIT_OBOX) {
         g_lastError = "unknown build or fit method";
         return -4;
     }
@@ -905,6 +1047,7 @@ int gpugi_bvh_build(const float* positions, uint32_t numVertices, const uint32_t
         }
         AssignEscapes(*b);
         if (fitMethod == GPUGI_FIT_ELLIPSOID) FitEllipsoids(*b, seed);
+        if (fitMethod == GPUGI_FIT_OBOX) FitOBoxes(*b);
         *out = b.release();
         return 0;
     } catch (const std::exception& e) {
@@ -927,7 +1070,17 @@ int gpugi_bvh_info(const gpugi_bvh* b, uint32_t* numNodes, uint32_t* numLeafBloc
 int gpugi_bvh_export(const gpugi_bvh* b, float* hierarchy, int32_t* slots, uint32_t* parents) {
     if (!b) return -1;
     const size_t nn = b->nodes.size();
-    if (hierarchy) {
+    if (hierarchy && b->boundsKind == GPUGI_FIT_OBOX) {
+        // Scene::TreeNode<OBox>: {center, firstChild}, {sidesHalf, escape}, rotationInv
+        for (size_t i = 0; i < nn; ++i) {
+            float* o = hierarchy + 12 * i;
+            const OBox& ob = b->oboxes[i];
+            uint32_t fc = b->nodes[i].left, esc = b->escapes[i];
+            o[0] = ob.center.x; o[1] = ob.center.y; o[2] = ob.center.z; std::memcpy(&o[3], &fc, 4);
+            o[4] = ob.halfSides.x; o[5] = ob.halfSides.y; o[6] = ob.halfSides.z; std::memcpy(&o[7], &esc, 4);
+            for (int k = 0; k < 4; ++k) o[8 + k] = ob.qInv[k];
+        }
+    } else if (hierarchy) {
         for (size_t i = 0; i < nn; ++i) {
             float* o = hierarchy + 8 * i;
             V3 a, c;
@@ -1002,10 +1155,29 @@ int gpugi_bvh_write_file(const gpugi_bvh* b, const char* path) {
             bv[6 * (size_t)i + 3 + k] = c[k];
         }
     }
+    // oriented boxes: {center, halfSides, orientation quaternion x y z w}, 40 B
+    // (the fields Scene::UploadHierarchy reads, scene.cpp:113-115; the GPU
+    // node holds the conjugate)
+    std::vector<float> ob;
+    if (b->boundsKind == GPUGI_FIT_OBOX) {
+        ob.resize((size_t)nn * 10);
+        for (uint32_t i = 0; i < nn; ++i) {
+            const OBox& o = b->oboxes[i];
+            float* e = &ob[10 * (size_t)i];
+            for (int k = 0; k < 3; ++k) {
+                e[k] = o.center[k];
+                e[3 + k] = o.halfSides[k];
+                e[6 + k] = -o.qInv[k];
+            }
+            e[9] = o.qInv[3];
+        }
+    }
     const uint32_t nBlocks = (uint32_t)(b->leaves.size() / (4 * b->leafSize));
     bool ok = WriteChunk(f, "vertices", nv, 32, verts.data()) &&
-              WriteChunk(f, b->boundsKind == GPUGI_FIT_ELLIPSOID ? "bounding_ellipsoid" : "bounding_aabox", nn, 24,
-                         bv.data()) &&
+              (b->boundsKind == GPUGI_FIT_OBOX
+                   ? WriteChunk(f, "bounding_obox", nn, 40, ob.data())
+                   : WriteChunk(f, b->boundsKind == GPUGI_FIT_ELLIPSOID ? "bounding_ellipsoid" : "bounding_aabox", nn,
+                                24, bv.data())) &&
               WriteChunk(f, "hierarchy", nn, 12, hier.data()) &&
               WriteChunk(f, "triangles", nBlocks, 16 * b->leafSize, b->leaves.data()) &&
               (b->materials.empty() ||
@@ -1039,7 +1211,7 @@ int gpugi_bvh_read_file(const char* path, gpugi_bvh** out) {
     }
     std::unique_ptr<gpugi_bvh> b(new gpugi_bvh());
     std::vector<uint32_t> hier;
-    std::vector<float> bv;
+    std::vector<float> bv, ob;
     bool haveBV = false, haveTris = false, haveHier = false;
     NamedArray h;
     int rc = 0;
@@ -1090,6 +1262,13 @@ int gpugi_bvh_read_file(const char* path, gpugi_bvh** out) {
             bv.resize((size_t)h.numElements * 6);
             std::memcpy(bv.data(), data.data(), bytes);
             haveBV = true;
+        } else if (name == "bounding_obox") {
+            if (h.elementSize != 40) { rc = -4; g_lastError = "oriented box element must be 40 bytes"; break; }
+            b->boundsKind = GPUGI_FIT_OBOX;
+            ob.resize((size_t)h.numElements * 10);
+            std::memcpy(ob.data(), data.data(), bytes);
+            bv.assign((size_t)h.numElements * 6, 0.0f);
+            haveBV = true;
         } else if (name == "triangles") {
             if (h.elementSize == 0 || h.elementSize % 16 != 0) { rc = -4; g_lastError = "triangles block size"; break; }
             b->leafSize = h.elementSize / 16;  // leaf size comes from the file
@@ -1114,6 +1293,19 @@ int gpugi_bvh_read_file(const char* path, gpugi_bvh** out) {
     b->parents.resize(nn);
     b->boxes.resize(nn);
     if (b->boundsKind == GPUGI_FIT_ELLIPSOID) b->ellipsoids.resize(nn);
+    if (b->boundsKind == GPUGI_FIT_OBOX) {
+        b->oboxes.resize(nn);
+        for (size_t i = 0; i < nn; ++i) {
+            const float* e = &ob[10 * i];
+            OBox& o = b->oboxes[i];
+            for (int k = 0; k < 3; ++k) {
+                o.center[k] = e[k];
+                o.halfSides[k] = e[3 + k];
+                o.qInv[k] = -e[6 + k];
+            }
+            o.qInv[3] = e[9];
+        }
+    }
     for (size_t i = 0; i < nn; ++i) {
         b->parents[i] = hier[3 * i];
         b->nodes[i].left = hier[3 * i + 1];

@@ -49,7 +49,7 @@ struct IVec2 {
     IVec2() = default;
     IVec2(int a, int b) : x(a), y(b) {}
 };
-enum class Types3D { BOX, ELLIPSOID };
+enum class Types3D { BOX, ELLIPSOID, OBOX };
 }  // namespace ei
 #endif
 

@@ -78,8 +78,10 @@ Scene::Scene(gpugi_ctx* ctx, const std::string& file) : m_ctx(ctx) {
     std::unique_ptr<gpugi_bvh, void (*)(gpugi_bvh*)> guard(bvh, gpugi_bvh_free);
     uint32_t boundsKind = 0;
     gpugi_bvh_info(bvh, &m_numNodes, &m_numLeafBlocks, &m_leafSize, &boundsKind, &m_maxDepth);
-    m_bvhType = boundsKind == GPUGI_FIT_ELLIPSOID ? ei::Types3D::ELLIPSOID : ei::Types3D::BOX;
-    std::vector<float> hierarchy((size_t)m_numNodes * 8);
+    m_bvhType = boundsKind == GPUGI_FIT_ELLIPSOID ? ei::Types3D::ELLIPSOID
+                : boundsKind == GPUGI_FIT_OBOX    ? ei::Types3D::OBOX
+                                                  : ei::Types3D::BOX;
+    std::vector<float> hierarchy((size_t)m_numNodes * (boundsKind == GPUGI_FIT_OBOX ? 12 : 8));
     std::vector<int32_t> slots((size_t)m_numLeafBlocks * m_leafSize * 4);
     gpugi_bvh_export(bvh, hierarchy.data(), slots.data(), nullptr);
     gpugi_bvh_vertices(bvh, &m_numVertices, nullptr);
@@ -133,6 +135,10 @@ Scene::Scene(gpugi_ctx* ctx, const std::string& file) : m_ctx(ctx) {
         if (m_bvhType == ei::Types3D::BOX) {
             m_boxMin = ei::Vec3(r[0], r[1], r[2]);
             m_boxMax = ei::Vec3(r[4], r[5], r[6]);
+        } else if (m_bvhType == ei::Types3D::OBOX) {  // a cube around the oriented root box
+            const float e = std::sqrt(r[4] * r[4] + r[5] * r[5] + r[6] * r[6]);
+            m_boxMin = ei::Vec3(r[0] - e, r[1] - e, r[2] - e);
+            m_boxMax = ei::Vec3(r[0] + e, r[1] + e, r[2] + e);
         } else {
             m_boxMin = ei::Vec3(r[0] - r[4], r[1] - r[5], r[2] - r[6]);
             m_boxMax = ei::Vec3(r[0] + r[4], r[1] + r[5], r[2] + r[6]);
@@ -155,7 +161,10 @@ Scene::Scene(gpugi_ctx* ctx, const std::string& file) : m_ctx(ctx) {
 Scene::~Scene() { gpugi_scene_destroy(m_scene); }
 
 const char* Scene::GetBvhTypeDefineString() const {
-    return m_bvhType == ei::Types3D::ELLIPSOID ? "#define BOUNDINGBOX_ELLIPSOID\n" : "#define BOUNDINGBOX_BOX\n";
+    // Scene::GetBvhTypeDefineString (scene.cpp:66-72): AABOX_BVH / OBOX_BVH
+    return m_bvhType == ei::Types3D::ELLIPSOID ? "#define BOUNDINGBOX_ELLIPSOID\n"
+           : m_bvhType == ei::Types3D::OBOX    ? "#define OBOX_BVH\n"
+                                               : "#define BOUNDINGBOX_BOX\n";
 }
 
 void Scene::AddPointLight(const PointLight& light) {

@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(128) k_shadow(RenderConst rc, ShadowSoA Q, int
 // Launch shapes and launches of the walkers for a scene: group walks when the
 // context's trace mode is 3 or 4, else lane walks with staged top nodes.
 struct Walkers {
-    bool ell = false;
+    int bounds = 0;  // node kind: 0 box, 1 ellipsoid, 2 oriented box
     uint32_t groupBelowE = 0, groupBelowS = 0;  // queue lengths below which groups walk
     WalkerLaunch LE, LS;
 };
@@ -1716,7 +1716,8 @@ GPUGI_D void persistent_walks_multi(uint32_t n, unsigned long long* work, uint32
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
             const bool done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? walk_step<ANY_HIT, 1>(w, *sc, err)
-                                                                      : walk_step<ANY_HIT, 0>(w, *sc, err);
+                              : sc->boundsKind == GPUGI_BOUNDS_OBOX    ? walk_step<ANY_HIT, 2>(w, *sc, err)
+                                                                       : walk_step<ANY_HIT, 0>(w, *sc, err);
             if (done) {
                 finish(ray, w.slot, w.len, w.u, w.v);
                 active = false;
@@ -1958,9 +1959,11 @@ static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheByt
 }
 
 static gpugi_status walkers_config(gpugi_ctx* ctx, const gpugi_scene* sc, Walkers& W) {
-    W.ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    const void* ke = W.ell ? (const void*)k_extend<1> : (const void*)k_extend<0>;
-    const void* ks = W.ell ? (const void*)k_shadow<1> : (const void*)k_shadow<0>;
+    W.bounds = (int)sc->dev.boundsKind;
+    const void* ke = W.bounds == 1 ? (const void*)k_extend<1>
+                     : W.bounds == 2 ? (const void*)k_extend<2> : (const void*)k_extend<0>;
+    const void* ks = W.bounds == 1 ? (const void*)k_shadow<1>
+                     : W.bounds == 2 ? (const void*)k_shadow<2> : (const void*)k_shadow<0>;
     gpugi_status st = walker_launch_config(ctx, sc, ke, 1ull << 40, ctx->renderSharedNodes, W.LE);
     if (!st) st = walker_launch_config(ctx, sc, ks, 1ull << 40, ctx->renderSharedNodes, W.LS);
     // group walks while fewer rays than twice the resident lanes are queued
@@ -1976,20 +1979,22 @@ static gpugi_status walkers_config(gpugi_ctx* ctx, const gpugi_scene* sc, Walker
 static void launch_extend(gpugi_ctx* ctx, const Walkers& W, const RenderConst& rc, const PathSoA& A, const HitSoA& H,
                           int depth) {
     const WalkerLaunch& L = W.LE;
-    if (W.ell) k_extend<1><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage, W.groupBelowE);
+    if (W.bounds == 1) k_extend<1><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage, W.groupBelowE);
+    else if (W.bounds == 2) k_extend<2><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage, W.groupBelowE);
     else k_extend<0><<<L.grid, 128, L.smem, ctx->stream>>>(rc, A, H, depth, L.stage, W.groupBelowE);
 }
 
 static void launch_shadow(gpugi_ctx* ctx, const Walkers& W, const RenderConst& rc, const ShadowSoA& Q, int depth) {
     const WalkerLaunch& L = W.LS;
-    if (W.ell) k_shadow<1><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage, W.groupBelowS);
+    if (W.bounds == 1) k_shadow<1><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage, W.groupBelowS);
+    else if (W.bounds == 2) k_shadow<2><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage, W.groupBelowS);
     else k_shadow<0><<<L.grid, 128, L.smem, ctx->stream>>>(rc, Q, depth, L.stage, W.groupBelowS);
 }
 
 // One chunk of `samples` iterations of a pass.
 static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderConst rc, uint32_t pass) {
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
-    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    const int bounds = (int)sc->dev.boundsKind;
     Walkers W;
     gpugi_status cst = walkers_config(ctx, sc, W);
     if (cst) return cst;
@@ -2064,7 +2069,8 @@ static gpugi_status render_chunk(gpugi_ctx* ctx, const gpugi_scene* sc, RenderCo
     } else if (pass == GPUGI_PASS_LT) {
         k_light_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A, false);
         if ((st = bounces(1))) return st;
-        if (ell) k_show_light_samples<1><<<ctx->numSMs, 128, 0, ctx->stream>>>(rc);
+        if (bounds == 1) k_show_light_samples<1><<<ctx->numSMs, 128, 0, ctx->stream>>>(rc);
+        else if (bounds == 2) k_show_light_samples<2><<<ctx->numSMs, 128, 0, ctx->stream>>>(rc);
         else k_show_light_samples<0><<<ctx->numSMs, 128, 0, ctx->stream>>>(rc);
     } else {
         k_light_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A, true);

@@ -146,7 +146,8 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     *out = nullptr;
     if (!hierarchy || !slots || !positions || numNodes == 0 || numSlots == 0 || numVertices == 0)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "empty scene: hierarchy, slots and positions are required");
-    if (boundsKind > GPUGI_BOUNDS_ELLIPSOID) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown bounds kind");
+    if (boundsKind > GPUGI_BOUNDS_OBOX) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "unknown bounds kind");
+    const size_t nf = boundsKind == GPUGI_BOUNDS_OBOX ? 12 : 8;  // floats per node
     if (leafSize == 0 || leafSize > 32 || numSlots % leafSize != 0)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "leafSize must be in [1, 32] and divide numSlots");
     if (numNodes >= 0x80000000u) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "too many nodes");
@@ -176,15 +177,15 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     }
     // Escape tree: children and escapes point strictly forward (preorder), so
     // every walk terminates within numNodes steps and stays in bounds.
-    std::vector<float> nodes(hierarchy, hierarchy + 8 * (size_t)numNodes);
+    std::vector<float> nodes(hierarchy, hierarchy + nf * (size_t)numNodes);
     for (uint32_t i = 0; i < numNodes; ++i) {
-        uint32_t child = bits_of(hierarchy[8 * (size_t)i + 3]);
-        uint32_t esc = bits_of(hierarchy[8 * (size_t)i + 7]);
+        uint32_t child = bits_of(hierarchy[nf * i + 3]);
+        uint32_t esc = bits_of(hierarchy[nf * i + 7]);
         if (child & LEAF_FLAG) {
             uint32_t blk = child & 0x7FFFFFFFu;
             if (blk >= numBlocks) return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "leaf block index out of range");
             uint32_t enc = LEAF_FLAG | (counts[blk] << LEAF_COUNT_SHIFT) | blk;
-            std::memcpy(&nodes[8 * (size_t)i + 3], &enc, 4);
+            std::memcpy(&nodes[nf * i + 3], &enc, 4);
         } else if (child <= i || child >= numNodes) {
             return fail(ctx, GPUGI_ERROR_INVALID_SCENE, "firstChild must point forward to a node (preorder)");
         }
@@ -193,7 +194,9 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     }
 
     std::vector<uint32_t> nodeMap;  // uploaded index -> device index (empty: the same)
-    const uint32_t topNodes = relayout_nodes(nodes, numNodes, ctx->sharedNodes, nodeMap);
+    // oriented-box nodes keep the preorder layout (no top-level staging)
+    const uint32_t topNodes =
+        boundsKind == GPUGI_BOUNDS_OBOX ? 0u : relayout_nodes(nodes, numNodes, ctx->sharedNodes, nodeMap);
     // Ellipsoid nodes travel as {center, firstChild}, {1 / (radii + 1e-15), escape}:
     // the node test then multiplies where the virtual-ellipsoid arithmetic
     // divides (the guard is the shader's, intersectiontests.glsl:29).
@@ -219,7 +222,7 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     };
     gpugi_status st;
     const float4* dNodes;
-    if ((st = upload(ctx, sc, reinterpret_cast<const float4*>(nodes.data()), 2 * (size_t)numNodes, &dNodes)))
+    if ((st = upload(ctx, sc, reinterpret_cast<const float4*>(nodes.data()), nf / 4 * (size_t)numNodes, &dNodes)))
         return cleanup(st);
     const int4* dSlots;
     if ((st = upload(ctx, sc, reinterpret_cast<const int4*>(slots), numSlots, &dSlots))) return cleanup(st);

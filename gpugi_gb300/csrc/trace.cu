@@ -11,20 +11,20 @@
 
 namespace gpugi {
 
-// Picks a kernel instantiation at run time: f receives (any hit, bounds kind,
-// triangle test) as integral constants and returns the kernel's address.
-template <typename F>
-static auto pick_variant(bool anyHit, bool ell, bool wt, F f) {
-    using B0 = std::false_type;
-    using B1 = std::true_type;
+// Picks a kernel instantiation at run time: f receives (any hit, bounds kind
+// 0/1/2, triangle test) as integral constants and returns the kernel's address.
+template <typename A, typename F>
+static auto pick_bounds(A a, int bounds, bool wt, F f) {
     using I0 = std::integral_constant<int, 0>;
     using I1 = std::integral_constant<int, 1>;
-    if (anyHit) {
-        if (ell) return wt ? f(B1{}, I1{}, I1{}) : f(B1{}, I1{}, I0{});
-        return wt ? f(B1{}, I0{}, I1{}) : f(B1{}, I0{}, I0{});
-    }
-    if (ell) return wt ? f(B0{}, I1{}, I1{}) : f(B0{}, I1{}, I0{});
-    return wt ? f(B0{}, I0{}, I1{}) : f(B0{}, I0{}, I0{});
+    using I2 = std::integral_constant<int, 2>;
+    if (bounds == GPUGI_BOUNDS_ELLIPSOID) return wt ? f(a, I1{}, I1{}) : f(a, I1{}, I0{});
+    if (bounds == GPUGI_BOUNDS_OBOX) return wt ? f(a, I2{}, I1{}) : f(a, I2{}, I0{});
+    return wt ? f(a, I0{}, I1{}) : f(a, I0{}, I0{});
+}
+template <typename F>
+static auto pick_variant(bool anyHit, int bounds, bool wt, F f) {
+    return anyHit ? pick_bounds(std::true_type{}, bounds, wt, f) : pick_bounds(std::false_type{}, bounds, wt, f);
 }
 
 template <int BOUNDS, int TRI>
@@ -138,8 +138,7 @@ gpugi_status launch_trace_persistent(gpugi_ctx* ctx, const gpugi_scene* sc, bool
     if (n == 0) return GPUGI_OK;
     unsigned long long* counter = reinterpret_cast<unsigned long long*>(ctx->scratch);
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
-    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    auto k = pick_variant(anyHit, ell, sc->dev.triangleTest != 0, [](auto A, auto B, auto T) {
+    auto k = pick_variant(anyHit, (int)sc->dev.boundsKind, sc->dev.triangleTest != 0, [](auto A, auto B, auto T) {
         return &k_trace_persistent<decltype(A)::value, decltype(B)::value, decltype(T)::value>;
     });
     WalkerLaunch L;
@@ -169,11 +168,10 @@ __global__ void __launch_bounds__(256) k_trace_root_filter(
         const float3 d = make_float3(__ldg(dx + i), __ldg(dy + i), __ldg(dz + i));
         const float len = __ldg(tmax + i);
         const float4 a = __ldg(s.nodes), b = __ldg(s.nodes + 1);
+        const float4 c = BOUNDS == 2 ? __ldg(s.nodes + 2) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         float firstHit;
-        bool hit;
-        if (BOUNDS == 0)
-            hit = intersect_box<TRI != 0>(o, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a, b, firstHit);
-        else hit = intersect_ellipsoid(o, d, a, b, firstHit);
+        const bool hit = bounds_test<BOUNDS, TRI != 0>(o, d, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a,
+                                                       b, c, firstHit);
         pass = hit && firstHit <= len;
         if (!pass) {
             if (ANY_HIT) {
@@ -212,6 +210,7 @@ __global__ void __launch_bounds__(256) k_trace_root_filter4(
         const float4 X = __ldg(ox + i), Y = __ldg(oy + i), Z = __ldg(oz + i);
         const float4 DX = __ldg(dx + i), DY = __ldg(dy + i), DZ = __ldg(dz + i), L = __ldg(tmax + i);
         const float4 a = __ldg(s.nodes), b = __ldg(s.nodes + 1);
+        const float4 c = BOUNDS == 2 ? __ldg(s.nodes + 2) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w}, zs[4] = {Z.x, Z.y, Z.z, Z.w};
         const float dxs[4] = {DX.x, DX.y, DX.z, DX.w}, dys[4] = {DY.x, DY.y, DY.z, DY.w},
                     dzs[4] = {DZ.x, DZ.y, DZ.z, DZ.w}, ls[4] = {L.x, L.y, L.z, L.w};
@@ -219,10 +218,8 @@ __global__ void __launch_bounds__(256) k_trace_root_filter4(
         for (int k = 0; k < 4; ++k) {
             const float3 o = make_float3(xs[k], ys[k], zs[k]), d = make_float3(dxs[k], dys[k], dzs[k]);
             float firstHit;
-            bool hit;
-            if (BOUNDS == 0)
-                hit = intersect_box<TRI != 0>(o, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)), a, b, firstHit);
-            else hit = intersect_ellipsoid(o, d, a, b, firstHit);
+            const bool hit = bounds_test<BOUNDS, TRI != 0>(o, d, make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z)),
+                                                           a, b, c, firstHit);
             if (hit && firstHit <= ls[k]) pass |= 1u << k;
         }
         if (ANY_HIT) {
@@ -369,7 +366,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
                                       unsigned long long* counters, cudaStream_t stream) {
     if (n == 0) return GPUGI_OK;
     cudaStream_t cs = stream ? stream : ctx->stream;
-    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
+    const int ell = (int)sc->dev.boundsKind;  // bounds kind: 0 box, 1 ellipsoid, 2 oriented box
     const bool wt = sc->dev.triangleTest != 0;
     // four rays per thread with 16-B accesses when every array allows it
     auto al = [](const void* p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; };
@@ -379,37 +376,25 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
     if (n4) {
         const unsigned grid4 = (unsigned)((n4 + 255) / 256);
         auto f4 = [](const float* p) { return reinterpret_cast<const float4*>(p); };
-#define GPUGI_FILTER4_ON(A, B)                                                                                        \
-    (wt ? k_trace_root_filter4<A, B, 1> : k_trace_root_filter4<A, B, 0>)<<<grid4, 256, 0, cs>>>( \
-        sc->dev, f4(ox), f4(oy), f4(oz), f4(dx), f4(dy), f4(dz), f4(tmax), n4, reinterpret_cast<int4*>(slot),          \
-        reinterpret_cast<float4*>(t), reinterpret_cast<float4*>(u), reinterpret_cast<float4*>(v),                     \
-        reinterpret_cast<uchar4*>(occluded), queue, counters)
-        if (!ell) {
-            if (anyHit) GPUGI_FILTER4_ON(true, 0);
-            else GPUGI_FILTER4_ON(false, 0);
-        } else {
-            if (anyHit) GPUGI_FILTER4_ON(true, 1);
-            else GPUGI_FILTER4_ON(false, 1);
-        }
-#undef GPUGI_FILTER4_ON
+        auto kf = pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {
+            return &k_trace_root_filter4<decltype(A)::value, decltype(B)::value, decltype(T)::value>;
+        });
+        kf<<<grid4, 256, 0, cs>>>(sc->dev, f4(ox), f4(oy), f4(oz), f4(dx), f4(dy), f4(dz), f4(tmax), n4,
+                                  reinterpret_cast<int4*>(slot), reinterpret_cast<float4*>(t),
+                                  reinterpret_cast<float4*>(u), reinterpret_cast<float4*>(v),
+                                  reinterpret_cast<uchar4*>(occluded), queue, counters);
     }
     if (head < n) {
         const uint64_t m = n - head;
         const unsigned grid1 = (unsigned)((m + 255) / 256);
         auto sh = [&](const float* p) { return p + head; };
-#define GPUGI_FILTER_ON(A, B)                                                                                        \
-    (wt ? k_trace_root_filter<A, B, 1> : k_trace_root_filter<A, B, 0>)<<<grid1, 256, 0, cs>>>( \
-        sc->dev, sh(ox), sh(oy), sh(oz), sh(dx), sh(dy), sh(dz), sh(tmax), m, slot ? slot + head : nullptr,            \
-        t ? t + head : nullptr, u ? u + head : nullptr, v ? v + head : nullptr, occluded ? occluded + head : nullptr, \
-        queue, counters, (uint32_t)head)
-        if (!ell) {
-            if (anyHit) GPUGI_FILTER_ON(true, 0);
-            else GPUGI_FILTER_ON(false, 0);
-        } else {
-            if (anyHit) GPUGI_FILTER_ON(true, 1);
-            else GPUGI_FILTER_ON(false, 1);
-        }
-#undef GPUGI_FILTER_ON
+        auto kf = pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {
+            return &k_trace_root_filter<decltype(A)::value, decltype(B)::value, decltype(T)::value>;
+        });
+        kf<<<grid1, 256, 0, cs>>>(sc->dev, sh(ox), sh(oy), sh(oz), sh(dx), sh(dy), sh(dz), sh(tmax), m,
+                                  slot ? slot + head : nullptr, t ? t + head : nullptr, u ? u + head : nullptr,
+                                  v ? v + head : nullptr, occluded ? occluded + head : nullptr, queue, counters,
+                                  (uint32_t)head);
     }
     if (ctx->traceMode >= 3) {
         auto kg = ctx->traceMode == 3
@@ -474,8 +459,7 @@ gpugi_status launch_trace_stats(gpugi_ctx* ctx, const gpugi_scene* sc, const flo
                                 const float* tmax, uint64_t n, uint32_t anyHit, unsigned long long* sums) {
     if (n == 0) return GPUGI_OK;
     const unsigned grid = (unsigned)((n + 255) / 256);
-    const bool ell = sc->dev.boundsKind == GPUGI_BOUNDS_ELLIPSOID;
-    auto k = pick_variant(anyHit != 0, ell, sc->dev.triangleTest != 0, [](auto A, auto B, auto T) {
+    auto k = pick_variant(anyHit != 0, (int)sc->dev.boundsKind, sc->dev.triangleTest != 0, [](auto A, auto B, auto T) {
         return &k_trace_stats<decltype(B)::value, decltype(A)::value, decltype(T)::value>;
     });
     k<<<grid, 256, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, sums, ctx->errWord);
@@ -495,7 +479,7 @@ gpugi_status launch_trace_closest(gpugi_ctx* ctx, const gpugi_scene* sc, const f
     if (ctx->traceMode == 1)
         return launch_trace_persistent(ctx, sc, false, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, nullptr);
     const uint32_t block = ctx->traceBlock;
-    auto k = pick_variant(false, sc->dev.boundsKind != GPUGI_BOUNDS_AABB, sc->dev.triangleTest != 0,
+    auto k = pick_variant(false, (int)sc->dev.boundsKind, sc->dev.triangleTest != 0,
                           [](auto, auto B, auto T) { return &k_trace_closest<decltype(B)::value, decltype(T)::value>; });
     k<<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v,
                                                      ctx->errWord);
@@ -515,7 +499,7 @@ gpugi_status launch_trace_any(gpugi_ctx* ctx, const gpugi_scene* sc, const float
         return launch_trace_persistent(ctx, sc, true, ox, oy, oz, dx, dy, dz, tmax, n, nullptr, nullptr, nullptr,
                                        nullptr, occluded);
     const uint32_t block = ctx->traceBlock;
-    auto k = pick_variant(true, sc->dev.boundsKind != GPUGI_BOUNDS_AABB, sc->dev.triangleTest != 0,
+    auto k = pick_variant(true, (int)sc->dev.boundsKind, sc->dev.triangleTest != 0,
                           [](auto, auto B, auto T) { return &k_trace_any<decltype(B)::value, decltype(T)::value>; });
     k<<<grid_for(n, block), block, 0, ctx->stream>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, n, occluded,
                                                      ctx->errWord);

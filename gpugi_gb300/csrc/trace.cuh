@@ -73,6 +73,42 @@ GPUGI_D bool intersect_ellipsoid(float3 ro, float3 rd, float4 c, float4 ir, floa
     return X::add(X::add(-phalf, rad), t) >= 0.0f;
 }
 
+// rotate(x, q) (intersectiontests.glsl:82-89) in the shader's operation order.
+GPUGI_D float3 qrotate(float3 x, float4 q) {
+    const float3 t = X::cross(make_float3(q.x, q.y, q.z), x);
+    const float3 u = make_float3(X::sub(X::add(X::mul(q.w, t.x), X::mul(q.y, t.z)), X::mul(q.z, t.y)),
+                                 X::sub(X::add(X::mul(q.w, t.y), X::mul(q.z, t.x)), X::mul(q.x, t.z)),
+                                 X::sub(X::add(X::mul(q.w, t.z), X::mul(q.x, t.y)), X::mul(q.y, t.x)));
+    return X::add3(x, X::scale(2.0f, u));
+}
+
+// FetchIntersectOBoxNode (intersectiontests.glsl:114-128) on the 48-B node
+// {center | child}, {sidesHalf | escape}, rotationInv: the ray is rotated
+// into the box frame (origin relative to the centre), its direction
+// inverted there, and the box [-sidesHalf, sidesHalf] tested with
+// IntersectBox (ROBUST: the watertight mode's box test).
+template <bool ROBUST = false>
+GPUGI_D bool intersect_obox(float3 ro, float3 rd, float4 a, float4 b, float4 rotationInv, float& firstHit) {
+    const float3 o = qrotate(X::sub3(ro, xyz(a)), rotationInv);
+    const float3 d = qrotate(rd, rotationInv);
+    const float3 inv = make_float3(X::rcp(d.x), X::rcp(d.y), X::rcp(d.z));
+    return intersect_box<ROBUST>(o, inv, make_float4(-b.x, -b.y, -b.z, 0.0f), b, firstHit);
+}
+
+// Node layouts: AABB and ellipsoid nodes take 2 float4, oriented boxes 3.
+template <int BOUNDS>
+constexpr uint32_t node_stride() {
+    return BOUNDS == 2 ? 3u : 2u;
+}
+// The bounds test of a node kind (0 box, 1 ellipsoid, 2 oriented box); c is
+// the oriented box's third texel (unused otherwise).
+template <int BOUNDS, bool ROBUST>
+GPUGI_D bool bounds_test(float3 o, float3 d, float3 inv, float4 a, float4 b, float4 c, float& firstHit) {
+    if (BOUNDS == 0) return intersect_box<ROBUST>(o, inv, a, b, firstHit);
+    if (BOUNDS == 1) return intersect_ellipsoid(o, d, a, b, firstHit);
+    return intersect_obox<ROBUST>(o, d, a, b, c, firstHit);
+}
+
 // IntersectTriangle (intersectiontests.glsl:63-79) on the precomputed record
 // {p0, e0, e1, n}. Returns hit distance and the two barycentrics (y, z).
 GPUGI_D bool intersect_triangle_v(float3 o, float3 d, float4 a, float4 b, float4 c, float& hit, float& by,
@@ -209,14 +245,14 @@ GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLe
             break;
         }
         if (COUNT) ++cnt->nodes;
-        const float4 a = __ldg(nodes + 2 * node);
-        const float4 b = __ldg(nodes + 2 * node + 1);
+        const float4* nd = nodes + node_stride<BOUNDS>() * (size_t)node;
+        const float4 a = __ldg(nd);
+        const float4 b = __ldg(nd + 1);
+        const float4 c = BOUNDS == 2 ? __ldg(nd + 2) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         const uint32_t child = __float_as_uint(a.w);
         const uint32_t escape = __float_as_uint(b.w);
         float firstHit;
-        bool hit;
-        if (BOUNDS == 0) hit = intersect_box<TRI != 0>(o, inv, a, b, firstHit);
-        else hit = intersect_ellipsoid(o, d, a, b, firstHit);
+        const bool hit = bounds_test<BOUNDS, TRI != 0>(o, d, inv, a, b, c, firstHit);
         if (hit && firstHit <= rayLength) {
             if (child & LEAF_FLAG) {
                 const uint32_t count = (child >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK;
@@ -286,6 +322,7 @@ GPUGI_D void walk_begin(WalkState& w, const DevScene& s, float3 o, float3 d, flo
 // Copy the first `count` nodes (the top tree levels, see DevScene::topNodes)
 // into shared memory. Called by every thread of a block before its walks.
 GPUGI_D void stage_top_nodes(const DevScene& s, float4* smem, uint32_t count) {
+    // oriented-box scenes stage nothing (their upload keeps the preorder layout)
     for (uint32_t i = threadIdx.x; i < 2 * count; i += blockDim.x) smem[i] = __ldg(s.nodes + i);
     __syncthreads();
 }
@@ -305,14 +342,17 @@ GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord, const
         return true;
     }
     float4 a, b, c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    constexpr uint32_t NS = node_stride<BOUNDS>();
     if (!isTri && w.node < topCount) {
-        a = top[2 * w.node];
-        b = top[2 * w.node + 1];
+        a = top[NS * w.node];
+        b = top[NS * w.node + 1];
+        if (BOUNDS == 2) c = top[NS * w.node + 2];
     } else {
-        const float4* src = isTri ? (TRI ? s.wtris : s.tris) + 3 * (size_t)w.cur : s.nodes + 2 * (size_t)w.node;
+        const float4* src =
+            isTri ? (TRI ? s.wtris : s.tris) + 3 * (size_t)w.cur : s.nodes + NS * (size_t)w.node;
         a = __ldg(src);
         b = __ldg(src + 1);
-        if (isTri) c = __ldg(src + 2);
+        if (isTri || BOUNDS == 2) c = __ldg(src + 2);
     }
     if (isTri) {
         float h, by, bz;
@@ -330,9 +370,7 @@ GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord, const
         const uint32_t child = __float_as_uint(a.w);
         const uint32_t escape = __float_as_uint(b.w);
         float firstHit;
-        bool hit;
-        if (BOUNDS == 0) hit = intersect_box<TRI != 0>(w.o, w.inv, a, b, firstHit);
-        else hit = intersect_ellipsoid(w.o, w.d, a, b, firstHit);
+        const bool hit = bounds_test<BOUNDS, TRI != 0>(w.o, w.d, w.inv, a, b, c, firstHit);
         if (hit && firstHit <= w.len) {
             if (child & LEAF_FLAG) {
                 w.cur = (child & LEAF_BLOCK_MASK) * s.leafSize;
@@ -430,13 +468,13 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
     const uint32_t p = g.node + gl;
     uint32_t next = kGroupDone, child = 0, escape = 0;
     if (p < s.numNodes) {
-        const float4 a = __ldg(s.nodes + 2 * (size_t)p), b = __ldg(s.nodes + 2 * (size_t)p + 1);
+        const float4* nd = s.nodes + node_stride<BOUNDS>() * (size_t)p;
+        const float4 a = __ldg(nd), b = __ldg(nd + 1);
+        const float4 c = BOUNDS == 2 ? __ldg(nd + 2) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         child = __float_as_uint(a.w);
         escape = __float_as_uint(b.w);
         float firstHit;
-        bool hit;
-        if (BOUNDS == 0) hit = intersect_box<TRI != 0>(g.o, g.inv, a, b, firstHit);
-        else hit = intersect_ellipsoid(g.o, g.d, a, b, firstHit);
+        const bool hit = bounds_test<BOUNDS, TRI != 0>(g.o, g.d, g.inv, a, b, c, firstHit);
         if (hit && firstHit <= g.len) next = (child & LEAF_FLAG) ? (kGroupLeaf | gl) : child;
         else next = escape ? escape : kGroupDone;
     }
@@ -499,9 +537,9 @@ GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long l
         bool done = false;
         while (!done) {
             if constexpr (MULTI)
-                done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID
-                           ? group_step<ANY_HIT, 1, G>(g, *sc, err, gl, gbase, gmask)
-                           : group_step<ANY_HIT, 0, G>(g, *sc, err, gl, gbase, gmask);
+                done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? group_step<ANY_HIT, 1, G>(g, *sc, err, gl, gbase, gmask)
+                       : sc->boundsKind == GPUGI_BOUNDS_OBOX    ? group_step<ANY_HIT, 2, G>(g, *sc, err, gl, gbase, gmask)
+                                                                : group_step<ANY_HIT, 0, G>(g, *sc, err, gl, gbase, gmask);
             else
                 done = group_step<ANY_HIT, BOUNDS, G, TRI>(g, scene, err, gl, gbase, gmask);
         }

@@ -123,7 +123,10 @@ gpugi_status gpugi_autotune(gpugi_ctx* ctx, const gpugi_scene* sc, uint32_t flag
         half = make_float3(0.5f * (root[1].x - root[0].x), 0.5f * (root[1].y - root[0].y), 0.5f * (root[1].z - root[0].z));
     } else {
         center = make_float3(root[0].x, root[0].y, root[0].z);
-        if (sc->hostRadii.size() >= 3)  // the device node holds reciprocal radii
+        if (sc->dev.boundsKind == GPUGI_BOUNDS_OBOX) {  // a cube around the oriented box
+            const float r = sqrtf(root[1].x * root[1].x + root[1].y * root[1].y + root[1].z * root[1].z);
+            half = make_float3(r, r, r);
+        } else if (sc->hostRadii.size() >= 3)  // the device node holds reciprocal radii
             half = make_float3(sc->hostRadii[0], sc->hostRadii[1], sc->hostRadii[2]);
         else
             half = make_float3(1.0f / root[1].x, 1.0f / root[1].y, 1.0f / root[1].z);

@@ -204,6 +204,7 @@ class DeviceScene:
             nn, ns = C.c_uint32(), C.c_uint32()
             ctx.check(lib().gpugi_scene_export(ctx.handle, self._h, C.byref(nn), C.byref(ns), None, None))
             self.num_nodes, self.num_slots, self.leaf_size = nn.value, ns.value, leaf_size
+            self.bounds_kind = 0
             return
         hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
         slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
@@ -219,13 +220,14 @@ class DeviceScene:
         self.num_nodes = hier.shape[0]
         self.num_slots = slots.shape[0]
         self.leaf_size = bvh.leaf_size
+        self.bounds_kind = bvh.bounds_kind
 
     def export(self):
         """The scene's hierarchy and leaf slots as a bvh.BVH (device node order)."""
         from . import bvh as B
         nn, ns = C.c_uint32(), C.c_uint32()
         self.ctx.check(lib().gpugi_scene_export(self.ctx.handle, self._h, C.byref(nn), C.byref(ns), None, None))
-        hier = np.zeros((nn.value, 8), np.float32)
+        hier = np.zeros((nn.value, 12 if self.bounds_kind == 2 else 8), np.float32)
         slots = np.zeros((ns.value, 4), np.int32)
         self.ctx.check(lib().gpugi_scene_export(self.ctx.handle, self._h, C.byref(nn), C.byref(ns), _ptr(hier),
                                                 _ptr(slots)))
@@ -235,7 +237,7 @@ class DeviceScene:
         left = child[inner]
         parents[left] = inner
         parents[hier[left, 7].view(np.uint32)] = inner
-        return B.BVH(hierarchy=hier, slots=slots, parents=parents, leaf_size=self.leaf_size, bounds_kind=0,
+        return B.BVH(hierarchy=hier, slots=slots, parents=parents, leaf_size=self.leaf_size, bounds_kind=self.bounds_kind,
                      max_depth=0)
 
     def set_triangle_test(self, watertight: bool) -> None:

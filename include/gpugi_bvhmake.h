@@ -35,7 +35,10 @@ extern "C" {
 typedef struct gpugi_bvh gpugi_bvh;
 
 enum gpugi_build_method { GPUGI_BUILD_KDTREE = 0, GPUGI_BUILD_SWEEP = 1, GPUGI_BUILD_LDS = 2 };
-enum gpugi_fit_method { GPUGI_FIT_AABOX = 0, GPUGI_FIT_ELLIPSOID = 1 };
+/* GPUGI_FIT_OBOX (an addition; bvhmake fits boxes and ellipsoids only):
+ * oriented boxes, the nodes of the reference's OBOX_BVH walk, fitted bottom
+ * up along the principal axes of each node's points. */
+enum gpugi_fit_method { GPUGI_FIT_AABOX = 0, GPUGI_FIT_ELLIPSOID = 1, GPUGI_FIT_OBOX = 2 };
 
 /* Build a hierarchy over `numTriangles` triangles, each 4 uint32
  * {v0, v1, v2, material}, indexing `positions` (3 floats per vertex).
@@ -46,13 +49,15 @@ int gpugi_bvh_build(const float* positions, uint32_t numVertices, const uint32_t
                     uint32_t numTriangles, uint32_t buildMethod, uint32_t fitMethod,
                     uint32_t leafSize, uint64_t seed, gpugi_bvh** out);
 
-/* Sizes of the built hierarchy. boundsKind: 0 = AABB, 1 = ellipsoid. */
+/* Sizes of the built hierarchy. boundsKind: 0 = AABB, 1 = ellipsoid, 2 = oriented box. */
 int gpugi_bvh_info(const gpugi_bvh* bvh, uint32_t* numNodes, uint32_t* numLeafBlocks,
                    uint32_t* leafSize, uint32_t* boundsKind, uint32_t* maxDepth);
 
 /* Export in the GPU layout of Scene::TreeNode<Box> (gpugi/scene/scene.hpp:30-38):
  * 8 floats per node {min.xyz, firstChild bits, max.xyz, escape bits}
- * (ellipsoid: {center.xyz, firstChild, radii.xyz, escape}), leafSize
+ * (ellipsoid: {center.xyz, firstChild, radii.xyz, escape}; oriented box:
+ * 12 floats, Scene::TreeNode<OBox> (scene.hpp:40-49) {center.xyz, firstChild,
+ * sidesHalf.xyz, escape, rotationInv quaternion x, y, z, w}), leafSize
  * int32x4 slots per leaf block {v0, v1, v2, material}, invalid = {0,0,0,0},
  * and optionally the parent index of every node (may be NULL). */
 int gpugi_bvh_export(const gpugi_bvh* bvh, float* hierarchy, int32_t* slots, uint32_t* parents);

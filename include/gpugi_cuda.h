@@ -50,7 +50,7 @@ typedef enum gpugi_status {
 #define GPUGI_DEVERR_BUILD 0x8u           /* the GPU hierarchy build found an inconsistent tree */
 #define GPUGI_DEVERR_HIERARCHY 0x10u      /* a hierarchy-importance walk to the root exceeded the node count */
 
-enum gpugi_bounds_kind { GPUGI_BOUNDS_AABB = 0, GPUGI_BOUNDS_ELLIPSOID = 1 };
+enum gpugi_bounds_kind { GPUGI_BOUNDS_AABB = 0, GPUGI_BOUNDS_ELLIPSOID = 1, GPUGI_BOUNDS_OBOX = 2 };
 
 typedef struct gpugi_ctx gpugi_ctx;
 typedef struct gpugi_scene gpugi_scene;
@@ -91,7 +91,13 @@ const char* gpugi_version(void);
 /* Upload a scene in the layout of gpugi's GPU buffers.
  *   hierarchy   8 floats per node: {min.xyz, firstChild bits, max.xyz, escape bits}
  *               (Scene::TreeNode<Box>, gpugi/scene/scene.hpp:30-38); for
- *               GPUGI_BOUNDS_ELLIPSOID {center.xyz, firstChild, radii.xyz, escape}
+ *               GPUGI_BOUNDS_ELLIPSOID {center.xyz, firstChild, radii.xyz, escape};
+ *               for GPUGI_BOUNDS_OBOX 12 floats per node, Scene::TreeNode<OBox>
+ *               (scene.hpp:40-49): {center.xyz, firstChild, sidesHalf.xyz,
+ *               escape, rotationInv quaternion x, y, z, w}, walked as the
+ *               reference's OBOX_BVH path (FetchIntersectOBoxNode,
+ *               intersectiontests.glsl:114-128). The hierarchy-importance
+ *               pass takes AABB hierarchies only.
  *   slots       4 int32 per leaf slot {v0, v1, v2, material}; leafSize slots
  *               per block; {0,0,0,0} (v0 == v1) ends a block early
  *   positions   3 floats per vertex (RGB32F, gpugi/scene/scene.cpp:87)
@@ -121,7 +127,7 @@ gpugi_status gpugi_scene_build(gpugi_ctx* ctx, const float* positions, uint32_t 
                                const gpugi_material* materials, uint32_t numMaterials, uint32_t leafSize,
                                gpugi_scene** out);
 
-/* The scene's hierarchy (8 floats per node, leaf words {0x80000000 | block})
+/* The scene's hierarchy (8 floats per node, 12 for oriented boxes; leaf words {0x80000000 | block})
  * in device node order and its leaf slots (4 int32 each). Call with
  * hierarchy and slots NULL for the sizes. */
 gpugi_status gpugi_scene_export(gpugi_ctx* ctx, const gpugi_scene* scene, uint32_t* numNodes, uint32_t* numSlots,

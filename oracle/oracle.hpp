@@ -5,7 +5,9 @@
 //   HierachyBuffer        2 texels (vec4) per node: {min.xyz | firstChild bits},
 //                         {max.xyz | escape bits}   (gpugi/scene/scene.hpp:30-38)
 //                         ellipsoid bounds use {center.xyz | firstChild},
-//                         {radii.xyz | escape} with the same stride.
+//                         {radii.xyz | escape} with the same stride; oriented
+//                         boxes 3 texels {center | firstChild}, {sidesHalf |
+//                         escape}, rotationInv (scene.hpp:40-49).
 //   TriangleBuffer        one ivec4 {v0, v1, v2, material} per leaf slot,
 //                         leafSize slots per leaf block  (scene.hpp:64-68)
 //   VertexPositionBuffer  tightly packed RGB32F, 12 bytes per vertex (scene.cpp:87)
@@ -16,7 +18,7 @@
 
 namespace oracle {
 
-enum BoundsKind : uint32_t { BOUNDS_AABB = 0, BOUNDS_ELLIPSOID = 1 };
+enum BoundsKind : uint32_t { BOUNDS_AABB = 0, BOUNDS_ELLIPSOID = 1, BOUNDS_OBOX = 2 };
 
 struct Scene {
     const glsl::vec4* hierarchy = nullptr;

@@ -35,8 +35,8 @@ def lib():
             raise OSError("oracle/_ref is not built (the reference tree is absent)")
         L = C.CDLL(str(path))
         P, I, U32, U64 = C.c_void_p, C.c_int, C.c_uint32, C.c_uint64
-        L.ref_trace_closest.argtypes = [P, P, P, I] + [P] * 7 + [U64, P, P, P, P, I]
-        L.ref_trace_any.argtypes = [P, P, P, I] + [P] * 7 + [U64, P, I]
+        L.ref_trace_closest.argtypes = [P, P, P, I, I] + [P] * 7 + [U64, P, P, P, P, I]
+        L.ref_trace_any.argtypes = [P, P, P, I, I] + [P] * 7 + [U64, P, I]
         L.ref_eval.argtypes = [I, U64, P, P]
         L.ref_render_pt.argtypes = [P, P, P, P, P, I, I, I, I, P, U32, P, I, P, P, I]
         for f in (L.ref_trace_closest, L.ref_trace_any, L.ref_eval, L.ref_render_pt):
@@ -67,9 +67,9 @@ def trace_closest(bvh, positions, rays) -> dict:
     n = r[0].shape[0]
     tri = np.empty((n, 4), np.int32)
     t, u, v = (np.empty(n, np.float32) for _ in range(3))
-    rc = lib().ref_trace_closest(_p(hier), _p(slots), _p(pos), bvh.leaf_size, *[_p(a) for a in r], n, _p(tri), _p(t),
-                                 _p(u), _p(v), _threads())
-    assert rc == 0, "leaf size must be 8 or 2"
+    rc = lib().ref_trace_closest(_p(hier), _p(slots), _p(pos), bvh.leaf_size, bvh.bounds_kind, *[_p(a) for a in r], n,
+                                 _p(tri), _p(t), _p(u), _p(v), _threads())
+    assert rc == 0, "AABB trees with leaf size 8 or 2, or oriented-box trees with leaf size 8"
     return dict(triangle=tri, t=t, u=u, v=v)
 
 
@@ -80,9 +80,9 @@ def trace_any(bvh, positions, rays) -> np.ndarray:
     r = _rays(rays)
     n = r[0].shape[0]
     occ = np.empty(n, np.uint8)
-    rc = lib().ref_trace_any(_p(hier), _p(slots), _p(pos), bvh.leaf_size, *[_p(a) for a in r], n, _p(occ),
-                             _threads())
-    assert rc == 0, "leaf size must be 8 or 2"
+    rc = lib().ref_trace_any(_p(hier), _p(slots), _p(pos), bvh.leaf_size, bvh.bounds_kind, *[_p(a) for a in r], n,
+                             _p(occ), _threads())
+    assert rc == 0, "AABB trees with leaf size 8 or 2, or oriented-box trees with leaf size 8"
     return occ
 
 

@@ -6,7 +6,8 @@
 // that tests/test_ref_pinned.py calls side by side with the oracle's.
 //   ref_trace_closest / ref_trace_any   TraceRay / TraceRayAnyHit
 //                                       (gpugi/shader/traceray.glsl with AABOX_BVH,
-//                                       intersectiontests.glsl), leaf blocks of 8 or 2
+//                                       intersectiontests.glsl), leaf blocks of 8 or 2;
+//                                       with OBOX_BVH (oriented boxes), leaf blocks of 8
 //   ref_eval                            random.glsl / helper.glsl functions
 //   ref_render_pt                       pathtracer.comp's main() per pixel
 #include <cstdint>
@@ -51,6 +52,25 @@ using namespace glslref;
 #undef TRIANGLES_PER_LEAF
 }  // namespace ref_leaf2
 
+// ------------------------------------------------ oriented-box nodes (OBOX_BVH), 8-slot leaves
+namespace ref_obox8 {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 8
+#undef AABOX_BVH
+#define OBOX_BVH
+#include "helper.glsl.h"
+#include "scenedata.glsl.h"
+#include "intersectiontests.glsl.h"
+#include "random.glsl.h"
+#include "traceray.glsl.h"
+#define ANY_HIT
+#include "traceray.glsl.h"
+#undef ANY_HIT
+#undef OBOX_BVH
+#define AABOX_BVH
+#undef TRIANGLES_PER_LEAF
+}  // namespace ref_obox8
+
 // ------------------------------------------------ the path tracer, 8-slot leaves
 namespace ref_pt {
 using namespace glslref;
@@ -94,12 +114,15 @@ extern "C" {
 // ({v0, v1, v2, material}, all -1 on a miss), t, u = barycentric.y,
 // v = barycentric.z.
 int ref_trace_closest(const float* hierarchy, const int32_t* slots, const float* positions, int leafSize,
-                      const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
-                      const float* dz, const float* tmax, uint64_t n, int32_t* outTri, float* outT, float* outU,
-                      float* outV, int numThreads) {
+                      int boundsKind, const float* ox, const float* oy, const float* oz, const float* dx,
+                      const float* dy, const float* dz, const float* tmax, uint64_t n, int32_t* outTri, float* outT,
+                      float* outU, float* outV, int numThreads) {
     using namespace glslref;
-    if (leafSize != 8 && leafSize != 2) return 1;
-    if (leafSize == 8) {
+    const bool obox = boundsKind == 2;
+    if ((leafSize != 8 && leafSize != 2) || (obox && leafSize != 8) || (boundsKind != 0 && !obox)) return 1;
+    if (obox) {
+        GPUGI_REF_BIND(ref_obox8)
+    } else if (leafSize == 8) {
         GPUGI_REF_BIND(ref_leaf8)
     } else {
         GPUGI_REF_BIND(ref_leaf2)
@@ -108,12 +131,14 @@ int ref_trace_closest(const float* hierarchy, const int32_t* slots, const float*
         for (uint64_t i = b; i < e; ++i) {
             ref_leaf8::Ray r8;
             ref_leaf2::Ray r2;
-            r8.Origin = r2.Origin = vec3(ox[i], oy[i], oz[i]);
-            r8.Direction = r2.Direction = vec3(dx[i], dy[i], dz[i]);
+            ref_obox8::Ray ro;
+            r8.Origin = r2.Origin = ro.Origin = vec3(ox[i], oy[i], oz[i]);
+            r8.Direction = r2.Direction = ro.Direction = vec3(dx[i], dy[i], dz[i]);
             float rayLength = tmax[i];
             vec3 bary(-1.0f);
             ivec4 tri(-1, -1, -1, -1);
-            if (leafSize == 8) ref_leaf8::TraceRay(r8, rayLength, bary, tri);
+            if (obox) ref_obox8::TraceRay(ro, rayLength, bary, tri);
+            else if (leafSize == 8) ref_leaf8::TraceRay(r8, rayLength, bary, tri);
             else ref_leaf2::TraceRay(r2, rayLength, bary, tri);
             // the shader leaves its out parameters unwritten on a miss
             const bool hit = rayLength < tmax[i];
@@ -130,11 +155,15 @@ int ref_trace_closest(const float* hierarchy, const int32_t* slots, const float*
 }
 
 int ref_trace_any(const float* hierarchy, const int32_t* slots, const float* positions, int leafSize,
-                  const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
-                  const float* dz, const float* tmax, uint64_t n, uint8_t* occluded, int numThreads) {
+                  int boundsKind, const float* ox, const float* oy, const float* oz, const float* dx,
+                  const float* dy, const float* dz, const float* tmax, uint64_t n, uint8_t* occluded,
+                  int numThreads) {
     using namespace glslref;
-    if (leafSize != 8 && leafSize != 2) return 1;
-    if (leafSize == 8) {
+    const bool obox = boundsKind == 2;
+    if ((leafSize != 8 && leafSize != 2) || (obox && leafSize != 8) || (boundsKind != 0 && !obox)) return 1;
+    if (obox) {
+        GPUGI_REF_BIND(ref_obox8)
+    } else if (leafSize == 8) {
         GPUGI_REF_BIND(ref_leaf8)
     } else {
         GPUGI_REF_BIND(ref_leaf2)
@@ -143,7 +172,12 @@ int ref_trace_any(const float* hierarchy, const int32_t* slots, const float* pos
         for (uint64_t i = b; i < e; ++i) {
             const vec3 o(ox[i], oy[i], oz[i]), d(dx[i], dy[i], dz[i]);
             bool hit;
-            if (leafSize == 8) {
+            if (obox) {
+                ref_obox8::Ray r;
+                r.Origin = o;
+                r.Direction = d;
+                hit = ref_obox8::TraceRayAnyHit(r, tmax[i]);
+            } else if (leafSize == 8) {
                 ref_leaf8::Ray r;
                 r.Origin = o;
                 r.Direction = d;

@@ -163,14 +163,34 @@ static inline vec3 Position(const Scene& s, int32_t idx) {
     return vec3(p[0], p[1], p[2]);
 }
 
-// FetchIntersectBoxNode (intersectiontests.glsl:100-111) and its ellipsoid twin.
+// rotate(x, q) (intersectiontests.glsl:82-89)
+static vec3 Rotate(vec3 x, vec4 q) {
+    vec3 t = cross(vec3(q.x, q.y, q.z), x);
+    return x + 2.0f * vec3(q.w * t.x + q.y * t.z - q.z * t.y, q.w * t.y + q.z * t.x - q.x * t.z,
+                           q.w * t.z + q.x * t.y - q.y * t.x);
+}
+
+// FetchIntersectBoxNode (intersectiontests.glsl:100-111), FetchIntersectOBoxNode
+// (:114-128; 48-B nodes {center, firstChild}, {sidesHalf, escape}, rotationInv:
+// the ray goes into the box frame and meets the box [-sidesHalf, sidesHalf])
+// and the ellipsoid node of this library.
 static inline bool FetchIntersectNode(const Scene& s, const Ray& ray, vec3 invRayDir, int nodeIdx,
                                       float& newHit, uint& childCode, int& escape) {
-    vec4 a = s.hierarchy[2 * nodeIdx];
-    vec4 b = s.hierarchy[2 * nodeIdx + 1];
+    const int stride = s.boundsKind == BOUNDS_OBOX ? 3 : 2;
+    vec4 a = s.hierarchy[stride * nodeIdx];
+    vec4 b = s.hierarchy[stride * nodeIdx + 1];
     childCode = floatBitsToUint(a.w);
     escape = floatBitsToInt(b.w);
     if (s.boundsKind == BOUNDS_ELLIPSOID) return IntersectEllipsoid(ray, a.xyz(), b.xyz(), newHit);
+    if (s.boundsKind == BOUNDS_OBOX) {
+        vec4 rotationInv = s.hierarchy[3 * nodeIdx + 2];
+        vec3 o = Rotate(ray.Origin - a.xyz(), rotationInv);
+        vec3 d = Rotate(ray.Direction, rotationInv);
+        vec3 inv = vec3(1.0f) / d;
+        float exitDist;
+        if (s.triangleTest) return IntersectBoxRobust(o, inv, -b.xyz(), b.xyz(), newHit);
+        return IntersectBox(o, inv, -b.xyz(), b.xyz(), newHit, exitDist);
+    }
     float exitDist;
     if (s.triangleTest) return IntersectBoxRobust(ray.Origin, invRayDir, a.xyz(), b.xyz(), newHit);
     return IntersectBox(ray.Origin, invRayDir, a.xyz(), b.xyz(), newHit, exitDist);

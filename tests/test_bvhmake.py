@@ -48,6 +48,8 @@ def _check_tree(b, tris, positions):
     assert (seen == 1).all(), "every triangle appears in exactly one leaf slot"
     if b.bounds_kind == 0:
         assert (b.hierarchy[:, 0:3] <= lo).all() and (b.hierarchy[:, 4:7] >= hi).all()
+    elif b.bounds_kind == 2:  # oriented box: every vertex below inside, in the shader's float rotation
+        _check_oboxes(b, positions)
     else:  # ellipsoid contains the box corners of everything below
         c, r = b.hierarchy[:, 0:3].astype(np.float64), b.hierarchy[:, 4:7].astype(np.float64)
         for corner in range(8):
@@ -64,6 +66,67 @@ def _check_tree(b, tris, positions):
                 block = block[block[:, 0] != block[:, 1]]
                 p = positions[block[:, :3].reshape(-1)].astype(np.float64)
                 assert (((p - c[i]) / r[i]) ** 2).sum(1).max() <= 1.0 + 1e-6
+
+
+def _qrotate(x, q):
+    """rotate(x, q) of intersectiontests.glsl:82-89 in float32, the shader's order."""
+    f = np.float32
+    x = x.astype(f)
+    qx, qy, qz, qw = (np.asarray(q[..., k], f)[..., None] for k in range(4))
+    t = np.stack([qy[..., 0] * x[..., 2] - qz[..., 0] * x[..., 1], qz[..., 0] * x[..., 0] - qx[..., 0] * x[..., 2],
+                  qx[..., 0] * x[..., 1] - qy[..., 0] * x[..., 0]], -1).astype(f)
+    u = np.stack([(qw[..., 0] * t[..., 0] + qy[..., 0] * t[..., 2]) - qz[..., 0] * t[..., 1],
+                  (qw[..., 0] * t[..., 1] + qz[..., 0] * t[..., 0]) - qx[..., 0] * t[..., 2],
+                  (qw[..., 0] * t[..., 2] + qx[..., 0] * t[..., 1]) - qy[..., 0] * t[..., 0]], -1).astype(f)
+    return (x + f(2.0) * u).astype(f)
+
+
+def _check_oboxes(b, positions):
+    """Every vertex below a node lies inside its oriented box, with the
+    rotation computed as the walk computes it; the quaternions are unit."""
+    H = b.hierarchy
+    assert H.shape[1] == 12
+    assert np.allclose((H[:, 8:12].astype(np.float64) ** 2).sum(1), 1.0, atol=1e-5)
+    fc = b.first_child
+    n, L = b.num_nodes, b.leaf_size
+    blo = np.zeros(n, np.int64)
+    bhi = np.zeros(n, np.int64)
+    for i in range(n - 1, -1, -1):
+        c = int(fc[i])
+        if c & 0x80000000:
+            blo[i] = bhi[i] = c & 0x7FFFFFFF
+        else:
+            r = int(b.escape[c])
+            blo[i], bhi[i] = min(blo[c], blo[r]), max(bhi[c], bhi[r])
+    for i in range(n):
+        block = b.slots[blo[i] * L:(bhi[i] + 1) * L]
+        block = block[block[:, 0] != block[:, 1]]
+        p = positions[block[:, :3].reshape(-1)].astype(np.float32)
+        local = _qrotate(p - H[i, 0:3], H[i, 8:12])
+        assert (np.abs(local) <= H[i, 4:7]).all(), i
+
+
+@pytest.mark.parametrize("method", ["sweep", "kdtree", "lds"])
+def test_oriented_box_fit(built, method):
+    sc = scenes.displaced_icosphere(3000, seed=6)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, fit="obox")
+    assert b.bounds_kind == 2 and b.hierarchy.shape == (b.num_nodes, 12)
+    _check_tree(b, sc["triangles"], sc["positions"])
+    # the topology is the method's own; only the bounds differ from the box fit
+    a = bvh.build_bvh(sc["positions"], sc["triangles"], method=method)
+    assert np.array_equal(a.first_child, b.first_child) and np.array_equal(a.escape, b.escape)
+    assert np.array_equal(a.slots, b.slots)
+
+
+def test_oriented_box_file_round_trip(built, tmp_path):
+    sc = scenes.displaced_icosphere(1500, seed=3)
+    p = tmp_path / "obox.bim"
+    bvh.write_bvh_file(sc["positions"], sc["triangles"], str(p), method="sweep", fit="obox")
+    b = bvh.read_bvh_file(str(p))
+    ref = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", fit="obox")
+    assert b.bounds_kind == 2
+    assert np.array_equal(b.hierarchy.view(np.uint32), ref.hierarchy.view(np.uint32))
+    assert np.array_equal(b.slots, ref.slots)
 
 
 @pytest.mark.parametrize("method", ["sweep", "kdtree", "lds"])

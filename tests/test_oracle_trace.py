@@ -134,3 +134,22 @@ def test_watertight_oracle_matches_bruteforce_and_reference_hits():
     hit = wt["slot"] >= 0
     assert np.allclose(wt["u"][both], ref["u"][both], atol=1e-4)
     assert hit.mean() > 0.3
+
+
+@pytest.mark.parametrize("method", ["sweep", "kdtree"])
+def test_oriented_box_walk_matches_bruteforce(method):
+    """The oracle's OBOX_BVH walk (FetchIntersectOBoxNode) over the fitted
+    oriented boxes finds the brute-force closest hits, the same ones as the
+    box hierarchy of the same topology, while testing fewer triangles."""
+    sc = scenes.displaced_icosphere(8192, seed=12)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, fit="obox")
+    a = bvh.build_bvh(sc["positions"], sc["triangles"], method=method)
+    rays = scenes.aimed_rays(30000, sc["positions"], seed=13)
+    o = oracle.trace_closest(b, sc["positions"], rays, counters=True)
+    bf = oracle.bruteforce_closest(b.slots, sc["positions"], rays)
+    assert (o["t"].view(np.uint32) == bf["t"].view(np.uint32)).mean() > 0.999
+    oa = oracle.trace_closest(a, sc["positions"], rays, counters=True)
+    assert (o["t"].view(np.uint32) == oa["t"].view(np.uint32)).mean() > 0.999
+    assert o["counters"][:, 2].sum() < oa["counters"][:, 2].sum()
+    occ = oracle.trace_any(b, sc["positions"], rays)["occluded"]
+    assert np.array_equal(occ.astype(bool), o["slot"] >= 0)

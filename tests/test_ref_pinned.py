@@ -7,7 +7,8 @@ as C++ into oracle/_ref/libgpugi_ref.so. These tests run it beside the
 oracle's restatement on the same inputs and require identical bits:
   * TraceRay / TraceRayAnyHit on the closest-hit query workload (2^20 rays,
     65,536-triangle displaced icosphere, bvhmake sweep hierarchy with 8-slot
-    leaves), on a 2-slot-leaf tree and on axis-parallel and box-plane rays
+    leaves), on a 2-slot-leaf tree, on an oriented-box tree (OBOX_BVH) and
+    on axis-parallel and box-plane rays
     with the tmax edge cases (the hit Triangle record, t, both barycentrics,
     the any-hit flag);
   * the random.glsl / helper.glsl functions on random inputs;
@@ -61,6 +62,18 @@ def test_traversal_aimed_rays_and_two_slot_leaves():
     for leaf in (8, 2):
         b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", leaf_size=leaf)
         rays = scenes.aimed_rays(100_000, sc["positions"], seed=8)
+        _same_closest(b, oracle.trace_closest(b, sc["positions"], rays), ref.trace_closest(b, sc["positions"], rays))
+        assert np.array_equal(ref.trace_any(b, sc["positions"], rays),
+                              oracle.trace_any(b, sc["positions"], rays)["occluded"])
+
+
+def test_traversal_oriented_boxes():
+    """traceray.glsl with OBOX_BVH (FetchIntersectOBoxNode, rotate) over the
+    fitted oriented-box hierarchy: identical to the oracle's walk."""
+    sc = scenes.displaced_icosphere(16384, seed=21)
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", fit="obox")
+    assert b.bounds_kind == 2
+    for rays in (scenes.random_rays(1 << 18, seed=22), scenes.aimed_rays(100_000, sc["positions"], seed=23)):
         _same_closest(b, oracle.trace_closest(b, sc["positions"], rays), ref.trace_closest(b, sc["positions"], rays))
         assert np.array_equal(ref.trace_any(b, sc["positions"], rays),
                               oracle.trace_any(b, sc["positions"], rays)["occluded"])

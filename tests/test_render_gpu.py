@@ -393,3 +393,40 @@ def test_photon_config_validation_and_progressive_radius(cuda_ctx, room):
     assert cuda_ctx.device_error_bits() == 0
     render.set_photon_config(cuda_ctx)
     img.close()
+
+
+def test_passes_on_oriented_box_hierarchy(cuda_ctx):
+    """The passes walk an oriented-box hierarchy (OBOX_BVH) like a box one:
+    depth-1 PT equals the oracle per pixel, and full-depth PT and LT images
+    equal those of the box hierarchy of the same scene (same seeds and light
+    samples; the closest hits are the same triangles)."""
+    sc = scenes.cornell_room(seed=1, sphere_level=3, wall_grid=8)
+    bo = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", fit="obox")
+    ba = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    vi = cuda.vertex_info(sc["normals"], sc["texcoords"])
+    do = cuda_ctx.upload_scene(bo, sc["positions"], vi, sc["materials"])
+    da = cuda_ctx.upload_scene(ba, sc["positions"], vi, sc["materials"])
+    W = H = 40
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    ls = _light_sets(do, 4, 128)
+    img = render.Image(cuda_ctx, W, H)
+    render.render(cuda_ctx, do, cam, img, "PT", max_path_length=1, samples=4, light_samples=ls)
+    g = img.read()
+    o = _oracle(bo, sc, "PT", W, H, cam, ls, 4, max_path_length=1)
+    assert np.abs(g[..., :3] - o[..., :3]).max() <= 1e-4 * np.abs(o[..., :3]).max() + 1e-6
+    img.close()
+    for pass_ in ("PT", "LT"):
+        nls = render.DEFAULT_LIGHT_SAMPLES[pass_]
+        ls = _light_sets(do, 8, nls, seed=9)
+        imgs = []
+        for ds in (do, da):
+            im = render.Image(cuda_ctx, W, H)
+            render.render(cuda_ctx, ds, cam, im, pass_, max_path_length=6, samples=8, light_samples=ls)
+            imgs.append(im.read()[..., :3])
+            im.close()
+        close = np.abs(imgs[0] - imgs[1]) <= 1e-3 * np.abs(imgs[1]).max() + 1e-5
+        assert close.all(-1).mean() > 0.98, (pass_, close.all(-1).mean())
+        assert abs(imgs[0].mean() / imgs[1].mean() - 1) < 0.01
+    assert cuda_ctx.device_error_bits() == 0
+    do.close()
+    da.close()

@@ -387,3 +387,42 @@ def test_stream_ordered_host_queries(cuda_ctx, icosphere_65536):
         _compare_closest({k: outs[i][k] for k in ("slot", "t", "u", "v")}, cuda.trace_closest(cuda_ctx, ds, host[i]))
         assert np.array_equal(outs[i]["occ"], cuda.trace_any(cuda_ctx, ds, host[i]))
     ds.close()
+
+
+@pytest.mark.parametrize("watertight", [False, True])
+def test_oriented_box_hierarchy_bit_exact(cuda_ctx, icosphere_65536, watertight):
+    """GPUGI_BOUNDS_OBOX scenes (48-B nodes, the reference's OBOX_BVH walk):
+    bit-exact against the oracle in every trace mode, in both triangle tests,
+    through the stream-ordered query too."""
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", fit="obox")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    ds.set_triangle_test(watertight)
+    try:
+        for rays in (scenes.random_rays(1 << 18, seed=61), scenes.aimed_rays(1 << 17, sc["positions"], seed=62)):
+            o = oracle.trace_closest(b, sc["positions"], rays, watertight=watertight)
+            oa = oracle.trace_any(b, sc["positions"], rays, watertight=watertight)["occluded"]
+            for mode in (0, 1, 2, 3, 4, 5):
+                cuda_ctx.set_trace_config(mode=mode)
+                _compare_closest(cuda.trace_closest(cuda_ctx, ds, rays), o)
+                assert np.array_equal(cuda.trace_any(cuda_ctx, ds, rays), oa)
+            cuda_ctx.set_trace_config(mode=3)
+            dev = {k: torch.from_numpy(rays[k]).cuda() for k in cuda.RAY_KEYS}
+            n = rays["ox"].shape[0]
+            out = dict(slot=torch.empty(n, dtype=torch.int32, device="cuda"), t=torch.empty(n, device="cuda"),
+                       u=torch.empty(n, device="cuda"), v=torch.empty(n, device="cuda"))
+            s = torch.cuda.Stream()
+            torch.cuda.synchronize()
+            cuda.trace_closest_device_async(cuda_ctx, ds, dev, out, s.cuda_stream)
+            s.synchronize()
+            _compare_closest({k: v.cpu().numpy() for k, v in out.items()}, o)
+        stats = cuda.trace_stats_device(cuda_ctx, ds, {k: torch.from_numpy(v).cuda() for k, v in rays.items()})
+        oc = oracle.trace_closest(b, sc["positions"], rays, counters=True, watertight=watertight)["counters"]
+        assert np.array_equal(np.asarray(stats, np.int64), oc.astype(np.int64).sum(0))
+    finally:
+        cuda_ctx.set_trace_config(mode=3)
+    assert cuda_ctx.device_error_bits() == 0
+    exported = ds.export()
+    assert np.array_equal(exported.hierarchy.view(np.uint32)[:, 8:], b.hierarchy.view(np.uint32)[:, 8:])
+    ds.close()
