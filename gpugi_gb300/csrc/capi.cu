@@ -277,7 +277,10 @@ void gpugi_destroy(gpugi_ctx* ctx) {
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->queue) cudaFree(ctx->queue);
     for (auto& ss : ctx->streamScratch) {
-        cudaStreamSynchronize(ss.stream);
+        if (ss.lastUse) {
+            cudaEventSynchronize(ss.lastUse);
+            cudaEventDestroy(ss.lastUse);
+        }
         if (ss.queue) cudaFree(ss.queue);
         if (ss.counters) cudaFree(ss.counters);
         if (ss.stage) cudaFree(ss.stage);
@@ -381,26 +384,38 @@ gpugi_status gpugi_trace_any_device(gpugi_ctx* ctx, const gpugi_scene* sc, const
 
 namespace gpugi {
 
-// Scratch of a caller stream: found by stream, grown when a call needs more
-// queue entries (after the stream's earlier work has finished with it).
+// Scratch of a caller stream: found by stream; a new stream takes a free set
+// or, with GPUGI_MAX_QUERY_STREAMS sets in use, the least recently used one
+// once the work that last used it has finished (its lastUse event; callers
+// create and destroy streams freely). Before a set is used the stream also
+// waits for that event, so a set never serves two streams at once even when
+// a destroyed stream's handle comes back for a new one. Grown when a call
+// needs more queue entries (after its last use has finished).
 static gpugi_status stream_scratch(gpugi_ctx* ctx, cudaStream_t s, uint64_t n, gpugi_ctx::StreamScratch** out) {
     gpugi_ctx::StreamScratch* ss = nullptr;
     for (auto& e : ctx->streamScratch)
         if (e.stream == s) ss = &e;
-    if (!ss) {
-        if (ctx->streamScratch.size() >= kMaxQueryStreams)
-            return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "more than GPUGI_MAX_QUERY_STREAMS caller streams");
+    if (!ss && ctx->streamScratch.size() < kMaxQueryStreams) {
         ctx->streamScratch.push_back({});
         ss = &ctx->streamScratch.back();
-        ss->stream = s;
-        if (cudaMalloc(&ss->counters, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+        if (cudaMalloc(&ss->counters, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ss->lastUse, cudaEventDisableTiming) != cudaSuccess) {
+            if (ss->counters) cudaFree(ss->counters);
             ctx->streamScratch.pop_back();
             return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "query counters");
         }
+        ss->stream = s;
+    }
+    if (!ss) {  // reuse the least recently used set
+        ss = &ctx->streamScratch[0];
+        for (auto& e : ctx->streamScratch)
+            if (e.tick < ss->tick) ss = &e;
+        GPUGI_CUDA_TRY(ctx, cudaEventSynchronize(ss->lastUse));
+        ss->stream = s;
     }
     if (n > ss->cap) {
         if (ss->queue) {
-            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            GPUGI_CUDA_TRY(ctx, cudaEventSynchronize(ss->lastUse));
             cudaFree(ss->queue);
             ss->queue = nullptr;
             ss->cap = 0;
@@ -412,6 +427,8 @@ static gpugi_status stream_scratch(gpugi_ctx* ctx, cudaStream_t s, uint64_t n, g
         }
         ss->cap = want;
     }
+    GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(s, ss->lastUse, 0));
+    ss->tick = ++ctx->streamTick;
     *out = ss;
     return GPUGI_OK;
 }
@@ -427,8 +444,11 @@ static gpugi_status trace_async(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyH
     gpugi_status st = stream_scratch(ctx, s, n, &ss);
     if (st) return st;
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(ss->counters, 0, 4 * sizeof(unsigned long long), s));
-    return launch_trace_filtered_on(ctx, sc, anyHit, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, occluded,
-                                    ss->queue, ss->counters, s);
+    st = launch_trace_filtered_on(ctx, sc, anyHit, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, occluded,
+                                  ss->queue, ss->counters, s);
+    if (st) return st;
+    GPUGI_CUDA_TRY(ctx, cudaEventRecord(ss->lastUse, s));
+    return GPUGI_OK;
 }
 
 // Host-pointer query on a caller stream: rays copied in, the two launches,
@@ -446,7 +466,7 @@ static gpugi_status trace_host_async(gpugi_ctx* ctx, const gpugi_scene* sc, bool
     const size_t col = align256(n * 4);
     if (ss->stageBytes < 11 * col) {
         if (ss->stage) {
-            GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            GPUGI_CUDA_TRY(ctx, cudaEventSynchronize(ss->lastUse));
             cudaFree(ss->stage);
             ss->stage = nullptr;
             ss->stageBytes = 0;
@@ -481,6 +501,7 @@ static gpugi_status trace_host_async(gpugi_ctx* ctx, const gpugi_scene* sc, bool
         GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(u, dU, n * 4, cudaMemcpyDeviceToHost, s));
         GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(v, dV, n * 4, cudaMemcpyDeviceToHost, s));
     }
+    GPUGI_CUDA_TRY(ctx, cudaEventRecord(ss->lastUse, s));
     return GPUGI_OK;
 }
 

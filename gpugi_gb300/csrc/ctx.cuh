@@ -55,7 +55,10 @@ struct gpugi_ctx {
         unsigned long long* counters = nullptr;
         void* stage = nullptr;  // host-pointer queries: device copies of the rays and results
         size_t stageBytes = 0;
+        cudaEvent_t lastUse = nullptr;  // recorded after the last work that used this set
+        uint64_t tick = 0;              // call counter at the last use (least recently used is reused)
     };
+    uint64_t streamTick = 0;
     std::vector<StreamScratch> streamScratch;
     // batched rendering
     uint32_t batchPaths = 16u << 20;  // path-queue capacity of one round

@@ -184,9 +184,11 @@ gpugi_status gpugi_trace_any_device(gpugi_ctx* ctx, const gpugi_scene* scene,
  * call after the work that writes its rays (and before the work that reads
  * its results) on that stream, as for any CUDA library call that takes a
  * stream. The library keeps one scratch set (ray-index queue and counters)
- * per stream, up to GPUGI_MAX_QUERY_STREAMS streams per context, allocated
- * at the first call on a stream and grown when n grows (which waits for the
- * stream). The context's trace mode selects the walker (modes 0 and 1 run
+ * per stream, allocated at the first call on a stream and grown when n grows
+ * (which waits for the set's previous work). Up to GPUGI_MAX_QUERY_STREAMS
+ * sets exist per context; a call on a further stream takes over the least
+ * recently used set once that set's last work has finished (streams may be
+ * created and destroyed freely; only as many as there are sets overlap). The context's trace mode selects the walker (modes 0 and 1 run
  * the mode-2 launches). No counterpart in the reference (its queries are
  * shader calls inside a dispatch). */
 #define GPUGI_MAX_QUERY_STREAMS 8

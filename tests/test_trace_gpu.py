@@ -426,3 +426,28 @@ def test_oriented_box_hierarchy_bit_exact(cuda_ctx, icosphere_65536, watertight)
     exported = ds.export()
     assert np.array_equal(exported.hierarchy.view(np.uint32)[:, 8:], b.hierarchy.view(np.uint32)[:, 8:])
     ds.close()
+
+
+def test_stream_ordered_queries_on_many_streams(cuda_ctx, icosphere_65536):
+    """More caller streams than scratch sets (GPUGI_MAX_QUERY_STREAMS = 8):
+    the least recently used set is taken over once its work has finished;
+    every batch still gets its own results."""
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    streams = [torch.cuda.Stream() for _ in range(13)]
+    host = [scenes.random_rays(20000 + 1000 * i, seed=700 + i) for i in range(13)]
+    dev = [{k: torch.from_numpy(r[k]).cuda() for k in cuda.RAY_KEYS} for r in host]
+    outs = [dict(slot=torch.empty(r["ox"].shape[0], dtype=torch.int32, device="cuda"),
+                 t=torch.empty(r["ox"].shape[0], device="cuda"), u=torch.empty(r["ox"].shape[0], device="cuda"),
+                 v=torch.empty(r["ox"].shape[0], device="cuda")) for r in host]
+    torch.cuda.synchronize()
+    for rep in range(2):
+        for i, s in enumerate(streams):
+            cuda.trace_closest_device_async(cuda_ctx, ds, dev[i], outs[i], s.cuda_stream)
+        torch.cuda.synchronize()
+        for i in range(len(streams)):
+            _compare_closest({k: v.cpu().numpy() for k, v in outs[i].items()}, cuda.trace_closest(cuda_ctx, ds, host[i]))
+    assert cuda_ctx.device_error_bits() == 0
+    ds.close()
