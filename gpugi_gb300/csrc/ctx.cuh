@@ -110,6 +110,8 @@ struct gpugi_scene {
     // Ellipsoid scenes: the radii as uploaded (3 floats per node, device
     // order); the device nodes hold their reciprocals.
     std::vector<float> hostRadii;
+    // material textures (texels, per-texture table, per-material map indices), one allocation
+    void* texBlock = nullptr;
     // hierarchy-importance renderer (hierarchy.cu), device node order
     gpugi::HierBuffers* hier = nullptr;
 };

@@ -789,6 +789,7 @@ gpugi_status check_scene(gpugi_ctx* ctx, const gpugi_scene* sc) {
 HierConst make_const(gpugi_ctx* ctx, gpugi_scene* sc, const gpugi_camera* cam, uint32_t width, uint32_t height) {
     HierConst c{};
     c.s = sc->dev;
+    c.s.matTex = nullptr;  // the hierarchy pass shades with the materials' constant values
     c.camU = f3(cam->U[0], cam->U[1], cam->U[2]);
     c.camV = f3(cam->V[0], cam->V[1], cam->V[2]);
     c.camW = f3(cam->W[0], cam->W[1], cam->W[2]);
@@ -984,7 +985,9 @@ gpugi_status gpugi_scene_set_hierarchy_ndf(gpugi_ctx* ctx, gpugi_scene* sc, cons
     GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(h->ndf, dev.data(), dev.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
     const unsigned nb = (nn + 127) / 128;
     k_hier_parents<<<nb, 128, 0, ctx->stream>>>(sc->dev, h->parents, h->arrive);
-    k_hier_materials<<<nb, 128, 0, ctx->stream>>>(sc->dev, h->parents, h->arrive, h->mats, ctx->errWord);
+    DevScene untextured = sc->dev;  // node materials average the materials' constant values
+    untextured.matTex = nullptr;
+    k_hier_materials<<<nb, 128, 0, ctx->stream>>>(untextured, h->parents, h->arrive, h->mats, ctx->errWord);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // `dev` goes out of scope
     h->ndfReady = true;

@@ -341,6 +341,7 @@ __global__ void k_light_generate(RenderConst rc, PathSoA A, bool withCache) {
 struct Hit {
     bool valid;
     float3 pos, N;
+    float2 tc;  // texture coordinate (GetTriangleHitInfo)
     int4 tri;
     MaterialData m;
     float t;
@@ -354,8 +355,8 @@ GPUGI_D Hit load_hit(const RenderConst& rc, const HitSoA& H, uint32_t k, float3 
     h.t = H.t[k];
     h.pos = X::add3(o, X::scale(h.t, d));  // ray.Origin + rayHit * ray.Direction, uncontracted
     h.tri = __ldg(rc.s.slots + slot);
-    h.N = hit_normal(rc.s, h.tri, H.u[k], H.v[k], nullptr);
-    h.m = load_material(rc.s, h.tri.w);
+    h.N = hit_normal(rc.s, h.tri, H.u[k], H.v[k], &h.tc);
+    h.m = load_material(rc.s, h.tri.w, h.tc);
     return h;
 }
 
@@ -534,7 +535,7 @@ GPUGI_D void light_shade_lane(const RenderConst& rc, const PathSoA& A, const Hit
     const int4 tri = __ldg(rc.s.slots + slot);
     float2 tc;
     const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], &tc);
-    const MaterialData m = load_material(rc.s, tri.w);
+    const MaterialData m = load_material(rc.s, tri.w, tc);
     const uint32_t s = L.info >> 8;
     if (withCache && m.Reflectiveness.w < 100.0f) {
         const uint32_t e = atomicAdd(rc.cacheCount + s, 1u);
@@ -702,7 +703,7 @@ GPUGI_D void bpt_shade_lane(const RenderConst& rc, const PathSoA& A, const HitSo
             if (lambertian) {
                 float cLtoE;
                 if (lmat != -1) {
-                    const MaterialData lm = load_material(rc.s, lmat);
+                    const MaterialData lm = load_material(rc.s, lmat, make_float2(e2.x, e2.y));
                     const float3 inc = unpack_normal(e3.x, e3.y);
                     const float3 lb = adjoint_bsdf(Ld, -inc, lm, lN, pdf);
                     intensity = flux * lb * cosLight;
@@ -953,8 +954,9 @@ __global__ void __launch_bounds__(128) k_photon_shade(RenderConst rc, PathSoA A,
                 const float3 gN = make_float3(rec.y, rec.z, rec.w);  // cross(e1, e0), not normalised
                 o = X::add3(o, X::scale(H.t[k], d));
                 const int4 tri = __ldg(rc.s.slots + slot);
-                const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], nullptr);
-                const MaterialData m = load_material(rc.s, tri.w);
+                float2 tc;
+                const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], &tc);
+                const MaterialData m = load_material(rc.s, tri.w, tc);
                 float3 thr = f3(1.0f);
                 float pdf;
                 bool diffuse = false;
@@ -1284,8 +1286,9 @@ __global__ void __launch_bounds__(128) k_im_photon_shade(RenderConst rc, PathSoA
                 const float3 gN = make_float3(rec.y, rec.z, rec.w);  // cross(e1, e0), not normalised
                 o = X::add3(o, X::scale(H.t[k], d));
                 const int4 tri = __ldg(rc.s.slots + slot);
-                const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], nullptr);
-                const MaterialData m = load_material(rc.s, tri.w);
+                float2 tc;
+                const float3 sN = hit_normal(rc.s, tri, H.u[k], H.v[k], &tc);
+                const MaterialData m = load_material(rc.s, tri.w, tc);
                 float3 preflect, prefract, pdiffuse;
                 decision_probabilities(m, preflect, prefract, pdiffuse);
                 const float3 bsdfTp = (pdiffuse * m.Diffuse) / kPI * tp;

@@ -286,11 +286,65 @@ extern "C" gpugi_status gpugi_scene_set_triangle_test(gpugi_ctx* ctx, gpugi_scen
     return GPUGI_OK;
 }
 
+extern "C" gpugi_status gpugi_scene_set_textures(gpugi_ctx* ctx, gpugi_scene* sc, const gpugi_texture* textures,
+                                                 uint32_t numTextures, const int32_t* materialTextures) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!sc) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "scene is NULL");
+    const uint32_t nm = sc->dev.numMaterials;
+    if (numTextures && (!textures || !materialTextures))
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "textures and materialTextures are required");
+    uint64_t texels = 0;
+    for (uint32_t i = 0; i < numTextures; ++i) {
+        const gpugi_texture& t = textures[i];
+        if (t.width == 0 || t.height == 0 || !t.rgba || t.width > (1u << 16) || t.height > (1u << 16))
+            return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "a texture needs RGBA texels and 1..65536 texels a side");
+        texels += (uint64_t)t.width * t.height;
+    }
+    if (texels >= (1ull << 32)) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "more than 2^32 texels");
+    for (uint64_t k = 0; numTextures && k < 4ull * nm; ++k)
+        if (materialTextures[k] < -1 || materialTextures[k] >= (int64_t)numTextures)
+            return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "material texture index out of range");
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // earlier passes may still read the old textures
+    if (sc->texBlock) cudaFree(sc->texBlock);
+    sc->texBlock = nullptr;
+    sc->dev.texels = nullptr;
+    sc->dev.texInfo = nullptr;
+    sc->dev.matTex = nullptr;
+    if (numTextures == 0) return GPUGI_OK;
+    const size_t texBytes = 16 * (size_t)texels, infoBytes = 16 * (size_t)numTextures, mapBytes = 16 * (size_t)nm;
+    const size_t infoAt = (texBytes + 255) & ~size_t(255), mapAt = (infoAt + infoBytes + 255) & ~size_t(255);
+    if (cudaMalloc(&sc->texBlock, mapAt + mapBytes + 16) != cudaSuccess) {
+        sc->texBlock = nullptr;
+        return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "texture allocation failed");
+    }
+    char* base = static_cast<char*>(sc->texBlock);
+    std::vector<uint32_t> info(4 * (size_t)numTextures);
+    uint64_t at = 0;
+    for (uint32_t i = 0; i < numTextures; ++i) {
+        const size_t n = (size_t)textures[i].width * textures[i].height;
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(base + 16 * at, textures[i].rgba, 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+        info[4 * i] = (uint32_t)at;
+        info[4 * i + 1] = textures[i].width;
+        info[4 * i + 2] = textures[i].height;
+        info[4 * i + 3] = 0;
+        at += n;
+    }
+    GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(base + infoAt, info.data(), infoBytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (nm)
+        GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(base + mapAt, materialTextures, mapBytes, cudaMemcpyHostToDevice, ctx->stream));
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    sc->dev.texels = reinterpret_cast<const float4*>(base);
+    sc->dev.texInfo = reinterpret_cast<const uint4*>(base + infoAt);
+    sc->dev.matTex = nm ? reinterpret_cast<const int4*>(base + mapAt) : nullptr;
+    return GPUGI_OK;
+}
+
 extern "C" void gpugi_scene_destroy(gpugi_scene* sc) {
     if (!sc) return;
     if (sc->ctx) cudaStreamSynchronize(sc->ctx->stream);
     detach_child(&sc->ctx);
     free_hierarchy(sc);
+    if (sc->texBlock) cudaFree(sc->texBlock);
     for (void* p : sc->allocations) cudaFree(p);
     delete sc;
 }

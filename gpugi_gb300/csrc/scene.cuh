@@ -42,6 +42,13 @@ struct DevScene {
     // Triangle test of the ray queries: 0 = the reference's (IntersectTriangle),
     // 1 = watertight (wtris holds its records).
     uint32_t triangleTest = 0;
+    // Material textures (gpugi_scene_set_textures), null without: RGBA32F
+    // texels of all textures, per texture {first texel, width, height, 0},
+    // per material the texture of {reflectiveness, opacity, diffuse,
+    // emissivity} or -1 for the record's constant.
+    const float4* texels = nullptr;
+    const uint4* texInfo = nullptr;
+    const int4* matTex = nullptr;
 };
 
 // Material view (constant-valued MaterialData, materials.glsl:9-30).
@@ -55,7 +62,42 @@ struct MaterialData {
     float3 Fresnel1;
 };
 
-GPUGI_D MaterialData load_material(const DevScene& s, int id) {
+// textureLod(sampler2D(handle), texcoord, 0.0) of a material texture: the
+// reference's sampler (scene.cpp:15-20: magnification LINEAR, wrap REPEAT;
+// level 0 of a texture without mipmaps is magnified) filters bilinearly
+// (OpenGL 4.5, 8.14.2: u = s w - 1/2, i0 = floor(u), weights from the
+// fractional parts, REPEAT wraps i0 and i0 + 1). The weights are computed in
+// float here (GL hardware quantises them to a few bits), with a fixed
+// operation order that the oracle restates.
+GPUGI_D float4 sample_texture(const DevScene& s, int tex, float2 tc) {
+    const uint4 info = __ldg(s.texInfo + tex);
+    const float w = (float)info.y, h = (float)info.z;
+    float u = __fsub_rn(__fmul_rn(tc.x, w), 0.5f), v = __fsub_rn(__fmul_rn(tc.y, h), 0.5f);
+    if (!isfinite(u)) u = 0.0f;
+    if (!isfinite(v)) v = 0.0f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = __fsub_rn(u, fu), b = __fsub_rn(v, fv);
+    float i0 = fmodf(fu, w), j0 = fmodf(fv, h);  // exact for every float
+    if (i0 < 0.0f) i0 = __fadd_rn(i0, w);
+    if (j0 < 0.0f) j0 = __fadd_rn(j0, h);
+    const uint32_t x0 = (uint32_t)i0 < info.y ? (uint32_t)i0 : 0u, y0 = (uint32_t)j0 < info.z ? (uint32_t)j0 : 0u;
+    const uint32_t x1 = x0 + 1 == info.y ? 0u : x0 + 1, y1 = y0 + 1 == info.z ? 0u : y0 + 1;
+    const float4* t = s.texels + info.x;
+    const float4 t00 = __ldg(t + (size_t)y0 * info.y + x0), t10 = __ldg(t + (size_t)y0 * info.y + x1);
+    const float4 t01 = __ldg(t + (size_t)y1 * info.y + x0), t11 = __ldg(t + (size_t)y1 * info.y + x1);
+    const float na = __fsub_rn(1.0f, a), nb = __fsub_rn(1.0f, b);
+    const float w00 = __fmul_rn(na, nb), w10 = __fmul_rn(a, nb), w01 = __fmul_rn(na, b), w11 = __fmul_rn(a, b);
+    auto mix4 = [&](float c00, float c10, float c01, float c11) {
+        return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(w00, c00), __fmul_rn(w10, c10)), __fmul_rn(w01, c01)),
+                         __fmul_rn(w11, c11));
+    };
+    return make_float4(mix4(t00.x, t10.x, t01.x, t11.x), mix4(t00.y, t10.y, t01.y, t11.y),
+                       mix4(t00.z, t10.z, t01.z, t11.z), mix4(t00.w, t10.w, t01.w, t11.w));
+}
+
+// SampleMaterialData (materials.glsl:19-30): the four maps at the hit's
+// texture coordinate (the record's constants where a material has no texture).
+GPUGI_D MaterialData load_material(const DevScene& s, int id, float2 tc = make_float2(0.0f, 0.0f)) {
     const float4* m = s.materials + 6 * id;
     float4 a = __ldg(m), b = __ldg(m + 1), c = __ldg(m + 2), d = __ldg(m + 3), e = __ldg(m + 4),
            f = __ldg(m + 5);
@@ -67,6 +109,13 @@ GPUGI_D MaterialData load_material(const DevScene& s, int id) {
     md.Emissivity = xyz(d);
     md.Fresnel0 = xyz(e);
     md.Fresnel1 = xyz(f);
+    if (s.matTex) {
+        const int4 tx = __ldg(s.matTex + id);
+        if (tx.x >= 0) md.Reflectiveness = sample_texture(s, tx.x, tc);
+        if (tx.y >= 0) md.Opacity = xyz(sample_texture(s, tx.y, tc));
+        if (tx.z >= 0) md.Diffuse = xyz(sample_texture(s, tx.z, tc));
+        if (tx.w >= 0) md.Emissivity = xyz(sample_texture(s, tx.w, tc));
+    }
     return md;
 }
 

@@ -56,6 +56,7 @@ def _declare(L):
     L.gpugi_scene_export.argtypes = [P, P, C.POINTER(U32), C.POINTER(U32), P, P]
     L.gpugi_scene_set_hierarchy_ndf.argtypes = [P, P, P]
     L.gpugi_scene_set_triangle_test.argtypes = [P, P, U32]
+    L.gpugi_scene_set_textures.argtypes = [P, P, P, U32, P]
     L.gpugi_hierarchy_importance.argtypes = [P, P, P, U32, U32, P, U32, U32]
     L.gpugi_hierarchy_read.argtypes = [P, P, P, P, P]
     for name in ("gpugi_trace_closest", "gpugi_trace_closest_device"):
@@ -244,6 +245,25 @@ class DeviceScene:
         """Triangle test of the ray queries on this scene: the reference's
         (False) or the watertight test (True), gpugi_scene_set_triangle_test."""
         self.ctx.check(lib().gpugi_scene_set_triangle_test(self.ctx.handle, self._h, 1 if watertight else 0))
+
+    def set_textures(self, textures, material_textures) -> None:
+        """Material textures (gpugi_scene_set_textures): textures is a list
+        of float32 (height, width, 4) RGBA arrays (row 0 at t = 0),
+        material_textures int32 (numMaterials, 4): the texture of each
+        material's {reflectiveness, opacity, diffuse, emissivity} map or -1.
+        An empty list removes the textures."""
+
+        class Tex(C.Structure):
+            _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgba", C.c_void_p)]
+
+        keep = [np.ascontiguousarray(t, dtype=np.float32) for t in textures]
+        arr = (Tex * max(1, len(keep)))()
+        for i, t in enumerate(keep):
+            assert t.ndim == 3 and t.shape[2] == 4
+            arr[i] = Tex(t.shape[1], t.shape[0], t.ctypes.data)
+        mt = np.ascontiguousarray(material_textures if keep else np.zeros((0, 4)), dtype=np.int32)
+        self.ctx.check(lib().gpugi_scene_set_textures(self.ctx.handle, self._h, C.cast(arr, C.c_void_p), len(keep),
+                                                      _ptr(mt) if keep else None))
 
     def set_hierarchy_ndf(self, sggx: np.ndarray) -> None:
         """Node NDFs (uint16 [numNodes, 6], bvhmake's approx_sggx in the

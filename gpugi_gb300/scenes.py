@@ -293,10 +293,14 @@ def random_rays(n: int, seed: int = 1, origin_lo: float = -2.0, origin_hi: float
 # --------------------------------------------------------------------------
 # Workload 2: enclosed room for the path tracer
 # --------------------------------------------------------------------------
-def _grid_quad(origin, eu, ev, n: int):
+def _grid_quad(origin, eu, ev, n: int, uv: bool = False):
     """A planar quad origin + [0,1]eu + [0,1]ev split into n x n cells (2 n^2
-    triangles). Winding makes the normal cross(eu, ev)."""
+    triangles). Winding makes the normal cross(eu, ev). With uv, a fourth
+    value: texcoords (u, v) = 2 (i, j) / n - 0.25, so a texture repeats about
+    twice across the quad and wraps through negative coordinates."""
     i, j = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    if uv:
+        return _grid_quad(origin, eu, ev, n) + (np.stack([2 * i / n - 0.25, 2 * j / n - 0.25], -1).reshape(-1, 2),)
     v = (np.asarray(origin, np.float64)[None, None] + (i / n)[..., None] * np.asarray(eu, np.float64)
          + (j / n)[..., None] * np.asarray(ev, np.float64)).reshape(-1, 3)
     a = (np.arange(n)[:, None] * (n + 1) + np.arange(n)[None, :]).reshape(-1)
@@ -309,20 +313,29 @@ def _grid_quad(origin, eu, ev, n: int):
 CORNELL_CAMERA = ((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0), 40.0)
 
 
-def cornell_room(seed: int = 1, sphere_level: int = 6, wall_grid: int = 40, light_radiance: float = 10.0):
+def cornell_room(seed: int = 1, sphere_level: int = 6, wall_grid: int = 40, light_radiance: float = 10.0,
+                 textured: bool = False):
     """Room [-1,1] x [0,2] x [-1,1] open towards +z: five wall quads (split
     into wall_grid^2 cells), two boxes rotated about y, an icosphere
     (level 6: 81,920 triangles) and a 0.5 x 0.5 ceiling light of radiance
     (10, 10, 10) facing down. Lambertian albedos uniform in [0.1, 0.9]^3.
-    Defaults give about 100k triangles. Camera: CORNELL_CAMERA."""
-    rs = Stream(seed, 5)
-    parts_v, parts_f, parts_n, mat_ids, mats = [], [], [], [], []
+    Defaults give about 100k triangles. Camera: CORNELL_CAMERA.
 
-    def add(v, f, n, mid):
+    textured: walls and light get texcoords (_grid_quad's uv) and the scene
+    three RGBA textures ("textures", "material_textures" keys, the
+    arguments of DeviceScene.set_textures): a 6 x 4 diffuse map on the
+    floor, back and left walls, a 3 x 5 reflectiveness map (specular in
+    [0, 0.3], exponent in [5, 60]) on the back wall and a 2 x 2 emissivity
+    map in [5, 15] on the light."""
+    rs = Stream(seed, 5)
+    parts_v, parts_f, parts_n, parts_t, mat_ids, mats = [], [], [], [], [], []
+
+    def add(v, f, n, mid, tc=None):
         base = sum(p.shape[0] for p in parts_v)
         parts_v.append(np.asarray(v, np.float64))
         parts_f.append(np.asarray(f) + base)
         parts_n.append(np.asarray(n, np.float64))
+        parts_t.append(np.zeros((len(v), 2)) if tc is None else np.asarray(tc, np.float64))
         mat_ids.append(np.full(len(f), mid, np.uint32))
 
     def new_material(rec):
@@ -340,8 +353,8 @@ def cornell_room(seed: int = 1, sphere_level: int = 6, wall_grid: int = 40, ligh
              ((-1, 0, -1), (0, 2, 0), (0, 0, 2)),    # left wall x=-1, normal +x
              ((1, 0, -1), (0, 0, 2), (0, 2, 0))]     # right wall x=1, normal -x
     for o, eu, ev in walls:
-        v, f, n = _grid_quad(o, eu, ev, g)
-        add(v, f, n, new_material(lambert(albedo())))
+        v, f, n, tc = _grid_quad(o, eu, ev, g, uv=True)
+        add(v, f, n, new_material(lambert(albedo())), tc if textured else None)
     for center, half, angle in (((-0.35, 0.6, -0.3), (0.3, 0.6, 0.3), 0.3), ((0.4, 0.3, 0.3), (0.3, 0.3, 0.3), -0.3)):
         c, s = math.cos(angle), math.sin(angle)
         rot = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
@@ -364,13 +377,28 @@ def cornell_room(seed: int = 1, sphere_level: int = 6, wall_grid: int = 40, ligh
                 add(v @ rot.T + np.asarray(center), f, n @ rot.T, mid)
     sv, sf = icosphere(sphere_level)
     add(sv * 0.25 + np.array([0.45, 0.85, 0.3]), sf, sv, new_material(lambert(albedo())))
-    lv, lf, ln = _grid_quad((-0.25, 1.999, -0.25), (0.5, 0, 0), (0, 0, 0.5), 1)  # normal -y
+    lv, lf, ln, lt = _grid_quad((-0.25, 1.999, -0.25), (0.5, 0, 0), (0, 0, 0.5), 1, uv=True)  # normal -y
     add(lv, lf, ln, new_material(material_record(albedo=(0.0, 0.0, 0.0), specular=(0.0, 0.0, 0.0),
-                                                 emissivity=(light_radiance,) * 3)))
+                                                 emissivity=(light_radiance,) * 3)), lt if textured else None)
     v = np.concatenate(parts_v)
     f = np.concatenate(parts_f)
     n = np.concatenate(parts_n)
-    return _pack(v, f, np.stack(mats), material_ids=np.concatenate(mat_ids), normals=n)
+    out = _pack(v, f, np.stack(mats), material_ids=np.concatenate(mat_ids), normals=n,
+                texcoords=np.concatenate(parts_t))
+    if textured:
+        ts = Stream(seed, 6)
+        diffuse = np.concatenate([ts.uniform(24, 0.1, 0.9).reshape(4, 6, 1).repeat(3, 2),
+                                  np.ones((4, 6, 1))], 2)
+        diffuse[..., 1] *= ts.uniform(24, 0.5, 1.0).reshape(4, 6)
+        refl = np.concatenate([ts.uniform(45, 0.0, 0.3).reshape(5, 3, 3), ts.uniform(15, 5.0, 60.0).reshape(5, 3, 1)], 2)
+        emis = np.concatenate([ts.uniform(4, 5.0, 15.0).reshape(2, 2, 1).repeat(3, 2), np.ones((2, 2, 1))], 2)
+        mt = np.full((len(mats), 4), -1, np.int32)
+        mt[[0, 2, 3], 2] = 0      # floor, back wall, left wall: diffuse map
+        mt[2, 0] = 1              # back wall: reflectiveness map
+        mt[len(mats) - 1, 3] = 2  # light: emissivity map
+        out["textures"] = [t.astype(np.float32) for t in (diffuse, refl, emis)]
+        out["material_textures"] = mt
+    return out
 
 
 def _value_noise(rs: Stream, n: int, cells: int) -> np.ndarray:

@@ -133,6 +133,28 @@ gpugi_status gpugi_scene_build(gpugi_ctx* ctx, const float* positions, uint32_t 
 gpugi_status gpugi_scene_export(gpugi_ctx* ctx, const gpugi_scene* scene, uint32_t* numNodes, uint32_t* numSlots,
                                 float* hierarchy, int32_t* slots);
 
+/* Material textures: the bindless textures of gpugi's materials
+ * (Material's four handles, gpugi/shader/scenedata.glsl:60-71, sampled by
+ * SampleMaterialData, materials.glsl:19-30; created by Scene::LoadMaterial,
+ * gpugi/scene/scene.cpp:132-187, for every map a material JSON names a file
+ * for). textures: RGBA32F texels, row-major, row 0 at t in [0, 1/height)
+ * (decoded by the caller: the image loader of the reference is not part of
+ * this path). materialTextures: 4 int32 per material (the scene's
+ * numMaterials) giving the texture of its {reflectiveness (w = Phong
+ * exponent), opacity, diffuse, emissivity} map, -1 for the material
+ * record's constant value. A pass samples them at the hit's texture
+ * coordinate as the reference's sampler does (bilinear, REPEAT; level 0).
+ * Emission for next-event estimation still comes from the records'
+ * constants (as LoadLightSources takes it); the hierarchy-importance pass
+ * uses the constants. A later call replaces the textures; numTextures 0
+ * removes them. Synchronous. */
+typedef struct gpugi_texture {
+    uint32_t width, height;
+    const float* rgba;  /* width * height * 4 floats */
+} gpugi_texture;
+gpugi_status gpugi_scene_set_textures(gpugi_ctx* ctx, gpugi_scene* scene, const gpugi_texture* textures,
+                                      uint32_t numTextures, const int32_t* materialTextures);
+
 /* Triangle test of the ray queries on a scene (gpugi_trace_closest / _any,
  * their _device forms, gpugi_trace_closest_noalloc and gpugi_trace_stats_device).
  *   GPUGI_TRIANGLE_REFERENCE   the reference's IntersectTriangle (OptiX-style

@@ -170,6 +170,31 @@ def render(bvh, scene: dict, pass_: str, width: int, height: int, camera: np.nda
     return accum
 
 
+_TEXTURES = None
+
+
+def set_textures(textures, material_textures) -> None:
+    """Material textures of the following rendering calls, as
+    DeviceScene.set_textures takes them; None or [] removes them."""
+    global _TEXTURES
+    L = lib()
+    L.oracle_set_textures.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]
+    L.oracle_set_textures.restype = None
+    if not textures:
+        _TEXTURES = None
+        L.oracle_set_textures(None, None, None, 0)
+        return
+    texels = np.ascontiguousarray(np.concatenate([np.asarray(t, np.float32).reshape(-1, 4) for t in textures]))
+    info = np.zeros((len(textures), 4), np.uint32)
+    at = 0
+    for i, t in enumerate(textures):
+        info[i] = (at, t.shape[1], t.shape[0], 0)
+        at += t.shape[0] * t.shape[1]
+    mt = np.ascontiguousarray(material_textures, dtype=np.int32).reshape(-1, 4)
+    _TEXTURES = (texels, info, mt)
+    L.oracle_set_textures(_p(texels), _p(info), _p(mt), mt.shape[0])
+
+
 def set_rng(rng: str) -> None:
     """Random streams of the following rendering calls ("pcg" or "reference")."""
     if rng not in ("pcg", "reference"):

@@ -151,7 +151,59 @@ struct RenderScene {
     uint32_t numMaterials = 0;
 };
 
-static MaterialData SampleMaterialData(const RenderScene& s, int id) {
+// Material textures of the scene (oracle_set_textures; the oracle serves one
+// caller at a time): RGBA32F texels, per texture {first texel, width,
+// height}, per material the texture of {reflectiveness, opacity, diffuse,
+// emissivity} or -1.
+static const float* g_texels = nullptr;
+static const uint32_t* g_texInfo = nullptr;
+static const int32_t* g_matTex = nullptr;
+static uint32_t g_numTexMaterials = 0;
+
+// textureLod(sampler2D, tc, 0.0) with the reference's sampler (scene.cpp:15-20:
+// magnified level 0 -> LINEAR, wrap REPEAT): bilinear per OpenGL 4.5 8.14.2,
+// u = s w - 1/2, weights from the fractional parts, float arithmetic in the
+// library's fixed order.
+static vec4 SampleTexture(int tex, vec2 tc) {
+    const uint32_t* info = g_texInfo + 4 * (size_t)tex;
+    const float w = (float)info[1], h = (float)info[2];
+    float u = tc.x * w - 0.5f, v = tc.y * h - 0.5f;
+    if (!std::isfinite(u)) u = 0.0f;
+    if (!std::isfinite(v)) v = 0.0f;
+    const float fu = std::floor(u), fv = std::floor(v);
+    const float a = u - fu, b = v - fv;
+    float i0 = std::fmod(fu, w), j0 = std::fmod(fv, h);
+    if (i0 < 0.0f) i0 = i0 + w;
+    if (j0 < 0.0f) j0 = j0 + h;
+    const uint32_t x0 = (uint32_t)i0 < info[1] ? (uint32_t)i0 : 0u, y0 = (uint32_t)j0 < info[2] ? (uint32_t)j0 : 0u;
+    const uint32_t x1 = x0 + 1 == info[1] ? 0u : x0 + 1, y1 = y0 + 1 == info[2] ? 0u : y0 + 1;
+    const float* t = g_texels + 4 * (size_t)info[0];
+    auto T = [&](uint32_t x, uint32_t y, int c) { return t[4 * ((size_t)y * info[1] + x) + c]; };
+    const float na = 1.0f - a, nb = 1.0f - b;
+    const float w00 = na * nb, w10 = a * nb, w01 = na * b, w11 = a * b;
+    float r[4];
+    for (int c = 0; c < 4; ++c)
+        r[c] = ((w00 * T(x0, y0, c) + w10 * T(x1, y0, c)) + w01 * T(x0, y1, c)) + w11 * T(x1, y1, c);
+    return vec4(r[0], r[1], r[2], r[3]);
+}
+
+static MaterialData SampleMaterialDataConst(const RenderScene& s, int id);
+
+// SampleMaterialData (materials.glsl:19-30): the textured maps at tc.
+static MaterialData SampleMaterialData(const RenderScene& s, int id, vec2 tc) {
+    MaterialData d = SampleMaterialDataConst(s, id);
+    if (g_matTex && (uint32_t)id < g_numTexMaterials) {
+        const int32_t* tx = g_matTex + 4 * (size_t)id;
+        if (tx[0] >= 0) d.Reflectiveness = SampleTexture(tx[0], tc);
+        if (tx[1] >= 0) d.Opacity = SampleTexture(tx[1], tc).xyz();
+        if (tx[2] >= 0) d.Diffuse = SampleTexture(tx[2], tc).xyz();
+        if (tx[3] >= 0) d.Emissivity = SampleTexture(tx[3], tc).xyz();
+    }
+    return d;
+}
+
+// The material record's constant values.
+static MaterialData SampleMaterialDataConst(const RenderScene& s, int id) {
     const float* m = s.materials + 24 * (size_t)id;
     MaterialData d;
     d.Diffuse = vec3(m[0], m[1], m[2]);
@@ -407,7 +459,7 @@ static vec3 PathtracePixel(const RenderScene& s, const Params& P, int x, int y) 
         vec3 hitNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w, tc);
         if (!didNEE) color += pathThroughput * m.Emissivity;
         didNEE = m.Reflectiveness.w < 500.0f;
         int sampleIndex = int(RandomUInt(seed) % (uint)P.numLightSamples);
@@ -452,7 +504,7 @@ static vec3 WhittedPixel(const RenderScene& s, const Params& P, int x, int y) {
         vec3 hitNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w, tc);
         color += pathThroughput * m.Emissivity;
         vec3 pdiffuse = GetDiffuseProbability(m, abs(dot(hitNormal, ray.Direction)));
         float pdiffuseAvg = GetLuminance(pdiffuse);
@@ -540,7 +592,7 @@ static void PhotonThread(const RenderScene& s, const Params& P, uint gid, int ph
         vec3 shadingNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, shadingNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w, tc);
         vec3 throughput(1.0f);
         float samplePDF;
         bool diffuse = false;
@@ -596,7 +648,7 @@ static vec3 GatherPixel(const RenderScene& s, const Params& P, const PhotonGrid&
         vec3 hitNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w, tc);
         color += pathThroughput * m.Emissivity;
         vec3 throughput(1.0f);
         float pdf;
@@ -693,7 +745,7 @@ static vec3 ImportonPixel(const RenderScene& s, const Params& P, int x, int y, G
         vec3 hitNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w, tc);
         if (i == 0) {
             vec3 gN = normalize(hit.normal);
             vec2 packed = PackNormal(dot(gN, ray.Direction) > 0.0f ? -gN : gN);
@@ -806,7 +858,7 @@ static void ImportonPhotonThread(const RenderScene& s, const Params& P, Image& i
         vec3 shadingNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, shadingNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w, tc);
         float cosThetaAbs = saturate(abs(dot(shadingNormal, ray.Direction)));
         vec3 bsdf = GetDiffuseProbability(m, cosThetaAbs) * m.Diffuse / PI;
         const int bx = (int)std::nearbyint(ray.Origin.x / grid.spacing);
@@ -942,7 +994,7 @@ static void LighttraceThread(const RenderScene& s, const Params& P, Image& img, 
         vec3 shadingNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, shadingNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w, tc);
         if (cache && m.Reflectiveness.w < 100.0f) {
             uint32_t k = cache->count.fetch_add(1);
             if (k < cache->capacity) {
@@ -1027,7 +1079,7 @@ static vec3 BidirPixel(const RenderScene& s, const Params& P, const LightCache& 
         vec3 hitNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialData(s, hit.triangle.w, tc);
         float incidentSurfaceCosSat = saturate(-dot(hitNormal, ray.Direction));
         float connectionLightToEyePath = DistanceMISHeuristic(rayHit, lastCosAbs) * MISHeuristic(incidentSurfaceCosSat / PI);
         mis = (i == 0) ? 1.0f : (lastConnectionProbability / max(lastConnectionProbability + connectionLightToEyePath, DIVISOR_EPSILON));
@@ -1067,7 +1119,7 @@ static vec3 BidirPixel(const RenderScene& s, const Params& P, const LightCache& 
                     float misLight = 1.0f;
                     if (e.Normal1 < 1.5f) {
                         if (e.MaterialIndex != -1) {
-                            MaterialData lm = SampleMaterialData(s, e.MaterialIndex);
+                            MaterialData lm = SampleMaterialData(s, e.MaterialIndex, e.Texcoord);
                             vec3 incidentDir = UnpackNormal(e.IncidentDirectionPacked);
                             vec3 lightBSDF = AdjointBSDF(lightRay.Direction, -incidentDir, lm, lightSampleHitNormal, pdf);
                             lightSampleIntensity = e.Flux * lightBSDF * cosLight;
@@ -1237,7 +1289,7 @@ static void AcquirePixel(const RenderScene& s, const Params& P, int iteration, i
         vec3 hitNormal;
         vec2 tc;
         GetTriangleHitInfo(s.geo, hit.triangle, hit.bary, hitNormal, tc);
-        MaterialData m = SampleMaterialData(s, hit.triangle.w);
+        MaterialData m = SampleMaterialDataConst(s, hit.triangle.w);  // hierarchy acquisition: constants
         ray.Origin = ray.Origin + rayHit * ray.Direction;
         pathImportance *= 0.5f;
         int sampleIndex = int(RandomUInt(seed) % (uint)P.numLightSamples);
@@ -1360,7 +1412,7 @@ static void HierarchyMaterials(const RenderScene& rs, uint* out) {
                 vec3 c = cross(p1 - p0, p2 - p0);
                 float triangleArea = sqrt(dot(c, c)) / 2.0f;
                 area += triangleArea;
-                MaterialData m = SampleMaterialData(rs, t.w);
+                MaterialData m = SampleMaterialDataConst(rs, t.w);  // hierarchy: constants
                 mat.Reflectiveness = mat.Reflectiveness + m.Reflectiveness * triangleArea;
                 mat.Opacity += m.Opacity * triangleArea;
                 mat.Diffuse += m.Diffuse * triangleArea;
@@ -1621,7 +1673,7 @@ static vec3 HierarchyPixel(const RenderScene& s, const Params& P, const float* i
         } else {
             vec2 tc;
             GetTriangleHitInfo(s.geo, h.triangle, h.bary, hitNormal, tc);
-            m = SampleMaterialData(s, h.triangle.w);
+            m = SampleMaterialDataConst(s, h.triangle.w);  // hierarchy: constants
         }
         float nextThreshold = pathImportanceThreshold * 20.0f;
         float epsilon = RAY_HIT_EPSILON;
@@ -1949,6 +2001,16 @@ uint32_t oracle_pcg_hash(uint32_t x) { return PcgHash(x); }
 // Random streams of the following calls: 1 PCG, 0 the reference's.
 void oracle_set_rng(int pcg) { g_rngPcg = pcg ? 1u : 0u; }
 
+// Material textures of the following rendering calls (the arrays must stay
+// alive until then); numMaterials 0 removes them.
+void oracle_set_textures(const float* texels, const uint32_t* info, const int32_t* materialTextures,
+                         uint32_t numMaterials) {
+    g_texels = texels;
+    g_texInfo = info;
+    g_matTex = numMaterials ? materialTextures : nullptr;
+    g_numTexMaterials = numMaterials;
+}
+
 // The restated random.glsl / helper.glsl functions over arrays, in the
 // reference's random streams; `kind` and layouts as ref_eval of the
 // reference-text build (oracle/ref_glue.cpp), so the two can be compared.
@@ -2010,6 +2072,11 @@ int oracle_eval(int kind, uint64_t n, const void* in, void* out) {
             break;
         }
         case 10: of[i] = GetLuminance(vec3(f[3 * i], f[3 * i + 1], f[3 * i + 2])); break;
+        case 11: {  // SampleTexture(texture f[0], tc f[1], f[2]) of the textures set by oracle_set_textures
+            vec4 r = SampleTexture((int)f[3 * i], vec2(f[3 * i + 1], f[3 * i + 2]));
+            of[4 * i] = r.x, of[4 * i + 1] = r.y, of[4 * i + 2] = r.z, of[4 * i + 3] = r.w;
+            break;
+        }
         default: return 1;
         }
     }

@@ -264,3 +264,37 @@ def test_light_sampler_restatement(built):
     area_flux = 10.0 * 0.25 * math.pi
     point_flux = math.log(1.0 + 1000.0 * 4 * math.pi)
     assert (both[:, 7] == 2.0).sum() == int(point_flux / (point_flux + area_flux) * 128)
+
+
+def test_texture_sampling_is_glsl_bilinear_repeat(built):
+    """The oracle's textureLod(.., 0) of a material texture: bilinear with
+    REPEAT wrapping (OpenGL 4.5 8.14.2, the reference's sampler,
+    scene.cpp:15-20), against a float64 restatement of that formula."""
+    import ctypes as C
+    rng = np.random.default_rng(3)
+    texs = [rng.uniform(0, 1, (5, 7, 4)).astype(np.float32), rng.uniform(0, 2, (1, 3, 4)).astype(np.float32)]
+    oracle.set_textures(texs, np.array([[0, -1, 1, -1]], np.int32))
+    try:
+        L = oracle.lib()
+        L.oracle_eval.argtypes = [C.c_int, C.c_uint64, C.c_void_p, C.c_void_p]
+        n = 2000
+        tex = rng.integers(0, 2, n)
+        tc = rng.uniform(-3, 3, (n, 2))
+        tc[:10] = [[0, 0], [1, 1], [0.5, 0.5], [-1e-7, 0.25], [0.999999, 0.1], [2.0, -2.0], [1e6, 3.25], [0.1, 0.0],
+                   [1 / 14, 1 / 10], [0.5 / 7, 0.5 / 5]]
+        inp = np.concatenate([tex[:, None], tc], 1).astype(np.float32)
+        out = np.zeros((n, 4), np.float32)
+        assert L.oracle_eval(11, n, inp.ctypes.data, out.ctypes.data) == 0
+        for i in range(n):
+            t = texs[tex[i]].astype(np.float64)
+            h, w = t.shape[:2]
+            u = float(np.float32(inp[i, 1])) * w - 0.5
+            v = float(np.float32(inp[i, 2])) * h - 0.5
+            i0, j0 = math.floor(u), math.floor(v)
+            a, b = u - i0, v - j0
+            x0, y0, x1, y1 = i0 % w, j0 % h, (i0 + 1) % w, (j0 + 1) % h
+            want = ((1 - a) * (1 - b) * t[y0, x0] + a * (1 - b) * t[y0, x1] + (1 - a) * b * t[y1, x0]
+                    + a * b * t[y1, x1])
+            assert np.allclose(out[i], want, rtol=1e-5, atol=1e-5), (i, inp[i], out[i], want)
+    finally:
+        oracle.set_textures(None, None)
