@@ -440,10 +440,14 @@ def run_ours(args, world, rank, local):
             "clocks": clk.summary()}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(b, sc["positions"], host_batches, seconds=args.cpu_seconds)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     ds.close()
     ctx.close()
+    if rank == 0 and world == 1 and not args.no_nrc:
+        with ClockSampler(local) as nclk:
+            line["nrc"] = nrc_headline(args)
+        line["nrc"]["clocks"] = nclk.summary()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def run_passes(args):
@@ -774,117 +778,195 @@ def run_batch(args):
     ctx.close()
 
 
-def run_nrc(args):
-    """Time to equal RMSE, rendering with the radiance cache vs the plain
-    renderer of the same pass. PT (default): the heightfield workload
-    (522k-triangle fBm terrain + 500 boxes, sun of irradiance 5, sky 0.5,
-    Lambertian albedos U[0.1, 0.8], depth 8). BPT (--nrc-pass BPT): the large
-    workload (~7.9M triangles in 20k instances, 64 Lambertian / Phong
-    materials, 256 area lights, ellipsoid hierarchy, depth 6), with eye
-    paths that stop at the cache vertex. RMSE is TextureMSE's, in FP64,
-    against an FP64-accumulated image of the plain pass with --nrc-ref-spp
-    samples. The plain pass accumulates 1024 spp (doubling chunks); its final
-    RMSE is the target and its wall time T_plain. The cache renderer first
-    trains for --nrc-warmup frames (timed, not accumulated), then accumulates
-    frames until its RMSE reaches the target or its time exceeds 3 T_plain.
-    Wall times: host clock around synchronised calls (both renderers
-    synchronise internally)."""
-    from gpugi_gb300 import bvh, cuda, nrc, render, scenes
-    pass_ = args.nrc_pass
-    W, H = args.nrc_size if args.nrc_size else ((640, 360) if pass_ == "PT" else (480, 270))
-    rr = args.nrc_rr
-    ctx = cuda.Context(0)
-    if pass_ == "PT":
-        depth, sky = 8, (0.5, 0.5, 0.5)
-        sc = scenes.heightfield_boxes(seed=1)
-        b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
-        box = ((-1.05, -0.25, -1.05), (1.05, 0.35, 1.05))
-        cam_args = scenes.HEIGHTFIELD_CAMERA
-        workload = "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8"
-    else:
-        depth, sky = 6, (0.0, 0.0, 0.0)
-        sc = scenes.large_instanced(seed=1)
-        b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", fit="ellipsoid")
-        box = ((-3.0, -3.0, -3.0), (103.0, 103.0, 103.0))
-        cam_args = scenes.LARGE_CAMERA
-        workload = ("~7.9M tris (20k instances in 100^3), 64 Lambertian/Phong materials, 256 area lights, "
-                    "ellipsoid BVH, depth 6")
-    ds = ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]), sc["materials"])
-    if pass_ == "PT":
-        render.add_directional_light(ds, scenes.HEIGHTFIELD_SUN, (5.0, 5.0, 5.0))
-    cam = render.camera_lookat(*cam_args, W, H)
+NRC_WORKLOAD_PT = "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8"
 
-    def timed(fn):
-        ctx.sync()
+
+class NrcSetup:
+    """Scene, camera and FP64 reference image of a time-to-equal-RMSE run.
+    PT: the heightfield workload (522k-triangle fBm terrain + 500 boxes, sun
+    of irradiance 5, sky 0.5, Lambertian albedos U[0.1, 0.8], depth 8). BPT:
+    the large workload (~7.9M triangles in 20k instances, 64 Lambertian /
+    Phong materials, 256 area lights, ellipsoid hierarchy, depth 6), with
+    eye paths that stop at the cache vertex. The reference is the plain pass
+    accumulated in FP64 over ref_spp samples; its noise adds the same
+    variance to both renderers' MSE, so it cancels out of the equal-RMSE
+    comparison."""
+
+    def __init__(self, pass_, W, H, ref_spp, rr):
+        from gpugi_gb300 import bvh, cuda, render, scenes
+        self.pass_, self.W, self.H, self.rr, self.ref_spp = pass_, W, H, rr, ref_spp
+        self.ctx = cuda.Context(0)
+        if pass_ == "PT":
+            self.depth, self.sky = 8, (0.5, 0.5, 0.5)
+            sc = scenes.heightfield_boxes(seed=1)
+            b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+            self.box = ((-1.05, -0.25, -1.05), (1.05, 0.35, 1.05))
+            cam_args = scenes.HEIGHTFIELD_CAMERA
+            self.workload = NRC_WORKLOAD_PT
+        else:
+            self.depth, self.sky = 6, (0.0, 0.0, 0.0)
+            sc = scenes.large_instanced(seed=1)
+            b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", fit="ellipsoid")
+            self.box = ((-3.0, -3.0, -3.0), (103.0, 103.0, 103.0))
+            cam_args = scenes.LARGE_CAMERA
+            self.workload = ("~7.9M tris (20k instances in 100^3), 64 Lambertian/Phong materials, 256 area lights, "
+                             "ellipsoid BVH, depth 6")
+        self.ds = self.ctx.upload_scene(b, sc["positions"], cuda.vertex_info(sc["normals"], sc["texcoords"]),
+                                        sc["materials"])
+        if pass_ == "PT":
+            render.add_directional_light(self.ds, scenes.HEIGHTFIELD_SUN, (5.0, 5.0, 5.0))
+        self.cam = render.camera_lookat(*cam_args, W, H)
+        conv = render.Image(self.ctx, W, H, fp64=True)
+        self.t_ref = self.timed(lambda: render.render(self.ctx, self.ds, self.cam, conv, pass_,
+                                                      max_path_length=self.depth, samples=ref_spp,
+                                                      iteration=1 << 24, rng_state=[99], sky=self.sky,
+                                                      rr_start_depth=rr))
+        self.ref = (conv.read64() / ref_spp).astype(np.float32)
+        conv.close()
+
+    def timed(self, fn):
+        """Host clock around a synchronised call (the renderers queue work on
+        the library's stream; both sides synchronise)."""
+        self.ctx.sync()
         t0 = time.perf_counter()
         fn()
-        ctx.sync()
+        self.ctx.sync()
         return time.perf_counter() - t0
 
-    conv = render.Image(ctx, W, H, fp64=True)
-    t_ref = timed(lambda: render.render(ctx, ds, cam, conv, pass_, max_path_length=depth, samples=args.nrc_ref_spp,
-                                        iteration=1 << 24, rng_state=[99], sky=sky, rr_start_depth=rr))
-    ref = (conv.read64() / args.nrc_ref_spp).astype(np.float32)
-    conv.close()
+    def rmse(self, img, n):
+        return float(np.sqrt(img.mse(n, self.ref, use_fp64=True)))
 
-    def rmse(img, n):
-        return float(np.sqrt(img.mse(n, ref, use_fp64=True)))
+    def plain(self, spp=1024):
+        """The plain pass to spp samples in doubling chunks: (time, final
+        RMSE = the target, curve of (spp, s, RMSE))."""
+        from gpugi_gb300 import render
+        pt = render.Image(self.ctx, self.W, self.H, fp64=True)
+        t, n, curve = 0.0, 0, []
+        chunks = [1, 1] + [1 << k for k in range(1, 20) if (1 << k) < spp]
+        for c in chunks:
+            c = min(c, spp - n)
+            if c <= 0:
+                break
+            t += self.timed(lambda: render.render(self.ctx, self.ds, self.cam, pt, self.pass_,
+                                                  max_path_length=self.depth, samples=c, iteration=n,
+                                                  rng_state=[7 + n], sky=self.sky, rr_start_depth=self.rr))
+            n += c
+            curve.append((n, round(t, 5), round(self.rmse(pt, n), 6)))
+        pt.close()
+        return t, curve[-1][2], curve
 
-    pt = render.Image(ctx, W, H, fp64=True)
-    t_pt, spp, pt_curve = 0.0, 0, []
-    for c in [1, 1, 2, 4, 8, 16, 32, 64, 128, 256, 512]:
-        t_pt += timed(lambda: render.render(ctx, ds, cam, pt, pass_, max_path_length=depth, samples=c, iteration=spp,
-                                            rng_state=[7 + spp], sky=sky, rr_start_depth=rr))
-        spp += c
-        pt_curve.append((spp, round(t_pt, 5), round(rmse(pt, spp), 6)))
-    target = pt_curve[-1][2]
-    pt.close()
-
-    configs = [tuple(int(x) for x in c.split(",")) for c in args.nrc_configs.split(";")] if args.nrc_configs else \
-        [(args.nrc_td, args.nrc_spf, args.nrc_train_steps)]
-    for td, spf, steps in configs:
+    def cache_run(self, t_pt, target, td, spf, steps, tl, spread, warmup, train_fraction=0.0, limit=3.0,
+                  at_frames=64):
+        """The cache renderer from a fresh network: `warmup` frames train
+        (timed, not accumulated), then frames accumulate until the RMSE
+        reaches the target or the time exceeds limit x t_pt."""
+        from gpugi_gb300 import nrc, render
+        W, H = self.W, self.H
         # training paths: about 1.5 x 65,536 vertices per frame (3 per path)
-        tf = args.nrc_train_fraction or min(0.05, 1.5 * 65536 / (3.0 * W * H * spf))
-        cache = nrc.RadianceCache(ctx, *box, seed=5)
-        opts = dict(max_path_length=depth, sky=sky, terminate_depth=td, train_fraction=tf, train_steps=steps,
-                    samples_per_frame=spf, rr_start_depth=rr, pass_=pass_)
-        scratch = render.Image(ctx, W, H)
-        t_nrc = timed(lambda: nrc.render_nrc(ctx, ds, cam, scratch, cache, samples=args.nrc_warmup * spf,
-                                             iteration=1 << 20, rng_state=[11], **opts))
+        tf = train_fraction or min(0.05, 1.5 * 65536 / (3.0 * W * H * spf))
+        cache = nrc.RadianceCache(self.ctx, *self.box, seed=5)
+        opts = dict(max_path_length=self.depth, sky=self.sky, terminate_depth=td, train_fraction=tf,
+                    train_steps=steps, samples_per_frame=spf, rr_start_depth=self.rr, pass_=self.pass_,
+                    train_length=tl, terminate_spread=spread)
+        t_nrc = 0.0
+        if warmup:
+            scratch = render.Image(self.ctx, W, H)
+            t_nrc = self.timed(lambda: nrc.render_nrc(self.ctx, self.ds, self.cam, scratch, cache,
+                                                      samples=warmup * spf, iteration=1 << 20, rng_state=[11],
+                                                      **opts))
+            scratch.close()
         t_warm = t_nrc
-        scratch.close()
-        img = render.Image(ctx, W, H, fp64=True)
-        frames, nrc_curve, reached, at_equal_time, chunk = 0, [], None, None, 1
-        while t_nrc < 3.0 * t_pt and frames * spf < 8192:
-            t_nrc += timed(lambda: nrc.render_nrc(ctx, ds, cam, img, cache, samples=chunk * spf,
-                                                  iteration=frames * spf, rng_state=[13 + frames], **opts))
+        img = render.Image(self.ctx, W, H, fp64=True)
+        frames, curve, reached, at_equal_time, at_n, chunk = 0, [], None, None, None, 1
+        while t_nrc < limit * t_pt and frames * spf < 8192:
+            t_nrc += self.timed(lambda: nrc.render_nrc(self.ctx, self.ds, self.cam, img, cache,
+                                                       samples=chunk * spf, iteration=frames * spf,
+                                                       rng_state=[13 + frames], **opts))
             frames += chunk
-            r = rmse(img, frames * spf)
-            nrc_curve.append((frames * spf, round(t_nrc, 5), round(r, 6)))
+            r = self.rmse(img, frames * spf)
+            curve.append((frames * spf, round(t_nrc, 5), round(r, 6)))
             if at_equal_time is None and t_nrc >= t_pt:
                 at_equal_time = r
+            if at_n is None and frames >= at_frames:
+                at_n = {"frames": frames, "s": round(t_nrc, 5), "rmse": round(r, 6)}
             if r <= target:
                 reached = t_nrc
                 break
-            chunk = min(chunk * 2, max(1, 64 // spf))
-        line = {"metric": f"time to the 1024-spp plain-{pass_} RMSE, {pass_} with the radiance cache vs plain {pass_}",
-                "unit": "ratio",
-                "value": (reached / t_pt) if reached else None, "higher_is_better": False,
-                "t_pt_s": round(t_pt, 4), "t_nrc_s": round(reached, 4) if reached else None,
-                "t_nrc_warmup_s": round(t_warm, 4), "target_rmse": target,
-                "nrc_rmse_at_equal_time": at_equal_time,
-                "config": {"workload": workload, "pass": pass_, "rr_start_depth": rr,
-                           "resolution": [W, H], "reference_spp": args.nrc_ref_spp, "reference_s": round(t_ref, 2),
-                           "nrc": {"terminate_depth": td, "train_fraction": round(tf, 5), "train_steps": steps,
-                                   "samples_per_frame": spf, "warmup_frames": args.nrc_warmup,
-                                   "max_train_samples": 65536, "ema": 0.99,
-                                   "mlp": "64-64x4-3 ReLU fp16, fp32 accumulate, Adam lr 1e-2"}},
-                "pt_curve": pt_curve, "nrc_curve": nrc_curve, "data": "synthetic", "dtype": "f32 paths, f16 MLP"}
-        print(json.dumps(line), flush=True)
+            chunk = min(chunk * 2, max(1, 64 // spf), max(1, at_frames - frames) if at_n is None else 1 << 30)
         img.close()
         cache.close()
-    ds.close()
-    ctx.close()
+        return {"value": (reached / t_pt) if reached else None, "t_nrc_s": round(reached, 4) if reached else None,
+                "t_nrc_warmup_s": round(t_warm, 4), "nrc_rmse_at_equal_time": at_equal_time,
+                f"after_{at_frames}_frames": at_n,
+                "nrc": {"terminate_depth": td, "train_fraction": round(tf, 5), "train_steps": steps,
+                        "train_length": tl, "unbiased_fraction": 1.0 / 16 if tl else None,
+                        "terminate_spread": spread, "samples_per_frame": spf, "warmup_frames": warmup,
+                        "max_train_samples": 65536, "ema": 0.99,
+                        "mlp": "64-64x4-3 ReLU fp16, fp32 accumulate, Adam lr 1e-2"},
+                "nrc_curve": curve}
+
+    def close(self):
+        self.ds.close()
+        self.ctx.close()
+
+
+def nrc_headline(args):
+    """The second headline, time to equal RMSE of the radiance cache against
+    plain PT on the heightfield workload at 1280 x 720, as the workload
+    states it: 1 spp per frame, 65,536 training samples per frame, ratio =
+    (cache time to the plain tracer's 1024-spp RMSE) / (plain time to 1024
+    spp); null when the cache does not get there within 3x the plain
+    time."""
+    st = NrcSetup("PT", 1280, 720, args.nrc_ref_spp, args.nrc_rr)
+    try:
+        t_pt, target, pt_curve = st.plain(1024)
+        r = st.cache_run(t_pt, target, args.nrc_td, 1, args.nrc_train_steps, args.nrc_train_length,
+                         args.nrc_spread, args.nrc_warmup)
+        plain_at_64 = next(c for c in pt_curve if c[0] >= 64)
+        out = {"metric": "time to the 1024-spp plain-PT RMSE, PT with the radiance cache / plain PT",
+               "unit": "ratio", "higher_is_better": False, "value": r.pop("value"),
+               "t_pt_s": round(t_pt, 4), "target_rmse": target, "plain_pt_at_64_spp": plain_at_64}
+        out.update(r)
+        out["config"] = {"workload": st.workload, "resolution": [1280, 720], "reference_spp": st.ref_spp,
+                         "reference_s": round(st.t_ref, 2), "rr_start_depth": st.rr,
+                         "timing": "host clock around synchronised calls"}
+        out["pt_curve"] = pt_curve
+        return out
+    finally:
+        st.close()
+
+
+def run_nrc(args):
+    """Time to equal RMSE, rendering with the radiance cache vs the plain
+    renderer of the same pass (NrcSetup): the plain pass accumulates 1024
+    spp (doubling chunks); its final RMSE is the target and its wall time
+    T_plain. Each cache setting (--nrc-configs) first trains for
+    --nrc-warmup frames (timed, not accumulated), then accumulates frames
+    until its RMSE reaches the target or its time exceeds 3 T_plain."""
+    pass_ = args.nrc_pass
+    W, H = args.nrc_size if args.nrc_size else ((640, 360) if pass_ == "PT" else (480, 270))
+    st = NrcSetup(pass_, W, H, args.nrc_ref_spp, args.nrc_rr)
+    t_pt, target, pt_curve = st.plain(1024)
+
+    def parse(c):
+        v = [float(x) for x in c.split(",")]
+        v += [args.nrc_train_length, args.nrc_spread][len(v) - 3:] if len(v) < 5 else []
+        return int(v[0]), int(v[1]), int(v[2]), int(v[3]), v[4]
+
+    configs = [parse(c) for c in args.nrc_configs.split(";")] if args.nrc_configs else \
+        [(args.nrc_td, args.nrc_spf, args.nrc_train_steps, args.nrc_train_length, args.nrc_spread)]
+    for td, spf, steps, tl, spread in configs:
+        r = st.cache_run(t_pt, target, td, spf, steps, tl, spread, args.nrc_warmup,
+                         train_fraction=args.nrc_train_fraction)
+        line = {"metric": f"time to the 1024-spp plain-{pass_} RMSE, {pass_} with the radiance cache vs plain {pass_}",
+                "unit": "ratio", "value": r.pop("value"), "higher_is_better": False,
+                "t_pt_s": round(t_pt, 4), "target_rmse": target}
+        line.update(r)
+        line["config"] = {"workload": st.workload, "pass": pass_, "rr_start_depth": st.rr, "resolution": [W, H],
+                          "reference_spp": st.ref_spp, "reference_s": round(st.t_ref, 2), "nrc": line.pop("nrc")}
+        line.update({"pt_curve": pt_curve, "data": "synthetic", "dtype": "f32 paths, f16 MLP"})
+        print(json.dumps(line), flush=True)
+    st.close()
 
 
 def main():
@@ -895,6 +977,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-nrc", action="store_true",
+                    help="leave out the radiance-cache time-to-equal-RMSE key of the default line")
     ap.add_argument("--passes", default=None,
                     help="passes workload: comma-separated subset of PT,LT,BPT,WHITTED,PM,IM,HIERARCHY")
     ap.add_argument("--shared-nodes", type=int, default=0,
@@ -918,13 +1002,18 @@ def main():
     ap.add_argument("--nrc-pass", choices=["PT", "BPT"], default="PT",
                     help="PT: heightfield workload; BPT: large workload (eye paths stop at the cache vertex)")
     ap.add_argument("--nrc-size", type=int, nargs=2, default=None, help="default 640 360 (PT), 480 270 (BPT)")
-    ap.add_argument("--nrc-ref-spp", type=int, default=16384)
+    ap.add_argument("--nrc-ref-spp", type=int, default=8192)
     ap.add_argument("--nrc-spf", type=int, default=16, help="samples per cache frame")
-    ap.add_argument("--nrc-warmup", type=int, default=16, help="training frames before accumulation")
+    ap.add_argument("--nrc-warmup", type=int, default=32, help="training frames before accumulation")
     ap.add_argument("--nrc-train-fraction", type=float, default=0.0,
                     help="share of training paths (0: about 98k training vertices per frame)")
-    ap.add_argument("--nrc-configs", default="", help="'td,spf,steps;...' several cache settings in one run")
+    ap.add_argument("--nrc-configs", default="",
+                    help="'td,spf,steps[,train_length[,spread]];...' several cache settings in one run")
     ap.add_argument("--nrc-train-steps", type=int, default=4)
+    ap.add_argument("--nrc-train-length", type=int, default=0,
+                    help="self-training: training paths take the cache's radiance at this vertex (0: off)")
+    ap.add_argument("--nrc-spread", type=float, default=0.0,
+                    help="path-spread termination constant c (0: stop at --nrc-td)")
     ap.add_argument("--nrc-td", type=int, default=2, help="path vertex where render paths query the cache")
     ap.add_argument("--nrc-rr", type=int, default=0, help="Russian roulette start depth of both tracers")
     args = ap.parse_args()

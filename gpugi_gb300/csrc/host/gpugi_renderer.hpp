@@ -79,6 +79,8 @@ public:
     // Accumulated sums, row 0 = bottom row of the screen (GL convention).
     std::vector<float> ReadRGBA() const;
     std::vector<double> ReadRGB64() const;
+    // Replaces the sums (gpugi_image_write); an empty rgb64 zeroes an FP64 accumulation.
+    void Write(const std::vector<float>& rgba, const std::vector<double>& rgb64);
     gpugi_image* GetHandle() const { return m_image; }
     gpugi_ctx* GetContext() const { return m_ctx; }
 
@@ -231,6 +233,20 @@ public:
     // light samples from the light sampler.
     void PerIterationBufferUpdate(bool iterationIncrement = true);
 
+    // Checkpoint of a long accumulation (an addition: the reference only
+    // saves the normalised backbuffer, Application::SaveImage,
+    // application.cpp:394-414). Writes <base>.pfm (the average, as SaveImage
+    // does), <base>.accum (the exact sums: height x width RGBA float32, then
+    // height x width RGB float64 with an FP64 backbuffer, little-endian) and
+    // <base>.json (size, iteration count, the frame index of the next
+    // iteration, the light sampler's state for the next iteration's light
+    // samples, the active renderer and the settings).
+    bool SaveCheckpoint(const std::string& base) const;
+    // Restores the sums, the iteration count and the light sampler from a
+    // checkpoint of the same screen size and renderer, so that further Draw
+    // calls continue the same estimator. Throws GpugiError on a mismatch.
+    void LoadCheckpoint(const std::string& base);
+
     // Parameters the reference keeps in GlobalConfig and shader defines.
     void SetMaxPathLength(unsigned int pathLength) { m_maxPathLength = pathLength; }
     unsigned int GetMaxPathLength() const { return m_maxPathLength; }
@@ -264,6 +280,7 @@ private:
     unsigned int m_numInitialLightSamples = 0;
     std::vector<float> m_lightSamples;  // 8 floats per initial light sample
     uint64_t m_lightSamplerState = 123;  // LightSampler's xorshift state
+    uint64_t m_lightSamplerStateBefore = 123;  // the state that drew m_lightSamples
     unsigned int m_maxPathLength = 8;
     unsigned int m_rrStartDepth = 0;
     bool m_referenceRng = false;

@@ -11,7 +11,11 @@
 //                  [--camera px py pz lx ly lz fovy] [--iterations N]
 //                  [--path-length L] [--rr-start D] [--sky r g b] [--reference-rng]
 //                  [--point-light px py pz ir ig ib] [--reference FILE.pfm]
-//                  [--out FILE.pfm] [--device D]
+//                  [--out FILE.pfm] [--checkpoint BASE] [--resume BASE] [--device D]
+//
+// --resume BASE restores a checkpoint (RendererSystem::LoadCheckpoint) before
+// drawing, --checkpoint BASE writes one after (SaveCheckpoint), so a long
+// accumulation can run as several invocations with the same settings.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -23,7 +27,7 @@
 namespace {
 
 struct Args {
-    std::string scene, renderer = "Pathtracer", out, reference;
+    std::string scene, renderer = "Pathtracer", out, reference, checkpoint, resume;
     int width = 256, height = 256, iterations = 16, device = 0;
     unsigned pathLength = 8, rrStart = 0;
     float cam[7] = {0.0f, 1.0f, 3.4f, 0.0f, 1.0f, 0.0f, 40.0f};
@@ -48,6 +52,8 @@ Args parse(int argc, char** argv) {
         else if (k == "--renderer") { need(i, 1); a.renderer = argv[++i]; }
         else if (k == "--out") { need(i, 1); a.out = argv[++i]; }
         else if (k == "--reference") { need(i, 1); a.reference = argv[++i]; }
+        else if (k == "--checkpoint") { need(i, 1); a.checkpoint = argv[++i]; }
+        else if (k == "--resume") { need(i, 1); a.resume = argv[++i]; }
         else if (k == "--size") { need(i, 2); a.width = std::atoi(argv[++i]); a.height = std::atoi(argv[++i]); }
         else if (k == "--iterations") { need(i, 1); a.iterations = std::atoi(argv[++i]); }
         else if (k == "--device") { need(i, 1); a.device = std::atoi(argv[++i]); }
@@ -101,7 +107,9 @@ int main(int argc, char** argv) {
         else if (a.renderer == "HierarchyImportance") system.SetRenderer<HierarchyImportance>();
         else usage("unknown renderer");
 
+        if (!a.resume.empty()) system.LoadCheckpoint(a.resume);
         for (int i = 0; i < a.iterations; ++i) system.Draw();
+        if (!a.checkpoint.empty() && !system.SaveCheckpoint(a.checkpoint)) usage("cannot write the checkpoint");
 
         const unsigned long iterations = system.GetIterationCount();
         double mse = -1.0;

@@ -2,6 +2,7 @@
 // C ABI of the CUDA library.
 #include "gpugi_renderer.hpp"
 
+#include <cctype>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -51,6 +52,14 @@ std::vector<double> DeviceImage::ReadRGB64() const {
     std::vector<double> out((size_t)m_width * m_height * 3);
     check_status(m_ctx, gpugi_image_read(m_ctx, m_image, nullptr, out.data()), "gpugi_image_read");
     return out;
+}
+
+void DeviceImage::Write(const std::vector<float>& rgba, const std::vector<double>& rgb64) {
+    const size_t n = (size_t)m_width * m_height;
+    if (rgba.size() != 4 * n || !(rgb64.empty() || rgb64.size() == 3 * n))
+        throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "image data of the wrong size");
+    check_status(m_ctx, gpugi_image_write(m_ctx, m_image, rgba.data(), rgb64.empty() ? nullptr : rgb64.data()),
+                 "gpugi_image_write");
 }
 
 // --------------------------------------------------------------------- Camera
@@ -259,9 +268,127 @@ void RendererSystem::ResetIterationCount() { m_iterationCount = 0; }
 // renderersystem.cpp:95-116: advance the iteration, draw the next light samples.
 void RendererSystem::PerIterationBufferUpdate(bool iterationIncrement) {
     if (iterationIncrement) ++m_iterationCount;
+    m_lightSamplerStateBefore = m_lightSamplerState;
     if (m_scene && m_numInitialLightSamples)
         Check(gpugi_generate_light_samples(m_scene->GetHandle(), &m_lightSamplerState, m_numInitialLightSamples,
                                            m_lightSamples.data()));
+}
+
+namespace {
+// Values of the flat JSON object the checkpoint sidecar is: the text after
+// "key": up to the next comma or brace.
+bool json_value(const std::string& text, const char* key, std::string& out) {
+    const std::string k = std::string("\"") + key + "\"";
+    size_t at = text.find(k);
+    if (at == std::string::npos) return false;
+    at = text.find(':', at + k.size());
+    if (at == std::string::npos) return false;
+    ++at;
+    while (at < text.size() && std::isspace((unsigned char)text[at])) ++at;
+    if (at < text.size() && text[at] == '"') {
+        const size_t end = text.find('"', at + 1);
+        if (end == std::string::npos) return false;
+        out = text.substr(at + 1, end - at - 1);
+        return true;
+    }
+    size_t end = at;
+    while (end < text.size() && text[end] != ',' && text[end] != '}' && text[end] != '\n') ++end;
+    out = text.substr(at, end - at);
+    while (!out.empty() && std::isspace((unsigned char)out.back())) out.pop_back();
+    return !out.empty();
+}
+
+uint64_t json_u64(const std::string& text, const char* key) {
+    std::string v;
+    if (!json_value(text, key, v)) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, std::string("checkpoint lacks ") + key);
+    return std::strtoull(v.c_str(), nullptr, 10);
+}
+
+std::string json_escape(const std::string& s) {
+    std::string out;
+    for (char c : s) {
+        if (c == '"' || c == '\\') out += '\\';
+        out += c;
+    }
+    return out;
+}
+
+std::string base_name(const std::string& path) {
+    const size_t slash = path.find_last_of('/');
+    return slash == std::string::npos ? path : path.substr(slash + 1);
+}
+
+std::string dir_name(const std::string& path) {
+    const size_t slash = path.find_last_of('/');
+    return slash == std::string::npos ? std::string() : path.substr(0, slash + 1);
+}
+}  // namespace
+
+bool RendererSystem::SaveCheckpoint(const std::string& base) const {
+    if (!m_backbuffer) return false;
+    const int w = m_backbuffer->GetWidth(), h = m_backbuffer->GetHeight();
+    const std::vector<float> rgba = m_backbuffer->ReadRGBA();
+    if (!WritePfm(rgba.data(), ei::IVec2(w, h), base + ".pfm", (std::uint32_t)m_iterationCount)) return false;
+    {
+        std::ofstream f((base + ".accum").c_str(), std::ios::binary);
+        if (!f) return false;
+        f.write(reinterpret_cast<const char*>(rgba.data()), (std::streamsize)(rgba.size() * sizeof(float)));
+        if (m_backbuffer->HasFP64()) {
+            const std::vector<double> rgb64 = m_backbuffer->ReadRGB64();
+            f.write(reinterpret_cast<const char*>(rgb64.data()), (std::streamsize)(rgb64.size() * sizeof(double)));
+        }
+        if (!f) return false;
+    }
+    std::ofstream j((base + ".json").c_str());
+    if (!j) return false;
+    const ei::Vec3 sky = GetSkyRadiance();
+    j << "{\n \"format\": \"gpugi_gb300 checkpoint\",\n \"version\": 1,\n"
+      << " \"width\": " << w << ",\n \"height\": " << h << ",\n"
+      << " \"fp64\": " << (m_backbuffer->HasFP64() ? "true" : "false") << ",\n"
+      << " \"iterations\": " << m_iterationCount << ",\n \"next_iteration\": " << m_iterationCount << ",\n"
+      << " \"rng_state\": " << m_lightSamplerStateBefore << ",\n"
+      << " \"image\": \"" << json_escape(base_name(base)) << ".pfm\",\n"
+      << " \"accumulation\": \"" << json_escape(base_name(base)) << ".accum\",\n"
+      << " \"renderer\": \"" << json_escape(m_activeRenderer ? m_activeRenderer->GetName() : std::string()) << "\",\n"
+      << " \"max_path_length\": " << m_maxPathLength << ",\n \"rr_start_depth\": " << m_rrStartDepth << ",\n"
+      << " \"random\": \"" << (m_referenceRng ? "reference" : "pcg") << "\",\n"
+      << " \"num_light_samples\": " << m_numInitialLightSamples << ",\n";
+    char skyText[96];
+    std::snprintf(skyText, sizeof skyText, " \"sky\": [%.9g, %.9g, %.9g]\n}\n", sky.x, sky.y, sky.z);
+    j << skyText;
+    return (bool)j;
+}
+
+void RendererSystem::LoadCheckpoint(const std::string& base) {
+    std::ifstream jf((base + ".json").c_str());
+    if (!jf) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "cannot read " + base + ".json");
+    const std::string text((std::istreambuf_iterator<char>(jf)), std::istreambuf_iterator<char>());
+    std::string v;
+    if (!json_value(text, "format", v) || v != "gpugi_gb300 checkpoint" || json_u64(text, "version") != 1)
+        throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, base + ".json is not a version-1 checkpoint");
+    if (!m_backbuffer || (int)json_u64(text, "width") != m_backbuffer->GetWidth() ||
+        (int)json_u64(text, "height") != m_backbuffer->GetHeight())
+        throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "checkpoint size differs from the screen size");
+    if (json_value(text, "renderer", v) && !v.empty() && m_activeRenderer && v != m_activeRenderer->GetName())
+        throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "checkpoint of renderer " + v);
+    const bool fp64 = json_value(text, "fp64", v) && v == "true";
+    std::string accum = base + ".accum";
+    if (json_value(text, "accumulation", v)) accum = dir_name(base) + v;
+    const size_t n = (size_t)m_backbuffer->GetWidth() * m_backbuffer->GetHeight();
+    std::vector<float> rgba(4 * n);
+    std::vector<double> rgb64;
+    std::ifstream af(accum.c_str(), std::ios::binary);
+    af.read(reinterpret_cast<char*>(rgba.data()), (std::streamsize)(rgba.size() * sizeof(float)));
+    if (fp64) {
+        rgb64.resize(3 * n);
+        af.read(reinterpret_cast<char*>(rgb64.data()), (std::streamsize)(rgb64.size() * sizeof(double)));
+    }
+    if (!af) throw GpugiError(GPUGI_ERROR_INVALID_ARGUMENT, "cannot read " + accum);
+    if (fp64 && !m_backbuffer->HasFP64()) rgb64.clear();  // the FP32 sums carry the estimate
+    m_backbuffer->Write(rgba, rgb64);
+    m_iterationCount = (unsigned long)json_u64(text, "next_iteration");
+    m_lightSamplerState = json_u64(text, "rng_state");
+    PerIterationBufferUpdate(false);  // the light samples of the next iteration
 }
 
 gpugi_render_params RendererSystem::MakeRenderParams(gpugi_pass pass) const {

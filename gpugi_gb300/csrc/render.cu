@@ -20,6 +20,8 @@
 //
 // Per-path RNG streams, the order of RNG draws and all shading formulas are
 // those of the shaders, so each estimator is the reference's.
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -92,6 +94,9 @@ struct RenderConst {
     // radiance cache (PT with NRC); unused by the other passes
     int nrcTerminateDepth;       // render paths query the cache at this vertex
     uint32_t nrcTrainThreshold;  // pixel hash below this: a training path
+    int nrcTrainLength;          // self-training: training paths query the cache at this vertex (0: off)
+    uint32_t nrcUnbiasedThreshold;  // training-path hash below this: never stops at the cache
+    float nrcSpread;             // > 0: render paths stop once the path spread exceeds this x a0
     float* tvRec;                // training vertices: 16 floats {pos, dir, normal, albedo, T, pad}
     float* tvC;                  // training vertices: 3 floats, radiance accumulated after the vertex
     uint32_t* tvCount;           // vertices recorded per training path
@@ -1353,11 +1358,13 @@ __global__ void k_nrc_generate(RenderConst rc, PathSoA A) {
             const uint32_t slot = atomicAdd(rc.trainPaths, 1u);
             if (slot < rc.trainCap) {
                 info |= 2u;
+                if (wanghash(slot ^ wanghash(frame + 0x7F4A7C15u)) < rc.nrcUnbiasedThreshold) info |= 4u;
                 slotBits = __uint_as_float(slot);
                 rc.tvCount[slot] = 0;
             }
         }
         store_path(A, p, rc.camPos, d, f3(1.0f), seed, pix, info, slotBits);
+        A.job[p] = 0u;
     }
 }
 
@@ -1369,18 +1376,33 @@ GPUGI_D void add3(float* p, float3 c) {
 
 // One bounce of the path tracer with a radiance cache, per lane. Render
 // paths stop at vertex nrcTerminateDepth and query the cache for the
-// radiance reflected there towards the previous vertex; training paths
+// radiance reflected there towards the previous vertex; with nrcSpread > 0
+// they stop earlier, at the first vertex n >= 1 where the path spread
+// a(x1..xn) exceeds nrcSpread x a0 (Mueller et al. 2021, "Real-time Neural
+// Radiance Caching for Path Tracing", section 3.4: sqrt(a) is the sum over
+// the segments of |x_{i-1} - x_i| / sqrt(p(w_i) |cos theta_i|), a0 =
+// |x0 - x1|^2 / (4 pi cos theta_1) at the primary vertex). Training paths
 // continue as plain path tracing and record every vertex {position,
 // outgoing direction, normal, albedo, throughput}; the radiance that later
 // reaches each vertex (NEE via the shadow queue, emission and sky found by
-// the next segment) is accumulated into the vertex's tvC entry. A training
-// path with pixel kNoPixel (BPT with the cache) only trains.
+// the next segment) is accumulated into the vertex's tvC entry. With
+// self-training (nrcTrainLength > 0) a training path stops at vertex
+// nrcTrainLength and queries the cache there; the query's radiance x
+// throughput goes to the previous vertex's tvC like emission found by the
+// segment, except for the unbiased training paths (info bit 2), which run
+// to the path's end. A training path with pixel kNoPixel (BPT with the
+// cache) only trains.
+// Spread state of a render path: job = sqrt(nrcSpread a0) as float bits,
+// lastP = half2 {sqrt(a) / sqrt(nrcSpread a0), 1 / sqrt(pdf of the last
+// sampled direction)}.
+constexpr uint32_t kTrainQuery = 0x80000000u;  // query record pixel: radiance goes to training vertex (low bits)
+
 struct NrcLane {
     bool survive = false, shadow = false, query = false;
     float3 o, d, tp, sro, srd, contrib, qN, qAlbedo, qT;
     float srl = 0.0f, lastP = 0.0f;
     Rng seed{0, 0};
-    uint32_t pixel = 0, info = 0, train = kNoTrain;
+    uint32_t pixel = 0, info = 0, train = kNoTrain, job = 0, qPixel = 0;
 };
 
 GPUGI_D void nrc_pt_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& H, uint32_t k, int depth,
@@ -1400,6 +1422,7 @@ GPUGI_D void nrc_pt_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& 
     const bool training = (L.info & 2u) != 0;
     const uint32_t tslot = __float_as_uint(L.lastP);
     const uint32_t prevVertex = (training && depth > 0) ? tslot * stride + depth - 1 : kNoTrain;
+    L.job = A.job[k];
     Hit h = load_hit(rc, H, k, o, d);
     if (!h.valid) {
         const float3 c = tp * rc.sky;
@@ -1413,11 +1436,25 @@ GPUGI_D void nrc_pt_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& 
         splat(rc, L.pixel, e);
         if (prevVertex != kNoTrain) add3(rc.tvC + 3 * (size_t)prevVertex, e);
     }
-    if (!training && depth == rc.nrcTerminateDepth) {
+    bool stop = training ? (rc.nrcTrainLength > 0 && depth == rc.nrcTrainLength && !(L.info & 4u))
+                         : depth == rc.nrcTerminateDepth;
+    float spreadSum = 0.0f;
+    if (!training && rc.nrcSpread > 0.0f) {
+        const float cosIn = fmaxf(fabsf(dot(h.N, d)), 1e-4f);
+        if (depth == 0) {
+            L.job = __float_as_uint(h.t * sqrtf(rc.nrcSpread / (4.0f * kPI * cosIn)));
+        } else {
+            const float2 st = __half22float2(*reinterpret_cast<const __half2*>(&L.lastP));
+            spreadSum = st.x + h.t * st.y / (sqrtf(cosIn) * fmaxf(__uint_as_float(L.job), 1e-30f));
+            stop = stop || spreadSum > 1.0f;
+        }
+    }
+    if (stop) {
         L.query = true;
         L.qN = h.N;
         L.qAlbedo = h.m.Diffuse;
         L.qT = tp;
+        L.qPixel = training ? (kTrainQuery | prevVertex) : L.pixel;
         return;
     }
     const bool didNEE = h.m.Reflectiveness.w < 500.0f;
@@ -1446,6 +1483,10 @@ GPUGI_D void nrc_pt_lane(const RenderConst& rc, const PathSoA& A, const HitSoA& 
     o = o + d * kRAY_HIT_EPSILON;
     tp *= thr;
     L.survive = roulette(rc, depth, thr, tp, L.seed) && depth + 1 < rc.maxPathLength;
+    if (!training && rc.nrcSpread > 0.0f) {
+        const __half2 st = __floats2half2_rn(fminf(spreadSum, 60000.0f), fminf(rsqrtf(fmaxf(pdf, 1e-8f)), 60000.0f));
+        L.lastP = *reinterpret_cast<const float*>(&st);
+    }
 }
 
 // Cache query record: 12 floats {position, direction towards the previous
@@ -1473,9 +1514,12 @@ __global__ void __launch_bounds__(128) k_nrc_shade(RenderConst rc, PathSoA A, Pa
         warp_append(&rc.cnt->shadow[depth], L.shadow, qs);
         if (L.shadow) store_shadow(Q, qs, L.sro, L.srd, L.srl, L.contrib, L.pixel, L.train);
         warp_append(rc.queryCount, L.query, qq);
-        if (L.query && qq < rc.queryCap) store_query(rc, qq, L.o, L.d, L.qN, L.qAlbedo, L.qT, L.pixel);
+        if (L.query && qq < rc.queryCap) store_query(rc, qq, L.o, L.d, L.qN, L.qAlbedo, L.qT, L.qPixel);
         warp_append(&rc.cnt->path[depth + 1], L.survive, qb);
-        if (L.survive) store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, L.lastP);
+        if (L.survive) {
+            store_path(B, qb, L.o, L.d, L.tp, L.seed, L.pixel, L.info, L.lastP);
+            B.job[qb] = L.job;
+        }
     }
 }
 
@@ -1525,20 +1569,21 @@ __global__ void __launch_bounds__(128) k_nrc_bpt_shade(RenderConst rc, PathSoA A
         float3 o, d, tp, sro, srd, contrib, qN, qA, qT;
         float srl = 0.0f, lastP = 0.0f, misProd = 1.0f;
         Rng seed{0, 0};
-    uint32_t pixel = 0, info = 0, train = kNoTrain;
+        uint32_t pixel = 0, info = 0, train = kNoTrain, qPixel = 0;
         if (valid) {
             if (A.info[k] & 2u) {
                 NrcLane L;
                 nrc_pt_lane(rc, A, H, k, depth, L);
-                survive = L.survive; shadow = L.shadow;
+                survive = L.survive; shadow = L.shadow; query = L.query;
                 o = L.o; d = L.d; tp = L.tp; sro = L.sro; srd = L.srd; contrib = L.contrib; srl = L.srl;
+                qN = L.qN; qA = L.qAlbedo; qT = L.qT; qPixel = L.qPixel;
                 lastP = L.lastP; seed = L.seed; pixel = L.pixel; info = L.info; train = L.train;
             } else {
                 BptLane L;
                 bpt_shade_lane(rc, A, H, k, depth, cap, rc.nrcTerminateDepth, L);
                 survive = L.survive; shadow = L.shadow; query = L.query;
                 o = L.o; d = L.d; tp = L.tp; sro = L.sro; srd = L.srd; contrib = L.contrib; srl = L.srl;
-                qN = L.qN; qA = L.qAlbedo; qT = L.qT;
+                qN = L.qN; qA = L.qAlbedo; qT = L.qT; qPixel = L.pixel;
                 lastP = L.lastP; misProd = L.misProd; seed = L.seed; pixel = L.pixel; info = L.info;
             }
         }
@@ -1546,7 +1591,7 @@ __global__ void __launch_bounds__(128) k_nrc_bpt_shade(RenderConst rc, PathSoA A
         warp_append(&rc.cnt->shadow[depth], shadow, qs);
         if (shadow) store_shadow(Q, qs, sro, srd, srl, contrib, pixel, train);
         warp_append(rc.queryCount, query, qq);
-        if (query && qq < rc.queryCap) store_query(rc, qq, o, d, qN, qA, qT, pixel);
+        if (query && qq < rc.queryCap) store_query(rc, qq, o, d, qN, qA, qT, qPixel);
         warp_append(&rc.cnt->path[depth + 1], survive, qb);
         if (survive) {
             store_path(B, qb, o, d, tp, seed, pixel, info, lastP);
@@ -1555,12 +1600,16 @@ __global__ void __launch_bounds__(128) k_nrc_bpt_shade(RenderConst rc, PathSoA A
     }
 }
 
-// Splat throughput x cache radiance for every query.
+// Splat throughput x cache radiance for every query; a self-training query
+// adds it to its training vertex instead.
 __global__ void k_nrc_apply(RenderConst rc, const float* __restrict__ radiance) {
     const uint32_t n = min(*rc.queryCount, rc.queryCap);
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const float3 t = make_float3(rc.qT[3 * q], rc.qT[3 * q + 1], rc.qT[3 * q + 2]);
-        splat(rc, rc.qPixel[q], t * make_float3(radiance[3 * q], radiance[3 * q + 1], radiance[3 * q + 2]));
+        const float3 c = t * make_float3(radiance[3 * q], radiance[3 * q + 1], radiance[3 * q + 2]);
+        const uint32_t pix = rc.qPixel[q];
+        if (pix != kNoPixel && (pix & kTrainQuery)) add3(rc.tvC + 3 * (size_t)(pix & ~kTrainQuery), c);
+        else splat(rc, pix, c);
     }
 }
 
@@ -2328,6 +2377,23 @@ gpugi_status gpugi_image_read(gpugi_ctx* ctx, const gpugi_image* im, float* rgba
     return gpugi_sync(ctx);
 }
 
+gpugi_status gpugi_image_write(gpugi_ctx* ctx, gpugi_image* im, const float* rgba, const double* rgb64) {
+    if (!ctx || !im) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!rgba) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "rgba is required");
+    if (rgb64 && !im->rgb64) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "image has no FP64 accumulation");
+    const size_t n = (size_t)im->width * im->height;
+    GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(im->rgba, rgba, n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    if (im->rgb64) {
+        if (rgb64)
+            GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(im->rgb64, rgb64, n * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                                                ctx->stream));
+        else
+            GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(im->rgb64, 0, n * 3 * sizeof(double), ctx->stream));
+    }
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return GPUGI_OK;
+}
+
 gpugi_status gpugi_image_mse(gpugi_ctx* ctx, const gpugi_image* im, double divisor, const float* reference,
                              uint32_t useFp64, double* mse) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
@@ -2478,6 +2544,10 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "either lightSamples or rngState is required");
     if (!(np->trainFraction >= 0.0f && np->trainFraction <= 1.0f))
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "trainFraction must be in [0, 1]");
+    if (!(np->unbiasedFraction >= 0.0f && np->unbiasedFraction <= 1.0f) || !(np->terminateSpread >= 0.0f) ||
+        np->trainLength >= p->maxPathLength + 1u)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT,
+                    "unbiasedFraction must be in [0, 1], terminateSpread >= 0, trainLength <= maxPathLength");
     const uint32_t numPixels = p->width * p->height;
     const uint32_t spf = std::max<uint32_t>(1u, std::min(np->samplesPerFrame, p->samples));
     if ((uint64_t)spf * numPixels > (64ull << 20))
@@ -2511,11 +2581,18 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     if ((st = ensure_host_lights(ctx, rb, lightBytes))) return st;
     const size_t trainCap = bpt ? (size_t)nTrain + 64 : (size_t)(np->trainFraction * framePaths * 1.25) + 64;
     const size_t sampleCap = np->maxTrainSamples ? np->maxTrainSamples : 65536;
-    if ((st = ensure_nrc_buffers(ctx, rb, framePaths, trainCap, p->maxPathLength, sampleCap))) return st;
+    if ((uint64_t)trainCap * p->maxPathLength >= (uint64_t)kTrainQuery)
+        return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "too many training vertices per frame");
+    // queries: one per render path, and one per self-training path
+    const size_t queryCap = (size_t)framePaths + (np->trainLength ? trainCap : 0);
+    if ((st = ensure_nrc_buffers(ctx, rb, queryCap, trainCap, p->maxPathLength, sampleCap))) return st;
 
     RenderConst rc = make_render_const(ctx, sc, cam, p, im, rb);
     rc.nrcTerminateDepth = (int)np->terminateDepth;
     rc.nrcTrainThreshold = (uint32_t)std::min(4294967295.0, (double)np->trainFraction * 4294967296.0);
+    rc.nrcTrainLength = (int)np->trainLength;
+    rc.nrcUnbiasedThreshold = (uint32_t)std::min(4294967295.0, (double)np->unbiasedFraction * 4294967296.0);
+    rc.nrcSpread = bpt ? 0.0f : np->terminateSpread;
     rc.tvRec = rb->tvRec;
     rc.tvC = rb->tvC;
     rc.tvCount = rb->tvCount;
@@ -2525,7 +2602,7 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     rc.qT = rb->qT;
     rc.qPixel = rb->qPixel;
     rc.queryCount = rb->nrcCounters;
-    rc.queryCap = framePaths;
+    rc.queryCap = (uint32_t)queryCap;
     rc.numRaysPerLightSample = (int)raysPerLight;
     rc.lightThreads = lightThreads;
     rc.cacheCap = (uint32_t)cachePerSample;
@@ -2579,7 +2656,7 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
         // cache lookups of this frame (the network as trained by earlier
         // frames); counts stay on the device, so frames queue back to back
-        if ((st = nrc_infer_counted(ctx, nn, rb->queries, framePaths, rb->nrcCounters, rb->radiance))) return st;
+        if ((st = nrc_infer_counted(ctx, nn, rb->queries, queryCap, rb->nrcCounters, rb->radiance))) return st;
         k_nrc_apply<<<ctx->numSMs * 4, 256, 0, ctx->stream>>>(rc, rb->radiance);
         // training on this frame's training paths
         if (np->train && np->trainFraction > 0.0f) {

@@ -47,6 +47,7 @@ def _declare():
     L.gpugi_image_destroy.restype = None
     L.gpugi_image_clear.argtypes = [P, P]
     L.gpugi_image_read.argtypes = [P, P, P, P]
+    L.gpugi_image_write.argtypes = [P, P, P, P]
     L.gpugi_image_mse.argtypes = [P, P, D, P, U32, C.POINTER(D)]
     L.gpugi_scene_add_point_light.argtypes = [P, P, P]
     L.gpugi_scene_add_directional_light.argtypes = [P, P, P]
@@ -98,6 +99,15 @@ class Image:
         out = np.zeros((self.height, self.width, 3), np.float64)
         self.ctx.check(_declare().gpugi_image_read(self.ctx.handle, self._h, None, cuda._ptr(out)))
         return out
+
+    def write(self, rgba: np.ndarray, rgb64: np.ndarray | None = None) -> None:
+        """Replace the sums (gpugi_image_write); rgb64 None zeroes an FP64 accumulation."""
+        a = np.ascontiguousarray(rgba, dtype=np.float32)
+        assert a.shape == (self.height, self.width, 4)
+        b = None if rgb64 is None else np.ascontiguousarray(rgb64, dtype=np.float64)
+        assert b is None or b.shape == (self.height, self.width, 3)
+        self.ctx.check(_declare().gpugi_image_write(self.ctx.handle, self._h, cuda._ptr(a),
+                                                    None if b is None else cuda._ptr(b)))
 
     def mse(self, divisor: float, reference: np.ndarray, use_fp64: bool = False) -> float:
         ref = np.ascontiguousarray(reference[..., :3], dtype=np.float32)

@@ -396,6 +396,11 @@ void gpugi_image_destroy(gpugi_image* image);
 gpugi_status gpugi_image_clear(gpugi_ctx* ctx, gpugi_image* image);
 /* Copy the accumulation to host memory (either pointer may be NULL). */
 gpugi_status gpugi_image_read(gpugi_ctx* ctx, const gpugi_image* image, float* rgba, double* rgb64);
+/* Replace the accumulation with host sums (the inverse of gpugi_image_read;
+ * resuming a checkpointed render, an addition: the reference only writes
+ * PFM, gpugi/imageut/hdrimage.cpp:6-33). rgba is required; rgb64 NULL
+ * zeroes an FP64 accumulation. Synchronous. */
+gpugi_status gpugi_image_write(gpugi_ctx* ctx, gpugi_image* image, const float* rgba, const double* rgb64);
 /* TextureMSE (gpugi/imageut/texturemse.cpp:39-65, utils/sqerror.frag):
  * mean over pixels of |rgb / divisor - reference|^2 (the RGB sum, not the
  * channel mean), reduced in FP64 on the device. reference: host, 3 floats per
@@ -464,7 +469,8 @@ gpugi_status gpugi_nrc_encode_device(gpugi_ctx* ctx, const gpugi_nrc* nrc, const
 /* Path tracing (params->pass PT) or bidirectional path tracing (BPT) with
  * the radiance cache. params->samples iterations run as frames of
  * samplesPerFrame iterations (one wavefront each).
- * PT: camera paths stop at vertex terminateDepth and add throughput x
+ * PT: camera paths stop at vertex terminateDepth (or earlier, by path
+ * spread, with terminateSpread > 0) and add throughput x
  * cache(vertex), except a trainFraction of the paths (chosen by a hash of
  * pixel and iteration) that trace full PT paths whose vertices become
  * training samples {query, radiance reflected towards the previous vertex}.
@@ -489,6 +495,20 @@ typedef struct gpugi_nrc_params {
     uint32_t trainSteps;      /* Adam steps per frame on all of the frame's samples (0 counts as 1) */
     uint32_t train;           /* 0: use the cache without updating it */
     uint32_t samplesPerFrame; /* samples (iterations) traced per frame, one wavefront (0 counts as 1) */
+    /* Self-training (Mueller et al. 2021, "Real-time Neural Radiance Caching
+     * for Path Tracing", section 5): with trainLength >= 1 a training path
+     * stops at vertex trainLength and takes the cache's radiance there, times
+     * its throughput, as the rest of its path; unbiasedFraction of the
+     * training paths (a hash of path and iteration) run to the path's end
+     * instead. trainLength 0: every training path runs to its end. */
+    uint32_t trainLength;
+    float unbiasedFraction;   /* in [0, 1]; read when trainLength >= 1 */
+    /* PT only: > 0 stops a render path at the first vertex n >= 1 whose path
+     * spread a(x1..xn) = (sum of |x_{i-1} - x_i| / sqrt(p(w_i) |cos theta_i|))^2
+     * exceeds terminateSpread x a0, a0 = |x0 - x1|^2 / (4 pi cos theta_1)
+     * (the same paper, section 3.4, c = 0.01 there), and at vertex
+     * terminateDepth at the latest. 0: at vertex terminateDepth. */
+    float terminateSpread;
 } gpugi_nrc_params;
 
 gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* scene, const gpugi_camera* camera,

@@ -130,3 +130,31 @@ def test_headless_reads_materials_from_scene_json(cuda_ctx, room_file, tmp_path)
     _run(["--scene", named] + common + ["--out", b_])
     ia, ib = _read_pfm(a), _read_pfm(b_)
     assert np.abs(ia - ib).max() <= 1e-5 * np.abs(ia).max() + 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("renderer", ["Pathtracer", "BidirectionalPathtracer"])
+def test_headless_checkpoint_resume_continues_the_estimator(cuda_ctx, room_file, tmp_path, renderer):
+    """8 iterations in one run equal 5 iterations, a checkpoint, and 3 more
+    iterations in a second run that resumes it (same frame indices, same
+    light-sample sets; the sums differ only by the order of the atomic
+    additions). The checkpoint's files are the documented format."""
+    from gpugi_gb300 import checkpoint
+    sc, path = room_file
+    base = ["--scene", str(path), "--renderer", renderer, "--size", 24, 20, "--camera", *CAM]
+    one = _run(base + ["--iterations", 8, "--out", tmp_path / "one.pfm"])
+    ck = tmp_path / "ck"
+    first = _run(base + ["--iterations", 5, "--checkpoint", ck])
+    side, rgba, rgb64 = checkpoint.read(str(ck))
+    assert side["iterations"] == side["next_iteration"] == 5 and side["renderer"] == first["renderer"]
+    assert rgb64 is None and rgba.shape == (20, 24, 4)
+    assert np.allclose(checkpoint.read_pfm(str(ck) + ".pfm"), rgba[..., :3] / 5, rtol=1e-6, atol=0)
+    two = _run(base + ["--resume", ck, "--iterations", 3, "--out", tmp_path / "two.pfm"])
+    assert two["iterations"] == one["iterations"] == 8
+    a, b = _read_pfm(tmp_path / "one.pfm"), _read_pfm(tmp_path / "two.pfm")
+    assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max() + 1e-7
+    # a checkpoint of another renderer or size is refused
+    other = "LightPathtracer"
+    r = subprocess.run([str(EXE), "--scene", str(path), "--renderer", other, "--size", "24", "20", "--resume", str(ck)],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 1 and "checkpoint of renderer" in r.stderr

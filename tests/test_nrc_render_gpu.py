@@ -137,3 +137,62 @@ def test_cache_beats_plain_pt_at_equal_samples(cuda_ctx, room):
     assert cuda_ctx.device_error_bits() == 0
     for x in (conv, pt, warm, img, cache):
         x.close()
+
+
+def test_spread_termination_brackets_fixed_depth(cuda_ctx, room):
+    """Path-spread termination (terminate_spread = c): a vanishing c stops
+    every render path at the first vertex it may (vertex 1), a huge c never
+    fires, leaving the terminate_depth cap; both equal the fixed-depth pass
+    with the same (untrained) cache."""
+    sc, b, ds = room
+    W = H = 32
+    frames = 4
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H)
+    ls = _light_sets(ds, frames)
+    cache = nrc.RadianceCache(cuda_ctx, *ROOM_BOX, seed=3)
+
+    def run(td, spread):
+        img = render.Image(cuda_ctx, W, H)
+        nrc.render_nrc(cuda_ctx, ds, cam, img, cache, max_path_length=6, samples=frames, light_samples=ls,
+                       terminate_depth=td, train_fraction=0.0, train=False, terminate_spread=spread)
+        out = img.read()[..., :3]
+        img.close()
+        return out
+
+    for a, r in ((run(5, 1e-30), run(1, 0.0)), (run(3, 1e30), run(3, 0.0))):
+        assert np.abs(a - r).max() <= 1e-5 * np.abs(r).max() + 1e-6
+    mid = run(5, 0.01)  # the paper's c: most paths stop at vertex 1, a few later
+    assert np.isfinite(mid).all() and mid.mean() > 0
+    assert cuda_ctx.device_error_bits() == 0
+    cache.close()
+
+
+@pytest.mark.parametrize("train_length", [0, 2])
+def test_self_training_keeps_the_cache_unbiased(cuda_ctx, room, train_length):
+    """Self-training (training paths take the cache's radiance at vertex
+    train_length, 1/16 of them run to the end): the trained cache's image
+    keeps its mean within 5 % of converged PT, as with full training paths
+    (dropping or misrouting the self-training queries loses the radiance of
+    every bounce after train_length, several percent of the image here)."""
+    sc, b, ds = room
+    W = H = 64
+    depth = 8
+    cam = render.camera_lookat((0.0, 1.2, 2.0), (0.0, 0.0, -0.3), (0.0, 1.0, 0.0), 40.0, W, H)
+    conv = render.Image(cuda_ctx, W, H, fp64=True)
+    n_ref = 2048
+    render.render(cuda_ctx, ds, cam, conv, "PT", max_path_length=depth, samples=n_ref, iteration=1000,
+                  rng_state=[99])
+    reference = conv.read64() / n_ref
+    cache = nrc.RadianceCache(cuda_ctx, *ROOM_BOX, seed=5)
+    opts = dict(max_path_length=depth, terminate_depth=1, train_fraction=0.25, train_steps=4,
+                train_length=train_length)
+    warm = render.Image(cuda_ctx, W, H)
+    nrc.render_nrc(cuda_ctx, ds, cam, warm, cache, samples=300, iteration=10000, rng_state=[11], **opts)
+    img = render.Image(cuda_ctx, W, H, fp64=True)
+    spp = 64
+    nrc.render_nrc(cuda_ctx, ds, cam, img, cache, samples=spp, iteration=20000, rng_state=[13], **opts)
+    mean_nrc = img.read64().mean() / spp
+    assert abs(mean_nrc / reference.mean() - 1) < 0.05, (mean_nrc, reference.mean())
+    assert cuda_ctx.device_error_bits() == 0
+    for x in (conv, warm, img, cache):
+        x.close()
