@@ -778,6 +778,75 @@ def run_batch(args):
     ctx.close()
 
 
+def run_mlp(args):
+    """The radiance cache's MLP kernels alone, both kernel sets (tcgen05 and
+    the warp-level mma.sync one): a training step (forward, backward, weight
+    gradients, Adam) on 65,536 samples and inference of 921,600 queries (the
+    cache lookups of one 1280 x 720 frame). CUDA events on the library's
+    stream around --steps queued calls after --warmup. Tensor work per
+    sample: forward 2 x 17,408 flops; training adds the backward products of
+    layers 4-1 (2 x 13,312) and the weight gradients (2 x 17,408); reported
+    against the measured dense bf16 peak (f16 runs at the same rate)."""
+    import torch
+    from gpugi_gb300 import cuda, nrc
+    ctx = cuda.Context(0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    rng = np.random.default_rng(1)
+
+    def queries(n):
+        q = np.concatenate([rng.uniform(-1, 1, (n, 3)), rng.normal(size=(n, 3)), rng.normal(size=(n, 3)),
+                            rng.uniform(0.1, 0.9, (n, 3))], 1).astype(np.float32)
+        q[:, 3:6] /= np.linalg.norm(q[:, 3:6], axis=1, keepdims=True)
+        q[:, 6:9] /= np.linalg.norm(q[:, 6:9], axis=1, keepdims=True)
+        return q
+
+    nt, ni = 65536, 921600
+    qt = queries(nt)
+    samples = torch.from_numpy(np.concatenate([qt, rng.uniform(0, 2, (nt, 3)).astype(np.float32)], 1)).to(dev)
+    qi = torch.from_numpy(queries(ni)).to(dev)
+    out = torch.empty((ni, 3), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    L = nrc._declare()
+    peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] if (ROOT / "MEASURED_PEAKS.json").exists() \
+        else 1900.0
+    res = {}
+    for k in ("tcgen05", "mma_sync"):
+        c = nrc.RadianceCache(ctx, (-1, -1, -1), (1, 1, 1), seed=3)
+        c.set_kernels(k)
+
+        def timed(fn):
+            for _ in range(args.warmup):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ctx.sync()
+            e0.record(stream)
+            for _ in range(args.steps):
+                fn()
+            e1.record(stream)
+            e1.synchronize()
+            return e0.elapsed_time(e1) / args.steps * 1e3  # us
+
+        t_train = timed(lambda: ctx.check(L.gpugi_nrc_train_device(ctx.handle, c.handle, cuda._ptr(samples), nt,
+                                                                   None)))
+        t_inf = timed(lambda: ctx.check(L.gpugi_nrc_infer_device(ctx.handle, c.handle, cuda._ptr(qi), ni,
+                                                                 cuda._ptr(out))))
+        f_train = 2.0 * nt * (17408 + 13312 + 17408)
+        f_inf = 2.0 * ni * 17408
+        res[k] = {"train_step_us": round(t_train, 2), "train_tflops": round(f_train / t_train / 1e6, 2),
+                  "train_frac_of_peak": round(f_train / t_train / 1e6 / peak, 4),
+                  "infer_us": round(t_inf, 2), "infer_tflops": round(f_inf / t_inf / 1e6, 2),
+                  "infer_frac_of_peak": round(f_inf / t_inf / 1e6 / peak, 4)}
+        c.close()
+    assert ctx.device_error_bits() == 0
+    print(json.dumps({"metric": "radiance-cache MLP: us per training step (65,536 samples) and per inference of "
+                                "921,600 queries", "results": res, "peak_tflops": peak,
+                      "peak_source": "MEASURED_PEAKS.json bf16_tflops (dense)", "steps": args.steps,
+                      "warmup": args.warmup, "data": "synthetic", "dtype": "f16 weights/activations, f32 accumulate"}),
+          flush=True)
+    ctx.close()
+
+
 NRC_WORKLOAD_PT = "heightfield 512x512 fBm (amplitude 0.2) + 500 boxes, sun 5, sky 0.5, depth 8"
 
 
@@ -995,10 +1064,11 @@ def main():
                     help="parts of a host-pointer query whose copies and traversal overlap")
     ap.add_argument("--zero-copy", action="store_true",
                     help="kernels read and write the page-locked host arrays directly instead of staging")
-    ap.add_argument("--workload", choices=["trace", "nrc", "passes", "batch", "large", "build"], default="trace",
+    ap.add_argument("--workload", choices=["trace", "nrc", "passes", "batch", "large", "build", "mlp"], default="trace",
                     help="trace: the closest-hit headline; nrc: time-to-equal-RMSE of the radiance cache; "
                          "passes: samples/s and Mrays/s of PT, LT and BPT; batch: batched vs per-job rendering; "
-                         "large: the 7.9M-triangle workload; build: GPU vs host hierarchy build")
+                         "large: the 7.9M-triangle workload; build: GPU vs host hierarchy build; "
+                         "mlp: the radiance-cache MLP kernels alone")
     ap.add_argument("--nrc-pass", choices=["PT", "BPT"], default="PT",
                     help="PT: heightfield workload; BPT: large workload (eye paths stop at the cache vertex)")
     ap.add_argument("--nrc-size", type=int, nargs=2, default=None, help="default 640 360 (PT), 480 270 (BPT)")
@@ -1021,7 +1091,7 @@ def main():
         from __graft_entry__ import build
         build()
         {"nrc": run_nrc, "passes": run_passes, "batch": run_batch, "large": run_large,
-         "build": run_build}[args.workload](args)
+         "build": run_build, "mlp": run_mlp}[args.workload](args)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -6,12 +6,14 @@
 // rows g and g+8, columns 2t and 2t+1 per lane) holds exactly the elements
 // the A fragment of the next layer needs, so activations stay in registers
 // across all five layers and only the weights come from shared memory.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "ctx.cuh"
 #include "nrc.cuh"
+#include "nrc_tc.cuh"
 
 using namespace gpugi;
 using namespace gpugi::nrc;
@@ -34,12 +36,16 @@ struct gpugi_nrc {
     // (decay emaDecay, bias-corrected; the raw weights while emaSteps == 0)
     float* ema = nullptr;      // fp32 running sum (1 - d) sum d^k w
     __half* wInf = nullptr;    // [l][out][in]
+    __half* wInfT = nullptr;   // the same, [l][in][out] (tcgen05 inference)
     float emaDecay = 0.99f;
     uint32_t emaSteps = 0;
     __half* acts = nullptr;    // training: X_l per sample, [l][n][64]
     __half* dys = nullptr;     // training: dY_l per sample (scaled), [l][n][64]
     float* lossSum = nullptr;  // device scalar
     uint64_t cap = 0;          // samples the training buffers hold
+    // training kernels: tcgen05 (default) or the warp-level mma.sync pair
+    uint32_t kernels = GPUGI_NRC_KERNELS_TCGEN05;
+    float* partials = nullptr;  // tcgen05 training: weight-gradient sums per CTA [numSMs][kParams]
 };
 
 namespace gpugi {
@@ -401,7 +407,7 @@ __global__ void k_nrc_adam(float* __restrict__ w, float* __restrict__ m, float* 
                            const float* __restrict__ grad, float gradScale, const uint32_t* __restrict__ count,
                            uint64_t cap, float lossScale, float lr, float b1, float b2, float eps, float c1, float c2,
                            __half* __restrict__ wFwd, __half* __restrict__ wBwd, float* __restrict__ ema,
-                           float emaDecay, float emaCorr, __half* __restrict__ wInf) {
+                           float emaDecay, float emaCorr, __half* __restrict__ wInf, __half* __restrict__ wInfT) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     bool update = true;
@@ -431,12 +437,13 @@ __global__ void k_nrc_adam(float* __restrict__ w, float* __restrict__ m, float* 
         inf = e * emaCorr;
     }
     wInf[layer_offset(l) + out * kIn + in] = __float2half(inf);
+    wInfT[i] = __float2half(inf);
 }
 
 // fp16 layouts of the master weights (after creation or set_weights); the
 // inference weights restart from them.
 __global__ void k_nrc_publish(const float* __restrict__ w, __half* __restrict__ wFwd, __half* __restrict__ wBwd,
-                              float* __restrict__ ema, __half* __restrict__ wInf) {
+                              float* __restrict__ ema, __half* __restrict__ wInf, __half* __restrict__ wInfT) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     const int l = i < 4 * 4096 ? i / 4096 : 4;
@@ -446,6 +453,7 @@ __global__ void k_nrc_publish(const float* __restrict__ w, __half* __restrict__ 
     wBwd[i] = h;
     wFwd[layer_offset(l) + out * kIn + in] = h;
     wInf[layer_offset(l) + out * kIn + in] = h;
+    wInfT[i] = h;
     ema[i] = 0.0f;
 }
 
@@ -457,6 +465,413 @@ __global__ void k_nrc_encode(const float* __restrict__ queries, uint64_t n, floa
     __half row[kIn];
     encode(load_query(queries, i), boxMin, boxInv, row);
     for (int k = 0; k < kIn; ++k) out[i * kIn + k] = row[k];
+}
+
+// ------------------------------------------------ tcgen05 training kernel
+// One CTA per SM runs 128-sample tiles: thread t owns sample t of a tile
+// (TMEM lane t). Per tile, ten MMA phases, each issued by thread 0 and
+// completed through one mbarrier: forward layers 0-4 (D = X_l W_l), backward
+// layers 4-1 (D = dY_l W_l^T), then the weight gradients of the tile,
+// accumulated in TMEM across all tiles of the CTA. Between phases the
+// threads read D from TMEM, apply ReLU (forward) or the ReLU derivative
+// (backward), and write the next operand to shared memory as fp16.
+// Shared memory (core-matrix layouts, see nrc_tc.cuh):
+//   W   the five weight matrices as stored, [in][out] with out contiguous:
+//       the forward B (K = in, MN-major) and, through a K-major descriptor of
+//       the same bytes, the backward B = W^T (K = out).
+//   X   inputs of all layers of the tile, 320 features per sample
+//       (X_l = features [64 l, 64 l + 64)), sample groups of 8 rows 5120 B
+//       apart: the forward A (K-major) and, MN-major, the A of the weight
+//       gradient of a layer pair: [X_l^T ; X_{l+1}^T] is M = 128.
+//   Y   output gradients of all layers (dY_l = features [64 l, 64 l +
+//       out_l), 272 features): the backward A and the weight-gradient B
+//       [dY_l | dY_{l+1}] (N = 128).
+// The weight gradient of a pair is the diagonal blocks of the 128 x 128
+// product: rows 0-63 x columns 0-63 = dW_l, rows 64-127 x columns 64-127 =
+// dW_{l+1}; layer 4 alone uses N = 16 (rows 64-127 of its D are unused).
+// TMEM (512 columns): D of a phase at column 0, weight gradients of pairs
+// (0,1), (2,3) and layer 4 at columns 128, 256 and 384. Each CTA writes its
+// weight-gradient sums to its own row of `partials`.
+namespace tcl {
+constexpr uint32_t kXSG = 40 * 128, kYSG = 34 * 128;
+constexpr uint32_t kWOff = 0, kWBytes = 4 * 8192 + 2048;
+constexpr uint32_t kXOff = kWBytes, kXBytes = 16 * kXSG;
+constexpr uint32_t kYOff = kXOff + kXBytes + 2048;  // 2 KB pad: rows 64-127 of layer 4's X^T read past X
+constexpr uint32_t kYBytes = 16 * kYSG;
+constexpr uint32_t kSmem = kYOff + kYBytes + 1024;  // + alignment slack
+constexpr uint32_t kColD = 0;
+GPUGI_HD constexpr uint32_t col_w(int pair) { return 128u * (uint32_t)(pair + 1); }  // 128, 256, 384
+GPUGI_HD constexpr uint32_t w_off(int l) { return kWOff + (uint32_t)l * 8192; }
+GPUGI_HD constexpr uint32_t w_kstride(int l) { return (uint32_t)out_of(l) / 8 * 128; }  // between 8-row groups of in
+}  // namespace tcl
+
+GPUGI_D uint4 pack8(const float* v, bool relu) {
+    uint32_t u[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float a = relu ? fmaxf(v[2 * i], 0.0f) : v[2 * i], b = relu ? fmaxf(v[2 * i + 1], 0.0f) : v[2 * i + 1];
+        u[i] = pack2(a, b);
+    }
+    return make_uint4(u[0], u[1], u[2], u[3]);
+}
+
+__global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const float* __restrict__ samples, uint64_t n,
+                                                         const uint32_t* __restrict__ count,
+                                                         const __half* __restrict__ wBwd, float3 boxMin,
+                                                         float3 boxInv, float lossScale, float* __restrict__ partials,
+                                                         float* lossSum, float* predOut, uint32_t* errWord) {
+    using namespace tc;
+    using namespace tcl;
+    if (count) n = min(n, (uint64_t)*count);
+    extern __shared__ uint8_t smemRaw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~uintptr_t(1023));
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmemBase;
+    __shared__ float lossWarp[4];
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    // weights, 16-byte chunks of 8 consecutive outputs
+    for (int l = 0; l < kLayers; ++l) {
+        const int outs = out_of(l), chunks = 64 * outs / 8;
+        const uint4* src = reinterpret_cast<const uint4*>(wBwd + layer_offset(l));
+        for (int c = t; c < chunks; c += blockDim.x) {
+            const int in = c / (outs / 8), o8 = c % (outs / 8);
+            *reinterpret_cast<uint4*>(sm + w_off(l) + cm_off(in, 8 * o8, w_kstride(l), 128)) = src[c];
+        }
+    }
+    if (t == 0) bar_init(&bar, 1);
+    if (warp == 0) tmem_alloc(&tmemBase, 512);
+    fence_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tm = tmemBase;
+    const uint32_t lanes = (uint32_t)(32 * warp) << 16;
+    const uint32_t xs = smem_addr(sm + kXOff), ys = smem_addr(sm + kYOff), ws = smem_addr(sm + kWOff);
+    uint8_t* xRow = sm + kXOff + (t / 8) * kXSG + (t % 8) * 16;  // + feature group x 128
+    uint8_t* yRow = sm + kYOff + (t / 8) * kYSG + (t % 8) * 16;
+    uint32_t parity = 0;
+    bool any = false, failed = false;
+    float lossAcc = 0.0f;
+    const float invCount = n ? 1.0f / (3.0f * (float)n) : 0.0f;
+    const uint64_t tiles = (n + 127) / 128;
+    // one MMA phase: thread 0 issues, everyone waits; false on a timeout
+    auto phase_wait = [&]() {
+        const bool ok = bar_wait(&bar, parity);
+        parity ^= 1u;
+        fence_after();
+        return ok;
+    };
+    for (uint64_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const uint64_t row = tile * 128 + (uint64_t)t;
+        const bool live = row < n;
+        __align__(16) __half enc[kIn];
+        float y[3] = {0.0f, 0.0f, 0.0f};
+        if (live) {
+            const float* p = samples + 15 * row;
+            Query q;
+            q.pos = make_float3(p[0], p[1], p[2]);
+            q.dir = make_float3(p[3], p[4], p[5]);
+            q.normal = make_float3(p[6], p[7], p[8]);
+            q.albedo = make_float3(p[9], p[10], p[11]);
+            encode(q, boxMin, boxInv, enc);
+            y[0] = p[12];
+            y[1] = p[13];
+            y[2] = p[14];
+        } else {
+#pragma unroll
+            for (int k = 0; k < kIn; ++k) enc[k] = __float2half(0.0f);
+        }
+        // the previous tile's weight-gradient MMAs read X and Y until here
+        if (any) failed = !phase_wait();
+#pragma unroll
+        for (int j = 0; j < 8; ++j) *reinterpret_cast<uint4*>(xRow + j * 128) = *reinterpret_cast<const uint4*>(enc + 8 * j);
+        fence_smem();
+        fence_before();
+        if (__syncthreads_or(failed)) break;
+        fence_after();
+        any = true;
+        // forward
+        for (int l = 0; l < kLayers && !failed; ++l) {
+            const int outs = out_of(l);
+            if (t == 0) {
+                const uint32_t id = idesc(128, outs, false, true);
+                for (int s = 0; s < 4; ++s)
+                    mma(tm + kColD, desc(xs + l * 1024 + s * 256, 128, kXSG),
+                        desc(ws + w_off(l) + s * 2 * w_kstride(l), w_kstride(l), 128), id, s > 0);
+                commit(&bar);
+            }
+            failed = !phase_wait();
+            if (l < 4) {
+                uint32_t r[4][16];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) ld16(tm + lanes + kColD + 16 * c, r[c]);
+                ld_wait();
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        float v[8];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[c][8 * h + i]);
+                        *reinterpret_cast<uint4*>(xRow + (8 * (l + 1) + 2 * c + h) * 128) = pack8(v, true);
+                    }
+            } else {
+                uint32_t r[16];
+                ld16(tm + lanes + kColD, r);
+                ld_wait();
+                float d[16];
+#pragma unroll
+                for (int c = 0; c < 16; ++c) d[c] = 0.0f;
+                if (live) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float pr = __uint_as_float(r[c]);
+                        const float den = pr * pr + 0.01f;
+                        lossAcc += (pr - y[c]) * (pr - y[c]) / den;
+                        d[c] = fminf(fmaxf(2.0f * (pr - y[c]) / den * lossScale, -30000.0f), 30000.0f);
+                        if (predOut) predOut[3 * row + c] = pr;
+                    }
+                }
+                *reinterpret_cast<uint4*>(yRow + 32 * 128) = pack8(d, false);
+                *reinterpret_cast<uint4*>(yRow + 33 * 128) = pack8(d + 8, false);
+            }
+            fence_smem();
+            fence_before();
+            failed = __syncthreads_or(failed);
+            fence_after();
+        }
+        // backward: dY_{l-1} = (dY_l W_l^T) * [X_l > 0]
+        for (int l = 4; l >= 1 && !failed; --l) {
+            if (t == 0) {
+                const uint32_t id = idesc(128, 64, false, false);
+                const int steps = l == 4 ? 1 : 4;
+                for (int s = 0; s < steps; ++s)
+                    mma(tm + kColD, desc(ys + l * 1024 + s * 256, 128, kYSG),
+                        desc(ws + w_off(l) + s * 256, 128, w_kstride(l)), id, s > 0);
+                commit(&bar);
+            }
+            failed = !phase_wait();
+            uint32_t r[4][16];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) ld16(tm + lanes + kColD + 16 * c, r[c]);
+            ld_wait();
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const uint4 xa = *reinterpret_cast<const uint4*>(xRow + (8 * l + 2 * c + h) * 128);
+                    const uint32_t xw[4] = {xa.x, xa.y, xa.z, xa.w};
+                    float v[8];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float2 xv = unpack2(xw[i]);
+                        v[2 * i] = xv.x > 0.0f ? __uint_as_float(r[c][8 * h + 2 * i]) : 0.0f;
+                        v[2 * i + 1] = xv.y > 0.0f ? __uint_as_float(r[c][8 * h + 2 * i + 1]) : 0.0f;
+                    }
+                    *reinterpret_cast<uint4*>(yRow + (8 * (l - 1) + 2 * c + h) * 128) = pack8(v, false);
+                }
+            fence_smem();
+            fence_before();
+            failed = __syncthreads_or(failed);
+            fence_after();
+        }
+        if (failed) break;
+        // weight gradients of the tile, accumulated over the CTA's tiles;
+        // completion is awaited before the next tile overwrites X and Y
+        if (t == 0) {
+            const bool first = tile == blockIdx.x;
+            for (int pr = 0; pr < 3; ++pr) {
+                const uint32_t id = idesc(128, pr < 2 ? 128 : 16, true, true);
+                for (int s = 0; s < 8; ++s)
+                    mma(tm + col_w(pr), desc(xs + 2 * pr * 1024 + s * 2 * kXSG, kXSG, 128),
+                        desc(ys + 2 * pr * 1024 + s * 2 * kYSG, kYSG, 128), id, !(first && s == 0));
+            }
+            commit(&bar);
+        }
+    }
+    if (any && !failed) failed = !phase_wait();
+    failed = __syncthreads_or(failed);
+    // this CTA's weight-gradient sums (zero when it had no tile)
+    float* P = partials + (size_t)blockIdx.x * kParams;
+    if (!failed && any) {
+        for (int pr = 0; pr < 2; ++pr) {
+            const int l = 2 * pr + (t >= 64 ? 1 : 0), in = t & 63;
+            const uint32_t col0 = col_w(pr) + (t >= 64 ? 64 : 0);
+            uint32_t r[4][16];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) ld16(tm + lanes + col0 + 16 * c, r[c]);
+            ld_wait();
+            float* G = P + layer_offset(l) + in * 64;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+#pragma unroll
+                for (int i = 0; i < 16; i += 4)
+                    *reinterpret_cast<float4*>(G + 16 * c + i) =
+                        make_float4(__uint_as_float(r[c][i]), __uint_as_float(r[c][i + 1]),
+                                    __uint_as_float(r[c][i + 2]), __uint_as_float(r[c][i + 3]));
+        }
+        if (t < 64) {
+            uint32_t r[16];
+            ld16(tm + lanes + col_w(2), r);
+            ld_wait();
+            float* G = P + layer_offset(4) + t * 16;
+#pragma unroll
+            for (int i = 0; i < 16; i += 4)
+                *reinterpret_cast<float4*>(G + i) = make_float4(__uint_as_float(r[i]), __uint_as_float(r[i + 1]),
+                                                                __uint_as_float(r[i + 2]), __uint_as_float(r[i + 3]));
+        } else {
+            uint32_t r[16];
+            ld16(tm + lanes + col_w(2), r);  // the warp-wide load of the unused rows 64-127
+            ld_wait();
+        }
+    } else {
+        for (int i = t; i < kParams; i += blockDim.x) P[i] = 0.0f;
+    }
+    if (failed && t == 0) atomicOr(errWord, GPUGI_DEVERR_WAIT_TIMEOUT);
+    for (int off = 16; off > 0; off >>= 1) lossAcc += __shfl_down_sync(0xffffffffu, lossAcc, off);
+    if (lane == 0) lossWarp[warp] = lossAcc;
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (t == 0 && lossSum) atomicAdd(lossSum, (lossWarp[0] + lossWarp[1] + lossWarp[2] + lossWarp[3]) * invCount);
+    if (warp == 0) tmem_free(tm, 512);
+}
+
+// ----------------------------------------------- tcgen05 inference kernel
+// Two warpgroups per CTA, each running its own chain of 128-query tiles:
+// thread t of a warpgroup owns query t of the tile (TMEM lane t), one
+// thread per warpgroup issues the five layers' MMAs (D = X W_l) into the
+// warpgroup's 64 TMEM columns and its mbarrier tracks them; between layers
+// the warpgroup turns D into the next layer's fp16 input (ReLU) in its own
+// 16 KB X buffer. The weights (the moving average, [in][out] as the
+// training weights) are staged once per CTA. 3 CTAs fit an SM (66 KB of
+// shared memory, 128 TMEM columns each), so six chains overlap their
+// latencies.
+namespace tci {
+constexpr uint32_t kXSG = 8 * 128, kXBytes = 16 * kXSG;
+constexpr uint32_t kWBytes = tcl::kWBytes;
+constexpr uint32_t kSmem = kWBytes + 2 * kXBytes + 1024;
+}  // namespace tci
+
+GPUGI_D void wg_sync(int wg) {
+    if (wg == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+    else asm volatile("bar.sync 2, 128;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(256) k_nrc_infer_tc(const float* __restrict__ queries, uint64_t n,
+                                                      const uint32_t* __restrict__ count,
+                                                      const __half* __restrict__ wInfT, float3 boxMin, float3 boxInv,
+                                                      float* __restrict__ out, uint32_t* errWord) {
+    using namespace tc;
+    using namespace tcl;
+    if (count) n = min(n, (uint64_t)*count);
+    extern __shared__ uint8_t smemRaw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~uintptr_t(1023));
+    __shared__ uint64_t bars[2];
+    __shared__ uint32_t tmemBase;
+    const int t = threadIdx.x, wg = t >> 7, lt = t & 127, warp = t >> 5;
+    for (int l = 0; l < kLayers; ++l) {
+        const int outs = out_of(l), chunks = 64 * outs / 8;
+        const uint4* src = reinterpret_cast<const uint4*>(wInfT + layer_offset(l));
+        for (int c = t; c < chunks; c += blockDim.x) {
+            const int in = c / (outs / 8), o8 = c % (outs / 8);
+            *reinterpret_cast<uint4*>(sm + w_off(l) + cm_off(in, 8 * o8, w_kstride(l), 128)) = src[c];
+        }
+    }
+    if (t == 0) {
+        bar_init(&bars[0], 1);
+        bar_init(&bars[1], 1);
+    }
+    if (warp == 0) tmem_alloc(&tmemBase, 128);
+    fence_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tm = tmemBase + 64u * (uint32_t)wg;
+    const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;
+    uint8_t* xb = sm + tci::kWBytes + (uint32_t)wg * tci::kXBytes;
+    const uint32_t xs = smem_addr(xb), ws = smem_addr(sm);
+    uint8_t* xRow = xb + (lt / 8) * tci::kXSG + (lt % 8) * 16;
+    uint64_t* bar = &bars[wg];
+    uint32_t parity = 0;
+    bool failed = false;
+    const uint64_t tiles = (n + 127) / 128;
+    for (uint64_t tile = 2 * (uint64_t)blockIdx.x + wg; tile < tiles && !failed; tile += 2 * (uint64_t)gridDim.x) {
+        const uint64_t row = tile * 128 + (uint64_t)lt;
+        {
+            __align__(16) __half enc[kIn];
+            if (row < n) {
+                const float* p = queries + 12 * row;
+                Query q;
+                q.pos = make_float3(p[0], p[1], p[2]);
+                q.dir = make_float3(p[3], p[4], p[5]);
+                q.normal = make_float3(p[6], p[7], p[8]);
+                q.albedo = make_float3(p[9], p[10], p[11]);
+                encode(q, boxMin, boxInv, enc);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kIn; ++k) enc[k] = __float2half(0.0f);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                *reinterpret_cast<uint4*>(xRow + j * 128) = *reinterpret_cast<const uint4*>(enc + 8 * j);
+        }
+        for (int l = 0; l < kLayers; ++l) {
+            fence_smem();
+            fence_before();
+            wg_sync(wg);
+            fence_after();
+            const int outs = out_of(l);
+            if (lt == 0) {
+                const uint32_t id = idesc(128, outs, false, true);
+                for (int s = 0; s < 4; ++s)
+                    mma(tm, desc(xs + s * 256, 128, tci::kXSG),
+                        desc(ws + w_off(l) + s * 2 * w_kstride(l), w_kstride(l), 128), id, s > 0);
+                commit(bar);
+            }
+            if (!bar_wait(bar, parity)) failed = true;
+            parity ^= 1u;
+            fence_after();
+            if (failed) break;
+            if (l < 4) {
+                // the MMA has read X: overwrite it with this layer's output
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    uint32_t r[16];
+                    ld16(tm + lanes + 16 * c, r);
+                    ld_wait();
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        float v[8];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[8 * h + i]);
+                        *reinterpret_cast<uint4*>(xRow + (2 * c + h) * 128) = pack8(v, true);
+                    }
+                }
+            } else {
+                uint32_t r[16];
+                ld16(tm + lanes, r);
+                ld_wait();
+                if (row < n)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) out[3 * row + c] = fmaxf(__uint_as_float(r[c]), 0.0f);
+            }
+        }
+    }
+    if (failed && lt == 0) atomicOr(errWord, GPUGI_DEVERR_WAIT_TIMEOUT);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_free(tmemBase, 128);
+}
+
+// grad[i] = sum over the CTAs' partial sums (fixed order: deterministic).
+__global__ void k_nrc_sum_partials(const float* __restrict__ partials, int rows, float* __restrict__ grad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    float s = 0.0f;
+    for (int r = 0; r < rows; ++r) s += partials[(size_t)r * kParams + i];
+    grad[i] = s;
 }
 
 constexpr size_t kInferSmem = (size_t)kLayers * 64 * kRow * 2 + 4 * 16 * kRow * 2;
@@ -475,7 +890,8 @@ static float ema_correction(gpugi_nrc* nn) {
 
 static gpugi_status nrc_publish(gpugi_ctx* ctx, gpugi_nrc* nn) {
     nn->emaSteps = 0;
-    k_nrc_publish<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->wFwd, nn->wBwd, nn->ema, nn->wInf);
+    k_nrc_publish<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->wFwd, nn->wBwd, nn->ema, nn->wInf,
+                                                                  nn->wInfT);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }
@@ -483,6 +899,20 @@ static gpugi_status nrc_publish(gpugi_ctx* ctx, gpugi_nrc* nn) {
 gpugi_status gpugi::nrc_infer_counted(gpugi_ctx* ctx, const gpugi_nrc* nn, const float* queries, uint64_t n,
                                       const uint32_t* count, float* out) {
     if (n == 0) return GPUGI_OK;
+    if (nn->kernels == GPUGI_NRC_KERNELS_TCGEN05) {
+        static bool tcAttr = false;
+        if (!tcAttr) {
+            GPUGI_CUDA_TRY(ctx, cudaFuncSetAttribute(k_nrc_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)tci::kSmem));
+            tcAttr = true;
+        }
+        const uint64_t tiles = (n + 127) / 128;
+        const uint64_t grid = std::min<uint64_t>((uint64_t)ctx->numSMs * 3, (tiles + 1) / 2);
+        k_nrc_infer_tc<<<(unsigned)grid, 256, tci::kSmem, ctx->stream>>>(queries, n, count, nn->wInfT, nn->boxMin,
+                                                                         nn->boxInv, out, ctx->errWord);
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+        return GPUGI_OK;
+    }
     static bool attr = false;
     if (!attr) {
         GPUGI_CUDA_TRY(ctx, cudaFuncSetAttribute(k_nrc_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem));
@@ -515,7 +945,7 @@ gpugi_status gpugi::nrc_train_counted(gpugi_ctx* ctx, gpugi_nrc* nn, const float
     k_nrc_adam<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->m, nn->v, nn->grad, 0.0f, count, cap,
                                                                 nn->lossScale, nn->lr, nn->beta1, nn->beta2, nn->eps,
                                                                 c1, c2, nn->wFwd, nn->wBwd, nn->ema, nn->emaDecay,
-                                                                emaCorr, nn->wInf);
+                                                                emaCorr, nn->wInf, nn->wInfT);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;
 }
@@ -538,6 +968,7 @@ gpugi_status gpugi_nrc_create(gpugi_ctx* ctx, const float boxMin[3], const float
               cudaMalloc(&nn->v, P * 4) == cudaSuccess && cudaMalloc(&nn->grad, P * 4) == cudaSuccess &&
               cudaMalloc(&nn->wFwd, P * 2) == cudaSuccess && cudaMalloc(&nn->wBwd, P * 2) == cudaSuccess &&
               cudaMalloc(&nn->ema, P * 4) == cudaSuccess && cudaMalloc(&nn->wInf, P * 2) == cudaSuccess &&
+              cudaMalloc(&nn->wInfT, P * 2) == cudaSuccess &&
               cudaMalloc(&nn->lossSum, 4) == cudaSuccess;
     if (!ok) {
         gpugi_nrc_destroy(nn);
@@ -574,8 +1005,8 @@ void gpugi_nrc_destroy(gpugi_nrc* nn) {
     if (nn->ctx) cudaStreamSynchronize(nn->ctx->stream);
     detach_child(&nn->ctx);
     for (void* p : {(void*)nn->master, (void*)nn->m, (void*)nn->v, (void*)nn->grad, (void*)nn->wFwd, (void*)nn->wBwd,
-                    (void*)nn->ema, (void*)nn->wInf,
-                    (void*)nn->acts, (void*)nn->dys, (void*)nn->lossSum})
+                    (void*)nn->ema, (void*)nn->wInf, (void*)nn->wInfT,
+                    (void*)nn->acts, (void*)nn->dys, (void*)nn->lossSum, (void*)nn->partials})
         if (p) cudaFree(p);
     delete nn;
 }
@@ -596,6 +1027,14 @@ gpugi_status gpugi_nrc_set_weights(gpugi_ctx* ctx, gpugi_nrc* nn, const float* w
     return GPUGI_OK;
 }
 
+gpugi_status gpugi_nrc_set_kernels(gpugi_ctx* ctx, gpugi_nrc* nn, uint32_t kernels) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!nn || kernels > GPUGI_NRC_KERNELS_MMA_SYNC) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "bad argument");
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    nn->kernels = kernels;
+    return GPUGI_OK;
+}
+
 gpugi_status gpugi_nrc_set_ema(gpugi_ctx* ctx, gpugi_nrc* nn, float decay) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!nn || !(decay >= 0.0f && decay < 1.0f)) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "decay in [0, 1)");
@@ -612,6 +1051,28 @@ gpugi_status gpugi_nrc_infer_device(gpugi_ctx* ctx, const gpugi_nrc* nn, const f
 
 static gpugi_status nrc_grad(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples, uint64_t n, float* predOut,
                              const uint32_t* count = nullptr) {
+    if (nn->kernels == GPUGI_NRC_KERNELS_TCGEN05) {
+        if (!nn->partials && cudaMalloc(&nn->partials, (size_t)ctx->numSMs * kParams * 4) != cudaSuccess) {
+            nn->partials = nullptr;
+            return fail(ctx, GPUGI_ERROR_OUT_OF_MEMORY, "NRC weight-gradient partial sums");
+        }
+        static bool tcAttr = false;
+        if (!tcAttr) {
+            GPUGI_CUDA_TRY(ctx, cudaFuncSetAttribute(k_nrc_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)tcl::kSmem));
+            tcAttr = true;
+        }
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(nn->lossSum, 0, 4, ctx->stream));
+        const uint64_t tiles = (n + 127) / 128;
+        const int grid = (int)std::min<uint64_t>((uint64_t)ctx->numSMs, std::max<uint64_t>(tiles, 1));
+        k_nrc_train_tc<<<grid, 128, tcl::kSmem, ctx->stream>>>(samples, n, count, nn->wBwd, nn->boxMin, nn->boxInv,
+                                                               nn->lossScale, nn->partials, nn->lossSum, predOut,
+                                                               ctx->errWord);
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+        k_nrc_sum_partials<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->partials, grid, nn->grad);
+        GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+        return GPUGI_OK;
+    }
     if (n > nn->cap) {
         if (nn->acts) cudaFree(nn->acts);
         if (nn->dys) cudaFree(nn->dys);
@@ -661,7 +1122,7 @@ gpugi_status gpugi_nrc_train_device(gpugi_ctx* ctx, gpugi_nrc* nn, const float* 
     k_nrc_adam<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->master, nn->m, nn->v, nn->grad, gradScale, nullptr,
                                                                 n, nn->lossScale, nn->lr, nn->beta1, nn->beta2, nn->eps,
                                                                 c1, c2, nn->wFwd, nn->wBwd, nn->ema, nn->emaDecay,
-                                                                emaCorr, nn->wInf);
+                                                                emaCorr, nn->wInf, nn->wInfT);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     if (loss) {
         GPUGI_CUDA_TRY(ctx, cudaMemcpyAsync(loss, nn->lossSum, 4, cudaMemcpyDeviceToHost, ctx->stream));

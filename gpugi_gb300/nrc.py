@@ -8,6 +8,7 @@ import numpy as np
 from . import cuda
 
 PARAMS = 17408
+KERNELS = {"tcgen05": 0, "mma_sync": 1}
 LAYER_SHAPES = [(64, 64)] * 4 + [(64, 16)]  # (in, out) per layer, output padded to 16
 
 
@@ -26,6 +27,7 @@ def _declare():
     L.gpugi_nrc_gradient_device.argtypes = [P, P, P, U64, P, P, P]
     L.gpugi_nrc_encode_device.argtypes = [P, P, P, U64, P]
     L.gpugi_nrc_set_ema.argtypes = [P, P, F]
+    L.gpugi_nrc_set_kernels.argtypes = [P, P, C.c_uint32]
     from . import render
     render._declare()
     L.gpugi_render_nrc.argtypes = [P, P, C.POINTER(render.Camera), C.POINTER(render.RenderParams), P,
@@ -79,6 +81,10 @@ class RadianceCache:
         w = np.ascontiguousarray(w, np.float32)
         assert w.shape == (PARAMS,)
         self.ctx.check(_declare().gpugi_nrc_set_weights(self.ctx.handle, self._h, cuda._ptr(w)))
+
+    def set_kernels(self, kernels: str):
+        """Training kernels: "tcgen05" (default) or "mma_sync"."""
+        self.ctx.check(_declare().gpugi_nrc_set_kernels(self.ctx.handle, self._h, KERNELS[kernels]))
 
     def set_ema(self, decay: float):
         """Decay of the moving average of the weights that inference uses (0: the trained weights)."""

@@ -448,6 +448,17 @@ void gpugi_nrc_destroy(gpugi_nrc* nrc);
 /* FP32 master weights, layer l at l*4096, row-major [in][out] (out = 16 for l = 4). */
 gpugi_status gpugi_nrc_get_weights(gpugi_ctx* ctx, const gpugi_nrc* nrc, float* weights);
 gpugi_status gpugi_nrc_set_weights(gpugi_ctx* ctx, gpugi_nrc* nrc, const float* weights);
+/* MLP kernels of the cache. GPUGI_NRC_KERNELS_TCGEN05 (the default): the
+ * fifth-generation tensor cores (tcgen05.mma, f16 operands in shared
+ * memory, f32 accumulators in tensor memory) on 128-sample tiles: one fused
+ * kernel per training step (forward, backward and the weight gradients,
+ * summed per CTA in tensor memory) and one for inference.
+ * GPUGI_NRC_KERNELS_MMA_SYNC: the warp-level mma.sync kernels (inference;
+ * forward + backward, then the weight-gradient GEMM), kept for comparison.
+ * Waits for the queued work first. */
+#define GPUGI_NRC_KERNELS_TCGEN05 0u
+#define GPUGI_NRC_KERNELS_MMA_SYNC 1u
+gpugi_status gpugi_nrc_set_kernels(gpugi_ctx* ctx, gpugi_nrc* nrc, uint32_t kernels);
 /* Inference (and the render pass) use an exponential moving average of the
  * trained weights, bias-corrected (decay 0.99 by default; 0 = the trained
  * weights themselves). Setting it, or the weights, restarts the average. */

@@ -60,10 +60,14 @@ def test_forward_matches_reference(cuda_ctx, cache):
     assert np.abs(got - expect).max() <= 0.02 * np.abs(expect).max() + 1e-3
 
 
-def test_gradient_matches_reference(cuda_ctx, cache):
+@pytest.mark.parametrize("kernels,n", [("tcgen05", 3000), ("tcgen05", 40000), ("mma_sync", 3000)])
+def test_gradient_matches_reference(cuda_ctx, cache, kernels, n):
+    """Both training kernels: the tcgen05 one with fewer tiles than CTAs
+    (3000 samples: 24 tiles, the last one partial) and with several tiles
+    per CTA accumulating in tensor memory (40000 samples)."""
     import torch
+    cache.set_kernels(kernels)
     rng = np.random.default_rng(3)
-    n = 3000
     q = _queries(rng, n)
     y = _target(q)
     w = (rng.uniform(-1, 1, nrc.PARAMS) * 0.2).astype(np.float32)
@@ -80,6 +84,32 @@ def test_gradient_matches_reference(cuda_ctx, cache):
         rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
         cos = float(a @ b) / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
         assert rel < 0.05 and cos > 0.995, (l, rel, cos)
+    cache.set_kernels("tcgen05")
+
+
+def test_training_kernels_agree(cuda_ctx):
+    """The tcgen05 kernel and the mma.sync pair compute the same loss,
+    predictions and gradient up to fp32 summation order (and the fp16
+    roundings that order can flip)."""
+    import torch
+    rng = np.random.default_rng(8)
+    n = 65536 + 77
+    q = _queries(rng, n)
+    samples = torch.from_numpy(np.concatenate([q, _target(q)], 1)).cuda()
+    c = nrc.RadianceCache(cuda_ctx, BOX_MIN, BOX_MAX, seed=13)
+    out = {}
+    for k in ("mma_sync", "tcgen05"):
+        c.set_kernels(k)
+        out[k] = c.gradient(samples)
+    (p0, g0, l0), (p1, g1, l1) = out["mma_sync"], out["tcgen05"]
+    assert abs(l1 / l0 - 1) < 1e-3, (l0, l1)
+    assert np.abs(p1 - p0).max() <= 1e-3 * np.abs(p0).max() + 1e-5
+    for l, (i, o) in enumerate(ref.LAYER_SHAPES):
+        a, b = g1[l * 4096: l * 4096 + i * o], g0[l * 4096: l * 4096 + i * o]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        assert rel < 1e-2, (l, rel)
+    assert cuda_ctx.device_error_bits() == 0
+    c.close()
 
 
 def test_adam_step_matches_reference(cuda_ctx, cache):
