@@ -1600,6 +1600,11 @@ __global__ void __launch_bounds__(128) k_nrc_bpt_shade(RenderConst rc, PathSoA A
     }
 }
 
+// Ray counters of a second wavefront lane folded into the first.
+__global__ void k_add_ray_counts(Counters* into, const Counters* from) {
+    if (threadIdx.x < 2) into->rays[threadIdx.x] += from->rays[threadIdx.x];
+}
+
 // Splat throughput x cache radiance for every query; a self-training query
 // adds it to its training vertex instead.
 __global__ void k_nrc_apply(RenderConst rc, const float* __restrict__ radiance) {
@@ -1929,11 +1934,21 @@ struct RenderBuffers {
     uint32_t jobCap = 0;
     cudaGraphExec_t batchExec = nullptr;
     std::vector<uintptr_t> batchKey;  // what the captured launches depend on
+    // radiance-cache frames alternate over two lanes (this set on the
+    // context's stream, lane2 on stream2), so one frame's wavefront tail
+    // overlaps the next frame's; the events order the network's inference
+    // and training across the lanes
+    RenderBuffers* lane2 = nullptr;
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t evSync[2] = {nullptr, nullptr}, evTrain[2] = {nullptr, nullptr};
 };
 
-static void free_render(gpugi_ctx* ctx) {
-    RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
+static void free_rb(RenderBuffers* rb) {
     if (!rb) return;
+    if (rb->lane2) free_rb(rb->lane2);
+    if (rb->stream2) cudaStreamDestroy(rb->stream2);
+    for (cudaEvent_t e : {rb->evSync[0], rb->evSync[1], rb->evTrain[0], rb->evTrain[1]})
+        if (e) cudaEventDestroy(e);
     if (rb->batchExec) cudaGraphExecDestroy(rb->batchExec);
     if (rb->dJobs) cudaFree(rb->dJobs);
     if (rb->dOffsets) cudaFree(rb->dOffsets);
@@ -1945,8 +1960,18 @@ static void free_render(gpugi_ctx* ctx) {
     if (rb->imBlock) cudaFree(rb->imBlock);
     if (rb->hostLights) cudaFreeHost(rb->hostLights);
     delete rb;
+}
+
+static void free_render(gpugi_ctx* ctx) {
+    RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
+    if (!rb) return;
+    if (rb->stream2) cudaStreamSynchronize(rb->stream2);
+    free_rb(rb);
     ctx->render = nullptr;
 }
+
+static gpugi_status ensure_buffers_in(gpugi_ctx* ctx, RenderBuffers* rb, size_t paths, size_t cacheBytes,
+                                      size_t lightBytes, uint32_t samples);
 
 static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheBytes, size_t lightBytes,
                                    uint32_t samples) {
@@ -1956,10 +1981,17 @@ static gpugi_status ensure_buffers(gpugi_ctx* ctx, size_t paths, size_t cacheByt
         ctx->render = rb;
         ctx->renderFree = free_render;
     }
+    return ensure_buffers_in(ctx, rb, paths, cacheBytes, lightBytes, samples);
+}
+
+static gpugi_status ensure_buffers_in(gpugi_ctx* ctx, RenderBuffers* rb, size_t paths, size_t cacheBytes,
+                                      size_t lightBytes, uint32_t samples) {
     if (paths <= rb->pathCap && cacheBytes <= rb->cacheBytes && lightBytes <= rb->lightBytes &&
         samples <= rb->maxSamples)
         return GPUGI_OK;
     cudaStreamSynchronize(ctx->stream);
+    if (RenderBuffers* r0 = static_cast<RenderBuffers*>(ctx->render); r0 && r0->stream2)
+        cudaStreamSynchronize(r0->stream2);
     if (rb->block) cudaFree(rb->block);
     rb->block = nullptr;
     paths = std::max(paths, rb->pathCap);
@@ -2198,6 +2230,8 @@ static gpugi_status ensure_nrc_buffers(gpugi_ctx* ctx, RenderBuffers* rb, size_t
         samples <= rb->nrcSampleCap)
         return GPUGI_OK;
     cudaStreamSynchronize(ctx->stream);
+    if (RenderBuffers* r0 = static_cast<RenderBuffers*>(ctx->render); r0 && r0->stream2)
+        cudaStreamSynchronize(r0->stream2);
     if (rb->nrcBlock) cudaFree(rb->nrcBlock);
     rb->nrcBlock = nullptr;
     queries = std::max(queries, rb->nrcQueryCap);
@@ -2587,25 +2621,46 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     const size_t queryCap = (size_t)framePaths + (np->trainLength ? trainCap : 0);
     if ((st = ensure_nrc_buffers(ctx, rb, queryCap, trainCap, p->maxPathLength, sampleCap))) return st;
 
-    RenderConst rc = make_render_const(ctx, sc, cam, p, im, rb);
-    rc.nrcTerminateDepth = (int)np->terminateDepth;
-    rc.nrcTrainThreshold = (uint32_t)std::min(4294967295.0, (double)np->trainFraction * 4294967296.0);
-    rc.nrcTrainLength = (int)np->trainLength;
-    rc.nrcUnbiasedThreshold = (uint32_t)std::min(4294967295.0, (double)np->unbiasedFraction * 4294967296.0);
-    rc.nrcSpread = bpt ? 0.0f : np->terminateSpread;
-    rc.tvRec = rb->tvRec;
-    rc.tvC = rb->tvC;
-    rc.tvCount = rb->tvCount;
-    rc.trainPaths = rb->nrcCounters + 1;
-    rc.trainCap = (uint32_t)trainCap;
-    rc.queries = rb->queries;
-    rc.qT = rb->qT;
-    rc.qPixel = rb->qPixel;
-    rc.queryCount = rb->nrcCounters;
-    rc.queryCap = (uint32_t)queryCap;
-    rc.numRaysPerLightSample = (int)raysPerLight;
-    rc.lightThreads = lightThreads;
-    rc.cacheCap = (uint32_t)cachePerSample;
+    // Frames alternate over two lanes (buffer sets and streams) when there
+    // are two or more: a frame's wavefront tail overlaps the next frame's
+    // bulk. The network's inference and training stay in frame order
+    // (events), so every frame sees the weights trained by the previous one.
+    const uint32_t nFrames = (p->samples + spf - 1) / spf;
+    const bool twoLanes = nFrames >= 2;
+    if (twoLanes) {
+        if (!rb->lane2) {
+            rb->lane2 = new RenderBuffers();
+            GPUGI_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&rb->stream2, cudaStreamNonBlocking));
+            for (cudaEvent_t* e : {&rb->evSync[0], &rb->evSync[1], &rb->evTrain[0], &rb->evTrain[1]})
+                GPUGI_CUDA_TRY(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        }
+        if ((st = ensure_buffers_in(ctx, rb->lane2, paths, (size_t)spf * cachePerSample * 64, 0, spf))) return st;
+        if ((st = ensure_nrc_buffers(ctx, rb->lane2, queryCap, trainCap, p->maxPathLength, sampleCap))) return st;
+    }
+    RenderBuffers* lanes[2] = {rb, twoLanes ? rb->lane2 : rb};
+    auto lane_const = [&](RenderBuffers* L) {
+        RenderConst c = make_render_const(ctx, sc, cam, p, im, L);
+        c.nrcTerminateDepth = (int)np->terminateDepth;
+        c.nrcTrainThreshold = (uint32_t)std::min(4294967295.0, (double)np->trainFraction * 4294967296.0);
+        c.nrcTrainLength = (int)np->trainLength;
+        c.nrcUnbiasedThreshold = (uint32_t)std::min(4294967295.0, (double)np->unbiasedFraction * 4294967296.0);
+        c.nrcSpread = bpt ? 0.0f : np->terminateSpread;
+        c.tvRec = L->tvRec;
+        c.tvC = L->tvC;
+        c.tvCount = L->tvCount;
+        c.trainPaths = L->nrcCounters + 1;
+        c.trainCap = (uint32_t)trainCap;
+        c.queries = L->queries;
+        c.qT = L->qT;
+        c.qPixel = L->qPixel;
+        c.queryCount = L->nrcCounters;
+        c.queryCap = (uint32_t)queryCap;
+        c.numRaysPerLightSample = (int)raysPerLight;
+        c.lightThreads = lightThreads;
+        c.cacheCap = (uint32_t)cachePerSample;
+        return c;
+    };
+    RenderConst rcs[2] = {lane_const(lanes[0]), lane_const(lanes[1])};
     Walkers W;
     if ((st = walkers_config(ctx, sc, W))) return st;
     int perSM = 0;
@@ -2613,20 +2668,44 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
                                                   128, 0);
     const int gridShade = ctx->numSMs * std::max(perSM, 1);
     const int genBlocks = ctx->numSMs * 8;
-    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), ctx->stream));
-    for (uint32_t frame = 0; frame < p->samples; frame += spf) {
+    const cudaStream_t base = ctx->stream;
+    // the library's launch helpers queue on ctx->stream: point it at the
+    // frame's lane, and back at the context's stream on every way out
+    struct StreamScope {
+        gpugi_ctx* c;
+        cudaStream_t s;
+        ~StreamScope() { c->stream = s; }
+    } scope{ctx, base};
+    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), base));
+    if (twoLanes) GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->lane2->cnt, 0, sizeof(Counters), base));
+    uint32_t fi = 0;
+    for (uint32_t frame = 0; frame < p->samples; frame += spf, ++fi) {
         const uint32_t ns = std::min(spf, p->samples - frame);
         const uint32_t inBlock = frame % blockSamples;
-        if (inBlock == 0 &&
-            (st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, frame,
-                                    std::min(blockSamples, p->samples - frame), p->numLightSamples)))
-            return st;
+        if (inBlock == 0) {
+            // the second lane has read the previous block of light samples
+            if (twoLanes && fi > 0) {
+                GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[1], rb->stream2));
+                GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(base, rb->evSync[1], 0));
+            }
+            if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, frame,
+                                        std::min(blockSamples, p->samples - frame), p->numLightSamples)))
+                return st;
+            if (twoLanes) {
+                GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[0], base));
+                GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(rb->stream2, rb->evSync[0], 0));
+            }
+        }
+        const int li = twoLanes ? (int)(fi & 1u) : 0;
+        RenderBuffers* L = lanes[li];
+        RenderConst& rc = rcs[li];
+        ctx->stream = li ? rb->stream2 : base;
         rc.lightSamples = rb->lights + 2 * (size_t)inBlock * p->numLightSamples;
         rc.samples = ns;
         rc.sampleBase = frame;
-        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), ctx->stream));
-        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->nrcCounters, 0, 64, ctx->stream));
-        PathSoA A = rb->A, B = rb->B;
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(L->cnt, 0, offsetof(Counters, rays), ctx->stream));
+        GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(L->nrcCounters, 0, 64, ctx->stream));
+        PathSoA A = L->A, B = L->B;
         if (bpt) {
             // light pass with the light cache (lighttracer.comp with
             // SAVE_LIGHT_CACHE), bounded to lightDepth bounces
@@ -2634,38 +2713,47 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
             rl.maxPathLength = (int)lightDepth;
             k_light_generate<<<genBlocks, 256, 0, ctx->stream>>>(rl, A, true);
             for (int depth = 0; depth < rl.maxPathLength; ++depth) {
-                launch_extend(ctx, W, rl, A, rb->H, depth);
-                k_light_shade<<<gridShade, 128, 0, ctx->stream>>>(rl, A, B, rb->H, rb->Q, depth, true);
-                launch_shadow(ctx, W, rl, rb->Q, depth);
+                launch_extend(ctx, W, rl, A, L->H, depth);
+                k_light_shade<<<gridShade, 128, 0, ctx->stream>>>(rl, A, B, L->H, L->Q, depth, true);
+                launch_shadow(ctx, W, rl, L->Q, depth);
                 std::swap(A, B);
             }
-            GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, offsetof(Counters, rays), ctx->stream));
-            A = rb->A;
-            B = rb->B;
+            GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(L->cnt, 0, offsetof(Counters, rays), ctx->stream));
+            A = L->A;
+            B = L->B;
             k_nrc_bpt_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A, nTrain);
         } else {
             k_nrc_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
         }
         for (int depth = 0; depth < rc.maxPathLength; ++depth) {
-            launch_extend(ctx, W, rc, A, rb->H, depth);
-            if (bpt) k_nrc_bpt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
-            else k_nrc_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, rb->H, rb->Q, depth);
-            launch_shadow(ctx, W, rc, rb->Q, depth);
+            launch_extend(ctx, W, rc, A, L->H, depth);
+            if (bpt) k_nrc_bpt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, L->H, L->Q, depth);
+            else k_nrc_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, L->H, L->Q, depth);
+            launch_shadow(ctx, W, rc, L->Q, depth);
             std::swap(A, B);
         }
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
-        // cache lookups of this frame (the network as trained by earlier
-        // frames); counts stay on the device, so frames queue back to back
-        if ((st = nrc_infer_counted(ctx, nn, rb->queries, queryCap, rb->nrcCounters, rb->radiance))) return st;
-        k_nrc_apply<<<ctx->numSMs * 4, 256, 0, ctx->stream>>>(rc, rb->radiance);
+        // cache lookups of this frame with the network as trained by the
+        // previous frame (on the other lane); counts stay on the device, so
+        // frames queue back to back
+        if (twoLanes && fi > 0) GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, rb->evTrain[li ^ 1], 0));
+        if ((st = nrc_infer_counted(ctx, nn, L->queries, queryCap, L->nrcCounters, L->radiance))) return st;
+        k_nrc_apply<<<ctx->numSMs * 4, 256, 0, ctx->stream>>>(rc, L->radiance);
         // training on this frame's training paths
         if (np->train && np->trainFraction > 0.0f) {
-            k_nrc_targets<<<ctx->numSMs * 2, 128, 0, ctx->stream>>>(rc, rb->samples, rb->nrcCounters + 2,
+            k_nrc_targets<<<ctx->numSMs * 2, 128, 0, ctx->stream>>>(rc, L->samples, L->nrcCounters + 2,
                                                                      (uint32_t)sampleCap);
             for (uint32_t k = 0; k < std::max<uint32_t>(1u, np->trainSteps); ++k)
-                if ((st = nrc_train_counted(ctx, nn, rb->samples, sampleCap, rb->nrcCounters + 2))) return st;
+                if ((st = nrc_train_counted(ctx, nn, L->samples, sampleCap, L->nrcCounters + 2))) return st;
         }
+        if (twoLanes) GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evTrain[li], ctx->stream));
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
+        ctx->stream = base;
+    }
+    if (twoLanes) {  // the call's work ends on the context's stream, its ray counts in the first lane's
+        GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[1], rb->stream2));
+        GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(base, rb->evSync[1], 0));
+        k_add_ray_counts<<<1, 32, 0, base>>>(rb->cnt, rb->lane2->cnt);
     }
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;

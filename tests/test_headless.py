@@ -159,7 +159,7 @@ def test_headless_checkpoint_resume_continues_the_estimator(cuda_ctx, room_file,
     else:
         assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max() + 1e-7
     # a checkpoint of another renderer or size is refused
-    other = "LightPathtracer"
+    other = "Pathtracer" if renderer != "Pathtracer" else "LightPathtracer"
     r = subprocess.run([str(EXE), "--scene", str(path), "--renderer", other, "--size", "24", "20", "--resume", str(ck)],
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 1 and "checkpoint of renderer" in r.stderr
