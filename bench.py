@@ -974,6 +974,54 @@ class NrcSetup:
                         "mlp": "64-64x4-3 ReLU fp16, fp32 accumulate, Adam lr 1e-2"},
                 "nrc_curve": curve}
 
+    def fixed_budget(self, spp, td, spf, steps, tl, spread, warmup, train_fraction=0.0):
+        """The cache renderer at a fixed sample budget (after `warmup`
+        training frames, timed) against the plain pass run until it reaches
+        the same RMSE: (plain time to the cache's RMSE) / (cache time)."""
+        from gpugi_gb300 import nrc, render
+        W, H = self.W, self.H
+        tf = train_fraction or min(0.05, 1.5 * 65536 / (3.0 * W * H * spf))
+        cache = nrc.RadianceCache(self.ctx, *self.box, seed=5)
+        opts = dict(max_path_length=self.depth, sky=self.sky, terminate_depth=td, train_fraction=tf,
+                    train_steps=steps, samples_per_frame=spf, rr_start_depth=self.rr, pass_=self.pass_,
+                    train_length=tl, terminate_spread=spread)
+        t_nrc = 0.0
+        if warmup:
+            scratch = render.Image(self.ctx, W, H)
+            t_nrc = self.timed(lambda: nrc.render_nrc(self.ctx, self.ds, self.cam, scratch, cache,
+                                                      samples=warmup * spf, iteration=1 << 20, rng_state=[11],
+                                                      **opts))
+            scratch.close()
+        img = render.Image(self.ctx, W, H, fp64=True)
+        t_nrc += self.timed(lambda: nrc.render_nrc(self.ctx, self.ds, self.cam, img, cache, samples=spp,
+                                                   iteration=0, rng_state=[13], **opts))
+        r_nrc = self.rmse(img, spp)
+        img.close()
+        cache.close()
+        pt = render.Image(self.ctx, W, H, fp64=True)
+        t, n, curve, reached, at_equal_time = 0.0, 0, [], None, None
+        c = 1
+        while n < 64 * spp and reached is None:
+            t += self.timed(lambda: render.render(self.ctx, self.ds, self.cam, pt, self.pass_,
+                                                  max_path_length=self.depth, samples=c, iteration=n,
+                                                  rng_state=[7 + n], sky=self.sky, rr_start_depth=self.rr))
+            n += c
+            r = self.rmse(pt, n)
+            curve.append((n, round(t, 5), round(r, 6)))
+            if at_equal_time is None and t >= t_nrc:
+                at_equal_time = r
+            if r <= r_nrc:
+                reached = t
+            c = n  # doubling
+        pt.close()
+        return {"value": (reached / t_nrc) if reached else None, "unit": "speed-up (plain time to the cache's RMSE / cache time)",
+                "nrc_spp": spp, "t_nrc_s": round(t_nrc, 4), "nrc_rmse": round(r_nrc, 6),
+                "t_plain_to_equal_rmse_s": round(reached, 4) if reached else None,
+                "plain_rmse_at_equal_time": at_equal_time, "plain_curve": curve,
+                "nrc": {"terminate_depth": td, "train_fraction": round(tf, 5), "train_steps": steps,
+                        "train_length": tl, "terminate_spread": spread, "samples_per_frame": spf,
+                        "warmup_frames": warmup}}
+
     def close(self):
         self.ds.close()
         self.ctx.close()
@@ -1015,7 +1063,6 @@ def run_nrc(args):
     pass_ = args.nrc_pass
     W, H = args.nrc_size if args.nrc_size else ((640, 360) if pass_ == "PT" else (480, 270))
     st = NrcSetup(pass_, W, H, args.nrc_ref_spp, args.nrc_rr)
-    t_pt, target, pt_curve = st.plain(1024)
 
     def parse(c):
         v = [float(x) for x in c.split(",")]
@@ -1024,6 +1071,20 @@ def run_nrc(args):
 
     configs = [parse(c) for c in args.nrc_configs.split(";")] if args.nrc_configs else \
         [(args.nrc_td, args.nrc_spf, args.nrc_train_steps, args.nrc_train_length, args.nrc_spread)]
+    if args.nrc_budget:
+        for td, spf, steps, tl, spread in configs:
+            r = st.fixed_budget(args.nrc_budget, td, spf, steps, tl, spread, args.nrc_warmup,
+                                train_fraction=args.nrc_train_fraction)
+            line = {"metric": f"{pass_} with the radiance cache at {args.nrc_budget} spp vs plain {pass_} at equal RMSE",
+                    "higher_is_better": True}
+            line.update(r)
+            line["config"] = {"workload": st.workload, "pass": pass_, "rr_start_depth": st.rr, "resolution": [W, H],
+                              "reference_spp": st.ref_spp, "reference_s": round(st.t_ref, 2), "nrc": line.pop("nrc")}
+            line.update({"data": "synthetic", "dtype": "f32 paths, f16 MLP"})
+            print(json.dumps(line), flush=True)
+        st.close()
+        return
+    t_pt, target, pt_curve = st.plain(1024)
     for td, spf, steps, tl, spread in configs:
         r = st.cache_run(t_pt, target, td, spf, steps, tl, spread, args.nrc_warmup,
                          train_fraction=args.nrc_train_fraction)
@@ -1079,12 +1140,15 @@ def main():
                     help="share of training paths (0: about 98k training vertices per frame)")
     ap.add_argument("--nrc-configs", default="",
                     help="'td,spf,steps[,train_length[,spread]];...' several cache settings in one run")
-    ap.add_argument("--nrc-train-steps", type=int, default=4)
-    ap.add_argument("--nrc-train-length", type=int, default=0,
+    ap.add_argument("--nrc-train-steps", type=int, default=2)
+    ap.add_argument("--nrc-train-length", type=int, default=3,
                     help="self-training: training paths take the cache's radiance at this vertex (0: off)")
     ap.add_argument("--nrc-spread", type=float, default=0.0,
                     help="path-spread termination constant c (0: stop at --nrc-td)")
-    ap.add_argument("--nrc-td", type=int, default=2, help="path vertex where render paths query the cache")
+    ap.add_argument("--nrc-td", type=int, default=3, help="path vertex where render paths query the cache")
+    ap.add_argument("--nrc-budget", type=int, default=0,
+                    help="cache renderer at this many spp against the plain pass at equal RMSE (0: time to the "
+                         "plain 1024-spp RMSE)")
     ap.add_argument("--nrc-rr", type=int, default=0, help="Russian roulette start depth of both tracers")
     args = ap.parse_args()
     if args.workload != "trace":

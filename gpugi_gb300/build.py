@@ -31,6 +31,9 @@ HOST_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
               "-I", str(INCLUDE), "-I", str(CSRC)] + ARCH
 
+# extra nvcc arguments (for example -D settings of the kernels), from the environment
+NVCC_FLAGS += os.environ.get("GPUGI_NVCC_EXTRA", "").split()
+
 CUDA_SOURCES = ["trace.cu", "scene.cu", "render.cu", "capi.cu", "host.cu", "noalloc.cu", "nrc.cu", "tune.cu", "build.cu",
                 "hierarchy.cu"]
 

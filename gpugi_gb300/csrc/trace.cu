@@ -9,6 +9,11 @@
 #include "ctx.cuh"
 #include "trace.cuh"
 
+// Resident blocks per SM the group walker is compiled for (registers).
+#ifndef GPUGI_GROUP_MIN_BLOCKS
+#define GPUGI_GROUP_MIN_BLOCKS 10
+#endif
+
 namespace gpugi {
 
 // Picks a kernel instantiation at run time: f receives (any hit, bounds kind
@@ -316,7 +321,7 @@ __global__ void __launch_bounds__(128) k_trace_queue(
 // lanes walk each queued ray together (group_step), which shortens the
 // dependent fetch chain of the longest walks.
 template <bool ANY_HIT, int BOUNDS, int G, int TRI>
-__global__ void __launch_bounds__(128, 10) k_trace_group(
+__global__ void __launch_bounds__(128, GPUGI_GROUP_MIN_BLOCKS) k_trace_group(
     DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
     const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
     const float* __restrict__ tmax, int32_t* __restrict__ slot, float* __restrict__ t, float* __restrict__ u,
