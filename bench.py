@@ -861,9 +861,10 @@ class NrcSetup:
     variance to both renderers' MSE, so it cancels out of the equal-RMSE
     comparison."""
 
-    def __init__(self, pass_, W, H, ref_spp, rr):
+    def __init__(self, pass_, W, H, ref_spp, rr, unbiased=1.0 / 16, lanes=2):
         from gpugi_gb300 import bvh, cuda, render, scenes
         self.pass_, self.W, self.H, self.rr, self.ref_spp = pass_, W, H, rr, ref_spp
+        self.unbiased, self.lanes = unbiased, lanes
         self.ctx = cuda.Context(0)
         if pass_ == "PT":
             self.depth, self.sky = 8, (0.5, 0.5, 0.5)
@@ -936,7 +937,7 @@ class NrcSetup:
         cache = nrc.RadianceCache(self.ctx, *self.box, seed=5)
         opts = dict(max_path_length=self.depth, sky=self.sky, terminate_depth=td, train_fraction=tf,
                     train_steps=steps, samples_per_frame=spf, rr_start_depth=self.rr, pass_=self.pass_,
-                    train_length=tl, terminate_spread=spread)
+                    train_length=tl, terminate_spread=spread, unbiased_fraction=self.unbiased, lanes=self.lanes)
         t_nrc = 0.0
         if warmup:
             scratch = render.Image(self.ctx, W, H)
@@ -968,8 +969,9 @@ class NrcSetup:
                 "t_nrc_warmup_s": round(t_warm, 4), "nrc_rmse_at_equal_time": at_equal_time,
                 f"after_{at_frames}_frames": at_n,
                 "nrc": {"terminate_depth": td, "train_fraction": round(tf, 5), "train_steps": steps,
-                        "train_length": tl, "unbiased_fraction": 1.0 / 16 if tl else None,
+                        "train_length": tl, "unbiased_fraction": self.unbiased if tl else None,
                         "terminate_spread": spread, "samples_per_frame": spf, "warmup_frames": warmup,
+                        "lanes": self.lanes,
                         "max_train_samples": 65536, "ema": 0.99,
                         "mlp": "64-64x4-3 ReLU fp16, fp32 accumulate, Adam lr 1e-2"},
                 "nrc_curve": curve}
@@ -984,7 +986,7 @@ class NrcSetup:
         cache = nrc.RadianceCache(self.ctx, *self.box, seed=5)
         opts = dict(max_path_length=self.depth, sky=self.sky, terminate_depth=td, train_fraction=tf,
                     train_steps=steps, samples_per_frame=spf, rr_start_depth=self.rr, pass_=self.pass_,
-                    train_length=tl, terminate_spread=spread)
+                    train_length=tl, terminate_spread=spread, unbiased_fraction=self.unbiased, lanes=self.lanes)
         t_nrc = 0.0
         if warmup:
             scratch = render.Image(self.ctx, W, H)
@@ -1034,7 +1036,7 @@ def nrc_headline(args):
     (cache time to the plain tracer's 1024-spp RMSE) / (plain time to 1024
     spp); null when the cache does not get there within 3x the plain
     time."""
-    st = NrcSetup("PT", 1280, 720, args.nrc_ref_spp, args.nrc_rr)
+    st = NrcSetup("PT", 1280, 720, args.nrc_ref_spp, args.nrc_rr, args.nrc_unbiased, args.nrc_lanes)
     try:
         t_pt, target, pt_curve = st.plain(1024)
         r = st.cache_run(t_pt, target, args.nrc_td, 1, args.nrc_train_steps, args.nrc_train_length,
@@ -1062,7 +1064,7 @@ def run_nrc(args):
     until its RMSE reaches the target or its time exceeds 3 T_plain."""
     pass_ = args.nrc_pass
     W, H = args.nrc_size if args.nrc_size else ((640, 360) if pass_ == "PT" else (480, 270))
-    st = NrcSetup(pass_, W, H, args.nrc_ref_spp, args.nrc_rr)
+    st = NrcSetup(pass_, W, H, args.nrc_ref_spp, args.nrc_rr, args.nrc_unbiased, args.nrc_lanes)
 
     def parse(c):
         v = [float(x) for x in c.split(",")]
@@ -1146,6 +1148,9 @@ def main():
     ap.add_argument("--nrc-spread", type=float, default=0.0,
                     help="path-spread termination constant c (0: stop at --nrc-td)")
     ap.add_argument("--nrc-td", type=int, default=3, help="path vertex where render paths query the cache")
+    ap.add_argument("--nrc-unbiased", type=float, default=1.0 / 16,
+                    help="self-training: share of training paths that run to their end")
+    ap.add_argument("--nrc-lanes", type=int, default=2, help="cache frames in flight (wavefront lanes)")
     ap.add_argument("--nrc-budget", type=int, default=0,
                     help="cache renderer at this many spp against the plain pass at equal RMSE (0: time to the "
                          "plain 1024-spp RMSE)")

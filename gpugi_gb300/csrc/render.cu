@@ -1934,21 +1934,32 @@ struct RenderBuffers {
     uint32_t jobCap = 0;
     cudaGraphExec_t batchExec = nullptr;
     std::vector<uintptr_t> batchKey;  // what the captured launches depend on
-    // radiance-cache frames alternate over two lanes (this set on the
-    // context's stream, lane2 on stream2), so one frame's wavefront tail
-    // overlaps the next frame's; the events order the network's inference
-    // and training across the lanes
-    RenderBuffers* lane2 = nullptr;
-    cudaStream_t stream2 = nullptr;
-    cudaEvent_t evSync[2] = {nullptr, nullptr}, evTrain[2] = {nullptr, nullptr};
+    // radiance-cache frames alternate over up to kMaxLanes lanes (this set
+    // on the context's stream, extra[l - 1] on xstream[l - 1]), so a frame's
+    // wavefront tail overlaps the next frames'; the events order the
+    // network's inference and training across the lanes
+    static constexpr int kMaxLanes = 4;
+    RenderBuffers* extra[kMaxLanes - 1] = {};
+    cudaStream_t xstream[kMaxLanes - 1] = {};
+    cudaEvent_t evSync[kMaxLanes] = {}, evTrain[kMaxLanes] = {};
 };
+
+// Wait (host) for the extra lanes' streams of the context's wavefront buffers.
+static void sync_lanes(gpugi_ctx* ctx) {
+    if (RenderBuffers* r0 = static_cast<RenderBuffers*>(ctx->render))
+        for (cudaStream_t st : r0->xstream)
+            if (st) cudaStreamSynchronize(st);
+}
 
 static void free_rb(RenderBuffers* rb) {
     if (!rb) return;
-    if (rb->lane2) free_rb(rb->lane2);
-    if (rb->stream2) cudaStreamDestroy(rb->stream2);
-    for (cudaEvent_t e : {rb->evSync[0], rb->evSync[1], rb->evTrain[0], rb->evTrain[1]})
-        if (e) cudaEventDestroy(e);
+    for (RenderBuffers* x : rb->extra) free_rb(x);
+    for (cudaStream_t st : rb->xstream)
+        if (st) cudaStreamDestroy(st);
+    for (int l = 0; l < RenderBuffers::kMaxLanes; ++l) {
+        if (rb->evSync[l]) cudaEventDestroy(rb->evSync[l]);
+        if (rb->evTrain[l]) cudaEventDestroy(rb->evTrain[l]);
+    }
     if (rb->batchExec) cudaGraphExecDestroy(rb->batchExec);
     if (rb->dJobs) cudaFree(rb->dJobs);
     if (rb->dOffsets) cudaFree(rb->dOffsets);
@@ -1965,7 +1976,7 @@ static void free_rb(RenderBuffers* rb) {
 static void free_render(gpugi_ctx* ctx) {
     RenderBuffers* rb = static_cast<RenderBuffers*>(ctx->render);
     if (!rb) return;
-    if (rb->stream2) cudaStreamSynchronize(rb->stream2);
+    sync_lanes(ctx);
     free_rb(rb);
     ctx->render = nullptr;
 }
@@ -1990,8 +2001,7 @@ static gpugi_status ensure_buffers_in(gpugi_ctx* ctx, RenderBuffers* rb, size_t 
         samples <= rb->maxSamples)
         return GPUGI_OK;
     cudaStreamSynchronize(ctx->stream);
-    if (RenderBuffers* r0 = static_cast<RenderBuffers*>(ctx->render); r0 && r0->stream2)
-        cudaStreamSynchronize(r0->stream2);
+    sync_lanes(ctx);
     if (rb->block) cudaFree(rb->block);
     rb->block = nullptr;
     paths = std::max(paths, rb->pathCap);
@@ -2230,8 +2240,7 @@ static gpugi_status ensure_nrc_buffers(gpugi_ctx* ctx, RenderBuffers* rb, size_t
         samples <= rb->nrcSampleCap)
         return GPUGI_OK;
     cudaStreamSynchronize(ctx->stream);
-    if (RenderBuffers* r0 = static_cast<RenderBuffers*>(ctx->render); r0 && r0->stream2)
-        cudaStreamSynchronize(r0->stream2);
+    sync_lanes(ctx);
     if (rb->nrcBlock) cudaFree(rb->nrcBlock);
     rb->nrcBlock = nullptr;
     queries = std::max(queries, rb->nrcQueryCap);
@@ -2621,23 +2630,32 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     const size_t queryCap = (size_t)framePaths + (np->trainLength ? trainCap : 0);
     if ((st = ensure_nrc_buffers(ctx, rb, queryCap, trainCap, p->maxPathLength, sampleCap))) return st;
 
-    // Frames alternate over two lanes (buffer sets and streams) when there
-    // are two or more: a frame's wavefront tail overlaps the next frame's
-    // bulk. The network's inference and training stay in frame order
-    // (events), so every frame sees the weights trained by the previous one.
+    // Frames alternate over `lanes` lanes (buffer sets and streams; 2 by
+    // default): a frame's wavefront tail overlaps the next frames' bulk. The
+    // network's inference and training stay in frame order (events), so
+    // every frame sees the weights trained by the previous one.
     const uint32_t nFrames = (p->samples + spf - 1) / spf;
-    const bool twoLanes = nFrames >= 2;
-    if (twoLanes) {
-        if (!rb->lane2) {
-            rb->lane2 = new RenderBuffers();
-            GPUGI_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&rb->stream2, cudaStreamNonBlocking));
-            for (cudaEvent_t* e : {&rb->evSync[0], &rb->evSync[1], &rb->evTrain[0], &rb->evTrain[1]})
-                GPUGI_CUDA_TRY(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    const int nLanes = (int)std::max<uint32_t>(
+        1u, std::min<uint32_t>(np->lanes ? std::min<uint32_t>(np->lanes, RenderBuffers::kMaxLanes) : 2u, nFrames));
+    RenderBuffers* lanes[RenderBuffers::kMaxLanes] = {rb, rb, rb, rb};
+    cudaStream_t streams[RenderBuffers::kMaxLanes] = {ctx->stream, ctx->stream, ctx->stream, ctx->stream};
+    if (nLanes > 1 && !rb->evSync[0])
+        for (int l = 0; l < RenderBuffers::kMaxLanes; ++l) {
+            GPUGI_CUDA_TRY(ctx, cudaEventCreateWithFlags(&rb->evSync[l], cudaEventDisableTiming));
+            GPUGI_CUDA_TRY(ctx, cudaEventCreateWithFlags(&rb->evTrain[l], cudaEventDisableTiming));
         }
-        if ((st = ensure_buffers_in(ctx, rb->lane2, paths, (size_t)spf * cachePerSample * 64, 0, spf))) return st;
-        if ((st = ensure_nrc_buffers(ctx, rb->lane2, queryCap, trainCap, p->maxPathLength, sampleCap))) return st;
+    for (int l = 1; l < nLanes; ++l) {
+        if (!rb->extra[l - 1]) {
+            rb->extra[l - 1] = new RenderBuffers();
+            GPUGI_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&rb->xstream[l - 1], cudaStreamNonBlocking));
+        }
+        if ((st = ensure_buffers_in(ctx, rb->extra[l - 1], paths, (size_t)spf * cachePerSample * 64, 0, spf)))
+            return st;
+        if ((st = ensure_nrc_buffers(ctx, rb->extra[l - 1], queryCap, trainCap, p->maxPathLength, sampleCap)))
+            return st;
+        lanes[l] = rb->extra[l - 1];
+        streams[l] = rb->xstream[l - 1];
     }
-    RenderBuffers* lanes[2] = {rb, twoLanes ? rb->lane2 : rb};
     auto lane_const = [&](RenderBuffers* L) {
         RenderConst c = make_render_const(ctx, sc, cam, p, im, L);
         c.nrcTerminateDepth = (int)np->terminateDepth;
@@ -2660,7 +2678,15 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         c.cacheCap = (uint32_t)cachePerSample;
         return c;
     };
-    RenderConst rcs[2] = {lane_const(lanes[0]), lane_const(lanes[1])};
+    RenderConst rcs[RenderBuffers::kMaxLanes];
+    for (int l = 0; l < nLanes; ++l) rcs[l] = lane_const(lanes[l]);
+    // The wavefront's bounces: render paths stop by vertex terminateDepth;
+    // training paths run to the path's end unless there are none or every
+    // one of them stops at trainLength (self-training, no unbiased share).
+    const bool trainingEnds = np->trainFraction <= 0.0f || (np->trainLength && np->unbiasedFraction <= 0.0f);
+    const int lastDepth = trainingEnds ? std::min<int>((int)p->maxPathLength,
+                                                       (int)std::max(np->terminateDepth, np->trainLength) + 1)
+                                       : (int)p->maxPathLength;
     Walkers W;
     if ((st = walkers_config(ctx, sc, W))) return st;
     int perSM = 0;
@@ -2676,30 +2702,27 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         cudaStream_t s;
         ~StreamScope() { c->stream = s; }
     } scope{ctx, base};
-    GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->cnt, 0, sizeof(Counters), base));
-    if (twoLanes) GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(rb->lane2->cnt, 0, sizeof(Counters), base));
+    for (int l = 0; l < nLanes; ++l) GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(lanes[l]->cnt, 0, sizeof(Counters), base));
     uint32_t fi = 0;
     for (uint32_t frame = 0; frame < p->samples; frame += spf, ++fi) {
         const uint32_t ns = std::min(spf, p->samples - frame);
         const uint32_t inBlock = frame % blockSamples;
         if (inBlock == 0) {
-            // the second lane has read the previous block of light samples
-            if (twoLanes && fi > 0) {
-                GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[1], rb->stream2));
-                GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(base, rb->evSync[1], 0));
+            // the other lanes have read the previous block of light samples
+            for (int l = 1; l < nLanes && fi > 0; ++l) {
+                GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[l], streams[l]));
+                GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(base, rb->evSync[l], 0));
             }
             if ((st = upload_light_sets(ctx, sc, rb, lightSamples, rngState, frame,
                                         std::min(blockSamples, p->samples - frame), p->numLightSamples)))
                 return st;
-            if (twoLanes) {
-                GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[0], base));
-                GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(rb->stream2, rb->evSync[0], 0));
-            }
+            if (nLanes > 1) GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[0], base));
+            for (int l = 1; l < nLanes; ++l) GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(streams[l], rb->evSync[0], 0));
         }
-        const int li = twoLanes ? (int)(fi & 1u) : 0;
+        const int li = (int)(fi % (uint32_t)nLanes);
         RenderBuffers* L = lanes[li];
         RenderConst& rc = rcs[li];
-        ctx->stream = li ? rb->stream2 : base;
+        ctx->stream = streams[li];
         rc.lightSamples = rb->lights + 2 * (size_t)inBlock * p->numLightSamples;
         rc.samples = ns;
         rc.sampleBase = frame;
@@ -2725,7 +2748,7 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         } else {
             k_nrc_generate<<<genBlocks, 256, 0, ctx->stream>>>(rc, A);
         }
-        for (int depth = 0; depth < rc.maxPathLength; ++depth) {
+        for (int depth = 0; depth < lastDepth; ++depth) {
             launch_extend(ctx, W, rc, A, L->H, depth);
             if (bpt) k_nrc_bpt_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, L->H, L->Q, depth);
             else k_nrc_shade<<<gridShade, 128, 0, ctx->stream>>>(rc, A, B, L->H, L->Q, depth);
@@ -2736,7 +2759,8 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
         // cache lookups of this frame with the network as trained by the
         // previous frame (on the other lane); counts stay on the device, so
         // frames queue back to back
-        if (twoLanes && fi > 0) GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, rb->evTrain[li ^ 1], 0));
+        if (nLanes > 1 && fi > 0)
+            GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, rb->evTrain[(li + nLanes - 1) % nLanes], 0));
         if ((st = nrc_infer_counted(ctx, nn, L->queries, queryCap, L->nrcCounters, L->radiance))) return st;
         k_nrc_apply<<<ctx->numSMs * 4, 256, 0, ctx->stream>>>(rc, L->radiance);
         // training on this frame's training paths
@@ -2746,14 +2770,14 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
             for (uint32_t k = 0; k < std::max<uint32_t>(1u, np->trainSteps); ++k)
                 if ((st = nrc_train_counted(ctx, nn, L->samples, sampleCap, L->nrcCounters + 2))) return st;
         }
-        if (twoLanes) GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evTrain[li], ctx->stream));
+        if (nLanes > 1) GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evTrain[li], ctx->stream));
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
         ctx->stream = base;
     }
-    if (twoLanes) {  // the call's work ends on the context's stream, its ray counts in the first lane's
-        GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[1], rb->stream2));
-        GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(base, rb->evSync[1], 0));
-        k_add_ray_counts<<<1, 32, 0, base>>>(rb->cnt, rb->lane2->cnt);
+    for (int l = 1; l < nLanes; ++l) {  // the call's work ends on the context's stream, its ray counts in lane 0's
+        GPUGI_CUDA_TRY(ctx, cudaEventRecord(rb->evSync[l], streams[l]));
+        GPUGI_CUDA_TRY(ctx, cudaStreamWaitEvent(base, rb->evSync[l], 0));
+        k_add_ray_counts<<<1, 32, 0, base>>>(rb->cnt, lanes[l]->cnt);
     }
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());
     return GPUGI_OK;

@@ -39,7 +39,8 @@ def _declare():
 class NrcParams(C.Structure):
     _fields_ = [("terminateDepth", C.c_uint32), ("trainFraction", C.c_float), ("maxTrainSamples", C.c_uint32),
                 ("trainSteps", C.c_uint32), ("train", C.c_uint32), ("samplesPerFrame", C.c_uint32),
-                ("trainLength", C.c_uint32), ("unbiasedFraction", C.c_float), ("terminateSpread", C.c_float)]
+                ("trainLength", C.c_uint32), ("unbiasedFraction", C.c_float), ("terminateSpread", C.c_float),
+                ("lanes", C.c_uint32)]
 
 
 def _torch_to_ctx():
@@ -148,14 +149,14 @@ def render_nrc(ctx: cuda.Context, scene: cuda.DeviceScene, camera, image, cache:
                rng_state: list | None = None, terminate_depth: int = 1, train_fraction: float = 0.03,
                max_train_samples: int = 65536, train_steps: int = 1, train: bool = True,
                samples_per_frame: int = 1, pass_: str = "PT", rng: str = "pcg", train_length: int = 0,
-               unbiased_fraction: float = 1.0 / 16.0, terminate_spread: float = 0.0) -> None:
+               unbiased_fraction: float = 1.0 / 16.0, terminate_spread: float = 0.0, lanes: int = 2) -> None:
     """`samples` iterations of path tracing (pass_ "PT") or bidirectional
     path tracing ("BPT") with the radiance cache (gpugi_render_nrc); rng
     selects the random streams as in render.render. train_length >= 1
     turns on self-training (training paths stop at that vertex and take the
     cache's radiance, except unbiased_fraction of them); terminate_spread > 0
     stops PT render paths by path spread (0.01 in the NRC paper), at vertex
-    terminate_depth at the latest."""
+    terminate_depth at the latest. lanes: frames in flight (1-4)."""
     from . import render
     L = _declare()
     if pass_ not in ("PT", "BPT"):
@@ -166,7 +167,7 @@ def render_nrc(ctx: cuda.Context, scene: cuda.DeviceScene, camera, image, cache:
     if ls is not None:
         assert ls.shape == (samples, num_light_samples, 8)
     q = NrcParams(terminate_depth, float(train_fraction), max_train_samples, train_steps, int(bool(train)),
-                  samples_per_frame, train_length, float(unbiased_fraction), float(terminate_spread))
+                  samples_per_frame, train_length, float(unbiased_fraction), float(terminate_spread), lanes)
     st = C.c_uint64(rng_state[0] if rng_state else 0)
     ctx.check(L.gpugi_render_nrc(ctx.handle, scene.handle, C.byref(camera), C.byref(p), cuda._ptr(ls),
                                  C.byref(st) if ls is None else None, cache.handle, C.byref(q), image.handle))

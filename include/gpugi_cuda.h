@@ -520,6 +520,11 @@ typedef struct gpugi_nrc_params {
      * (the same paper, section 3.4, c = 0.01 there), and at vertex
      * terminateDepth at the latest. 0: at vertex terminateDepth. */
     float terminateSpread;
+    /* Frames in flight: frames alternate over this many wavefront lanes
+     * (buffer sets and streams; 0 = 2, at most 4), so a frame's walker tails
+     * overlap the next frames' bounces; the network's inference and training
+     * stay in frame order. */
+    uint32_t lanes;
 } gpugi_nrc_params;
 
 gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* scene, const gpugi_camera* camera,

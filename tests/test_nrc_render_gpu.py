@@ -36,8 +36,8 @@ def _light_sets(ds, n_sets, n=128, seed=123):
     return np.stack([render.generate_light_samples(ds, state, n) for _ in range(n_sets)])
 
 
-@pytest.mark.parametrize("train_fraction", [0.0, 1.0])
-def test_without_lookups_the_pass_is_plain_pt(cuda_ctx, room, train_fraction):
+@pytest.mark.parametrize("train_fraction,lanes", [(0.0, 2), (1.0, 2), (1.0, 1), (1.0, 3)])
+def test_without_lookups_the_pass_is_plain_pt(cuda_ctx, room, train_fraction, lanes):
     sc, b, ds = room
     W = H = 32
     frames = 4
@@ -49,7 +49,7 @@ def test_without_lookups_the_pass_is_plain_pt(cuda_ctx, room, train_fraction):
     img = render.Image(cuda_ctx, W, H)
     # terminate_depth beyond the path length: no render path ever queries
     nrc.render_nrc(cuda_ctx, ds, cam, img, cache, max_path_length=6, samples=frames, light_samples=ls,
-                   terminate_depth=6, train_fraction=train_fraction, train=False)
+                   terminate_depth=6, train_fraction=train_fraction, train=False, lanes=lanes)
     a, r = img.read()[..., :3], ref.read()[..., :3]
     assert np.abs(a - r).max() <= 1e-5 * np.abs(r).max() + 1e-6
     assert cuda_ctx.device_error_bits() == 0
@@ -167,8 +167,8 @@ def test_spread_termination_brackets_fixed_depth(cuda_ctx, room):
     cache.close()
 
 
-@pytest.mark.parametrize("train_length", [0, 2])
-def test_self_training_keeps_the_cache_unbiased(cuda_ctx, room, train_length):
+@pytest.mark.parametrize("train_length,unbiased", [(0, 0.0), (2, 1.0 / 16), (2, 0.0)])
+def test_self_training_keeps_the_cache_unbiased(cuda_ctx, room, train_length, unbiased):
     """Self-training (training paths take the cache's radiance at vertex
     train_length, 1/16 of them run to the end): the trained cache's image
     keeps its mean near converged PT: within 5 % with full training paths,
@@ -187,7 +187,7 @@ def test_self_training_keeps_the_cache_unbiased(cuda_ctx, room, train_length):
     reference = conv.read64() / n_ref
     cache = nrc.RadianceCache(cuda_ctx, *ROOM_BOX, seed=5)
     opts = dict(max_path_length=depth, terminate_depth=1, train_fraction=0.25, train_steps=4,
-                train_length=train_length)
+                train_length=train_length, unbiased_fraction=unbiased)
     warm = render.Image(cuda_ctx, W, H)
     nrc.render_nrc(cuda_ctx, ds, cam, warm, cache, samples=300, iteration=10000, rng_state=[11], **opts)
     img = render.Image(cuda_ctx, W, H, fp64=True)
