@@ -44,7 +44,8 @@ KERNELS = {0: "k_trace_closest<AABB>", 1: "k_trace_persistent<closest, AABB>",
            2: "k_trace_root_filter<closest, AABB> + k_trace_queue<closest, AABB>",
            3: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 8>",
            4: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 4>",
-           5: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 16>"}
+           5: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 16>",
+           6: "k_trace_root_filter<closest, AABB> + k_trace_group_spec<closest, AABB>"}
 
 
 def peaks():
@@ -1130,7 +1131,7 @@ def main():
                     help="streams the end-to-end host-buffer steps alternate over")
     ap.add_argument("--trace-mode", type=int, default=3,
                     help="0: thread per ray, 1: persistent lane refill, 2: root prefilter + persistent, "
-                         "3/4: root prefilter + 8/4-lane group walker")
+                         "3/4/5: root prefilter + 8/4/16-lane group walker, 6: speculative 8-lane group walker")
     ap.add_argument("--batch-seed", type=int, default=1)
     ap.add_argument("--host-parts", type=int, default=2,
                     help="parts of a host-pointer query whose copies and traversal overlap")
@@ -1159,7 +1160,7 @@ def main():
     ap.add_argument("--nrc-td", type=int, default=3, help="path vertex where render paths query the cache")
     ap.add_argument("--nrc-unbiased", type=float, default=1.0 / 16,
                     help="self-training: share of training paths that run to their end")
-    ap.add_argument("--nrc-lanes", type=int, default=2, help="cache frames in flight (wavefront lanes)")
+    ap.add_argument("--nrc-lanes", type=int, default=3, help="cache frames in flight (wavefront lanes)")
     ap.add_argument("--nrc-budget", type=int, default=0,
                     help="cache renderer at this many spp against the plain pass at equal RMSE (0: time to the "
                          "plain 1024-spp RMSE)")

@@ -865,13 +865,20 @@ __global__ void __launch_bounds__(256) k_nrc_infer_tc(const float* __restrict__ 
     if (warp == 0) tmem_free(tmemBase, 128);
 }
 
-// grad[i] = sum over the CTAs' partial sums (fixed order: deterministic).
-__global__ void k_nrc_sum_partials(const float* __restrict__ partials, int rows, float* __restrict__ grad) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kParams) return;
+// grad[i] = sum over the CTAs' partial sums, in a fixed order
+// (deterministic): a block of 256 threads sums 64 parameters, four row
+// groups of it in parallel, then the four group sums in order.
+__global__ void __launch_bounds__(256) k_nrc_sum_partials(const float* __restrict__ partials, int rows,
+                                                          float* __restrict__ grad) {
+    __shared__ float part[4][64];
+    const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
+    const int i = blockIdx.x * 64 + c;
     float s = 0.0f;
-    for (int r = 0; r < rows; ++r) s += partials[(size_t)r * kParams + i];
-    grad[i] = s;
+    if (i < kParams)
+        for (int r = g; r < rows; r += 4) s += partials[(size_t)r * kParams + i];
+    part[g][c] = s;
+    __syncthreads();
+    if (g == 0 && i < kParams) grad[i] = ((part[0][c] + part[1][c]) + part[2][c]) + part[3][c];
 }
 
 constexpr size_t kInferSmem = (size_t)kLayers * 64 * kRow * 2 + 4 * 16 * kRow * 2;
@@ -1069,7 +1076,7 @@ static gpugi_status nrc_grad(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples
                                                                nn->lossScale, nn->partials, nn->lossSum, predOut,
                                                                ctx->errWord);
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
-        k_nrc_sum_partials<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(nn->partials, grid, nn->grad);
+        k_nrc_sum_partials<<<(kParams + 63) / 64, 256, 0, ctx->stream>>>(nn->partials, grid, nn->grad);
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
         return GPUGI_OK;
     }
