@@ -554,18 +554,20 @@ GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long l
 // Trace mode 6: the four 8-lane groups of a warp walk in step. In a group
 // walk each group alternates node rounds and leaf rounds on its own, so a
 // warp whose groups are in different phases runs both code paths with half
-// its lanes idle. Here (the speculative traversal of Aila and Laine, "Understanding the
-// efficiency of ray traversal on GPUs", HPG 2009) a group that reaches a
-// leaf records it as pending and keeps walking from the leaf's escape; it
-// records a second leaf and then waits; the warp runs a leaf round only
-// when no group can walk on, so every group's pending leaf is tested in
-// one convergent round. Pending leaves are tested in walk order, so any
-// hit finds the same first leaf. For the closest hit the nodes walked past a
-// pending leaf are tested with the rayLength before that leaf: the walk can
-// only enter subtrees the sequential walk culls (their entry distance
-// exceeds that sequential rayLength), and their triangles, tested later
-// against the rayLength of every leaf before them, are never accepted.
-// So the results equal trace_ray's.
+// its lanes idle. Here (the speculative traversal of Aila and Laine,
+// "Understanding the efficiency of ray traversal on GPUs", HPG 2009) a
+// group that reaches a leaf records it as pending and walks on from the
+// leaf's escape; a second leaf is recorded too and the group then waits.
+// The warp runs node rounds while some group has no pending leaf, and a
+// leaf round, testing every group's first pending leaf in one convergent
+// round, once each group has one (or has finished its walk). Leaves are
+// tested in walk order. The nodes walked past a pending leaf are decided
+// with the rayLength before that leaf: when the leaf's test accepts a
+// triangle (closest hit), whatever the walk found after it is dropped and
+// the walk goes on from the leaf's escape with the new rayLength, exactly
+// as the sequential walk does; when it accepts none, the walk already made
+// is the sequential one. Any hit ends at the first leaf with a hit. So the
+// results equal trace_ray's.
 enum : uint32_t { kSpecWalk = 0, kSpecDone = 1, kSpecLeaf = 2 };
 
 template <int BOUNDS, int G, int TRI>
@@ -655,8 +657,10 @@ GPUGI_D void group_walks_spec(const DevScene& s, uint64_t n, unsigned long long*
     const uint64_t groups = (uint64_t)gridDim.x * perBlock;
     GroupWalk g;
     uint64_t my = (uint64_t)blockIdx.x * perBlock + threadIdx.x / G;
-    bool active = false, exhausted = false, fresh = true;
-    uint32_t ac = 0, ae = 0, bc = 0, be = 0;  // pending leaves A (first) and B, slot ranges
+    bool active = false, exhausted = false, fresh = true, aHit = false;
+    // pending leaves in walk order: A = slots [ac, ae), B = [bc, be), and
+    // the node the walk continues from after each (its escape)
+    uint32_t ac = 0, ae = 0, ar = 0, bc = 0, be = 0, br = 0;
     while (true) {
         if (!active && !exhausted) {
             if (!fresh) {  // the first item needs no atomic (as group_walks)
@@ -671,34 +675,47 @@ GPUGI_D void group_walks_spec(const DevScene& s, uint64_t n, unsigned long long*
                 load(my, o, d, tmax);
                 group_begin(g, s, o, d, tmax);
                 ac = ae = bc = be = 0;
+                aHit = false;
                 active = true;
             } else {
                 exhausted = true;
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        const bool searching = active && g.node != kGroupDone && be <= bc;
+        const bool walking = active && g.node != kGroupDone;
+        const bool needsLeaf = walking && ae <= ac;
         bool finished = false;
-        if (__any_sync(0xffffffffu, searching)) {
-            if (searching) {
+        if (__any_sync(0xffffffffu, needsLeaf)) {
+            if (walking && be <= bc) {
                 uint32_t lc = 0, le = 0;
                 if (spec_node_round<BOUNDS, G, TRI>(g, s, err, gl, gbase, gmask, lc, le) == kSpecLeaf && lc < le) {
                     if (ae <= ac) {
                         ac = lc;
                         ae = le;
+                        ar = g.node;
                     } else {
                         bc = lc;
                         be = le;
+                        br = g.node;
                     }
                 }
             }
         } else if (active && ac < ae) {
+            const float lenBefore = g.len;
             finished = spec_leaf_round<ANY_HIT, G, TRI>(g, s, gl, gbase, gmask, ac, ae);
+            aHit = aHit || g.len != lenBefore;
             ac += G;
             if (ac >= ae) {
-                ac = bc;
-                ae = be;
-                bc = be = 0;
+                if (!ANY_HIT && aHit) {  // rayLength changed: walk on from this leaf as the sequential walk
+                    g.node = ar;
+                    ac = ae = bc = be = 0;
+                } else {
+                    ac = bc;
+                    ae = be;
+                    ar = br;
+                    bc = be = 0;
+                }
+                aHit = false;
             }
         }
         if (active && (finished || (g.node == kGroupDone && ae <= ac && be <= bc))) {
