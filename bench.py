@@ -44,8 +44,7 @@ KERNELS = {0: "k_trace_closest<AABB>", 1: "k_trace_persistent<closest, AABB>",
            2: "k_trace_root_filter<closest, AABB> + k_trace_queue<closest, AABB>",
            3: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 8>",
            4: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 4>",
-           5: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 16>",
-           6: "k_trace_root_filter<closest, AABB> + k_trace_group_spec<closest, AABB>"}
+           5: "k_trace_root_filter<closest, AABB> + k_trace_group<closest, AABB, 16>"}
 
 
 def peaks():
@@ -1131,7 +1130,7 @@ def main():
                     help="streams the end-to-end host-buffer steps alternate over")
     ap.add_argument("--trace-mode", type=int, default=3,
                     help="0: thread per ray, 1: persistent lane refill, 2: root prefilter + persistent, "
-                         "3/4/5: root prefilter + 8/4/16-lane group walker, 6: speculative 8-lane group walker")
+                         "3/4/5: root prefilter + 8/4/16-lane group walker")
     ap.add_argument("--batch-seed", type=int, default=1)
     ap.add_argument("--host-parts", type=int, default=2,
                     help="parts of a host-pointer query whose copies and traversal overlap")

@@ -332,10 +332,10 @@ gpugi_status gpugi_device_error_bits(gpugi_ctx* ctx, uint32_t* bits) {
 
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
-    if (mode > 6)
+    if (mode > 5)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT,
-                    "mode must be 0 (thread per ray), 1 (persistent), 2 (root prefilter + persistent), "
-                    "3/4/5 (root prefilter + 8/4/16-lane group walker) or 6 (speculative 8-lane group walker)");
+                    "mode must be 0 (thread per ray), 1 (persistent), 2 (root prefilter + persistent) or "
+                    "3/4/5 (root prefilter + 8/4/16-lane group walker)");
     if (blockSize == 0 || blockSize > 256 || blockSize % 32 != 0)
         return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "blockSize must be a multiple of 32 in [32, 256]");
     ctx->traceMode = mode;

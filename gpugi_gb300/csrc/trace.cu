@@ -348,35 +348,6 @@ __global__ void __launch_bounds__(128, GPUGI_GROUP_MIN_BLOCKS) k_trace_group(
         });
 }
 
-// Speculative group walker (mode 6): group_walks_spec over the queue.
-template <bool ANY_HIT, int BOUNDS, int TRI>
-__global__ void __launch_bounds__(128, GPUGI_GROUP_MIN_BLOCKS) k_trace_group_spec(
-    DevScene s, const float* __restrict__ ox, const float* __restrict__ oy, const float* __restrict__ oz,
-    const float* __restrict__ dx, const float* __restrict__ dy, const float* __restrict__ dz,
-    const float* __restrict__ tmax, int32_t* __restrict__ slot, float* __restrict__ t, float* __restrict__ u,
-    float* __restrict__ v, uint8_t* __restrict__ occluded, const uint32_t* __restrict__ queue,
-    unsigned long long* counters, uint32_t* err) {
-    group_walks_spec<ANY_HIT, BOUNDS, TRI>(
-        s, counters[1], counters + 2, err,
-        [&](uint64_t i, float3& o, float3& d, float& len) {
-            const uint32_t ray = __ldg(queue + i);
-            o = make_float3(__ldg(ox + ray), __ldg(oy + ray), __ldg(oz + ray));
-            d = make_float3(__ldg(dx + ray), __ldg(dy + ray), __ldg(dz + ray));
-            len = __ldg(tmax + ray);
-        },
-        [&](uint64_t i, const GroupWalk& g) {
-            const uint32_t ray = __ldg(queue + i);
-            if (ANY_HIT) {
-                occluded[ray] = g.slot >= 0 ? 1 : 0;
-            } else {
-                slot[ray] = g.slot;
-                t[ray] = g.len;
-                u[ray] = g.u;
-                v[ray] = g.v;
-            }
-        });
-}
-
 gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
                                    const float* oy, const float* oz, const float* dx, const float* dy,
                                    const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
@@ -434,10 +405,6 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         auto kg = ctx->traceMode == 3
                       ? pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {
                             return &k_trace_group<decltype(A)::value, decltype(B)::value, 8, decltype(T)::value>;
-                        })
-                  : ctx->traceMode == 6
-                      ? pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {
-                            return &k_trace_group_spec<decltype(A)::value, decltype(B)::value, decltype(T)::value>;
                         })
                   : ctx->traceMode == 4
                       ? pick_variant(anyHit, ell, wt, [](auto A, auto B, auto T) {

@@ -550,181 +550,6 @@ GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long l
     }
 }
 
-// ------------------------------------------------ speculative group walk
-// Trace mode 6: the four 8-lane groups of a warp walk in step. In a group
-// walk each group alternates node rounds and leaf rounds on its own, so a
-// warp whose groups are in different phases runs both code paths with half
-// its lanes idle. Here (the speculative traversal of Aila and Laine,
-// "Understanding the efficiency of ray traversal on GPUs", HPG 2009) a
-// group that reaches a leaf records it as pending and walks on from the
-// leaf's escape; a second leaf is recorded too and the group then waits.
-// The warp runs node rounds while some group has no pending leaf, and a
-// leaf round, testing every group's first pending leaf in one convergent
-// round, once each group has one (or has finished its walk). Leaves are
-// tested in walk order. The nodes walked past a pending leaf are decided
-// with the rayLength before that leaf: when the leaf's test accepts a
-// triangle (closest hit), whatever the walk found after it is dropped and
-// the walk goes on from the leaf's escape with the new rayLength, exactly
-// as the sequential walk does; when it accepts none, the walk already made
-// is the sequential one. Any hit ends at the first leaf with a hit. So the
-// results equal trace_ray's.
-enum : uint32_t { kSpecWalk = 0, kSpecDone = 1, kSpecLeaf = 2 };
-
-template <int BOUNDS, int G, int TRI>
-GPUGI_D uint32_t spec_node_round(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned gl, unsigned gbase,
-                                 unsigned gmask, uint32_t& leafCur, uint32_t& leafEnd) {
-    if (g.budget-- == 0) {
-        raise_error(err, DEVERR_TRAVERSAL_CAP);
-        g.node = kGroupDone;
-        return kSpecDone;
-    }
-    const uint32_t p = g.node + gl;
-    uint32_t next = kGroupDone, child = 0, escape = 0;
-    if (p < s.numNodes) {
-        const float4* nd = s.nodes + node_stride<BOUNDS>() * (size_t)p;
-        const float4 a = __ldg(nd), b = __ldg(nd + 1);
-        const float4 c = BOUNDS == 2 ? __ldg(nd + 2) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        child = __float_as_uint(a.w);
-        escape = __float_as_uint(b.w);
-        float firstHit;
-        const bool hit = bounds_test<BOUNDS, TRI != 0>(g.o, g.d, g.inv, a, b, c, firstHit);
-        if (hit && firstHit <= g.len) next = (child & LEAF_FLAG) ? (kGroupLeaf | gl) : child;
-        else next = escape ? escape : kGroupDone;
-    }
-#pragma unroll
-    for (int r = 1; r < G; r <<= 1) {
-        const bool chase = next < kGroupLeaf && next - g.node < (uint32_t)G;
-        const uint32_t w = __shfl_sync(gmask, next, gbase + (chase ? next - g.node : gl));
-        next = chase ? w : next;
-    }
-    const uint32_t r0 = __shfl_sync(gmask, next, gbase);
-    if (r0 == kGroupDone) {
-        g.node = kGroupDone;
-        return kSpecDone;
-    }
-    if (r0 & kGroupLeaf) {
-        const unsigned src = gbase + (r0 & (kGroupLeaf - 1u));
-        const uint32_t lc = __shfl_sync(gmask, child, src), le = __shfl_sync(gmask, escape, src);
-        leafCur = (lc & LEAF_BLOCK_MASK) * s.leafSize;
-        leafEnd = leafCur + ((lc >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK);
-        g.node = le ? le : kGroupDone;
-        return kSpecLeaf;
-    }
-    g.node = r0;
-    return kSpecWalk;
-}
-
-// One leaf round over slots [cur, min(cur + G, end)); true when an any-hit
-// walk found its hit (g.slot set).
-template <bool ANY_HIT, int G, int TRI>
-GPUGI_D bool spec_leaf_round(GroupWalk& g, const DevScene& s, unsigned gl, unsigned gbase, unsigned gmask,
-                             uint32_t cur, uint32_t end) {
-    const uint32_t k = cur + gl;
-    float h = 0.0f, by = 0.0f, bz = 0.0f;
-    bool ok = false;
-    if (k < end) ok = slot_test<TRI>(s, g.o, g.d, g.wt, k, h, by, bz) && h < g.len;
-    if (ANY_HIT) {
-        const uint32_t key = __reduce_min_sync(gmask, ok ? k : kGroupDone);
-        if (key != kGroupDone) {
-            g.slot = (int32_t)key;
-            return true;
-        }
-        return false;
-    }
-    const uint32_t hb = __reduce_min_sync(gmask, ok ? __float_as_uint(h) : kGroupDone);
-    const unsigned tie = __ballot_sync(gmask, ok && __float_as_uint(h) == hb);
-    const unsigned src = tie ? (unsigned)(__ffs(tie) - 1) : gbase;
-    const float wu = __shfl_sync(gmask, by, src), wv = __shfl_sync(gmask, bz, src);
-    if (tie) {
-        g.slot = (int32_t)(cur + (src - gbase));
-        g.len = __uint_as_float(hb);
-        g.u = wu;
-        g.v = wv;
-    }
-    return false;
-}
-
-// Persistent loop of speculative group walks (8-lane groups, whole warps in
-// step): as group_walks, with the rounds chosen per warp.
-template <bool ANY_HIT, int BOUNDS, int TRI, typename Load, typename Finish>
-GPUGI_D void group_walks_spec(const DevScene& s, uint64_t n, unsigned long long* work, uint32_t* err, Load load,
-                              Finish finish) {
-    constexpr int G = 8;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned gl = lane & (G - 1), gbase = lane & ~(unsigned)(G - 1);
-    const unsigned gmask = ((1u << G) - 1u) << gbase;
-    const uint64_t perBlock = blockDim.x / G;
-    const uint64_t groups = (uint64_t)gridDim.x * perBlock;
-    GroupWalk g;
-    uint64_t my = (uint64_t)blockIdx.x * perBlock + threadIdx.x / G;
-    bool active = false, exhausted = false, fresh = true, aHit = false;
-    // pending leaves in walk order: A = slots [ac, ae), B = [bc, be), and
-    // the node the walk continues from after each (its escape)
-    uint32_t ac = 0, ae = 0, ar = 0, bc = 0, be = 0, br = 0;
-    while (true) {
-        if (!active && !exhausted) {
-            if (!fresh) {  // the first item needs no atomic (as group_walks)
-                unsigned long long next = 0;
-                if (gl == 0) next = atomicAdd(work, 1ull);
-                my = groups + __shfl_sync(gmask, next, gbase);
-            }
-            fresh = false;
-            if (my < n) {
-                float3 o, d;
-                float tmax;
-                load(my, o, d, tmax);
-                group_begin(g, s, o, d, tmax);
-                ac = ae = bc = be = 0;
-                aHit = false;
-                active = true;
-            } else {
-                exhausted = true;
-            }
-        }
-        if (!__any_sync(0xffffffffu, active)) break;
-        const bool walking = active && g.node != kGroupDone;
-        const bool needsLeaf = walking && ae <= ac;
-        bool finished = false;
-        if (__any_sync(0xffffffffu, needsLeaf)) {
-            if (walking && be <= bc) {
-                uint32_t lc = 0, le = 0;
-                if (spec_node_round<BOUNDS, G, TRI>(g, s, err, gl, gbase, gmask, lc, le) == kSpecLeaf && lc < le) {
-                    if (ae <= ac) {
-                        ac = lc;
-                        ae = le;
-                        ar = g.node;
-                    } else {
-                        bc = lc;
-                        be = le;
-                        br = g.node;
-                    }
-                }
-            }
-        } else if (active && ac < ae) {
-            const float lenBefore = g.len;
-            finished = spec_leaf_round<ANY_HIT, G, TRI>(g, s, gl, gbase, gmask, ac, ae);
-            aHit = aHit || g.len != lenBefore;
-            ac += G;
-            if (ac >= ae) {
-                if (!ANY_HIT && aHit) {  // rayLength changed: walk on from this leaf as the sequential walk
-                    g.node = ar;
-                    ac = ae = bc = be = 0;
-                } else {
-                    ac = bc;
-                    ae = be;
-                    ar = br;
-                    bc = be = 0;
-                }
-                aHit = false;
-            }
-        }
-        if (active && (finished || (g.node == kGroupDone && ae <= ac && be <= bc))) {
-            if (gl == 0) finish(my, g);
-            active = false;
-        }
-    }
-}
-
 template <bool ANY_HIT, int BOUNDS, int G, int TRI = 0, typename Load, typename Finish>
 GPUGI_D void group_walks(const DevScene& scene, uint64_t n, unsigned long long* work, uint32_t* err, Load load,
                          Finish finish) {

@@ -145,7 +145,7 @@ gpugi_status gpugi_autotune(gpugi_ctx* ctx, const gpugi_scene* sc, uint32_t flag
         struct Cand {
             uint32_t mode, block;
         };
-        const Cand cands[] = {{0, 64}, {0, 128}, {0, 256}, {1, 128}, {2, 128}, {3, 128}, {4, 128}, {5, 128}, {6, 128}};
+        const Cand cands[] = {{0, 64}, {0, 128}, {0, 256}, {1, 128}, {2, 128}, {3, 128}, {4, 128}, {5, 128}};
         const uint32_t keepMode = ctx->traceMode, keepBlock = ctx->traceBlock;
         double best = -1.0;
         gpugi_status st = GPUGI_OK;

@@ -286,11 +286,8 @@ gpugi_status gpugi_trace_stats_device(gpugi_ctx* ctx, const gpugi_scene* scene,
  * rest (warp-ballot compaction) for the persistent walker; modes 3
  * (default), 4 and 5: the same prefilter, then groups of 8 (mode 3), 4
  * (mode 4) or 16 (mode 5) lanes walk one ray together, testing a window of
- * consecutive preorder nodes or leaf slots per round; mode 6: the 8-lane
- * groups of a warp walk in step, a group that reaches a leaf keeps walking
- * and its pending leaves are tested when no group of the warp can walk on
- * (speculative traversal; leaves are tested in walk order). All modes
- * return identical results (TraceRay's). blockSize applies to mode 0. */
+ * consecutive preorder nodes or leaf slots per round. All modes make the same decisions per ray as TraceRay and
+ * return identical results. blockSize applies to mode 0. */
 gpugi_status gpugi_set_trace_config(gpugi_ctx* ctx, uint32_t mode, uint32_t blockSize);
 
 /* Host-pointer ray queries (gpugi_trace_closest / gpugi_trace_any). The

@@ -107,7 +107,7 @@ def test_instanced_ellipsoid_hierarchy_bit_exact(cuda_ctx, instanced_ellipsoids)
     oa = oracle.trace_any(b, sc["positions"], rays)["occluded"]
     assert (o["slot"] >= 0).mean() > 0.5
     try:
-        for mode in (0, 1, 2, 3, 4, 5, 6):
+        for mode in (0, 1, 2, 3, 4, 5):
             cuda_ctx.set_trace_config(mode=mode)
             g = cuda.trace_closest(cuda_ctx, ds, rays)
             assert np.array_equal(g["slot"], o["slot"]), (mode, (g["slot"] != o["slot"]).sum())

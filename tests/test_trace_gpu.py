@@ -43,7 +43,7 @@ def test_closest_and_any_match_oracle(cuda_ctx, icosphere_65536, method, leaf):
     b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, leaf_size=leaf)
     ds = cuda_ctx.upload_scene(b, sc["positions"])
     try:
-        for mode in (0, 1, 2, 3, 4, 5, 6):  # thread per ray / lane refill / root prefilter + persistent / + 8-, 4-, 16-lane groups
+        for mode in (0, 1, 2, 3, 4, 5):  # thread per ray / lane refill / root prefilter + persistent / + 8-, 4-, 16-lane groups
             cuda_ctx.set_trace_config(mode=mode)
             for rays in (scenes.random_rays(1 << 18, seed=3), scenes.aimed_rays(1 << 18, sc["positions"], seed=4)):
                 g = cuda.trace_closest(cuda_ctx, ds, rays)
@@ -66,7 +66,7 @@ def test_ellipsoid_bounds_match_oracle_and_bruteforce(cuda_ctx, method):
     b = bvh.build_bvh(sc["positions"], sc["triangles"], method=method, fit="ellipsoid")
     assert b.bounds_kind == 1
     ds = cuda_ctx.upload_scene(b, sc["positions"])
-    for mode in (0, 1, 2, 3, 4, 5, 6):
+    for mode in (0, 1, 2, 3, 4, 5):
         cuda_ctx.set_trace_config(mode=mode)
         for rays in (scenes.aimed_rays(40_000, sc["positions"], seed=13), scenes.random_rays(40_000, seed=14)):
             g = cuda.trace_closest(cuda_ctx, ds, rays)
@@ -91,7 +91,7 @@ def test_staged_layouts_give_identical_results(cuda_ctx, icosphere_65536, shared
         rays = scenes.aimed_rays(1 << 17, sc["positions"], seed=77, spread=2.5)
         o = oracle.trace_closest(b, sc["positions"], rays)
         oa = oracle.trace_any(b, sc["positions"], rays)["occluded"]
-        for mode in (0, 1, 2, 3, 4, 5, 6):
+        for mode in (0, 1, 2, 3, 4, 5):
             cuda_ctx.set_trace_config(mode=mode)
             _compare_closest(cuda.trace_closest(cuda_ctx, ds, rays), o)
             assert np.array_equal(cuda.trace_any(cuda_ctx, ds, rays), oa)
@@ -403,7 +403,7 @@ def test_oriented_box_hierarchy_bit_exact(cuda_ctx, icosphere_65536, watertight)
         for rays in (scenes.random_rays(1 << 18, seed=61), scenes.aimed_rays(1 << 17, sc["positions"], seed=62)):
             o = oracle.trace_closest(b, sc["positions"], rays, watertight=watertight)
             oa = oracle.trace_any(b, sc["positions"], rays, watertight=watertight)["occluded"]
-            for mode in (0, 1, 2, 3, 4, 5, 6):
+            for mode in (0, 1, 2, 3, 4, 5):
                 cuda_ctx.set_trace_config(mode=mode)
                 _compare_closest(cuda.trace_closest(cuda_ctx, ds, rays), o)
                 assert np.array_equal(cuda.trace_any(cuda_ctx, ds, rays), oa)
