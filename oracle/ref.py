@@ -139,3 +139,37 @@ def render_pt(bvh, scene: dict, width: int, height: int, camera: np.ndarray, fra
                              _p(accum), _threads())
     assert rc == 0
     return accum
+
+
+def render_lt(bvh, scene: dict, width: int, height: int, camera: np.ndarray, frame_seed: int,
+              light_samples: np.ndarray, max_path_length: int = 8, accum: np.ndarray | None = None,
+              bidir: bool = False) -> np.ndarray:
+    """One iteration of LightPathtracer::Draw with the reference's
+    lighttracer.comp and showlightcaches.comp, or (bidir) of
+    BidirectionalPathtracer::Draw with lighttracer.comp (SAVE_LIGHT_CACHE)
+    and pathtracer_bidir.comp; invocations in order on one thread,
+    accumulated into accum (H, W, 4) float32. Rays per light sample as
+    LightPathtracer::SetScreenSize (lightpathtracer.cpp:34)."""
+    from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
+    assert bvh.leaf_size == 8 and bvh.bounds_kind == 0, "the light tracer is built for 8-slot AABB hierarchies"
+    L = lib()
+    L.ref_render_lt.argtypes = [C.c_void_p] * 5 + [C.c_int] * 4 + [C.c_void_p, C.c_uint32, C.c_void_p, C.c_int,
+                                                                    C.c_int, C.c_int, C.c_void_p]
+    L.ref_render_lt.restype = C.c_int
+    hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
+    slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
+    pos = np.ascontiguousarray(scene["positions"], dtype=np.float32)
+    vi = np.ascontiguousarray(vertex_info(scene["normals"], scene["texcoords"]), dtype=np.float32)
+    mats = np.ascontiguousarray(scene["materials"], dtype=np.float32).reshape(-1, 24)
+    cam = np.ascontiguousarray(camera, dtype=np.float32)
+    ls = np.ascontiguousarray(light_samples, dtype=np.float32).reshape(-1, 8)
+    rays = max(64, (width * height // ls.shape[0] // 64) * 64)
+    if accum is None:
+        accum = np.zeros((height, width, 4), np.float32)
+    assert accum.dtype == np.float32 and accum.flags.c_contiguous
+    rc = L.ref_render_lt(_p(hier), _p(slots), _p(pos), _p(vi), _p(mats), mats.shape[0], width, height,
+                         max_path_length, _p(cam), frame_seed & 0xFFFFFFFF, _p(ls), ls.shape[0], rays, int(bidir),
+                         _p(accum))
+    assert rc == 0
+    return accum
+

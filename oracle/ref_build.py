@@ -5,8 +5,11 @@ compute shaders (gpugi/shader/), which need an OpenGL 4.5 context that no
 machine here has. Their text is nearly C++ already, so this recipe rewrites
 it mechanically and compiles it on the CPU against oracle/ref_shim.hpp (the
 GLSL built-ins). The library it builds, oracle/_ref/libgpugi_ref.so, is the
-reference's own code for the path; tests/test_ref_pinned.py checks the
-oracle's restatement (oracle/*.cpp) against it bit for bit.
+reference's own code for the path (traversal, the random and helper
+functions, pathtracer.comp, lighttracer.comp with and without
+SAVE_LIGHT_CACHE, showlightcaches.comp and pathtracer_bidir.comp);
+tests/test_ref_pinned.py checks the oracle's restatement (oracle/*.cpp)
+against it bit for bit.
 
 The rewrite (nothing else is changed; no reference text is stored in the
 repository: the rewritten copies live in oracle/_ref/gen/, which is
@@ -51,7 +54,9 @@ DEFAULT_REFERENCE = Path(os.environ.get("GPUGI_REFERENCE", "/root/reference")) /
 
 # Shader files the glue includes (directly or through #include).
 FILES = ["helper.glsl", "scenedata.glsl", "intersectiontests.glsl", "random.glsl", "traceray.glsl",
-         "globaluniforms.glsl", "materials.glsl", "lightsource.glsl", "stdheader.glsl", "pathtracer.comp"]
+         "globaluniforms.glsl", "materials.glsl", "lightsource.glsl", "stdheader.glsl", "pathtracer.comp",
+         "lighttracer.comp", "screenreproject.glsl", "showlightcaches.comp", "bidirpathtracer/lightcache.glsl",
+         "bidirpathtracer/pathtracer_bidir.comp"]
 OVERRIDABLE = {"TRIANGLES_PER_LEAF"}
 
 _CTOR = re.compile(r"\b((?:i|u|b)?vec[234])\s*\(")

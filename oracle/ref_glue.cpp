@@ -10,6 +10,9 @@
 //                                       with OBOX_BVH (oriented boxes), leaf blocks of 8
 //   ref_eval                            random.glsl / helper.glsl functions
 //   ref_render_pt                       pathtracer.comp's main() per pixel
+//   ref_render_lt                       lighttracer.comp + showlightcaches.comp (LightPathtracer::Draw),
+//                                       or with bidir the cache-filling light pass + pathtracer_bidir.comp
+#include <algorithm>
 #include <cstdint>
 #include <thread>
 #include <vector>
@@ -83,6 +86,86 @@ int g_maxPathLength = 8;  // MAX_PATHLENGTH, injected by the application (applic
 #undef TRIANGLES_PER_LEAF
 #undef MAX_PATHLENGTH
 }  // namespace ref_pt
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+
+// ------------------------------------------------ lighttracer.comp (LightPathtracer's shader)
+namespace ref_lt {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define main LighttracerMain
+#include "lighttracer.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_lt
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+
+// ------------------------------------------------ showlightcaches.comp (RendererSystem::DispatchShowLightCacheShader)
+namespace ref_slc {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define main ShowLightCachesMain
+#include "showlightcaches.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_slc
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+
+// ------------------------------------------------ BidirectionalPathtracer's shaders
+// the light pass: lighttracer.comp with SAVE_LIGHT_CACHE (bidirectionalpathtracer.cpp:146-147)
+namespace ref_bpl {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define SAVE_LIGHT_CACHE
+#define main BidirLightMain
+#include "lighttracer.comp.h"
+#undef main
+#undef SAVE_LIGHT_CACHE
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_bpl
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+
+// the eye pass: bidirpathtracer/pathtracer_bidir.comp
+namespace ref_bpe {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define main BidirEyeMain
+#include "bidirpathtracer/pathtracer_bidir.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_bpe
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
 
 namespace {
 
@@ -317,7 +400,7 @@ int ref_render_pt(const float* hierarchy, const int32_t* slots, const float* pos
     P::FrameSeed = frameSeed;
     P::IterationCount = 0;
     P::EnvironmentMap.colour = vec3(sky[0], sky[1], sky[2]);
-    P::OutputTexture = image2D{reinterpret_cast<vec4*>(accum), width};
+    P::OutputTexture = image2D{reinterpret_cast<vec4*>(accum), width, height};
     P::g_maxPathLength = maxPathLength;
     parallel_for((uint64_t)width * height, numThreads, [&](uint64_t b, uint64_t e) {
         for (uint64_t i = b; i < e; ++i) {
@@ -325,6 +408,108 @@ int ref_render_pt(const float* hierarchy, const int32_t* slots, const float* pos
             P::PathtracerMain();
         }
     });
+    g_textureColours = nullptr;
+    return 0;
+}
+
+// One iteration of LightPathtracer::Draw (lightpathtracer.cpp:45-51), or
+// with bidir of BidirectionalPathtracer::Draw: the
+// light tracer over numLightSamples x raysPerLightSample invocations, then
+// showlightcaches.comp over the light samples (the reference dispatches it
+// with 64 invocations per light sample, lightpathtracer.cpp:48 via
+// renderersystem.cpp:280; the ones past the last sample read zero light
+// samples and add nothing). Invocations run in order on one thread, so the
+// image sums are in a fixed order.
+int ref_render_lt(const float* hierarchy, const int32_t* slots, const float* positions, const float* vertexInfo,
+                  const float* materials, int numMaterials, int width, int height, int maxPathLength,
+                  const float* cam, uint32_t frameSeed, const float* lightSamples, int numLightSamples,
+                  int raysPerLightSample, int bidir, float* accum) {
+    using namespace glslref;
+    if (numMaterials > 256) return 1;
+    std::vector<vec4> colours(4 * (size_t)numMaterials);
+    auto bind = [&](auto& M, int m, const float* r) {
+        M.diffuseTexHandle = uvec2(4 * m + 0, 0);
+        M.opacityTexHandle = uvec2(4 * m + 1, 0);
+        M.reflectivenessTexHandle = uvec2(4 * m + 2, 0);
+        M.emissivityTexHandle = uvec2(4 * m + 3, 0);
+        M.Fresnel0 = vec3(r[16], r[17], r[18]);
+        M.RefractionIndexAvg = r[3];
+        M.Fresnel1 = vec3(r[20], r[21], r[22]);
+    };
+    for (int m = 0; m < numMaterials; ++m) {
+        const float* r = materials + 24 * (size_t)m;
+        colours[4 * m + 0] = vec4(r[0], r[1], r[2], 1.0f);
+        colours[4 * m + 1] = vec4(r[4], r[5], r[6], 1.0f);
+        colours[4 * m + 2] = vec4(r[8], r[9], r[10], r[11]);
+        colours[4 * m + 3] = vec4(r[12], r[13], r[14], 1.0f);
+        bind(ref_lt::Materials[m], m, r);
+        bind(ref_slc::Materials[m], m, r);
+        bind(ref_bpl::Materials[m], m, r);
+        bind(ref_bpe::Materials[m], m, r);
+    }
+    g_textureColours = colours.data();
+#define GPUGI_REF_SCENE(NS)                                                           \
+    NS::HierachyBuffer = samplerBuffer{hierarchy, 4};                                 \
+    NS::TriangleBuffer = isamplerBuffer{reinterpret_cast<const ivec4*>(slots)};       \
+    NS::VertexPositionBuffer = samplerBuffer{positions, 3};                           \
+    NS::VertexInfoBuffer = samplerBuffer{vertexInfo, 4};                              \
+    NS::InitialLightSampleBuffer = samplerBuffer{lightSamples, 4};                    \
+    NS::BackbufferSize = ivec2(width, height);                                        \
+    NS::NumInitialLightSamples = numLightSamples;                                     \
+    NS::CameraU = vec3(cam[0], cam[1], cam[2]);                                       \
+    NS::CameraV = vec3(cam[3], cam[4], cam[5]);                                       \
+    NS::CameraW = vec3(cam[6], cam[7], cam[8]);                                       \
+    NS::CameraPosition = vec3(cam[9], cam[10], cam[11]);                              \
+    NS::PixelArea = cam[12];                                                          \
+    NS::FrameSeed = frameSeed;                                                        \
+    NS::IterationCount = 0;                                                           \
+    NS::OutputTexture = image2D{reinterpret_cast<vec4*>(accum), width, height};       \
+    NS::g_maxPathLength = maxPathLength;
+    GPUGI_REF_SCENE(ref_lt)
+    GPUGI_REF_SCENE(ref_slc)
+    GPUGI_REF_SCENE(ref_bpl)
+    GPUGI_REF_SCENE(ref_bpe)
+#undef GPUGI_REF_SCENE
+    const uint64_t n = (uint64_t)numLightSamples * raysPerLightSample;
+    if (!bidir) {
+        ref_lt::NumRaysPerLightSample = raysPerLightSample;
+        for (uint64_t i = 0; i < n; ++i) {
+            gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+            ref_lt::LighttracerMain();
+        }
+        for (int i = 0; i < numLightSamples; ++i) {
+            gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+            ref_slc::ShowLightCachesMain();
+        }
+    } else {
+        // BidirectionalPathtracer::Draw: resetcounter.comp, the light pass
+        // filling the cache, then the eye pass per pixel. The capacity is the
+        // worst case (every light path stores at most maxPathLength + 1
+        // entries) instead of the warm-up estimate, so nothing is dropped.
+        std::vector<ref_bpl::LightCacheEntry> cache(n * (uint64_t)(maxPathLength + 1));
+        ref_bpl::LightCacheEntries = cache.data();
+        ref_bpl::NumRaysPerLightSample = raysPerLightSample;
+        ref_bpl::LightRayPixelWeight = 2.0f * 3.14159265358979f / (float)raysPerLightSample;
+        ref_bpl::LightCacheCapacity = (int)cache.size();
+        ref_bpl::AverageLightPathLength = 1;
+        ref_bpl::NumLightCacheEntries = raysPerLightSample * numLightSamples;  // resetcounter.comp
+        ref_bpl::LightPathLengthSum = 0;
+        for (uint64_t i = 0; i < n; ++i) {
+            gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+            ref_bpl::BidirLightMain();
+        }
+        ref_bpe::LightCacheEntries = reinterpret_cast<ref_bpe::LightCacheEntry*>(cache.data());
+        ref_bpe::NumLightCacheEntries = std::min<int>(ref_bpl::NumLightCacheEntries, (int)cache.size());
+        ref_bpe::NumRaysPerLightSample = raysPerLightSample;
+        ref_bpe::LightRayPixelWeight = ref_bpl::LightRayPixelWeight;
+        ref_bpe::LightCacheCapacity = (int)cache.size();
+        ref_bpe::AverageLightPathLength = 1;
+        for (int y = 0; y < height; ++y)
+            for (int x = 0; x < width; ++x) {
+                gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
+                ref_bpe::BidirEyeMain();
+            }
+    }
     g_textureColours = nullptr;
     return 0;
 }

@@ -268,12 +268,44 @@ struct samplerCubeArray {
 };
 inline vec4 textureLod(const samplerCubeArray& s, vec4, float) { return vec4(s.colour, 1.0f); }
 
-// image2D: RGBA32F texels, row-major, width given.
+// image2D: RGBA32F texels, row-major, width x height. As in GL, a store
+// outside the image is discarded and a load there returns zero.
 struct image2D {
     vec4* texels = nullptr;
     int width = 0;
+    int height = 0;
 };
-inline vec4 imageLoad(const image2D& im, ivec2 p) { return im.texels[(int64_t)p.y * im.width + p.x]; }
-inline void imageStore(image2D& im, ivec2 p, vec4 v) { im.texels[(int64_t)p.y * im.width + p.x] = v; }
+inline bool image_inside(const image2D& im, ivec2 p, int widthScale = 1) {
+    return p.x >= 0 && p.y >= 0 && p.x < widthScale * im.width && p.y < im.height;
+}
+inline vec4 imageLoad(const image2D& im, ivec2 p) {
+    return image_inside(im, p) ? im.texels[(int64_t)p.y * im.width + p.x] : vec4(0.0f);
+}
+inline void imageStore(image2D& im, ivec2 p, vec4 v) {
+    if (image_inside(im, p)) im.texels[(int64_t)p.y * im.width + p.x] = v;
+}
+// The light tracer binds the same RGBA32F image as r32f, four floats per
+// texel side by side (screenreproject.glsl:7, 44-47): the float at column x
+// of row y. Atomic (a compare-and-swap loop on the bits); returns the old value.
+inline float imageAtomicAdd(image2D& im, ivec2 p, float v) {
+    if (!image_inside(im, p, 4)) return 0.0f;
+    uint32_t* u = reinterpret_cast<uint32_t*>(reinterpret_cast<float*>(im.texels) + (int64_t)p.y * 4 * im.width + p.x);
+    uint32_t old = __atomic_load_n(u, __ATOMIC_RELAXED), next;
+    float f;
+    do {
+        std::memcpy(&f, &old, 4);
+        const float n = f + v;
+        std::memcpy(&next, &n, 4);
+    } while (!__atomic_compare_exchange_n(u, &old, next, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED));
+    return f;
+}
+// atomicAdd on a storage-buffer integer (the light cache's entry counter,
+// lightcache.glsl:27-35): returns the old value.
+inline int atomicAdd(int& x, int v) { return __atomic_fetch_add(&x, v, __ATOMIC_RELAXED); }
+// The lock image of the reference's commented-out spin lock (declared, unused).
+struct uimage2D {
+    uint32_t* texels = nullptr;
+    int width = 0;
+};
 
 }  // namespace glslref

@@ -14,7 +14,13 @@ oracle's restatement on the same inputs and require identical bits:
   * the random.glsl / helper.glsl functions on random inputs;
   * whole path-traced images (pathtracer.comp's main per pixel) on the
     Cornell room and on a room with glossy surfaces, depth 1 and depth 8,
-    with the reference's random streams and Russian roulette.
+    with the reference's random streams and Russian roulette;
+  * whole light-traced images (LightPathtracer::Draw: lighttracer.comp,
+    then showlightcaches.comp) and bidirectional images
+    (BidirectionalPathtracer::Draw: lighttracer.comp with SAVE_LIGHT_CACHE,
+    then pathtracer_bidir.comp per pixel) on the same rooms; both sides run
+    their invocations in order on one thread, so the atomic image sums and
+    the light-cache order are the same.
 The GPU kernels are in turn checked against the oracle (tests/test_trace_gpu.py:
 bit-exact traversal; tests/test_render_gpu.py: images). The tests skip where
 the reference tree is absent and the library was not built.
@@ -153,3 +159,26 @@ def test_path_tracer_images(room, depth, sky):
                               rng="reference")
         assert np.array_equal(acc_r.view(np.uint32), acc_o.view(np.uint32)), (it, np.abs(acc_r - acc_o).max())
     assert acc_r[..., :3].mean() > 0
+
+
+@pytest.mark.parametrize("pass_", ["LT", "BPT"])
+@pytest.mark.parametrize("room,depth", [("diffuse", 1), ("diffuse", 6), ("glossy", 8)])
+def test_light_and_bidirectional_images(room, depth, pass_):
+    """lighttracer.comp + showlightcaches.comp, and the light-cache pass +
+    pathtracer_bidir.comp (the reference's text), against the oracle's LT and
+    BPT restatements: identical images, iteration by iteration."""
+    sc = scenes.cornell_room(seed=1, sphere_level=3, wall_grid=8) if room == "diffuse" else _glossy_room()
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    W, H = 40, 32
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H).as_array()
+    acc_r = acc_o = None
+    st = [321]
+    for it in range(2):
+        ls = oracle.light_samples(sc["positions"], b.slots, sc["materials"], render.DEFAULT_LIGHT_SAMPLES[pass_], st)
+        fs = render.frame_seed(it, "reference")
+        acc_r = ref.render_lt(b, sc, W, H, cam, fs, ls, max_path_length=depth, accum=acc_r, bidir=pass_ == "BPT")
+        acc_o = oracle.render(b, sc, pass_, W, H, cam, fs, ls, max_path_length=depth, accum=acc_o, rng="reference",
+                              num_threads=1)
+        assert np.array_equal(acc_r.view(np.uint32), acc_o.view(np.uint32)), (it, np.abs(acc_r - acc_o).max())
+    assert acc_r[..., :3].mean() > 0
+
