@@ -173,3 +173,15 @@ def render_lt(bvh, scene: dict, width: int, height: int, camera: np.ndarray, fra
     assert rc == 0
     return accum
 
+
+def _render_light(bvh, scene, width, height, camera, frame_seed, light_samples, max_path_length, accum, kind):
+    return render_lt(bvh, scene, width, height, camera, frame_seed, light_samples, max_path_length, accum, kind)
+
+
+def render_whitted(bvh, scene: dict, width: int, height: int, camera: np.ndarray, frame_seed: int,
+                   light_samples: np.ndarray, max_path_length: int = 8, accum: np.ndarray | None = None) -> np.ndarray:
+    """One iteration of WhittedRayTracer::Draw with the reference's
+    whittedraytracer.comp (STOP_ON_DIFFUSE_BOUNCE, whittedraytracer.cpp:40),
+    pixels in order on one thread, accumulated into accum (H, W, 4)."""
+    return _render_light(bvh, scene, width, height, camera, frame_seed, light_samples, max_path_length, accum, 2)
+

@@ -7,7 +7,8 @@ it mechanically and compiles it on the CPU against oracle/ref_shim.hpp (the
 GLSL built-ins). The library it builds, oracle/_ref/libgpugi_ref.so, is the
 reference's own code for the path (traversal, the random and helper
 functions, pathtracer.comp, lighttracer.comp with and without
-SAVE_LIGHT_CACHE, showlightcaches.comp and pathtracer_bidir.comp);
+SAVE_LIGHT_CACHE, showlightcaches.comp, pathtracer_bidir.comp and
+whittedraytracer.comp);
 tests/test_ref_pinned.py checks the oracle's restatement (oracle/*.cpp)
 against it bit for bit.
 
@@ -56,7 +57,7 @@ DEFAULT_REFERENCE = Path(os.environ.get("GPUGI_REFERENCE", "/root/reference")) /
 FILES = ["helper.glsl", "scenedata.glsl", "intersectiontests.glsl", "random.glsl", "traceray.glsl",
          "globaluniforms.glsl", "materials.glsl", "lightsource.glsl", "stdheader.glsl", "pathtracer.comp",
          "lighttracer.comp", "screenreproject.glsl", "showlightcaches.comp", "bidirpathtracer/lightcache.glsl",
-         "bidirpathtracer/pathtracer_bidir.comp"]
+         "bidirpathtracer/pathtracer_bidir.comp", "whittedraytracer.comp"]
 OVERRIDABLE = {"TRIANGLES_PER_LEAF"}
 
 _CTOR = re.compile(r"\b((?:i|u|b)?vec[234])\s*\(")

@@ -11,7 +11,8 @@
 //   ref_eval                            random.glsl / helper.glsl functions
 //   ref_render_pt                       pathtracer.comp's main() per pixel
 //   ref_render_lt                       lighttracer.comp + showlightcaches.comp (LightPathtracer::Draw),
-//                                       or with bidir the cache-filling light pass + pathtracer_bidir.comp
+//                                       or with bidir the cache-filling light pass + pathtracer_bidir.comp,
+//                                       or (bidir = 2) whittedraytracer.comp per pixel
 #include <algorithm>
 #include <cstdint>
 #include <thread>
@@ -161,6 +162,26 @@ int g_maxPathLength = 8;
 #undef TRIANGLES_PER_LEAF
 #undef MAX_PATHLENGTH
 }  // namespace ref_bpe
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+
+// ------------------------------------------------ whittedraytracer.comp (WhittedRayTracer's shader)
+namespace ref_wh {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define STOP_ON_DIFFUSE_BOUNCE  // whittedraytracer.cpp:40
+#define main WhittedMain
+#include "whittedraytracer.comp.h"
+#undef main
+#undef STOP_ON_DIFFUSE_BOUNCE
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_wh
 // the shader's own switches end with it
 #undef TRINORMAL_OUTPUT
 #undef SAMPLING_DECISION_OUTPUT
@@ -446,6 +467,7 @@ int ref_render_lt(const float* hierarchy, const int32_t* slots, const float* pos
         bind(ref_slc::Materials[m], m, r);
         bind(ref_bpl::Materials[m], m, r);
         bind(ref_bpe::Materials[m], m, r);
+        bind(ref_wh::Materials[m], m, r);
     }
     g_textureColours = colours.data();
 #define GPUGI_REF_SCENE(NS)                                                           \
@@ -469,9 +491,16 @@ int ref_render_lt(const float* hierarchy, const int32_t* slots, const float* pos
     GPUGI_REF_SCENE(ref_slc)
     GPUGI_REF_SCENE(ref_bpl)
     GPUGI_REF_SCENE(ref_bpe)
+    GPUGI_REF_SCENE(ref_wh)
 #undef GPUGI_REF_SCENE
     const uint64_t n = (uint64_t)numLightSamples * raysPerLightSample;
-    if (!bidir) {
+    if (bidir == 2) {  // WhittedRayTracer::Draw: whittedraytracer.comp per pixel
+        for (int y = 0; y < height; ++y)
+            for (int x = 0; x < width; ++x) {
+                gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
+                ref_wh::WhittedMain();
+            }
+    } else if (!bidir) {
         ref_lt::NumRaysPerLightSample = raysPerLightSample;
         for (uint64_t i = 0; i < n; ++i) {
             gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
