@@ -143,7 +143,8 @@ def render_pt(bvh, scene: dict, width: int, height: int, camera: np.ndarray, fra
 
 def render_lt(bvh, scene: dict, width: int, height: int, camera: np.ndarray, frame_seed: int,
               light_samples: np.ndarray, max_path_length: int = 8, accum: np.ndarray | None = None,
-              bidir: bool = False) -> np.ndarray:
+              bidir: bool = False, rays_per_light_sample: int | None = None, param: float = 0.0,
+              position: np.ndarray | None = None) -> np.ndarray:
     """One iteration of LightPathtracer::Draw with the reference's
     lighttracer.comp and showlightcaches.comp, or (bidir) of
     BidirectionalPathtracer::Draw with lighttracer.comp (SAVE_LIGHT_CACHE)
@@ -154,7 +155,8 @@ def render_lt(bvh, scene: dict, width: int, height: int, camera: np.ndarray, fra
     assert bvh.leaf_size == 8 and bvh.bounds_kind == 0, "the light tracer is built for 8-slot AABB hierarchies"
     L = lib()
     L.ref_render_lt.argtypes = [C.c_void_p] * 5 + [C.c_int] * 4 + [C.c_void_p, C.c_uint32, C.c_void_p, C.c_int,
-                                                                    C.c_int, C.c_int, C.c_void_p]
+                                                                    C.c_int, C.c_int, C.c_float, C.c_void_p,
+                                                                    C.c_void_p]
     L.ref_render_lt.restype = C.c_int
     hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
     slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
@@ -163,13 +165,13 @@ def render_lt(bvh, scene: dict, width: int, height: int, camera: np.ndarray, fra
     mats = np.ascontiguousarray(scene["materials"], dtype=np.float32).reshape(-1, 24)
     cam = np.ascontiguousarray(camera, dtype=np.float32)
     ls = np.ascontiguousarray(light_samples, dtype=np.float32).reshape(-1, 8)
-    rays = max(64, (width * height // ls.shape[0] // 64) * 64)
+    rays = rays_per_light_sample or max(64, (width * height // ls.shape[0] // 64) * 64)
     if accum is None:
         accum = np.zeros((height, width, 4), np.float32)
     assert accum.dtype == np.float32 and accum.flags.c_contiguous
     rc = L.ref_render_lt(_p(hier), _p(slots), _p(pos), _p(vi), _p(mats), mats.shape[0], width, height,
                          max_path_length, _p(cam), frame_seed & 0xFFFFFFFF, _p(ls), ls.shape[0], rays, int(bidir),
-                         _p(accum))
+                         float(param), _p(accum), None if position is None else _p(position))
     assert rc == 0
     return accum
 
@@ -184,4 +186,27 @@ def render_whitted(bvh, scene: dict, width: int, height: int, camera: np.ndarray
     whittedraytracer.comp (STOP_ON_DIFFUSE_BOUNCE, whittedraytracer.cpp:40),
     pixels in order on one thread, accumulated into accum (H, W, 4)."""
     return _render_light(bvh, scene, width, height, camera, frame_seed, light_samples, max_path_length, accum, 2)
+
+
+def render_pm(bvh, scene: dict, width: int, height: int, camera: np.ndarray, frame_seed: int,
+              light_samples: np.ndarray, max_path_length: int = 8, accum: np.ndarray | None = None,
+              photons_per_light_sample: int = 2048, query_radius: float = 0.01) -> np.ndarray:
+    """One iteration of PhotonMapper::Draw with the reference's
+    photondistribution.comp and gather.comp (lossless hash map,
+    maps/hashmap.glsl), invocations in order on one thread."""
+    return render_lt(bvh, scene, width, height, camera, frame_seed, light_samples, max_path_length, accum, 3,
+                     rays_per_light_sample=photons_per_light_sample, param=query_radius)
+
+
+def render_im(bvh, scene: dict, width: int, height: int, camera: np.ndarray, frame_seed: int,
+              light_samples: np.ndarray, accum: np.ndarray, position: np.ndarray, max_path_length: int = 8,
+              photons_per_light_sample: int = 2048, query_radius: float = 0.005) -> np.ndarray:
+    """One iteration of PixelMapLighttracer::Draw with the reference's
+    importondistribution.comp and photontracing.comp (DEPTH_BUFFER_OCCLUSION_TEST,
+    lossless hash map), invocations in order on one thread. accum (H, W, 4)
+    holds the reference's image (alpha: the first hit's packed normal x),
+    position (H, W, 4) its position texture; both carry over iterations."""
+    assert position.dtype == np.float32 and position.shape == (height, width, 4) and position.flags.c_contiguous
+    return render_lt(bvh, scene, width, height, camera, frame_seed, light_samples, max_path_length, accum, 4,
+                     rays_per_light_sample=photons_per_light_sample, param=query_radius, position=position)
 

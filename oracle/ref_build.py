@@ -7,8 +7,10 @@ it mechanically and compiles it on the CPU against oracle/ref_shim.hpp (the
 GLSL built-ins). The library it builds, oracle/_ref/libgpugi_ref.so, is the
 reference's own code for the path (traversal, the random and helper
 functions, pathtracer.comp, lighttracer.comp with and without
-SAVE_LIGHT_CACHE, showlightcaches.comp, pathtracer_bidir.comp and
-whittedraytracer.comp);
+SAVE_LIGHT_CACHE, showlightcaches.comp, pathtracer_bidir.comp,
+whittedraytracer.comp, the photon mapper's photondistribution.comp and
+gather.comp, and the importon map light tracer's importondistribution.comp
+and photontracing.comp, both with the lossless hash map);
 tests/test_ref_pinned.py checks the oracle's restatement (oracle/*.cpp)
 against it bit for bit.
 
@@ -57,7 +59,9 @@ DEFAULT_REFERENCE = Path(os.environ.get("GPUGI_REFERENCE", "/root/reference")) /
 FILES = ["helper.glsl", "scenedata.glsl", "intersectiontests.glsl", "random.glsl", "traceray.glsl",
          "globaluniforms.glsl", "materials.glsl", "lightsource.glsl", "stdheader.glsl", "pathtracer.comp",
          "lighttracer.comp", "screenreproject.glsl", "showlightcaches.comp", "bidirpathtracer/lightcache.glsl",
-         "bidirpathtracer/pathtracer_bidir.comp", "whittedraytracer.comp"]
+         "bidirpathtracer/pathtracer_bidir.comp", "whittedraytracer.comp", "photonmapper/photondistribution.comp",
+         "photonmapper/gather.comp", "photonmapper/photonmap.glsl", "maps/hashmap.glsl", "maps/grid.glsl",
+         "pixelmaplt/importondistribution.comp", "pixelmaplt/photontracing.comp", "pixelmaplt/importonmap.glsl"]
 OVERRIDABLE = {"TRIANGLES_PER_LEAF"}
 
 _CTOR = re.compile(r"\b((?:i|u|b)?vec[234])\s*\(")

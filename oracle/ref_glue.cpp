@@ -188,6 +188,94 @@ int g_maxPathLength = 8;
 #undef NUM_LIGHT_SAMPLES
 #undef LOCAL_SIZE
 
+// ------------------------------------------------ PhotonMapper's shaders (lossless hash map)
+namespace ref_pmd {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define main PhotonDistributionMain
+#include "photonmapper/photondistribution.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_pmd
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+namespace ref_pmg {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define main PhotonGatherMain
+#include "photonmapper/gather.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_pmg
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+// ------------------------------------------------ PixelMapLighttracer's shaders (pixelmaplighttracer.cpp:128-142)
+namespace ref_imd {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define DEPTH_BUFFER_OCCLUSION_TEST
+#define main ImportonDistributionMain
+#include "pixelmaplt/importondistribution.comp.h"
+#undef main
+#undef DEPTH_BUFFER_OCCLUSION_TEST
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_imd
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+namespace ref_imp {
+using namespace glslref;
+int g_maxPathLength = 8;
+#define MAX_PATHLENGTH g_maxPathLength
+#define TRIANGLES_PER_LEAF 8
+#define DEPTH_BUFFER_OCCLUSION_TEST
+#define main ImportonPhotonMain
+#include "pixelmaplt/photontracing.comp.h"
+#undef main
+#undef DEPTH_BUFFER_OCCLUSION_TEST
+#undef REPROJECT
+#undef USE_PIXEL_CACHE
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+}  // namespace ref_imp
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
 namespace {
 
 template <typename F>
@@ -444,7 +532,7 @@ int ref_render_pt(const float* hierarchy, const int32_t* slots, const float* pos
 int ref_render_lt(const float* hierarchy, const int32_t* slots, const float* positions, const float* vertexInfo,
                   const float* materials, int numMaterials, int width, int height, int maxPathLength,
                   const float* cam, uint32_t frameSeed, const float* lightSamples, int numLightSamples,
-                  int raysPerLightSample, int bidir, float* accum) {
+                  int raysPerLightSample, int bidir, float param, float* accum, float* position) {
     using namespace glslref;
     if (numMaterials > 256) return 1;
     std::vector<vec4> colours(4 * (size_t)numMaterials);
@@ -468,6 +556,10 @@ int ref_render_lt(const float* hierarchy, const int32_t* slots, const float* pos
         bind(ref_bpl::Materials[m], m, r);
         bind(ref_bpe::Materials[m], m, r);
         bind(ref_wh::Materials[m], m, r);
+        bind(ref_pmd::Materials[m], m, r);
+        bind(ref_pmg::Materials[m], m, r);
+        bind(ref_imd::Materials[m], m, r);
+        bind(ref_imp::Materials[m], m, r);
     }
     g_textureColours = colours.data();
 #define GPUGI_REF_SCENE(NS)                                                           \
@@ -485,16 +577,96 @@ int ref_render_lt(const float* hierarchy, const int32_t* slots, const float* pos
     NS::PixelArea = cam[12];                                                          \
     NS::FrameSeed = frameSeed;                                                        \
     NS::IterationCount = 0;                                                           \
-    NS::OutputTexture = image2D{reinterpret_cast<vec4*>(accum), width, height};       \
     NS::g_maxPathLength = maxPathLength;
     GPUGI_REF_SCENE(ref_lt)
     GPUGI_REF_SCENE(ref_slc)
     GPUGI_REF_SCENE(ref_bpl)
     GPUGI_REF_SCENE(ref_bpe)
     GPUGI_REF_SCENE(ref_wh)
+    GPUGI_REF_SCENE(ref_pmd)
+    GPUGI_REF_SCENE(ref_pmg)
+    GPUGI_REF_SCENE(ref_imd)
+    GPUGI_REF_SCENE(ref_imp)
 #undef GPUGI_REF_SCENE
+    for (image2D* im : {&ref_lt::OutputTexture, &ref_slc::OutputTexture, &ref_bpl::OutputTexture,
+                        &ref_bpe::OutputTexture, &ref_wh::OutputTexture, &ref_pmg::OutputTexture,
+                        &ref_imd::OutputTexture, &ref_imp::OutputTexture})
+        *im = image2D{reinterpret_cast<vec4*>(accum), width, height};
     const uint64_t n = (uint64_t)numLightSamples * raysPerLightSample;
-    if (bidir == 2) {  // WhittedRayTracer::Draw: whittedraytracer.comp per pixel
+    if (bidir == 4) {
+        // PixelMapLighttracer::Draw (pixelmaplighttracer.cpp:76-125): the map
+        // cleared, importondistribution.comp per pixel (importons at index
+        // 2 x pixel; the first hit's position and packed normal y into the
+        // position texture, its packed normal x into the image's alpha),
+        // then photontracing.comp over numLightSamples x photonsPerLightSample
+        // invocations; param = the query radius. position: the position
+        // texture (H x W x 4), carried between iterations like the image.
+        const float radius = param;
+        uint32_t size = (uint32_t)std::max<uint64_t>(1031, 4 * (uint64_t)width * height + 1);
+        auto prime = [](uint32_t v) {
+            if (v < 2) return false;
+            for (uint32_t d = 2; (uint64_t)d * d <= v; ++d)
+                if (v % d == 0) return false;
+            return true;
+        };
+        while (!prime(size)) ++size;
+        std::vector<uvec2> map(size, uvec2(0xffffffffu, 0xffffffffu));
+        std::vector<ivec4> data(2 * (size_t)width * height + 2);
+        ref_imd::HashMap = ref_imp::HashMap = map.data();
+        ref_imd::HashMapData = ref_imp::HashMapData = data.data();
+        ref_imd::HashMapSize = ref_imp::HashMapSize = size;
+        ref_imd::NumPhotonsPerLightSample = ref_imp::NumPhotonsPerLightSample = raysPerLightSample;
+        ref_imd::HashGridSpacing = ref_imp::HashGridSpacing = radius * 2.01f;
+        ref_imd::PhotonQueryRadiusSq = ref_imp::PhotonQueryRadiusSq = radius * radius;
+        ref_imd::PositionTexture = ref_imp::PositionTexture =
+            image2D{reinterpret_cast<vec4*>(position), width, height};
+        for (int y = 0; y < height; ++y)
+            for (int x = 0; x < width; ++x) {
+                gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
+                ref_imd::ImportonDistributionMain();
+            }
+        for (uint64_t i = 0; i < n; ++i) {
+            gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+            ref_imp::ImportonPhotonMain();
+        }
+    } else if (bidir == 3) {
+        // PhotonMapper::Draw (photonmapper.cpp:69-112): the hash map cleared to
+        // all ones and its data to zero, photondistribution.comp over
+        // numLightSamples x photonsPerLightSample (raysPerLightSample)
+        // invocations, then gather.comp per pixel; param = the query radius
+        // r (HashGridSpacing = 2.01 r, PhotonQueryRadiusSq = r^2). The
+        // map's size is a prime above four entries per possible photon
+        // (the reference sizes it from its own photon estimate), so probing
+        // never fills it; the data holds two texels per photon.
+        const float radius = param;
+        const uint64_t maxPhotons = n * (uint64_t)maxPathLength;
+        uint32_t size = (uint32_t)std::max<uint64_t>(1031, 4 * maxPhotons + 1);
+        auto prime = [](uint32_t v) {
+            if (v < 2) return false;
+            for (uint32_t d = 2; (uint64_t)d * d <= v; ++d)
+                if (v % d == 0) return false;
+            return true;
+        };
+        while (!prime(size)) ++size;
+        std::vector<uvec2> map(size, uvec2(0xffffffffu, 0xffffffffu));
+        std::vector<ivec4> data(2 * maxPhotons + 2);
+        ref_pmd::HashMap = ref_pmg::HashMap = map.data();
+        ref_pmd::HashMapData = ref_pmg::HashMapData = data.data();
+        ref_pmd::HashMapCounter = ref_pmg::HashMapCounter = 0;
+        for (auto* u : {&ref_pmd::HashMapSize, &ref_pmg::HashMapSize}) *u = size;
+        ref_pmd::NumPhotonsPerLightSample = ref_pmg::NumPhotonsPerLightSample = raysPerLightSample;
+        ref_pmd::HashGridSpacing = ref_pmg::HashGridSpacing = radius * 2.01f;
+        ref_pmd::PhotonQueryRadiusSq = ref_pmg::PhotonQueryRadiusSq = radius * radius;
+        for (uint64_t i = 0; i < n; ++i) {
+            gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+            ref_pmd::PhotonDistributionMain();
+        }
+        for (int y = 0; y < height; ++y)
+            for (int x = 0; x < width; ++x) {
+                gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
+                ref_pmg::PhotonGatherMain();
+            }
+    } else if (bidir == 2) {  // WhittedRayTracer::Draw: whittedraytracer.comp per pixel
         for (int y = 0; y < height; ++y)
             for (int x = 0; x < width; ++x) {
                 gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);

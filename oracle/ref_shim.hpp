@@ -64,6 +64,15 @@ struct vec3 {
     GR_SW2(vec2, y, z) GR_SW2(vec2, z, x) GR_SW2(vec2, z, y) GR_SW2(vec2, z, z)
     GR_SW3(vec3, x, y, z) GR_SW3(vec3, z, y, x)
 };
+// `v.xyz` of a vec4 as an lvalue (`color.xyz += c`, importondistribution.comp,
+// screenreproject.glsl): reads as a vec3, assigns component by component.
+struct VecSwizzle3 {
+    float *a, *b, *c;
+    inline operator vec3() const;
+    inline VecSwizzle3& operator=(const vec3& v);
+    inline VecSwizzle3& operator+=(const vec3& v);
+    inline VecSwizzle3& operator-=(const vec3& v);
+};
 struct vec4 {
     union { float x, r; };
     union { float y, g; };
@@ -79,8 +88,22 @@ struct vec4 {
     GR_SW2(vec2, x, y) GR_SW2(vec2, z, w) GR_SW2(vec2, x, z) GR_SW2(vec2, y, z) GR_SW2(vec2, y, w)
     GR_SW2(vec2, x, w)
     GR_SW3(vec3, x, y, z) GR_SW3(vec3, y, z, w)
+    VecSwizzle3 xyz() { return VecSwizzle3{&x, &y, &z}; }
     vec3 rgb() const { return vec3(x, y, z); }
 };
+inline VecSwizzle3::operator vec3() const { return vec3(*a, *b, *c); }
+inline VecSwizzle3& VecSwizzle3::operator=(const vec3& v) {
+    *a = v.x, *b = v.y, *c = v.z;
+    return *this;
+}
+inline VecSwizzle3& VecSwizzle3::operator+=(const vec3& v) {
+    *a += v.x, *b += v.y, *c += v.z;
+    return *this;
+}
+inline VecSwizzle3& VecSwizzle3::operator-=(const vec3& v) {
+    *a -= v.x, *b -= v.y, *c -= v.z;
+    return *this;
+}
 struct ivec2 {
     int32_t x, y;
     ivec2() : x(0), y(0) {}
@@ -104,11 +127,33 @@ struct ivec3 {
     int32_t x, y, z;
     ivec3() : x(0), y(0), z(0) {}
     ivec3(int32_t a, int32_t b, int32_t c) : x(a), y(b), z(c) {}
+    ivec3(const ivec2& a, int32_t c) : x(a.x), y(a.y), z(c) {}
+    explicit ivec3(const vec3& v) : x((int32_t)v.x), y((int32_t)v.y), z((int32_t)v.z) {}
+};
+inline ivec3 operator+(ivec3 a, ivec3 b) { return ivec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+// A three-component swizzle of an ivec4 that can be read or assigned
+// (`HashMapData[i].yzw = v`, photonmapper/photondistribution.comp).
+struct ivec4;
+struct IvecSwizzle3 {
+    int32_t *a, *b, *c;
+    operator ivec3() const { return ivec3(*a, *b, *c); }
+    IvecSwizzle3& operator=(const ivec3& v) {
+        *a = v.x;
+        *b = v.y;
+        *c = v.z;
+        return *this;
+    }
 };
 struct ivec4 {
     int32_t x, y, z, w;
     ivec4() : x(0), y(0), z(0), w(0) {}
     ivec4(int32_t a, int32_t b, int32_t c, int32_t d) : x(a), y(b), z(c), w(d) {}
+    ivec4(const ivec3& v, int32_t d) : x(v.x), y(v.y), z(v.z), w(d) {}
+    IvecSwizzle3 xyz() { return IvecSwizzle3{&x, &y, &z}; }
+    IvecSwizzle3 yzw() { return IvecSwizzle3{&y, &z, &w}; }
+    ivec3 xyz() const { return ivec3(x, y, z); }
+    ivec3 yzw() const { return ivec3(y, z, w); }
+    ivec2 yz() const { return ivec2(y, z); }
 };
 struct bvec3 {
     bool x, y, z;
@@ -151,6 +196,7 @@ inline bool operator==(vec3 a, vec3 b) { return a.x == b.x && a.y == b.y && a.z 
 inline bool operator!=(vec3 a, vec3 b) { return !(a == b); }
 inline ivec2 operator+(ivec2 a, ivec2 b) { return ivec2(a.x + b.x, a.y + b.y); }
 inline ivec2 operator-(ivec2 a, ivec2 b) { return ivec2(a.x - b.x, a.y - b.y); }
+inline ivec2 operator*(ivec2 a, ivec2 b) { return ivec2(a.x * b.x, a.y * b.y); }
 
 // ---------------------------------------------------------------- built-ins
 inline float min(float a, float b) { return std::fmin(a, b); }
@@ -224,6 +270,12 @@ inline uint floatBitsToUint(float f) { uint u; std::memcpy(&u, &f, 4); return u;
 inline int floatBitsToInt(float f) { int u; std::memcpy(&u, &f, 4); return u; }
 inline float uintBitsToFloat(uint u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline float intBitsToFloat(int u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline ivec3 floatBitsToInt(vec3 v) { return ivec3(floatBitsToInt(v.x), floatBitsToInt(v.y), floatBitsToInt(v.z)); }
+inline vec3 intBitsToFloat(ivec3 v) { return vec3(intBitsToFloat(v.x), intBitsToFloat(v.y), intBitsToFloat(v.z)); }
+inline ivec2 floatBitsToInt(vec2 v) { return ivec2(floatBitsToInt(v.x), floatBitsToInt(v.y)); }
+inline vec2 intBitsToFloat(ivec2 v) { return vec2(intBitsToFloat(v.x), intBitsToFloat(v.y)); }
+inline vec3 ceil(vec3 v) { return vec3(ceil(v.x), ceil(v.y), ceil(v.z)); }
+inline vec3 round(vec3 v) { return vec3(round(v.x), round(v.y), round(v.z)); }
 // packSnorm2x16: round(clamp(c, -1, +1) * 32767.0), x in the low 16 bits
 inline uint packSnorm2x16(vec2 v) {
     auto c = [](float f) { return (uint)(uint16_t)(int16_t)round(clamp(f, -1.0f, 1.0f) * 32767.0f); };
@@ -302,6 +354,13 @@ inline float imageAtomicAdd(image2D& im, ivec2 p, float v) {
 // atomicAdd on a storage-buffer integer (the light cache's entry counter,
 // lightcache.glsl:27-35): returns the old value.
 inline int atomicAdd(int& x, int v) { return __atomic_fetch_add(&x, v, __ATOMIC_RELAXED); }
+inline uint atomicAdd(uint& x, uint v) { return __atomic_fetch_add(&x, v, __ATOMIC_RELAXED); }
+// the hash map's cell keys and list heads (maps/hashmap.glsl): return the old value
+inline uint atomicCompSwap(uint& x, uint compare, uint data) {
+    __atomic_compare_exchange_n(&x, &compare, data, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
+    return compare;
+}
+inline uint atomicExchange(uint& x, uint data) { return __atomic_exchange_n(&x, data, __ATOMIC_RELAXED); }
 // The lock image of the reference's commented-out spin lock (declared, unused).
 struct uimage2D {
     uint32_t* texels = nullptr;

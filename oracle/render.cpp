@@ -662,8 +662,10 @@ static vec3 GatherPixel(const RenderScene& s, const Params& P, const PhotonGrid&
             for (int c = 0; c < 8; ++c) {
                 auto it = grid.cells.find(CellKey{bx + (c & 1), by + ((c >> 1) & 1), bz + ((c >> 2) & 1)});
                 if (it == grid.cells.end()) continue;
-                for (uint32_t k : it->second)
-                    irradiance += IrradianceEstimate(grid.photons[k], ray, m, hitNormal, grid.radiusSq);
+                // the cell's linked list, newest photon first (insertToHashGrid
+                // prepends with atomicExchange, maps/hashmap.glsl)
+                for (auto k = it->second.rbegin(); k != it->second.rend(); ++k)
+                    irradiance += IrradianceEstimate(grid.photons[*k], ray, m, hitNormal, grid.radiusSq);
             }
             color += irradiance * pathThroughput;
             break;
@@ -867,8 +869,9 @@ static void ImportonPhotonThread(const RenderScene& s, const Params& P, Image& i
         for (int c = 0; c < 8; ++c) {
             auto it = grid.cells.find(CellKey{bx + (c & 1), by + ((c >> 1) & 1), bz + ((c >> 2) & 1)});
             if (it == grid.cells.end()) continue;
-            for (uint32_t k : it->second) {  // radianceEstimate (photontracing.comp:15-36)
-                const Importon& im = grid.importons[k];
+            // radianceEstimate (photontracing.comp:15-36) over the cell's list, newest first
+            for (auto kk = it->second.rbegin(); kk != it->second.rend(); ++kk) {
+                const Importon& im = grid.importons[*kk];
                 vec3 toImporton = im.pos - ray.Origin;
                 vec3 incidentDirection = UnpackNormal32(im.dir);
                 if (dot(toImporton, toImporton) <= grid.radiusSq && abs(dot(toImporton, shadingNormal)) < 0.01f &&

@@ -182,3 +182,61 @@ def test_light_and_bidirectional_images(room, depth, pass_):
         assert np.array_equal(acc_r.view(np.uint32), acc_o.view(np.uint32)), (it, np.abs(acc_r - acc_o).max())
     assert acc_r[..., :3].mean() > 0
 
+
+@pytest.mark.parametrize("room,depth", [("diffuse", 6), ("glossy", 8)])
+def test_whitted_images(room, depth):
+    """whittedraytracer.comp (the reference's text, with the
+    STOP_ON_DIFFUSE_BOUNCE define its renderer adds) against the oracle's
+    Whitted restatement: identical images, iteration by iteration."""
+    sc = scenes.cornell_room(seed=1, sphere_level=3, wall_grid=8) if room == "diffuse" else _glossy_room()
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    W, H = 40, 32
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H).as_array()
+    acc_r = acc_o = None
+    st = [5]
+    for it in range(2):
+        ls = oracle.light_samples(sc["positions"], b.slots, sc["materials"], 128, st)
+        fs = render.frame_seed(it, "reference")
+        acc_r = ref.render_whitted(b, sc, W, H, cam, fs, ls, max_path_length=depth, accum=acc_r)
+        acc_o = oracle.render(b, sc, "WHITTED", W, H, cam, fs, ls, max_path_length=depth, accum=acc_o,
+                              rng="reference", num_threads=1)
+        assert np.array_equal(acc_r.view(np.uint32), acc_o.view(np.uint32)), (it, np.abs(acc_r - acc_o).max())
+    assert acc_r[..., :3].mean() > 0
+
+
+@pytest.mark.parametrize("room", ["diffuse", "glossy"])
+def test_photon_map_and_importon_map_images(room):
+    """The photon mapper's and the importon map light tracer's shaders (the
+    reference's text) against the oracle's PM and IM restatements: identical
+    images, iteration by iteration (the importon map carries its position
+    texture and the image's alpha, the first hit's packed normal x, between
+    iterations; the oracle carries its G-buffer)."""
+    sc = scenes.cornell_room(seed=1, sphere_level=3, wall_grid=8) if room == "diffuse" else _glossy_room()
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    W, H = 40, 32
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H).as_array()
+    st = [7]
+    acc_r = acc_o = None
+    for it in range(2):
+        ls = oracle.light_samples(sc["positions"], b.slots, sc["materials"], 32, st)
+        fs = render.frame_seed(it, "reference")
+        acc_r = ref.render_pm(b, sc, W, H, cam, fs, ls, max_path_length=6, accum=acc_r, photons_per_light_sample=256,
+                              query_radius=0.05)
+        acc_o = oracle.render(b, sc, "PM", W, H, cam, fs, ls, max_path_length=6, accum=acc_o, rng="reference",
+                              num_threads=1, photons_per_light_sample=256, query_radius=0.05)
+        assert np.array_equal(acc_r.view(np.uint32), acc_o.view(np.uint32)), (it, np.abs(acc_r - acc_o).max())
+    assert acc_r[..., :3].mean() > 0
+    st = [9]
+    acc_r, pos_r = np.zeros((H, W, 4), np.float32), np.zeros((H, W, 4), np.float32)
+    acc_o, gbuf = None, np.zeros((H, W, 5), np.float32)
+    for it in range(3):
+        ls = oracle.light_samples(sc["positions"], b.slots, sc["materials"], 32, st)
+        fs = render.frame_seed(it, "reference")
+        ref.render_im(b, sc, W, H, cam, fs, ls, acc_r, pos_r, max_path_length=6, photons_per_light_sample=256,
+                      query_radius=0.03)
+        acc_o = oracle.render(b, sc, "IM", W, H, cam, fs, ls, max_path_length=6, accum=acc_o, rng="reference",
+                              num_threads=1, photons_per_light_sample=256, query_radius=0.03, gbuffer=gbuf)
+        assert np.array_equal(acc_r[..., :3].view(np.uint32), acc_o[..., :3].view(np.uint32)), \
+            (it, np.abs(acc_r[..., :3] - acc_o[..., :3]).max())
+    assert acc_r[..., :3].mean() > 0
+
