@@ -1064,6 +1064,48 @@ def nrc_headline(args):
         st.close()
 
 
+def run_nrc_frames(args):
+    """Cache frames alone on the heightfield workload (1280 x 720, 1 spp per
+    frame, the cache settings of the `nrc` options): --warmup frames, then
+    --steps frames in one call, beside plain PT of --steps spp in one call
+    and in 1-spp calls; ms per frame / spp, host clock around synchronised
+    calls. For launch lists and per-frame costs."""
+    from gpugi_gb300 import nrc, render
+    st = NrcSetup("PT", 1280, 720, 1, args.nrc_rr, args.nrc_unbiased, args.nrc_lanes)
+    tf = min(0.05, 1.5 * 65536 / (3.0 * 1280 * 720))
+    cache = nrc.RadianceCache(st.ctx, *st.box, seed=5)
+    img = render.Image(st.ctx, 1280, 720, fp64=True)
+    opts = dict(max_path_length=st.depth, sky=st.sky, terminate_depth=args.nrc_td, train_fraction=tf,
+                train_steps=args.nrc_train_steps, samples_per_frame=1, train_length=args.nrc_train_length,
+                terminate_spread=args.nrc_spread, unbiased_fraction=args.nrc_unbiased, lanes=args.nrc_lanes)
+    nrc.render_nrc(st.ctx, st.ds, st.cam, img, cache, samples=max(args.warmup, 1), iteration=0, rng_state=[1],
+                   **opts)
+    t_frames = st.timed(lambda: nrc.render_nrc(st.ctx, st.ds, st.cam, img, cache, samples=args.steps,
+                                               iteration=1000, rng_state=[2], **opts))
+    pt = render.Image(st.ctx, 1280, 720, fp64=True)
+    render.render(st.ctx, st.ds, st.cam, pt, "PT", max_path_length=st.depth, samples=max(args.warmup, 1),
+                  iteration=0, rng_state=[3], sky=st.sky)
+    t_pt = st.timed(lambda: render.render(st.ctx, st.ds, st.cam, pt, "PT", max_path_length=st.depth,
+                                          samples=args.steps, iteration=100, rng_state=[4], sky=st.sky))
+
+    def single():
+        for k in range(args.steps):
+            render.render(st.ctx, st.ds, st.cam, pt, "PT", max_path_length=st.depth, samples=1,
+                          iteration=10000 + k, rng_state=[5 + k], sky=st.sky)
+    t_pt1 = st.timed(single)
+    print(json.dumps({"metric": "ms per 1-spp cache frame and per plain PT sample, heightfield 1280 x 720",
+                      "nrc_ms_per_frame": round(t_frames / args.steps * 1e3, 4),
+                      "pt_ms_per_spp_one_call": round(t_pt / args.steps * 1e3, 4),
+                      "pt_ms_per_spp_one_spp_calls": round(t_pt1 / args.steps * 1e3, 4),
+                      "frames": args.steps, "warmup": args.warmup,
+                      "nrc": {"terminate_depth": args.nrc_td, "train_steps": args.nrc_train_steps,
+                              "train_length": args.nrc_train_length, "lanes": args.nrc_lanes},
+                      "data": "synthetic"}), flush=True)
+    for x in (img, pt, cache):
+        x.close()
+    st.close()
+
+
 def run_nrc(args):
     """Time to equal RMSE, rendering with the radiance cache vs the plain
     renderer of the same pass (NrcSetup): the plain pass accumulates 1024
@@ -1136,11 +1178,11 @@ def main():
                     help="parts of a host-pointer query whose copies and traversal overlap")
     ap.add_argument("--zero-copy", action="store_true",
                     help="kernels read and write the page-locked host arrays directly instead of staging")
-    ap.add_argument("--workload", choices=["trace", "nrc", "passes", "batch", "large", "build", "mlp"], default="trace",
+    ap.add_argument("--workload", choices=["trace", "nrc", "passes", "batch", "large", "build", "mlp", "nrc-frames"], default="trace",
                     help="trace: the closest-hit headline; nrc: time-to-equal-RMSE of the radiance cache; "
                          "passes: samples/s and Mrays/s of PT, LT and BPT; batch: batched vs per-job rendering; "
                          "large: the 7.9M-triangle workload; build: GPU vs host hierarchy build; "
-                         "mlp: the radiance-cache MLP kernels alone")
+                         "mlp: the radiance-cache MLP kernels alone; nrc-frames: 1-spp cache frames alone")
     ap.add_argument("--nrc-pass", choices=["PT", "BPT"], default="PT",
                     help="PT: heightfield workload; BPT: large workload (eye paths stop at the cache vertex)")
     ap.add_argument("--nrc-size", type=int, nargs=2, default=None, help="default 640 360 (PT), 480 270 (BPT)")
@@ -1169,7 +1211,7 @@ def main():
         from __graft_entry__ import build
         build()
         {"nrc": run_nrc, "passes": run_passes, "batch": run_batch, "large": run_large,
-         "build": run_build, "mlp": run_mlp}[args.workload](args)
+         "build": run_build, "mlp": run_mlp, "nrc-frames": run_nrc_frames}[args.workload](args)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -198,3 +198,43 @@ def test_self_training_keeps_the_cache_unbiased(cuda_ctx, room, train_length, un
     assert cuda_ctx.device_error_bits() == 0
     for x in (conv, warm, img, cache):
         x.close()
+
+
+def test_cache_bias_stays_below_the_plain_1024_spp_rmse(cuda_ctx, room):
+    """The cached image's bias against converged PT (the cache trained, then
+    frozen) stays below the RMSE of 1024 spp of plain PT on the same view:
+    two independent 256-spp cache images A and B give
+    bias^2 = MSE(A) - MSE(A - B) / 2 (the variance of one image is half the
+    expected squared difference of two), the reference's own noise
+    (16,384 spp) being negligible beside both."""
+    sc, b, ds = room
+    W = H = 64
+    depth = 8
+    cam = render.camera_lookat((0.0, 1.2, 2.0), (0.0, 0.0, -0.3), (0.0, 1.0, 0.0), 40.0, W, H)
+    conv = render.Image(cuda_ctx, W, H, fp64=True)
+    render.render(cuda_ctx, ds, cam, conv, "PT", max_path_length=depth, samples=16384, iteration=1 << 20,
+                  rng_state=[99])
+    reference = conv.read64() / 16384
+    pt = render.Image(cuda_ctx, W, H, fp64=True)
+    render.render(cuda_ctx, ds, cam, pt, "PT", max_path_length=depth, samples=1024, iteration=0, rng_state=[7])
+    target = np.sqrt(((pt.read64() / 1024 - reference) ** 2).sum(-1).mean())
+    cache = nrc.RadianceCache(cuda_ctx, *ROOM_BOX, seed=5)
+    opts = dict(max_path_length=depth, terminate_depth=2, train_fraction=0.25, train_steps=4, samples_per_frame=4)
+    warm = render.Image(cuda_ctx, W, H)
+    nrc.render_nrc(cuda_ctx, ds, cam, warm, cache, samples=1200, iteration=10000, rng_state=[11], **opts)
+    spp = 256
+    imgs = []
+    for k in range(2):
+        img = render.Image(cuda_ctx, W, H, fp64=True)
+        nrc.render_nrc(cuda_ctx, ds, cam, img, cache, samples=spp, iteration=20000 + 10000 * k, rng_state=[13 + k],
+                       train=False, **dict(opts, train_fraction=0.0))
+        imgs.append(img.read64() / spp)
+        img.close()
+    a, bb = imgs
+    mse_a = ((a - reference) ** 2).sum(-1).mean()
+    var_a = ((a - bb) ** 2).sum(-1).mean() / 2
+    bias = np.sqrt(max(mse_a - var_a, 0.0))
+    assert bias < target, (bias, target, np.sqrt(mse_a))
+    assert cuda_ctx.device_error_bits() == 0
+    for x in (conv, pt, warm, cache):
+        x.close()
