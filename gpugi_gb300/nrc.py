@@ -173,3 +173,32 @@ def render_nrc(ctx: cuda.Context, scene: cuda.DeviceScene, camera, image, cache:
                                  C.byref(st) if ls is None else None, cache.handle, C.byref(q), image.handle))
     if rng_state is not None and ls is None:
         rng_state[0] = st.value
+
+
+def smoke_check(ctx: cuda.Context) -> None:
+    """The cache's tcgen05 kernels on a small batch (used by smoke()): the
+    training step's loss and gradient agree with the mma.sync kernels, and
+    inference is finite."""
+    import torch
+    rng = np.random.default_rng(1)
+    n = 2000
+    q = np.concatenate([rng.uniform(-1, 1, (n, 3)), rng.normal(size=(n, 3)), rng.normal(size=(n, 3)),
+                        rng.uniform(0.1, 0.9, (n, 3))], 1).astype(np.float32)
+    q[:, 3:6] /= np.linalg.norm(q[:, 3:6], axis=1, keepdims=True)
+    q[:, 6:9] /= np.linalg.norm(q[:, 6:9], axis=1, keepdims=True)
+    samples = torch.from_numpy(np.concatenate([q, rng.uniform(0, 1, (n, 3)).astype(np.float32)], 1)).cuda()
+    c = RadianceCache(ctx, (-1, -1, -1), (1, 1, 1), seed=3)
+    try:
+        out = {}
+        for k in ("mma_sync", "tcgen05"):
+            c.set_kernels(k)
+            out[k] = c.gradient(samples)
+        (_, g0, l0), (_, g1, l1) = out["mma_sync"], out["tcgen05"]
+        assert abs(l1 / l0 - 1) < 1e-2, (l0, l1)
+        assert np.linalg.norm(g1 - g0) <= 2e-2 * np.linalg.norm(g0), "tcgen05 gradient differs"
+        c.train(samples)
+        r = c.infer(samples[:, :12].contiguous()).cpu().numpy()
+        assert np.isfinite(r).all() and ctx.device_error_bits() == 0
+    finally:
+        c.close()
+
