@@ -31,6 +31,12 @@
 #include "shade.cuh"
 #include "trace.cuh"
 
+// The passes' walkers walk a queue with 8-lane groups while it holds fewer
+// rays than this many times the resident lanes, and a ray per lane otherwise.
+#ifndef GPUGI_GROUP_BELOW_LANES
+#define GPUGI_GROUP_BELOW_LANES 2u
+#endif
+
 namespace gpugi {
 
 constexpr int kMaxDepth = 64;
@@ -2065,8 +2071,8 @@ static gpugi_status walkers_config(gpugi_ctx* ctx, const gpugi_scene* sc, Walker
     // workload: 0.5x, 2x, 8x, 64x the lanes gave PT 262 / 264.5 / 250 / 167 M
     // samples/s and the photon mapper 124 / 133 / 133 / 133)
     const bool group = ctx->traceMode >= 3;
-    W.groupBelowE = group ? W.LE.grid * 128u * 2u : 0u;
-    W.groupBelowS = group ? W.LS.grid * 128u * 2u : 0u;
+    W.groupBelowE = group ? W.LE.grid * 128u * GPUGI_GROUP_BELOW_LANES : 0u;
+    W.groupBelowS = group ? W.LS.grid * 128u * GPUGI_GROUP_BELOW_LANES : 0u;
     return st;
 }
 
