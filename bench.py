@@ -1201,7 +1201,7 @@ def main():
     ap.add_argument("--nrc-td", type=int, default=3, help="path vertex where render paths query the cache")
     ap.add_argument("--nrc-unbiased", type=float, default=1.0 / 16,
                     help="self-training: share of training paths that run to their end")
-    ap.add_argument("--nrc-lanes", type=int, default=3, help="cache frames in flight (wavefront lanes)")
+    ap.add_argument("--nrc-lanes", type=int, default=4, help="cache frames in flight (wavefront lanes)")
     ap.add_argument("--nrc-budget", type=int, default=0,
                     help="cache renderer at this many spp against the plain pass at equal RMSE (0: time to the "
                          "plain 1024-spp RMSE)")

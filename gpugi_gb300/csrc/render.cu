@@ -2636,13 +2636,13 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
     const size_t queryCap = (size_t)framePaths + (np->trainLength ? trainCap : 0);
     if ((st = ensure_nrc_buffers(ctx, rb, queryCap, trainCap, p->maxPathLength, sampleCap))) return st;
 
-    // Frames alternate over `lanes` lanes (buffer sets and streams; 3 by
+    // Frames alternate over `lanes` lanes (buffer sets and streams; 4 by
     // default): a frame's wavefront tail overlaps the next frames' bulk. The
     // network's inference and training stay in frame order (events), so
     // every frame sees the weights trained by the previous one.
     const uint32_t nFrames = (p->samples + spf - 1) / spf;
     const int nLanes = (int)std::max<uint32_t>(
-        1u, std::min<uint32_t>(np->lanes ? std::min<uint32_t>(np->lanes, RenderBuffers::kMaxLanes) : 3u, nFrames));
+        1u, std::min<uint32_t>(np->lanes ? std::min<uint32_t>(np->lanes, RenderBuffers::kMaxLanes) : 4u, nFrames));
     RenderBuffers* lanes[RenderBuffers::kMaxLanes] = {rb, rb, rb, rb};
     cudaStream_t streams[RenderBuffers::kMaxLanes] = {ctx->stream, ctx->stream, ctx->stream, ctx->stream};
     if (nLanes > 1 && !rb->evSync[0])

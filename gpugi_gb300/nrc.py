@@ -149,7 +149,7 @@ def render_nrc(ctx: cuda.Context, scene: cuda.DeviceScene, camera, image, cache:
                rng_state: list | None = None, terminate_depth: int = 1, train_fraction: float = 0.03,
                max_train_samples: int = 65536, train_steps: int = 1, train: bool = True,
                samples_per_frame: int = 1, pass_: str = "PT", rng: str = "pcg", train_length: int = 0,
-               unbiased_fraction: float = 1.0 / 16.0, terminate_spread: float = 0.0, lanes: int = 3) -> None:
+               unbiased_fraction: float = 1.0 / 16.0, terminate_spread: float = 0.0, lanes: int = 4) -> None:
     """`samples` iterations of path tracing (pass_ "PT") or bidirectional
     path tracing ("BPT") with the radiance cache (gpugi_render_nrc); rng
     selects the random streams as in render.render. train_length >= 1

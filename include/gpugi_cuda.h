@@ -521,7 +521,7 @@ typedef struct gpugi_nrc_params {
      * terminateDepth at the latest. 0: at vertex terminateDepth. */
     float terminateSpread;
     /* Frames in flight: frames alternate over this many wavefront lanes
-     * (buffer sets and streams; 0 = 3, at most 4), so a frame's walker tails
+     * (buffer sets and streams; 0 = 4, at most 4), so a frame's walker tails
      * overlap the next frames' bounces; the network's inference and training
      * stay in frame order. */
     uint32_t lanes;
