@@ -217,8 +217,9 @@ GPUGI_D bool trace_importance(const DevScene& s, const float2* __restrict__ imp,
                     out->nodeImportance = im.x;
                     out->nodeSizeSq = lastSizeSq;
                     out->node = (int32_t)node;
-                    const float r = X::div(__uint2float_rn(wanghash(__float_as_uint(lh)) % 8388593u), 8388593.0f);
-                    len = X::add(fh, X::mul(X::sub(lh, fh), r));
+                    // fh + ((lh - fh) * h) / 8388593, grouped as traceray.glsl:95 groups it
+                    const float h = __uint2float_rn(wanghash(__float_as_uint(lh)) % 8388593u);
+                    len = X::add(fh, X::div(X::mul(X::sub(lh, fh), h), 8388593.0f));
                     out->slot = -1;
                 }
                 node = escape;

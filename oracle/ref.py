@@ -210,3 +210,38 @@ def render_im(bvh, scene: dict, width: int, height: int, camera: np.ndarray, fra
     return render_lt(bvh, scene, width, height, camera, frame_seed, light_samples, max_path_length, accum, 4,
                      rays_per_light_sample=photons_per_light_sample, param=query_radius, position=position)
 
+
+
+def render_hier(bvh, scene: dict, width: int, height: int, camera: np.ndarray, frame_seed: int,
+                light_samples: np.ndarray, importance: np.ndarray, materials: np.ndarray, sggx: np.ndarray,
+                sky=(0.0, 0.0, 0.0), accum: np.ndarray | None = None) -> np.ndarray:
+    """One iteration of HierarchyImportance's renderer with the reference's
+    hierarchypathtracer.comp (its own MAX_PATHLENGTH 4), pixels in order on
+    one thread, accumulated into accum (H, W, 4) float32. importance: (nodes
+    + slots, 2) float32; materials: the node materials as packed halves
+    (uint32, six RGBA16F texels per node); sggx: (nodes, 6) uint16."""
+    from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
+    assert bvh.leaf_size == 8 and bvh.bounds_kind == 0, "the path tracer is built for 8-slot AABB hierarchies"
+    L = lib()
+    P, I, U64 = C.c_void_p, C.c_int, C.c_uint64
+    L.ref_render_hier.argtypes = [P] * 5 + [I, I, I, P, C.c_uint32, P, I, P, P, P, U64, P, U64, P]
+    L.ref_render_hier.restype = I
+    hier = np.ascontiguousarray(bvh.hierarchy, dtype=np.float32)
+    slots = np.ascontiguousarray(bvh.slots, dtype=np.int32)
+    pos = np.ascontiguousarray(scene["positions"], dtype=np.float32)
+    vi = np.ascontiguousarray(vertex_info(scene["normals"], scene["texcoords"]), dtype=np.float32)
+    mats = np.ascontiguousarray(scene["materials"], dtype=np.float32).reshape(-1, 24)
+    cam = np.ascontiguousarray(camera, dtype=np.float32)
+    ls = np.ascontiguousarray(light_samples, dtype=np.float32).reshape(-1, 8)
+    imp = np.ascontiguousarray(importance, dtype=np.float32)
+    hm = np.ascontiguousarray(materials, dtype=np.uint32).view(np.uint16).reshape(-1)
+    sg = np.ascontiguousarray(sggx, dtype=np.uint16).reshape(-1)
+    skya = np.asarray(sky, dtype=np.float32)
+    if accum is None:
+        accum = np.zeros((height, width, 4), np.float32)
+    assert accum.dtype == np.float32 and accum.flags.c_contiguous
+    rc = L.ref_render_hier(_p(hier), _p(slots), _p(pos), _p(vi), _p(mats), mats.shape[0], width, height, _p(cam),
+                           frame_seed & 0xFFFFFFFF, _p(ls), ls.shape[0], _p(skya), _p(imp), _p(hm), hm.size, _p(sg),
+                           sg.size, _p(accum))
+    assert rc == 0
+    return accum

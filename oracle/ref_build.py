@@ -9,8 +9,9 @@ reference's own code for the path (traversal, the random and helper
 functions, pathtracer.comp, lighttracer.comp with and without
 SAVE_LIGHT_CACHE, showlightcaches.comp, pathtracer_bidir.comp,
 whittedraytracer.comp, the photon mapper's photondistribution.comp and
-gather.comp, and the importon map light tracer's importondistribution.comp
-and photontracing.comp, both with the lossless hash map);
+gather.comp, the importon map light tracer's importondistribution.comp
+and photontracing.comp, both with the lossless hash map, and the hierarchy
+renderer's hierarchypathtracer.comp);
 tests/test_ref_pinned.py checks the oracle's restatement (oracle/*.cpp)
 against it bit for bit.
 
@@ -61,7 +62,8 @@ FILES = ["helper.glsl", "scenedata.glsl", "intersectiontests.glsl", "random.glsl
          "lighttracer.comp", "screenreproject.glsl", "showlightcaches.comp", "bidirpathtracer/lightcache.glsl",
          "bidirpathtracer/pathtracer_bidir.comp", "whittedraytracer.comp", "photonmapper/photondistribution.comp",
          "photonmapper/gather.comp", "photonmapper/photonmap.glsl", "maps/hashmap.glsl", "maps/grid.glsl",
-         "pixelmaplt/importondistribution.comp", "pixelmaplt/photontracing.comp", "pixelmaplt/importonmap.glsl"]
+         "pixelmaplt/importondistribution.comp", "pixelmaplt/photontracing.comp", "pixelmaplt/importonmap.glsl",
+         "hierarchy/hierarchypathtracer.comp", "hierarchy/sggx.glsl"]
 OVERRIDABLE = {"TRIANGLES_PER_LEAF"}
 
 _CTOR = re.compile(r"\b((?:i|u|b)?vec[234])\s*\(")

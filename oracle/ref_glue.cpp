@@ -15,6 +15,7 @@
 //                                       or (bidir = 2) whittedraytracer.comp per pixel
 #include <algorithm>
 #include <cstdint>
+#include <cstring>
 #include <thread>
 #include <vector>
 
@@ -267,6 +268,28 @@ int g_maxPathLength = 8;
 #undef TRIANGLES_PER_LEAF
 #undef MAX_PATHLENGTH
 }  // namespace ref_imp
+// the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+// ------------------------------------------------ hierarchypathtracer.comp (HierarchyImportance's renderer)
+namespace ref_hpt {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 8
+#define main HierarchyPathtracerMain
+#include "hierarchy/hierarchypathtracer.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef MAX_PATHLENGTH
+#undef IMPORTANCE_THRESHOLD
+#undef HIT_INDEX_OUTPUT
+#undef TRACERAY_IMPORTANCE_BREAK
+}  // namespace ref_hpt
 // the shader's own switches end with it
 #undef TRINORMAL_OUTPUT
 #undef SAMPLING_DECISION_OUTPUT
@@ -711,6 +734,92 @@ int ref_render_lt(const float* hierarchy, const int32_t* slots, const float* pos
                 ref_bpe::BidirEyeMain();
             }
     }
+    g_textureColours = nullptr;
+    return 0;
+}
+
+// One iteration of hierarchypathtracer.comp (the shader's own
+// MAX_PATHLENGTH 4) per pixel in order: importance (RG32F, two floats per
+// node), the hierarchy materials (RGBA16F, six texels per inner node, as
+// halves) and the node NDFs (RG16, three texels per inner node) as the
+// renderer binds them (hierarchyimportance.cpp:34-68).
+int ref_render_hier(const float* hierarchy, const int32_t* slots, const float* positions, const float* vertexInfo,
+                    const float* materials, int numMaterials, int width, int height, const float* cam,
+                    uint32_t frameSeed, const float* lightSamples, int numLightSamples, const float* sky,
+                    const float* importance, const uint16_t* hierMaterialHalves, uint64_t numHierMaterialHalves,
+                    const uint16_t* sggx, uint64_t numSggx, float* accum) {
+    using namespace glslref;
+    if (numMaterials > 256) return 1;
+    namespace P = ref_hpt;
+    std::vector<vec4> colours(4 * (size_t)numMaterials);
+    for (int m = 0; m < numMaterials; ++m) {
+        const float* r = materials + 24 * (size_t)m;
+        colours[4 * m + 0] = vec4(r[0], r[1], r[2], 1.0f);
+        colours[4 * m + 1] = vec4(r[4], r[5], r[6], 1.0f);
+        colours[4 * m + 2] = vec4(r[8], r[9], r[10], r[11]);
+        colours[4 * m + 3] = vec4(r[12], r[13], r[14], 1.0f);
+        P::Material& M = P::Materials[m];
+        M.diffuseTexHandle = uvec2(4 * m + 0, 0);
+        M.opacityTexHandle = uvec2(4 * m + 1, 0);
+        M.reflectivenessTexHandle = uvec2(4 * m + 2, 0);
+        M.emissivityTexHandle = uvec2(4 * m + 3, 0);
+        M.Fresnel0 = vec3(r[16], r[17], r[18]);
+        M.RefractionIndexAvg = r[3];
+        M.Fresnel1 = vec3(r[20], r[21], r[22]);
+    }
+    g_textureColours = colours.data();
+    // the texture units' conversions: half to float (exact), unorm16 to float (c / 65535)
+    auto half = [](uint16_t h) {
+        const uint32_t sign = (uint32_t)(h >> 15) << 31, e = (h >> 10) & 31u, m = h & 1023u;
+        uint32_t bits;
+        if (e == 0) {
+            if (m == 0) {
+                bits = sign;
+            } else {  // subnormal: normalise
+                int k = -1;
+                uint32_t mm = m;
+                do {
+                    ++k;
+                    mm <<= 1;
+                } while (!(mm & 1024u));
+                bits = sign | ((uint32_t)(127 - 15 - k) << 23) | ((mm & 1023u) << 13);
+            }
+        } else if (e == 31) {
+            bits = sign | 0x7F800000u | (m << 13);
+        } else {
+            bits = sign | ((e + 112u) << 23) | (m << 13);
+        }
+        float f;
+        std::memcpy(&f, &bits, 4);
+        return f;
+    };
+    std::vector<float> matTexels(numHierMaterialHalves), ndf(numSggx);
+    for (uint64_t i = 0; i < numHierMaterialHalves; ++i) matTexels[i] = half(hierMaterialHalves[i]);
+    for (uint64_t i = 0; i < numSggx; ++i) ndf[i] = (float)sggx[i] / 65535.0f;
+    P::HierachyBuffer = samplerBuffer{hierarchy, 4};
+    P::TriangleBuffer = isamplerBuffer{reinterpret_cast<const ivec4*>(slots)};
+    P::VertexPositionBuffer = samplerBuffer{positions, 3};
+    P::VertexInfoBuffer = samplerBuffer{vertexInfo, 4};
+    P::InitialLightSampleBuffer = samplerBuffer{lightSamples, 4};
+    P::HierarchyImportanceBuffer = samplerBuffer{importance, 2};
+    P::HierarchyMaterialBuffer = samplerBuffer{matTexels.data(), 4};
+    P::SGGXBuffer = samplerBuffer{ndf.data(), 2};
+    P::BackbufferSize = ivec2(width, height);
+    P::NumInitialLightSamples = numLightSamples;
+    P::CameraU = vec3(cam[0], cam[1], cam[2]);
+    P::CameraV = vec3(cam[3], cam[4], cam[5]);
+    P::CameraW = vec3(cam[6], cam[7], cam[8]);
+    P::CameraPosition = vec3(cam[9], cam[10], cam[11]);
+    P::PixelArea = cam[12];
+    P::FrameSeed = frameSeed;
+    P::IterationCount = 0;
+    P::EnvironmentMap.colour = vec3(sky[0], sky[1], sky[2]);
+    P::OutputTexture = image2D{reinterpret_cast<vec4*>(accum), width, height};
+    for (int y = 0; y < height; ++y)
+        for (int x = 0; x < width; ++x) {
+            gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
+            P::HierarchyPathtracerMain();
+        }
     g_textureColours = nullptr;
     return 0;
 }

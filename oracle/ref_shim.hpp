@@ -58,6 +58,7 @@ struct vec3 {
     explicit vec3(float s) : x(s), y(s), z(s) {}
     vec3(float a, float b_, float c) : x(a), y(b_), z(c) {}
     vec3(const vec2& v, float c) : x(v.x), y(v.y), z(c) {}
+    vec3(float a, const vec2& v) : x(a), y(v.x), z(v.y) {}
     float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
     float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
     GR_SW2(vec2, x, x) GR_SW2(vec2, x, y) GR_SW2(vec2, x, z) GR_SW2(vec2, y, x) GR_SW2(vec2, y, y)
@@ -164,6 +165,12 @@ inline ivec2::ivec2(const uvec2& v) : x((int32_t)v.x), y((int32_t)v.y) {}
 struct mat4 {
     vec4 c[4];
 };
+// mat3x3: three columns; m[i][j] is column i, row j.
+struct mat3x3 {
+    vec3 c[3];
+    vec3& operator[](int i) { return c[i]; }
+    const vec3& operator[](int i) const { return c[i]; }
+};
 
 // ---------------------------------------------------------------- operators
 #define GR_BIN2(OP)                                                                          \
@@ -252,6 +259,8 @@ inline vec3 cross(vec3 a, vec3 b) {
     return vec3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 inline float length(vec3 v) { return sqrt(dot(v, v)); }
+// the columns combined left to right: (c0 v.x + c1 v.y) + c2 v.z
+inline vec3 operator*(const mat3x3& m, vec3 v) { return (m.c[0] * v.x + m.c[1] * v.y) + m.c[2] * v.z; }
 inline float length(vec2 v) { return sqrt(dot(v, v)); }
 inline vec3 normalize(vec3 v) { return v / sqrt(dot(v, v)); }
 inline vec3 reflect(vec3 i, vec3 n) { return i - 2.0f * dot(n, i) * n; }

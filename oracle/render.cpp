@@ -1546,8 +1546,9 @@ static bool TraceImportance(const Scene& s, const float* imp, const Ray& ray, fl
                         out->nodeImportance = ix;
                         out->nodeSizeSq = lastNodeSizeSq;
                         out->node = currentNodeIndex;
+                        // grouped as the shader: newHit + ((exitDist - newHit) * h) / 8388593
                         rayLength = newHit + (exitDist - newHit) *
-                                                 ((float)(wanghash(floatBitsToUint(exitDist)) % 8388593u) / 8388593.0f);
+                                                 (float)(wanghash(floatBitsToUint(exitDist)) % 8388593u) / 8388593.0f;
                         out->slot = -1;
                     }
                     currentNodeIndex = escape;

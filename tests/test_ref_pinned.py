@@ -240,3 +240,28 @@ def test_photon_map_and_importon_map_images(room):
             (it, np.abs(acc_r[..., :3] - acc_o[..., :3]).max())
     assert acc_r[..., :3].mean() > 0
 
+
+
+@pytest.mark.parametrize("room", ["diffuse", "glossy"])
+def test_hierarchy_path_tracer_images(room):
+    """hierarchypathtracer.comp (the reference's text) against the oracle's
+    restatement over the importance that the oracle's acquisition and
+    propagation passes produce (so some nodes are cut short and shade their
+    node materials and NDFs): identical images, iteration by iteration."""
+    sc = scenes.cornell_room(seed=1, sphere_level=3, wall_grid=8) if room == "diffuse" else _glossy_room()
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", normals=sc["normals"])
+    W, H = 40, 32
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H).as_array()
+    st = [11]
+    ls = oracle.light_samples(sc["positions"], b.slots, sc["materials"], 128, st)
+    imp, _ = oracle.hier_importance(b, sc, W, H, cam, ls, iterations=4)
+    mats = oracle.hier_materials(b, sc)
+    acc_r = acc_o = None
+    for it in range(3):
+        ls = oracle.light_samples(sc["positions"], b.slots, sc["materials"], 128, st)
+        fs = render.frame_seed(it, "reference")
+        acc_r = ref.render_hier(b, sc, W, H, cam, fs, ls, imp, mats, b.sggx, accum=acc_r)
+        acc_o = oracle.render_hier(b, sc, W, H, cam, fs, ls, imp, mats, b.sggx, accum=acc_o, num_threads=1,
+                                   rng="reference")
+        assert np.array_equal(acc_r.view(np.uint32), acc_o.view(np.uint32)), (it, np.abs(acc_r - acc_o).max())
+    assert acc_r[..., :3].mean() > 0
