@@ -245,3 +245,50 @@ def render_hier(bvh, scene: dict, width: int, height: int, camera: np.ndarray, f
                            sg.size, _p(accum))
     assert rc == 0
     return accum
+
+
+def _hier_scene(bvh, scene):
+    from gpugi_gb300.cuda import vertex_info  # host-side layout helper (no compute)
+    assert bvh.leaf_size == 8 and bvh.bounds_kind == 0, "the hierarchy passes are built for 8-slot AABB hierarchies"
+    return (np.ascontiguousarray(bvh.hierarchy, dtype=np.float32), np.ascontiguousarray(bvh.slots, dtype=np.int32),
+            np.ascontiguousarray(scene["positions"], dtype=np.float32),
+            np.ascontiguousarray(vertex_info(scene["normals"], scene["texcoords"]), dtype=np.float32),
+            np.ascontiguousarray(scene["materials"], dtype=np.float32).reshape(-1, 24))
+
+
+def hier_importance(bvh, scene: dict, width: int, height: int, camera: np.ndarray, light_samples: np.ndarray,
+                    iterations: int = 10):
+    """HierarchyImportance's importance pass with the reference's
+    acquisition2.comp (NumImportanceIterations = 1..iterations), then
+    hierarchypropagation_init.comp and hierarchypropagation_nodes.comp until
+    nothing changes; invocations in order on one thread. Returns (importance
+    float32 [nodes + slots, 2], subtree float32 [nodes])."""
+    L = lib()
+    P, I = C.c_void_p, C.c_int
+    L.ref_hier_importance.argtypes = [P, I, P, I, P, P, P, I, I, I, P, P, I, I, P, P]
+    L.ref_hier_importance.restype = I
+    hier, slots, pos, vi, mats = _hier_scene(bvh, scene)
+    cam = np.ascontiguousarray(camera, dtype=np.float32)
+    ls = np.ascontiguousarray(light_samples, dtype=np.float32).reshape(-1, 8)
+    imp = np.zeros((hier.shape[0] + slots.shape[0], 2), np.float32)
+    sub = np.zeros(hier.shape[0], np.float32)
+    rc = L.ref_hier_importance(_p(hier), hier.shape[0], _p(slots), slots.shape[0], _p(pos), _p(vi), _p(mats),
+                               mats.shape[0], width, height, _p(cam), _p(ls), ls.shape[0], iterations, _p(imp),
+                               _p(sub))
+    assert rc == 0
+    return imp, sub
+
+
+def hier_materials(bvh, scene: dict) -> np.ndarray:
+    """Node materials with the reference's sampleleafmaterials.comp, then
+    pullmaterials.comp once per tree level: uint32 [nodes, 12], six pairs of
+    packed halves per node."""
+    L = lib()
+    P, I = C.c_void_p, C.c_int
+    L.ref_hier_materials.argtypes = [P, I, P, P, P, P, I, P]
+    L.ref_hier_materials.restype = I
+    hier, slots, pos, vi, mats = _hier_scene(bvh, scene)
+    out = np.zeros((hier.shape[0], 12), np.uint32)
+    rc = L.ref_hier_materials(_p(hier), hier.shape[0], _p(slots), _p(pos), _p(vi), _p(mats), mats.shape[0], _p(out))
+    assert rc == 0
+    return out

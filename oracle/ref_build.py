@@ -11,7 +11,8 @@ SAVE_LIGHT_CACHE, showlightcaches.comp, pathtracer_bidir.comp,
 whittedraytracer.comp, the photon mapper's photondistribution.comp and
 gather.comp, the importon map light tracer's importondistribution.comp
 and photontracing.comp, both with the lossless hash map, and the hierarchy
-renderer's hierarchypathtracer.comp);
+renderer's hierarchypathtracer.comp, acquisition2.comp, propagation and
+node-material passes);
 tests/test_ref_pinned.py checks the oracle's restatement (oracle/*.cpp)
 against it bit for bit.
 
@@ -63,7 +64,10 @@ FILES = ["helper.glsl", "scenedata.glsl", "intersectiontests.glsl", "random.glsl
          "bidirpathtracer/pathtracer_bidir.comp", "whittedraytracer.comp", "photonmapper/photondistribution.comp",
          "photonmapper/gather.comp", "photonmapper/photonmap.glsl", "maps/hashmap.glsl", "maps/grid.glsl",
          "pixelmaplt/importondistribution.comp", "pixelmaplt/photontracing.comp", "pixelmaplt/importonmap.glsl",
-         "hierarchy/hierarchypathtracer.comp", "hierarchy/sggx.glsl"]
+         "hierarchy/hierarchypathtracer.comp", "hierarchy/sggx.glsl", "hierarchy/acquisition2.comp",
+         "hierarchy/counthits.glsl", "hierarchy/importanceubo.glsl", "hierarchy/hierarchypropagation_init.comp",
+         "hierarchy/hierarchypropagation_nodes.comp", "hierarchy/hierarchymaterialbuffer.glsl",
+         "hierarchy/sampleleafmaterials.comp", "hierarchy/pullmaterials.comp"]
 OVERRIDABLE = {"TRIANGLES_PER_LEAF"}
 
 _CTOR = re.compile(r"\b((?:i|u|b)?vec[234])\s*\(")

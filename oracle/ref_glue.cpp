@@ -12,7 +12,11 @@
 //   ref_render_pt                       pathtracer.comp's main() per pixel
 //   ref_render_lt                       lighttracer.comp + showlightcaches.comp (LightPathtracer::Draw),
 //                                       or with bidir the cache-filling light pass + pathtracer_bidir.comp,
-//                                       or (bidir = 2) whittedraytracer.comp per pixel
+//                                       or (bidir = 2) whittedraytracer.comp per pixel,
+//                                       (3) the photon mapper, (4) the importon map light tracer
+//   ref_render_hier                     hierarchy/hierarchypathtracer.comp per pixel
+//   ref_hier_importance                 acquisition2.comp x iterations + the propagation shaders
+//   ref_hier_materials                  sampleleafmaterials.comp + pullmaterials.comp per tree level
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -291,6 +295,100 @@ using namespace glslref;
 #undef TRACERAY_IMPORTANCE_BREAK
 }  // namespace ref_hpt
 // the shader's own switches end with it
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+// ------------------------------------------------ the hierarchy-importance passes
+// acquisition2.comp (+ counthits.glsl), hierarchypropagation_init.comp and
+// _nodes.comp, sampleleafmaterials.comp and pullmaterials.comp; each in its
+// own namespace, bound to the same arrays by the entry points below.
+namespace ref_acq {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 8
+#define main AcquisitionMain
+#include "hierarchy/acquisition2.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef NEXT_EVENT_IMPORTANCE
+#undef HIT_INDEX_OUTPUT
+#undef MAX_PATHLENGTH
+}  // namespace ref_acq
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+namespace ref_pinit {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 8
+// hierarchypropagation_init.comp reads the node's minimum corner from an
+// undeclared `hierarchy0` (the shader does not compile for AABB
+// hierarchies as written); it is the node's first texel, as
+// hierarchypropagation_nodes.comp declares it.
+#define hierarchy0 texelFetch(HierachyBuffer, int(gl_GlobalInvocationID.x) * HierarchyBufferStride)
+#define main PropagationInitMain
+#include "hierarchy/hierarchypropagation_init.comp.h"
+#undef main
+#undef hierarchy0
+#undef TRIANGLES_PER_LEAF
+}  // namespace ref_pinit
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+namespace ref_pnodes {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 8
+#define main PropagationNodesMain
+#include "hierarchy/hierarchypropagation_nodes.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+#undef TRIINDEX_OUTPUT
+}  // namespace ref_pnodes
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+namespace ref_leafm {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 8
+#define main SampleLeafMaterialsMain
+#include "hierarchy/sampleleafmaterials.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+}  // namespace ref_leafm
+#undef TRINORMAL_OUTPUT
+#undef SAMPLING_DECISION_OUTPUT
+#undef NUM_LIGHT_SAMPLES
+#undef LOCAL_SIZE
+#undef QUADRATIC_PROBING
+#undef HASH_MAP_BINDIDX
+#undef HASH_MAP_DATA_BINDIDX
+
+namespace ref_pullm {
+using namespace glslref;
+#define TRIANGLES_PER_LEAF 8
+#define main PullMaterialsMain
+#include "hierarchy/pullmaterials.comp.h"
+#undef main
+#undef TRIANGLES_PER_LEAF
+}  // namespace ref_pullm
 #undef TRINORMAL_OUTPUT
 #undef SAMPLING_DECISION_OUTPUT
 #undef NUM_LIGHT_SAMPLES
@@ -819,6 +917,181 @@ int ref_render_hier(const float* hierarchy, const int32_t* slots, const float* p
         for (int x = 0; x < width; ++x) {
             gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
             P::HierarchyPathtracerMain();
+        }
+    g_textureColours = nullptr;
+    return 0;
+}
+
+}  // extern "C"
+
+namespace {
+// Parent of every inner node (the scene's parent buffer, an R32I texture
+// buffer the propagation and material passes read through a float view):
+// both children of a binary node point at it; the root points at itself.
+std::vector<float> ParentPointers(const float* hierarchy, int numNodes) {
+    std::vector<float> parent((size_t)numNodes);
+    auto put = [&](int i, int32_t v) { std::memcpy(&parent[(size_t)i], &v, 4); };
+    if (numNodes > 0) put(0, 0);
+    for (int i = 0; i < numNodes; ++i) {
+        uint32_t child;
+        std::memcpy(&child, hierarchy + 8 * (size_t)i + 3, 4);
+        if (child & 0x80000000u) continue;
+        int32_t second;
+        std::memcpy(&second, hierarchy + 8 * (size_t)child + 7, 4);
+        put((int)child, i);
+        if (second > 0 && second < numNodes) put(second, i);
+    }
+    return parent;
+}
+// Number of tree levels (ComputeHierarchyMaterials runs pullmaterials.comp
+// once per level): one more than the deepest inner node's depth.
+int TreeLevels(const float* hierarchy, int numNodes) {
+    std::vector<int> depth((size_t)numNodes, 0);
+    int levels = numNodes > 0 ? 1 : 0;
+    for (int i = 0; i < numNodes; ++i) {  // parents precede their children
+        uint32_t child;
+        std::memcpy(&child, hierarchy + 8 * (size_t)i + 3, 4);
+        if (child & 0x80000000u) continue;
+        int32_t second;
+        std::memcpy(&second, hierarchy + 8 * (size_t)child + 7, 4);
+        depth[child] = depth[i] + 1;
+        if (second > 0 && second < numNodes) depth[second] = depth[i] + 1;
+        levels = std::max(levels, depth[i] + 2);
+    }
+    return levels;
+}
+void BindConstantMaterials(std::vector<glslref::vec4>& colours, const float* materials, int numMaterials) {
+    using namespace glslref;
+    colours.assign(4 * (size_t)numMaterials, vec4());
+    for (int m = 0; m < numMaterials; ++m) {
+        const float* r = materials + 24 * (size_t)m;
+        colours[4 * m + 0] = vec4(r[0], r[1], r[2], 1.0f);
+        colours[4 * m + 1] = vec4(r[4], r[5], r[6], 1.0f);
+        colours[4 * m + 2] = vec4(r[8], r[9], r[10], r[11]);
+        colours[4 * m + 3] = vec4(r[12], r[13], r[14], 1.0f);
+    }
+    g_textureColours = colours.data();
+}
+template <class M>
+void BindMaterial(M& mat, int m, const float* materials) {
+    using namespace glslref;
+    const float* r = materials + 24 * (size_t)m;
+    mat.diffuseTexHandle = uvec2(4 * m + 0, 0);
+    mat.opacityTexHandle = uvec2(4 * m + 1, 0);
+    mat.reflectivenessTexHandle = uvec2(4 * m + 2, 0);
+    mat.emissivityTexHandle = uvec2(4 * m + 3, 0);
+    mat.Fresnel0 = vec3(r[16], r[17], r[18]);
+    mat.RefractionIndexAvg = r[3];
+    mat.Fresnel1 = vec3(r[20], r[21], r[22]);
+}
+}  // namespace
+
+extern "C" {
+
+// HierarchyImportance::Draw's importance pass (hierarchyimportance.cpp:
+// 87-108, 119-152): `iterations` runs of acquisition2.comp over every pixel
+// (NumImportanceIterations = 1..iterations), then
+// hierarchypropagation_init.comp over the inner nodes and
+// hierarchypropagation_nodes.comp until no node changes. Invocations run in
+// order on one thread. imp: {x, y} per inner node, then per leaf slot;
+// subtree: per inner node.
+int ref_hier_importance(const float* hierarchy, int numNodes, const int32_t* slots, int numSlots,
+                        const float* positions, const float* vertexInfo, const float* materials, int numMaterials,
+                        int width, int height, const float* cam, const float* lightSamples, int numLightSamples,
+                        int iterations, float* imp, float* subtree) {
+    using namespace glslref;
+    if (numMaterials > 256 || iterations < 1) return 1;
+    std::vector<vec4> colours;
+    BindConstantMaterials(colours, materials, numMaterials);
+    for (int m = 0; m < numMaterials; ++m) BindMaterial(ref_acq::Materials[m], m, materials);
+    std::vector<float> parent = ParentPointers(hierarchy, numNodes);
+    std::fill(imp, imp + 2 * ((size_t)numNodes + numSlots), 0.0f);
+    std::fill(subtree, subtree + numNodes, 0.0f);
+    namespace A = ref_acq;
+    A::HierachyBuffer = samplerBuffer{hierarchy, 4};
+    A::TriangleBuffer = isamplerBuffer{reinterpret_cast<const ivec4*>(slots)};
+    A::VertexPositionBuffer = samplerBuffer{positions, 3};
+    A::VertexInfoBuffer = samplerBuffer{vertexInfo, 4};
+    A::InitialLightSampleBuffer = samplerBuffer{lightSamples, 4};
+    A::BackbufferSize = ivec2(width, height);
+    A::NumInitialLightSamples = numLightSamples;
+    A::CameraU = vec3(cam[0], cam[1], cam[2]);
+    A::CameraV = vec3(cam[3], cam[4], cam[5]);
+    A::CameraW = vec3(cam[6], cam[7], cam[8]);
+    A::CameraPosition = vec3(cam[9], cam[10], cam[11]);
+    A::PixelArea = cam[12];
+    A::HierarchyImportance = reinterpret_cast<vec2*>(imp);
+    A::NumInnerNodes = numNodes;
+    A::NumTriangles = numSlots;
+    A::HierarchyBufferStride = 2;
+    for (int it = 1; it <= iterations; ++it) {
+        A::NumImportanceIterations = it;
+        for (int y = 0; y < height; ++y)
+            for (int x = 0; x < width; ++x) {
+                gl_GlobalInvocationID = uvec3((uint)x, (uint)y, 0u);
+                A::AcquisitionMain();
+            }
+    }
+    namespace I = ref_pinit;
+    namespace N = ref_pnodes;
+    I::HierachyBuffer = N::HierachyBuffer = samplerBuffer{hierarchy, 4};
+    I::HierarchyImportance = N::HierarchyImportance = reinterpret_cast<vec2*>(imp);
+    I::SubtreeImportance = N::SubtreeImportance = subtree;
+    I::ParentPointerBuffer = N::ParentPointerBuffer = samplerBuffer{parent.data(), 1};
+    I::NumInnerNodes = N::NumInnerNodes = numNodes;
+    I::NumTriangles = N::NumTriangles = numSlots;
+    I::NumImportanceIterations = N::NumImportanceIterations = iterations;
+    I::HierarchyBufferStride = N::HierarchyBufferStride = 2;
+    for (int i = 0; i < numNodes; ++i) {
+        gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+        I::PropagationInitMain();
+    }
+    int passes = 0;
+    do {
+        N::ChangedAnything = 0;
+        for (int i = 0; i < numNodes; ++i) {
+            gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+            N::PropagationNodesMain();
+        }
+        if (++passes > numNodes + 1) return 2;  // no convergence: a malformed tree
+    } while (N::ChangedAnything != 0);
+    g_textureColours = nullptr;
+    return 0;
+}
+
+// HierarchyImportance::ComputeHierarchyMaterials (hierarchyimportance.cpp:
+// 154-181): sampleleafmaterials.comp over the inner nodes, then
+// pullmaterials.comp once per tree level. out: six uvec2 per inner node.
+int ref_hier_materials(const float* hierarchy, int numNodes, const int32_t* slots, const float* positions,
+                       const float* vertexInfo, const float* materials, int numMaterials, uint32_t* out) {
+    using namespace glslref;
+    if (numMaterials > 256) return 1;
+    std::vector<vec4> colours;
+    BindConstantMaterials(colours, materials, numMaterials);
+    for (int m = 0; m < numMaterials; ++m) BindMaterial(ref_leafm::Materials[m], m, materials);
+    std::vector<float> parent = ParentPointers(hierarchy, numNodes);
+    std::fill(out, out + 12 * (size_t)numNodes, 0u);
+    namespace L = ref_leafm;
+    namespace U = ref_pullm;
+    L::HierachyBuffer = U::HierachyBuffer = samplerBuffer{hierarchy, 4};
+    L::TriangleBuffer = isamplerBuffer{reinterpret_cast<const ivec4*>(slots)};
+    L::VertexPositionBuffer = samplerBuffer{positions, 3};
+    L::VertexInfoBuffer = samplerBuffer{vertexInfo, 4};
+    L::hierarchyMaterial = reinterpret_cast<L::HierarchyMaterial*>(out);
+    U::hierarchyMaterial = reinterpret_cast<U::HierarchyMaterial*>(out);
+    static_assert(sizeof(L::HierarchyMaterial) == 48 && sizeof(U::HierarchyMaterial) == 48, "six uvec2 per node");
+    U::ParentPointerBuffer = samplerBuffer{parent.data(), 1};
+    L::NumInnerNodes = U::NumInnerNodes = numNodes;
+    L::HierarchyBufferStride = U::HierarchyBufferStride = 2;
+    for (int i = 0; i < numNodes; ++i) {
+        gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+        L::SampleLeafMaterialsMain();
+    }
+    const int levels = TreeLevels(hierarchy, numNodes);
+    for (int pass = 0; pass < levels; ++pass)
+        for (int i = 0; i < numNodes; ++i) {
+            gl_GlobalInvocationID = uvec3((uint)i, 0u, 0u);
+            U::PullMaterialsMain();
         }
     g_textureColours = nullptr;
     return 0;

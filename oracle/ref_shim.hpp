@@ -50,6 +50,24 @@ struct vec2 {
     float operator[](int i) const { return i == 0 ? x : y; }
     GR_SW2(vec2, x, x) GR_SW2(vec2, x, y) GR_SW2(vec2, y, x) GR_SW2(vec2, y, y)
 };
+// `v.xy` / `v.zw` of a vec3 or vec4 as an lvalue (`mat.Opacity.xy += c`,
+// pullmaterials.comp): reads as a vec2, assigns component by component.
+struct VecSwizzle2 {
+    float *a, *b;
+    inline operator vec2() const { return vec2(*a, *b); }
+    inline VecSwizzle2& operator=(const vec2& v) {
+        *a = v.x, *b = v.y;
+        return *this;
+    }
+    inline VecSwizzle2& operator+=(const vec2& v) {
+        *a += v.x, *b += v.y;
+        return *this;
+    }
+    inline VecSwizzle2& operator-=(const vec2& v) {
+        *a -= v.x, *b -= v.y;
+        return *this;
+    }
+};
 struct vec3 {
     union { float x, r; };
     union { float y, g; };
@@ -64,6 +82,7 @@ struct vec3 {
     GR_SW2(vec2, x, x) GR_SW2(vec2, x, y) GR_SW2(vec2, x, z) GR_SW2(vec2, y, x) GR_SW2(vec2, y, y)
     GR_SW2(vec2, y, z) GR_SW2(vec2, z, x) GR_SW2(vec2, z, y) GR_SW2(vec2, z, z)
     GR_SW3(vec3, x, y, z) GR_SW3(vec3, z, y, x)
+    VecSwizzle2 xy() { return VecSwizzle2{&x, &y}; }
 };
 // `v.xyz` of a vec4 as an lvalue (`color.xyz += c`, importondistribution.comp,
 // screenreproject.glsl): reads as a vec3, assigns component by component.
@@ -90,6 +109,8 @@ struct vec4 {
     GR_SW2(vec2, x, w)
     GR_SW3(vec3, x, y, z) GR_SW3(vec3, y, z, w)
     VecSwizzle3 xyz() { return VecSwizzle3{&x, &y, &z}; }
+    VecSwizzle2 xy() { return VecSwizzle2{&x, &y}; }
+    VecSwizzle2 zw() { return VecSwizzle2{&z, &w}; }
     vec3 rgb() const { return vec3(x, y, z); }
 };
 inline VecSwizzle3::operator vec3() const { return vec3(*a, *b, *c); }
@@ -359,6 +380,31 @@ inline float imageAtomicAdd(image2D& im, ivec2 p, float v) {
         std::memcpy(&next, &n, 4);
     } while (!__atomic_compare_exchange_n(u, &old, next, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED));
     return f;
+}
+// atomicAdd on a storage-buffer float (counthits.glsl's importance sums;
+// GL_NV_shader_atomic_float). The passes that use it run their invocations
+// one at a time, in order, so the sum is a plain add.
+inline float atomicAdd(float& x, float v) {
+    const float o = x;
+    x = o + v;
+    return o;
+}
+// packHalf2x16 / unpackHalf2x16 through the compiler's IEEE binary16 type
+// (round to nearest even; GLSL leaves the rounding open, NVIDIA's converter
+// rounds to nearest even).
+inline uint packHalf2x16(vec2 v) {
+    const _Float16 a = (_Float16)v.x, b = (_Float16)v.y;
+    uint16_t ua, ub;
+    std::memcpy(&ua, &a, 2);
+    std::memcpy(&ub, &b, 2);
+    return (uint)ua | ((uint)ub << 16);
+}
+inline vec2 unpackHalf2x16(uint p) {
+    const uint16_t ua = (uint16_t)(p & 0xFFFFu), ub = (uint16_t)(p >> 16);
+    _Float16 a, b;
+    std::memcpy(&a, &ua, 2);
+    std::memcpy(&b, &ub, 2);
+    return vec2((float)a, (float)b);
 }
 // atomicAdd on a storage-buffer integer (the light cache's entry counter,
 // lightcache.glsl:27-35): returns the old value.

@@ -265,3 +265,23 @@ def test_hierarchy_path_tracer_images(room):
                                    rng="reference")
         assert np.array_equal(acc_r.view(np.uint32), acc_o.view(np.uint32)), (it, np.abs(acc_r - acc_o).max())
     assert acc_r[..., :3].mean() > 0
+
+
+@pytest.mark.parametrize("room", ["diffuse", "glossy"])
+def test_hierarchy_importance_and_materials(room):
+    """acquisition2.comp + the two propagation shaders, and
+    sampleleafmaterials.comp + pullmaterials.comp (the reference's text),
+    against the oracle's restatements: identical importance {x, y}, subtree
+    importance and packed node materials."""
+    sc = scenes.cornell_room(seed=1, sphere_level=3, wall_grid=8) if room == "diffuse" else _glossy_room()
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep", normals=sc["normals"])
+    W, H = 40, 32
+    cam = render.camera_lookat(*scenes.CORNELL_CAMERA, W, H).as_array()
+    ls = oracle.light_samples(sc["positions"], b.slots, sc["materials"], 128, [13])
+    imp_r, sub_r = ref.hier_importance(b, sc, W, H, cam, ls, iterations=3)
+    imp_o, sub_o = oracle.hier_importance(b, sc, W, H, cam, ls, iterations=3, num_threads=1)
+    assert imp_r[0, 0] > 0 and (sub_r > 0).all()
+    assert np.array_equal(imp_r.view(np.uint32), imp_o.view(np.uint32)), np.abs(imp_r - imp_o).max()
+    assert np.array_equal(sub_r.view(np.uint32), sub_o.view(np.uint32))
+    mat_r, mat_o = ref.hier_materials(b, sc), oracle.hier_materials(b, sc)
+    assert np.array_equal(mat_r, mat_o), np.argwhere(mat_r != mat_o)[:5]
