@@ -367,12 +367,19 @@ def run_ours(args, world, rank, local):
     # issued with gpugi_trace_closest_async over several streams, so one
     # batch's results travel back while the next batch's rays travel in; the
     # synchronous call (gpugi_trace_closest, one batch at a time) is timed too.
+    # The host rays of a batch are one page-locked structure-of-arrays block
+    # (ox | oy | oz | dx | dy | dz | tmax) and its results another (slot | t
+    # | u | v): the library moves evenly spaced columns with one copy each way.
     ns = max(1, args.e2e_streams)
-    pin = [{k: torch.from_numpy(rb[k]).pin_memory().numpy() for k in cuda.RAY_KEYS}
-           for rb in host_batches[:max(ns, 2)]]
-    res = [dict(slot=torch.empty(N_RAYS, dtype=torch.int32).pin_memory().numpy(),
-                t=torch.empty(N_RAYS).pin_memory().numpy(), u=torch.empty(N_RAYS).pin_memory().numpy(),
-                v=torch.empty(N_RAYS).pin_memory().numpy()) for _ in range(max(ns, 2))]
+    pin, res = [], []
+    for rb in host_batches[:max(ns, 2)]:
+        blk = torch.empty((len(cuda.RAY_KEYS), N_RAYS), dtype=torch.float32).pin_memory().numpy()
+        for i, key in enumerate(cuda.RAY_KEYS):
+            blk[i] = rb[key]
+        pin.append({key: blk[i] for i, key in enumerate(cuda.RAY_KEYS)})
+    for _ in range(max(ns, 2)):
+        blk = torch.empty((4, N_RAYS), dtype=torch.float32).pin_memory().numpy()
+        res.append(dict(slot=blk[0].view(np.int32), t=blk[1], u=blk[2], v=blk[3]))
     lib = cuda.lib()
     lib.gpugi_trace_closest_async.argtypes = [ctypes.c_void_p] * 9 + [ctypes.c_uint64] + [ctypes.c_void_p] * 5
     estreams = [torch.cuda.Stream(device=dev) for _ in range(ns)]

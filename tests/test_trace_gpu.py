@@ -275,6 +275,64 @@ def test_host_paths_give_identical_results(cuda_ctx, icosphere_65536, parts, pin
         ds.close()
 
 
+@pytest.mark.parametrize("parts,pad,pinned", [(1, 0, True), (2, 0, True), (3, 5, True), (2, 1000, True),
+                                             (1, 0, False)])
+def test_host_soa_blocks(cuda_ctx, icosphere_65536, parts, pad, pinned):
+    """Rays and results in structure-of-arrays blocks (evenly spaced
+    columns, packed or with a gap between them: one 2D copy each way) give
+    the oracle's results through the synchronous call (staged in parts) and
+    the stream-ordered call."""
+    import ctypes as C
+
+    import torch
+    sc = icosphere_65536
+    b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
+    ds = cuda_ctx.upload_scene(b, sc["positions"])
+    n = 200_003
+    w = n + pad
+    rays = scenes.aimed_rays(n, sc["positions"], seed=23, spread=2.5)
+
+    def block(rows):
+        a = torch.empty(rows * w, dtype=torch.float32)
+        return (a.pin_memory() if pinned else a).numpy()
+
+    rb, ob, occb = block(7), block(4), block(1)
+    cols = {k: rb[i * w:i * w + n] for i, k in enumerate(cuda.RAY_KEYS)}
+    for k in cuda.RAY_KEYS:
+        cols[k][:] = rays[k]
+    out = dict(slot=ob[0:n].view(np.int32), t=ob[w:w + n], u=ob[2 * w:2 * w + n], v=ob[3 * w:3 * w + n])
+    occ = occb.view(np.uint8)[:n]
+    want = oracle.trace_closest(b, sc["positions"], rays)
+    want_occ = oracle.trace_any(b, sc["positions"], rays)["occluded"]
+    L = cuda.lib()
+    cuda_ctx.set_host_pipeline(parts)
+    try:
+        cuda_ctx.check(L.gpugi_trace_closest(cuda_ctx.handle, ds.handle, *[cuda._ptr(cols[k]) for k in cuda.RAY_KEYS],
+                                             n, *[cuda._ptr(out[k]) for k in ("slot", "t", "u", "v")]))
+        _compare_closest(out, want)
+        cuda_ctx.check(L.gpugi_trace_any(cuda_ctx.handle, ds.handle, *[cuda._ptr(cols[k]) for k in cuda.RAY_KEYS], n,
+                                         cuda._ptr(occ)))
+        assert np.array_equal(occ, want_occ)
+        ob[:] = np.nan
+        occ[:] = 7
+        L.gpugi_trace_closest_async.argtypes = [C.c_void_p] * 9 + [C.c_uint64] + [C.c_void_p] * 5
+        L.gpugi_trace_any_async.argtypes = [C.c_void_p] * 9 + [C.c_uint64, C.c_void_p, C.c_void_p]
+        st = torch.cuda.Stream()
+        cuda_ctx.check(L.gpugi_trace_closest_async(cuda_ctx.handle, ds.handle,
+                                                   *[cuda._ptr(cols[k]) for k in cuda.RAY_KEYS], n,
+                                                   *[cuda._ptr(out[k]) for k in ("slot", "t", "u", "v")],
+                                                   C.c_void_p(st.cuda_stream)))
+        cuda_ctx.check(L.gpugi_trace_any_async(cuda_ctx.handle, ds.handle, *[cuda._ptr(cols[k]) for k in cuda.RAY_KEYS],
+                                               n, cuda._ptr(occ), C.c_void_p(st.cuda_stream)))
+        st.synchronize()
+        assert cuda_ctx.device_error_bits() == 0
+        _compare_closest(out, want)
+        assert np.array_equal(occ, want_occ)
+    finally:
+        cuda_ctx.set_host_pipeline(2)
+        ds.close()
+
+
 @pytest.mark.parametrize("parts,zero_copy", [(1, False), (2, False), (1, True)])
 def test_device_guard_bits_reach_the_caller(cuda_ctx, icosphere_65536, parts, zero_copy):
     """A guard bit set on the device (here by the test-support call, as a
