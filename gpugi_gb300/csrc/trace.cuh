@@ -26,10 +26,14 @@ namespace gpugi {
 // triangles there.
 template <bool ROBUST = false>
 GPUGI_D bool intersect_box(float3 o, float3 inv, float4 lo, float4 hi, float& firstHit) {
-    float tbx = X::mul(inv.x, X::sub(lo.x, o.x)), tby = X::mul(inv.y, X::sub(lo.y, o.y)),
-          tbz = X::mul(inv.z, X::sub(lo.z, o.z));
-    float ttx = X::mul(inv.x, X::sub(hi.x, o.x)), tty = X::mul(inv.y, X::sub(hi.y, o.y)),
-          ttz = X::mul(inv.z, X::sub(hi.z, o.z));
+    // x and y slabs as packed pairs (add.f32x2 / mul.f32x2: per component
+    // the same IEEE round-to-nearest results as the scalar operations;
+    // lo - o as lo + (-o), exact for every input including signed zeros)
+    const float2 no = make_float2(-o.x, -o.y), ixy = make_float2(inv.x, inv.y);
+    const float2 b2 = __fmul2_rn(__fadd2_rn(make_float2(lo.x, lo.y), no), ixy);
+    const float2 t2 = __fmul2_rn(__fadd2_rn(make_float2(hi.x, hi.y), no), ixy);
+    float tbx = b2.x, tby = b2.y, tbz = X::mul(inv.z, X::sub(lo.z, o.z));
+    float ttx = t2.x, tty = t2.y, ttz = X::mul(inv.z, X::sub(hi.z, o.z));
     float mnx = fminf(ttx, tbx), mny = fminf(tty, tby), mnz = fminf(ttz, tbz);
     float mxx = fmaxf(ttx, tbx), mxy = fmaxf(tty, tby), mxz = fmaxf(ttz, tbz);
     if (ROBUST) {
