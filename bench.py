@@ -55,6 +55,44 @@ def peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
+def link_bound(rays_block: np.ndarray, results_block: np.ndarray, dev) -> dict:
+    """The host link's bound on the end-to-end rate: one step's rays copied
+    in and its results copied out at the same time (one copy each way, on two
+    streams), timed with CUDA events; the copies in both directions share
+    the link, so this is below the sum of the one-way rates. The blocks are
+    the page-locked (7, N) ray and (4, N) result arrays of one step."""
+    import torch
+    hin_t, hout_t = torch.from_numpy(rays_block), torch.from_numpy(results_block)
+    din = torch.empty(hin_t.shape, dtype=torch.float32, device=dev)
+    dout = torch.empty(hout_t.shape, dtype=torch.float32, device=dev)
+    s_in, s_out = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    cur = torch.cuda.current_stream(dev)
+
+    def step():
+        s_in.wait_stream(cur)
+        s_out.wait_stream(cur)
+        with torch.cuda.stream(s_in):
+            din.copy_(hin_t, non_blocking=True)
+        with torch.cuda.stream(s_out):
+            hout_t.copy_(dout, non_blocking=True)
+        cur.wait_stream(s_in)
+        cur.wait_stream(s_out)
+
+    for _ in range(3):
+        step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    e0.record(cur)
+    for _ in range(reps):
+        step()
+    e1.record(cur)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    return {"value": N_RAYS / (ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms,
+            "bytes_in": int(hin_t.numel() * 4), "bytes_out": int(hout_t.numel() * 4),
+            "what": "one step's rays in and results out copied concurrently (one copy each way), CUDA events"}
+
+
 def l2_read_gbs(ctx) -> float:
     """L2 read bandwidth (gpugi_measure_l2_bandwidth: one launch re-reads an
     L2-resident 32 MiB buffer 200 times). The driver's peaks file has no L2
@@ -371,15 +409,17 @@ def run_ours(args, world, rank, local):
     # (ox | oy | oz | dx | dy | dz | tmax) and its results another (slot | t
     # | u | v): the library moves evenly spaced columns with one copy each way.
     ns = max(1, args.e2e_streams)
-    pin, res = [], []
+    pin, res, blocks = [], [], []
     for rb in host_batches[:max(ns, 2)]:
         blk = torch.empty((len(cuda.RAY_KEYS), N_RAYS), dtype=torch.float32).pin_memory().numpy()
         for i, key in enumerate(cuda.RAY_KEYS):
             blk[i] = rb[key]
         pin.append({key: blk[i] for i, key in enumerate(cuda.RAY_KEYS)})
-    for _ in range(max(ns, 2)):
+        blocks.append(blk)
+    for k in range(max(ns, 2)):
         blk = torch.empty((4, N_RAYS), dtype=torch.float32).pin_memory().numpy()
         res.append(dict(slot=blk[0].view(np.int32), t=blk[1], u=blk[2], v=blk[3]))
+        blocks[k] = (blocks[k], blk)
     lib = cuda.lib()
     lib.gpugi_trace_closest_async.argtypes = [ctypes.c_void_p] * 9 + [ctypes.c_uint64] + [ctypes.c_void_p] * 5
     estreams = [torch.cuda.Stream(device=dev) for _ in range(ns)]
@@ -417,6 +457,7 @@ def run_ours(args, world, rank, local):
     e2e_sync_s = reduce_max(time.perf_counter() - t0, world, dev)
     e2e_sync = {"value": world * args.steps * N_RAYS / e2e_sync_s / 1e6, "unit": UNIT,
                 "call": "gpugi_trace_closest (synchronous, one batch at a time)"}
+    link = link_bound(blocks[0][0], blocks[0][1], dev)
 
     peak, peak_src = peaks()
     avg_launch_s = float(np.mean(per_launch_ms)) / 1e3
@@ -434,7 +475,7 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N_RAYS * 28,
                     "d2h_bytes_per_step": N_RAYS * 16,
                     "call": f"gpugi_trace_closest_async from page-locked host arrays over {ns} streams",
-                    "synchronous": e2e_sync},
+                    "synchronous": e2e_sync, "link_bound": link},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per step, read from "
