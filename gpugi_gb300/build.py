@@ -65,18 +65,24 @@ def build_bvhmake(force=False) -> Path:
     return out
 
 
-def build_cuda(force=False, jobs=None) -> Path:
-    out = LIB / "libgpugi_cuda.so"
-    OBJ.mkdir(parents=True, exist_ok=True)
+def build_cuda(force=False, jobs=None, checked=False) -> Path:
+    """libgpugi_cuda.so, or with checked=True libgpugi_cuda_checked.so: the
+    same sources compiled with -DGPUGI_CHECKED=1 (device indexes checked
+    before every node, slot, vertex and material fetch; a bad one sets
+    GPUGI_DEVERR_BOUNDS and the fetch is skipped)."""
+    out = LIB / ("libgpugi_cuda_checked.so" if checked else "libgpugi_cuda.so")
+    obj = OBJ / "checked" if checked else OBJ
+    obj.mkdir(parents=True, exist_ok=True)
+    flags = NVCC_FLAGS + (["-DGPUGI_CHECKED=1"] if checked else [])
     srcs = [CSRC / s for s in CUDA_SOURCES if (CSRC / s).exists()]
     hdrs = _headers()
     objs = []
     todo = []
     for s in srcs:
-        o = OBJ / (s.stem + ".o")
+        o = obj / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            todo.append([NVCC] + NVCC_FLAGS + ["-c", str(s), "-o", str(o)])
+            todo.append([NVCC] + flags + ["-c", str(s), "-o", str(o)])
     with cf.ThreadPoolExecutor(max_workers=jobs or max(1, len(todo))) as ex:
         list(ex.map(_run, todo))
     if force or todo or _stale(out, objs):
@@ -99,11 +105,13 @@ def build_headless(force=False) -> Path | None:
 
 def build_all(force=False):
     LIB.mkdir(parents=True, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
         f1 = ex.submit(build_bvhmake, force)
         f2 = ex.submit(build_cuda, force)
+        f3 = ex.submit(build_cuda, force, None, True)
         f1.result()
         f2.result()
+        f3.result()
     build_headless(force)
 
 

@@ -579,7 +579,9 @@ static gpugi_status build_into(gpugi_ctx* ctx, gpugi_scene* sc, const float* pos
     sc->dev.positions = dPos;
     sc->dev.vinfo = dInfo;
     sc->dev.materials = dMat;
+    sc->dev.err = ctx->errWord;
     sc->dev.numNodes = numNodes;
+    sc->numNodesUploaded = numNodes;
     sc->dev.numSlots = numSlots;
     sc->dev.leafSize = leafSize;
     sc->dev.boundsKind = GPUGI_BOUNDS_AABB;

@@ -273,7 +273,9 @@ using namespace gpugi;
 
 extern "C" {
 
-const char* gpugi_version(void) { return "gpugi_gb300 0.1 (sm_103a)"; }
+const char* gpugi_version(void) {
+    return gpugi::kChecked ? "gpugi_gb300 0.1 (sm_103a) checked" : "gpugi_gb300 0.1 (sm_103a)";
+}
 
 gpugi_status gpugi_create(gpugi_ctx** out, const gpugi_opts* opts) {
     if (!out) return GPUGI_ERROR_INVALID_ARGUMENT;

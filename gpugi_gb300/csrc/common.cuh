@@ -86,6 +86,18 @@ constexpr uint32_t DEVERR_QUEUE_OVERFLOW = 0x2u;
 constexpr uint32_t DEVERR_WAIT_TIMEOUT = 0x4u;
 constexpr uint32_t DEVERR_BUILD = 0x8u;  // GPU hierarchy build: a walk to the root exceeded the tree depth bound
 constexpr uint32_t DEVERR_HIERARCHY = 0x10u;  // hierarchy importance: a walk to the root exceeded the node count
+constexpr uint32_t DEVERR_BOUNDS = 0x20u;  // checked builds: an index outside its array (the access was skipped)
+
+// Bounds-checked builds (compiled with -DGPUGI_CHECKED=1 into
+// libgpugi_cuda_checked.so): node, leaf-slot, vertex and material indexes
+// are checked before every fetch; a bad index sets DEVERR_BOUNDS and the
+// fetch is skipped (the walk or the shading of that item ends). The
+// wavefront queues and light caches check their capacity in every build.
+#ifdef GPUGI_CHECKED
+constexpr bool kChecked = true;
+#else
+constexpr bool kChecked = false;
+#endif
 
 GPUGI_D void raise_error(uint32_t* word, uint32_t bits) {
     if (word) atomicOr(word, bits);

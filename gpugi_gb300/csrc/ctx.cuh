@@ -96,6 +96,7 @@ struct gpugi_scene {
     std::vector<int32_t> hostSlots;
     std::vector<float> hostMaterials;
     uint32_t numLeafBlocks = 0;
+    uint32_t numNodesUploaded = 0;  // dev.numNodes before gpugi_debug_limit_nodes
     // light tables (Scene::LoadLightSources / ComputePointLightTable)
     bool lightsReady = false;
     std::vector<gpugi::LightTriangle> lightTris;

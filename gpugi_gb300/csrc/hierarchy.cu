@@ -201,6 +201,10 @@ GPUGI_D bool trace_importance(const DevScene& s, const float2* __restrict__ imp,
             raise_error(err, DEVERR_TRAVERSAL_CAP);
             return false;
         }
+        if (kChecked && node >= s.numNodes) {
+            raise_error(err, DEVERR_BOUNDS);
+            return false;
+        }
         const float4 a = __ldg(s.nodes + 2 * node), b = __ldg(s.nodes + 2 * node + 1);
         const uint32_t child = __float_as_uint(a.w), escape = __float_as_uint(b.w);
         float fh, lh;
@@ -226,6 +230,10 @@ GPUGI_D bool trace_importance(const DevScene& s, const float2* __restrict__ imp,
             } else if (child & LEAF_FLAG) {
                 const uint32_t count = (child >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK;
                 const uint32_t slot0 = (child & LEAF_BLOCK_MASK) * s.leafSize;
+                if (kChecked && (uint64_t)slot0 + count > s.numSlots) {
+                    raise_error(err, DEVERR_BOUNDS);
+                    return false;
+                }
                 for (uint32_t k = 0; k < count; ++k) {
                     float h, by, bz;
                     if (intersect_triangle(o, d, s.tris + 3 * (size_t)(slot0 + k), h, by, bz) && h < len) {

@@ -249,7 +249,9 @@ extern "C" gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarch
     sc->dev.positions = dPos;
     sc->dev.vinfo = dInfo;
     sc->dev.materials = dMat;
+    sc->dev.err = ctx->errWord;
     sc->dev.numNodes = numNodes;
+    sc->numNodesUploaded = numNodes;
     sc->dev.numSlots = numSlots;
     sc->dev.leafSize = leafSize;
     sc->dev.boundsKind = boundsKind;
@@ -347,4 +349,12 @@ extern "C" void gpugi_scene_destroy(gpugi_scene* sc) {
     if (sc->texBlock) cudaFree(sc->texBlock);
     for (void* p : sc->allocations) cudaFree(p);
     delete sc;
+}
+
+extern "C" gpugi_status gpugi_debug_limit_nodes(gpugi_scene* sc, uint32_t numNodes) {
+    if (!sc) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (numNodes > sc->numNodesUploaded)
+        return fail(sc->ctx, GPUGI_ERROR_INVALID_ARGUMENT, "the node limit can only be lowered");
+    sc->dev.numNodes = numNodes ? numNodes : sc->numNodesUploaded;
+    return GPUGI_OK;
 }

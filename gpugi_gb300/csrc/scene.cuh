@@ -49,6 +49,9 @@ struct DevScene {
     const float4* texels = nullptr;
     const uint4* texInfo = nullptr;
     const int4* matTex = nullptr;
+    // The owning context's device error word: the checked library reports
+    // out-of-range indexes met while shading this scene there.
+    uint32_t* err = nullptr;
 };
 
 // Material view (constant-valued MaterialData, materials.glsl:9-30).
@@ -98,6 +101,10 @@ GPUGI_D float4 sample_texture(const DevScene& s, int tex, float2 tc) {
 // SampleMaterialData (materials.glsl:19-30): the four maps at the hit's
 // texture coordinate (the record's constants where a material has no texture).
 GPUGI_D MaterialData load_material(const DevScene& s, int id, float2 tc = make_float2(0.0f, 0.0f)) {
+    if (kChecked && (id < 0 || (uint32_t)id >= s.numMaterials)) {
+        raise_error(s.err, DEVERR_BOUNDS);
+        id = 0;
+    }
     const float4* m = s.materials + 6 * id;
     float4 a = __ldg(m), b = __ldg(m + 1), c = __ldg(m + 2), d = __ldg(m + 3), e = __ldg(m + 4),
            f = __ldg(m + 5);

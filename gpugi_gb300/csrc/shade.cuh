@@ -139,6 +139,12 @@ GPUGI_D float2 pack_normal(float3 n) {
 
 // GetTriangleHitInfo (scenedata.glsl:94-105): interpolated shading normal.
 GPUGI_D float3 hit_normal(const DevScene& s, int4 tri, float u, float v, float2* texcoord) {
+    if (kChecked && ((uint32_t)tri.x >= s.numVertices || (uint32_t)tri.y >= s.numVertices ||
+                     (uint32_t)tri.z >= s.numVertices)) {
+        raise_error(s.err, DEVERR_BOUNDS);
+        if (texcoord) *texcoord = make_float2(0.0f, 0.0f);
+        return make_float3(0.0f, 0.0f, 1.0f);
+    }
     float4 a = __ldg(s.vinfo + tri.x), b = __ldg(s.vinfo + tri.y), c = __ldg(s.vinfo + tri.z);
     float w = 1.0f - (v + u);
     float3 n = unpack_normal(a.x, a.y) * w + unpack_normal(b.x, b.y) * u + unpack_normal(c.x, c.y) * v;

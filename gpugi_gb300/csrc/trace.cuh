@@ -248,6 +248,10 @@ GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLe
             raise_error(errWord, DEVERR_TRAVERSAL_CAP);
             break;
         }
+        if (kChecked && node >= s.numNodes) {
+            raise_error(errWord, DEVERR_BOUNDS);
+            break;
+        }
         if (COUNT) ++cnt->nodes;
         const float4* nd = nodes + node_stride<BOUNDS>() * (size_t)node;
         const float4 a = __ldg(nd);
@@ -261,6 +265,10 @@ GPUGI_D TraceResult trace_ray(const DevScene& s, float3 o, float3 d, float rayLe
             if (child & LEAF_FLAG) {
                 const uint32_t count = (child >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK;
                 const uint32_t slot0 = (child & LEAF_BLOCK_MASK) * s.leafSize;
+                if (kChecked && (uint64_t)slot0 + count > s.numSlots) {
+                    raise_error(errWord, DEVERR_BOUNDS);
+                    break;
+                }
                 if (COUNT) cnt->slots += count < s.leafSize ? count + 1 : count;
                 for (uint32_t k = 0; k < count; ++k) {
                     if (COUNT) ++cnt->tris;
@@ -342,6 +350,12 @@ GPUGI_D bool walk_step(WalkState& w, const DevScene& s, uint32_t* errWord, const
     const bool isTri = w.cur < w.end;
     if (!isTri && w.budget-- == 0) {
         raise_error(errWord, DEVERR_TRAVERSAL_CAP);
+        w.node = NODE_DONE;
+        return true;
+    }
+    if (kChecked && (isTri ? w.cur >= s.numSlots : w.node >= s.numNodes)) {
+        raise_error(errWord, DEVERR_BOUNDS);
+        w.cur = w.end;
         w.node = NODE_DONE;
         return true;
     }
@@ -469,6 +483,10 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
         raise_error(err, DEVERR_TRAVERSAL_CAP);
         return true;
     }
+    if (kChecked && g.node >= s.numNodes) {
+        raise_error(err, DEVERR_BOUNDS);
+        return true;
+    }
     const uint32_t p = g.node + gl;
     uint32_t next = kGroupDone, child = 0, escape = 0;
     if (p < s.numNodes) {
@@ -496,6 +514,10 @@ GPUGI_D bool group_step(GroupWalk& g, const DevScene& s, uint32_t* err, unsigned
         g.cur = (lc & LEAF_BLOCK_MASK) * s.leafSize;
         g.end = g.cur + ((lc >> LEAF_COUNT_SHIFT) & LEAF_COUNT_MASK);
         g.resume = le ? le : kGroupDone;
+        if (kChecked && g.end > s.numSlots) {
+            raise_error(err, DEVERR_BOUNDS);
+            return true;
+        }
         if (g.cur >= g.end) {  // empty leaf block
             g.node = g.resume;
             return g.node == kGroupDone;

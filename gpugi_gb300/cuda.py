@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import atexit
 import ctypes as C
+import os
 import weakref
 from pathlib import Path
 
@@ -26,9 +27,12 @@ class GpugiError(RuntimeError):
 
 
 def lib():
+    """The CUDA library: libgpugi_cuda.so, or with GPUGI_CHECKED=1 in the
+    environment the bounds-checked libgpugi_cuda_checked.so."""
     global _LIB
     if _LIB is None:
-        path = LIB_DIR / "libgpugi_cuda.so"
+        checked = os.environ.get("GPUGI_CHECKED", "0") not in ("", "0")
+        path = LIB_DIR / ("libgpugi_cuda_checked.so" if checked else "libgpugi_cuda.so")
         if not path.exists():
             raise RuntimeError(f"{path} is missing: the CUDA extension must be built (python -m gpugi_gb300.build)")
         _LIB = C.CDLL(str(path))
@@ -52,6 +56,7 @@ def _declare(L):
     L.gpugi_scene_destroy.argtypes = [P]
     L.gpugi_scene_destroy.restype = None
     L.gpugi_debug_raise_device_error.argtypes = [P, U32]
+    L.gpugi_debug_limit_nodes.argtypes = [P, U32]
     L.gpugi_scene_build.argtypes = [P, P, U32, P, U32, P, P, U32, U32, C.POINTER(P)]
     L.gpugi_scene_export.argtypes = [P, P, C.POINTER(U32), C.POINTER(U32), P, P]
     L.gpugi_scene_set_hierarchy_ndf.argtypes = [P, P, P]

@@ -53,6 +53,7 @@ typedef enum gpugi_status {
 #define GPUGI_DEVERR_WAIT_TIMEOUT 0x4u    /* a bounded device wait ran out */
 #define GPUGI_DEVERR_BUILD 0x8u           /* the GPU hierarchy build found an inconsistent tree */
 #define GPUGI_DEVERR_HIERARCHY 0x10u      /* a hierarchy-importance walk to the root exceeded the node count */
+#define GPUGI_DEVERR_BOUNDS 0x20u         /* checked library only: an index outside its array (fetch skipped) */
 
 enum gpugi_bounds_kind { GPUGI_BOUNDS_AABB = 0, GPUGI_BOUNDS_ELLIPSOID = 1, GPUGI_BOUNDS_OBOX = 2 };
 
@@ -89,7 +90,7 @@ gpugi_status gpugi_device_error_bits(gpugi_ctx* ctx, uint32_t* bits);
 gpugi_status gpugi_debug_raise_device_error(gpugi_ctx* ctx, uint32_t bits);
 /* The cudaStream_t the context enqueues on (returned as void*). */
 void* gpugi_stream(gpugi_ctx* ctx);
-/* Library version string. */
+/* Library version string ("... checked" for the bounds-checked library). */
 const char* gpugi_version(void);
 
 /* Upload a scene in the layout of gpugi's GPU buffers.
@@ -116,6 +117,12 @@ gpugi_status gpugi_scene_upload(gpugi_ctx* ctx, const float* hierarchy, uint32_t
                                 uint32_t numVertices, const gpugi_material* materials,
                                 uint32_t numMaterials, gpugi_scene** out);
 void gpugi_scene_destroy(gpugi_scene* scene);
+/* Test support: the node count the device code checks indexes against is
+ * lowered to numNodes (at most the scene's own; 0 restores it). The node
+ * array itself is unchanged, so every fetch stays inside it; walks that
+ * reach a node at or past the limit end, and the checked library
+ * (libgpugi_cuda_checked.so) reports GPUGI_DEVERR_BOUNDS for them. */
+gpugi_status gpugi_debug_limit_nodes(gpugi_scene* scene, uint32_t numNodes);
 
 /* Build the hierarchy on the GPU and create the scene. Replaces a host
  * build with bvhmake (BVHBuilder::BuildBVH + FitBox + ExportBVH/

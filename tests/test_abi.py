@@ -34,6 +34,19 @@ def test_exports_every_declared_symbol(built, header, libname):
     assert not missing, f"{libname} lacks {missing}"
 
 
+def test_checked_library_exports_the_same_symbols(built):
+    """The bounds-checked build (-DGPUGI_CHECKED=1) is the same C ABI."""
+    names = declared_functions(ROOT / "include" / "gpugi_cuda.h")
+    lib = C.CDLL(str(LIB / "libgpugi_cuda_checked.so"))
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, f"libgpugi_cuda_checked.so lacks {missing}"
+    lib.gpugi_version.restype = C.c_char_p
+    assert lib.gpugi_version().endswith(b"checked")
+    plain = C.CDLL(str(LIB / "libgpugi_cuda.so"))
+    plain.gpugi_version.restype = C.c_char_p
+    assert not plain.gpugi_version().endswith(b"checked")
+
+
 def test_all_headers_covered():
     for h in (ROOT / "include").glob("*.h"):
         assert h.name in HEADERS, f"{h.name} has no library mapping in this test"
