@@ -12,10 +12,18 @@
 //                  [--path-length L] [--rr-start D] [--sky r g b] [--reference-rng]
 //                  [--point-light px py pz ir ig ib] [--reference FILE.pfm]
 //                  [--out FILE.pfm] [--checkpoint BASE] [--resume BASE] [--device D]
+//                  [--mse-check-interval N] [--wait-mse X]
 //
+// --mse-check-interval N computes the MSE against --reference every N
+// iterations and prints it as a JSON line (Application::MSEChecks,
+// application.cpp:345-376, the GlobalConfig `mseCheckInterval`);
+// --wait-mse X stops drawing at the first check whose MSE is below X, or
+// whose MSE is NaN (the script command `waitMSE`), with --iterations as the
+// cap. The summary line then says whether X was reached and when.
 // --resume BASE restores a checkpoint (RendererSystem::LoadCheckpoint) before
 // drawing, --checkpoint BASE writes one after (SaveCheckpoint), so a long
 // accumulation can run as several invocations with the same settings.
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -28,7 +36,8 @@ namespace {
 
 struct Args {
     std::string scene, renderer = "Pathtracer", out, reference, checkpoint, resume;
-    int width = 256, height = 256, iterations = 16, device = 0;
+    int width = 256, height = 256, iterations = 16, device = 0, mseCheckInterval = 0;
+    double waitMse = 0.0;
     unsigned pathLength = 8, rrStart = 0;
     float cam[7] = {0.0f, 1.0f, 3.4f, 0.0f, 1.0f, 0.0f, 40.0f};
     float sky[3] = {0.0f, 0.0f, 0.0f};
@@ -57,6 +66,8 @@ Args parse(int argc, char** argv) {
         else if (k == "--size") { need(i, 2); a.width = std::atoi(argv[++i]); a.height = std::atoi(argv[++i]); }
         else if (k == "--iterations") { need(i, 1); a.iterations = std::atoi(argv[++i]); }
         else if (k == "--device") { need(i, 1); a.device = std::atoi(argv[++i]); }
+        else if (k == "--mse-check-interval") { need(i, 1); a.mseCheckInterval = std::atoi(argv[++i]); }
+        else if (k == "--wait-mse") { need(i, 1); a.waitMse = std::strtod(argv[++i], nullptr); }
         else if (k == "--path-length") { need(i, 1); a.pathLength = (unsigned)std::atoi(argv[++i]); }
         else if (k == "--rr-start") { need(i, 1); a.rrStart = (unsigned)std::atoi(argv[++i]); }
         else if (k == "--reference-rng") { a.referenceRng = true; }
@@ -75,6 +86,10 @@ Args parse(int argc, char** argv) {
     }
     if (a.scene.empty()) usage("--scene is required");
     if (a.width <= 0 || a.height <= 0 || a.iterations < 0) usage("bad size or iteration count");
+    if (a.mseCheckInterval < 0) usage("--mse-check-interval must be >= 0");
+    if (a.mseCheckInterval > 0 && a.reference.empty()) usage("--mse-check-interval needs --reference");
+    // the reference refuses waitMSE without an MSE check interval or a reference image
+    if (a.waitMse > 0.0 && a.mseCheckInterval <= 0) usage("--wait-mse needs --mse-check-interval > 0");
     return a;
 }
 
@@ -108,26 +123,60 @@ int main(int argc, char** argv) {
         else usage("unknown renderer");
 
         if (!a.resume.empty()) system.LoadCheckpoint(a.resume);
-        for (int i = 0; i < a.iterations; ++i) system.Draw();
+        TextureMSE tmse;
+        if (!a.reference.empty()) {
+            tmse.LoadReferenceFromPFM(a.reference);
+            if (!tmse.HasValidReferenceImage()) usage("cannot read the reference image");
+        }
+        // Draw, with the MSE checks of Application::MSEChecks every
+        // mseCheckInterval iterations; waitMSE ends the loop once the MSE is
+        // below the goal (or NaN).
+        const auto t0 = std::chrono::steady_clock::now();
+        auto wallMs = [&] {
+            return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        };
+        bool waiting = a.waitMse > 0.0, reached = false, nanMse = false;
+        double reachedWallMs = -1.0;
+        unsigned long reachedIteration = 0;
+        int sinceCheck = 0;
+        for (int i = 0; i < a.iterations && !(a.waitMse > 0.0 && !waiting); ++i) {
+            system.Draw();
+            if (a.mseCheckInterval > 0 && ++sinceCheck >= a.mseCheckInterval) {
+                sinceCheck = 0;
+                const unsigned long it = system.GetIterationCount();
+                const double m = tmse.ComputeCurrentMSE64(system.GetBackbuffer(), (unsigned)it);
+                std::printf("{\"iteration\": %lu, \"render_ms\": %llu, \"wall_ms\": %.3f, \"mse\": %.9g}\n", it,
+                            (unsigned long long)system.GetRenderTime(), wallMs(), m);
+                if (waiting && (m != m || a.waitMse > m)) {
+                    waiting = false;
+                    nanMse = m != m;
+                    reached = !nanMse;
+                    reachedWallMs = wallMs();
+                    reachedIteration = it;
+                }
+            }
+        }
+        std::fflush(stdout);
         if (!a.checkpoint.empty() && !system.SaveCheckpoint(a.checkpoint)) usage("cannot write the checkpoint");
 
         const unsigned long iterations = system.GetIterationCount();
         double mse = -1.0;
-        if (!a.reference.empty()) {
-            TextureMSE tmse;
-            tmse.LoadReferenceFromPFM(a.reference);
-            if (!tmse.HasValidReferenceImage()) usage("cannot read the reference image");
-            mse = tmse.ComputeCurrentMSE64(system.GetBackbuffer(), (unsigned)iterations);
-        }
+        if (!a.reference.empty()) mse = tmse.ComputeCurrentMSE64(system.GetBackbuffer(), (unsigned)iterations);
         if (!a.out.empty()) {
             const std::vector<float> rgba = system.GetBackbuffer().ReadRGBA();
             if (!WritePfm(rgba.data(), ei::IVec2(a.width, a.height), a.out, (std::uint32_t)iterations)) return 1;
         }
         std::printf(
             "{\"renderer\": \"%s\", \"iterations\": %lu, \"render_ms\": %llu, \"width\": %d, \"height\": %d, "
-            "\"mse\": %.9g}\n",
+            "\"mse\": %.9g",
             system.GetActiveRenderer()->GetName().c_str(), iterations, (unsigned long long)system.GetRenderTime(),
             a.width, a.height, mse);
+        if (a.waitMse > 0.0)
+            std::printf(", \"wait_mse\": %.9g, \"reached\": %s, \"mse_nan\": %s, \"reached_iteration\": %lu, "
+                        "\"reached_wall_ms\": %.3f",
+                        a.waitMse, reached ? "true" : "false", nanMse ? "true" : "false", reachedIteration,
+                        reachedWallMs);
+        std::printf("}\n");
         scene.reset();
         return 0;
     } catch (const std::exception& e) {

@@ -30,6 +30,12 @@ def test_cli_rejects_bad_arguments(built):
     assert r.returncode == 2 and "--scene is required" in r.stderr
     r = subprocess.run([str(EXE), "--scene", "x.bim", "--size", "0", "4"], capture_output=True, text=True)
     assert r.returncode == 2
+    # waitMSE needs an MSE check interval, and the checks need a reference
+    # image (the reference logs these cases as errors; here they are refused)
+    r = subprocess.run([str(EXE), "--scene", "x.bim", "--wait-mse", "0.1"], capture_output=True, text=True)
+    assert r.returncode == 2 and "--mse-check-interval" in r.stderr
+    r = subprocess.run([str(EXE), "--scene", "x.bim", "--mse-check-interval", "2"], capture_output=True, text=True)
+    assert r.returncode == 2 and "--reference" in r.stderr
 
 
 @pytest.fixture(scope="module")
@@ -107,6 +113,37 @@ def test_headless_texture_mse_and_nrc(cuda_ctx, room_file, tmp_path):
         assert info_nrc["renderer"] == renderer
         img = _read_pfm(nrc)
         assert np.isfinite(img).all() and img.mean() > 0
+
+
+@pytest.mark.gpu
+def test_headless_mse_checks_and_wait_mse(cuda_ctx, room_file, tmp_path):
+    """--mse-check-interval prints the MSE against the reference every N
+    iterations (Application::MSEChecks); --wait-mse stops at the first check
+    below the goal (the script command waitMSE), well before the cap."""
+    sc, path = room_file
+    ref = tmp_path / "ref.pfm"
+    common = ["--scene", path, "--size", 32, 32, "--camera", *CAM, "--path-length", 6]
+    _run(common + ["--iterations", 256, "--out", ref])
+    r = subprocess.run([str(EXE)] + [str(a) for a in common + ["--iterations", 12, "--reference", ref,
+                                                                  "--mse-check-interval", 4]],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(x) for x in r.stdout.strip().splitlines()]
+    checks, summary = lines[:-1], lines[-1]
+    assert [c["iteration"] for c in checks] == [4, 8, 12]
+    assert checks[-1]["mse"] == pytest.approx(summary["mse"], rel=1e-6)
+    assert checks[0]["mse"] > checks[-1]["mse"] > 0
+    goal = 0.5 * (checks[0]["mse"] + checks[-1]["mse"])  # between the 4- and the 12-iteration MSE
+    r = subprocess.run([str(EXE)] + [str(a) for a in common + ["--iterations", 200, "--reference", ref,
+                                                                  "--mse-check-interval", 2, "--wait-mse", goal]],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(x) for x in r.stdout.strip().splitlines()]
+    checks, summary = lines[:-1], lines[-1]
+    assert summary["reached"] is True and summary["mse_nan"] is False
+    assert summary["iterations"] == summary["reached_iteration"] == checks[-1]["iteration"] < 200
+    assert checks[-1]["mse"] < goal and all(c["mse"] >= goal for c in checks[:-1])
+    assert summary["reached_wall_ms"] > 0
 
 
 @pytest.mark.gpu
