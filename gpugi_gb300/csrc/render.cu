@@ -1752,7 +1752,9 @@ template <bool ANY_HIT, typename Load, typename Finish>
 GPUGI_D void persistent_walks_multi(uint32_t n, unsigned long long* work, uint32_t* err, Load load, Finish finish) {
     const unsigned lane = threadIdx.x & 31u;
     WalkState w;
-    const DevScene* sc = nullptr;
+    // the ray's scene, copied when its walk starts: the few fields a step
+    // reads then stay in registers instead of being loaded every step
+    DevScene sc;
     uint32_t ray = 0;
     bool active = false, exhausted = false;
     while (true) {
@@ -1768,8 +1770,8 @@ GPUGI_D void persistent_walks_multi(uint32_t n, unsigned long long* work, uint32
                     ray = (uint32_t)my;
                     float3 o, d;
                     float tmax;
-                    sc = load(ray, o, d, tmax);
-                    walk_begin(w, *sc, o, d, tmax);
+                    sc = *load(ray, o, d, tmax);
+                    walk_begin(w, sc, o, d, tmax);
                     active = true;
                 } else {
                     exhausted = true;
@@ -1778,9 +1780,9 @@ GPUGI_D void persistent_walks_multi(uint32_t n, unsigned long long* work, uint32
         }
         if (!__any_sync(0xffffffffu, active)) break;
         if (active) {
-            const bool done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? walk_step<ANY_HIT, 1>(w, *sc, err)
-                              : sc->boundsKind == GPUGI_BOUNDS_OBOX    ? walk_step<ANY_HIT, 2>(w, *sc, err)
-                                                                       : walk_step<ANY_HIT, 0>(w, *sc, err);
+            const bool done = sc.boundsKind == GPUGI_BOUNDS_ELLIPSOID ? walk_step<ANY_HIT, 1>(w, sc, err)
+                              : sc.boundsKind == GPUGI_BOUNDS_OBOX    ? walk_step<ANY_HIT, 2>(w, sc, err)
+                                                                      : walk_step<ANY_HIT, 0>(w, sc, err);
             if (done) {
                 finish(ray, w.slot, w.len, w.u, w.v);
                 active = false;

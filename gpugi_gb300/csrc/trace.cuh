@@ -549,13 +549,13 @@ GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long l
     const uint64_t perBlock = blockDim.x / G;
     const uint64_t groups = (uint64_t)gridDim.x * perBlock;
     GroupWalk g;
-    const DevScene* sc = nullptr;
+    DevScene sc;  // MULTI: the ray's scene, copied at its walk's start (fields stay in registers)
     for (uint64_t my = (uint64_t)blockIdx.x * perBlock + threadIdx.x / G; my < n;) {
         float3 o, d;
         float tmax;
         if constexpr (MULTI) {
-            sc = load(my, o, d, tmax);
-            group_begin(g, *sc, o, d, tmax);
+            sc = *load(my, o, d, tmax);
+            group_begin(g, sc, o, d, tmax);
         } else {
             load(my, o, d, tmax);
             group_begin(g, scene, o, d, tmax);
@@ -563,9 +563,9 @@ GPUGI_D void group_walks_impl(const DevScene& scene, uint64_t n, unsigned long l
         bool done = false;
         while (!done) {
             if constexpr (MULTI)
-                done = sc->boundsKind == GPUGI_BOUNDS_ELLIPSOID ? group_step<ANY_HIT, 1, G>(g, *sc, err, gl, gbase, gmask)
-                       : sc->boundsKind == GPUGI_BOUNDS_OBOX    ? group_step<ANY_HIT, 2, G>(g, *sc, err, gl, gbase, gmask)
-                                                                : group_step<ANY_HIT, 0, G>(g, *sc, err, gl, gbase, gmask);
+                done = sc.boundsKind == GPUGI_BOUNDS_ELLIPSOID ? group_step<ANY_HIT, 1, G>(g, sc, err, gl, gbase, gmask)
+                       : sc.boundsKind == GPUGI_BOUNDS_OBOX    ? group_step<ANY_HIT, 2, G>(g, sc, err, gl, gbase, gmask)
+                                                               : group_step<ANY_HIT, 0, G>(g, sc, err, gl, gbase, gmask);
             else
                 done = group_step<ANY_HIT, BOUNDS, G, TRI>(g, scene, err, gl, gbase, gmask);
         }
