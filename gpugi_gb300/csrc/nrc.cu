@@ -46,6 +46,12 @@ struct gpugi_nrc {
     // training kernels: tcgen05 (default) or the warp-level mma.sync pair
     uint32_t kernels = GPUGI_NRC_KERNELS_TCGEN05;
     float* partials = nullptr;  // tcgen05 training: weight-gradient sums per CTA [numSMs][kParams]
+    // limit of every mbarrier wait of the tcgen05 kernels (a wait that runs
+    // out sets GPUGI_DEVERR_WAIT_TIMEOUT and the kernel ends cleanly)
+    uint64_t waitNs = 1000000000ull;
+    // test support: the tcgen05 kernels issue no MMA and no commit, so
+    // their first wait runs out (gpugi_nrc_debug_stall)
+    uint32_t stall = 0;
 };
 
 namespace gpugi {
@@ -519,7 +525,8 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const float* __restrict
                                                          const uint32_t* __restrict__ count,
                                                          const __half* __restrict__ wBwd, float3 boxMin,
                                                          float3 boxInv, float lossScale, float* __restrict__ partials,
-                                                         float* lossSum, float* predOut, uint32_t* errWord) {
+                                                         float* lossSum, float* predOut, uint32_t* errWord,
+                                                         uint64_t waitNs, uint32_t stall) {
     using namespace tc;
     using namespace tcl;
     if (count) n = min(n, (uint64_t)*count);
@@ -556,7 +563,7 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const float* __restrict
     const uint64_t tiles = (n + 127) / 128;
     // one MMA phase: thread 0 issues, everyone waits; false on a timeout
     auto phase_wait = [&]() {
-        const bool ok = bar_wait(&bar, parity);
+        const bool ok = bar_wait(&bar, parity, waitNs);
         parity ^= 1u;
         fence_after();
         return ok;
@@ -593,7 +600,7 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const float* __restrict
         // forward
         for (int l = 0; l < kLayers && !failed; ++l) {
             const int outs = out_of(l);
-            if (t == 0) {
+            if (t == 0 && !stall) {
                 const uint32_t id = idesc(128, outs, false, true);
                 for (int s = 0; s < 4; ++s)
                     mma(tm + kColD, desc(xs + l * 1024 + s * 256, 128, kXSG),
@@ -642,7 +649,7 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const float* __restrict
         }
         // backward: dY_{l-1} = (dY_l W_l^T) * [X_l > 0]
         for (int l = 4; l >= 1 && !failed; --l) {
-            if (t == 0) {
+            if (t == 0 && !stall) {
                 const uint32_t id = idesc(128, 64, false, false);
                 const int steps = l == 4 ? 1 : 4;
                 for (int s = 0; s < steps; ++s)
@@ -678,7 +685,7 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const float* __restrict
         if (failed) break;
         // weight gradients of the tile, accumulated over the CTA's tiles;
         // completion is awaited before the next tile overwrites X and Y
-        if (t == 0) {
+        if (t == 0 && !stall) {
             const bool first = tile == blockIdx.x;
             for (int pr = 0; pr < 3; ++pr) {
                 const uint32_t id = idesc(128, pr < 2 ? 128 : 16, true, true);
@@ -753,15 +760,27 @@ constexpr uint32_t kWBytes = tcl::kWBytes;
 constexpr uint32_t kSmem = kWBytes + 2 * kXBytes + 1024;
 }  // namespace tci
 
-GPUGI_D void wg_sync(int wg) {
-    if (wg == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
-    else asm volatile("bar.sync 2, 128;" ::: "memory");
+// A barrier of the warpgroup's 128 threads that also ORs a flag over them.
+GPUGI_D bool wg_any(int wg, bool v) {
+    uint32_t r;
+    if (wg == 0)
+        asm volatile("{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.or.pred p, 1, 128, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(r)
+                     : "r"((uint32_t)v)
+                     : "memory");
+    else
+        asm volatile("{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.or.pred p, 2, 128, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(r)
+                     : "r"((uint32_t)v)
+                     : "memory");
+    return r != 0;
 }
 
 __global__ void __launch_bounds__(256) k_nrc_infer_tc(const float* __restrict__ queries, uint64_t n,
                                                       const uint32_t* __restrict__ count,
                                                       const __half* __restrict__ wInfT, float3 boxMin, float3 boxInv,
-                                                      float* __restrict__ out, uint32_t* errWord) {
+                                                      float* __restrict__ out, uint32_t* errWord, uint64_t waitNs,
+                                                      uint32_t stall) {
     using namespace tc;
     using namespace tcl;
     if (count) n = min(n, (uint64_t)*count);
@@ -817,22 +836,25 @@ __global__ void __launch_bounds__(256) k_nrc_infer_tc(const float* __restrict__ 
                 *reinterpret_cast<uint4*>(xRow + j * 128) = *reinterpret_cast<const uint4*>(enc + 8 * j);
         }
         for (int l = 0; l < kLayers; ++l) {
+            // the layer's barrier also agrees on a timeout: a warpgroup
+            // leaves together, never with some threads waiting here
             fence_smem();
             fence_before();
-            wg_sync(wg);
+            failed = wg_any(wg, failed);
             fence_after();
+            if (failed) break;
             const int outs = out_of(l);
-            if (lt == 0) {
+            if (lt == 0 && !stall) {
                 const uint32_t id = idesc(128, outs, false, true);
                 for (int s = 0; s < 4; ++s)
                     mma(tm, desc(xs + s * 256, 128, tci::kXSG),
                         desc(ws + w_off(l) + s * 2 * w_kstride(l), w_kstride(l), 128), id, s > 0);
                 commit(bar);
             }
-            if (!bar_wait(bar, parity)) failed = true;
+            if (!bar_wait(bar, parity, waitNs)) failed = true;
             parity ^= 1u;
             fence_after();
-            if (failed) break;
+            if (failed) continue;  // on to the next layer's barrier, which ends the tile
             if (l < 4) {
                 // the MMA has read X: overwrite it with this layer's output
 #pragma unroll
@@ -857,6 +879,7 @@ __global__ void __launch_bounds__(256) k_nrc_infer_tc(const float* __restrict__ 
                     for (int c = 0; c < 3; ++c) out[3 * row + c] = fmaxf(__uint_as_float(r[c]), 0.0f);
             }
         }
+        failed = wg_any(wg, failed);  // the warpgroup takes its next tile, or leaves, together
     }
     if (failed && lt == 0) atomicOr(errWord, GPUGI_DEVERR_WAIT_TIMEOUT);
     fence_before();
@@ -916,7 +939,8 @@ gpugi_status gpugi::nrc_infer_counted(gpugi_ctx* ctx, const gpugi_nrc* nn, const
         const uint64_t tiles = (n + 127) / 128;
         const uint64_t grid = std::min<uint64_t>((uint64_t)ctx->numSMs * 3, (tiles + 1) / 2);
         k_nrc_infer_tc<<<(unsigned)grid, 256, tci::kSmem, ctx->stream>>>(queries, n, count, nn->wInfT, nn->boxMin,
-                                                                         nn->boxInv, out, ctx->errWord);
+                                                                         nn->boxInv, out, ctx->errWord, nn->waitNs,
+                                                                         nn->stall);
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
         return GPUGI_OK;
     }
@@ -1042,6 +1066,15 @@ gpugi_status gpugi_nrc_set_kernels(gpugi_ctx* ctx, gpugi_nrc* nn, uint32_t kerne
     return GPUGI_OK;
 }
 
+gpugi_status gpugi_nrc_debug_stall(gpugi_ctx* ctx, gpugi_nrc* nn, uint32_t stall, uint64_t waitNs) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (!nn) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "bad argument");
+    GPUGI_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    nn->stall = stall ? 1u : 0u;
+    nn->waitNs = waitNs ? waitNs : 1000000000ull;
+    return GPUGI_OK;
+}
+
 gpugi_status gpugi_nrc_set_ema(gpugi_ctx* ctx, gpugi_nrc* nn, float decay) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     if (!nn || !(decay >= 0.0f && decay < 1.0f)) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "decay in [0, 1)");
@@ -1074,7 +1107,7 @@ static gpugi_status nrc_grad(gpugi_ctx* ctx, gpugi_nrc* nn, const float* samples
         const int grid = (int)std::min<uint64_t>((uint64_t)ctx->numSMs, std::max<uint64_t>(tiles, 1));
         k_nrc_train_tc<<<grid, 128, tcl::kSmem, ctx->stream>>>(samples, n, count, nn->wBwd, nn->boxMin, nn->boxInv,
                                                                nn->lossScale, nn->partials, nn->lossSum, predOut,
-                                                               ctx->errWord);
+                                                               ctx->errWord, nn->waitNs, nn->stall);
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
         k_nrc_sum_partials<<<(kParams + 63) / 64, 256, 0, ctx->stream>>>(nn->partials, grid, nn->grad);
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());

@@ -58,9 +58,18 @@ GPUGI_D void bar_init(uint64_t* bar, uint32_t count) {
 
 // Bounded wait for the phase with the given parity; false when it ran out
 // (about 2^22 polls, tens of milliseconds).
-GPUGI_D bool bar_wait(uint64_t* bar, uint32_t parity) {
+GPUGI_D uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Wait for the phase `parity` of an mbarrier, at most limitNs nanoseconds
+// of the global timer (and at most 2^24 polls, should the timer not
+// advance); false when the wait ran out.
+GPUGI_D bool bar_wait(uint64_t* bar, uint32_t parity, uint64_t limitNs) {
     const uint32_t a = smem_addr(bar);
-    for (uint32_t it = 0; it < (1u << 22); ++it) {
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 0; it < (1u << 24); ++it) {
         uint32_t done;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
@@ -68,6 +77,7 @@ GPUGI_D bool bar_wait(uint64_t* bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if ((it & 255u) == 255u && globaltimer_ns() - t0 > limitNs) return false;
     }
     return false;
 }

@@ -57,6 +57,7 @@ def _declare(L):
     L.gpugi_scene_destroy.restype = None
     L.gpugi_debug_raise_device_error.argtypes = [P, U32]
     L.gpugi_debug_limit_nodes.argtypes = [P, U32]
+    L.gpugi_nrc_debug_stall.argtypes = [P, P, U32, U64]
     L.gpugi_scene_build.argtypes = [P, P, U32, P, U32, P, P, U32, U32, C.POINTER(P)]
     L.gpugi_scene_export.argtypes = [P, P, C.POINTER(U32), C.POINTER(U32), P, P]
     L.gpugi_scene_set_hierarchy_ndf.argtypes = [P, P, P]

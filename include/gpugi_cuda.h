@@ -470,6 +470,13 @@ gpugi_status gpugi_nrc_set_weights(gpugi_ctx* ctx, gpugi_nrc* nrc, const float* 
 #define GPUGI_NRC_KERNELS_TCGEN05 0u
 #define GPUGI_NRC_KERNELS_MMA_SYNC 1u
 gpugi_status gpugi_nrc_set_kernels(gpugi_ctx* ctx, gpugi_nrc* nrc, uint32_t kernels);
+/* Every mbarrier wait of the tcgen05 kernels is bounded (1 s of the global
+ * timer by default); a wait that runs out sets GPUGI_DEVERR_WAIT_TIMEOUT, the
+ * kernel frees its tensor memory and ends, and the context stays usable.
+ * Test support: with stall = 1 those kernels issue no MMA and no commit, so
+ * their first wait runs out after waitNs nanoseconds (0 = the default 1 s);
+ * stall = 0 restores normal work. Waits for the queued work first. */
+gpugi_status gpugi_nrc_debug_stall(gpugi_ctx* ctx, gpugi_nrc* nrc, uint32_t stall, uint64_t waitNs);
 /* Inference (and the render pass) use an exponential moving average of the
  * trained weights, bias-corrected (decay 0.99 by default; 0 = the trained
  * weights themselves). Setting it, or the weights, restarts the average. */

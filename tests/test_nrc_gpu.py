@@ -112,6 +112,51 @@ def test_training_kernels_agree(cuda_ctx):
     c.close()
 
 
+def test_tcgen05_wait_timeouts_are_reported_and_recoverable(cuda_ctx):
+    """Every mbarrier wait of the tcgen05 kernels is bounded: with their MMAs
+    and commits left out (gpugi_nrc_debug_stall, a barrier that nothing
+    completes) the first wait of the inference and of the training kernel
+    runs out after 20 ms; the call reports GPUGI_DEVERR_WAIT_TIMEOUT, the
+    kernels free their tensor memory and end, and the next calls on the same
+    context compute as before."""
+    import re
+
+    import torch
+    from gpugi_gb300 import cuda
+    rng = np.random.default_rng(9)
+    q = _queries(rng, 4096)
+    tq = torch.from_numpy(q).cuda()
+    samples = torch.from_numpy(np.concatenate([q, _target(q)], 1)).cuda()
+    c = nrc.RadianceCache(cuda_ctx, BOX_MIN, BOX_MAX, seed=21)
+    c.set_kernels("tcgen05")
+    before = c.infer(tq).cpu().numpy()
+    _, g_before, l_before = c.gradient(samples)
+    L = nrc._declare()
+
+    def stalled_bits(call):
+        try:
+            call()
+            return cuda_ctx.device_error_bits()
+        except cuda.GpugiError as e:
+            m = re.search(r"error bits (0x[0-9a-f]+)", str(e))
+            assert e.status == 5 and m, str(e)
+            return int(m.group(1), 16)
+
+    cuda_ctx.check(L.gpugi_nrc_debug_stall(cuda_ctx.handle, c.handle, 1, 20_000_000))
+    try:
+        assert stalled_bits(lambda: c.infer(tq)) & 0x4
+        assert stalled_bits(lambda: c.gradient(samples)) & 0x4
+    finally:
+        cuda_ctx.check(L.gpugi_nrc_debug_stall(cuda_ctx.handle, c.handle, 0, 0))
+    assert cuda_ctx.device_error_bits() == 0
+    assert np.array_equal(c.infer(tq).cpu().numpy(), before)
+    _, g_after, l_after = c.gradient(samples)
+    # the gradient sums run in a fixed order; the loss is summed with atomics
+    assert np.array_equal(g_after, g_before) and abs(l_after / l_before - 1) < 1e-5
+    assert cuda_ctx.device_error_bits() == 0
+    c.close()
+
+
 def test_adam_step_matches_reference(cuda_ctx, cache):
     import torch
     rng = np.random.default_rng(4)
