@@ -56,8 +56,7 @@ GPUGI_D void bar_init(uint64_t* bar, uint32_t count) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Bounded wait for the phase with the given parity; false when it ran out
-// (about 2^22 polls, tens of milliseconds).
+// The global timer in nanoseconds.
 GPUGI_D uint64_t globaltimer_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
