@@ -310,11 +310,15 @@ def run_ours(args, world, rank, local):
     alg = [cuda.algorithmic_bytes(cuda.trace_stats_device(ctx, ds, bt), N_RAYS) for bt in batches]
     alg_bytes = float(np.mean(alg))
 
-    # Steps alternate between two streams (gpugi_trace_closest_device_async):
+    # Steps alternate between several streams (gpugi_trace_closest_device_async):
     # independent batches, so the walker tail of step k (its few deepest
-    # rays) overlaps the filter and walk of step k+1. The same K steps on the
-    # context's single stream are timed too ("single_stream").
+    # rays) overlaps the filter and walk of the next steps; each stream-ordered
+    # walk launches a share of the persistent grid (--walker-share, the
+    # library's default 50 %), so two or more walks run side by side. The same
+    # K steps as synchronous calls on the context's stream, with the full
+    # grid, are timed too ("single_stream").
     qstreams = [torch.cuda.Stream(device=dev) for _ in range(args.streams)]
+    ctx.set_async_walker_share(args.walker_share)
 
     def issue(k):
         s = qstreams[k % len(qstreams)]
@@ -491,6 +495,7 @@ def run_ours(args, world, rank, local):
             "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
                             "peak_source": "measured in this run: L2 reads of an L2-resident 32 MiB buffer"},
             "streams": len(qstreams),
+            "async_walker_share": args.walker_share,
             "single_stream": single,
             "watertight": watertight,
             "gpu_launches": args.steps * (2 if args.trace_mode >= 2 else 1),
@@ -1214,8 +1219,10 @@ def main():
                     help="passes workload: comma-separated subset of PT,LT,BPT,WHITTED,PM,IM,HIERARCHY")
     ap.add_argument("--shared-nodes", type=int, default=0,
                     help="top-of-tree nodes staged in shared memory by the walkers")
-    ap.add_argument("--streams", type=int, default=3,
+    ap.add_argument("--streams", type=int, default=4,
                     help="caller streams the headline steps alternate over (1 = no overlap)")
+    ap.add_argument("--walker-share", type=int, default=50,
+                    help="percent of the persistent walker grid a stream-ordered device-array query launches")
     ap.add_argument("--e2e-streams", type=int, default=3,
                     help="streams the end-to-end host-buffer steps alternate over")
     ap.add_argument("--trace-mode", type=int, default=3,

@@ -392,6 +392,13 @@ gpugi_status gpugi_set_host_pipeline(gpugi_ctx* ctx, uint32_t parts, uint32_t ze
     return GPUGI_OK;
 }
 
+gpugi_status gpugi_set_async_walker_share(gpugi_ctx* ctx, uint32_t percent) {
+    if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
+    if (percent < 1 || percent > 100) return fail(ctx, GPUGI_ERROR_INVALID_ARGUMENT, "percent must be in [1, 100]");
+    ctx->asyncWalkerShare = percent;
+    return GPUGI_OK;
+}
+
 gpugi_status gpugi_set_scene_layout(gpugi_ctx* ctx, uint32_t sharedNodes, uint32_t renderSharedNodes) {
     if (!ctx) return GPUGI_ERROR_INVALID_ARGUMENT;
     // 227 KB of shared memory per block at most: 7,000 nodes of 32 B
@@ -486,7 +493,7 @@ static gpugi_status trace_async(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyH
     if (st) return st;
     GPUGI_CUDA_TRY(ctx, cudaMemsetAsync(ss->counters, 0, 4 * sizeof(unsigned long long), s));
     st = launch_trace_filtered_on(ctx, sc, anyHit, ox, oy, oz, dx, dy, dz, tmax, n, slot, t, u, v, occluded,
-                                  ss->queue, ss->counters, s);
+                                  ss->queue, ss->counters, s, ctx->asyncWalkerShare);
     if (st) return st;
     GPUGI_CUDA_TRY(ctx, cudaEventRecord(ss->lastUse, s));
     return GPUGI_OK;
@@ -532,6 +539,8 @@ static gpugi_status trace_host_async(gpugi_ctx* ctx, const gpugi_scene* sc, bool
     st = launch_trace_filtered_on(ctx, sc, anyHit, d[0], d[1], d[2], d[3], d[4], d[5], d[6], n,
                                   anyHit ? nullptr : dSlot, anyHit ? nullptr : dT, anyHit ? nullptr : dU,
                                   anyHit ? nullptr : dV, anyHit ? dOcc : nullptr, ss->queue, ss->counters, s);
+    // (the full walker grid: host-array queries are paced by their copies,
+    // and a shorter walk keeps each stream's copy-trace-copy cycle short)
     if (st) return st;
     if ((st = copy_results_out(ctx, anyHit, dRes, 0, slot, t, u, v, occ, 0, n, s))) return st;
     GPUGI_CUDA_TRY(ctx, cudaEventRecord(ss->lastUse, s));

@@ -42,6 +42,11 @@ struct gpugi_ctx {
     // host-pointer ray queries: copies in, traversal and copies out of
     // hostParts parts of a call overlap on three streams (trace modes 2-5)
     uint32_t hostParts = 2;
+    // percent of the persistent walker grid a stream-ordered query on device
+    // arrays launches:
+    // queries on several streams then run two or more walks side by side,
+    // each one's tail overlapping the others' bulk (gpugi_set_async_walker_share)
+    uint32_t asyncWalkerShare = 50;
     uint32_t hostZeroCopy = 0;  // 1: page-locked host arrays are read and written by the kernels directly
     cudaStream_t copyIn = nullptr, copyOut = nullptr;
     cudaStream_t compute2 = nullptr;  // second traversal stream of the host-pointer pipeline
@@ -175,7 +180,8 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
                                       const float* oy, const float* oz, const float* dx, const float* dy,
                                       const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
                                       float* u, float* v, uint8_t* occluded, uint32_t* queue,
-                                      unsigned long long* counters, cudaStream_t stream = nullptr);
+                                      unsigned long long* counters, cudaStream_t stream = nullptr,
+                                      uint32_t walkerShare = 100);
 // Launch shape of a persistent walker: grid, dynamic shared memory and the
 // number of top-of-tree nodes it stages (at most maxStage).
 struct WalkerLaunch {

@@ -348,6 +348,13 @@ __global__ void __launch_bounds__(128, GPUGI_GROUP_MIN_BLOCKS) k_trace_group(
         });
 }
 
+// walkerShare percent of a persistent walker grid (at least one block).
+static unsigned share_of_grid(unsigned grid, uint32_t walkerShare) {
+    if (walkerShare >= 100) return grid;
+    const uint64_t g = (uint64_t)grid * (walkerShare ? walkerShare : 1) / 100;
+    return g ? (unsigned)g : 1u;
+}
+
 gpugi_status launch_trace_filtered(gpugi_ctx* ctx, const gpugi_scene* sc, bool anyHit, const float* ox,
                                    const float* oy, const float* oz, const float* dx, const float* dy,
                                    const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
@@ -368,7 +375,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
                                       const float* oy, const float* oz, const float* dx, const float* dy,
                                       const float* dz, const float* tmax, uint64_t n, int32_t* slot, float* t,
                                       float* u, float* v, uint8_t* occluded, uint32_t* queue,
-                                      unsigned long long* counters, cudaStream_t stream) {
+                                      unsigned long long* counters, cudaStream_t stream, uint32_t walkerShare) {
     if (n == 0) return GPUGI_OK;
     cudaStream_t cs = stream ? stream : ctx->stream;
     const int ell = (int)sc->dev.boundsKind;  // bounds kind: 0 box, 1 ellipsoid, 2 oriented box
@@ -416,6 +423,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
         WalkerLaunch L;
         gpugi_status st = walker_launch_config(ctx, sc, (const void*)kg, 1ull << 40, 0, L);
         if (st) return st;
+        L.grid = share_of_grid(L.grid, walkerShare);
         kg<<<L.grid, 128, 0, cs>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded, queue,
                                            counters, ctx->errWord);
         GPUGI_CUDA_TRY(ctx, cudaGetLastError());
@@ -427,6 +435,7 @@ gpugi_status launch_trace_filtered_on(gpugi_ctx* ctx, const gpugi_scene* sc, boo
     WalkerLaunch L;
     gpugi_status st = walker_launch_config(ctx, sc, (const void*)k, n, ctx->sharedNodes, L);
     if (st) return st;
+    L.grid = share_of_grid(L.grid, walkerShare);
     k<<<L.grid, 128, L.smem, cs>>>(sc->dev, ox, oy, oz, dx, dy, dz, tmax, slot, t, u, v, occluded, queue,
                                             counters, ctx->errWord, L.stage);
     GPUGI_CUDA_TRY(ctx, cudaGetLastError());

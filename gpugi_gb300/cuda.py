@@ -57,6 +57,7 @@ def _declare(L):
     L.gpugi_scene_destroy.restype = None
     L.gpugi_debug_raise_device_error.argtypes = [P, U32]
     L.gpugi_debug_limit_nodes.argtypes = [P, U32]
+    L.gpugi_set_async_walker_share.argtypes = [P, U32]
     L.gpugi_nrc_debug_stall.argtypes = [P, P, U32, U64]
     L.gpugi_scene_build.argtypes = [P, P, U32, P, U32, P, P, U32, U32, C.POINTER(P)]
     L.gpugi_scene_export.argtypes = [P, P, C.POINTER(U32), C.POINTER(U32), P, P]
@@ -157,6 +158,10 @@ class Context:
         """Host-pointer queries: staging split into `parts` overlapping parts (1: no overlap),
         or kernels accessing page-locked arrays directly (zero_copy)."""
         self.check(lib().gpugi_set_host_pipeline(self._h, parts, int(bool(zero_copy))))
+
+    def set_async_walker_share(self, percent: int = 50):
+        """Percent of the persistent walker grid a stream-ordered device-array query launches."""
+        self.check(lib().gpugi_set_async_walker_share(self._h, int(percent)))
 
     def set_scene_layout(self, shared_nodes: int = 0, render_shared_nodes: int = 0):
         """Top-of-tree nodes staged in shared memory, for scenes uploaded afterwards."""

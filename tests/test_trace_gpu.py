@@ -382,12 +382,15 @@ def test_l2_bandwidth_measurement(cuda_ctx):
         cuda_ctx.check(lib.gpugi_measure_l2_bandwidth(cuda_ctx.handle, 1000, 1, C.byref(g)))
 
 
-def test_stream_ordered_queries_overlap_and_match(cuda_ctx, icosphere_65536):
+@pytest.mark.parametrize("share", [50, 100, 1])
+def test_stream_ordered_queries_overlap_and_match(cuda_ctx, icosphere_65536, share):
     """gpugi_trace_*_device_async on several caller streams: batches issued
     alternately on three streams (and one on the context stream, NULL) give
-    the results of the context-stream calls; a larger batch on a stream
-    grows its scratch."""
+    the results of the context-stream calls, whatever share of the walker
+    grid the stream-ordered walks launch; a larger batch on a stream grows
+    its scratch."""
     import torch
+    cuda_ctx.set_async_walker_share(share)
     sc = icosphere_65536
     b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
     ds = cuda_ctx.upload_scene(b, sc["positions"])
@@ -410,6 +413,7 @@ def test_stream_ordered_queries_overlap_and_match(cuda_ctx, icosphere_65536):
         _compare_closest(g, cuda.trace_closest(cuda_ctx, ds, host[i]))
         assert np.array_equal(occ[i].cpu().numpy(), cuda.trace_any(cuda_ctx, ds, host[i]))
     assert cuda_ctx.device_error_bits() == 0
+    cuda_ctx.set_async_walker_share(50)
     ds.close()
 
 
