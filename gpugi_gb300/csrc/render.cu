@@ -2697,6 +2697,20 @@ gpugi_status gpugi_render_nrc(gpugi_ctx* ctx, const gpugi_scene* sc, const gpugi
                                        : (int)p->maxPathLength;
     Walkers W;
     if ((st = walkers_config(ctx, sc, W))) return st;
+    // Frames in flight on several lanes: each lane's walkers launch 150 /
+    // lanes percent of the persistent grid (37 % with four lanes), so about
+    // one and a half grids of walks run side by side and one frame's walker
+    // tails overlap the others' bulk instead of waiting for the SMs a
+    // full-grid walker holds (1-spp frames on the 1280 x 720 heightfield:
+    // 2.12 ms per frame with full grids, 1.90 at 50 %, 1.84 at 35 %, 1.89
+    // at 25 %, 2.15 at 20 %). The group-walk threshold follows the grid.
+    if (nLanes > 1) {
+        const unsigned share = std::min(100u, 150u / (unsigned)nLanes);
+        W.LE.grid = std::max(1u, W.LE.grid * share / 100u);
+        W.LS.grid = std::max(1u, W.LS.grid * share / 100u);
+        if (W.groupBelowE) W.groupBelowE = W.LE.grid * 128u * GPUGI_GROUP_BELOW_LANES;
+        if (W.groupBelowS) W.groupBelowS = W.LS.grid * 128u * GPUGI_GROUP_BELOW_LANES;
+    }
     int perSM = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, bpt ? (const void*)k_nrc_bpt_shade : (const void*)k_nrc_shade,
                                                   128, 0);
