@@ -390,6 +390,9 @@ def test_stream_ordered_queries_overlap_and_match(cuda_ctx, icosphere_65536, sha
     grid the stream-ordered walks launch; a larger batch on a stream grows
     its scratch."""
     import torch
+    for bad in (0, 101):
+        with pytest.raises(cuda.GpugiError):
+            cuda_ctx.set_async_walker_share(bad)
     cuda_ctx.set_async_walker_share(share)
     sc = icosphere_65536
     b = bvh.build_bvh(sc["positions"], sc["triangles"], method="sweep")
